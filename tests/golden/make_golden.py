@@ -1,0 +1,311 @@
+"""Generate the golden fixtures in this folder from the unmodified jax_cosmo source.
+
+Usage (in a container where the jax_cosmo source tree is present; no GPU needed)::
+
+    python tests/golden/make_golden.py --reference /root/reference [--procs 8]
+
+The reference package runs on top of ``jax_standin`` (NumPy, float64).  Every
+fixture is written as a compressed ``.npz``; the committed files are what the
+oracle tests (``tests/test_oracle_golden.py``) check against.  The reference
+source itself is never copied: only its outputs are stored.
+
+Fixtures
+--------
+background.npz  chi / growth tables and point queries   (background.py:199-242, 443-488)
+power.npz       Eisenstein-Hu T(k), sigma^2(8), linear and halofit P(k, a),
+                halofit (k_nl, n_eff, C)                  (transfer.py, power.py)
+tracers.npz     smail n(z), WL lensing kernel, NC density kernel, noise
+                                                          (redshift.py, probes.py)
+cl_wl2.npz      angular_cl, 2 WeakLensing bins (z0 = 0.5, 1.0; zmax = 4), 50 ell
+cl_mixed.npz    angular_cl, 2 WeakLensing + 2 NumberCounts bins, 2 cosmologies
+cov_like.npz    gaussian_cl_covariance_and_mean + gaussian_log_likelihood
+sparse.npz      sparse.inv / slogdet / to_dense / dot on a random SPD block matrix
+"""
+import argparse
+import os
+import sys
+import time
+import warnings
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+# Cosmologies used across fixtures: rows of
+# (Omega_c, Omega_b, h, n_s, sigma8, Omega_k, w0, wa)
+COSMOS = np.array(
+    [
+        [0.2589, 0.0486, 0.6774, 0.9667, 0.8159, 0.0, -1.0, 0.0],  # Planck15
+        [0.30, 0.05, 0.70, 0.96, 0.80, 0.0, -1.0, 0.0],  # reference test cosmology
+        [0.25, 0.045, 0.72, 0.95, 0.78, 0.0, -0.9, 0.1],  # w0wa
+        [0.35, 0.04, 0.60, 1.00, 1.00, 0.0, -1.3, 0.0],  # corner of the batch box
+    ]
+)
+
+_REF = None
+
+
+def _setup(reference):
+    global _REF
+    if _REF is not None:
+        return _REF
+    sys.path.insert(0, HERE)
+    import jax_standin
+
+    jax_standin.install()
+    sys.path.insert(0, reference)
+    warnings.filterwarnings("ignore")
+    import jax_cosmo
+
+    _REF = jax_cosmo
+    return jax_cosmo
+
+
+def _cosmo(jc, row):
+    names = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
+    return jc.Cosmology(**{n: float(v) for n, v in zip(names, row)})
+
+
+def make_background(jc):
+    a_q = np.concatenate(
+        [
+            np.logspace(-3, 0, 97),
+            np.linspace(0.05, 1.0, 64),
+            np.array([1e-3, 0.2, 0.25, 0.5, 0.999, 1.0]),
+        ]
+    )
+    out = {"cosmos": COSMOS, "a_q": a_q}
+    chitab, gtab, chi, D, H, dchi = [], [], [], [], [], []
+    for row in COSMOS:
+        c = _cosmo(jc, row)
+        chi.append(jc.background.radial_comoving_distance(c, a_q))
+        D.append(jc.background.growth_factor(c, a_q))
+        H.append(jc.background.H(c, a_q))
+        dchi.append(jc.background.dchioverda(c, a_q))
+        chitab.append(c._workspace["background.radial_comoving_distance"]["chi"])
+        gtab.append(c._workspace["background.growth_factor"]["g"])
+    out.update(
+        chitab=np.array(chitab),
+        gtab=np.array(gtab),
+        chi=np.array(chi),
+        D=np.array(D),
+        H=np.array(H),
+        dchioverda=np.array(dchi),
+    )
+    return out
+
+
+def make_power(jc):
+    k = np.logspace(-4, 4, 161)
+    a_list = np.array([1.0, 0.7, 0.4, 0.2])
+    a_hf = np.linspace(0.08, 1.0, 33)
+    # elementwise (k, a) pairs, the way the Limber integrand calls halofit
+    rng = np.random.default_rng(7)
+    a_pairs = np.sort(rng.uniform(0.1, 1.0, 64))
+    k_pairs = np.exp(rng.uniform(np.log(1e-3), np.log(50.0), 64))
+    out = {"cosmos": COSMOS, "k": k, "a_list": a_list, "a_hf": a_hf}
+    out["a_pairs"], out["k_pairs"] = a_pairs, k_pairs
+    T, s8, plin, pnl, knl, neff, C, pnl_pairs = [], [], [], [], [], [], [], []
+    for row in COSMOS:
+        c = _cosmo(jc, row)
+        T.append(jc.transfer.Eisenstein_Hu(c, k))
+        s8.append(jc.power.sigmasqr(c, 8.0, jc.transfer.Eisenstein_Hu))
+        plin.append([jc.power.linear_matter_power(c, k, a) for a in a_list])
+        pnl.append([jc.power.nonlinear_matter_power(c, k, a) for a in a_list])
+        kk, nn, cc = jc.power._halofit_parameters(c, a_hf, jc.transfer.Eisenstein_Hu)
+        knl.append(kk)
+        neff.append(nn)
+        C.append(cc)
+        pnl_pairs.append(jc.power.nonlinear_matter_power(c, k_pairs, a_pairs))
+    out.update(
+        T=np.array(T),
+        sigmasqr8=np.array(s8),
+        plin=np.array(plin),
+        pnl=np.array(pnl),
+        k_nl=np.array(knl),
+        n_eff=np.array(neff),
+        C=np.array(C),
+        pnl_pairs=np.array(pnl_pairs),
+    )
+    return out
+
+
+def make_tracers(jc):
+    z = np.linspace(0.0, 5.0, 101)
+    smail = np.array([[1.0, 2.0, 0.5, 4.0], [1.0, 2.0, 1.0, 4.0], [2.0, 1.5, 0.8, 10.0]])
+    nz_vals, norms = [], []
+    for a_, b_, z0, zmax in smail:
+        nz = jc.redshift.smail_nz(a_, b_, z0, zmax=zmax)
+        nz_vals.append(nz(z))
+        norms.append(nz._norm)
+    out = {"z": z, "smail": smail, "nz": np.array(nz_vals), "nz_norm": np.array(norms)}
+    zk = np.linspace(0.01, 3.9, 40)
+    out["z_kernel"] = zk
+    wl, nc = [], []
+    for row in COSMOS[:3]:
+        c = _cosmo(jc, row)
+        pz = [
+            jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10, zmax=4.0),
+            jc.redshift.smail_nz(1.0, 2.0, 1.0, gals_per_arcmin2=10, zmax=4.0),
+        ]
+        wl.append(jc.probes.WeakLensing(pz, sigma_e=0.26).kernel(c, zk, 100.0))
+        nc.append(
+            jc.probes.NumberCounts(pz, jc.bias.constant_linear_bias(1.2)).kernel(
+                c, zk, 100.0
+            )
+        )
+    out["wl_kernel"] = np.array(wl)
+    out["nc_kernel"] = np.array(nc)
+    pz = [
+        jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10, zmax=4.0),
+        jc.redshift.smail_nz(1.0, 2.0, 1.0, gals_per_arcmin2=3, zmax=4.0),
+    ]
+    out["wl_noise"] = jc.probes.WeakLensing(pz, sigma_e=0.3).noise()
+    out["nc_noise"] = jc.probes.NumberCounts(pz, jc.bias.constant_linear_bias(1.0)).noise()
+    return out
+
+
+# ---- angular_cl fixtures: one ell per worker process ----------------------------
+def _probes(jc, kind):
+    if kind == "wl2":
+        pz = [
+            jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10, zmax=4.0),
+            jc.redshift.smail_nz(1.0, 2.0, 1.0, gals_per_arcmin2=10, zmax=4.0),
+        ]
+        return [jc.probes.WeakLensing(pz, sigma_e=0.26)]
+    if kind == "mixed":
+        pz = [
+            jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10),
+            jc.redshift.smail_nz(1.0, 2.0, 1.0, gals_per_arcmin2=10),
+        ]
+        return [
+            jc.probes.WeakLensing(pz, sigma_e=0.26),
+            jc.probes.NumberCounts(pz, jc.bias.constant_linear_bias(1.2)),
+        ]
+    raise ValueError(kind)
+
+
+def _cl_worker(args):
+    reference, kind, row, ell = args
+    jc = _setup(reference)
+    c = _cosmo(jc, row)
+    return jc.angular_cl.angular_cl(c, np.array([ell]), _probes(jc, kind))[:, 0]
+
+
+def make_cl(reference, pool, kind, cosmo_rows, ell):
+    jobs = [(reference, kind, row, float(l)) for row in cosmo_rows for l in ell]
+    res = pool.map(_cl_worker, jobs)
+    n_c, n_l = len(cosmo_rows), len(ell)
+    cl = np.array(res).reshape(n_c, n_l, -1).transpose(0, 2, 1)
+    return {"cosmos": np.array(cosmo_rows), "ell": np.asarray(ell), "cl": cl}
+
+
+def make_cov_like(jc):
+    out = {}
+    # The reference's own likelihood test set-up (tests/test_likelihood.py:12-35)
+    ell = np.logspace(1, 3, 5)
+    nz1 = jc.redshift.smail_nz(1.0, 2.0, 1.0)
+    nz2 = jc.redshift.smail_nz(1.0, 2.0, 0.5)
+    P = [jc.probes.NumberCounts([nz1, nz2], jc.bias.constant_linear_bias(1.0))]
+    c = jc.Planck15()
+    mu, cov_sp = jc.angular_cl.gaussian_cl_covariance_and_mean(c, ell, P, sparse=True)
+    mu_d, cov_d = jc.angular_cl.gaussian_cl_covariance_and_mean(c, ell, P, sparse=False)
+    data = 1.1 * mu
+    ll = {}
+    for inc in (True, False):
+        ll[f"sparse_{inc}"] = jc.likelihood.gaussian_log_likelihood(
+            data, mu, cov_sp, include_logdet=inc
+        )
+        for m in ("inverse", "cholesky"):
+            ll[f"{m}_{inc}"] = jc.likelihood.gaussian_log_likelihood(
+                data, mu, cov_d, include_logdet=inc, inverse_method=m
+            )
+    out.update(
+        nc_ell=ell,
+        nc_mu=mu,
+        nc_cov_sparse=cov_sp,
+        nc_cov_dense=cov_d,
+        nc_data=data,
+        nc_cl_noise=jc.angular_cl.noise_cl(ell, P),
+    )
+    for k_, v in ll.items():
+        out["nc_ll_" + k_] = np.asarray(v)
+    # Covariance from fixed signal (tests/test_angular_cl.py:201-213 pattern)
+    ell2 = np.logspace(1, 3, 25)
+    sig = np.random.default_rng(3).uniform(0.5, 2.0, (3, 25))
+    noi = np.random.default_rng(4).uniform(0.1, 0.3, (3, 25))
+    out["fixed_ell"] = ell2
+    out["fixed_signal"] = sig
+    out["fixed_noise"] = noi
+    out["fixed_cov_dense"] = jc.angular_cl.gaussian_cl_covariance(
+        ell2, P, sig, noi, f_sky=0.3, sparse=False
+    )
+    out["fixed_cov_sparse"] = jc.angular_cl.gaussian_cl_covariance(
+        ell2, P, sig, noi, f_sky=0.3, sparse=True
+    )
+    return out
+
+
+def make_sparse(jc):
+    rng = np.random.default_rng(11)
+    n, nd = 4, 6
+    # SPD per-diagonal blocks: A_l = B_l B_l^T + n I
+    B = rng.normal(size=(nd, n, n))
+    A = np.einsum("lij,lkj->lik", B, B) + n * np.eye(n)[None]
+    sp = np.transpose(A, (1, 2, 0)).copy()  # (n, n, nd)
+    v = rng.normal(size=n * nd)
+    out = {"sparse": sp, "v": v}
+    out["inv"] = jc.sparse.inv(sp)
+    s, ld = jc.sparse.slogdet(sp)
+    out["sign"], out["logdet"] = np.asarray(s), np.asarray(ld)
+    out["dense"] = jc.sparse.to_dense(sp)
+    out["dot_vec"] = jc.sparse.dot(sp, v)
+    out["vec_dot"] = jc.sparse.dot(v, sp)
+    out["bilinear"] = jc.sparse.dot(v.reshape(1, -1), sp, v.reshape(-1, 1))
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", required=True)
+    ap.add_argument("--procs", type=int, default=os.cpu_count())
+    ap.add_argument("--only", default="")
+    args = ap.parse_args()
+    jc = _setup(args.reference)
+    only = set(args.only.split(",")) if args.only else None
+
+    def want(name):
+        return only is None or name in only
+
+    def save(name, d):
+        np.savez_compressed(os.path.join(HERE, name + ".npz"), **d)
+        print(f"wrote {name}.npz ({time.time() - t0:.1f}s)", flush=True)
+
+    t0 = time.time()
+    if want("background"):
+        save("background", make_background(jc))
+    if want("power"):
+        save("power", make_power(jc))
+    if want("tracers"):
+        save("tracers", make_tracers(jc))
+    if want("cov_like"):
+        save("cov_like", make_cov_like(jc))
+    if want("sparse"):
+        save("sparse", make_sparse(jc))
+    if want("cl_wl2") or want("cl_mixed"):
+        import multiprocessing as mp
+
+        with mp.get_context("spawn").Pool(args.procs) as pool:
+            if want("cl_wl2"):
+                ell = np.logspace(1, np.log10(3000.0), 50)
+                save("cl_wl2", make_cl(args.reference, pool, "wl2", COSMOS[:2], ell))
+            if want("cl_mixed"):
+                ell = np.logspace(1, np.log10(5000.0), 12)
+                save(
+                    "cl_mixed",
+                    make_cl(args.reference, pool, "mixed", COSMOS[[0, 2]], ell),
+                )
+
+
+if __name__ == "__main__":
+    main()
