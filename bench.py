@@ -1,0 +1,379 @@
+"""Benchmark: batched angular power spectra on GB300.
+
+Workload (the batched configuration of the benchmark set): 4096 cosmologies
+drawn from a seeded uniform box (Omega_c in [0.20, 0.35], Omega_b in
+[0.04, 0.06], h in [0.60, 0.80], n_s in [0.90, 1.00], sigma8 in [0.60, 1.00],
+w0 in [-1.3, -0.7], wa = 0, Omega_k = 0), 5 WeakLensing smail_nz bins (a = 1,
+b = 2, z0 = linspace(0.3, 1.5, 5), zmax = 10), 100 log-spaced ell in
+[20, 3000], Limber N = 512.  15 spectra per cosmology, 6.144M C_ell per step.
+
+A step is one angular_cl pass over the whole batch: background tables, halofit
+rows, tracer kernels, Limber integral (fp32c: float32 integrand with
+compensated sums, float64 tables).  ``value`` is C_ell evaluations per second
+with inputs resident in HBM; ``e2e`` is the same through the public API with
+the parameters copied from pinned host memory and the C_ell copied back each
+step.  The plain float64 method is timed on the same workload as
+``fp64_value``.
+
+``--impl reference`` times the CPU reference of the path instead (the float64
+oracle port on the host cores; JAX is not available on the GPU host).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+B_DEFAULT = 4096
+N_ELL = 100
+Z0 = np.linspace(0.3, 1.5, 5)
+SEED = 20261203
+BOX = {
+    "Omega_c": (0.20, 0.35),
+    "Omega_b": (0.04, 0.06),
+    "h": (0.60, 0.80),
+    "n_s": (0.90, 1.00),
+    "sigma8": (0.60, 1.00),
+    "w0": (-1.3, -0.7),
+}
+ORDER = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
+MUFU_PER_NODE = 27  # ex2/lg2/rcp/sin per Limber node in the fp32c integrand
+
+
+def draw_params(B, seed=SEED):
+    rng = np.random.default_rng(seed)
+    P = np.zeros((B, 8))
+    for i, n in enumerate(ORDER):
+        if n in BOX:
+            lo, hi = BOX[n]
+            P[:, i] = rng.uniform(lo, hi, B)
+    return P
+
+
+def ell_grid():
+    return np.logspace(np.log10(20.0), np.log10(3000.0), N_ELL)
+
+
+# ------------------------------------------------------------ CPU baseline --
+def _oracle_worker(rows):
+    import torch
+
+    torch.set_num_threads(1)
+    from oracle import jc_oracle as O
+
+    probes = [O.Probe("wl", [O.Smail(1.0, 2.0, float(z0), 10.0, 10.0) for z0 in Z0], sigma_e=0.26)]
+    ell = ell_grid()
+    for r in rows:
+        O.angular_cl(O.Cosmo.from_vector(r), ell, probes, n_limber=512)
+    return len(rows)
+
+
+def cpu_baseline(params, budget_s=12.0, procs=None):
+    """Oracle port on the host cores, spawn pool, bounded to ~budget_s."""
+    import multiprocessing as mp
+
+    procs = procs or os.cpu_count() or 1
+    ctx = mp.get_context("spawn")
+    n_cls = 15
+    with ctx.Pool(procs) as pool:
+        # warm-up: imports and first call in every worker
+        pool.map(_oracle_worker, [[params[i % len(params)]] for i in range(procs)])
+        done, t0, k = 0, time.perf_counter(), 0
+        while time.perf_counter() - t0 < budget_s:
+            chunk = [[params[(k + i) % len(params)]] for i in range(procs)]
+            k += procs
+            done += sum(pool.map(_oracle_worker, chunk))
+        dt = time.perf_counter() - t0
+    return {
+        "value": done * n_cls * N_ELL / dt,
+        "unit": "C_ell/s",
+        "cores": procs,
+        "kind": "port",
+        "sample": f"{done} cosmologies of the workload (float64 oracle, one process per core), {dt:.1f} s",
+    }
+
+
+# ------------------------------------------------------------------ clocks --
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.dev = device_index
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def start(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                                "sw_power_cap"], f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(smax)),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# --------------------------------------------------------------- GPU arm ----
+def gpu_arm(args, rank, world, device):
+    import torch
+
+    import jax_cosmo_gb300 as jc
+    from jax_cosmo_gb300 import _geometry, _lib
+    from jax_cosmo_gb300.angular_cl import angular_cl_device
+
+    B = args.batch
+    P = draw_params(B, SEED + rank)
+    nz = [jc.redshift.smail_nz(1.0, 2.0, float(z0), gals_per_arcmin2=10.0) for z0 in Z0]
+    probes = [jc.probes.WeakLensing(nz, sigma_e=0.26)]
+    ell_np = ell_grid()
+    params = torch.as_tensor(P, device=device).contiguous()
+    n_cls, n_ell = 15, N_ELL
+    cl = torch.empty(B, n_cls, n_ell, dtype=torch.float64, device=device)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=device)  # > L2 (126 MB)
+    stream = torch.cuda.current_stream(device)
+
+    def step(prec):
+        angular_cl_device(params, ell_np, probes, prec, 512, out=cl)
+
+    def timed(fn, K, W):
+        for _ in range(W):
+            fn()
+        torch.cuda.synchronize(device)
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize(device)
+        times = []
+        for _ in range(K):
+            flush.fill_(1.0)  # evict L2 between timed iterations (not timed)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+        torch.cuda.synchronize(device)
+        return float(np.sum(times)), times
+
+    # headline: fp32c, inputs resident
+    clocks = ClockSampler(device.index)
+    clocks.start()
+    t_fast, per = timed(lambda: step("fp32c"), args.steps, args.warmup)
+    clk = clocks.stop()
+    # plain float64 method on the same workload (fewer steps: it is ~100x slower)
+    t64, per64 = timed(lambda: step("fp64"), max(1, min(args.steps, 2)), 1)
+    # e2e through the public API: pinned host params in, C_ell out
+    host_p = torch.as_tensor(P).pin_memory()
+    host_cl = torch.empty(B, n_cls, n_ell, dtype=torch.float64).pin_memory()
+    cosmo_cols = None
+
+    def e2e_step():
+        dev_p = host_p.to(device, non_blocking=True)
+        cosmo = jc.Cosmology(*[dev_p[:, i] for i in range(8)])
+        out = jc.cl.angular_cl(cosmo, ell_np, probes, precision="fp32c")
+        host_cl.copy_(out, non_blocking=True)
+
+    t_e2e, _ = timed(e2e_step, args.steps, args.warmup)
+    # Limber kernel alone (the dominant kernel) for the roofline, same stream
+    g, geo, _ = _geometry.get_geometry(probes, ell_np, 512, device)
+    import ctypes
+
+    wsz = ctypes.c_size_t()
+    _lib.call("jcg_workspace_size", ctypes.byref(g), B, _lib.FP32C, ctypes.byref(wsz))
+    ws = _lib.workspace(wsz.value, device)
+    st = _lib.stream_of(device)
+    args_common = (ctypes.byref(g), _lib.ptr(geo), _lib.ptr(params), B, _lib.FP32C)
+    _lib.call("jcg_stage_cosmo_tables", ctypes.byref(g), _lib.ptr(params), B, _lib.FP32C,
+              _lib.ptr(ws), ctypes.c_size_t(ws.numel()), st)
+    _lib.call("jcg_stage_halofit_rows", *args_common, _lib.ptr(ws), ctypes.c_size_t(ws.numel()), st)
+    _lib.call("jcg_stage_tracer_kernels", *args_common, _lib.ptr(ws), ctypes.c_size_t(ws.numel()), st)
+    t_limber, per_l = timed(
+        lambda: _lib.call("jcg_stage_limber", *args_common, _lib.ptr(cl), _lib.ptr(ws),
+                          ctypes.c_size_t(ws.numel()), st), args.steps, args.warmup)
+    ms_limber = t_limber / args.steps
+    stages = {}
+    for name in ("jcg_stage_cosmo_tables", "jcg_stage_halofit_rows", "jcg_stage_tracer_kernels"):
+        if name == "jcg_stage_cosmo_tables":
+            fn = lambda: _lib.call(name, ctypes.byref(g), _lib.ptr(params), B, _lib.FP32C,
+                                   _lib.ptr(ws), ctypes.c_size_t(ws.numel()), st)
+        else:
+            fn = lambda n=name: _lib.call(n, *args_common, _lib.ptr(ws), ctypes.c_size_t(ws.numel()), st)
+        t, _ = timed(fn, args.steps, 1)
+        stages[name.replace("jcg_stage_", "")] = t / args.steps
+    stages["limber"] = ms_limber
+
+    # max over ranks
+    def allmax(x):
+        if world == 1:
+            return x
+        tt = torch.tensor([x], dtype=torch.float64, device=device)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        return float(tt.item())
+
+    t_fast, t64, t_e2e = allmax(t_fast), allmax(t64), allmax(t_e2e)
+    ncl_step = B * n_cls * n_ell
+    K = args.steps
+    res = {
+        "t_fast": t_fast, "t64": t64, "n64": len(per64), "t_e2e": t_e2e, "K": K,
+        "ncl_step": ncl_step, "clocks": clk, "stages_ms": stages, "ms_limber": ms_limber,
+        "h2d": int(host_p.numel() * 8), "d2h": int(host_cl.numel() * 8),
+        "sm_count": torch.cuda.get_device_properties(device).multi_processor_count,
+    }
+    # sanity: the fp32c result vs fp64 on this workload
+    step("fp64")
+    c64 = cl.clone()
+    step("fp32c")
+    res["fp32c_max_rel_err_vs_fp64"] = float(((cl - c64).abs() / c64.abs()).max())
+    return res
+
+
+def roofline(res, B):
+    """Algorithmic bytes of the Limber launch vs measured HBM peak; SFU issue beside it."""
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    na, n_tr, n_cls, n_ell = 513, 5, 15, N_ELL
+    # rows32 (16 f32) + R_U (f64) + radial kernels (f64) per node, C_ell out (f64)
+    bytes_launch = B * (na * (16 * 4 + 8) + n_tr * na * 8) + B * n_cls * n_ell * 8
+    t = res["ms_limber"] * 1e-3
+    ach = bytes_launch / t / 1e9
+    nodes = B * n_ell * na
+    clk = (res.get("clocks") or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
+    sfu_peak = res["sm_count"] * 16 * clk * 1e6  # MUFU ops/s: 16 per SM per clock
+    sfu_ach = nodes * MUFU_PER_NODE / t
+    return (
+        {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+         "traffic": None, "kernel": "limber_kernel<fp32c>", "bytes_per_launch": bytes_launch,
+         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
+        {"bound": "sfu", "achieved": sfu_ach / 1e9, "peak": sfu_peak / 1e9, "unit": "GMUFU/s",
+         "frac": sfu_ach / sfu_peak, "nodes_per_launch": nodes, "mufu_per_node": MUFU_PER_NODE,
+         "clock_mhz": clk},
+    )
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=B_DEFAULT)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    config = {"workload": "batched angular_cl: 4096 cosmologies x 5 WL bins x 100 ell (15 spectra), N=512",
+              "n_cosmo_per_gpu": args.batch, "n_tracers": 5, "n_cls": 15, "n_ell": N_ELL,
+              "n_limber": 512, "ell_range": [20, 3000], "seed": SEED,
+              "l2": "flushed (256 MB write) between timed steps", "parallelism": f"replicas x{args.gpus}"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        P = draw_params(args.batch)
+        vals = []
+        for _ in range(args.warmup):
+            cpu_baseline(P, budget_s=2.0)
+        cb = None
+        for _ in range(args.steps):
+            cb = cpu_baseline(P, budget_s=max(3.0, 30.0 / max(args.steps, 1)))
+            vals.append(cb["value"])
+        v = float(np.median(vals))
+        print(json.dumps({
+            "impl": "reference", "metric": "C_ell evals/s (batched angular_cl)", "value": v,
+            "unit": "C_ell/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config,
+            "cpu_baseline": {**cb, "value": v},
+            "e2e": {"value": v, "unit": "C_ell/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "reference JAX CPU path unavailable on this host (no jax); the float64 oracle "
+                    "port of the path is timed with one process per core",
+        }))
+        return
+
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        # spawn pool before the first CUDA call
+        cb = cpu_baseline(draw_params(args.batch), budget_s=12.0)
+
+    import torch
+
+    if world > 1:
+        torch.distributed.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    res = gpu_arm(args, rank, world, device)
+    if rank != 0:
+        return
+    K = res["K"]
+    ms = res["t_fast"] / K
+    value = res["ncl_step"] * world / (ms * 1e-3)
+    fp64_value = res["ncl_step"] * world / (res["t64"] / res["n64"] * 1e-3)
+    e2e = res["ncl_step"] * world / (res["t_e2e"] / K * 1e-3)
+    rl, rl_sfu = roofline(res, args.batch)
+    out = {
+        "metric": "C_ell evals/s (batched angular_cl, fp32c at <=1e-4 rel err vs fp64)",
+        "value": value, "unit": "C_ell/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
+        "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32c+f64", "data": "synthetic", "config": config,
+        "fp64_value": fp64_value, "fp32c_over_fp64": value / fp64_value,
+        "fp32c_max_rel_err_vs_fp64": res["fp32c_max_rel_err_vs_fp64"],
+        "cosmologies_per_s": value / 1500.0,
+        "e2e": {"value": e2e, "unit": "C_ell/s", "h2d_bytes_per_step": res["h2d"],
+                "d2h_bytes_per_step": res["d2h"]},
+        "gpu_launches": 4 * K,
+        "stage_ms": res["stages_ms"],
+        "roofline": rl, "roofline_sfu": rl_sfu,
+        "clocks": res["clocks"],
+        "cpu_baseline": cb,
+    }
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,214 @@
+/* libjcg — GB300-native angular power spectra with jax_cosmo's semantics.
+ *
+ * C ABI of the CUDA library behind jax_cosmo_gb300.  Every entry point:
+ *   - takes caller-owned DEVICE pointers (the library never frees them) and a
+ *     cudaStream_t, and is asynchronous on that stream (no host synchronisation
+ *     unless stated);
+ *   - returns 0 (JCG_OK) or a negative JCG_ERR_* code, never aborts; the text of
+ *     the last error of the calling thread is in jcg_last_error_string();
+ *   - validates shapes, parameter values and workspace sizes on the host before
+ *     launching anything.
+ *
+ * Reference citations are paths in the jax_cosmo project (DifferentiableUniverse
+ * Initiative/jax_cosmo), file:line.
+ *
+ * Layout conventions
+ *   params  [n_cosmo][8] float64: Omega_c, Omega_b, h, n_s, sigma8, Omega_k, w0, wa
+ *           (the pytree leaves of Cosmology, core.py:98-108)
+ *   cl      [n_cosmo][n_cls][n_ell] float64, pairs (i <= j) in the order of
+ *           angular_cl._get_cl_ordering (angular_cl.py:15-25)
+ *   sparse covariance [n_cls][n_cls][n_ell] float64 (sparse.py:1-11 format)
+ *   dense covariance  [n_cls*n_ell][n_cls*n_ell] float64, index p*n_ell + l
+ *           (angular_cl.py:158-162)
+ */
+#ifndef JCG_H
+#define JCG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#include <cuda_runtime.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define JCG_ABI_VERSION 1
+#define JCG_MAX_TRACERS 16
+#define JCG_MAX_PAIRS (JCG_MAX_TRACERS * (JCG_MAX_TRACERS + 1) / 2)
+#define JCG_MAX_ELL 4096
+#define JCG_MAX_LIMBER 4096
+
+/* status codes */
+#define JCG_OK 0
+#define JCG_ERR_ARG -1         /* null pointer, bad enum, bad count */
+#define JCG_ERR_SHAPE -2       /* inconsistent sizes */
+#define JCG_ERR_ODD_N -3       /* Simpson rule needs an even N (scipy/integrate.py:193) */
+#define JCG_ERR_VALUE -4       /* NaN / out-of-domain parameter */
+#define JCG_ERR_WORKSPACE -5   /* workspace or geometry buffer too small */
+#define JCG_ERR_CUDA -6        /* a CUDA call failed */
+#define JCG_ERR_UNSUPPORTED -7 /* option the reference also rejects (NotImplementedError) */
+#define JCG_ERR_TIMEOUT -8     /* a bounded device wait gave up */
+#define JCG_ERR_ABI -9         /* descriptor abi_version mismatch */
+
+/* tracer kinds: probes.WeakLensing (probes.py:132) / probes.NumberCounts (probes.py:226) */
+#define JCG_TRACER_WL 0
+#define JCG_TRACER_NC 1
+
+/* arithmetic of the Limber stage */
+#define JCG_FP64 0  /* plain: float64 everywhere */
+#define JCG_FP32C 1 /* float32 Limber integrand + compensated Simpson sums, float64 tables */
+
+/* One request's tracers and grids (cosmology independent).
+ * Replaces the probe/redshift containers consumed by angular_cl
+ * (probes.py:132-281, redshift.py:15-77, bias.py:10-22). */
+typedef struct jcg_geometry {
+  int abi_version;     /* = JCG_ABI_VERSION */
+  int n_tracers;       /* total redshift bins over all probes, <= JCG_MAX_TRACERS */
+  int n_ell;           /* <= JCG_MAX_ELL */
+  int n_limber;        /* Simpson intervals in a (angular_cl.py:96 uses 512); even */
+  int n_nodes;         /* 0: Limber grid; > 0: that many caller redshift nodes
+                          (jcg_geometry_build_nodes), n_limber ignored */
+  double zmax;         /* max over probes of probe zmax (angular_cl.py:63) */
+  int kind[JCG_MAX_TRACERS];          /* JCG_TRACER_* */
+  double nz_a[JCG_MAX_TRACERS];       /* smail_nz a, b, z0 (redshift.py:75-77) */
+  double nz_b[JCG_MAX_TRACERS];
+  double nz_z0[JCG_MAX_TRACERS];
+  double nz_zmax[JCG_MAX_TRACERS];    /* n(z) normalisation range (redshift.py:30) */
+  double probe_zmax[JCG_MAX_TRACERS]; /* lensing integral upper limit (probes.py:25) */
+  double bias[JCG_MAX_TRACERS];       /* NumberCounts constant_linear_bias b (bias.py:21) */
+  double mult[JCG_MAX_TRACERS];       /* WeakLensing multiplicative bias m (probes.py:207) */
+  double noise[JCG_MAX_TRACERS];      /* per-bin noise power (probes.py:210-223, 274-281) */
+} jcg_geometry;
+
+/* ------------------------------------------------------------- misc ---- */
+int jcg_abi_version(void);
+const char* jcg_last_error_string(void);
+
+/* -------------------------------------------------------- geometry ---- */
+/* Size in bytes of the cosmology-independent geometry buffer for g. */
+int jcg_geometry_size(const jcg_geometry* g, size_t* bytes);
+
+/* Build the geometry buffer: Limber nodes in a (angular_cl.py:96), n(z)
+ * normalisation (redshift.py:27-31), n(z) on the Limber and lensing grids
+ * (probes.py:44-51, 87), interpolation segments of every table lookup
+ * (scipy/interpolate.py:34-59), WeakLensing ell factors (probes.py:73).
+ * ell_dev: [n_ell] float64 device array. */
+int jcg_geometry_build(const jcg_geometry* g, const double* ell_dev, void* geo_dev,
+                       size_t geo_bytes, cudaStream_t stream);
+
+/* Same tables on caller-given redshift nodes z_dev [g->n_nodes] instead of the
+ * Limber grid: the radial kernels of probes.WeakLensing.kernel /
+ * NumberCounts.kernel at arbitrary z (probes.py:188-208, 260-272).  Only the
+ * cosmology-table and tracer-kernel stages are meaningful on such a geometry;
+ * jcg_geometry_size covers it. */
+int jcg_geometry_build_nodes(const jcg_geometry* g, const double* ell_dev, const double* z_dev,
+                             void* geo_dev, size_t geo_bytes, cudaStream_t stream);
+
+/* ------------------------------------------------------ angular_cl ---- */
+/* Workspace bytes for n_cosmo cosmologies on geometry g. */
+int jcg_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t* bytes);
+
+/* C_ell of n_cosmo cosmologies sharing one geometry, one fused pipeline:
+ * background tables -> halofit rows -> tracer kernels -> Limber integral.
+ * Replaces angular_cl.angular_cl (angular_cl.py:49-98) with the default
+ * transfer_fn = Eisenstein_Hu (transfer.py:10) and nonlinear_fn = halofit
+ * takahashi2012 (power.py:144).  cl_dev: [n_cosmo][n_cls][n_ell]. */
+int jcg_angular_cl(const jcg_geometry* g, const void* geo_dev, const double* params_dev,
+                   int n_cosmo, int precision, double* cl_dev, void* workspace,
+                   size_t workspace_bytes, cudaStream_t stream);
+
+/* Stage entry points of the same pipeline (for tests and for callers that keep
+ * tables resident).  The workspace is the one of jcg_angular_cl. */
+int jcg_stage_cosmo_tables(const jcg_geometry* g, const double* params_dev, int n_cosmo,
+                           int precision, void* workspace, size_t workspace_bytes,
+                           cudaStream_t stream);
+int jcg_stage_halofit_rows(const jcg_geometry* g, const void* geo_dev, const double* params_dev,
+                           int n_cosmo, int precision, void* workspace, size_t workspace_bytes,
+                           cudaStream_t stream);
+int jcg_stage_tracer_kernels(const jcg_geometry* g, const void* geo_dev, const double* params_dev,
+                             int n_cosmo, int precision, void* workspace, size_t workspace_bytes,
+                             cudaStream_t stream);
+int jcg_stage_limber(const jcg_geometry* g, const void* geo_dev, const double* params_dev,
+                     int n_cosmo, int precision, double* cl_dev, void* workspace,
+                     size_t workspace_bytes, cudaStream_t stream);
+
+/* Copy stage outputs for cosmology `index` out of a workspace (device to device).
+ * what: 0 chi table [256], 1 growth table [128], 2 scalars [32],
+ *       3 halofit rows [na][24] (FP64), 4 radial kernels [n_tracers][na]. */
+int jcg_workspace_read(const jcg_geometry* g, int n_cosmo, int precision, const void* workspace,
+                       int index, int what, double* out_dev, size_t out_count,
+                       cudaStream_t stream);
+
+/* Pointwise table functions at n (k, a) points for n_cosmo cosmologies
+ * (out [n_cosmo][n]).  what:
+ *   0 radial_comoving_distance(a)   background.py:199-242
+ *   1 growth_factor(a)              background.py:371-398
+ *   2 H(a)                          background.py:129-142
+ *   3 dchioverda(a)                 background.py:270-294
+ *   4 Eisenstein_Hu(k)              transfer.py:10-156
+ *   5 linear_matter_power(k, a)     power.py:21-53
+ *   6 nonlinear_matter_power(k, a)  power.py:265-272 (halofit)
+ *   7 k_nl(a)  8 n_eff(a)  9 C(a)   power.py:86-141
+ * Needs a workspace of jcg_workspace_size(g=NULL -> tables only). */
+int jcg_eval_points(const double* params_dev, int n_cosmo, const double* a_dev,
+                    const double* k_dev, int n, int what, double* out_dev, void* workspace,
+                    size_t workspace_bytes, cudaStream_t stream);
+int jcg_eval_workspace_size(int n_cosmo, size_t* bytes);
+
+/* -------------------------------------------------- covariance ---------- */
+/* Gaussian covariance of n_cosmo C_ell sets: angular_cl.py:120-163.
+ * ell_dev [n_ell] (n_ell >= 2, np.gradient), cl_signal_dev [n_cosmo][n_cls][n_ell]
+ * with n_cls = n_tracers (n_tracers + 1) / 2.  The noise added to the signal is
+ * cl_noise_dev [n_cls][n_ell] when given (shared by all cosmologies), else the
+ * auto-spectrum noise of noise_cl (angular_cl.py:101-117) built from
+ * tracer_noise_dev [n_tracers] when given, else zero.
+ * sparse != 0: out [n_cosmo][n_cls][n_cls][n_ell]; else dense
+ * [n_cosmo][N][N], N = n_cls*n_ell. */
+int jcg_gaussian_covariance(const double* ell_dev, int n_ell, int n_tracers,
+                            const double* cl_signal_dev, const double* cl_noise_dev,
+                            const double* tracer_noise_dev, int n_cosmo, double f_sky, int sparse,
+                            double* out_dev, cudaStream_t stream);
+
+/* Gaussian log-likelihood with a covariance in the sparse block format
+ * (likelihood.py:9-61; sparse.py:295-366): per-ell blocks factored by
+ * Cholesky in float64.  data/mu [n_cosmo][n_cls*n_ell] (p*n_ell + l),
+ * cov [n_cosmo][n_cls][n_cls][n_ell]; out [n_cosmo].  Returns
+ * -0.5 * (r^T C^-1 r - logdet) when include_logdet, as likelihood.py:61.
+ * status_dev [n_cosmo] (may be NULL): 0 ok, 2 a block is not positive
+ * definite (out = NaN). */
+int jcg_gaussian_loglike_sparse(const double* data_dev, const double* mu_dev, const double* cov_dev,
+                                int n_cosmo, int n_cls, int n_ell, int include_logdet,
+                                double* out_dev, int* status_dev, void* workspace,
+                                size_t workspace_bytes, cudaStream_t stream);
+int jcg_loglike_workspace_size(int n_cosmo, int n_cls, int n_ell, size_t* bytes);
+
+/* Dense covariance [n_cosmo][N][N], N = n_cls*n_ell, in the layout of
+ * angular_cl.py:158-162.  A device pass checks that every n_ell x n_ell block
+ * is diagonal; such matrices are factored per ell like the sparse form (the
+ * same value as likelihood.py:242-248 for either inverse_method, up to
+ * rounding).  status_dev [n_cosmo]: 0 ok, 1 not block-diagonal in ell
+ * (out = NaN: factor it densely instead), 2 not positive definite. */
+int jcg_gaussian_loglike_dense(const double* data_dev, const double* mu_dev, const double* cov_dev,
+                               int n_cosmo, int n_cls, int n_ell, int include_logdet,
+                               double* out_dev, int* status_dev, void* workspace,
+                               size_t workspace_bytes, cudaStream_t stream);
+
+/* sparse.inv / sparse.slogdet of (n, n, ndiag) block-diagonal matrices
+ * (sparse.py:295-366), float64, one matrix. */
+int jcg_sparse_inv(const double* sparse_dev, int n, int ndiag, double* out_dev, cudaStream_t stream);
+/* work_dev: 2*ndiag float64 of caller-owned scratch (per-diagonal partials). */
+int jcg_sparse_slogdet(const double* sparse_dev, int n, int ndiag, double* sign_dev,
+                       double* logdet_dev, double* work_dev, cudaStream_t stream);
+/* sparse.to_dense (sparse.py:52-68): (n, m, d) -> (n*d, m*d). */
+int jcg_sparse_to_dense(const double* sparse_dev, int n, int m, int ndiag, double* out_dev,
+                        cudaStream_t stream);
+/* sparse.dot(A, v) / sparse.dot(v, A) for sparse A (n, m, d) (sparse.py:71-137). */
+int jcg_sparse_dot_vec(const double* sparse_dev, int n, int m, int ndiag, const double* v_dev,
+                       int transpose, double* out_dev, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JCG_H */

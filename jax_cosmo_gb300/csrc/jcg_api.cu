@@ -1,0 +1,531 @@
+// extern "C" entry points of libjcg: validation, buffer layouts, launches.
+//
+// Every function validates on the host, launches asynchronously on the given
+// stream and returns a JCG_* status; nothing here aborts.  The error text of the
+// last failure of the calling thread is kept in a thread-local buffer.
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "jcg_internal.cuh"
+
+namespace jcg {
+void launch_covariance(const double* ell, int n_ell, int n_tr, const double* cl,
+                       const double* cl_noise, const double* tr_noise, int n_cosmo, double f_sky,
+                       int sparse, double* out, cudaStream_t st);
+void launch_loglike(const double* data, const double* mu, const double* cov, int n_cosmo, int n_cls,
+                    int n_ell, int include_logdet, int dense, double* out, int* status,
+                    double* partial, int* structure, cudaStream_t st);
+void launch_sparse_inv(const double* sp, int n, int nd, double* out, cudaStream_t st);
+void launch_sparse_slogdet(const double* sp, int n, int nd, double* sign_part, double* ld_part,
+                           double* sign_out, double* ld_out, cudaStream_t st);
+void launch_sparse_to_dense(const double* sp, int n, int m, int nd, double* out, cudaStream_t st);
+void launch_sparse_dot_vec(const double* sp, int n, int m, int nd, const double* v, int transpose,
+                           double* out, cudaStream_t st);
+}  // namespace jcg
+
+using namespace jcg;
+
+// ------------------------------------------------------------- errors -------
+static thread_local char g_err[512] = "";
+
+static int fail(int code, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+  return code;
+}
+
+static int cuda_check(const char* what) {
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return fail(JCG_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+  return JCG_OK;
+}
+
+// --------------------------------------------------- device constants -------
+// One set of constant grids per device, in static device memory (no allocation).
+static __device__ ConstTables g_const;
+static std::mutex g_init_mu;
+static bool g_init_done[64];
+static ConstTables* g_const_ptr[64];
+
+static int const_tables(ConstTables** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(JCG_ERR_CUDA, "cudaGetDevice failed");
+  if (dev < 0 || dev >= 64) return fail(JCG_ERR_CUDA, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_init_mu);
+  if (!g_init_done[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_const);
+    if (e != cudaSuccess) return fail(JCG_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    ConstTables* c = static_cast<ConstTables*>(p);
+    cudaStream_t s;
+    e = cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking);
+    if (e != cudaSuccess) return fail(JCG_ERR_CUDA, "cudaStreamCreate: %s", cudaGetErrorString(e));
+    launch_const_init(c, s);
+    e = cudaStreamSynchronize(s);
+    cudaStreamDestroy(s);
+    if (e != cudaSuccess) return fail(JCG_ERR_CUDA, "constant tables: %s", cudaGetErrorString(e));
+    g_const_ptr[dev] = c;
+    g_init_done[dev] = true;
+  }
+  *out = g_const_ptr[dev];
+  return JCG_OK;
+}
+
+// ----------------------------------------------------------- geometry -------
+static int64_t align8(int64_t v) { return (v + 7) & ~int64_t(7); }  // 64-byte units
+
+static int make_header(const jcg_geometry* g, GeoHeader* h) {
+  const int n_nodes = g ? g->n_nodes : 0;
+  if (!g) return fail(JCG_ERR_ARG, "geometry is NULL");
+  if (g->abi_version != JCG_ABI_VERSION)
+    return fail(JCG_ERR_ABI, "geometry abi_version %d, library %d", g->abi_version, JCG_ABI_VERSION);
+  if (g->n_tracers < 1 || g->n_tracers > JCG_MAX_TRACERS)
+    return fail(JCG_ERR_SHAPE, "n_tracers = %d (1..%d)", g->n_tracers, JCG_MAX_TRACERS);
+  if (g->n_ell < 1 || g->n_ell > JCG_MAX_ELL)
+    return fail(JCG_ERR_SHAPE, "n_ell = %d (1..%d)", g->n_ell, JCG_MAX_ELL);
+  if (n_nodes == 0) {
+    if (g->n_limber < 2 || g->n_limber > JCG_MAX_LIMBER)
+      return fail(JCG_ERR_SHAPE, "n_limber = %d (2..%d)", g->n_limber, JCG_MAX_LIMBER);
+    if (g->n_limber % 2 == 1)
+      return fail(JCG_ERR_ODD_N, "N must be an even integer (n_limber = %d)", g->n_limber);
+  } else if (n_nodes < 0 || n_nodes > 1 << 20) {
+    return fail(JCG_ERR_SHAPE, "n_z = %d", n_nodes);
+  }
+  if (!(g->zmax > 0.0) || !isfinite(g->zmax)) return fail(JCG_ERR_VALUE, "zmax = %g", g->zmax);
+  memset(h, 0, sizeof(*h));
+  h->magic = GEO_MAGIC;
+  h->n_tr = g->n_tracers;
+  h->n_ell = g->n_ell;
+  h->n_limber = n_nodes ? 0 : g->n_limber;
+  h->na = n_nodes ? n_nodes : g->n_limber + 1;
+  h->custom_nodes = n_nodes ? 1 : 0;
+  h->zmax = g->zmax;
+  h->dx_limber = n_nodes ? 0.0 : (1.0 - 1.0 / (1.0 + g->zmax)) / g->n_limber;
+  double zmx = 0.0;
+  for (int t = 0; t < g->n_tracers; ++t) {
+    const int k = g->kind[t];
+    if (k != JCG_TRACER_WL && k != JCG_TRACER_NC) return fail(JCG_ERR_ARG, "tracer %d: kind %d", t, k);
+    const double vals[] = {g->nz_a[t], g->nz_b[t], g->nz_z0[t], g->nz_zmax[t], g->bias[t], g->mult[t], g->noise[t]};
+    for (double v : vals)
+      if (!isfinite(v)) return fail(JCG_ERR_VALUE, "tracer %d has a non-finite parameter", t);
+    if (!(g->nz_z0[t] > 0.0)) return fail(JCG_ERR_VALUE, "tracer %d: z0 = %g", t, g->nz_z0[t]);
+    if (!(g->nz_zmax[t] > 0.0)) return fail(JCG_ERR_VALUE, "tracer %d: zmax = %g", t, g->nz_zmax[t]);
+    h->kind[t] = k;
+    h->nz_a[t] = g->nz_a[t];
+    h->nz_b[t] = g->nz_b[t];
+    h->nz_z0[t] = g->nz_z0[t];
+    h->nz_zmax[t] = g->nz_zmax[t];
+    h->bias[t] = g->bias[t];
+    h->mult[t] = g->mult[t];
+    h->noise[t] = g->noise[t];
+    h->probe_zmax[t] = g->probe_zmax[t];
+    if (k == JCG_TRACER_WL) {
+      h->n_wl++;
+      const double pz = g->probe_zmax[t];
+      if (!(pz > 0.0) || !isfinite(pz)) return fail(JCG_ERR_VALUE, "tracer %d: probe_zmax = %g", t, pz);
+      int grp = -1;
+      for (int q = 0; q < h->n_groups; ++q)
+        if (h->group_zmax[q] == pz) grp = q;
+      if (grp < 0) {
+        grp = h->n_groups++;
+        h->group_zmax[grp] = pz;
+      }
+      h->group[t] = grp;
+      if (pz > zmx) zmx = pz;
+    } else {
+      h->n_nc++;
+      h->group[t] = -1;
+    }
+  }
+  int p = 0;
+  for (int i = 0; i < h->n_tr; ++i)
+    for (int j = i; j < h->n_tr; ++j) {
+      h->pair_i[p] = i;
+      h->pair_j[p] = j;
+      ++p;
+    }
+  h->n_cls = p;
+  // offsets (8-byte units), sections aligned to 64 bytes
+  const int na = h->na;
+  int64_t o = align8((int64_t)((sizeof(GeoHeader) + 7) / 8));
+  auto take = [&](int64_t n) {
+    const int64_t r = o;
+    o = align8(o + n);
+    return r;
+  };
+  h->off_a = take(na);
+  h->off_z = take(na);
+  h->off_wsimp = take(na);
+  h->off_awl = take(na);
+  h->off_seg_chi = take(na);
+  h->off_seg_grow = take(na);
+  h->off_seg_chiwl = take(na);
+  h->off_nzl = take((int64_t)h->n_tr * na);
+  h->off_ell = take(h->n_ell);
+  h->off_ellfac = take((int64_t)h->n_tr * h->n_ell);
+  h->off_lg2ellh = take(h->n_ell);
+  for (int q = 0; q < h->n_groups; ++q) {
+    h->off_ap[q] = take((int64_t)na * NZP);
+    h->off_segp[q] = take((int64_t)na * NZP);
+  }
+  for (int t = 0; t < h->n_tr; ++t)
+    if (h->kind[t] == JCG_TRACER_WL) h->off_W[t] = take((int64_t)na * NZP);
+  h->total = o;
+  (void)zmx;
+  return JCG_OK;
+}
+
+// ---------------------------------------------------------- workspace -------
+struct WsLayout {
+  size_t ctab, rows64, rows32, kern, total;
+};
+
+static size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
+
+static WsLayout ws_layout(const GeoHeader* h, int n_cosmo, int precision) {
+  WsLayout L;
+  size_t o = 0;
+  L.ctab = o;
+  o = align256(o + sizeof(CosmoTab) * (size_t)n_cosmo);
+  const size_t na = h ? (size_t)h->na : 0;
+  const size_t ntr = h ? (size_t)h->n_tr : 0;
+  L.rows64 = o;
+  o = align256(o + sizeof(double) * NROW64 * na * n_cosmo);
+  L.rows32 = o;
+  if (precision == JCG_FP32C) o = align256(o + sizeof(float) * NROW32 * na * n_cosmo);
+  L.kern = o;
+  o = align256(o + sizeof(double) * ntr * na * n_cosmo);
+  L.total = o;
+  return L;
+}
+
+static int check_common(const double* params, int n_cosmo, int precision, const void* ws,
+                        size_t ws_bytes, size_t need) {
+  if (!params) return fail(JCG_ERR_ARG, "params is NULL");
+  if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  if (precision != JCG_FP64 && precision != JCG_FP32C) return fail(JCG_ERR_ARG, "precision = %d", precision);
+  if (!ws) return fail(JCG_ERR_ARG, "workspace is NULL");
+  if (ws_bytes < need) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need);
+  if (((uintptr_t)ws) % 256 != 0) return fail(JCG_ERR_ARG, "workspace must be 256-byte aligned");
+  return JCG_OK;
+}
+
+static Batch make_batch(const GeoHeader* h, const void* geo, const double* params, int n_cosmo,
+                        int precision, void* ws, double* cl) {
+  const WsLayout L = ws_layout(h, n_cosmo, precision);
+  char* base = static_cast<char*>(ws);
+  Batch b;
+  memset(&b, 0, sizeof(b));
+  b.n_items = n_cosmo;
+  b.listed = 0;
+  b.items = nullptr;
+  b.params = params;
+  b.geo = static_cast<const GeoHeader*>(geo);
+  b.ctab = reinterpret_cast<CosmoTab*>(base + L.ctab);
+  b.rows64 = reinterpret_cast<double*>(base + L.rows64);
+  b.rows32 = precision == JCG_FP32C ? reinterpret_cast<float*>(base + L.rows32) : nullptr;
+  b.kern = reinterpret_cast<double*>(base + L.kern);
+  b.cl = cl;
+  b.precision = precision;
+  b.max_na = h ? h->na : 0;
+  b.max_ell = h ? h->n_ell : 0;
+  b.max_cls = h ? h->n_cls : 0;
+  b.max_tr = h ? h->n_tr : 0;
+  return b;
+}
+
+static int limber_tile(int n_ell) {
+  const int tiles = (n_ell + 31) / 32;
+  return (n_ell + tiles - 1) / tiles;
+}
+
+// --------------------------------------------------------------- C ABI ------
+extern "C" {
+
+int jcg_abi_version(void) { return JCG_ABI_VERSION; }
+
+const char* jcg_last_error_string(void) { return g_err; }
+
+int jcg_geometry_size(const jcg_geometry* g, size_t* bytes) {
+  if (!bytes) return fail(JCG_ERR_ARG, "bytes is NULL");
+  GeoHeader h;
+  const int rc = make_header(g, &h);
+  if (rc) return rc;
+  *bytes = (size_t)h.total * 8;
+  return JCG_OK;
+}
+
+int jcg_geometry_build(const jcg_geometry* g, const double* ell_dev, void* geo_dev, size_t geo_bytes,
+                       cudaStream_t stream) {
+  GeoHeader h;
+  int rc = make_header(g, &h);
+  if (rc) return rc;
+  if (h.custom_nodes) return fail(JCG_ERR_ARG, "n_nodes > 0: use jcg_geometry_build_nodes");
+  if (!ell_dev || !geo_dev) return fail(JCG_ERR_ARG, "ell or geometry buffer is NULL");
+  if (geo_bytes < (size_t)h.total * 8)
+    return fail(JCG_ERR_WORKSPACE, "geometry buffer %zu bytes, need %zu", geo_bytes, (size_t)h.total * 8);
+  if (((uintptr_t)geo_dev) % 64 != 0) return fail(JCG_ERR_ARG, "geometry buffer must be 64-byte aligned");
+  ConstTables* c = nullptr;
+  if ((rc = const_tables(&c))) return rc;
+  double* geo = static_cast<double*>(geo_dev);
+  if (cudaMemcpyAsync(geo + h.off_ell, ell_dev, sizeof(double) * h.n_ell, cudaMemcpyDeviceToDevice,
+                      stream) != cudaSuccess)
+    return cuda_check("copy ell");
+  launch_geometry_build(h, geo, c, stream);
+  return cuda_check("geometry build");
+}
+
+int jcg_geometry_build_nodes(const jcg_geometry* g, const double* ell_dev, const double* z_dev,
+                             void* geo_dev, size_t geo_bytes, cudaStream_t stream) {
+  GeoHeader h;
+  if (!g || g->n_nodes < 1) return fail(JCG_ERR_SHAPE, "geometry n_nodes must be > 0");
+  const int n_z = g->n_nodes;
+  int rc = make_header(g, &h);
+  if (rc) return rc;
+  if (!ell_dev || !geo_dev || !z_dev) return fail(JCG_ERR_ARG, "ell, z or geometry buffer is NULL");
+  if (geo_bytes < (size_t)h.total * 8)
+    return fail(JCG_ERR_WORKSPACE, "geometry buffer %zu bytes, need %zu", geo_bytes, (size_t)h.total * 8);
+  if (((uintptr_t)geo_dev) % 64 != 0) return fail(JCG_ERR_ARG, "geometry buffer must be 64-byte aligned");
+  ConstTables* c = nullptr;
+  if ((rc = const_tables(&c))) return rc;
+  double* geo = static_cast<double*>(geo_dev);
+  if (cudaMemcpyAsync(geo + h.off_ell, ell_dev, sizeof(double) * h.n_ell, cudaMemcpyDeviceToDevice,
+                      stream) != cudaSuccess ||
+      cudaMemcpyAsync(geo + h.off_z, z_dev, sizeof(double) * n_z, cudaMemcpyDeviceToDevice,
+                      stream) != cudaSuccess)
+    return cuda_check("copy ell / z");
+  launch_geometry_build(h, geo, c, stream);
+  return cuda_check("geometry build");
+}
+
+int jcg_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t* bytes) {
+  if (!bytes) return fail(JCG_ERR_ARG, "bytes is NULL");
+  if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  if (precision != JCG_FP64 && precision != JCG_FP32C) return fail(JCG_ERR_ARG, "precision = %d", precision);
+  GeoHeader h;
+  const int rc = make_header(g, &h);
+  if (rc) return rc;
+  *bytes = ws_layout(&h, n_cosmo, precision).total;
+  return JCG_OK;
+}
+
+static int stage_prepare(const jcg_geometry* g, const void* geo_dev, const double* params,
+                         int n_cosmo, int precision, void* ws, size_t ws_bytes, GeoHeader* h,
+                         ConstTables** c, bool need_geo) {
+  int rc = make_header(g, h);
+  if (rc) return rc;
+  if (need_geo && !geo_dev) return fail(JCG_ERR_ARG, "geometry buffer is NULL");
+  const WsLayout L = ws_layout(h, n_cosmo, precision);
+  if ((rc = check_common(params, n_cosmo, precision, ws, ws_bytes, L.total))) return rc;
+  return const_tables(c);
+}
+
+int jcg_stage_cosmo_tables(const jcg_geometry* g, const double* params, int n_cosmo, int precision,
+                           void* ws, size_t ws_bytes, cudaStream_t stream) {
+  GeoHeader h;
+  ConstTables* c;
+  int rc = stage_prepare(g, nullptr, params, n_cosmo, precision, ws, ws_bytes, &h, &c, false);
+  if (rc) return rc;
+  const Batch b = make_batch(&h, nullptr, params, n_cosmo, precision, ws, nullptr);
+  launch_cosmo_tables(b, c, stream);
+  return cuda_check("cosmology tables");
+}
+
+int jcg_stage_halofit_rows(const jcg_geometry* g, const void* geo, const double* params, int n_cosmo,
+                           int precision, void* ws, size_t ws_bytes, cudaStream_t stream) {
+  GeoHeader h;
+  ConstTables* c;
+  int rc = stage_prepare(g, geo, params, n_cosmo, precision, ws, ws_bytes, &h, &c, true);
+  if (rc) return rc;
+  const Batch b = make_batch(&h, geo, params, n_cosmo, precision, ws, nullptr);
+  launch_halofit_rows(b, c, stream);
+  return cuda_check("halofit rows");
+}
+
+int jcg_stage_tracer_kernels(const jcg_geometry* g, const void* geo, const double* params,
+                             int n_cosmo, int precision, void* ws, size_t ws_bytes,
+                             cudaStream_t stream) {
+  GeoHeader h;
+  ConstTables* c;
+  int rc = stage_prepare(g, geo, params, n_cosmo, precision, ws, ws_bytes, &h, &c, true);
+  if (rc) return rc;
+  const Batch b = make_batch(&h, geo, params, n_cosmo, precision, ws, nullptr);
+  launch_tracer_kernels(b, c, stream);
+  return cuda_check("tracer kernels");
+}
+
+int jcg_stage_limber(const jcg_geometry* g, const void* geo, const double* params, int n_cosmo,
+                     int precision, double* cl, void* ws, size_t ws_bytes, cudaStream_t stream) {
+  GeoHeader h;
+  ConstTables* c;
+  int rc = stage_prepare(g, geo, params, n_cosmo, precision, ws, ws_bytes, &h, &c, true);
+  if (rc) return rc;
+  if (!cl) return fail(JCG_ERR_ARG, "cl output is NULL");
+  const Batch b = make_batch(&h, geo, params, n_cosmo, precision, ws, cl);
+  launch_limber(b, c, limber_tile(h.n_ell), stream);
+  return cuda_check("limber");
+}
+
+int jcg_angular_cl(const jcg_geometry* g, const void* geo, const double* params, int n_cosmo,
+                   int precision, double* cl, void* ws, size_t ws_bytes, cudaStream_t stream) {
+  GeoHeader h;
+  ConstTables* c;
+  int rc = stage_prepare(g, geo, params, n_cosmo, precision, ws, ws_bytes, &h, &c, true);
+  if (rc) return rc;
+  if (!cl) return fail(JCG_ERR_ARG, "cl output is NULL");
+  const Batch b = make_batch(&h, geo, params, n_cosmo, precision, ws, cl);
+  launch_cosmo_tables(b, c, stream);
+  launch_halofit_rows(b, c, stream);
+  launch_tracer_kernels(b, c, stream);
+  launch_limber(b, c, limber_tile(h.n_ell), stream);
+  return cuda_check("angular_cl");
+}
+
+int jcg_workspace_read(const jcg_geometry* g, int n_cosmo, int precision, const void* ws, int index,
+                       int what, double* out, size_t out_count, cudaStream_t stream) {
+  GeoHeader h;
+  int rc = make_header(g, &h);
+  if (rc) return rc;
+  if (!ws || !out) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (index < 0 || index >= n_cosmo) return fail(JCG_ERR_SHAPE, "index %d of %d", index, n_cosmo);
+  const WsLayout L = ws_layout(&h, n_cosmo, precision);
+  const char* base = static_cast<const char*>(ws);
+  const CosmoTab* ct = reinterpret_cast<const CosmoTab*>(base + L.ctab) + index;
+  const void* src = nullptr;
+  size_t count = 0;
+  switch (what) {
+    case 0: src = ct->chi; count = NCHI; break;
+    case 1: src = ct->g; count = NGROW; break;
+    case 2: src = ct->s; count = NSCAL; break;
+    case 3:
+      src = reinterpret_cast<const double*>(base + L.rows64) + (size_t)index * h.na * NROW64;
+      count = (size_t)h.na * NROW64;
+      break;
+    case 4:
+      src = reinterpret_cast<const double*>(base + L.kern) + (size_t)index * h.n_tr * h.na;
+      count = (size_t)h.n_tr * h.na;
+      break;
+    default: return fail(JCG_ERR_ARG, "what = %d", what);
+  }
+  if (out_count < count) return fail(JCG_ERR_SHAPE, "output holds %zu values, need %zu", out_count, count);
+  if (cudaMemcpyAsync(out, src, count * sizeof(double), cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+    return cuda_check("workspace read");
+  return JCG_OK;
+}
+
+int jcg_eval_workspace_size(int n_cosmo, size_t* bytes) {
+  if (!bytes) return fail(JCG_ERR_ARG, "bytes is NULL");
+  if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  *bytes = ws_layout(nullptr, n_cosmo, JCG_FP64).total;
+  return JCG_OK;
+}
+
+int jcg_eval_points(const double* params, int n_cosmo, const double* a, const double* k, int n,
+                    int what, double* out, void* ws, size_t ws_bytes, cudaStream_t stream) {
+  int rc = check_common(params, n_cosmo, JCG_FP64, ws, ws_bytes, ws_layout(nullptr, n_cosmo, JCG_FP64).total);
+  if (rc) return rc;
+  if (n < 1) return fail(JCG_ERR_SHAPE, "n = %d", n);
+  if (what < 0 || what > 9) return fail(JCG_ERR_ARG, "what = %d", what);
+  const bool need_a = (what <= 3) || what >= 5;
+  const bool need_k = (what >= 4 && what <= 6);
+  if ((need_a && !a) || (need_k && !k) || !out) return fail(JCG_ERR_ARG, "NULL input or output");
+  ConstTables* c;
+  if ((rc = const_tables(&c))) return rc;
+  const Batch b = make_batch(nullptr, nullptr, params, n_cosmo, JCG_FP64, ws, nullptr);
+  launch_cosmo_tables(b, c, stream);
+  launch_eval_points(params, n_cosmo, b.ctab, c, a, k, n, what, out, stream);
+  return cuda_check("eval points");
+}
+
+int jcg_gaussian_covariance(const double* ell, int n_ell, int n_tr, const double* cl,
+                            const double* cl_noise, const double* tr_noise, int n_cosmo, double f_sky,
+                            int sparse, double* out, cudaStream_t stream) {
+  if (!ell || !cl || !out) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  if (n_tr < 1 || n_tr > JCG_MAX_TRACERS) return fail(JCG_ERR_SHAPE, "n_tracers = %d", n_tr);
+  if (n_ell < 2) return fail(JCG_ERR_SHAPE, "np.gradient needs at least 2 ell values (n_ell = %d)", n_ell);
+  if (!isfinite(f_sky)) return fail(JCG_ERR_VALUE, "f_sky = %g", f_sky);
+  launch_covariance(ell, n_ell, n_tr, cl, cl_noise, tr_noise, n_cosmo, f_sky, sparse ? 1 : 0, out,
+                    stream);
+  return cuda_check("covariance");
+}
+
+int jcg_loglike_workspace_size(int n_cosmo, int n_cls, int n_ell, size_t* bytes) {
+  if (!bytes) return fail(JCG_ERR_ARG, "bytes is NULL");
+  if (n_cosmo < 1 || n_cls < 1 || n_ell < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
+  *bytes = align256(sizeof(double) * 2 * (size_t)n_cosmo * n_ell) + align256(sizeof(int) * 2 * (size_t)n_cosmo);
+  return JCG_OK;
+}
+
+static int loglike_common(const double* data, const double* mu, const double* cov, int n_cosmo,
+                          int n_cls, int n_ell, int include_logdet, int dense, double* out,
+                          int* status, void* ws, size_t ws_bytes, cudaStream_t stream) {
+  if (!data || !mu || !cov || !out || !ws) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n_cosmo < 1 || n_cls < 1 || n_ell < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
+  if (n_cls > 160) return fail(JCG_ERR_SHAPE, "n_cls = %d above the per-ell block limit 160", n_cls);
+  size_t need = 0;
+  jcg_loglike_workspace_size(n_cosmo, n_cls, n_ell, &need);
+  if (ws_bytes < need) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need);
+  char* base = static_cast<char*>(ws);
+  double* partial = reinterpret_cast<double*>(base);
+  int* ints = reinterpret_cast<int*>(base + align256(sizeof(double) * 2 * (size_t)n_cosmo * n_ell));
+  int* structure = ints;
+  int* st = status ? status : ints + n_cosmo;
+  launch_loglike(data, mu, cov, n_cosmo, n_cls, n_ell, include_logdet ? 1 : 0, dense, out, st,
+                 partial, structure, stream);
+  return cuda_check("loglike");
+}
+
+int jcg_gaussian_loglike_sparse(const double* data, const double* mu, const double* cov, int n_cosmo,
+                                int n_cls, int n_ell, int include_logdet, double* out, int* status,
+                                void* ws, size_t ws_bytes, cudaStream_t stream) {
+  return loglike_common(data, mu, cov, n_cosmo, n_cls, n_ell, include_logdet, 0, out, status, ws,
+                        ws_bytes, stream);
+}
+
+int jcg_gaussian_loglike_dense(const double* data, const double* mu, const double* cov, int n_cosmo,
+                               int n_cls, int n_ell, int include_logdet, double* out, int* status,
+                               void* ws, size_t ws_bytes, cudaStream_t stream) {
+  return loglike_common(data, mu, cov, n_cosmo, n_cls, n_ell, include_logdet, 1, out, status, ws,
+                        ws_bytes, stream);
+}
+
+int jcg_sparse_inv(const double* sp, int n, int nd, double* out, cudaStream_t stream) {
+  if (!sp || !out) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n < 1 || nd < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
+  if (n > 80) return fail(JCG_ERR_SHAPE, "n = %d above the per-diagonal block limit 80", n);
+  launch_sparse_inv(sp, n, nd, out, stream);
+  return cuda_check("sparse inv");
+}
+
+int jcg_sparse_slogdet(const double* sp, int n, int nd, double* sign, double* logdet, double* work,
+                       cudaStream_t stream) {
+  if (!sp || !sign || !logdet || !work) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n < 1 || nd < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
+  if (n > 80) return fail(JCG_ERR_SHAPE, "n = %d above the per-diagonal block limit 80", n);
+  launch_sparse_slogdet(sp, n, nd, work, work + nd, sign, logdet, stream);
+  return cuda_check("sparse slogdet");
+}
+
+int jcg_sparse_to_dense(const double* sp, int n, int m, int nd, double* out, cudaStream_t stream) {
+  if (!sp || !out) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n < 1 || m < 1 || nd < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
+  launch_sparse_to_dense(sp, n, m, nd, out, stream);
+  return cuda_check("sparse to_dense");
+}
+
+int jcg_sparse_dot_vec(const double* sp, int n, int m, int nd, const double* v, int transpose,
+                       double* out, cudaStream_t stream) {
+  if (!sp || !v || !out) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n < 1 || m < 1 || nd < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
+  launch_sparse_dot_vec(sp, n, m, nd, v, transpose ? 1 : 0, out, stream);
+  return cuda_check("sparse dot");
+}
+
+}  // extern "C"

@@ -1,0 +1,360 @@
+// Internal layouts and device helpers shared by the libjcg translation units.
+//
+// Numbers of nodes, grid formulas and operation order follow jax_cosmo (paths
+// relative to the jax_cosmo project root); each helper cites the line it restates.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <type_traits>
+
+#include "../../include/jcg.h"
+
+namespace jcg {
+
+// ------------------------------------------------------------------ sizes ---
+constexpr int NCHI = 256;    // background.py:199  radial_comoving_distance steps
+constexpr int NGROW = 128;   // background.py:443  _growth_factor_ODE steps
+constexpr int NRT = 256;     // power.py:93        log R nodes of the sigma^2(R) table
+constexpr int NKH = 257;     // power.py:111,136   simps(..., 256) over ln k
+constexpr int NROMB = 129;   // power.py:77        romb(divmax=7): 2 + 1 + 2 + ... + 64
+constexpr int NZP = 257;     // probes.py:51       simps(integrand, z, zmax, 256)
+constexpr int NNORM = 257;   // redshift.py:30     simps(pz_fn, 0, zmax, 256)
+constexpr int MAXTR = JCG_MAX_TRACERS;
+constexpr int MAXPAIR = JCG_MAX_PAIRS;
+
+// physical constants: constants.py:9-27
+constexpr double C_KMS = 299792.458;
+constexpr double TCMB = 2.726;
+constexpr double RH = 2997.92458;
+constexpr double H0 = 100.0;
+constexpr double PI = 3.141592653589793;
+constexpr double EULER_E = 2.718281828459045;  // np.exp(1.0)
+
+// ------------------------------------------------ cosmology-wide constants ---
+// Grids shared by every cosmology and every geometry, built once per device.
+struct ConstTables {
+  double atab_chi[NCHI];   // logspace(-3, 0, 256)
+  double lna_chi[NCHI];    // log(atab_chi): the RK4 abscissae of background.py:231
+  double atab_grow[NGROW]; // logspace(-3, 0, 128)
+  double logk[NKH];        // linspace(log 1e-4, log 1e4, 257)
+  double kh[NKH];          // exp(logk)
+  double kh3[NKH];         // kh**3
+  double logr[NRT];        // linspace(log 1e-4, log 10, 256)
+  double simpson_kh[NKH];  // Simpson weights (1,4,2,...,4,1) * dx/3 on the ln k grid
+  double romb_logk[NROMB]; // romb abscissae in evaluation order (scipy/integrate.py:129-146)
+  double E[NKH * NRT];     // exp(-(k_i r_j)^2), i-major: power.py:99-109
+};
+
+// ------------------------------------------------- per-cosmology tables -----
+// Scalars of one cosmology (FP64).  Index names for CosmoTab::s.
+enum Scalar {
+  S_OMEGA_C = 0, S_OMEGA_B, S_H, S_NS, S_SIGMA8, S_OMEGA_K, S_W0, S_WA,
+  S_OMEGA_M, S_OMEGA_DE,
+  // Eisenstein & Hu 1998 (transfer.py:47-153)
+  S_K_EQ, S_Z_EQ, S_Z_D, S_R_D, S_R_EQ, S_SH_D, S_K_SILK, S_ALPHA_C, S_BETA_C,
+  S_ALPHA_B, S_BETA_B, S_BETA_NODE, S_FB, S_FC,
+  S_SIGMASQR8,  // power.py:56-78 at R = 8
+  S_PKNORM,     // sigma8^2 / sigmasqr(8): power.py:47
+  S_G1,         // growth_factor(a = 1) from the table (power.py:44 with a = 1)
+  S_NSCALAR
+};
+constexpr int NSCAL = 32;
+static_assert(S_NSCALAR <= NSCAL, "scalar block too small");
+
+struct CosmoTab {
+  double s[NSCAL];
+  double chi[NCHI];    // background.py:231-233  chi table on atab_chi
+  double g[NGROW];     // background.py:483      growth table on atab_grow
+  double sig[NRT];     // sigma^2(R_j) at a = 1 without the g(a)^2 factor
+  double pk3[NKH];     // linear_matter_power(k_i, a=1) * k_i^3
+  double pad[7];
+};
+static_assert(sizeof(CosmoTab) % 64 == 0, "CosmoTab must keep 64-byte alignment");
+
+// ------------------------------------------------- per-(cosmology, a) rows --
+// FP64 row written by the halofit-row kernel for every Limber node.
+enum Row64 {
+  R_CHI = 0,   // radial_comoving_distance(a)              angular_cl.py:70
+  R_G,         // growth_factor(a)                         power.py:44
+  R_KNL,       // k_nl                                     power.py:118
+  R_NEFF,      // n_eff                                    power.py:138
+  R_C,         // C                                        power.py:139
+  R_OMM,       // Omega_m(a)                               power.py:177
+  R_OMDE,      // Omega_de(a)                              power.py:178
+  R_W,         // w(a)                                     power.py:179
+  R_DCHI,      // dchioverda(a)                            angular_cl.py:91
+  R_AN, R_BN, R_CN, R_GAMMAN, R_ALPHAN, R_BETAN, R_NUN,    // power.py:200-224
+  R_F1, R_F2, R_F3,                                        // power.py:228-238
+  R_U,         // simpson weight * dchi / max(chi^2,1) / c^2
+  NROW64_USED
+};
+constexpr int NROW64 = 24;
+static_assert(NROW64_USED <= NROW64, "row too small");
+
+// FP32 row for the compensated fast path (derived, MUFU-friendly forms).
+enum Row32 {
+  F_INVCHI = 0,  // 1 / max(chi, 1)
+  F_LG2INVCHI,   // log2(1 / max(chi, 1))
+  F_LG2KNL,      // log2(k_nl)
+  F_D2FAC,       // g^2 * pknorm / (2 pi^2)
+  F_BETAN, F_ALPHAN, F_AN, F_3F1, F_F2, F_BN, F_LG2CF3, F_3MGAMMA, F_NUN,
+  F_INVKNL,      // 1 / k_nl
+  F_CHIC,        // max(chi, 1)
+  NROW32_USED
+};
+constexpr int NROW32 = 16;
+static_assert(NROW32_USED <= NROW32, "fp32 row too small");
+
+// ------------------------------------------------------ geometry tables ----
+// Cosmology-independent description of one request, stored at the start of the
+// geometry buffer (device), followed by the tables at the offsets below
+// (offsets in units of 8 bytes from the buffer start).
+struct GeoHeader {
+  int magic;
+  int n_tr, n_wl, n_nc, n_ell, n_limber, na, n_cls, n_groups;
+  int custom_nodes;        // 1: nodes are caller-given redshifts (in the z section)
+  int kind[MAXTR];
+  int group[MAXTR];        // lensing group (distinct probe zmax) of a WL tracer
+  int pair_i[MAXPAIR], pair_j[MAXPAIR];
+  double zmax;             // angular_cl.py:63
+  double dx_limber;        // (1 - z2a(zmax)) / N
+  double nz_a[MAXTR], nz_b[MAXTR], nz_z0[MAXTR], nz_zmax[MAXTR];
+  double bias[MAXTR], mult[MAXTR], noise[MAXTR], probe_zmax[MAXTR];
+  double group_zmax[MAXTR];
+  double nz_norm[MAXTR];   // redshift.py:30
+  // offsets (8-byte units)
+  int64_t off_a, off_z, off_wsimp, off_awl;
+  int64_t off_seg_chi, off_seg_grow, off_seg_chiwl;  // int32 pairs, packed as int64 per node
+  int64_t off_nzl;                                   // [n_tr][na] n_t(z_n)
+  int64_t off_ell, off_ellfac;                       // [n_ell], [n_tr][n_ell]
+  int64_t off_lg2ellh;                               // [n_ell] log2(ell + 1/2) (fp32 path)
+  int64_t off_ap[MAXTR];                             // per group [na][NZP] a' nodes
+  int64_t off_segp[MAXTR];                           // per group [na][NZP] packed segments
+  int64_t off_W[MAXTR];                              // per WL tracer [na][NZP] weights
+  int64_t total;                                     // bytes / 8
+};
+constexpr int GEO_MAGIC = 0x4a434731;  // "JCG1"
+
+// ----------------------------------------------------------- batch ---------
+// A batch of items = (cosmology, geometry) pairs.  The uniform form derives
+// every pointer from strides; the listed form reads an Item array (ragged
+// requests of the serving loop).
+struct Item {
+  const double* params;  // 8 parameters
+  const GeoHeader* geo;
+  CosmoTab* ctab;
+  double* rows64;        // [na][NROW64]
+  float* rows32;         // [na][NROW32]
+  double* kern;          // [n_tr][na]
+  double* cl;            // [n_cls][n_ell] (output)
+  int precision;
+  int pad;
+};
+
+struct Batch {
+  int n_items;
+  int listed;            // 0: uniform strides, 1: items[]
+  const Item* items;
+  // uniform form
+  const double* params;
+  const GeoHeader* geo;
+  CosmoTab* ctab;
+  double* rows64;
+  float* rows32;
+  double* kern;
+  double* cl;
+  int precision;
+  int max_na, max_ell, max_cls, max_tr;
+};
+
+__device__ __forceinline__ Item batch_item(const Batch& b, int i) {
+  if (b.listed) return b.items[i];
+  Item it;
+  const int na = b.max_na;
+  it.params = b.params + 8 * (size_t)i;
+  it.geo = b.geo;
+  it.ctab = b.ctab + i;
+  it.rows64 = b.rows64 ? b.rows64 + (size_t)i * na * NROW64 : nullptr;
+  it.rows32 = b.rows32 ? b.rows32 + (size_t)i * na * NROW32 : nullptr;
+  it.kern = b.kern + (size_t)i * b.max_tr * na;
+  it.cl = b.cl + (size_t)i * b.max_cls * b.max_ell;
+  it.precision = b.precision;
+  it.pad = 0;
+  return it;
+}
+
+template <typename T>
+__device__ __forceinline__ const T* geo_ptr(const GeoHeader* g, int64_t off) {
+  return reinterpret_cast<const T*>(reinterpret_cast<const double*>(g) + off);
+}
+
+// ------------------------------------------------------- exact helpers -----
+// numpy's float power uses fast paths for these scalar exponents
+// (x**2 -> square, x**1 -> copy, x**0.5 -> sqrt, x**-1 -> reciprocal).
+__device__ __forceinline__ double npow(double x, double y) {
+  if (y == 2.0) return x * x;
+  if (y == 1.0) return x;
+  if (y == 0.5) return sqrt(x);
+  if (y == -1.0) return 1.0 / x;
+  if (y == 0.0) return 1.0;
+  return pow(x, y);
+}
+
+// jnp.clip(x, lo) / jnp.clip(x, lo, hi)
+__device__ __forceinline__ double clip_lo(double x, double lo) { return fmax(x, lo); }
+__device__ __forceinline__ double clip_lohi(double x, double lo, double hi) {
+  return fmin(fmax(x, lo), hi);
+}
+
+// numpy linspace node i of [start, stop] with `div` intervals: i*step + start,
+// exact stop at i == div (numpy/core/function_base.py linspace).
+__device__ __forceinline__ double np_linspace(double start, double stop, int div, int i) {
+  if (i == div) return stop;
+  const double step = (stop - start) / (double)div;
+  return __dadd_rn(__dmul_rn((double)i, step), start);
+}
+
+// Nearest node of argmin((x - xp)^2) over an increasing table (first index on
+// ties), found from a bracketing guess and a local scan; then the side rule of
+// scipy/interpolate.py:47-57.  Returns packed (i0, i1) of the segment used.
+__device__ __forceinline__ int2 interp_segment_inc(double x, const double* xp, int n, int guess) {
+  int lo = guess < 0 ? 0 : (guess > n - 1 ? n - 1 : guess);
+  // walk to the bracketing position: xp[lo] <= x < xp[lo+1] (or an end)
+  while (lo > 0 && xp[lo] > x) --lo;
+  while (lo < n - 1 && xp[lo + 1] <= x) ++lo;
+  // candidates lo-1 .. lo+2, argmin with first-index tie rule
+  int best = -1;
+  double bestd = 0.0;
+  for (int j = lo - 1; j <= lo + 2; ++j) {
+    if (j < 0 || j >= n) continue;
+    const double d = x - xp[j];
+    const double d2 = d * d;
+    if (best < 0 || d2 < bestd) { best = j; bestd = d2; }
+  }
+  int ind = best < 1 ? 1 : (best > n - 2 ? n - 2 : best);
+  const double xc = clip_lohi(x, xp[1], xp[n - 2]);
+  const double sgn = xc - xp[ind];
+  const int s = (sgn >= 0.0) ? 1 : -1;  // copysign(1, sign(.)) with sign(0) = 0 -> +1
+  return make_int2(ind, ind + s);
+}
+
+// The linear evaluation of scipy/interpolate.py:55-59 on a chosen segment.
+__device__ __forceinline__ double interp_eval(double x, const double* xp, const double* fp, int2 seg) {
+  const double a = (fp[seg.y] - fp[seg.x]) / (xp[seg.y] - xp[seg.x]);
+  const double b = fp[seg.x] - a * xp[seg.x];
+  return a * x + b;
+}
+
+__device__ __forceinline__ int64_t pack_seg(int2 s) {
+  return (int64_t)(((uint64_t)(uint32_t)s.y << 32) | (uint32_t)s.x);
+}
+__device__ __forceinline__ int2 unpack_seg(int64_t v) {
+  return make_int2((int)(uint32_t)(v & 0xffffffffu), (int)(uint32_t)((uint64_t)v >> 32));
+}
+
+// Guess for logspace(-3, 0, n): position of x in log10 units.
+__device__ __forceinline__ int logspace_guess(double x, int n) {
+  if (!(x > 0.0)) return 0;
+  const double t = (log10(x) + 3.0) * (double)(n - 1) / 3.0;
+  if (t < 0.0) return 0;
+  if (t > (double)(n - 1)) return n - 1;
+  return (int)t;
+}
+
+// --------------------------------------------------------- background ------
+// background.py:25-196, 270-294 with the reference operation order.
+struct Bg {
+  double Om, Ok, Ode, w0, wa;
+};
+__device__ __forceinline__ Bg make_bg(const double* s) {
+  Bg b;
+  b.Om = s[S_OMEGA_M];
+  b.Ok = s[S_OMEGA_K];
+  b.Ode = s[S_OMEGA_DE];
+  b.w0 = s[S_W0];
+  b.wa = s[S_WA];
+  return b;
+}
+__device__ __forceinline__ double bg_w(const Bg& c, double a) { return c.w0 + (1.0 - a) * c.wa; }
+__device__ __forceinline__ double bg_fde(const Bg& c, double a) {
+  return -3.0 * (1.0 + c.w0 + c.wa) * log(a) + 3.0 * c.wa * (a - 1.0);
+}
+__device__ __forceinline__ double bg_esqr(const Bg& c, double a) {
+  return c.Om * pow(a, -3.0) + c.Ok * pow(a, -2.0) + c.Ode * exp(bg_fde(c, a));
+}
+__device__ __forceinline__ double bg_H(const Bg& c, double a) { return H0 * sqrt(bg_esqr(c, a)); }
+__device__ __forceinline__ double bg_omm(const Bg& c, double a) {
+  return c.Om * pow(a, -3.0) / bg_esqr(c, a);
+}
+__device__ __forceinline__ double bg_omde(const Bg& c, double a) {
+  return c.Ode * exp(bg_fde(c, a)) / bg_esqr(c, a);
+}
+__device__ __forceinline__ double bg_dchioverda(const Bg& c, double a) {
+  return RH / ((a * a) * sqrt(bg_esqr(c, a)));
+}
+
+// ------------------------------------------------------ Eisenstein & Hu ----
+// transfer.py:107-153 (eisenhu_osc), per-k part, FP64, reference order.
+__device__ __forceinline__ double eh_T_tilde(double k1, double alpha, double beta, double k_eq) {
+  const double q = k1 / (13.41 * k_eq);
+  const double L = log(EULER_E + 1.8 * beta * q);
+  const double C = 14.2 / alpha + 386.0 / (1.0 + 69.9 * pow(q, 1.08));
+  return L / (L + C * q * q);
+}
+
+__device__ __forceinline__ double eh_transfer(const double* s, double k) {
+  const double k_eq = s[S_K_EQ], sh_d = s[S_SH_D];
+  const double ksh54 = k * sh_d / 5.4;
+  const double f = 1.0 / (1.0 + pow(ksh54, 4.0));
+  const double Tc = f * eh_T_tilde(k, 1.0, s[S_BETA_C], k_eq) +
+                    (1.0 - f) * eh_T_tilde(k, s[S_ALPHA_C], s[S_BETA_C], k_eq);
+  const double bn = s[S_BETA_NODE] / (k * sh_d);
+  const double tilde_s = sh_d / pow(1.0 + pow(bn, 3.0), 1.0 / 3.0);
+  const double ksh52 = k * sh_d / 5.2;
+  const double bb = s[S_BETA_B] / (k * sh_d);
+  const double xs = k * tilde_s / PI;
+  const double px = PI * xs;
+  const double sinc = sin(px) / px;  // np.sinc(x) = sin(pi x) / (pi x), x != 0
+  const double Tb = (eh_T_tilde(k, 1.0, 1.0, k_eq) / (1.0 + ksh52 * ksh52) +
+                     s[S_ALPHA_B] / (1.0 + pow(bb, 3.0)) * exp(-pow(k / s[S_K_SILK], 1.4))) *
+                    sinc;
+  return s[S_FB] * Tb + s[S_FC] * Tc;
+}
+
+// linear_matter_power(k, a) with g = growth_factor(a): power.py:42-53
+__device__ __forceinline__ double pk_linear(const double* s, double k, double g) {
+  const double t = eh_transfer(s, k);
+  double pk = pow(k, s[S_NS]) * (t * t) * (g * g);
+  return pk * s[S_PKNORM];
+}
+
+// halofit takahashi2012 per-node evaluation: power.py:246-260
+__device__ __forceinline__ double halofit_node(const double* s, const double* row, double k) {
+  const double pklin = pk_linear(s, k, row[R_G]);
+  const double d2l = pow(k, 3.0) * pklin / (2.0 * (PI * PI));
+  const double y = k / row[R_KNL];
+  const double fy = y / 4.0 + (y * y) / 8.0;
+  const double d2q = d2l * (pow(1.0 + d2l, row[R_BETAN]) / (1 + row[R_ALPHAN] * d2l)) * exp(-fy);
+  const double d2hprime =
+      row[R_AN] * pow(y, 3 * row[R_F1]) /
+      (1.0 + row[R_BN] * pow(y, row[R_F2]) + pow(row[R_CN] * row[R_F3] * y, 3.0 - row[R_GAMMAN]));
+  const double d2h = d2hprime / (1.0 + 0.0 / y + row[R_NUN] / (y * y));
+  return 2.0 * (PI * PI) / pow(k, 3.0) * (d2q + d2h);
+}
+
+// ------------------------------------------------------------- launches ----
+// Host-side launchers implemented in the kernel translation units.
+void launch_const_init(ConstTables* c, cudaStream_t st);
+void launch_geometry_build(const GeoHeader& h, double* geo, const ConstTables* c, cudaStream_t st);
+void launch_cosmo_tables(const Batch& b, const ConstTables* c, cudaStream_t st);
+void launch_halofit_rows(const Batch& b, const ConstTables* c, cudaStream_t st);
+void launch_tracer_kernels(const Batch& b, const ConstTables* c, cudaStream_t st);
+void launch_limber(const Batch& b, const ConstTables* c, int lt, cudaStream_t st);
+// pointwise queries of the table functions (API: background / power modules)
+void launch_eval_points(const double* params, int n_cosmo, CosmoTab* ctab, const ConstTables* c,
+                        const double* a, const double* k, int n, int what, double* out,
+                        cudaStream_t st);
+
+}  // namespace jcg

@@ -1,0 +1,261 @@
+// Fused Limber integral (angular_cl.py:49-98).
+//
+//   C_ij(l) = ef_i(l) ef_j(l) * sum_a  P_nl(k = (l + 1/2) / max(chi_a, 1), a) * M_ij(a)
+//   M_ij(a) = w_a * dchi/da / max(chi_a^2, 1) / c^2 * K_i(a) K_j(a)
+//
+// w_a are the Simpson weights of simps(integrand, z2a(zmax), 1, N)
+// (scipy/integrate.py:195-198), K_i the ell-independent radial kernels and
+// ef_i the WeakLensing ell factor (probes.py:73; 1 for NumberCounts).
+//
+// One CTA per (ell tile, cosmology).  The a axis is walked in chunks of TA
+// nodes: the chunk's per-a rows and M_ij are staged in shared memory, every
+// thread evaluates Eisenstein-Hu x primordial x halofit at (ell, a) nodes into
+// a P tile, then the CTA contracts the P tile with M into per-thread
+// accumulators.  FP64: the reference's formula order.  FP32C: MUFU forms of the
+// same formulas (ex2/lg2/rcp/sin), per-chunk partial sums added with Kahan
+// compensation across chunks.
+#include "jcg_internal.cuh"
+
+namespace jcg {
+
+constexpr int LB_THREADS = 256;
+constexpr int LB_TA = 32;   // a nodes per chunk
+constexpr int LB_MAXLT = 32;
+constexpr int LB_MAXO = (LB_MAXLT * MAXPAIR + LB_THREADS - 1) / LB_THREADS;  // 17
+
+// ---------------------------------------------------------- FP32 helpers ---
+__device__ __forceinline__ float ex2f(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2f(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float rcpf(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float sinf_approx(float x) {
+  float y;
+  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+// sin(x) for x >= 0: reduce by 2 pi in two parts (Cody & Waite), then the
+// hardware approximation on [-pi, pi].
+__device__ __forceinline__ float sin_reduced(float x) {
+  const float n = rintf(x * 0.15915494309189535f);
+  float r = fmaf(-n, 6.28125f, x);                // 6.28125 = 201/32, exact products
+  r = fmaf(-n, 1.9353071795864769e-3f, r);        // 2 pi - 6.28125
+  return sinf_approx(r);
+}
+
+constexpr float LOG2E_F = 1.4426950408889634f;
+constexpr float LN2_F = 0.6931471805599453f;
+constexpr float E_F = 2.718281828459045f;
+constexpr float TWO_PI2_F = 19.739208802178716f;
+
+// Per-cosmology Eisenstein & Hu constants of the FP32 node.
+struct EH32 {
+  float qinv, lg2_qinv, sh, inv_sh, c18bc, c142ac, alpha_b, beta_b, beta_node, lg2_ksilk, fb, fc,
+      ns3;
+};
+
+__device__ void make_eh32(const double* s, EH32* e) {
+  const double qinv = 1.0 / (13.41 * s[S_K_EQ]);
+  e->qinv = (float)qinv;
+  e->lg2_qinv = (float)log2(qinv);
+  e->sh = (float)s[S_SH_D];
+  e->inv_sh = (float)(1.0 / s[S_SH_D]);
+  e->c18bc = (float)(1.8 * s[S_BETA_C]);
+  e->c142ac = (float)(14.2 / s[S_ALPHA_C]);
+  e->alpha_b = (float)s[S_ALPHA_B];
+  e->beta_b = (float)s[S_BETA_B];
+  e->beta_node = (float)s[S_BETA_NODE];
+  e->lg2_ksilk = (float)log2(s[S_K_SILK]);
+  e->fb = (float)s[S_FB];
+  e->fc = (float)s[S_FC];
+  e->ns3 = (float)(s[S_NS] + 3.0);
+}
+
+// Eisenstein-Hu (transfer.py:107-153) x primordial x halofit (power.py:246-260)
+// at one node in FP32.  kh = l + 1/2, lg2kh = log2(kh), invkh = 1 / kh.
+__device__ __forceinline__ float node32(const EH32& e, const float* r, float kh, float lg2kh,
+                                        float invkh) {
+  const float k = kh * r[F_INVCHI];
+  const float lk = lg2kh + r[F_LG2INVCHI];
+  const float invk = invkh * r[F_CHIC];
+  // cold dark matter transfer (EH98 10-12, 17-18)
+  const float q = k * e.qinv;
+  const float lq = lk + e.lg2_qinv;
+  const float q108 = ex2f(1.08f * lq);
+  const float Cb = 386.f * rcpf(1.f + 69.9f * q108);
+  const float L1 = LN2_F * lg2f(E_F + e.c18bc * q);
+  const float L2 = LN2_F * lg2f(E_F + 1.8f * q);
+  const float qq = q * q;
+  const float Ta = L1 * rcpf(L1 + (14.2f + Cb) * qq);
+  const float Tb = L1 * rcpf(L1 + (e.c142ac + Cb) * qq);
+  const float Tn = L2 * rcpf(L2 + (14.2f + Cb) * qq);
+  const float ks = k * e.sh;
+  const float x54 = ks * (1.f / 5.4f);
+  const float x54_2 = x54 * x54;
+  const float f = rcpf(1.f + x54_2 * x54_2);
+  const float Tc = f * Ta + (1.f - f) * Tb;
+  // baryon transfer (EH98 14, 19, 21-24)
+  const float iks = invk * e.inv_sh;
+  const float x52 = ks * (1.f / 5.2f);
+  const float bb = e.beta_b * iks;
+  const float silk = ex2f(-LOG2E_F * ex2f(1.4f * (lk - e.lg2_ksilk)));
+  const float bn = e.beta_node * iks;
+  const float st = e.sh * ex2f((-1.f / 3.f) * lg2f(1.f + bn * bn * bn));
+  const float arg = k * st;
+  const float sinc = sin_reduced(arg) * rcpf(arg);
+  const float Tbar = (Tn * rcpf(1.f + x52 * x52) + e.alpha_b * rcpf(1.f + bb * bb * bb) * silk) * sinc;
+  const float T = e.fb * Tbar + e.fc * Tc;
+  // linear and halofit power
+  const float d2l = ex2f(e.ns3 * lk) * (T * T) * r[F_D2FAC];
+  const float y = k * r[F_INVKNL];
+  const float ly = lk - r[F_LG2KNL];
+  const float fy = y * (0.25f + 0.125f * y);
+  const float d2q = d2l * ex2f(r[F_BETAN] * lg2f(1.f + d2l)) * rcpf(1.f + r[F_ALPHAN] * d2l) *
+                    ex2f(-LOG2E_F * fy);
+  const float yf1 = ex2f(r[F_3F1] * ly);
+  const float yf2 = ex2f(r[F_F2] * ly);
+  const float ycg = ex2f(r[F_3MGAMMA] * (r[F_LG2CF3] + ly));
+  const float y2 = y * y;
+  const float d2h = r[F_AN] * yf1 * rcpf(1.f + r[F_BN] * yf2 + ycg) * y2 * rcpf(y2 + r[F_NUN]);
+  return TWO_PI2_F * (invk * invk * invk) * (d2q + d2h);
+}
+
+// ---------------------------------------------------------------- kernel ---
+template <bool FP32>
+__global__ void __launch_bounds__(LB_THREADS)
+    limber_kernel(Batch bt, const ConstTables* __restrict__ c, int LT) {
+  using T = typename std::conditional<FP32, float, double>::type;
+  constexpr int RW = FP32 ? NROW32 : NROW64;
+  const int item = blockIdx.y;
+  if (item >= bt.n_items) return;
+  const Item it = batch_item(bt, item);
+  const GeoHeader* geo = it.geo;
+  const int n_ell = geo->n_ell, n_cls = geo->n_cls, na = geo->na;
+  const int l0 = blockIdx.x * LT;
+  if (l0 >= n_ell) return;
+  const int lt = min(LT, n_ell - l0);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* s = reinterpret_cast<double*>(smem_raw);  // NSCAL
+  EH32* e32 = reinterpret_cast<EH32*>(s + NSCAL);   // 1 (padded to 8 doubles)
+  T* rowsS = reinterpret_cast<T*>(s + NSCAL + 8);   // TA * RW
+  T* Ms = rowsS + LB_TA * RW;                        // TA * n_cls
+  T* Pt = Ms + LB_TA * n_cls;                        // TA * LT
+  const int tid = threadIdx.x;
+  for (int i = tid; i < NSCAL; i += LB_THREADS) s[i] = it.ctab->s[i];
+  __syncthreads();
+  if (FP32 && tid == 0) make_eh32(s, e32);
+  __syncthreads();
+  const double* ELL = geo_ptr<double>(geo, geo->off_ell);
+  const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
+  const double* LG = geo_ptr<double>(geo, geo->off_lg2ellh);
+  const double* rows64 = it.rows64;
+  const float* rows32 = it.rows32;
+  const double* kern = it.kern;
+  // per-thread P-phase ell values (constant over chunks)
+  const int nout = lt * n_cls;
+  T acc[LB_MAXO], comp[LB_MAXO];
+#pragma unroll
+  for (int r = 0; r < LB_MAXO; ++r) {
+    acc[r] = 0;
+    comp[r] = 0;
+  }
+  for (int base = 0; base < na; base += LB_TA) {
+    const int tc = min(LB_TA, na - base);
+    // stage rows
+    if (FP32) {
+      for (int i = tid; i < tc * RW; i += LB_THREADS)
+        rowsS[i] = (T)rows32[(size_t)base * NROW32 + i];
+    } else {
+      for (int i = tid; i < tc * RW; i += LB_THREADS)
+        rowsS[i] = (T)rows64[(size_t)base * NROW64 + i];
+    }
+    // M_ij(a) = u_a K_i(a) K_j(a)
+    for (int q = tid; q < tc * n_cls; q += LB_THREADS) {
+      const int t = q / n_cls, p = q - (q / n_cls) * n_cls;
+      const int n = base + t;
+      const double ki = kern[(size_t)geo->pair_i[p] * na + n];
+      const double kj = kern[(size_t)geo->pair_j[p] * na + n];
+      Ms[t * n_cls + p] = (T)((ki * kj) * rows64[(size_t)n * NROW64 + R_U]);
+    }
+    __syncthreads();
+    // P tile: nodes (t, l)
+    for (int q = tid; q < tc * lt; q += LB_THREADS) {
+      const int t = q / lt, l = q - (q / lt) * lt;
+      const double ell = ELL[l0 + l];
+      T pv;
+      if (FP32) {
+        const float kh = (float)(ell + 0.5);
+        pv = (T)node32(*e32, reinterpret_cast<const float*>(rowsS) + t * NROW32, kh,
+                       (float)LG[l0 + l], (float)(1.0 / (ell + 0.5)));
+      } else {
+        const double* row = reinterpret_cast<const double*>(rowsS) + t * NROW64;
+        const double k = (ell + 0.5) / fmax(row[R_CHI], 1.0);
+        pv = (T)halofit_node(s, row, k);
+      }
+      Pt[t * LT + l] = pv;
+    }
+    __syncthreads();
+    // contraction
+#pragma unroll
+    for (int r = 0; r < LB_MAXO; ++r) {
+      const int o = tid + r * LB_THREADS;
+      if (o < nout) {
+        const int l = o % lt, p = o / lt;
+        T part = 0;
+        for (int t = 0; t < tc; ++t) part += Pt[t * LT + l] * Ms[t * n_cls + p];
+        if (FP32) {
+          const T y = part - comp[r];
+          const T tt = acc[r] + y;
+          comp[r] = (tt - acc[r]) - y;
+          acc[r] = tt;
+        } else {
+          acc[r] += part;
+        }
+      }
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < LB_MAXO; ++r) {
+    const int o = tid + r * LB_THREADS;
+    if (o < nout) {
+      const int l = o % lt, p = o / lt;
+      const int ell = l0 + l;
+      const double efi = EF[(size_t)geo->pair_i[p] * n_ell + ell];
+      const double efj = EF[(size_t)geo->pair_j[p] * n_ell + ell];
+      const double v = FP32 ? ((double)acc[r] - (double)comp[r]) : (double)acc[r];
+      it.cl[(size_t)p * n_ell + ell] = v * efi * efj;
+    }
+  }
+}
+
+size_t limber_smem_bytes(bool fp32, int n_cls, int LT) {
+  const size_t el = fp32 ? 4 : 8;
+  const size_t rw = fp32 ? NROW32 : NROW64;
+  return (NSCAL + 8) * 8 + el * (LB_TA * rw + (size_t)LB_TA * n_cls + (size_t)LB_TA * LT);
+}
+
+void launch_limber(const Batch& b, const ConstTables* c, int lt, cudaStream_t st) {
+  const bool fp32 = b.precision == JCG_FP32C;
+  const size_t smem = limber_smem_bytes(fp32, b.max_cls, lt);
+  dim3 grid((b.max_ell + lt - 1) / lt, b.n_items);
+  if (fp32) {
+    cudaFuncSetAttribute(limber_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    limber_kernel<true><<<grid, LB_THREADS, smem, st>>>(b, c, lt);
+  } else {
+    cudaFuncSetAttribute(limber_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    limber_kernel<false><<<grid, LB_THREADS, smem, st>>>(b, c, lt);
+  }
+}
+
+}  // namespace jcg

@@ -1,0 +1,408 @@
+// Gaussian covariance, log-likelihood and the block-diagonal ("sparse") matrix
+// algebra, FP64.
+//
+// The covariance of angular_cl.py:120-163 is, after permuting (cls, ell) to
+// (ell, cls), block diagonal with one n_cls x n_cls block per ell.  The
+// log-likelihood of likelihood.py:9-61 therefore factors into per-ell Cholesky
+// solves: r^T C^-1 r = sum_l r_l^T A_l^-1 r_l and logdet C = sum_l logdet A_l,
+// which is what the reference's sparse path (sparse.py:295-366) computes by
+// inverse and Schur complements, and its dense path by a full inverse.
+#include "jcg_internal.cuh"
+
+namespace jcg {
+
+// index of pair (min(a,b), max(a,b)) in the ordering of angular_cl.py:15-25
+__device__ __forceinline__ int pair_index(int a, int b, int n) {
+  const int i = a < b ? a : b, j = a < b ? b : a;
+  return i * n - (i * (i - 1)) / 2 + (j - i);
+}
+
+// np.gradient(ell) with unit spacing and first-order edges.
+__device__ __forceinline__ double ell_gradient(const double* ell, int n, int l) {
+  if (l == 0) return (ell[1] - ell[0]) / 1.0;
+  if (l == n - 1) return (ell[n - 1] - ell[n - 2]) / 1.0;
+  return (ell[l + 1] - ell[l - 1]) / 2.0;
+}
+
+// pair p -> (i, j) of the ordering of angular_cl.py:15-25
+__device__ __forceinline__ int2 pair_of(int p, int n) {
+  int i = 0;
+  while (i < n - 1 && p >= (i + 1) * n - ((i + 1) * i) / 2) ++i;
+  const int j = p - (i * n - (i * (i - 1)) / 2) + i;
+  return make_int2(i, j);
+}
+
+// cl_obs = cl_signal + cl_noise (angular_cl.py:135); the noise of noise_cl
+// (angular_cl.py:101-117) is noise[i] * delta_ij on auto-spectra.
+__device__ __forceinline__ double cl_obs(const double* sig, const double* cl_noise,
+                                         const double* tr_noise, int x, int l, int n_ell,
+                                         int n_tr) {
+  double nz = 0.0;
+  if (cl_noise) {
+    nz = cl_noise[(size_t)x * n_ell + l];
+  } else if (tr_noise) {
+    const int2 ij = pair_of(x, n_tr);
+    const double delta = 1.0 - fmin(fmax(fabs((double)(ij.x - ij.y)), 0.0), 1.0);
+    nz = __dmul_rn(__dmul_rn(tr_noise[ij.x], delta), 1.0);
+  }
+  return __dadd_rn(sig[(size_t)x * n_ell + l], nz);
+}
+
+// One thread per sparse element (p, q, l) of one cosmology, or per dense
+// element.  angular_cl.py:138-162.
+__global__ void covariance_kernel(const double* __restrict__ ell, int n_ell, int n_tr,
+                                  const double* __restrict__ cl, const double* __restrict__ cl_noise,
+                                  const double* __restrict__ tr_noise, int n_cosmo, double f_sky,
+                                  int sparse, double* __restrict__ out) {
+  const int n_cls = n_tr * (n_tr + 1) / 2;
+  const size_t N = (size_t)n_cls * n_ell;
+  const size_t per = sparse ? (size_t)n_cls * n_cls * n_ell : N * N;
+  const size_t total = per * n_cosmo;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t ci = idx / per, e = idx % per;
+    int p, q, l;
+    if (sparse) {
+      l = (int)(e % n_ell);
+      q = (int)((e / n_ell) % n_cls);
+      p = (int)(e / ((size_t)n_ell * n_cls));
+    } else {
+      const size_t row = e / N, col = e % N;
+      p = (int)(row / n_ell);
+      l = (int)(row % n_ell);
+      q = (int)(col / n_ell);
+      const int l2 = (int)(col % n_ell);
+      if (l2 != l) {
+        out[idx] = 0.0;
+        continue;
+      }
+    }
+    const double* sig = cl + ci * (size_t)n_cls * n_ell;
+    const int2 ij = pair_of(p, n_tr), mn = pair_of(q, n_tr);
+    const int i = ij.x, j = ij.y, m = mn.x, n = mn.y;
+    // (find(i,m), find(j,n), find(i,n), find(j,m))  angular_cl.py:41-45
+    const int a = pair_index(i, m, n_tr), b = pair_index(j, n, n_tr);
+    const int c = pair_index(i, n, n_tr), d = pair_index(j, m, n_tr);
+    // unfused multiply / add: the same roundings as the reference's NumPy ops
+    const double norm =
+        __dmul_rn(__dmul_rn(__dadd_rn(__dmul_rn(2.0, ell[l]), 1.0), ell_gradient(ell, n_ell, l)), f_sky);
+    const double oa = cl_obs(sig, cl_noise, tr_noise, a, l, n_ell, n_tr);
+    const double ob = cl_obs(sig, cl_noise, tr_noise, b, l, n_ell, n_tr);
+    const double oc = cl_obs(sig, cl_noise, tr_noise, c, l, n_ell, n_tr);
+    const double od = cl_obs(sig, cl_noise, tr_noise, d, l, n_ell, n_tr);
+    out[idx] = __ddiv_rn(__dadd_rn(__dmul_rn(oa, ob), __dmul_rn(oc, od)), norm);
+  }
+}
+
+void launch_covariance(const double* ell, int n_ell, int n_tr, const double* cl,
+                       const double* cl_noise, const double* tr_noise, int n_cosmo, double f_sky,
+                       int sparse, double* out, cudaStream_t st) {
+  const int n_cls = n_tr * (n_tr + 1) / 2;
+  const size_t N = (size_t)n_cls * n_ell;
+  const size_t total = (sparse ? (size_t)n_cls * n_cls * n_ell : N * N) * n_cosmo;
+  const size_t blocks = (total + 255) / 256;
+  const unsigned nb = (unsigned)(blocks < 152 * 64 ? (blocks ? blocks : 1) : 152 * 64);
+  covariance_kernel<<<nb, 256, 0, st>>>(ell, n_ell, n_tr, cl, cl_noise, tr_noise, n_cosmo, f_sky,
+                                        sparse, out);
+}
+
+// ------------------------------------------------------ block Cholesky -----
+// In-place lower Cholesky of the n x n matrix A (shared memory, row-major).
+// Returns false if a pivot is not positive.
+__device__ bool block_cholesky(double* A, int n, volatile int* flag) {
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int k = 0; k < n; ++k) {
+    if (tid == 0) {
+      const double d = A[k * n + k];
+      if (!(d > 0.0)) *flag = 1;
+      A[k * n + k] = sqrt(d);
+    }
+    __syncthreads();
+    const double dk = A[k * n + k];
+    for (int i = k + 1 + tid; i < n; i += nt) A[i * n + k] /= dk;
+    __syncthreads();
+    const int m = n - k - 1;
+    for (int e = tid; e < m * m; e += nt) {
+      const int i = k + 1 + e / m, j = k + 1 + e % m;
+      if (j <= i) A[i * n + j] -= A[i * n + k] * A[j * n + k];
+    }
+    __syncthreads();
+  }
+  return *flag == 0;
+}
+
+// r^T A^-1 r and logdet A from the Cholesky factor (single thread: n is small).
+__device__ void chol_quad_logdet(const double* L, const double* r, double* z, int n, double* quad,
+                                 double* logdet) {
+  double q = 0.0, ld = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double v = r[i];
+    for (int j = 0; j < i; ++j) v -= L[i * n + j] * z[j];
+    z[i] = v / L[i * n + i];
+    q += z[i] * z[i];
+    ld += log(L[i * n + i]);
+  }
+  *quad = q;
+  *logdet = 2.0 * ld;
+}
+
+// One CTA per (ell, cosmology): block A_l[p][q] from the sparse or dense input,
+// Cholesky, then r_l^T A_l^-1 r_l and logdet A_l into the partials.
+__global__ void loglike_blocks_kernel(const double* __restrict__ data, const double* __restrict__ mu,
+                                      const double* __restrict__ cov, int n_cls, int n_ell,
+                                      int dense, const int* __restrict__ structure,
+                                      double* __restrict__ partial, int* __restrict__ status) {
+  const int l = blockIdx.x, ci = blockIdx.y;
+  extern __shared__ double sm[];
+  double* A = sm;
+  double* r = A + n_cls * n_cls;
+  double* z = r + n_cls;
+  __shared__ int flag;
+  const size_t N = (size_t)n_cls * n_ell;
+  if (threadIdx.x == 0) flag = 0;
+  if (dense && structure && structure[ci] != 0) {
+    if (threadIdx.x == 0) {
+      partial[((size_t)ci * n_ell + l) * 2 + 0] = NAN;
+      partial[((size_t)ci * n_ell + l) * 2 + 1] = NAN;
+    }
+    return;
+  }
+  for (int e = threadIdx.x; e < n_cls * n_cls; e += blockDim.x) {
+    const int p = e / n_cls, q = e % n_cls;
+    double v;
+    if (dense) {
+      v = cov[(size_t)ci * N * N + ((size_t)p * n_ell + l) * N + (size_t)q * n_ell + l];
+    } else {
+      v = cov[(((size_t)ci * n_cls + p) * n_cls + q) * n_ell + l];
+    }
+    A[e] = v;
+  }
+  for (int p = threadIdx.x; p < n_cls; p += blockDim.x) {
+    const size_t o = (size_t)ci * N + (size_t)p * n_ell + l;
+    r[p] = mu[o] - data[o];  // likelihood.py:38
+  }
+  __syncthreads();
+  const bool ok = block_cholesky(A, n_cls, &flag);
+  if (threadIdx.x == 0) {
+    double q = NAN, ld = NAN;
+    if (ok) chol_quad_logdet(A, r, z, n_cls, &q, &ld);
+    else atomicMax(status + ci, 2);
+    partial[((size_t)ci * n_ell + l) * 2 + 0] = q;
+    partial[((size_t)ci * n_ell + l) * 2 + 1] = ld;
+  }
+}
+
+// Fixed-order sum over ell of the partials: -0.5 * (quad - logdet) (likelihood.py:61).
+__global__ void loglike_reduce_kernel(const double* __restrict__ partial, int n_cosmo, int n_ell,
+                                      int include_logdet, double* __restrict__ out) {
+  const int ci = blockIdx.x * blockDim.x + threadIdx.x;
+  if (ci >= n_cosmo) return;
+  double q = 0.0, ld = 0.0;
+  for (int l = 0; l < n_ell; ++l) {
+    q += partial[((size_t)ci * n_ell + l) * 2 + 0];
+    ld += partial[((size_t)ci * n_ell + l) * 2 + 1];
+  }
+  out[ci] = include_logdet ? -0.5 * (q - ld) : -0.5 * q;
+}
+
+// Dense input: flag cosmologies whose matrix has a non-zero outside the
+// per-ell diagonals of its n_ell x n_ell blocks.
+__global__ void dense_structure_kernel(const double* __restrict__ cov, int n_cosmo, int n_cls,
+                                       int n_ell, int* __restrict__ structure) {
+  const size_t N = (size_t)n_cls * n_ell;
+  const size_t total = N * N * n_cosmo;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t e = idx % (N * N);
+    const size_t row = e / N, col = e % N;
+    if ((row % n_ell) != (col % n_ell) && cov[idx] != 0.0) {
+      structure[idx / (N * N)] = 1;
+    }
+  }
+}
+
+__global__ void merge_structure_kernel(const int* structure, int* status, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n && structure[i]) status[i] = 1;
+}
+
+__global__ void zero_int_kernel(int* p, int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) p[i] = 0;
+}
+
+void launch_loglike(const double* data, const double* mu, const double* cov, int n_cosmo, int n_cls,
+                    int n_ell, int include_logdet, int dense, double* out, int* status,
+                    double* partial, int* structure, cudaStream_t st) {
+  zero_int_kernel<<<(n_cosmo + 255) / 256, 256, 0, st>>>(status, n_cosmo);
+  if (dense) {
+    zero_int_kernel<<<(n_cosmo + 255) / 256, 256, 0, st>>>(structure, n_cosmo);
+    const size_t N = (size_t)n_cls * n_ell;
+    const size_t total = N * N * n_cosmo;
+    size_t blocks = (total + 255) / 256;
+    if (blocks > 152 * 32) blocks = 152 * 32;
+    dense_structure_kernel<<<(unsigned)blocks, 256, 0, st>>>(cov, n_cosmo, n_cls, n_ell, structure);
+  }
+  const size_t smem = ((size_t)n_cls * n_cls + 2 * n_cls) * sizeof(double);
+  cudaFuncSetAttribute(loglike_blocks_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dim3 grid(n_ell, n_cosmo);
+  const int threads = n_cls >= 64 ? 256 : 128;
+  loglike_blocks_kernel<<<grid, threads, smem, st>>>(data, mu, cov, n_cls, n_ell, dense,
+                                                      dense ? structure : nullptr, partial, status);
+  loglike_reduce_kernel<<<(n_cosmo + 127) / 128, 128, 0, st>>>(partial, n_cosmo, n_ell,
+                                                               include_logdet, out);
+  if (dense) {
+    // status 1 where the dense matrix is not block diagonal in ell
+    merge_structure_kernel<<<(n_cosmo + 255) / 256, 256, 0, st>>>(structure, status, n_cosmo);
+  }
+}
+
+// -------------------------------------------------- sparse-format algebra ---
+// One CTA per diagonal index l: Gauss-Jordan with partial pivoting of the
+// n x n matrix A_l[i][j] = sparse[i][j][l] (sparse.py:295-315), or its
+// log|det| and sign (sparse.py:322-366 computes the same by Schur complements).
+__global__ void sparse_lu_kernel(const double* __restrict__ sp, int n, int nd, int mode,
+                                 double* __restrict__ out, double* __restrict__ sign_out,
+                                 double* __restrict__ logdet_part) {
+  const int l = blockIdx.x;
+  extern __shared__ double sm[];
+  double* A = sm;          // n x n
+  double* X = A + n * n;   // n x n (inverse)
+  __shared__ int piv;
+  __shared__ double sgn, ld;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  for (int e = tid; e < n * n; e += nt) {
+    const int i = e / n, j = e % n;
+    A[e] = sp[((size_t)i * n + j) * nd + l];
+    X[e] = (i == j) ? 1.0 : 0.0;
+  }
+  if (tid == 0) {
+    sgn = 1.0;
+    ld = 0.0;
+  }
+  __syncthreads();
+  for (int k = 0; k < n; ++k) {
+    if (tid == 0) {
+      int p = k;
+      double best = fabs(A[k * n + k]);
+      for (int i = k + 1; i < n; ++i) {
+        const double v = fabs(A[i * n + k]);
+        if (v > best) { best = v; p = i; }
+      }
+      piv = p;
+    }
+    __syncthreads();
+    const int p = piv;
+    if (p != k) {
+      for (int j = tid; j < n; j += nt) {
+        double t = A[k * n + j]; A[k * n + j] = A[p * n + j]; A[p * n + j] = t;
+        t = X[k * n + j]; X[k * n + j] = X[p * n + j]; X[p * n + j] = t;
+      }
+    }
+    __syncthreads();
+    const double d = A[k * n + k];
+    if (tid == 0) {
+      if (p != k) sgn = -sgn;
+      sgn *= (d > 0.0) ? 1.0 : ((d < 0.0) ? -1.0 : 0.0);
+      ld += log(fabs(d));
+    }
+    // normalise row k, eliminate column k from all other rows
+    for (int j = tid; j < n; j += nt) {
+      A[k * n + j] /= d;
+      X[k * n + j] /= d;
+    }
+    __syncthreads();
+    for (int e = tid; e < n * n; e += nt) {
+      const int i = e / n, j = e % n;
+      if (i == k) continue;
+      const double f = A[i * n + k];
+      if (j != k) A[i * n + j] -= f * A[k * n + j];
+      X[i * n + j] -= f * X[k * n + j];
+    }
+    __syncthreads();
+    for (int i = tid; i < n; i += nt)
+      if (i != k) A[i * n + k] = 0.0;
+    __syncthreads();
+  }
+  if (mode == 0) {
+    for (int e = tid; e < n * n; e += nt) {
+      const int i = e / n, j = e % n;
+      out[((size_t)i * n + j) * nd + l] = X[e];
+    }
+  } else if (tid == 0) {
+    sign_out[l] = sgn;
+    logdet_part[l] = ld;
+  }
+}
+
+__global__ void sparse_slogdet_reduce(const double* sign_part, const double* ld_part, int nd,
+                                      double* sign_out, double* logdet_out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) {
+    double s = 1.0, ld = 0.0;
+    for (int l = 0; l < nd; ++l) {
+      s *= sign_part[l];
+      ld += ld_part[l];
+    }
+    *sign_out = s;
+    *logdet_out = ld;
+  }
+}
+
+void launch_sparse_inv(const double* sp, int n, int nd, double* out, cudaStream_t st) {
+  const size_t smem = 2 * (size_t)n * n * sizeof(double);
+  cudaFuncSetAttribute(sparse_lu_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  sparse_lu_kernel<<<nd, 128, smem, st>>>(sp, n, nd, 0, out, nullptr, nullptr);
+}
+
+void launch_sparse_slogdet(const double* sp, int n, int nd, double* sign_part, double* ld_part,
+                           double* sign_out, double* ld_out, cudaStream_t st) {
+  const size_t smem = 2 * (size_t)n * n * sizeof(double);
+  cudaFuncSetAttribute(sparse_lu_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  sparse_lu_kernel<<<nd, 128, smem, st>>>(sp, n, nd, 1, nullptr, sign_part, ld_part);
+  sparse_slogdet_reduce<<<1, 32, 0, st>>>(sign_part, ld_part, nd, sign_out, ld_out);
+}
+
+// sparse.to_dense (sparse.py:52-68)
+__global__ void sparse_to_dense_kernel(const double* __restrict__ sp, int n, int m, int nd,
+                                       double* __restrict__ out) {
+  const size_t R = (size_t)n * nd, C = (size_t)m * nd;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < R * C;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t row = idx / C, col = idx % C;
+    const int i = (int)(row / nd), l = (int)(row % nd), j = (int)(col / nd), l2 = (int)(col % nd);
+    out[idx] = (l == l2) ? sp[((size_t)i * m + j) * nd + l] : 0.0;
+  }
+}
+
+// sparse @ v (transpose = 0) or v @ sparse (transpose = 1) (sparse.py:140-233)
+__global__ void sparse_dot_vec_kernel(const double* __restrict__ sp, int n, int m, int nd,
+                                      const double* __restrict__ v, int transpose,
+                                      double* __restrict__ out) {
+  const int rows = transpose ? m : n;
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= rows * nd) return;
+  const int i = idx / nd, l = idx % nd;
+  double acc = 0.0;
+  if (!transpose) {
+    for (int j = 0; j < m; ++j) acc += sp[((size_t)i * m + j) * nd + l] * v[(size_t)j * nd + l];
+  } else {
+    for (int j = 0; j < n; ++j) acc += v[(size_t)j * nd + l] * sp[((size_t)j * m + i) * nd + l];
+  }
+  out[idx] = acc;
+}
+
+void launch_sparse_to_dense(const double* sp, int n, int m, int nd, double* out, cudaStream_t st) {
+  const size_t total = (size_t)n * nd * m * nd;
+  size_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  if (blocks == 0) blocks = 1;
+  sparse_to_dense_kernel<<<(unsigned)blocks, 256, 0, st>>>(sp, n, m, nd, out);
+}
+
+void launch_sparse_dot_vec(const double* sp, int n, int m, int nd, const double* v, int transpose,
+                           double* out, cudaStream_t st) {
+  const int rows = (transpose ? m : n) * nd;
+  sparse_dot_vec_kernel<<<(rows + 127) / 128, 128, 0, st>>>(sp, n, m, nd, v, transpose, out);
+}
+
+}  // namespace jcg

@@ -1,0 +1,298 @@
+"""GPU parity: libjcg (through the C ABI, via the Python API) against the golden
+fixtures of the unmodified reference and against the float64 oracle.
+
+Tolerances: FP64 path 1e-9 relative (libm vs CUDA transcendental rounding,
+summation order); FP32C path 1e-4 relative per C_ell (the stated bound of the
+compensated form).
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+import jax_cosmo_gb300 as jc  # noqa: E402
+from oracle import jc_oracle as O  # noqa: E402
+
+RT64 = 1e-9
+RT32 = 1e-4
+
+NAMES = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
+
+
+def rel(a, b):
+    a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else np.asarray(a)
+    b = b.detach().cpu().numpy() if isinstance(b, torch.Tensor) else np.asarray(b)
+    return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
+
+
+def cosmo_of(row):
+    return jc.Cosmology(**{n: float(v) for n, v in zip(NAMES, row)})
+
+
+def cosmo_batch(rows):
+    rows = np.asarray(rows)
+    return jc.Cosmology(**{n: torch.tensor(rows[:, i]) for i, n in enumerate(NAMES)})
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    torch.cuda.set_device(0)
+
+
+# ------------------------------------------------------------- background ---
+def test_background_points_vs_golden(golden):
+    g = golden("background")
+    a = g["a_q"]
+    for i, row in enumerate(g["cosmos"]):
+        c = cosmo_of(row)
+        chi = jc.background.radial_comoving_distance(c, a)
+        pos = g["chi"][i] > 0
+        assert rel(chi[torch.as_tensor(pos)], g["chi"][i][pos]) < RT64
+        assert float(chi[torch.as_tensor(~pos)].abs().max()) < 1e-6
+        assert rel(jc.background.growth_factor(c, a), g["D"][i]) < RT64
+        assert rel(jc.background.H(c, a), g["H"][i]) < RT64
+        assert rel(jc.background.dchioverda(c, a), g["dchioverda"][i]) < RT64
+
+
+def test_background_batched_matches_single(golden):
+    g = golden("background")
+    cb = cosmo_batch(g["cosmos"])
+    chi = jc.background.radial_comoving_distance(cb, g["a_q"])
+    assert chi.shape == (len(g["cosmos"]), len(g["a_q"]))
+    for i, row in enumerate(g["cosmos"]):
+        assert torch.equal(chi[i], jc.background.radial_comoving_distance(cosmo_of(row), g["a_q"]))
+
+
+# ------------------------------------------------------------------ power ---
+def test_power_points_vs_golden(golden):
+    p = golden("power")
+    k = p["k"]
+    for i, row in enumerate(p["cosmos"]):
+        c = cosmo_of(row)
+        assert rel(jc.transfer.Eisenstein_Hu(c, k), p["T"][i]) < RT64
+        for j, a in enumerate(p["a_list"]):
+            assert rel(jc.power.linear_matter_power(c, k, a), p["plin"][i][j]) < RT64
+            assert rel(jc.power.nonlinear_matter_power(c, k, a), p["pnl"][i][j]) < RT64
+        kn, ne, C = jc.power.halofit_parameters(c, p["a_hf"])
+        assert rel(kn, p["k_nl"][i]) < RT64
+        assert rel(ne, p["n_eff"][i]) < RT64
+        assert rel(C, p["C"][i]) < RT64
+        assert rel(jc.power.nonlinear_matter_power(c, p["k_pairs"], p["a_pairs"]), p["pnl_pairs"][i]) < RT64
+
+
+# ---------------------------------------------------------------- tracers ---
+def test_probe_kernels_vs_golden(golden):
+    t = golden("tracers")
+    b = golden("background")
+    zk = t["z_kernel"]
+    for i, row in enumerate(b["cosmos"][:3]):
+        c = cosmo_of(row)
+        pz = [jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10, zmax=4.0),
+              jc.redshift.smail_nz(1.0, 2.0, 1.0, gals_per_arcmin2=10, zmax=4.0)]
+        wl = jc.probes.WeakLensing(pz, sigma_e=0.26).kernel(c, zk, 100.0)
+        assert rel(wl, t["wl_kernel"][i]) < RT64
+        nc = jc.probes.NumberCounts(pz, jc.bias.constant_linear_bias(1.2)).kernel(c, zk, 100.0)
+        assert rel(nc, t["nc_kernel"][i]) < RT64
+
+
+# ------------------------------------------------------------- angular_cl ---
+def _wl2():
+    pz = [jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10, zmax=4.0),
+          jc.redshift.smail_nz(1.0, 2.0, 1.0, gals_per_arcmin2=10, zmax=4.0)]
+    return [jc.probes.WeakLensing(pz, sigma_e=0.26)]
+
+
+def _mixed():
+    pz = [jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10),
+          jc.redshift.smail_nz(1.0, 2.0, 1.0, gals_per_arcmin2=10)]
+    return [jc.probes.WeakLensing(pz, sigma_e=0.26),
+            jc.probes.NumberCounts(pz, jc.bias.constant_linear_bias(1.2))]
+
+
+@pytest.mark.parametrize("name,probes", [("cl_wl2", _wl2), ("cl_mixed", _mixed)])
+def test_angular_cl_vs_golden(golden, name, probes):
+    g = golden(name)
+    for i, row in enumerate(g["cosmos"]):
+        cl = jc.cl.angular_cl(cosmo_of(row), g["ell"], probes())
+        assert cl.shape == g["cl"][i].shape
+        assert rel(cl, g["cl"][i]) < RT64
+        cl32 = jc.cl.angular_cl(cosmo_of(row), g["ell"], probes(), precision="fp32c")
+        assert rel(cl32, g["cl"][i]) < RT32
+
+
+def _oracle_probes(spec):
+    out = []
+    for kind, bins, extra in spec:
+        out.append(O.Probe(kind, [O.Smail(*b) for b in bins], **extra))
+    return out
+
+
+def _jc_probes(spec):
+    out = []
+    for kind, bins, extra in spec:
+        nz = [jc.redshift.smail_nz(a, b, z0, gals_per_arcmin2=ng, zmax=zm) for a, b, z0, zm, ng in bins]
+        if kind == "wl":
+            out.append(jc.probes.WeakLensing(nz, sigma_e=extra.get("sigma_e", 0.26),
+                                             multiplicative_bias=extra.get("m", 0.0)))
+        else:
+            out.append(jc.probes.NumberCounts(nz, jc.bias.constant_linear_bias(extra["bias"])))
+    return out
+
+
+def _oracle_spec(spec):
+    res = []
+    for kind, bins, extra in spec:
+        e = dict(extra)
+        if kind == "wl" and "m" in e:
+            pass
+        res.append((kind, bins, e))
+    return res
+
+
+C1_SPEC = [("wl", [(1.0, 2.0, 0.5, 4.0, 10), (1.0, 2.0, 1.0, 4.0, 10)], {"sigma_e": 0.26})]
+C2_BINS = [(1.0, 2.0, z0, 10.0, 10) for z0 in np.linspace(0.3, 1.5, 5)]
+C2_SPEC = [("wl", C2_BINS, {"sigma_e": 0.26}), ("nc", C2_BINS, {"bias": 1.2})]
+
+
+@pytest.mark.parametrize(
+    "spec,ell,n_limber",
+    [
+        (C1_SPEC, np.logspace(1, np.log10(3000), 50), 256),  # BASELINE config 1: N = 256, zmax = 4
+        (C2_SPEC, np.logspace(1, np.log10(5000), 24), 512),  # config 2 tracers, 55 spectra
+        ([("wl", [(1.0, 2.0, 0.7, 3.0, 5)], {"sigma_e": 0.3, "m": 0.02}),
+          ("nc", [(2.0, 1.5, 0.4, 2.5, 3), (1.0, 2.0, 0.9, 5.0, 4)], {"bias": 0.9})],
+         np.array([2.0, 7.5, 33.0, 480.0, 2999.0]), 200),   # ragged zmax, m != 0, odd ell
+    ],
+)
+def test_angular_cl_vs_oracle(spec, ell, n_limber):
+    rows = [[0.2589, 0.0486, 0.6774, 0.9667, 0.8159, 0.0, -1.0, 0.0],
+            [0.31, 0.045, 0.66, 0.98, 0.72, 0.0, -0.85, 0.15]]
+    oracle_probes = []
+    for kind, bins, extra in spec:
+        e = {}
+        if kind == "wl":
+            e["sigma_e"] = extra.get("sigma_e", 0.26)
+            e["m"] = extra.get("m", 0.0)
+        else:
+            e["bias"] = extra["bias"]
+        oracle_probes.append(O.Probe(kind, [O.Smail(a, b, z0, zm, ng) for a, b, z0, zm, ng in bins], **e))
+    cb = cosmo_batch(rows)
+    cl = jc.cl.angular_cl(cb, ell, _jc_probes(spec), n_limber=n_limber)
+    cl32 = jc.cl.angular_cl(cb, ell, _jc_probes(spec), n_limber=n_limber, precision="fp32c")
+    for i, row in enumerate(rows):
+        ref = O.angular_cl(O.Cosmo.from_vector(row), ell, oracle_probes, n_limber=n_limber)
+        assert rel(cl[i], ref) < RT64
+        assert rel(cl32[i], ref) < RT32
+        # batch entry == single call, bit for bit
+        single = jc.cl.angular_cl(cosmo_of(row), ell, _jc_probes(spec), n_limber=n_limber)
+        assert torch.equal(single, cl[i])
+
+
+def test_angular_cl_edge_cases():
+    c = jc.Planck15()
+    # one ell, one tracer
+    p1 = [jc.probes.NumberCounts([jc.redshift.smail_nz(1.0, 2.0, 0.8)], jc.bias.constant_linear_bias(1.0))]
+    cl = jc.cl.angular_cl(c, 100.0, p1)
+    ref = O.angular_cl(O.planck15(), [100.0], [O.Probe("nc", [O.Smail(1.0, 2.0, 0.8)], bias=1.0)])
+    assert cl.shape == (1, 1) and rel(cl, ref) < RT64
+    with pytest.raises(ValueError):
+        jc.cl.angular_cl(c, [10.0, 20.0], p1, n_limber=255)  # Simpson needs even N
+    with pytest.raises(NotImplementedError):
+        jc.cl.angular_cl(c, [10.0], p1, transfer_fn=lambda *a: None)
+    # 16 tracers (136 spectra): the maximum request size
+    nz = [jc.redshift.smail_nz(1.0, 2.0, z0) for z0 in np.linspace(0.3, 1.5, 8)]
+    p16 = [jc.probes.WeakLensing(nz), jc.probes.NumberCounts(nz, jc.bias.constant_linear_bias(1.1))]
+    ell = np.logspace(1, 3, 6)
+    cl16 = jc.cl.angular_cl(c, ell, p16)
+    o16 = [O.Probe("wl", [O.Smail(1.0, 2.0, z0) for z0 in np.linspace(0.3, 1.5, 8)]),
+           O.Probe("nc", [O.Smail(1.0, 2.0, z0) for z0 in np.linspace(0.3, 1.5, 8)], bias=1.1)]
+    ref16 = O.angular_cl(O.planck15(), ell, o16)
+    assert cl16.shape == (136, 6) and rel(cl16, ref16) < RT64
+    assert torch.isfinite(jc.cl.angular_cl(c, ell, p16, precision="fp32c")).all()
+
+
+# ------------------------------------------------------ covariance / like ---
+def test_covariance_and_likelihood_vs_golden(golden):
+    cv = golden("cov_like")
+    nz1 = jc.redshift.smail_nz(1.0, 2.0, 1.0)
+    nz2 = jc.redshift.smail_nz(1.0, 2.0, 0.5)
+    P = [jc.probes.NumberCounts([nz1, nz2], jc.bias.constant_linear_bias(1.0))]
+    c = jc.Planck15()
+    mu, cov_sp = jc.cl.gaussian_cl_covariance_and_mean(c, cv["nc_ell"], P, sparse=True)
+    mu_d, cov_d = jc.cl.gaussian_cl_covariance_and_mean(c, cv["nc_ell"], P, sparse=False)
+    assert rel(mu, cv["nc_mu"]) < RT64
+    assert rel(cov_sp, cv["nc_cov_sparse"]) < RT64
+    nzm = cv["nc_cov_dense"] != 0
+    assert np.array_equal(cov_d.cpu().numpy() != 0, nzm)
+    assert rel(cov_d.cpu().numpy()[nzm], cv["nc_cov_dense"][nzm]) < RT64
+    assert rel(jc.cl.noise_cl(cv["nc_ell"], P), cv["nc_cl_noise"]) < 1e-14
+    data = torch.as_tensor(cv["nc_data"])
+    mu_g = torch.as_tensor(cv["nc_mu"])
+    for inc in (True, False):
+        ll = jc.likelihood.gaussian_log_likelihood(data, mu_g, torch.as_tensor(cv["nc_cov_sparse"]), inc)
+        assert rel(ll, cv[f"nc_ll_sparse_{inc}"]) < 1e-10
+        for m in ("inverse", "cholesky"):
+            ll = jc.likelihood.gaussian_log_likelihood(data, mu_g, torch.as_tensor(cv["nc_cov_dense"]), inc, m)
+            assert rel(ll, cv[f"nc_ll_{m}_{inc}"]) < 1e-10
+    # fixed signal / noise (tests/test_angular_cl.py:201-213 pattern): exact
+    sig, noi = cv["fixed_signal"], cv["fixed_noise"]
+    d = jc.cl.gaussian_cl_covariance(cv["fixed_ell"], P, sig, noi, f_sky=0.3, sparse=False)
+    s = jc.cl.gaussian_cl_covariance(cv["fixed_ell"], P, sig, noi, f_sky=0.3, sparse=True)
+    assert np.array_equal(d.cpu().numpy(), cv["fixed_cov_dense"])
+    assert np.array_equal(s.cpu().numpy(), cv["fixed_cov_sparse"])
+    assert torch.equal(jc.sparse.to_dense(s), d)
+
+
+def test_likelihood_unstructured_dense_and_batched():
+    torch.manual_seed(0)
+    N = 12
+    A = torch.randn(N, N, dtype=torch.float64)
+    C = A @ A.T + N * torch.eye(N, dtype=torch.float64)
+    mu = torch.randn(N, dtype=torch.float64)
+    data = torch.randn(N, dtype=torch.float64)
+    ll = jc.likelihood.gaussian_log_likelihood(data, mu, C)
+    ref = O.gaussian_log_likelihood(data, mu, C)
+    assert rel(ll, ref) < 1e-11
+    # batched sparse
+    sp = torch.rand(3, 3, 5, dtype=torch.float64)
+    sp = torch.einsum("ijl,kjl->ikl", sp, sp) + 3 * torch.eye(3, dtype=torch.float64)[:, :, None]
+    spb = torch.stack([sp, 2 * sp])
+    mub = torch.randn(2, 15, dtype=torch.float64)
+    db = torch.randn(2, 15, dtype=torch.float64)
+    llb = jc.likelihood.gaussian_log_likelihood(db, mub, spb)
+    for i in range(2):
+        assert rel(llb[i], O.gaussian_log_likelihood(db[i], mub[i], spb[i])) < 1e-11
+
+
+# ----------------------------------------------------------------- sparse ---
+def test_sparse_vs_golden(golden):
+    sp = golden("sparse")
+    S = torch.as_tensor(sp["sparse"])
+    assert rel(jc.sparse.inv(S), sp["inv"]) < 1e-11
+    sign, ld = jc.sparse.slogdet(S)
+    assert float(sign) == float(sp["sign"]) and rel(ld, sp["logdet"]) < 1e-12
+    assert np.array_equal(jc.sparse.to_dense(S).cpu().numpy(), sp["dense"])
+    assert rel(jc.sparse.dot(S, sp["v"]), sp["dot_vec"]) < 1e-12
+    assert rel(jc.sparse.dot(sp["v"], S), sp["vec_dot"]) < 1e-12
+    assert rel(jc.sparse.dot(sp["v"].reshape(1, -1), S, sp["v"].reshape(-1, 1)), sp["bilinear"]) < 1e-12
+
+
+def test_sparse_known_answers():
+    """The integer known-answer cases of the reference's tests/test_sparse.py."""
+    X = torch.tensor([[[1, 2, 3], [4, 5, 6], [-1, -2, -3]], [[1, 2, 3], [-4, -5, -6], [7, 8, 9]]],
+                     dtype=torch.float64)
+    D = jc.sparse.to_dense(X).cpu()
+    assert D.shape == (6, 9)
+    assert D[0, 3] == 4 and D[1, 4] == 5 and D[5, 8] == 9 and D[3, 3] == -4 and D[0, 1] == 0
+    with pytest.raises(ValueError):
+        jc.sparse.to_dense([1, 2, 3])
+    Xi = torch.tensor([[[1.0, 1.0], [1.0, 1.0]], [[1.0, 1.0], [2.0, 2.0]]], dtype=torch.float64)
+    ans = torch.tensor([[[2.0, 2.0], [-1.0, -1.0]], [[-1.0, -1.0], [1.0, 1.0]]], dtype=torch.float64)
+    assert rel(jc.sparse.inv(Xi), ans) < 1e-14
+    Xd = torch.tensor([[[1, 2, 3], [4, 5, 6], [-1, 7, -2]], [[1, 2, 3], [-4, -5, -6], [2, -3, 9]],
+                       [[7, 8, 9], [5, -4, 6], [-3, -2, -1]]], dtype=torch.float64)
+    assert float(-jc.sparse.det(-Xd)) == pytest.approx(float(jc.sparse.det(Xd)), rel=1e-12)
+    assert float(jc.sparse.det(Xd)) == pytest.approx(float(np.linalg.det(jc.sparse.to_dense(Xd).cpu().numpy())), rel=1e-6)

@@ -1,0 +1,88 @@
+"""Host-side logic of the Python API (no GPU): descriptors, orderings, batching."""
+import numpy as np
+import pytest
+import torch
+
+import jax_cosmo_gb300 as jc
+from jax_cosmo_gb300 import _geometry, _lib
+from oracle import jc_oracle as O
+
+
+def _probes():
+    nz = [jc.redshift.smail_nz(1.0, 2.0, z0, gals_per_arcmin2=10 + i) for i, z0 in enumerate((0.5, 1.0))]
+    return [
+        jc.probes.WeakLensing(nz, sigma_e=0.3, multiplicative_bias=[0.01, -0.02]),
+        jc.probes.NumberCounts(nz, jc.bias.constant_linear_bias(1.2)),
+    ]
+
+
+def test_describe_fills_descriptor():
+    g = _geometry.describe(_probes(), 7, 256)
+    assert g.n_tracers == 4 and g.n_ell == 7 and g.n_limber == 256 and g.zmax == 10.0
+    assert list(g.kind)[:4] == [_lib.TRACER_WL] * 2 + [_lib.TRACER_NC] * 2
+    assert g.mult[0] == 0.01 and g.mult[1] == -0.02 and g.mult[2] == 0.0
+    assert g.bias[2] == 1.2 and g.bias[0] == 0.0
+    # noise of probes.py:210-223 and 274-281
+    assert g.noise[0] == pytest.approx(0.3**2 / (10 * 11818102.86004228), rel=1e-15)
+    assert g.noise[3] == pytest.approx(1.0 / (11 * 11818102.86004228), rel=1e-15)
+    assert _geometry.n_cls_of(g) == 10
+
+
+def test_describe_rejects_unsupported():
+    nz = [jc.redshift.smail_nz(1.0, 2.0, 1.0)]
+    with pytest.raises(NotImplementedError):
+        _geometry.describe([jc.probes.WeakLensing(nz, ia_bias=jc.bias.constant_linear_bias(1.0))], 3)
+
+    class other_nz(jc.redshift.redshift_distribution):
+        def pz_fn(self, z):
+            return z
+
+    with pytest.raises(NotImplementedError):
+        _geometry.describe([jc.probes.WeakLensing([other_nz(zmax=3.0)])], 3)
+    with pytest.raises(ValueError):
+        _geometry.describe([jc.probes.WeakLensing([jc.redshift.smail_nz(1, 2, 1)] * 17)], 3)
+
+
+def test_orderings_match_reference_rules():
+    P = _probes()
+    assert jc.cl._get_cl_ordering(P) == O.cl_ordering(4)
+    assert jc.cl._get_cov_blocks_ordering(P) == O.cov_blocks_ordering(4)
+
+
+def test_cosmology_batching():
+    c = jc.Planck15()
+    assert c.batch_size is None
+    p = c.param_tensor("cpu")
+    assert p.shape == (1, 8) and p.dtype == torch.float64
+    assert p[0, 0].item() == 0.2589 and p[0, 6].item() == -1.0
+    cb = jc.Planck15(Omega_c=torch.linspace(0.2, 0.3, 5), sigma8=np.full(5, 0.8))
+    assert cb.batch_size == 5
+    pb = cb.param_tensor("cpu")
+    assert pb.shape == (5, 8)
+    assert torch.allclose(pb[:, 0], torch.linspace(0.2, 0.3, 5, dtype=torch.float64))
+    assert (pb[:, 2] == 0.6774).all()
+    with pytest.raises(ValueError):
+        jc.Planck15(Omega_c=torch.ones(3), h=torch.ones(4)).batch_size
+    with pytest.raises(ValueError):
+        jc.Planck15(Omega_c=float("nan")).param_tensor("cpu")
+    assert jc.Planck15().Omega_m == pytest.approx(0.3075)
+    assert jc.Cosmology.tree_unflatten(*reversed(c.tree_flatten())).h == 0.6774
+
+
+def test_smail_nz_host_evaluation_matches_oracle():
+    nz = jc.redshift.smail_nz(1.0, 2.0, 0.5, zmax=4.0)
+    z = torch.linspace(0, 4, 41, dtype=torch.float64)
+    ref = O.Smail(1.0, 2.0, 0.5, 4.0)(z)
+    assert torch.allclose(nz(z), ref, rtol=1e-14, atol=0)
+
+
+def test_unsupported_options_raise():
+    c = jc.Planck15()
+    with pytest.raises(NotImplementedError):
+        jc.cl._check_fns(lambda *a: None, jc.power.halofit)
+    with pytest.raises(NotImplementedError):
+        jc.cl._check_fns(jc.transfer.Eisenstein_Hu, lambda *a: None)
+    with pytest.raises(ValueError):
+        jc.cl._precision_code("fp16")
+    with pytest.raises(NotImplementedError):
+        jc.Cosmology(0.25, 0.05, 0.7, 0.96, 0.8, 0.0, -1.0, 0.0, gamma=0.55).param_tensor("cpu")
