@@ -118,6 +118,29 @@ int jcg_angular_cl(const jcg_geometry* g, const void* geo_dev, const double* par
                    int n_cosmo, int precision, double* cl_dev, void* workspace,
                    size_t workspace_bytes, cudaStream_t stream);
 
+/* jcg_angular_cl for callers that cannot allocate device memory.
+ * No counterpart in the reference (jax_cosmo lets XLA manage all buffers).
+ * Some callers cannot call cudaMalloc: code running inside another
+ * framework's device callback (an XLA custom call or a JAX host callback)
+ * where the framework has already reserved most of the GPU memory and offers
+ * no way to request scratch, so a cudaMalloc there fails or stalls every
+ * stream of the device.  This entry point takes the same inputs and output as
+ * jcg_angular_cl but no workspace: its scratch is one fixed array of
+ * JCG_NOALLOC_SCRATCH_BYTES in the library's static device memory, which
+ * every GPU that loads libjcg holds until the process exits.  Requests whose
+ * scratch (jcg_workspace_size) exceeds that size are rejected with
+ * JCG_ERR_WORKSPACE before anything runs.  The call allocates nothing.
+ * The first call on a device looks up the array's device address and, if no
+ * earlier call did, builds the constant tables, synchronising `stream` once;
+ * make that first call before any stream capture.  All calls share the one
+ * array: calls whose kernels can overlap on the GPU (different streams without
+ * an ordering between them, or several host threads) race on it, so order
+ * them on one stream.  Every scratch value is written before it is read within
+ * a call, so the contents left by the previous call do not matter. */
+#define JCG_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int jcg_angular_cl_noalloc(const jcg_geometry* g, const void* geo_dev, const double* params_dev,
+                           int n_cosmo, int precision, double* cl_dev, cudaStream_t stream);
+
 /* Stage entry points of the same pipeline (for tests and for callers that keep
  * tables resident).  The workspace is the one of jcg_angular_cl. */
 int jcg_stage_cosmo_tables(const jcg_geometry* g, const double* params_dev, int n_cosmo,

@@ -22,6 +22,7 @@ MAX_TRACERS = 16
 MAX_PAIRS = MAX_TRACERS * (MAX_TRACERS + 1) // 2
 MAX_ELL = 4096
 MAX_LIMBER = 4096
+NOALLOC_SCRATCH_BYTES = 32 * 1024 * 1024
 
 OK = 0
 ERR_ARG = -1
@@ -87,6 +88,7 @@ SIGNATURES = {
     "jcg_geometry_build_nodes": [_PG, _P, _P, _P, _SZ, _P],
     "jcg_workspace_size": [_PG, _I, _I, _PSZ],
     "jcg_angular_cl": [_PG, _P, _P, _I, _I, _P, _P, _SZ, _P],
+    "jcg_angular_cl_noalloc": [_PG, _P, _P, _I, _I, _P, _P],
     "jcg_stage_cosmo_tables": [_PG, _P, _I, _I, _P, _SZ, _P],
     "jcg_stage_halofit_rows": [_PG, _P, _P, _I, _I, _P, _SZ, _P],
     "jcg_stage_tracer_kernels": [_PG, _P, _P, _I, _I, _P, _SZ, _P],

@@ -529,3 +529,82 @@ int jcg_sparse_dot_vec(const double* sp, int n, int m, int nd, const double* v, 
 }
 
 }  // extern "C"
+
+// ------------------------------------------------- no-allocation variant -----
+// Scratch of jcg_angular_cl_noalloc: one fixed array in static device memory,
+// shared by every call on a device (see include/jcg.h for the contract).  It
+// holds the same workspace layout as jcg_angular_cl (per-cosmology tables,
+// halofit rows, radial kernels); every element a call reads is written earlier
+// in the same call, so nothing has to be cleared between calls.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[JCG_NOALLOC_SCRATCH_BYTES];
+static std::mutex g_noalloc_mu;
+static void* g_noalloc_ptr[64];
+
+// Device address of the scratch array for the current device, looked up once
+// per device with that device current.  A host-side reference to the array's
+// name is not a device address, so only this pointer is passed to kernels.
+static int noalloc_scratch(void** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(JCG_ERR_CUDA, "cudaGetDevice failed");
+  if (dev < 0 || dev >= 64) return fail(JCG_ERR_CUDA, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_noalloc_mu);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(JCG_ERR_CUDA, "cudaGetSymbolAddress(scratch): %s", cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = p;
+  }
+  *out = g_noalloc_ptr[dev];
+  return JCG_OK;
+}
+
+// Constant tables for the no-allocation path: built on the caller's stream
+// (no stream of our own is created) and waited for once per device.
+static int const_tables_on(cudaStream_t stream, ConstTables** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return fail(JCG_ERR_CUDA, "cudaGetDevice failed");
+  if (dev < 0 || dev >= 64) return fail(JCG_ERR_CUDA, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lk(g_init_mu);
+  if (!g_init_done[dev]) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_const);
+    if (e != cudaSuccess) return fail(JCG_ERR_CUDA, "cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+    ConstTables* c = static_cast<ConstTables*>(p);
+    launch_const_init(c, stream);
+    e = cudaStreamSynchronize(stream);
+    if (e != cudaSuccess) return fail(JCG_ERR_CUDA, "constant tables: %s", cudaGetErrorString(e));
+    g_const_ptr[dev] = c;
+    g_init_done[dev] = true;
+  }
+  *out = g_const_ptr[dev];
+  return JCG_OK;
+}
+
+extern "C" int jcg_angular_cl_noalloc(const jcg_geometry* g, const void* geo, const double* params,
+                                      int n_cosmo, int precision, double* cl, cudaStream_t stream) {
+  GeoHeader h;
+  int rc = make_header(g, &h);
+  if (rc) return rc;
+  if (!geo || !params || !cl) return fail(JCG_ERR_ARG, "geometry, params or cl is NULL");
+  if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  if (precision != JCG_FP64 && precision != JCG_FP32C) return fail(JCG_ERR_ARG, "precision = %d", precision);
+  if (h.custom_nodes) return fail(JCG_ERR_ARG, "a geometry with caller redshift nodes has no Limber grid");
+  const size_t need = ws_layout(&h, n_cosmo, precision).total;
+  if (need > (size_t)JCG_NOALLOC_SCRATCH_BYTES)
+    return fail(JCG_ERR_WORKSPACE,
+                "jcg_angular_cl_noalloc: %d cosmologies on this geometry need %zu bytes of scratch, "
+                "above the fixed limit of %u bytes; split the batch or use jcg_angular_cl with a "
+                "workspace",
+                n_cosmo, need, (unsigned)JCG_NOALLOC_SCRATCH_BYTES);
+  void* scratch = nullptr;
+  if ((rc = noalloc_scratch(&scratch))) return rc;
+  ConstTables* c = nullptr;
+  if ((rc = const_tables_on(stream, &c))) return rc;
+  const Batch b = make_batch(&h, geo, params, n_cosmo, precision, scratch, cl);
+  launch_cosmo_tables(b, c, stream);
+  launch_halofit_rows(b, c, stream);
+  launch_tracer_kernels(b, c, stream);
+  launch_limber(b, c, limber_tile(h.n_ell), stream);
+  return cuda_check("angular_cl_noalloc");
+}
