@@ -170,12 +170,20 @@ static int make_header(const jcg_geometry* g, GeoHeader* h) {
   h->off_ell = take(h->n_ell);
   h->off_ellfac = take((int64_t)h->n_tr * h->n_ell);
   h->off_lg2ellh = take(h->n_ell);
+  const int64_t half = ((int64_t)na * NZP + 1) / 2;  // 4-byte arrays in 8-byte units
   for (int q = 0; q < h->n_groups; ++q) {
     h->off_ap[q] = take((int64_t)na * NZP);
     h->off_segp[q] = take((int64_t)na * NZP);
+    h->off_q32[q] = take(half);
+    h->off_dx32[q] = take(half);
   }
   for (int t = 0; t < h->n_tr; ++t)
-    if (h->kind[t] == JCG_TRACER_WL) h->off_W[t] = take((int64_t)na * NZP);
+    if (h->kind[t] == JCG_TRACER_WL) {
+      h->off_W[t] = take((int64_t)na * NZP);
+      h->off_W32[t] = take(half);
+    }
+  h->off_qwl32 = take((na + 1) / 2);
+  h->off_dxwl32 = take((na + 1) / 2);
   h->total = o;
   (void)zmx;
   return JCG_OK;

@@ -1,15 +1,23 @@
 // Halofit parameters per Limber node (FP64) and pointwise table queries.
 //
-// One warp per scale-factor node: the sigma^2(R) root find of power.py:96-118
-// (exact argmin over the 256-node table + the decreasing-table side rule of
-// scipy/interpolate.py:47-57) and the spectral moments of power.py:121-139,
-// then the takahashi2012 coefficients of power.py:177-238.
+// Phase 1, one warp per scale-factor node: the sigma^2(R) root find of
+// power.py:96-118 and the spectral moments of power.py:121-139.
+// Phase 2, one thread per node: the takahashi2012 coefficients of
+// power.py:177-238 and the Limber weights.  (Scalar per-node work done by one
+// lane of a warp would hold the float64 pipe for all 32 lanes; GB300's FP64
+// rate is ~1/70 of its FP32 rate, so the per-node scalar work runs
+// thread-parallel instead.)
 #include "jcg_internal.cuh"
 
 namespace jcg {
 
 constexpr double TWO_PI2 = 2.0 * (PI * PI);  // 2.0 * np.pi**2
 constexpr double C2 = C_KMS * C_KMS;          // const.c**2
+constexpr double LN10 = 2.302585092994046;
+constexpr double LOG_KMIN = -0x1.26bb1bbb55515p+3;  // np.log(1e-4)
+constexpr double DLOGK = (0x1.26bb1bbb55516p+3 - -0x1.26bb1bbb55515p+3) / 256.0;
+constexpr double Y2_TAYLOR = 1e-3;  // below: exp(-y^2) by its Taylor series
+constexpr double Y2_SKIP = 60.0;    // above: exp(-y^2) y^4 P k^3 < 1e-20 of the sum
 
 struct HfParams {
   double knl, neff, C;
@@ -21,25 +29,46 @@ __device__ __forceinline__ double warp_sum(double v) {
   return v;
 }
 
+// argmin_j (1 - sig_j g2)^2 with the first index on ties (scipy/interpolate.py:47).
+// v_j = sig_j g2 is strictly decreasing, so (1 - v_j)^2 is unimodal and the
+// minimum is at c - 1 or c, c = #{j : v_j > 1}; c is found by a warp ballot on
+// every 8th node and then on the 8 nodes of the bracket.
+__device__ __forceinline__ int root_argmin_warp(const double* sig, double g2, int lane) {
+  const unsigned full = 0xffffffffu;
+  const bool b1 = sig[8 * lane] * g2 > 1.0;
+  const int L = __popc(__ballot_sync(full, b1));  // v_{8i} > 1 for i < L
+  int c;
+  if (L == 0) {
+    c = 0;
+  } else {
+    const int base = 8 * (L - 1) + 1;  // v_{base-1} > 1
+    const int j = base + (lane & 7);
+    const bool b2 = (lane < 8) && (j < NRT) && (sig[j] * g2 > 1.0);
+    c = base + __popc(__ballot_sync(full, b2));
+  }
+  int best = c < NRT ? c : NRT - 1;
+  if (c >= 1) {
+    const double dlo = 1.0 - sig[c - 1] * g2;
+    const double d2lo = dlo * dlo;
+    if (c < NRT) {
+      const double dhi = 1.0 - sig[c] * g2;
+      best = (d2lo <= dhi * dhi) ? c - 1 : c;
+    } else {
+      best = c - 1;
+    }
+  }
+  return best;
+}
+
 // power.py:96-139 at one scale factor with growth g, for the warp.
-// sig/pk3 may live in shared or global memory.
-__device__ HfParams halofit_params_warp(const double* sig, const double* pk3, double g,
-                                        const ConstTables* __restrict__ c, int lane) {
+// FAST: the moments evaluate exp only for y^2 in [1e-3, 60]; below, the
+// Taylor prefix sums of the cosmology table; above, terms under 1e-20 of the
+// sum are dropped.  Otherwise all 257 nodes with exp, as the reference.
+template <bool FAST>
+__device__ HfParams halofit_params_warp(const double* sig, const double* pk3, const double* ptay,
+                                        double g, const ConstTables* __restrict__ c, int lane) {
   const double g2 = g * g;
-  // argmin_j (1 - sigma_j)^2, first index on ties  (scipy/interpolate.py:47)
-  double bestd = 0.0;
-  int best = -1;
-  for (int j = lane; j < NRT; j += 32) {
-    const double d = 1.0 - sig[j] * g2;
-    const double d2 = d * d;
-    if (best < 0 || d2 < bestd) { bestd = d2; best = j; }
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const double od = __shfl_xor_sync(0xffffffffu, bestd, o);
-    const int oj = __shfl_xor_sync(0xffffffffu, best, o);
-    if (od < bestd || (od == bestd && oj < best)) { bestd = od; best = oj; }
-  }
+  const int best = root_argmin_warp(sig, g2, lane);
   const int ind = best < 1 ? 1 : (best > NRT - 2 ? NRT - 2 : best);
   const double xp_ind = sig[ind] * g2;
   const double lo = sig[1] * g2, hi = sig[NRT - 2] * g2;
@@ -53,58 +82,98 @@ __device__ HfParams halofit_params_warp(const double* sig, const double* pk3, do
   const double R = fmax(exp(root), 1e-6);  // power.py:113-115
   HfParams hp;
   hp.knl = 1.0 / R;  // power.py:118
-  // moments (power.py:121-139): y = k * (1 / k_nl)
-  const double inv = 1.0 / hp.knl;
+  const double inv = 1.0 / hp.knl;  // y = k * (1 / k_nl)
   double s1 = 0.0, s2 = 0.0;
-  for (int i = lane; i < NKH; i += 32) {
-    const double y = c->kh[i] * inv;
-    const double y2 = y * y;
-    const double res = pk3[i] * exp(-y2) * g2 / TWO_PI2;
-    const double t1 = 2 * res * y2;
-    const double t2 = 4 * res * (y2 - y2 * y2);
-    s1 += c->simpson_kh[i] * t1;
-    s2 += c->simpson_kh[i] * t2;
+  if (!FAST) {
+    for (int i = lane; i < NKH; i += 32) {
+      const double y = c->kh[i] * inv;
+      const double y2 = y * y;
+      const double res = pk3[i] * exp(-y2) * g2 / TWO_PI2;
+      s1 += c->simpson_kh[i] * (2 * res * y2);
+      s2 += c->simpson_kh[i] * (4 * res * (y2 - y2 * y2));
+    }
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+  } else {
+    // index range with y_i^2 in [Y2_TAYLOR, Y2_SKIP]
+    const double linv = log(inv);
+    int ilo = (int)floor((0.5 * log(Y2_TAYLOR) - linv - LOG_KMIN) / DLOGK);
+    int ihi = (int)ceil((0.5 * log(Y2_SKIP) - linv - LOG_KMIN) / DLOGK);
+    ilo = max(0, min(ilo, NKH));
+    ihi = max(ilo - 1, min(ihi, NKH - 1));
+    for (int i = ilo + lane; i <= ihi; i += 32) {
+      const double y = c->kh[i] * inv;
+      const double y2 = y * y;
+      const double r = c->simpson_kh[i] * pk3[i] * exp(-y2);
+      s1 += 2 * r * y2;
+      s2 += 4 * r * (y2 - y2 * y2);
+    }
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
+    // sum_{i < ilo} w pk3 y^2 exp(-y^2) = sum_m (-1)^m / m! inv^(2m+2) P_m[ilo]
+    double t1 = 0.0, t2 = 0.0;
+    if (ilo > 0) {
+      const double iv2 = inv * inv;
+      double pw = iv2;  // inv^(2m+2)
+      double fact = 1.0;
+      for (int m = 0; m < NTAYLOR - 1; ++m) {
+        const double sg = (m & 1) ? -1.0 : 1.0;
+        const double a = ptay[m * (NKH + 1) + ilo] * pw;
+        const double a2 = ptay[(m + 1) * (NKH + 1) + ilo] * pw * iv2;
+        t1 += sg / fact * a;
+        t2 += sg / fact * (a - a2);
+        pw *= iv2;
+        fact *= (double)(m + 1);
+      }
+    }
+    s1 = (s1 + 2.0 * t1) * g2 / TWO_PI2;
+    s2 = (s2 + 4.0 * t2) * g2 / TWO_PI2;
   }
-  s1 = warp_sum(s1);
-  s2 = warp_sum(s2);
   hp.neff = s1 - 3.0;
   hp.C = s1 * s1 + s2;
   return hp;
 }
 
-// takahashi2012 coefficients (power.py:177-238) into a FP64 row.
-__device__ void halofit_coefs(const Bg& bg, double a, const HfParams& hp, double* row) {
+// takahashi2012 coefficients (power.py:177-238) into a FP64 row; one thread.
+__device__ void halofit_coefs(const Bg& bg, double a, double lna, const HfParams& hp, double* row) {
   const double n = hp.neff, C = hp.C;
-  const double om_m = bg_omm(bg, a);
-  const double om_de = bg_omde(bg, a);
+  double om_m, om_de;
+  bg_om_l(bg, a, lna, &om_m, &om_de);
   const double w = bg_w(bg, a);
-  const double n2 = n * n, n3 = pow(n, 3.0), n4 = pow(n, 4.0);
+  const double n2 = n * n, n3 = n2 * n, n4 = n2 * n2;
   row[R_KNL] = hp.knl;
   row[R_NEFF] = n;
   row[R_C] = C;
   row[R_OMM] = om_m;
   row[R_OMDE] = om_de;
   row[R_W] = w;
-  row[R_AN] = pow(10.0, 1.5222 + 2.8553 * n + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 -
-                            0.6038 * C + 0.1749 * om_de * (1 + w));
-  row[R_BN] = pow(10.0, -0.5642 + 0.5864 * n + 0.5716 * n2 - 1.5474 * C + 0.2279 * om_de * (1 + w));
-  row[R_CN] = pow(10.0, 0.3698 + 2.0404 * n + 0.8161 * n2 + 0.5869 * C);
+  const double e_an = 1.5222 + 2.8553 * n + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 - 0.6038 * C +
+                      0.1749 * om_de * (1 + w);
+  const double e_bn = -0.5642 + 0.5864 * n + 0.5716 * n2 - 1.5474 * C + 0.2279 * om_de * (1 + w);
+  const double e_cn = 0.3698 + 2.0404 * n + 0.8161 * n2 + 0.5869 * C;
+  row[R_AN] = exp(LN10 * e_an);
+  row[R_BN] = exp(LN10 * e_bn);
+  row[R_CN] = exp(LN10 * e_cn);
   row[R_GAMMAN] = 0.1971 - 0.0843 * n + 0.8460 * C;
   row[R_ALPHAN] = fabs(6.0835 + 1.3373 * n - 0.1959 * n2 - 5.5274 * C);
   row[R_BETAN] = 2.0379 - 0.7354 * n + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
-  row[R_NUN] = pow(10.0, 5.2105 + 3.6902 * n);
-  row[R_F1] = pow(om_m, -0.0307);
-  row[R_F2] = pow(om_m, -0.0585);
-  row[R_F3] = pow(om_m, 0.0743);
+  row[R_NUN] = exp(LN10 * (5.2105 + 3.6902 * n));
+  const double lom = log(om_m);
+  row[R_F1] = exp(-0.0307 * lom);
+  row[R_F2] = exp(-0.0585 * lom);
+  row[R_F3] = exp(0.0743 * lom);
+  row[R_LGKNL] = log(hp.knl);
+  row[R_LGCF3] = LN10 * e_cn + 0.0743 * lom;  // log(c_n f3)
 }
 
 // FP32 row of the compensated fast path from the FP64 row.
 __device__ void row32_from_row64(const double* s, const double* r, float* f) {
   const double chic = fmax(r[R_CHI], 1.0);
+  constexpr double LOG2E = 1.4426950408889634;
   f[F_INVCHI] = (float)(1.0 / chic);
   f[F_CHIC] = (float)chic;
-  f[F_LG2INVCHI] = (float)(-log2(chic));
-  f[F_LG2KNL] = (float)log2(r[R_KNL]);
+  f[F_LG2INVCHI] = (float)(-LOG2E * r[R_LGCHIC]);
+  f[F_LG2KNL] = (float)(LOG2E * r[R_LGKNL]);
   f[F_INVKNL] = (float)(1.0 / r[R_KNL]);
   f[F_D2FAC] = (float)(r[R_G] * r[R_G] * s[S_PKNORM] / TWO_PI2);
   f[F_BETAN] = (float)r[R_BETAN];
@@ -113,15 +182,63 @@ __device__ void row32_from_row64(const double* s, const double* r, float* f) {
   f[F_3F1] = (float)(3.0 * r[R_F1]);
   f[F_F2] = (float)r[R_F2];
   f[F_BN] = (float)r[R_BN];
-  f[F_LG2CF3] = (float)log2(r[R_CN] * r[R_F3]);
+  f[F_LG2CF3] = (float)(LOG2E * r[R_LGCF3]);
   f[F_3MGAMMA] = (float)(3.0 - r[R_GAMMAN]);
   f[F_NUN] = (float)r[R_NUN];
   for (int i = NROW32_USED; i < NROW32; ++i) f[i] = 0.f;
 }
 
+// chi and growth at a from the tables (background.py:242, 488) with the
+// segment chosen by the reference's rule and the precomputed chi slopes.
+__device__ __forceinline__ double chi_at(const CosmoTab* ct, const ConstTables* c, double a, int2 seg) {
+  const int k = min(seg.x, seg.y);
+  return fmax(ct->chi[seg.x] + ct->chi_slope[k] * (a - c->atab_chi[seg.x]), 0.0);
+}
+
 constexpr int HF_WARPS = 8;
 constexpr int HF_NODES_PER_BLOCK = 64;
 
+// Root find of one node by one thread: c = #{j : sig_j g2 > 1} by bisection
+// (the sequence is strictly decreasing), then the argmin among c - 1, c with
+// the first index on ties -- the same index as argmin((1 - sig g2)^2).
+__device__ __forceinline__ double root_knl_thread(const double* sig, double g2,
+                                                  const ConstTables* __restrict__ c) {
+  int lo = 0, hi = NRT;  // invariant: v_j > 1 for j < lo, v_j <= 1 for j >= hi
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (sig[mid] * g2 > 1.0) lo = mid + 1;
+    else hi = mid;
+  }
+  const int cc = lo;
+  int best = cc < NRT ? cc : NRT - 1;
+  if (cc >= 1) {
+    const double dlo = 1.0 - sig[cc - 1] * g2;
+    if (cc < NRT) {
+      const double dhi = 1.0 - sig[cc] * g2;
+      best = (dlo * dlo <= dhi * dhi) ? cc - 1 : cc;
+    } else {
+      best = cc - 1;
+    }
+  }
+  const int ind = best < 1 ? 1 : (best > NRT - 2 ? NRT - 2 : best);
+  const double xp_ind = sig[ind] * g2;
+  const double lo_v = sig[1] * g2, hi_v = sig[NRT - 2] * g2;
+  const double xc = fmin(fmax(1.0, lo_v), hi_v);  // clip(x, xp[1], xp[-2])
+  const int sgn = (xc - xp_ind >= 0.0) ? 1 : -1;
+  const int j2 = ind + sgn;
+  const double slope = (c->logr[j2] - c->logr[ind]) / (sig[j2] * g2 - xp_ind);
+  const double b = c->logr[ind] - slope * xp_ind;
+  const double root = slope * 1.0 + b;
+  const double R = fmax(exp(root), 1e-6);  // power.py:113-115
+  return 1.0 / R;                          // power.py:118
+}
+
+// Three phases per block of 64 Limber nodes of one cosmology:
+//  1a thread per node: growth, chi, root find, k_nl; FAST: the exp index
+//     range and the Taylor part of the moments;
+//  1b warp per node: the exp part of the moments (power.py:121-136);
+//  2  thread per node: n_eff, C and the takahashi2012 coefficients.
+template <bool FAST>
 __global__ void __launch_bounds__(HF_WARPS * 32)
     halofit_rows_kernel(Batch bt, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
@@ -131,60 +248,145 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   const int na = geo->na;
   const int n0 = blockIdx.x * HF_NODES_PER_BLOCK;
   if (n0 >= na) return;
+  constexpr int NB = HF_NODES_PER_BLOCK;
   __shared__ double sig[NRT];
   __shared__ double pk3[NKH];
   __shared__ double s[NSCAL];
-  __shared__ double chi[NCHI];
-  __shared__ double gt[NGROW];
+  __shared__ double knl_s[NB], inv_s[NB], g_s[NB], chi_s[NB], t1_s[NB], t2_s[NB], s1_s[NB], s2_s[NB];
+  __shared__ int ilo_s[NB], ihi_s[NB];
   const CosmoTab* ct = it.ctab;
   for (int i = threadIdx.x; i < NRT; i += blockDim.x) sig[i] = ct->sig[i];
   for (int i = threadIdx.x; i < NKH; i += blockDim.x) pk3[i] = ct->pk3[i];
   for (int i = threadIdx.x; i < NSCAL; i += blockDim.x) s[i] = ct->s[i];
-  for (int i = threadIdx.x; i < NCHI; i += blockDim.x) chi[i] = ct->chi[i];
-  for (int i = threadIdx.x; i < NGROW; i += blockDim.x) gt[i] = ct->g[i];
   __syncthreads();
-  const Bg bg = make_bg(s);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double* A = geo_ptr<double>(geo, geo->off_a);
   const double* WS = geo_ptr<double>(geo, geo->off_wsimp);
   const int64_t* SC = geo_ptr<int64_t>(geo, geo->off_seg_chi);
   const int64_t* SG = geo_ptr<int64_t>(geo, geo->off_seg_grow);
-  const int n_end = min(na, n0 + HF_NODES_PER_BLOCK);
-  for (int n = n0 + warp; n < n_end; n += HF_WARPS) {
+  const int cnt = min(na - n0, NB);
+  // phase 1a
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int n = n0 + t;
     const double a = A[n];
-    const double chiv = fmax(interp_eval(a, c->atab_chi, chi, unpack_seg(SC[n])), 0.0);
-    const double g = clip_lohi(interp_eval(a, c->atab_grow, gt, unpack_seg(SG[n])), 0.0, 1.0);
-    const HfParams hp = halofit_params_warp(sig, pk3, g, c, lane);
+    const double g = clip_lohi(interp_eval(a, c->atab_grow, ct->g, unpack_seg(SG[n])), 0.0, 1.0);
+    const double g2 = g * g;
+    const double knl = root_knl_thread(sig, g2, c);
+    const double inv = 1.0 / knl;  // y = k * (1 / k_nl)
+    g_s[t] = g;
+    knl_s[t] = knl;
+    inv_s[t] = inv;
+    chi_s[t] = chi_at(ct, c, a, unpack_seg(SC[n]));
+    int ilo = 0, ihi = NKH - 1;
+    double t1 = 0.0, t2 = 0.0;
+    if (FAST) {
+      // exp only for y^2 in [Y2_TAYLOR, Y2_SKIP]
+      const double linv = log(inv);
+      ilo = (int)floor((0.5 * log(Y2_TAYLOR) - linv - LOG_KMIN) / DLOGK);
+      ihi = (int)ceil((0.5 * log(Y2_SKIP) - linv - LOG_KMIN) / DLOGK);
+      ilo = max(0, min(ilo, NKH));
+      ihi = max(ilo - 1, min(ihi, NKH - 1));
+      // sum_{i < ilo} w pk3 y^2 e^{-y^2} = sum_m (-1)^m / m! inv^(2m+2) P_m[ilo]
+      if (ilo > 0) {
+        const double iv2 = inv * inv;
+        double pw = iv2, fact = 1.0;
+        for (int m = 0; m < NTAYLOR - 1; ++m) {
+          const double sg = (m & 1) ? -1.0 : 1.0;
+          const double p0 = ct->ptay[m][ilo] * pw;
+          const double p1 = ct->ptay[m + 1][ilo] * pw * iv2;
+          t1 += sg / fact * p0;
+          t2 += sg / fact * (p0 - p1);
+          pw *= iv2;
+          fact *= (double)(m + 1);
+        }
+      }
+    }
+    ilo_s[t] = ilo;
+    ihi_s[t] = ihi;
+    t1_s[t] = t1;
+    t2_s[t] = t2;
+  }
+  __syncthreads();
+  // phase 1b
+  for (int t = warp; t < cnt; t += HF_WARPS) {
+    const double inv = inv_s[t];
+    double s1 = 0.0, s2 = 0.0;
+    if (FAST) {
+      for (int i = ilo_s[t] + lane; i <= ihi_s[t]; i += 32) {
+        const double y = c->kh[i] * inv;
+        const double y2 = y * y;
+        const double r = c->simpson_kh[i] * pk3[i] * exp(-y2);
+        s1 += 2 * r * y2;
+        s2 += 4 * r * (y2 - y2 * y2);
+      }
+    } else {
+      const double g2 = g_s[t] * g_s[t];
+      for (int i = lane; i < NKH; i += 32) {
+        const double y = c->kh[i] * inv;
+        const double y2 = y * y;
+        const double res = pk3[i] * exp(-y2) * g2 / TWO_PI2;
+        s1 += c->simpson_kh[i] * (2 * res * y2);
+        s2 += c->simpson_kh[i] * (4 * res * (y2 - y2 * y2));
+      }
+    }
+    s1 = warp_sum(s1);
+    s2 = warp_sum(s2);
     if (lane == 0) {
-      double row[NROW64];
-      for (int i = 0; i < NROW64; ++i) row[i] = 0.0;
-      row[R_CHI] = chiv;
-      row[R_G] = g;
-      halofit_coefs(bg, a, hp, row);
-      const double dchi = bg_dchioverda(bg, a);
-      row[R_DCHI] = dchi;
-      row[R_U] = WS[n] * dchi / fmax(chiv * chiv, 1.0) / C2;
-      if (it.rows64) {
-        double* dst = it.rows64 + (size_t)n * NROW64;
-        for (int i = 0; i < NROW64; ++i) dst[i] = row[i];
-      }
-      if (it.rows32) {
-        float f[NROW32];
-        row32_from_row64(s, row, f);
-        float* dst = it.rows32 + (size_t)n * NROW32;
-        for (int i = 0; i < NROW32; ++i) dst[i] = f[i];
-      }
+      s1_s[t] = s1;
+      s2_s[t] = s2;
+    }
+  }
+  __syncthreads();
+  // phase 2
+  const Bg bg = make_bg(s);
+  for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+    const int n = n0 + t;
+    const double a = A[n];
+    const double lna = log(a);
+    double s1 = s1_s[t], s2 = s2_s[t];
+    if (FAST) {
+      const double g2 = g_s[t] * g_s[t];
+      s1 = (s1 + 2.0 * t1_s[t]) * g2 / TWO_PI2;
+      s2 = (s2 + 4.0 * t2_s[t]) * g2 / TWO_PI2;
+    }
+    HfParams hp;
+    hp.knl = knl_s[t];
+    hp.neff = s1 - 3.0;  // power.py:138-139
+    hp.C = s1 * s1 + s2;
+    double row[NROW64];
+    for (int i = 0; i < NROW64; ++i) row[i] = 0.0;
+    const double chiv = chi_s[t];
+    row[R_CHI] = chiv;
+    row[R_G] = g_s[t];
+    halofit_coefs(bg, a, lna, hp, row);
+    const double dchi = bg_dchioverda_l(bg, a, lna);
+    row[R_DCHI] = dchi;
+    row[R_U] = WS[n] * dchi / fmax(chiv * chiv, 1.0) / C2;
+    row[R_LGCHIC] = log(fmax(chiv, 1.0));
+    if (it.rows64) {
+      double* dst = it.rows64 + (size_t)n * NROW64;
+      for (int i = 0; i < NROW64; ++i) dst[i] = row[i];
+    }
+    if (it.rows32) {
+      float f[NROW32];
+      row32_from_row64(s, row, f);
+      float* dst = it.rows32 + (size_t)n * NROW32;
+      for (int i = 0; i < NROW32; ++i) dst[i] = f[i];
     }
   }
 }
 
 void launch_halofit_rows(const Batch& b, const ConstTables* c, cudaStream_t st) {
   dim3 grid((b.max_na + HF_NODES_PER_BLOCK - 1) / HF_NODES_PER_BLOCK, b.n_items);
-  halofit_rows_kernel<<<grid, HF_WARPS * 32, 0, st>>>(b, c);
+  if (b.precision == JCG_FP32C)
+    halofit_rows_kernel<true><<<grid, HF_WARPS * 32, 0, st>>>(b, c);
+  else
+    halofit_rows_kernel<false><<<grid, HF_WARPS * 32, 0, st>>>(b, c);
 }
 
 // ------------------------------------------------------ pointwise queries ---
-// One warp per (cosmology, point).  `what` as documented in jcg.h.
+// One warp per (cosmology, point).  `what` as documented in jcg.h.  FP64, the
+// full (reference) form of the moments.
 __global__ void eval_points_kernel(const double* __restrict__ params, int n_cosmo,
                                    const CosmoTab* __restrict__ ctab,
                                    const ConstTables* __restrict__ c, const double* __restrict__ av,
@@ -219,11 +421,11 @@ __global__ void eval_points_kernel(const double* __restrict__ params, int n_cosm
     v = pk_linear(s, k, growth(a));
   } else {
     const double g = growth(a);
-    const HfParams hp = halofit_params_warp(ct->sig, ct->pk3, g, c, lane);
+    const HfParams hp = halofit_params_warp<false>(ct->sig, ct->pk3, nullptr, g, c, lane);
     if (what == 6) {
       double row[NROW64];
       row[R_G] = g;
-      halofit_coefs(bg, a, hp, row);
+      halofit_coefs(bg, a, log(a), hp, row);
       v = halofit_node(s, row, k);
     } else if (what == 7) {
       v = hp.knl;

@@ -58,9 +58,13 @@ enum Scalar {
   S_SIGMASQR8,  // power.py:56-78 at R = 8
   S_PKNORM,     // sigma8^2 / sigmasqr(8): power.py:47
   S_G1,         // growth_factor(a = 1) from the table (power.py:44 with a = 1)
+  S_LGQ,        // log(13.41 k_eq): log q = log k - S_LGQ (transfer.py:122)
+  S_LGKSILK,    // log(k_silk)
   S_NSCALAR
 };
 constexpr int NSCAL = 32;
+constexpr int NTAYLOR = 8;       // Taylor terms of exp(-y^2) below y^2 = 1e-3
+constexpr int PAD_CT = 7;        // keeps sizeof(CosmoTab) a multiple of 64
 static_assert(S_NSCALAR <= NSCAL, "scalar block too small");
 
 struct CosmoTab {
@@ -69,7 +73,13 @@ struct CosmoTab {
   double g[NGROW];     // background.py:483      growth table on atab_grow
   double sig[NRT];     // sigma^2(R_j) at a = 1 without the g(a)^2 factor
   double pk3[NKH];     // linear_matter_power(k_i, a=1) * k_i^3
-  double pad[7];
+  double chi_slope[NCHI];  // slope of the chi table on segment [k, k+1] (k < 255)
+  float chi32[NCHI];       // chi table, float (FP32 lensing kernel)
+  float slope32[NCHI];     // chi_slope, float
+  // prefix sums over the ln k grid of w_i P(k_i) k_i^3 k_i^(2(m+1)), m < NTAYLOR:
+  // the small-y part of the halofit moments as a Taylor series in y^2
+  double ptay[NTAYLOR][NKH + 1];
+  double pad[PAD_CT];
 };
 static_assert(sizeof(CosmoTab) % 64 == 0, "CosmoTab must keep 64-byte alignment");
 
@@ -88,6 +98,9 @@ enum Row64 {
   R_AN, R_BN, R_CN, R_GAMMAN, R_ALPHAN, R_BETAN, R_NUN,    // power.py:200-224
   R_F1, R_F2, R_F3,                                        // power.py:228-238
   R_U,         // simpson weight * dchi / max(chi^2,1) / c^2
+  R_LGKNL,     // log(k_nl)
+  R_LGCF3,     // log(c_n f3)
+  R_LGCHIC,    // log(max(chi, 1))
   NROW64_USED
 };
 constexpr int NROW64 = 24;
@@ -132,6 +145,11 @@ struct GeoHeader {
   int64_t off_lg2ellh;                               // [n_ell] log2(ell + 1/2) (fp32 path)
   int64_t off_ap[MAXTR];                             // per group [na][NZP] a' nodes
   int64_t off_segp[MAXTR];                           // per group [na][NZP] packed segments
+  int64_t off_q32[MAXTR];      // per group [na][NZP] int32: nearest node | segment << 16
+  int64_t off_dx32[MAXTR];     // per group [na][NZP] float: a' - atab_chi[nearest]
+  int64_t off_W32[MAXTR];      // per WL tracer [na][NZP] float weights
+  int64_t off_qwl32;           // [na] int32 chi_wl query (nearest | segment << 16)
+  int64_t off_dxwl32;          // [na] float
   int64_t off_W[MAXTR];                              // per WL tracer [na][NZP] weights
   int64_t total;                                     // bytes / 8
 };
@@ -278,70 +296,115 @@ __device__ __forceinline__ Bg make_bg(const double* s) {
   return b;
 }
 __device__ __forceinline__ double bg_w(const Bg& c, double a) { return c.w0 + (1.0 - a) * c.wa; }
-__device__ __forceinline__ double bg_fde(const Bg& c, double a) {
-  return -3.0 * (1.0 + c.w0 + c.wa) * log(a) + 3.0 * c.wa * (a - 1.0);
+// f_de with ln a given (background.py:90)
+__device__ __forceinline__ double bg_fde_l(const Bg& c, double a, double lna) {
+  return -3.0 * (1.0 + c.w0 + c.wa) * lna + 3.0 * c.wa * (a - 1.0);
 }
-__device__ __forceinline__ double bg_esqr(const Bg& c, double a) {
-  return c.Om * pow(a, -3.0) + c.Ok * pow(a, -2.0) + c.Ode * exp(bg_fde(c, a));
+__device__ __forceinline__ double bg_fde(const Bg& c, double a) { return bg_fde_l(c, a, log(a)); }
+// E^2(a) (background.py:122-126); a^-3, a^-2 by products of 1/a (no float64
+// pow), exp(f_de) skipped when f_de == 0 (w0 = -1, wa = 0), where it is 1.
+__device__ __forceinline__ double bg_esqr_l(const Bg& c, double a, double lna, double* efde) {
+  const double f = bg_fde_l(c, a, lna);
+  const double ef = (f == 0.0) ? 1.0 : exp(f);
+  if (efde) *efde = ef;
+  const double ia = 1.0 / a, ia2 = ia * ia;
+  return c.Om * (ia2 * ia) + c.Ok * ia2 + c.Ode * ef;
 }
+__device__ __forceinline__ double bg_esqr(const Bg& c, double a) { return bg_esqr_l(c, a, log(a), nullptr); }
 __device__ __forceinline__ double bg_H(const Bg& c, double a) { return H0 * sqrt(bg_esqr(c, a)); }
+// Omega_m(a), Omega_de(a) sharing one E^2 (background.py:168, 196)
+__device__ __forceinline__ void bg_om_l(const Bg& c, double a, double lna, double* omm, double* omde) {
+  double ef;
+  const double e2 = bg_esqr_l(c, a, lna, &ef);
+  const double ia = 1.0 / a;
+  *omm = c.Om * (ia * ia * ia) / e2;
+  *omde = c.Ode * ef / e2;
+}
 __device__ __forceinline__ double bg_omm(const Bg& c, double a) {
-  return c.Om * pow(a, -3.0) / bg_esqr(c, a);
+  double m, d;
+  bg_om_l(c, a, log(a), &m, &d);
+  return m;
 }
 __device__ __forceinline__ double bg_omde(const Bg& c, double a) {
-  return c.Ode * exp(bg_fde(c, a)) / bg_esqr(c, a);
+  double m, d;
+  bg_om_l(c, a, log(a), &m, &d);
+  return d;
+}
+// dchi/da = rh / (a^2 E(a)) (background.py:294)
+__device__ __forceinline__ double bg_dchioverda_l(const Bg& c, double a, double lna) {
+  return RH / ((a * a) * sqrt(bg_esqr_l(c, a, lna, nullptr)));
 }
 __device__ __forceinline__ double bg_dchioverda(const Bg& c, double a) {
-  return RH / ((a * a) * sqrt(bg_esqr(c, a)));
+  return bg_dchioverda_l(c, a, log(a));
 }
 
 // ------------------------------------------------------ Eisenstein & Hu ----
-// transfer.py:107-153 (eisenhu_osc), per-k part, FP64, reference order.
-__device__ __forceinline__ double eh_T_tilde(double k1, double alpha, double beta, double k_eq) {
-  const double q = k1 / (13.41 * k_eq);
-  const double L = log(EULER_E + 1.8 * beta * q);
-  const double C = 14.2 / alpha + 386.0 / (1.0 + 69.9 * pow(q, 1.08));
-  return L / (L + C * q * q);
+// transfer.py:107-153 (eisenhu_osc), per-k part, FP64.  Powers are taken as
+// exp(y log x) with the logs shared between terms (log k, log q); on GB300 a
+// float64 pow costs about two exps, and the shared forms change results only
+// at the 1e-15 level.  lk = log(k).
+__device__ __forceinline__ double eh_transfer_lk(const double* s, double k, double lk) {
+  const double k_eq = s[S_K_EQ], sh_d = s[S_SH_D];
+  const double q = k / (13.41 * k_eq);
+  const double q108 = exp(1.08 * (lk - s[S_LGQ]));
+  const double Cb = 386.0 / (1.0 + 69.9 * q108);
+  const double qq = q * q;
+  // T_tilde(k, 1, beta_c), T_tilde(k, alpha_c, beta_c) share L; T_tilde(k, 1, 1)
+  const double L1 = log(EULER_E + 1.8 * s[S_BETA_C] * q);
+  const double L2 = log(EULER_E + 1.8 * q);
+  const double Ta = L1 / (L1 + (14.2 + Cb) * qq);
+  const double Tb = L1 / (L1 + (14.2 / s[S_ALPHA_C] + Cb) * qq);
+  const double Tn = L2 / (L2 + (14.2 + Cb) * qq);
+  const double ksh = k * sh_d;
+  const double x54 = ksh / 5.4, x54s = x54 * x54;
+  const double f = 1.0 / (1.0 + x54s * x54s);
+  const double Tc = f * Ta + (1.0 - f) * Tb;
+  const double bn = s[S_BETA_NODE] / ksh;
+  const double tilde_s = sh_d / cbrt(1.0 + bn * bn * bn);
+  const double x52 = ksh / 5.2;
+  const double bb = s[S_BETA_B] / ksh;
+  const double silk = exp(-exp(1.4 * (lk - s[S_LGKSILK])));
+  const double arg = k * tilde_s;
+  const double sinc = sin(arg) / arg;  // np.sinc(k tilde_s / pi), k > 0
+  const double Tbar = (Tn / (1.0 + x52 * x52) + s[S_ALPHA_B] / (1.0 + bb * bb * bb) * silk) * sinc;
+  return s[S_FB] * Tbar + s[S_FC] * Tc;
 }
 
 __device__ __forceinline__ double eh_transfer(const double* s, double k) {
-  const double k_eq = s[S_K_EQ], sh_d = s[S_SH_D];
-  const double ksh54 = k * sh_d / 5.4;
-  const double f = 1.0 / (1.0 + pow(ksh54, 4.0));
-  const double Tc = f * eh_T_tilde(k, 1.0, s[S_BETA_C], k_eq) +
-                    (1.0 - f) * eh_T_tilde(k, s[S_ALPHA_C], s[S_BETA_C], k_eq);
-  const double bn = s[S_BETA_NODE] / (k * sh_d);
-  const double tilde_s = sh_d / pow(1.0 + pow(bn, 3.0), 1.0 / 3.0);
-  const double ksh52 = k * sh_d / 5.2;
-  const double bb = s[S_BETA_B] / (k * sh_d);
-  const double xs = k * tilde_s / PI;
-  const double px = PI * xs;
-  const double sinc = sin(px) / px;  // np.sinc(x) = sin(pi x) / (pi x), x != 0
-  const double Tb = (eh_T_tilde(k, 1.0, 1.0, k_eq) / (1.0 + ksh52 * ksh52) +
-                     s[S_ALPHA_B] / (1.0 + pow(bb, 3.0)) * exp(-pow(k / s[S_K_SILK], 1.4))) *
-                    sinc;
-  return s[S_FB] * Tb + s[S_FC] * Tc;
+  return eh_transfer_lk(s, k, log(k));
 }
 
 // linear_matter_power(k, a) with g = growth_factor(a): power.py:42-53
-__device__ __forceinline__ double pk_linear(const double* s, double k, double g) {
-  const double t = eh_transfer(s, k);
-  double pk = pow(k, s[S_NS]) * (t * t) * (g * g);
+__device__ __forceinline__ double pk_linear_lk(const double* s, double k, double lk, double g) {
+  const double t = eh_transfer_lk(s, k, lk);
+  double pk = exp(s[S_NS] * lk) * (t * t) * (g * g);
   return pk * s[S_PKNORM];
 }
+__device__ __forceinline__ double pk_linear(const double* s, double k, double g) {
+  return pk_linear_lk(s, k, log(k), g);
+}
 
-// halofit takahashi2012 per-node evaluation: power.py:246-260
-__device__ __forceinline__ double halofit_node(const double* s, const double* row, double k) {
-  const double pklin = pk_linear(s, k, row[R_G]);
-  const double d2l = pow(k, 3.0) * pklin / (2.0 * (PI * PI));
+// halofit takahashi2012 per-node evaluation (power.py:246-260), FP64, with
+// log k given and the row's log k_nl and log(c_n f3).
+__device__ __forceinline__ double halofit_node_lk(const double* s, const double* row, double k,
+                                                  double lk) {
+  const double pklin = pk_linear_lk(s, k, lk, row[R_G]);
+  const double k3 = k * k * k;
+  const double d2l = k3 * pklin / (2.0 * (PI * PI));
   const double y = k / row[R_KNL];
+  const double ly = lk - row[R_LGKNL];
   const double fy = y / 4.0 + (y * y) / 8.0;
-  const double d2q = d2l * (pow(1.0 + d2l, row[R_BETAN]) / (1 + row[R_ALPHAN] * d2l)) * exp(-fy);
+  const double d2q =
+      d2l * (exp(row[R_BETAN] * log(1.0 + d2l)) / (1 + row[R_ALPHAN] * d2l)) * exp(-fy);
   const double d2hprime =
-      row[R_AN] * pow(y, 3 * row[R_F1]) /
-      (1.0 + row[R_BN] * pow(y, row[R_F2]) + pow(row[R_CN] * row[R_F3] * y, 3.0 - row[R_GAMMAN]));
-  const double d2h = d2hprime / (1.0 + 0.0 / y + row[R_NUN] / (y * y));
-  return 2.0 * (PI * PI) / pow(k, 3.0) * (d2q + d2h);
+      row[R_AN] * exp(3 * row[R_F1] * ly) /
+      (1.0 + row[R_BN] * exp(row[R_F2] * ly) + exp((3.0 - row[R_GAMMAN]) * (row[R_LGCF3] + ly)));
+  const double y2 = y * y;
+  const double d2h = d2hprime * y2 / (y2 + row[R_NUN]);
+  return 2.0 * (PI * PI) / k3 * (d2q + d2h);
+}
+__device__ __forceinline__ double halofit_node(const double* s, const double* row, double k) {
+  return halofit_node_lk(s, row, k, log(k));
 }
 
 // ------------------------------------------------------------- launches ----

@@ -131,7 +131,8 @@ __device__ __forceinline__ float node32(const EH32& e, const float* r, float kh,
 }
 
 // ---------------------------------------------------------------- kernel ---
-template <bool FP32>
+// MAXO: accumulators per thread, >= ceil(LT * n_cls / LB_THREADS).
+template <bool FP32, int MAXO>
 __global__ void __launch_bounds__(LB_THREADS)
     limber_kernel(Batch bt, const ConstTables* __restrict__ c, int LT) {
   using T = typename std::conditional<FP32, float, double>::type;
@@ -145,27 +146,36 @@ __global__ void __launch_bounds__(LB_THREADS)
   if (l0 >= n_ell) return;
   const int lt = min(LT, n_ell - l0);
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* s = reinterpret_cast<double*>(smem_raw);  // NSCAL
-  EH32* e32 = reinterpret_cast<EH32*>(s + NSCAL);   // 1 (padded to 8 doubles)
-  T* rowsS = reinterpret_cast<T*>(s + NSCAL + 8);   // TA * RW
-  T* Ms = rowsS + LB_TA * RW;                        // TA * n_cls
-  T* Pt = Ms + LB_TA * n_cls;                        // TA * LT
+  double* s = reinterpret_cast<double*>(smem_raw);    // NSCAL
+  EH32* e32 = reinterpret_cast<EH32*>(s + NSCAL);     // 1 (padded to 8 doubles)
+  double* ellv = s + NSCAL + 8;                        // LB_MAXLT: l + 1/2 (FP64 path)
+  double* lellv = ellv + LB_MAXLT;                     // LB_MAXLT: log(l + 1/2)
+  float* kh32 = reinterpret_cast<float*>(lellv + LB_MAXLT);  // 3 * LB_MAXLT floats
+  T* rowsS = reinterpret_cast<T*>(kh32 + 3 * LB_MAXLT);      // TA * RW
+  T* Ms = rowsS + LB_TA * RW;                                // TA * n_cls
+  T* Pt = Ms + LB_TA * n_cls;                                // TA * LT
   const int tid = threadIdx.x;
+  const double* ELL = geo_ptr<double>(geo, geo->off_ell);
+  const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
   for (int i = tid; i < NSCAL; i += LB_THREADS) s[i] = it.ctab->s[i];
+  for (int l = tid; l < lt; l += LB_THREADS) {
+    const double e = ELL[l0 + l] + 0.5;
+    ellv[l] = e;
+    lellv[l] = log(e);
+    kh32[3 * l + 0] = (float)e;                               // k = kh / max(chi, 1)
+    kh32[3 * l + 1] = (float)(1.4426950408889634 * log(e));   // log2(kh)
+    kh32[3 * l + 2] = (float)(1.0 / e);                       // 1 / kh
+  }
   __syncthreads();
   if (FP32 && tid == 0) make_eh32(s, e32);
   __syncthreads();
-  const double* ELL = geo_ptr<double>(geo, geo->off_ell);
-  const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
-  const double* LG = geo_ptr<double>(geo, geo->off_lg2ellh);
   const double* rows64 = it.rows64;
   const float* rows32 = it.rows32;
   const double* kern = it.kern;
-  // per-thread P-phase ell values (constant over chunks)
   const int nout = lt * n_cls;
-  T acc[LB_MAXO], comp[LB_MAXO];
+  T acc[MAXO], comp[MAXO];
 #pragma unroll
-  for (int r = 0; r < LB_MAXO; ++r) {
+  for (int r = 0; r < MAXO; ++r) {
     acc[r] = 0;
     comp[r] = 0;
   }
@@ -185,29 +195,31 @@ __global__ void __launch_bounds__(LB_THREADS)
       const int n = base + t;
       const double ki = kern[(size_t)geo->pair_i[p] * na + n];
       const double kj = kern[(size_t)geo->pair_j[p] * na + n];
-      Ms[t * n_cls + p] = (T)((ki * kj) * rows64[(size_t)n * NROW64 + R_U]);
+      const double u = rows64[(size_t)n * NROW64 + R_U];
+      if (FP32)
+        Ms[t * n_cls + p] = (T)((float)ki * (float)kj * (float)u);
+      else
+        Ms[t * n_cls + p] = (T)((ki * kj) * u);
     }
     __syncthreads();
     // P tile: nodes (t, l)
     for (int q = tid; q < tc * lt; q += LB_THREADS) {
       const int t = q / lt, l = q - (q / lt) * lt;
-      const double ell = ELL[l0 + l];
       T pv;
       if (FP32) {
-        const float kh = (float)(ell + 0.5);
-        pv = (T)node32(*e32, reinterpret_cast<const float*>(rowsS) + t * NROW32, kh,
-                       (float)LG[l0 + l], (float)(1.0 / (ell + 0.5)));
+        pv = (T)node32(*e32, reinterpret_cast<const float*>(rowsS) + t * NROW32, kh32[3 * l],
+                       kh32[3 * l + 1], kh32[3 * l + 2]);
       } else {
         const double* row = reinterpret_cast<const double*>(rowsS) + t * NROW64;
-        const double k = (ell + 0.5) / fmax(row[R_CHI], 1.0);
-        pv = (T)halofit_node(s, row, k);
+        const double k = ellv[l] / fmax(row[R_CHI], 1.0);
+        pv = (T)halofit_node_lk(s, row, k, lellv[l] - row[R_LGCHIC]);
       }
       Pt[t * LT + l] = pv;
     }
     __syncthreads();
     // contraction
 #pragma unroll
-    for (int r = 0; r < LB_MAXO; ++r) {
+    for (int r = 0; r < MAXO; ++r) {
       const int o = tid + r * LB_THREADS;
       if (o < nout) {
         const int l = o % lt, p = o / lt;
@@ -226,7 +238,7 @@ __global__ void __launch_bounds__(LB_THREADS)
     __syncthreads();
   }
 #pragma unroll
-  for (int r = 0; r < LB_MAXO; ++r) {
+  for (int r = 0; r < MAXO; ++r) {
     const int o = tid + r * LB_THREADS;
     if (o < nout) {
       const int l = o % lt, p = o / lt;
@@ -242,20 +254,37 @@ __global__ void __launch_bounds__(LB_THREADS)
 size_t limber_smem_bytes(bool fp32, int n_cls, int LT) {
   const size_t el = fp32 ? 4 : 8;
   const size_t rw = fp32 ? NROW32 : NROW64;
-  return (NSCAL + 8) * 8 + el * (LB_TA * rw + (size_t)LB_TA * n_cls + (size_t)LB_TA * LT);
+  return (NSCAL + 8 + 2 * LB_MAXLT) * 8 + 3 * LB_MAXLT * 4 +
+         el * (LB_TA * rw + (size_t)LB_TA * n_cls + (size_t)LB_TA * LT);
+}
+
+template <bool FP32, int MAXO>
+static void launch_limber_t(const Batch& b, const ConstTables* c, int lt, size_t smem, dim3 grid,
+                            cudaStream_t st) {
+  cudaFuncSetAttribute(limber_kernel<FP32, MAXO>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  limber_kernel<FP32, MAXO><<<grid, LB_THREADS, smem, st>>>(b, c, lt);
+}
+
+template <bool FP32>
+static void launch_limber_p(const Batch& b, const ConstTables* c, int lt, size_t smem, dim3 grid,
+                            cudaStream_t st) {
+  const int need = (lt * b.max_cls + LB_THREADS - 1) / LB_THREADS;
+  if (need <= 1) launch_limber_t<FP32, 1>(b, c, lt, smem, grid, st);
+  else if (need <= 2) launch_limber_t<FP32, 2>(b, c, lt, smem, grid, st);
+  else if (need <= 4) launch_limber_t<FP32, 4>(b, c, lt, smem, grid, st);
+  else if (need <= 8) launch_limber_t<FP32, 8>(b, c, lt, smem, grid, st);
+  else launch_limber_t<FP32, LB_MAXO>(b, c, lt, smem, grid, st);
 }
 
 void launch_limber(const Batch& b, const ConstTables* c, int lt, cudaStream_t st) {
   const bool fp32 = b.precision == JCG_FP32C;
   const size_t smem = limber_smem_bytes(fp32, b.max_cls, lt);
   dim3 grid((b.max_ell + lt - 1) / lt, b.n_items);
-  if (fp32) {
-    cudaFuncSetAttribute(limber_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    limber_kernel<true><<<grid, LB_THREADS, smem, st>>>(b, c, lt);
-  } else {
-    cudaFuncSetAttribute(limber_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    limber_kernel<false><<<grid, LB_THREADS, smem, st>>>(b, c, lt);
-  }
+  if (fp32)
+    launch_limber_p<true>(b, c, lt, smem, grid, st);
+  else
+    launch_limber_p<false>(b, c, lt, smem, grid, st);
 }
 
 }  // namespace jcg

@@ -131,7 +131,10 @@ __global__ void geo_tables_kernel(const GeoHeader* __restrict__ hp, double* geo,
     AWL[n] = awl;
     SC[n] = pack_seg(interp_segment_inc(a, c->atab_chi, NCHI, logspace_guess(a, NCHI)));
     SG[n] = pack_seg(interp_segment_inc(a, c->atab_grow, NGROW, logspace_guess(a, NGROW)));
-    SW[n] = pack_seg(interp_segment_inc(awl, c->atab_chi, NCHI, logspace_guess(awl, NCHI)));
+    const int2 swl = interp_segment_inc(awl, c->atab_chi, NCHI, logspace_guess(awl, NCHI));
+    SW[n] = pack_seg(swl);
+    reinterpret_cast<int32_t*>(geo + h.off_qwl32)[n] = swl.x | (min(swl.x, swl.y) << 16);
+    reinterpret_cast<float*>(geo + h.off_dxwl32)[n] = (float)(awl - c->atab_chi[swl.x]);
     for (int t = 0; t < h.n_tr; ++t) NZL[(size_t)t * na + n] = smail_pz(h, t, z) / h.nz_norm[t];
   }
   // ell grid factors (probes.py:73; NumberCounts: 1)
@@ -159,13 +162,19 @@ __global__ void geo_tables_kernel(const GeoHeader* __restrict__ hp, double* geo,
       const double zp = np_linspace(z, zp_max, NZP - 1, j);
       const double ap = 1.0 / (1.0 + zp);
       AP[q] = ap;
-      SP[q] = pack_seg(interp_segment_inc(ap, c->atab_chi, NCHI, logspace_guess(ap, NCHI)));
+      const int2 sg = interp_segment_inc(ap, c->atab_chi, NCHI, logspace_guess(ap, NCHI));
+      SP[q] = pack_seg(sg);
+      // FP32 lensing kernel: nearest node | segment << 16, and a' - a[nearest]
+      reinterpret_cast<int32_t*>(geo + h.off_q32[g])[q] = sg.x | (min(sg.x, sg.y) << 16);
+      reinterpret_cast<float*>(geo + h.off_dx32[g])[q] = (float)(ap - c->atab_chi[sg.x]);
       const double dx = (zp_max - z) / 256;
       const double w = (j == 0 || j == NZP - 1) ? 1.0 : ((j & 1) ? 4.0 : 2.0);
       for (int t = 0; t < h.n_tr; ++t) {
         if (h.kind[t] != JCG_TRACER_WL || h.group[t] != g) continue;
         double* W = geo + h.off_W[t];
-        W[q] = dx / 3 * w * (smail_pz(h, t, zp) / h.nz_norm[t]);
+        const double wv = dx / 3 * w * (smail_pz(h, t, zp) / h.nz_norm[t]);
+        W[q] = wv;
+        reinterpret_cast<float*>(geo + h.off_W32[t])[q] = (float)wv;
       }
     }
   }
@@ -237,18 +246,21 @@ __device__ void cosmo_scalars(const double* p, double* s) {
   s[S_BETA_NODE] = beta_node;
   s[S_FB] = fb;
   s[S_FC] = fc;
+  s[S_LGQ] = log(13.41 * k_eq);
+  s[S_LGKSILK] = log(k_silk);
 }
 
 // dchi/dln a = dchioverda(exp(x)) * exp(x)   (background.py:227-229)
 __device__ __forceinline__ double dchi_dlna(const Bg& b, double x) {
   const double xa = exp(x);
-  return bg_dchioverda(b, xa) * xa;
+  return bg_dchioverda_l(b, xa, x) * xa;
 }
 
 // growth ODE coefficients: D'' = -q D' + r D  (background.py:96-106)
 __device__ __forceinline__ void growth_qr(const Bg& b, double x, double& q, double& r) {
-  const double omm = bg_omm(b, x);
-  q = (2.0 - 0.5 * (omm + (1.0 + 3.0 * bg_w(b, x)) * bg_omde(b, x))) / x;
+  double omm, omde;
+  bg_om_l(b, x, log(x), &omm, &omde);
+  q = (2.0 - 0.5 * (omm + (1.0 + 3.0 * bg_w(b, x)) * omde)) / x;
   r = 1.5 * omm / x / x;
 }
 
@@ -385,6 +397,27 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
     out->sig[j] = dx / 3 * acc;
   }
   for (int i = t; i < NSCAL; i += blockDim.x) out->s[i] = s[i];
+  for (int i = t; i < NCHI; i += blockDim.x) {
+    // segment [i, i+1] slope of the chi table: the `a` of scipy/interpolate.py:55
+    const double sl = (i < NCHI - 1)
+                          ? (chis[i + 1] - chis[i]) / (c->atab_chi[i + 1] - c->atab_chi[i])
+                          : 0.0;
+    out->chi_slope[i] = sl;
+    out->chi32[i] = (float)chis[i];
+    out->slope32[i] = (float)sl;
+  }
+  // Taylor prefix sums of the halofit moments: P_m[i] = sum_{i' < i} w pk3 k^(2m+2)
+  if (t < NTAYLOR) {
+    double acc = 0.0;
+    out->ptay[t][0] = 0.0;
+    for (int i = 0; i < NKH; ++i) {
+      const double k2 = c->kh[i] * c->kh[i];
+      double kp = k2;
+      for (int m = 0; m < t; ++m) kp *= k2;
+      acc += c->simpson_kh[i] * pk3[i] * kp;
+      out->ptay[t][i + 1] = acc;
+    }
+  }
   for (int i = t; i < NCHI; i += blockDim.x) out->chi[i] = chis[i];
   for (int i = t; i < NGROW; i += blockDim.x) out->g[i] = gs[i];
   for (int i = t; i < NKH; i += blockDim.x) out->pk3[i] = pk3[i];
