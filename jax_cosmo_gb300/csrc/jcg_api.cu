@@ -245,6 +245,8 @@ static Batch make_batch(const GeoHeader* h, const void* geo, const double* param
   b.max_ell = h ? h->n_ell : 0;
   b.max_cls = h ? h->n_cls : 0;
   b.max_tr = h ? h->n_tr : 0;
+  b.n_wl = h ? h->n_wl : 0;
+  b.n_wl_groups = h ? h->n_groups : 0;
   return b;
 }
 

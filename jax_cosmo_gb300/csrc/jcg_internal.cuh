@@ -185,6 +185,7 @@ struct Batch {
   double* cl;
   int precision;
   int max_na, max_ell, max_cls, max_tr;
+  int n_wl, n_wl_groups;  // uniform form: WeakLensing tracers and lensing groups
 };
 
 __device__ __forceinline__ Item batch_item(const Batch& b, int i) {

@@ -140,7 +140,121 @@ __global__ void __launch_bounds__(TK_WARPS * 32)
   }
 }
 
+// FP32 lensing kernel for a batch sharing one geometry: lanes are 32
+// cosmologies, warps walk the nodes.  The cosmology-independent lensing grid of
+// a node (segments, offsets, n(z') weights) is the same for every lane, so it
+// is read once per 32 cosmologies; each lane reads its cosmology's chi table
+// from shared memory ([segment][cosmology], conflict-free).
+constexpr int TU_NODES = 32;
+constexpr int TU_PAD = 33;
+
+template <int NW>  // WeakLensing tracers (one lensing group)
+__global__ void __launch_bounds__(256)
+    tracer32_uniform_kernel(Batch bt, const ConstTables* __restrict__ c) {
+  const GeoHeader* geo = bt.geo;
+  const int na = geo->na;
+  const int n0 = blockIdx.x * TU_NODES;
+  const int c0 = blockIdx.y * 32;
+  if (n0 >= na || c0 >= bt.n_items) return;
+  extern __shared__ float tu_smem[];
+  float* chiT = tu_smem;               // [NCHI][TU_PAD]
+  float* slT = tu_smem + NCHI * TU_PAD;  // [NCHI][TU_PAD]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int idx = tid; idx < 32 * NCHI; idx += blockDim.x) {
+    const int cc = idx / NCHI, sidx = idx % NCHI;
+    const int ci = c0 + cc;
+    float cv = 0.f, sv = 0.f;
+    if (ci < bt.n_items) {
+      const CosmoTab* ct = bt.ctab + ci;
+      cv = ct->chi32[sidx];
+      sv = ct->slope32[sidx];
+    }
+    chiT[sidx * TU_PAD + cc] = cv;
+    slT[sidx * TU_PAD + cc] = sv;
+  }
+  __syncthreads();
+  const int ci = c0 + lane;
+  const bool live = ci < bt.n_items;
+  const CosmoTab* ct = bt.ctab + (live ? ci : 0);
+  const double om = ct->s[S_OMEGA_M];
+  const Bg bg = make_bg(ct->s);
+  const double cf = 3.0 * (H0 * H0) * om / 2.0 / C_KMS;  // probes.py:71
+  const int n_tr = geo->n_tr;
+  const double* Z = geo_ptr<double>(geo, geo->off_z);
+  const double* AWL = geo_ptr<double>(geo, geo->off_awl);
+  const int32_t* QWL = geo_ptr<int32_t>(geo, geo->off_qwl32);
+  const float* DXWL = geo_ptr<float>(geo, geo->off_dxwl32);
+  const double* NZL = geo_ptr<double>(geo, geo->off_nzl);
+  double* kern = bt.kern + (size_t)(live ? ci : 0) * bt.max_tr * na;
+  const int n_end = min(na, n0 + TU_NODES);
+  // the WeakLensing tracers in order, and their float weights
+  int wl_t[NW];
+  {
+    int u = 0;
+    for (int t = 0; t < n_tr && u < NW; ++t)
+      if (geo->kind[t] == JCG_TRACER_WL) wl_t[u++] = t;
+  }
+  const int32_t* Q32b = geo_ptr<int32_t>(geo, geo->off_q32[0]);
+  const float* DX32b = geo_ptr<float>(geo, geo->off_dx32[0]);
+  for (int n = n0 + warp; n < n_end; n += 8) {
+    const int qw = QWL[n];
+    const float chi_wl =
+        fmaxf(chiT[(qw & 0xffff) * TU_PAD + lane] + slT[(qw >> 16) * TU_PAD + lane] * DXWL[n], 0.f);
+    float acc[NW];
+#pragma unroll
+    for (int u = 0; u < NW; ++u) acc[u] = 0.f;
+    const size_t row = (size_t)n * NZP;
+    const float* Wr[NW];
+#pragma unroll
+    for (int u = 0; u < NW; ++u) Wr[u] = geo_ptr<float>(geo, geo->off_W32[wl_t[u]]) + row;
+    for (int j = 0; j < NZP; ++j) {
+      const int q = Q32b[row + j];
+      const float chip = fmaxf(
+          chiT[(q & 0xffff) * TU_PAD + lane] + slT[(q >> 16) * TU_PAD + lane] * DX32b[row + j], 0.f);
+      const float ratio = fmaxf(chip - chi_wl, 0.f) * rcp_approx(fmaxf(chip, 1.f));
+#pragma unroll
+      for (int u = 0; u < NW; ++u) acc[u] += Wr[u][j] * ratio;
+    }
+    if (live) {
+      const double z = Z[n];
+#pragma unroll
+      for (int u = 0; u < NW; ++u) {
+        const int t = wl_t[u];
+        kern[(size_t)t * na + n] =
+            cf * ((double)acc[u] * (1.0 + z) * (double)chi_wl) * (1.0 + geo->mult[t]);
+      }
+      if (geo->n_nc > 0) {
+        const double hz = bg_H(bg, AWL[n]);
+        for (int t = 0; t < n_tr; ++t)
+          if (geo->kind[t] != JCG_TRACER_WL)
+            kern[(size_t)t * na + n] = NZL[(size_t)t * na + n] * geo->bias[t] * hz;
+      }
+    }
+  }
+}
+
+template <int NW>
+static void launch_tu(const Batch& b, const ConstTables* c, cudaStream_t st) {
+  const size_t smem = 2 * NCHI * TU_PAD * sizeof(float);
+  cudaFuncSetAttribute(tracer32_uniform_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)smem);
+  dim3 grid((b.max_na + TU_NODES - 1) / TU_NODES, (b.n_items + 31) / 32);
+  tracer32_uniform_kernel<NW><<<grid, 256, smem, st>>>(b, c);
+}
+
 void launch_tracer_kernels(const Batch& b, const ConstTables* c, cudaStream_t st) {
+  if (b.precision == JCG_FP32C && !b.listed && b.n_wl_groups == 1 && b.n_wl >= 1 && b.n_wl <= 8) {
+    switch (b.n_wl) {
+      case 1: launch_tu<1>(b, c, st); return;
+      case 2: launch_tu<2>(b, c, st); return;
+      case 3: launch_tu<3>(b, c, st); return;
+      case 4: launch_tu<4>(b, c, st); return;
+      case 5: launch_tu<5>(b, c, st); return;
+      case 6: launch_tu<6>(b, c, st); return;
+      case 7: launch_tu<7>(b, c, st); return;
+      default: launch_tu<8>(b, c, st); return;
+    }
+  }
   dim3 grid((b.max_na + TK_NODES_PER_BLOCK - 1) / TK_NODES_PER_BLOCK, b.n_items);
   if (b.precision == JCG_FP32C)
     tracer_kernels_kernel<true><<<grid, TK_WARPS * 32, 0, st>>>(b, c);

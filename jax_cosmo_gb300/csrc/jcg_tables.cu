@@ -270,6 +270,8 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   const Item it = batch_item(bt, item);
   __shared__ double s[NSCAL];
   __shared__ double inc[NCHI];
+  __shared__ double fnode[NCHI];
+  __shared__ double pq[NKH];
   __shared__ double qa[NGROW], ra[NGROW], qm[NGROW], rm[NGROW];
   __shared__ double fr[NROMB];
   __shared__ double pk3[NKH];
@@ -279,19 +281,15 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   if (t == 0) cosmo_scalars(it.params, s);
   __syncthreads();
   const Bg bg = make_bg(s);
-  // chi increments of RK4 in ln a (background.py:227-231, scipy/ode.py:11-19)
+  // chi RK4 in ln a (background.py:227-231, scipy/ode.py:11-19): the
+  // right-hand side does not depend on chi, so each step needs f at its two
+  // ends (shared with the neighbouring steps) and at its midpoint.
   if (t < NCHI) {
-    double v = 0.0;
+    fnode[t] = dchi_dlna(bg, c->lna_chi[t]);
     if (t > 0) {
       const double t0 = c->lna_chi[t - 1], t1 = c->lna_chi[t];
-      const double hh = t1 - t0;
-      const double k1 = dchi_dlna(bg, t0);
-      const double k2 = dchi_dlna(bg, t0 + hh / 2);
-      const double k3 = k2;
-      const double k4 = dchi_dlna(bg, t1);
-      v = 1.0 / 6.0 * hh * (k1 + 2 * k2 + 2 * k3 + k4);
+      inc[t] = dchi_dlna(bg, t0 + (t1 - t0) / 2);
     }
-    inc[t] = v;
   }
   // growth ODE coefficients at nodes and midpoints
   if (t < NGROW) {
@@ -316,10 +314,14 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   }
   __syncthreads();
   if (t == 0) {
-    // chi: sequential prefix sum in the reference's order, then chi[-1] - chi
+    // chi: RK4 increments summed sequentially in the reference's order, then
+    // chi[-1] - chi.  The first step has h = 0 (scipy/ode.py:21).
     double y = 0.0;
-    for (int i = 0; i < NCHI; ++i) {
-      y = y + inc[i];
+    inc[0] = 0.0;
+    for (int i = 1; i < NCHI; ++i) {
+      const double hh = c->lna_chi[i] - c->lna_chi[i - 1];
+      const double fm = inc[i];
+      y = y + 1.0 / 6.0 * hh * (fnode[i - 1] + 2 * fm + 2 * fm + fnode[i]);
       inc[i] = y;
     }
     for (int i = 0; i < NCHI; ++i) chis[i] = inc[NCHI - 1] - inc[i];
@@ -383,14 +385,16 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   }
   __syncthreads();
   // sigma^2(R_j) without g^2: simps over ln k of pk k^3 exp(-(k R)^2) / (2 pi^2)
+  // (the division by 2 pi^2 is taken once per k node, not per (k, R) term)
+  for (int i = t; i < NKH; i += blockDim.x) pq[i] = pk3[i] / (2.0 * (PI * PI));
+  __syncthreads();
   CosmoTab* out = it.ctab;
   for (int j = t; j < NRT; j += blockDim.x) {
-    const double twopi2 = 2.0 * (PI * PI);
     double acc = 0.0;
     for (int m = 0; m < 128; ++m) {
-      const double y0 = pk3[2 * m] * c->E[(2 * m) * NRT + j] / twopi2;
-      const double y1 = pk3[2 * m + 1] * c->E[(2 * m + 1) * NRT + j] / twopi2;
-      const double y2 = pk3[2 * m + 2] * c->E[(2 * m + 2) * NRT + j] / twopi2;
+      const double y0 = pq[2 * m] * c->E[(2 * m) * NRT + j];
+      const double y1 = pq[2 * m + 1] * c->E[(2 * m + 1) * NRT + j];
+      const double y2 = pq[2 * m + 2] * c->E[(2 * m + 2) * NRT + j];
       acc += y0 + 4 * y1 + y2;
     }
     const double dx = (kLogKMax - kLogKMin) / 256;
@@ -406,16 +410,30 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
     out->chi32[i] = (float)chis[i];
     out->slope32[i] = (float)sl;
   }
-  // Taylor prefix sums of the halofit moments: P_m[i] = sum_{i' < i} w pk3 k^(2m+2)
-  if (t < NTAYLOR) {
-    double acc = 0.0;
-    out->ptay[t][0] = 0.0;
-    for (int i = 0; i < NKH; ++i) {
-      const double k2 = c->kh[i] * c->kh[i];
-      double kp = k2;
-      for (int m = 0; m < t; ++m) kp *= k2;
-      acc += c->simpson_kh[i] * pk3[i] * kp;
-      out->ptay[t][i + 1] = acc;
+  // Taylor prefix sums of the halofit moments: P_m[i] = sum_{i' < i} w pk3 k^(2m+2),
+  // one warp per m with a warp-wide inclusive scan over chunks of 32 nodes.
+  {
+    const int m = t >> 5, lane = t & 31;
+    if (m < NTAYLOR) {
+      if (lane == 0) out->ptay[m][0] = 0.0;
+      double carry = 0.0;
+      for (int base = 0; base < NKH; base += 32) {
+        const int i = base + lane;
+        double v = 0.0;
+        if (i < NKH) {
+          const double k2 = c->kh[i] * c->kh[i];
+          double kp = k2;
+          for (int q = 0; q < m; ++q) kp *= k2;
+          v = c->simpson_kh[i] * pk3[i] * kp;
+        }
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const double u = __shfl_up_sync(0xffffffffu, v, o);
+          if (lane >= o) v += u;
+        }
+        if (i < NKH) out->ptay[m][i + 1] = carry + v;
+        carry += __shfl_sync(0xffffffffu, v, 31);
+      }
     }
   }
   for (int i = t; i < NCHI; i += blockDim.x) out->chi[i] = chis[i];

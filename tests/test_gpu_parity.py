@@ -165,6 +165,9 @@ C2_SPEC = [("wl", C2_BINS, {"sigma_e": 0.26}), ("nc", C2_BINS, {"bias": 1.2})]
         ([("wl", [(1.0, 2.0, 0.7, 3.0, 5)], {"sigma_e": 0.3, "m": 0.02}),
           ("nc", [(2.0, 1.5, 0.4, 2.5, 3), (1.0, 2.0, 0.9, 5.0, 4)], {"bias": 0.9})],
          np.array([2.0, 7.5, 33.0, 480.0, 2999.0]), 200),   # ragged zmax, m != 0, odd ell
+        ([("wl", [(1.0, 2.0, 0.6, 3.0, 8)], {"sigma_e": 0.28}),
+          ("wl", [(1.0, 2.0, 1.1, 6.0, 8), (1.0, 2.0, 0.4, 6.0, 6)], {"sigma_e": 0.25})],
+         np.logspace(1, 3.5, 9), 128),   # two lensing groups (probe zmax 3 and 6)
     ],
 )
 def test_angular_cl_vs_oracle(spec, ell, n_limber):
