@@ -16,7 +16,7 @@ constexpr double C2 = C_KMS * C_KMS;          // const.c**2
 constexpr double LN10 = 2.302585092994046;
 constexpr double LOG_KMIN = -0x1.26bb1bbb55515p+3;  // np.log(1e-4)
 constexpr double DLOGK = (0x1.26bb1bbb55516p+3 - -0x1.26bb1bbb55515p+3) / 256.0;
-constexpr double Y2_TAYLOR = 1e-3;  // below: exp(-y^2) by its Taylor series
+constexpr double Y2_TAYLOR = 1e-2;  // below: exp(-y^2) by its Taylor series (NTAYLOR terms)
 constexpr double Y2_SKIP = 60.0;    // above: exp(-y^2) y^4 P k^3 < 1e-20 of the sum
 
 struct HfParams {
@@ -166,6 +166,80 @@ __device__ void halofit_coefs(const Bg& bg, double a, double lna, const HfParams
   row[R_LGCF3] = LN10 * e_cn + 0.0743 * lom;  // log(c_n f3)
 }
 
+__device__ __forceinline__ float ex2a(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float lg2a(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// fp32c: the takahashi2012 coefficients (power.py:199-238) in float32 from the
+// float64 n_eff, C and background; the Limber integrand consumes them as
+// float32, so only Omega_m(a), Omega_de(a) (background) stay float64.  Fills
+// the float row and the coefficient fields of the float64 row.
+__device__ void halofit_coefs_fast(const Bg& bg, const double* s, double a, double lna,
+                                   const HfParams& hp, double chiv, double g, double* row,
+                                   float* f) {
+  double om_m, om_de;
+  bg_om_l(bg, a, lna, &om_m, &om_de);
+  const double wv = bg_w(bg, a);
+  const float n = (float)hp.neff, C = (float)hp.C, omde = (float)om_de, w = (float)wv;
+  const float n2 = n * n, n3 = n2 * n, n4 = n2 * n2;
+  constexpr float LOG2_10 = 3.321928094887362f;
+  const float e_an = 1.5222f + 2.8553f * n + 2.3706f * n2 + 0.9903f * n3 + 0.2250f * n4 -
+                     0.6038f * C + 0.1749f * omde * (1 + w);
+  const float e_bn = -0.5642f + 0.5864f * n + 0.5716f * n2 - 1.5474f * C + 0.2279f * omde * (1 + w);
+  const float e_cn = 0.3698f + 2.0404f * n + 0.8161f * n2 + 0.5869f * C;
+  const float an = ex2a(LOG2_10 * e_an), bn = ex2a(LOG2_10 * e_bn), cn = ex2a(LOG2_10 * e_cn);
+  const float gam = 0.1971f - 0.0843f * n + 0.8460f * C;
+  const float alpha = fabsf(6.0835f + 1.3373f * n - 0.1959f * n2 - 5.5274f * C);
+  const float beta = 2.0379f - 0.7354f * n + 0.3157f * n2 + 1.2490f * n3 + 0.3980f * n4 - 0.1682f * C;
+  const float nun = ex2a(LOG2_10 * (5.2105f + 3.6902f * n));
+  const float l2om = lg2a((float)om_m);
+  const float f1 = ex2a(-0.0307f * l2om), f2 = ex2a(-0.0585f * l2om), f3 = ex2a(0.0743f * l2om);
+  const float knl = (float)hp.knl;
+  const float chic = fmaxf((float)chiv, 1.f);
+  f[F_INVCHI] = 1.f / chic;
+  f[F_CHIC] = chic;
+  f[F_LG2INVCHI] = -lg2a(chic);
+  f[F_LG2KNL] = lg2a(knl);
+  f[F_INVKNL] = 1.f / knl;
+  f[F_D2FAC] = (float)(g * g * s[S_PKNORM] * (1.0 / TWO_PI2));
+  f[F_BETAN] = beta;
+  f[F_ALPHAN] = alpha;
+  f[F_AN] = an;
+  f[F_3F1] = 3.f * f1;
+  f[F_F2] = f2;
+  f[F_BN] = bn;
+  f[F_LG2CF3] = LOG2_10 * e_cn + 0.0743f * l2om;
+  f[F_3MGAMMA] = 3.f - gam;
+  f[F_NUN] = nun;
+  for (int i = NROW32_USED; i < NROW32; ++i) f[i] = 0.f;
+  row[R_KNL] = hp.knl;
+  row[R_NEFF] = hp.neff;
+  row[R_C] = hp.C;
+  row[R_OMM] = om_m;
+  row[R_OMDE] = om_de;
+  row[R_W] = wv;
+  row[R_AN] = an;
+  row[R_BN] = bn;
+  row[R_CN] = cn;
+  row[R_GAMMAN] = gam;
+  row[R_ALPHAN] = alpha;
+  row[R_BETAN] = beta;
+  row[R_NUN] = nun;
+  row[R_F1] = f1;
+  row[R_F2] = f2;
+  row[R_F3] = f3;
+  row[R_LGKNL] = 0.6931471805599453 * f[F_LG2KNL];
+  row[R_LGCF3] = 0.6931471805599453 * f[F_LG2CF3];
+  row[R_LGCHIC] = -0.6931471805599453 * f[F_LG2INVCHI];
+}
+
 // FP32 row of the compensated fast path from the FP64 row.
 __device__ void row32_from_row64(const double* s, const double* r, float* f) {
   const double chic = fmax(r[R_CHI], 1.0);
@@ -254,7 +328,9 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   __shared__ double s[NSCAL];
   __shared__ double knl_s[NB], inv_s[NB], g_s[NB], chi_s[NB], t1_s[NB], t2_s[NB], s1_s[NB], s2_s[NB];
   __shared__ int ilo_s[NB], ihi_s[NB];
+  __shared__ double e2tab[64];
   const CosmoTab* ct = it.ctab;
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) e2tab[i] = kExp2Tab64[i];
   for (int i = threadIdx.x; i < NRT; i += blockDim.x) sig[i] = ct->sig[i];
   for (int i = threadIdx.x; i < NKH; i += blockDim.x) pk3[i] = ct->pk3[i];
   for (int i = threadIdx.x; i < NSCAL; i += blockDim.x) s[i] = ct->s[i];
@@ -315,7 +391,7 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
       for (int i = ilo_s[t] + lane; i <= ihi_s[t]; i += 32) {
         const double y = c->kh[i] * inv;
         const double y2 = y * y;
-        const double r = c->simpson_kh[i] * pk3[i] * exp(-y2);
+        const double r = c->simpson_kh[i] * pk3[i] * exp_tang(-y2, e2tab);
         s1 += 2 * r * y2;
         s2 += 4 * r * (y2 - y2 * y2);
       }
@@ -358,18 +434,22 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
     const double chiv = chi_s[t];
     row[R_CHI] = chiv;
     row[R_G] = g_s[t];
-    halofit_coefs(bg, a, lna, hp, row);
+    float f[NROW32];
+    if (FAST) {
+      halofit_coefs_fast(bg, s, a, lna, hp, chiv, g_s[t], row, f);
+    } else {
+      halofit_coefs(bg, a, lna, hp, row);
+      row[R_LGCHIC] = log(fmax(chiv, 1.0));
+    }
     const double dchi = bg_dchioverda_l(bg, a, lna);
     row[R_DCHI] = dchi;
     row[R_U] = WS[n] * dchi / fmax(chiv * chiv, 1.0) / C2;
-    row[R_LGCHIC] = log(fmax(chiv, 1.0));
     if (it.rows64) {
       double* dst = it.rows64 + (size_t)n * NROW64;
       for (int i = 0; i < NROW64; ++i) dst[i] = row[i];
     }
     if (it.rows32) {
-      float f[NROW32];
-      row32_from_row64(s, row, f);
+      if (!FAST) row32_from_row64(s, row, f);
       float* dst = it.rows32 + (size_t)n * NROW32;
       for (int i = 0; i < NROW32; ++i) dst[i] = f[i];
     }

@@ -63,7 +63,7 @@ enum Scalar {
   S_NSCALAR
 };
 constexpr int NSCAL = 32;
-constexpr int NTAYLOR = 8;       // Taylor terms of exp(-y^2) below y^2 = 1e-3
+constexpr int NTAYLOR = 12;      // Taylor terms of exp(-y^2) below y^2 = 1e-2
 constexpr int PAD_CT = 7;        // keeps sizeof(CosmoTab) a multiple of 64
 static_assert(S_NSCALAR <= NSCAL, "scalar block too small");
 
@@ -280,6 +280,51 @@ __device__ __forceinline__ int logspace_guess(double x, int n) {
   if (t < 0.0) return 0;
   if (t > (double)(n - 1)) return n - 1;
   return (int)t;
+}
+
+// 2^(j/64), j = 0..63, correctly rounded (table of the exponential below).
+__device__ __constant__ const double kExp2Tab64[64] = {
+    0x1.0000000000000p+0, 0x1.02c9a3e778061p+0, 0x1.059b0d3158574p+0, 0x1.0874518759bc8p+0,
+    0x1.0b5586cf9890fp+0, 0x1.0e3ec32d3d1a2p+0, 0x1.11301d0125b51p+0, 0x1.1429aaea92de0p+0,
+    0x1.172b83c7d517bp+0, 0x1.1a35beb6fcb75p+0, 0x1.1d4873168b9aap+0, 0x1.2063b88628cd6p+0,
+    0x1.2387a6e756238p+0, 0x1.26b4565e27cddp+0, 0x1.29e9df51fdee1p+0, 0x1.2d285a6e4030bp+0,
+    0x1.306fe0a31b715p+0, 0x1.33c08b26416ffp+0, 0x1.371a7373aa9cbp+0, 0x1.3a7db34e59ff7p+0,
+    0x1.3dea64c123422p+0, 0x1.4160a21f72e2ap+0, 0x1.44e086061892dp+0, 0x1.486a2b5c13cd0p+0,
+    0x1.4bfdad5362a27p+0, 0x1.4f9b2769d2ca7p+0, 0x1.5342b569d4f82p+0, 0x1.56f4736b527dap+0,
+    0x1.5ab07dd485429p+0, 0x1.5e76f15ad2148p+0, 0x1.6247eb03a5585p+0, 0x1.6623882552225p+0,
+    0x1.6a09e667f3bcdp+0, 0x1.6dfb23c651a2fp+0, 0x1.71f75e8ec5f74p+0, 0x1.75feb564267c9p+0,
+    0x1.7a11473eb0187p+0, 0x1.7e2f336cf4e62p+0, 0x1.82589994cce13p+0, 0x1.868d99b4492edp+0,
+    0x1.8ace5422aa0dbp+0, 0x1.8f1ae99157736p+0, 0x1.93737b0cdc5e5p+0, 0x1.97d829fde4e50p+0,
+    0x1.9c49182a3f090p+0, 0x1.a0c667b5de565p+0, 0x1.a5503b23e255dp+0, 0x1.a9e6b5579fdbfp+0,
+    0x1.ae89f995ad3adp+0, 0x1.b33a2b84f15fbp+0, 0x1.b7f76f2fb5e47p+0, 0x1.bcc1e904bc1d2p+0,
+    0x1.c199bdd85529cp+0, 0x1.c67f12e57d14bp+0, 0x1.cb720dcef9069p+0, 0x1.d072d4a07897cp+0,
+    0x1.d5818dcfba487p+0, 0x1.da9e603db3285p+0, 0x1.dfc97337b9b5fp+0, 0x1.e502ee78b3ff6p+0,
+    0x1.ea4afa2a490dap+0, 0x1.efa1bee615a27p+0, 0x1.f50765b6e4540p+0, 0x1.fa7c1819e90d8p+0,
+};
+
+// exp(x) for -700 < x <= 0 by the table-driven method of P. T. P. Tang
+// ("Table-driven implementation of the exponential function in IEEE
+// floating-point arithmetic", ACM TOMS 15, 1989): x = (64 m + j) ln2/64 + r
+// with |r| <= ln2/128, exp(x) = 2^m 2^(j/64) e^r, e^r by its Taylor polynomial
+// of degree 6 (truncation < 3e-20 relative).  ln2/64 is split in a 40-bit
+// high part (exact products for |k| < 2^13) and the rest.  `tab` is a copy of
+// kExp2Tab64 in shared memory (lanes index it independently).
+__device__ __forceinline__ double exp_tang(double x, const double* tab) {
+  constexpr double INV_LN2_64 = 92.33248261689366;
+  constexpr double LN2_64_HI = 0x1.62e42fefa2000p-7;
+  constexpr double LN2_64_LO = 0x1.9ef35793c7673p-47;
+  const double kd = rint(x * INV_LN2_64);
+  const double r = fma(-kd, LN2_64_LO, fma(-kd, LN2_64_HI, x));
+  double p = 1.0 / 720.0;
+  p = fma(p, r, 1.0 / 120.0);
+  p = fma(p, r, 1.0 / 24.0);
+  p = fma(p, r, 1.0 / 6.0);
+  p = fma(p, r, 0.5);
+  p = fma(p, r, 1.0);
+  p = fma(p, r, 1.0);
+  const int k = (int)kd;
+  const double two_m = __hiloint2double(((k >> 6) + 1023) << 20, 0);
+  return tab[k & 63] * p * two_m;
 }
 
 // --------------------------------------------------------- background ------

@@ -412,9 +412,9 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   }
   // Taylor prefix sums of the halofit moments: P_m[i] = sum_{i' < i} w pk3 k^(2m+2),
   // one warp per m with a warp-wide inclusive scan over chunks of 32 nodes.
-  {
-    const int m = t >> 5, lane = t & 31;
-    if (m < NTAYLOR) {
+  for (int m = t >> 5; m < NTAYLOR; m += (int)(blockDim.x >> 5)) {
+    const int lane = t & 31;
+    {
       if (lane == 0) out->ptay[m][0] = 0.0;
       double carry = 0.0;
       for (int base = 0; base < NKH; base += 32) {
