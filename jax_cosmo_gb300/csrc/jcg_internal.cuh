@@ -63,7 +63,7 @@ enum Scalar {
   S_NSCALAR
 };
 constexpr int NSCAL = 32;
-constexpr int NTAYLOR = 12;      // Taylor terms of exp(-y^2) below y^2 = 1e-2
+constexpr int NTAYLOR = 20;      // Taylor terms of exp(-y^2) below y^2 = 1 (1/19! < 1e-17)
 constexpr int PAD_CT = 7;        // keeps sizeof(CosmoTab) a multiple of 64
 static_assert(S_NSCALAR <= NSCAL, "scalar block too small");
 
