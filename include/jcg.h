@@ -156,6 +156,18 @@ int jcg_stage_limber(const jcg_geometry* g, const void* geo_dev, const double* p
                      int n_cosmo, int precision, double* cl_dev, void* workspace,
                      size_t workspace_bytes, cudaStream_t stream);
 
+/* Derivatives of angular_cl with respect to the 8 Cosmology leaves, float64:
+ * jac_dev [n_cosmo][n_cls][n_ell][8] = dC_ij(l)/d(Omega_c, Omega_b, h, n_s,
+ * sigma8, Omega_k, w0, wa), and cl_dev (may be NULL) the C_ell themselves.
+ * Replaces jax.grad / jax.jacfwd through angular_cl (angular_cl.py:49-98;
+ * README.md:14-27): the vector-Jacobian product of a likelihood is
+ * sum_ij,l v_ij(l) jac_ij(l).  Tables are differentiated forward (tangents),
+ * the Limber integrand by a reverse sweep; all recomputed from params_dev. */
+int jcg_jacobian_workspace_size(const jcg_geometry* g, int n_cosmo, size_t* bytes);
+int jcg_angular_cl_jacobian(const jcg_geometry* g, const void* geo_dev, const double* params_dev,
+                            int n_cosmo, double* cl_dev, double* jac_dev, void* workspace,
+                            size_t workspace_bytes, cudaStream_t stream);
+
 /* Copy stage outputs for cosmology `index` out of a workspace (device to device).
  * what: 0 chi table [256], 1 growth table [128], 2 scalars [32],
  *       3 halofit rows [na][24] (FP64), 4 radial kernels [n_tracers][na]. */
@@ -199,10 +211,12 @@ int jcg_gaussian_covariance(const double* ell_dev, int n_ell, int n_tracers,
  * cov [n_cosmo][n_cls][n_cls][n_ell]; out [n_cosmo].  Returns
  * -0.5 * (r^T C^-1 r - logdet) when include_logdet, as likelihood.py:61.
  * status_dev [n_cosmo] (may be NULL): 0 ok, 2 a block is not positive
- * definite (out = NaN). */
+ * definite (out = NaN).  alpha_dev [n_cosmo][n_cls*n_ell] (may be NULL)
+ * receives C^-1 (mu - data), from which the derivatives follow:
+ * d logL / d mu = -alpha, d logL / d C = (alpha alpha^T + C^-1) / 2. */
 int jcg_gaussian_loglike_sparse(const double* data_dev, const double* mu_dev, const double* cov_dev,
                                 int n_cosmo, int n_cls, int n_ell, int include_logdet,
-                                double* out_dev, int* status_dev, void* workspace,
+                                double* out_dev, int* status_dev, double* alpha_dev, void* workspace,
                                 size_t workspace_bytes, cudaStream_t stream);
 int jcg_loglike_workspace_size(int n_cosmo, int n_cls, int n_ell, size_t* bytes);
 
@@ -214,7 +228,7 @@ int jcg_loglike_workspace_size(int n_cosmo, int n_cls, int n_ell, size_t* bytes)
  * (out = NaN: factor it densely instead), 2 not positive definite. */
 int jcg_gaussian_loglike_dense(const double* data_dev, const double* mu_dev, const double* cov_dev,
                                int n_cosmo, int n_cls, int n_ell, int include_logdet,
-                               double* out_dev, int* status_dev, void* workspace,
+                               double* out_dev, int* status_dev, double* alpha_dev, void* workspace,
                                size_t workspace_bytes, cudaStream_t stream);
 
 /* sparse.inv / sparse.slogdet of (n, n, ndiag) block-diagonal matrices

@@ -97,9 +97,11 @@ SIGNATURES = {
     "jcg_eval_points": [_P, _I, _P, _P, _I, _I, _P, _P, _SZ, _P],
     "jcg_eval_workspace_size": [_I, _PSZ],
     "jcg_gaussian_covariance": [_P, _I, _I, _P, _P, _P, _I, _D, _I, _P, _P],
-    "jcg_gaussian_loglike_sparse": [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _SZ, _P],
+    "jcg_gaussian_loglike_sparse": [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _SZ, _P],
     "jcg_loglike_workspace_size": [_I, _I, _I, _PSZ],
-    "jcg_gaussian_loglike_dense": [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _SZ, _P],
+    "jcg_gaussian_loglike_dense": [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _SZ, _P],
+    "jcg_jacobian_workspace_size": [_PG, _I, _PSZ],
+    "jcg_angular_cl_jacobian": [_PG, _P, _P, _I, _P, _P, _P, _SZ, _P],
     "jcg_sparse_inv": [_P, _I, _I, _P, _P],
     "jcg_sparse_slogdet": [_P, _I, _I, _P, _P, _P, _P],
     "jcg_sparse_to_dense": [_P, _I, _I, _I, _P, _P],

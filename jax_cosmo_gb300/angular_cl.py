@@ -177,6 +177,10 @@ def gaussian_cl_covariance(ell, probes, cl_signal, cl_noise, f_sky=0.25, sparse=
     n_tr = sum(p.n_tracers for p in probes)
     if not isinstance(cl_signal, torch.Tensor):
         cl_signal = torch.as_tensor(np.asarray(cl_signal, dtype=np.float64))
+    if cl_signal.requires_grad:
+        from jax_cosmo_gb300 import autodiff
+
+        return autodiff.covariance_autograd(cl_signal, ell_t, n_tr, cl_noise, None, f_sky, sparse)
     return _covariance(ell_t, n_tr, cl_signal, cl_noise, None, f_sky, sparse)
 
 
@@ -193,7 +197,8 @@ def gaussian_cl_covariance_and_mean(
 ):
     """(signal mean flattened [n_cls*n_ell], covariance) (angular_cl.py:166-196).
 
-    The mean is the signal only; the covariance uses signal + noise.
+    The mean is the signal only; the covariance uses signal + noise.  Both are
+    differentiable in the Cosmology parameters that require grad.
     """
     device = _lib.require_cuda()
     ell_np = _geometry.ell_host(ell)
@@ -201,7 +206,12 @@ def gaussian_cl_covariance_and_mean(
     _, _, ell_t = _geometry.get_geometry(probes, ell_np, n_limber, device)
     tracer_noise = torch.cat([p.noise() for p in probes])
     n_tr = tracer_noise.numel()
-    cov = _covariance(ell_t, n_tr, cl_signal.detach(), None, tracer_noise, f_sky, sparse)
+    if cl_signal.requires_grad:
+        from jax_cosmo_gb300 import autodiff
+
+        cov = autodiff.covariance_autograd(cl_signal, ell_t, n_tr, None, tracer_noise, f_sky, sparse)
+    else:
+        cov = _covariance(ell_t, n_tr, cl_signal, None, tracer_noise, f_sky, sparse)
     if cl_signal.dim() == 3:
         return cl_signal.reshape(cl_signal.shape[0], -1), cov
     return cl_signal.flatten(), cov

@@ -1,0 +1,241 @@
+"""Derivatives of the angular_cl path for torch.autograd.
+
+jax_cosmo differentiates its whole stack with ``jax.grad`` / ``jax.hessian``
+(README.md:14-27).  Here the three functions of the path are
+``torch.autograd.Function``s whose backward passes run in libjcg:
+
+* ``angular_cl``: backward = v^T J with J = dC_ell/dtheta from
+  ``jcg_angular_cl_jacobian`` (tables differentiated forward, the Limber
+  integrand by a hand-written reverse sweep, FP64; theta = the 8 Cosmology
+  leaves of core.py:98-108);
+* ``gaussian_cl_covariance``: the Knox formula (angular_cl.py:144-147) is a
+  product of two C_ell, its vector-Jacobian product is applied with index
+  additions on the device;
+* ``gaussian_log_likelihood``: d logL / d mu = -C^-1 r (C^-1 r from the same
+  per-ell Cholesky as the value), d logL / d C = (C^-1 r r^T C^-1 + C^-1) / 2
+  with the reference's +0.5 logdet sign (likelihood.py:61).
+
+``angular_cl_jacobian`` returns J itself, and ``fisher_matrix`` the Gaussian
+Fisher matrix J^T C^-1 J of a C_ell data vector (the construction of the
+reference's intro notebook).
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from jax_cosmo_gb300 import _geometry, _lib
+
+PARAM_ORDER = ("Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa")
+FISHER_PARAMS = ("Omega_c", "Omega_b", "h", "n_s", "sigma8", "w0", "wa")
+
+
+def jacobian_device(params, ell, probes, n_limber=512):
+    """(C_ell [B, n_cls, n_ell], dC/dtheta [B, n_cls, n_ell, 8]) for [B, 8] params on the device."""
+    device = params.device
+    g, geo, _ = _geometry.get_geometry(probes, ell, n_limber, device)
+    B = params.shape[0]
+    n_cls = _geometry.n_cls_of(g)
+    wsz = ctypes.c_size_t()
+    _lib.call("jcg_jacobian_workspace_size", ctypes.byref(g), B, ctypes.byref(wsz))
+    ws = _lib.workspace(wsz.value, device)
+    cl = torch.empty(B, n_cls, g.n_ell, dtype=torch.float64, device=device)
+    jac = torch.empty(B, n_cls, g.n_ell, len(PARAM_ORDER), dtype=torch.float64, device=device)
+    _lib.call(
+        "jcg_angular_cl_jacobian", ctypes.byref(g), _lib.ptr(geo), _lib.ptr(params.contiguous()), B,
+        _lib.ptr(cl), _lib.ptr(jac), _lib.ptr(ws), ctypes.c_size_t(ws.numel()), _lib.stream_of(device),
+    )
+    return cl, jac
+
+
+class _AngularCl(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, params, ell, probes, precision, n_limber):
+        from jax_cosmo_gb300.angular_cl import angular_cl_device
+
+        ctx.meta = (ell, probes, n_limber)
+        ctx.save_for_backward(params)
+        return angular_cl_device(params.detach().contiguous(), ell, probes, precision, n_limber)
+
+    @staticmethod
+    def backward(ctx, gcl):
+        (params,) = ctx.saved_tensors
+        ell, probes, n_limber = ctx.meta
+        _, jac = jacobian_device(params.detach().contiguous(), ell, probes, n_limber)
+        gp = torch.einsum("bpl,bpld->bd", gcl.to(torch.float64), jac)
+        return gp, None, None, None, None
+
+
+def angular_cl_autograd(cosmo, ell, probes, precision="fp64", n_limber=512):
+    device = _lib.require_cuda()
+    params = cosmo.param_tensor(device, differentiable=True)
+    return _AngularCl.apply(params, ell, probes, precision, n_limber)
+
+
+def angular_cl_jacobian(cosmo, ell, probes, n_limber=512):
+    """(C_ell, dC_ell/dtheta) with theta = (Omega_c, Omega_b, h, n_s, sigma8, Omega_k, w0, wa).
+
+    Shapes [n_cls, n_ell] and [n_cls, n_ell, 8] (a leading batch axis for a
+    batched Cosmology).
+    """
+    device = _lib.require_cuda()
+    params = cosmo.param_tensor(device)
+    cl, jac = jacobian_device(params, _geometry.ell_host(ell), probes, n_limber)
+    if cosmo.batch_size is None:
+        return cl[0], jac[0]
+    return cl, jac
+
+
+# ------------------------------------------------------------- covariance ----
+def _cov_index(n_tr, device):
+    from jax_cosmo_gb300.angular_cl import _get_cov_blocks_ordering
+
+    class _P:  # minimal probe stand-in with n_tracers
+        n_tracers = n_tr
+
+    blocks = torch.as_tensor(np.array(_get_cov_blocks_ordering([_P()])), device=device)
+    return blocks[:, 0], blocks[:, 1], blocks[:, 2], blocks[:, 3]
+
+
+class _Covariance(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, cl_signal, ell_t, n_tr, cl_noise, tracer_noise, f_sky, sparse):
+        from jax_cosmo_gb300.angular_cl import _covariance
+
+        ctx.meta = (ell_t, n_tr, cl_noise, tracer_noise, f_sky, sparse)
+        ctx.save_for_backward(cl_signal)
+        return _covariance(ell_t, n_tr, cl_signal.detach(), cl_noise, tracer_noise, f_sky, sparse)
+
+    @staticmethod
+    def backward(ctx, gcov):
+        (sig,) = ctx.saved_tensors
+        ell_t, n_tr, cl_noise, tracer_noise, f_sky, sparse = ctx.meta
+        batched = sig.dim() == 3
+        s3 = sig if batched else sig[None]
+        g = gcov if batched else gcov[None]
+        B, n_cls, n_ell = s3.shape
+        if not sparse:  # the entries that depend on C_ell: the per-ell diagonals of each block
+            g4 = g.reshape(B, n_cls, n_ell, n_cls, n_ell)
+            idx = torch.arange(n_ell, device=g.device)
+            g = g4[:, :, idx, :, idx].permute(1, 2, 3, 0)  # [B, n_cls, n_cls, n_ell]
+        ell = ell_t.detach().cpu().numpy()
+        norm = torch.as_tensor((2 * ell + 1) * np.gradient(ell) * f_sky, device=g.device)
+        obs = s3.detach().clone()
+        if cl_noise is not None:
+            obs = obs + torch.as_tensor(cl_noise, dtype=torch.float64, device=g.device)
+        elif tracer_noise is not None:
+            tn = tracer_noise.to(g.device, torch.float64)
+            from jax_cosmo_gb300.angular_cl import _get_cl_ordering
+
+            class _P:
+                n_tracers = n_tr
+
+            for k, (i, j) in enumerate(_get_cl_ordering([_P()])):
+                if i == j:
+                    obs[:, k] = obs[:, k] + tn[i]
+        a, b, c, d = _cov_index(n_tr, g.device)
+        gn = g.reshape(B, n_cls * n_cls, n_ell) / norm
+        go = torch.zeros_like(obs)
+        go.index_add_(1, a, gn * obs[:, b])
+        go.index_add_(1, b, gn * obs[:, a])
+        go.index_add_(1, c, gn * obs[:, d])
+        go.index_add_(1, d, gn * obs[:, c])
+        return (go if batched else go[0]), None, None, None, None, None, None
+
+
+def covariance_autograd(cl_signal, ell_t, n_tr, cl_noise, tracer_noise, f_sky, sparse):
+    return _Covariance.apply(cl_signal, ell_t, n_tr, cl_noise, tracer_noise, f_sky, sparse)
+
+
+# ------------------------------------------------------------- likelihood ----
+class _LogLike(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, data, mu, C, include_logdet, sparse, n_cls, n_ell):
+        from jax_cosmo_gb300.likelihood import _loglike_core
+
+        C = C.detach().contiguous()
+        alpha = torch.empty(mu.shape, dtype=torch.float64, device=mu.device)
+        out, status = _loglike_core(data.detach().contiguous(), mu.detach().contiguous(), C, sparse,
+                                    n_cls, n_ell, include_logdet, alpha=alpha)
+        ctx.meta = (include_logdet, sparse, n_cls, n_ell)
+        ctx.save_for_backward(alpha, C, status)
+        return out
+
+    @staticmethod
+    def backward(ctx, gout):
+        alpha, C, status = ctx.saved_tensors
+        include_logdet, sparse, n_cls, n_ell = ctx.meta
+        go = gout.to(torch.float64)
+        g_data = alpha * go[:, None]
+        g_mu = -g_data
+        g_C = None
+        if ctx.needs_input_grad[2]:
+            B = alpha.shape[0]
+            if sparse:
+                a3 = alpha.reshape(B, n_cls, n_ell)
+                g = torch.einsum("bpl,bql->bpql", a3, a3)
+                if include_logdet:
+                    g = g + _sparse_inv_batched(C)
+                g_C = 0.5 * g * go[:, None, None, None]
+            else:
+                g = torch.einsum("bi,bj->bij", alpha, alpha)
+                if include_logdet:
+                    g = g + _dense_inverse(C, status, n_cls, n_ell)
+                g_C = 0.5 * g * go[:, None, None]
+        return g_data, g_mu, g_C, None, None, None, None
+
+
+def _dense_blocks(C, n_cls, n_ell):
+    """[B, N, N] (cls, ell)-ordered, block diagonal in ell -> [B, n_cls, n_cls, n_ell]."""
+    B = C.shape[0]
+    g4 = C.reshape(B, n_cls, n_ell, n_cls, n_ell)
+    idx = torch.arange(n_ell, device=C.device)
+    return g4[:, :, idx, :, idx].permute(1, 2, 3, 0).contiguous()
+
+
+def _sparse_inv_batched(S):
+    from jax_cosmo_gb300 import sparse as sp
+
+    return torch.stack([sp.inv(S[i]) for i in range(S.shape[0])])
+
+
+def _dense_inverse(C, status, n_cls, n_ell):
+    """C^-1 per batch entry: per-ell block inverses where C is block diagonal in ell."""
+    from jax_cosmo_gb300 import sparse as sp
+
+    st = status.tolist()
+    out = torch.empty_like(C)
+    for i, s in enumerate(st):
+        if s == 1:
+            out[i] = torch.cholesky_inverse(torch.linalg.cholesky(C[i]))
+        else:
+            out[i] = sp.to_dense(sp.inv(_dense_blocks(C[i : i + 1], n_cls, n_ell)[0]))
+    return out
+
+
+def loglike_autograd(data2, mu2, Cb, include_logdet, sparse, n_cls, n_ell):
+    return _LogLike.apply(data2, mu2, Cb, include_logdet, sparse, n_cls, n_ell)
+
+
+# ----------------------------------------------------------------- Fisher ----
+def fisher_matrix(cosmo, ell, probes, f_sky=0.25, n_limber=512, params=FISHER_PARAMS):
+    """Gaussian Fisher matrix F = J^T C^-1 J of the C_ell data vector.
+
+    J = dC_ell/dtheta for the named parameters (a subset of PARAM_ORDER), C the
+    Gaussian covariance with noise (angular_cl.py:120-163) at ``cosmo``, inverted
+    per ell block.
+    """
+    from jax_cosmo_gb300.angular_cl import gaussian_cl_covariance, noise_cl
+
+    cl, jac = angular_cl_jacobian(cosmo, ell, probes, n_limber)
+    if cl.dim() != 2:
+        raise ValueError("fisher_matrix takes a single (unbatched) cosmology")
+    sel = [PARAM_ORDER.index(p) for p in params]
+    J = jac[..., sel]  # [n_cls, n_ell, P]
+    cov = gaussian_cl_covariance(ell, probes, cl, noise_cl(ell, probes), f_sky, sparse=True)
+    Cl = cov.permute(2, 0, 1)  # [n_ell, n_cls, n_cls]
+    Jl = J.permute(1, 0, 2)  # [n_ell, n_cls, P]
+    X = torch.linalg.solve(Cl, Jl)
+    return torch.einsum("lcp,lcq->pq", Jl, X)

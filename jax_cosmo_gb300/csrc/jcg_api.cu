@@ -18,7 +18,7 @@ void launch_covariance(const double* ell, int n_ell, int n_tr, const double* cl,
                        int sparse, double* out, cudaStream_t st);
 void launch_loglike(const double* data, const double* mu, const double* cov, int n_cosmo, int n_cls,
                     int n_ell, int include_logdet, int dense, double* out, int* status,
-                    double* partial, int* structure, cudaStream_t st);
+                    double* partial, int* structure, double* alpha, cudaStream_t st);
 void launch_sparse_inv(const double* sp, int n, int nd, double* out, cudaStream_t st);
 void launch_sparse_slogdet(const double* sp, int n, int nd, double* sign_part, double* ld_part,
                            double* sign_out, double* ld_out, cudaStream_t st);
@@ -475,7 +475,8 @@ int jcg_loglike_workspace_size(int n_cosmo, int n_cls, int n_ell, size_t* bytes)
 
 static int loglike_common(const double* data, const double* mu, const double* cov, int n_cosmo,
                           int n_cls, int n_ell, int include_logdet, int dense, double* out,
-                          int* status, void* ws, size_t ws_bytes, cudaStream_t stream) {
+                          int* status, double* alpha, void* ws, size_t ws_bytes,
+                          cudaStream_t stream) {
   if (!data || !mu || !cov || !out || !ws) return fail(JCG_ERR_ARG, "NULL pointer");
   if (n_cosmo < 1 || n_cls < 1 || n_ell < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
   if (n_cls > 160) return fail(JCG_ERR_SHAPE, "n_cls = %d above the per-ell block limit 160", n_cls);
@@ -488,22 +489,22 @@ static int loglike_common(const double* data, const double* mu, const double* co
   int* structure = ints;
   int* st = status ? status : ints + n_cosmo;
   launch_loglike(data, mu, cov, n_cosmo, n_cls, n_ell, include_logdet ? 1 : 0, dense, out, st,
-                 partial, structure, stream);
+                 partial, structure, alpha, stream);
   return cuda_check("loglike");
 }
 
 int jcg_gaussian_loglike_sparse(const double* data, const double* mu, const double* cov, int n_cosmo,
                                 int n_cls, int n_ell, int include_logdet, double* out, int* status,
-                                void* ws, size_t ws_bytes, cudaStream_t stream) {
-  return loglike_common(data, mu, cov, n_cosmo, n_cls, n_ell, include_logdet, 0, out, status, ws,
-                        ws_bytes, stream);
+                                double* alpha, void* ws, size_t ws_bytes, cudaStream_t stream) {
+  return loglike_common(data, mu, cov, n_cosmo, n_cls, n_ell, include_logdet, 0, out, status,
+                        alpha, ws, ws_bytes, stream);
 }
 
 int jcg_gaussian_loglike_dense(const double* data, const double* mu, const double* cov, int n_cosmo,
                                int n_cls, int n_ell, int include_logdet, double* out, int* status,
-                               void* ws, size_t ws_bytes, cudaStream_t stream) {
-  return loglike_common(data, mu, cov, n_cosmo, n_cls, n_ell, include_logdet, 1, out, status, ws,
-                        ws_bytes, stream);
+                               double* alpha, void* ws, size_t ws_bytes, cudaStream_t stream) {
+  return loglike_common(data, mu, cov, n_cosmo, n_cls, n_ell, include_logdet, 1, out, status,
+                        alpha, ws, ws_bytes, stream);
 }
 
 int jcg_sparse_inv(const double* sp, int n, int nd, double* out, cudaStream_t stream) {
@@ -617,4 +618,33 @@ extern "C" int jcg_angular_cl_noalloc(const jcg_geometry* g, const void* geo, co
   launch_tracer_kernels(b, c, stream);
   launch_limber(b, c, limber_tile(h.n_ell), stream);
   return cuda_check("angular_cl_noalloc");
+}
+
+// --------------------------------------------------------- derivatives -----
+extern "C" int jcg_jacobian_workspace_size(const jcg_geometry* g, int n_cosmo, size_t* bytes) {
+  if (!bytes) return fail(JCG_ERR_ARG, "bytes is NULL");
+  if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  GeoHeader h;
+  const int rc = make_header(g, &h);
+  if (rc) return rc;
+  *bytes = grad_workspace_bytes(h, n_cosmo);
+  return JCG_OK;
+}
+
+extern "C" int jcg_angular_cl_jacobian(const jcg_geometry* g, const void* geo, const double* params,
+                                       int n_cosmo, double* cl, double* jac, void* ws,
+                                       size_t ws_bytes, cudaStream_t stream) {
+  GeoHeader h;
+  int rc = make_header(g, &h);
+  if (rc) return rc;
+  if (!geo || !params || !jac || !ws) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  if (h.custom_nodes) return fail(JCG_ERR_ARG, "a geometry with caller redshift nodes has no Limber grid");
+  const size_t need = grad_workspace_bytes(h, n_cosmo);
+  if (ws_bytes < need) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need);
+  if (((uintptr_t)ws) % 256 != 0) return fail(JCG_ERR_ARG, "workspace must be 256-byte aligned");
+  ConstTables* c = nullptr;
+  if ((rc = const_tables(&c))) return rc;
+  grad_run(static_cast<const GeoHeader*>(geo), h, params, n_cosmo, cl, jac, ws, c, stream);
+  return cuda_check("angular_cl_jacobian");
 }

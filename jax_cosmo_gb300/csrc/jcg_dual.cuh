@@ -1,0 +1,376 @@
+// Forward-mode (tangent) arithmetic for the derivative kernels, and the FP64
+// physics of the tables written once for a number type T (double or Dual<N>).
+//
+// Dual<N> carries a value and N tangents.  The derivative kernels use it two
+// ways: Dual<1> with one tangent direction per lane (8 lanes = the 8 Cosmology
+// leaves of core.py:98-108; register use stays that of plain FP64), and
+// Dual<8> for short per-term loops (spectral moments, lensing integrand) where
+// the value part is shared by the 8 directions.
+//
+// Derivative conventions follow JAX's for the reference's operations:
+// max(x, c) / min(x, c) pass the tangent of x where x is the selected branch;
+// the interpolation segment (argmin) is locally constant.
+#pragma once
+
+#include "jcg_internal.cuh"
+
+namespace jcg {
+
+constexpr int NDIR = 8;  // d/d(Omega_c, Omega_b, h, n_s, sigma8, Omega_k, w0, wa)
+
+template <int N>
+struct Dual {
+  double v;
+  double d[N];
+};
+
+template <int N>
+__device__ __forceinline__ Dual<N> dconst(double v) {
+  Dual<N> r;
+  r.v = v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = 0.0;
+  return r;
+}
+
+__device__ __forceinline__ double val(double x) { return x; }
+template <int N>
+__device__ __forceinline__ double val(const Dual<N>& x) {
+  return x.v;
+}
+
+#define JCG_DUAL_BIN(OP, VEXPR, DEXPR)                                                       \
+  template <int N>                                                                           \
+  __device__ __forceinline__ Dual<N> operator OP(const Dual<N>& a, const Dual<N>& b) {       \
+    Dual<N> r;                                                                               \
+    r.v = VEXPR;                                                                             \
+    _Pragma("unroll") for (int i = 0; i < N; ++i) r.d[i] = DEXPR;                            \
+    return r;                                                                                \
+  }
+
+JCG_DUAL_BIN(+, a.v + b.v, a.d[i] + b.d[i])
+JCG_DUAL_BIN(-, a.v - b.v, a.d[i] - b.d[i])
+JCG_DUAL_BIN(*, a.v * b.v, a.d[i] * b.v + a.v * b.d[i])
+#undef JCG_DUAL_BIN
+
+template <int N>
+__device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a.v / b.v;
+  const double ib = 1.0 / b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - r.v * b.d[i]) * ib;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator-(const Dual<N>& a) {
+  Dual<N> r;
+  r.v = -a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator+(const Dual<N>& a, double b) {
+  Dual<N> r = a;
+  r.v = a.v + b;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator+(double a, const Dual<N>& b) {
+  return b + a;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator-(const Dual<N>& a, double b) {
+  Dual<N> r = a;
+  r.v = a.v - b;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator-(double a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator*(const Dual<N>& a, double b) {
+  Dual<N> r;
+  r.v = a.v * b;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator*(double a, const Dual<N>& b) {
+  return b * a;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator/(const Dual<N>& a, double b) {
+  Dual<N> r;
+  r.v = a.v / b;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] / b;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> operator/(double a, const Dual<N>& b) {
+  Dual<N> r;
+  r.v = a / b.v;
+  const double s = -r.v / b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = s * b.d[i];
+  return r;
+}
+
+// elementary functions: xf(double) = CUDA libm, xf(Dual) = chain rule
+__device__ __forceinline__ double xexp(double x) { return exp(x); }
+__device__ __forceinline__ double xlog(double x) { return log(x); }
+__device__ __forceinline__ double xsqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ double xcbrt(double x) { return cbrt(x); }
+__device__ __forceinline__ double xsin(double x) { return sin(x); }
+__device__ __forceinline__ double xcos(double x) { return cos(x); }
+__device__ __forceinline__ double xfabs(double x) { return fabs(x); }
+__device__ __forceinline__ double xpow(double x, double e) { return pow(x, e); }
+__device__ __forceinline__ double xfmax(double x, double c) { return fmax(x, c); }
+__device__ __forceinline__ double xfmin(double x, double c) { return fmin(x, c); }
+
+template <int N>
+__device__ __forceinline__ Dual<N> scale_d(double v, double s, const Dual<N>& a) {
+  Dual<N> r;
+  r.v = v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = s * a.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> xexp(const Dual<N>& a) {
+  const double e = exp(a.v);
+  return scale_d(e, e, a);
+}
+template <int N>
+__device__ __forceinline__ Dual<N> xlog(const Dual<N>& a) {
+  return scale_d(log(a.v), 1.0 / a.v, a);
+}
+template <int N>
+__device__ __forceinline__ Dual<N> xsqrt(const Dual<N>& a) {
+  const double s = sqrt(a.v);
+  return scale_d(s, 0.5 / s, a);
+}
+template <int N>
+__device__ __forceinline__ Dual<N> xcbrt(const Dual<N>& a) {
+  const double c = cbrt(a.v);
+  return scale_d(c, c / (3.0 * a.v), a);
+}
+template <int N>
+__device__ __forceinline__ Dual<N> xsin(const Dual<N>& a) {
+  return scale_d(sin(a.v), cos(a.v), a);
+}
+template <int N>
+__device__ __forceinline__ Dual<N> xcos(const Dual<N>& a) {
+  return scale_d(cos(a.v), -sin(a.v), a);
+}
+template <int N>
+__device__ __forceinline__ Dual<N> xfabs(const Dual<N>& a) {
+  return a.v < 0.0 ? -a : a;
+}
+template <int N>
+__device__ __forceinline__ Dual<N> xpow(const Dual<N>& a, double e) {
+  const double p = pow(a.v, e);
+  return scale_d(p, e * p / a.v, a);
+}
+template <int N>
+__device__ __forceinline__ Dual<N> xpow(const Dual<N>& a, const Dual<N>& e) {
+  return xexp(e * xlog(a));
+}
+template <int N>
+__device__ __forceinline__ Dual<N> xfmax(const Dual<N>& a, double c) {
+  return a.v >= c ? a : dconst<N>(c);
+}
+template <int N>
+__device__ __forceinline__ Dual<N> xfmin(const Dual<N>& a, double c) {
+  return a.v <= c ? a : dconst<N>(c);
+}
+
+// value of lane `src` of a warp for a Dual<1> (the tangent of direction src)
+__device__ __forceinline__ Dual<1> shfl_d1(const Dual<1>& x, int src) {
+  Dual<1> r;
+  r.v = __shfl_sync(0xffffffffu, x.v, src);
+  r.d[0] = __shfl_sync(0xffffffffu, x.d[0], src);
+  return r;
+}
+
+// Gather the 8 directions held by lanes 0..7 (one Dual<1> each) into a Dual<8>.
+__device__ __forceinline__ Dual<NDIR> gather8(const Dual<1>& x) {
+  Dual<NDIR> r;
+  r.v = __shfl_sync(0xffffffffu, x.v, 0);
+#pragma unroll
+  for (int i = 0; i < NDIR; ++i) r.d[i] = __shfl_sync(0xffffffffu, x.d[0], i);
+  return r;
+}
+
+// ------------------------------------------------------- templated physics --
+// The float64 formulas of jcg_internal.cuh / jcg_tables.cu / jcg_halofit.cu
+// written for a number type T; grid abscissae (a, k) stay double.
+
+template <class T>
+struct BgT {
+  T Om, Ok, Ode, w0, wa;
+};
+
+template <class T>
+__device__ __forceinline__ BgT<T> make_bgT(const T* s) {
+  BgT<T> b;
+  b.Om = s[S_OMEGA_M];
+  b.Ok = s[S_OMEGA_K];
+  b.Ode = s[S_OMEGA_DE];
+  b.w0 = s[S_W0];
+  b.wa = s[S_WA];
+  return b;
+}
+
+// background.py:90, 122-126
+template <class T>
+__device__ __forceinline__ T esqrT(const BgT<T>& c, double a, double lna, T* efde) {
+  const T f = -3.0 * (1.0 + c.w0 + c.wa) * lna + 3.0 * c.wa * (a - 1.0);
+  const T ef = xexp(f);
+  if (efde) *efde = ef;
+  const double ia = 1.0 / a, ia2 = ia * ia;
+  return c.Om * (ia2 * ia) + c.Ok * ia2 + c.Ode * ef;
+}
+// background.py:168, 196
+template <class T>
+__device__ __forceinline__ void omT(const BgT<T>& c, double a, double lna, T& omm, T& omde) {
+  T ef;
+  const T e2 = esqrT(c, a, lna, &ef);
+  const double ia = 1.0 / a;
+  omm = c.Om * (ia * ia * ia) / e2;
+  omde = c.Ode * ef / e2;
+}
+// background.py:294
+template <class T>
+__device__ __forceinline__ T dchioverdaT(const BgT<T>& c, double a, double lna) {
+  return RH / ((a * a) * xsqrt(esqrT(c, a, lna, (T*)nullptr)));
+}
+// background.py:53
+template <class T>
+__device__ __forceinline__ T wT(const BgT<T>& c, double a) {
+  return c.w0 + (1.0 - a) * c.wa;
+}
+// background.py:227-229
+template <class T>
+__device__ __forceinline__ T dchi_dlnaT(const BgT<T>& c, double x) {
+  const double xa = exp(x);
+  return dchioverdaT(c, xa, x) * xa;
+}
+// background.py:96-106
+template <class T>
+__device__ __forceinline__ void growth_qrT(const BgT<T>& b, double x, T& q, T& r) {
+  T omm, omde;
+  omT(b, x, log(x), omm, omde);
+  q = (2.0 - 0.5 * (omm + (1.0 + 3.0 * wT(b, x)) * omde)) / x;
+  r = 1.5 * omm / x / x;
+}
+
+// transfer.py:47-142, core.py:145-162 (cosmo_scalars of jcg_tables.cu)
+template <class T>
+__device__ void cosmo_scalarsT(const T* p, T* s) {
+  for (int i = 0; i < NSCAL; ++i) s[i] = T(p[0] * 0.0);
+  const T Oc = p[0], Ob = p[1], h = p[2];
+  s[S_OMEGA_C] = Oc;
+  s[S_OMEGA_B] = Ob;
+  s[S_H] = h;
+  s[S_NS] = p[3];
+  s[S_SIGMA8] = p[4];
+  s[S_OMEGA_K] = p[5];
+  s[S_W0] = p[6];
+  s[S_WA] = p[7];
+  const T Om = Ob + Oc;
+  s[S_OMEGA_M] = Om;
+  s[S_OMEGA_DE] = (1.0 - p[5]) - Om;
+  const double T27 = (TCMB / 2.7) * (TCMB / 2.7);
+  const T h2 = h * h;
+  const T w_m = Om * h2;
+  const T w_b = Ob * h2;
+  const T fb = Ob / Om;
+  const T fc = (Om - Ob) / Om;
+  const T k_eq = 7.46e-2 * w_m / T27 / h;
+  const T z_eq = 2.50e4 * w_m / (T27 * T27);
+  T b1 = 0.313 * xpow(w_m, -0.419) * (1.0 + 0.607 * xpow(w_m, 0.674));
+  T b2 = 0.238 * xpow(w_m, 0.223);
+  const T z_d = 1291.0 * xpow(w_m, 0.251) / (1.0 + 0.659 * xpow(w_m, 0.828)) *
+                (1.0 + b1 * xpow(w_b, b2));
+  const T R_d = 31.5 * w_b / (T27 * T27) * (1.0e3 / z_d);
+  const T R_eq = 31.5 * w_b / (T27 * T27) * (1.0e3 / z_eq);
+  const T sh_d = 2.0 / (3.0 * k_eq) * xsqrt(6.0 / R_eq) *
+                 xlog((xsqrt(1.0 + R_d) + xsqrt(R_eq + R_d)) / (1.0 + xsqrt(R_eq)));
+  const T k_silk = 1.6 * xpow(w_b, 0.52) * xpow(w_m, 0.73) * (1.0 + xpow(10.4 * w_m, -0.95)) / h;
+  const T a1 = xpow(46.9 * w_m, 0.670) * (1.0 + xpow(32.1 * w_m, -0.532));
+  const T a2 = xpow(12.0 * w_m, 0.424) * (1.0 + xpow(45.0 * w_m, -0.582));
+  const T alpha_c = xpow(a1, -fb) * xpow(a2, -(fb * fb * fb));
+  b1 = 0.944 / (1.0 + xpow(458.0 * w_m, -0.708));
+  b2 = xpow(0.395 * w_m, -0.0266);
+  T beta_c = 1.0 + b1 * (xpow(fc, b2) - 1.0);
+  beta_c = 1.0 / beta_c;
+  const T y = (1.0 + z_eq) / (1.0 + z_d);
+  const T x = xsqrt(1.0 + y);
+  const T G = y * (-6.0 * x + (2.0 + 3.0 * y) * xlog((x + 1.0) / (x - 1.0)));
+  const T alpha_b = 2.07 * k_eq * sh_d * xpow(1.0 + R_d, -0.75) * G;
+  const T beta_node = 8.41 * xpow(w_m, 0.435);
+  const T beta_b = 0.5 + fb + (3.0 - 2.0 * fb) * xsqrt((17.2 * w_m) * (17.2 * w_m) + 1.0);
+  s[S_K_EQ] = k_eq;
+  s[S_Z_EQ] = z_eq;
+  s[S_Z_D] = z_d;
+  s[S_R_D] = R_d;
+  s[S_R_EQ] = R_eq;
+  s[S_SH_D] = sh_d;
+  s[S_K_SILK] = k_silk;
+  s[S_ALPHA_C] = alpha_c;
+  s[S_BETA_C] = beta_c;
+  s[S_ALPHA_B] = alpha_b;
+  s[S_BETA_B] = beta_b;
+  s[S_BETA_NODE] = beta_node;
+  s[S_FB] = fb;
+  s[S_FC] = fc;
+  s[S_LGQ] = xlog(13.41 * k_eq);
+  s[S_LGKSILK] = xlog(k_silk);
+}
+
+// transfer.py:107-153 at a fixed wavenumber k (lk = log k)
+template <class T>
+__device__ __forceinline__ T eh_transferT(const T* s, double k, double lk) {
+  const T k_eq = s[S_K_EQ], sh_d = s[S_SH_D];
+  const T q = k / (13.41 * k_eq);
+  const T q108 = xexp(1.08 * (lk - s[S_LGQ]));
+  const T Cb = 386.0 / (1.0 + 69.9 * q108);
+  const T qq = q * q;
+  const T L1 = xlog(EULER_E + 1.8 * s[S_BETA_C] * q);
+  const T L2 = xlog(EULER_E + 1.8 * q);
+  const T Ta = L1 / (L1 + (14.2 + Cb) * qq);
+  const T Tb = L1 / (L1 + (14.2 / s[S_ALPHA_C] + Cb) * qq);
+  const T Tn = L2 / (L2 + (14.2 + Cb) * qq);
+  const T ksh = k * sh_d;
+  const T x54 = ksh / 5.4, x54s = x54 * x54;
+  const T f = 1.0 / (1.0 + x54s * x54s);
+  const T Tc = f * Ta + (1.0 - f) * Tb;
+  const T bn = s[S_BETA_NODE] / ksh;
+  const T tilde_s = sh_d / xcbrt(1.0 + bn * bn * bn);
+  const T x52 = ksh / 5.2;
+  const T bb = s[S_BETA_B] / ksh;
+  const T silk = xexp(-xexp(1.4 * (lk - s[S_LGKSILK])));
+  const T arg = k * tilde_s;
+  const T sinc = xsin(arg) / arg;
+  const T Tbar = (Tn / (1.0 + x52 * x52) + s[S_ALPHA_B] / (1.0 + bb * bb * bb) * silk) * sinc;
+  return s[S_FB] * Tbar + s[S_FC] * Tc;
+}
+
+// power.py:42-53 at a fixed wavenumber
+template <class T>
+__device__ __forceinline__ T pk_linearT(const T* s, double k, double lk, const T& g) {
+  const T t = eh_transferT(s, k, lk);
+  const T pk = xexp(s[S_NS] * lk) * (t * t) * (g * g);
+  return pk * s[S_PKNORM];
+}
+
+}  // namespace jcg

@@ -1,0 +1,915 @@
+// Derivatives of C_ell with respect to the 8 Cosmology leaves (core.py:98-108):
+// the Jacobian dC_ij(l)/dtheta of angular_cl (angular_cl.py:49-98), FP64.
+//
+// Tables (background ODEs, sigma8, sigma^2(R), P(k) k^3), per-node halofit
+// parameters and radial kernels are differentiated forward: value + 8
+// tangents.  Scalar chains run with one tangent direction per lane (lanes 0-7
+// of a warp each carry Dual<1>), per-term loops with Dual<8>.  The Limber
+// integrand, evaluated n_ell x Na times, is differentiated backward by a
+// hand-written reverse sweep (node_fb) that returns dP/d(inputs); contracting
+// with the inputs' tangents gives dP/dtheta, and
+//   dC_ij(l)/dtheta = ef_ij(l) sum_a [dP(l,a)/dtheta M_ij(a) + P(l,a) dM_ij(a)/dtheta].
+// The tables are recomputed here from the parameters, not taken from a
+// forward pass.  Derivative conventions are JAX's for the reference's
+// operations (max/min pass the tangent of the selected branch; the
+// interpolation segment is locally constant).
+#include "jcg_dual.cuh"
+
+namespace jcg {
+
+constexpr double TWO_PI2_G = 2.0 * (PI * PI);
+constexpr double C2_G = C_KMS * C_KMS;
+constexpr double LN10_G = 2.302585092994046;
+
+// ------------------------------------------------------------ dual tables ---
+struct TabD {
+  double sv[NSCAL];
+  double sd[NDIR][NSCAL];
+  double chiv[NCHI];
+  double chid[NDIR][NCHI];
+  double gv[NGROW];
+  double gd[NDIR][NGROW];
+  double sigv[NRT];
+  double sigd[NDIR][NRT];
+  double pk3v[NKH];
+  double pk3d[NDIR][NKH];
+  double pad[7];
+};
+static_assert(sizeof(TabD) % 64 == 0, "TabD alignment");
+
+// per-node inputs of the Limber integrand (node_fb), value + 8 tangents
+enum NodeA { A_CHIC = 0, A_G, A_KNL, A_BETA, A_ALPHA, A_AN, A_BN, A_LCF3, A_F1, A_F2, A_GAM, A_NU, A_U, NA_IN };
+constexpr int NROWD = NA_IN * (NDIR + 1);  // [NA_IN] values then [NDIR][NA_IN] tangents
+// per-cosmology inputs of the integrand
+enum NodeC { C_KEQ = 0, C_SH, C_BETAC, C_ALPHAC, C_ALPHAB, C_BETAB, C_BETANODE, C_KSILK, C_FB, C_FC, C_NS, C_PKNORM, NC_IN };
+__device__ __constant__ const int kNodeCScalar[NC_IN] = {S_K_EQ,  S_SH_D,      S_BETA_C,  S_ALPHA_C,
+                                                         S_ALPHA_B, S_BETA_B, S_BETA_NODE, S_K_SILK,
+                                                         S_FB,    S_FC,        S_NS,      S_PKNORM};
+
+struct GradBatch {
+  int n_items;
+  const double* params;
+  const GeoHeader* geo;
+  TabD* tab;
+  double* rowd;    // [B][na][NROWD]
+  double* kernd;   // [B][n_tr][na][NDIR + 1]
+  double* part;    // [n_split][B][n_cls][n_ell][NDIR + 1] partial sums over a
+  double* cl;      // [B][n_cls][n_ell]
+  double* jac;     // [B][n_cls][n_ell][NDIR]
+  int na, n_tr, n_cls, n_ell, n_split;
+};
+
+typedef Dual<1> D1;
+typedef Dual<NDIR> D8;
+
+__device__ __forceinline__ D1 mk1(double v, double d) {
+  D1 r;
+  r.v = v;
+  r.d[0] = d;
+  return r;
+}
+
+// interpolation (scipy/interpolate.py:55-59) with a dual table fp
+__device__ __forceinline__ D1 interp_d1(double x, const double* xp, const double* fv, const double* fd,
+                                        int2 sg) {
+  const D1 f0 = mk1(fv[sg.x], fd[sg.x]), f1 = mk1(fv[sg.y], fd[sg.y]);
+  const D1 a = (f1 - f0) / (xp[sg.y] - xp[sg.x]);
+  const D1 b = f0 - a * xp[sg.x];
+  return a * x + b;
+}
+
+// Tables of one cosmology with tangents.  Lanes: dir = tid & 7, item = tid >> 3.
+__global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+  const int item = blockIdx.x;
+  if (item >= gb.n_items) return;
+  extern __shared__ double sm[];
+  double* sv = sm;                      // NSCAL
+  double* sd = sv + NSCAL;              // [NDIR][NSCAL]
+  double* fn = sd + NDIR * NSCAL;       // [NDIR+1][NCHI] f at nodes
+  double* fm = fn + (NDIR + 1) * NCHI;  // [NDIR+1][NCHI] f at midpoints
+  double* qr = fm + (NDIR + 1) * NCHI;  // [4][NDIR+1][NGROW] qa, ra, qm, rm
+  double* fr = qr + 4 * (NDIR + 1) * NGROW;   // [NDIR+1][NROMB]
+  double* chi = fr + (NDIR + 1) * NROMB;      // [NDIR+1][NCHI]
+  double* gt = chi + (NDIR + 1) * NCHI;       // [NDIR+1][NGROW]
+  double* pq = gt + (NDIR + 1) * NGROW;       // [NDIR+1][NKH]
+  double* g1s = pq + (NDIR + 1) * NKH;        // [NDIR+1]
+  const int t = threadIdx.x, dir = t & 7, it = t >> 3;
+  const double* P = gb.params + 8 * (size_t)item;
+  TabD* out = gb.tab + item;
+  // scalars (lanes 0-7 of warp 0)
+  if (t < NDIR) {
+    D1 p[8];
+    for (int i = 0; i < 8; ++i) p[i] = mk1(P[i], i == dir ? 1.0 : 0.0);
+    D1 s[NSCAL];
+    cosmo_scalarsT(p, s);
+    for (int i = 0; i < NSCAL; ++i) {
+      if (dir == 0) sv[i] = s[i].v;
+      sd[dir * NSCAL + i] = s[i].d[0];
+    }
+  }
+  __syncthreads();
+  D1 sD[NSCAL];
+  for (int i = 0; i < NSCAL; ++i) sD[i] = mk1(sv[i], sd[dir * NSCAL + i]);
+  const BgT<D1> bg = make_bgT(sD);
+  auto put = [&](double* arr, int stride, int e, const D1& x) {
+    if (dir == 0) arr[e] = x.v;
+    arr[(1 + dir) * stride + e] = x.d[0];
+  };
+  // chi RK4 right-hand side at nodes and midpoints (background.py:227-231)
+  for (int e = it; e < 2 * NCHI; e += 32) {
+    if (e < NCHI) {
+      put(fn, NCHI, e, dchi_dlnaT(bg, c->lna_chi[e]));
+    } else if (e > NCHI) {
+      const int i = e - NCHI;
+      const double t0 = c->lna_chi[i - 1], t1 = c->lna_chi[i];
+      put(fm, NCHI, i, dchi_dlnaT(bg, t0 + (t1 - t0) / 2));
+    }
+  }
+  // growth ODE coefficients (background.py:96-106)
+  for (int e = it; e < 2 * NGROW; e += 32) {
+    D1 q, r;
+    if (e < NGROW) {
+      growth_qrT(bg, c->atab_grow[e], q, r);
+      put(qr + 0 * (NDIR + 1) * NGROW, NGROW, e, q);
+      put(qr + 1 * (NDIR + 1) * NGROW, NGROW, e, r);
+    } else if (e > NGROW) {
+      const int i = e - NGROW;
+      const double x = c->atab_grow[i], xp = c->atab_grow[i - 1];
+      growth_qrT(bg, xp + (x - xp) / 2, q, r);
+      put(qr + 2 * (NDIR + 1) * NGROW, NGROW, i, q);
+      put(qr + 3 * (NDIR + 1) * NGROW, NGROW, i, r);
+    }
+  }
+  // sigmasqr(8) integrand at the romb nodes (power.py:70-75)
+  for (int e = it; e < NROMB; e += 32) {
+    const double logk = c->romb_logk[e];
+    const double k = exp(logk);
+    const double x = k * 8.0;
+    const double wf = 3.0 * (sin(x) - x * cos(x)) / (x * x * x);
+    const D1 T = eh_transferT(sD, k, logk);
+    const D1 pk = (T * T) * xexp(sD[S_NS] * logk);
+    const double kw = k * wf;
+    put(fr, NROMB, e, k * (kw * kw) * pk);
+  }
+  __syncthreads();
+  const int warp = t >> 5, lane = t & 31;
+  if (lane < NDIR) {
+    const int d = lane;
+    auto gv = [&](const double* arr, int stride, int e) { return mk1(arr[e], arr[(1 + d) * stride + e]); };
+    if (warp == 0) {
+      // chi prefix sum (scipy/ode.py:21 first step h = 0), then chi[-1] - chi
+      D1 y = mk1(0.0, 0.0);
+      D1 ys[NCHI];
+      ys[0] = y;
+      for (int i = 1; i < NCHI; ++i) {
+        const double hh = c->lna_chi[i] - c->lna_chi[i - 1];
+        const D1 fmv = gv(fm, NCHI, i);
+        y = y + 1.0 / 6.0 * hh * (gv(fn, NCHI, i - 1) + 2 * fmv + 2 * fmv + gv(fn, NCHI, i));
+        ys[i] = y;
+      }
+      for (int i = 0; i < NCHI; ++i) {
+        const D1 v = ys[NCHI - 1] - ys[i];
+        if (d == 0) chi[i] = v.v;
+        chi[(1 + d) * NCHI + i] = v.d[0];
+      }
+    } else if (warp == 1) {
+      // growth RK4 in a (background.py:108-111)
+      const double* QA = qr;
+      const double* RA = qr + (NDIR + 1) * NGROW;
+      const double* QM = qr + 2 * (NDIR + 1) * NGROW;
+      const double* RM = qr + 3 * (NDIR + 1) * NGROW;
+      D1 y0 = mk1(c->atab_grow[0], 0.0), y1 = mk1(1.0, 0.0);
+      D1 ys[NGROW];
+      ys[0] = y0;
+      for (int i = 1; i < NGROW; ++i) {
+        const double hh = c->atab_grow[i] - c->atab_grow[i - 1];
+        const D1 qa0 = gv(QA, NGROW, i - 1), ra0 = gv(RA, NGROW, i - 1);
+        const D1 qm = gv(QM, NGROW, i), rm = gv(RM, NGROW, i);
+        const D1 qa1 = gv(QA, NGROW, i), ra1 = gv(RA, NGROW, i);
+        const D1 k1a = y1, k1b = -qa0 * y1 + ra0 * y0;
+        const D1 y0b = y0 + hh * k1a / 2, y1b = y1 + hh * k1b / 2;
+        const D1 k2a = y1b, k2b = -qm * y1b + rm * y0b;
+        const D1 y0c = y0 + hh * k2a / 2, y1c = y1 + hh * k2b / 2;
+        const D1 k3a = y1c, k3b = -qm * y1c + rm * y0c;
+        const D1 y0d = y0 + hh * k3a, y1d = y1 + hh * k3b;
+        const D1 k4a = y1d, k4b = -qa1 * y1d + ra1 * y0d;
+        y0 = y0 + 1.0 / 6.0 * hh * (k1a + 2 * k2a + 2 * k3a + k4a);
+        y1 = y1 + 1.0 / 6.0 * hh * (k1b + 2 * k2b + 2 * k3b + k4b);
+        ys[i] = y0;
+      }
+      for (int i = 0; i < NGROW; ++i) {
+        const D1 v = ys[i] / y0;
+        if (d == 0) gt[i] = v.v;
+        gt[(1 + d) * NGROW + i] = v.d[0];
+      }
+    } else if (warp == 2) {
+      // romb combination (scipy/integrate.py:131-159), divmax = 7
+      const double a = -4.0, b = 3.0, intrange = b - a;
+      D1 ordsum = 0.5 * (gv(fr, NROMB, 0) + gv(fr, NROMB, 1));
+      D1 state[8];
+      for (int i = 0; i < 8; ++i) state[i] = intrange * ordsum;
+      int pos = 2;
+      for (int lev = 1; lev <= 7; ++lev) {
+        const int n = 1 << lev, numtosum = n / 2;
+        D1 sum = mk1(0.0, 0.0);
+        for (int m = 0; m < numtosum; ++m) sum = sum + gv(fr, NROMB, pos + m);
+        pos += numtosum;
+        ordsum = ordsum + sum;
+        D1 x = intrange * ordsum / (double)n;
+        D1 ns[8];
+        ns[0] = x;
+        for (int kk = 0; kk < 7; ++kk) {
+          const double tmp = ldexp(1.0, 2 * (kk + 1));
+          x = (tmp * x - state[kk]) / (tmp - 1.0);
+          ns[kk + 1] = x;
+        }
+        for (int i = 0; i < 8; ++i) state[i] = ns[i];
+      }
+      const D1 sig8 = 1.0 / (2.0 * (PI * PI)) * state[7];
+      const D1 s8 = mk1(sv[S_SIGMA8], sd[d * NSCAL + S_SIGMA8]);
+      const D1 pkn = (s8 * s8) / sig8;
+      if (d == 0) {
+        sv[S_SIGMASQR8] = sig8.v;
+        sv[S_PKNORM] = pkn.v;
+      }
+      sd[d * NSCAL + S_SIGMASQR8] = sig8.d[0];
+      sd[d * NSCAL + S_PKNORM] = pkn.d[0];
+    }
+  }
+  __syncthreads();
+  if (t < NDIR) {
+    // growth_factor(1.0)
+    const int2 sg = interp_segment_inc(1.0, c->atab_grow, NGROW, NGROW - 1);
+    D1 g1 = interp_d1(1.0, c->atab_grow, gt, gt + (1 + dir) * NGROW, sg);
+    g1 = xfmin(xfmax(g1, 0.0), 1.0);
+    if (dir == 0) g1s[0] = g1.v;
+    g1s[1 + dir] = g1.d[0];
+  }
+  __syncthreads();
+  for (int i = 0; i < NSCAL; ++i) sD[i] = mk1(sv[i], sd[dir * NSCAL + i]);
+  const D1 g1 = mk1(g1s[0], g1s[1 + dir]);
+  // P(k_i, a = 1) k_i^3 and pk3 / (2 pi^2) on the halofit grid
+  for (int e = it; e < NKH; e += 32) {
+    const double k = c->kh[e];
+    const D1 p3 = pk_linearT(sD, k, c->logk[e], g1) * c->kh3[e];
+    if (dir == 0) out->pk3v[e] = p3.v;
+    out->pk3d[dir][e] = p3.d[0];
+    put(pq, NKH, e, p3 / (2.0 * (PI * PI)));
+  }
+  __syncthreads();
+  // sigma^2(R_j) without g^2 (power.py:98-111), value and tangents
+  const double dx = (c->logk[NKH - 1] - c->logk[0]) / 256;
+  for (int e = t; e < (NDIR + 1) * NRT; e += blockDim.x) {
+    const int comp = e / NRT, j = e % NRT;
+    const double* w = pq + comp * NKH;
+    double acc = 0.0;
+    for (int m = 0; m < 128; ++m) {
+      const double y0 = w[2 * m] * c->E[(2 * m) * NRT + j];
+      const double y1 = w[2 * m + 1] * c->E[(2 * m + 1) * NRT + j];
+      const double y2 = w[2 * m + 2] * c->E[(2 * m + 2) * NRT + j];
+      acc += y0 + 4 * y1 + y2;
+    }
+    if (comp == 0) out->sigv[j] = dx / 3 * acc;
+    else out->sigd[comp - 1][j] = dx / 3 * acc;
+  }
+  for (int i = t; i < NSCAL; i += blockDim.x) {
+    out->sv[i] = sv[i];
+    for (int d = 0; d < NDIR; ++d) out->sd[d][i] = sd[d * NSCAL + i];
+  }
+  for (int i = t; i < NCHI; i += blockDim.x) {
+    out->chiv[i] = chi[i];
+    for (int d = 0; d < NDIR; ++d) out->chid[d][i] = chi[(1 + d) * NCHI + i];
+  }
+  for (int i = t; i < NGROW; i += blockDim.x) {
+    out->gv[i] = gt[i];
+    for (int d = 0; d < NDIR; ++d) out->gd[d][i] = gt[(1 + d) * NGROW + i];
+  }
+}
+
+size_t grad_tables_smem() {
+  return sizeof(double) * (NSCAL * (1 + NDIR) + (NDIR + 1) * (2 * NCHI + 4 * NGROW + NROMB + NCHI + NGROW + NKH + 1));
+}
+
+// ----------------------------------------------------------- dual rows -----
+// One warp per Limber node: growth, chi and the halofit root find with
+// tangents on lanes 0-7, the spectral moments over 32 lanes in Dual<8>, then
+// the takahashi2012 coefficients and the Limber weight on lanes 0-7.
+__global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+  const int item = blockIdx.y;
+  if (item >= gb.n_items) return;
+  const GeoHeader* geo = gb.geo;
+  const int na = geo->na;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = blockIdx.x * 8 + warp;
+  if (n >= na) return;
+  const TabD* tb = gb.tab + item;
+  const int dir = lane & 7;
+  const double* A = geo_ptr<double>(geo, geo->off_a);
+  const double* WS = geo_ptr<double>(geo, geo->off_wsimp);
+  const int64_t* SC = geo_ptr<int64_t>(geo, geo->off_seg_chi);
+  const int64_t* SG = geo_ptr<int64_t>(geo, geo->off_seg_grow);
+  const double a = A[n];
+  // prelude on every lane (lanes 8..31 duplicate lanes 0..7)
+  D1 g = interp_d1(a, c->atab_grow, tb->gv, tb->gd[dir], unpack_seg(SG[n]));
+  g = xfmin(xfmax(g, 0.0), 1.0);
+  D1 chi = interp_d1(a, c->atab_chi, tb->chiv, tb->chid[dir], unpack_seg(SC[n]));
+  chi = xfmax(chi, 0.0);
+  const D1 g2 = g * g;
+  // root find: index from values (same arithmetic as the forward), tangents through the formula
+  int best;
+  {
+    int lo = 0, hi = NRT;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (tb->sigv[mid] * g2.v > 1.0) lo = mid + 1;
+      else hi = mid;
+    }
+    const int cc = lo;
+    best = cc < NRT ? cc : NRT - 1;
+    if (cc >= 1) {
+      const double dlo = 1.0 - tb->sigv[cc - 1] * g2.v;
+      if (cc < NRT) {
+        const double dhi = 1.0 - tb->sigv[cc] * g2.v;
+        best = (dlo * dlo <= dhi * dhi) ? cc - 1 : cc;
+      } else {
+        best = cc - 1;
+      }
+    }
+  }
+  const int ind = best < 1 ? 1 : (best > NRT - 2 ? NRT - 2 : best);
+  const double xpi = tb->sigv[ind] * g2.v;
+  const double xc = fmin(fmax(1.0, tb->sigv[1] * g2.v), tb->sigv[NRT - 2] * g2.v);
+  const int j2 = ind + ((xc - xpi >= 0.0) ? 1 : -1);
+  const D1 xp0 = mk1(tb->sigv[ind], tb->sigd[dir][ind]) * g2;
+  const D1 xp1 = mk1(tb->sigv[j2], tb->sigd[dir][j2]) * g2;
+  const D1 slope = (c->logr[j2] - c->logr[ind]) / (xp1 - xp0);
+  const D1 bb = c->logr[ind] - slope * xp0;
+  const D1 root = slope * 1.0 + bb;
+  const D1 R = xfmax(xexp(root), 1e-6);
+  const D1 knl = 1.0 / R;
+  const D1 inv = 1.0 / knl;
+  // moments (power.py:121-139) in Dual<8>; terms with y^2 > 60 are below 1e-20 of the sums
+  const D8 inv8 = gather8(inv);
+  const D8 g2_8 = gather8(g2);
+  D8 s1 = dconst<NDIR>(0.0), s2 = dconst<NDIR>(0.0);
+  for (int i = lane; i < NKH; i += 32) {
+    const D8 y = c->kh[i] * inv8;
+    const D8 y2 = y * y;
+    if (y2.v > 60.0) continue;
+    D8 p3;
+    p3.v = tb->pk3v[i];
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) p3.d[d] = tb->pk3d[d][i];
+    const D8 res = p3 * xexp(-y2) * g2_8 / TWO_PI2_G;
+    s1 = s1 + c->simpson_kh[i] * (2 * res * y2);
+    s2 = s2 + c->simpson_kh[i] * (4 * res * (y2 - y2 * y2));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s1.v += __shfl_xor_sync(0xffffffffu, s1.v, o);
+    s2.v += __shfl_xor_sync(0xffffffffu, s2.v, o);
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) {
+      s1.d[d] += __shfl_xor_sync(0xffffffffu, s1.d[d], o);
+      s2.d[d] += __shfl_xor_sync(0xffffffffu, s2.d[d], o);
+    }
+  }
+  double s1d = 0.0, s2d = 0.0;
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d)
+    if (d == dir) {
+      s1d = s1.d[d];
+      s2d = s2.d[d];
+    }
+  const D1 I1 = mk1(s1.v, s1d), I2 = mk1(s2.v, s2d);
+  const D1 neff = I1 - 3.0;
+  const D1 C = I1 * I1 + I2;
+  // coefficients (power.py:177-238)
+  D1 sD[NSCAL];
+  for (int i = 0; i < NSCAL; ++i) sD[i] = mk1(tb->sv[i], tb->sd[dir][i]);
+  const BgT<D1> bg = make_bgT(sD);
+  const double lna = log(a);
+  D1 om_m, om_de;
+  omT(bg, a, lna, om_m, om_de);
+  const D1 w = wT(bg, a);
+  const D1 n2 = neff * neff, n3 = n2 * neff, n4 = n2 * n2;
+  const D1 e_an = 1.5222 + 2.8553 * neff + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 - 0.6038 * C +
+                  0.1749 * om_de * (1.0 + w);
+  const D1 e_bn = -0.5642 + 0.5864 * neff + 0.5716 * n2 - 1.5474 * C + 0.2279 * om_de * (1.0 + w);
+  const D1 e_cn = 0.3698 + 2.0404 * neff + 0.8161 * n2 + 0.5869 * C;
+  const D1 lom = xlog(om_m);
+  D1 outv[NA_IN];
+  outv[A_CHIC] = xfmax(chi, 1.0);
+  outv[A_G] = g;
+  outv[A_KNL] = knl;
+  outv[A_BETA] = 2.0379 - 0.7354 * neff + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
+  outv[A_ALPHA] = xfabs(6.0835 + 1.3373 * neff - 0.1959 * n2 - 5.5274 * C);
+  outv[A_AN] = xexp(LN10_G * e_an);
+  outv[A_BN] = xexp(LN10_G * e_bn);
+  outv[A_LCF3] = LN10_G * e_cn + 0.0743 * lom;
+  outv[A_F1] = xexp(-0.0307 * lom);
+  outv[A_F2] = xexp(-0.0585 * lom);
+  outv[A_GAM] = 0.1971 - 0.0843 * neff + 0.8460 * C;
+  outv[A_NU] = xexp(LN10_G * (5.2105 + 3.6902 * neff));
+  const D1 dchi = dchioverdaT(bg, a, lna);
+  outv[A_U] = WS[n] * dchi / xfmax(chi * chi, 1.0) / C2_G;
+  if (lane < NDIR) {
+    double* row = gb.rowd + ((size_t)item * na + n) * NROWD;
+    for (int i = 0; i < NA_IN; ++i) {
+      if (dir == 0) row[i] = outv[i].v;
+      row[NA_IN * (1 + dir) + i] = outv[i].d[0];
+    }
+  }
+}
+
+// ------------------------------------------------------ dual radial kernels -
+// One warp per node: chi_wl and H on lanes 0-7, the lensing integrand over 32
+// lanes in Dual<8> (probes.py:44-51), four tracers per pass.
+__global__ void __launch_bounds__(256) grad_kern_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+  const int item = blockIdx.y;
+  if (item >= gb.n_items) return;
+  const GeoHeader* geo = gb.geo;
+  const int na = geo->na, n_tr = geo->n_tr;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = blockIdx.x * 8 + warp;
+  if (n >= na) return;
+  const TabD* tb = gb.tab + item;
+  const int dir = lane & 7;
+  const double* Z = geo_ptr<double>(geo, geo->off_z);
+  const double* AWL = geo_ptr<double>(geo, geo->off_awl);
+  const int64_t* SW = geo_ptr<int64_t>(geo, geo->off_seg_chiwl);
+  const double* NZL = geo_ptr<double>(geo, geo->off_nzl);
+  const double awl = AWL[n], z = Z[n];
+  D1 sD[NSCAL];
+  for (int i = 0; i < NSCAL; ++i) sD[i] = mk1(tb->sv[i], tb->sd[dir][i]);
+  const D1 chi_wl = xfmax(interp_d1(awl, c->atab_chi, tb->chiv, tb->chid[dir], unpack_seg(SW[n])), 0.0);
+  const D1 cf = 3.0 * (H0 * H0) * sD[S_OMEGA_M] / 2.0 / C_KMS;  // probes.py:71
+  const D8 chiwl8 = gather8(chi_wl);
+  double* kd = gb.kernd + (size_t)item * n_tr * na * (NDIR + 1);
+  for (int t0 = 0; t0 < n_tr; t0 += 4) {
+    int tl[4];
+    int cnt = 0;
+    for (int t = t0; t < min(t0 + 4, n_tr); ++t) tl[cnt++] = t;
+    D8 acc[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) acc[u] = dconst<NDIR>(0.0);
+    bool any_wl = false;
+    for (int u = 0; u < cnt; ++u) any_wl |= geo->kind[tl[u]] == JCG_TRACER_WL;
+    if (any_wl) {
+      for (int g = 0; g < geo->n_groups; ++g) {
+        const size_t row = (size_t)n * NZP;
+        const double* AP = geo_ptr<double>(geo, geo->off_ap[g]) + row;
+        const int64_t* SP = geo_ptr<int64_t>(geo, geo->off_segp[g]) + row;
+        for (int j = lane; j < NZP; j += 32) {
+          const double ap = AP[j];
+          const int2 sg = unpack_seg(SP[j]);
+          const double ixp = 1.0 / (c->atab_chi[sg.y] - c->atab_chi[sg.x]);
+          D8 chip;
+          {
+            const double a_s = (tb->chiv[sg.y] - tb->chiv[sg.x]) * ixp;
+            const double b_s = tb->chiv[sg.x] - a_s * c->atab_chi[sg.x];
+            chip.v = a_s * ap + b_s;
+#pragma unroll
+            for (int d = 0; d < NDIR; ++d) {
+              const double ad = (tb->chid[d][sg.y] - tb->chid[d][sg.x]) * ixp;
+              chip.d[d] = tb->chid[d][sg.x] + ad * (ap - c->atab_chi[sg.x]);
+            }
+          }
+          chip = xfmax(chip, 0.0);
+          const D8 ratio = xfmax(chip - chiwl8, 0.0) / xfmax(chip, 1.0);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            if (u < cnt && geo->kind[tl[u]] == JCG_TRACER_WL && geo->group[tl[u]] == g) {
+              const double Wv = geo_ptr<double>(geo, geo->off_W[tl[u]])[row + j];
+              acc[u] = acc[u] + Wv * ratio;
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          acc[u].v += __shfl_xor_sync(0xffffffffu, acc[u].v, o);
+#pragma unroll
+          for (int d = 0; d < NDIR; ++d) acc[u].d[d] += __shfl_xor_sync(0xffffffffu, acc[u].d[d], o);
+        }
+      }
+    }
+    if (lane < NDIR) {
+      for (int u = 0; u < cnt; ++u) {
+        const int t = tl[u];
+        D1 kv;
+        if (geo->kind[t] == JCG_TRACER_WL) {
+          double ad = 0.0;
+#pragma unroll
+          for (int d = 0; d < NDIR; ++d)
+            if (d == dir) ad = acc[u].d[d];
+          const D1 rk = mk1(acc[u].v, ad) * (1.0 + z) * chi_wl;
+          kv = cf * rk * (1.0 + geo->mult[t]);
+        } else {
+          const BgT<D1> bg = make_bgT(sD);
+          const D1 H = H0 * xsqrt(esqrT(bg, awl, log(awl), (D1*)nullptr));
+          kv = NZL[(size_t)t * na + n] * geo->bias[t] * H;
+        }
+        double* dst = kd + ((size_t)t * na + n) * (NDIR + 1);
+        if (dir == 0) dst[0] = kv.v;
+        dst[1 + dir] = kv.d[0];
+      }
+    }
+  }
+}
+
+// ------------------------------------------------ Limber integrand adjoint --
+struct NodeX {
+  double chic, g, knl, beta, alpha, an, bn, lcf3, f1, f2, gam, nu;
+};
+struct NodeK {
+  double keq, sh, betac, alphac, alphab, betab, betanode, ksilk, fb, fc, ns, pknorm;
+};
+
+// P(k = kh / chic, a) of halofit_node_lk (Eisenstein-Hu x primordial x
+// takahashi2012, transfer.py:107-153, power.py:42-53, 246-260) and its
+// partial derivatives: ga[NodeA] (per-node inputs) and gc[NodeC]
+// (per-cosmology inputs) receive dP/d(input).  Hand-written reverse sweep.
+__device__ double node_fb(double kh, double lkh, const NodeX& x, const NodeK& c, double* ga, double* gc) {
+  // forward
+  const double k = kh / x.chic;
+  const double lk = lkh - log(x.chic);
+  const double q13 = 13.41 * c.keq;
+  const double q = k / q13;
+  const double u1 = exp(1.08 * (lk - log(q13)));
+  const double den_c = 1.0 + 69.9 * u1;
+  const double Cb = 386.0 / den_c;
+  const double qq = q * q;
+  const double A1 = EULER_E + 1.8 * c.betac * q, L1 = log(A1);
+  const double A2 = EULER_E + 1.8 * q, L2 = log(A2);
+  const double cA = 14.2 + Cb, cB = 14.2 / c.alphac + Cb;
+  const double Da = L1 + cA * qq, Db = L1 + cB * qq, Dn = L2 + cA * qq;
+  const double Ta = L1 / Da, Tb = L1 / Db, Tn = L2 / Dn;
+  const double ksh = k * c.sh;
+  const double x54 = ksh / 5.4, x2 = x54 * x54;
+  const double f = 1.0 / (1.0 + x2 * x2);
+  const double Tc = f * Ta + (1.0 - f) * Tb;
+  const double bn = c.betanode / ksh;
+  const double B3 = 1.0 + bn * bn * bn;
+  const double cb = cbrt(B3);
+  const double ts = c.sh / cb;
+  const double x52 = ksh / 5.2, E52 = 1.0 + x52 * x52;
+  const double bb = c.betab / ksh, Bb = 1.0 + bb * bb * bb;
+  const double ex1 = exp(1.4 * (lk - log(c.ksilk)));
+  const double silk = exp(-ex1);
+  const double arg = k * ts;
+  double sn, cs;
+  sincos(arg, &sn, &cs);
+  const double sinc = sn / arg;
+  const double Tbr0 = Tn / E52 + c.alphab / Bb * silk;
+  const double Tbar = Tbr0 * sinc;
+  const double T = c.fb * Tbar + c.fc * Tc;
+  const double eP = exp(c.ns * lk);
+  const double gg = x.g * x.g;
+  const double pklin = eP * (T * T) * gg * c.pknorm;
+  const double k3 = k * k * k;
+  const double d2l = k3 * pklin / TWO_PI2_G;
+  const double y = k / x.knl;
+  const double ly = lk - log(x.knl);
+  const double fy = y / 4.0 + (y * y) / 8.0;
+  const double efy = exp(-fy);
+  const double ld = log(1.0 + d2l);
+  const double pb = exp(x.beta * ld);
+  const double den_a = 1.0 + x.alpha * d2l;
+  const double Q = pb / den_a * efy;
+  const double d2q = d2l * Q;
+  const double H1 = exp(3.0 * x.f1 * ly);
+  const double H2 = exp(x.f2 * ly);
+  const double E3a = 3.0 - x.gam, E3b = x.lcf3 + ly;
+  const double H3 = exp(E3a * E3b);
+  const double D = 1.0 + x.bn * H2 + H3;
+  const double d2hp = x.an * H1 / D;
+  const double y2 = y * y, yn = y2 + x.nu;
+  const double Rr = y2 / yn;
+  const double d2h = d2hp * Rr;
+  const double S = d2q + d2h;
+  const double P = TWO_PI2_G / k3 * S;
+  // reverse, seed dP/dP = 1
+  const double Sb = TWO_PI2_G / k3;
+  double k3b = -P / k3;
+  const double d2qb = Sb, d2hb = Sb;
+  const double d2hpb = d2hb * Rr;
+  const double Rb = d2hb * d2hp;
+  ga[A_NU] += -Rb * y2 / (yn * yn);
+  double yb = 2.0 * y * (Rb * x.nu / (yn * yn));
+  ga[A_AN] += d2hpb * H1 / D;
+  const double H1b = d2hpb * x.an / D;
+  const double Dbar = -d2hpb * d2hp / D;
+  ga[A_BN] += Dbar * H2;
+  const double H2b = Dbar * x.bn;
+  const double E3 = Dbar * H3;  // adjoint of the exponent of H3
+  double lyb = H1b * H1 * 3.0 * x.f1 + H2b * H2 * x.f2 + E3 * E3a;
+  ga[A_F1] += H1b * H1 * 3.0 * ly;
+  ga[A_F2] += H2b * H2 * ly;
+  ga[A_GAM] += -E3 * E3b;
+  ga[A_LCF3] += E3 * E3a;
+  double d2lb = d2qb * Q;
+  const double Qb = d2qb * d2l;
+  const double pbb = Qb * efy / den_a;
+  const double denab = -Qb * Q / den_a;
+  const double efyb = Qb * pb / den_a;
+  ga[A_ALPHA] += denab * d2l;
+  d2lb += denab * x.alpha;
+  ga[A_BETA] += pbb * pb * ld;
+  d2lb += pbb * pb * x.beta / (1.0 + d2l);
+  yb += -efyb * efy * (0.25 + y / 4.0);
+  double lkb = lyb;
+  double knlb = -lyb / x.knl - yb * y / x.knl;
+  double kb = yb / x.knl;
+  k3b += d2lb * pklin / TWO_PI2_G;
+  const double pklinb = d2lb * k3 / TWO_PI2_G;
+  kb += k3b * 3.0 * k * k;
+  const double ePb = pklinb * (T * T) * gg * c.pknorm;
+  const double Tbarr = pklinb * eP * 2.0 * T * gg * c.pknorm;
+  ga[A_G] += pklinb * eP * (T * T) * 2.0 * x.g * c.pknorm;
+  gc[C_PKNORM] += pklinb * eP * (T * T) * gg;
+  gc[C_NS] += ePb * eP * lk;
+  lkb += ePb * eP * c.ns;
+  gc[C_FB] += Tbarr * Tbar;
+  gc[C_FC] += Tbarr * Tc;
+  const double Tbarb = Tbarr * c.fb;
+  const double Tcb = Tbarr * c.fc;
+  const double Tbr0b = Tbarb * sinc;
+  const double sincb = Tbarb * Tbr0;
+  const double argb = sincb * (cs - sinc) / arg;
+  kb += argb * ts;
+  const double tsb = argb * k;
+  const double Tnb = Tbr0b / E52;
+  const double E52b = -Tbr0b * Tn / (E52 * E52);
+  gc[C_ALPHAB] += Tbr0b * silk / Bb;
+  const double silkb = Tbr0b * c.alphab / Bb;
+  const double Bbb = -Tbr0b * c.alphab * silk / (Bb * Bb);
+  const double ex1b = -silkb * silk;
+  lkb += ex1b * ex1 * 1.4;
+  gc[C_KSILK] += -ex1b * ex1 * 1.4 / c.ksilk;
+  const double bbb = Bbb * 3.0 * bb * bb;
+  gc[C_BETAB] += bbb / ksh;
+  double kshb = -bbb * bb / ksh + E52b * 2.0 * x52 / 5.2;
+  gc[C_SH] += tsb / cb;
+  const double cbb = -tsb * ts / cb;
+  const double bnb = cbb * cb / (3.0 * B3) * 3.0 * bn * bn;
+  gc[C_BETANODE] += bnb / ksh;
+  kshb += -bnb * bn / ksh;
+  const double fbar = Tcb * (Ta - Tb);
+  const double Tab = Tcb * f, Tbb = Tcb * (1.0 - f);
+  kshb += (-fbar * f * f * 2.0 * x2) * 2.0 * x54 / 5.4;
+  kb += kshb * c.sh;
+  gc[C_SH] += kshb * k;
+  const double Dab = -Tab * Ta / Da, Dbb = -Tbb * Tb / Db, Dnb = -Tnb * Tn / Dn;
+  const double L1b = Tab / Da + Tbb / Db + Dab + Dbb;
+  const double L2b = Tnb / Dn + Dnb;
+  const double Cbb = (Dab + Dbb + Dnb) * qq;
+  gc[C_ALPHAC] += Dbb * qq * (-14.2 / (c.alphac * c.alphac));
+  double qb = (Dab * cA + Dbb * cB + Dnb * cA) * 2.0 * q;
+  const double A1b = L1b / A1;
+  gc[C_BETAC] += A1b * 1.8 * q;
+  qb += A1b * 1.8 * c.betac + L2b / A2 * 1.8;
+  const double u1b = -Cbb * Cb * 69.9 / den_c;
+  lkb += u1b * u1 * 1.08;
+  gc[C_KEQ] += -u1b * u1 * 1.08 / c.keq - qb * q / c.keq;
+  kb += qb / q13;
+  ga[A_CHIC] += -lkb / x.chic - kb * k / x.chic;
+  ga[A_KNL] += knlb;
+  return P;
+}
+
+constexpr int GL_TA = 16;     // a nodes per chunk
+constexpr int GL_THREADS = 256;
+constexpr int GL_MAXO = 17;   // accumulators per thread
+
+// One CTA per (l tile, a split, cosmology): C_ell and dC_ell/dtheta partial sums.
+__global__ void __launch_bounds__(GL_THREADS)
+    grad_limber_kernel(GradBatch gb, const ConstTables* __restrict__ c, int LT) {
+  const int item = blockIdx.z, split = blockIdx.y;
+  if (item >= gb.n_items) return;
+  const GeoHeader* geo = gb.geo;
+  const int n_ell = geo->n_ell, n_cls = geo->n_cls, na = geo->na;
+  const int l0 = blockIdx.x * LT;
+  if (l0 >= n_ell) return;
+  const int lt = min(LT, n_ell - l0);
+  const int per = (na + gb.n_split - 1) / gb.n_split;
+  const int a_begin = split * per, a_end = min(na, a_begin + per);
+  extern __shared__ double sm[];
+  double* cvs = sm;                                   // [NC_IN] values
+  double* cds = cvs + NC_IN;                          // [NC_IN][NDIR]
+  double* khs = cds + NC_IN * NDIR;                   // [LT]
+  double* lkhs = khs + 32;                            // [LT]
+  double* rv = lkhs + 32;                             // [GL_TA][NA_IN]
+  double* rd = rv + GL_TA * NA_IN;                    // [GL_TA][NA_IN][NDIR]
+  double* Mv = rd + GL_TA * NA_IN * NDIR;             // [GL_TA][n_cls]
+  double* Md = Mv + GL_TA * n_cls;                    // [GL_TA][n_cls][NDIR]
+  double* Pv = Md + GL_TA * n_cls * NDIR;             // [GL_TA][LT]
+  double* Pd = Pv + GL_TA * LT;                       // [GL_TA][LT][NDIR]
+  const int tid = threadIdx.x;
+  const TabD* tb = gb.tab + item;
+  for (int i = tid; i < NC_IN; i += GL_THREADS) {
+    const int si = kNodeCScalar[i];
+    cvs[i] = tb->sv[si];
+    for (int d = 0; d < NDIR; ++d) cds[i * NDIR + d] = tb->sd[d][si];
+  }
+  const double* ELL = geo_ptr<double>(geo, geo->off_ell);
+  const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
+  for (int l = tid; l < lt; l += GL_THREADS) {
+    khs[l] = ELL[l0 + l] + 0.5;
+    lkhs[l] = log(khs[l]);
+  }
+  __syncthreads();
+  NodeK ck;
+  ck.keq = cvs[C_KEQ]; ck.sh = cvs[C_SH]; ck.betac = cvs[C_BETAC]; ck.alphac = cvs[C_ALPHAC];
+  ck.alphab = cvs[C_ALPHAB]; ck.betab = cvs[C_BETAB]; ck.betanode = cvs[C_BETANODE];
+  ck.ksilk = cvs[C_KSILK]; ck.fb = cvs[C_FB]; ck.fc = cvs[C_FC]; ck.ns = cvs[C_NS];
+  ck.pknorm = cvs[C_PKNORM];
+  const double* rowd = gb.rowd + (size_t)item * na * NROWD;
+  const double* kd = gb.kernd + (size_t)item * geo->n_tr * na * (NDIR + 1);
+  const int nout = lt * n_cls * (NDIR + 1);
+  double acc[GL_MAXO];
+#pragma unroll
+  for (int r = 0; r < GL_MAXO; ++r) acc[r] = 0.0;
+  for (int base = a_begin; base < a_end; base += GL_TA) {
+    const int tc = min(GL_TA, a_end - base);
+    for (int e = tid; e < tc * NA_IN; e += GL_THREADS) {
+      const int t = e / NA_IN, x = e % NA_IN;
+      const double* r = rowd + (size_t)(base + t) * NROWD;
+      rv[e] = r[x];
+      for (int d = 0; d < NDIR; ++d) rd[e * NDIR + d] = r[NA_IN * (1 + d) + x];
+    }
+    __syncthreads();
+    // M_ij(a) = u K_i K_j with tangents
+    for (int e = tid; e < tc * n_cls; e += GL_THREADS) {
+      const int t = e / n_cls, p = e % n_cls, n = base + t;
+      const double* Ki = kd + ((size_t)geo->pair_i[p] * na + n) * (NDIR + 1);
+      const double* Kj = kd + ((size_t)geo->pair_j[p] * na + n) * (NDIR + 1);
+      const double u = rv[t * NA_IN + A_U];
+      Mv[e] = u * Ki[0] * Kj[0];
+      for (int d = 0; d < NDIR; ++d)
+        Md[e * NDIR + d] = rd[(t * NA_IN + A_U) * NDIR + d] * Ki[0] * Kj[0] +
+                           u * (Ki[1 + d] * Kj[0] + Ki[0] * Kj[1 + d]);
+    }
+    // integrand with its tangents
+    for (int e = tid; e < tc * lt; e += GL_THREADS) {
+      const int t = e / lt, l = e % lt;
+      const double* xv = rv + t * NA_IN;
+      NodeX nx;
+      nx.chic = xv[A_CHIC]; nx.g = xv[A_G]; nx.knl = xv[A_KNL]; nx.beta = xv[A_BETA];
+      nx.alpha = xv[A_ALPHA]; nx.an = xv[A_AN]; nx.bn = xv[A_BN]; nx.lcf3 = xv[A_LCF3];
+      nx.f1 = xv[A_F1]; nx.f2 = xv[A_F2]; nx.gam = xv[A_GAM]; nx.nu = xv[A_NU];
+      double ga[NA_IN], gcv[NC_IN];
+      for (int i = 0; i < NA_IN; ++i) ga[i] = 0.0;
+      for (int i = 0; i < NC_IN; ++i) gcv[i] = 0.0;
+      const double P = node_fb(khs[l], lkhs[l], nx, ck, ga, gcv);
+      Pv[t * LT + l] = P;
+      for (int d = 0; d < NDIR; ++d) {
+        double s = 0.0;
+        for (int i = 0; i < A_U; ++i) s += ga[i] * rd[(t * NA_IN + i) * NDIR + d];
+        for (int i = 0; i < NC_IN; ++i) s += gcv[i] * cds[i * NDIR + d];
+        Pd[(t * LT + l) * NDIR + d] = s;
+      }
+    }
+    __syncthreads();
+    // contraction: outputs (l, p, s), s = 0 value, 1..8 tangents
+#pragma unroll
+    for (int r = 0; r < GL_MAXO; ++r) {
+      const int o = tid + r * GL_THREADS;
+      if (o < nout) {
+        const int s = o % (NDIR + 1);
+        const int lp = o / (NDIR + 1);
+        const int l = lp % lt, p = lp / lt;
+        double part = 0.0;
+        if (s == 0) {
+          for (int t = 0; t < tc; ++t) part += Pv[t * LT + l] * Mv[t * n_cls + p];
+        } else {
+          const int d = s - 1;
+          for (int t = 0; t < tc; ++t)
+            part += Pd[(t * LT + l) * NDIR + d] * Mv[t * n_cls + p] +
+                    Pv[t * LT + l] * Md[(t * n_cls + p) * NDIR + d];
+        }
+        acc[r] += part;
+      }
+    }
+    __syncthreads();
+  }
+  double* part = gb.part + (size_t)split * gb.n_items * n_cls * n_ell * (NDIR + 1);
+#pragma unroll
+  for (int r = 0; r < GL_MAXO; ++r) {
+    const int o = tid + r * GL_THREADS;
+    if (o < nout) {
+      const int s = o % (NDIR + 1);
+      const int lp = o / (NDIR + 1);
+      const int l = lp % lt, p = lp / lt;
+      const int ell = l0 + l;
+      const double ef = EF[(size_t)geo->pair_i[p] * n_ell + ell] * EF[(size_t)geo->pair_j[p] * n_ell + ell];
+      part[(((size_t)item * n_cls + p) * n_ell + ell) * (NDIR + 1) + s] = acc[r] * ef;
+    }
+  }
+}
+
+// Fixed-order sum over the a splits; C_ell and the Jacobian out.
+__global__ void grad_reduce_kernel(GradBatch gb) {
+  const size_t per = (size_t)gb.n_cls * gb.n_ell;
+  const size_t total = per * gb.n_items;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (size_t)gridDim.x * blockDim.x) {
+    double v[NDIR + 1];
+    for (int s = 0; s <= NDIR; ++s) v[s] = 0.0;
+    for (int sp = 0; sp < gb.n_split; ++sp) {
+      const double* p = gb.part + ((size_t)sp * total + idx) * (NDIR + 1);
+      for (int s = 0; s <= NDIR; ++s) v[s] += p[s];
+    }
+    if (gb.cl) gb.cl[idx] = v[0];
+    for (int d = 0; d < NDIR; ++d) gb.jac[idx * NDIR + d] = v[1 + d];
+  }
+}
+
+size_t grad_limber_smem(int n_cls, int LT) {
+  return sizeof(double) * (NC_IN * (1 + NDIR) + 64 + GL_TA * NA_IN * (1 + NDIR) +
+                           (size_t)GL_TA * n_cls * (1 + NDIR) + (size_t)GL_TA * LT * (1 + NDIR));
+}
+
+int grad_limber_tile(int n_ell, int n_cls) {
+  int lt = (GL_THREADS * GL_MAXO) / (n_cls * (NDIR + 1));
+  if (lt > 32) lt = 32;
+  if (lt < 1) lt = 1;
+  const int tiles = (n_ell + lt - 1) / lt;
+  return (n_ell + tiles - 1) / tiles;
+}
+
+void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
+  const size_t smt = grad_tables_smem();
+  cudaFuncSetAttribute(grad_tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+  grad_tables_kernel<<<gb.n_items, 256, smt, st>>>(gb, c);
+  dim3 gr((gb.na + 7) / 8, gb.n_items);
+  grad_rows_kernel<<<gr, 256, 0, st>>>(gb, c);
+  grad_kern_kernel<<<gr, 256, 0, st>>>(gb, c);
+  const int lt = grad_limber_tile(gb.n_ell, gb.n_cls);
+  const size_t sml = grad_limber_smem(gb.n_cls, lt);
+  cudaFuncSetAttribute(grad_limber_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sml);
+  dim3 gl((gb.n_ell + lt - 1) / lt, gb.n_split, gb.n_items);
+  grad_limber_kernel<<<gl, GL_THREADS, sml, st>>>(gb, c, lt);
+  const size_t total = (size_t)gb.n_cls * gb.n_ell * gb.n_items;
+  size_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  grad_reduce_kernel<<<(unsigned)(blocks ? blocks : 1), 256, 0, st>>>(gb);
+}
+
+size_t grad_tab_bytes() { return sizeof(TabD); }
+
+}  // namespace jcg
+
+namespace jcg {
+
+// a-splits of the Limber Jacobian: enough CTAs to fill the GPU for small batches
+int grad_n_split(const GeoHeader& h, int n_cosmo) {
+  const int lt = grad_limber_tile(h.n_ell, h.n_cls);
+  const int tiles = (h.n_ell + lt - 1) / lt;
+  const int ctas = tiles * n_cosmo;
+  int ns = (2 * 152 + ctas - 1) / ctas;
+  const int max_ns = (h.na + GL_TA - 1) / GL_TA;
+  if (ns > max_ns) ns = max_ns;
+  if (ns < 1) ns = 1;
+  return ns;
+}
+
+static size_t al256(size_t v) { return (v + 255) & ~size_t(255); }
+
+size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo) {
+  const int ns = grad_n_split(h, n_cosmo);
+  size_t o = al256(sizeof(TabD) * (size_t)n_cosmo);
+  o += al256(sizeof(double) * (size_t)n_cosmo * h.na * NROWD);
+  o += al256(sizeof(double) * (size_t)n_cosmo * h.n_tr * h.na * (NDIR + 1));
+  o += al256(sizeof(double) * (size_t)ns * n_cosmo * h.n_cls * h.n_ell * (NDIR + 1));
+  return o;
+}
+
+void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, double* cl,
+              double* jac, void* ws, const ConstTables* c, cudaStream_t st) {
+  GradBatch gb;
+  gb.n_items = n_cosmo;
+  gb.params = params;
+  gb.geo = geo;
+  char* base = static_cast<char*>(ws);
+  size_t o = 0;
+  gb.tab = reinterpret_cast<TabD*>(base + o);
+  o += al256(sizeof(TabD) * (size_t)n_cosmo);
+  gb.rowd = reinterpret_cast<double*>(base + o);
+  o += al256(sizeof(double) * (size_t)n_cosmo * h.na * NROWD);
+  gb.kernd = reinterpret_cast<double*>(base + o);
+  o += al256(sizeof(double) * (size_t)n_cosmo * h.n_tr * h.na * (NDIR + 1));
+  gb.part = reinterpret_cast<double*>(base + o);
+  gb.cl = cl;
+  gb.jac = jac;
+  gb.na = h.na;
+  gb.n_tr = h.n_tr;
+  gb.n_cls = h.n_cls;
+  gb.n_ell = h.n_ell;
+  gb.n_split = grad_n_split(h, n_cosmo);
+  launch_grad(gb, c, st);
+}
+
+}  // namespace jcg

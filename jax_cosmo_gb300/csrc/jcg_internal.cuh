@@ -461,6 +461,10 @@ void launch_cosmo_tables(const Batch& b, const ConstTables* c, cudaStream_t st);
 void launch_halofit_rows(const Batch& b, const ConstTables* c, cudaStream_t st);
 void launch_tracer_kernels(const Batch& b, const ConstTables* c, cudaStream_t st);
 void launch_limber(const Batch& b, const ConstTables* c, int lt, cudaStream_t st);
+// derivatives (jcg_grad.cu)
+size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo);
+void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, double* cl,
+              double* jac, void* ws, const ConstTables* c, cudaStream_t st);
 // pointwise queries of the table functions (API: background / power modules)
 void launch_eval_points(const double* params, int n_cosmo, CosmoTab* ctab, const ConstTables* c,
                         const double* a, const double* k, int n, int what, double* out,

@@ -151,7 +151,8 @@ __device__ void chol_quad_logdet(const double* L, const double* r, double* z, in
 __global__ void loglike_blocks_kernel(const double* __restrict__ data, const double* __restrict__ mu,
                                       const double* __restrict__ cov, int n_cls, int n_ell,
                                       int dense, const int* __restrict__ structure,
-                                      double* __restrict__ partial, int* __restrict__ status) {
+                                      double* __restrict__ partial, int* __restrict__ status,
+                                      double* __restrict__ alpha) {
   const int l = blockIdx.x, ci = blockIdx.y;
   extern __shared__ double sm[];
   double* A = sm;
@@ -189,6 +190,15 @@ __global__ void loglike_blocks_kernel(const double* __restrict__ data, const dou
     else atomicMax(status + ci, 2);
     partial[((size_t)ci * n_ell + l) * 2 + 0] = q;
     partial[((size_t)ci * n_ell + l) * 2 + 1] = ld;
+    if (alpha) {
+      // C^-1 r = L^-T z (back substitution), the gradient of r^T C^-1 r / 2
+      for (int i = n_cls - 1; i >= 0; --i) {
+        double v = ok ? z[i] : NAN;
+        for (int j = i + 1; j < n_cls; ++j) v -= A[j * n_cls + i] * z[j];
+        z[i] = ok ? v / A[i * n_cls + i] : NAN;
+        alpha[(size_t)ci * N + (size_t)i * n_ell + l] = z[i];
+      }
+    }
   }
 }
 
@@ -233,7 +243,7 @@ __global__ void zero_int_kernel(int* p, int n) {
 
 void launch_loglike(const double* data, const double* mu, const double* cov, int n_cosmo, int n_cls,
                     int n_ell, int include_logdet, int dense, double* out, int* status,
-                    double* partial, int* structure, cudaStream_t st) {
+                    double* partial, int* structure, double* alpha, cudaStream_t st) {
   zero_int_kernel<<<(n_cosmo + 255) / 256, 256, 0, st>>>(status, n_cosmo);
   if (dense) {
     zero_int_kernel<<<(n_cosmo + 255) / 256, 256, 0, st>>>(structure, n_cosmo);
@@ -248,7 +258,8 @@ void launch_loglike(const double* data, const double* mu, const double* cov, int
   dim3 grid(n_ell, n_cosmo);
   const int threads = n_cls >= 64 ? 256 : 128;
   loglike_blocks_kernel<<<grid, threads, smem, st>>>(data, mu, cov, n_cls, n_ell, dense,
-                                                      dense ? structure : nullptr, partial, status);
+                                                      dense ? structure : nullptr, partial, status,
+                                                      alpha);
   loglike_reduce_kernel<<<(n_cosmo + 127) / 128, 128, 0, st>>>(partial, n_cosmo, n_ell,
                                                                include_logdet, out);
   if (dense) {

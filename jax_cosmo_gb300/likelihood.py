@@ -42,7 +42,8 @@ def _dense_n_ell(C):
     return N
 
 
-def _loglike_blocks(r_data, mu, C, n_cls, n_ell, include_logdet, dense):
+def _loglike_blocks(r_data, mu, C, n_cls, n_ell, include_logdet, dense, alpha=None):
+    """libjcg per-ell block Cholesky; also writes alpha = C^-1 (mu - data) if given."""
     device = mu.device
     B = mu.shape[0]
     wsz = ctypes.c_size_t()
@@ -52,48 +53,76 @@ def _loglike_blocks(r_data, mu, C, n_cls, n_ell, include_logdet, dense):
     status = torch.zeros(B, dtype=torch.int32, device=device)
     name = "jcg_gaussian_loglike_dense" if dense else "jcg_gaussian_loglike_sparse"
     _lib.call(name, _lib.ptr(r_data), _lib.ptr(mu), _lib.ptr(C), B, n_cls, n_ell,
-              1 if include_logdet else 0, _lib.ptr(out), _lib.ptr(status), _lib.ptr(ws),
+              1 if include_logdet else 0, _lib.ptr(out), _lib.ptr(status), _lib.ptr(alpha), _lib.ptr(ws),
               ctypes.c_size_t(ws.numel()), _lib.stream_of(device))
     return out, status
 
 
-def gaussian_log_likelihood(data, mu, C, include_logdet=True, inverse_method="inverse"):
-    """Log-likelihood of ``data`` under N(mu, C); batched if mu is 2-D."""
-    if inverse_method not in ("inverse", "cholesky"):
-        raise NotImplementedError
-    device = _lib.require_cuda()
+def _loglike_core(data2, mu2, Cb, sparse, n_cls, n_ell, include_logdet, alpha=None):
+    """[B] log-likelihoods of prepared batched operands (and C^-1 r into ``alpha``).
+
+    Returns (out, status); status 1 marks a dense matrix that is not block
+    diagonal in ell, factored as a whole.
+    """
+    B, N = mu2.shape
+    device = mu2.device
+    if sparse:
+        return _loglike_blocks(data2, mu2, Cb, n_cls, n_ell, include_logdet, dense=False, alpha=alpha)
+    if n_cls <= 160:
+        out, status = _loglike_blocks(data2, mu2, Cb, n_cls, n_ell, include_logdet, dense=True, alpha=alpha)
+    else:
+        out = torch.full((B,), float("nan"), dtype=torch.float64, device=device)
+        status = torch.ones(B, dtype=torch.int32, device=device)
+    unstructured = (status == 1).nonzero().flatten().tolist()
+    for i in unstructured:
+        # not block diagonal in ell: whole-matrix Cholesky
+        L = torch.linalg.cholesky(Cb[i])
+        r = mu2[i] - data2[i]
+        y = torch.cholesky_solve(r[:, None], L)[:, 0]
+        q = torch.dot(r, y)
+        ld = 2.0 * torch.log(torch.diagonal(L)).sum()
+        out[i] = -0.5 * (q - ld) if include_logdet else -0.5 * q
+        if alpha is not None:
+            alpha[i] = y
+    return out, status
+
+
+def _prepare(data, mu, C, device):
     mu_t = _t(mu, device)
     data_t = _t(data, device)
     C_t = _t(C, device)
     batched = mu_t.dim() == 2
-    mu2 = (mu_t if batched else mu_t[None]).contiguous()
-    data2 = data_t.expand_as(mu2).contiguous() if data_t.dim() == 1 else data_t.contiguous()
+    mu2 = mu_t if batched else mu_t[None]
+    data2 = data_t.expand_as(mu2) if data_t.dim() == 1 else data_t
     B, N = mu2.shape
     sparse = C_t.dim() == (4 if batched else 3)
+    Cb = C_t if batched else C_t[None]
     if sparse:
-        Cb = (C_t if batched else C_t[None]).contiguous()
         n_cls, n_ell = Cb.shape[1], Cb.shape[3]
         if Cb.shape[2] != n_cls or n_cls * n_ell != N:
             raise ValueError(f"sparse covariance {tuple(C_t.shape)} does not match data length {N}")
-        out, status = _loglike_blocks(data2, mu2, Cb, n_cls, n_ell, include_logdet, dense=False)
     else:
-        Cb = (C_t if batched else C_t[None]).contiguous()
         if Cb.shape[1:] != (N, N):
             raise ValueError(f"covariance {tuple(C_t.shape)} does not match data length {N}")
-        n_ell = _dense_n_ell(C_t)
+        n_ell = _dense_n_ell(C_t.detach())
         n_cls = N // n_ell
-        if n_cls <= 160:
-            out, status = _loglike_blocks(data2, mu2, Cb, n_cls, n_ell, include_logdet, dense=True)
-        else:
-            out = torch.full((B,), float("nan"), dtype=torch.float64, device=device)
-            status = torch.ones(B, dtype=torch.int32, device=device)
-        unstructured = (status == 1).nonzero().flatten().tolist()
-        for i in unstructured:
-            # not block diagonal in ell: whole-matrix Cholesky
-            L = torch.linalg.cholesky(Cb[i])
-            r = mu2[i] - data2[i]
-            y = torch.cholesky_solve(r[:, None], L)[:, 0]
-            q = torch.dot(r, y)
-            ld = 2.0 * torch.log(torch.diagonal(L)).sum()
-            out[i] = -0.5 * (q - ld) if include_logdet else -0.5 * q
+    return batched, data2, mu2, Cb, sparse, n_cls, n_ell
+
+
+def gaussian_log_likelihood(data, mu, C, include_logdet=True, inverse_method="inverse"):
+    """Log-likelihood of ``data`` under N(mu, C); batched if mu is 2-D.
+
+    Differentiable (torch.autograd) in data, mu and C.
+    """
+    if inverse_method not in ("inverse", "cholesky"):
+        raise NotImplementedError
+    device = _lib.require_cuda()
+    batched, data2, mu2, Cb, sparse, n_cls, n_ell = _prepare(data, mu, C, device)
+    if any(isinstance(x, torch.Tensor) and x.requires_grad for x in (data, mu, C)):
+        from jax_cosmo_gb300 import autodiff
+
+        out = autodiff.loglike_autograd(data2, mu2, Cb, include_logdet, sparse, n_cls, n_ell)
+    else:
+        out, _ = _loglike_core(data2.contiguous(), mu2.contiguous(), Cb.contiguous(), sparse,
+                               n_cls, n_ell, include_logdet)
     return out if batched else out[0]
