@@ -168,6 +168,46 @@ int jcg_angular_cl_jacobian(const jcg_geometry* g, const void* geo_dev, const do
                             int n_cosmo, double* cl_dev, double* jac_dev, void* workspace,
                             size_t workspace_bytes, cudaStream_t stream);
 
+/* ------------------------------------------------ ragged requests ------ */
+/* A list of requests, each with its own geometry (tracers, n(z), ell grid)
+ * and cosmology, computed in one launch sequence: the continuous-batching form
+ * of a serving loop.  Replaces a Python loop of angular_cl calls
+ * (angular_cl.py:49-98) over sampler chains with different probes and ell,
+ * each followed by jax.grad of the chain's likelihood (likelihood.py:9-61 with
+ * the covariance held fixed, docs/notebooks/jax-cosmo-intro.ipynb).
+ * Every request's result depends only on its own inputs: the same alone and
+ * in any mix.  mode:
+ *   JCG_REQ_CL_FP64 / JCG_REQ_CL_FP32C: cl -> C_ell [n_cls][n_ell];
+ *   JCG_REQ_JACOBIAN: jac -> dC_ell/dtheta [n_cls][n_ell][8], cl (may be NULL);
+ *   JCG_REQ_LOGLIKE_GRAD: out -> [9] = logL = -r^T P r / 2 with r = C_ell - data
+ *     and its gradient -(dC/dtheta)^T P r over the 8 Cosmology leaves; data
+ *     [n_cls*n_ell] in (cls, ell) order, prec [n_ell][n_cls][n_cls] the inverse
+ *     covariance blocks; cl / jac optional outputs (NULL: workspace). */
+#define JCG_REQ_CL_FP64 0
+#define JCG_REQ_CL_FP32C 1
+#define JCG_REQ_JACOBIAN 2
+#define JCG_REQ_LOGLIKE_GRAD 3
+#define JCG_MAX_REQUESTS 65536
+
+typedef struct {
+  const jcg_geometry* g;   /* host description of the request's geometry */
+  const void* geo_dev;     /* its device buffer (jcg_geometry_build) */
+  const double* params_dev;/* 8 parameters */
+  double* cl_dev;
+  double* jac_dev;
+  const double* data_dev;
+  const double* prec_dev;
+  double* out_dev;
+} jcg_request;
+
+/* Workspace for n requests: *bytes_min with no a-splits of the Jacobian,
+ * *bytes_full with the splits that fill the GPU for small batches;
+ * jcg_requests_run uses as many splits as ws_bytes allows. */
+int jcg_requests_workspace_size(const jcg_request* reqs, int n, int mode, size_t* bytes_min,
+                                size_t* bytes_full);
+int jcg_requests_run(const jcg_request* reqs, int n, int mode, void* workspace,
+                     size_t workspace_bytes, cudaStream_t stream);
+
 /* Copy stage outputs for cosmology `index` out of a workspace (device to device).
  * what: 0 chi table [256], 1 growth table [128], 2 scalars [32],
  *       3 halofit rows [na][24] (FP64), 4 radial kernels [n_tracers][na]. */

@@ -9,6 +9,7 @@
 #include <string.h>
 
 #include <mutex>
+#include <vector>
 
 #include "jcg_internal.cuh"
 
@@ -647,4 +648,164 @@ extern "C" int jcg_angular_cl_jacobian(const jcg_geometry* g, const void* geo, c
   if ((rc = const_tables(&c))) return rc;
   grad_run(static_cast<const GeoHeader*>(geo), h, params, n_cosmo, cl, jac, ws, c, stream);
   return cuda_check("angular_cl_jacobian");
+}
+
+// ------------------------------------------------------ ragged requests -----
+namespace {
+
+struct ReqPlan {
+  std::vector<GeoHeader> hdr;
+  std::vector<GradReq> greq;
+};
+
+size_t cl_item_bytes(const GeoHeader& h, int precision) {
+  size_t o = align256(sizeof(CosmoTab));
+  o += align256(sizeof(double) * NROW64 * (size_t)h.na);
+  if (precision == JCG_FP32C) o += align256(sizeof(float) * NROW32 * (size_t)h.na);
+  o += align256(sizeof(double) * (size_t)h.n_tr * h.na);
+  return o;
+}
+
+// host validation of every request; headers into plan
+int plan_requests(const jcg_request* reqs, int n, int mode, ReqPlan* plan) {
+  if (!reqs) return fail(JCG_ERR_ARG, "requests is NULL");
+  if (n < 1 || n > JCG_MAX_REQUESTS) return fail(JCG_ERR_SHAPE, "n = %d (1..%d)", n, JCG_MAX_REQUESTS);
+  if (mode < JCG_REQ_CL_FP64 || mode > JCG_REQ_LOGLIKE_GRAD) return fail(JCG_ERR_ARG, "mode = %d", mode);
+  plan->hdr.resize(n);
+  plan->greq.resize(n);
+  for (int i = 0; i < n; ++i) {
+    const jcg_request& r = reqs[i];
+    int rc = make_header(r.g, &plan->hdr[i]);
+    if (rc) {
+      char why[sizeof(g_err)];
+      memcpy(why, g_err, sizeof(why));
+      return fail(rc, "request %d: %s", i, why);
+    }
+    if (plan->hdr[i].custom_nodes) return fail(JCG_ERR_ARG, "request %d: geometry without a Limber grid", i);
+    if (!r.geo_dev || !r.params_dev) return fail(JCG_ERR_ARG, "request %d: NULL geometry or params", i);
+    if (mode <= JCG_REQ_CL_FP32C && !r.cl_dev) return fail(JCG_ERR_ARG, "request %d: cl is NULL", i);
+    if (mode == JCG_REQ_JACOBIAN && !r.jac_dev) return fail(JCG_ERR_ARG, "request %d: jac is NULL", i);
+    if (mode == JCG_REQ_LOGLIKE_GRAD && (!r.data_dev || !r.prec_dev || !r.out_dev))
+      return fail(JCG_ERR_ARG, "request %d: data, prec or out is NULL", i);
+    GradReq& q = plan->greq[i];
+    q.h = &plan->hdr[i];
+    q.geo = static_cast<const GeoHeader*>(r.geo_dev);
+    q.params = r.params_dev;
+    q.cl = r.cl_dev;
+    q.jac = r.jac_dev;
+  }
+  return JCG_OK;
+}
+
+size_t cl_listed_bytes(const ReqPlan& p, int precision) {
+  size_t o = align256(sizeof(Item) * p.hdr.size());
+  for (const GeoHeader& h : p.hdr) o += cl_item_bytes(h, precision);
+  return o;
+}
+
+size_t ll_extra_bytes(int n) { return align256(sizeof(ReqLL) * (size_t)n); }
+
+}  // namespace
+
+extern "C" int jcg_requests_workspace_size(const jcg_request* reqs, int n, int mode, size_t* bytes_min,
+                                           size_t* bytes_full) {
+  if (!bytes_min || !bytes_full) return fail(JCG_ERR_ARG, "bytes is NULL");
+  static thread_local ReqPlan plan;
+  int rc = plan_requests(reqs, n, mode, &plan);
+  if (rc) return rc;
+  if (mode <= JCG_REQ_CL_FP32C) {
+    *bytes_min = *bytes_full = cl_listed_bytes(plan, mode);
+    return JCG_OK;
+  }
+  const size_t extra = mode == JCG_REQ_LOGLIKE_GRAD ? ll_extra_bytes(n) : 0;
+  const int ns = grad_listed_auto_split(plan.greq.data(), n);
+  *bytes_min = extra + grad_listed_bytes(plan.greq.data(), n, 1);
+  *bytes_full = extra + grad_listed_bytes(plan.greq.data(), n, ns);
+  return JCG_OK;
+}
+
+extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, void* ws, size_t ws_bytes,
+                                cudaStream_t stream) {
+  static thread_local ReqPlan plan;
+  int rc = plan_requests(reqs, n, mode, &plan);
+  if (rc) return rc;
+  if (!ws) return fail(JCG_ERR_ARG, "workspace is NULL");
+  if (((uintptr_t)ws) % 256 != 0) return fail(JCG_ERR_ARG, "workspace must be 256-byte aligned");
+  ConstTables* c = nullptr;
+  if ((rc = const_tables(&c))) return rc;
+  char* base = static_cast<char*>(ws);
+  if (mode <= JCG_REQ_CL_FP32C) {
+    const int precision = mode;
+    const size_t need = cl_listed_bytes(plan, precision);
+    if (ws_bytes < need) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need);
+    static thread_local std::vector<Item> items;
+    items.resize(n);
+    Item* dev_items = reinterpret_cast<Item*>(base);
+    size_t o = align256(sizeof(Item) * (size_t)n);
+    Batch b;
+    memset(&b, 0, sizeof(b));
+    for (int i = 0; i < n; ++i) {
+      const GeoHeader& h = plan.hdr[i];
+      Item& it = items[i];
+      it.params = reqs[i].params_dev;
+      it.geo = static_cast<const GeoHeader*>(reqs[i].geo_dev);
+      it.ctab = reinterpret_cast<CosmoTab*>(base + o);
+      o += align256(sizeof(CosmoTab));
+      it.rows64 = reinterpret_cast<double*>(base + o);
+      o += align256(sizeof(double) * NROW64 * (size_t)h.na);
+      it.rows32 = nullptr;
+      if (precision == JCG_FP32C) {
+        it.rows32 = reinterpret_cast<float*>(base + o);
+        o += align256(sizeof(float) * NROW32 * (size_t)h.na);
+      }
+      it.kern = reinterpret_cast<double*>(base + o);
+      o += align256(sizeof(double) * (size_t)h.n_tr * h.na);
+      it.cl = reqs[i].cl_dev;
+      it.precision = precision;
+      it.pad = 0;
+      b.max_na = max(b.max_na, h.na);
+      b.max_ell = max(b.max_ell, h.n_ell);
+      b.max_cls = max(b.max_cls, h.n_cls);
+      b.max_tr = max(b.max_tr, h.n_tr);
+    }
+    // pageable source: staged before the call returns
+    if (cudaMemcpyAsync(dev_items, items.data(), sizeof(Item) * (size_t)n, cudaMemcpyHostToDevice,
+                        stream) != cudaSuccess)
+      return cuda_check("request table copy");
+    b.n_items = n;
+    b.listed = 1;
+    b.items = dev_items;
+    b.precision = precision;
+    launch_cosmo_tables(b, c, stream);
+    launch_halofit_rows(b, c, stream);
+    launch_tracer_kernels(b, c, stream);
+    launch_limber(b, c, limber_tile(b.max_ell), stream);
+    return cuda_check("requests angular_cl");
+  }
+  const size_t extra = mode == JCG_REQ_LOGLIKE_GRAD ? ll_extra_bytes(n) : 0;
+  const size_t need1 = extra + grad_listed_bytes(plan.greq.data(), n, 1);
+  if (ws_bytes < need1) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need1);
+  int ns = grad_listed_auto_split(plan.greq.data(), n);
+  while (ns > 1 && extra + grad_listed_bytes(plan.greq.data(), n, ns) > ws_bytes) --ns;
+  if (cudaError_t e = grad_run_listed(plan.greq.data(), n, ns, base + extra, c, stream))
+    return fail(JCG_ERR_CUDA, "requests jacobian: %s", cudaGetErrorString(e));
+  if (mode == JCG_REQ_LOGLIKE_GRAD) {
+    static thread_local std::vector<ReqLL> ll;
+    ll.resize(n);
+    for (int i = 0; i < n; ++i) {
+      ll[i].cl = plan.greq[i].cl;
+      ll[i].jac = plan.greq[i].jac;
+      ll[i].data = reqs[i].data_dev;
+      ll[i].prec = reqs[i].prec_dev;
+      ll[i].out = reqs[i].out_dev;
+      ll[i].n_cls = plan.hdr[i].n_cls;
+      ll[i].n_ell = plan.hdr[i].n_ell;
+    }
+    ReqLL* dev_ll = reinterpret_cast<ReqLL*>(base);
+    if (cudaMemcpyAsync(dev_ll, ll.data(), sizeof(ReqLL) * (size_t)n, cudaMemcpyHostToDevice, stream) !=
+        cudaSuccess)
+      return cuda_check("request loglike table copy");
+    launch_request_loglike(dev_ll, n, stream);
+  }
+  return cuda_check("requests jacobian");
 }

@@ -13,6 +13,10 @@
 // forward pass.  Derivative conventions are JAX's for the reference's
 // operations (max/min pass the tangent of the selected branch; the
 // interpolation segment is locally constant).
+#include <string.h>
+
+#include <vector>
+
 #include "jcg_dual.cuh"
 
 namespace jcg {
@@ -46,18 +50,49 @@ __device__ __constant__ const int kNodeCScalar[NC_IN] = {S_K_EQ,  S_SH_D,      S
                                                          S_ALPHA_B, S_BETA_B, S_BETA_NODE, S_K_SILK,
                                                          S_FB,    S_FC,        S_NS,      S_PKNORM};
 
+// One (cosmology, geometry) pair of a Jacobian batch.
+struct GradItem {
+  const double* params;   // 8 parameters
+  const GeoHeader* geo;
+  TabD* tab;
+  double* rowd;    // [na][NROWD]
+  double* kernd;   // [n_tr][na][NDIR + 1]
+  double* part;    // [n_split][n_cls][n_ell][NDIR + 1] partial sums over a
+  double* cl;      // [n_cls][n_ell] (may be NULL)
+  double* jac;     // [n_cls][n_ell][NDIR]
+};
+
+// Uniform form: one geometry, per-item pointers from strides.  Listed form:
+// items[] (ragged requests), sizes below are the maxima over the items.
 struct GradBatch {
   int n_items;
+  int listed;
+  const GradItem* items;
   const double* params;
   const GeoHeader* geo;
   TabD* tab;
-  double* rowd;    // [B][na][NROWD]
-  double* kernd;   // [B][n_tr][na][NDIR + 1]
-  double* part;    // [n_split][B][n_cls][n_ell][NDIR + 1] partial sums over a
-  double* cl;      // [B][n_cls][n_ell]
-  double* jac;     // [B][n_cls][n_ell][NDIR]
+  double* rowd;
+  double* kernd;
+  double* part;
+  double* cl;
+  double* jac;
   int na, n_tr, n_cls, n_ell, n_split;
 };
+
+__device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
+  if (gb.listed) return gb.items[i];
+  GradItem r;
+  const size_t per = (size_t)gb.n_cls * gb.n_ell;
+  r.params = gb.params + 8 * (size_t)i;
+  r.geo = gb.geo;
+  r.tab = gb.tab + i;
+  r.rowd = gb.rowd + (size_t)i * gb.na * NROWD;
+  r.kernd = gb.kernd + (size_t)i * gb.n_tr * gb.na * (NDIR + 1);
+  r.part = gb.part + (size_t)i * gb.n_split * per * (NDIR + 1);
+  r.cl = gb.cl ? gb.cl + (size_t)i * per : nullptr;
+  r.jac = gb.jac + (size_t)i * per * NDIR;
+  return r;
+}
 
 typedef Dual<1> D1;
 typedef Dual<NDIR> D8;
@@ -94,8 +129,9 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
   double* pq = gt + (NDIR + 1) * NGROW;       // [NDIR+1][NKH]
   double* g1s = pq + (NDIR + 1) * NKH;        // [NDIR+1]
   const int t = threadIdx.x, dir = t & 7, it = t >> 3;
-  const double* P = gb.params + 8 * (size_t)item;
-  TabD* out = gb.tab + item;
+  const GradItem gi = grad_item(gb, item);
+  const double* P = gi.params;
+  TabD* out = gi.tab;
   // scalars (lanes 0-7 of warp 0)
   if (t < NDIR) {
     D1 p[8];
@@ -297,12 +333,13 @@ size_t grad_tables_smem() {
 __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
-  const GeoHeader* geo = gb.geo;
+  const GradItem gi = grad_item(gb, item);
+  const GeoHeader* geo = gi.geo;
   const int na = geo->na;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = blockIdx.x * 8 + warp;
   if (n >= na) return;
-  const TabD* tb = gb.tab + item;
+  const TabD* tb = gi.tab;
   const int dir = lane & 7;
   const double* A = geo_ptr<double>(geo, geo->off_a);
   const double* WS = geo_ptr<double>(geo, geo->off_wsimp);
@@ -414,7 +451,7 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
   const D1 dchi = dchioverdaT(bg, a, lna);
   outv[A_U] = WS[n] * dchi / xfmax(chi * chi, 1.0) / C2_G;
   if (lane < NDIR) {
-    double* row = gb.rowd + ((size_t)item * na + n) * NROWD;
+    double* row = gi.rowd + (size_t)n * NROWD;
     for (int i = 0; i < NA_IN; ++i) {
       if (dir == 0) row[i] = outv[i].v;
       row[NA_IN * (1 + dir) + i] = outv[i].d[0];
@@ -428,12 +465,13 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
 __global__ void __launch_bounds__(256) grad_kern_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
-  const GeoHeader* geo = gb.geo;
+  const GradItem gi = grad_item(gb, item);
+  const GeoHeader* geo = gi.geo;
   const int na = geo->na, n_tr = geo->n_tr;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int n = blockIdx.x * 8 + warp;
   if (n >= na) return;
-  const TabD* tb = gb.tab + item;
+  const TabD* tb = gi.tab;
   const int dir = lane & 7;
   const double* Z = geo_ptr<double>(geo, geo->off_z);
   const double* AWL = geo_ptr<double>(geo, geo->off_awl);
@@ -445,7 +483,7 @@ __global__ void __launch_bounds__(256) grad_kern_kernel(GradBatch gb, const Cons
   const D1 chi_wl = xfmax(interp_d1(awl, c->atab_chi, tb->chiv, tb->chid[dir], unpack_seg(SW[n])), 0.0);
   const D1 cf = 3.0 * (H0 * H0) * sD[S_OMEGA_M] / 2.0 / C_KMS;  // probes.py:71
   const D8 chiwl8 = gather8(chi_wl);
-  double* kd = gb.kernd + (size_t)item * n_tr * na * (NDIR + 1);
+  double* kd = gi.kernd;
   for (int t0 = 0; t0 < n_tr; t0 += 4) {
     int tl[4];
     int cnt = 0;
@@ -689,7 +727,8 @@ __global__ void __launch_bounds__(GL_THREADS)
     grad_limber_kernel(GradBatch gb, const ConstTables* __restrict__ c, int LT) {
   const int item = blockIdx.z, split = blockIdx.y;
   if (item >= gb.n_items) return;
-  const GeoHeader* geo = gb.geo;
+  const GradItem gi = grad_item(gb, item);
+  const GeoHeader* geo = gi.geo;
   const int n_ell = geo->n_ell, n_cls = geo->n_cls, na = geo->na;
   const int l0 = blockIdx.x * LT;
   if (l0 >= n_ell) return;
@@ -708,7 +747,7 @@ __global__ void __launch_bounds__(GL_THREADS)
   double* Pv = Md + GL_TA * n_cls * NDIR;             // [GL_TA][LT]
   double* Pd = Pv + GL_TA * LT;                       // [GL_TA][LT][NDIR]
   const int tid = threadIdx.x;
-  const TabD* tb = gb.tab + item;
+  const TabD* tb = gi.tab;
   for (int i = tid; i < NC_IN; i += GL_THREADS) {
     const int si = kNodeCScalar[i];
     cvs[i] = tb->sv[si];
@@ -726,8 +765,8 @@ __global__ void __launch_bounds__(GL_THREADS)
   ck.alphab = cvs[C_ALPHAB]; ck.betab = cvs[C_BETAB]; ck.betanode = cvs[C_BETANODE];
   ck.ksilk = cvs[C_KSILK]; ck.fb = cvs[C_FB]; ck.fc = cvs[C_FC]; ck.ns = cvs[C_NS];
   ck.pknorm = cvs[C_PKNORM];
-  const double* rowd = gb.rowd + (size_t)item * na * NROWD;
-  const double* kd = gb.kernd + (size_t)item * geo->n_tr * na * (NDIR + 1);
+  const double* rowd = gi.rowd;
+  const double* kd = gi.kernd;
   const int nout = lt * n_cls * (NDIR + 1);
   double acc[GL_MAXO];
 #pragma unroll
@@ -795,7 +834,7 @@ __global__ void __launch_bounds__(GL_THREADS)
     }
     __syncthreads();
   }
-  double* part = gb.part + (size_t)split * gb.n_items * n_cls * n_ell * (NDIR + 1);
+  double* part = gi.part + (size_t)split * n_cls * n_ell * (NDIR + 1);
 #pragma unroll
   for (int r = 0; r < GL_MAXO; ++r) {
     const int o = tid + r * GL_THREADS;
@@ -805,25 +844,27 @@ __global__ void __launch_bounds__(GL_THREADS)
       const int l = lp % lt, p = lp / lt;
       const int ell = l0 + l;
       const double ef = EF[(size_t)geo->pair_i[p] * n_ell + ell] * EF[(size_t)geo->pair_j[p] * n_ell + ell];
-      part[(((size_t)item * n_cls + p) * n_ell + ell) * (NDIR + 1) + s] = acc[r] * ef;
+      part[((size_t)p * n_ell + ell) * (NDIR + 1) + s] = acc[r] * ef;
     }
   }
 }
 
-// Fixed-order sum over the a splits; C_ell and the Jacobian out.
+// Fixed-order sum over the a splits; C_ell and the Jacobian out.  Grid (x, item).
 __global__ void grad_reduce_kernel(GradBatch gb) {
-  const size_t per = (size_t)gb.n_cls * gb.n_ell;
-  const size_t total = per * gb.n_items;
-  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+  const int item = blockIdx.y;
+  if (item >= gb.n_items) return;
+  const GradItem gi = grad_item(gb, item);
+  const size_t per = (size_t)gi.geo->n_cls * gi.geo->n_ell;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < per;
        idx += (size_t)gridDim.x * blockDim.x) {
     double v[NDIR + 1];
     for (int s = 0; s <= NDIR; ++s) v[s] = 0.0;
     for (int sp = 0; sp < gb.n_split; ++sp) {
-      const double* p = gb.part + ((size_t)sp * total + idx) * (NDIR + 1);
+      const double* p = gi.part + ((size_t)sp * per + idx) * (NDIR + 1);
       for (int s = 0; s <= NDIR; ++s) v[s] += p[s];
     }
-    if (gb.cl) gb.cl[idx] = v[0];
-    for (int d = 0; d < NDIR; ++d) gb.jac[idx * NDIR + d] = v[1 + d];
+    if (gi.cl) gi.cl[idx] = v[0];
+    for (int d = 0; d < NDIR; ++d) gi.jac[idx * NDIR + d] = v[1 + d];
   }
 }
 
@@ -852,10 +893,11 @@ void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
   cudaFuncSetAttribute(grad_limber_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sml);
   dim3 gl((gb.n_ell + lt - 1) / lt, gb.n_split, gb.n_items);
   grad_limber_kernel<<<gl, GL_THREADS, sml, st>>>(gb, c, lt);
-  const size_t total = (size_t)gb.n_cls * gb.n_ell * gb.n_items;
-  size_t blocks = (total + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
-  grad_reduce_kernel<<<(unsigned)(blocks ? blocks : 1), 256, 0, st>>>(gb);
+  const size_t per = (size_t)gb.n_cls * gb.n_ell;
+  size_t bx = (per + 255) / 256;
+  const size_t cap = (152 * 16 + gb.n_items - 1) / gb.n_items;
+  if (bx > cap) bx = cap;
+  grad_reduce_kernel<<<dim3((unsigned)(bx ? bx : 1), gb.n_items), 256, 0, st>>>(gb);
 }
 
 size_t grad_tab_bytes() { return sizeof(TabD); }
@@ -909,7 +951,97 @@ void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, in
   gb.n_cls = h.n_cls;
   gb.n_ell = h.n_ell;
   gb.n_split = grad_n_split(h, n_cosmo);
+  gb.listed = 0;
+  gb.items = nullptr;
   launch_grad(gb, c, st);
+}
+
+// ----------------------------------------------------- ragged requests -----
+// Listed form: every request has its own geometry; the workspace holds the
+// GradItem array, then per request its tables, rows, kernels, a-split partial
+// sums and (when the caller gave none) its C_ell and Jacobian.
+static size_t grad_item_bytes(const GeoHeader& h, int n_split, bool own_cl, bool own_jac) {
+  const size_t per = (size_t)h.n_cls * h.n_ell;
+  size_t o = al256(sizeof(TabD));
+  o += al256(sizeof(double) * (size_t)h.na * NROWD);
+  o += al256(sizeof(double) * (size_t)h.n_tr * h.na * (NDIR + 1));
+  o += al256(sizeof(double) * (size_t)n_split * per * (NDIR + 1));
+  if (own_cl) o += al256(sizeof(double) * per);
+  if (own_jac) o += al256(sizeof(double) * per * NDIR);
+  return o;
+}
+
+int grad_listed_auto_split(const GradReq* r, int n) {
+  int max_ell = 0, max_cls = 0, min_na = 1 << 30;
+  for (int i = 0; i < n; ++i) {
+    max_ell = max(max_ell, r[i].h->n_ell);
+    max_cls = max(max_cls, r[i].h->n_cls);
+    min_na = min(min_na, r[i].h->na);
+  }
+  const int lt = grad_limber_tile(max_ell, max_cls);
+  long ctas = 0;
+  for (int i = 0; i < n; ++i) ctas += (r[i].h->n_ell + lt - 1) / lt;
+  int ns = (int)((2 * 152 + ctas - 1) / ctas);
+  const int max_ns = (min_na + GL_TA - 1) / GL_TA;
+  if (ns > max_ns) ns = max_ns;
+  return ns < 1 ? 1 : ns;
+}
+
+size_t grad_listed_bytes(const GradReq* r, int n, int n_split) {
+  size_t o = al256(sizeof(GradItem) * (size_t)n);
+  for (int i = 0; i < n; ++i) o += grad_item_bytes(*r[i].h, n_split, !r[i].cl, !r[i].jac);
+  return o;
+}
+
+cudaError_t grad_run_listed(GradReq* r, int n, int n_split, void* ws, const ConstTables* c,
+                            cudaStream_t st) {
+  static thread_local std::vector<GradItem> host;
+  host.resize(n);
+  char* base = static_cast<char*>(ws);
+  GradItem* dev_items = reinterpret_cast<GradItem*>(base);
+  size_t o = al256(sizeof(GradItem) * (size_t)n);
+  GradBatch gb;
+  memset(&gb, 0, sizeof(gb));
+  for (int i = 0; i < n; ++i) {
+    const GeoHeader& h = *r[i].h;
+    const size_t per = (size_t)h.n_cls * h.n_ell;
+    GradItem& it = host[i];
+    it.params = r[i].params;
+    it.geo = r[i].geo;
+    it.tab = reinterpret_cast<TabD*>(base + o);
+    o += al256(sizeof(TabD));
+    it.rowd = reinterpret_cast<double*>(base + o);
+    o += al256(sizeof(double) * (size_t)h.na * NROWD);
+    it.kernd = reinterpret_cast<double*>(base + o);
+    o += al256(sizeof(double) * (size_t)h.n_tr * h.na * (NDIR + 1));
+    it.part = reinterpret_cast<double*>(base + o);
+    o += al256(sizeof(double) * (size_t)n_split * per * (NDIR + 1));
+    if (!r[i].cl) {
+      r[i].cl = reinterpret_cast<double*>(base + o);
+      o += al256(sizeof(double) * per);
+    }
+    if (!r[i].jac) {
+      r[i].jac = reinterpret_cast<double*>(base + o);
+      o += al256(sizeof(double) * per * NDIR);
+    }
+    it.cl = r[i].cl;
+    it.jac = r[i].jac;
+    gb.na = max(gb.na, h.na);
+    gb.n_tr = max(gb.n_tr, h.n_tr);
+    gb.n_cls = max(gb.n_cls, h.n_cls);
+    gb.n_ell = max(gb.n_ell, h.n_ell);
+  }
+  // pageable source: the copy is staged before the call returns, so the
+  // host vector can be reused by the next call of this thread
+  const cudaError_t e = cudaMemcpyAsync(dev_items, host.data(), sizeof(GradItem) * (size_t)n,
+                                        cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  gb.n_items = n;
+  gb.listed = 1;
+  gb.items = dev_items;
+  gb.n_split = n_split;
+  launch_grad(gb, c, st);
+  return cudaSuccess;
 }
 
 }  // namespace jcg

@@ -465,6 +465,28 @@ void launch_limber(const Batch& b, const ConstTables* c, int lt, cudaStream_t st
 size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo);
 void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, double* cl,
               double* jac, void* ws, const ConstTables* c, cudaStream_t st);
+// one request of a ragged Jacobian batch; cl / jac NULL: carved from the workspace
+struct GradReq {
+  const GeoHeader* h;      // host copy of the header
+  const GeoHeader* geo;    // device geometry
+  const double* params;    // device, 8 parameters
+  double* cl;
+  double* jac;
+};
+int grad_listed_auto_split(const GradReq* r, int n);
+size_t grad_listed_bytes(const GradReq* r, int n, int n_split);
+cudaError_t grad_run_listed(GradReq* r, int n, int n_split, void* ws, const ConstTables* c,
+                            cudaStream_t st);
+// log-likelihood and its gradient for a fixed inverse covariance (jcg_stats.cu)
+struct ReqLL {
+  const double* cl;     // [n_cls][n_ell]
+  const double* jac;    // [n_cls][n_ell][8]
+  const double* data;   // [n_cls * n_ell]
+  const double* prec;   // [n_ell][n_cls][n_cls]
+  double* out;          // [9]
+  int n_cls, n_ell;
+};
+void launch_request_loglike(const ReqLL* items_dev, int n, cudaStream_t st);
 // pointwise queries of the table functions (API: background / power modules)
 void launch_eval_points(const double* params, int n_cosmo, CosmoTab* ctab, const ConstTables* c,
                         const double* a, const double* k, int n, int what, double* out,

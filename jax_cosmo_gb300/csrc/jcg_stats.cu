@@ -241,6 +241,50 @@ __global__ void zero_int_kernel(int* p, int n) {
   if (i < n) p[i] = 0;
 }
 
+// Log-likelihood with a fixed inverse covariance P (the covariance held
+// constant, as in the reference's intro notebook) and its gradient:
+//   r = C_ell - data, logL = -r^T P r / 2, dlogL/dtheta = -(dC_ell/dtheta)^T P r.
+// One CTA per request; fixed-order reductions (same result alone or in a batch).
+__global__ void __launch_bounds__(256) request_loglike_kernel(const ReqLL* __restrict__ items, int n) {
+  const int item = blockIdx.x;
+  if (item >= n) return;
+  const ReqLL q = items[item];
+  const int n_cls = q.n_cls, n_ell = q.n_ell;
+  double acc[9];
+  for (int s = 0; s < 9; ++s) acc[s] = 0.0;
+  const int total = n_cls * n_ell;
+  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
+    const int l = idx / n_cls, p = idx % n_cls;
+    const double* Pl = q.prec + ((size_t)l * n_cls + p) * n_cls;
+    double alpha = 0.0;
+    for (int k = 0; k < n_cls; ++k) {
+      const size_t o = (size_t)k * n_ell + l;
+      alpha += Pl[k] * (q.cl[o] - q.data[o]);
+    }
+    const size_t op = (size_t)p * n_ell + l;
+    acc[0] += (q.cl[op] - q.data[op]) * alpha;
+    const double* J = q.jac + op * 8;
+    for (int d = 0; d < 8; ++d) acc[1 + d] += alpha * J[d];
+  }
+  __shared__ double red[8][9];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int s = 0; s < 9; ++s) {
+    double v = acc[s];
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_xor_sync(0xffffffffu, v, off);
+    if (lane == 0) red[warp][s] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 9) {
+    double v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
+    q.out[threadIdx.x] = threadIdx.x == 0 ? -0.5 * v : -v;
+  }
+}
+
+void launch_request_loglike(const ReqLL* items_dev, int n, cudaStream_t st) {
+  request_loglike_kernel<<<n, 256, 0, st>>>(items_dev, n);
+}
+
 void launch_loglike(const double* data, const double* mu, const double* cov, int n_cosmo, int n_cls,
                     int n_ell, int include_logdet, int dense, double* out, int* status,
                     double* partial, int* structure, double* alpha, cudaStream_t st) {
