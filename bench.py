@@ -15,6 +15,12 @@ the parameters copied from pinned host memory and the C_ell copied back each
 step.  The plain float64 method is timed on the same workload as
 ``fp64_value``.
 
+Beside the headline: the plain float64 method one cosmology per call (the
+per-cosmology rate the batched form is compared with), C_ell plus the Jacobian
+dC_ell/dtheta over the whole batch (``cl_grad``), and the serving loop under 64
+synthetic HMC chains (``serving``: requests/s, p50/p99 log-likelihood+gradient
+latency).
+
 ``--impl reference`` times the CPU reference of the path instead (the float64
 oracle port on the host cores; JAX is not available on the GPU host).
 """
@@ -264,7 +270,126 @@ def gpu_arm(args, rank, world, device):
     c64 = cl.clone()
     step("fp32c")
     res["fp32c_max_rel_err_vs_fp64"] = float(((cl - c64).abs() / c64.abs()).max())
+
+    # plain float64 method, one cosmology per call (the per-cosmology rate)
+    p1 = params[:1].contiguous()
+    cl1 = torch.empty(1, n_cls, n_ell, dtype=torch.float64, device=device)
+    t1, _ = timed(lambda: angular_cl_device(p1, ell_np, probes, "fp64", 512, out=cl1), args.steps, args.warmup)
+    res["plain_fp64_single"] = {"ms_per_call": t1 / args.steps,
+                                "cl_per_s": n_cls * n_ell / (t1 / args.steps * 1e-3)}
+
+    # C_ell + dC_ell/dtheta (8 leaves), float64, whole batch
+    from jax_cosmo_gb300.autodiff import jacobian_device
+
+    kj = max(1, min(args.steps, 3))
+    tj, _ = timed(lambda: jacobian_device(params, ell_np, probes, 512), kj, 1)
+    res["jacobian"] = {"batch": B, "ms_per_step": tj / kj, "dtype": "f64",
+                       "cl_grad_per_s": ncl_step / (tj / kj * 1e-3)}
+    cl_j, jac = jacobian_device(params[:64].contiguous(), ell_np, probes, 512)
+    step("fp64")
+    res["jacobian"]["cl_max_rel_err_vs_fp64"] = float(((cl_j - cl[:64]).abs() / cl[:64].abs()).max())
+    del jac
     return res
+
+
+def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, seed=SEED):
+    """64 synthetic HMC chains against the continuous-batching server.
+
+    Each chain (seeded): 1-10 tracers (WeakLensing / NumberCounts mix, smail_nz
+    a=1, b=2, z0 in U[0.3, 1.5]), 20-500 log-spaced ell in [10, 5000], data =
+    C_ell at its start point (box of the batched workload) with 1% noise,
+    covariance fixed at the start point.  A chain submits its next request an
+    exponential think time (mean think_ms) after its previous result, its
+    parameters jittered by 1% of the box width (Poisson arrivals per chain).
+    """
+    import heapq
+    import queue
+
+    import torch
+
+    import jax_cosmo_gb300 as jc
+    from jax_cosmo_gb300 import serving
+
+    lo = np.array([BOX.get(n, (0.0, 0.0))[0] for n in ORDER])
+    hi = np.array([BOX.get(n, (0.0, 0.0))[1] for n in ORDER])
+    width = hi - lo
+    models, pos, rngs = [], [], []
+    for c in range(n_chains):
+        rng = np.random.default_rng(seed + 1000 + c)
+        n_tr = int(rng.integers(1, 11))
+        n_wl = int(rng.integers(0, n_tr + 1))
+        z0 = rng.uniform(0.3, 1.5, n_tr)
+        n_ell = int(rng.integers(20, 501))
+        ell = np.logspace(1, np.log10(5000.0), n_ell)
+        probes = []
+        if n_wl:
+            probes.append(jc.probes.WeakLensing([jc.redshift.smail_nz(1.0, 2.0, float(z), gals_per_arcmin2=10.0)
+                                                 for z in z0[:n_wl]], sigma_e=0.26))
+        if n_tr > n_wl:
+            probes.append(jc.probes.NumberCounts([jc.redshift.smail_nz(1.0, 2.0, float(z), gals_per_arcmin2=10.0)
+                                                  for z in z0[n_wl:]], jc.bias.constant_linear_bias(1.2)))
+        p0 = lo + width * rng.uniform(size=8)
+        start = jc.Cosmology(*[float(v) for v in p0])
+        mu = jc.cl.angular_cl(start, ell, probes).flatten()
+        data = mu * (1.0 + 0.01 * torch.as_tensor(rng.standard_normal(mu.numel()), device=mu.device))
+        models.append(serving.ChainModel(probes, ell, data, fiducial=start))
+        pos.append(p0)
+        rngs.append(rng)
+    done_q = queue.Queue()
+    srv = serving.Server(device=device, hbm_budget=8 << 30, max_batch=256, n_streams=2).start()
+
+    def submit(c):
+        step = rngs[c].normal(0.0, 0.01, 8) * width
+        pos[c] = np.clip(pos[c] + step, lo, hi)
+        f = srv.submit(models[c], pos[c])
+        f.add_done_callback(lambda _f, c=c: done_q.put(c))
+        return f
+
+    heap = [(time.perf_counter() + rngs[c].exponential(think_ms * 1e-3), c) for c in range(n_chains)]
+    heapq.heapify(heap)
+    t_start = time.perf_counter()
+    t_measure = t_start + warm_s
+    t_end = t_measure + duration_s
+    reset = False
+    sample = []
+    while True:
+        now = time.perf_counter()
+        if not reset and now >= t_measure:
+            srv.reset_stats()
+            reset = True
+        if now >= t_end:
+            break
+        while heap and heap[0][0] <= now:
+            _, c = heapq.heappop(heap)
+            f = submit(c)
+            if reset and len(sample) < 8 and c % 8 == len(sample):
+                sample.append((c, pos[c].copy(), f))
+        timeout = max(0.0, heap[0][0] - now) if heap else 0.01
+        try:
+            c = done_q.get(timeout=min(timeout, 0.01))
+            heapq.heappush(heap, (time.perf_counter() + rngs[c].exponential(think_ms * 1e-3), c))
+            while True:
+                c = done_q.get_nowait()
+                heapq.heappush(heap, (time.perf_counter() + rngs[c].exponential(think_ms * 1e-3), c))
+        except queue.Empty:
+            pass
+    st = srv.stats()
+    srv.stop()
+    # served log-likelihoods against the plain float64 method (public API)
+    err = 0.0
+    for c, p, f in sample:
+        r = f.result()
+        m = models[c]
+        mu = jc.cl.angular_cl(jc.Cosmology(*[float(v) for v in p]), m.ell, m.probes).flatten()
+        res = (mu - m.data).reshape(m.n_cls, m.n_ell)
+        ll = -0.5 * float((res * torch.einsum("lpq,ql->pl", m.prec, res)).sum())
+        err = max(err, abs(r.loglike - ll) / abs(ll))
+    st["loglike_max_rel_err_vs_fp64"] = err
+    st["checked_requests"] = len(sample)
+    st.update({"chains": n_chains, "think_ms_mean": think_ms, "duration_s": duration_s,
+               "tracers_per_chain": [int(m.g.n_tracers) for m in models],
+               "n_ell_per_chain": [int(m.n_ell) for m in models], "dtype": "f64"})
+    return st
 
 
 def roofline(res, B):
@@ -302,6 +427,8 @@ def main():
     ap.add_argument("--batch", type=int, default=B_DEFAULT)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-serving", action="store_true")
+    ap.add_argument("--serve-seconds", type=float, default=10.0)
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -325,7 +452,9 @@ def main():
             vals.append(cb["value"])
         v = float(np.median(vals))
         print(json.dumps({
-            "impl": "reference", "metric": "C_ell evals/s (batched angular_cl)", "value": v,
+            "impl": "reference",
+            "metric": "C_ell evals/s batched vs plain at \u22641e-4 rel err; p50/p99 loglike+grad latency",
+            "value": v,
             "unit": "C_ell/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": config,
@@ -348,6 +477,9 @@ def main():
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
     res = gpu_arm(args, rank, world, device)
+    serve = None
+    if rank == 0 and not args.no_serving:
+        serve = serving_arm(device, duration_s=args.serve_seconds)
     if rank != 0:
         return
     K = res["K"]
@@ -356,12 +488,20 @@ def main():
     fp64_value = res["ncl_step"] * world / (res["t64"] / res["n64"] * 1e-3)
     e2e = res["ncl_step"] * world / (res["t_e2e"] / K * 1e-3)
     rl, rl_sfu = roofline(res, args.batch)
+    plain = res["plain_fp64_single"]["cl_per_s"]
+    jac = res["jacobian"]
+    jac["over_plain_fp64_single"] = jac["cl_grad_per_s"] / plain
     out = {
-        "metric": "C_ell evals/s (batched angular_cl, fp32c at <=1e-4 rel err vs fp64)",
+        "metric": "C_ell evals/s batched vs plain at \u22641e-4 rel err; p50/p99 loglike+grad latency",
         "value": value, "unit": "C_ell/s", "n_gpus": world, "steps": K, "warmup": args.warmup,
         "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32c+f64", "data": "synthetic", "config": config,
         "fp64_value": fp64_value, "fp32c_over_fp64": value / fp64_value,
+        "plain_fp64_single": res["plain_fp64_single"],
+        "batched_over_plain_fp64_single": value / plain,
+        "cl_grad": jac,
+        "loglike_grad_latency_ms": ({"p50": serve["p50_ms"], "p99": serve["p99_ms"]} if serve else None),
+        "serving": serve,
         "fp32c_max_rel_err_vs_fp64": res["fp32c_max_rel_err_vs_fp64"],
         "cosmologies_per_s": value / 1500.0,
         "e2e": {"value": e2e, "unit": "C_ell/s", "h2d_bytes_per_step": res["h2d"],

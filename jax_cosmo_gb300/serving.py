@@ -74,6 +74,7 @@ class ChainModel:
         from jax_cosmo_gb300.parameters import Planck15
 
         self.device = _lib.require_cuda(device)
+        self.probes = probes
         self.ell = _geometry.ell_host(ell)
         self.g, self.geo, _ = _geometry.get_geometry(probes, self.ell, n_limber, self.device)
         self.n_cls = _geometry.n_cls_of(self.g)
@@ -290,9 +291,18 @@ class Server:
     def __exit__(self, *exc):
         self.stop()
 
+    def reset_stats(self):
+        """Forget latencies and counts so far (e.g. after a warm-up period)."""
+        self._lat = []
+        self._batch_sizes = []
+        self._completed = 0
+        self._failed = 0
+        self._t_first = time.perf_counter()
+        self._t_last = None
+
     def stats(self):
         lat = np.asarray(self._lat)
-        span = (self._t_last - self._t_first) if self._completed and self._t_last > self._t_first else 0.0
+        span = (self._t_last - self._t_first) if self._completed and self._t_last and self._t_last > self._t_first else 0.0
         return {
             "completed": self._completed,
             "failed": self._failed,
