@@ -156,16 +156,19 @@ int jcg_stage_limber(const jcg_geometry* g, const void* geo_dev, const double* p
                      int n_cosmo, int precision, double* cl_dev, void* workspace,
                      size_t workspace_bytes, cudaStream_t stream);
 
-/* Derivatives of angular_cl with respect to the 8 Cosmology leaves, float64:
+/* Derivatives of angular_cl with respect to the 8 Cosmology leaves:
  * jac_dev [n_cosmo][n_cls][n_ell][8] = dC_ij(l)/d(Omega_c, Omega_b, h, n_s,
  * sigma8, Omega_k, w0, wa), and cl_dev (may be NULL) the C_ell themselves.
  * Replaces jax.grad / jax.jacfwd through angular_cl (angular_cl.py:49-98;
  * README.md:14-27): the vector-Jacobian product of a likelihood is
  * sum_ij,l v_ij(l) jac_ij(l).  Tables are differentiated forward (tangents),
- * the Limber integrand by a reverse sweep; all recomputed from params_dev. */
-int jcg_jacobian_workspace_size(const jcg_geometry* g, int n_cosmo, size_t* bytes);
+ * the Limber integrand by a reverse sweep; all recomputed from params_dev.
+ * precision: JCG_FP64 everywhere, or JCG_FP32C (float64 tables, root find and
+ * moments; float32 lensing kernels and Limber integrand + reverse sweep with
+ * compensated a-sums). */
+int jcg_jacobian_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t* bytes);
 int jcg_angular_cl_jacobian(const jcg_geometry* g, const void* geo_dev, const double* params_dev,
-                            int n_cosmo, double* cl_dev, double* jac_dev, void* workspace,
+                            int n_cosmo, int precision, double* cl_dev, double* jac_dev, void* workspace,
                             size_t workspace_bytes, cudaStream_t stream);
 
 /* ------------------------------------------------ ragged requests ------ */
@@ -176,17 +179,16 @@ int jcg_angular_cl_jacobian(const jcg_geometry* g, const void* geo_dev, const do
  * each followed by jax.grad of the chain's likelihood (likelihood.py:9-61 with
  * the covariance held fixed, docs/notebooks/jax-cosmo-intro.ipynb).
  * Every request's result depends only on its own inputs: the same alone and
- * in any mix.  mode:
- *   JCG_REQ_CL_FP64 / JCG_REQ_CL_FP32C: cl -> C_ell [n_cls][n_ell];
+ * in any mix.  mode (with precision JCG_FP64 or JCG_FP32C):
+ *   JCG_REQ_CL: cl -> C_ell [n_cls][n_ell];
  *   JCG_REQ_JACOBIAN: jac -> dC_ell/dtheta [n_cls][n_ell][8], cl (may be NULL);
  *   JCG_REQ_LOGLIKE_GRAD: out -> [9] = logL = -r^T P r / 2 with r = C_ell - data
  *     and its gradient -(dC/dtheta)^T P r over the 8 Cosmology leaves; data
  *     [n_cls*n_ell] in (cls, ell) order, prec [n_ell][n_cls][n_cls] the inverse
  *     covariance blocks; cl / jac optional outputs (NULL: workspace). */
-#define JCG_REQ_CL_FP64 0
-#define JCG_REQ_CL_FP32C 1
-#define JCG_REQ_JACOBIAN 2
-#define JCG_REQ_LOGLIKE_GRAD 3
+#define JCG_REQ_CL 0
+#define JCG_REQ_JACOBIAN 1
+#define JCG_REQ_LOGLIKE_GRAD 2
 #define JCG_MAX_REQUESTS 65536
 
 typedef struct {
@@ -203,9 +205,9 @@ typedef struct {
 /* Workspace for n requests: *bytes_min with no a-splits of the Jacobian,
  * *bytes_full with the splits that fill the GPU for small batches;
  * jcg_requests_run uses as many splits as ws_bytes allows. */
-int jcg_requests_workspace_size(const jcg_request* reqs, int n, int mode, size_t* bytes_min,
-                                size_t* bytes_full);
-int jcg_requests_run(const jcg_request* reqs, int n, int mode, void* workspace,
+int jcg_requests_workspace_size(const jcg_request* reqs, int n, int mode, int precision,
+                                size_t* bytes_min, size_t* bytes_full);
+int jcg_requests_run(const jcg_request* reqs, int n, int mode, int precision, void* workspace,
                      size_t workspace_bytes, cudaStream_t stream);
 
 /* Copy stage outputs for cosmology `index` out of a workspace (device to device).

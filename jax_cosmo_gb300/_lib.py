@@ -44,7 +44,7 @@ FP32C = 1
 EVAL_CHI, EVAL_GROWTH, EVAL_H, EVAL_DCHI, EVAL_TRANSFER, EVAL_PLIN, EVAL_PNL = range(7)
 EVAL_KNL, EVAL_NEFF, EVAL_C = 7, 8, 9
 
-REQ_CL_FP64, REQ_CL_FP32C, REQ_JACOBIAN, REQ_LOGLIKE_GRAD = 0, 1, 2, 3
+REQ_CL, REQ_JACOBIAN, REQ_LOGLIKE_GRAD = 0, 1, 2
 MAX_REQUESTS = 65536
 # jcg_request (include/jcg.h): eight pointers, filled column-wise for a batch
 REQUEST_DTYPE = np.dtype([(n, np.uint64) for n in ("g", "geo", "params", "cl", "jac", "data", "prec", "out")])
@@ -106,10 +106,10 @@ SIGNATURES = {
     "jcg_gaussian_loglike_sparse": [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _SZ, _P],
     "jcg_loglike_workspace_size": [_I, _I, _I, _PSZ],
     "jcg_gaussian_loglike_dense": [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _SZ, _P],
-    "jcg_jacobian_workspace_size": [_PG, _I, _PSZ],
-    "jcg_angular_cl_jacobian": [_PG, _P, _P, _I, _P, _P, _P, _SZ, _P],
-    "jcg_requests_workspace_size": [_P, _I, _I, _PSZ, _PSZ],
-    "jcg_requests_run": [_P, _I, _I, _P, _SZ, _P],
+    "jcg_jacobian_workspace_size": [_PG, _I, _I, _PSZ],
+    "jcg_angular_cl_jacobian": [_PG, _P, _P, _I, _I, _P, _P, _P, _SZ, _P],
+    "jcg_requests_workspace_size": [_P, _I, _I, _I, _PSZ, _PSZ],
+    "jcg_requests_run": [_P, _I, _I, _I, _P, _SZ, _P],
     "jcg_sparse_inv": [_P, _I, _I, _P, _P],
     "jcg_sparse_slogdet": [_P, _I, _I, _P, _P, _P, _P],
     "jcg_sparse_to_dense": [_P, _I, _I, _I, _P, _P],

@@ -32,19 +32,26 @@ PARAM_ORDER = ("Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"
 FISHER_PARAMS = ("Omega_c", "Omega_b", "h", "n_s", "sigma8", "w0", "wa")
 
 
-def jacobian_device(params, ell, probes, n_limber=512):
-    """(C_ell [B, n_cls, n_ell], dC/dtheta [B, n_cls, n_ell, 8]) for [B, 8] params on the device."""
+def jacobian_device(params, ell, probes, n_limber=512, precision="fp64"):
+    """(C_ell [B, n_cls, n_ell], dC/dtheta [B, n_cls, n_ell, 8]) for [B, 8] params on the device.
+
+    precision "fp64" (plain) or "fp32c" (float32 lensing kernels and Limber
+    integrand with its reverse sweep, compensated a-sums; float64 tables).
+    """
+    from jax_cosmo_gb300.angular_cl import _precision_code
+
+    prec = _precision_code(precision)
     device = params.device
     g, geo, _ = _geometry.get_geometry(probes, ell, n_limber, device)
     B = params.shape[0]
     n_cls = _geometry.n_cls_of(g)
     wsz = ctypes.c_size_t()
-    _lib.call("jcg_jacobian_workspace_size", ctypes.byref(g), B, ctypes.byref(wsz))
+    _lib.call("jcg_jacobian_workspace_size", ctypes.byref(g), B, prec, ctypes.byref(wsz))
     ws = _lib.workspace(wsz.value, device)
     cl = torch.empty(B, n_cls, g.n_ell, dtype=torch.float64, device=device)
     jac = torch.empty(B, n_cls, g.n_ell, len(PARAM_ORDER), dtype=torch.float64, device=device)
     _lib.call(
-        "jcg_angular_cl_jacobian", ctypes.byref(g), _lib.ptr(geo), _lib.ptr(params.contiguous()), B,
+        "jcg_angular_cl_jacobian", ctypes.byref(g), _lib.ptr(geo), _lib.ptr(params.contiguous()), B, prec,
         _lib.ptr(cl), _lib.ptr(jac), _lib.ptr(ws), ctypes.c_size_t(ws.numel()), _lib.stream_of(device),
     )
     return cl, jac
@@ -55,15 +62,15 @@ class _AngularCl(torch.autograd.Function):
     def forward(ctx, params, ell, probes, precision, n_limber):
         from jax_cosmo_gb300.angular_cl import angular_cl_device
 
-        ctx.meta = (ell, probes, n_limber)
+        ctx.meta = (ell, probes, n_limber, precision)
         ctx.save_for_backward(params)
         return angular_cl_device(params.detach().contiguous(), ell, probes, precision, n_limber)
 
     @staticmethod
     def backward(ctx, gcl):
         (params,) = ctx.saved_tensors
-        ell, probes, n_limber = ctx.meta
-        _, jac = jacobian_device(params.detach().contiguous(), ell, probes, n_limber)
+        ell, probes, n_limber, precision = ctx.meta
+        _, jac = jacobian_device(params.detach().contiguous(), ell, probes, n_limber, precision)
         gp = torch.einsum("bpl,bpld->bd", gcl.to(torch.float64), jac)
         return gp, None, None, None, None
 
@@ -74,15 +81,15 @@ def angular_cl_autograd(cosmo, ell, probes, precision="fp64", n_limber=512):
     return _AngularCl.apply(params, ell, probes, precision, n_limber)
 
 
-def angular_cl_jacobian(cosmo, ell, probes, n_limber=512):
+def angular_cl_jacobian(cosmo, ell, probes, n_limber=512, precision="fp64"):
     """(C_ell, dC_ell/dtheta) with theta = (Omega_c, Omega_b, h, n_s, sigma8, Omega_k, w0, wa).
 
     Shapes [n_cls, n_ell] and [n_cls, n_ell, 8] (a leading batch axis for a
-    batched Cosmology).
+    batched Cosmology).  precision "fp64" or "fp32c".
     """
     device = _lib.require_cuda()
     params = cosmo.param_tensor(device)
-    cl, jac = jacobian_device(params, _geometry.ell_host(ell), probes, n_limber)
+    cl, jac = jacobian_device(params, _geometry.ell_host(ell), probes, n_limber, precision)
     if cosmo.batch_size is None:
         return cl[0], jac[0]
     return cl, jac
@@ -220,7 +227,7 @@ def loglike_autograd(data2, mu2, Cb, include_logdet, sparse, n_cls, n_ell):
 
 
 # ----------------------------------------------------------------- Fisher ----
-def fisher_matrix(cosmo, ell, probes, f_sky=0.25, n_limber=512, params=FISHER_PARAMS):
+def fisher_matrix(cosmo, ell, probes, f_sky=0.25, n_limber=512, params=FISHER_PARAMS, precision="fp64"):
     """Gaussian Fisher matrix F = J^T C^-1 J of the C_ell data vector.
 
     J = dC_ell/dtheta for the named parameters (a subset of PARAM_ORDER), C the
@@ -229,7 +236,7 @@ def fisher_matrix(cosmo, ell, probes, f_sky=0.25, n_limber=512, params=FISHER_PA
     """
     from jax_cosmo_gb300.angular_cl import gaussian_cl_covariance, noise_cl
 
-    cl, jac = angular_cl_jacobian(cosmo, ell, probes, n_limber)
+    cl, jac = angular_cl_jacobian(cosmo, ell, probes, n_limber, precision)
     if cl.dim() != 2:
         raise ValueError("fisher_matrix takes a single (unbatched) cosmology")
     sel = [PARAM_ORDER.index(p) for p in params]

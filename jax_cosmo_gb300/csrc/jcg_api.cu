@@ -622,31 +622,33 @@ extern "C" int jcg_angular_cl_noalloc(const jcg_geometry* g, const void* geo, co
 }
 
 // --------------------------------------------------------- derivatives -----
-extern "C" int jcg_jacobian_workspace_size(const jcg_geometry* g, int n_cosmo, size_t* bytes) {
+extern "C" int jcg_jacobian_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t* bytes) {
   if (!bytes) return fail(JCG_ERR_ARG, "bytes is NULL");
   if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  if (precision != JCG_FP64 && precision != JCG_FP32C) return fail(JCG_ERR_ARG, "precision = %d", precision);
   GeoHeader h;
   const int rc = make_header(g, &h);
   if (rc) return rc;
-  *bytes = grad_workspace_bytes(h, n_cosmo);
+  *bytes = grad_workspace_bytes(h, n_cosmo, precision);
   return JCG_OK;
 }
 
 extern "C" int jcg_angular_cl_jacobian(const jcg_geometry* g, const void* geo, const double* params,
-                                       int n_cosmo, double* cl, double* jac, void* ws,
+                                       int n_cosmo, int precision, double* cl, double* jac, void* ws,
                                        size_t ws_bytes, cudaStream_t stream) {
   GeoHeader h;
   int rc = make_header(g, &h);
   if (rc) return rc;
   if (!geo || !params || !jac || !ws) return fail(JCG_ERR_ARG, "NULL pointer");
   if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  if (precision != JCG_FP64 && precision != JCG_FP32C) return fail(JCG_ERR_ARG, "precision = %d", precision);
   if (h.custom_nodes) return fail(JCG_ERR_ARG, "a geometry with caller redshift nodes has no Limber grid");
-  const size_t need = grad_workspace_bytes(h, n_cosmo);
+  const size_t need = grad_workspace_bytes(h, n_cosmo, precision);
   if (ws_bytes < need) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need);
   if (((uintptr_t)ws) % 256 != 0) return fail(JCG_ERR_ARG, "workspace must be 256-byte aligned");
   ConstTables* c = nullptr;
   if ((rc = const_tables(&c))) return rc;
-  grad_run(static_cast<const GeoHeader*>(geo), h, params, n_cosmo, cl, jac, ws, c, stream);
+  grad_run(static_cast<const GeoHeader*>(geo), h, params, n_cosmo, precision, cl, jac, ws, c, stream);
   return cuda_check("angular_cl_jacobian");
 }
 
@@ -667,10 +669,11 @@ size_t cl_item_bytes(const GeoHeader& h, int precision) {
 }
 
 // host validation of every request; headers into plan
-int plan_requests(const jcg_request* reqs, int n, int mode, ReqPlan* plan) {
+int plan_requests(const jcg_request* reqs, int n, int mode, int precision, ReqPlan* plan) {
   if (!reqs) return fail(JCG_ERR_ARG, "requests is NULL");
   if (n < 1 || n > JCG_MAX_REQUESTS) return fail(JCG_ERR_SHAPE, "n = %d (1..%d)", n, JCG_MAX_REQUESTS);
-  if (mode < JCG_REQ_CL_FP64 || mode > JCG_REQ_LOGLIKE_GRAD) return fail(JCG_ERR_ARG, "mode = %d", mode);
+  if (mode < JCG_REQ_CL || mode > JCG_REQ_LOGLIKE_GRAD) return fail(JCG_ERR_ARG, "mode = %d", mode);
+  if (precision != JCG_FP64 && precision != JCG_FP32C) return fail(JCG_ERR_ARG, "precision = %d", precision);
   plan->hdr.resize(n);
   plan->greq.resize(n);
   for (int i = 0; i < n; ++i) {
@@ -683,7 +686,7 @@ int plan_requests(const jcg_request* reqs, int n, int mode, ReqPlan* plan) {
     }
     if (plan->hdr[i].custom_nodes) return fail(JCG_ERR_ARG, "request %d: geometry without a Limber grid", i);
     if (!r.geo_dev || !r.params_dev) return fail(JCG_ERR_ARG, "request %d: NULL geometry or params", i);
-    if (mode <= JCG_REQ_CL_FP32C && !r.cl_dev) return fail(JCG_ERR_ARG, "request %d: cl is NULL", i);
+    if (mode == JCG_REQ_CL && !r.cl_dev) return fail(JCG_ERR_ARG, "request %d: cl is NULL", i);
     if (mode == JCG_REQ_JACOBIAN && !r.jac_dev) return fail(JCG_ERR_ARG, "request %d: jac is NULL", i);
     if (mode == JCG_REQ_LOGLIKE_GRAD && (!r.data_dev || !r.prec_dev || !r.out_dev))
       return fail(JCG_ERR_ARG, "request %d: data, prec or out is NULL", i);
@@ -707,35 +710,34 @@ size_t ll_extra_bytes(int n) { return align256(sizeof(ReqLL) * (size_t)n); }
 
 }  // namespace
 
-extern "C" int jcg_requests_workspace_size(const jcg_request* reqs, int n, int mode, size_t* bytes_min,
-                                           size_t* bytes_full) {
+extern "C" int jcg_requests_workspace_size(const jcg_request* reqs, int n, int mode, int precision,
+                                           size_t* bytes_min, size_t* bytes_full) {
   if (!bytes_min || !bytes_full) return fail(JCG_ERR_ARG, "bytes is NULL");
   static thread_local ReqPlan plan;
-  int rc = plan_requests(reqs, n, mode, &plan);
+  int rc = plan_requests(reqs, n, mode, precision, &plan);
   if (rc) return rc;
-  if (mode <= JCG_REQ_CL_FP32C) {
-    *bytes_min = *bytes_full = cl_listed_bytes(plan, mode);
+  if (mode == JCG_REQ_CL) {
+    *bytes_min = *bytes_full = cl_listed_bytes(plan, precision);
     return JCG_OK;
   }
   const size_t extra = mode == JCG_REQ_LOGLIKE_GRAD ? ll_extra_bytes(n) : 0;
-  const int ns = grad_listed_auto_split(plan.greq.data(), n);
-  *bytes_min = extra + grad_listed_bytes(plan.greq.data(), n, 1);
-  *bytes_full = extra + grad_listed_bytes(plan.greq.data(), n, ns);
+  const int ns = grad_listed_auto_split(plan.greq.data(), n, precision);
+  *bytes_min = extra + grad_listed_bytes(plan.greq.data(), n, 1, precision);
+  *bytes_full = extra + grad_listed_bytes(plan.greq.data(), n, ns, precision);
   return JCG_OK;
 }
 
-extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, void* ws, size_t ws_bytes,
-                                cudaStream_t stream) {
+extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, int precision, void* ws,
+                                size_t ws_bytes, cudaStream_t stream) {
   static thread_local ReqPlan plan;
-  int rc = plan_requests(reqs, n, mode, &plan);
+  int rc = plan_requests(reqs, n, mode, precision, &plan);
   if (rc) return rc;
   if (!ws) return fail(JCG_ERR_ARG, "workspace is NULL");
   if (((uintptr_t)ws) % 256 != 0) return fail(JCG_ERR_ARG, "workspace must be 256-byte aligned");
   ConstTables* c = nullptr;
   if ((rc = const_tables(&c))) return rc;
   char* base = static_cast<char*>(ws);
-  if (mode <= JCG_REQ_CL_FP32C) {
-    const int precision = mode;
+  if (mode == JCG_REQ_CL) {
     const size_t need = cl_listed_bytes(plan, precision);
     if (ws_bytes < need) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need);
     static thread_local std::vector<Item> items;
@@ -783,11 +785,11 @@ extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, void* 
     return cuda_check("requests angular_cl");
   }
   const size_t extra = mode == JCG_REQ_LOGLIKE_GRAD ? ll_extra_bytes(n) : 0;
-  const size_t need1 = extra + grad_listed_bytes(plan.greq.data(), n, 1);
+  const size_t need1 = extra + grad_listed_bytes(plan.greq.data(), n, 1, precision);
   if (ws_bytes < need1) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need1);
-  int ns = grad_listed_auto_split(plan.greq.data(), n);
-  while (ns > 1 && extra + grad_listed_bytes(plan.greq.data(), n, ns) > ws_bytes) --ns;
-  if (cudaError_t e = grad_run_listed(plan.greq.data(), n, ns, base + extra, c, stream))
+  int ns = grad_listed_auto_split(plan.greq.data(), n, precision);
+  while (ns > 1 && extra + grad_listed_bytes(plan.greq.data(), n, ns, precision) > ws_bytes) --ns;
+  if (cudaError_t e = grad_run_listed(plan.greq.data(), n, ns, precision, base + extra, c, stream))
     return fail(JCG_ERR_CUDA, "requests jacobian: %s", cudaGetErrorString(e));
   if (mode == JCG_REQ_LOGLIKE_GRAD) {
     static thread_local std::vector<ReqLL> ll;

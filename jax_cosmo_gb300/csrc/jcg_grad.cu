@@ -17,92 +17,9 @@
 
 #include <vector>
 
-#include "jcg_dual.cuh"
+#include "jcg_grad.cuh"
 
 namespace jcg {
-
-constexpr double TWO_PI2_G = 2.0 * (PI * PI);
-constexpr double C2_G = C_KMS * C_KMS;
-constexpr double LN10_G = 2.302585092994046;
-
-// ------------------------------------------------------------ dual tables ---
-struct TabD {
-  double sv[NSCAL];
-  double sd[NDIR][NSCAL];
-  double chiv[NCHI];
-  double chid[NDIR][NCHI];
-  double gv[NGROW];
-  double gd[NDIR][NGROW];
-  double sigv[NRT];
-  double sigd[NDIR][NRT];
-  double pk3v[NKH];
-  double pk3d[NDIR][NKH];
-  double pad[7];
-};
-static_assert(sizeof(TabD) % 64 == 0, "TabD alignment");
-
-// per-node inputs of the Limber integrand (node_fb), value + 8 tangents
-enum NodeA { A_CHIC = 0, A_G, A_KNL, A_BETA, A_ALPHA, A_AN, A_BN, A_LCF3, A_F1, A_F2, A_GAM, A_NU, A_U, NA_IN };
-constexpr int NROWD = NA_IN * (NDIR + 1);  // [NA_IN] values then [NDIR][NA_IN] tangents
-// per-cosmology inputs of the integrand
-enum NodeC { C_KEQ = 0, C_SH, C_BETAC, C_ALPHAC, C_ALPHAB, C_BETAB, C_BETANODE, C_KSILK, C_FB, C_FC, C_NS, C_PKNORM, NC_IN };
-__device__ __constant__ const int kNodeCScalar[NC_IN] = {S_K_EQ,  S_SH_D,      S_BETA_C,  S_ALPHA_C,
-                                                         S_ALPHA_B, S_BETA_B, S_BETA_NODE, S_K_SILK,
-                                                         S_FB,    S_FC,        S_NS,      S_PKNORM};
-
-// One (cosmology, geometry) pair of a Jacobian batch.
-struct GradItem {
-  const double* params;   // 8 parameters
-  const GeoHeader* geo;
-  TabD* tab;
-  double* rowd;    // [na][NROWD]
-  double* kernd;   // [n_tr][na][NDIR + 1]
-  double* part;    // [n_split][n_cls][n_ell][NDIR + 1] partial sums over a
-  double* cl;      // [n_cls][n_ell] (may be NULL)
-  double* jac;     // [n_cls][n_ell][NDIR]
-};
-
-// Uniform form: one geometry, per-item pointers from strides.  Listed form:
-// items[] (ragged requests), sizes below are the maxima over the items.
-struct GradBatch {
-  int n_items;
-  int listed;
-  const GradItem* items;
-  const double* params;
-  const GeoHeader* geo;
-  TabD* tab;
-  double* rowd;
-  double* kernd;
-  double* part;
-  double* cl;
-  double* jac;
-  int na, n_tr, n_cls, n_ell, n_split;
-};
-
-__device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
-  if (gb.listed) return gb.items[i];
-  GradItem r;
-  const size_t per = (size_t)gb.n_cls * gb.n_ell;
-  r.params = gb.params + 8 * (size_t)i;
-  r.geo = gb.geo;
-  r.tab = gb.tab + i;
-  r.rowd = gb.rowd + (size_t)i * gb.na * NROWD;
-  r.kernd = gb.kernd + (size_t)i * gb.n_tr * gb.na * (NDIR + 1);
-  r.part = gb.part + (size_t)i * gb.n_split * per * (NDIR + 1);
-  r.cl = gb.cl ? gb.cl + (size_t)i * per : nullptr;
-  r.jac = gb.jac + (size_t)i * per * NDIR;
-  return r;
-}
-
-typedef Dual<1> D1;
-typedef Dual<NDIR> D8;
-
-__device__ __forceinline__ D1 mk1(double v, double d) {
-  D1 r;
-  r.v = v;
-  r.d[0] = d;
-  return r;
-}
 
 // interpolation (scipy/interpolate.py:55-59) with a dual table fp
 __device__ __forceinline__ D1 interp_d1(double x, const double* xp, const double* fv, const double* fd,
@@ -451,10 +368,50 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
   const D1 dchi = dchioverdaT(bg, a, lna);
   outv[A_U] = WS[n] * dchi / xfmax(chi * chi, 1.0) / C2_G;
   if (lane < NDIR) {
-    double* row = gi.rowd + (size_t)n * NROWD;
-    for (int i = 0; i < NA_IN; ++i) {
-      if (dir == 0) row[i] = outv[i].v;
-      row[NA_IN * (1 + dir) + i] = outv[i].d[0];
+    if (gb.precision == JCG_FP64) {
+      double* row = gi.rowd + (size_t)n * NROWD;
+      for (int i = 0; i < NA_IN; ++i) {
+        if (dir == 0) row[i] = outv[i].v;
+        row[NA_IN * (1 + dir) + i] = outv[i].d[0];
+      }
+    } else {
+      // FP32 row: values in the forward row's units, tangents of the inputs
+      constexpr double LOG2E = 1.4426950408889634;
+      float* row = gi.rowg + (size_t)n * NROWG;
+      const D1 chic = outv[A_CHIC], kn = outv[A_KNL];
+      const D1 d2fac = outv[A_G] * outv[A_G] * sD[S_PKNORM] / TWO_PI2_G;
+      if (dir == 0) {
+        row[F_INVCHI] = (float)(1.0 / chic.v);
+        row[F_LG2INVCHI] = (float)(-log2(chic.v));
+        row[F_CHIC] = (float)chic.v;
+        row[F_LG2KNL] = (float)log2(kn.v);
+        row[F_INVKNL] = (float)(1.0 / kn.v);
+        row[F_D2FAC] = (float)d2fac.v;
+        row[F_BETAN] = (float)outv[A_BETA].v;
+        row[F_ALPHAN] = (float)outv[A_ALPHA].v;
+        row[F_AN] = (float)outv[A_AN].v;
+        row[F_3F1] = (float)(3.0 * outv[A_F1].v);
+        row[F_F2] = (float)outv[A_F2].v;
+        row[F_BN] = (float)outv[A_BN].v;
+        row[F_LG2CF3] = (float)(LOG2E * outv[A_LCF3].v);
+        row[F_3MGAMMA] = (float)(3.0 - outv[A_GAM].v);
+        row[F_NUN] = (float)outv[A_NU].v;
+        row[F_U] = (float)outv[A_U].v;
+      }
+      float* tg = row + NROW32;
+      tg[T_CHIC * NDIR + dir] = (float)chic.d[0];
+      tg[T_D2FAC * NDIR + dir] = (float)d2fac.d[0];
+      tg[T_KNL * NDIR + dir] = (float)kn.d[0];
+      tg[T_BETAN * NDIR + dir] = (float)outv[A_BETA].d[0];
+      tg[T_ALPHAN * NDIR + dir] = (float)outv[A_ALPHA].d[0];
+      tg[T_AN * NDIR + dir] = (float)outv[A_AN].d[0];
+      tg[T_3F1 * NDIR + dir] = (float)(3.0 * outv[A_F1].d[0]);
+      tg[T_F2 * NDIR + dir] = (float)outv[A_F2].d[0];
+      tg[T_BN * NDIR + dir] = (float)outv[A_BN].d[0];
+      tg[T_LG2CF3 * NDIR + dir] = (float)(LOG2E * outv[A_LCF3].d[0]);
+      tg[T_3MG * NDIR + dir] = (float)(-outv[A_GAM].d[0]);
+      tg[T_NUN * NDIR + dir] = (float)outv[A_NU].d[0];
+      tg[T_U * NDIR + dir] = (float)outv[A_U].d[0];
     }
   }
 }
@@ -887,12 +844,17 @@ void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
   grad_tables_kernel<<<gb.n_items, 256, smt, st>>>(gb, c);
   dim3 gr((gb.na + 7) / 8, gb.n_items);
   grad_rows_kernel<<<gr, 256, 0, st>>>(gb, c);
-  grad_kern_kernel<<<gr, 256, 0, st>>>(gb, c);
-  const int lt = grad_limber_tile(gb.n_ell, gb.n_cls);
-  const size_t sml = grad_limber_smem(gb.n_cls, lt);
-  cudaFuncSetAttribute(grad_limber_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sml);
-  dim3 gl((gb.n_ell + lt - 1) / lt, gb.n_split, gb.n_items);
-  grad_limber_kernel<<<gl, GL_THREADS, sml, st>>>(gb, c, lt);
+  if (gb.precision == JCG_FP32C) {
+    launch_grad_kern32(gb, c, st);
+    launch_grad_limber32(gb, c, st);
+  } else {
+    grad_kern_kernel<<<gr, 256, 0, st>>>(gb, c);
+    const int lt = grad_limber_tile(gb.n_ell, gb.n_cls);
+    const size_t sml = grad_limber_smem(gb.n_cls, lt);
+    cudaFuncSetAttribute(grad_limber_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sml);
+    dim3 gl((gb.n_ell + lt - 1) / lt, gb.n_split, gb.n_items);
+    grad_limber_kernel<<<gl, GL_THREADS, sml, st>>>(gb, c, lt);
+  }
   const size_t per = (size_t)gb.n_cls * gb.n_ell;
   size_t bx = (per + 255) / 256;
   const size_t cap = (152 * 16 + gb.n_items - 1) / gb.n_items;
@@ -906,13 +868,24 @@ size_t grad_tab_bytes() { return sizeof(TabD); }
 
 namespace jcg {
 
+// ell tile and a-chunk of the Limber Jacobian kernel of each precision
+int grad_tile(int precision, int n_ell, int n_cls) {
+  if (precision == JCG_FP32C) return grad_limber32_tile(n_ell, n_cls);
+  return grad_limber_tile(n_ell, n_cls);
+}
+
+static int grad_chunk(int precision, int n_cls) {
+  return precision == JCG_FP32C ? grad_limber32_chunk(n_cls) : GL_TA;
+}
+
 // a-splits of the Limber Jacobian: enough CTAs to fill the GPU for small batches
-int grad_n_split(const GeoHeader& h, int n_cosmo) {
-  const int lt = grad_limber_tile(h.n_ell, h.n_cls);
+int grad_n_split(const GeoHeader& h, int n_cosmo, int precision) {
+  const int lt = grad_tile(precision, h.n_ell, h.n_cls);
   const int tiles = (h.n_ell + lt - 1) / lt;
   const int ctas = tiles * n_cosmo;
   int ns = (2 * 152 + ctas - 1) / ctas;
-  const int max_ns = (h.na + GL_TA - 1) / GL_TA;
+  const int ta = grad_chunk(precision, h.n_cls);
+  const int max_ns = (h.na + ta - 1) / ta;
   if (ns > max_ns) ns = max_ns;
   if (ns < 1) ns = 1;
   return ns;
@@ -920,29 +893,47 @@ int grad_n_split(const GeoHeader& h, int n_cosmo) {
 
 static size_t al256(size_t v) { return (v + 255) & ~size_t(255); }
 
-size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo) {
-  const int ns = grad_n_split(h, n_cosmo);
+// per-cosmology row and kernel sections of one precision
+static size_t rows_bytes(const GeoHeader& h, int precision) {
+  return precision == JCG_FP32C ? al256(sizeof(float) * (size_t)h.na * NROWG)
+                                : al256(sizeof(double) * (size_t)h.na * NROWD);
+}
+static size_t kern_bytes(const GeoHeader& h, int precision) {
+  const size_t el = precision == JCG_FP32C ? sizeof(float) : sizeof(double);
+  return al256(el * (size_t)h.n_tr * h.na * (NDIR + 1));
+}
+
+size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
+  const int ns = grad_n_split(h, n_cosmo, precision);
+  GeoHeader hb = h;
+  hb.na = h.na * n_cosmo;  // the uniform form keeps the sections batch-contiguous
   size_t o = al256(sizeof(TabD) * (size_t)n_cosmo);
-  o += al256(sizeof(double) * (size_t)n_cosmo * h.na * NROWD);
-  o += al256(sizeof(double) * (size_t)n_cosmo * h.n_tr * h.na * (NDIR + 1));
+  o += rows_bytes(hb, precision);
+  o += kern_bytes(hb, precision);
   o += al256(sizeof(double) * (size_t)ns * n_cosmo * h.n_cls * h.n_ell * (NDIR + 1));
   return o;
 }
 
-void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, double* cl,
-              double* jac, void* ws, const ConstTables* c, cudaStream_t st) {
+void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, int precision,
+              double* cl, double* jac, void* ws, const ConstTables* c, cudaStream_t st) {
   GradBatch gb;
+  memset(&gb, 0, sizeof(gb));
   gb.n_items = n_cosmo;
+  gb.precision = precision;
   gb.params = params;
   gb.geo = geo;
+  GeoHeader hb = h;
+  hb.na = h.na * n_cosmo;
   char* base = static_cast<char*>(ws);
   size_t o = 0;
   gb.tab = reinterpret_cast<TabD*>(base + o);
   o += al256(sizeof(TabD) * (size_t)n_cosmo);
-  gb.rowd = reinterpret_cast<double*>(base + o);
-  o += al256(sizeof(double) * (size_t)n_cosmo * h.na * NROWD);
-  gb.kernd = reinterpret_cast<double*>(base + o);
-  o += al256(sizeof(double) * (size_t)n_cosmo * h.n_tr * h.na * (NDIR + 1));
+  if (precision == JCG_FP32C) gb.rowg = reinterpret_cast<float*>(base + o);
+  else gb.rowd = reinterpret_cast<double*>(base + o);
+  o += rows_bytes(hb, precision);
+  if (precision == JCG_FP32C) gb.kernf = reinterpret_cast<float*>(base + o);
+  else gb.kernd = reinterpret_cast<double*>(base + o);
+  o += kern_bytes(hb, precision);
   gb.part = reinterpret_cast<double*>(base + o);
   gb.cl = cl;
   gb.jac = jac;
@@ -950,7 +941,7 @@ void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, in
   gb.n_tr = h.n_tr;
   gb.n_cls = h.n_cls;
   gb.n_ell = h.n_ell;
-  gb.n_split = grad_n_split(h, n_cosmo);
+  gb.n_split = grad_n_split(h, n_cosmo, precision);
   gb.listed = 0;
   gb.items = nullptr;
   launch_grad(gb, c, st);
@@ -960,40 +951,41 @@ void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, in
 // Listed form: every request has its own geometry; the workspace holds the
 // GradItem array, then per request its tables, rows, kernels, a-split partial
 // sums and (when the caller gave none) its C_ell and Jacobian.
-static size_t grad_item_bytes(const GeoHeader& h, int n_split, bool own_cl, bool own_jac) {
+static size_t grad_item_bytes(const GeoHeader& h, int n_split, bool own_cl, bool own_jac, int precision) {
   const size_t per = (size_t)h.n_cls * h.n_ell;
   size_t o = al256(sizeof(TabD));
-  o += al256(sizeof(double) * (size_t)h.na * NROWD);
-  o += al256(sizeof(double) * (size_t)h.n_tr * h.na * (NDIR + 1));
+  o += rows_bytes(h, precision);
+  o += kern_bytes(h, precision);
   o += al256(sizeof(double) * (size_t)n_split * per * (NDIR + 1));
   if (own_cl) o += al256(sizeof(double) * per);
   if (own_jac) o += al256(sizeof(double) * per * NDIR);
   return o;
 }
 
-int grad_listed_auto_split(const GradReq* r, int n) {
+int grad_listed_auto_split(const GradReq* r, int n, int precision) {
   int max_ell = 0, max_cls = 0, min_na = 1 << 30;
   for (int i = 0; i < n; ++i) {
     max_ell = max(max_ell, r[i].h->n_ell);
     max_cls = max(max_cls, r[i].h->n_cls);
     min_na = min(min_na, r[i].h->na);
   }
-  const int lt = grad_limber_tile(max_ell, max_cls);
+  const int lt = grad_tile(precision, max_ell, max_cls);
   long ctas = 0;
   for (int i = 0; i < n; ++i) ctas += (r[i].h->n_ell + lt - 1) / lt;
   int ns = (int)((2 * 152 + ctas - 1) / ctas);
-  const int max_ns = (min_na + GL_TA - 1) / GL_TA;
+  const int ta = grad_chunk(precision, max_cls);
+  const int max_ns = (min_na + ta - 1) / ta;
   if (ns > max_ns) ns = max_ns;
   return ns < 1 ? 1 : ns;
 }
 
-size_t grad_listed_bytes(const GradReq* r, int n, int n_split) {
+size_t grad_listed_bytes(const GradReq* r, int n, int n_split, int precision) {
   size_t o = al256(sizeof(GradItem) * (size_t)n);
-  for (int i = 0; i < n; ++i) o += grad_item_bytes(*r[i].h, n_split, !r[i].cl, !r[i].jac);
+  for (int i = 0; i < n; ++i) o += grad_item_bytes(*r[i].h, n_split, !r[i].cl, !r[i].jac, precision);
   return o;
 }
 
-cudaError_t grad_run_listed(GradReq* r, int n, int n_split, void* ws, const ConstTables* c,
+cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void* ws, const ConstTables* c,
                             cudaStream_t st) {
   static thread_local std::vector<GradItem> host;
   host.resize(n);
@@ -1006,14 +998,17 @@ cudaError_t grad_run_listed(GradReq* r, int n, int n_split, void* ws, const Cons
     const GeoHeader& h = *r[i].h;
     const size_t per = (size_t)h.n_cls * h.n_ell;
     GradItem& it = host[i];
+    memset(&it, 0, sizeof(it));
     it.params = r[i].params;
     it.geo = r[i].geo;
     it.tab = reinterpret_cast<TabD*>(base + o);
     o += al256(sizeof(TabD));
-    it.rowd = reinterpret_cast<double*>(base + o);
-    o += al256(sizeof(double) * (size_t)h.na * NROWD);
-    it.kernd = reinterpret_cast<double*>(base + o);
-    o += al256(sizeof(double) * (size_t)h.n_tr * h.na * (NDIR + 1));
+    if (precision == JCG_FP32C) it.rowg = reinterpret_cast<float*>(base + o);
+    else it.rowd = reinterpret_cast<double*>(base + o);
+    o += rows_bytes(h, precision);
+    if (precision == JCG_FP32C) it.kernf = reinterpret_cast<float*>(base + o);
+    else it.kernd = reinterpret_cast<double*>(base + o);
+    o += kern_bytes(h, precision);
     it.part = reinterpret_cast<double*>(base + o);
     o += al256(sizeof(double) * (size_t)n_split * per * (NDIR + 1));
     if (!r[i].cl) {
@@ -1038,6 +1033,7 @@ cudaError_t grad_run_listed(GradReq* r, int n, int n_split, void* ws, const Cons
   if (e != cudaSuccess) return e;
   gb.n_items = n;
   gb.listed = 1;
+  gb.precision = precision;
   gb.items = dev_items;
   gb.n_split = n_split;
   launch_grad(gb, c, st);

@@ -1,0 +1,118 @@
+// Shared definitions of the Jacobian kernels (jcg_grad.cu: FP64 and the
+// common stages; jcg_grad32.cu: the FP32 compensated Limber and lensing stages).
+#pragma once
+
+#include "jcg_dual.cuh"
+
+namespace jcg {
+
+typedef Dual<1> D1;
+typedef Dual<NDIR> D8;
+
+__device__ __forceinline__ D1 mk1(double v, double d) {
+  D1 r;
+  r.v = v;
+  r.d[0] = d;
+  return r;
+}
+
+constexpr double TWO_PI2_G = 2.0 * (PI * PI);
+constexpr double C2_G = C_KMS * C_KMS;
+constexpr double LN10_G = 2.302585092994046;
+
+// ------------------------------------------------------------ dual tables ---
+struct TabD {
+  double sv[NSCAL];
+  double sd[NDIR][NSCAL];
+  double chiv[NCHI];
+  double chid[NDIR][NCHI];
+  double gv[NGROW];
+  double gd[NDIR][NGROW];
+  double sigv[NRT];
+  double sigd[NDIR][NRT];
+  double pk3v[NKH];
+  double pk3d[NDIR][NKH];
+  double pad[7];
+};
+static_assert(sizeof(TabD) % 64 == 0, "TabD alignment");
+
+// per-node inputs of the Limber integrand (node_fb), value + 8 tangents
+enum NodeA { A_CHIC = 0, A_G, A_KNL, A_BETA, A_ALPHA, A_AN, A_BN, A_LCF3, A_F1, A_F2, A_GAM, A_NU, A_U, NA_IN };
+constexpr int NROWD = NA_IN * (NDIR + 1);  // [NA_IN] values then [NDIR][NA_IN] tangents
+// per-cosmology inputs of the integrand
+enum NodeC { C_KEQ = 0, C_SH, C_BETAC, C_ALPHAC, C_ALPHAB, C_BETAB, C_BETANODE, C_KSILK, C_FB, C_FC, C_NS, C_PKNORM, NC_IN };
+__device__ __constant__ const int kNodeCScalar[NC_IN] = {S_K_EQ,  S_SH_D,      S_BETA_C,  S_ALPHA_C,
+                                                         S_ALPHA_B, S_BETA_B, S_BETA_NODE, S_K_SILK,
+                                                         S_FB,    S_FC,        S_NS,      S_PKNORM};
+
+// FP32 rows of the compensated Limber Jacobian, per node: the 16 values of
+// the forward FP32 row (Row32 order, slot 15 = the Limber weight u), then the
+// tangents [NGT][NDIR] of the independent inputs below (chi_c and k_nl raw,
+// the others in the units of their Row32 slot).
+enum GTan { T_CHIC = 0, T_D2FAC, T_KNL, T_BETAN, T_ALPHAN, T_AN, T_3F1, T_F2, T_BN, T_LG2CF3, T_3MG,
+            T_NUN, T_U, NGT };
+constexpr int F_U = 15;
+constexpr int NROWG = NROW32 + NGT * NDIR;  // 120 floats
+// per-cosmology Eisenstein-Hu inputs of the FP32 integrand with tangents
+enum ETan { E_KEQ = 0, E_SH, E_C18BC, E_C142AC, E_ALPHAB, E_BETAB, E_BETANODE, E_LG2KSILK, E_FB, E_FC,
+            E_NS3, NET };
+
+// One (cosmology, geometry) pair of a Jacobian batch.  FP64: rowd / kernd;
+// FP32C: rowg / kernf.
+struct GradItem {
+  const double* params;   // 8 parameters
+  const GeoHeader* geo;
+  TabD* tab;
+  double* rowd;    // [na][NROWD]
+  double* kernd;   // [n_tr][na][NDIR + 1]
+  float* rowg;     // [na][NROWG]
+  float* kernf;    // [n_tr][na][NDIR + 1]
+  double* part;    // [n_split][n_cls][n_ell][NDIR + 1] partial sums over a
+  double* cl;      // [n_cls][n_ell] (may be NULL)
+  double* jac;     // [n_cls][n_ell][NDIR]
+};
+
+// Uniform form: one geometry, per-item pointers from strides.  Listed form:
+// items[] (ragged requests), sizes below are the maxima over the items.
+struct GradBatch {
+  int n_items;
+  int listed;
+  int precision;
+  const GradItem* items;
+  const double* params;
+  const GeoHeader* geo;
+  TabD* tab;
+  double* rowd;
+  double* kernd;
+  float* rowg;
+  float* kernf;
+  double* part;
+  double* cl;
+  double* jac;
+  int na, n_tr, n_cls, n_ell, n_split;
+};
+
+__device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
+  if (gb.listed) return gb.items[i];
+  GradItem r;
+  const size_t per = (size_t)gb.n_cls * gb.n_ell;
+  r.params = gb.params + 8 * (size_t)i;
+  r.geo = gb.geo;
+  r.tab = gb.tab + i;
+  r.rowd = gb.rowd ? gb.rowd + (size_t)i * gb.na * NROWD : nullptr;
+  r.kernd = gb.kernd ? gb.kernd + (size_t)i * gb.n_tr * gb.na * (NDIR + 1) : nullptr;
+  r.rowg = gb.rowg ? gb.rowg + (size_t)i * gb.na * NROWG : nullptr;
+  r.kernf = gb.kernf ? gb.kernf + (size_t)i * gb.n_tr * gb.na * (NDIR + 1) : nullptr;
+  r.part = gb.part + (size_t)i * gb.n_split * per * (NDIR + 1);
+  r.cl = gb.cl ? gb.cl + (size_t)i * per : nullptr;
+  r.jac = gb.jac + (size_t)i * per * NDIR;
+  return r;
+}
+
+// FP32 compensated stages (jcg_grad32.cu)
+void launch_grad_kern32(const GradBatch& gb, const ConstTables* c, cudaStream_t st);
+void launch_grad_limber32(const GradBatch& gb, const ConstTables* c, cudaStream_t st);
+int grad_limber32_tile(int n_ell, int n_cls);
+int grad_limber32_chunk(int n_cls);
+
+}  // namespace jcg

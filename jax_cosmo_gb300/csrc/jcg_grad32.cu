@@ -1,0 +1,614 @@
+// FP32 compensated ("fp32c") stages of the Jacobian dC_ell/dtheta: the radial
+// kernels with tangents and the Limber integrand with its reverse sweep.
+//
+// The tables, halofit rows and their tangents come from the FP64 stages
+// (jcg_grad.cu) -- background ODEs, sigma8, the root find and the spectral
+// moments stay in float64 -- and are handed over as FP32 rows (GTan layout,
+// jcg_grad.cuh).  Here, per Limber node (cosmology, ell, a):
+//
+//   P(k, a)           Eisenstein-Hu x primordial x takahashi2012 in FP32 with
+//                     MUFU ex2/lg2/rcp/sin/cos (the forward fp32c integrand);
+//   dP/d(inputs)      hand-written reverse sweep of the same operations;
+//   dP/dtheta         the adjoints contracted with the inputs' tangents;
+//   C, dC/dtheta      sum_a [P M, dP M + P dM] in FP32 per chunk of a nodes,
+//                     chunks added with Kahan compensation, then FP64.
+#include "jcg_fp32.cuh"
+#include "jcg_grad.cuh"
+
+namespace jcg {
+
+// ---------------------------------------------------------- radial kernels --
+// One warp per node, lanes over the 257 lensing z' points, four tracers per
+// pass.  Lensing efficiency (probes.py:44-51) with tangents:
+//   r_j = max(chi'_j - chi, 0) / max(chi'_j, 1)
+//   dr_j = ic_j (dchi'_j (1 - r_j [chi'_j > 1]) - dchi)  where chi'_j > chi
+// accumulated as sum W r, sum W ic, sum W ic (1 - r) dchi'.
+constexpr int GK_NODES = 64;  // nodes per CTA (8 warps x 8)
+
+__global__ void __launch_bounds__(256) grad_kern32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+  const int item = blockIdx.y;
+  if (item >= gb.n_items) return;
+  const GradItem gi = grad_item(gb, item);
+  const GeoHeader* geo = gi.geo;
+  const int na = geo->na, n_tr = geo->n_tr;
+  const int n0 = blockIdx.x * GK_NODES;
+  if (n0 >= na) return;
+  __shared__ float chi[NCHI], slope[NCHI];
+  __shared__ float dchi[NDIR][NCHI], dslope[NDIR][NCHI];
+  const TabD* tb = gi.tab;
+  for (int i = threadIdx.x; i < NCHI; i += blockDim.x) {
+    chi[i] = (float)tb->chiv[i];
+    double sl = 0.0;
+    if (i + 1 < NCHI) sl = (tb->chiv[i + 1] - tb->chiv[i]) / (c->atab_chi[i + 1] - c->atab_chi[i]);
+    slope[i] = (float)sl;
+  }
+  for (int e = threadIdx.x; e < NDIR * NCHI; e += blockDim.x) {
+    const int d = e / NCHI, i = e % NCHI;
+    dchi[d][i] = (float)tb->chid[d][i];
+    double sl = 0.0;
+    if (i + 1 < NCHI) sl = (tb->chid[d][i + 1] - tb->chid[d][i]) / (c->atab_chi[i + 1] - c->atab_chi[i]);
+    dslope[d][i] = (float)sl;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double* Z = geo_ptr<double>(geo, geo->off_z);
+  const double* AWL = geo_ptr<double>(geo, geo->off_awl);
+  const int32_t* QWL = geo_ptr<int32_t>(geo, geo->off_qwl32);
+  const float* DXWL = geo_ptr<float>(geo, geo->off_dxwl32);
+  const double* NZL = geo_ptr<double>(geo, geo->off_nzl);
+  const int dir = lane & 7;
+  const double om = tb->sv[S_OMEGA_M], dom = tb->sd[dir][S_OMEGA_M];
+  const double cf = 3.0 * (H0 * H0) * om / 2.0 / C_KMS;  // probes.py:71
+  const double dcf = cf * dom / om;
+  const int n_end = min(na, n0 + GK_NODES);
+  for (int n = n0 + warp; n < n_end; n += 8) {
+    const int qw = QWL[n];
+    const int xw = qw & 0xffff, mw = qw >> 16;
+    const float craw_w = chi[xw] + slope[mw] * DXWL[n];
+    const float chi_wl = fmaxf(craw_w, 0.f);
+    float dchi_wl[NDIR];
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) dchi_wl[d] = craw_w > 0.f ? dchi[d][xw] + dslope[d][mw] * DXWL[n] : 0.f;
+    const double z = Z[n];
+    for (int t0 = 0; t0 < n_tr; t0 += 4) {
+      int tl[4];
+      int cnt = 0;
+      for (int t = t0; t < min(t0 + 4, n_tr); ++t) tl[cnt++] = t;
+      float av[4], at[4], ad[4][NDIR];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        av[u] = 0.f;
+        at[u] = 0.f;
+#pragma unroll
+        for (int d = 0; d < NDIR; ++d) ad[u][d] = 0.f;
+      }
+      bool any_wl = false;
+      for (int u = 0; u < cnt; ++u) any_wl |= geo->kind[tl[u]] == JCG_TRACER_WL;
+      if (any_wl) {
+        for (int g = 0; g < geo->n_groups; ++g) {
+          const size_t row = (size_t)n * NZP;
+          const int32_t* Q32 = geo_ptr<int32_t>(geo, geo->off_q32[g]) + row;
+          const float* DX32 = geo_ptr<float>(geo, geo->off_dx32[g]) + row;
+          const float* W[4];
+          bool on[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            on[u] = u < cnt && geo->kind[tl[u]] == JCG_TRACER_WL && geo->group[tl[u]] == g;
+            W[u] = on[u] ? geo_ptr<float>(geo, geo->off_W32[tl[u]]) + row : nullptr;
+          }
+          if (!(on[0] || on[1] || on[2] || on[3])) continue;
+          for (int j = lane; j < NZP; j += 32) {
+            const int q = Q32[j];
+            const int x = q & 0xffff, m = q >> 16;
+            const float dx = DX32[j];
+            const float craw = chi[x] + slope[m] * dx;
+            const float chip = fmaxf(craw, 0.f);
+            const float diff = chip - chi_wl;
+            if (!(diff > 0.f)) continue;
+            const float ic = rcpf(fmaxf(chip, 1.f));
+            const float r = diff * ic;
+            const float h = chip > 1.f ? ic * (1.f - r) : ic;
+            float dcp[NDIR];
+#pragma unroll
+            for (int d = 0; d < NDIR; ++d) dcp[d] = craw > 0.f ? (dchi[d][x] + dslope[d][m] * dx) * h : 0.f;
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+              if (on[u]) {
+                const float w = W[u][j];
+                av[u] = fmaf(w, r, av[u]);
+                at[u] = fmaf(w, ic, at[u]);
+#pragma unroll
+                for (int d = 0; d < NDIR; ++d) ad[u][d] = fmaf(w, dcp[d], ad[u][d]);
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            av[u] += __shfl_xor_sync(0xffffffffu, av[u], o);
+            at[u] += __shfl_xor_sync(0xffffffffu, at[u], o);
+#pragma unroll
+            for (int d = 0; d < NDIR; ++d) ad[u][d] += __shfl_xor_sync(0xffffffffu, ad[u][d], o);
+          }
+        }
+      }
+      if (lane < NDIR) {
+        for (int u = 0; u < cnt; ++u) {
+          const int t = tl[u];
+          double kv, kd;
+          if (geo->kind[t] == JCG_TRACER_WL) {
+            float adir = 0.f, dcw = 0.f;
+#pragma unroll
+            for (int d = 0; d < NDIR; ++d)
+              if (d == dir) {
+                adir = ad[u][d];
+                dcw = dchi_wl[d];
+              }
+            const double fac = (1.0 + z) * (1.0 + geo->mult[t]);
+            const double acc = av[u], cw = chi_wl;
+            kv = cf * fac * cw * acc;
+            kd = fac * (dcf * cw * acc + cf * (double)dcw * acc +
+                        cf * cw * ((double)adir - (double)dcw * (double)at[u]));
+          } else {
+            D1 sD[NSCAL];
+            for (int i = 0; i < NSCAL; ++i) sD[i] = mk1(tb->sv[i], tb->sd[dir][i]);
+            const BgT<D1> bg = make_bgT(sD);
+            const double awl = AWL[n];
+            const D1 H = H0 * xsqrt(esqrT(bg, awl, log(awl), (D1*)nullptr));
+            const double w = NZL[(size_t)t * na + n] * geo->bias[t];
+            kv = w * H.v;
+            kd = w * H.d[0];
+          }
+          float* dst = gi.kernf + ((size_t)t * na + n) * (NDIR + 1);
+          if (dir == 0) dst[0] = (float)kv;
+          dst[1 + dir] = (float)kd;
+        }
+      }
+    }
+  }
+}
+
+void launch_grad_kern32(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
+  dim3 grid((gb.na + GK_NODES - 1) / GK_NODES, gb.n_items);
+  grad_kern32_kernel<<<grid, 256, 0, st>>>(gb, c);
+}
+
+// ---------------------------------------------------------- Limber adjoint --
+// Per-cosmology Eisenstein-Hu inputs of the FP32 integrand.
+struct EHg {
+  float qinv, lg2_qinv, sh, inv_sh, c18bc, c142ac, alpha_b, beta_b, beta_node, lg2_ksilk, fb, fc, ns3,
+      inv_keq;
+};
+
+// P of node32 (the forward fp32c integrand) and its reverse sweep.  an[GTan]
+// (T_CHIC..T_NUN) and ae[ETan] receive dP/d(input) in the units of the
+// stored tangents.
+__device__ __forceinline__ float node32_fb(const EHg& e, const float* r, float kh, float lg2kh, float invkh,
+                                           float* an, float* ae) {
+  // ---- forward (same operations as node32)
+  const float k = kh * r[F_INVCHI];
+  const float lk = lg2kh + r[F_LG2INVCHI];
+  const float invk = invkh * r[F_CHIC];
+  const float q = k * e.qinv;
+  const float lq = lk + e.lg2_qinv;
+  const float q108 = ex2f(1.08f * lq);
+  const float rden_c = rcpf(1.f + 69.9f * q108);
+  const float Cb = 386.f * rden_c;
+  const float A1 = E_F + e.c18bc * q;
+  const float A2 = E_F + 1.8f * q;
+  const float L1 = LN2_F * lg2f(A1);
+  const float L2 = LN2_F * lg2f(A2);
+  const float qq = q * q;
+  const float cA = 14.2f + Cb, cB = e.c142ac + Cb;
+  const float rDa = rcpf(L1 + cA * qq), rDb = rcpf(L1 + cB * qq), rDn = rcpf(L2 + cA * qq);
+  const float Ta = L1 * rDa, Tb = L1 * rDb, Tn = L2 * rDn;
+  const float ks = k * e.sh;
+  const float x54 = ks * (1.f / 5.4f);
+  const float x54_2 = x54 * x54;
+  const float f = rcpf(1.f + x54_2 * x54_2);
+  const float Tc = f * Ta + (1.f - f) * Tb;
+  const float iks = invk * e.inv_sh;
+  const float x52 = ks * (1.f / 5.2f);
+  const float rE52 = rcpf(1.f + x52 * x52);
+  const float bb = e.beta_b * iks;
+  const float rBb = rcpf(1.f + bb * bb * bb);
+  const float ex1 = ex2f(1.4f * (lk - e.lg2_ksilk));
+  const float silk = ex2f(-LOG2E_F * ex1);
+  const float bn = e.beta_node * iks;
+  const float B3 = 1.f + bn * bn * bn;
+  const float cbi = ex2f((-1.f / 3.f) * lg2f(B3));
+  const float st = e.sh * cbi;
+  const float arg = k * st;
+  float sn, cs;
+  sincos_reduced(arg, &sn, &cs);
+  const float rarg = rcpf(arg);
+  const float sinc = sn * rarg;
+  const float Tbr0 = Tn * rE52 + e.alpha_b * rBb * silk;
+  const float Tbar = Tbr0 * sinc;
+  const float T = e.fb * Tbar + e.fc * Tc;
+  const float eP = ex2f(e.ns3 * lk);
+  const float T2 = T * T;
+  const float d2l = eP * T2 * r[F_D2FAC];
+  const float y = k * r[F_INVKNL];
+  const float ly = lk - r[F_LG2KNL];
+  const float efy = ex2f(-LOG2E_F * (y * (0.25f + 0.125f * y)));
+  const float lg1 = lg2f(1.f + d2l);
+  const float pb = ex2f(r[F_BETAN] * lg1);
+  const float rden_a = rcpf(1.f + r[F_ALPHAN] * d2l);
+  const float Q = pb * rden_a * efy;
+  const float d2q = d2l * Q;
+  const float H1 = ex2f(r[F_3F1] * ly);
+  const float H2 = ex2f(r[F_F2] * ly);
+  const float E3b = r[F_LG2CF3] + ly;
+  const float H3 = ex2f(r[F_3MGAMMA] * E3b);
+  const float rD = rcpf(1.f + r[F_BN] * H2 + H3);
+  const float d2hp = r[F_AN] * H1 * rD;
+  const float y2 = y * y;
+  const float ryn = rcpf(y2 + r[F_NUN]);
+  const float Rr = y2 * ryn;
+  const float d2h = d2hp * Rr;
+  const float S = d2q + d2h;
+  const float ik3 = invk * invk * invk;
+  const float P = TWO_PI2_F * ik3 * S;
+  // ---- reverse, seed dP/dP = 1
+  const float Sb = TWO_PI2_F * ik3;
+  float invkb = TWO_PI2_F * S * 3.f * invk * invk;
+  // d2h = d2hp y^2 / (y^2 + nu)
+  const float d2hpb = Sb * Rr;
+  const float Rrb = Sb * d2hp;
+  const float y2b = Rrb * ryn * (1.f - Rr);
+  const float NUNb = -Rrb * Rr * ryn;
+  float yb = 2.f * y * y2b;
+  const float ANb = d2hpb * H1 * rD;
+  const float H1b = d2hpb * r[F_AN] * rD;
+  const float Dbar = -d2hpb * d2hp * rD;
+  const float BNb = Dbar * H2;
+  const float H2b = Dbar * r[F_BN];
+  const float u1 = H1b * H1 * LN2_F, u2 = H2b * H2 * LN2_F, u3 = Dbar * H3 * LN2_F;
+  const float F3F1b = u1 * ly, F2b = u2 * ly, F3MGb = u3 * E3b, LG2CF3b = u3 * r[F_3MGAMMA];
+  float lkb = u1 * r[F_3F1] + u2 * r[F_F2] + u3 * r[F_3MGAMMA];  // through ly
+  const float LG2KNLb = -lkb;
+  // d2q = d2l Q, Q = (1 + d2l)^beta / (1 + alpha d2l) exp(-f(y))
+  float d2lb = Sb * Q;
+  const float Qb = Sb * d2l;
+  const float pbb = Qb * rden_a * efy;
+  const float denab = -Qb * Q * rden_a;
+  const float efyb = Qb * pb * rden_a;
+  const float ALPHANb = denab * d2l;
+  d2lb += denab * r[F_ALPHAN];
+  const float vpb = pbb * pb * LN2_F;
+  const float BETANb = vpb * lg1;
+  d2lb += vpb * r[F_BETAN] * LOG2E_F * rcpf(1.f + d2l);
+  yb -= efyb * efy * (0.25f + 0.25f * y);
+  float kb = yb * r[F_INVKNL];
+  const float INVKNLb = yb * k;
+  // d2l = k^(ns+3) T^2 D2FAC
+  const float ePb = d2lb * T2 * r[F_D2FAC];
+  const float Tbv = d2lb * eP * 2.f * T * r[F_D2FAC];
+  const float D2FACb = d2lb * eP * T2;
+  const float vep = ePb * eP * LN2_F;
+  const float ns3b = vep * lk;
+  lkb += vep * e.ns3;
+  // T = fb Tbar + fc Tc
+  const float fbb = Tbv * Tbar, fcb = Tbv * Tc;
+  const float Tbarb = Tbv * e.fb, Tcb = Tbv * e.fc;
+  const float Tbr0b = Tbarb * sinc;
+  const float sincb = Tbarb * Tbr0;
+  float dsinc;
+  if (arg < 0.1f) {
+    const float a2 = arg * arg;
+    dsinc = arg * (-1.f / 3.f + a2 * (1.f / 30.f));
+  } else {
+    dsinc = (cs - sinc) * rarg;
+  }
+  const float argb = sincb * dsinc;
+  kb += argb * st;
+  const float stb = argb * k;
+  float shb = stb * cbi;
+  const float cbib = stb * e.sh;
+  const float B3b = cbib * (-1.f / 3.f) * cbi * rcpf(B3);
+  const float bnb = B3b * 3.f * bn * bn;
+  const float betanodeb = bnb * iks;
+  float iksb = bnb * e.beta_node;
+  const float Tnb = Tbr0b * rE52;
+  const float E52b = -Tbr0b * Tn * rE52 * rE52;
+  const float alphabb = Tbr0b * rBb * silk;
+  const float Bbb = -Tbr0b * e.alpha_b * silk * rBb * rBb;
+  const float silkb = Tbr0b * e.alpha_b * rBb;
+  const float vex = -silkb * silk * ex1 * LN2_F * 1.4f;
+  lkb += vex;
+  const float lg2ksilkb = -vex;
+  const float bbb = Bbb * 3.f * bb * bb;
+  const float betabb = bbb * iks;
+  iksb += bbb * e.beta_b;
+  float ksb = E52b * 2.f * x52 * (1.f / 5.2f);
+  invkb += iksb * e.inv_sh;
+  const float invshb = iksb * invk;
+  // Tc = f Ta + (1 - f) Tb, f = 1 / (1 + (ks / 5.4)^4)
+  const float fbar = Tcb * (Ta - Tb);
+  const float Tab = Tcb * f, Tbb = Tcb * (1.f - f);
+  ksb -= fbar * f * f * 4.f * x54_2 * x54 * (1.f / 5.4f);
+  kb += ksb * e.sh;
+  shb += ksb * k;
+  // Ta = L1 / (L1 + cA q^2), Tb = L1 / (L1 + cB q^2), Tn = L2 / (L2 + cA q^2)
+  const float Dab = -Tab * Ta * rDa, Dbb = -Tbb * Tb * rDb, Dnb = -Tnb * Tn * rDn;
+  const float L1b = Tab * rDa + Tbb * rDb + Dab + Dbb;
+  const float L2b = Tnb * rDn + Dnb;
+  const float cAb = (Dab + Dnb) * qq, cBb = Dbb * qq;
+  const float Cbb = cAb + cBb;
+  float qb = (Dab * cA + Dbb * cB + Dnb * cA) * 2.f * q;
+  const float A1b = L1b * rcpf(A1), A2b = L2b * rcpf(A2);
+  const float c18bcb = A1b * q;
+  qb += A1b * e.c18bc + A2b * 1.8f;
+  const float q108b = -Cbb * Cb * rden_c * 69.9f;
+  const float lqb = q108b * q108 * LN2_F * 1.08f;
+  lkb += lqb;
+  kb += qb * e.qinv;
+  const float qinvb = qb * k;
+  // k = kh INVCHI, lk = lg2 kh + LG2INVCHI, 1/k = CHIC / kh
+  const float INVCHIb = kb * kh, CHICb = invkb * invkh;
+  an[T_CHIC] = -INVCHIb * r[F_INVCHI] * r[F_INVCHI] - lkb * LOG2E_F * r[F_INVCHI] + CHICb;
+  an[T_D2FAC] = D2FACb;
+  an[T_KNL] = -INVKNLb * r[F_INVKNL] * r[F_INVKNL] + LG2KNLb * LOG2E_F * r[F_INVKNL];
+  an[T_BETAN] = BETANb;
+  an[T_ALPHAN] = ALPHANb;
+  an[T_AN] = ANb;
+  an[T_3F1] = F3F1b;
+  an[T_F2] = F2b;
+  an[T_BN] = BNb;
+  an[T_LG2CF3] = LG2CF3b;
+  an[T_3MG] = F3MGb;
+  an[T_NUN] = NUNb;
+  ae[E_KEQ] = -(qinvb * e.qinv + lqb * LOG2E_F) * e.inv_keq;
+  ae[E_SH] = shb - invshb * e.inv_sh * e.inv_sh;
+  ae[E_C18BC] = c18bcb;
+  ae[E_C142AC] = cBb;
+  ae[E_ALPHAB] = alphabb;
+  ae[E_BETAB] = betabb;
+  ae[E_BETANODE] = betanodeb;
+  ae[E_LG2KSILK] = lg2ksilkb;
+  ae[E_FB] = fbb;
+  ae[E_FC] = fcb;
+  ae[E_NS3] = ns3b;
+  return P;
+}
+
+constexpr int L32_THREADS = 256;
+constexpr int L32_G = 2;      // pairs per contraction unit
+constexpr int L32_MAXLT = 32;
+
+int grad_limber32_chunk(int n_cls) { return n_cls <= 64 ? 32 : 16; }
+
+int grad_limber32_tile(int n_ell, int n_cls) {
+  const int groups = (n_cls + L32_G - 1) / L32_G;
+  int lt = L32_THREADS / groups;
+  if (lt > L32_MAXLT) lt = L32_MAXLT;
+  if (lt < 1) lt = 1;
+  const int tiles = (n_ell + lt - 1) / lt;
+  return (n_ell + tiles - 1) / tiles;
+}
+
+static size_t limber32_smem_floats(int n_cls, int n_tr, int LT, int TA) {
+  return 128 + 128 + (size_t)TA * NROWG + (size_t)TA * n_tr * (NDIR + 1) + (size_t)TA * n_cls * (NDIR + 1) +
+         (size_t)TA * LT * (NDIR + 1);
+}
+
+// One CTA per (ell tile, a split, cosmology).
+//   phase K: the chunk's FP32 rows and kernels into shared memory;
+//   phase M: M_p(a) = u K_i K_j and its tangents;
+//   phase A: per (a, ell) P and dP/dtheta (reverse sweep + projection);
+//   phase B: per (ell, pair group) the 9 sums over the chunk, Kahan-added.
+__global__ void __launch_bounds__(L32_THREADS)
+    grad_limber32_kernel(GradBatch gb, const ConstTables* __restrict__ c, int LT, int TA) {
+  const int item = blockIdx.z, split = blockIdx.y;
+  if (item >= gb.n_items) return;
+  const GradItem gi = grad_item(gb, item);
+  const GeoHeader* geo = gi.geo;
+  const int n_ell = geo->n_ell, n_cls = geo->n_cls, na = geo->na, n_tr = geo->n_tr;
+  const int l0 = blockIdx.x * LT;
+  if (l0 >= n_ell) return;
+  const int lt = min(LT, n_ell - l0);
+  const int per = (na + gb.n_split - 1) / gb.n_split;
+  const int a_begin = split * per, a_end = min(na, a_begin + per);
+  extern __shared__ __align__(16) float sm32[];
+  float* ev = sm32;                                   // EHg values (14)
+  float* et = ev + 16;                                // [NET][NDIR] tangents
+  float* khv = sm32 + 128;                            // [32] l + 1/2
+  float* lkhv = khv + 32;                             // [32] log2(l + 1/2)
+  float* ikhv = lkhv + 32;                            // [32] 1 / (l + 1/2)
+  float* R = sm32 + 256;                              // [TA][NROWG]
+  float* Ks = R + (size_t)TA * NROWG;                 // [TA][n_tr][NDIR + 1]
+  float* Mv = Ks + (size_t)TA * n_tr * (NDIR + 1);    // [TA][n_cls]
+  float* Md = Mv + (size_t)TA * n_cls;                // [TA][n_cls][NDIR]
+  float* Pv = Md + (size_t)TA * n_cls * NDIR;         // [TA][LT]
+  float* Pd = Pv + (size_t)TA * LT;                   // [TA][NDIR][LT]
+  const int tid = threadIdx.x;
+  const TabD* tb = gi.tab;
+  if (tid < NDIR + 1) {
+    // tid 0: values; tid 1..8: tangents of direction tid - 1
+    const int d = tid - 1;
+    const double keq = tb->sv[S_K_EQ], sh = tb->sv[S_SH_D], bc = tb->sv[S_BETA_C], ac = tb->sv[S_ALPHA_C];
+    const double ks = tb->sv[S_K_SILK];
+    if (tid == 0) {
+      const double qinv = 1.0 / (13.41 * keq);
+      ev[0] = (float)qinv;
+      ev[1] = (float)log2(qinv);
+      ev[2] = (float)sh;
+      ev[3] = (float)(1.0 / sh);
+      ev[4] = (float)(1.8 * bc);
+      ev[5] = (float)(14.2 / ac);
+      ev[6] = (float)tb->sv[S_ALPHA_B];
+      ev[7] = (float)tb->sv[S_BETA_B];
+      ev[8] = (float)tb->sv[S_BETA_NODE];
+      ev[9] = (float)log2(ks);
+      ev[10] = (float)tb->sv[S_FB];
+      ev[11] = (float)tb->sv[S_FC];
+      ev[12] = (float)(tb->sv[S_NS] + 3.0);
+      ev[13] = (float)(1.0 / keq);
+    } else {
+      const double* sd = tb->sd[d];
+      et[E_KEQ * NDIR + d] = (float)sd[S_K_EQ];
+      et[E_SH * NDIR + d] = (float)sd[S_SH_D];
+      et[E_C18BC * NDIR + d] = (float)(1.8 * sd[S_BETA_C]);
+      et[E_C142AC * NDIR + d] = (float)(-14.2 * sd[S_ALPHA_C] / (ac * ac));
+      et[E_ALPHAB * NDIR + d] = (float)sd[S_ALPHA_B];
+      et[E_BETAB * NDIR + d] = (float)sd[S_BETA_B];
+      et[E_BETANODE * NDIR + d] = (float)sd[S_BETA_NODE];
+      et[E_LG2KSILK * NDIR + d] = (float)(sd[S_K_SILK] / (ks * 0.6931471805599453));
+      et[E_FB * NDIR + d] = (float)sd[S_FB];
+      et[E_FC * NDIR + d] = (float)sd[S_FC];
+      et[E_NS3 * NDIR + d] = (float)sd[S_NS];
+    }
+  }
+  const double* ELL = geo_ptr<double>(geo, geo->off_ell);
+  const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
+  for (int l = tid; l < lt; l += L32_THREADS) {
+    const double e = ELL[l0 + l] + 0.5;
+    khv[l] = (float)e;
+    lkhv[l] = (float)log2(e);
+    ikhv[l] = (float)(1.0 / e);
+  }
+  __syncthreads();
+  EHg eh;
+  eh.qinv = ev[0]; eh.lg2_qinv = ev[1]; eh.sh = ev[2]; eh.inv_sh = ev[3]; eh.c18bc = ev[4];
+  eh.c142ac = ev[5]; eh.alpha_b = ev[6]; eh.beta_b = ev[7]; eh.beta_node = ev[8]; eh.lg2_ksilk = ev[9];
+  eh.fb = ev[10]; eh.fc = ev[11]; eh.ns3 = ev[12]; eh.inv_keq = ev[13];
+  // contraction unit of this thread: ell l_u, pairs [p0, p1)
+  const int groups = (n_cls + L32_G - 1) / L32_G;
+  const int l_u = tid % LT, pg = tid / LT;
+  const bool unit_on = pg < groups && l_u < lt;
+  const int p0 = pg * L32_G, p1 = min(n_cls, p0 + L32_G);
+  float acc[L32_G][NDIR + 1], cmp[L32_G][NDIR + 1];
+#pragma unroll
+  for (int g = 0; g < L32_G; ++g)
+#pragma unroll
+    for (int s = 0; s <= NDIR; ++s) {
+      acc[g][s] = 0.f;
+      cmp[g][s] = 0.f;
+    }
+  for (int base = a_begin; base < a_end; base += TA) {
+    const int tc = min(TA, a_end - base);
+    // phase K
+    {
+      const float4* src = reinterpret_cast<const float4*>(gi.rowg + (size_t)base * NROWG);
+      float4* dst = reinterpret_cast<float4*>(R);
+      for (int i = tid; i < tc * (NROWG / 4); i += L32_THREADS) dst[i] = src[i];
+      for (int i = tid; i < tc * n_tr * (NDIR + 1); i += L32_THREADS) {
+        const int t = i / (n_tr * (NDIR + 1)), rem = i % (n_tr * (NDIR + 1));
+        const int tr = rem / (NDIR + 1), s = rem % (NDIR + 1);
+        Ks[i] = gi.kernf[((size_t)tr * na + base + t) * (NDIR + 1) + s];
+      }
+    }
+    __syncthreads();
+    // phase M
+    for (int i = tid; i < tc * n_cls; i += L32_THREADS) {
+      const int t = i / n_cls, p = i % n_cls;
+      const float* Ki = Ks + ((size_t)t * n_tr + geo->pair_i[p]) * (NDIR + 1);
+      const float* Kj = Ks + ((size_t)t * n_tr + geo->pair_j[p]) * (NDIR + 1);
+      const float* row = R + (size_t)t * NROWG;
+      const float u = row[F_U];
+      const float kk = Ki[0] * Kj[0];
+      Mv[i] = u * kk;
+      const float* du = row + NROW32 + T_U * NDIR;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) Md[(size_t)i * NDIR + d] = du[d] * kk + u * (Ki[1 + d] * Kj[0] + Ki[0] * Kj[1 + d]);
+    }
+    // phase A
+    for (int i = tid; i < tc * lt; i += L32_THREADS) {
+      const int t = i / lt, l = i % lt;
+      const float* row = R + (size_t)t * NROWG;
+      float an[NGT], ae[NET];
+      const float P = node32_fb(eh, row, khv[l], lkhv[l], ikhv[l], an, ae);
+      float pd[NDIR];
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) pd[d] = 0.f;
+      const float* tg = row + NROW32;
+#pragma unroll
+      for (int j = 0; j < T_U; ++j) {
+        const float4 a = *reinterpret_cast<const float4*>(tg + j * NDIR);
+        const float4 b = *reinterpret_cast<const float4*>(tg + j * NDIR + 4);
+        pd[0] = fmaf(an[j], a.x, pd[0]); pd[1] = fmaf(an[j], a.y, pd[1]);
+        pd[2] = fmaf(an[j], a.z, pd[2]); pd[3] = fmaf(an[j], a.w, pd[3]);
+        pd[4] = fmaf(an[j], b.x, pd[4]); pd[5] = fmaf(an[j], b.y, pd[5]);
+        pd[6] = fmaf(an[j], b.z, pd[6]); pd[7] = fmaf(an[j], b.w, pd[7]);
+      }
+#pragma unroll
+      for (int j = 0; j < NET; ++j) {
+        const float4 a = *reinterpret_cast<const float4*>(et + j * NDIR);
+        const float4 b = *reinterpret_cast<const float4*>(et + j * NDIR + 4);
+        pd[0] = fmaf(ae[j], a.x, pd[0]); pd[1] = fmaf(ae[j], a.y, pd[1]);
+        pd[2] = fmaf(ae[j], a.z, pd[2]); pd[3] = fmaf(ae[j], a.w, pd[3]);
+        pd[4] = fmaf(ae[j], b.x, pd[4]); pd[5] = fmaf(ae[j], b.y, pd[5]);
+        pd[6] = fmaf(ae[j], b.z, pd[6]); pd[7] = fmaf(ae[j], b.w, pd[7]);
+      }
+      Pv[t * LT + l] = P;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) Pd[((size_t)t * NDIR + d) * LT + l] = pd[d];
+    }
+    __syncthreads();
+    // phase B
+    if (unit_on) {
+      float part[L32_G][NDIR + 1];
+#pragma unroll
+      for (int g = 0; g < L32_G; ++g)
+#pragma unroll
+        for (int s = 0; s <= NDIR; ++s) part[g][s] = 0.f;
+      for (int t = 0; t < tc; ++t) {
+        const float pv = Pv[t * LT + l_u];
+        float pd[NDIR];
+#pragma unroll
+        for (int d = 0; d < NDIR; ++d) pd[d] = Pd[((size_t)t * NDIR + d) * LT + l_u];
+#pragma unroll
+        for (int g = 0; g < L32_G; ++g) {
+          const int p = p0 + g;
+          if (p < p1) {
+            const float mv = Mv[t * n_cls + p];
+            const float4 a = *reinterpret_cast<const float4*>(Md + ((size_t)t * n_cls + p) * NDIR);
+            const float4 b = *reinterpret_cast<const float4*>(Md + ((size_t)t * n_cls + p) * NDIR + 4);
+            const float md[NDIR] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+            part[g][0] = fmaf(pv, mv, part[g][0]);
+#pragma unroll
+            for (int d = 0; d < NDIR; ++d) part[g][1 + d] = fmaf(pd[d], mv, fmaf(pv, md[d], part[g][1 + d]));
+          }
+        }
+      }
+#pragma unroll
+      for (int g = 0; g < L32_G; ++g)
+#pragma unroll
+        for (int s = 0; s <= NDIR; ++s) {
+          const float y = part[g][s] - cmp[g][s];
+          const float tt = acc[g][s] + y;
+          cmp[g][s] = (tt - acc[g][s]) - y;
+          acc[g][s] = tt;
+        }
+    }
+    __syncthreads();
+  }
+  if (unit_on) {
+    const int ell = l0 + l_u;
+    double* part = gi.part + (size_t)split * n_cls * n_ell * (NDIR + 1);
+#pragma unroll
+    for (int g = 0; g < L32_G; ++g) {
+      const int p = p0 + g;
+      if (p < p1) {
+        const double ef = EF[(size_t)geo->pair_i[p] * n_ell + ell] * EF[(size_t)geo->pair_j[p] * n_ell + ell];
+        double* dst = part + ((size_t)p * n_ell + ell) * (NDIR + 1);
+#pragma unroll
+        for (int s = 0; s <= NDIR; ++s) dst[s] = ((double)acc[g][s] - (double)cmp[g][s]) * ef;
+      }
+    }
+  }
+}
+
+void launch_grad_limber32(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
+  const int lt = grad_limber32_tile(gb.n_ell, gb.n_cls);
+  const int ta = grad_limber32_chunk(gb.n_cls);
+  const size_t smem = sizeof(float) * limber32_smem_floats(gb.n_cls, gb.n_tr, lt, ta);
+  cudaFuncSetAttribute(grad_limber32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dim3 grid((gb.n_ell + lt - 1) / lt, gb.n_split, gb.n_items);
+  grad_limber32_kernel<<<grid, L32_THREADS, smem, st>>>(gb, c, lt, ta);
+}
+
+}  // namespace jcg

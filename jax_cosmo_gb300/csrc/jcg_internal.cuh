@@ -462,9 +462,9 @@ void launch_halofit_rows(const Batch& b, const ConstTables* c, cudaStream_t st);
 void launch_tracer_kernels(const Batch& b, const ConstTables* c, cudaStream_t st);
 void launch_limber(const Batch& b, const ConstTables* c, int lt, cudaStream_t st);
 // derivatives (jcg_grad.cu)
-size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo);
-void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, double* cl,
-              double* jac, void* ws, const ConstTables* c, cudaStream_t st);
+size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision);
+void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, int precision,
+              double* cl, double* jac, void* ws, const ConstTables* c, cudaStream_t st);
 // one request of a ragged Jacobian batch; cl / jac NULL: carved from the workspace
 struct GradReq {
   const GeoHeader* h;      // host copy of the header
@@ -473,9 +473,9 @@ struct GradReq {
   double* cl;
   double* jac;
 };
-int grad_listed_auto_split(const GradReq* r, int n);
-size_t grad_listed_bytes(const GradReq* r, int n, int n_split);
-cudaError_t grad_run_listed(GradReq* r, int n, int n_split, void* ws, const ConstTables* c,
+int grad_listed_auto_split(const GradReq* r, int n, int precision);
+size_t grad_listed_bytes(const GradReq* r, int n, int n_split, int precision);
+cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void* ws, const ConstTables* c,
                             cudaStream_t st);
 // log-likelihood and its gradient for a fixed inverse covariance (jcg_stats.cu)
 struct ReqLL {

@@ -15,6 +15,7 @@
 // same formulas (ex2/lg2/rcp/sin), per-chunk partial sums added with Kahan
 // compensation across chunks.
 #include "jcg_internal.cuh"
+#include "jcg_fp32.cuh"
 
 namespace jcg {
 
@@ -22,41 +23,6 @@ constexpr int LB_THREADS = 256;
 constexpr int LB_TA = 32;   // a nodes per chunk
 constexpr int LB_MAXLT = 32;
 constexpr int LB_MAXO = (LB_MAXLT * MAXPAIR + LB_THREADS - 1) / LB_THREADS;  // 17
-
-// ---------------------------------------------------------- FP32 helpers ---
-__device__ __forceinline__ float ex2f(float x) {
-  float y;
-  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float lg2f(float x) {
-  float y;
-  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float rcpf(float x) {
-  float y;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-__device__ __forceinline__ float sinf_approx(float x) {
-  float y;
-  asm("sin.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-// sin(x) for x >= 0: reduce by 2 pi in two parts (Cody & Waite), then the
-// hardware approximation on [-pi, pi].
-__device__ __forceinline__ float sin_reduced(float x) {
-  const float n = rintf(x * 0.15915494309189535f);
-  float r = fmaf(-n, 6.28125f, x);                // 6.28125 = 201/32, exact products
-  r = fmaf(-n, 1.9353071795864769e-3f, r);        // 2 pi - 6.28125
-  return sinf_approx(r);
-}
-
-constexpr float LOG2E_F = 1.4426950408889634f;
-constexpr float LN2_F = 0.6931471805599453f;
-constexpr float E_F = 2.718281828459045f;
-constexpr float TWO_PI2_F = 19.739208802178716f;
 
 // Per-cosmology Eisenstein & Hu constants of the FP32 node.
 struct EH32 {

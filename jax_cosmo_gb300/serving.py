@@ -17,7 +17,9 @@ It then submits ``(model, parameters)`` requests to a ``Server``, which
 * runs every admitted request, whatever its tracer count and ell grid, in one
   launch sequence (``jcg_requests_run``, mode LOGLIKE_GRAD: tables with
   tangents, halofit rows, radial kernels, the Limber Jacobian, then logL and
-  its gradient over the 8 Cosmology leaves, FP64);
+  its gradient over the 8 Cosmology leaves; ``precision`` "fp32c" -- float64
+  tables, float32 Limber integrand and lensing kernels with compensated sums --
+  or "fp64");
 * keeps up to ``n_streams`` such batches on the GPU at once, each on its own
   CUDA stream, so that requests arriving while a batch runs are admitted and
   launched as soon as a stream slot and arena space are free (their work
@@ -98,11 +100,14 @@ class ChainModel:
                       self.prec.data_ptr())
         table = np.zeros(1, _lib.REQUEST_DTYPE)
         self._fill(table, 0, self.geo.data_ptr(), self.data.data_ptr())
-        lo, _ = ctypes.c_size_t(), ctypes.c_size_t()
-        _lib.call("jcg_requests_workspace_size", ctypes.c_void_p(table.ctypes.data), 1,
-                  _lib.REQ_LOGLIKE_GRAD, ctypes.byref(lo), ctypes.byref(_))
-        # workspace share of one request (no a-splits); additive over a batch
-        self.footprint = _round(lo.value)
+        # workspace share of one request (no a-splits), additive over a batch;
+        # the larger of the two precisions
+        self.footprint = 0
+        for prec in (_lib.FP64, _lib.FP32C):
+            lo, hi = ctypes.c_size_t(), ctypes.c_size_t()
+            _lib.call("jcg_requests_workspace_size", ctypes.c_void_p(table.ctypes.data), 1,
+                      _lib.REQ_LOGLIKE_GRAD, prec, ctypes.byref(lo), ctypes.byref(hi))
+            self.footprint = max(self.footprint, _round(lo.value))
 
     def _fill(self, table, i, params_ptr, out_ptr):
         g, geo, data, prec = self._addr
@@ -151,8 +156,9 @@ class _Arena:
 class _CudaBackend:
     """One CUDA stream, pinned staging and device slots per batch slot."""
 
-    def __init__(self, device, arena_bytes, n_streams, max_batch):
+    def __init__(self, device, arena_bytes, n_streams, max_batch, precision):
         self.device = _lib.require_cuda(device)
+        self.precision = precision
         self.arena = torch.empty(max(int(arena_bytes), _ALIGN), dtype=torch.uint8, device=self.device)
         self.streams = [torch.cuda.Stream(self.device) for _ in range(n_streams)]
         self.events = [None] * n_streams
@@ -172,7 +178,7 @@ class _CudaBackend:
             m._fill(table, i, m.geo.data_ptr(), m.data.data_ptr())
         lo, hi = ctypes.c_size_t(), ctypes.c_size_t()
         _lib.call("jcg_requests_workspace_size", ctypes.c_void_p(table.ctypes.data), len(models),
-                  _lib.REQ_LOGLIKE_GRAD, ctypes.byref(lo), ctypes.byref(hi))
+                  _lib.REQ_LOGLIKE_GRAD, self.precision, ctypes.byref(lo), ctypes.byref(hi))
         return lo.value, hi.value
 
     def launch(self, slot, reqs, off, nbytes):
@@ -187,7 +193,7 @@ class _CudaBackend:
         with torch.cuda.stream(s):
             pd[:n].copy_(ph[:n], non_blocking=True)
             _lib.call("jcg_requests_run", ctypes.c_void_p(table.ctypes.data), n, _lib.REQ_LOGLIKE_GRAD,
-                      ctypes.c_void_p(self.arena.data_ptr() + off), ctypes.c_size_t(nbytes),
+                      self.precision, ctypes.c_void_p(self.arena.data_ptr() + off), ctypes.c_size_t(nbytes),
                       ctypes.c_void_p(s.cuda_stream))
             self.out_host[slot][:n].copy_(self.out_dev[slot][:n], non_blocking=True)
             ev = torch.cuda.Event()
@@ -232,15 +238,19 @@ class Server:
     """
 
     def __init__(self, device=None, hbm_budget=1 << 30, max_batch=512, n_streams=2, timeout_s=60.0,
-                 poll_s=50e-6, backend=None):
+                 poll_s=50e-6, precision="fp32c", backend=None):
+        from jax_cosmo_gb300.angular_cl import _precision_code
+
         if n_streams < 1 or max_batch < 1:
             raise ValueError("n_streams and max_batch must be >= 1")
+        self.precision = precision
+        prec = _precision_code(precision)
         self.max_batch = int(max_batch)
         self.timeout_s = float(timeout_s)
         self.poll_s = float(poll_s)
         self._arena = _Arena(hbm_budget)
         self._backend = backend if backend is not None else _CudaBackend(device, self._arena.size, n_streams,
-                                                                          self.max_batch)
+                                                                          self.max_batch, prec)
         self._slots = [None] * n_streams
         self._dead = [False] * n_streams
         self._pending = collections.deque()
@@ -430,7 +440,7 @@ def angular_cl_ragged(items, precision="fp32c", n_limber=512, device=None):
     """
     from jax_cosmo_gb300.angular_cl import _precision_code
 
-    mode = _precision_code(precision)
+    prec = _precision_code(precision)
     device = _lib.require_cuda(device)
     items = list(items)
     n = len(items)
@@ -450,8 +460,9 @@ def angular_cl_ragged(items, precision="fp32c", n_limber=512, device=None):
         table[i] = (ctypes.addressof(g), geo.data_ptr(), params.data_ptr() + 64 * i, out.data_ptr(), 0, 0, 0, 0)
     lo, hi = ctypes.c_size_t(), ctypes.c_size_t()
     tp = ctypes.c_void_p(table.ctypes.data)
-    _lib.call("jcg_requests_workspace_size", tp, n, mode, ctypes.byref(lo), ctypes.byref(hi))
+    _lib.call("jcg_requests_workspace_size", tp, n, _lib.REQ_CL, prec, ctypes.byref(lo), ctypes.byref(hi))
     ws = _lib.workspace(hi.value, device)
-    _lib.call("jcg_requests_run", tp, n, mode, _lib.ptr(ws), ctypes.c_size_t(ws.numel()), _lib.stream_of(device))
+    _lib.call("jcg_requests_run", tp, n, _lib.REQ_CL, prec, _lib.ptr(ws), ctypes.c_size_t(ws.numel()),
+              _lib.stream_of(device))
     del keep
     return outs

@@ -4,10 +4,12 @@
   tracer count and ell grid) equals angular_cl of that request alone (FP64:
   1e-14 relative; FP32C: 1e-4 of FP64);
 * served log-likelihood + gradient (covariance fixed) against the public API
-  differentiated by torch.autograd (1e-10 / 1e-8 of the largest component) and
-  against the float64 oracle differentiated by torch autograd (1e-8);
-* each result is the same alone and in a mix of chains (1e-12 of the largest
-  component: only the grouping of the a-split partial sums may differ);
+  differentiated by torch.autograd (fp64: 1e-10 / 1e-8 of the largest
+  component) and against the float64 oracle differentiated by torch autograd
+  (fp64: 1e-8; fp32c: 1e-4);
+* each result is the same alone and in a mix of chains (fp64: 1e-12, fp32c:
+  1e-6 of the largest component: only the grouping of the a-split partial sums
+  may differ);
 * admission under a small HBM budget completes every request within budget.
 """
 import numpy as np
@@ -93,11 +95,13 @@ def test_ragged_forward_matches_single():
         assert float(((b - ref) / ref).abs().max()) < 1e-4
 
 
-def test_served_matches_api_and_oracle():
+@pytest.mark.parametrize("precision", ["fp64", "fp32c"])
+def test_served_matches_api_and_oracle(precision):
     model, probes, ell, spec = make_model(21, max_ell=60)
     row = [0.27, 0.05, 0.70, 0.95, 0.78, 0.0, -0.9, 0.0]
-    with serving.Server(hbm_budget=256 << 20) as srv:
+    with serving.Server(hbm_budget=256 << 20, precision=precision) as srv:
         r = srv.submit(model, row).result(timeout=120)
+    tv, tg = (1e-10, 1e-8) if precision == "fp64" else (1e-4, 1e-4)
     # public API: angular_cl differentiated by autograd, covariance fixed
     c = cosmo_of(row, grad=True)
     mu = jc.cl.angular_cl(c, ell, probes).flatten()
@@ -106,8 +110,8 @@ def test_served_matches_api_and_oracle():
     ll = -0.5 * torch.dot(res, alpha)
     ll.backward()
     g = np.array([float(getattr(c, n).grad) for n in NAMES])
-    assert abs(r.loglike - float(ll.detach())) <= 1e-10 * abs(float(ll.detach()))
-    assert scale_err(r.grad, g) < 1e-8
+    assert abs(r.loglike - float(ll.detach())) <= tv * abs(float(ll.detach()))
+    assert scale_err(r.grad, g) < tg
     # oracle differentiated by torch autograd
     v = torch.tensor(row, dtype=torch.float64, requires_grad=True)
     mu_o = O.angular_cl(O.Cosmo.from_vector(v), ell, spec).flatten()
@@ -115,27 +119,28 @@ def test_served_matches_api_and_oracle():
     P = model.prec.cpu()
     ll_o = -0.5 * torch.dot(res_o, torch.einsum("lpq,ql->pl", P, res_o.reshape(model.n_cls, model.n_ell)).flatten())
     ll_o.backward()
-    assert abs(r.loglike - float(ll_o.detach())) <= 1e-8 * abs(float(ll_o.detach()))
-    assert scale_err(r.grad, v.grad.numpy()) < 1e-8
+    assert abs(r.loglike - float(ll_o.detach())) <= max(tv, 1e-8) * abs(float(ll_o.detach()))
+    assert scale_err(r.grad, v.grad.numpy()) < tg
 
 
-def test_alone_equals_mix():
+@pytest.mark.parametrize("precision,tol", [("fp64", 1e-12), ("fp32c", 1e-6)])
+def test_alone_equals_mix(precision, tol):
     models = [make_model(s, max_ell=150)[0] for s in (31, 32, 33, 34, 35, 36)]
     rng = np.random.default_rng(9)
     rows = [[box_point(rng) for _ in range(3)] for _ in models]
     alone = {}
-    with serving.Server(hbm_budget=512 << 20, n_streams=1) as srv:
+    with serving.Server(hbm_budget=512 << 20, n_streams=1, precision=precision) as srv:
         for i, m in enumerate(models):
             for j, row in enumerate(rows[i]):
                 alone[(i, j)] = srv.submit(m, row).result(timeout=120)
-    with serving.Server(hbm_budget=512 << 20, n_streams=2) as srv:
+    with serving.Server(hbm_budget=512 << 20, n_streams=2, precision=precision) as srv:
         futs = {(i, j): srv.submit(m, row) for i, m in enumerate(models) for j, row in enumerate(rows[i])}
         mix = {k: f.result(timeout=120) for k, f in futs.items()}
         st = srv.stats()
     assert st["max_batch"] > 1  # the mix did share launches
     for k in alone:
-        assert abs(mix[k].loglike - alone[k].loglike) <= 1e-12 * abs(alone[k].loglike)
-        assert scale_err(mix[k].grad, alone[k].grad) < 1e-12
+        assert abs(mix[k].loglike - alone[k].loglike) <= tol * abs(alone[k].loglike)
+        assert scale_err(mix[k].grad, alone[k].grad) < tol
 
 
 def test_small_hbm_budget_admission():
