@@ -210,6 +210,35 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
     put(pq, NKH, e, p3 / (2.0 * (PI * PI)));
   }
   __syncthreads();
+  if (gi.ptt) {
+    // Taylor prefix tables (fp32c moments): ptt[i][m][s] = sum_{k < i} w_k q3_k kh_k^(2(m+1)),
+    // s = 0 value, 1..8 tangents; one warp per component s, lanes over k
+    const int warp = t >> 5, lane = t & 31;
+    for (int sc = warp; sc < NDIR + 1; sc += (int)(blockDim.x >> 5)) {
+      const double* w = pq + sc * NKH;
+      if (lane < NTAYLOR) gi.ptt[(size_t)lane * (NDIR + 1) + sc] = 0.0;
+      double carry[NTAYLOR];
+#pragma unroll
+      for (int m = 0; m < NTAYLOR; ++m) carry[m] = 0.0;
+      for (int base = 0; base < NKH; base += 32) {
+        const int i = base + lane;
+        const double k2 = i < NKH ? c->kh[i] * c->kh[i] : 0.0;
+        double v = i < NKH ? c->simpson_kh[i] * w[i] : 0.0;
+#pragma unroll
+        for (int m = 0; m < NTAYLOR; ++m) {
+          v *= k2;
+          double x = v;
+#pragma unroll
+          for (int o = 1; o < 32; o <<= 1) {
+            const double u = __shfl_up_sync(0xffffffffu, x, o);
+            if (lane >= o) x += u;
+          }
+          if (i < NKH) gi.ptt[((size_t)(i + 1) * NTAYLOR + m) * (NDIR + 1) + sc] = carry[m] + x;
+          carry[m] += __shfl_sync(0xffffffffu, x, 31);
+        }
+      }
+    }
+  }
   // sigma^2(R_j) without g^2 (power.py:98-111), value and tangents
   const double dx = (c->logk[NKH - 1] - c->logk[0]) / 256;
   for (int e = t; e < (NDIR + 1) * NRT; e += blockDim.x) {
@@ -244,32 +273,47 @@ size_t grad_tables_smem() {
 }
 
 // ----------------------------------------------------------- dual rows -----
-// One warp per Limber node: growth, chi and the halofit root find with
-// tangents on lanes 0-7, the spectral moments over 32 lanes in Dual<8>, then
-// the takahashi2012 coefficients and the Limber weight on lanes 0-7.
+// One warp per 4 Limber nodes: lane = 8 * node slot + tangent direction.
+//   prelude (per lane, Dual<1>): growth, chi, the root find (index from the
+//     values with the forward's arithmetic, tangent through the interpolation
+//     formula), R = 1 / k_nl;
+//   moments (power.py:121-139), node by node over all 32 lanes, as scalar sums
+//     with their R-derivatives and their P(k) k^3 tangents:
+//       S1 = sum w q3 2 y^2 e^{-y^2},  S2 = sum w q3 4 (y^2 - y^4) e^{-y^2},
+//       y = k R, q3 = P(k) k^3 / (2 pi^2);  dS = S_q3[d] + dS/dR dR[d];
+//     FP32C: exp only for y^2 in [1, 60], below it the Taylor series of
+//     e^{-y^2} on prefix tables of w q3 k^(2(m+1)) and their tangents (ptt),
+//     as the forward fp32c rows do; FP64: every term with y^2 <= 60;
+//   epilogue (per lane, Dual<1>): n_eff, C, takahashi2012 coefficients, the
+//     Limber weight; rows out.
 __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
+  __shared__ double e2tab[64];
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) e2tab[i] = kExp2Tab64[i];
+  __syncthreads();
   const GradItem gi = grad_item(gb, item);
   const GeoHeader* geo = gi.geo;
   const int na = geo->na;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int n = blockIdx.x * 8 + warp;
-  if (n >= na) return;
+  const int slot = lane >> 3, dir = lane & 7;
+  const int n_first = (blockIdx.x * 8 + warp) * 4;
+  if (n_first >= na) return;
+  const int n_raw = n_first + slot;
+  const bool live = n_raw < na;
+  const int n = live ? n_raw : na - 1;  // dead slots evaluate a valid node, write nothing
+  const bool fast = gb.precision == JCG_FP32C;
   const TabD* tb = gi.tab;
-  const int dir = lane & 7;
   const double* A = geo_ptr<double>(geo, geo->off_a);
   const double* WS = geo_ptr<double>(geo, geo->off_wsimp);
   const int64_t* SC = geo_ptr<int64_t>(geo, geo->off_seg_chi);
   const int64_t* SG = geo_ptr<int64_t>(geo, geo->off_seg_grow);
   const double a = A[n];
-  // prelude on every lane (lanes 8..31 duplicate lanes 0..7)
   D1 g = interp_d1(a, c->atab_grow, tb->gv, tb->gd[dir], unpack_seg(SG[n]));
   g = xfmin(xfmax(g, 0.0), 1.0);
   D1 chi = interp_d1(a, c->atab_chi, tb->chiv, tb->chid[dir], unpack_seg(SC[n]));
   chi = xfmax(chi, 0.0);
   const D1 g2 = g * g;
-  // root find: index from values (same arithmetic as the forward), tangents through the formula
   int best;
   {
     int lo = 0, hi = NRT;
@@ -302,40 +346,103 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
   const D1 R = xfmax(xexp(root), 1e-6);
   const D1 knl = 1.0 / R;
   const D1 inv = 1.0 / knl;
-  // moments (power.py:121-139) in Dual<8>; terms with y^2 > 60 are below 1e-20 of the sums
-  const D8 inv8 = gather8(inv);
-  const D8 g2_8 = gather8(g2);
-  D8 s1 = dconst<NDIR>(0.0), s2 = dconst<NDIR>(0.0);
-  for (int i = lane; i < NKH; i += 32) {
-    const D8 y = c->kh[i] * inv8;
-    const D8 y2 = y * y;
-    if (y2.v > 60.0) continue;
-    D8 p3;
-    p3.v = tb->pk3v[i];
-#pragma unroll
-    for (int d = 0; d < NDIR; ++d) p3.d[d] = tb->pk3d[d][i];
-    const D8 res = p3 * xexp(-y2) * g2_8 / TWO_PI2_G;
-    s1 = s1 + c->simpson_kh[i] * (2 * res * y2);
-    s2 = s2 + c->simpson_kh[i] * (4 * res * (y2 - y2 * y2));
+  // exp range [ilo, ihi] of this lane's node (the forward fp32c rows' rule)
+  int ilo = 0, ihi = NKH - 1;
+  if (fast) {
+    const double linv = log(inv.v);
+    ilo = (int)floor((0.5 * log(Y2_TAYLOR) - linv - LOG_KMIN) / DLOGK);
+    ihi = (int)ceil((0.5 * log(Y2_SKIP) - linv - LOG_KMIN) / DLOGK);
+    ilo = max(0, min(ilo, NKH));
+    ihi = max(ilo - 1, min(ihi, NKH - 1));
   }
+  // explicit terms, node by node over the warp
+  double m_s1 = 0, m_s2 = 0, m_s1r = 0, m_s2r = 0, m_s1d = 0, m_s2d = 0;
+  const double q3s = 1.0 / TWO_PI2_G;
+  for (int q = 0; q < 4; ++q) {
+    const double Rq = __shfl_sync(0xffffffffu, inv.v, q * 8);
+    const int lo = __shfl_sync(0xffffffffu, ilo, q * 8), hi = __shfl_sync(0xffffffffu, ihi, q * 8);
+    const double iRq = 1.0 / Rq;
+    double s1 = 0, s2 = 0, s1r = 0, s2r = 0, s1d[NDIR], s2d[NDIR];
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    s1.v += __shfl_xor_sync(0xffffffffu, s1.v, o);
-    s2.v += __shfl_xor_sync(0xffffffffu, s2.v, o);
+    for (int d = 0; d < NDIR; ++d) s1d[d] = s2d[d] = 0.0;
+    for (int i = lo + lane; i <= hi; i += 32) {
+      const double y = c->kh[i] * Rq;
+      const double y2 = y * y;
+      if (!fast && y2 > Y2_SKIP) continue;
+      const double E = fast ? exp_tang(-y2, e2tab) : exp(-y2);
+      const double wq = c->simpson_kh[i] * E * q3s;
+      const double Av = wq * tb->pk3v[i];
+      const double c1 = 2.0 * y2, c2 = 4.0 * (y2 - y2 * y2);
+      s1 += Av * c1;
+      s2 += Av * c2;
+      s1r += 4.0 * Av * y2 * (1.0 - y2) * iRq;
+      s2r += 8.0 * Av * y2 * (1.0 - 3.0 * y2 + y2 * y2) * iRq;
+      const double w1 = wq * c1, w2 = wq * c2;
 #pragma unroll
-    for (int d = 0; d < NDIR; ++d) {
-      s1.d[d] += __shfl_xor_sync(0xffffffffu, s1.d[d], o);
-      s2.d[d] += __shfl_xor_sync(0xffffffffu, s2.d[d], o);
+      for (int d = 0; d < NDIR; ++d) {
+        const double p = tb->pk3d[d][i];
+        s1d[d] += w1 * p;
+        s2d[d] += w2 * p;
+      }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      s1 += __shfl_xor_sync(0xffffffffu, s1, o);
+      s2 += __shfl_xor_sync(0xffffffffu, s2, o);
+      s1r += __shfl_xor_sync(0xffffffffu, s1r, o);
+      s2r += __shfl_xor_sync(0xffffffffu, s2r, o);
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) {
+        s1d[d] += __shfl_xor_sync(0xffffffffu, s1d[d], o);
+        s2d[d] += __shfl_xor_sync(0xffffffffu, s2d[d], o);
+      }
+    }
+    if (slot == q) {
+      m_s1 = s1;
+      m_s2 = s2;
+      m_s1r = s1r;
+      m_s2r = s2r;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d)
+        if (d == dir) {
+          m_s1d = s1d[d];
+          m_s2d = s2d[d];
+        }
     }
   }
-  double s1d = 0.0, s2d = 0.0;
-#pragma unroll
-  for (int d = 0; d < NDIR; ++d)
-    if (d == dir) {
-      s1d = s1.d[d];
-      s2d = s2.d[d];
+  // Taylor part below ilo: sum_m (-1)^m / m! R^(2m+2) T_m
+  if (fast && ilo > 0) {
+    const double* T = gi.ptt + (size_t)ilo * NTAYLOR * (NDIR + 1);
+    const double Rv = inv.v, R2 = Rv * Rv;
+    double pw = R2, dpw = 2.0 * Rv, fact = 1.0;
+    double t1 = 0, t2 = 0, t1r = 0, t2r = 0, t1d = 0, t2d = 0;
+    for (int m = 0; m < NTAYLOR - 1; ++m) {
+      const double sg = ((m & 1) ? -1.0 : 1.0) / fact;
+      const double Tm = T[m * (NDIR + 1)], Tm1 = T[(m + 1) * (NDIR + 1)];
+      const double Dm = T[m * (NDIR + 1) + 1 + dir], Dm1 = T[(m + 1) * (NDIR + 1) + 1 + dir];
+      const double pw1 = pw * R2, dpw1 = dpw * R2 + pw * 2.0 * Rv;  // R^(2m+4) and its R-derivative
+      t1 += sg * Tm * pw;
+      t2 += sg * (Tm * pw - Tm1 * pw1);
+      t1r += sg * Tm * dpw;
+      t2r += sg * (Tm * dpw - Tm1 * dpw1);
+      t1d += sg * Dm * pw;
+      t2d += sg * (Dm * pw - Dm1 * pw1);
+      pw = pw1;
+      dpw = dpw1;
+      fact *= (double)(m + 1);
     }
-  const D1 I1 = mk1(s1.v, s1d), I2 = mk1(s2.v, s2d);
+    m_s1 += 2.0 * t1;
+    m_s2 += 4.0 * t2;
+    m_s1r += 2.0 * t1r;
+    m_s2r += 4.0 * t2r;
+    m_s1d += 2.0 * t1d;
+    m_s2d += 4.0 * t2d;
+  }
+  // moments with their tangents in this lane's direction, times g^2
+  const D1 S1 = mk1(m_s1, m_s1d + m_s1r * inv.d[0]);
+  const D1 S2 = mk1(m_s2, m_s2d + m_s2r * inv.d[0]);
+  const D1 I1 = S1 * g2, I2 = S2 * g2;
+
   const D1 neff = I1 - 3.0;
   const D1 C = I1 * I1 + I2;
   // coefficients (power.py:177-238)
@@ -367,7 +474,7 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
   outv[A_NU] = xexp(LN10_G * (5.2105 + 3.6902 * neff));
   const D1 dchi = dchioverdaT(bg, a, lna);
   outv[A_U] = WS[n] * dchi / xfmax(chi * chi, 1.0) / C2_G;
-  if (lane < NDIR) {
+  if (live) {
     if (gb.precision == JCG_FP64) {
       double* row = gi.rowd + (size_t)n * NROWD;
       for (int i = 0; i < NA_IN; ++i) {
@@ -842,8 +949,9 @@ void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
   const size_t smt = grad_tables_smem();
   cudaFuncSetAttribute(grad_tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
   grad_tables_kernel<<<gb.n_items, 256, smt, st>>>(gb, c);
+  dim3 grw((gb.na + 31) / 32, gb.n_items);
+  grad_rows_kernel<<<grw, 256, 0, st>>>(gb, c);
   dim3 gr((gb.na + 7) / 8, gb.n_items);
-  grad_rows_kernel<<<gr, 256, 0, st>>>(gb, c);
   if (gb.precision == JCG_FP32C) {
     launch_grad_kern32(gb, c, st);
     launch_grad_limber32(gb, c, st);
@@ -902,12 +1010,17 @@ static size_t kern_bytes(const GeoHeader& h, int precision) {
   const size_t el = precision == JCG_FP32C ? sizeof(float) : sizeof(double);
   return al256(el * (size_t)h.n_tr * h.na * (NDIR + 1));
 }
+// Taylor prefix tables of the fp32c moments, per cosmology
+static size_t ptt_bytes(int precision) {
+  return precision == JCG_FP32C ? al256(sizeof(double) * NPTT) : 0;
+}
 
 size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
   const int ns = grad_n_split(h, n_cosmo, precision);
   GeoHeader hb = h;
   hb.na = h.na * n_cosmo;  // the uniform form keeps the sections batch-contiguous
   size_t o = al256(sizeof(TabD) * (size_t)n_cosmo);
+  o += ptt_bytes(precision) * n_cosmo;
   o += rows_bytes(hb, precision);
   o += kern_bytes(hb, precision);
   o += al256(sizeof(double) * (size_t)ns * n_cosmo * h.n_cls * h.n_ell * (NDIR + 1));
@@ -928,6 +1041,8 @@ void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, in
   size_t o = 0;
   gb.tab = reinterpret_cast<TabD*>(base + o);
   o += al256(sizeof(TabD) * (size_t)n_cosmo);
+  if (precision == JCG_FP32C) gb.ptt = reinterpret_cast<double*>(base + o);
+  o += ptt_bytes(precision) * n_cosmo;
   if (precision == JCG_FP32C) gb.rowg = reinterpret_cast<float*>(base + o);
   else gb.rowd = reinterpret_cast<double*>(base + o);
   o += rows_bytes(hb, precision);
@@ -954,6 +1069,7 @@ void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, in
 static size_t grad_item_bytes(const GeoHeader& h, int n_split, bool own_cl, bool own_jac, int precision) {
   const size_t per = (size_t)h.n_cls * h.n_ell;
   size_t o = al256(sizeof(TabD));
+  o += ptt_bytes(precision);
   o += rows_bytes(h, precision);
   o += kern_bytes(h, precision);
   o += al256(sizeof(double) * (size_t)n_split * per * (NDIR + 1));
@@ -1003,6 +1119,8 @@ cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void*
     it.geo = r[i].geo;
     it.tab = reinterpret_cast<TabD*>(base + o);
     o += al256(sizeof(TabD));
+    if (precision == JCG_FP32C) it.ptt = reinterpret_cast<double*>(base + o);
+    o += ptt_bytes(precision);
     if (precision == JCG_FP32C) it.rowg = reinterpret_cast<float*>(base + o);
     else it.rowd = reinterpret_cast<double*>(base + o);
     o += rows_bytes(h, precision);

@@ -52,6 +52,7 @@ __device__ __constant__ const int kNodeCScalar[NC_IN] = {S_K_EQ,  S_SH_D,      S
 enum GTan { T_CHIC = 0, T_D2FAC, T_KNL, T_BETAN, T_ALPHAN, T_AN, T_3F1, T_F2, T_BN, T_LG2CF3, T_3MG,
             T_NUN, T_U, NGT };
 constexpr int F_U = 15;
+constexpr int NPTT = (NKH + 1) * NTAYLOR * (NDIR + 1);  // Taylor prefix table entries
 constexpr int NROWG = NROW32 + NGT * NDIR;  // 120 floats
 // per-cosmology Eisenstein-Hu inputs of the FP32 integrand with tangents
 enum ETan { E_KEQ = 0, E_SH, E_C18BC, E_C142AC, E_ALPHAB, E_BETAB, E_BETANODE, E_LG2KSILK, E_FB, E_FC,
@@ -67,6 +68,7 @@ struct GradItem {
   double* kernd;   // [n_tr][na][NDIR + 1]
   float* rowg;     // [na][NROWG]
   float* kernf;    // [n_tr][na][NDIR + 1]
+  double* ptt;     // FP32C: [NKH + 1][NTAYLOR][NDIR + 1] Taylor prefix tables
   double* part;    // [n_split][n_cls][n_ell][NDIR + 1] partial sums over a
   double* cl;      // [n_cls][n_ell] (may be NULL)
   double* jac;     // [n_cls][n_ell][NDIR]
@@ -86,6 +88,7 @@ struct GradBatch {
   double* kernd;
   float* rowg;
   float* kernf;
+  double* ptt;
   double* part;
   double* cl;
   double* jac;
@@ -103,6 +106,7 @@ __device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
   r.kernd = gb.kernd ? gb.kernd + (size_t)i * gb.n_tr * gb.na * (NDIR + 1) : nullptr;
   r.rowg = gb.rowg ? gb.rowg + (size_t)i * gb.na * NROWG : nullptr;
   r.kernf = gb.kernf ? gb.kernf + (size_t)i * gb.n_tr * gb.na * (NDIR + 1) : nullptr;
+  r.ptt = gb.ptt ? gb.ptt + (size_t)i * ((NPTT + 31) & ~31) : nullptr;
   r.part = gb.part + (size_t)i * gb.n_split * per * (NDIR + 1);
   r.cl = gb.cl ? gb.cl + (size_t)i * per : nullptr;
   r.jac = gb.jac + (size_t)i * per * NDIR;

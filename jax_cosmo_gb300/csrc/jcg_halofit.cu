@@ -14,10 +14,6 @@ namespace jcg {
 constexpr double TWO_PI2 = 2.0 * (PI * PI);  // 2.0 * np.pi**2
 constexpr double C2 = C_KMS * C_KMS;          // const.c**2
 constexpr double LN10 = 2.302585092994046;
-constexpr double LOG_KMIN = -0x1.26bb1bbb55515p+3;  // np.log(1e-4)
-constexpr double DLOGK = (0x1.26bb1bbb55516p+3 - -0x1.26bb1bbb55515p+3) / 256.0;
-constexpr double Y2_TAYLOR = 1.0;   // below: exp(-y^2) by its Taylor series (NTAYLOR terms)
-constexpr double Y2_SKIP = 60.0;    // above: exp(-y^2) y^4 P k^3 < 1e-20 of the sum
 
 struct HfParams {
   double knl, neff, C;

@@ -64,6 +64,11 @@ enum Scalar {
 };
 constexpr int NSCAL = 32;
 constexpr int NTAYLOR = 20;      // Taylor terms of exp(-y^2) below y^2 = 1 (1/19! < 1e-17)
+// ln k grid of the spectral moments: simps over [ln 1e-4, ln 1e4], 256 intervals (power.py:136)
+constexpr double LOG_KMIN = -0x1.26bb1bbb55515p+3;  // np.log(1e-4)
+constexpr double DLOGK = (0x1.26bb1bbb55516p+3 - -0x1.26bb1bbb55515p+3) / 256.0;
+constexpr double Y2_TAYLOR = 1.0;   // below: exp(-y^2) by its Taylor series (NTAYLOR terms)
+constexpr double Y2_SKIP = 60.0;    // above: exp(-y^2) y^4 P k^3 < 1e-20 of the sum
 constexpr int PAD_CT = 7;        // keeps sizeof(CosmoTab) a multiple of 64
 static_assert(S_NSCALAR <= NSCAL, "scalar block too small");
 
