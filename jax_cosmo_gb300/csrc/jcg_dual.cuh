@@ -193,6 +193,187 @@ __device__ __forceinline__ Dual<N> xfmin(const Dual<N>& a, double c) {
   return a.v <= c ? a : dconst<N>(c);
 }
 
+// ---------------------------------------------------------------- DualF ----
+// Value in FP64, N tangents in FP32 (the fp32c Jacobian's table and row
+// stages): the value arithmetic is exactly that of double, each tangent
+// update is one FP32 operation with a factor rounded from FP64.
+template <int N>
+struct DualF {
+  double v;
+  float d[N];
+};
+
+template <int N>
+__device__ __forceinline__ DualF<N> fconst(double v) {
+  DualF<N> r;
+  r.v = v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = 0.f;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ double val(const DualF<N>& x) {
+  return x.v;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator+(const DualF<N>& a, const DualF<N>& b) {
+  DualF<N> r;
+  r.v = a.v + b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] + b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator-(const DualF<N>& a, const DualF<N>& b) {
+  DualF<N> r;
+  r.v = a.v - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] - b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator*(const DualF<N>& a, const DualF<N>& b) {
+  DualF<N> r;
+  r.v = a.v * b.v;
+  const float av = (float)a.v, bv = (float)b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = fmaf(a.d[i], bv, av * b.d[i]);
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator/(const DualF<N>& a, const DualF<N>& b) {
+  DualF<N> r;
+  r.v = a.v / b.v;
+  const float ib = (float)(1.0 / b.v), rv = (float)r.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - rv * b.d[i]) * ib;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator-(const DualF<N>& a) {
+  DualF<N> r;
+  r.v = -a.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -a.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator+(const DualF<N>& a, double b) {
+  DualF<N> r = a;
+  r.v = a.v + b;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator+(double a, const DualF<N>& b) {
+  return b + a;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator-(const DualF<N>& a, double b) {
+  DualF<N> r = a;
+  r.v = a.v - b;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator-(double a, const DualF<N>& b) {
+  DualF<N> r;
+  r.v = a - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator*(const DualF<N>& a, double b) {
+  DualF<N> r;
+  r.v = a.v * b;
+  const float bf = (float)b;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * bf;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator*(double a, const DualF<N>& b) {
+  return b * a;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator/(const DualF<N>& a, double b) {
+  DualF<N> r;
+  r.v = a.v / b;
+  const float ib = (float)(1.0 / b);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * ib;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> operator/(double a, const DualF<N>& b) {
+  DualF<N> r;
+  r.v = a / b.v;
+  const float s = (float)(-r.v / b.v);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = s * b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> scale_f(double v, double s, const DualF<N>& a) {
+  DualF<N> r;
+  r.v = v;
+  const float sf = (float)s;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = sf * a.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> xexp(const DualF<N>& a) {
+  const double e = exp(a.v);
+  return scale_f(e, e, a);
+}
+template <int N>
+__device__ __forceinline__ DualF<N> xlog(const DualF<N>& a) {
+  return scale_f(log(a.v), 1.0 / a.v, a);
+}
+template <int N>
+__device__ __forceinline__ DualF<N> xsqrt(const DualF<N>& a) {
+  const double s = sqrt(a.v);
+  return scale_f(s, 0.5 / s, a);
+}
+template <int N>
+__device__ __forceinline__ DualF<N> xcbrt(const DualF<N>& a) {
+  const double c = cbrt(a.v);
+  return scale_f(c, c / (3.0 * a.v), a);
+}
+template <int N>
+__device__ __forceinline__ DualF<N> xsin(const DualF<N>& a) {
+  double sn, cs;
+  sincos(a.v, &sn, &cs);
+  return scale_f(sn, cs, a);
+}
+template <int N>
+__device__ __forceinline__ DualF<N> xcos(const DualF<N>& a) {
+  double sn, cs;
+  sincos(a.v, &sn, &cs);
+  return scale_f(cs, -sn, a);
+}
+template <int N>
+__device__ __forceinline__ DualF<N> xfabs(const DualF<N>& a) {
+  return a.v < 0.0 ? -a : a;
+}
+template <int N>
+__device__ __forceinline__ DualF<N> xpow(const DualF<N>& a, double e) {
+  const double p = pow(a.v, e);
+  return scale_f(p, e * p / a.v, a);
+}
+template <int N>
+__device__ __forceinline__ DualF<N> xpow(const DualF<N>& a, const DualF<N>& e) {
+  return xexp(e * xlog(a));
+}
+template <int N>
+__device__ __forceinline__ DualF<N> xfmax(const DualF<N>& a, double c) {
+  return a.v >= c ? a : fconst<N>(c);
+}
+template <int N>
+__device__ __forceinline__ DualF<N> xfmin(const DualF<N>& a, double c) {
+  return a.v <= c ? a : fconst<N>(c);
+}
+
 // value of lane `src` of a warp for a Dual<1> (the tangent of direction src)
 __device__ __forceinline__ Dual<1> shfl_d1(const Dual<1>& x, int src) {
   Dual<1> r;

@@ -31,6 +31,13 @@ __device__ __forceinline__ D1 interp_d1(double x, const double* xp, const double
 }
 
 // Tables of one cosmology with tangents.  Lanes: dir = tid & 7, item = tid >> 3.
+// F32T (fp32c Jacobian): the per-node evaluations (ODE right-hand sides,
+// Eisenstein-Hu at the Romberg and halofit k nodes) run one node per thread in
+// DualF<8> -- value in FP64, tangents in FP32 -- instead of one direction per
+// lane; the sigma^2(R) tangents are FP32 sums; float copies of the chi and
+// P(k) k^3 tangent tables are written for the FP32 stages.  The sequential
+// scans (chi prefix sum, growth RK4, Romberg) stay FP64 Dual<1>.
+template <bool F32T>
 __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.x;
   if (item >= gb.n_items) return;
@@ -68,41 +75,85 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
     if (dir == 0) arr[e] = x.v;
     arr[(1 + dir) * stride + e] = x.d[0];
   };
-  // chi RK4 right-hand side at nodes and midpoints (background.py:227-231)
-  for (int e = it; e < 2 * NCHI; e += 32) {
-    if (e < NCHI) {
-      put(fn, NCHI, e, dchi_dlnaT(bg, c->lna_chi[e]));
-    } else if (e > NCHI) {
-      const int i = e - NCHI;
-      const double t0 = c->lna_chi[i - 1], t1 = c->lna_chi[i];
-      put(fm, NCHI, i, dchi_dlnaT(bg, t0 + (t1 - t0) / 2));
+  auto putf = [&](double* arr, int stride, int e, const F8& x) {
+    arr[e] = x.v;
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) arr[(1 + d) * stride + e] = x.d[d];
+  };
+  if (!F32T) {
+    // chi RK4 right-hand side at nodes and midpoints (background.py:227-231)
+    for (int e = it; e < 2 * NCHI; e += 32) {
+      if (e < NCHI) {
+        put(fn, NCHI, e, dchi_dlnaT(bg, c->lna_chi[e]));
+      } else if (e > NCHI) {
+        const int i = e - NCHI;
+        const double t0 = c->lna_chi[i - 1], t1 = c->lna_chi[i];
+        put(fm, NCHI, i, dchi_dlnaT(bg, t0 + (t1 - t0) / 2));
+      }
     }
-  }
-  // growth ODE coefficients (background.py:96-106)
-  for (int e = it; e < 2 * NGROW; e += 32) {
-    D1 q, r;
-    if (e < NGROW) {
-      growth_qrT(bg, c->atab_grow[e], q, r);
-      put(qr + 0 * (NDIR + 1) * NGROW, NGROW, e, q);
-      put(qr + 1 * (NDIR + 1) * NGROW, NGROW, e, r);
-    } else if (e > NGROW) {
-      const int i = e - NGROW;
-      const double x = c->atab_grow[i], xp = c->atab_grow[i - 1];
-      growth_qrT(bg, xp + (x - xp) / 2, q, r);
-      put(qr + 2 * (NDIR + 1) * NGROW, NGROW, i, q);
-      put(qr + 3 * (NDIR + 1) * NGROW, NGROW, i, r);
+    // growth ODE coefficients (background.py:96-106)
+    for (int e = it; e < 2 * NGROW; e += 32) {
+      D1 q, r;
+      if (e < NGROW) {
+        growth_qrT(bg, c->atab_grow[e], q, r);
+        put(qr + 0 * (NDIR + 1) * NGROW, NGROW, e, q);
+        put(qr + 1 * (NDIR + 1) * NGROW, NGROW, e, r);
+      } else if (e > NGROW) {
+        const int i = e - NGROW;
+        const double x = c->atab_grow[i], xp = c->atab_grow[i - 1];
+        growth_qrT(bg, xp + (x - xp) / 2, q, r);
+        put(qr + 2 * (NDIR + 1) * NGROW, NGROW, i, q);
+        put(qr + 3 * (NDIR + 1) * NGROW, NGROW, i, r);
+      }
     }
-  }
-  // sigmasqr(8) integrand at the romb nodes (power.py:70-75)
-  for (int e = it; e < NROMB; e += 32) {
-    const double logk = c->romb_logk[e];
-    const double k = exp(logk);
-    const double x = k * 8.0;
-    const double wf = 3.0 * (sin(x) - x * cos(x)) / (x * x * x);
-    const D1 T = eh_transferT(sD, k, logk);
-    const D1 pk = (T * T) * xexp(sD[S_NS] * logk);
-    const double kw = k * wf;
-    put(fr, NROMB, e, k * (kw * kw) * pk);
+    // sigmasqr(8) integrand at the romb nodes (power.py:70-75)
+    for (int e = it; e < NROMB; e += 32) {
+      const double logk = c->romb_logk[e];
+      const double k = exp(logk);
+      const double x = k * 8.0;
+      const double wf = 3.0 * (sin(x) - x * cos(x)) / (x * x * x);
+      const D1 T = eh_transferT(sD, k, logk);
+      const D1 pk = (T * T) * xexp(sD[S_NS] * logk);
+      const double kw = k * wf;
+      put(fr, NROMB, e, k * (kw * kw) * pk);
+    }
+  } else {
+    F8 sF[NSCAL];
+    for (int i = 0; i < NSCAL; ++i) sF[i] = f8_of(sv[i], sd + i, NSCAL);
+    const BgT<F8> bgf = make_bgT(sF);
+    for (int e = t; e < 2 * NCHI; e += blockDim.x) {
+      if (e < NCHI) {
+        putf(fn, NCHI, e, dchi_dlnaT(bgf, c->lna_chi[e]));
+      } else if (e > NCHI) {
+        const int i = e - NCHI;
+        const double t0 = c->lna_chi[i - 1], t1 = c->lna_chi[i];
+        putf(fm, NCHI, i, dchi_dlnaT(bgf, t0 + (t1 - t0) / 2));
+      }
+    }
+    for (int e = t; e < 2 * NGROW; e += blockDim.x) {
+      F8 q, r;
+      if (e < NGROW) {
+        growth_qrT(bgf, c->atab_grow[e], q, r);
+        putf(qr + 0 * (NDIR + 1) * NGROW, NGROW, e, q);
+        putf(qr + 1 * (NDIR + 1) * NGROW, NGROW, e, r);
+      } else if (e > NGROW) {
+        const int i = e - NGROW;
+        const double x = c->atab_grow[i], xp = c->atab_grow[i - 1];
+        growth_qrT(bgf, xp + (x - xp) / 2, q, r);
+        putf(qr + 2 * (NDIR + 1) * NGROW, NGROW, i, q);
+        putf(qr + 3 * (NDIR + 1) * NGROW, NGROW, i, r);
+      }
+    }
+    for (int e = t; e < NROMB; e += blockDim.x) {
+      const double logk = c->romb_logk[e];
+      const double k = exp(logk);
+      const double x = k * 8.0;
+      const double wf = 3.0 * (sin(x) - x * cos(x)) / (x * x * x);
+      const F8 T = eh_transferT(sF, k, logk);
+      const F8 pk = (T * T) * xexp(sF[S_NS] * logk);
+      const double kw = k * wf;
+      putf(fr, NROMB, e, k * (kw * kw) * pk);
+    }
   }
   __syncthreads();
   const int warp = t >> 5, lane = t & 31;
@@ -202,12 +253,29 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
   for (int i = 0; i < NSCAL; ++i) sD[i] = mk1(sv[i], sd[dir * NSCAL + i]);
   const D1 g1 = mk1(g1s[0], g1s[1 + dir]);
   // P(k_i, a = 1) k_i^3 and pk3 / (2 pi^2) on the halofit grid
-  for (int e = it; e < NKH; e += 32) {
-    const double k = c->kh[e];
-    const D1 p3 = pk_linearT(sD, k, c->logk[e], g1) * c->kh3[e];
-    if (dir == 0) out->pk3v[e] = p3.v;
-    out->pk3d[dir][e] = p3.d[0];
-    put(pq, NKH, e, p3 / (2.0 * (PI * PI)));
+  if (!F32T) {
+    for (int e = it; e < NKH; e += 32) {
+      const double k = c->kh[e];
+      const D1 p3 = pk_linearT(sD, k, c->logk[e], g1) * c->kh3[e];
+      if (dir == 0) out->pk3v[e] = p3.v;
+      out->pk3d[dir][e] = p3.d[0];
+      put(pq, NKH, e, p3 / (2.0 * (PI * PI)));
+    }
+  } else {
+    F8 sF[NSCAL];
+    for (int i = 0; i < NSCAL; ++i) sF[i] = f8_of(sv[i], sd + i, NSCAL);
+    const F8 g1f = f8_of(g1s[0], g1s + 1, 1);
+    for (int e = t; e < NKH; e += blockDim.x) {
+      const double k = c->kh[e];
+      const F8 p3 = pk_linearT(sF, k, c->logk[e], g1f) * c->kh3[e];
+      out->pk3v[e] = p3.v;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) {
+        out->pk3d[d][e] = p3.d[d];
+        out->pk3df[e][d] = p3.d[d];
+      }
+      putf(pq, NKH, e, p3 / (2.0 * (PI * PI)));
+    }
   }
   __syncthreads();
   if (gi.ptt) {
@@ -241,7 +309,34 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
   }
   // sigma^2(R_j) without g^2 (power.py:98-111), value and tangents
   const double dx = (c->logk[NKH - 1] - c->logk[0]) / 256;
-  for (int e = t; e < (NDIR + 1) * NRT; e += blockDim.x) {
+  if (F32T) {
+    // value FP64, tangents FP32 (pq tangents rounded once into a float copy)
+    float* pqf = reinterpret_cast<float*>(fn);  // fn / fm are free here
+    for (int e = t; e < NDIR * NKH; e += blockDim.x) {
+      const int d = e / NKH, i = e % NKH;
+      pqf[i * NDIR + d] = (float)pq[(1 + d) * NKH + i];
+    }
+    __syncthreads();
+    for (int j = t; j < NRT; j += blockDim.x) {
+      double acc = 0.0;
+      float ad[NDIR];
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) ad[d] = 0.f;
+      for (int m = 0; m < 128; ++m) {
+        const double e0 = c->E[(2 * m) * NRT + j], e1 = c->E[(2 * m + 1) * NRT + j],
+                     e2 = c->E[(2 * m + 2) * NRT + j];
+        acc += pq[2 * m] * e0 + 4 * (pq[2 * m + 1] * e1) + pq[2 * m + 2] * e2;
+        const float f0 = (float)e0, f1 = 4.f * (float)e1, f2 = (float)e2;
+        const float* q0 = pqf + (2 * m) * NDIR;
+#pragma unroll
+        for (int d = 0; d < NDIR; ++d) ad[d] += q0[d] * f0 + q0[NDIR + d] * f1 + q0[2 * NDIR + d] * f2;
+      }
+      out->sigv[j] = dx / 3 * acc;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) out->sigd[d][j] = dx / 3 * (double)ad[d];
+    }
+  }
+  for (int e = F32T ? (NDIR + 1) * NRT : t; e < (NDIR + 1) * NRT; e += blockDim.x) {
     const int comp = e / NRT, j = e % NRT;
     const double* w = pq + comp * NKH;
     double acc = 0.0;
@@ -261,6 +356,17 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
   for (int i = t; i < NCHI; i += blockDim.x) {
     out->chiv[i] = chi[i];
     for (int d = 0; d < NDIR; ++d) out->chid[d][i] = chi[(1 + d) * NCHI + i];
+  }
+  if (F32T) {
+    // float chi tables and segment slopes with tangents (the FP32 lensing stage)
+    for (int e = t; e < (NDIR + 1) * NCHI; e += blockDim.x) {
+      const int comp = e / NCHI, i = e % NCHI;
+      const double* ch = chi + comp * NCHI;
+      double sl = 0.0;
+      if (i + 1 < NCHI) sl = (ch[i + 1] - ch[i]) / (c->atab_chi[i + 1] - c->atab_chi[i]);
+      out->c32[comp][i] = (float)ch[i];
+      out->s32[comp][i] = (float)sl;
+    }
   }
   for (int i = t; i < NGROW; i += blockDim.x) {
     out->gv[i] = gt[i];
@@ -520,6 +626,228 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
       tg[T_NUN * NDIR + dir] = (float)outv[A_NU].d[0];
       tg[T_U * NDIR + dir] = (float)outv[A_U].d[0];
     }
+  }
+}
+
+// ------------------------------------------------------- fp32c rows -------
+__device__ __forceinline__ F8 interp_f8(double x, const double* xp, const double* fv, const double* fd,
+                                        int stride, int2 sg) {
+  const F8 f0 = f8_of(fv[sg.x], fd + sg.x, stride), f1 = f8_of(fv[sg.y], fd + sg.y, stride);
+  const F8 a = (f1 - f0) / (xp[sg.y] - xp[sg.x]);
+  const F8 b = f0 - a * xp[sg.x];
+  return a * x + b;
+}
+
+// fp32c Jacobian rows: one node per thread in DualF<8> (value FP64, the 8
+// tangents FP32), the same operations as grad_rows_kernel's FP32C path: root
+// find, moments (exp terms for y^2 in [1, 60], Taylor prefix tables below),
+// takahashi2012 coefficients, Limber weight; the row is written as computed.
+constexpr int GR32_THREADS = 64;
+
+__global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+  const int item = blockIdx.y;
+  if (item >= gb.n_items) return;
+  __shared__ double e2tab[64];
+  for (int i = threadIdx.x; i < 64; i += blockDim.x) e2tab[i] = kExp2Tab64[i];
+  __syncthreads();
+  const GradItem gi = grad_item(gb, item);
+  const GeoHeader* geo = gi.geo;
+  const int na = geo->na;
+  const int n = blockIdx.x * GR32_THREADS + threadIdx.x;
+  if (n >= na) return;
+  const TabD* tb = gi.tab;
+  const double* A = geo_ptr<double>(geo, geo->off_a);
+  const double* WS = geo_ptr<double>(geo, geo->off_wsimp);
+  const int64_t* SC = geo_ptr<int64_t>(geo, geo->off_seg_chi);
+  const int64_t* SG = geo_ptr<int64_t>(geo, geo->off_seg_grow);
+  const double a = A[n];
+  float* row = gi.rowg + (size_t)n * NROWG;
+  float* tg = row + NROW32;
+  auto put_t = [&](int slot, const F8& x, float sc) {
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) tg[slot * NDIR + d] = x.d[d] * sc;
+  };
+  F8 g = interp_f8(a, c->atab_grow, tb->gv, &tb->gd[0][0], NGROW, unpack_seg(SG[n]));
+  g = xfmin(xfmax(g, 0.0), 1.0);
+  F8 chi = interp_f8(a, c->atab_chi, tb->chiv, &tb->chid[0][0], NCHI, unpack_seg(SC[n]));
+  chi = xfmax(chi, 0.0);
+  const F8 g2 = g * g;
+  int best;
+  {
+    int lo = 0, hi = NRT;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (tb->sigv[mid] * g2.v > 1.0) lo = mid + 1;
+      else hi = mid;
+    }
+    const int cc = lo;
+    best = cc < NRT ? cc : NRT - 1;
+    if (cc >= 1) {
+      const double dlo = 1.0 - tb->sigv[cc - 1] * g2.v;
+      if (cc < NRT) {
+        const double dhi = 1.0 - tb->sigv[cc] * g2.v;
+        best = (dlo * dlo <= dhi * dhi) ? cc - 1 : cc;
+      } else {
+        best = cc - 1;
+      }
+    }
+  }
+  const int ind = best < 1 ? 1 : (best > NRT - 2 ? NRT - 2 : best);
+  const double xpi = tb->sigv[ind] * g2.v;
+  const double xc = fmin(fmax(1.0, tb->sigv[1] * g2.v), tb->sigv[NRT - 2] * g2.v);
+  const int j2 = ind + ((xc - xpi >= 0.0) ? 1 : -1);
+  const F8 xp0 = f8_of(tb->sigv[ind], &tb->sigd[0][ind], NRT) * g2;
+  const F8 xp1 = f8_of(tb->sigv[j2], &tb->sigd[0][j2], NRT) * g2;
+  const F8 slope = (c->logr[j2] - c->logr[ind]) / (xp1 - xp0);
+  const F8 bb = c->logr[ind] - slope * xp0;
+  const F8 root = slope * 1.0 + bb;
+  const F8 R = xfmax(xexp(root), 1e-6);
+  const F8 knl = 1.0 / R;
+  const F8 inv = 1.0 / knl;
+  row[F_LG2KNL] = (float)log2(knl.v);
+  row[F_INVKNL] = (float)(1.0 / knl.v);
+  put_t(T_KNL, knl, 1.f);
+  // moments
+  const double Rv = inv.v, iR = 1.0 / Rv, linv = log(Rv);
+  int ilo = (int)floor((0.5 * log(Y2_TAYLOR) - linv - LOG_KMIN) / DLOGK);
+  int ihi = (int)ceil((0.5 * log(Y2_SKIP) - linv - LOG_KMIN) / DLOGK);
+  ilo = max(0, min(ilo, NKH));
+  ihi = max(ilo - 1, min(ihi, NKH - 1));
+  const double q3s = 1.0 / TWO_PI2_G;
+  double s1 = 0, s2 = 0, s1r = 0, s2r = 0;
+  float s1d[NDIR], s2d[NDIR];
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) s1d[d] = s2d[d] = 0.f;
+  for (int i = ilo; i <= ihi; ++i) {
+    const double y = c->kh[i] * Rv;
+    const double y2 = y * y;
+    const double wq = c->simpson_kh[i] * exp_tang(-y2, e2tab) * q3s;
+    const double Av = wq * tb->pk3v[i];
+    const double c1 = 2.0 * y2, c2 = 4.0 * (y2 - y2 * y2);
+    s1 += Av * c1;
+    s2 += Av * c2;
+    s1r += 4.0 * Av * y2 * (1.0 - y2) * iR;
+    s2r += 8.0 * Av * y2 * (1.0 - 3.0 * y2 + y2 * y2) * iR;
+    const float w1 = (float)(wq * c1), w2 = (float)(wq * c2);
+    const float4 pa = *reinterpret_cast<const float4*>(&tb->pk3df[i][0]);
+    const float4 pb = *reinterpret_cast<const float4*>(&tb->pk3df[i][4]);
+    const float p[NDIR] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w};
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) {
+      s1d[d] = fmaf(w1, p[d], s1d[d]);
+      s2d[d] = fmaf(w2, p[d], s2d[d]);
+    }
+  }
+  double t1d[NDIR], t2d[NDIR];
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) t1d[d] = t2d[d] = 0.0;
+  if (ilo > 0) {
+    const double* T = gi.ptt + (size_t)ilo * NTAYLOR * (NDIR + 1);
+    const double R2 = Rv * Rv;
+    double pw = R2, dpw = 2.0 * Rv, fact = 1.0;
+    double t1 = 0, t2 = 0, t1r = 0, t2r = 0;
+    for (int m = 0; m < NTAYLOR - 1; ++m) {
+      const double sg = ((m & 1) ? -1.0 : 1.0) / fact;
+      const double* Tm = T + m * (NDIR + 1);
+      const double* Tm1 = Tm + (NDIR + 1);
+      const double pw1 = pw * R2, dpw1 = dpw * R2 + pw * 2.0 * Rv;
+      t1 += sg * Tm[0] * pw;
+      t2 += sg * (Tm[0] * pw - Tm1[0] * pw1);
+      t1r += sg * Tm[0] * dpw;
+      t2r += sg * (Tm[0] * dpw - Tm1[0] * dpw1);
+      const double a1 = sg * pw, a2 = sg * pw1;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) {
+        t1d[d] += a1 * Tm[1 + d];
+        t2d[d] += a1 * Tm[1 + d] - a2 * Tm1[1 + d];
+      }
+      pw = pw1;
+      dpw = dpw1;
+      fact *= (double)(m + 1);
+    }
+    s1 += 2.0 * t1;
+    s2 += 4.0 * t2;
+    s1r += 2.0 * t1r;
+    s2r += 4.0 * t2r;
+  }
+  F8 S1, S2;
+  S1.v = s1;
+  S2.v = s2;
+  const float f1r = (float)s1r, f2r = (float)s2r;
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) {
+    S1.d[d] = s1d[d] + (float)(2.0 * t1d[d]) + f1r * inv.d[d];
+    S2.d[d] = s2d[d] + (float)(4.0 * t2d[d]) + f2r * inv.d[d];
+  }
+  const F8 I1 = S1 * g2, I2 = S2 * g2;
+  const F8 neff = I1 - 3.0;
+  const F8 C = I1 * I1 + I2;
+  // coefficients (power.py:177-238)
+  BgT<F8> bg;
+  bg.Om = f8_of(tb->sv[S_OMEGA_M], &tb->sd[0][S_OMEGA_M], NSCAL);
+  bg.Ok = f8_of(tb->sv[S_OMEGA_K], &tb->sd[0][S_OMEGA_K], NSCAL);
+  bg.Ode = f8_of(tb->sv[S_OMEGA_DE], &tb->sd[0][S_OMEGA_DE], NSCAL);
+  bg.w0 = f8_of(tb->sv[S_W0], &tb->sd[0][S_W0], NSCAL);
+  bg.wa = f8_of(tb->sv[S_WA], &tb->sd[0][S_WA], NSCAL);
+  const double lna = log(a);
+  F8 om_m, om_de;
+  omT(bg, a, lna, om_m, om_de);
+  const F8 opw = om_de * (1.0 + wT(bg, a));
+  const F8 n2 = neff * neff, n3 = n2 * neff, n4 = n2 * n2;
+  {
+    const F8 beta = 2.0379 - 0.7354 * neff + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
+    row[F_BETAN] = (float)beta.v;
+    put_t(T_BETAN, beta, 1.f);
+    const F8 alpha = xfabs(6.0835 + 1.3373 * neff - 0.1959 * n2 - 5.5274 * C);
+    row[F_ALPHAN] = (float)alpha.v;
+    put_t(T_ALPHAN, alpha, 1.f);
+  }
+  {
+    const F8 e_an = 1.5222 + 2.8553 * neff + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 - 0.6038 * C + 0.1749 * opw;
+    const F8 an = xexp(LN10_G * e_an);
+    row[F_AN] = (float)an.v;
+    put_t(T_AN, an, 1.f);
+    const F8 e_bn = -0.5642 + 0.5864 * neff + 0.5716 * n2 - 1.5474 * C + 0.2279 * opw;
+    const F8 bn = xexp(LN10_G * e_bn);
+    row[F_BN] = (float)bn.v;
+    put_t(T_BN, bn, 1.f);
+  }
+  {
+    constexpr double LOG2E = 1.4426950408889634;
+    const F8 lom = xlog(om_m);
+    const F8 e_cn = 0.3698 + 2.0404 * neff + 0.8161 * n2 + 0.5869 * C;
+    const F8 lcf3 = LN10_G * e_cn + 0.0743 * lom;
+    row[F_LG2CF3] = (float)(LOG2E * lcf3.v);
+    put_t(T_LG2CF3, lcf3, (float)LOG2E);
+    const F8 f1 = xexp(-0.0307 * lom);
+    row[F_3F1] = (float)(3.0 * f1.v);
+    put_t(T_3F1, f1, 3.f);
+    const F8 f2 = xexp(-0.0585 * lom);
+    row[F_F2] = (float)f2.v;
+    put_t(T_F2, f2, 1.f);
+  }
+  {
+    const F8 gam = 0.1971 - 0.0843 * neff + 0.8460 * C;
+    row[F_3MGAMMA] = (float)(3.0 - gam.v);
+    put_t(T_3MG, gam, -1.f);
+    const F8 nu = xexp(LN10_G * (5.2105 + 3.6902 * neff));
+    row[F_NUN] = (float)nu.v;
+    put_t(T_NUN, nu, 1.f);
+  }
+  {
+    const F8 chic = xfmax(chi, 1.0);
+    row[F_INVCHI] = (float)(1.0 / chic.v);
+    row[F_LG2INVCHI] = (float)(-log2(chic.v));
+    row[F_CHIC] = (float)chic.v;
+    put_t(T_CHIC, chic, 1.f);
+    const F8 pkn = f8_of(tb->sv[S_PKNORM], &tb->sd[0][S_PKNORM], NSCAL);
+    const F8 d2fac = g * g * pkn / TWO_PI2_G;
+    row[F_D2FAC] = (float)d2fac.v;
+    put_t(T_D2FAC, d2fac, 1.f);
+    const F8 dchi = dchioverdaT(bg, a, lna);
+    const F8 u = WS[n] * dchi / xfmax(chi * chi, 1.0) / C2_G;
+    row[F_U] = (float)u.v;
+    put_t(T_U, u, 1.f);
   }
 }
 
@@ -947,10 +1275,20 @@ int grad_limber_tile(int n_ell, int n_cls) {
 
 void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
   const size_t smt = grad_tables_smem();
-  cudaFuncSetAttribute(grad_tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
-  grad_tables_kernel<<<gb.n_items, 256, smt, st>>>(gb, c);
-  dim3 grw((gb.na + 31) / 32, gb.n_items);
-  grad_rows_kernel<<<grw, 256, 0, st>>>(gb, c);
+  if (gb.precision == JCG_FP32C) {
+    cudaFuncSetAttribute(grad_tables_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+    grad_tables_kernel<true><<<gb.n_items, 256, smt, st>>>(gb, c);
+  } else {
+    cudaFuncSetAttribute(grad_tables_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+    grad_tables_kernel<false><<<gb.n_items, 256, smt, st>>>(gb, c);
+  }
+  if (gb.precision == JCG_FP32C) {
+    dim3 grw((gb.na + GR32_THREADS - 1) / GR32_THREADS, gb.n_items);
+    grad_rows32_kernel<<<grw, GR32_THREADS, 0, st>>>(gb, c);
+  } else {
+    dim3 grw((gb.na + 31) / 32, gb.n_items);
+    grad_rows_kernel<<<grw, 256, 0, st>>>(gb, c);
+  }
   dim3 gr((gb.na + 7) / 8, gb.n_items);
   if (gb.precision == JCG_FP32C) {
     launch_grad_kern32(gb, c, st);

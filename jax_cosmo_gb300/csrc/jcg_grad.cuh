@@ -16,6 +16,17 @@ __device__ __forceinline__ D1 mk1(double v, double d) {
   return r;
 }
 
+typedef DualF<NDIR> F8;
+
+// DualF<8> from a value and 8 double tangents at stride `stride`
+__device__ __forceinline__ F8 f8_of(double v, const double* d, int stride) {
+  F8 r;
+  r.v = v;
+#pragma unroll
+  for (int i = 0; i < NDIR; ++i) r.d[i] = (float)d[i * stride];
+  return r;
+}
+
 constexpr double TWO_PI2_G = 2.0 * (PI * PI);
 constexpr double C2_G = C_KMS * C_KMS;
 constexpr double LN10_G = 2.302585092994046;
@@ -33,6 +44,11 @@ struct TabD {
   double pk3v[NKH];
   double pk3d[NDIR][NKH];
   double pad[7];
+  // fp32c Jacobian only: float copies for the FP32 stages
+  float c32[NDIR + 1][NCHI];   // chi (row 0) and its tangents
+  float s32[NDIR + 1][NCHI];   // segment slopes (chi[i+1] - chi[i]) / (a[i+1] - a[i]) and tangents
+  float pk3df[NKH][NDIR];      // P(k) k^3 tangents, node-major
+  float padf[8];
 };
 static_assert(sizeof(TabD) % 64 == 0, "TabD alignment");
 

@@ -23,7 +23,7 @@ namespace jcg {
 //   r_j = max(chi'_j - chi, 0) / max(chi'_j, 1)
 //   dr_j = ic_j (dchi'_j (1 - r_j [chi'_j > 1]) - dchi)  where chi'_j > chi
 // accumulated as sum W r, sum W ic, sum W ic (1 - r) dchi'.
-constexpr int GK_NODES = 64;  // nodes per CTA (8 warps x 8)
+constexpr int GK_NODES = 128;  // nodes per CTA (8 warps x 16)
 
 __global__ void __launch_bounds__(256) grad_kern32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
@@ -33,23 +33,24 @@ __global__ void __launch_bounds__(256) grad_kern32_kernel(GradBatch gb, const Co
   const int na = geo->na, n_tr = geo->n_tr;
   const int n0 = blockIdx.x * GK_NODES;
   if (n0 >= na) return;
-  __shared__ float chi[NCHI], slope[NCHI];
-  __shared__ float dchi[NDIR][NCHI], dslope[NDIR][NCHI];
+  __shared__ __align__(16) float ctab[NDIR + 1][NCHI];  // chi, then its tangents
+  __shared__ __align__(16) float stab[NDIR + 1][NCHI];  // segment slopes, then tangents
   const TabD* tb = gi.tab;
-  for (int i = threadIdx.x; i < NCHI; i += blockDim.x) {
-    chi[i] = (float)tb->chiv[i];
-    double sl = 0.0;
-    if (i + 1 < NCHI) sl = (tb->chiv[i + 1] - tb->chiv[i]) / (c->atab_chi[i + 1] - c->atab_chi[i]);
-    slope[i] = (float)sl;
-  }
-  for (int e = threadIdx.x; e < NDIR * NCHI; e += blockDim.x) {
-    const int d = e / NCHI, i = e % NCHI;
-    dchi[d][i] = (float)tb->chid[d][i];
-    double sl = 0.0;
-    if (i + 1 < NCHI) sl = (tb->chid[d][i + 1] - tb->chid[d][i]) / (c->atab_chi[i + 1] - c->atab_chi[i]);
-    dslope[d][i] = (float)sl;
+  {
+    const float4* sc = reinterpret_cast<const float4*>(&tb->c32[0][0]);
+    const float4* ss = reinterpret_cast<const float4*>(&tb->s32[0][0]);
+    float4* dc = reinterpret_cast<float4*>(&ctab[0][0]);
+    float4* ds = reinterpret_cast<float4*>(&stab[0][0]);
+    for (int i = threadIdx.x; i < (NDIR + 1) * NCHI / 4; i += blockDim.x) {
+      dc[i] = sc[i];
+      ds[i] = ss[i];
+    }
   }
   __syncthreads();
+  const float* chi = ctab[0];
+  const float* slope = stab[0];
+  const float(*dchi)[NCHI] = ctab + 1;
+  const float(*dslope)[NCHI] = stab + 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double* Z = geo_ptr<double>(geo, geo->off_z);
   const double* AWL = geo_ptr<double>(geo, geo->off_awl);
@@ -152,9 +153,12 @@ __global__ void __launch_bounds__(256) grad_kern32_kernel(GradBatch gb, const Co
             kd = fac * (dcf * cw * acc + cf * (double)dcw * acc +
                         cf * cw * ((double)adir - (double)dcw * (double)at[u]));
           } else {
-            D1 sD[NSCAL];
-            for (int i = 0; i < NSCAL; ++i) sD[i] = mk1(tb->sv[i], tb->sd[dir][i]);
-            const BgT<D1> bg = make_bgT(sD);
+            BgT<D1> bg;
+            bg.Om = mk1(tb->sv[S_OMEGA_M], tb->sd[dir][S_OMEGA_M]);
+            bg.Ok = mk1(tb->sv[S_OMEGA_K], tb->sd[dir][S_OMEGA_K]);
+            bg.Ode = mk1(tb->sv[S_OMEGA_DE], tb->sd[dir][S_OMEGA_DE]);
+            bg.w0 = mk1(tb->sv[S_W0], tb->sd[dir][S_W0]);
+            bg.wa = mk1(tb->sv[S_WA], tb->sd[dir][S_WA]);
             const double awl = AWL[n];
             const D1 H = H0 * xsqrt(esqrT(bg, awl, log(awl), (D1*)nullptr));
             const double w = NZL[(size_t)t * na + n] * geo->bias[t];
