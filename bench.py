@@ -201,6 +201,14 @@ def gpu_arm(args, rank, world, device):
         torch.cuda.synchronize(device)
         return float(np.sum(times)), times
 
+    if args.jacobian_only:
+        # the fp32c Jacobian alone (a profiling entry: one kernel family per launch list)
+        from jax_cosmo_gb300.autodiff import jacobian_device
+
+        tj, _ = timed(lambda: jacobian_device(params, ell_np, probes, 512, "fp32c"), args.steps, args.warmup)
+        return {"jacobian_only": {"batch": B, "ms_per_step": tj / args.steps,
+                                  "cl_grad_per_s": B * 15 * N_ELL / (tj / args.steps * 1e-3)}}
+
     # headline: fp32c, inputs resident
     clocks = ClockSampler(device.index)
     clocks.start()
@@ -278,17 +286,24 @@ def gpu_arm(args, rank, world, device):
     res["plain_fp64_single"] = {"ms_per_call": t1 / args.steps,
                                 "cl_per_s": n_cls * n_ell / (t1 / args.steps * 1e-3)}
 
-    # C_ell + dC_ell/dtheta (8 leaves), float64, whole batch
+    # C_ell + dC_ell/dtheta (8 leaves), whole batch: fp32c and the plain fp64 form
     from jax_cosmo_gb300.autodiff import jacobian_device
 
-    kj = max(1, min(args.steps, 3))
-    tj, _ = timed(lambda: jacobian_device(params, ell_np, probes, 512), kj, 1)
-    res["jacobian"] = {"batch": B, "ms_per_step": tj / kj, "dtype": "f64",
-                       "cl_grad_per_s": ncl_step / (tj / kj * 1e-3)}
-    cl_j, jac = jacobian_device(params[:64].contiguous(), ell_np, probes, 512)
-    step("fp64")
-    res["jacobian"]["cl_max_rel_err_vs_fp64"] = float(((cl_j - cl[:64]).abs() / cl[:64].abs()).max())
-    del jac
+    res["jacobian"] = {}
+    for prec in ("fp32c", "fp64"):
+        kj = max(1, min(args.steps, 5 if prec == "fp32c" else 2))
+        tj, _ = timed(lambda p=prec: jacobian_device(params, ell_np, probes, 512, p), kj, 1)
+        res["jacobian"][prec] = {"batch": B, "ms_per_step": tj / kj, "steps": kj,
+                                 "cl_grad_per_s": ncl_step / (tj / kj * 1e-3)}
+    # accuracy of the fp32c Jacobian against the fp64 one (64 cosmologies of the batch)
+    p64 = params[:64].contiguous()
+    c64, j64 = jacobian_device(p64, ell_np, probes, 512, "fp64")
+    c32, j32 = jacobian_device(p64, ell_np, probes, 512, "fp32c")
+    scale = j64.abs().amax(dim=(1, 2), keepdim=True)
+    res["jacobian"]["fp32c"]["cl_max_rel_err_vs_fp64"] = float(((c32 - c64) / c64).abs().max())
+    res["jacobian"]["fp32c"]["jac_max_err_vs_fp64"] = float(((j32 - j64).abs() / scale).max())
+    res["jacobian"]["fp32c"]["jac_err_note"] = "max |J32 - J64| / max |J64| per (cosmology, parameter)"
+    del j64, j32
     return res
 
 
@@ -429,6 +444,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-serving", action="store_true")
     ap.add_argument("--serve-seconds", type=float, default=10.0)
+    ap.add_argument("--jacobian-only", action="store_true",
+                    help="time only the fp32c C_ell + Jacobian of the batch (profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -477,6 +494,10 @@ def main():
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
     res = gpu_arm(args, rank, world, device)
+    if "jacobian_only" in res:
+        if rank == 0:
+            print(json.dumps(res["jacobian_only"]))
+        return
     serve = None
     if rank == 0 and not args.no_serving:
         serve = serving_arm(device, duration_s=args.serve_seconds)
@@ -490,7 +511,8 @@ def main():
     rl, rl_sfu = roofline(res, args.batch)
     plain = res["plain_fp64_single"]["cl_per_s"]
     jac = res["jacobian"]
-    jac["over_plain_fp64_single"] = jac["cl_grad_per_s"] / plain
+    for prec in jac:
+        jac[prec]["over_plain_fp64_single"] = jac[prec]["cl_grad_per_s"] / plain
     out = {
         "metric": "C_ell evals/s batched vs plain at \u22641e-4 rel err; p50/p99 loglike+grad latency",
         "value": value, "unit": "C_ell/s", "n_gpus": world, "steps": K, "warmup": args.warmup,

@@ -38,7 +38,7 @@ __device__ __forceinline__ D1 interp_d1(double x, const double* xp, const double
 // P(k) k^3 tangent tables are written for the FP32 stages.  The sequential
 // scans (chi prefix sum, growth RK4, Romberg) stay FP64 Dual<1>.
 template <bool F32T>
-__global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+__global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.x;
   if (item >= gb.n_items) return;
   extern __shared__ double sm[];
@@ -48,14 +48,13 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
   double* fm = fn + (NDIR + 1) * NCHI;  // [NDIR+1][NCHI] f at midpoints
   double* qr = fm + (NDIR + 1) * NCHI;  // [4][NDIR+1][NGROW] qa, ra, qm, rm
   double* fr = qr + 4 * (NDIR + 1) * NGROW;   // [NDIR+1][NROMB]
-  double* chi = fr + (NDIR + 1) * NROMB;      // [NDIR+1][NCHI]
-  double* gt = chi + (NDIR + 1) * NCHI;       // [NDIR+1][NGROW]
-  double* pq = gt + (NDIR + 1) * NGROW;       // [NDIR+1][NKH]
-  double* g1s = pq + (NDIR + 1) * NKH;        // [NDIR+1]
+  double* g1s = fr + (NDIR + 1) * NROMB;      // [NDIR+1]
+  double* pq = qr;                            // [NDIR+1][NKH], after the growth RK4
   const int t = threadIdx.x, dir = t & 7, it = t >> 3;
   const GradItem gi = grad_item(gb, item);
   const double* P = gi.params;
   TabD* out = gi.tab;
+  // the chi and growth tables go straight to the output (read back after a barrier)
   // scalars (lanes 0-7 of warp 0)
   if (t < NDIR) {
     D1 p[8];
@@ -173,8 +172,8 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
       }
       for (int i = 0; i < NCHI; ++i) {
         const D1 v = ys[NCHI - 1] - ys[i];
-        if (d == 0) chi[i] = v.v;
-        chi[(1 + d) * NCHI + i] = v.d[0];
+        if (d == 0) out->chiv[i] = v.v;
+        out->chid[d][i] = v.d[0];
       }
     } else if (warp == 1) {
       // growth RK4 in a (background.py:108-111)
@@ -203,8 +202,8 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
       }
       for (int i = 0; i < NGROW; ++i) {
         const D1 v = ys[i] / y0;
-        if (d == 0) gt[i] = v.v;
-        gt[(1 + d) * NGROW + i] = v.d[0];
+        if (d == 0) out->gv[i] = v.v;
+        out->gd[d][i] = v.d[0];
       }
     } else if (warp == 2) {
       // romb combination (scipy/integrate.py:131-159), divmax = 7
@@ -244,7 +243,7 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
   if (t < NDIR) {
     // growth_factor(1.0)
     const int2 sg = interp_segment_inc(1.0, c->atab_grow, NGROW, NGROW - 1);
-    D1 g1 = interp_d1(1.0, c->atab_grow, gt, gt + (1 + dir) * NGROW, sg);
+    D1 g1 = interp_d1(1.0, c->atab_grow, out->gv, out->gd[dir], sg);
     g1 = xfmin(xfmax(g1, 0.0), 1.0);
     if (dir == 0) g1s[0] = g1.v;
     g1s[1 + dir] = g1.d[0];
@@ -278,20 +277,31 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
     }
   }
   __syncthreads();
-  if (gi.ptt) {
-    // Taylor prefix tables (fp32c moments): ptt[i][m][s] = sum_{k < i} w_k q3_k kh_k^(2(m+1)),
-    // s = 0 value, 1..8 tangents; one warp per component s, lanes over k
+  if (F32T && gi.ptt) {
+    // Taylor prefix tables of the fp32c moments.  Values (FP64, warp 0, the
+    // forward's tables): P_m[i] = sum_{k < i} w_k q3_k kh_k^(2(m+1)).  Tangents
+    // (FP32, one thread per (m, d)), scaled to the table row so that no power
+    // of k overflows: Q_m[i] = sum_{k < i} w_k dq3_k (kh_k / kh_i)^(2(m+1)),
+    // kh_i = exp(ln 1e-4 + i dlnk), by the contracting recurrence
+    // Q_m[i+1] = (Q_m[i] + w_i dq3_i) (kh_i / kh_{i+1})^(2(m+1)).
     const int warp = t >> 5, lane = t & 31;
-    for (int sc = warp; sc < NDIR + 1; sc += (int)(blockDim.x >> 5)) {
-      const double* w = pq + sc * NKH;
-      if (lane < NTAYLOR) gi.ptt[(size_t)lane * (NDIR + 1) + sc] = 0.0;
+    double* pv = gi.ptt;
+    float* pdv = ptt_tangents(gi.ptt);
+    float* pqw = reinterpret_cast<float*>(fn);  // [NKH][NDIR] w dq3, fn is free here
+    for (int e = t; e < NDIR * NKH; e += blockDim.x) {
+      const int d = e / NKH, i = e % NKH;
+      pqw[i * NDIR + d] = (float)(c->simpson_kh[i] * pq[(1 + d) * NKH + i]);
+    }
+    __syncthreads();
+    if (warp == 0) {
+      if (lane < NTAYLOR) pv[lane] = 0.0;
       double carry[NTAYLOR];
 #pragma unroll
       for (int m = 0; m < NTAYLOR; ++m) carry[m] = 0.0;
       for (int base = 0; base < NKH; base += 32) {
         const int i = base + lane;
         const double k2 = i < NKH ? c->kh[i] * c->kh[i] : 0.0;
-        double v = i < NKH ? c->simpson_kh[i] * w[i] : 0.0;
+        double v = i < NKH ? c->simpson_kh[i] * pq[i] : 0.0;
 #pragma unroll
         for (int m = 0; m < NTAYLOR; ++m) {
           v *= k2;
@@ -301,11 +311,22 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
             const double u = __shfl_up_sync(0xffffffffu, x, o);
             if (lane >= o) x += u;
           }
-          if (i < NKH) gi.ptt[((size_t)(i + 1) * NTAYLOR + m) * (NDIR + 1) + sc] = carry[m] + x;
+          if (i < NKH) pv[(size_t)(i + 1) * NTAYLOR + m] = carry[m] + x;
           carry[m] += __shfl_sync(0xffffffffu, x, 31);
         }
       }
     }
+    for (int job = t; job < NTAYLOR * NDIR; job += blockDim.x) {
+      const int m = job / NDIR, d = job % NDIR;
+      const float rho = (float)exp(-2.0 * DLOGK * (m + 1));
+      float acc = 0.f;
+      pdv[(size_t)m * NDIR + d] = 0.f;
+      for (int i = 0; i < NKH; ++i) {
+        acc = (acc + pqw[i * NDIR + d]) * rho;
+        pdv[((size_t)(i + 1) * NTAYLOR + m) * NDIR + d] = acc;
+      }
+    }
+    __syncthreads();
   }
   // sigma^2(R_j) without g^2 (power.py:98-111), value and tangents
   const double dx = (c->logk[NKH - 1] - c->logk[0]) / 256;
@@ -353,33 +374,27 @@ __global__ void __launch_bounds__(256) grad_tables_kernel(GradBatch gb, const Co
     out->sv[i] = sv[i];
     for (int d = 0; d < NDIR; ++d) out->sd[d][i] = sd[d * NSCAL + i];
   }
-  for (int i = t; i < NCHI; i += blockDim.x) {
-    out->chiv[i] = chi[i];
-    for (int d = 0; d < NDIR; ++d) out->chid[d][i] = chi[(1 + d) * NCHI + i];
-  }
   if (F32T) {
     // float chi tables and segment slopes with tangents (the FP32 lensing stage)
     for (int e = t; e < (NDIR + 1) * NCHI; e += blockDim.x) {
       const int comp = e / NCHI, i = e % NCHI;
-      const double* ch = chi + comp * NCHI;
+      const double* ch = comp == 0 ? out->chiv : out->chid[comp - 1];
       double sl = 0.0;
       if (i + 1 < NCHI) sl = (ch[i + 1] - ch[i]) / (c->atab_chi[i + 1] - c->atab_chi[i]);
       out->c32[comp][i] = (float)ch[i];
       out->s32[comp][i] = (float)sl;
     }
   }
-  for (int i = t; i < NGROW; i += blockDim.x) {
-    out->gv[i] = gt[i];
-    for (int d = 0; d < NDIR; ++d) out->gd[d][i] = gt[(1 + d) * NGROW + i];
-  }
 }
 
 size_t grad_tables_smem() {
-  return sizeof(double) * (NSCAL * (1 + NDIR) + (NDIR + 1) * (2 * NCHI + 4 * NGROW + NROMB + NCHI + NGROW + NKH + 1));
+  static_assert(4 * NGROW >= NKH, "P(k) k^3 staging aliases the growth coefficients");
+  return sizeof(double) * (NSCAL * (1 + NDIR) + (NDIR + 1) * (2 * NCHI + 4 * NGROW + NROMB + 1));
 }
 
 // ----------------------------------------------------------- dual rows -----
-// One warp per 4 Limber nodes: lane = 8 * node slot + tangent direction.
+// FP64 Jacobian rows.  One warp per 4 Limber nodes: lane = 8 * node slot +
+// tangent direction.
 //   prelude (per lane, Dual<1>): growth, chi, the root find (index from the
 //     values with the forward's arithmetic, tangent through the interpolation
 //     formula), R = 1 / k_nl;
@@ -387,17 +402,12 @@ size_t grad_tables_smem() {
 //     with their R-derivatives and their P(k) k^3 tangents:
 //       S1 = sum w q3 2 y^2 e^{-y^2},  S2 = sum w q3 4 (y^2 - y^4) e^{-y^2},
 //       y = k R, q3 = P(k) k^3 / (2 pi^2);  dS = S_q3[d] + dS/dR dR[d];
-//     FP32C: exp only for y^2 in [1, 60], below it the Taylor series of
-//     e^{-y^2} on prefix tables of w q3 k^(2(m+1)) and their tangents (ptt),
-//     as the forward fp32c rows do; FP64: every term with y^2 <= 60;
+//     every term with y^2 <= 60 (the rest is below 1e-20 of the sums);
 //   epilogue (per lane, Dual<1>): n_eff, C, takahashi2012 coefficients, the
 //     Limber weight; rows out.
 __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
-  __shared__ double e2tab[64];
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) e2tab[i] = kExp2Tab64[i];
-  __syncthreads();
   const GradItem gi = grad_item(gb, item);
   const GeoHeader* geo = gi.geo;
   const int na = geo->na;
@@ -408,7 +418,6 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
   const int n_raw = n_first + slot;
   const bool live = n_raw < na;
   const int n = live ? n_raw : na - 1;  // dead slots evaluate a valid node, write nothing
-  const bool fast = gb.precision == JCG_FP32C;
   const TabD* tb = gi.tab;
   const double* A = geo_ptr<double>(geo, geo->off_a);
   const double* WS = geo_ptr<double>(geo, geo->off_wsimp);
@@ -452,15 +461,7 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
   const D1 R = xfmax(xexp(root), 1e-6);
   const D1 knl = 1.0 / R;
   const D1 inv = 1.0 / knl;
-  // exp range [ilo, ihi] of this lane's node (the forward fp32c rows' rule)
-  int ilo = 0, ihi = NKH - 1;
-  if (fast) {
-    const double linv = log(inv.v);
-    ilo = (int)floor((0.5 * log(Y2_TAYLOR) - linv - LOG_KMIN) / DLOGK);
-    ihi = (int)ceil((0.5 * log(Y2_SKIP) - linv - LOG_KMIN) / DLOGK);
-    ilo = max(0, min(ilo, NKH));
-    ihi = max(ilo - 1, min(ihi, NKH - 1));
-  }
+  const int ilo = 0, ihi = NKH - 1;
   // explicit terms, node by node over the warp
   double m_s1 = 0, m_s2 = 0, m_s1r = 0, m_s2r = 0, m_s1d = 0, m_s2d = 0;
   const double q3s = 1.0 / TWO_PI2_G;
@@ -474,8 +475,8 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
     for (int i = lo + lane; i <= hi; i += 32) {
       const double y = c->kh[i] * Rq;
       const double y2 = y * y;
-      if (!fast && y2 > Y2_SKIP) continue;
-      const double E = fast ? exp_tang(-y2, e2tab) : exp(-y2);
+      if (y2 > Y2_SKIP) continue;
+      const double E = exp(-y2);
       const double wq = c->simpson_kh[i] * E * q3s;
       const double Av = wq * tb->pk3v[i];
       const double c1 = 2.0 * y2, c2 = 4.0 * (y2 - y2 * y2);
@@ -515,34 +516,6 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
           m_s2d = s2d[d];
         }
     }
-  }
-  // Taylor part below ilo: sum_m (-1)^m / m! R^(2m+2) T_m
-  if (fast && ilo > 0) {
-    const double* T = gi.ptt + (size_t)ilo * NTAYLOR * (NDIR + 1);
-    const double Rv = inv.v, R2 = Rv * Rv;
-    double pw = R2, dpw = 2.0 * Rv, fact = 1.0;
-    double t1 = 0, t2 = 0, t1r = 0, t2r = 0, t1d = 0, t2d = 0;
-    for (int m = 0; m < NTAYLOR - 1; ++m) {
-      const double sg = ((m & 1) ? -1.0 : 1.0) / fact;
-      const double Tm = T[m * (NDIR + 1)], Tm1 = T[(m + 1) * (NDIR + 1)];
-      const double Dm = T[m * (NDIR + 1) + 1 + dir], Dm1 = T[(m + 1) * (NDIR + 1) + 1 + dir];
-      const double pw1 = pw * R2, dpw1 = dpw * R2 + pw * 2.0 * Rv;  // R^(2m+4) and its R-derivative
-      t1 += sg * Tm * pw;
-      t2 += sg * (Tm * pw - Tm1 * pw1);
-      t1r += sg * Tm * dpw;
-      t2r += sg * (Tm * dpw - Tm1 * dpw1);
-      t1d += sg * Dm * pw;
-      t2d += sg * (Dm * pw - Dm1 * pw1);
-      pw = pw1;
-      dpw = dpw1;
-      fact *= (double)(m + 1);
-    }
-    m_s1 += 2.0 * t1;
-    m_s2 += 4.0 * t2;
-    m_s1r += 2.0 * t1r;
-    m_s2r += 4.0 * t2r;
-    m_s1d += 2.0 * t1d;
-    m_s2d += 4.0 * t2d;
   }
   // moments with their tangents in this lane's direction, times g^2
   const D1 S1 = mk1(m_s1, m_s1d + m_s1r * inv.d[0]);
@@ -738,28 +711,37 @@ __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb,
       s2d[d] = fmaf(w2, p[d], s2d[d]);
     }
   }
-  double t1d[NDIR], t2d[NDIR];
+  float t1d[NDIR], t2d[NDIR];
 #pragma unroll
-  for (int d = 0; d < NDIR; ++d) t1d[d] = t2d[d] = 0.0;
+  for (int d = 0; d < NDIR; ++d) t1d[d] = t2d[d] = 0.f;
   if (ilo > 0) {
-    const double* T = gi.ptt + (size_t)ilo * NTAYLOR * (NDIR + 1);
+    const double* T = gi.ptt + (size_t)ilo * NTAYLOR;
+    const float* TD = ptt_tangents(gi.ptt) + (size_t)ilo * NTAYLOR * NDIR;
     const double R2 = Rv * Rv;
-    double pw = R2, dpw = 2.0 * Rv, fact = 1.0;
+    // tangent tables are scaled by kh_ilo^-(2(m+1)): powers of yl = R kh_ilo (<= ~1)
+    const double yl2 = R2 * exp(2.0 * (LOG_KMIN + ilo * DLOGK));
+    double pw = R2, dpw = 2.0 * Rv, fact = 1.0, ps = yl2;
     double t1 = 0, t2 = 0, t1r = 0, t2r = 0;
     for (int m = 0; m < NTAYLOR - 1; ++m) {
       const double sg = ((m & 1) ? -1.0 : 1.0) / fact;
-      const double* Tm = T + m * (NDIR + 1);
-      const double* Tm1 = Tm + (NDIR + 1);
       const double pw1 = pw * R2, dpw1 = dpw * R2 + pw * 2.0 * Rv;
-      t1 += sg * Tm[0] * pw;
-      t2 += sg * (Tm[0] * pw - Tm1[0] * pw1);
-      t1r += sg * Tm[0] * dpw;
-      t2r += sg * (Tm[0] * dpw - Tm1[0] * dpw1);
-      const double a1 = sg * pw, a2 = sg * pw1;
+      const double ps1 = ps * yl2;
+      t1 += sg * T[m] * pw;
+      t2 += sg * (T[m] * pw - T[m + 1] * pw1);
+      t1r += sg * T[m] * dpw;
+      t2r += sg * (T[m] * dpw - T[m + 1] * dpw1);
+      const float a1 = (float)(sg * ps), a2 = (float)(sg * ps1);
+      ps = ps1;
+      const float4 u0 = *reinterpret_cast<const float4*>(TD + m * NDIR);
+      const float4 u1 = *reinterpret_cast<const float4*>(TD + m * NDIR + 4);
+      const float4 v0 = *reinterpret_cast<const float4*>(TD + (m + 1) * NDIR);
+      const float4 v1 = *reinterpret_cast<const float4*>(TD + (m + 1) * NDIR + 4);
+      const float dm[NDIR] = {u0.x, u0.y, u0.z, u0.w, u1.x, u1.y, u1.z, u1.w};
+      const float dm1[NDIR] = {v0.x, v0.y, v0.z, v0.w, v1.x, v1.y, v1.z, v1.w};
 #pragma unroll
       for (int d = 0; d < NDIR; ++d) {
-        t1d[d] += a1 * Tm[1 + d];
-        t2d[d] += a1 * Tm[1 + d] - a2 * Tm1[1 + d];
+        t1d[d] = fmaf(a1, dm[d], t1d[d]);
+        t2d[d] = fmaf(a1, dm[d], fmaf(-a2, dm1[d], t2d[d]));
       }
       pw = pw1;
       dpw = dpw1;
@@ -776,8 +758,8 @@ __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb,
   const float f1r = (float)s1r, f2r = (float)s2r;
 #pragma unroll
   for (int d = 0; d < NDIR; ++d) {
-    S1.d[d] = s1d[d] + (float)(2.0 * t1d[d]) + f1r * inv.d[d];
-    S2.d[d] = s2d[d] + (float)(4.0 * t2d[d]) + f2r * inv.d[d];
+    S1.d[d] = s1d[d] + 2.f * t1d[d] + f1r * inv.d[d];
+    S2.d[d] = s2d[d] + 4.f * t2d[d] + f2r * inv.d[d];
   }
   const F8 I1 = S1 * g2, I2 = S2 * g2;
   const F8 neff = I1 - 3.0;
@@ -1277,7 +1259,7 @@ void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
   const size_t smt = grad_tables_smem();
   if (gb.precision == JCG_FP32C) {
     cudaFuncSetAttribute(grad_tables_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
-    grad_tables_kernel<true><<<gb.n_items, 256, smt, st>>>(gb, c);
+    grad_tables_kernel<true><<<gb.n_items, 128, smt, st>>>(gb, c);
   } else {
     cudaFuncSetAttribute(grad_tables_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
     grad_tables_kernel<false><<<gb.n_items, 256, smt, st>>>(gb, c);
@@ -1350,7 +1332,7 @@ static size_t kern_bytes(const GeoHeader& h, int precision) {
 }
 // Taylor prefix tables of the fp32c moments, per cosmology
 static size_t ptt_bytes(int precision) {
-  return precision == JCG_FP32C ? al256(sizeof(double) * NPTT) : 0;
+  return precision == JCG_FP32C ? PTT_STRIDE * sizeof(double) : 0;
 }
 
 size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {

@@ -18,6 +18,7 @@ __device__ __forceinline__ D1 mk1(double v, double d) {
 
 typedef DualF<NDIR> F8;
 
+
 // DualF<8> from a value and 8 double tangents at stride `stride`
 __device__ __forceinline__ F8 f8_of(double v, const double* d, int stride) {
   F8 r;
@@ -68,7 +69,14 @@ __device__ __constant__ const int kNodeCScalar[NC_IN] = {S_K_EQ,  S_SH_D,      S
 enum GTan { T_CHIC = 0, T_D2FAC, T_KNL, T_BETAN, T_ALPHAN, T_AN, T_3F1, T_F2, T_BN, T_LG2CF3, T_3MG,
             T_NUN, T_U, NGT };
 constexpr int F_U = 15;
-constexpr int NPTT = (NKH + 1) * NTAYLOR * (NDIR + 1);  // Taylor prefix table entries
+// Taylor prefix tables of the fp32c moments, per cosmology: values double
+// [NKH + 1][NTAYLOR], then tangents float [NKH + 1][NTAYLOR][NDIR]
+constexpr int NPTTV = (NKH + 1) * NTAYLOR;
+constexpr size_t PTT_STRIDE = ((size_t)NPTTV * 8 + (size_t)NPTTV * NDIR * 4 + 255) / 256 * 256 / 8;  // doubles
+__device__ __forceinline__ float* ptt_tangents(double* p) { return reinterpret_cast<float*>(p + NPTTV); }
+__device__ __forceinline__ const float* ptt_tangents(const double* p) {
+  return reinterpret_cast<const float*>(p + NPTTV);
+}
 constexpr int NROWG = NROW32 + NGT * NDIR;  // 120 floats
 // per-cosmology Eisenstein-Hu inputs of the FP32 integrand with tangents
 enum ETan { E_KEQ = 0, E_SH, E_C18BC, E_C142AC, E_ALPHAB, E_BETAB, E_BETANODE, E_LG2KSILK, E_FB, E_FC,
@@ -84,7 +92,7 @@ struct GradItem {
   double* kernd;   // [n_tr][na][NDIR + 1]
   float* rowg;     // [na][NROWG]
   float* kernf;    // [n_tr][na][NDIR + 1]
-  double* ptt;     // FP32C: [NKH + 1][NTAYLOR][NDIR + 1] Taylor prefix tables
+  double* ptt;     // FP32C: Taylor prefix tables (values, then float tangents)
   double* part;    // [n_split][n_cls][n_ell][NDIR + 1] partial sums over a
   double* cl;      // [n_cls][n_ell] (may be NULL)
   double* jac;     // [n_cls][n_ell][NDIR]
@@ -122,7 +130,7 @@ __device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
   r.kernd = gb.kernd ? gb.kernd + (size_t)i * gb.n_tr * gb.na * (NDIR + 1) : nullptr;
   r.rowg = gb.rowg ? gb.rowg + (size_t)i * gb.na * NROWG : nullptr;
   r.kernf = gb.kernf ? gb.kernf + (size_t)i * gb.n_tr * gb.na * (NDIR + 1) : nullptr;
-  r.ptt = gb.ptt ? gb.ptt + (size_t)i * ((NPTT + 31) & ~31) : nullptr;
+  r.ptt = gb.ptt ? gb.ptt + (size_t)i * PTT_STRIDE : nullptr;
   r.part = gb.part + (size_t)i * gb.n_split * per * (NDIR + 1);
   r.cl = gb.cl ? gb.cl + (size_t)i * per : nullptr;
   r.jac = gb.jac + (size_t)i * per * NDIR;

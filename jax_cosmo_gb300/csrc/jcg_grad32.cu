@@ -25,7 +25,20 @@ namespace jcg {
 // accumulated as sum W r, sum W ic, sum W ic (1 - r) dchi'.
 constexpr int GK_NODES = 128;  // nodes per CTA (8 warps x 16)
 
-__global__ void __launch_bounds__(256) grad_kern32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+// NumberCounts kernel n(z) b H(a) (probes.py:94) and its tangent in direction dir
+__device__ __noinline__ void nc_kernel_d1(const TabD* tb, int dir, double awl, double w, float* kv, float* kd) {
+  BgT<D1> bg;
+  bg.Om = mk1(tb->sv[S_OMEGA_M], tb->sd[dir][S_OMEGA_M]);
+  bg.Ok = mk1(tb->sv[S_OMEGA_K], tb->sd[dir][S_OMEGA_K]);
+  bg.Ode = mk1(tb->sv[S_OMEGA_DE], tb->sd[dir][S_OMEGA_DE]);
+  bg.w0 = mk1(tb->sv[S_W0], tb->sd[dir][S_W0]);
+  bg.wa = mk1(tb->sv[S_WA], tb->sd[dir][S_WA]);
+  const D1 H = H0 * xsqrt(esqrT(bg, awl, log(awl), (D1*)nullptr));
+  *kv = (float)(w * H.v);
+  *kd = (float)(w * H.d[0]);
+}
+
+__global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
   const GradItem gi = grad_item(gb, item);
@@ -58,9 +71,9 @@ __global__ void __launch_bounds__(256) grad_kern32_kernel(GradBatch gb, const Co
   const float* DXWL = geo_ptr<float>(geo, geo->off_dxwl32);
   const double* NZL = geo_ptr<double>(geo, geo->off_nzl);
   const int dir = lane & 7;
-  const double om = tb->sv[S_OMEGA_M], dom = tb->sd[dir][S_OMEGA_M];
-  const double cf = 3.0 * (H0 * H0) * om / 2.0 / C_KMS;  // probes.py:71
-  const double dcf = cf * dom / om;
+  const double om = tb->sv[S_OMEGA_M];
+  const float cff = (float)(3.0 * (H0 * H0) * om / 2.0 / C_KMS);  // probes.py:71
+  const float dlcf = (float)(tb->sd[dir][S_OMEGA_M] / om);         // d ln(cf)
   const int n_end = min(na, n0 + GK_NODES);
   for (int n = n0 + warp; n < n_end; n += 8) {
     const int qw = QWL[n];
@@ -70,7 +83,7 @@ __global__ void __launch_bounds__(256) grad_kern32_kernel(GradBatch gb, const Co
     float dchi_wl[NDIR];
 #pragma unroll
     for (int d = 0; d < NDIR; ++d) dchi_wl[d] = craw_w > 0.f ? dchi[d][xw] + dslope[d][mw] * DXWL[n] : 0.f;
-    const double z = Z[n];
+    const float zp1 = (float)(1.0 + Z[n]);
     for (int t0 = 0; t0 < n_tr; t0 += 4) {
       int tl[4];
       int cnt = 0;
@@ -138,7 +151,7 @@ __global__ void __launch_bounds__(256) grad_kern32_kernel(GradBatch gb, const Co
       if (lane < NDIR) {
         for (int u = 0; u < cnt; ++u) {
           const int t = tl[u];
-          double kv, kd;
+          float kv, kd;
           if (geo->kind[t] == JCG_TRACER_WL) {
             float adir = 0.f, dcw = 0.f;
 #pragma unroll
@@ -147,27 +160,17 @@ __global__ void __launch_bounds__(256) grad_kern32_kernel(GradBatch gb, const Co
                 adir = ad[u][d];
                 dcw = dchi_wl[d];
               }
-            const double fac = (1.0 + z) * (1.0 + geo->mult[t]);
-            const double acc = av[u], cw = chi_wl;
-            kv = cf * fac * cw * acc;
-            kd = fac * (dcf * cw * acc + cf * (double)dcw * acc +
-                        cf * cw * ((double)adir - (double)dcw * (double)at[u]));
+            // K = cf (1 + z)(1 + m) chi acc, FP32 (the stored precision)
+            const float fac = cff * zp1 * (1.f + (float)geo->mult[t]);
+            const float acc = av[u];
+            kv = fac * chi_wl * acc;
+            kd = fac * (dlcf * chi_wl * acc + dcw * acc + chi_wl * (adir - dcw * at[u]));
           } else {
-            BgT<D1> bg;
-            bg.Om = mk1(tb->sv[S_OMEGA_M], tb->sd[dir][S_OMEGA_M]);
-            bg.Ok = mk1(tb->sv[S_OMEGA_K], tb->sd[dir][S_OMEGA_K]);
-            bg.Ode = mk1(tb->sv[S_OMEGA_DE], tb->sd[dir][S_OMEGA_DE]);
-            bg.w0 = mk1(tb->sv[S_W0], tb->sd[dir][S_W0]);
-            bg.wa = mk1(tb->sv[S_WA], tb->sd[dir][S_WA]);
-            const double awl = AWL[n];
-            const D1 H = H0 * xsqrt(esqrT(bg, awl, log(awl), (D1*)nullptr));
-            const double w = NZL[(size_t)t * na + n] * geo->bias[t];
-            kv = w * H.v;
-            kd = w * H.d[0];
+            nc_kernel_d1(tb, dir, AWL[n], NZL[(size_t)t * na + n] * geo->bias[t], &kv, &kd);
           }
           float* dst = gi.kernf + ((size_t)t * na + n) * (NDIR + 1);
-          if (dir == 0) dst[0] = (float)kv;
-          dst[1 + dir] = (float)kd;
+          if (dir == 0) dst[0] = kv;
+          dst[1 + dir] = kd;
         }
       }
     }
@@ -404,7 +407,7 @@ static size_t limber32_smem_floats(int n_cls, int n_tr, int LT, int TA) {
 //   phase M: M_p(a) = u K_i K_j and its tangents;
 //   phase A: per (a, ell) P and dP/dtheta (reverse sweep + projection);
 //   phase B: per (ell, pair group) the 9 sums over the chunk, Kahan-added.
-__global__ void __launch_bounds__(L32_THREADS)
+__global__ void __launch_bounds__(L32_THREADS, 2)
     grad_limber32_kernel(GradBatch gb, const ConstTables* __restrict__ c, int LT, int TA) {
   const int item = blockIdx.z, split = blockIdx.y;
   if (item >= gb.n_items) return;
