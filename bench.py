@@ -52,7 +52,22 @@ BOX = {
     "w0": (-1.3, -0.7),
 }
 ORDER = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
-MUFU_PER_NODE = 27  # ex2/lg2/rcp/sin per Limber node in the fp32c integrand
+MUFU_PER_NODE = 27  # ex2/lg2/rcp/sin per Limber node in the fp32c integrand (node32)
+# Per-cosmology figures of the fp32c step's kernels on this workload (na = 513
+# Limber nodes, 5 WL tracers, 100 ell), from one ncu capture at 512
+# cosmologies (profiles/: fp32c_step_kernels_b512.md), divided by 512:
+#   FP64 operations = DFMA x 2 + DADD + DMUL thread instructions;
+#   traffic = dram__bytes_read.sum + dram__bytes_write.sum.
+FP64_OPS = {"cosmo_tables": 707_012, "halofit_rows": 1_012_985}
+TRAFFIC_PER_COSMO = {"cosmo_tables": 1_627, "halofit_rows": 45_078, "limber": 122_084}
+# algorithmic bytes per cosmology: what each kernel must read and write once
+#   cosmo_tables: 8 parameters in, the CosmoTab record out (52,864 B)
+#   halofit_rows: the CosmoTab record in, FP64 + FP32 rows out (513 x (24 x 8 + 16 x 4))
+#   limber: FP32 rows (16 x 4) + u (8) + 5 radial kernels (5 x 8) per node in, 15 x 100 C_ell out
+ALG_BYTES = {"cosmo_tables": 64 + 52_864, "halofit_rows": 52_864 + 513 * (24 * 8 + 16 * 4),
+             "limber": 513 * (16 * 4 + 8) + 5 * 513 * 8 + 15 * N_ELL * 8}
+KERNEL_NAMES = {"cosmo_tables": "cosmo_tables_kernel", "halofit_rows": "halofit_rows_kernel<fp32c>",
+                "tracer_kernels": "tracer32_uniform_kernel<5>", "limber": "limber_kernel<fp32c>"}
 
 
 def draw_params(B, seed=SEED):
@@ -403,35 +418,73 @@ def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, 
     st["checked_requests"] = len(sample)
     st.update({"chains": n_chains, "think_ms_mean": think_ms, "duration_s": duration_s,
                "tracers_per_chain": [int(m.g.n_tracers) for m in models],
-               "n_ell_per_chain": [int(m.n_ell) for m in models], "dtype": "f64"})
+               "n_ell_per_chain": [int(m.n_ell) for m in models], "precision": srv.precision,
+               "dtype": "f32c+f64" if srv.precision == "fp32c" else "f64"})
     return st
 
 
-def roofline(res, B):
-    """Algorithmic bytes of the Limber launch vs measured HBM peak; SFU issue beside it."""
+def measure_peaks(device):
+    """FP64 FMA and MUFU ex2 issue peaks of this GPU (calibration kernels of libjcg)."""
+    import ctypes
+
+    import torch
+
+    from jax_cosmo_gb300 import _lib
+
+    sms = torch.cuda.get_device_properties(device).multi_processor_count
+    blocks = sms * 8
+    st = _lib.stream_of(device)
+    out64 = torch.empty(blocks * 256, dtype=torch.float64, device=device)
+    out32 = torch.empty(blocks * 256, dtype=torch.float32, device=device)
+    res = {}
+    for name, fn, buf, iters in (("fp64", "jcg_peak_fp64", out64, 200), ("mufu", "jcg_peak_mufu", out32, 4000)):
+        for _ in range(2):
+            _lib.call(fn, _lib.ptr(buf), blocks, iters, st)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        _lib.call(fn, _lib.ptr(buf), blocks, iters, st)
+        e1.record()
+        e1.synchronize()
+        ops = blocks * 256 * iters * 128
+        res[name] = ops / (e0.elapsed_time(e1) * 1e-3)
+    return {"fp64_tflops": 2.0 * res["fp64"] / 1e12, "dfma_per_s": res["fp64"], "mufu_per_s": res["mufu"],
+            "sm_count": sms, "how": "libjcg calibration kernels: 8 chains x 16 unrolled DFMA / ex2.approx per "
+                                   "iteration, SMs x 8 blocks x 256 threads, CUDA events"}
+
+
+def rooflines(res, B, live):
+    """Per-kernel rooflines of the fp32c step; the dominant kernel first."""
     peaks = {}
     try:
         peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
     except Exception:
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
-    na, n_tr, n_cls, n_ell = 513, 5, 15, N_ELL
-    # rows32 (16 f32) + R_U (f64) + radial kernels (f64) per node, C_ell out (f64)
-    bytes_launch = B * (na * (16 * 4 + 8) + n_tr * na * 8) + B * n_cls * n_ell * 8
-    t = res["ms_limber"] * 1e-3
-    ach = bytes_launch / t / 1e9
-    nodes = B * n_ell * na
-    clk = (res.get("clocks") or {}).get("sm_mhz") or peaks.get("sm_max_mhz", 2070.0)
-    sfu_peak = res["sm_count"] * 16 * clk * 1e6  # MUFU ops/s: 16 per SM per clock
-    sfu_ach = nodes * MUFU_PER_NODE / t
-    return (
-        {"bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-         "traffic": None, "kernel": "limber_kernel<fp32c>", "bytes_per_launch": bytes_launch,
-         "peak_source": "measured" if "hbm_gbs" in peaks else "fallback"},
-        {"bound": "sfu", "achieved": sfu_ach / 1e9, "peak": sfu_peak / 1e9, "unit": "GMUFU/s",
-         "frac": sfu_ach / sfu_peak, "nodes_per_launch": nodes, "mufu_per_node": MUFU_PER_NODE,
-         "clock_mhz": clk},
-    )
+    stages = res["stages_ms"]
+    out = {}
+    for k, ms in stages.items():
+        t = ms * 1e-3
+        e = {"kernel": KERNEL_NAMES.get(k, k), "ms": ms}
+        if k in ALG_BYTES:
+            e["algorithmic_bytes_per_launch"] = ALG_BYTES[k] * B
+            e["hbm_frac"] = ALG_BYTES[k] * B / t / 1e9 / hbm
+        if k in TRAFFIC_PER_COSMO:
+            e["traffic"] = TRAFFIC_PER_COSMO[k] * B
+        if k in FP64_OPS:
+            ach = FP64_OPS[k] * B / t / 1e12
+            e.update({"bound": "fp64", "achieved": ach, "peak": live["fp64_tflops"], "unit": "TFLOP/s",
+                      "frac": ach / live["fp64_tflops"], "peak_source": "measured live (calibration kernel)"})
+        elif k == "limber":
+            nodes = B * N_ELL * 513
+            ach = nodes * MUFU_PER_NODE / t
+            e.update({"bound": "sfu", "achieved": ach / 1e9, "peak": live["mufu_per_s"] / 1e9, "unit": "GMUFU/s",
+                      "frac": ach / live["mufu_per_s"], "mufu_per_node": MUFU_PER_NODE,
+                      "peak_source": "measured live (calibration kernel)"})
+        else:
+            e.update({"bound": "latency", "note": "FP32 lensing integral, lanes over cosmologies"})
+        out[k] = e
+    dom = max(stages, key=lambda k: stages[k])
+    return dom, out
 
 
 def main():
@@ -508,7 +561,9 @@ def main():
     value = res["ncl_step"] * world / (ms * 1e-3)
     fp64_value = res["ncl_step"] * world / (res["t64"] / res["n64"] * 1e-3)
     e2e = res["ncl_step"] * world / (res["t_e2e"] / K * 1e-3)
-    rl, rl_sfu = roofline(res, args.batch)
+    live = measure_peaks(device)
+    dom, rls = rooflines(res, args.batch, live)
+    rl = dict(rls[dom])
     plain = res["plain_fp64_single"]["cl_per_s"]
     jac = res["jacobian"]
     for prec in jac:
@@ -530,7 +585,7 @@ def main():
                 "d2h_bytes_per_step": res["d2h"]},
         "gpu_launches": 4 * K,
         "stage_ms": res["stages_ms"],
-        "roofline": rl, "roofline_sfu": rl_sfu,
+        "roofline": rl, "rooflines": rls, "peaks_live": live,
         "clocks": res["clocks"],
         "cpu_baseline": cb,
     }

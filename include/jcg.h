@@ -286,6 +286,14 @@ int jcg_sparse_to_dense(const double* sparse_dev, int n, int m, int ndiag, doubl
 int jcg_sparse_dot_vec(const double* sparse_dev, int n, int m, int ndiag, const double* v_dev,
                        int transpose, double* out_dev, cudaStream_t stream);
 
+/* ------------------------------------------------------- calibration ---- */
+/* Not a reference interface: the FP64 FMA and MUFU (ex2) issue peaks of this
+ * GPU, the denominators of the FP64-bound and SFU-bound rooflines the
+ * benchmark reports.  blocks x 256 threads x iters x 128 operations; out_dev
+ * holds blocks * 256 results. */
+int jcg_peak_fp64(double* out_dev, int blocks, int iters, cudaStream_t stream);
+int jcg_peak_mufu(float* out_dev, int blocks, int iters, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif
