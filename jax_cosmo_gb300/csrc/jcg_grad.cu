@@ -300,12 +300,10 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       for (int m = 0; m < NTAYLOR; ++m) carry[m] = 0.0;
       for (int base = 0; base < NKH; base += 32) {
         const int i = base + lane;
-        const double k2 = i < NKH ? c->kh[i] * c->kh[i] : 0.0;
-        double v = i < NKH ? c->simpson_kh[i] * pq[i] : 0.0;
+        const double q = i < NKH ? pq[i] : 0.0;
 #pragma unroll
         for (int m = 0; m < NTAYLOR; ++m) {
-          v *= k2;
-          double x = v;
+          double x = i < NKH ? c->kpw[m][i] * q : 0.0;
 #pragma unroll
           for (int o = 1; o < 32; o <<= 1) {
             const double u = __shfl_up_sync(0xffffffffu, x, o);
@@ -333,28 +331,29 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
   if (F32T) {
     // value FP64, tangents FP32 (pq tangents rounded once into a float copy)
     float* pqf = reinterpret_cast<float*>(fn);  // fn / fm are free here
+    double* pqs = fm;
     for (int e = t; e < NDIR * NKH; e += blockDim.x) {
       const int d = e / NKH, i = e % NKH;
-      pqf[i * NDIR + d] = (float)pq[(1 + d) * NKH + i];
+      pqf[i * NDIR + d] = (float)(c->simpson_kh[i] * pq[(1 + d) * NKH + i]);
     }
+    for (int i = t; i < NKH; i += blockDim.x) pqs[i] = pq[i] * c->simpson_kh[i];
     __syncthreads();
     for (int j = t; j < NRT; j += blockDim.x) {
       double acc = 0.0;
       float ad[NDIR];
 #pragma unroll
       for (int d = 0; d < NDIR; ++d) ad[d] = 0.f;
-      for (int m = 0; m < 128; ++m) {
-        const double e0 = c->E[(2 * m) * NRT + j], e1 = c->E[(2 * m + 1) * NRT + j],
-                     e2 = c->E[(2 * m + 2) * NRT + j];
-        acc += pq[2 * m] * e0 + 4 * (pq[2 * m + 1] * e1) + pq[2 * m + 2] * e2;
-        const float f0 = (float)e0, f1 = 4.f * (float)e1, f2 = (float)e2;
-        const float* q0 = pqf + (2 * m) * NDIR;
+      for (int i = 0; i < NKH; ++i) {
+        const double e = c->E[i * NRT + j];
+        acc = fma(pqs[i], e, acc);
+        const float f = (float)e;
+        const float* q0 = pqf + i * NDIR;
 #pragma unroll
-        for (int d = 0; d < NDIR; ++d) ad[d] += q0[d] * f0 + q0[NDIR + d] * f1 + q0[2 * NDIR + d] * f2;
+        for (int d = 0; d < NDIR; ++d) ad[d] = fmaf(q0[d], f, ad[d]);
       }
-      out->sigv[j] = dx / 3 * acc;
+      out->sigv[j] = acc;
 #pragma unroll
-      for (int d = 0; d < NDIR; ++d) out->sigd[d][j] = dx / 3 * (double)ad[d];
+      for (int d = 0; d < NDIR; ++d) out->sigd[d][j] = (double)ad[d];
     }
   }
   for (int e = F32T ? (NDIR + 1) * NRT : t; e < (NDIR + 1) * NRT; e += blockDim.x) {

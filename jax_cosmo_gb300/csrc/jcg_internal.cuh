@@ -34,6 +34,8 @@ constexpr double EULER_E = 2.718281828459045;  // np.exp(1.0)
 
 // ------------------------------------------------ cosmology-wide constants ---
 // Grids shared by every cosmology and every geometry, built once per device.
+constexpr int NTAYLOR = 20;      // Taylor terms of exp(-y^2) below y^2 = 1 (1/19! < 1e-17)
+
 struct ConstTables {
   double atab_chi[NCHI];   // logspace(-3, 0, 256)
   double lna_chi[NCHI];    // log(atab_chi): the RK4 abscissae of background.py:231
@@ -45,6 +47,7 @@ struct ConstTables {
   double simpson_kh[NKH];  // Simpson weights (1,4,2,...,4,1) * dx/3 on the ln k grid
   double romb_logk[NROMB]; // romb abscissae in evaluation order (scipy/integrate.py:129-146)
   double E[NKH * NRT];     // exp(-(k_i r_j)^2), i-major: power.py:99-109
+  double kpw[NTAYLOR][NKH];  // simpson_kh[i] * kh[i]^(2(m+1)): the Taylor prefix sums' weights
 };
 
 // ------------------------------------------------- per-cosmology tables -----
@@ -63,7 +66,6 @@ enum Scalar {
   S_NSCALAR
 };
 constexpr int NSCAL = 32;
-constexpr int NTAYLOR = 20;      // Taylor terms of exp(-y^2) below y^2 = 1 (1/19! < 1e-17)
 // ln k grid of the spectral moments: simps over [ln 1e-4, ln 1e4], 256 intervals (power.py:136)
 constexpr double LOG_KMIN = -0x1.26bb1bbb55515p+3;  // np.log(1e-4)
 constexpr double DLOGK = (0x1.26bb1bbb55516p+3 - -0x1.26bb1bbb55515p+3) / 256.0;

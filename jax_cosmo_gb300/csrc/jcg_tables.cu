@@ -36,7 +36,14 @@ __global__ void const_init_kernel(ConstTables* c) {
     c->kh[i] = k;
     c->kh3[i] = pow(k, 3.0);
     const double w = (i == 0 || i == NKH - 1) ? 1.0 : ((i & 1) ? 4.0 : 2.0);
-    c->simpson_kh[i] = dxk / 3 * w;
+    const double sw = dxk / 3 * w;
+    c->simpson_kh[i] = sw;
+    const double k2 = k * k;
+    double kp = k2;
+    for (int m = 0; m < NTAYLOR; ++m) {
+      c->kpw[m][i] = sw * kp;
+      kp *= k2;
+    }
   }
   for (int j = tid; j < NRT; j += nth) {
     c->logr[j] = np_linspace(kLogKMin, kLogRMax, NRT - 1, j);
@@ -384,21 +391,16 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
     pk3[i] = pk_linear(s, c->kh[i], s[S_G1]) * c->kh3[i];
   }
   __syncthreads();
-  // sigma^2(R_j) without g^2: simps over ln k of pk k^3 exp(-(k R)^2) / (2 pi^2)
-  // (the division by 2 pi^2 is taken once per k node, not per (k, R) term)
-  for (int i = t; i < NKH; i += blockDim.x) pq[i] = pk3[i] / (2.0 * (PI * PI));
+  // sigma^2(R_j) without g^2: simps over ln k of pk k^3 exp(-(k R)^2) / (2 pi^2),
+  // with the Simpson weights and 1 / (2 pi^2) folded into the k-node factor:
+  // one FMA per (k, R) term
+  for (int i = t; i < NKH; i += blockDim.x) pq[i] = c->simpson_kh[i] * (pk3[i] / (2.0 * (PI * PI)));
   __syncthreads();
   CosmoTab* out = it.ctab;
   for (int j = t; j < NRT; j += blockDim.x) {
     double acc = 0.0;
-    for (int m = 0; m < 128; ++m) {
-      const double y0 = pq[2 * m] * c->E[(2 * m) * NRT + j];
-      const double y1 = pq[2 * m + 1] * c->E[(2 * m + 1) * NRT + j];
-      const double y2 = pq[2 * m + 2] * c->E[(2 * m + 2) * NRT + j];
-      acc += y0 + 4 * y1 + y2;
-    }
-    const double dx = (kLogKMax - kLogKMin) / 256;
-    out->sig[j] = dx / 3 * acc;
+    for (int i = 0; i < NKH; ++i) acc = fma(pq[i], c->E[i * NRT + j], acc);
+    out->sig[j] = acc;
   }
   for (int i = t; i < NSCAL; i += blockDim.x) out->s[i] = s[i];
   for (int i = t; i < NCHI; i += blockDim.x) {
@@ -410,9 +412,10 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
     out->chi32[i] = (float)chis[i];
     out->slope32[i] = (float)sl;
   }
-  // Taylor prefix sums of the halofit moments: P_m[i] = sum_{i' < i} w pk3 k^(2m+2),
-  // one warp per m with a warp-wide inclusive scan over chunks of 32 nodes.
-  for (int m = t >> 5; m < NTAYLOR; m += (int)(blockDim.x >> 5)) {
+  // Taylor prefix sums of the halofit moments (fp32c rows only):
+  // P_m[i] = sum_{i' < i} w pk3 k^(2m+2), one warp per m with a warp-wide
+  // inclusive scan over chunks of 32 nodes.
+  for (int m = t >> 5; it.precision == JCG_FP32C && m < NTAYLOR; m += (int)(blockDim.x >> 5)) {
     const int lane = t & 31;
     {
       if (lane == 0) out->ptay[m][0] = 0.0;
@@ -420,12 +423,7 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
       for (int base = 0; base < NKH; base += 32) {
         const int i = base + lane;
         double v = 0.0;
-        if (i < NKH) {
-          const double k2 = c->kh[i] * c->kh[i];
-          double kp = k2;
-          for (int q = 0; q < m; ++q) kp *= k2;
-          v = c->simpson_kh[i] * pk3[i] * kp;
-        }
+        if (i < NKH) v = c->kpw[m][i] * pk3[i];
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
           const double u = __shfl_up_sync(0xffffffffu, v, o);
