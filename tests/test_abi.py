@@ -91,3 +91,63 @@ def test_error_mapping():
         _lib.check(_lib.ERR_UNSUPPORTED)
     with pytest.raises(_lib.JcgError):
         _lib.check(_lib.ERR_CUDA)
+
+
+def test_jacobian_and_request_validation_on_the_host():
+    """Argument checks of the Jacobian and ragged-request entry points return
+    error codes before any device work."""
+    import numpy as np
+
+    lib = _lib.load()
+    g = _geom()
+    sz = ctypes.c_size_t()
+    assert lib.jcg_jacobian_workspace_size(ctypes.byref(g), 0, _lib.FP64, ctypes.byref(sz)) == _lib.ERR_SHAPE
+    assert lib.jcg_jacobian_workspace_size(ctypes.byref(g), 2, 7, ctypes.byref(sz)) == _lib.ERR_ARG
+    assert lib.jcg_jacobian_workspace_size(ctypes.byref(g), 2, _lib.FP32C, ctypes.byref(sz)) == 0
+    s64, s32 = ctypes.c_size_t(), ctypes.c_size_t()
+    lib.jcg_jacobian_workspace_size(ctypes.byref(g), 64, _lib.FP64, ctypes.byref(s64))
+    lib.jcg_jacobian_workspace_size(ctypes.byref(g), 64, _lib.FP32C, ctypes.byref(s32))
+    assert s64.value > 0 and s32.value > 0
+    assert lib.jcg_angular_cl_jacobian(ctypes.byref(g), None, None, 1, _lib.FP64, None, None, None, 0,
+                                       None) == _lib.ERR_ARG
+    lo, hi = ctypes.c_size_t(), ctypes.c_size_t()
+    table = np.zeros(2, _lib.REQUEST_DTYPE)
+    tp = ctypes.c_void_p(table.ctypes.data)
+    # no requests, too many, unknown mode or precision
+    assert lib.jcg_requests_workspace_size(tp, 0, _lib.REQ_CL, _lib.FP64, ctypes.byref(lo),
+                                           ctypes.byref(hi)) == _lib.ERR_SHAPE
+    assert lib.jcg_requests_workspace_size(tp, _lib.MAX_REQUESTS + 1, _lib.REQ_CL, _lib.FP64, ctypes.byref(lo),
+                                           ctypes.byref(hi)) == _lib.ERR_SHAPE
+    assert lib.jcg_requests_workspace_size(tp, 2, 9, _lib.FP64, ctypes.byref(lo), ctypes.byref(hi)) == _lib.ERR_ARG
+    assert lib.jcg_requests_workspace_size(tp, 2, _lib.REQ_CL, 5, ctypes.byref(lo), ctypes.byref(hi)) == _lib.ERR_ARG
+    # a request without a geometry, then one whose pointers are missing
+    assert lib.jcg_requests_workspace_size(tp, 2, _lib.REQ_CL, _lib.FP64, ctypes.byref(lo),
+                                           ctypes.byref(hi)) == _lib.ERR_ARG
+    g2 = _geom(n_tr=3, n_ell=7)
+    fake = 4096  # host-side checks only look at NULL-ness; nothing is dereferenced
+    for i, gg in enumerate((g, g2)):
+        table[i] = (ctypes.addressof(gg), fake, fake, fake, 0, 0, 0, 0)
+    assert lib.jcg_requests_workspace_size(tp, 2, _lib.REQ_CL, _lib.FP64, ctypes.byref(lo), ctypes.byref(hi)) == 0
+    assert lo.value == hi.value > 0
+    assert lib.jcg_requests_workspace_size(tp, 2, _lib.REQ_JACOBIAN, _lib.FP32C, ctypes.byref(lo),
+                                           ctypes.byref(hi)) == _lib.ERR_ARG  # jac NULL
+    assert lib.jcg_requests_workspace_size(tp, 2, _lib.REQ_LOGLIKE_GRAD, _lib.FP32C, ctypes.byref(lo),
+                                           ctypes.byref(hi)) == _lib.ERR_ARG  # data / prec / out NULL
+    for i, gg in enumerate((g, g2)):
+        table[i] = (ctypes.addressof(gg), fake, fake, 0, 0, fake, fake, fake)
+    assert lib.jcg_requests_workspace_size(tp, 2, _lib.REQ_LOGLIKE_GRAD, _lib.FP32C, ctypes.byref(lo),
+                                           ctypes.byref(hi)) == 0
+    assert hi.value >= lo.value > 0
+    # the workspace is additive in the requests: two requests need more than one
+    one_lo = ctypes.c_size_t()
+    lib.jcg_requests_workspace_size(tp, 1, _lib.REQ_LOGLIKE_GRAD, _lib.FP32C, ctypes.byref(one_lo),
+                                    ctypes.byref(hi))
+    assert lo.value > one_lo.value
+    # run refuses a NULL or misaligned workspace before any launch
+    assert lib.jcg_requests_run(tp, 2, _lib.REQ_LOGLIKE_GRAD, _lib.FP32C, None, 0, None) == _lib.ERR_ARG
+    # a geometry with an odd Limber N inside a request is reported with its index
+    g2.n_limber = 511
+    rc = lib.jcg_requests_workspace_size(tp, 2, _lib.REQ_LOGLIKE_GRAD, _lib.FP32C, ctypes.byref(lo),
+                                         ctypes.byref(hi))
+    assert rc == _lib.ERR_ODD_N
+    assert b"request 1" in lib.jcg_last_error_string()
