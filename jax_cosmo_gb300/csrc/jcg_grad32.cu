@@ -38,6 +38,7 @@ __device__ __noinline__ void nc_kernel_d1(const TabD* tb, int dir, double awl, d
   *kd = (float)(w * H.d[0]);
 }
 
+template <int TP>
 __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
@@ -46,6 +47,27 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
   const int na = geo->na, n_tr = geo->n_tr;
   const int n0 = blockIdx.x * GK_NODES;
   if (n0 >= na) return;
+  // passes: WeakLensing tracers of one lensing group, up to TP per pass
+  __shared__ int ptr_t[JCG_MAX_TRACERS * TP];
+  __shared__ int pgroup[JCG_MAX_TRACERS];
+  __shared__ int npass_s;
+  if (threadIdx.x == 0) {
+    int np = 0;
+    for (int g = 0; g < geo->n_groups; ++g) {
+      int u = TP;
+      for (int t = 0; t < n_tr; ++t) {
+        if (geo->kind[t] != JCG_TRACER_WL || geo->group[t] != g) continue;
+        if (u == TP) {
+          pgroup[np] = g;
+          for (int v = 0; v < TP; ++v) ptr_t[np * TP + v] = -1;
+          ++np;
+          u = 0;
+        }
+        ptr_t[(np - 1) * TP + u++] = t;
+      }
+    }
+    npass_s = np;
+  }
   __shared__ __align__(16) float ctab[NDIR + 1][NCHI];  // chi, then its tangents
   __shared__ __align__(16) float stab[NDIR + 1][NCHI];  // segment slopes, then tangents
   const TabD* tb = gi.tab;
@@ -60,6 +82,7 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
     }
   }
   __syncthreads();
+  const int npass = npass_s;
   const float* chi = ctab[0];
   const float* slope = stab[0];
   const float(*dchi)[NCHI] = ctab + 1;
@@ -84,94 +107,93 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
 #pragma unroll
     for (int d = 0; d < NDIR; ++d) dchi_wl[d] = craw_w > 0.f ? dchi[d][xw] + dslope[d][mw] * DXWL[n] : 0.f;
     const float zp1 = (float)(1.0 + Z[n]);
-    for (int t0 = 0; t0 < n_tr; t0 += 4) {
-      int tl[4];
-      int cnt = 0;
-      for (int t = t0; t < min(t0 + 4, n_tr); ++t) tl[cnt++] = t;
-      float av[4], at[4], ad[4][NDIR];
+    const size_t row = (size_t)n * NZP;
+    // WeakLensing tracers: passes of up to TP tracers of one lensing group
+    for (int pass = 0; pass < npass; ++pass) {
+      const int g = pgroup[pass];
+      int tl[TP];
+      const float* W[TP];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < TP; ++u) {
+        tl[u] = ptr_t[pass * TP + u];
+        W[u] = tl[u] >= 0 ? geo_ptr<float>(geo, geo->off_W32[tl[u]]) + row : nullptr;
+      }
+      float av[TP], at[TP], ad[TP][NDIR];
+#pragma unroll
+      for (int u = 0; u < TP; ++u) {
         av[u] = 0.f;
         at[u] = 0.f;
 #pragma unroll
         for (int d = 0; d < NDIR; ++d) ad[u][d] = 0.f;
       }
-      bool any_wl = false;
-      for (int u = 0; u < cnt; ++u) any_wl |= geo->kind[tl[u]] == JCG_TRACER_WL;
-      if (any_wl) {
-        for (int g = 0; g < geo->n_groups; ++g) {
-          const size_t row = (size_t)n * NZP;
-          const int32_t* Q32 = geo_ptr<int32_t>(geo, geo->off_q32[g]) + row;
-          const float* DX32 = geo_ptr<float>(geo, geo->off_dx32[g]) + row;
-          const float* W[4];
-          bool on[4];
+      const int32_t* Q32 = geo_ptr<int32_t>(geo, geo->off_q32[g]) + row;
+      const float* DX32 = geo_ptr<float>(geo, geo->off_dx32[g]) + row;
+      for (int j = lane; j < NZP; j += 32) {
+        const int q = Q32[j];
+        const int x = q & 0xffff, m = q >> 16;
+        const float dx = DX32[j];
+        const float craw = chi[x] + slope[m] * dx;
+        const float chip = fmaxf(craw, 0.f);
+        const float diff = chip - chi_wl;
+        if (!(diff > 0.f)) continue;  // then craw > 0 too
+        const float ic = rcpf(fmaxf(chip, 1.f));
+        const float r = diff * ic;
+        const float h = chip > 1.f ? ic * (1.f - r) : ic;
+        float dcp[NDIR];
 #pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            on[u] = u < cnt && geo->kind[tl[u]] == JCG_TRACER_WL && geo->group[tl[u]] == g;
-            W[u] = on[u] ? geo_ptr<float>(geo, geo->off_W32[tl[u]]) + row : nullptr;
-          }
-          if (!(on[0] || on[1] || on[2] || on[3])) continue;
-          for (int j = lane; j < NZP; j += 32) {
-            const int q = Q32[j];
-            const int x = q & 0xffff, m = q >> 16;
-            const float dx = DX32[j];
-            const float craw = chi[x] + slope[m] * dx;
-            const float chip = fmaxf(craw, 0.f);
-            const float diff = chip - chi_wl;
-            if (!(diff > 0.f)) continue;
-            const float ic = rcpf(fmaxf(chip, 1.f));
-            const float r = diff * ic;
-            const float h = chip > 1.f ? ic * (1.f - r) : ic;
-            float dcp[NDIR];
+        for (int d = 0; d < NDIR; ++d) dcp[d] = fmaf(dslope[d][m], dx, dchi[d][x]) * h;
 #pragma unroll
-            for (int d = 0; d < NDIR; ++d) dcp[d] = craw > 0.f ? (dchi[d][x] + dslope[d][m] * dx) * h : 0.f;
+        for (int u = 0; u < TP; ++u) {
+          if (tl[u] >= 0) {
+            const float w = W[u][j];
+            av[u] = fmaf(w, r, av[u]);
+            at[u] = fmaf(w, ic, at[u]);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
-              if (on[u]) {
-                const float w = W[u][j];
-                av[u] = fmaf(w, r, av[u]);
-                at[u] = fmaf(w, ic, at[u]);
-#pragma unroll
-                for (int d = 0; d < NDIR; ++d) ad[u][d] = fmaf(w, dcp[d], ad[u][d]);
-              }
-            }
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            av[u] += __shfl_xor_sync(0xffffffffu, av[u], o);
-            at[u] += __shfl_xor_sync(0xffffffffu, at[u], o);
-#pragma unroll
-            for (int d = 0; d < NDIR; ++d) ad[u][d] += __shfl_xor_sync(0xffffffffu, ad[u][d], o);
+            for (int d = 0; d < NDIR; ++d) ad[u][d] = fmaf(w, dcp[d], ad[u][d]);
           }
         }
       }
-      if (lane < NDIR) {
-        for (int u = 0; u < cnt; ++u) {
-          const int t = tl[u];
-          float kv, kd;
-          if (geo->kind[t] == JCG_TRACER_WL) {
-            float adir = 0.f, dcw = 0.f;
 #pragma unroll
-            for (int d = 0; d < NDIR; ++d)
-              if (d == dir) {
-                adir = ad[u][d];
-                dcw = dchi_wl[d];
-              }
-            // K = cf (1 + z)(1 + m) chi acc, FP32 (the stored precision)
-            const float fac = cff * zp1 * (1.f + (float)geo->mult[t]);
-            const float acc = av[u];
-            kv = fac * chi_wl * acc;
-            kd = fac * (dlcf * chi_wl * acc + dcw * acc + chi_wl * (adir - dcw * at[u]));
-          } else {
-            nc_kernel_d1(tb, dir, AWL[n], NZL[(size_t)t * na + n] * geo->bias[t], &kv, &kd);
-          }
-          float* dst = gi.kernf + ((size_t)t * na + n) * (NDIR + 1);
-          if (dir == 0) dst[0] = kv;
-          dst[1 + dir] = kd;
+      for (int u = 0; u < TP; ++u) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          av[u] += __shfl_xor_sync(0xffffffffu, av[u], o);
+          at[u] += __shfl_xor_sync(0xffffffffu, at[u], o);
+#pragma unroll
+          for (int d = 0; d < NDIR; ++d) ad[u][d] += __shfl_xor_sync(0xffffffffu, ad[u][d], o);
         }
+      }
+      if (lane < NDIR) {
+        float dcw = 0.f;
+#pragma unroll
+        for (int d = 0; d < NDIR; ++d)
+          if (d == dir) dcw = dchi_wl[d];
+#pragma unroll
+        for (int u = 0; u < TP; ++u) {
+          const int t = tl[u];
+          if (t < 0) continue;
+          float adir = 0.f;
+#pragma unroll
+          for (int d = 0; d < NDIR; ++d)
+            if (d == dir) adir = ad[u][d];
+          // K = cf (1 + z)(1 + m) chi acc, FP32 (the stored precision)
+          const float fac = cff * zp1 * (1.f + (float)geo->mult[t]);
+          const float acc = av[u];
+          float* dst = gi.kernf + ((size_t)t * na + n) * (NDIR + 1);
+          if (dir == 0) dst[0] = fac * chi_wl * acc;
+          dst[1 + dir] = fac * (dlcf * chi_wl * acc + dcw * acc + chi_wl * (adir - dcw * at[u]));
+        }
+      }
+    }
+    // NumberCounts tracers
+    if (lane < NDIR) {
+      for (int t = 0; t < n_tr; ++t) {
+        if (geo->kind[t] == JCG_TRACER_WL) continue;
+        float kv, kd;
+        nc_kernel_d1(tb, dir, AWL[n], NZL[(size_t)t * na + n] * geo->bias[t], &kv, &kd);
+        float* dst = gi.kernf + ((size_t)t * na + n) * (NDIR + 1);
+        if (dir == 0) dst[0] = kv;
+        dst[1 + dir] = kd;
       }
     }
   }
@@ -179,7 +201,9 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
 
 void launch_grad_kern32(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
   dim3 grid((gb.na + GK_NODES - 1) / GK_NODES, gb.n_items);
-  grad_kern32_kernel<<<grid, 256, 0, st>>>(gb, c);
+  if (gb.n_tr <= 3) grad_kern32_kernel<3><<<grid, 256, 0, st>>>(gb, c);
+  else if (gb.n_tr <= 5) grad_kern32_kernel<5><<<grid, 256, 0, st>>>(gb, c);
+  else grad_kern32_kernel<8><<<grid, 256, 0, st>>>(gb, c);
 }
 
 // ---------------------------------------------------------- Limber adjoint --
