@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define JCG_ABI_VERSION 1
+#define JCG_ABI_VERSION 2
 #define JCG_MAX_TRACERS 16
 #define JCG_MAX_PAIRS (JCG_MAX_TRACERS * (JCG_MAX_TRACERS + 1) / 2)
 #define JCG_MAX_ELL 4096
@@ -54,6 +54,19 @@ extern "C" {
 /* tracer kinds: probes.WeakLensing (probes.py:132) / probes.NumberCounts (probes.py:226) */
 #define JCG_TRACER_WL 0
 #define JCG_TRACER_NC 1
+
+/* Bias models (bias.py:10-57): the NumberCounts galaxy bias, or the
+ * WeakLensing intrinsic-alignment amplitude of the NLA model (probes.py:102-129;
+ * JCG_BIAS_NONE on a WeakLensing tracer: no intrinsic alignment).
+ *   CONSTANT    b                                 constant_linear_bias
+ *   INV_GROWTH  b / D(a)                          inverse_growth_linear_bias
+ *   DES_Y1      A ((1 + z) / (1 + z0))^eta        des_y1_ia_bias
+ * with b or A in `bias`, eta and z0 in `bias_eta`, `bias_z0`.  On a
+ * NumberCounts tracer JCG_BIAS_NONE means CONSTANT. */
+#define JCG_BIAS_NONE 0
+#define JCG_BIAS_CONSTANT 1
+#define JCG_BIAS_INV_GROWTH 2
+#define JCG_BIAS_DES_Y1 3
 
 /* arithmetic of the Limber stage */
 #define JCG_FP64 0  /* plain: float64 everywhere */
@@ -76,9 +89,12 @@ typedef struct jcg_geometry {
   double nz_z0[JCG_MAX_TRACERS];
   double nz_zmax[JCG_MAX_TRACERS];    /* n(z) normalisation range (redshift.py:30) */
   double probe_zmax[JCG_MAX_TRACERS]; /* lensing integral upper limit (probes.py:25) */
-  double bias[JCG_MAX_TRACERS];       /* NumberCounts constant_linear_bias b (bias.py:21) */
+  double bias[JCG_MAX_TRACERS];       /* bias amplitude b or A (bias.py:21, 38, 56) */
   double mult[JCG_MAX_TRACERS];       /* WeakLensing multiplicative bias m (probes.py:207) */
   double noise[JCG_MAX_TRACERS];      /* per-bin noise power (probes.py:210-223, 274-281) */
+  int bias_kind[JCG_MAX_TRACERS];     /* JCG_BIAS_*: galaxy bias (NC) or NLA bias (WL) */
+  double bias_eta[JCG_MAX_TRACERS];   /* des_y1_ia_bias eta, z0 (bias.py:55-57) */
+  double bias_z0[JCG_MAX_TRACERS];
 } jcg_geometry;
 
 /* ------------------------------------------------------------- misc ---- */

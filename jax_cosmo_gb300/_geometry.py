@@ -30,19 +30,15 @@ def describe(probes, n_ell, n_limber=512, n_nodes=0, zmax=None):
     n = 0
     for p in probes:
         if isinstance(p, WeakLensing):
-            if p.config.get("ia_enabled", False):
-                raise NotImplementedError(
-                    "intrinsic alignment (probes.py:102-129) is not on the accelerated path"
-                )
             ms = p.multiplicative_biases()
             noise = p.noise().numpy()
             kind = _lib.TRACER_WL
-            biases = [0.0] * p.n_tracers
+            biases = p.ia_specs()
         elif isinstance(p, NumberCounts):
             ms = [0.0] * p.n_tracers
             noise = p.noise().numpy()
             kind = _lib.TRACER_NC
-            biases = p.bias_values()
+            biases = p.bias_specs()
         else:
             raise NotImplementedError(f"probe type {type(p).__name__} is not supported")
         pzmax = p.zmax
@@ -57,7 +53,11 @@ def describe(probes, n_ell, n_limber=512, n_nodes=0, zmax=None):
             g.kind[n] = kind
             g.nz_a[n], g.nz_b[n], g.nz_z0[n], g.nz_zmax[n] = a, bb, z0, zm
             g.probe_zmax[n] = float(pzmax)
-            g.bias[n] = float(biases[b])
+            bk, bamp, beta, bz0 = biases[b]
+            g.bias_kind[n] = int(bk)
+            g.bias[n] = bamp
+            g.bias_eta[n] = beta
+            g.bias_z0[n] = bz0
             g.mult[n] = float(ms[b])
             g.noise[n] = float(noise[b])
             n += 1

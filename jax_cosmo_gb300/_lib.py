@@ -18,7 +18,7 @@ import torch
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libjcg.so")
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 MAX_TRACERS = 16
 MAX_PAIRS = MAX_TRACERS * (MAX_TRACERS + 1) // 2
 MAX_ELL = 4096
@@ -38,6 +38,7 @@ ERR_ABI = -9
 
 TRACER_WL = 0
 TRACER_NC = 1
+BIAS_NONE, BIAS_CONSTANT, BIAS_INV_GROWTH, BIAS_DES_Y1 = 0, 1, 2, 3
 FP64 = 0
 FP32C = 1
 
@@ -75,6 +76,9 @@ class Geometry(ctypes.Structure):
         ("bias", ctypes.c_double * MAX_TRACERS),
         ("mult", ctypes.c_double * MAX_TRACERS),
         ("noise", ctypes.c_double * MAX_TRACERS),
+        ("bias_kind", ctypes.c_int * MAX_TRACERS),
+        ("bias_eta", ctypes.c_double * MAX_TRACERS),
+        ("bias_z0", ctypes.c_double * MAX_TRACERS),
     ]
 
 

@@ -123,6 +123,17 @@ static int make_header(const jcg_geometry* g, GeoHeader* h) {
     h->nz_z0[t] = g->nz_z0[t];
     h->nz_zmax[t] = g->nz_zmax[t];
     h->bias[t] = g->bias[t];
+    int bk = g->bias_kind[t];
+    if (bk < JCG_BIAS_NONE || bk > JCG_BIAS_DES_Y1) return fail(JCG_ERR_ARG, "tracer %d: bias_kind %d", t, bk);
+    if (k == JCG_TRACER_NC && bk == JCG_BIAS_NONE) bk = JCG_BIAS_CONSTANT;
+    if (bk == JCG_BIAS_DES_Y1) {
+      if (!isfinite(g->bias_eta[t]) || !isfinite(g->bias_z0[t]) || !(1.0 + g->bias_z0[t] > 0.0))
+        return fail(JCG_ERR_VALUE, "tracer %d: des_y1_ia_bias eta = %g, z0 = %g", t, g->bias_eta[t], g->bias_z0[t]);
+    }
+    h->bias_kind[t] = bk;
+    h->bias_eta[t] = bk == JCG_BIAS_DES_Y1 ? g->bias_eta[t] : 0.0;
+    h->bias_z0[t] = bk == JCG_BIAS_DES_Y1 ? g->bias_z0[t] : 0.0;
+    if ((k == JCG_TRACER_WL && bk != JCG_BIAS_NONE) || bk >= JCG_BIAS_INV_GROWTH) h->special_bias = 1;
     h->mult[t] = g->mult[t];
     h->noise[t] = g->noise[t];
     h->probe_zmax[t] = g->probe_zmax[t];
@@ -248,6 +259,7 @@ static Batch make_batch(const GeoHeader* h, const void* geo, const double* param
   b.max_tr = h ? h->n_tr : 0;
   b.n_wl = h ? h->n_wl : 0;
   b.n_wl_groups = h ? h->n_groups : 0;
+  b.special_bias = h ? h->special_bias : 0;
   return b;
 }
 

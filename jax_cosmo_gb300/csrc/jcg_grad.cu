@@ -917,11 +917,17 @@ __global__ void __launch_bounds__(256) grad_kern_kernel(GradBatch gb, const Cons
           for (int d = 0; d < NDIR; ++d)
             if (d == dir) ad = acc[u].d[d];
           const D1 rk = mk1(acc[u].v, ad) * (1.0 + z) * chi_wl;
-          kv = cf * rk * (1.0 + geo->mult[t]);
+          kv = cf * rk;
+          if (geo->bias_kind[t] != JCG_BIAS_NONE) {
+            double iv, id;
+            bias_term_d1(tb, c, geo, t, dir, awl, z, NZL[(size_t)t * na + n], true, &iv, &id);
+            kv = kv + mk1(iv, id);
+          }
+          kv = kv * (1.0 + geo->mult[t]);
         } else {
-          const BgT<D1> bg = make_bgT(sD);
-          const D1 H = H0 * xsqrt(esqrT(bg, awl, log(awl), (D1*)nullptr));
-          kv = NZL[(size_t)t * na + n] * geo->bias[t] * H;
+          double iv, id;
+          bias_term_d1(tb, c, geo, t, dir, awl, z, NZL[(size_t)t * na + n], false, &iv, &id);
+          kv = mk1(iv, id);
         }
         double* dst = kd + ((size_t)t * na + n) * (NDIR + 1);
         if (dir == 0) dst[0] = kv.v;

@@ -137,6 +137,37 @@ __device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
   return r;
 }
 
+// n(z) b(z) H(a) of a NumberCounts tracer (probes.py:94), or the NLA
+// intrinsic-alignment term n(z) b(z) H(a) (-C_1 rho_crit Omega_m / D(a)) of a
+// WeakLensing tracer (probes.py:102-129), with its tangent in direction dir;
+// a = z2a(z), D = growth_factor(a) from the tangent tables.
+static __device__ __noinline__ void bias_term_d1(const TabD* tb, const ConstTables* c, const GeoHeader* geo, int t,
+                                          int dir, double awl, double z, double nzl, bool nla, double* kv,
+                                          double* kd) {
+  BgT<D1> bg;
+  bg.Om = mk1(tb->sv[S_OMEGA_M], tb->sd[dir][S_OMEGA_M]);
+  bg.Ok = mk1(tb->sv[S_OMEGA_K], tb->sd[dir][S_OMEGA_K]);
+  bg.Ode = mk1(tb->sv[S_OMEGA_DE], tb->sd[dir][S_OMEGA_DE]);
+  bg.w0 = mk1(tb->sv[S_W0], tb->sd[dir][S_W0]);
+  bg.wa = mk1(tb->sv[S_WA], tb->sd[dir][S_WA]);
+  const D1 H = H0 * xsqrt(esqrT(bg, awl, log(awl), (D1*)nullptr));
+  D1 D = mk1(1.0, 0.0);
+  const int kind = geo->bias_kind[t];
+  if (nla || kind == JCG_BIAS_INV_GROWTH) {
+    const int2 sg = interp_segment_inc(awl, c->atab_grow, NGROW, logspace_guess(awl, NGROW));
+    const D1 f0 = mk1(tb->gv[sg.x], tb->gd[dir][sg.x]), f1 = mk1(tb->gv[sg.y], tb->gd[dir][sg.y]);
+    const D1 sl = (f1 - f0) / (c->atab_grow[sg.y] - c->atab_grow[sg.x]);
+    D = xfmin(xfmax(sl * awl + (f0 - sl * c->atab_grow[sg.x]), 0.0), 1.0);
+  }
+  D1 b;
+  if (kind == JCG_BIAS_INV_GROWTH) b = geo->bias[t] / D;
+  else b = mk1(bias_at(geo, t, z, 1.0), 0.0);
+  D1 k = nzl * b * H;
+  if (nla) k = k * (-IA_C1_RHOCRIT * bg.Om / D);
+  *kv = k.v;
+  *kd = k.d[0];
+}
+
 // FP32 compensated stages (jcg_grad32.cu)
 void launch_grad_kern32(const GradBatch& gb, const ConstTables* c, cudaStream_t st);
 void launch_grad_limber32(const GradBatch& gb, const ConstTables* c, cudaStream_t st);

@@ -25,19 +25,6 @@ namespace jcg {
 // accumulated as sum W r, sum W ic, sum W ic (1 - r) dchi'.
 constexpr int GK_NODES = 128;  // nodes per CTA (8 warps x 16)
 
-// NumberCounts kernel n(z) b H(a) (probes.py:94) and its tangent in direction dir
-__device__ __noinline__ void nc_kernel_d1(const TabD* tb, int dir, double awl, double w, float* kv, float* kd) {
-  BgT<D1> bg;
-  bg.Om = mk1(tb->sv[S_OMEGA_M], tb->sd[dir][S_OMEGA_M]);
-  bg.Ok = mk1(tb->sv[S_OMEGA_K], tb->sd[dir][S_OMEGA_K]);
-  bg.Ode = mk1(tb->sv[S_OMEGA_DE], tb->sd[dir][S_OMEGA_DE]);
-  bg.w0 = mk1(tb->sv[S_W0], tb->sd[dir][S_W0]);
-  bg.wa = mk1(tb->sv[S_WA], tb->sd[dir][S_WA]);
-  const D1 H = H0 * xsqrt(esqrT(bg, awl, log(awl), (D1*)nullptr));
-  *kv = (float)(w * H.v);
-  *kd = (float)(w * H.d[0]);
-}
-
 template <int TP>
 __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
@@ -176,24 +163,35 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
 #pragma unroll
           for (int d = 0; d < NDIR; ++d)
             if (d == dir) adir = ad[u][d];
-          // K = cf (1 + z)(1 + m) chi acc, FP32 (the stored precision)
-          const float fac = cff * zp1 * (1.f + (float)geo->mult[t]);
+          // K = (cf (1 + z) chi acc + NLA) (1 + m), FP32 (the stored precision)
+          const float m1 = 1.f + (float)geo->mult[t];
+          const float fac = cff * zp1;
           const float acc = av[u];
+          const float kv = fac * chi_wl * acc;
+          const float kd = fac * (dlcf * chi_wl * acc + dcw * acc + chi_wl * (adir - dcw * at[u]));
           float* dst = gi.kernf + ((size_t)t * na + n) * (NDIR + 1);
-          if (dir == 0) dst[0] = fac * chi_wl * acc;
-          dst[1 + dir] = fac * (dlcf * chi_wl * acc + dcw * acc + chi_wl * (adir - dcw * at[u]));
+          if (dir == 0) dst[0] = kv * m1;
+          dst[1 + dir] = kd * m1;
         }
       }
     }
-    // NumberCounts tracers
+    // NumberCounts tracers, and the NLA term of WeakLensing tracers with IA
+    // (added to the shear part this lane wrote above, times 1 + m)
     if (lane < NDIR) {
       for (int t = 0; t < n_tr; ++t) {
-        if (geo->kind[t] == JCG_TRACER_WL) continue;
-        float kv, kd;
-        nc_kernel_d1(tb, dir, AWL[n], NZL[(size_t)t * na + n] * geo->bias[t], &kv, &kd);
+        const bool wl = geo->kind[t] == JCG_TRACER_WL;
+        if (wl && geo->bias_kind[t] == JCG_BIAS_NONE) continue;
+        double kv, kd;
+        bias_term_d1(tb, c, geo, t, dir, AWL[n], Z[n], NZL[(size_t)t * na + n], wl, &kv, &kd);
         float* dst = gi.kernf + ((size_t)t * na + n) * (NDIR + 1);
-        if (dir == 0) dst[0] = kv;
-        dst[1 + dir] = kd;
+        if (wl) {
+          const float m1 = 1.f + (float)geo->mult[t];
+          if (dir == 0) dst[0] += (float)kv * m1;
+          dst[1 + dir] += (float)kd * m1;
+        } else {
+          if (dir == 0) dst[0] = (float)kv;
+          dst[1 + dir] = (float)kd;
+        }
       }
     }
   }

@@ -142,6 +142,9 @@ struct GeoHeader {
   double dx_limber;        // (1 - z2a(zmax)) / N
   double nz_a[MAXTR], nz_b[MAXTR], nz_z0[MAXTR], nz_zmax[MAXTR];
   double bias[MAXTR], mult[MAXTR], noise[MAXTR], probe_zmax[MAXTR];
+  int bias_kind[MAXTR];    // JCG_BIAS_*: NC galaxy bias, WL NLA bias (NONE: no IA)
+  double bias_eta[MAXTR], bias_z0[MAXTR];
+  int special_bias;        // 1: some tracer has IA or a redshift-dependent bias
   double group_zmax[MAXTR];
   double nz_norm[MAXTR];   // redshift.py:30
   // offsets (8-byte units)
@@ -193,6 +196,7 @@ struct Batch {
   int precision;
   int max_na, max_ell, max_cls, max_tr;
   int n_wl, n_wl_groups;  // uniform form: WeakLensing tracers and lensing groups
+  int special_bias;       // uniform form: IA or a redshift-dependent bias present
 };
 
 __device__ __forceinline__ Item batch_item(const Batch& b, int i) {
@@ -365,6 +369,24 @@ __device__ __forceinline__ double bg_esqr_l(const Bg& c, double a, double lna, d
 }
 __device__ __forceinline__ double bg_esqr(const Bg& c, double a) { return bg_esqr_l(c, a, log(a), nullptr); }
 __device__ __forceinline__ double bg_H(const Bg& c, double a) { return H0 * sqrt(bg_esqr(c, a)); }
+
+// ------------------------------------------------------ bias models -------
+constexpr double IA_C1_RHOCRIT = 5e-14 * 2.7750e11;  // C_1 rho_crit (constants.py), NLA normalisation
+
+// growth_factor(cosmo, a) (background.py:371-398): clip(interp(a), 0, 1)
+__device__ __forceinline__ double growth_at(const double* gtab, const ConstTables* c, double a) {
+  const int2 sg = interp_segment_inc(a, c->atab_grow, NGROW, logspace_guess(a, NGROW));
+  return clip_lohi(interp_eval(a, c->atab_grow, gtab, sg), 0.0, 1.0);
+}
+
+// b(cosmo, z) of tracer t's bias model (bias.py:10-57), D = growth_factor(z2a(z))
+__device__ __forceinline__ double bias_at(const GeoHeader* g, int t, double z, double D) {
+  switch (g->bias_kind[t]) {
+    case JCG_BIAS_INV_GROWTH: return g->bias[t] / D;
+    case JCG_BIAS_DES_Y1: return g->bias[t] * pow((1.0 + z) / (1.0 + g->bias_z0[t]), g->bias_eta[t]);
+    default: return g->bias[t];
+  }
+}
 // Omega_m(a), Omega_de(a) sharing one E^2 (background.py:168, 196)
 __device__ __forceinline__ void bg_om_l(const Bg& c, double a, double lna, double* omm, double* omde) {
   double ef;

@@ -121,8 +121,9 @@ __global__ void __launch_bounds__(TK_WARPS * 32)
       }
     }
     const double z = Z[n];
-    double hz = 0.0;
-    if (geo->n_nc > 0) hz = bg_H(make_bg(s), awl);
+    double hz = 0.0, dz = 1.0;
+    if (geo->n_nc > 0 || geo->special_bias) hz = bg_H(make_bg(s), awl);
+    if (geo->special_bias) dz = growth_at(ct->g, c, awl);
     // lanes write one tracer each (acc indices stay compile-time)
 #pragma unroll
     for (int t = 0; t < MAXTR; ++t) {
@@ -130,9 +131,15 @@ __global__ void __launch_bounds__(TK_WARPS * 32)
         double kv;
         if (geo->kind[t] == JCG_TRACER_WL) {
           const double rk = (double)acc[t] * (1.0 + z) * (double)chi_wl;
-          kv = cf * rk * (1.0 + geo->mult[t]);
+          kv = cf * rk;
+          if (geo->bias_kind[t] != JCG_BIAS_NONE) {
+            // NLA intrinsic alignment (probes.py:102-129), same ell factor as the shear
+            const double nla = NZL[(size_t)t * na + n] * bias_at(geo, t, z, dz) * hz;
+            kv = kv + nla * (-IA_C1_RHOCRIT * s[S_OMEGA_M] / dz);
+          }
+          kv = kv * (1.0 + geo->mult[t]);
         } else {
-          kv = NZL[(size_t)t * na + n] * geo->bias[t] * hz;
+          kv = NZL[(size_t)t * na + n] * bias_at(geo, t, z, dz) * hz;
         }
         it.kern[(size_t)t * na + n] = kv;
       }
@@ -243,7 +250,8 @@ static void launch_tu(const Batch& b, const ConstTables* c, cudaStream_t st) {
 }
 
 void launch_tracer_kernels(const Batch& b, const ConstTables* c, cudaStream_t st) {
-  if (b.precision == JCG_FP32C && !b.listed && b.n_wl_groups == 1 && b.n_wl >= 1 && b.n_wl <= 8) {
+  if (b.precision == JCG_FP32C && !b.listed && !b.special_bias && b.n_wl_groups == 1 && b.n_wl >= 1 &&
+      b.n_wl <= 8) {
     switch (b.n_wl) {
       case 1: launch_tu<1>(b, c, st); return;
       case 2: launch_tu<2>(b, c, st); return;

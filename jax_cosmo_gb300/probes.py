@@ -5,9 +5,11 @@ split and ``n_tracers`` / ``zmax`` / ``noise`` / ``kernel`` methods.  Their radi
 kernels are computed by libjcg (FP64): the lensing efficiency integral of
 probes.py:16-74 and the density kernel of probes.py:77-99.
 
-Not on the accelerated path (the reference's optional branches):
-intrinsic alignment (``ia_bias``, probes.py:102-129, 200-203), ``delta_nz``
-bins (probes.py:53-64) and non-Smail n(z); they raise NotImplementedError.
+Intrinsic alignment (``ia_bias``: the NLA model of probes.py:102-129, added to
+the shear kernel before the multiplicative bias, probes.py:200-207) and the
+three bias models of bias.py are on the accelerated path.  Not on it (they
+raise NotImplementedError): ``delta_nz`` bins (probes.py:53-64) and non-Smail
+n(z).
 """
 from __future__ import annotations
 
@@ -17,6 +19,21 @@ import torch
 from jax_cosmo_gb300.jax_utils import container
 
 __all__ = ["WeakLensing", "NumberCounts"]
+
+
+def _bias_specs(bias, n):
+    """Bias specs of n bins from one bias object or a list (probes.py:89-93)."""
+    from jax_cosmo_gb300.bias import constant_linear_bias, des_y1_ia_bias, inverse_growth_linear_bias
+
+    blist = bias if isinstance(bias, list) else [bias] * n
+    if len(blist) != n:
+        raise ValueError(f"{len(blist)} biases for {n} redshift bins")
+    out = []
+    for b in blist:
+        if not isinstance(b, (constant_linear_bias, inverse_growth_linear_bias, des_y1_ia_bias)):
+            raise NotImplementedError(f"bias model {type(b).__name__} is not on the accelerated path")
+        out.append(b.spec())
+    return out
 
 
 class WeakLensing(container):
@@ -40,6 +57,12 @@ class WeakLensing(container):
     @property
     def zmax(self):
         return max([pz.zmax for pz in self.params[0]])
+
+    def ia_specs(self):
+        """(kind, amplitude, eta, z0) of each bin's NLA bias; kind 0 without IA."""
+        if not self.config.get("ia_enabled", False):
+            return [(0, 0.0, 0.0, 0.0)] * self.n_tracers
+        return _bias_specs(self.params[2], self.n_tracers)
 
     def multiplicative_biases(self):
         m = self.params[1]
@@ -78,19 +101,9 @@ class NumberCounts(container):
     def n_tracers(self):
         return len(self.params[0])
 
-    def bias_values(self):
-        from jax_cosmo_gb300.bias import constant_linear_bias
-
-        bias = self.params[1]
-        blist = bias if isinstance(bias, list) else [bias] * self.n_tracers
-        out = []
-        for b in blist:
-            if not isinstance(b, constant_linear_bias):
-                raise NotImplementedError(
-                    "only constant_linear_bias is on the accelerated path (bias.py:10-22)"
-                )
-            out.append(float(b.params[0]))
-        return out
+    def bias_specs(self):
+        """(kind, amplitude, eta, z0) of each bin's galaxy bias."""
+        return _bias_specs(self.params[1], self.n_tracers)
 
     def kernel(self, cosmo, z, ell):
         """n(z) b(z) H(z) per bin, shape (nbins, nz) (probes.py:260-272)."""

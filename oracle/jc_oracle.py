@@ -44,6 +44,7 @@ C_KMS = 299792.458
 TCMB = 2.726
 RH = 2997.92458
 H0 = 100.0
+RHOCRIT = 2.7750 * 1e11  # constants.py:30
 STERADIAN_TO_ARCMIN2 = 11818102.86004228
 
 PARAM_NAMES = ("Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa")
@@ -509,13 +510,20 @@ class Smail:
 
 @dataclass
 class Probe:
-    """A WeakLensing ('wl') or NumberCounts ('nc') probe (probes.py:132-281)."""
+    """A WeakLensing ('wl') or NumberCounts ('nc') probe (probes.py:132-281).
+
+    ``bias`` (NC galaxy bias) and ``ia`` (WL NLA bias, None = no intrinsic
+    alignment) are a number (constant_linear_bias), a bias spec tuple
+    ("const", b) / ("invg", b) / ("desy1", A, eta, z0) (bias.py:10-57), or a
+    list of those, one per bin.
+    """
 
     kind: str
     bins: list
     sigma_e: float = 0.26
-    bias: float = 1.0
+    bias: object = 1.0
     m: float = 0.0
+    ia: object = None
 
     @property
     def n_tracers(self):
@@ -549,18 +557,58 @@ def weak_lensing_kernel(c, pzs, z, ell):
     return constant_factor * ell_factor * rk
 
 
+def _mult(probe):
+    """1 + m, m a number or one value per bin (probes.py:204-207)."""
+    if isinstance(probe.m, (list, tuple)):
+        return 1.0 + _t(np.asarray(probe.m, dtype=np.float64))[..., None]
+    return 1.0 + probe.m
+
+
+def bias_eval(c, spec, z):
+    """b(cosmo, z) of one bias model (bias.py:10-57)."""
+    if not isinstance(spec, tuple):
+        spec = ("const", spec)
+    if spec[0] == "const":  # bias.py:21-22
+        return spec[1] * torch.ones_like(z)
+    if spec[0] == "invg":  # bias.py:38-39
+        return spec[1] / growth_factor(c, z2a(z))
+    if spec[0] == "desy1":  # bias.py:56-57
+        A, eta, z0 = spec[1:]
+        return A * ((1.0 + z) / (1.0 + z0)) ** eta
+    raise ValueError(spec)
+
+
+def _bias_stack(c, bias, z, n):
+    """probes.py:89-93 / 113-117: a list gives one bias per bin."""
+    if isinstance(bias, list):
+        return torch.stack([bias_eval(c, b, z) for b in bias], dim=0)
+    return bias_eval(c, bias, z)
+
+
 def density_kernel(c, pzs, bias, z):
-    """probes.py:77-99 with a constant linear bias (bias.py:10-22)."""
+    """probes.py:77-99"""
     dndz = torch.stack([pz(z) for pz in pzs], dim=0)
-    b = bias * torch.ones_like(z)
+    b = _bias_stack(c, bias, z, len(pzs))
     return 1.0 * 1.0 * (dndz * b * H(c, z2a(z)))
+
+
+def nla_radial(c, pzs, bias, z):
+    """The ell-independent part of nla_kernel (probes.py:102-129)."""
+    dndz = torch.stack([pz(z) for pz in pzs], dim=0)
+    b = _bias_stack(c, bias, z, len(pzs))
+    rk = dndz * b * H(c, z2a(z))
+    return rk * (-(5e-14 * RHOCRIT) * c.Omega_m / growth_factor(c, z2a(z)))
 
 
 def probe_kernel(c, probe, z, ell):
     """probes.py:188-208 / 260-272."""
     if probe.kind == "wl":
         k = weak_lensing_kernel(c, probe.bins, z, ell)
-        return k * (1.0 + probe.m)
+        if probe.ia is not None:
+            ell_t = _t(ell)
+            ef = torch.sqrt((ell_t - 1) * (ell_t) * (ell_t + 1) * (ell_t + 2)) / (ell_t + 0.5) ** 2
+            k = k + 1.0 * ef * nla_radial(c, probe.bins, probe.ia, torch.atleast_1d(z))
+        return k * _mult(probe)
     return density_kernel(c, probe.bins, probe.bias, z)
 
 
@@ -588,7 +636,9 @@ def probe_kernels_all_ell(c, probe, z, ell):
         constant_factor = 3.0 * H0**2 * c.Omega_m / 2.0 / C_KMS
         ef = torch.sqrt((ell - 1) * (ell) * (ell + 1) * (ell + 2)) / (ell + 0.5) ** 2
         k = (constant_factor * ef)[:, None, None] * rk[None]
-        return k * (1.0 + probe.m)
+        if probe.ia is not None:
+            k = k + (1.0 * ef)[:, None, None] * nla_radial(c, probe.bins, probe.ia, z)[None]
+        return k * _mult(probe)
     k = density_kernel(c, probe.bins, probe.bias, z)
     return k[None].expand(ell.shape[0], -1, -1)
 

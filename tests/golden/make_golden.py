@@ -18,6 +18,9 @@ tracers.npz     smail n(z), WL lensing kernel, NC density kernel, noise
                                                           (redshift.py, probes.py)
 cl_wl2.npz      angular_cl, 2 WeakLensing bins (z0 = 0.5, 1.0; zmax = 4), 50 ell
 cl_mixed.npz    angular_cl, 2 WeakLensing + 2 NumberCounts bins, 2 cosmologies
+cl_ia.npz       angular_cl with NLA intrinsic alignment (des_y1, constant and
+                inverse-growth IA biases, a list of biases per bin), two lensing
+                groups, NumberCounts with inverse-growth and constant biases
 cov_like.npz    gaussian_cl_covariance_and_mean + gaussian_log_likelihood
 sparse.npz      sparse.inv / slogdet / to_dense / dot on a random SPD block matrix
 """
@@ -182,6 +185,22 @@ def _probes(jc, kind):
             jc.probes.WeakLensing(pz, sigma_e=0.26),
             jc.probes.NumberCounts(pz, jc.bias.constant_linear_bias(1.2)),
         ]
+    if kind == "ia":
+        pa = jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10)
+        pb = jc.redshift.smail_nz(1.0, 2.0, 1.0, gals_per_arcmin2=10)
+        pc = jc.redshift.smail_nz(1.0, 2.0, 0.8, gals_per_arcmin2=5, zmax=4.0)
+        return [
+            jc.probes.WeakLensing(
+                [pa, pb],
+                ia_bias=[jc.bias.des_y1_ia_bias(1.2, 0.6, 0.62), jc.bias.constant_linear_bias(0.8)],
+                multiplicative_bias=[0.01, -0.02],
+                sigma_e=0.26,
+            ),
+            jc.probes.WeakLensing([pc], ia_bias=jc.bias.inverse_growth_linear_bias(0.7), sigma_e=0.3),
+            jc.probes.NumberCounts(
+                [pa, pc], [jc.bias.inverse_growth_linear_bias(1.3), jc.bias.constant_linear_bias(1.1)]
+            ),
+        ]
     raise ValueError(kind)
 
 
@@ -292,7 +311,7 @@ def main():
         save("cov_like", make_cov_like(jc))
     if want("sparse"):
         save("sparse", make_sparse(jc))
-    if want("cl_wl2") or want("cl_mixed"):
+    if want("cl_wl2") or want("cl_mixed") or want("cl_ia"):
         import multiprocessing as mp
 
         with mp.get_context("spawn").Pool(args.procs) as pool:
@@ -305,6 +324,9 @@ def main():
                     "cl_mixed",
                     make_cl(args.reference, pool, "mixed", COSMOS[[0, 2]], ell),
                 )
+            if want("cl_ia"):
+                ell = np.logspace(1, np.log10(5000.0), 12)
+                save("cl_ia", make_cl(args.reference, pool, "ia", COSMOS[[0, 2]], ell))
 
 
 if __name__ == "__main__":

@@ -113,6 +113,34 @@ def test_jacobian_vs_oracle_autograd(spec, ell, n_limber):
         assert col_err(J32, J_o) < TOL_J32, col_err(J32, J_o)
 
 
+def test_jacobian_with_intrinsic_alignment_vs_oracle():
+    """NLA intrinsic alignment (des_y1, constant, inverse-growth biases) and
+    inverse-growth NumberCounts bias: Jacobian vs the oracle's autograd."""
+    ell = np.geomspace(10, 3000, 5)
+    pa = jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10)
+    pc = jc.redshift.smail_nz(1.0, 2.0, 0.8, gals_per_arcmin2=5, zmax=4.0)
+    probes = [jc.probes.WeakLensing([pa, pc], ia_bias=[jc.bias.des_y1_ia_bias(1.2, 0.6, 0.62),
+                                                       jc.bias.inverse_growth_linear_bias(0.7)],
+                                    multiplicative_bias=[0.01, -0.02]),
+              jc.probes.NumberCounts([pa], jc.bias.inverse_growth_linear_bias(1.3))]
+    oa, oc = O.Smail(1, 2, 0.5, 10.0, 10), O.Smail(1, 2, 0.8, 4.0, 5)
+    oprobes = [O.Probe("wl", [oa, oc], m=[0.01, -0.02], ia=[("desy1", 1.2, 0.6, 0.62), ("invg", 0.7)]),
+               O.Probe("nc", [oa], bias=("invg", 1.3))]
+
+    def f(v):
+        return O.angular_cl(O.Cosmo.from_vector(v), ell, oprobes, n_limber=128)
+
+    v0 = torch.tensor(OTHER, dtype=torch.float64)
+    cl_o = f(v0)
+    J_o = torch.autograd.functional.jacobian(f, v0, strategy="forward-mode", vectorize=True)
+    for prec, tc, tj in (("fp64", 1e-9, TOL_J), ("fp32c", 1e-4, TOL_J32)):
+        cl, J = jc.autodiff.angular_cl_jacobian(cosmo_of(OTHER), ell, probes, 128, prec)
+        fwd = jc.cl.angular_cl(cosmo_of(OTHER), ell, probes, n_limber=128, precision=prec)
+        assert float(((fwd.cpu() - cl_o) / cl_o).abs().max()) < tc
+        assert float(((cl.cpu() - cl_o) / cl_o).abs().max()) < tc
+        assert col_err(J, J_o) < tj, (prec, col_err(J, J_o))
+
+
 def test_jacobian_vs_central_fd():
     ell = np.geomspace(10, 3000, 8)
     probes = jc_probes(MIXED)

@@ -112,7 +112,21 @@ def _mixed():
             jc.probes.NumberCounts(pz, jc.bias.constant_linear_bias(1.2))]
 
 
-@pytest.mark.parametrize("name,probes", [("cl_wl2", _wl2), ("cl_mixed", _mixed)])
+def _ia():
+    """The intrinsic-alignment fixture's probes (tests/golden/make_golden.py, kind "ia")."""
+    pa = jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10)
+    pb = jc.redshift.smail_nz(1.0, 2.0, 1.0, gals_per_arcmin2=10)
+    pc = jc.redshift.smail_nz(1.0, 2.0, 0.8, gals_per_arcmin2=5, zmax=4.0)
+    return [
+        jc.probes.WeakLensing([pa, pb], ia_bias=[jc.bias.des_y1_ia_bias(1.2, 0.6, 0.62),
+                                                 jc.bias.constant_linear_bias(0.8)],
+                              multiplicative_bias=[0.01, -0.02], sigma_e=0.26),
+        jc.probes.WeakLensing([pc], ia_bias=jc.bias.inverse_growth_linear_bias(0.7), sigma_e=0.3),
+        jc.probes.NumberCounts([pa, pc], [jc.bias.inverse_growth_linear_bias(1.3), jc.bias.constant_linear_bias(1.1)]),
+    ]
+
+
+@pytest.mark.parametrize("name,probes", [("cl_wl2", _wl2), ("cl_mixed", _mixed), ("cl_ia", _ia)])
 def test_angular_cl_vs_golden(golden, name, probes):
     g = golden(name)
     for i, row in enumerate(g["cosmos"]):

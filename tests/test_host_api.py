@@ -1,4 +1,6 @@
 """Host-side logic of the Python API (no GPU): descriptors, orderings, batching."""
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -28,10 +30,37 @@ def test_describe_fills_descriptor():
     assert _geometry.n_cls_of(g) == 10
 
 
+def test_describe_bias_models():
+    nz = [jc.redshift.smail_nz(1.0, 2.0, 1.0), jc.redshift.smail_nz(1.0, 2.0, 0.5)]
+    P = [jc.probes.WeakLensing(nz, ia_bias=[jc.bias.des_y1_ia_bias(1.2, 0.6, 0.62),
+                                            jc.bias.constant_linear_bias(0.8)], multiplicative_bias=[0.01, 0.0]),
+         jc.probes.WeakLensing(nz[:1]),
+         jc.probes.NumberCounts(nz, jc.bias.inverse_growth_linear_bias(1.3))]
+    g = _geometry.describe(P, 3)
+    assert list(g.bias_kind)[:5] == [_lib.BIAS_DES_Y1, _lib.BIAS_CONSTANT, _lib.BIAS_NONE,
+                                     _lib.BIAS_INV_GROWTH, _lib.BIAS_INV_GROWTH]
+    assert (g.bias[0], g.bias_eta[0], g.bias_z0[0]) == (1.2, 0.6, 0.62)
+    assert g.bias[1] == 0.8 and g.bias[3] == 1.3 and g.mult[0] == 0.01
+    sz = ctypes.c_size_t()
+    assert _lib.load().jcg_geometry_size(ctypes.byref(g), ctypes.byref(sz)) == 0
+    # the library validates the bias descriptors
+    g.bias_kind[0] = 9
+    assert _lib.load().jcg_geometry_size(ctypes.byref(g), ctypes.byref(sz)) == _lib.ERR_ARG
+    g.bias_kind[0] = _lib.BIAS_DES_Y1
+    g.bias_z0[0] = -2.0
+    assert _lib.load().jcg_geometry_size(ctypes.byref(g), ctypes.byref(sz)) == _lib.ERR_VALUE
+    with pytest.raises(ValueError):
+        _geometry.describe([jc.probes.NumberCounts(nz, [jc.bias.constant_linear_bias(1.0)])], 3)
+
+
 def test_describe_rejects_unsupported():
     nz = [jc.redshift.smail_nz(1.0, 2.0, 1.0)]
+
+    class other_bias(jc.jax_utils.container):
+        pass
+
     with pytest.raises(NotImplementedError):
-        _geometry.describe([jc.probes.WeakLensing(nz, ia_bias=jc.bias.constant_linear_bias(1.0))], 3)
+        _geometry.describe([jc.probes.NumberCounts(nz, other_bias(1.0))], 3)
 
     class other_nz(jc.redshift.redshift_distribution):
         def pz_fn(self, z):

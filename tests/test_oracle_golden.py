@@ -74,7 +74,17 @@ def test_redshift_and_kernels(golden):
     assert rel(O.Probe("nc", pz).noise(), t["nc_noise"]) < RTOL
 
 
-@pytest.mark.parametrize("name", ["cl_wl2", "cl_mixed"])
+def ia_probes():
+    """The intrinsic-alignment fixture's probes (make_golden.py, kind "ia")."""
+    pa, pb, pc = O.Smail(1, 2, 0.5, 10.0, 10), O.Smail(1, 2, 1.0, 10.0, 10), O.Smail(1, 2, 0.8, 4.0, 5)
+    return [
+        O.Probe("wl", [pa, pb], sigma_e=0.26, m=[0.01, -0.02], ia=[("desy1", 1.2, 0.6, 0.62), ("const", 0.8)]),
+        O.Probe("wl", [pc], sigma_e=0.3, ia=("invg", 0.7)),
+        O.Probe("nc", [pa, pc], bias=[("invg", 1.3), ("const", 1.1)]),
+    ]
+
+
+@pytest.mark.parametrize("name", ["cl_wl2", "cl_mixed", "cl_ia"])
 def test_angular_cl(golden, name):
     g = golden(name)
     for i, row in enumerate(g["cosmos"]):
@@ -82,6 +92,8 @@ def test_angular_cl(golden, name):
         if name == "cl_wl2":
             pz = [O.Smail(1, 2, 0.5, 4.0, 10), O.Smail(1, 2, 1.0, 4.0, 10)]
             P = [O.Probe("wl", pz, sigma_e=0.26)]
+        elif name == "cl_ia":
+            P = ia_probes()
         else:
             pz = [O.Smail(1, 2, 0.5, 10.0, 10), O.Smail(1, 2, 1.0, 10.0, 10)]
             P = [O.Probe("wl", pz, sigma_e=0.26), O.Probe("nc", pz, bias=1.2)]
