@@ -63,6 +63,14 @@ extern "C" {
  *   DES_Y1      A ((1 + z) / (1 + z0))^eta        des_y1_ia_bias
  * with b or A in `bias`, eta and z0 in `bias_eta`, `bias_z0`.  On a
  * NumberCounts tracer JCG_BIAS_NONE means CONSTANT. */
+/* n(z) of a tracer: JCG_NZ_SMAIL (nz_a, nz_b, nz_z0, evaluated by the library,
+ * redshift.py:61-77) or JCG_NZ_TABLE (any redshift_distribution: the caller
+ * evaluates its un-normalised pz_fn at the points jcg_geometry_nz_points lists
+ * and passes them to jcg_geometry_build_nz; the library normalises them with
+ * simps(pz_fn, 0, zmax, 256) as redshift.py:27-31 does). */
+#define JCG_NZ_SMAIL 0
+#define JCG_NZ_TABLE 1
+
 #define JCG_BIAS_NONE 0
 #define JCG_BIAS_CONSTANT 1
 #define JCG_BIAS_INV_GROWTH 2
@@ -95,6 +103,7 @@ typedef struct jcg_geometry {
   int bias_kind[JCG_MAX_TRACERS];     /* JCG_BIAS_*: galaxy bias (NC) or NLA bias (WL) */
   double bias_eta[JCG_MAX_TRACERS];   /* des_y1_ia_bias eta, z0 (bias.py:55-57) */
   double bias_z0[JCG_MAX_TRACERS];
+  int nz_kind[JCG_MAX_TRACERS];       /* JCG_NZ_* */
 } jcg_geometry;
 
 /* ------------------------------------------------------------- misc ---- */
@@ -118,6 +127,20 @@ int jcg_geometry_build(const jcg_geometry* g, const double* ell_dev, void* geo_d
  * NumberCounts.kernel at arbitrary z (probes.py:188-208, 260-272).  Only the
  * cosmology-table and tracer-kernel stages are meaningful on such a geometry;
  * jcg_geometry_size covers it. */
+/* Tabulated n(z) (JCG_NZ_TABLE tracers).  The points where the reference
+ * evaluates each tracer's pz_fn, tracer after tracer: 257 normalisation points
+ * linspace(0, zmax, 257) (redshift.py:30), the n_a Limber nodes (or the
+ * caller's z nodes, z_nodes_dev, when n_nodes > 0), and for a WeakLensing
+ * tracer n_a x 257 lensing points linspace(z_n, probe zmax, 257)
+ * (probes.py:51).  *count receives the number of points; z_out_dev (may be
+ * NULL for a size query) receives them.  jcg_geometry_build_nz then takes the
+ * un-normalised pz_fn values at those points (entries of JCG_NZ_SMAIL tracers
+ * are ignored) and builds the geometry like jcg_geometry_build(_nodes). */
+int jcg_geometry_nz_points(const jcg_geometry* g, const double* z_nodes_dev, double* z_out_dev,
+                           size_t* count, cudaStream_t stream);
+int jcg_geometry_build_nz(const jcg_geometry* g, const double* ell_dev, const double* z_nodes_dev,
+                          const double* pz_dev, size_t pz_count, void* geo_dev, size_t geo_bytes,
+                          cudaStream_t stream);
 int jcg_geometry_build_nodes(const jcg_geometry* g, const double* ell_dev, const double* z_dev,
                              void* geo_dev, size_t geo_bytes, cudaStream_t stream);
 

@@ -16,7 +16,7 @@ import torch
 
 from jax_cosmo_gb300 import _lib
 from jax_cosmo_gb300.probes import NumberCounts, WeakLensing
-from jax_cosmo_gb300.redshift import smail_nz
+from jax_cosmo_gb300.redshift import delta_nz, redshift_distribution, smail_nz
 
 _CACHE_SIZE = 64
 _cache = collections.OrderedDict()
@@ -43,15 +43,20 @@ def describe(probes, n_ell, n_limber=512, n_nodes=0, zmax=None):
             raise NotImplementedError(f"probe type {type(p).__name__} is not supported")
         pzmax = p.zmax
         for b, pz in enumerate(p.params[0]):
-            if not isinstance(pz, smail_nz):
+            if isinstance(pz, delta_nz) or not isinstance(pz, redshift_distribution):
                 raise NotImplementedError(
                     f"redshift distribution {type(pz).__name__} is not on the accelerated path"
                 )
             if n >= _lib.MAX_TRACERS:
                 raise ValueError(f"at most {_lib.MAX_TRACERS} redshift bins per request")
-            a, bb, z0, zm = pz.device_params()
             g.kind[n] = kind
-            g.nz_a[n], g.nz_b[n], g.nz_z0[n], g.nz_zmax[n] = a, bb, z0, zm
+            if isinstance(pz, smail_nz):
+                a, bb, z0, zm = pz.device_params()
+                g.nz_kind[n] = _lib.NZ_SMAIL
+                g.nz_a[n], g.nz_b[n], g.nz_z0[n], g.nz_zmax[n] = a, bb, z0, zm
+            else:
+                g.nz_kind[n] = _lib.NZ_TABLE
+                g.nz_a[n], g.nz_b[n], g.nz_z0[n], g.nz_zmax[n] = 0.0, 0.0, 1.0, float(pz.zmax)
             g.probe_zmax[n] = float(pzmax)
             bk, bamp, beta, bz0 = biases[b]
             g.bias_kind[n] = int(bk)
@@ -82,6 +87,44 @@ def ell_host(ell):
     return np.atleast_1d(np.asarray(ell, dtype=np.float64)).reshape(-1)
 
 
+def _bins(probes):
+    return [pz for p in probes for pz in p.params[0]]
+
+
+def _nz_key(probes):
+    """Cache identity of the tabulated n(z) bins (Smail bins live in the descriptor)."""
+    return tuple(pz.cache_key() if not isinstance(pz, smail_nz) else "" for pz in _bins(probes))
+
+
+def _build(g, probes, ell_t, z_nodes, geo, device):
+    """Build the geometry; tabulated n(z) bins are evaluated at libjcg's points on the device."""
+    st = _lib.stream_of(device)
+    bins = _bins(probes)
+    if all(isinstance(pz, smail_nz) for pz in bins):
+        if z_nodes is None:
+            _lib.call("jcg_geometry_build", ctypes.byref(g), _lib.ptr(ell_t), _lib.ptr(geo),
+                      ctypes.c_size_t(geo.numel()), st)
+        else:
+            _lib.call("jcg_geometry_build_nodes", ctypes.byref(g), _lib.ptr(ell_t), _lib.ptr(z_nodes),
+                      _lib.ptr(geo), ctypes.c_size_t(geo.numel()), st)
+        return
+    count = ctypes.c_size_t()
+    _lib.call("jcg_geometry_nz_points", ctypes.byref(g), _lib.ptr(z_nodes), None, ctypes.byref(count), st)
+    zp = torch.empty(count.value, dtype=torch.float64, device=device)
+    _lib.call("jcg_geometry_nz_points", ctypes.byref(g), _lib.ptr(z_nodes), _lib.ptr(zp), ctypes.byref(count), st)
+    pzv = torch.zeros_like(zp)
+    na = g.n_nodes if g.n_nodes > 0 else g.n_limber + 1
+    off = 0
+    for t, pz in enumerate(bins):
+        cnt = 257 + na + (na * 257 if g.kind[t] == _lib.TRACER_WL else 0)
+        if not isinstance(pz, smail_nz):
+            with torch.cuda.device(device):
+                pzv[off : off + cnt] = torch.as_tensor(pz.pz_fn(zp[off : off + cnt]), dtype=torch.float64)
+        off += cnt
+    _lib.call("jcg_geometry_build_nz", ctypes.byref(g), _lib.ptr(ell_t), _lib.ptr(z_nodes), _lib.ptr(pzv),
+              ctypes.c_size_t(pzv.numel()), _lib.ptr(geo), ctypes.c_size_t(geo.numel()), st)
+
+
 def get_geometry(probes, ell, n_limber, device):
     """(descriptor, device buffer, device ell) for probes on the ell grid, cached.
 
@@ -90,7 +133,7 @@ def get_geometry(probes, ell, n_limber, device):
     """
     ell_np = ell_host(ell)
     g = describe(probes, ell_np.size, n_limber)
-    key = (bytes(g), ell_np.tobytes(), str(device))
+    key = (bytes(g), ell_np.tobytes(), str(device), _nz_key(probes))
     with _cache_lock:
         hit = _cache.get(key)
         if hit is not None:
@@ -100,14 +143,7 @@ def get_geometry(probes, ell, n_limber, device):
     size = ctypes.c_size_t()
     _lib.call("jcg_geometry_size", ctypes.byref(g), ctypes.byref(size))
     buf = _lib.workspace(size.value, device)
-    _lib.call(
-        "jcg_geometry_build",
-        ctypes.byref(g),
-        _lib.ptr(ell_t),
-        _lib.ptr(buf),
-        ctypes.c_size_t(buf.numel()),
-        _lib.stream_of(device),
-    )
+    _build(g, probes, ell_t, None, buf, device)
     val = (g, buf, ell_t)
     with _cache_lock:
         _cache[key] = val
@@ -136,8 +172,7 @@ def probe_kernel(probe, cosmo, z, ell):
     _lib.call("jcg_geometry_size", ctypes.byref(g), ctypes.byref(size))
     geo = _lib.workspace(size.value, device)
     st = _lib.stream_of(device)
-    _lib.call("jcg_geometry_build_nodes", ctypes.byref(g), _lib.ptr(ell_t), _lib.ptr(z_t),
-              _lib.ptr(geo), ctypes.c_size_t(geo.numel()), st)
+    _build(g, [probe], ell_t, z_t, geo, device)
     params = cosmo.param_tensor(device)
     B = params.shape[0]
     wsz = ctypes.c_size_t()

@@ -39,6 +39,7 @@ ERR_ABI = -9
 TRACER_WL = 0
 TRACER_NC = 1
 BIAS_NONE, BIAS_CONSTANT, BIAS_INV_GROWTH, BIAS_DES_Y1 = 0, 1, 2, 3
+NZ_SMAIL, NZ_TABLE = 0, 1
 FP64 = 0
 FP32C = 1
 
@@ -79,6 +80,7 @@ class Geometry(ctypes.Structure):
         ("bias_kind", ctypes.c_int * MAX_TRACERS),
         ("bias_eta", ctypes.c_double * MAX_TRACERS),
         ("bias_z0", ctypes.c_double * MAX_TRACERS),
+        ("nz_kind", ctypes.c_int * MAX_TRACERS),
     ]
 
 
@@ -96,6 +98,8 @@ SIGNATURES = {
     "jcg_geometry_size": [_PG, _PSZ],
     "jcg_geometry_build": [_PG, _P, _P, _SZ, _P],
     "jcg_geometry_build_nodes": [_PG, _P, _P, _P, _SZ, _P],
+    "jcg_geometry_nz_points": [_PG, _P, _P, _PSZ, _P],
+    "jcg_geometry_build_nz": [_PG, _P, _P, _P, _SZ, _P, _SZ, _P],
     "jcg_workspace_size": [_PG, _I, _I, _PSZ],
     "jcg_angular_cl": [_PG, _P, _P, _I, _I, _P, _P, _SZ, _P],
     "jcg_angular_cl_noalloc": [_PG, _P, _P, _I, _I, _P, _P],

@@ -130,6 +130,9 @@ static int make_header(const jcg_geometry* g, GeoHeader* h) {
       if (!isfinite(g->bias_eta[t]) || !isfinite(g->bias_z0[t]) || !(1.0 + g->bias_z0[t] > 0.0))
         return fail(JCG_ERR_VALUE, "tracer %d: des_y1_ia_bias eta = %g, z0 = %g", t, g->bias_eta[t], g->bias_z0[t]);
     }
+    if (g->nz_kind[t] != JCG_NZ_SMAIL && g->nz_kind[t] != JCG_NZ_TABLE)
+      return fail(JCG_ERR_ARG, "tracer %d: nz_kind %d", t, g->nz_kind[t]);
+    h->nz_kind[t] = g->nz_kind[t];
     h->bias_kind[t] = bk;
     h->bias_eta[t] = bk == JCG_BIAS_DES_Y1 ? g->bias_eta[t] : 0.0;
     h->bias_z0[t] = bk == JCG_BIAS_DES_Y1 ? g->bias_z0[t] : 0.0;
@@ -197,6 +200,13 @@ static int make_header(const jcg_geometry* g, GeoHeader* h) {
   h->off_qwl32 = take((na + 1) / 2);
   h->off_dxwl32 = take((na + 1) / 2);
   h->total = o;
+  // n(z) points of tabulated tracers: normalisation grid, nodes, lensing grid (WL)
+  int64_t np_ = 0;
+  for (int t = 0; t < h->n_tr; ++t) {
+    h->nzp_off[t] = np_;
+    np_ += NZP + na + (h->kind[t] == JCG_TRACER_WL ? (int64_t)na * NZP : 0);
+  }
+  h->nzp_total = np_;
   (void)zmx;
   return JCG_OK;
 }
@@ -284,13 +294,22 @@ int jcg_geometry_size(const jcg_geometry* g, size_t* bytes) {
   return JCG_OK;
 }
 
-int jcg_geometry_build(const jcg_geometry* g, const double* ell_dev, void* geo_dev, size_t geo_bytes,
-                       cudaStream_t stream) {
+// Shared by the geometry builds: z_dev are the caller's redshift nodes (n_nodes > 0),
+// pz_dev the tabulated n(z) values (JCG_NZ_TABLE tracers).
+static int geometry_build(const jcg_geometry* g, const double* ell_dev, const double* z_dev,
+                          const double* pz_dev, size_t pz_count, void* geo_dev, size_t geo_bytes,
+                          cudaStream_t stream) {
   GeoHeader h;
   int rc = make_header(g, &h);
   if (rc) return rc;
-  if (h.custom_nodes) return fail(JCG_ERR_ARG, "n_nodes > 0: use jcg_geometry_build_nodes");
+  if (h.custom_nodes && !z_dev) return fail(JCG_ERR_ARG, "n_nodes > 0: the z nodes are NULL");
+  if (!h.custom_nodes && z_dev) return fail(JCG_ERR_ARG, "z nodes given for a Limber-grid geometry");
   if (!ell_dev || !geo_dev) return fail(JCG_ERR_ARG, "ell or geometry buffer is NULL");
+  bool table = false;
+  for (int t = 0; t < h.n_tr; ++t) table |= h.nz_kind[t] == JCG_NZ_TABLE;
+  if (table && (!pz_dev || pz_count < (size_t)h.nzp_total))
+    return fail(JCG_ERR_ARG, "tabulated n(z): %zu values given, %lld needed", pz_count,
+                (long long)h.nzp_total);
   if (geo_bytes < (size_t)h.total * 8)
     return fail(JCG_ERR_WORKSPACE, "geometry buffer %zu bytes, need %zu", geo_bytes, (size_t)h.total * 8);
   if (((uintptr_t)geo_dev) % 64 != 0) return fail(JCG_ERR_ARG, "geometry buffer must be 64-byte aligned");
@@ -300,31 +319,56 @@ int jcg_geometry_build(const jcg_geometry* g, const double* ell_dev, void* geo_d
   if (cudaMemcpyAsync(geo + h.off_ell, ell_dev, sizeof(double) * h.n_ell, cudaMemcpyDeviceToDevice,
                       stream) != cudaSuccess)
     return cuda_check("copy ell");
-  launch_geometry_build(h, geo, c, stream);
+  if (h.custom_nodes && cudaMemcpyAsync(geo + h.off_z, z_dev, sizeof(double) * h.na,
+                                        cudaMemcpyDeviceToDevice, stream) != cudaSuccess)
+    return cuda_check("copy z");
+  launch_geometry_build(h, geo, table ? pz_dev : nullptr, c, stream);
   return cuda_check("geometry build");
+}
+
+static int no_table(const jcg_geometry* g) {
+  for (int t = 0; g && t < g->n_tracers && t < JCG_MAX_TRACERS; ++t)
+    if (g->nz_kind[t] == JCG_NZ_TABLE) return fail(JCG_ERR_ARG, "tabulated n(z): use jcg_geometry_build_nz");
+  return JCG_OK;
+}
+
+int jcg_geometry_build(const jcg_geometry* g, const double* ell_dev, void* geo_dev, size_t geo_bytes,
+                       cudaStream_t stream) {
+  if (g && g->n_nodes > 0) return fail(JCG_ERR_ARG, "n_nodes > 0: use jcg_geometry_build_nodes");
+  if (int rc = no_table(g)) return rc;
+  return geometry_build(g, ell_dev, nullptr, nullptr, 0, geo_dev, geo_bytes, stream);
 }
 
 int jcg_geometry_build_nodes(const jcg_geometry* g, const double* ell_dev, const double* z_dev,
                              void* geo_dev, size_t geo_bytes, cudaStream_t stream) {
-  GeoHeader h;
   if (!g || g->n_nodes < 1) return fail(JCG_ERR_SHAPE, "geometry n_nodes must be > 0");
-  const int n_z = g->n_nodes;
+  if (!z_dev) return fail(JCG_ERR_ARG, "ell, z or geometry buffer is NULL");
+  if (int rc = no_table(g)) return rc;
+  return geometry_build(g, ell_dev, z_dev, nullptr, 0, geo_dev, geo_bytes, stream);
+}
+
+int jcg_geometry_build_nz(const jcg_geometry* g, const double* ell_dev, const double* z_nodes_dev,
+                          const double* pz_dev, size_t pz_count, void* geo_dev, size_t geo_bytes,
+                          cudaStream_t stream) {
+  return geometry_build(g, ell_dev, z_nodes_dev, pz_dev, pz_count, geo_dev, geo_bytes, stream);
+}
+
+int jcg_geometry_nz_points(const jcg_geometry* g, const double* z_nodes_dev, double* z_out_dev, size_t* count,
+                           cudaStream_t stream) {
+  if (!count) return fail(JCG_ERR_ARG, "count is NULL");
+  GeoHeader h;
   int rc = make_header(g, &h);
   if (rc) return rc;
-  if (!ell_dev || !geo_dev || !z_dev) return fail(JCG_ERR_ARG, "ell, z or geometry buffer is NULL");
-  if (geo_bytes < (size_t)h.total * 8)
-    return fail(JCG_ERR_WORKSPACE, "geometry buffer %zu bytes, need %zu", geo_bytes, (size_t)h.total * 8);
-  if (((uintptr_t)geo_dev) % 64 != 0) return fail(JCG_ERR_ARG, "geometry buffer must be 64-byte aligned");
-  ConstTables* c = nullptr;
-  if ((rc = const_tables(&c))) return rc;
-  double* geo = static_cast<double*>(geo_dev);
-  if (cudaMemcpyAsync(geo + h.off_ell, ell_dev, sizeof(double) * h.n_ell, cudaMemcpyDeviceToDevice,
-                      stream) != cudaSuccess ||
-      cudaMemcpyAsync(geo + h.off_z, z_dev, sizeof(double) * n_z, cudaMemcpyDeviceToDevice,
-                      stream) != cudaSuccess)
-    return cuda_check("copy ell / z");
-  launch_geometry_build(h, geo, c, stream);
-  return cuda_check("geometry build");
+  if (!z_out_dev) {
+    *count = (size_t)h.nzp_total;
+    return JCG_OK;
+  }
+  if (*count < (size_t)h.nzp_total) return fail(JCG_ERR_WORKSPACE, "%zu points room, %lld needed", *count,
+                                                (long long)h.nzp_total);
+  if (h.custom_nodes && !z_nodes_dev) return fail(JCG_ERR_ARG, "n_nodes > 0: the z nodes are NULL");
+  launch_nz_points(h, h.custom_nodes ? z_nodes_dev : nullptr, z_out_dev, stream);
+  *count = (size_t)h.nzp_total;
+  return cuda_check("n(z) points");
 }
 
 int jcg_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t* bytes) {

@@ -145,6 +145,9 @@ struct GeoHeader {
   int bias_kind[MAXTR];    // JCG_BIAS_*: NC galaxy bias, WL NLA bias (NONE: no IA)
   double bias_eta[MAXTR], bias_z0[MAXTR];
   int special_bias;        // 1: some tracer has IA or a redshift-dependent bias
+  int nz_kind[MAXTR];      // JCG_NZ_*
+  int64_t nzp_off[MAXTR];  // offset of tracer t's points in the n(z) point list
+  int64_t nzp_total;       // points over all tracers
   double group_zmax[MAXTR];
   double nz_norm[MAXTR];   // redshift.py:30
   // offsets (8-byte units)
@@ -485,7 +488,9 @@ __device__ __forceinline__ double halofit_node(const double* s, const double* ro
 // ------------------------------------------------------------- launches ----
 // Host-side launchers implemented in the kernel translation units.
 void launch_const_init(ConstTables* c, cudaStream_t st);
-void launch_geometry_build(const GeoHeader& h, double* geo, const ConstTables* c, cudaStream_t st);
+void launch_geometry_build(const GeoHeader& h, double* geo, const double* pz, const ConstTables* c,
+                           cudaStream_t st);
+void launch_nz_points(const GeoHeader& h, const double* z_nodes, double* out, cudaStream_t st);
 void launch_cosmo_tables(const Batch& b, const ConstTables* c, cudaStream_t st);
 void launch_halofit_rows(const Batch& b, const ConstTables* c, cudaStream_t st);
 void launch_tracer_kernels(const Batch& b, const ConstTables* c, cudaStream_t st);

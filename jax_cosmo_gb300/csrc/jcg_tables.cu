@@ -82,9 +82,16 @@ __device__ __forceinline__ double smail_pz(const GeoHeader& h, int t, double z) 
   return npow(z, h.nz_a[t]) * exp(-npow(z / h.nz_z0[t], h.nz_b[t]));
 }
 
+// Un-normalised pz_fn of tracer t at z, the `idx`-th point of its n(z) point
+// list: Smail analytically, a tabulated tracer from the caller's values.
+__device__ __forceinline__ double tracer_pz(const GeoHeader& h, const double* pz, int t, int64_t idx, double z) {
+  if (h.nz_kind[t] == JCG_NZ_TABLE) return pz[h.nzp_off[t] + idx];
+  return smail_pz(h, t, z);
+}
+
 // n(z) normalisation (redshift.py:27-31): simps(pz_fn, 0, zmax, 256); also
 // stores the header at the start of the geometry buffer.
-__global__ void geo_norm_kernel(GeoHeader h, double* geo) {
+__global__ void geo_norm_kernel(GeoHeader h, double* geo, const double* pz) {
   GeoHeader* dh = reinterpret_cast<GeoHeader*>(geo);
   const int t = threadIdx.x;
   if (t == 0) *dh = h;
@@ -94,16 +101,47 @@ __global__ void geo_norm_kernel(GeoHeader h, double* geo) {
     const double dx = (zm - 0.0) / 256;
     double acc = 0.0;
     for (int m = 0; m < 128; ++m) {
-      const double y0 = smail_pz(h, t, np_linspace(0.0, zm, 256, 2 * m));
-      const double y1 = smail_pz(h, t, np_linspace(0.0, zm, 256, 2 * m + 1));
-      const double y2 = smail_pz(h, t, np_linspace(0.0, zm, 256, 2 * m + 2));
+      const double y0 = tracer_pz(h, pz, t, 2 * m, np_linspace(0.0, zm, 256, 2 * m));
+      const double y1 = tracer_pz(h, pz, t, 2 * m + 1, np_linspace(0.0, zm, 256, 2 * m + 1));
+      const double y2 = tracer_pz(h, pz, t, 2 * m + 2, np_linspace(0.0, zm, 256, 2 * m + 2));
       acc += y0 + 4 * y1 + y2;
     }
     dh->nz_norm[t] = dx / 3 * acc;
   }
 }
 
-__global__ void geo_tables_kernel(const GeoHeader* __restrict__ hp, double* geo,
+// The points of every tracer's n(z) point list (the same expressions as the
+// geometry build below, so that tabulated values sit at the exact points).
+__global__ void nz_points_kernel(GeoHeader h, const double* __restrict__ zn, double* out) {
+  const int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nth = (int64_t)gridDim.x * blockDim.x;
+  const int na = h.na, N = h.n_limber;
+  const double a0 = 1.0 / (1.0 + h.zmax);
+  for (int64_t q = tid; q < h.nzp_total; q += nth) {
+    int t = 0;
+    while (t + 1 < h.n_tr && h.nzp_off[t + 1] <= q) ++t;
+    const int64_t idx = q - h.nzp_off[t];
+    double z;
+    if (idx < NZP) {
+      z = np_linspace(0.0, h.nz_zmax[t], 256, (int)idx);
+    } else if (idx < NZP + na) {
+      const int n = (int)(idx - NZP);
+      z = zn ? zn[n] : 1.0 / np_linspace(a0, 1.0, N, n) - 1.0;
+    } else {
+      const int64_t r = idx - NZP - na;
+      const int n = (int)(r / NZP), j = (int)(r % NZP);
+      const double zl = zn ? zn[n] : 1.0 / np_linspace(a0, 1.0, N, n) - 1.0;
+      z = np_linspace(zl, h.group_zmax[h.group[t]], NZP - 1, j);
+    }
+    out[q] = z;
+  }
+}
+
+void launch_nz_points(const GeoHeader& h, const double* z_nodes, double* out, cudaStream_t st) {
+  nz_points_kernel<<<296, 256, 0, st>>>(h, z_nodes, out);
+}
+
+__global__ void geo_tables_kernel(const GeoHeader* __restrict__ hp, double* geo, const double* __restrict__ pz,
                                   const ConstTables* __restrict__ c) {
   const GeoHeader& h = *hp;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x;
@@ -142,7 +180,7 @@ __global__ void geo_tables_kernel(const GeoHeader* __restrict__ hp, double* geo,
     SW[n] = pack_seg(swl);
     reinterpret_cast<int32_t*>(geo + h.off_qwl32)[n] = swl.x | (min(swl.x, swl.y) << 16);
     reinterpret_cast<float*>(geo + h.off_dxwl32)[n] = (float)(awl - c->atab_chi[swl.x]);
-    for (int t = 0; t < h.n_tr; ++t) NZL[(size_t)t * na + n] = smail_pz(h, t, z) / h.nz_norm[t];
+    for (int t = 0; t < h.n_tr; ++t) NZL[(size_t)t * na + n] = tracer_pz(h, pz, t, NZP + n, z) / h.nz_norm[t];
   }
   // ell grid factors (probes.py:73; NumberCounts: 1)
   const double* ell = geo + h.off_ell;
@@ -179,7 +217,7 @@ __global__ void geo_tables_kernel(const GeoHeader* __restrict__ hp, double* geo,
       for (int t = 0; t < h.n_tr; ++t) {
         if (h.kind[t] != JCG_TRACER_WL || h.group[t] != g) continue;
         double* W = geo + h.off_W[t];
-        const double wv = dx / 3 * w * (smail_pz(h, t, zp) / h.nz_norm[t]);
+        const double wv = dx / 3 * w * (tracer_pz(h, pz, t, NZP + na + (int64_t)q, zp) / h.nz_norm[t]);
         W[q] = wv;
         reinterpret_cast<float*>(geo + h.off_W32[t])[q] = (float)wv;
       }
@@ -187,9 +225,10 @@ __global__ void geo_tables_kernel(const GeoHeader* __restrict__ hp, double* geo,
   }
 }
 
-void launch_geometry_build(const GeoHeader& h, double* geo, const ConstTables* c, cudaStream_t st) {
-  geo_norm_kernel<<<1, 32, 0, st>>>(h, geo);
-  geo_tables_kernel<<<148, 256, 0, st>>>(reinterpret_cast<const GeoHeader*>(geo), geo, c);
+void launch_geometry_build(const GeoHeader& h, double* geo, const double* pz, const ConstTables* c,
+                           cudaStream_t st) {
+  geo_norm_kernel<<<1, 32, 0, st>>>(h, geo, pz);
+  geo_tables_kernel<<<148, 256, 0, st>>>(reinterpret_cast<const GeoHeader*>(geo), geo, pz, c);
 }
 
 // ------------------------------------------------------ cosmology tables ----

@@ -508,6 +508,59 @@ class Smail:
         return self.gals_per_arcmin2 * STERADIAN_TO_ARCMIN2
 
 
+class _NZ:
+    """Normalised n(z) of a pz_fn (redshift.py:15-58): pz_fn(z) / simps(pz_fn, 0, zmax, 256)."""
+
+    zmax = 10.0
+    gals_per_arcmin2 = 1.0
+
+    @property
+    def norm(self):
+        return simps(self.pz_fn, 0.0, self.zmax, 256)
+
+    def __call__(self, z):
+        return self.pz_fn(z) / self.norm
+
+    @property
+    def gals_per_steradian(self):
+        return self.gals_per_arcmin2 * STERADIAN_TO_ARCMIN2
+
+
+class Fu(_NZ):
+    """redshift.py:80-105: (z^a + z^(a b)) / (z^b + c)."""
+
+    def __init__(self, a, b, c, zmax=10.0, gals_per_arcmin2=1.0):
+        self.a, self.b, self.c, self.zmax, self.gals_per_arcmin2 = a, b, c, zmax, gals_per_arcmin2
+
+    def pz_fn(self, z):
+        return (z**self.a + z ** (self.a * self.b)) / (z**self.b + self.c)
+
+
+class Kde(_NZ):
+    """redshift.py:125-156: Gaussian KDE of a weighted catalog."""
+
+    def __init__(self, zcat, w, bw, zmax=10.0, gals_per_arcmin2=1.0):
+        self.zcat, self.w, self.bw = _t(zcat), _t(w), bw
+        self.zmax, self.gals_per_arcmin2 = zmax, gals_per_arcmin2
+
+    def pz_fn(self, z):
+        shape = z.shape
+        zf = z.reshape(-1)
+        X = self.zcat[:, None]
+        k = (1.0 / math.sqrt(2 * math.pi) / self.bw) * torch.exp(-((X - zf[None, :]) ** 2) / (self.bw**2 * 2.0))
+        return (k.T @ self.w / torch.sum(self.w)).reshape(shape)
+
+
+class Shift(_NZ):
+    """redshift.py:159-171: parent pz_fn at clip(z - bias, 0)."""
+
+    def __init__(self, parent, bias, zmax=10.0, gals_per_arcmin2=1.0):
+        self.parent, self.bias, self.zmax, self.gals_per_arcmin2 = parent, bias, zmax, gals_per_arcmin2
+
+    def pz_fn(self, z):
+        return self.parent.pz_fn(clip(z - self.bias, 0.0))
+
+
 @dataclass
 class Probe:
     """A WeakLensing ('wl') or NumberCounts ('nc') probe (probes.py:132-281).

@@ -21,6 +21,8 @@ cl_mixed.npz    angular_cl, 2 WeakLensing + 2 NumberCounts bins, 2 cosmologies
 cl_ia.npz       angular_cl with NLA intrinsic alignment (des_y1, constant and
                 inverse-growth IA biases, a list of biases per bin), two lensing
                 groups, NumberCounts with inverse-growth and constant biases
+cl_nz.npz       angular_cl with fu_nz, kde_nz (a seeded 200-galaxy catalog, stored
+                with the fixture) and systematic_shift(smail_nz) bins
 cov_like.npz    gaussian_cl_covariance_and_mean + gaussian_log_likelihood
 sparse.npz      sparse.inv / slogdet / to_dense / dot on a random SPD block matrix
 """
@@ -201,7 +203,24 @@ def _probes(jc, kind):
                 [pa, pc], [jc.bias.inverse_growth_linear_bias(1.3), jc.bias.constant_linear_bias(1.1)]
             ),
         ]
+    if kind == "nz":
+        zcat, w = nz_catalog()
+        fu = jc.redshift.fu_nz(0.471, 5.1843, 0.7259, gals_per_arcmin2=30)
+        kde = jc.redshift.kde_nz(zcat, w, bw=0.1, gals_per_arcmin2=10, zmax=4.0)
+        shift = jc.redshift.systematic_shift(jc.redshift.smail_nz(1.0, 2.0, 0.7, gals_per_arcmin2=10), 0.05)
+        return [
+            jc.probes.WeakLensing([fu, kde, shift], sigma_e=0.26),
+            jc.probes.NumberCounts([kde], jc.bias.constant_linear_bias(1.2)),
+        ]
     raise ValueError(kind)
+
+
+def nz_catalog():
+    """The seeded catalog of the kde_nz fixture: 200 redshifts and weights."""
+    rng = np.random.default_rng(20261204)
+    zcat = np.clip(rng.normal(0.8, 0.3, 200), 0.05, None)
+    w = rng.uniform(0.5, 1.0, 200)
+    return zcat, w
 
 
 def _cl_worker(args):
@@ -311,7 +330,7 @@ def main():
         save("cov_like", make_cov_like(jc))
     if want("sparse"):
         save("sparse", make_sparse(jc))
-    if want("cl_wl2") or want("cl_mixed") or want("cl_ia"):
+    if want("cl_wl2") or want("cl_mixed") or want("cl_ia") or want("cl_nz"):
         import multiprocessing as mp
 
         with mp.get_context("spawn").Pool(args.procs) as pool:
@@ -327,6 +346,11 @@ def main():
             if want("cl_ia"):
                 ell = np.logspace(1, np.log10(5000.0), 12)
                 save("cl_ia", make_cl(args.reference, pool, "ia", COSMOS[[0, 2]], ell))
+            if want("cl_nz"):
+                ell = np.logspace(1, np.log10(5000.0), 10)
+                d = make_cl(args.reference, pool, "nz", COSMOS[[0, 2]], ell)
+                d["zcat"], d["w"] = nz_catalog()
+                save("cl_nz", d)
 
 
 if __name__ == "__main__":

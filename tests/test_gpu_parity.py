@@ -349,3 +349,47 @@ def test_fast_moments_match_full_moments():
     for col in (2, 3, 4):  # k_nl, n_eff, C
         err = ((fast[..., col] - full[..., col]).abs() / full[..., col].abs()).max().item()
         assert err < 1e-12, (col, err)
+
+
+def _nz_probes(g):
+    """The tabulated n(z) fixture's probes (tests/golden/make_golden.py, kind "nz")."""
+    kde = jc.redshift.kde_nz(g["zcat"], g["w"], bw=0.1, gals_per_arcmin2=10, zmax=4.0)
+    fu = jc.redshift.fu_nz(0.471, 5.1843, 0.7259, gals_per_arcmin2=30)
+    shift = jc.redshift.systematic_shift(jc.redshift.smail_nz(1.0, 2.0, 0.7, gals_per_arcmin2=10), 0.05)
+    return [jc.probes.WeakLensing([fu, kde, shift], sigma_e=0.26),
+            jc.probes.NumberCounts([kde], jc.bias.constant_linear_bias(1.2))]
+
+
+def test_tabulated_nz_vs_golden(golden):
+    """fu_nz, kde_nz and systematic_shift bins: pz_fn evaluated on the device at
+    libjcg's points, against the unmodified reference's C_ell; the Jacobian
+    with tabulated bins against the oracle's autograd."""
+    g = golden("cl_nz")
+    cb = cosmo_batch(g["cosmos"])
+    cl = jc.cl.angular_cl(cb, g["ell"], _nz_probes(g))
+    cl32 = jc.cl.angular_cl(cb, g["ell"], _nz_probes(g), precision="fp32c")
+    for i in range(len(g["cosmos"])):
+        assert rel(cl[i], g["cl"][i]) < RT64
+        assert rel(cl32[i], g["cl"][i]) < RT32
+    # kernels at arbitrary redshifts go through the same tabulation
+    zq = np.linspace(0.05, 2.5, 7)
+    kq = _nz_probes(g)[1].kernel(cosmo_of(g["cosmos"][0]), zq, 100.0)
+    kde = O.Kde(g["zcat"], g["w"], 0.1, zmax=4.0, gals_per_arcmin2=10)
+    kref = O.probe_kernel(O.Cosmo.from_vector(g["cosmos"][0]), O.Probe("nc", [kde], bias=1.2),
+                          torch.tensor(zq), 100.0)
+    assert rel(kq, kref) < RT64
+    ell = g["ell"][::3]
+    oprobes = [O.Probe("wl", [O.Fu(0.471, 5.1843, 0.7259, gals_per_arcmin2=30), kde,
+                              O.Shift(O.Smail(1.0, 2.0, 0.7, 10.0, 10), 0.05)], sigma_e=0.26),
+               O.Probe("nc", [kde], bias=1.2)]
+    row = list(g["cosmos"][1])
+
+    def f(v):
+        return O.angular_cl(O.Cosmo.from_vector(v), ell, oprobes, n_limber=128)
+
+    J_o = torch.autograd.functional.jacobian(f, torch.tensor(row, dtype=torch.float64), strategy="forward-mode",
+                                             vectorize=True)
+    _, J = jc.autodiff.angular_cl_jacobian(cosmo_of(row), ell, _nz_probes(g), 128)
+    err = max(float((J[..., d].cpu() - J_o[..., d]).abs().max() / J_o[..., d].abs().max().clamp_min(1e-300))
+              for d in range(8))
+    assert err < 1e-8, err

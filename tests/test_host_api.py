@@ -66,8 +66,15 @@ def test_describe_rejects_unsupported():
         def pz_fn(self, z):
             return z
 
+    # any redshift_distribution is tabulated; single-plane bins are not supported
+    g = _geometry.describe([jc.probes.WeakLensing([other_nz(zmax=3.0), jc.redshift.smail_nz(1, 2, 1)])], 3)
+    assert list(g.nz_kind)[:2] == [_lib.NZ_TABLE, _lib.NZ_SMAIL] and g.nz_zmax[0] == 3.0
     with pytest.raises(NotImplementedError):
-        _geometry.describe([jc.probes.WeakLensing([other_nz(zmax=3.0)])], 3)
+        _geometry.describe([jc.probes.WeakLensing([jc.redshift.delta_nz(1.0)])], 3)
+    # the point list has 257 + na (+ na x 257 for lensing) entries per tracer
+    cnt = ctypes.c_size_t()
+    assert _lib.load().jcg_geometry_nz_points(ctypes.byref(g), None, None, ctypes.byref(cnt), None) == 0
+    assert cnt.value == 2 * (257 + 513 + 513 * 257)
     with pytest.raises(ValueError):
         _geometry.describe([jc.probes.WeakLensing([jc.redshift.smail_nz(1, 2, 1)] * 17)], 3)
 

@@ -84,7 +84,15 @@ def ia_probes():
     ]
 
 
-@pytest.mark.parametrize("name", ["cl_wl2", "cl_mixed", "cl_ia"])
+def nz_probes(g):
+    """The n(z) fixture's probes (make_golden.py, kind "nz")."""
+    kde = O.Kde(g["zcat"], g["w"], 0.1, zmax=4.0, gals_per_arcmin2=10)
+    fu = O.Fu(0.471, 5.1843, 0.7259, gals_per_arcmin2=30)
+    shift = O.Shift(O.Smail(1.0, 2.0, 0.7, 10.0, 10), 0.05)
+    return [O.Probe("wl", [fu, kde, shift], sigma_e=0.26), O.Probe("nc", [kde], bias=1.2)]
+
+
+@pytest.mark.parametrize("name", ["cl_wl2", "cl_mixed", "cl_ia", "cl_nz"])
 def test_angular_cl(golden, name):
     g = golden(name)
     for i, row in enumerate(g["cosmos"]):
@@ -94,6 +102,8 @@ def test_angular_cl(golden, name):
             P = [O.Probe("wl", pz, sigma_e=0.26)]
         elif name == "cl_ia":
             P = ia_probes()
+        elif name == "cl_nz":
+            P = nz_probes(g)
         else:
             pz = [O.Smail(1, 2, 0.5, 10.0, 10), O.Smail(1, 2, 1.0, 10.0, 10)]
             P = [O.Probe("wl", pz, sigma_e=0.26), O.Probe("nc", pz, bias=1.2)]
