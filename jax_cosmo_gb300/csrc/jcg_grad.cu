@@ -30,6 +30,30 @@ __device__ __forceinline__ D1 interp_d1(double x, const double* xp, const double
   return a * x + b;
 }
 
+// One RK4 step of the growth ODE (background.py:96-111) from (y0, y1) = (D, dD/da):
+// dy0/da = y1, dy1/da = -q y1 + r y0, coefficients at the step's start (qa0,
+// ra0), midpoint (qm, rm) and end (qa1, ra1).
+template <class T>
+__device__ __forceinline__ void growth_rk4_step(const T& y0, const T& y1, const T& qa0, const T& ra0, const T& qm,
+                                                const T& rm, const T& qa1, const T& ra1, double hh, T& o0, T& o1) {
+  const T k1a = y1, k1b = -qa0 * y1 + ra0 * y0;
+  const T y0b = y0 + hh * k1a / 2, y1b = y1 + hh * k1b / 2;
+  const T k2a = y1b, k2b = -qm * y1b + rm * y0b;
+  const T y0c = y0 + hh * k2a / 2, y1c = y1 + hh * k2b / 2;
+  const T k3a = y1c, k3b = -qm * y1c + rm * y0c;
+  const T y0d = y0 + hh * k3a, y1d = y1 + hh * k3b;
+  const T k4a = y1d, k4b = -qa1 * y1d + ra1 * y0d;
+  o0 = y0 + 1.0 / 6.0 * hh * (k1a + 2 * k2a + 2 * k3a + k4a);
+  o1 = y1 + 1.0 / 6.0 * hh * (k1b + 2 * k2b + 2 * k3b + k4b);
+}
+
+// 2 x 2 row-major products: r = a b, and a vector v <- a v
+__device__ __forceinline__ void mat2_mul(const double* a, const double* b, double* r) {
+  const double r0 = a[0] * b[0] + a[1] * b[2], r1 = a[0] * b[1] + a[1] * b[3];
+  const double r2 = a[2] * b[0] + a[3] * b[2], r3 = a[2] * b[1] + a[3] * b[3];
+  r[0] = r0, r[1] = r1, r[2] = r2, r[3] = r3;
+}
+
 // Tables of one cosmology with tangents.  Lanes: dir = tid & 7, item = tid >> 3.
 // F32T (fp32c Jacobian): the per-node evaluations (ODE right-hand sides,
 // Eisenstein-Hu at the Romberg and halofit k nodes) run one node per thread in
@@ -156,7 +180,174 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
   }
   __syncthreads();
   const int warp = t >> 5, lane = t & 31;
-  if (lane < NDIR) {
+  if (F32T) {
+    // fp32c: the three sequential scans as parallel scans (128 threads).
+    // Growth: one RK4 step is linear in y = (D, dD/da), y_i = M_i y_{i-1};
+    // thread i forms M_i (FP64) and its tangents dM_i (FP32) by running the
+    // step on the unit vectors in DualF<8>.
+    double m4[4] = {1.0, 0.0, 0.0, 1.0};
+    float dm4[4][NDIR];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) dm4[q][d] = 0.f;
+    if (t >= 1 && t < NGROW) {
+      const double* QA = qr;
+      const double* RA = qr + (NDIR + 1) * NGROW;
+      const double* QM = qr + 2 * (NDIR + 1) * NGROW;
+      const double* RM = qr + 3 * (NDIR + 1) * NGROW;
+      auto g8 = [&](const double* arr, int e) { return f8_of(arr[e], arr + NGROW + e, NGROW); };
+      const F8 qa0 = g8(QA, t - 1), ra0 = g8(RA, t - 1), qm = g8(QM, t), rm = g8(RM, t);
+      const F8 qa1 = g8(QA, t), ra1 = g8(RA, t);
+      const double hh = c->atab_grow[t] - c->atab_grow[t - 1];
+      const F8 one = fconst<NDIR>(1.0), zero = fconst<NDIR>(0.0);
+      F8 o0, o1;
+      growth_rk4_step(one, zero, qa0, ra0, qm, rm, qa1, ra1, hh, o0, o1);  // column 0
+      m4[0] = o0.v, m4[2] = o1.v;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) dm4[0][d] = o0.d[d], dm4[2][d] = o1.d[d];
+      growth_rk4_step(zero, one, qa0, ra0, qm, rm, qa1, ra1, hh, o0, o1);  // column 1
+      m4[1] = o0.v, m4[3] = o1.v;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) dm4[1][d] = o0.d[d], dm4[3][d] = o1.d[d];
+    }
+    __syncthreads();  // every read of the growth coefficients is done
+    double* Mv = qr;                                          // [NGROW][4]
+    float* dMv = reinterpret_cast<float*>(qr + 4 * NGROW);    // [NGROW][4][NDIR]
+    double* Yv = qr + 4 * NGROW + 2 * NDIR * NGROW;           // [NGROW][2] y_i
+    if (t < NGROW) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        Mv[t * 4 + q] = m4[q];
+#pragma unroll
+        for (int d = 0; d < NDIR; ++d) dMv[(t * 4 + q) * NDIR + d] = dm4[q][d];
+      }
+    }
+    __syncthreads();
+    if (warp == 0) {
+      // y_i = M_i ... M_1 y_0: lane l holds steps 4l .. 4l + 3 (M_0 = I)
+      double A[4];
+      A[0] = Mv[lane * 16 + 0], A[1] = Mv[lane * 16 + 1], A[2] = Mv[lane * 16 + 2], A[3] = Mv[lane * 16 + 3];
+      for (int k = 1; k < 4; ++k) mat2_mul(Mv + (lane * 4 + k) * 4, A, A);
+      for (int o = 1; o < 32; o <<= 1) {
+        double P[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) P[q] = __shfl_up_sync(0xffffffffu, A[q], o);
+        if (lane >= o) mat2_mul(A, P, A);
+      }
+      double E[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) E[q] = __shfl_up_sync(0xffffffffu, A[q], 1);
+      if (lane == 0) E[0] = 1.0, E[1] = 0.0, E[2] = 0.0, E[3] = 1.0;
+      const double ya = c->atab_grow[0], yb = 1.0;
+      double u0 = E[0] * ya + E[1] * yb, u1 = E[2] * ya + E[3] * yb;
+      double ys[4];
+      for (int k = 0; k < 4; ++k) {
+        const double* M = Mv + (lane * 4 + k) * 4;
+        const double v0 = M[0] * u0 + M[1] * u1, v1 = M[2] * u0 + M[3] * u1;
+        u0 = v0, u1 = v1;
+        ys[k] = u0;
+        Yv[(lane * 4 + k) * 2 + 0] = u0;
+        Yv[(lane * 4 + k) * 2 + 1] = u1;
+      }
+      const double yf = __shfl_sync(0xffffffffu, u0, 31);
+      for (int k = 0; k < 4; ++k) out->gv[lane * 4 + k] = ys[k] / yf;
+    } else {
+      // chi: prefix sums of the RK4 increments (scipy/ode.py:21, first step
+      // h = 0) for the value and the 8 tangents, chi = Y[-1] - Y; lane l
+      // holds nodes 8l .. 8l + 7
+      for (int comp = warp - 1; comp < NDIR + 1; comp += 3) {
+        const double* f0 = fn + comp * NCHI;
+        const double* f1 = fm + comp * NCHI;
+        double loc[8], s = 0.0;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int i = lane * 8 + k;
+          if (i > 0) {
+            const double hh = c->lna_chi[i] - c->lna_chi[i - 1];
+            s += 1.0 / 6.0 * hh * (f0[i - 1] + 2 * f1[i] + 2 * f1[i] + f0[i]);
+          }
+          loc[k] = s;
+        }
+        double x = s;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const double u = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o) x += u;
+        }
+        double off = __shfl_up_sync(0xffffffffu, x, 1);
+        if (lane == 0) off = 0.0;
+        const double tot = __shfl_sync(0xffffffffu, x, 31);
+        double* dst = comp == 0 ? out->chiv : out->chid[comp - 1];
+#pragma unroll
+        for (int k = 0; k < 8; ++k) dst[lane * 8 + k] = tot - (off + loc[k]);
+      }
+      // sigmasqr(8) (power.py:70-78): romb is linear in the integrand values,
+      // sum_e w_e f_e with the weights of the Richardson combination
+      for (int comp = warp - 1; comp < NDIR + 1; comp += 3) {
+        double s = 0.0;
+        for (int e = lane; e < NROMB; e += 32) s = fma(c->romb_w[e], fr[comp * NROMB + e], s);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) {
+          const double sig8 = 1.0 / (2.0 * (PI * PI)) * s;
+          if (comp == 0) sv[S_SIGMASQR8] = sig8;
+          else sd[(comp - 1) * NSCAL + S_SIGMASQR8] = sig8;
+        }
+      }
+    }
+    __syncthreads();
+    // growth tangents: dy_i = M_i dy_{i-1} + dM_i y_{i-1}, dy_0 = 0, as an
+    // FP32 scan of affine maps (A, b), one direction per warp and pass
+    for (int d = warp; d < NDIR; d += 4) {
+      float A[4] = {1.f, 0.f, 0.f, 1.f}, b[2] = {0.f, 0.f};
+      float Mf[4][4], bf[4][2];
+      for (int k = 0; k < 4; ++k) {
+        const int i = lane * 4 + k;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) Mf[k][q] = (float)Mv[i * 4 + q];
+        const float yp0 = i > 0 ? (float)Yv[(i - 1) * 2] : 0.f, yp1 = i > 0 ? (float)Yv[(i - 1) * 2 + 1] : 0.f;
+        const float* dM = dMv + i * 4 * NDIR + d;
+        bf[k][0] = dM[0] * yp0 + dM[NDIR] * yp1;
+        bf[k][1] = dM[2 * NDIR] * yp0 + dM[3 * NDIR] * yp1;
+        const float a0 = Mf[k][0] * A[0] + Mf[k][1] * A[2], a1 = Mf[k][0] * A[1] + Mf[k][1] * A[3];
+        const float a2 = Mf[k][2] * A[0] + Mf[k][3] * A[2], a3 = Mf[k][2] * A[1] + Mf[k][3] * A[3];
+        const float b0 = Mf[k][0] * b[0] + Mf[k][1] * b[1] + bf[k][0];
+        const float b1 = Mf[k][2] * b[0] + Mf[k][3] * b[1] + bf[k][1];
+        A[0] = a0, A[1] = a1, A[2] = a2, A[3] = a3, b[0] = b0, b[1] = b1;
+      }
+      for (int o = 1; o < 32; o <<= 1) {
+        float P[4], p[2];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) P[q] = __shfl_up_sync(0xffffffffu, A[q], o);
+        p[0] = __shfl_up_sync(0xffffffffu, b[0], o);
+        p[1] = __shfl_up_sync(0xffffffffu, b[1], o);
+        if (lane >= o) {
+          // (A, b) after (P, p): x -> A (P x + p) + b
+          const float b0 = A[0] * p[0] + A[1] * p[1] + b[0], b1 = A[2] * p[0] + A[3] * p[1] + b[1];
+          const float a0 = A[0] * P[0] + A[1] * P[2], a1 = A[0] * P[1] + A[1] * P[3];
+          const float a2 = A[2] * P[0] + A[3] * P[2], a3 = A[2] * P[1] + A[3] * P[3];
+          A[0] = a0, A[1] = a1, A[2] = a2, A[3] = a3, b[0] = b0, b[1] = b1;
+        }
+      }
+      float x0 = __shfl_up_sync(0xffffffffu, b[0], 1), x1 = __shfl_up_sync(0xffffffffu, b[1], 1);
+      if (lane == 0) x0 = 0.f, x1 = 0.f;
+      float dy[4];
+      for (int k = 0; k < 4; ++k) {
+        const float v0 = Mf[k][0] * x0 + Mf[k][1] * x1 + bf[k][0];
+        const float v1 = Mf[k][2] * x0 + Mf[k][3] * x1 + bf[k][1];
+        x0 = v0, x1 = v1;
+        dy[k] = x0;
+      }
+      const float dyf = __shfl_sync(0xffffffffu, x0, 31);
+      const double yf = Yv[(NGROW - 1) * 2];
+      for (int k = 0; k < 4; ++k) {
+        const int i = lane * 4 + k;
+        const double D = Yv[i * 2] / yf;
+        out->gd[d][i] = ((double)dy[k] - D * (double)dyf) / yf;
+      }
+    }
+  } else if (lane < NDIR) {
     const int d = lane;
     auto gv = [&](const double* arr, int stride, int e) { return mk1(arr[e], arr[(1 + d) * stride + e]); };
     if (warp == 0) {
@@ -240,6 +431,14 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     }
   }
   __syncthreads();
+  if (F32T && t < NDIR) {
+    // P(k) normalisation sigma8^2 / sigmasqr(8) (power.py:47)
+    const D1 s8 = mk1(sv[S_SIGMA8], sd[dir * NSCAL + S_SIGMA8]);
+    const D1 pkn = (s8 * s8) / mk1(sv[S_SIGMASQR8], sd[dir * NSCAL + S_SIGMASQR8]);
+    __syncwarp(0xffu);
+    if (dir == 0) sv[S_PKNORM] = pkn.v;
+    sd[dir * NSCAL + S_PKNORM] = pkn.d[0];
+  }
   if (t < NDIR) {
     // growth_factor(1.0)
     const int2 sg = interp_segment_inc(1.0, c->atab_grow, NGROW, NGROW - 1);
@@ -293,25 +492,19 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       pqw[i * NDIR + d] = (float)(c->simpson_kh[i] * pq[(1 + d) * NKH + i]);
     }
     __syncthreads();
-    if (warp == 0) {
-      if (lane < NTAYLOR) pv[lane] = 0.0;
-      double carry[NTAYLOR];
-#pragma unroll
-      for (int m = 0; m < NTAYLOR; ++m) carry[m] = 0.0;
+    if (t < NTAYLOR) pv[t] = 0.0;
+    for (int m = warp; m < NTAYLOR; m += 4) {
+      double carry = 0.0;
       for (int base = 0; base < NKH; base += 32) {
         const int i = base + lane;
-        const double q = i < NKH ? pq[i] : 0.0;
+        double x = i < NKH ? c->kpw[m][i] * pq[i] : 0.0;
 #pragma unroll
-        for (int m = 0; m < NTAYLOR; ++m) {
-          double x = i < NKH ? c->kpw[m][i] * q : 0.0;
-#pragma unroll
-          for (int o = 1; o < 32; o <<= 1) {
-            const double u = __shfl_up_sync(0xffffffffu, x, o);
-            if (lane >= o) x += u;
-          }
-          if (i < NKH) pv[(size_t)(i + 1) * NTAYLOR + m] = carry[m] + x;
-          carry[m] += __shfl_sync(0xffffffffu, x, 31);
+        for (int o = 1; o < 32; o <<= 1) {
+          const double u = __shfl_up_sync(0xffffffffu, x, o);
+          if (lane >= o) x += u;
         }
+        if (i < NKH) pv[(size_t)(i + 1) * NTAYLOR + m] = carry + x;
+        carry += __shfl_sync(0xffffffffu, x, 31);
       }
     }
     for (int job = t; job < NTAYLOR * NDIR; job += blockDim.x) {

@@ -18,21 +18,22 @@
 namespace jcg {
 
 // ---------------------------------------------------------- radial kernels --
-// One warp per node, lanes over the 257 lensing z' points, four tracers per
-// pass.  Lensing efficiency (probes.py:44-51) with tangents:
+// One warp per node, lanes over the 257 lensing z' points, the WeakLensing
+// tracers of one lensing group per pass; `npc` nodes per CTA (fewer for small
+// batches, so that the grid still covers the GPU).  Lensing efficiency (probes.py:44-51) with tangents:
 //   r_j = max(chi'_j - chi, 0) / max(chi'_j, 1)
 //   dr_j = ic_j (dchi'_j (1 - r_j [chi'_j > 1]) - dchi)  where chi'_j > chi
 // accumulated as sum W r, sum W ic, sum W ic (1 - r) dchi'.
-constexpr int GK_NODES = 128;  // nodes per CTA (8 warps x 16)
+constexpr int GK_NODES = 128;  // nodes per CTA at most (8 warps x 16)
 
 template <int TP>
-__global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+__global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const ConstTables* __restrict__ c, int npc) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
   const GradItem gi = grad_item(gb, item);
   const GeoHeader* geo = gi.geo;
   const int na = geo->na, n_tr = geo->n_tr;
-  const int n0 = blockIdx.x * GK_NODES;
+  const int n0 = blockIdx.x * npc;
   if (n0 >= na) return;
   // passes: WeakLensing tracers of one lensing group, up to TP per pass
   __shared__ int ptr_t[JCG_MAX_TRACERS * TP];
@@ -84,7 +85,7 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
   const double om = tb->sv[S_OMEGA_M];
   const float cff = (float)(3.0 * (H0 * H0) * om / 2.0 / C_KMS);  // probes.py:71
   const float dlcf = (float)(tb->sd[dir][S_OMEGA_M] / om);         // d ln(cf)
-  const int n_end = min(na, n0 + GK_NODES);
+  const int n_end = min(na, n0 + npc);
   for (int n = n0 + warp; n < n_end; n += 8) {
     const int qw = QWL[n];
     const int xw = qw & 0xffff, mw = qw >> 16;
@@ -176,9 +177,11 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
       }
     }
     // NumberCounts tracers, and the NLA term of WeakLensing tracers with IA
-    // (added to the shear part this lane wrote above, times 1 + m)
-    if (lane < NDIR) {
-      for (int t = 0; t < n_tr; ++t) {
+    // (added to the shear part written above, times 1 + m): four tracers at a
+    // time, lanes 8u .. 8u + 7 on tracer u
+    __syncwarp();
+    {
+      for (int t = lane >> 3; t < n_tr; t += 4) {
         const bool wl = geo->kind[t] == JCG_TRACER_WL;
         if (wl && geo->bias_kind[t] == JCG_BIAS_NONE) continue;
         double kv, kd;
@@ -198,10 +201,15 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
 }
 
 void launch_grad_kern32(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
-  dim3 grid((gb.na + GK_NODES - 1) / GK_NODES, gb.n_items);
-  if (gb.n_tr <= 3) grad_kern32_kernel<3><<<grid, 256, 0, st>>>(gb, c);
-  else if (gb.n_tr <= 5) grad_kern32_kernel<5><<<grid, 256, 0, st>>>(gb, c);
-  else grad_kern32_kernel<8><<<grid, 256, 0, st>>>(gb, c);
+  // halve the nodes per CTA (down to one per warp) until the grid has two
+  // CTAs per SM
+  const long target = 2L * device_sm_count();
+  int npc = GK_NODES;
+  while (npc > 8 && (long)((gb.na + npc - 1) / npc) * gb.n_items < target) npc /= 2;
+  dim3 grid((gb.na + npc - 1) / npc, gb.n_items);
+  if (gb.n_tr <= 3) grad_kern32_kernel<3><<<grid, 256, 0, st>>>(gb, c, npc);
+  else if (gb.n_tr <= 5) grad_kern32_kernel<5><<<grid, 256, 0, st>>>(gb, c, npc);
+  else grad_kern32_kernel<8><<<grid, 256, 0, st>>>(gb, c, npc);
 }
 
 // ---------------------------------------------------------- Limber adjoint --

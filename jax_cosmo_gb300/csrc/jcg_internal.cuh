@@ -36,6 +36,15 @@ constexpr double EULER_E = 2.718281828459045;  // np.exp(1.0)
 // Grids shared by every cosmology and every geometry, built once per device.
 constexpr int NTAYLOR = 20;      // Taylor terms of exp(-y^2) below y^2 = 1 (1/19! < 1e-17)
 
+// Number of SMs of the current device (grid sizing); 152 if the query fails.
+inline int device_sm_count() {
+  int dev = 0, n = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+      n <= 0)
+    return 152;
+  return n;
+}
+
 struct ConstTables {
   double atab_chi[NCHI];   // logspace(-3, 0, 256)
   double lna_chi[NCHI];    // log(atab_chi): the RK4 abscissae of background.py:231
@@ -48,6 +57,7 @@ struct ConstTables {
   double romb_logk[NROMB]; // romb abscissae in evaluation order (scipy/integrate.py:129-146)
   double E[NKH * NRT];     // exp(-(k_i r_j)^2), i-major: power.py:99-109
   double kpw[NTAYLOR][NKH];  // simpson_kh[i] * kh[i]^(2(m+1)): the Taylor prefix sums' weights
+  double romb_w[NROMB];      // romb's Richardson combination as weights on romb_logk's values
 };
 
 // ------------------------------------------------- per-cosmology tables -----

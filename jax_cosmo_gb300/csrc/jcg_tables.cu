@@ -62,6 +62,30 @@ __global__ void const_init_kernel(ConstTables* c) {
       for (int m = 0; m < numtosum; ++m) c->romb_logk[pos++] = lox + h * (double)m;
     }
   }
+  // romb is linear in the integrand values: the weight of abscissa e is the
+  // combination (scipy/integrate.py:131-159, divmax = 7) of the unit vector e
+  for (int e = tid; e < NROMB; e += nth) {
+    const double a = -4.0, b = 3.0, intrange = b - a;
+    double ordsum = 0.5 * ((e == 0 ? 1.0 : 0.0) + (e == 1 ? 1.0 : 0.0));
+    double state[8];
+    for (int i = 0; i < 8; ++i) state[i] = intrange * ordsum;
+    int pos = 2;
+    for (int lev = 1; lev <= 7; ++lev) {
+      const int n = 1 << lev, numtosum = n / 2;
+      ordsum += (e >= pos && e < pos + numtosum) ? 1.0 : 0.0;
+      pos += numtosum;
+      double x = intrange * ordsum / (double)n;
+      double ns[8];
+      ns[0] = x;
+      for (int kk = 0; kk < 7; ++kk) {
+        const double tmp = ldexp(1.0, 2 * (kk + 1));
+        x = (tmp * x - state[kk]) / (tmp - 1.0);
+        ns[kk + 1] = x;
+      }
+      for (int i = 0; i < 8; ++i) state[i] = ns[i];
+    }
+    c->romb_w[e] = state[7];
+  }
   // exp(-(k_i r_j)^2), i-major
   for (int q = tid; q < NKH * NRT; q += nth) {
     const int i = q / NRT, j = q % NRT;
