@@ -53,4 +53,32 @@ __device__ __forceinline__ void sincos_reduced(float x, float* s, float* c) {
   *c = cosf_approx(r);
 }
 
+// 2^f for |f| <= 0.5 + 2^-20: Taylor series of exp(f ln 2) to degree 7
+// (truncation < 6e-9 relative), Horner in FP32.
+__device__ __forceinline__ float exp2_frac(float f) {
+  float p = 1.5252733804059840e-05f;
+  p = fmaf(p, f, 1.5403530393381609e-04f);
+  p = fmaf(p, f, 1.3333558146428443e-03f);
+  p = fmaf(p, f, 9.6181291076284772e-03f);
+  p = fmaf(p, f, 5.5504108664821580e-02f);
+  p = fmaf(p, f, 2.4022650695910071e-01f);
+  p = fmaf(p, f, 6.9314718055994531e-01f);
+  return fmaf(p, f, 1.0f);
+}
+
+// exp(-x) for x = xh + xl (a float pair, 0 <= x <= 87): m = -x log2(e) in
+// two parts (the product's rounding error recovered by an FMA), 2^m =
+// 2^rint(m) * 2^frac.  Relative error a few 1e-8, independent of x's size.
+__device__ __forceinline__ float exp_neg_pair(float xh, float xl) {
+  constexpr float L_HI = 1.44269502162933349609375f;        // float(log2 e)
+  constexpr float L_LO = 1.92596298909109e-08f;             // log2 e - L_HI
+  const float mh = -xh * L_HI;
+  float ml = fmaf(-xh, L_HI, -mh);
+  ml = fmaf(-xh, L_LO, ml);
+  ml = fmaf(-xl, L_HI, ml);
+  const float nf = rintf(mh);
+  const float f = (mh - nf) + ml;
+  return exp2_frac(f) * __int_as_float(((int)nf + 127) << 23);
+}
+
 }  // namespace jcg

@@ -30,30 +30,6 @@ __device__ __forceinline__ D1 interp_d1(double x, const double* xp, const double
   return a * x + b;
 }
 
-// One RK4 step of the growth ODE (background.py:96-111) from (y0, y1) = (D, dD/da):
-// dy0/da = y1, dy1/da = -q y1 + r y0, coefficients at the step's start (qa0,
-// ra0), midpoint (qm, rm) and end (qa1, ra1).
-template <class T>
-__device__ __forceinline__ void growth_rk4_step(const T& y0, const T& y1, const T& qa0, const T& ra0, const T& qm,
-                                                const T& rm, const T& qa1, const T& ra1, double hh, T& o0, T& o1) {
-  const T k1a = y1, k1b = -qa0 * y1 + ra0 * y0;
-  const T y0b = y0 + hh * k1a / 2, y1b = y1 + hh * k1b / 2;
-  const T k2a = y1b, k2b = -qm * y1b + rm * y0b;
-  const T y0c = y0 + hh * k2a / 2, y1c = y1 + hh * k2b / 2;
-  const T k3a = y1c, k3b = -qm * y1c + rm * y0c;
-  const T y0d = y0 + hh * k3a, y1d = y1 + hh * k3b;
-  const T k4a = y1d, k4b = -qa1 * y1d + ra1 * y0d;
-  o0 = y0 + 1.0 / 6.0 * hh * (k1a + 2 * k2a + 2 * k3a + k4a);
-  o1 = y1 + 1.0 / 6.0 * hh * (k1b + 2 * k2b + 2 * k3b + k4b);
-}
-
-// 2 x 2 row-major products: r = a b, and a vector v <- a v
-__device__ __forceinline__ void mat2_mul(const double* a, const double* b, double* r) {
-  const double r0 = a[0] * b[0] + a[1] * b[2], r1 = a[0] * b[1] + a[1] * b[3];
-  const double r2 = a[2] * b[0] + a[3] * b[2], r3 = a[2] * b[1] + a[3] * b[3];
-  r[0] = r0, r[1] = r1, r[2] = r2, r[3] = r3;
-}
-
 // Tables of one cosmology with tangents.  Lanes: dir = tid & 7, item = tid >> 3.
 // F32T (fp32c Jacobian): the per-node evaluations (ODE right-hand sides,
 // Eisenstein-Hu at the Romberg and halofit k nodes) run one node per thread in
@@ -225,63 +201,14 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     }
     __syncthreads();
     if (warp == 0) {
-      // y_i = M_i ... M_1 y_0: lane l holds steps 4l .. 4l + 3 (M_0 = I)
-      double A[4];
-      A[0] = Mv[lane * 16 + 0], A[1] = Mv[lane * 16 + 1], A[2] = Mv[lane * 16 + 2], A[3] = Mv[lane * 16 + 3];
-      for (int k = 1; k < 4; ++k) mat2_mul(Mv + (lane * 4 + k) * 4, A, A);
-      for (int o = 1; o < 32; o <<= 1) {
-        double P[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) P[q] = __shfl_up_sync(0xffffffffu, A[q], o);
-        if (lane >= o) mat2_mul(A, P, A);
-      }
-      double E[4];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) E[q] = __shfl_up_sync(0xffffffffu, A[q], 1);
-      if (lane == 0) E[0] = 1.0, E[1] = 0.0, E[2] = 0.0, E[3] = 1.0;
-      const double ya = c->atab_grow[0], yb = 1.0;
-      double u0 = E[0] * ya + E[1] * yb, u1 = E[2] * ya + E[3] * yb;
       double ys[4];
-      for (int k = 0; k < 4; ++k) {
-        const double* M = Mv + (lane * 4 + k) * 4;
-        const double v0 = M[0] * u0 + M[1] * u1, v1 = M[2] * u0 + M[3] * u1;
-        u0 = v0, u1 = v1;
-        ys[k] = u0;
-        Yv[(lane * 4 + k) * 2 + 0] = u0;
-        Yv[(lane * 4 + k) * 2 + 1] = u1;
-      }
-      const double yf = __shfl_sync(0xffffffffu, u0, 31);
+      const double yf = growth_scan_warp(Mv, c->atab_grow[0], 1.0, lane, ys, Yv);
       for (int k = 0; k < 4; ++k) out->gv[lane * 4 + k] = ys[k] / yf;
     } else {
-      // chi: prefix sums of the RK4 increments (scipy/ode.py:21, first step
-      // h = 0) for the value and the 8 tangents, chi = Y[-1] - Y; lane l
-      // holds nodes 8l .. 8l + 7
-      for (int comp = warp - 1; comp < NDIR + 1; comp += 3) {
-        const double* f0 = fn + comp * NCHI;
-        const double* f1 = fm + comp * NCHI;
-        double loc[8], s = 0.0;
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-          const int i = lane * 8 + k;
-          if (i > 0) {
-            const double hh = c->lna_chi[i] - c->lna_chi[i - 1];
-            s += 1.0 / 6.0 * hh * (f0[i - 1] + 2 * f1[i] + 2 * f1[i] + f0[i]);
-          }
-          loc[k] = s;
-        }
-        double x = s;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const double u = __shfl_up_sync(0xffffffffu, x, o);
-          if (lane >= o) x += u;
-        }
-        double off = __shfl_up_sync(0xffffffffu, x, 1);
-        if (lane == 0) off = 0.0;
-        const double tot = __shfl_sync(0xffffffffu, x, 31);
-        double* dst = comp == 0 ? out->chiv : out->chid[comp - 1];
-#pragma unroll
-        for (int k = 0; k < 8; ++k) dst[lane * 8 + k] = tot - (off + loc[k]);
-      }
+      // chi for the value and the 8 tangents
+      for (int comp = warp - 1; comp < NDIR + 1; comp += 3)
+        chi_scan_warp(fn + comp * NCHI, fm + comp * NCHI, c->lna_chi, lane,
+                      comp == 0 ? out->chiv : out->chid[comp - 1]);
       // sigmasqr(8) (power.py:70-78): romb is linear in the integrand values,
       // sum_e w_e f_e with the weights of the Richardson combination
       for (int comp = warp - 1; comp < NDIR + 1; comp += 3) {

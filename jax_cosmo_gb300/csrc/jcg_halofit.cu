@@ -7,6 +7,7 @@
 // lane of a warp would hold the float64 pipe for all 32 lanes; GB300's FP64
 // rate is ~1/70 of its FP32 rate, so the per-node scalar work runs
 // thread-parallel instead.)
+#include "jcg_fp32.cuh"
 #include "jcg_internal.cuh"
 
 namespace jcg {
@@ -173,17 +174,14 @@ __device__ __forceinline__ float lg2a(float x) {
   return y;
 }
 
-// fp32c: the takahashi2012 coefficients (power.py:199-238) in float32 from the
-// float64 n_eff, C and background; the Limber integrand consumes them as
-// float32, so only Omega_m(a), Omega_de(a) (background) stay float64.  Fills
-// the float row and the coefficient fields of the float64 row.
-__device__ void halofit_coefs_fast(const Bg& bg, const double* s, double a, double lna,
+// fp32c: the takahashi2012 coefficients (power.py:199-238) in float32 from
+// n_eff, C and the float32 background Omega_m(a), Omega_de(a), w(a); the
+// Limber integrand consumes them as float32.  Fills the float row and the
+// coefficient fields of the float64 row.
+__device__ void halofit_coefs_fast(const double* s, float om_m, float om_de, float wv,
                                    const HfParams& hp, double chiv, double g, double* row,
                                    float* f) {
-  double om_m, om_de;
-  bg_om_l(bg, a, lna, &om_m, &om_de);
-  const double wv = bg_w(bg, a);
-  const float n = (float)hp.neff, C = (float)hp.C, omde = (float)om_de, w = (float)wv;
+  const float n = (float)hp.neff, C = (float)hp.C, omde = om_de, w = wv;
   const float n2 = n * n, n3 = n2 * n, n4 = n2 * n2;
   constexpr float LOG2_10 = 3.321928094887362f;
   const float e_an = 1.5222f + 2.8553f * n + 2.3706f * n2 + 0.9903f * n3 + 0.2250f * n4 -
@@ -195,7 +193,7 @@ __device__ void halofit_coefs_fast(const Bg& bg, const double* s, double a, doub
   const float alpha = fabsf(6.0835f + 1.3373f * n - 0.1959f * n2 - 5.5274f * C);
   const float beta = 2.0379f - 0.7354f * n + 0.3157f * n2 + 1.2490f * n3 + 0.3980f * n4 - 0.1682f * C;
   const float nun = ex2a(LOG2_10 * (5.2105f + 3.6902f * n));
-  const float l2om = lg2a((float)om_m);
+  const float l2om = lg2a(om_m);
   const float f1 = ex2a(-0.0307f * l2om), f2 = ex2a(-0.0585f * l2om), f3 = ex2a(0.0743f * l2om);
   const float knl = (float)hp.knl;
   const float chic = fmaxf((float)chiv, 1.f);
@@ -320,15 +318,23 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   if (n0 >= na) return;
   constexpr int NB = HF_NODES_PER_BLOCK;
   __shared__ double sig[NRT];
-  __shared__ double pk3[NKH];
+  __shared__ double pk3[FAST ? 1 : NKH];
   __shared__ double s[NSCAL];
   __shared__ double knl_s[NB], inv_s[NB], g_s[NB], chi_s[NB], t1_s[NB], t2_s[NB], s1_s[NB], s2_s[NB];
   __shared__ int ilo_s[NB], ihi_s[NB];
-  __shared__ double e2tab[64];
+  __shared__ float iv2h_s[NB], iv2l_s[NB];
+  __shared__ float wpf[FAST ? NKH : 1], k2h[FAST ? NKH : 1], k2l[FAST ? NKH : 1];
   const CosmoTab* ct = it.ctab;
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) e2tab[i] = kExp2Tab64[i];
   for (int i = threadIdx.x; i < NRT; i += blockDim.x) sig[i] = ct->sig[i];
-  for (int i = threadIdx.x; i < NKH; i += blockDim.x) pk3[i] = ct->pk3[i];
+  if (FAST) {
+    for (int i = threadIdx.x; i < NKH; i += blockDim.x) {
+      wpf[i] = ct->wpk3f[i];
+      k2h[i] = c->kh2_hi[i];
+      k2l[i] = c->kh2_lo[i];
+    }
+  } else {
+    for (int i = threadIdx.x; i < NKH; i += blockDim.x) pk3[i] = ct->pk3[i];
+  }
   for (int i = threadIdx.x; i < NSCAL; i += blockDim.x) s[i] = ct->s[i];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -352,12 +358,19 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
     int ilo = 0, ihi = NKH - 1;
     double t1 = 0.0, t2 = 0.0;
     if (FAST) {
-      // exp only for y^2 in [Y2_TAYLOR, Y2_SKIP]
-      const double linv = log(inv);
-      ilo = (int)floor((0.5 * log(Y2_TAYLOR) - linv - LOG_KMIN) / DLOGK);
-      ihi = (int)ceil((0.5 * log(Y2_SKIP) - linv - LOG_KMIN) / DLOGK);
+      // exp only for y^2 in [Y2_TAYLOR, Y2_SKIP] (the split point only needs
+      // to be consistent, so it is found in FP32); y^2 = kh^2 inv^2 with
+      // inv^2 as a float pair for the FP32 terms
+      const float linv = LN2_F * lg2f((float)inv);
+      constexpr float HLY2T = 0.0f, HLY2S = 2.0471425f;  // 0.5 log(Y2_TAYLOR), 0.5 log(Y2_SKIP)
+      ilo = (int)floorf((HLY2T - linv - (float)LOG_KMIN) * (float)(1.0 / DLOGK));
+      ihi = (int)ceilf((HLY2S - linv - (float)LOG_KMIN) * (float)(1.0 / DLOGK));
       ilo = max(0, min(ilo, NKH));
       ihi = max(ilo - 1, min(ihi, NKH - 1));
+      const double iv2d = inv * inv;
+      const float ih = (float)iv2d;
+      iv2h_s[t] = ih;
+      iv2l_s[t] = (float)(iv2d - (double)ih);
       // sum_{i < ilo} w pk3 y^2 e^{-y^2} = sum_m (-1)^m / m! inv^(2m+2) P_m[ilo]
       if (ilo > 0) {
         const double iv2 = inv * inv;
@@ -384,13 +397,28 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
     const double inv = inv_s[t];
     double s1 = 0.0, s2 = 0.0;
     if (FAST) {
+      // FP32 terms: y^2 = kh^2 inv^2 as a float pair (hi p, lo e), exp(-y^2)
+      // from the pair, weights w pk3 rounded once to float
+      const float ih = iv2h_s[t], il = iv2l_s[t];
+      float f1 = 0.f, f2 = 0.f;
       for (int i = ilo_s[t] + lane; i <= ihi_s[t]; i += 32) {
-        const double y = c->kh[i] * inv;
-        const double y2 = y * y;
-        const double r = c->simpson_kh[i] * pk3[i] * exp_tang(-y2, e2tab);
-        s1 += 2 * r * y2;
-        s2 += 4 * r * (y2 - y2 * y2);
+        const float kh = k2h[i];
+        const float p = kh * ih;
+        float e = fmaf(kh, ih, -p);
+        e = fmaf(kh, il, e);
+        e = fmaf(k2l[i], ih, e);
+        const float r = wpf[i] * exp_neg_pair(p, e);
+        const float y2 = p + e;
+        f1 = fmaf(2.f * r, y2, f1);
+        f2 = fmaf(4.f * r, y2 * ((1.f - p) - e), f2);
       }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        f1 += __shfl_xor_sync(0xffffffffu, f1, o);
+        f2 += __shfl_xor_sync(0xffffffffu, f2, o);
+      }
+      s1 = (double)f1;
+      s2 = (double)f2;
     } else {
       const double g2 = g_s[t] * g_s[t];
       for (int i = lane; i < NKH; i += 32) {
@@ -401,8 +429,10 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
         s2 += c->simpson_kh[i] * (4 * res * (y2 - y2 * y2));
       }
     }
-    s1 = warp_sum(s1);
-    s2 = warp_sum(s2);
+    if (!FAST) {
+      s1 = warp_sum(s1);
+      s2 = warp_sum(s2);
+    }
     if (lane == 0) {
       s1_s[t] = s1;
       s2_s[t] = s2;
@@ -414,7 +444,6 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
     const int n = n0 + t;
     const double a = A[n];
-    const double lna = log(a);
     double s1 = s1_s[t], s2 = s2_s[t];
     if (FAST) {
       const double g2 = g_s[t] * g_s[t];
@@ -432,14 +461,29 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
     row[R_G] = g_s[t];
     float f[NROW32];
     if (FAST) {
-      halofit_coefs_fast(bg, s, a, lna, hp, chiv, g_s[t], row, f);
+      // background in FP32 (background.py:122-126, 168, 196, 270-294):
+      // E^2(a), Omega_m(a), Omega_de(a), w(a), dchi/da
+      const float af = (float)a, ia = rcpf(af), ia2 = ia * ia;
+      const float w0 = (float)s[S_W0], wa = (float)s[S_WA];
+      const float fde = -3.f * (1.f + w0 + wa) * (LN2_F * lg2f(af)) + 3.f * wa * (af - 1.f);
+      const float ef = fde == 0.f ? 1.f : ex2f(fde * LOG2E_F);
+      const float om3 = (float)s[S_OMEGA_M] * (ia2 * ia), ode = (float)s[S_OMEGA_DE] * ef;
+      const float e2 = om3 + (float)s[S_OMEGA_K] * ia2 + ode;
+      const float ie2 = rcpf(e2);
+      const float omm = om3 * ie2, omde = ode * ie2, wv = w0 + (1.f - af) * wa;
+      halofit_coefs_fast(s, omm, omde, wv, hp, chiv, g_s[t], row, f);
+      const float dchi = (float)RH * ia2 * rsqrtf(e2);
+      const float chic = fmaxf((float)chiv, 1.f);
+      row[R_DCHI] = dchi;
+      row[R_U] = (double)((float)WS[n] * dchi * rcpf(chic * chic) * (float)(1.0 / C2));
     } else {
+      const double lna = log(a);
       halofit_coefs(bg, a, lna, hp, row);
       row[R_LGCHIC] = log(fmax(chiv, 1.0));
+      const double dchi = bg_dchioverda_l(bg, a, lna);
+      row[R_DCHI] = dchi;
+      row[R_U] = WS[n] * dchi / fmax(chiv * chiv, 1.0) / C2;
     }
-    const double dchi = bg_dchioverda_l(bg, a, lna);
-    row[R_DCHI] = dchi;
-    row[R_U] = WS[n] * dchi / fmax(chiv * chiv, 1.0) / C2;
     if (it.rows64) {
       double* dst = it.rows64 + (size_t)n * NROW64;
       for (int i = 0; i < NROW64; ++i) dst[i] = row[i];

@@ -58,6 +58,8 @@ struct ConstTables {
   double E[NKH * NRT];     // exp(-(k_i r_j)^2), i-major: power.py:99-109
   double kpw[NTAYLOR][NKH];  // simpson_kh[i] * kh[i]^(2(m+1)): the Taylor prefix sums' weights
   double romb_w[NROMB];      // romb's Richardson combination as weights on romb_logk's values
+  float kh2_hi[NKH];         // kh[i]^2 as a float pair hi + lo (fp32c halofit moments)
+  float kh2_lo[NKH];
 };
 
 // ------------------------------------------------- per-cosmology tables -----
@@ -93,6 +95,7 @@ struct CosmoTab {
   double chi_slope[NCHI];  // slope of the chi table on segment [k, k+1] (k < 255)
   float chi32[NCHI];       // chi table, float (FP32 lensing kernel)
   float slope32[NCHI];     // chi_slope, float
+  float wpk3f[NKH + 15];   // simpson_kh[i] * pk3[i], float (fp32c halofit moments); padded to 64 bytes
   // prefix sums over the ln k grid of w_i P(k_i) k_i^3 k_i^(2(m+1)), m < NTAYLOR:
   // the small-y part of the halofit moments as a Taylor series in y^2
   double ptay[NTAYLOR][NKH + 1];
@@ -382,6 +385,97 @@ __device__ __forceinline__ double bg_esqr_l(const Bg& c, double a, double lna, d
 }
 __device__ __forceinline__ double bg_esqr(const Bg& c, double a) { return bg_esqr_l(c, a, log(a), nullptr); }
 __device__ __forceinline__ double bg_H(const Bg& c, double a) { return H0 * sqrt(bg_esqr(c, a)); }
+
+// ---------------------------------------------------- background scans ----
+// One RK4 step of the growth ODE (background.py:96-111) from (y0, y1) = (D, dD/da):
+// dy0/da = y1, dy1/da = -q y1 + r y0, coefficients at the step's start (qa0,
+// ra0), midpoint (qm, rm) and end (qa1, ra1).
+template <class T>
+__device__ __forceinline__ void growth_rk4_step(const T& y0, const T& y1, const T& qa0, const T& ra0, const T& qm,
+                                                const T& rm, const T& qa1, const T& ra1, double hh, T& o0, T& o1) {
+  const T k1a = y1, k1b = -qa0 * y1 + ra0 * y0;
+  const T y0b = y0 + hh * k1a / 2, y1b = y1 + hh * k1b / 2;
+  const T k2a = y1b, k2b = -qm * y1b + rm * y0b;
+  const T y0c = y0 + hh * k2a / 2, y1c = y1 + hh * k2b / 2;
+  const T k3a = y1c, k3b = -qm * y1c + rm * y0c;
+  const T y0d = y0 + hh * k3a, y1d = y1 + hh * k3b;
+  const T k4a = y1d, k4b = -qa1 * y1d + ra1 * y0d;
+  o0 = y0 + 1.0 / 6.0 * hh * (k1a + 2 * k2a + 2 * k3a + k4a);
+  o1 = y1 + 1.0 / 6.0 * hh * (k1b + 2 * k2b + 2 * k3b + k4b);
+}
+
+// 2 x 2 row-major products: r = a b, and a vector v <- a v
+__device__ __forceinline__ void mat2_mul(const double* a, const double* b, double* r) {
+  const double r0 = a[0] * b[0] + a[1] * b[2], r1 = a[0] * b[1] + a[1] * b[3];
+  const double r2 = a[2] * b[0] + a[3] * b[2], r3 = a[2] * b[1] + a[3] * b[3];
+  r[0] = r0, r[1] = r1, r[2] = r2, r[3] = r3;
+}
+
+// Growth ODE values from the per-step matrices Mv[i] (2 x 2 row-major,
+// Mv[0] = I; y_i = M_i y_{i-1}) for one warp: y_i = M_i ... M_1 y_0 by a
+// warp scan of matrix products, lane l holding steps 4l .. 4l + 3.  Returns
+// D at the lane's 4 nodes in d4 and writes y_i to Yv[i][2] if Yv is set; the
+// result is D at the last node.
+__device__ __forceinline__ double growth_scan_warp(const double* Mv, double ya, double yb, int lane, double* d4,
+                                                   double* Yv) {
+  double A[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) A[q] = Mv[lane * 16 + q];
+  for (int k = 1; k < 4; ++k) mat2_mul(Mv + (lane * 4 + k) * 4, A, A);
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    double P[4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q) P[q] = __shfl_up_sync(0xffffffffu, A[q], o);
+    if (lane >= o) mat2_mul(A, P, A);
+  }
+  double E[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) E[q] = __shfl_up_sync(0xffffffffu, A[q], 1);
+  if (lane == 0) E[0] = 1.0, E[1] = 0.0, E[2] = 0.0, E[3] = 1.0;
+  double u0 = E[0] * ya + E[1] * yb, u1 = E[2] * ya + E[3] * yb;
+  for (int k = 0; k < 4; ++k) {
+    const double* M = Mv + (lane * 4 + k) * 4;
+    const double v0 = M[0] * u0 + M[1] * u1, v1 = M[2] * u0 + M[3] * u1;
+    u0 = v0, u1 = v1;
+    d4[k] = u0;
+    if (Yv) {
+      Yv[(lane * 4 + k) * 2 + 0] = u0;
+      Yv[(lane * 4 + k) * 2 + 1] = u1;
+    }
+  }
+  return __shfl_sync(0xffffffffu, u0, 31);
+}
+
+// chi table (background.py:227-233) for one warp: prefix sums of the RK4
+// increments h/6 (f_{i-1} + 2 fm_i + 2 fm_i + f_i) in ln a (scipy/ode.py:21,
+// the first step has h = 0), then chi_i = Y[-1] - Y_i.  fnode: f at the
+// nodes; fmid[i]: f at the midpoint of step i (i >= 1).  Lane l holds nodes
+// 8l .. 8l + 7; the sums are associated per lane, then across lanes.
+__device__ __forceinline__ void chi_scan_warp(const double* fnode, const double* fmid, const double* lna, int lane,
+                                              double* out) {
+  double loc[8], s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int i = lane * 8 + k;
+    if (i > 0) {
+      const double hh = lna[i] - lna[i - 1];
+      s += 1.0 / 6.0 * hh * (fnode[i - 1] + 2 * fmid[i] + 2 * fmid[i] + fnode[i]);
+    }
+    loc[k] = s;
+  }
+  double x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const double u = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += u;
+  }
+  double off = __shfl_up_sync(0xffffffffu, x, 1);
+  if (lane == 0) off = 0.0;
+  const double tot = __shfl_sync(0xffffffffu, x, 31);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) out[lane * 8 + k] = tot - (off + loc[k]);
+}
 
 // ------------------------------------------------------ bias models -------
 constexpr double IA_C1_RHOCRIT = 5e-14 * 2.7750e11;  // C_1 rho_crit (constants.py), NLA normalisation

@@ -39,6 +39,8 @@ __global__ void const_init_kernel(ConstTables* c) {
     const double sw = dxk / 3 * w;
     c->simpson_kh[i] = sw;
     const double k2 = k * k;
+    c->kh2_hi[i] = (float)k2;
+    c->kh2_lo[i] = (float)(k2 - (double)(float)k2);
     double kp = k2;
     for (int m = 0; m < NTAYLOR; ++m) {
       c->kpw[m][i] = sw * kp;
@@ -347,6 +349,7 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   __shared__ double pk3[NKH];
   __shared__ double chis[NCHI];
   __shared__ double gs[NGROW];
+  __shared__ double mv[4 * NGROW];  // per-step growth matrices
   const int t = threadIdx.x;
   if (t == 0) cosmo_scalars(it.params, s);
   __syncthreads();
@@ -383,64 +386,43 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
     fr[t] = k * (kw * kw) * pk;
   }
   __syncthreads();
-  if (t == 0) {
-    // chi: RK4 increments summed sequentially in the reference's order, then
-    // chi[-1] - chi.  The first step has h = 0 (scipy/ode.py:21).
-    double y = 0.0;
-    inc[0] = 0.0;
-    for (int i = 1; i < NCHI; ++i) {
-      const double hh = c->lna_chi[i] - c->lna_chi[i - 1];
-      const double fm = inc[i];
-      y = y + 1.0 / 6.0 * hh * (fnode[i - 1] + 2 * fm + 2 * fm + fnode[i]);
-      inc[i] = y;
-    }
-    for (int i = 0; i < NCHI; ++i) chis[i] = inc[NCHI - 1] - inc[i];
-  } else if (t == 32) {
-    // growth: RK4 in a, y0 = [a_min, 1]  (background.py:108-111)
-    double y0 = c->atab_grow[0], y1 = 1.0;
-    gs[0] = y0;
-    for (int i = 1; i < NGROW; ++i) {
+  // growth: one RK4 step is linear in y = (D, dD/da), y_i = M_i y_{i-1};
+  // threads 128 + i form M_i (the step on the unit vectors), warp 1 scans
+  if (t >= 128 && t < 128 + NGROW) {
+    const int i = t - 128;
+    double* M = mv + 4 * i;
+    if (i == 0) {
+      M[0] = 1.0, M[1] = 0.0, M[2] = 0.0, M[3] = 1.0;
+    } else {
       const double hh = c->atab_grow[i] - c->atab_grow[i - 1];
-      // k = f(y, x) = [y1, -q y1 + r y0]
-      const double k1a = y1, k1b = -qa[i - 1] * y1 + ra[i - 1] * y0;
-      const double y0b = y0 + hh * k1a / 2, y1b = y1 + hh * k1b / 2;
-      const double k2a = y1b, k2b = -qm[i] * y1b + rm[i] * y0b;
-      const double y0c = y0 + hh * k2a / 2, y1c = y1 + hh * k2b / 2;
-      const double k3a = y1c, k3b = -qm[i] * y1c + rm[i] * y0c;
-      const double y0d = y0 + hh * k3a, y1d = y1 + hh * k3b;
-      const double k4a = y1d, k4b = -qa[i] * y1d + ra[i] * y0d;
-      y0 = y0 + 1.0 / 6.0 * hh * (k1a + 2 * k2a + 2 * k3a + k4a);
-      y1 = y1 + 1.0 / 6.0 * hh * (k1b + 2 * k2b + 2 * k3b + k4b);
-      gs[i] = y0;
+      double o0, o1;
+      growth_rk4_step(1.0, 0.0, qa[i - 1], ra[i - 1], qm[i], rm[i], qa[i], ra[i], hh, o0, o1);
+      M[0] = o0, M[2] = o1;
+      growth_rk4_step(0.0, 1.0, qa[i - 1], ra[i - 1], qm[i], rm[i], qa[i], ra[i], hh, o0, o1);
+      M[1] = o0, M[3] = o1;
     }
-    for (int i = 0; i < NGROW; ++i) gs[i] = gs[i] / y0;
-  } else if (t == 64) {
-    // romb combination (scipy/integrate.py:131-159), divmax = 7
-    const double a = -4.0, b = 3.0, intrange = b - a;
-    double ordsum = 0.5 * (fr[0] + fr[1]);
-    double state[8];
-    for (int i = 0; i < 8; ++i) state[i] = intrange * ordsum;
-    int pos = 2;
-    for (int lev = 1; lev <= 7; ++lev) {
-      const int n = 1 << lev;
-      const int numtosum = n / 2;
-      double sum = 0.0;
-      for (int m = 0; m < numtosum; ++m) sum += fr[pos + m];
-      pos += numtosum;
-      ordsum = ordsum + sum;
-      double x = intrange * ordsum / n;
-      double ns[8];
-      ns[0] = x;
-      for (int kk = 0; kk < 7; ++kk) {
-        const double tmp = ldexp(1.0, 2 * (kk + 1));  // 4.0 ** (kk + 1), exact
-        x = (tmp * x - state[kk]) / (tmp - 1.0);
-        ns[kk + 1] = x;
-      }
-      for (int i = 0; i < 8; ++i) state[i] = ns[i];
+  }
+  const int warp = t >> 5, lane = t & 31;
+  if (warp == 0) {
+    chi_scan_warp(fnode, inc, c->lna_chi, lane, chis);
+  } else if (warp == 2) {
+    // sigmasqr(8) (power.py:70-78): romb is linear in the integrand values,
+    // sum_e w_e f_e with the weights of its Richardson combination
+    double acc = 0.0;
+    for (int e = lane; e < NROMB; e += 32) acc = fma(c->romb_w[e], fr[e], acc);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0) {
+      const double sig8 = 1.0 / (2.0 * (PI * PI)) * acc;
+      s[S_SIGMASQR8] = sig8;
+      s[S_PKNORM] = (s[S_SIGMA8] * s[S_SIGMA8]) / sig8;
     }
-    const double sig8 = 1.0 / (2.0 * (PI * PI)) * state[7];
-    s[S_SIGMASQR8] = sig8;
-    s[S_PKNORM] = (s[S_SIGMA8] * s[S_SIGMA8]) / sig8;
+  }
+  __syncthreads();
+  if (warp == 1) {
+    double d4[4];
+    const double yf = growth_scan_warp(mv, c->atab_grow[0], 1.0, lane, d4, nullptr);
+    for (int k = 0; k < 4; ++k) gs[lane * 4 + k] = d4[k] / yf;
   }
   __syncthreads();
   if (t == 0) {
@@ -475,6 +457,7 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
     out->chi32[i] = (float)chis[i];
     out->slope32[i] = (float)sl;
   }
+  for (int i = t; i < NKH + 15; i += blockDim.x) out->wpk3f[i] = i < NKH ? (float)(c->simpson_kh[i] * pk3[i]) : 0.f;
   // Taylor prefix sums of the halofit moments (fp32c rows only):
   // P_m[i] = sum_{i' < i} w pk3 k^(2m+2), one warp per m with a warp-wide
   // inclusive scan over chunks of 32 nodes.

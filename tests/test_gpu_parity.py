@@ -317,8 +317,10 @@ def test_sparse_known_answers():
 
 def test_fast_moments_match_full_moments():
     """fp32c mode evaluates the halofit moments with exp only where it matters
-    (Taylor prefix sums below y^2 = 1e-3, terms under 1e-20 dropped above
-    y^2 = 60); k_nl, n_eff and C must equal the full float64 sum to ~1e-12."""
+    (Taylor prefix sums below y^2 = 1, terms under 1e-20 dropped above
+    y^2 = 60), the exp terms in float32 from a float pair y^2.  k_nl comes
+    from the float64 sigma^2 table and root find: equal to ~1e-12; n_eff and C
+    carry the float32 terms' rounding (a few 1e-7 relative)."""
     import ctypes
 
     from jax_cosmo_gb300 import _geometry, _lib
@@ -346,9 +348,9 @@ def test_fast_moments_match_full_moments():
                       _lib.ptr(r[i]), ctypes.c_size_t(na * 24), st)
         out[prec] = r
     full, fast = out[_lib.FP64], out[_lib.FP32C]
-    for col in (2, 3, 4):  # k_nl, n_eff, C
+    for col, tol in ((2, 1e-12), (3, 2e-6), (4, 2e-5)):  # k_nl, n_eff, C
         err = ((fast[..., col] - full[..., col]).abs() / full[..., col].abs()).max().item()
-        assert err < 1e-12, (col, err)
+        assert err < tol, (col, err)
 
 
 def _nz_probes(g):
