@@ -81,4 +81,37 @@ __device__ __forceinline__ float exp_neg_pair(float xh, float xl) {
   return exp2_frac(f) * __int_as_float(((int)nf + 127) << 23);
 }
 
+// ------------------------------------------------------------ float pairs --
+// A value as hi + lo floats (about 48 significant bits), with the error-free
+// transforms of Knuth (two-sum) and Dekker (product by FMA).
+struct FF {
+  float hi, lo;
+};
+__device__ __forceinline__ FF ff_fast_two_sum(float a, float b) {  // |a| >= |b|
+  FF r;
+  r.hi = a + b;
+  r.lo = b - (r.hi - a);
+  return r;
+}
+__device__ __forceinline__ FF ff_add(FF x, FF y) {
+  const float s = x.hi + y.hi;
+  const float bb = s - x.hi;
+  const float e = (x.hi - (s - bb)) + (y.hi - bb);
+  return ff_fast_two_sum(s, e + (x.lo + y.lo));
+}
+__device__ __forceinline__ FF ff_mul(FF x, FF y) {
+  const float p = x.hi * y.hi;
+  float e = fmaf(x.hi, y.hi, -p);
+  e = fmaf(x.hi, y.lo, e);
+  e = fmaf(x.lo, y.hi, e);
+  return ff_fast_two_sum(p, e);
+}
+__device__ __forceinline__ FF ff_of(double v) {
+  FF r;
+  r.hi = (float)v;
+  r.lo = (float)(v - (double)r.hi);
+  return r;
+}
+__device__ __forceinline__ double ff_to_double(FF x) { return (double)x.hi + (double)x.lo; }
+
 }  // namespace jcg

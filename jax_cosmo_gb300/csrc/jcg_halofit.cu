@@ -57,13 +57,10 @@ __device__ __forceinline__ int root_argmin_warp(const double* sig, double g2, in
   return best;
 }
 
-// power.py:96-139 at one scale factor with growth g, for the warp.
-// FAST: the moments evaluate exp only for y^2 in [1e-3, 60]; below, the
-// Taylor prefix sums of the cosmology table; above, terms under 1e-20 of the
-// sum are dropped.  Otherwise all 257 nodes with exp, as the reference.
-template <bool FAST>
-__device__ HfParams halofit_params_warp(const double* sig, const double* pk3, const double* ptay,
-                                        double g, const ConstTables* __restrict__ c, int lane) {
+// power.py:96-139 at one scale factor with growth g, for the warp: the root
+// find and the moments over all 257 nodes with exp, as the reference.
+__device__ HfParams halofit_params_warp(const double* sig, const double* pk3, double g,
+                                        const ConstTables* __restrict__ c, int lane) {
   const double g2 = g * g;
   const int best = root_argmin_warp(sig, g2, lane);
   const int ind = best < 1 ? 1 : (best > NRT - 2 ? NRT - 2 : best);
@@ -81,51 +78,15 @@ __device__ HfParams halofit_params_warp(const double* sig, const double* pk3, co
   hp.knl = 1.0 / R;  // power.py:118
   const double inv = 1.0 / hp.knl;  // y = k * (1 / k_nl)
   double s1 = 0.0, s2 = 0.0;
-  if (!FAST) {
-    for (int i = lane; i < NKH; i += 32) {
-      const double y = c->kh[i] * inv;
-      const double y2 = y * y;
-      const double res = pk3[i] * exp(-y2) * g2 / TWO_PI2;
-      s1 += c->simpson_kh[i] * (2 * res * y2);
-      s2 += c->simpson_kh[i] * (4 * res * (y2 - y2 * y2));
-    }
-    s1 = warp_sum(s1);
-    s2 = warp_sum(s2);
-  } else {
-    // index range with y_i^2 in [Y2_TAYLOR, Y2_SKIP]
-    const double linv = log(inv);
-    int ilo = (int)floor((0.5 * log(Y2_TAYLOR) - linv - LOG_KMIN) / DLOGK);
-    int ihi = (int)ceil((0.5 * log(Y2_SKIP) - linv - LOG_KMIN) / DLOGK);
-    ilo = max(0, min(ilo, NKH));
-    ihi = max(ilo - 1, min(ihi, NKH - 1));
-    for (int i = ilo + lane; i <= ihi; i += 32) {
-      const double y = c->kh[i] * inv;
-      const double y2 = y * y;
-      const double r = c->simpson_kh[i] * pk3[i] * exp(-y2);
-      s1 += 2 * r * y2;
-      s2 += 4 * r * (y2 - y2 * y2);
-    }
-    s1 = warp_sum(s1);
-    s2 = warp_sum(s2);
-    // sum_{i < ilo} w pk3 y^2 exp(-y^2) = sum_m (-1)^m / m! inv^(2m+2) P_m[ilo]
-    double t1 = 0.0, t2 = 0.0;
-    if (ilo > 0) {
-      const double iv2 = inv * inv;
-      double pw = iv2;  // inv^(2m+2)
-      double fact = 1.0;
-      for (int m = 0; m < NTAYLOR - 1; ++m) {
-        const double sg = (m & 1) ? -1.0 : 1.0;
-        const double a = ptay[m * (NKH + 1) + ilo] * pw;
-        const double a2 = ptay[(m + 1) * (NKH + 1) + ilo] * pw * iv2;
-        t1 += sg / fact * a;
-        t2 += sg / fact * (a - a2);
-        pw *= iv2;
-        fact *= (double)(m + 1);
-      }
-    }
-    s1 = (s1 + 2.0 * t1) * g2 / TWO_PI2;
-    s2 = (s2 + 4.0 * t2) * g2 / TWO_PI2;
+  for (int i = lane; i < NKH; i += 32) {
+    const double y = c->kh[i] * inv;
+    const double y2 = y * y;
+    const double res = pk3[i] * exp(-y2) * g2 / TWO_PI2;
+    s1 += c->simpson_kh[i] * (2 * res * y2);
+    s2 += c->simpson_kh[i] * (4 * res * (y2 - y2 * y2));
   }
+  s1 = warp_sum(s1);
+  s2 = warp_sum(s2);
   hp.neff = s1 - 3.0;
   hp.C = s1 * s1 + s2;
   return hp;
@@ -322,13 +283,13 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   __shared__ double s[NSCAL];
   __shared__ double knl_s[NB], inv_s[NB], g_s[NB], chi_s[NB], t1_s[NB], t2_s[NB], s1_s[NB], s2_s[NB];
   __shared__ int ilo_s[NB], ihi_s[NB];
-  __shared__ float iv2h_s[NB], iv2l_s[NB];
-  __shared__ float wpf[FAST ? NKH : 1], k2h[FAST ? NKH : 1], k2l[FAST ? NKH : 1];
+  __shared__ float iv2h_s[NB], iv2l_s[NB], f1_s[NB], f2_s[NB];
+  __shared__ float wpf[FAST ? NKH : 1], k2h[FAST ? NKH + 1 : 1], k2l[FAST ? NKH + 1 : 1];
   const CosmoTab* ct = it.ctab;
   for (int i = threadIdx.x; i < NRT; i += blockDim.x) sig[i] = ct->sig[i];
   if (FAST) {
-    for (int i = threadIdx.x; i < NKH; i += blockDim.x) {
-      wpf[i] = ct->wpk3f[i];
+    for (int i = threadIdx.x; i < NKH + 1; i += blockDim.x) {
+      if (i < NKH) wpf[i] = ct->wpk3f[i];
       k2h[i] = c->kh2_hi[i];
       k2l[i] = c->kh2_lo[i];
     }
@@ -367,23 +328,31 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
       ihi = (int)ceilf((HLY2S - linv - (float)LOG_KMIN) * (float)(1.0 / DLOGK));
       ilo = max(0, min(ilo, NKH));
       ihi = max(ilo - 1, min(ihi, NKH - 1));
-      const double iv2d = inv * inv;
-      const float ih = (float)iv2d;
-      iv2h_s[t] = ih;
-      iv2l_s[t] = (float)(iv2d - (double)ih);
-      // sum_{i < ilo} w pk3 y^2 e^{-y^2} = sum_m (-1)^m / m! inv^(2m+2) P_m[ilo]
+      const FF iv2 = ff_of(inv * inv);
+      iv2h_s[t] = iv2.hi;
+      iv2l_s[t] = iv2.lo;
+      // sum_{i < ilo} w pk3 y^2 e^{-y^2} = sum_m (-1)^m / m! x^(m+1) Q_m[ilo]
+      // with x = y_ilo^2 = (kh_ilo inv)^2: t1 = x F(x), and the y^4 moment
+      // gives t2 = t1 + x^2 F'(x), F(x) = sum_m R_m[ilo] x^m (Horner with
+      // the derivative, float pairs)
       if (ilo > 0) {
-        const double iv2 = inv * inv;
-        double pw = iv2, fact = 1.0;
-        for (int m = 0; m < NTAYLOR - 1; ++m) {
-          const double sg = (m & 1) ? -1.0 : 1.0;
-          const double p0 = ct->ptay[m][ilo] * pw;
-          const double p1 = ct->ptay[m + 1][ilo] * pw * iv2;
-          t1 += sg / fact * p0;
-          t2 += sg / fact * (p0 - p1);
-          pw *= iv2;
-          fact *= (double)(m + 1);
+        FF kk;
+        kk.hi = k2h[ilo], kk.lo = k2l[ilo];
+        const FF x = ff_mul(kk, iv2);
+        const float2* R = &ct->rtay[0][ilo];
+        FF P, D;
+        P.hi = R[(NTAYLOR - 1) * (NKH + 1)].x, P.lo = R[(NTAYLOR - 1) * (NKH + 1)].y;
+        D.hi = 0.f, D.lo = 0.f;
+        for (int m = NTAYLOR - 2; m >= 0; --m) {
+          D = ff_add(ff_mul(D, x), P);
+          FF r;
+          r.hi = R[m * (NKH + 1)].x, r.lo = R[m * (NKH + 1)].y;
+          P = ff_add(ff_mul(P, x), r);
         }
+        const FF f1 = ff_mul(x, P);
+        const FF f2 = ff_mul(ff_mul(x, x), D);
+        t1 = ff_to_double(f1);
+        t2 = t1 + ff_to_double(f2);
       }
     }
     ilo_s[t] = ilo;
@@ -417,8 +386,10 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
         f1 += __shfl_xor_sync(0xffffffffu, f1, o);
         f2 += __shfl_xor_sync(0xffffffffu, f2, o);
       }
-      s1 = (double)f1;
-      s2 = (double)f2;
+      if (lane == 0) {
+        f1_s[t] = f1;
+        f2_s[t] = f2;
+      }
     } else {
       const double g2 = g_s[t] * g_s[t];
       for (int i = lane; i < NKH; i += 32) {
@@ -432,10 +403,10 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
     if (!FAST) {
       s1 = warp_sum(s1);
       s2 = warp_sum(s2);
-    }
-    if (lane == 0) {
-      s1_s[t] = s1;
-      s2_s[t] = s2;
+      if (lane == 0) {
+        s1_s[t] = s1;
+        s2_s[t] = s2;
+      }
     }
   }
   __syncthreads();
@@ -444,7 +415,7 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
     const int n = n0 + t;
     const double a = A[n];
-    double s1 = s1_s[t], s2 = s2_s[t];
+    double s1 = FAST ? (double)f1_s[t] : s1_s[t], s2 = FAST ? (double)f2_s[t] : s2_s[t];
     if (FAST) {
       const double g2 = g_s[t] * g_s[t];
       s1 = (s1 + 2.0 * t1_s[t]) * g2 / TWO_PI2;
@@ -541,7 +512,7 @@ __global__ void eval_points_kernel(const double* __restrict__ params, int n_cosm
     v = pk_linear(s, k, growth(a));
   } else {
     const double g = growth(a);
-    const HfParams hp = halofit_params_warp<false>(ct->sig, ct->pk3, nullptr, g, c, lane);
+    const HfParams hp = halofit_params_warp(ct->sig, ct->pk3, g, c, lane);
     if (what == 6) {
       double row[NROW64];
       row[R_G] = g;

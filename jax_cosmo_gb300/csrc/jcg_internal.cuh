@@ -58,8 +58,13 @@ struct ConstTables {
   double E[NKH * NRT];     // exp(-(k_i r_j)^2), i-major: power.py:99-109
   double kpw[NTAYLOR][NKH];  // simpson_kh[i] * kh[i]^(2(m+1)): the Taylor prefix sums' weights
   double romb_w[NROMB];      // romb's Richardson combination as weights on romb_logk's values
-  float kh2_hi[NKH];         // kh[i]^2 as a float pair hi + lo (fp32c halofit moments)
-  float kh2_lo[NKH];
+  // fp32c halofit moments: kh[i]^2 as a float pair hi + lo, with a virtual
+  // node kh[NKH] = kh[NKH - 1] e^dlnk; the Taylor tables' factors
+  // rho_m = e^(-2 (m + 1) dlnk) and c_m = (-1)^m / m! as float pairs
+  float kh2_hi[NKH + 1];
+  float kh2_lo[NKH + 1];
+  float tay_rho[NTAYLOR][2];
+  float tay_c[NTAYLOR][2];
 };
 
 // ------------------------------------------------- per-cosmology tables -----
@@ -96,9 +101,10 @@ struct CosmoTab {
   float chi32[NCHI];       // chi table, float (FP32 lensing kernel)
   float slope32[NCHI];     // chi_slope, float
   float wpk3f[NKH + 15];   // simpson_kh[i] * pk3[i], float (fp32c halofit moments); padded to 64 bytes
-  // prefix sums over the ln k grid of w_i P(k_i) k_i^3 k_i^(2(m+1)), m < NTAYLOR:
-  // the small-y part of the halofit moments as a Taylor series in y^2
-  double ptay[NTAYLOR][NKH + 1];
+  // fp32c: the small-y part of the halofit moments as a Taylor series in y^2.
+  // Float pairs R_m[i] = c_m Q_m[i], c_m = (-1)^m / m!,
+  // Q_m[i] = sum_{k < i} w_k P(k_k) k_k^3 (k_k / k_i)^(2(m+1)), m < NTAYLOR
+  float2 rtay[NTAYLOR][NKH + 1];
   double pad[PAD_CT];
 };
 static_assert(sizeof(CosmoTab) % 64 == 0, "CosmoTab must keep 64-byte alignment");

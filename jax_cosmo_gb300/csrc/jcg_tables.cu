@@ -5,6 +5,7 @@
 // (growth), power.py:56-78 (sigmasqr / romb), power.py:86-111 (sigma^2(R)),
 // redshift.py:27-31 (n(z) normalisation), probes.py:16-99 (tracer grids),
 // angular_cl.py:63-96 (Limber grid).
+#include "jcg_fp32.cuh"
 #include "jcg_internal.cuh"
 
 namespace jcg {
@@ -41,6 +42,11 @@ __global__ void const_init_kernel(ConstTables* c) {
     const double k2 = k * k;
     c->kh2_hi[i] = (float)k2;
     c->kh2_lo[i] = (float)(k2 - (double)(float)k2);
+    if (i == NKH - 1) {
+      const double kv2 = k2 * exp(2.0 * DLOGK);
+      c->kh2_hi[NKH] = (float)kv2;
+      c->kh2_lo[NKH] = (float)(kv2 - (double)(float)kv2);
+    }
     double kp = k2;
     for (int m = 0; m < NTAYLOR; ++m) {
       c->kpw[m][i] = sw * kp;
@@ -49,6 +55,16 @@ __global__ void const_init_kernel(ConstTables* c) {
   }
   for (int j = tid; j < NRT; j += nth) {
     c->logr[j] = np_linspace(kLogKMin, kLogRMax, NRT - 1, j);
+  }
+  for (int m = tid; m < NTAYLOR; m += nth) {
+    const double rho = exp(-2.0 * DLOGK * (m + 1));
+    double cm = 1.0;
+    for (int j = 1; j <= m; ++j) cm /= (double)j;
+    if (m & 1) cm = -cm;
+    c->tay_rho[m][0] = (float)rho;
+    c->tay_rho[m][1] = (float)(rho - (double)(float)rho);
+    c->tay_c[m][0] = (float)cm;
+    c->tay_c[m][1] = (float)(cm - (double)(float)cm);
   }
   // romb(int_sigma, -4, 3, divmax=7) abscissae in evaluation order
   // (scipy/integrate.py:129-146): a, b, then the new midpoints of each level.
@@ -350,6 +366,7 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   __shared__ double chis[NCHI];
   __shared__ double gs[NGROW];
   __shared__ double mv[4 * NGROW];  // per-step growth matrices
+  __shared__ float2 wpp[NKH];       // fp32c: w pk3 as float pairs
   const int t = threadIdx.x;
   if (t == 0) cosmo_scalars(it.params, s);
   __syncthreads();
@@ -457,26 +474,34 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
     out->chi32[i] = (float)chis[i];
     out->slope32[i] = (float)sl;
   }
-  for (int i = t; i < NKH + 15; i += blockDim.x) out->wpk3f[i] = i < NKH ? (float)(c->simpson_kh[i] * pk3[i]) : 0.f;
-  // Taylor prefix sums of the halofit moments (fp32c rows only):
-  // P_m[i] = sum_{i' < i} w pk3 k^(2m+2), one warp per m with a warp-wide
-  // inclusive scan over chunks of 32 nodes.
-  for (int m = t >> 5; it.precision == JCG_FP32C && m < NTAYLOR; m += (int)(blockDim.x >> 5)) {
-    const int lane = t & 31;
-    {
-      if (lane == 0) out->ptay[m][0] = 0.0;
-      double carry = 0.0;
-      for (int base = 0; base < NKH; base += 32) {
-        const int i = base + lane;
-        double v = 0.0;
-        if (i < NKH) v = c->kpw[m][i] * pk3[i];
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const double u = __shfl_up_sync(0xffffffffu, v, o);
-          if (lane >= o) v += u;
-        }
-        if (i < NKH) out->ptay[m][i + 1] = carry + v;
-        carry += __shfl_sync(0xffffffffu, v, 31);
+  if (it.precision == JCG_FP32C) {
+    // fp32c halofit moments: w pk3 as float pairs (float copy for the exp
+    // terms), then the Taylor tables by the contracting recurrence
+    // Q_m[i + 1] = (Q_m[i] + w_i pk3_i) rho_m in float pairs, one lane per m
+    for (int i = t; i < NKH + 15; i += blockDim.x) {
+      float hi = 0.f;
+      if (i < NKH) {
+        const FF w = ff_of(c->simpson_kh[i] * pk3[i]);
+        hi = w.hi;
+        wpp[i] = make_float2(w.hi, w.lo);
+      }
+      out->wpk3f[i] = hi;
+    }
+    __syncthreads();
+    if (t < NTAYLOR) {
+      const int m = t;
+      FF rho, cm, q;
+      rho.hi = c->tay_rho[m][0], rho.lo = c->tay_rho[m][1];
+      cm.hi = c->tay_c[m][0], cm.lo = c->tay_c[m][1];
+      q.hi = 0.f, q.lo = 0.f;
+      float2* dst = out->rtay[m];
+      dst[0] = make_float2(0.f, 0.f);
+      for (int i = 0; i < NKH; ++i) {
+        FF w;
+        w.hi = wpp[i].x, w.lo = wpp[i].y;
+        q = ff_mul(ff_add(q, w), rho);
+        const FF r = ff_mul(cm, q);
+        dst[i + 1] = make_float2(r.hi, r.lo);
       }
     }
   }
