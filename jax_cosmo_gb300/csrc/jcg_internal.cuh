@@ -58,6 +58,21 @@ struct ConstTables {
   double E[NKH * NRT];     // exp(-(k_i r_j)^2), i-major: power.py:99-109
   double kpw[NTAYLOR][NKH];  // simpson_kh[i] * kh[i]^(2(m+1)): the Taylor prefix sums' weights
   double romb_w[NROMB];      // romb's Richardson combination as weights on romb_logk's values
+  // cosmology-independent factors of the table kernel's right-hand sides
+  double romb_k[NROMB];      // exp(romb_logk)
+  double romb_ik[NROMB];     // 1 / romb_k
+  double romb_kw2[NROMB];    // k (k W(8k))^2, W the top-hat window (power.py:70-75)
+  double ikh[NKH];           // 1 / kh
+  double chi_a[NCHI];        // exp(lna_chi): the chi RK4 nodes
+  double chi_ia[NCHI];       // 1 / chi_a
+  double chi_lnam[NCHI];     // step midpoints lna_chi[i-1] + (lna_chi[i] - lna_chi[i-1]) / 2 (i >= 1)
+  double chi_am[NCHI];       // exp(chi_lnam)
+  double chi_iam[NCHI];      // 1 / chi_am
+  double grow_lna[NGROW];    // log(atab_grow)
+  double grow_ia[NGROW];     // 1 / atab_grow
+  double grow_am[NGROW];     // step midpoints atab_grow[i-1] + (atab_grow[i] - atab_grow[i-1]) / 2 (i >= 1)
+  double grow_lnam[NGROW];   // log(grow_am)
+  double grow_iam[NGROW];    // 1 / grow_am
   // fp32c halofit moments: kh[i]^2 as a float pair hi + lo, with a virtual
   // node kh[NKH] = kh[NKH - 1] e^dlnk; the Taylor tables' factors
   // rho_m = e^(-2 (m + 1) dlnk) and c_m = (-1)^m / m! as float pairs
@@ -80,6 +95,9 @@ enum Scalar {
   S_G1,         // growth_factor(a = 1) from the table (power.py:44 with a = 1)
   S_LGQ,        // log(13.41 k_eq): log q = log k - S_LGQ (transfer.py:122)
   S_LGKSILK,    // log(k_silk)
+  S_QINV,       // 1 / (13.41 k_eq)
+  S_ISH,        // 1 / sh_d
+  S_C142AC,     // 14.2 / alpha_c
   S_NSCALAR
 };
 constexpr int NSCAL = 32;
@@ -527,39 +545,75 @@ __device__ __forceinline__ double bg_dchioverda(const Bg& c, double a) {
 }
 
 // ------------------------------------------------------ Eisenstein & Hu ----
-// transfer.py:107-153 (eisenhu_osc), per-k part, FP64.  Powers are taken as
-// exp(y log x) with the logs shared between terms (log k, log q); on GB300 a
-// float64 pow costs about two exps, and the shared forms change results only
-// at the 1e-15 level.  lk = log(k).
-__device__ __forceinline__ double eh_transfer_lk(const double* s, double k, double lk) {
-  const double k_eq = s[S_K_EQ], sh_d = s[S_SH_D];
-  const double q = k / (13.41 * k_eq);
+// transfer.py:107-153 (eisenhu_osc), per-k part, FP64, at k with lk = log k
+// and ik = 1 / k.  Powers are taken as exp(y log x) with the logs shared
+// between terms (log k, log q); the divisions are shared too: one reciprocal
+// for the three T_tilde denominators, one for the three damping factors, and
+// rcbrt for tilde_s.  On GB300 a float64 pow costs about two exps and a
+// division about ten float64 operations; the shared forms change results only
+// at the 1e-15 level.
+__device__ __forceinline__ double eh_transfer_lki(const double* s, double k, double lk, double ik) {
+  const double sh_d = s[S_SH_D];
+  const double q = k * s[S_QINV];
   const double q108 = exp(1.08 * (lk - s[S_LGQ]));
   const double Cb = 386.0 / (1.0 + 69.9 * q108);
   const double qq = q * q;
-  // T_tilde(k, 1, beta_c), T_tilde(k, alpha_c, beta_c) share L; T_tilde(k, 1, 1)
   const double L1 = log(EULER_E + 1.8 * s[S_BETA_C] * q);
   const double L2 = log(EULER_E + 1.8 * q);
-  const double Ta = L1 / (L1 + (14.2 + Cb) * qq);
-  const double Tb = L1 / (L1 + (14.2 / s[S_ALPHA_C] + Cb) * qq);
-  const double Tn = L2 / (L2 + (14.2 + Cb) * qq);
-  const double ksh = k * sh_d;
-  const double x54 = ksh / 5.4, x54s = x54 * x54;
-  const double f = 1.0 / (1.0 + x54s * x54s);
+  const double da = L1 + (14.2 + Cb) * qq;
+  const double db = L1 + (s[S_C142AC] + Cb) * qq;
+  const double dn = L2 + (14.2 + Cb) * qq;
+  const double dab = da * db;
+  const double r3 = 1.0 / (dab * dn);
+  const double Ta = L1 * (db * dn) * r3;
+  const double Tb = L1 * (da * dn) * r3;
+  const double Tn = L2 * dab * r3;
+  const double ksh = k * sh_d, iksh = ik * s[S_ISH];
+  const double x54 = ksh * (1.0 / 5.4), x54s = x54 * x54;
+  const double x52 = ksh * (1.0 / 5.2);
+  const double bb = s[S_BETA_B] * iksh;
+  const double bn = s[S_BETA_NODE] * iksh;
+  const double d1 = 1.0 + x54s * x54s, d2 = 1.0 + x52 * x52, d3 = 1.0 + bb * bb * bb;
+  const double d12 = d1 * d2;
+  const double r6 = 1.0 / (d12 * d3);
+  const double f = d2 * d3 * r6;
   const double Tc = f * Ta + (1.0 - f) * Tb;
-  const double bn = s[S_BETA_NODE] / ksh;
-  const double tilde_s = sh_d / cbrt(1.0 + bn * bn * bn);
-  const double x52 = ksh / 5.2;
-  const double bb = s[S_BETA_B] / ksh;
+  const double tilde_s = sh_d * rcbrt(1.0 + bn * bn * bn);
   const double silk = exp(-exp(1.4 * (lk - s[S_LGKSILK])));
   const double arg = k * tilde_s;
-  const double sinc = sin(arg) / arg;  // np.sinc(k tilde_s / pi), k > 0
-  const double Tbar = (Tn / (1.0 + x52 * x52) + s[S_ALPHA_B] / (1.0 + bb * bb * bb) * silk) * sinc;
+  const double sinc = sin(arg) / arg;
+  const double Tbar = (Tn * (d1 * d3 * r6) + s[S_ALPHA_B] * (d12 * r6) * silk) * sinc;
   return s[S_FB] * Tbar + s[S_FC] * Tc;
+}
+
+__device__ __forceinline__ double eh_transfer_lk(const double* s, double k, double lk) {
+  return eh_transfer_lki(s, k, lk, 1.0 / k);
 }
 
 __device__ __forceinline__ double eh_transfer(const double* s, double k) {
   return eh_transfer_lk(s, k, log(k));
+}
+
+// dchi/dln a = dchioverda(a) a = R_H / (a sqrt(E^2(a))) (background.py:227-229)
+// with ln a and 1 / a given
+__device__ __forceinline__ double dchi_dlna_c(const Bg& b, double a, double lna, double ia) {
+  const double f = bg_fde_l(b, a, lna);
+  const double ef = (f == 0.0) ? 1.0 : exp(f);
+  const double ia2 = ia * ia;
+  const double e2 = b.Om * (ia2 * ia) + b.Ok * ia2 + b.Ode * ef;
+  return RH * ia * rsqrt(e2);
+}
+
+// growth ODE coefficients D'' = -q D' + r D (background.py:96-106) with ln x
+// and 1 / x given
+__device__ __forceinline__ void growth_qr_c(const Bg& b, double x, double lnx, double ix, double& q, double& r) {
+  const double f = bg_fde_l(b, x, lnx);
+  const double ef = (f == 0.0) ? 1.0 : exp(f);
+  const double ix2 = ix * ix, ix3 = ix2 * ix;
+  const double ie2 = 1.0 / (b.Om * ix3 + b.Ok * ix2 + b.Ode * ef);
+  const double omm = b.Om * ix3 * ie2, omde = b.Ode * ef * ie2;
+  q = (2.0 - 0.5 * (omm + (1.0 + 3.0 * bg_w(b, x)) * omde)) * ix;
+  r = 1.5 * omm * ix2;
 }
 
 // linear_matter_power(k, a) with g = growth_factor(a): power.py:42-53

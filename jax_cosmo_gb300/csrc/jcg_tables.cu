@@ -24,10 +24,32 @@ __global__ void const_init_kernel(ConstTables* c) {
     const double y = np_linspace(-3.0, 0.0, NCHI - 1, i);
     const double a = pow(10.0, y);
     c->atab_chi[i] = a;
-    c->lna_chi[i] = log(a);
+    const double x = log(a);
+    c->lna_chi[i] = x;
+    c->chi_a[i] = exp(x);
+    c->chi_ia[i] = 1.0 / exp(x);
+    double xm = 0.0;
+    if (i > 0) {
+      const double x0 = log(pow(10.0, np_linspace(-3.0, 0.0, NCHI - 1, i - 1)));
+      xm = x0 + (x - x0) / 2;
+    }
+    c->chi_lnam[i] = xm;
+    c->chi_am[i] = i > 0 ? exp(xm) : 0.0;
+    c->chi_iam[i] = i > 0 ? 1.0 / exp(xm) : 0.0;
   }
   for (int i = tid; i < NGROW; i += nth) {
-    c->atab_grow[i] = pow(10.0, np_linspace(-3.0, 0.0, NGROW - 1, i));
+    const double x = pow(10.0, np_linspace(-3.0, 0.0, NGROW - 1, i));
+    c->atab_grow[i] = x;
+    c->grow_lna[i] = log(x);
+    c->grow_ia[i] = 1.0 / x;
+    double xm = 0.0;
+    if (i > 0) {
+      const double xp = pow(10.0, np_linspace(-3.0, 0.0, NGROW - 1, i - 1));
+      xm = xp + (x - xp) / 2;
+    }
+    c->grow_am[i] = xm;
+    c->grow_lnam[i] = i > 0 ? log(xm) : 0.0;
+    c->grow_iam[i] = i > 0 ? 1.0 / xm : 0.0;
   }
   const double dxk = (kLogKMax - kLogKMin) / 256.0;
   for (int i = tid; i < NKH; i += nth) {
@@ -35,6 +57,7 @@ __global__ void const_init_kernel(ConstTables* c) {
     const double k = exp(lk);
     c->logk[i] = lk;
     c->kh[i] = k;
+    c->ikh[i] = 1.0 / k;
     c->kh3[i] = pow(k, 3.0);
     const double w = (i == 0 || i == NKH - 1) ? 1.0 : ((i & 1) ? 4.0 : 2.0);
     const double sw = dxk / 3 * w;
@@ -79,6 +102,16 @@ __global__ void const_init_kernel(ConstTables* c) {
       const double lox = a + 0.5 * h;
       for (int m = 0; m < numtosum; ++m) c->romb_logk[pos++] = lox + h * (double)m;
     }
+  }
+  __syncthreads();
+  for (int e = tid; e < NROMB; e += nth) {
+    const double k = exp(c->romb_logk[e]);
+    const double x = k * 8.0;
+    const double wf = 3.0 * (sin(x) - x * cos(x)) / (x * x * x);
+    const double kw = k * wf;
+    c->romb_k[e] = k;
+    c->romb_ik[e] = 1.0 / k;
+    c->romb_kw2[e] = k * (kw * kw);
   }
   // romb is linear in the integrand values: the weight of abscissa e is the
   // combination (scipy/integrate.py:131-159, divmax = 7) of the unit vector e
@@ -336,20 +369,9 @@ __device__ void cosmo_scalars(const double* p, double* s) {
   s[S_FC] = fc;
   s[S_LGQ] = log(13.41 * k_eq);
   s[S_LGKSILK] = log(k_silk);
-}
-
-// dchi/dln a = dchioverda(exp(x)) * exp(x)   (background.py:227-229)
-__device__ __forceinline__ double dchi_dlna(const Bg& b, double x) {
-  const double xa = exp(x);
-  return bg_dchioverda_l(b, xa, x) * xa;
-}
-
-// growth ODE coefficients: D'' = -q D' + r D  (background.py:96-106)
-__device__ __forceinline__ void growth_qr(const Bg& b, double x, double& q, double& r) {
-  double omm, omde;
-  bg_om_l(b, x, log(x), &omm, &omde);
-  q = (2.0 - 0.5 * (omm + (1.0 + 3.0 * bg_w(b, x)) * omde)) / x;
-  r = 1.5 * omm / x / x;
+  s[S_QINV] = 1.0 / (13.41 * k_eq);
+  s[S_ISH] = 1.0 / sh_d;
+  s[S_C142AC] = 14.2 / alpha_c;
 }
 
 __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const ConstTables* __restrict__ c) {
@@ -375,32 +397,20 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   // right-hand side does not depend on chi, so each step needs f at its two
   // ends (shared with the neighbouring steps) and at its midpoint.
   if (t < NCHI) {
-    fnode[t] = dchi_dlna(bg, c->lna_chi[t]);
-    if (t > 0) {
-      const double t0 = c->lna_chi[t - 1], t1 = c->lna_chi[t];
-      inc[t] = dchi_dlna(bg, t0 + (t1 - t0) / 2);
-    }
+    fnode[t] = dchi_dlna_c(bg, c->chi_a[t], c->lna_chi[t], c->chi_ia[t]);
+    if (t > 0) inc[t] = dchi_dlna_c(bg, c->chi_am[t], c->chi_lnam[t], c->chi_iam[t]);
   }
   // growth ODE coefficients at nodes and midpoints
   if (t < NGROW) {
-    const double x = c->atab_grow[t];
-    growth_qr(bg, x, qa[t], ra[t]);
-    if (t > 0) {
-      const double xp = c->atab_grow[t - 1];
-      const double hh = x - xp;
-      growth_qr(bg, xp + hh / 2, qm[t], rm[t]);
-    }
+    growth_qr_c(bg, c->atab_grow[t], c->grow_lna[t], c->grow_ia[t], qa[t], ra[t]);
+    if (t > 0) growth_qr_c(bg, c->grow_am[t], c->grow_lnam[t], c->grow_iam[t], qm[t], rm[t]);
   }
-  // sigmasqr(8) integrand at the romb nodes (power.py:70-75)
+  // sigmasqr(8) integrand at the romb nodes (power.py:70-75): the window
+  // factor k (k W(8k))^2 is a constant of the node
   if (t < NROMB) {
     const double logk = c->romb_logk[t];
-    const double k = exp(logk);
-    const double x = k * 8.0;
-    const double wf = 3.0 * (sin(x) - x * cos(x)) / (x * x * x);
-    const double T = eh_transfer(s, k);
-    const double pk = (T * T) * pow(k, s[S_NS]);
-    const double kw = k * wf;
-    fr[t] = k * (kw * kw) * pk;
+    const double T = eh_transfer_lki(s, c->romb_k[t], logk, c->romb_ik[t]);
+    fr[t] = c->romb_kw2[t] * ((T * T) * exp(s[S_NS] * logk));
   }
   __syncthreads();
   // growth: one RK4 step is linear in y = (D, dD/da), y_i = M_i y_{i-1};
@@ -450,7 +460,9 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   __syncthreads();
   // linear P(k_i, a = 1) * k_i^3 on the halofit k grid (power.py:102, 124)
   for (int i = t; i < NKH; i += blockDim.x) {
-    pk3[i] = pk_linear(s, c->kh[i], s[S_G1]) * c->kh3[i];
+    const double tk = eh_transfer_lki(s, c->kh[i], c->logk[i], c->ikh[i]);
+    const double g1 = s[S_G1];
+    pk3[i] = exp(s[S_NS] * c->logk[i]) * (tk * tk) * (g1 * g1) * s[S_PKNORM] * c->kh3[i];
   }
   __syncthreads();
   // sigma^2(R_j) without g^2: simps over ln k of pk k^3 exp(-(k R)^2) / (2 pi^2),
