@@ -217,6 +217,182 @@ __global__ void __launch_bounds__(LB_THREADS)
   }
 }
 
+// ------------------------------------------------------- fp32c kernel ----
+// The fp32c Limber integral with a register-blocked contraction: a work unit
+// is (ell, 4 consecutive spectra, residue of the a node mod nsplit); per a
+// node it loads P(ell, a) once and M_ij(a) of its 4 spectra as one float4
+// (a broadcast within the warp), and keeps 4 Kahan-compensated accumulators.
+// Small outputs (lt x ceil(n_cls / 4) < LB_THREADS) split the a nodes over
+// nsplit units, added in float64 at the end.  The kernels K_i(a) and the
+// weights u_a of a chunk are staged once as floats, then M_ij(a) =
+// (K_i K_j) u in the order of the generic kernel.
+constexpr int L32_MAXU = 5;  // ceil(LB_MAXLT * ceil(MAXPAIR / 4) / LB_THREADS)
+
+struct L32Layout {
+  size_t e32, kh32, rows, ks, us, ms, pt, red, total;
+};
+__host__ __device__ inline L32Layout l32_layout(int n_tr, int n_cls, int LT) {
+  L32Layout L;
+  size_t o = NSCAL * 8;
+  L.e32 = o;
+  o += 8 * 8;
+  L.kh32 = o;
+  o += 3 * LB_MAXLT * 4;
+  L.rows = o;
+  o += (size_t)LB_TA * NROW32 * 4;
+  L.ks = o;
+  o += (size_t)n_tr * LB_TA * 4;
+  L.us = o;
+  o += LB_TA * 4;
+  o = (o + 15) & ~(size_t)15;
+  L.ms = o;
+  o += (size_t)LB_TA * ((n_cls + 3) & ~3) * 4;
+  L.pt = o;
+  o += (size_t)LB_TA * LT * 4;
+  o = (o + 15) & ~(size_t)15;
+  L.red = o;
+  o += (size_t)LB_THREADS * 4 * 8;
+  L.total = o;
+  return L;
+}
+
+template <int MAXU>
+__global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2))
+    limber32_kernel(Batch bt, const ConstTables* __restrict__ c, int LT) {
+  const int item = blockIdx.y;
+  if (item >= bt.n_items) return;
+  const Item it = batch_item(bt, item);
+  const GeoHeader* geo = it.geo;
+  const int n_ell = geo->n_ell, n_cls = geo->n_cls, na = geo->na, n_tr = geo->n_tr;
+  const int l0 = blockIdx.x * LT;
+  if (l0 >= n_ell) return;
+  const int lt = min(LT, n_ell - l0);
+  const int npg = (n_cls + 3) >> 2, ncp = npg * 4;
+  const int items = lt * npg;
+  const int nsplit = items >= LB_THREADS ? 1 : min(8, LB_THREADS / items);
+  const int units = items * nsplit;
+  const L32Layout L = l32_layout(n_tr, n_cls, LT);
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* s = reinterpret_cast<double*>(smem_raw);
+  EH32* e32 = reinterpret_cast<EH32*>(smem_raw + L.e32);
+  float* kh32 = reinterpret_cast<float*>(smem_raw + L.kh32);
+  float* rowsS = reinterpret_cast<float*>(smem_raw + L.rows);
+  float* Ks = reinterpret_cast<float*>(smem_raw + L.ks);
+  float* us = reinterpret_cast<float*>(smem_raw + L.us);
+  float* Ms = reinterpret_cast<float*>(smem_raw + L.ms);
+  const float4* Ms4 = reinterpret_cast<const float4*>(Ms);
+  float* Pt = reinterpret_cast<float*>(smem_raw + L.pt);
+  double* red = reinterpret_cast<double*>(smem_raw + L.red);
+  const int tid = threadIdx.x;
+  const double* ELL = geo_ptr<double>(geo, geo->off_ell);
+  const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
+  for (int i = tid; i < NSCAL; i += LB_THREADS) s[i] = it.ctab->s[i];
+  for (int l = tid; l < lt; l += LB_THREADS) {
+    const double e = ELL[l0 + l] + 0.5;
+    kh32[3 * l + 0] = (float)e;                               // k = kh / max(chi, 1)
+    kh32[3 * l + 1] = (float)(1.4426950408889634 * log(e));   // log2(kh)
+    kh32[3 * l + 2] = (float)(1.0 / e);                       // 1 / kh
+  }
+  __syncthreads();
+  if (tid == 0) make_eh32(s, e32);
+  const float* rows32 = it.rows32;
+  const double* rows64 = it.rows64;
+  const double* kern = it.kern;
+  float acc[MAXU][4], comp[MAXU][4];
+#pragma unroll
+  for (int r = 0; r < MAXU; ++r)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[r][j] = 0.f, comp[r][j] = 0.f;
+  for (int base = 0; base < na; base += LB_TA) {
+    const int tc = min(LB_TA, na - base);
+    for (int i = tid; i < tc * NROW32; i += LB_THREADS) rowsS[i] = rows32[(size_t)base * NROW32 + i];
+    for (int q = tid; q < n_tr * tc; q += LB_THREADS) {
+      const int tr = q / tc, t = q - tr * tc;
+      Ks[tr * LB_TA + t] = (float)kern[(size_t)tr * na + base + t];
+    }
+    for (int t = tid; t < tc; t += LB_THREADS) us[t] = (float)rows64[(size_t)(base + t) * NROW64 + R_U];
+    __syncthreads();
+    // M_ij(a) = (K_i K_j) u_a, zero-padded to ncp spectra
+    for (int q = tid; q < tc * ncp; q += LB_THREADS) {
+      const int t = q / ncp, p = q - t * ncp;
+      float m = 0.f;
+      if (p < n_cls) m = Ks[geo->pair_i[p] * LB_TA + t] * Ks[geo->pair_j[p] * LB_TA + t] * us[t];
+      Ms[q] = m;
+    }
+    // P tile: nodes (t, l)
+    for (int q = tid; q < tc * lt; q += LB_THREADS) {
+      const int t = q / lt, l = q - t * lt;
+      Pt[t * LT + l] = node32(*e32, rowsS + t * NROW32, kh32[3 * l], kh32[3 * l + 1], kh32[3 * l + 2]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int r = 0; r < MAXU; ++r) {
+      const int u = tid + r * LB_THREADS;
+      if (u < units) {
+        const int itm = u % items, sp = u / items;
+        const int l = itm % lt, pg = itm / lt;
+        float p0 = 0.f, p1 = 0.f, p2 = 0.f, p3 = 0.f;
+        for (int t = sp; t < tc; t += nsplit) {
+          const float pv = Pt[t * LT + l];
+          const float4 m = Ms4[t * npg + pg];
+          p0 = fmaf(pv, m.x, p0);
+          p1 = fmaf(pv, m.y, p1);
+          p2 = fmaf(pv, m.z, p2);
+          p3 = fmaf(pv, m.w, p3);
+        }
+        const float part[4] = {p0, p1, p2, p3};
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const float y = part[j] - comp[r][j];
+          const float tt = acc[r][j] + y;
+          comp[r][j] = (tt - acc[r][j]) - y;
+          acc[r][j] = tt;
+        }
+      }
+    }
+    __syncthreads();
+  }
+  // a nodes split over nsplit units: partial sums added in float64
+  if (nsplit > 1) {
+    if (tid < units) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) red[tid * 4 + j] = (double)acc[0][j] - (double)comp[0][j];
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int r = 0; r < MAXU; ++r) {
+    const int u = tid + r * LB_THREADS;
+    if (u < items) {
+      const int l = u % lt, pg = u / lt;
+      const int ell = l0 + l;
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int p = pg * 4 + j;
+        if (p >= n_cls) break;
+        double v;
+        if (nsplit > 1) {
+          v = 0.0;
+          for (int sp = 0; sp < nsplit; ++sp) v += red[(u + sp * items) * 4 + j];
+        } else {
+          v = (double)acc[r][j] - (double)comp[r][j];
+        }
+        const double efi = EF[(size_t)geo->pair_i[p] * n_ell + ell];
+        const double efj = EF[(size_t)geo->pair_j[p] * n_ell + ell];
+        it.cl[(size_t)p * n_ell + ell] = v * efi * efj;
+      }
+    }
+  }
+}
+
+template <int MAXU>
+static void launch_limber32_t(const Batch& b, const ConstTables* c, int lt, cudaStream_t st) {
+  const L32Layout L = l32_layout(b.max_tr, b.max_cls, lt);
+  cudaFuncSetAttribute(limber32_kernel<MAXU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+  dim3 grid((b.max_ell + lt - 1) / lt, b.n_items);
+  limber32_kernel<MAXU><<<grid, LB_THREADS, L.total, st>>>(b, c, lt);
+}
+
 size_t limber_smem_bytes(bool fp32, int n_cls, int LT) {
   const size_t el = fp32 ? 4 : 8;
   const size_t rw = fp32 ? NROW32 : NROW64;
@@ -244,13 +420,19 @@ static void launch_limber_p(const Batch& b, const ConstTables* c, int lt, size_t
 }
 
 void launch_limber(const Batch& b, const ConstTables* c, int lt, cudaStream_t st) {
-  const bool fp32 = b.precision == JCG_FP32C;
-  const size_t smem = limber_smem_bytes(fp32, b.max_cls, lt);
+  if (b.precision == JCG_FP32C) {
+    // units per thread: the split path needs one, otherwise lt x ceil(n_cls / 4)
+    const int items = lt * ((b.max_cls + 3) / 4);
+    const int need = items >= LB_THREADS ? (items + LB_THREADS - 1) / LB_THREADS : 1;
+    if (need <= 1) launch_limber32_t<1>(b, c, lt, st);
+    else if (need <= 2) launch_limber32_t<2>(b, c, lt, st);
+    else if (need <= 3) launch_limber32_t<3>(b, c, lt, st);
+    else launch_limber32_t<L32_MAXU>(b, c, lt, st);
+    return;
+  }
+  const size_t smem = limber_smem_bytes(false, b.max_cls, lt);
   dim3 grid((b.max_ell + lt - 1) / lt, b.n_items);
-  if (fp32)
-    launch_limber_p<true>(b, c, lt, smem, grid, st);
-  else
-    launch_limber_p<false>(b, c, lt, smem, grid, st);
+  launch_limber_p<false>(b, c, lt, smem, grid, st);
 }
 
 }  // namespace jcg
