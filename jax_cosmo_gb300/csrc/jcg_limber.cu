@@ -237,7 +237,7 @@ __host__ __device__ inline L32Layout l32_layout(int n_tr, int n_cls, int LT) {
   L.e32 = o;
   o += 8 * 8;
   L.kh32 = o;
-  o += 3 * LB_MAXLT * 4;
+  o += 4 * LB_MAXLT * 4;
   L.rows = o;
   o += (size_t)LB_TA * NROW32 * 4;
   L.ks = o;
@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* s = reinterpret_cast<double*>(smem_raw);
   EH32* e32 = reinterpret_cast<EH32*>(smem_raw + L.e32);
-  float* kh32 = reinterpret_cast<float*>(smem_raw + L.kh32);
+  float4* kh4 = reinterpret_cast<float4*>(smem_raw + L.kh32);
   float* rowsS = reinterpret_cast<float*>(smem_raw + L.rows);
   float* Ks = reinterpret_cast<float*>(smem_raw + L.ks);
   float* us = reinterpret_cast<float*>(smem_raw + L.us);
@@ -289,12 +289,14 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
   for (int i = tid; i < NSCAL; i += LB_THREADS) s[i] = it.ctab->s[i];
   for (int l = tid; l < lt; l += LB_THREADS) {
     const double e = ELL[l0 + l] + 0.5;
-    kh32[3 * l + 0] = (float)e;                               // k = kh / max(chi, 1)
-    kh32[3 * l + 1] = (float)(1.4426950408889634 * log(e));   // log2(kh)
-    kh32[3 * l + 2] = (float)(1.0 / e);                       // 1 / kh
+    // k = kh / max(chi, 1): kh, log2(kh), 1 / kh
+    kh4[l] = make_float4((float)e, (float)(1.4426950408889634 * log(e)), (float)(1.0 / e), 0.f);
   }
   __syncthreads();
   if (tid == 0) make_eh32(s, e32);
+  // (t, l) and (t, p) from flat indices without integer division: q < 32 * 136,
+  // so (q + 1/2) / n in float is off by far less than 1 / (2 n) of an integer
+  const float inv_lt = 1.f / (float)lt, inv_ncp = 1.f / (float)ncp;
   const float* rows32 = it.rows32;
   const double* rows64 = it.rows64;
   const double* kern = it.kern;
@@ -314,15 +316,16 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
     __syncthreads();
     // M_ij(a) = (K_i K_j) u_a, zero-padded to ncp spectra
     for (int q = tid; q < tc * ncp; q += LB_THREADS) {
-      const int t = q / ncp, p = q - t * ncp;
+      const int t = __float2int_rz(((float)q + 0.5f) * inv_ncp), p = q - t * ncp;
       float m = 0.f;
       if (p < n_cls) m = Ks[geo->pair_i[p] * LB_TA + t] * Ks[geo->pair_j[p] * LB_TA + t] * us[t];
       Ms[q] = m;
     }
     // P tile: nodes (t, l)
     for (int q = tid; q < tc * lt; q += LB_THREADS) {
-      const int t = q / lt, l = q - t * lt;
-      Pt[t * LT + l] = node32(*e32, rowsS + t * NROW32, kh32[3 * l], kh32[3 * l + 1], kh32[3 * l + 2]);
+      const int t = __float2int_rz(((float)q + 0.5f) * inv_lt), l = q - t * lt;
+      const float4 kk = kh4[l];
+      Pt[t * LT + l] = node32(*e32, rowsS + t * NROW32, kk.x, kk.y, kk.z);
     }
     __syncthreads();
 #pragma unroll
