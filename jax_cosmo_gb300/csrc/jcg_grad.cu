@@ -52,20 +52,11 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
   double* pq = qr;                            // [NDIR+1][NKH], after the growth RK4
   const int t = threadIdx.x, dir = t & 7, it = t >> 3;
   const GradItem gi = grad_item(gb, item);
-  const double* P = gi.params;
   TabD* out = gi.tab;
   // the chi and growth tables go straight to the output (read back after a barrier)
-  // scalars (lanes 0-7 of warp 0)
-  if (t < NDIR) {
-    D1 p[8];
-    for (int i = 0; i < 8; ++i) p[i] = mk1(P[i], i == dir ? 1.0 : 0.0);
-    D1 s[NSCAL];
-    cosmo_scalarsT(p, s);
-    for (int i = 0; i < NSCAL; ++i) {
-      if (dir == 0) sv[i] = s[i].v;
-      sd[dir * NSCAL + i] = s[i].d[0];
-    }
-  }
+  // scalars and their tangents (from grad_scalars_kernel)
+  for (int i = t; i < NSCAL; i += blockDim.x) sv[i] = out->sv[i];
+  for (int i = t; i < NDIR * NSCAL; i += blockDim.x) sd[i] = out->sd[i / NSCAL][i % NSCAL];
   __syncthreads();
   D1 sD[NSCAL];
   for (int i = 0; i < NSCAL; ++i) sD[i] = mk1(sv[i], sd[dir * NSCAL + i]);
@@ -1380,8 +1371,26 @@ int grad_limber_tile(int n_ell, int n_cls) {
   return (n_ell + tiles - 1) / tiles;
 }
 
+// Scalars with tangents, one thread per (cosmology, direction): the Dual<1>
+// chain of pow / log / sqrt with all lanes of a warp busy.
+__global__ void __launch_bounds__(128) grad_scalars_kernel(GradBatch gb) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int item = idx / NDIR, dir = idx % NDIR;
+  if (item >= gb.n_items) return;
+  const GradItem gi = grad_item(gb, item);
+  D1 p[8];
+  for (int i = 0; i < 8; ++i) p[i] = mk1(gi.params[i], i == dir ? 1.0 : 0.0);
+  D1 s[NSCAL];
+  cosmo_scalarsT(p, s);
+  for (int i = 0; i < NSCAL; ++i) {
+    if (dir == 0) gi.tab->sv[i] = s[i].v;
+    gi.tab->sd[dir][i] = s[i].d[0];
+  }
+}
+
 void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
   const size_t smt = grad_tables_smem();
+  grad_scalars_kernel<<<(gb.n_items * NDIR + 127) / 128, 128, 0, st>>>(gb);
   if (gb.precision == JCG_FP32C) {
     cudaFuncSetAttribute(grad_tables_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
     grad_tables_kernel<true><<<gb.n_items, 128, smt, st>>>(gb, c);

@@ -225,7 +225,10 @@ __device__ __forceinline__ double chi_at(const CosmoTab* ct, const ConstTables* 
 }
 
 constexpr int HF_WARPS = 8;
-constexpr int HF_NODES_PER_BLOCK = 64;
+// Limber nodes per CTA: the fp32c rows keep every thread busy in the
+// thread-per-node phases (256 nodes); the float64 rows, whose warp-per-node
+// moments dominate, use 64
+__host__ __device__ constexpr int hf_nodes_per_block(bool fast) { return fast ? 256 : 64; }
 
 // Root find of one node by one thread: c = #{j : sig_j g2 > 1} by bisection
 // (the sequence is strictly decreasing), then the argmin among c - 1, c with
@@ -275,9 +278,9 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   const Item it = batch_item(bt, item);
   const GeoHeader* geo = it.geo;
   const int na = geo->na;
-  const int n0 = blockIdx.x * HF_NODES_PER_BLOCK;
+  const int n0 = blockIdx.x * hf_nodes_per_block(FAST);
   if (n0 >= na) return;
-  constexpr int NB = HF_NODES_PER_BLOCK;
+  constexpr int NB = hf_nodes_per_block(FAST);
   __shared__ double sig[NRT];
   __shared__ double pk3[FAST ? 1 : NKH];
   __shared__ double s[NSCAL];
@@ -468,7 +471,8 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
 }
 
 void launch_halofit_rows(const Batch& b, const ConstTables* c, cudaStream_t st) {
-  dim3 grid((b.max_na + HF_NODES_PER_BLOCK - 1) / HF_NODES_PER_BLOCK, b.n_items);
+  const int nb = hf_nodes_per_block(b.precision == JCG_FP32C);
+  dim3 grid((b.max_na + nb - 1) / nb, b.n_items);
   if (b.precision == JCG_FP32C)
     halofit_rows_kernel<true><<<grid, HF_WARPS * 32, 0, st>>>(b, c);
   else

@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   __shared__ double mv[4 * NGROW];  // per-step growth matrices
   __shared__ float2 wpp[NKH];       // fp32c: w pk3 as float pairs
   const int t = threadIdx.x;
-  if (t == 0) cosmo_scalars(it.params, s);
+  for (int i = t; i < NSCAL; i += blockDim.x) s[i] = it.ctab->s[i];  // from cosmo_scalars_kernel
   __syncthreads();
   const Bg bg = make_bg(s);
   // chi RK4 in ln a (background.py:227-231, scipy/ode.py:11-19): the
@@ -522,7 +522,20 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   for (int i = t; i < NKH; i += blockDim.x) out->pk3[i] = pk3[i];
 }
 
+// The scalars, one thread per cosmology: their float64 chain of pow / log /
+// sqrt runs with all 32 lanes of a warp busy (on one lane of the table
+// kernel it would hold the float64 pipe as long as a full warp would).
+__global__ void __launch_bounds__(128) cosmo_scalars_kernel(Batch bt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= bt.n_items) return;
+  const Item it = batch_item(bt, i);
+  double sv[NSCAL];
+  cosmo_scalars(it.params, sv);
+  for (int k = 0; k < NSCAL; ++k) it.ctab->s[k] = sv[k];
+}
+
 void launch_cosmo_tables(const Batch& b, const ConstTables* c, cudaStream_t st) {
+  cosmo_scalars_kernel<<<(b.n_items + 127) / 128, 128, 0, st>>>(b);
   cosmo_tables_kernel<<<b.n_items, 256, 0, st>>>(b, c);
 }
 
