@@ -214,13 +214,26 @@ __global__ void __launch_bounds__(256)
     const float* Wr[NW];
 #pragma unroll
     for (int u = 0; u < NW; ++u) Wr[u] = geo_ptr<float>(geo, geo->off_W32[wl_t[u]]) + row;
-    for (int j = 0; j < NZP; ++j) {
-      const int q = Q32b[row + j];
-      const float chip = fmaxf(
-          chiT[(q & 0xffff) * TU_PAD + lane] + slT[(q >> 16) * TU_PAD + lane] * DX32b[row + j], 0.f);
-      const float ratio = fmaxf(chip - chi_wl, 0.f) * rcp_approx(fmaxf(chip, 1.f));
+    // the node's lensing grid in chunks of 32 z' points: one coalesced load
+    // per lane, then broadcast point by point with shuffles (same order of
+    // accumulation as a plain loop over j)
+    for (int j0 = 0; j0 < NZP; j0 += 32) {
+      const int jl = j0 + lane;
+      const bool in = jl < NZP;
+      const int qv = in ? Q32b[row + jl] : 0;
+      const float dxv = in ? DX32b[row + jl] : 0.f;
+      float wv[NW];
 #pragma unroll
-      for (int u = 0; u < NW; ++u) acc[u] += Wr[u][j] * ratio;
+      for (int u = 0; u < NW; ++u) wv[u] = in ? Wr[u][jl] : 0.f;
+      const int cnt = min(32, NZP - j0);
+      for (int jj = 0; jj < cnt; ++jj) {
+        const int q = __shfl_sync(0xffffffffu, qv, jj);
+        const float dx = __shfl_sync(0xffffffffu, dxv, jj);
+        const float chip = fmaxf(chiT[(q & 0xffff) * TU_PAD + lane] + slT[(q >> 16) * TU_PAD + lane] * dx, 0.f);
+        const float ratio = fmaxf(chip - chi_wl, 0.f) * rcp_approx(fmaxf(chip, 1.f));
+#pragma unroll
+        for (int u = 0; u < NW; ++u) acc[u] += __shfl_sync(0xffffffffu, wv[u], jj) * ratio;
+      }
     }
     if (live) {
       const double z = Z[n];
