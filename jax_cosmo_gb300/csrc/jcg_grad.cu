@@ -17,6 +17,7 @@
 
 #include <vector>
 
+#include "jcg_fp32.cuh"
 #include "jcg_grad.cuh"
 
 namespace jcg {
@@ -395,34 +396,44 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
   }
   __syncthreads();
   if (F32T && gi.ptt) {
-    // Taylor prefix tables of the fp32c moments.  Values (FP64, warp 0, the
-    // forward's tables): P_m[i] = sum_{k < i} w_k q3_k kh_k^(2(m+1)).  Tangents
-    // (FP32, one thread per (m, d)), scaled to the table row so that no power
-    // of k overflows: Q_m[i] = sum_{k < i} w_k dq3_k (kh_k / kh_i)^(2(m+1)),
-    // kh_i = exp(ln 1e-4 + i dlnk), by the contracting recurrence
-    // Q_m[i+1] = (Q_m[i] + w_i dq3_i) (kh_i / kh_{i+1})^(2(m+1)).
-    const int warp = t >> 5, lane = t & 31;
-    double* pv = gi.ptt;
+    // Taylor tables of the fp32c moments, scaled to the table row so that no
+    // power of k overflows.  Values: float pairs R_m[i] = c_m Q_m[i],
+    // c_m = (-1)^m / m!, Q_m[i] = sum_{k < i} w_k q3_k (kh_k / kh_i)^(2(m+1))
+    // (one lane per m); tangents (FP32, one thread per (m, d)):
+    // sum_{k < i} w_k dq3_k (kh_k / kh_i)^(2(m+1)).  Both by the contracting
+    // recurrence Q_m[i+1] = (Q_m[i] + w_i q3_i) (kh_i / kh_{i+1})^(2(m+1)),
+    // kh_i = exp(ln 1e-4 + i dlnk).
+    float2* pv = reinterpret_cast<float2*>(gi.ptt);  // [NKH + 1][NTAYLOR]
     float* pdv = ptt_tangents(gi.ptt);
     float* pqw = reinterpret_cast<float*>(fn);  // [NKH][NDIR] w dq3, fn is free here
+    float2* wpp = reinterpret_cast<float2*>(fm);  // [NKH] w q3 as float pairs, fm is free here
     for (int e = t; e < NDIR * NKH; e += blockDim.x) {
       const int d = e / NKH, i = e % NKH;
       pqw[i * NDIR + d] = (float)(c->simpson_kh[i] * pq[(1 + d) * NKH + i]);
     }
+    for (int i = t; i < NKH + 15; i += blockDim.x) {
+      float hi = 0.f;
+      if (i < NKH) {
+        const FF w = ff_of(c->simpson_kh[i] * pq[i]);
+        wpp[i] = make_float2(w.hi, w.lo);
+        hi = w.hi;
+      }
+      out->wq3f[i] = hi;
+    }
     __syncthreads();
-    if (t < NTAYLOR) pv[t] = 0.0;
-    for (int m = warp; m < NTAYLOR; m += 4) {
-      double carry = 0.0;
-      for (int base = 0; base < NKH; base += 32) {
-        const int i = base + lane;
-        double x = i < NKH ? c->kpw[m][i] * pq[i] : 0.0;
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-          const double u = __shfl_up_sync(0xffffffffu, x, o);
-          if (lane >= o) x += u;
-        }
-        if (i < NKH) pv[(size_t)(i + 1) * NTAYLOR + m] = carry + x;
-        carry += __shfl_sync(0xffffffffu, x, 31);
+    if (t < NTAYLOR) {
+      const int m = t;
+      FF rho, cm, q;
+      rho.hi = c->tay_rho[m][0], rho.lo = c->tay_rho[m][1];
+      cm.hi = c->tay_c[m][0], cm.lo = c->tay_c[m][1];
+      q.hi = 0.f, q.lo = 0.f;
+      pv[m] = make_float2(0.f, 0.f);
+      for (int i = 0; i < NKH; ++i) {
+        FF w;
+        w.hi = wpp[i].x, w.lo = wpp[i].y;
+        q = ff_mul(ff_add(q, w), rho);
+        const FF r = ff_mul(cm, q);
+        pv[(size_t)(i + 1) * NTAYLOR + m] = make_float2(r.hi, r.lo);
       }
     }
     for (int job = t; job < NTAYLOR * NDIR; job += blockDim.x) {
@@ -730,9 +741,6 @@ constexpr int GR32_THREADS = 64;
 __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
-  __shared__ double e2tab[64];
-  for (int i = threadIdx.x; i < 64; i += blockDim.x) e2tab[i] = kExp2Tab64[i];
-  __syncthreads();
   const GradItem gi = grad_item(gb, item);
   const GeoHeader* geo = gi.geo;
   const int na = geo->na;
@@ -790,28 +798,45 @@ __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb,
   row[F_LG2KNL] = (float)log2(knl.v);
   row[F_INVKNL] = (float)(1.0 / knl.v);
   put_t(T_KNL, knl, 1.f);
-  // moments
-  const double Rv = inv.v, iR = 1.0 / Rv, linv = log(Rv);
-  int ilo = (int)floor((0.5 * log(Y2_TAYLOR) - linv - LOG_KMIN) / DLOGK);
-  int ihi = (int)ceil((0.5 * log(Y2_SKIP) - linv - LOG_KMIN) / DLOGK);
+  // moments: the exp terms for y^2 in [Y2_TAYLOR, Y2_SKIP] in FP32 from a
+  // float-pair y^2 (values summed in float pairs), below Y2_TAYLOR the Taylor
+  // series from the float-pair tables (Horner with derivatives); the
+  // derivatives with respect to R and the tangents in FP32
+  const double Rv = inv.v;
+  const float iR = (float)(1.0 / Rv);
+  const float linv = LN2_F * lg2f((float)Rv);
+  constexpr float HLY2T = 0.0f, HLY2S = 2.0471425f;  // 0.5 log(Y2_TAYLOR), 0.5 log(Y2_SKIP)
+  int ilo = (int)floorf((HLY2T - linv - (float)LOG_KMIN) * (float)(1.0 / DLOGK));
+  int ihi = (int)ceilf((HLY2S - linv - (float)LOG_KMIN) * (float)(1.0 / DLOGK));
   ilo = max(0, min(ilo, NKH));
   ihi = max(ilo - 1, min(ihi, NKH - 1));
-  const double q3s = 1.0 / TWO_PI2_G;
-  double s1 = 0, s2 = 0, s1r = 0, s2r = 0;
+  const FF R2 = ff_of(Rv * Rv);
+  constexpr float Q3S = (float)(1.0 / TWO_PI2_G);
+  FF s1p, s2p;
+  s1p.hi = s1p.lo = s2p.hi = s2p.lo = 0.f;
+  float s1r = 0.f, s2r = 0.f;
   float s1d[NDIR], s2d[NDIR];
 #pragma unroll
   for (int d = 0; d < NDIR; ++d) s1d[d] = s2d[d] = 0.f;
   for (int i = ilo; i <= ihi; ++i) {
-    const double y = c->kh[i] * Rv;
-    const double y2 = y * y;
-    const double wq = c->simpson_kh[i] * exp_tang(-y2, e2tab) * q3s;
-    const double Av = wq * tb->pk3v[i];
-    const double c1 = 2.0 * y2, c2 = 4.0 * (y2 - y2 * y2);
-    s1 += Av * c1;
-    s2 += Av * c2;
-    s1r += 4.0 * Av * y2 * (1.0 - y2) * iR;
-    s2r += 8.0 * Av * y2 * (1.0 - 3.0 * y2 + y2 * y2) * iR;
-    const float w1 = (float)(wq * c1), w2 = (float)(wq * c2);
+    const float kh = c->kh2_hi[i];
+    const float pp = kh * R2.hi;
+    float ee = fmaf(kh, R2.hi, -pp);
+    ee = fmaf(kh, R2.lo, ee);
+    ee = fmaf(c->kh2_lo[i], R2.hi, ee);
+    const float ex = exp_neg_pair(pp, ee);
+    const float y2 = pp + ee, om = (1.f - pp) - ee;  // y^2, 1 - y^2
+    const float Av = tb->wq3f[i] * ex;
+    const float c1 = 2.f * y2, c2 = 4.f * y2 * om;
+    FF t;
+    t.hi = Av * c1, t.lo = 0.f;
+    s1p = ff_add(s1p, t);
+    t.hi = Av * c2;
+    s2p = ff_add(s2p, t);
+    s1r = fmaf(4.f * Av * y2 * om, iR, s1r);
+    s2r = fmaf(8.f * Av * y2 * (om - 2.f * y2 + y2 * y2), iR, s2r);
+    const float wq = c->simpson_f[i] * Q3S * ex;
+    const float w1 = wq * c1, w2 = wq * c2;
     const float4 pa = *reinterpret_cast<const float4*>(&tb->pk3df[i][0]);
     const float4 pb = *reinterpret_cast<const float4*>(&tb->pk3df[i][4]);
     const float p[NDIR] = {pa.x, pa.y, pa.z, pa.w, pb.x, pb.y, pb.z, pb.w};
@@ -821,26 +846,43 @@ __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb,
       s2d[d] = fmaf(w2, p[d], s2d[d]);
     }
   }
+  double s1 = ff_to_double(s1p), s2 = ff_to_double(s2p);
   float t1d[NDIR], t2d[NDIR];
 #pragma unroll
   for (int d = 0; d < NDIR; ++d) t1d[d] = t2d[d] = 0.f;
   if (ilo > 0) {
-    const double* T = gi.ptt + (size_t)ilo * NTAYLOR;
+    // x = y_ilo^2 = (kh_ilo R)^2, F(x) = sum_m R_m[ilo] x^m: t1 = x F,
+    // t2 = t1 + x^2 F', d/dR through dx/dR = 2 x / R
+    const float2* T = reinterpret_cast<const float2*>(gi.ptt) + (size_t)ilo * NTAYLOR;
     const float* TD = ptt_tangents(gi.ptt) + (size_t)ilo * NTAYLOR * NDIR;
-    const double R2 = Rv * Rv;
-    // tangent tables are scaled by kh_ilo^-(2(m+1)): powers of yl = R kh_ilo (<= ~1)
-    const double yl2 = R2 * exp(2.0 * (LOG_KMIN + ilo * DLOGK));
-    double pw = R2, dpw = 2.0 * Rv, fact = 1.0, ps = yl2;
-    double t1 = 0, t2 = 0, t1r = 0, t2r = 0;
+    FF kk;
+    kk.hi = c->kh2_hi[ilo], kk.lo = c->kh2_lo[ilo];
+    const FF x = ff_mul(kk, R2);
+    FF P, D;
+    P.hi = T[NTAYLOR - 1].x, P.lo = T[NTAYLOR - 1].y;
+    D.hi = D.lo = 0.f;
+    float pf = P.hi, df = 0.f, ddf = 0.f;
+    for (int m = NTAYLOR - 2; m >= 0; --m) {
+      D = ff_add(ff_mul(D, x), P);
+      FF r;
+      r.hi = T[m].x, r.lo = T[m].y;
+      P = ff_add(ff_mul(P, x), r);
+      ddf = fmaf(ddf, x.hi, df);
+      df = fmaf(df, x.hi, pf);
+      pf = fmaf(pf, x.hi, r.hi);
+    }
+    const FF f1 = ff_mul(x, P);
+    const double t1 = ff_to_double(f1);
+    const double t2 = t1 + ff_to_double(ff_mul(ff_mul(x, x), D));
+    const float xs = x.hi, dxr = 2.f * xs * iR;
+    const float t1r = (pf + xs * df) * dxr;
+    const float t2r = (pf + 3.f * xs * df + xs * xs * (2.f * ddf)) * dxr;
+    // tangent tables are scaled by kh_ilo^-(2(m+1)): powers of x
+    float ps = xs;
     for (int m = 0; m < NTAYLOR - 1; ++m) {
-      const double sg = ((m & 1) ? -1.0 : 1.0) / fact;
-      const double pw1 = pw * R2, dpw1 = dpw * R2 + pw * 2.0 * Rv;
-      const double ps1 = ps * yl2;
-      t1 += sg * T[m] * pw;
-      t2 += sg * (T[m] * pw - T[m + 1] * pw1);
-      t1r += sg * T[m] * dpw;
-      t2r += sg * (T[m] * dpw - T[m + 1] * dpw1);
-      const float a1 = (float)(sg * ps), a2 = (float)(sg * ps1);
+      const float sg = c->tay_c[m][0];
+      const float ps1 = ps * xs;
+      const float a1 = sg * ps, a2 = sg * ps1;
       ps = ps1;
       const float4 u0 = *reinterpret_cast<const float4*>(TD + m * NDIR);
       const float4 u1 = *reinterpret_cast<const float4*>(TD + m * NDIR + 4);
@@ -853,19 +895,16 @@ __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb,
         t1d[d] = fmaf(a1, dm[d], t1d[d]);
         t2d[d] = fmaf(a1, dm[d], fmaf(-a2, dm1[d], t2d[d]));
       }
-      pw = pw1;
-      dpw = dpw1;
-      fact *= (double)(m + 1);
     }
     s1 += 2.0 * t1;
     s2 += 4.0 * t2;
-    s1r += 2.0 * t1r;
-    s2r += 4.0 * t2r;
+    s1r += 2.f * t1r;
+    s2r += 4.f * t2r;
   }
   F8 S1, S2;
   S1.v = s1;
   S2.v = s2;
-  const float f1r = (float)s1r, f2r = (float)s2r;
+  const float f1r = s1r, f2r = s2r;
 #pragma unroll
   for (int d = 0; d < NDIR; ++d) {
     S1.d[d] = s1d[d] + 2.f * t1d[d] + f1r * inv.d[d];

@@ -50,6 +50,7 @@ struct TabD {
   float s32[NDIR + 1][NCHI];   // segment slopes (chi[i+1] - chi[i]) / (a[i+1] - a[i]) and tangents
   float pk3df[NKH][NDIR];      // P(k) k^3 tangents, node-major
   float padf[8];
+  float wq3f[NKH + 15];        // simpson_kh[i] * P(k_i) k_i^3 / (2 pi^2), float; padded to 64 bytes
 };
 static_assert(sizeof(TabD) % 64 == 0, "TabD alignment");
 
@@ -69,8 +70,9 @@ __device__ __constant__ const int kNodeCScalar[NC_IN] = {S_K_EQ,  S_SH_D,      S
 enum GTan { T_CHIC = 0, T_D2FAC, T_KNL, T_BETAN, T_ALPHAN, T_AN, T_3F1, T_F2, T_BN, T_LG2CF3, T_3MG,
             T_NUN, T_U, NGT };
 constexpr int F_U = 15;
-// Taylor prefix tables of the fp32c moments, per cosmology: values double
-// [NKH + 1][NTAYLOR], then tangents float [NKH + 1][NTAYLOR][NDIR]
+// Taylor tables of the fp32c moments, per cosmology: values as float pairs
+// [NKH + 1][NTAYLOR] (in the first NPTTV doubles), then tangents float
+// [NKH + 1][NTAYLOR][NDIR]
 constexpr int NPTTV = (NKH + 1) * NTAYLOR;
 constexpr size_t PTT_STRIDE = ((size_t)NPTTV * 8 + (size_t)NPTTV * NDIR * 4 + 255) / 256 * 256 / 8;  // doubles
 __device__ __forceinline__ float* ptt_tangents(double* p) { return reinterpret_cast<float*>(p + NPTTV); }

@@ -76,6 +76,7 @@ struct ConstTables {
   // fp32c halofit moments: kh[i]^2 as a float pair hi + lo, with a virtual
   // node kh[NKH] = kh[NKH - 1] e^dlnk; the Taylor tables' factors
   // rho_m = e^(-2 (m + 1) dlnk) and c_m = (-1)^m / m! as float pairs
+  float simpson_f[NKH];      // simpson_kh, float
   float kh2_hi[NKH + 1];
   float kh2_lo[NKH + 1];
   float tay_rho[NTAYLOR][2];

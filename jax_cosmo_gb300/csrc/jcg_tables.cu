@@ -62,6 +62,7 @@ __global__ void const_init_kernel(ConstTables* c) {
     const double w = (i == 0 || i == NKH - 1) ? 1.0 : ((i & 1) ? 4.0 : 2.0);
     const double sw = dxk / 3 * w;
     c->simpson_kh[i] = sw;
+    c->simpson_f[i] = (float)sw;
     const double k2 = k * k;
     c->kh2_hi[i] = (float)k2;
     c->kh2_lo[i] = (float)(k2 - (double)(float)k2);
