@@ -52,22 +52,27 @@ BOX = {
     "w0": (-1.3, -0.7),
 }
 ORDER = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
-MUFU_PER_NODE = 27  # ex2/lg2/rcp/sin per Limber node in the fp32c integrand (node32)
 # Per-cosmology figures of the fp32c step's kernels on this workload (na = 513
 # Limber nodes, 5 WL tracers, 100 ell), from one ncu capture at 512
-# cosmologies (profiles/: fp32c_step_kernels_b512.md), divided by 512:
-#   FP64 operations = DFMA x 2 + DADD + DMUL thread instructions;
-#   traffic = dram__bytes_read.sum + dram__bytes_write.sum.
-FP64_OPS = {"cosmo_tables": 707_012, "halofit_rows": 1_012_985}
-TRAFFIC_PER_COSMO = {"cosmo_tables": 1_627, "halofit_rows": 45_078, "limber": 122_084}
+# cosmologies (profiles/fp32c_step_kernels_b512.md), divided by 512:
+#   FP64 operations = DFMA x 2 + DADD + DMUL thread instructions (the
+#     cosmo_tables stage is cosmo_scalars_kernel + cosmo_tables_kernel);
+#   traffic = dram__bytes_read.sum + dram__bytes_write.sum;
+#   per Limber node (512 x 100 x 513 nodes): XU (MUFU) thread operations and
+#     warp instructions issued (sm__inst_executed) of limber32_kernel.
+FP64_OPS = {"cosmo_tables": 350_440, "halofit_rows": 83_620}
+TRAFFIC_PER_COSMO = {"cosmo_tables": 1_964, "halofit_rows": 44_141, "tracer_kernels": 9_679, "limber": 123_554}
+MUFU_PER_NODE = 31
+WARP_INSTR_PER_NODE = 9.279
 # algorithmic bytes per cosmology: what each kernel must read and write once
-#   cosmo_tables: 8 parameters in, the CosmoTab record out (52,864 B)
+#   cosmo_tables: 8 parameters in, the CosmoTab record out (53,952 B)
 #   halofit_rows: the CosmoTab record in, FP64 + FP32 rows out (513 x (24 x 8 + 16 x 4))
 #   limber: FP32 rows (16 x 4) + u (8) + 5 radial kernels (5 x 8) per node in, 15 x 100 C_ell out
-ALG_BYTES = {"cosmo_tables": 64 + 52_864, "halofit_rows": 52_864 + 513 * (24 * 8 + 16 * 4),
+ALG_BYTES = {"cosmo_tables": 64 + 53_952, "halofit_rows": 53_952 + 513 * (24 * 8 + 16 * 4),
              "limber": 513 * (16 * 4 + 8) + 5 * 513 * 8 + 15 * N_ELL * 8}
-KERNEL_NAMES = {"cosmo_tables": "cosmo_tables_kernel", "halofit_rows": "halofit_rows_kernel<fp32c>",
-                "tracer_kernels": "tracer32_uniform_kernel<5>", "limber": "limber_kernel<fp32c>"}
+KERNEL_NAMES = {"cosmo_tables": "cosmo_scalars_kernel + cosmo_tables_kernel",
+                "halofit_rows": "halofit_rows_kernel<fp32c>",
+                "tracer_kernels": "tracer32_uniform_kernel<5>", "limber": "limber32_kernel<1>"}
 
 
 def draw_params(B, seed=SEED):
@@ -475,13 +480,21 @@ def rooflines(res, B, live):
             e.update({"bound": "fp64", "achieved": ach, "peak": live["fp64_tflops"], "unit": "TFLOP/s",
                       "frac": ach / live["fp64_tflops"], "peak_source": "measured live (calibration kernel)"})
         elif k == "limber":
+            # issue-bound: every pipe below half busy, 66% of cycles issue
             nodes = B * N_ELL * 513
-            ach = nodes * MUFU_PER_NODE / t
-            e.update({"bound": "sfu", "achieved": ach / 1e9, "peak": live["mufu_per_s"] / 1e9, "unit": "GMUFU/s",
-                      "frac": ach / live["mufu_per_s"], "mufu_per_node": MUFU_PER_NODE,
-                      "peak_source": "measured live (calibration kernel)"})
+            mhz = (res.get("clocks") or {}).get("sm_mhz") or 2070.0
+            peak_issue = 4 * res.get("sm_count", 152) * mhz * 1e6
+            ach = nodes * WARP_INSTR_PER_NODE / t
+            mufu = nodes * MUFU_PER_NODE / t
+            e.update({"bound": "issue", "achieved": ach / 1e9, "peak": peak_issue / 1e9, "unit": "Gwarp-instr/s",
+                      "frac": ach / peak_issue, "warp_instr_per_node": WARP_INSTR_PER_NODE,
+                      "peak_source": "4 warp instructions per SM per clock x SMs x sampled SM clock",
+                      "sfu": {"achieved_gmufu_s": mufu / 1e9, "peak_gmufu_s": live["mufu_per_s"] / 1e9,
+                              "frac": mufu / live["mufu_per_s"], "mufu_per_node": MUFU_PER_NODE,
+                              "peak_source": "measured live (calibration kernel)"}})
         else:
-            e.update({"bound": "latency", "note": "FP32 lensing integral, lanes over cosmologies"})
+            e.update({"bound": "lsu", "note": "FP32 lensing integral, lanes over cosmologies; z' grid broadcast "
+                                              "by shuffles (LSU pipe 54% busy at 512 cosmologies)"})
         out[k] = e
     dom = max(stages, key=lambda k: stages[k])
     return dom, out
