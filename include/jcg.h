@@ -266,6 +266,10 @@ int jcg_workspace_read(const jcg_geometry* g, int n_cosmo, int precision, const 
  *   5 linear_matter_power(k, a)     power.py:21-53
  *   6 nonlinear_matter_power(k, a)  power.py:265-272 (halofit)
  *   7 k_nl(a)  8 n_eff(a)  9 C(a)   power.py:86-141
+ *  10 transverse_comoving_distance(a)  background.py:297-344
+ *  11 angular_diameter_distance(a)     background.py:347-368
+ *  12 a_of_chi(chi), chi in a_dev      background.py:245-267
+ *  13 growth_rate(a)                   background.py:401-440 (ODE growth) 
  * Needs a workspace of jcg_workspace_size(g=NULL -> tables only). */
 int jcg_eval_points(const double* params_dev, int n_cosmo, const double* a_dev,
                     const double* k_dev, int n, int what, double* out_dev, void* workspace,

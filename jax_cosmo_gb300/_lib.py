@@ -45,6 +45,7 @@ FP32C = 1
 
 EVAL_CHI, EVAL_GROWTH, EVAL_H, EVAL_DCHI, EVAL_TRANSFER, EVAL_PLIN, EVAL_PNL = range(7)
 EVAL_KNL, EVAL_NEFF, EVAL_C = 7, 8, 9
+EVAL_TRANSVERSE, EVAL_DA, EVAL_A_OF_CHI, EVAL_GROWTH_RATE = 10, 11, 12, 13
 
 REQ_CL, REQ_JACOBIAN, REQ_LOGLIKE_GRAD = 0, 1, 2
 MAX_REQUESTS = 65536

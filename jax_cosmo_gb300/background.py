@@ -1,8 +1,9 @@
-"""Background cosmology (jax_cosmo/background.py:25-294, 371-488).
+"""Background cosmology (jax_cosmo/background.py:25-512).
 
-``radial_comoving_distance``, ``growth_factor``, ``H`` and ``dchioverda`` run in
-libjcg (FP64 RK4 tables on the reference's grids, then the reference's
-interpolation rule).  The closed forms ``w``, ``f_de``, ``Esqr``, ``Omega_m_a``,
+``radial_comoving_distance``, ``a_of_chi``, ``transverse_comoving_distance``,
+``angular_diameter_distance``, ``growth_factor``, ``growth_rate``, ``H`` and
+``dchioverda`` run in libjcg (FP64 RK4 tables on the reference's grids, then
+the reference's interpolation rule).  The closed forms ``w``, ``f_de``, ``Esqr``, ``Omega_m_a``,
 ``Omega_de_a`` are one-line expressions evaluated with torch on the parameters'
 device; the accelerated path evaluates them inside its kernels.
 """
@@ -13,7 +14,8 @@ import torch
 from jax_cosmo_gb300 import _lib, _points
 
 __all__ = ["w", "f_de", "Esqr", "H", "Omega_m_a", "Omega_de_a", "radial_comoving_distance",
-           "dchioverda", "growth_factor"]
+           "a_of_chi", "dchioverda", "transverse_comoving_distance", "angular_diameter_distance",
+           "growth_factor", "growth_rate"]
 
 
 def _a(a):
@@ -72,3 +74,27 @@ def growth_factor(cosmo, a):
     if cosmo._flags.get("gamma_growth"):
         raise NotImplementedError("gamma growth (background.py:515-582) is not accelerated")
     return _points.evaluate(cosmo, _lib.EVAL_GROWTH, a=a)
+
+
+def a_of_chi(cosmo, chi):
+    """Scale factor at radial comoving distance chi [Mpc/h], by the reference's
+    interpolation of the chi table (background.py:245-267)."""
+    return _points.evaluate(cosmo, _lib.EVAL_A_OF_CHI, a=chi)
+
+
+def transverse_comoving_distance(cosmo, a):
+    """f_k(a) [Mpc/h]: chi for Omega_k = 0, R_H / sqrt|Omega_k| sinh / sin of
+    sqrt|Omega_k| chi / R_H for open / closed universes (background.py:297-344)."""
+    return _points.evaluate(cosmo, _lib.EVAL_TRANSVERSE, a=a)
+
+
+def angular_diameter_distance(cosmo, a):
+    """d_A(a) = a f_k(a) [Mpc/h] (background.py:347-368)."""
+    return _points.evaluate(cosmo, _lib.EVAL_DA, a=a)
+
+
+def growth_rate(cosmo, a):
+    """Growth rate dlnD/dlna from the growth ODE table (background.py:401-440, 491-512)."""
+    if cosmo._flags.get("gamma_growth"):
+        raise NotImplementedError("gamma growth (background.py:515-582) is not accelerated")
+    return _points.evaluate(cosmo, _lib.EVAL_GROWTH_RATE, a=a)

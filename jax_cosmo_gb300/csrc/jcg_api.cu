@@ -498,8 +498,8 @@ int jcg_eval_points(const double* params, int n_cosmo, const double* a, const do
   int rc = check_common(params, n_cosmo, JCG_FP64, ws, ws_bytes, ws_layout(nullptr, n_cosmo, JCG_FP64).total);
   if (rc) return rc;
   if (n < 1) return fail(JCG_ERR_SHAPE, "n = %d", n);
-  if (what < 0 || what > 9) return fail(JCG_ERR_ARG, "what = %d", what);
-  const bool need_a = (what <= 3) || what >= 5;
+  if (what < 0 || what > 13) return fail(JCG_ERR_ARG, "what = %d", what);
+  const bool need_a = (what <= 3) || what >= 5;  // a_of_chi (12) takes chi in a_dev
   const bool need_k = (what >= 4 && what <= 6);
   if ((need_a && !a) || (need_k && !k) || !out) return fail(JCG_ERR_ARG, "NULL input or output");
   ConstTables* c;

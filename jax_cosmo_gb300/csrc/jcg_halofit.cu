@@ -480,6 +480,31 @@ void launch_halofit_rows(const Batch& b, const ConstTables* c, cudaStream_t st) 
 }
 
 // ------------------------------------------------------ pointwise queries ---
+// interp(x, xp, fp) of scipy/interpolate.py:12-37 for any table, by a warp:
+// the nearest node by argmin (x - xp)^2 (first index on ties), clipped to
+// [1, n - 2], then the segment on the side of sign(clip(x, xp[1], xp[-2]) - xp[ind])
+// with clip = min(max(x, lo), hi) and sign 0 taken as +1.
+__device__ double interp_ref_warp(double x, const double* xp, const double* fp, int n, int lane) {
+  double best = INFINITY;
+  int bi = n;
+  for (int j = lane; j < n; j += 32) {
+    const double d = (x - xp[j]) * (x - xp[j]);
+    if (d < best) best = d, bi = j;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const double ob = __shfl_xor_sync(0xffffffffu, best, o);
+    const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+    if (ob < best || (ob == best && oi < bi)) best = ob, bi = oi;
+  }
+  const int ind = bi < 1 ? 1 : (bi > n - 2 ? n - 2 : bi);
+  const double xc = fmin(fmax(x, xp[1]), xp[n - 2]);
+  const int j2 = ind + ((xc - xp[ind] < 0.0) ? -1 : 1);
+  const double sl = (fp[j2] - fp[ind]) / (xp[j2] - xp[ind]);
+  const double b = fp[ind] - sl * xp[ind];
+  return sl * x + b;
+}
+
 // One warp per (cosmology, point).  `what` as documented in jcg.h.  FP64, the
 // full (reference) form of the moments.
 __global__ void eval_points_kernel(const double* __restrict__ params, int n_cosmo,
@@ -501,9 +526,28 @@ __global__ void eval_points_kernel(const double* __restrict__ params, int n_cosm
     const int2 sg = interp_segment_inc(x, c->atab_grow, NGROW, logspace_guess(x, NGROW));
     return clip_lohi(interp_eval(x, c->atab_grow, ct->g, sg), 0.0, 1.0);
   };
+  auto chi_of = [&](double x) {
+    const int2 sg = interp_segment_inc(x, c->atab_chi, NCHI, logspace_guess(x, NCHI));
+    return fmax(interp_eval(x, c->atab_chi, ct->chi, sg), 0.0);
+  };
   if (what == 0) {
-    const int2 sg = interp_segment_inc(a, c->atab_chi, NCHI, logspace_guess(a, NCHI));
-    v = fmax(interp_eval(a, c->atab_chi, ct->chi, sg), 0.0);
+    v = chi_of(a);
+  } else if (what == 10 || what == 11) {
+    // transverse_comoving_distance (background.py:297-344): k = -sign(Omega_k)
+    const double chi = chi_of(a), ok = s[S_OMEGA_K];
+    const double sk = sqrt(fabs(ok));
+    double fk = chi;
+    if (ok > 0.0) fk = RH / sk * sinh(sk * chi / RH);
+    else if (ok < 0.0) fk = RH / sk * sin(sk * chi / RH);
+    v = what == 10 ? fk : a * fk;  // angular_diameter_distance = a f_k (background.py:347-368)
+  } else if (what == 12) {
+    // a_of_chi (background.py:245-267): interp(chi, chi table, a table) with the
+    // reference's rule on the decreasing chi table
+    v = interp_ref_warp(a, ct->chi, c->atab_chi, NCHI, lane);
+  } else if (what == 13) {
+    // growth_rate (background.py:401-440, 491-512): interp(a, atab, ftab), no clip
+    const int2 sg = interp_segment_inc(a, c->atab_grow, NGROW, logspace_guess(a, NGROW));
+    v = interp_eval(a, c->atab_grow, ct->f, sg);
   } else if (what == 1) {
     v = growth(a);
   } else if (what == 2) {

@@ -114,6 +114,7 @@ struct CosmoTab {
   double s[NSCAL];
   double chi[NCHI];    // background.py:231-233  chi table on atab_chi
   double g[NGROW];     // background.py:483      growth table on atab_grow
+  double f[NGROW];     // background.py:485      growth rate dlnD/dlna on atab_grow
   double sig[NRT];     // sigma^2(R_j) at a = 1 without the g(a)^2 factor
   double pk3[NKH];     // linear_matter_power(k_i, a=1) * k_i^3
   double chi_slope[NCHI];  // slope of the chi table on segment [k, k+1] (k < 255)

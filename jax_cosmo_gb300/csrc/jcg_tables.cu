@@ -389,6 +389,7 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   __shared__ double chis[NCHI];
   __shared__ double gs[NGROW];
   __shared__ double mv[4 * NGROW];  // per-step growth matrices
+  __shared__ double yv[2 * NGROW];  // growth ODE solution (D, dD/da) unnormalised
   __shared__ float2 wpp[NKH];       // fp32c: w pk3 as float pairs
   const int t = threadIdx.x;
   for (int i = t; i < NSCAL; i += blockDim.x) s[i] = it.ctab->s[i];  // from cosmo_scalars_kernel
@@ -449,8 +450,14 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   __syncthreads();
   if (warp == 1) {
     double d4[4];
-    const double yf = growth_scan_warp(mv, c->atab_grow[0], 1.0, lane, d4, nullptr);
-    for (int k = 0; k < 4; ++k) gs[lane * 4 + k] = d4[k] / yf;
+    const double yf = growth_scan_warp(mv, c->atab_grow[0], 1.0, lane, d4, yv);
+    for (int k = 0; k < 4; ++k) {
+      const int i = lane * 4 + k;
+      const double g = d4[k] / yf;
+      gs[i] = g;
+      // dlnD/dlna = a / D dD/da (background.py:484-485)
+      it.ctab->f[i] = yv[2 * i + 1] / yf * c->atab_grow[i] / g;
+    }
   }
   __syncthreads();
   if (t == 0) {

@@ -266,7 +266,10 @@ def growth_table(c, log10_amin=-3, steps=128):
         y = odeint_rk4(D_derivs, y0, atab)
         y1 = y[:, 0]
         gtab = y1 / y1[-1]
+        # dlnD/dlna = a / D dD/da (background.py:484-485)
+        ftab = y[:, 1] / y1[-1] * atab / gtab
         c.cache[key] = (atab, gtab)
+        c.cache[("growth_rate",) + key[1:]] = (atab, ftab)
     return c.cache[key]
 
 
@@ -275,6 +278,40 @@ def growth_factor(c, a):
     atab, gtab = growth_table(c)
     a = torch.atleast_1d(_t(a) if not isinstance(a, torch.Tensor) else a)
     return clip(interp(a, atab, gtab), 0.0, 1.0)
+
+
+def growth_rate(c, a):
+    """background.py:401-440, 491-512: interp(a, atab, ftab) of the ODE growth, no clip."""
+    growth_table(c)
+    atab, ftab = c.cache[("growth_rate", -3, 128)]
+    a = torch.atleast_1d(_t(a) if not isinstance(a, torch.Tensor) else a)
+    return interp(a, atab, ftab)
+
+
+def a_of_chi(c, chi):
+    """background.py:245-267: interp(chi, chi table, a table) (the decreasing chi table)."""
+    atab, chitab = chi_table(c)
+    chi = torch.atleast_1d(_t(chi) if not isinstance(chi, torch.Tensor) else chi)
+    return interp(chi, chitab, atab)
+
+
+def transverse_comoving_distance(c, a):
+    """background.py:297-344: branch by k = -sign(Omega_k) (core.py:169-174)."""
+    chi = radial_comoving_distance(c, a)
+    ok = c.Omega_k
+    ok_v = float(ok.detach()) if isinstance(ok, torch.Tensor) else float(ok)
+    if ok_v == 0.0:
+        return chi
+    sk = torch.sqrt(torch.abs(_t(ok) if not isinstance(ok, torch.Tensor) else ok))
+    if ok_v > 0.0:
+        return RH / sk * torch.sinh(sk * chi / RH)
+    return RH / sk * torch.sin(sk * chi / RH)
+
+
+def angular_diameter_distance(c, a):
+    """background.py:347-368: a f_k(a)."""
+    a_t = torch.atleast_1d(_t(a) if not isinstance(a, torch.Tensor) else a)
+    return a_t * transverse_comoving_distance(c, a_t)
 
 
 # ---------------------------------------------------------------- transfer ----

@@ -23,6 +23,8 @@ cl_ia.npz       angular_cl with NLA intrinsic alignment (des_y1, constant and
                 groups, NumberCounts with inverse-growth and constant biases
 cl_nz.npz       angular_cl with fu_nz, kde_nz (a seeded 200-galaxy catalog, stored
                 with the fixture) and systematic_shift(smail_nz) bins
+background2.npz transverse / angular diameter distances (Omega_k = 0, > 0, < 0),
+                a_of_chi, growth_rate                     (background.py:245-368, 401-512)
 cov_like.npz    gaussian_cl_covariance_and_mean + gaussian_log_likelihood
 sparse.npz      sparse.inv / slogdet / to_dense / dot on a random SPD block matrix
 """
@@ -97,6 +99,31 @@ def make_background(jc):
         H=np.array(H),
         dchioverda=np.array(dchi),
     )
+    return out
+
+
+# Omega_k = 0, open and closed universes for the curvature-dependent distances
+COSMOS_K = np.array(
+    [
+        [0.2589, 0.0486, 0.6774, 0.9667, 0.8159, 0.0, -1.0, 0.0],
+        [0.30, 0.05, 0.70, 0.96, 0.80, 0.05, -1.0, 0.0],
+        [0.25, 0.045, 0.72, 0.95, 0.78, -0.04, -0.9, 0.1],
+    ]
+)
+
+
+def make_background2(jc):
+    a_q = np.concatenate([np.logspace(-2.5, 0, 61), np.array([0.2, 0.5, 0.999, 1.0])])
+    chi_q = np.concatenate([np.linspace(1.0, 6000.0, 41), np.array([0.5, 100.0, 2500.0])])
+    out = {"cosmos": COSMOS_K, "a_q": a_q, "chi_q": chi_q}
+    fk, da, aoc, f = [], [], [], []
+    for row in COSMOS_K:
+        c = _cosmo(jc, row)
+        fk.append(jc.background.transverse_comoving_distance(c, a_q))
+        da.append(jc.background.angular_diameter_distance(c, a_q))
+        aoc.append(jc.background.a_of_chi(c, chi_q))
+        f.append(jc.background.growth_rate(c, a_q))
+    out.update(transverse=np.array(fk), d_a=np.array(da), a_of_chi=np.array(aoc), growth_rate=np.array(f))
     return out
 
 
@@ -322,6 +349,8 @@ def main():
     t0 = time.time()
     if want("background"):
         save("background", make_background(jc))
+    if want("background2"):
+        save("background2", make_background2(jc))
     if want("power"):
         save("power", make_power(jc))
     if want("tracers"):

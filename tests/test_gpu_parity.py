@@ -57,6 +57,21 @@ def test_background_points_vs_golden(golden):
         assert rel(jc.background.dchioverda(c, a), g["dchioverda"][i]) < RT64
 
 
+def test_background_distances_and_growth_rate_vs_golden(golden):
+    """background.py:245-368, 401-512 on the device: curvature branches, the
+    reference's interpolation of the decreasing chi table, the growth rate."""
+    g = golden("background2")
+    for i, row in enumerate(g["cosmos"]):
+        c = cosmo_of(row)
+        assert rel(jc.background.transverse_comoving_distance(c, g["a_q"]), g["transverse"][i]) < RT64
+        assert rel(jc.background.angular_diameter_distance(c, g["a_q"]), g["d_a"][i]) < RT64
+        assert rel(jc.background.a_of_chi(c, g["chi_q"]), g["a_of_chi"][i]) < RT64
+        assert rel(jc.background.growth_rate(c, g["a_q"]), g["growth_rate"][i]) < RT64
+    cb = cosmo_batch(g["cosmos"])
+    fk = jc.background.transverse_comoving_distance(cb, g["a_q"])
+    assert fk.shape == (len(g["cosmos"]), len(g["a_q"]))
+
+
 def test_background_batched_matches_single(golden):
     g = golden("background")
     cb = cosmo_batch(g["cosmos"])

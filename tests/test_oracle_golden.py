@@ -19,6 +19,19 @@ def rel(a, b):
     return float(np.max(np.abs(a - b) / np.maximum(np.abs(b), 1e-300)))
 
 
+def test_background_distances_and_growth_rate(golden):
+    """transverse / angular diameter distances for Omega_k = 0, > 0, < 0,
+    a_of_chi on the decreasing chi table, growth_rate (background.py:245-512)."""
+    g = golden("background2")
+    a, chi = torch.tensor(g["a_q"]), torch.tensor(g["chi_q"])
+    for i, row in enumerate(g["cosmos"]):
+        c = O.Cosmo.from_vector(row)
+        assert rel(O.transverse_comoving_distance(c, a), g["transverse"][i]) < RTOL
+        assert rel(O.angular_diameter_distance(c, a), g["d_a"][i]) < RTOL
+        assert rel(O.a_of_chi(c, chi), g["a_of_chi"][i]) < RTOL
+        assert rel(O.growth_rate(c, a), g["growth_rate"][i]) < RTOL
+
+
 def test_background_tables_and_queries(golden):
     g = golden("background")
     a = torch.tensor(g["a_q"])
