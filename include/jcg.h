@@ -70,6 +70,7 @@ extern "C" {
  * simps(pz_fn, 0, zmax, 256) as redshift.py:27-31 does). */
 #define JCG_NZ_SMAIL 0
 #define JCG_NZ_TABLE 1
+#define JCG_NZ_DELTA 2   /* single plane at nz_z0, WeakLensing only (redshift.py:108-122, probes.py:53-64) */
 
 #define JCG_BIAS_NONE 0
 #define JCG_BIAS_CONSTANT 1

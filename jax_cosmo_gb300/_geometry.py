@@ -43,10 +43,12 @@ def describe(probes, n_ell, n_limber=512, n_nodes=0, zmax=None):
             raise NotImplementedError(f"probe type {type(p).__name__} is not supported")
         pzmax = p.zmax
         for b, pz in enumerate(p.params[0]):
-            if isinstance(pz, delta_nz) or not isinstance(pz, redshift_distribution):
+            if not isinstance(pz, redshift_distribution):
                 raise NotImplementedError(
                     f"redshift distribution {type(pz).__name__} is not on the accelerated path"
                 )
+            if isinstance(pz, delta_nz) and kind != _lib.TRACER_WL:
+                raise NotImplementedError("single-plane delta_nz bins are supported on WeakLensing probes only")
             if n >= _lib.MAX_TRACERS:
                 raise ValueError(f"at most {_lib.MAX_TRACERS} redshift bins per request")
             g.kind[n] = kind
@@ -54,6 +56,10 @@ def describe(probes, n_ell, n_limber=512, n_nodes=0, zmax=None):
                 a, bb, z0, zm = pz.device_params()
                 g.nz_kind[n] = _lib.NZ_SMAIL
                 g.nz_a[n], g.nz_b[n], g.nz_z0[n], g.nz_zmax[n] = a, bb, z0, zm
+            elif isinstance(pz, delta_nz):
+                # probes.py:53-64: the plane's redshift, no z' integral
+                g.nz_kind[n] = _lib.NZ_DELTA
+                g.nz_a[n], g.nz_b[n], g.nz_z0[n], g.nz_zmax[n] = 0.0, 0.0, float(pz.params[0]), float(pz.zmax)
             else:
                 g.nz_kind[n] = _lib.NZ_TABLE
                 g.nz_a[n], g.nz_b[n], g.nz_z0[n], g.nz_zmax[n] = 0.0, 0.0, 1.0, float(pz.zmax)
@@ -93,14 +99,14 @@ def _bins(probes):
 
 def _nz_key(probes):
     """Cache identity of the tabulated n(z) bins (Smail bins live in the descriptor)."""
-    return tuple(pz.cache_key() if not isinstance(pz, smail_nz) else "" for pz in _bins(probes))
+    return tuple(pz.cache_key() if not isinstance(pz, (smail_nz, delta_nz)) else "" for pz in _bins(probes))
 
 
 def _build(g, probes, ell_t, z_nodes, geo, device):
     """Build the geometry; tabulated n(z) bins are evaluated at libjcg's points on the device."""
     st = _lib.stream_of(device)
     bins = _bins(probes)
-    if all(isinstance(pz, smail_nz) for pz in bins):
+    if all(isinstance(pz, (smail_nz, delta_nz)) for pz in bins):
         if z_nodes is None:
             _lib.call("jcg_geometry_build", ctypes.byref(g), _lib.ptr(ell_t), _lib.ptr(geo),
                       ctypes.c_size_t(geo.numel()), st)
@@ -117,7 +123,7 @@ def _build(g, probes, ell_t, z_nodes, geo, device):
     off = 0
     for t, pz in enumerate(bins):
         cnt = 257 + na + (na * 257 if g.kind[t] == _lib.TRACER_WL else 0)
-        if not isinstance(pz, smail_nz):
+        if not isinstance(pz, (smail_nz, delta_nz)):
             with torch.cuda.device(device):
                 pzv[off : off + cnt] = torch.as_tensor(pz.pz_fn(zp[off : off + cnt]), dtype=torch.float64)
         off += cnt

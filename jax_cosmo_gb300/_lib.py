@@ -39,7 +39,7 @@ ERR_ABI = -9
 TRACER_WL = 0
 TRACER_NC = 1
 BIAS_NONE, BIAS_CONSTANT, BIAS_INV_GROWTH, BIAS_DES_Y1 = 0, 1, 2, 3
-NZ_SMAIL, NZ_TABLE = 0, 1
+NZ_SMAIL, NZ_TABLE, NZ_DELTA = 0, 1, 2
 FP64 = 0
 FP32C = 1
 

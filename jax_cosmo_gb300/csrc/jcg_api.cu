@@ -130,8 +130,12 @@ static int make_header(const jcg_geometry* g, GeoHeader* h) {
       if (!isfinite(g->bias_eta[t]) || !isfinite(g->bias_z0[t]) || !(1.0 + g->bias_z0[t] > 0.0))
         return fail(JCG_ERR_VALUE, "tracer %d: des_y1_ia_bias eta = %g, z0 = %g", t, g->bias_eta[t], g->bias_z0[t]);
     }
-    if (g->nz_kind[t] != JCG_NZ_SMAIL && g->nz_kind[t] != JCG_NZ_TABLE)
+    if (g->nz_kind[t] != JCG_NZ_SMAIL && g->nz_kind[t] != JCG_NZ_TABLE && g->nz_kind[t] != JCG_NZ_DELTA)
       return fail(JCG_ERR_ARG, "tracer %d: nz_kind %d", t, g->nz_kind[t]);
+    if (g->nz_kind[t] == JCG_NZ_DELTA) {
+      if (k != JCG_TRACER_WL) return fail(JCG_ERR_ARG, "tracer %d: single-plane n(z) on a NumberCounts tracer", t);
+      h->has_delta = 1;
+    }
     h->nz_kind[t] = g->nz_kind[t];
     h->bias_kind[t] = bk;
     h->bias_eta[t] = bk == JCG_BIAS_DES_Y1 ? g->bias_eta[t] : 0.0;
@@ -270,6 +274,7 @@ static Batch make_batch(const GeoHeader* h, const void* geo, const double* param
   b.n_wl = h ? h->n_wl : 0;
   b.n_wl_groups = h ? h->n_groups : 0;
   b.special_bias = h ? h->special_bias : 0;
+  b.has_delta = h ? h->has_delta : 0;
   return b;
 }
 

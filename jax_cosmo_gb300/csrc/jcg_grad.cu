@@ -22,14 +22,6 @@
 
 namespace jcg {
 
-// interpolation (scipy/interpolate.py:55-59) with a dual table fp
-__device__ __forceinline__ D1 interp_d1(double x, const double* xp, const double* fv, const double* fd,
-                                        int2 sg) {
-  const D1 f0 = mk1(fv[sg.x], fd[sg.x]), f1 = mk1(fv[sg.y], fd[sg.y]);
-  const D1 a = (f1 - f0) / (xp[sg.y] - xp[sg.x]);
-  const D1 b = f0 - a * xp[sg.x];
-  return a * x + b;
-}
 
 // Tables of one cosmology with tangents.  Lanes: dir = tid & 7, item = tid >> 3.
 // F32T (fp32c Jacobian): the per-node evaluations (ODE right-hand sides,
@@ -1066,7 +1058,15 @@ __global__ void __launch_bounds__(256) grad_kern_kernel(GradBatch gb, const Cons
 #pragma unroll
           for (int d = 0; d < NDIR; ++d)
             if (d == dir) ad = acc[u].d[d];
-          const D1 rk = mk1(acc[u].v, ad) * (1.0 + z) * chi_wl;
+          D1 racc = mk1(acc[u].v, ad);
+          if (geo->nz_kind[t] == JCG_NZ_DELTA) {
+            // single plane (probes.py:53-64): clip(chi(z0) - chi, 0) / clip(chi(z0), 1)
+            const double a0 = 1.0 / (1.0 + geo->nz_z0[t]);
+            const int2 sg0 = interp_segment_inc(a0, c->atab_chi, NCHI, logspace_guess(a0, NCHI));
+            const D1 chi0 = xfmax(interp_d1(a0, c->atab_chi, tb->chiv, tb->chid[dir], sg0), 0.0);
+            racc = xfmax(chi0 - chi_wl, 0.0) / xfmax(chi0, 1.0);
+          }
+          const D1 rk = racc * (1.0 + z) * chi_wl;
           kv = cf * rk;
           if (geo->bias_kind[t] != JCG_BIAS_NONE) {
             double iv, id;

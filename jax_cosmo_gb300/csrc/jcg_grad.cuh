@@ -18,6 +18,16 @@ __device__ __forceinline__ D1 mk1(double v, double d) {
 
 typedef DualF<NDIR> F8;
 
+// interpolation (scipy/interpolate.py:55-59) with a dual table fp
+__device__ __forceinline__ D1 interp_d1(double x, const double* xp, const double* fv, const double* fd,
+                                        int2 sg) {
+  const D1 f0 = mk1(fv[sg.x], fd[sg.x]), f1 = mk1(fv[sg.y], fd[sg.y]);
+  const D1 a = (f1 - f0) / (xp[sg.y] - xp[sg.x]);
+  const D1 b = f0 - a * xp[sg.x];
+  return a * x + b;
+}
+
+
 
 // DualF<8> from a value and 8 double tangents at stride `stride`
 __device__ __forceinline__ F8 f8_of(double v, const double* d, int stride) {

@@ -183,7 +183,27 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
     {
       for (int t = lane >> 3; t < n_tr; t += 4) {
         const bool wl = geo->kind[t] == JCG_TRACER_WL;
-        if (wl && geo->bias_kind[t] == JCG_BIAS_NONE) continue;
+        const bool delta = wl && geo->nz_kind[t] == JCG_NZ_DELTA;
+        if (wl && !delta && geo->bias_kind[t] == JCG_BIAS_NONE) continue;
+        if (delta) {
+          // single plane (probes.py:53-64): K = cf (1 + z) chi r (1 + m),
+          // r = clip(chi(z0) - chi, 0) / clip(chi(z0), 1), replacing the
+          // (zero) z' integral written above
+          float dcw = 0.f;
+#pragma unroll
+          for (int d = 0; d < NDIR; ++d)
+            if (d == dir) dcw = dchi_wl[d];
+          const double a0 = 1.0 / (1.0 + geo->nz_z0[t]);
+          const int2 sg0 = interp_segment_inc(a0, c->atab_chi, NCHI, logspace_guess(a0, NCHI));
+          const D1 chi0 = xfmax(interp_d1(a0, c->atab_chi, tb->chiv, tb->chid[dir], sg0), 0.0);
+          const D1 r = xfmax(chi0 - mk1((double)chi_wl, (double)dcw), 0.0) / xfmax(chi0, 1.0);
+          const float rv = (float)r.v, rd = (float)r.d[0];
+          const float fac = cff * zp1, m1 = 1.f + (float)geo->mult[t];
+          float* dst = gi.kernf + ((size_t)t * na + n) * (NDIR + 1);
+          if (dir == 0) dst[0] = fac * chi_wl * rv * m1;
+          dst[1 + dir] = fac * (dlcf * chi_wl * rv + dcw * rv + chi_wl * rd) * m1;
+          if (geo->bias_kind[t] == JCG_BIAS_NONE) continue;
+        }
         double kv, kd;
         bias_term_d1(tb, c, geo, t, dir, AWL[n], Z[n], NZL[(size_t)t * na + n], wl, &kv, &kd);
         float* dst = gi.kernf + ((size_t)t * na + n) * (NDIR + 1);

@@ -184,6 +184,7 @@ struct GeoHeader {
   int bias_kind[MAXTR];    // JCG_BIAS_*: NC galaxy bias, WL NLA bias (NONE: no IA)
   double bias_eta[MAXTR], bias_z0[MAXTR];
   int special_bias;        // 1: some tracer has IA or a redshift-dependent bias
+  int has_delta;           // 1: some WeakLensing tracer has a single-plane n(z)
   int nz_kind[MAXTR];      // JCG_NZ_*
   int64_t nzp_off[MAXTR];  // offset of tracer t's points in the n(z) point list
   int64_t nzp_total;       // points over all tracers
@@ -239,6 +240,7 @@ struct Batch {
   int max_na, max_ell, max_cls, max_tr;
   int n_wl, n_wl_groups;  // uniform form: WeakLensing tracers and lensing groups
   int special_bias;       // uniform form: IA or a redshift-dependent bias present
+  int has_delta;          // uniform form: a single-plane WeakLensing n(z) present
 };
 
 __device__ __forceinline__ Item batch_item(const Batch& b, int i) {

@@ -130,7 +130,15 @@ __global__ void __launch_bounds__(TK_WARPS * 32)
       if (t < n_tr && lane == (t & 31)) {
         double kv;
         if (geo->kind[t] == JCG_TRACER_WL) {
-          const double rk = (double)acc[t] * (1.0 + z) * (double)chi_wl;
+          double acc_t = (double)acc[t];
+          if (geo->nz_kind[t] == JCG_NZ_DELTA) {
+            // single plane (probes.py:53-64): clip(chi(z0) - chi, 0) / clip(chi(z0), 1)
+            const double a0 = 1.0 / (1.0 + geo->nz_z0[t]);
+            const int2 sg = interp_segment_inc(a0, c->atab_chi, NCHI, logspace_guess(a0, NCHI));
+            const double chi0 = fmax(interp_eval(a0, c->atab_chi, ct->chi, sg), 0.0);
+            acc_t = fmax(chi0 - (double)chi_wl, 0.0) / fmax(chi0, 1.0);
+          }
+          const double rk = acc_t * (1.0 + z) * (double)chi_wl;
           kv = cf * rk;
           if (geo->bias_kind[t] != JCG_BIAS_NONE) {
             // NLA intrinsic alignment (probes.py:102-129), same ell factor as the shear
@@ -263,7 +271,7 @@ static void launch_tu(const Batch& b, const ConstTables* c, cudaStream_t st) {
 }
 
 void launch_tracer_kernels(const Batch& b, const ConstTables* c, cudaStream_t st) {
-  if (b.precision == JCG_FP32C && !b.listed && !b.special_bias && b.n_wl_groups == 1 && b.n_wl >= 1 &&
+  if (b.precision == JCG_FP32C && !b.listed && !b.special_bias && !b.has_delta && b.n_wl_groups == 1 && b.n_wl >= 1 &&
       b.n_wl <= 8) {
     switch (b.n_wl) {
       case 1: launch_tu<1>(b, c, st); return;

@@ -162,6 +162,7 @@ __device__ __forceinline__ double smail_pz(const GeoHeader& h, int t, double z) 
 // list: Smail analytically, a tabulated tracer from the caller's values.
 __device__ __forceinline__ double tracer_pz(const GeoHeader& h, const double* pz, int t, int64_t idx, double z) {
   if (h.nz_kind[t] == JCG_NZ_TABLE) return pz[h.nzp_off[t] + idx];
+  if (h.nz_kind[t] == JCG_NZ_DELTA) return z == h.nz_z0[t] ? 1.0 : 0.0;  // redshift.py:121-122
   return smail_pz(h, t, z);
 }
 
@@ -182,7 +183,7 @@ __global__ void geo_norm_kernel(GeoHeader h, double* geo, const double* pz) {
       const double y2 = tracer_pz(h, pz, t, 2 * m + 2, np_linspace(0.0, zm, 256, 2 * m + 2));
       acc += y0 + 4 * y1 + y2;
     }
-    dh->nz_norm[t] = dx / 3 * acc;
+    dh->nz_norm[t] = h.nz_kind[t] == JCG_NZ_DELTA ? 1.0 : dx / 3 * acc;  // delta_nz: _norm = 1
   }
 }
 
@@ -293,7 +294,10 @@ __global__ void geo_tables_kernel(const GeoHeader* __restrict__ hp, double* geo,
       for (int t = 0; t < h.n_tr; ++t) {
         if (h.kind[t] != JCG_TRACER_WL || h.group[t] != g) continue;
         double* W = geo + h.off_W[t];
-        const double wv = dx / 3 * w * (tracer_pz(h, pz, t, NZP + na + (int64_t)q, zp) / h.nz_norm[t]);
+        // single-plane tracers take no part in the z' integral (probes.py:53-64)
+        const double wv = h.nz_kind[t] == JCG_NZ_DELTA
+                              ? 0.0
+                              : dx / 3 * w * (tracer_pz(h, pz, t, NZP + na + (int64_t)q, zp) / h.nz_norm[t]);
         W[q] = wv;
         reinterpret_cast<float*>(geo + h.off_W32[t])[q] = (float)wv;
       }

@@ -7,7 +7,8 @@ Limber and lensing grids on the device.  Every other distribution (``fu_nz``,
 its ``pz_fn`` is evaluated with torch on the device at the exact points
 libjcg lists (``jcg_geometry_nz_points``), and libjcg normalises it with
 ``simps(pz_fn, 0, zmax, 256)`` (redshift.py:27-31).  ``delta_nz`` single-plane
-bins (probes.py:53-64) are not on the accelerated path.
+bins of WeakLensing probes take the reference's separate branch
+(probes.py:53-64): the lensing ratio at the plane's redshift, no z' integral.
 """
 from __future__ import annotations
 
@@ -105,7 +106,7 @@ class fu_nz(redshift_distribution):
 
 
 class delta_nz(redshift_distribution):
-    """Single plane at z0 (redshift.py:108-122); not on the accelerated path."""
+    """Single plane at z0 (redshift.py:108-122); WeakLensing bins only on the accelerated path."""
 
     def __init__(self, *args, **kwargs):
         super(delta_nz, self).__init__(*args, **kwargs)

@@ -598,6 +598,20 @@ class Shift(_NZ):
         return self.parent.pz_fn(clip(z - self.bias, 0.0))
 
 
+class Delta(_NZ):
+    """redshift.py:108-122: a single plane at z0, norm 1, pz_fn = (z == z0)."""
+
+    def __init__(self, z0, zmax=10.0, gals_per_arcmin2=1.0):
+        self.z0, self.zmax, self.gals_per_arcmin2 = z0, zmax, gals_per_arcmin2
+
+    @property
+    def norm(self):
+        return 1.0
+
+    def pz_fn(self, z):
+        return torch.where(z == self.z0, 1.0, 0.0).to(torch.float64)
+
+
 @dataclass
 class Probe:
     """A WeakLensing ('wl') or NumberCounts ('nc') probe (probes.py:132-281).
@@ -631,16 +645,9 @@ class Probe:
 
 
 def weak_lensing_kernel(c, pzs, z, ell):
-    """probes.py:16-74 (extended n(z) branch) -> [n_bins, len(z)]."""
+    """probes.py:16-74 -> [n_bins, len(z)]."""
     z = torch.atleast_1d(z)
-    zmax = max(pz.zmax for pz in pzs)
-    chi = radial_comoving_distance(c, z2a(z))
-    zp = _t(np.linspace(z.detach().numpy(), zmax, 257))  # [257, nz]
-    dx = (zmax - z) / 256
-    chi_p = radial_comoving_distance(c, z2a(zp.reshape(-1))).reshape(zp.shape)
-    dndz = torch.stack([pz(zp) for pz in pzs], dim=1)  # [257, nb, nz]
-    integ = dndz * (clip(chi_p - chi[None, :], 0.0) / clip(chi_p, 1.0))[:, None, :]
-    rk = simps_weights_apply(integ, dx) * (1.0 + z) * chi
+    rk = _wl_radial(c, pzs, z)
     constant_factor = 3.0 * H0**2 * c.Omega_m / 2.0 / C_KMS
     ell = _t(ell)
     ell_factor = torch.sqrt((ell - 1) * (ell) * (ell + 1) * (ell + 2)) / (ell + 0.5) ** 2
@@ -703,15 +710,27 @@ def probe_kernel(c, probe, z, ell):
 
 
 def _wl_radial(c, pzs, z):
-    """The ell-independent part of probes.py:24-68 (radial_kernel)."""
+    """The ell-independent part of probes.py:24-68 (radial_kernel): Simpson
+    over z' in [z, zmax] for extended bins, the single-plane ratio at z0 for
+    delta_nz bins (probes.py:53-64), in the bins' order."""
     zmax = max(pz.zmax for pz in pzs)
     chi = radial_comoving_distance(c, z2a(z))
-    zp = _t(np.linspace(z.detach().numpy(), zmax, 257))
-    dx = (zmax - z) / 256
-    chi_p = radial_comoving_distance(c, z2a(zp.reshape(-1))).reshape(zp.shape)
-    dndz = torch.stack([pz(zp) for pz in pzs], dim=1)
-    integ = dndz * (clip(chi_p - chi[None, :], 0.0) / clip(chi_p, 1.0))[:, None, :]
-    return simps_weights_apply(integ, dx) * (1.0 + z) * chi
+    ext = [i for i, pz in enumerate(pzs) if not isinstance(pz, Delta)]
+    out = [None] * len(pzs)
+    if ext:
+        zp = _t(np.linspace(z.detach().numpy(), zmax, 257))
+        dx = (zmax - z) / 256
+        chi_p = radial_comoving_distance(c, z2a(zp.reshape(-1))).reshape(zp.shape)
+        dndz = torch.stack([pzs[i](zp) for i in ext], dim=1)
+        integ = dndz * (clip(chi_p - chi[None, :], 0.0) / clip(chi_p, 1.0))[:, None, :]
+        rk = simps_weights_apply(integ, dx) * (1.0 + z) * chi
+        for j, i in enumerate(ext):
+            out[i] = rk[j]
+    for i, pz in enumerate(pzs):
+        if isinstance(pz, Delta):
+            chi0 = radial_comoving_distance(c, z2a(_t([pz.z0])))
+            out[i] = clip(chi0 - chi, 0.0) / clip(chi0, 1.0) * (1.0 + z) * chi
+    return torch.stack(out, dim=0)
 
 
 def probe_kernels_all_ell(c, probe, z, ell):

@@ -23,6 +23,8 @@ cl_ia.npz       angular_cl with NLA intrinsic alignment (des_y1, constant and
                 groups, NumberCounts with inverse-growth and constant biases
 cl_nz.npz       angular_cl with fu_nz, kde_nz (a seeded 200-galaxy catalog, stored
                 with the fixture) and systematic_shift(smail_nz) bins
+cl_delta.npz    angular_cl with single-plane delta_nz WeakLensing bins beside a
+                smail bin, and a NumberCounts bin
 background2.npz transverse / angular diameter distances (Omega_k = 0, > 0, < 0),
                 a_of_chi, growth_rate                     (background.py:245-368, 401-512)
 cov_like.npz    gaussian_cl_covariance_and_mean + gaussian_log_likelihood
@@ -239,6 +241,15 @@ def _probes(jc, kind):
             jc.probes.WeakLensing([fu, kde, shift], sigma_e=0.26),
             jc.probes.NumberCounts([kde], jc.bias.constant_linear_bias(1.2)),
         ]
+    if kind == "delta":
+        pa = jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10)
+        return [
+            jc.probes.WeakLensing(
+                [pa, jc.redshift.delta_nz(1.0, gals_per_arcmin2=5), jc.redshift.delta_nz(0.4)],
+                multiplicative_bias=[0.0, 0.01, -0.02], sigma_e=0.26,
+            ),
+            jc.probes.NumberCounts([pa], jc.bias.constant_linear_bias(1.2)),
+        ]
     raise ValueError(kind)
 
 
@@ -359,7 +370,7 @@ def main():
         save("cov_like", make_cov_like(jc))
     if want("sparse"):
         save("sparse", make_sparse(jc))
-    if want("cl_wl2") or want("cl_mixed") or want("cl_ia") or want("cl_nz"):
+    if want("cl_wl2") or want("cl_mixed") or want("cl_ia") or want("cl_nz") or want("cl_delta"):
         import multiprocessing as mp
 
         with mp.get_context("spawn").Pool(args.procs) as pool:
@@ -380,6 +391,9 @@ def main():
                 d = make_cl(args.reference, pool, "nz", COSMOS[[0, 2]], ell)
                 d["zcat"], d["w"] = nz_catalog()
                 save("cl_nz", d)
+            if want("cl_delta"):
+                ell = np.logspace(1, np.log10(5000.0), 10)
+                save("cl_delta", make_cl(args.reference, pool, "delta", COSMOS[[0, 2]], ell))
 
 
 if __name__ == "__main__":

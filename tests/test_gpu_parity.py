@@ -410,3 +410,41 @@ def test_tabulated_nz_vs_golden(golden):
     err = max(float((J[..., d].cpu() - J_o[..., d]).abs().max() / J_o[..., d].abs().max().clamp_min(1e-300))
               for d in range(8))
     assert err < 1e-8, err
+
+
+def _delta_probes():
+    """The single-plane fixture's probes (tests/golden/make_golden.py, kind "delta")."""
+    pa = jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10)
+    return [jc.probes.WeakLensing([pa, jc.redshift.delta_nz(1.0, gals_per_arcmin2=5), jc.redshift.delta_nz(0.4)],
+                                  multiplicative_bias=[0.0, 0.01, -0.02], sigma_e=0.26),
+            jc.probes.NumberCounts([pa], jc.bias.constant_linear_bias(1.2))]
+
+
+def test_single_plane_nz_vs_golden(golden):
+    """delta_nz WeakLensing bins (probes.py:53-64) beside an extended bin,
+    against the unmodified reference's C_ell, FP64 and fp32c; the Jacobian
+    against the oracle's autograd in both precisions."""
+    g = golden("cl_delta")
+    cb = cosmo_batch(g["cosmos"])
+    cl = jc.cl.angular_cl(cb, g["ell"], _delta_probes())
+    cl32 = jc.cl.angular_cl(cb, g["ell"], _delta_probes(), precision="fp32c")
+    for i in range(len(g["cosmos"])):
+        assert rel(cl[i], g["cl"][i]) < RT64
+        assert rel(cl32[i], g["cl"][i]) < RT32
+    ell = g["ell"][::3]
+    pa = O.Smail(1, 2, 0.5, 10.0, 10)
+    oprobes = [O.Probe("wl", [pa, O.Delta(1.0, gals_per_arcmin2=5), O.Delta(0.4)], sigma_e=0.26,
+                       m=[0.0, 0.01, -0.02]),
+               O.Probe("nc", [pa], bias=1.2)]
+    row = list(g["cosmos"][1])
+
+    def f(v):
+        return O.angular_cl(O.Cosmo.from_vector(v), ell, oprobes, n_limber=128)
+
+    J_o = torch.autograd.functional.jacobian(f, torch.tensor(row, dtype=torch.float64), strategy="forward-mode",
+                                             vectorize=True)
+    for prec, tol in (("fp64", 1e-8), ("fp32c", 1e-4)):
+        _, J = jc.autodiff.angular_cl_jacobian(cosmo_of(row), ell, _delta_probes(), 128, prec)
+        err = max(float((J[..., d].cpu() - J_o[..., d]).abs().max() / J_o[..., d].abs().max().clamp_min(1e-300))
+                  for d in range(8))
+        assert err < tol, (prec, err)

@@ -66,11 +66,17 @@ def test_describe_rejects_unsupported():
         def pz_fn(self, z):
             return z
 
-    # any redshift_distribution is tabulated; single-plane bins are not supported
+    # any redshift_distribution is tabulated; single-plane bins on WeakLensing only
     g = _geometry.describe([jc.probes.WeakLensing([other_nz(zmax=3.0), jc.redshift.smail_nz(1, 2, 1)])], 3)
     assert list(g.nz_kind)[:2] == [_lib.NZ_TABLE, _lib.NZ_SMAIL] and g.nz_zmax[0] == 3.0
+    gd = _geometry.describe([jc.probes.WeakLensing([jc.redshift.delta_nz(1.5)])], 3)
+    assert gd.nz_kind[0] == _lib.NZ_DELTA and gd.nz_z0[0] == 1.5 and gd.nz_zmax[0] == 10.0
+    sz = ctypes.c_size_t()
+    assert _lib.load().jcg_geometry_size(ctypes.byref(gd), ctypes.byref(sz)) == 0
     with pytest.raises(NotImplementedError):
-        _geometry.describe([jc.probes.WeakLensing([jc.redshift.delta_nz(1.0)])], 3)
+        _geometry.describe([jc.probes.NumberCounts([jc.redshift.delta_nz(1.0)], jc.bias.constant_linear_bias(1.0))], 3)
+    gd.kind[0] = _lib.TRACER_NC  # the library refuses a single plane on NumberCounts too
+    assert _lib.load().jcg_geometry_size(ctypes.byref(gd), ctypes.byref(sz)) == _lib.ERR_ARG
     # the point list has 257 + na (+ na x 257 for lensing) entries per tracer
     cnt = ctypes.c_size_t()
     assert _lib.load().jcg_geometry_nz_points(ctypes.byref(g), None, None, ctypes.byref(cnt), None) == 0

@@ -105,7 +105,15 @@ def nz_probes(g):
     return [O.Probe("wl", [fu, kde, shift], sigma_e=0.26), O.Probe("nc", [kde], bias=1.2)]
 
 
-@pytest.mark.parametrize("name", ["cl_wl2", "cl_mixed", "cl_ia", "cl_nz"])
+def delta_probes():
+    """The single-plane fixture's probes (make_golden.py, kind "delta")."""
+    pa = O.Smail(1, 2, 0.5, 10.0, 10)
+    return [O.Probe("wl", [pa, O.Delta(1.0, gals_per_arcmin2=5), O.Delta(0.4)], sigma_e=0.26,
+                    m=[0.0, 0.01, -0.02]),
+            O.Probe("nc", [pa], bias=1.2)]
+
+
+@pytest.mark.parametrize("name", ["cl_wl2", "cl_mixed", "cl_ia", "cl_nz", "cl_delta"])
 def test_angular_cl(golden, name):
     g = golden(name)
     for i, row in enumerate(g["cosmos"]):
@@ -117,6 +125,8 @@ def test_angular_cl(golden, name):
             P = ia_probes()
         elif name == "cl_nz":
             P = nz_probes(g)
+        elif name == "cl_delta":
+            P = delta_probes()
         else:
             pz = [O.Smail(1, 2, 0.5, 10.0, 10), O.Smail(1, 2, 1.0, 10.0, 10)]
             P = [O.Probe("wl", pz, sigma_e=0.26), O.Probe("nc", pz, bias=1.2)]
