@@ -767,7 +767,12 @@ size_t cl_listed_bytes(const ReqPlan& p, int precision) {
   return o;
 }
 
-size_t ll_extra_bytes(int n) { return align256(sizeof(ReqLL) * (size_t)n); }
+// the request table and the ell-tile partials of the request log-likelihood
+size_t ll_extra_bytes(const ReqPlan& p, int n) {
+  size_t tiles = 0;
+  for (int i = 0; i < n; ++i) tiles += rl_tiles(p.hdr[i].n_ell);
+  return align256(sizeof(ReqLL) * (size_t)n) + align256(sizeof(double) * 9 * tiles);
+}
 
 }  // namespace
 
@@ -781,7 +786,7 @@ extern "C" int jcg_requests_workspace_size(const jcg_request* reqs, int n, int m
     *bytes_min = *bytes_full = cl_listed_bytes(plan, precision);
     return JCG_OK;
   }
-  const size_t extra = mode == JCG_REQ_LOGLIKE_GRAD ? ll_extra_bytes(n) : 0;
+  const size_t extra = mode == JCG_REQ_LOGLIKE_GRAD ? ll_extra_bytes(plan, n) : 0;
   const int ns = grad_listed_auto_split(plan.greq.data(), n, precision);
   *bytes_min = extra + grad_listed_bytes(plan.greq.data(), n, 1, precision);
   *bytes_full = extra + grad_listed_bytes(plan.greq.data(), n, ns, precision);
@@ -845,7 +850,7 @@ extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, int pr
     launch_limber(b, c, limber_tile(b.max_ell), stream);
     return cuda_check("requests angular_cl");
   }
-  const size_t extra = mode == JCG_REQ_LOGLIKE_GRAD ? ll_extra_bytes(n) : 0;
+  const size_t extra = mode == JCG_REQ_LOGLIKE_GRAD ? ll_extra_bytes(plan, n) : 0;
   const size_t need1 = extra + grad_listed_bytes(plan.greq.data(), n, 1, precision);
   if (ws_bytes < need1) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need1);
   int ns = grad_listed_auto_split(plan.greq.data(), n, precision);
@@ -855,20 +860,26 @@ extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, int pr
   if (mode == JCG_REQ_LOGLIKE_GRAD) {
     static thread_local std::vector<ReqLL> ll;
     ll.resize(n);
+    double* part = reinterpret_cast<double*>(base + align256(sizeof(ReqLL) * (size_t)n));
+    int max_tiles = 1, max_cls = 1;
     for (int i = 0; i < n; ++i) {
       ll[i].cl = plan.greq[i].cl;
       ll[i].jac = plan.greq[i].jac;
       ll[i].data = reqs[i].data_dev;
       ll[i].prec = reqs[i].prec_dev;
       ll[i].out = reqs[i].out_dev;
+      ll[i].part = part;
       ll[i].n_cls = plan.hdr[i].n_cls;
       ll[i].n_ell = plan.hdr[i].n_ell;
+      part += 9 * (size_t)rl_tiles(ll[i].n_ell);
+      max_tiles = max(max_tiles, rl_tiles(ll[i].n_ell));
+      max_cls = max(max_cls, ll[i].n_cls);
     }
     ReqLL* dev_ll = reinterpret_cast<ReqLL*>(base);
     if (cudaMemcpyAsync(dev_ll, ll.data(), sizeof(ReqLL) * (size_t)n, cudaMemcpyHostToDevice, stream) !=
         cudaSuccess)
       return cuda_check("request loglike table copy");
-    launch_request_loglike(dev_ll, n, stream);
+    launch_request_loglike(dev_ll, n, max_tiles, max_cls, stream);
   }
   return cuda_check("requests jacobian");
 }

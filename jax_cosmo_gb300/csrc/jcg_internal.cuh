@@ -686,9 +686,12 @@ struct ReqLL {
   const double* data;   // [n_cls * n_ell]
   const double* prec;   // [n_ell][n_cls][n_cls]
   double* out;          // [9]
+  double* part;         // [n_tiles][9] partial sums of the ell tiles (workspace)
   int n_cls, n_ell;
 };
-void launch_request_loglike(const ReqLL* items_dev, int n, cudaStream_t st);
+constexpr int RL_ELL = 8;  // ell per CTA of the request log-likelihood
+__host__ __device__ inline int rl_tiles(int n_ell) { return (n_ell + RL_ELL - 1) / RL_ELL; }
+void launch_request_loglike(const ReqLL* items_dev, int n, int max_tiles, int max_cls, cudaStream_t st);
 // pointwise queries of the table functions (API: background / power modules)
 void launch_eval_points(const double* params, int n_cosmo, CosmoTab* ctab, const ConstTables* c,
                         const double* a, const double* k, int n, int what, double* out,

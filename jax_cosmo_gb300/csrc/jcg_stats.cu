@@ -244,29 +244,38 @@ __global__ void zero_int_kernel(int* p, int n) {
 // Log-likelihood with a fixed inverse covariance P (the covariance held
 // constant, as in the reference's intro notebook) and its gradient:
 //   r = C_ell - data, logL = -r^T P r / 2, dlogL/dtheta = -(dC_ell/dtheta)^T P r.
-// One CTA per request; fixed-order reductions (same result alone or in a batch).
-__global__ void __launch_bounds__(256) request_loglike_kernel(const ReqLL* __restrict__ items, int n) {
-  const int item = blockIdx.x;
+// One CTA per (tile of RL_ELL ell, request): r of the tile staged in shared
+// memory, per (ell, spectrum) alpha = (P r) and its 9 contributions, the
+// CTA's sums to the tile's partial; a second kernel adds the tiles in order.
+// Fixed-order reductions: the same result alone or in a batch.
+__global__ void __launch_bounds__(128) request_loglike_part_kernel(const ReqLL* __restrict__ items, int n) {
+  const int item = blockIdx.y, tile = blockIdx.x;
   if (item >= n) return;
   const ReqLL q = items[item];
   const int n_cls = q.n_cls, n_ell = q.n_ell;
+  const int l0 = tile * RL_ELL;
+  if (l0 >= n_ell) return;
+  const int lt = min(RL_ELL, n_ell - l0);
+  extern __shared__ double rs[];  // [n_cls][RL_ELL]
+  for (int e = threadIdx.x; e < n_cls * lt; e += blockDim.x) {
+    const int k = e / lt, j = e - k * lt;
+    const size_t o = (size_t)k * n_ell + l0 + j;
+    rs[k * RL_ELL + j] = q.cl[o] - q.data[o];
+  }
+  __syncthreads();
   double acc[9];
   for (int s = 0; s < 9; ++s) acc[s] = 0.0;
-  const int total = n_cls * n_ell;
-  for (int idx = threadIdx.x; idx < total; idx += blockDim.x) {
-    const int l = idx / n_cls, p = idx % n_cls;
+  for (int idx = threadIdx.x; idx < lt * n_cls; idx += blockDim.x) {
+    const int j = idx / n_cls, p = idx - j * n_cls;
+    const int l = l0 + j;
     const double* Pl = q.prec + ((size_t)l * n_cls + p) * n_cls;
     double alpha = 0.0;
-    for (int k = 0; k < n_cls; ++k) {
-      const size_t o = (size_t)k * n_ell + l;
-      alpha += Pl[k] * (q.cl[o] - q.data[o]);
-    }
-    const size_t op = (size_t)p * n_ell + l;
-    acc[0] += (q.cl[op] - q.data[op]) * alpha;
-    const double* J = q.jac + op * 8;
+    for (int k = 0; k < n_cls; ++k) alpha += Pl[k] * rs[k * RL_ELL + j];
+    acc[0] += rs[p * RL_ELL + j] * alpha;
+    const double* J = q.jac + ((size_t)p * n_ell + l) * 8;
     for (int d = 0; d < 8; ++d) acc[1 + d] += alpha * J[d];
   }
-  __shared__ double red[8][9];
+  __shared__ double red[4][9];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   for (int s = 0; s < 9; ++s) {
     double v = acc[s];
@@ -277,12 +286,26 @@ __global__ void __launch_bounds__(256) request_loglike_kernel(const ReqLL* __res
   if (threadIdx.x < 9) {
     double v = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v += red[w][threadIdx.x];
-    q.out[threadIdx.x] = threadIdx.x == 0 ? -0.5 * v : -v;
+    q.part[(size_t)tile * 9 + threadIdx.x] = v;
   }
 }
 
-void launch_request_loglike(const ReqLL* items_dev, int n, cudaStream_t st) {
-  request_loglike_kernel<<<n, 256, 0, st>>>(items_dev, n);
+__global__ void request_loglike_sum_kernel(const ReqLL* __restrict__ items, int n) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int item = idx / 9, s = idx % 9;
+  if (item >= n) return;
+  const ReqLL q = items[item];
+  const int tiles = rl_tiles(q.n_ell);
+  double v = 0.0;
+  for (int t = 0; t < tiles; ++t) v += q.part[(size_t)t * 9 + s];
+  q.out[s] = s == 0 ? -0.5 * v : -v;
+}
+
+void launch_request_loglike(const ReqLL* items_dev, int n, int max_tiles, int max_cls, cudaStream_t st) {
+  const size_t smem = sizeof(double) * (size_t)max_cls * RL_ELL;
+  dim3 grid(max_tiles, n);
+  request_loglike_part_kernel<<<grid, 128, smem, st>>>(items_dev, n);
+  request_loglike_sum_kernel<<<(9 * n + 127) / 128, 128, 0, st>>>(items_dev, n);
 }
 
 void launch_loglike(const double* data, const double* mu, const double* cov, int n_cosmo, int n_cls,
