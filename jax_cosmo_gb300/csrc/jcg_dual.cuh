@@ -240,11 +240,14 @@ __device__ __forceinline__ DualF<N> operator*(const DualF<N>& a, const DualF<N>&
   for (int i = 0; i < N; ++i) r.d[i] = fmaf(a.d[i], bv, av * b.d[i]);
   return r;
 }
+// The tangent factors of division and the elementary functions are formed
+// in FP32 from the rounded value (one float64 division per operation, not
+// two): the tangents are FP32 anyway.
 template <int N>
 __device__ __forceinline__ DualF<N> operator/(const DualF<N>& a, const DualF<N>& b) {
   DualF<N> r;
   r.v = a.v / b.v;
-  const float ib = (float)(1.0 / b.v), rv = (float)r.v;
+  const float ib = 1.f / (float)b.v, rv = (float)r.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = (a.d[i] - rv * b.d[i]) * ib;
   return r;
@@ -307,7 +310,7 @@ template <int N>
 __device__ __forceinline__ DualF<N> operator/(double a, const DualF<N>& b) {
   DualF<N> r;
   r.v = a / b.v;
-  const float s = (float)(-r.v / b.v);
+  const float s = -(float)r.v / (float)b.v;
 #pragma unroll
   for (int i = 0; i < N; ++i) r.d[i] = s * b.d[i];
   return r;
@@ -327,18 +330,26 @@ __device__ __forceinline__ DualF<N> xexp(const DualF<N>& a) {
   return scale_f(e, e, a);
 }
 template <int N>
+__device__ __forceinline__ DualF<N> scale_ff(double v, float s, const DualF<N>& a) {
+  DualF<N> r;
+  r.v = v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = s * a.d[i];
+  return r;
+}
+template <int N>
 __device__ __forceinline__ DualF<N> xlog(const DualF<N>& a) {
-  return scale_f(log(a.v), 1.0 / a.v, a);
+  return scale_ff(log(a.v), 1.f / (float)a.v, a);
 }
 template <int N>
 __device__ __forceinline__ DualF<N> xsqrt(const DualF<N>& a) {
   const double s = sqrt(a.v);
-  return scale_f(s, 0.5 / s, a);
+  return scale_ff(s, 0.5f / (float)s, a);
 }
 template <int N>
 __device__ __forceinline__ DualF<N> xcbrt(const DualF<N>& a) {
   const double c = cbrt(a.v);
-  return scale_f(c, c / (3.0 * a.v), a);
+  return scale_ff(c, (float)c / (3.f * (float)a.v), a);
 }
 template <int N>
 __device__ __forceinline__ DualF<N> xsin(const DualF<N>& a) {
@@ -438,6 +449,26 @@ __device__ __forceinline__ T dchioverdaT(const BgT<T>& c, double a, double lna) 
 template <class T>
 __device__ __forceinline__ T wT(const BgT<T>& c, double a) {
   return c.w0 + (1.0 - a) * c.wa;
+}
+// dchi/dln a = R_H / (a sqrt(E^2(a))) with ln a and 1 / a given (background.py:227-229, 294)
+template <class T>
+__device__ __forceinline__ T dchi_dlna_cT(const BgT<T>& c, double a, double lna, double ia) {
+  const T f = -3.0 * (1.0 + c.w0 + c.wa) * lna + 3.0 * c.wa * (a - 1.0);
+  const T ef = xexp(f);
+  const double ia2 = ia * ia;
+  const T e2 = c.Om * (ia2 * ia) + c.Ok * ia2 + c.Ode * ef;
+  return (RH * ia) / xsqrt(e2);
+}
+// growth ODE coefficients with ln x and 1 / x given (background.py:96-106)
+template <class T>
+__device__ __forceinline__ void growth_qr_cT(const BgT<T>& b, double x, double lnx, double ix, T& q, T& r) {
+  const T f = -3.0 * (1.0 + b.w0 + b.wa) * lnx + 3.0 * b.wa * (x - 1.0);
+  const T ef = xexp(f);
+  const double ix2 = ix * ix, ix3 = ix2 * ix;
+  const T ie2 = 1.0 / (b.Om * ix3 + b.Ok * ix2 + b.Ode * ef);
+  const T omm = b.Om * ix3 * ie2, omde = b.Ode * ef * ie2;
+  q = (2.0 - 0.5 * (omm + (1.0 + 3.0 * wT(b, x)) * omde)) * ix;
+  r = 1.5 * omm * ix2;
 }
 // background.py:227-229
 template <class T>

@@ -104,38 +104,33 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     F8 sF[NSCAL];
     for (int i = 0; i < NSCAL; ++i) sF[i] = f8_of(sv[i], sd + i, NSCAL);
     const BgT<F8> bgf = make_bgT(sF);
+    // cosmology-independent abscissae, logs, reciprocals and window factors
+    // from the constant grids
     for (int e = t; e < 2 * NCHI; e += blockDim.x) {
       if (e < NCHI) {
-        putf(fn, NCHI, e, dchi_dlnaT(bgf, c->lna_chi[e]));
+        putf(fn, NCHI, e, dchi_dlna_cT(bgf, c->chi_a[e], c->lna_chi[e], c->chi_ia[e]));
       } else if (e > NCHI) {
         const int i = e - NCHI;
-        const double t0 = c->lna_chi[i - 1], t1 = c->lna_chi[i];
-        putf(fm, NCHI, i, dchi_dlnaT(bgf, t0 + (t1 - t0) / 2));
+        putf(fm, NCHI, i, dchi_dlna_cT(bgf, c->chi_am[i], c->chi_lnam[i], c->chi_iam[i]));
       }
     }
     for (int e = t; e < 2 * NGROW; e += blockDim.x) {
       F8 q, r;
       if (e < NGROW) {
-        growth_qrT(bgf, c->atab_grow[e], q, r);
+        growth_qr_cT(bgf, c->atab_grow[e], c->grow_lna[e], c->grow_ia[e], q, r);
         putf(qr + 0 * (NDIR + 1) * NGROW, NGROW, e, q);
         putf(qr + 1 * (NDIR + 1) * NGROW, NGROW, e, r);
       } else if (e > NGROW) {
         const int i = e - NGROW;
-        const double x = c->atab_grow[i], xp = c->atab_grow[i - 1];
-        growth_qrT(bgf, xp + (x - xp) / 2, q, r);
+        growth_qr_cT(bgf, c->grow_am[i], c->grow_lnam[i], c->grow_iam[i], q, r);
         putf(qr + 2 * (NDIR + 1) * NGROW, NGROW, i, q);
         putf(qr + 3 * (NDIR + 1) * NGROW, NGROW, i, r);
       }
     }
     for (int e = t; e < NROMB; e += blockDim.x) {
       const double logk = c->romb_logk[e];
-      const double k = exp(logk);
-      const double x = k * 8.0;
-      const double wf = 3.0 * (sin(x) - x * cos(x)) / (x * x * x);
-      const F8 T = eh_transferT(sF, k, logk);
-      const F8 pk = (T * T) * xexp(sF[S_NS] * logk);
-      const double kw = k * wf;
-      putf(fr, NROMB, e, k * (kw * kw) * pk);
+      const F8 T = eh_transferT(sF, c->romb_k[e], logk);
+      putf(fr, NROMB, e, c->romb_kw2[e] * ((T * T) * xexp(sF[S_NS] * logk)));
     }
   }
   __syncthreads();
