@@ -100,6 +100,10 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       const double kw = k * wf;
       put(fr, NROMB, e, k * (kw * kw) * pk);
     }
+  } else if (gb.gnode) {
+    // node values from grad_nodes_kernel: the same layout as fn .. fr here
+    const double* src = gb.gnode + (size_t)item * GNODE_STRIDE;
+    for (int i = t; i < GNODE_U; i += blockDim.x) fn[i] = src[i];
   } else {
     F8 sF[NSCAL];
     for (int i = 0; i < NSCAL; ++i) sF[i] = f8_of(sv[i], sd + i, NSCAL);
@@ -369,9 +373,17 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     F8 sF[NSCAL];
     for (int i = 0; i < NSCAL; ++i) sF[i] = f8_of(sv[i], sd + i, NSCAL);
     const F8 g1f = f8_of(g1s[0], g1s + 1, 1);
+    const double* gu = gb.gnode ? gb.gnode + (size_t)item * GNODE_STRIDE + GNODE_U : nullptr;
     for (int e = t; e < NKH; e += blockDim.x) {
       const double k = c->kh[e];
-      const F8 p3 = pk_linearT(sF, k, c->logk[e], g1f) * c->kh3[e];
+      F8 p3;
+      if (gu) {
+        // pk_linearT's order: ((exp(n_s ln k) T^2) g^2) pknorm, then k^3
+        const F8 u = f8_of(gu[e], gu + NKH + e, NKH);
+        p3 = ((u * (g1f * g1f)) * sF[S_PKNORM]) * c->kh3[e];
+      } else {
+        p3 = pk_linearT(sF, k, c->logk[e], g1f) * c->kh3[e];
+      }
       out->pk3v[e] = p3.v;
 #pragma unroll
       for (int d = 0; d < NDIR; ++d) {
@@ -1405,6 +1417,68 @@ int grad_limber_tile(int n_ell, int n_cls) {
   return (n_ell + tiles - 1) / tiles;
 }
 
+// Small fp32c batches: the table kernel's per-node evaluations (chi
+// right-hand sides, growth coefficients, Romberg integrand, exp(n_s ln k) T^2
+// on the P(k) grid), one per thread over GNODE_CTAS CTAs per cosmology, in
+// DualF<8> as in the table kernel.
+__global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+  const int item = blockIdx.y;
+  if (item >= gb.n_items) return;
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= GNODE_WORK) return;
+  const GradItem gi = grad_item(gb, item);
+  const TabD* tb = gi.tab;
+  F8 sF[NSCAL];
+  for (int i = 0; i < NSCAL; ++i) sF[i] = f8_of(tb->sv[i], &tb->sd[0][i], NSCAL);
+  const BgT<F8> bgf = make_bgT(sF);
+  double* dst = gb.gnode + (size_t)item * GNODE_STRIDE;
+  auto putf = [&](int off, int stride, int i, const F8& x) {
+    dst[off + i] = x.v;
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) dst[off + (1 + d) * stride + i] = x.d[d];
+  };
+  int w = e;
+  if (w < NCHI) {
+    putf(0, NCHI, w, dchi_dlna_cT(bgf, c->chi_a[w], c->lna_chi[w], c->chi_ia[w]));
+    return;
+  }
+  w -= NCHI;
+  if (w < NCHI - 1) {
+    const int i = w + 1;
+    putf(GNODE_FM, NCHI, i, dchi_dlna_cT(bgf, c->chi_am[i], c->chi_lnam[i], c->chi_iam[i]));
+    return;
+  }
+  w -= NCHI - 1;
+  if (w < NGROW) {
+    F8 q, r;
+    growth_qr_cT(bgf, c->atab_grow[w], c->grow_lna[w], c->grow_ia[w], q, r);
+    putf(GNODE_QR, NGROW, w, q);
+    putf(GNODE_QR + (NDIR + 1) * NGROW, NGROW, w, r);
+    return;
+  }
+  w -= NGROW;
+  if (w < NGROW - 1) {
+    const int i = w + 1;
+    F8 q, r;
+    growth_qr_cT(bgf, c->grow_am[i], c->grow_lnam[i], c->grow_iam[i], q, r);
+    putf(GNODE_QR + 2 * (NDIR + 1) * NGROW, NGROW, i, q);
+    putf(GNODE_QR + 3 * (NDIR + 1) * NGROW, NGROW, i, r);
+    return;
+  }
+  w -= NGROW - 1;
+  if (w < NROMB) {
+    const double logk = c->romb_logk[w];
+    const F8 T = eh_transferT(sF, c->romb_k[w], logk);
+    putf(GNODE_FR, NROMB, w, c->romb_kw2[w] * ((T * T) * xexp(sF[S_NS] * logk)));
+    return;
+  }
+  w -= NROMB;
+  {
+    const F8 T = eh_transferT(sF, c->kh[w], c->logk[w]);
+    putf(GNODE_U, NKH, w, xexp(sF[S_NS] * c->logk[w]) * (T * T));
+  }
+}
+
 // Scalars with tangents, one thread per (cosmology, direction): the Dual<1>
 // chain of pow / log / sqrt with all lanes of a warp busy.
 __global__ void __launch_bounds__(128) grad_scalars_kernel(GradBatch gb) {
@@ -1425,6 +1499,7 @@ __global__ void __launch_bounds__(128) grad_scalars_kernel(GradBatch gb) {
 void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
   const size_t smt = grad_tables_smem();
   grad_scalars_kernel<<<(gb.n_items * NDIR + 127) / 128, 128, 0, st>>>(gb);
+  if (gb.gnode) grad_nodes_kernel<<<dim3(GNODE_CTAS, gb.n_items), 128, 0, st>>>(gb, c);
   if (gb.precision == JCG_FP32C) {
     cudaFuncSetAttribute(grad_tables_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
     grad_tables_kernel<true><<<gb.n_items, 128, smt, st>>>(gb, c);
@@ -1503,6 +1578,11 @@ static size_t ptt_bytes(int precision) {
   return precision == JCG_FP32C ? PTT_STRIDE * sizeof(double) : 0;
 }
 
+// node scratch of the small-batch fp32c table path
+static size_t gnode_bytes(int n, int precision) {
+  return (precision == JCG_FP32C && n <= GNODE_MAX_ITEMS) ? al256(sizeof(double) * GNODE_STRIDE * (size_t)n) : 0;
+}
+
 size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
   const int ns = grad_n_split(h, n_cosmo, precision);
   GeoHeader hb = h;
@@ -1512,6 +1592,7 @@ size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
   o += rows_bytes(hb, precision);
   o += kern_bytes(hb, precision);
   o += al256(sizeof(double) * (size_t)ns * n_cosmo * h.n_cls * h.n_ell * (NDIR + 1));
+  o += gnode_bytes(n_cosmo, precision);
   return o;
 }
 
@@ -1538,6 +1619,8 @@ void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, in
   else gb.kernd = reinterpret_cast<double*>(base + o);
   o += kern_bytes(hb, precision);
   gb.part = reinterpret_cast<double*>(base + o);
+  o += al256(sizeof(double) * (size_t)grad_n_split(h, n_cosmo, precision) * n_cosmo * h.n_cls * h.n_ell * (NDIR + 1));
+  gb.gnode = gnode_bytes(n_cosmo, precision) ? reinterpret_cast<double*>(base + o) : nullptr;
   gb.cl = cl;
   gb.jac = jac;
   gb.na = h.na;
@@ -1586,7 +1669,7 @@ int grad_listed_auto_split(const GradReq* r, int n, int precision) {
 size_t grad_listed_bytes(const GradReq* r, int n, int n_split, int precision) {
   size_t o = al256(sizeof(GradItem) * (size_t)n);
   for (int i = 0; i < n; ++i) o += grad_item_bytes(*r[i].h, n_split, !r[i].cl, !r[i].jac, precision);
-  return o;
+  return o + gnode_bytes(n, precision);
 }
 
 cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void* ws, const ConstTables* c,
@@ -1642,6 +1725,7 @@ cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void*
   gb.precision = precision;
   gb.items = dev_items;
   gb.n_split = n_split;
+  gb.gnode = gnode_bytes(n, precision) ? reinterpret_cast<double*>(base + o) : nullptr;
   launch_grad(gb, c, st);
   return cudaSuccess;
 }

@@ -128,8 +128,24 @@ struct GradBatch {
   double* part;
   double* cl;
   double* jac;
+  double* gnode;  // fp32c, small batches: the table kernel's node values, per item GNODE_STRIDE doubles
   int na, n_tr, n_cls, n_ell, n_split;
 };
+
+// Small fp32c batches spread the table kernel's per-node evaluations over
+// GNODE_CTAS CTAs per cosmology (grad_nodes_kernel) and hand them over in
+// the table kernel's shared-memory layout: chi right-hand sides at nodes and
+// midpoints [2][NDIR + 1][NCHI], growth coefficients [4][NDIR + 1][NGROW],
+// the Romberg integrand [NDIR + 1][NROMB], then exp(n_s ln k) T(k)^2 on the
+// P(k) grid [NDIR + 1][NKH] (value, then 8 tangents).
+constexpr int GNODE_MAX_ITEMS = 128;
+constexpr int GNODE_FM = (NDIR + 1) * NCHI;
+constexpr int GNODE_QR = 2 * (NDIR + 1) * NCHI;
+constexpr int GNODE_FR = GNODE_QR + 4 * (NDIR + 1) * NGROW;
+constexpr int GNODE_U = GNODE_FR + (NDIR + 1) * NROMB;
+constexpr size_t GNODE_STRIDE = (size_t)(GNODE_U + (NDIR + 1) * NKH + 31) / 32 * 32;
+constexpr int GNODE_WORK = NCHI + (NCHI - 1) + NGROW + (NGROW - 1) + NROMB + NKH;  // 1152
+constexpr int GNODE_CTAS = (GNODE_WORK + 127) / 128;
 
 __device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
   if (gb.listed) return gb.items[i];
