@@ -549,6 +549,151 @@ __device__ void cosmo_scalarsT(const T* p, T* s) {
   s[S_LGKSILK] = xlog(k_silk);
 }
 
+// Warp shuffles of a double or a Dual<1>.
+__device__ __forceinline__ double shfl_t(double x, int src) { return __shfl_sync(0xffffffffu, x, src); }
+__device__ __forceinline__ Dual<1> shfl_t(const Dual<1>& x, int src) {
+  Dual<1> r;
+  r.v = __shfl_sync(0xffffffffu, x.v, src);
+  r.d[0] = __shfl_sync(0xffffffffu, x.d[0], src);
+  return r;
+}
+
+// The scalars of transfer.py:47-142 and core.py:145-162 for a whole warp
+// (all 32 lanes, converged): the formulas and calls of the reference's order
+// (cosmo_scalarsT), but the independent pow / sqrt / log calls
+// of each level run on different lanes at once (one call site per function
+// and level, lane-selected arguments, results broadcast by shuffles).  The
+// chain's latency is that of 5 levels instead of about 25 calls.  s is
+// written by every lane.
+template <class T>
+__device__ void cosmo_scalars_warpT(const T* p, T* s, int lane) {
+  const T one = T(p[0] * 0.0 + 1.0);
+  for (int i = 0; i < NSCAL; ++i) s[i] = T(p[0] * 0.0);
+  const T Oc = p[0], Ob = p[1], h = p[2];
+  s[S_OMEGA_C] = Oc;
+  s[S_OMEGA_B] = Ob;
+  s[S_H] = h;
+  s[S_NS] = p[3];
+  s[S_SIGMA8] = p[4];
+  s[S_OMEGA_K] = p[5];
+  s[S_W0] = p[6];
+  s[S_WA] = p[7];
+  const T Om = Ob + Oc;
+  s[S_OMEGA_M] = Om;
+  s[S_OMEGA_DE] = (1.0 - p[5]) - Om;
+  const double T27 = (TCMB / 2.7) * (TCMB / 2.7);
+  const T h2 = h * h;
+  const T w_m = Om * h2;
+  const T w_b = Ob * h2;
+  const T fb = Ob / Om;
+  const T fc = (Om - Ob) / Om;
+  const T k_eq = 7.46e-2 * w_m / T27 / h;
+  const T z_eq = 2.50e4 * w_m / (T27 * T27);
+  const T R_eq = 31.5 * w_b / (T27 * T27) * (1.0e3 / z_eq);
+  // level 1: pow(w, e), sqrt, log of the parameters
+  T pb = one, sq = one, lg = one;
+  double pe = 1.0;
+  switch (lane) {
+    case 0: pb = w_m, pe = -0.419; break;
+    case 1: pb = w_m, pe = 0.674; break;
+    case 2: pb = w_m, pe = 0.223; break;
+    case 3: pb = w_m, pe = 0.251; break;
+    case 4: pb = w_m, pe = 0.828; break;
+    case 5: pb = w_b, pe = 0.52; break;
+    case 6: pb = w_m, pe = 0.73; break;
+    case 7: pb = 10.4 * w_m, pe = -0.95; break;
+    case 8: pb = 46.9 * w_m, pe = 0.670; break;
+    case 9: pb = 32.1 * w_m, pe = -0.532; break;
+    case 10: pb = 12.0 * w_m, pe = 0.424; break;
+    case 11: pb = 45.0 * w_m, pe = -0.582; break;
+    case 12: pb = 458.0 * w_m, pe = -0.708; break;
+    case 13: pb = 0.395 * w_m, pe = -0.0266; break;
+    case 14: pb = w_m, pe = 0.435; break;
+    case 15: pb = fb, pe = 3.0; break;
+    default: break;
+  }
+  switch (lane) {
+    case 0: sq = 6.0 / R_eq; break;
+    case 1: sq = R_eq; break;
+    case 2: sq = (17.2 * w_m) * (17.2 * w_m) + 1.0; break;
+    default: break;
+  }
+  if (lane == 0) lg = 13.41 * k_eq;
+  const T P1 = xpow(pb, pe), S1 = xsqrt(sq), L1 = xlog(lg);
+  const T A0 = shfl_t(P1, 0), A1 = shfl_t(P1, 1), A2 = shfl_t(P1, 2), A3 = shfl_t(P1, 3);
+  const T A4 = shfl_t(P1, 4), A5 = shfl_t(P1, 5), A6 = shfl_t(P1, 6), A7 = shfl_t(P1, 7);
+  const T A8 = shfl_t(P1, 8), A9 = shfl_t(P1, 9), A10 = shfl_t(P1, 10), A11 = shfl_t(P1, 11);
+  const T A12 = shfl_t(P1, 12), A13 = shfl_t(P1, 13), A14 = shfl_t(P1, 14), FB3 = shfl_t(P1, 15);
+  const T sq6 = shfl_t(S1, 0), sqeq = shfl_t(S1, 1), sqbb = shfl_t(S1, 2);
+  const T lgq = shfl_t(L1, 0);
+  // level 2: pows with parameter-dependent exponents, log(k_silk)
+  const T b1 = 0.313 * A0 * (1.0 + 0.607 * A1);
+  const T b2 = 0.238 * A2;
+  const T k_silk = 1.6 * A5 * A6 * (1.0 + A7) / h;
+  const T a1 = A8 * (1.0 + A9);
+  const T a2 = A10 * (1.0 + A11);
+  const T b1c = 0.944 / (1.0 + A12);
+  const T b2c = A13;
+  T qb = one, qe = one;
+  switch (lane) {
+    case 0: qb = w_b, qe = b2; break;
+    case 1: qb = a1, qe = -fb; break;
+    case 2: qb = a2, qe = -FB3; break;
+    case 3: qb = fc, qe = b2c; break;
+    default: break;
+  }
+  const T P2 = xpow(qb, qe), L2 = xlog(lane == 0 ? k_silk : one);
+  const T B0 = shfl_t(P2, 0), B1 = shfl_t(P2, 1), B2 = shfl_t(P2, 2), B3 = shfl_t(P2, 3);
+  const T lgks = shfl_t(L2, 0);
+  // level 3
+  const T z_d = 1291.0 * A3 / (1.0 + 0.659 * A4) * (1.0 + b1 * B0);
+  const T R_d = 31.5 * w_b / (T27 * T27) * (1.0e3 / z_d);
+  const T alpha_c = B1 * B2;
+  T beta_c = 1.0 + b1c * (B3 - 1.0);
+  beta_c = 1.0 / beta_c;
+  const T y = (1.0 + z_eq) / (1.0 + z_d);
+  T sq3 = one;
+  switch (lane) {
+    case 0: sq3 = 1.0 + R_d; break;
+    case 1: sq3 = R_eq + R_d; break;
+    case 2: sq3 = 1.0 + y; break;
+    default: break;
+  }
+  const T S3 = xsqrt(sq3), P3 = xpow(lane == 0 ? 1.0 + R_d : one, lane == 0 ? -0.75 : 1.0);
+  const T C0 = shfl_t(S3, 0), C1 = shfl_t(S3, 1), x = shfl_t(S3, 2), C3 = shfl_t(P3, 0);
+  // level 4
+  T lg4 = one;
+  if (lane == 0) lg4 = (C0 + C1) / (1.0 + sqeq);
+  if (lane == 1) lg4 = (x + 1.0) / (x - 1.0);
+  const T L4 = xlog(lg4);
+  const T D0 = shfl_t(L4, 0), D1v = shfl_t(L4, 1);
+  // level 5
+  const T sh_d = 2.0 / (3.0 * k_eq) * sq6 * D0;
+  const T G = y * (-6.0 * x + (2.0 + 3.0 * y) * D1v);
+  const T alpha_b = 2.07 * k_eq * sh_d * C3 * G;
+  const T beta_node = 8.41 * A14;
+  const T beta_b = 0.5 + fb + (3.0 - 2.0 * fb) * sqbb;
+  s[S_K_EQ] = k_eq;
+  s[S_Z_EQ] = z_eq;
+  s[S_Z_D] = z_d;
+  s[S_R_D] = R_d;
+  s[S_R_EQ] = R_eq;
+  s[S_SH_D] = sh_d;
+  s[S_K_SILK] = k_silk;
+  s[S_ALPHA_C] = alpha_c;
+  s[S_BETA_C] = beta_c;
+  s[S_ALPHA_B] = alpha_b;
+  s[S_BETA_B] = beta_b;
+  s[S_BETA_NODE] = beta_node;
+  s[S_FB] = fb;
+  s[S_FC] = fc;
+  s[S_LGQ] = lgq;
+  s[S_LGKSILK] = lgks;
+  s[S_QINV] = 1.0 / (13.41 * k_eq);
+  s[S_ISH] = 1.0 / sh_d;
+  s[S_C142AC] = 14.2 / alpha_c;
+}
+
 // transfer.py:107-153 at a fixed wavenumber k (lk = log k)
 template <class T>
 __device__ __forceinline__ T eh_transferT(const T* s, double k, double lk) {

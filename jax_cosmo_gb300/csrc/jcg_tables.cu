@@ -7,6 +7,7 @@
 // angular_cl.py:63-96 (Limber grid).
 #include "jcg_fp32.cuh"
 #include "jcg_internal.cuh"
+#include "jcg_dual.cuh"
 
 namespace jcg {
 
@@ -312,72 +313,6 @@ void launch_geometry_build(const GeoHeader& h, double* geo, const double* pz, co
 }
 
 // ------------------------------------------------------ cosmology tables ----
-// Scalars and Eisenstein & Hu constants (transfer.py:47-142, core.py:145-162).
-__device__ void cosmo_scalars(const double* p, double* s) {
-  for (int i = 0; i < NSCAL; ++i) s[i] = 0.0;
-  const double Oc = p[0], Ob = p[1], h = p[2];
-  s[S_OMEGA_C] = Oc;
-  s[S_OMEGA_B] = Ob;
-  s[S_H] = h;
-  s[S_NS] = p[3];
-  s[S_SIGMA8] = p[4];
-  s[S_OMEGA_K] = p[5];
-  s[S_W0] = p[6];
-  s[S_WA] = p[7];
-  const double Om = Ob + Oc;
-  s[S_OMEGA_M] = Om;
-  s[S_OMEGA_DE] = (1.0 - p[5]) - Om;
-  const double T27 = (TCMB / 2.7) * (TCMB / 2.7);
-  const double h2 = h * h;
-  const double w_m = Om * h2;
-  const double w_b = Ob * h2;
-  const double fb = Ob / Om;
-  const double fc = (Om - Ob) / Om;
-  const double k_eq = 7.46e-2 * w_m / T27 / h;
-  const double z_eq = 2.50e4 * w_m / (T27 * T27);
-  double b1 = 0.313 * pow(w_m, -0.419) * (1.0 + 0.607 * pow(w_m, 0.674));
-  double b2 = 0.238 * pow(w_m, 0.223);
-  const double z_d =
-      1291.0 * pow(w_m, 0.251) / (1.0 + 0.659 * pow(w_m, 0.828)) * (1.0 + b1 * pow(w_b, b2));
-  const double R_d = 31.5 * w_b / (T27 * T27) * (1.0e3 / z_d);
-  const double R_eq = 31.5 * w_b / (T27 * T27) * (1.0e3 / z_eq);
-  const double sh_d = 2.0 / (3.0 * k_eq) * sqrt(6.0 / R_eq) *
-                      log((sqrt(1.0 + R_d) + sqrt(R_eq + R_d)) / (1.0 + sqrt(R_eq)));
-  const double k_silk =
-      1.6 * pow(w_b, 0.52) * pow(w_m, 0.73) * (1.0 + pow(10.4 * w_m, -0.95)) / h;
-  const double a1 = pow(46.9 * w_m, 0.670) * (1.0 + pow(32.1 * w_m, -0.532));
-  const double a2 = pow(12.0 * w_m, 0.424) * (1.0 + pow(45.0 * w_m, -0.582));
-  const double alpha_c = pow(a1, -fb) * pow(a2, -pow(fb, 3.0));
-  b1 = 0.944 / (1.0 + pow(458.0 * w_m, -0.708));
-  b2 = pow(0.395 * w_m, -0.0266);
-  double beta_c = 1.0 + b1 * (pow(fc, b2) - 1.0);
-  beta_c = 1.0 / beta_c;
-  const double y = (1.0 + z_eq) / (1.0 + z_d);
-  const double x = sqrt(1.0 + y);
-  const double G = y * (-6.0 * x + (2.0 + 3.0 * y) * log((x + 1.0) / (x - 1.0)));
-  const double alpha_b = 2.07 * k_eq * sh_d * pow(1.0 + R_d, -0.75) * G;
-  const double beta_node = 8.41 * pow(w_m, 0.435);
-  const double beta_b = 0.5 + fb + (3.0 - 2.0 * fb) * sqrt((17.2 * w_m) * (17.2 * w_m) + 1.0);
-  s[S_K_EQ] = k_eq;
-  s[S_Z_EQ] = z_eq;
-  s[S_Z_D] = z_d;
-  s[S_R_D] = R_d;
-  s[S_R_EQ] = R_eq;
-  s[S_SH_D] = sh_d;
-  s[S_K_SILK] = k_silk;
-  s[S_ALPHA_C] = alpha_c;
-  s[S_BETA_C] = beta_c;
-  s[S_ALPHA_B] = alpha_b;
-  s[S_BETA_B] = beta_b;
-  s[S_BETA_NODE] = beta_node;
-  s[S_FB] = fb;
-  s[S_FC] = fc;
-  s[S_LGQ] = log(13.41 * k_eq);
-  s[S_LGKSILK] = log(k_silk);
-  s[S_QINV] = 1.0 / (13.41 * k_eq);
-  s[S_ISH] = 1.0 / sh_d;
-  s[S_C142AC] = 14.2 / alpha_c;
-}
 
 __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const ConstTables* __restrict__ c) {
   const int item = blockIdx.x;
@@ -534,20 +469,25 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   for (int i = t; i < NKH; i += blockDim.x) out->pk3[i] = pk3[i];
 }
 
-// The scalars, one thread per cosmology: their float64 chain of pow / log /
-// sqrt runs with all 32 lanes of a warp busy (on one lane of the table
-// kernel it would hold the float64 pipe as long as a full warp would).
+// The scalars, one warp per cosmology: the independent pow / sqrt / log
+// calls of each level of cosmo_scalars' chain on different lanes at once
+// (cosmo_scalars_warpT, the same operations and values), so the chain's
+// latency is 5 calls deep and every lane of the float64 pipe's warps is busy.
 __global__ void __launch_bounds__(128) cosmo_scalars_kernel(Batch bt) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   if (i >= bt.n_items) return;
   const Item it = batch_item(bt, i);
   double sv[NSCAL];
-  cosmo_scalars(it.params, sv);
-  for (int k = 0; k < NSCAL; ++k) it.ctab->s[k] = sv[k];
+  cosmo_scalars_warpT<double>(it.params, sv, lane);
+  double v = 0.0;
+#pragma unroll
+  for (int k = 0; k < NSCAL; ++k)
+    if (k == lane) v = sv[k];
+  it.ctab->s[lane] = v;
 }
 
 void launch_cosmo_tables(const Batch& b, const ConstTables* c, cudaStream_t st) {
-  cosmo_scalars_kernel<<<(b.n_items + 127) / 128, 128, 0, st>>>(b);
+  cosmo_scalars_kernel<<<(b.n_items + 3) / 4, 128, 0, st>>>(b);
   cosmo_tables_kernel<<<b.n_items, 256, 0, st>>>(b, c);
 }
 
