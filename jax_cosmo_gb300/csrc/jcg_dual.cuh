@@ -549,22 +549,23 @@ __device__ void cosmo_scalarsT(const T* p, T* s) {
   s[S_LGKSILK] = xlog(k_silk);
 }
 
-// Warp shuffles of a double or a Dual<1>.
-__device__ __forceinline__ double shfl_t(double x, int src) { return __shfl_sync(0xffffffffu, x, src); }
+// Shuffles of a double or a Dual<1> within a 16-lane half warp (every lane
+// of the warp executes them).
+__device__ __forceinline__ double shfl_t(double x, int src) { return __shfl_sync(0xffffffffu, x, src, 16); }
 __device__ __forceinline__ Dual<1> shfl_t(const Dual<1>& x, int src) {
   Dual<1> r;
-  r.v = __shfl_sync(0xffffffffu, x.v, src);
-  r.d[0] = __shfl_sync(0xffffffffu, x.d[0], src);
+  r.v = __shfl_sync(0xffffffffu, x.v, src, 16);
+  r.d[0] = __shfl_sync(0xffffffffu, x.d[0], src, 16);
   return r;
 }
 
-// The scalars of transfer.py:47-142 and core.py:145-162 for a whole warp
-// (all 32 lanes, converged): the formulas and calls of the reference's order
-// (cosmo_scalarsT), but the independent pow / sqrt / log calls
-// of each level run on different lanes at once (one call site per function
-// and level, lane-selected arguments, results broadcast by shuffles).  The
-// chain's latency is that of 5 levels instead of about 25 calls.  s is
-// written by every lane.
+// The scalars of transfer.py:47-142 and core.py:145-162 for a 16-lane half
+// warp (lane in [0, 16); both halves of the warp execute it, converged): the
+// formulas and calls of the reference's order (cosmo_scalarsT), but the
+// independent pow / sqrt / log calls of each level run on different lanes at
+// once (one call site per function and level, lane-selected arguments,
+// results broadcast by shuffles).  The chain's latency is that of 5 levels
+// instead of about 25 calls.  s is written by every lane.
 template <class T>
 __device__ void cosmo_scalars_warpT(const T* p, T* s, int lane) {
   const T one = T(p[0] * 0.0 + 1.0);

@@ -1496,28 +1496,32 @@ __global__ void __launch_bounds__(128) grad_scalars_kernel(GradBatch gb) {
   }
 }
 
-// Small batches: one warp per (cosmology, direction), the chain's
+// Small batches: one half warp per (cosmology, direction), the chain's
 // independent calls on different lanes (cosmo_scalars_warpT).
-__global__ void __launch_bounds__(256) grad_scalars_warp_kernel(GradBatch gb) {
-  const int item = blockIdx.x, dir = threadIdx.x >> 5, lane = threadIdx.x & 31;
+__global__ void __launch_bounds__(128) grad_scalars_warp_kernel(GradBatch gb) {
+  const int item = blockIdx.x, dir = threadIdx.x >> 4, lane = threadIdx.x & 15;
   if (item >= gb.n_items) return;
   const GradItem gi = grad_item(gb, item);
   D1 p[8];
   for (int i = 0; i < 8; ++i) p[i] = mk1(gi.params[i], i == dir ? 1.0 : 0.0);
   D1 s[NSCAL];
   cosmo_scalars_warpT<D1>(p, s, lane);
-  D1 v = mk1(0.0, 0.0);
+  D1 v0 = mk1(0.0, 0.0), v1 = v0;
 #pragma unroll
-  for (int k = 0; k < NSCAL; ++k)
-    if (k == lane) v = s[k];
-  if (dir == 0) gi.tab->sv[lane] = v.v;
-  gi.tab->sd[dir][lane] = v.d[0];
+  for (int k = 0; k < 16; ++k)
+    if (k == lane) v0 = s[k], v1 = s[k + 16];
+  if (dir == 0) {
+    gi.tab->sv[lane] = v0.v;
+    gi.tab->sv[lane + 16] = v1.v;
+  }
+  gi.tab->sd[dir][lane] = v0.d[0];
+  gi.tab->sd[dir][lane + 16] = v1.d[0];
 }
 
 void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
   const size_t smt = grad_tables_smem();
   if (gb.n_items <= GNODE_MAX_ITEMS)
-    grad_scalars_warp_kernel<<<gb.n_items, 32 * NDIR, 0, st>>>(gb);
+    grad_scalars_warp_kernel<<<gb.n_items, 16 * NDIR, 0, st>>>(gb);
   else
     grad_scalars_kernel<<<(gb.n_items * NDIR + 127) / 128, 128, 0, st>>>(gb);
   if (gb.gnode) grad_nodes_kernel<<<dim3(GNODE_CTAS, gb.n_items), 128, 0, st>>>(gb, c);

@@ -469,25 +469,30 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   for (int i = t; i < NKH; i += blockDim.x) out->pk3[i] = pk3[i];
 }
 
-// The scalars, one warp per cosmology: the independent pow / sqrt / log
-// calls of each level of cosmo_scalars' chain on different lanes at once
-// (cosmo_scalars_warpT, the same operations and values), so the chain's
-// latency is 5 calls deep and every lane of the float64 pipe's warps is busy.
+// The scalars, one half warp per cosmology: the independent pow / sqrt /
+// log calls of each level of the chain on different lanes at once
+// (cosmo_scalars_warpT), so the chain's latency is 5 calls deep.  Both
+// halves of a warp run (the last one on a copy of the last cosmology when
+// the count is odd) since the shuffles need every lane.
 __global__ void __launch_bounds__(128) cosmo_scalars_kernel(Batch bt) {
-  const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
-  if (i >= bt.n_items) return;
-  const Item it = batch_item(bt, i);
+  const int g = (blockIdx.x * blockDim.x + threadIdx.x) >> 4, lane = threadIdx.x & 15;
+  if (((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * 2 >= bt.n_items) return;  // whole warps only
+  const bool valid = g < bt.n_items;
+  const Item it = batch_item(bt, valid ? g : bt.n_items - 1);
   double sv[NSCAL];
   cosmo_scalars_warpT<double>(it.params, sv, lane);
-  double v = 0.0;
+  double v0 = 0.0, v1 = 0.0;
 #pragma unroll
-  for (int k = 0; k < NSCAL; ++k)
-    if (k == lane) v = sv[k];
-  it.ctab->s[lane] = v;
+  for (int k = 0; k < 16; ++k)
+    if (k == lane) v0 = sv[k], v1 = sv[k + 16];
+  if (valid) {
+    it.ctab->s[lane] = v0;
+    it.ctab->s[lane + 16] = v1;
+  }
 }
 
 void launch_cosmo_tables(const Batch& b, const ConstTables* c, cudaStream_t st) {
-  cosmo_scalars_kernel<<<(b.n_items + 3) / 4, 128, 0, st>>>(b);
+  cosmo_scalars_kernel<<<(b.n_items + 7) / 8, 128, 0, st>>>(b);
   cosmo_tables_kernel<<<b.n_items, 256, 0, st>>>(b, c);
 }
 
