@@ -56,19 +56,25 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
     }
     npass_s = np;
   }
-  // chi and segment slopes per table node: the value at [x][0], the 8
-  // tangents at [x][4 .. 11] (two float4 loads per node)
-  __shared__ __align__(16) float ctab[NCHI][12];
-  __shared__ __align__(16) float stab[NCHI][12];
+  __shared__ __align__(16) float ctab[NDIR + 1][NCHI];  // chi, then its tangents
+  __shared__ __align__(16) float stab[NDIR + 1][NCHI];  // segment slopes, then tangents
   const TabD* tb = gi.tab;
-  for (int i = threadIdx.x; i < (NDIR + 1) * NCHI; i += blockDim.x) {
-    const int comp = i / NCHI, x = i - comp * NCHI;
-    const int col = comp == 0 ? 0 : 3 + comp;
-    ctab[x][col] = tb->c32[comp][x];
-    stab[x][col] = tb->s32[comp][x];
+  {
+    const float4* sc = reinterpret_cast<const float4*>(&tb->c32[0][0]);
+    const float4* ss = reinterpret_cast<const float4*>(&tb->s32[0][0]);
+    float4* dc = reinterpret_cast<float4*>(&ctab[0][0]);
+    float4* ds = reinterpret_cast<float4*>(&stab[0][0]);
+    for (int i = threadIdx.x; i < (NDIR + 1) * NCHI / 4; i += blockDim.x) {
+      dc[i] = sc[i];
+      ds[i] = ss[i];
+    }
   }
   __syncthreads();
   const int npass = npass_s;
+  const float* chi = ctab[0];
+  const float* slope = stab[0];
+  const float(*dchi)[NCHI] = ctab + 1;
+  const float(*dslope)[NCHI] = stab + 1;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double* Z = geo_ptr<double>(geo, geo->off_z);
   const double* AWL = geo_ptr<double>(geo, geo->off_awl);
@@ -83,12 +89,11 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
   for (int n = n0 + warp; n < n_end; n += 8) {
     const int qw = QWL[n];
     const int xw = qw & 0xffff, mw = qw >> 16;
-    const float dxw = DXWL[n];
-    const float craw_w = ctab[xw][0] + stab[mw][0] * dxw;
+    const float craw_w = chi[xw] + slope[mw] * DXWL[n];
     const float chi_wl = fmaxf(craw_w, 0.f);
     float dchi_wl[NDIR];
 #pragma unroll
-    for (int d = 0; d < NDIR; ++d) dchi_wl[d] = craw_w > 0.f ? ctab[xw][4 + d] + stab[mw][4 + d] * dxw : 0.f;
+    for (int d = 0; d < NDIR; ++d) dchi_wl[d] = craw_w > 0.f ? dchi[d][xw] + dslope[d][mw] * DXWL[n] : 0.f;
     const float zp1 = (float)(1.0 + Z[n]);
     const size_t row = (size_t)n * NZP;
     // WeakLensing tracers: passes of up to TP tracers of one lensing group
@@ -115,20 +120,16 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
         const int q = Q32[j];
         const int x = q & 0xffff, m = q >> 16;
         const float dx = DX32[j];
-        const float craw = ctab[x][0] + stab[m][0] * dx;
+        const float craw = chi[x] + slope[m] * dx;
         const float chip = fmaxf(craw, 0.f);
         const float diff = chip - chi_wl;
         if (!(diff > 0.f)) continue;  // then craw > 0 too
         const float ic = rcpf(fmaxf(chip, 1.f));
         const float r = diff * ic;
         const float h = chip > 1.f ? ic * (1.f - r) : ic;
-        const float4 c0 = *reinterpret_cast<const float4*>(&ctab[x][4]);
-        const float4 c1 = *reinterpret_cast<const float4*>(&ctab[x][8]);
-        const float4 s0 = *reinterpret_cast<const float4*>(&stab[m][4]);
-        const float4 s1 = *reinterpret_cast<const float4*>(&stab[m][8]);
-        const float dcp[NDIR] = {fmaf(s0.x, dx, c0.x) * h, fmaf(s0.y, dx, c0.y) * h, fmaf(s0.z, dx, c0.z) * h,
-                                 fmaf(s0.w, dx, c0.w) * h, fmaf(s1.x, dx, c1.x) * h, fmaf(s1.y, dx, c1.y) * h,
-                                 fmaf(s1.z, dx, c1.z) * h, fmaf(s1.w, dx, c1.w) * h};
+        float dcp[NDIR];
+#pragma unroll
+        for (int d = 0; d < NDIR; ++d) dcp[d] = fmaf(dslope[d][m], dx, dchi[d][x]) * h;
 #pragma unroll
         for (int u = 0; u < TP; ++u) {
           if (tl[u] >= 0) {
