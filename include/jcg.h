@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define JCG_ABI_VERSION 2
+#define JCG_ABI_VERSION 3
 #define JCG_MAX_TRACERS 16
 #define JCG_MAX_PAIRS (JCG_MAX_TRACERS * (JCG_MAX_TRACERS + 1) / 2)
 #define JCG_MAX_ELL 4096
@@ -77,6 +77,21 @@ extern "C" {
 #define JCG_BIAS_INV_GROWTH 2
 #define JCG_BIAS_DES_Y1 3
 
+/* Physics switches: jcg_geometry.physics, and bits 8 and up of the `what` word
+ * of jcg_eval_points.  The matter power model (the nonlinear_fn of
+ * angular_cl, angular_cl.py:49-98) in the low four bits:
+ *   TAKAHASHI2012  power.halofit, prescription "takahashi2012" (the default)
+ *   SMITH2003      power.halofit, prescription "smith2003" (power.py:182-198, 226-242)
+ *   LINEAR         power.linear_matter_power (power.py:21-53), no halofit
+ * and the transfer function (transfer_fn):
+ *   NOWIGGLE       transfer.Eisenstein_Hu with type "eisenhu" (transfer.py:99-105),
+ *                  the zero-baryon fit without oscillations; unset: "eisenhu_osc". */
+#define JCG_PK_TAKAHASHI2012 0
+#define JCG_PK_SMITH2003 1
+#define JCG_PK_LINEAR 2
+#define JCG_PK_MASK 0x0f
+#define JCG_TF_NOWIGGLE 0x10
+
 /* arithmetic of the Limber stage */
 #define JCG_FP64 0  /* plain: float64 everywhere */
 #define JCG_FP32C 1 /* float32 Limber integrand + compensated Simpson sums, float64 tables */
@@ -105,6 +120,7 @@ typedef struct jcg_geometry {
   double bias_eta[JCG_MAX_TRACERS];   /* des_y1_ia_bias eta, z0 (bias.py:55-57) */
   double bias_z0[JCG_MAX_TRACERS];
   int nz_kind[JCG_MAX_TRACERS];       /* JCG_NZ_* */
+  int physics;                        /* JCG_PK_* | JCG_TF_* (0: the reference defaults) */
 } jcg_geometry;
 
 /* ------------------------------------------------------------- misc ---- */
@@ -270,7 +286,9 @@ int jcg_workspace_read(const jcg_geometry* g, int n_cosmo, int precision, const 
  *  10 transverse_comoving_distance(a)  background.py:297-344
  *  11 angular_diameter_distance(a)     background.py:347-368
  *  12 a_of_chi(chi), chi in a_dev      background.py:245-267
- *  13 growth_rate(a)                   background.py:401-440 (ODE growth) 
+ *  13 growth_rate(a)                   background.py:401-440 (ODE growth)
+ * in the low byte of `what`; bits 8 and up hold the physics switches
+ * (JCG_PK_* | JCG_TF_*) << 8 for 4-9.
  * Needs a workspace of jcg_workspace_size(g=NULL -> tables only). */
 int jcg_eval_points(const double* params_dev, int n_cosmo, const double* a_dev,
                     const double* k_dev, int n, int what, double* out_dev, void* workspace,

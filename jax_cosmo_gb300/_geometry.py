@@ -23,10 +23,11 @@ _cache = collections.OrderedDict()
 _cache_lock = threading.Lock()
 
 
-def describe(probes, n_ell, n_limber=512, n_nodes=0, zmax=None):
+def describe(probes, n_ell, n_limber=512, n_nodes=0, zmax=None, physics=0):
     """Fill a ``jcg_geometry`` from a list of probes (angular_cl.py:63, probes.py)."""
     g = _lib.Geometry()
     g.abi_version = _lib.ABI_VERSION
+    g.physics = int(physics)
     n = 0
     for p in probes:
         if isinstance(p, WeakLensing):
@@ -131,14 +132,14 @@ def _build(g, probes, ell_t, z_nodes, geo, device):
               ctypes.c_size_t(pzv.numel()), _lib.ptr(geo), ctypes.c_size_t(geo.numel()), st)
 
 
-def get_geometry(probes, ell, n_limber, device):
+def get_geometry(probes, ell, n_limber, device, physics=0):
     """(descriptor, device buffer, device ell) for probes on the ell grid, cached.
 
     The cache key is the descriptor bytes and the ell values, so repeated calls
     with the same survey set-up build nothing and copy nothing.
     """
     ell_np = ell_host(ell)
-    g = describe(probes, ell_np.size, n_limber)
+    g = describe(probes, ell_np.size, n_limber, physics=physics)
     key = (bytes(g), ell_np.tobytes(), str(device), _nz_key(probes))
     with _cache_lock:
         hit = _cache.get(key)

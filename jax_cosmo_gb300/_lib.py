@@ -18,7 +18,7 @@ import torch
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libjcg.so")
 
-ABI_VERSION = 2
+ABI_VERSION = 3
 MAX_TRACERS = 16
 MAX_PAIRS = MAX_TRACERS * (MAX_TRACERS + 1) // 2
 MAX_ELL = 4096
@@ -42,6 +42,9 @@ BIAS_NONE, BIAS_CONSTANT, BIAS_INV_GROWTH, BIAS_DES_Y1 = 0, 1, 2, 3
 NZ_SMAIL, NZ_TABLE, NZ_DELTA = 0, 1, 2
 FP64 = 0
 FP32C = 1
+# physics switches (jcg_geometry.physics; bits 8+ of jcg_eval_points' what)
+PK_TAKAHASHI2012, PK_SMITH2003, PK_LINEAR = 0, 1, 2
+TF_NOWIGGLE = 0x10
 
 EVAL_CHI, EVAL_GROWTH, EVAL_H, EVAL_DCHI, EVAL_TRANSFER, EVAL_PLIN, EVAL_PNL = range(7)
 EVAL_KNL, EVAL_NEFF, EVAL_C = 7, 8, 9
@@ -82,6 +85,7 @@ class Geometry(ctypes.Structure):
         ("bias_eta", ctypes.c_double * MAX_TRACERS),
         ("bias_z0", ctypes.c_double * MAX_TRACERS),
         ("nz_kind", ctypes.c_int * MAX_TRACERS),
+        ("physics", ctypes.c_int),
     ]
 
 

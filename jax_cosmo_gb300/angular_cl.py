@@ -63,11 +63,17 @@ def _get_cov_blocks_ordering(probes):
     return cov_blocks
 
 
-def _check_fns(transfer_fn, nonlinear_fn):
-    if transfer_fn is not tklib.Eisenstein_Hu:
-        raise NotImplementedError("only transfer.Eisenstein_Hu (eisenhu_osc) is accelerated")
-    if nonlinear_fn is not power.halofit:
-        raise NotImplementedError("only power.halofit (takahashi2012) is accelerated")
+def physics_code(transfer_fn, nonlinear_fn):
+    """libjcg physics switches for the operator points of angular_cl.
+
+    transfer_fn: ``transfer.Eisenstein_Hu`` with type "eisenhu_osc" (default) or
+    "eisenhu" (transfer.py:99-153), bound with ``functools.partial``;
+    nonlinear_fn: ``power.halofit`` with prescription "takahashi2012" (default)
+    or "smith2003" (power.py:182-244), or ``power.linear_matter_power``.
+    Anything else raises NotImplementedError, as the reference does for an
+    unknown type or prescription (transfer.py:155, power.py:226).
+    """
+    return tklib.transfer_bits(transfer_fn) | power.model_bits(nonlinear_fn)
 
 
 def _precision_code(precision):
@@ -77,15 +83,16 @@ def _precision_code(precision):
         raise ValueError(f"precision must be one of {sorted(_PRECISION)}") from None
 
 
-def angular_cl_device(params, ell, probes, precision="fp64", n_limber=512, out=None):
+def angular_cl_device(params, ell, probes, precision="fp64", n_limber=512, out=None, physics=0):
     """C_ell for a [B, 8] float64 parameter tensor on the device -> [B, n_cls, n_ell].
 
     Lower-level entry used by the public function, the autograd wrapper and the
     serving loop; ``params`` (and ``out``) live on the device, ``ell`` is a host
-    array (the device copy is cached with the geometry).
+    array (the device copy is cached with the geometry); ``physics`` is the
+    code of ``physics_code``.
     """
     device = params.device
-    g, geo, _ = _geometry.get_geometry(probes, ell, n_limber, device)
+    g, geo, _ = _geometry.get_geometry(probes, ell, n_limber, device, physics)
     B = params.shape[0]
     prec = _precision_code(precision)
     n_cls = _geometry.n_cls_of(g)
@@ -115,16 +122,16 @@ def angular_cl(
     A batched cosmology gives [B, n_cls, n_ell].  Differentiable with respect to
     Cosmology parameters that are tensors with ``requires_grad``.
     """
-    _check_fns(transfer_fn, nonlinear_fn)
+    physics = physics_code(transfer_fn, nonlinear_fn)
     device = _lib.require_cuda()
     ell_np = _geometry.ell_host(ell)
     if cosmo.requires_grad():
         from jax_cosmo_gb300 import autodiff
 
-        cl = autodiff.angular_cl_autograd(cosmo, ell_np, probes, precision, n_limber)
+        cl = autodiff.angular_cl_autograd(cosmo, ell_np, probes, precision, n_limber, physics)
     else:
         params = cosmo.param_tensor(device)
-        cl = angular_cl_device(params, ell_np, probes, precision, n_limber)
+        cl = angular_cl_device(params, ell_np, probes, precision, n_limber, physics=physics)
     return cl if cosmo.batch_size is not None else cl[0]
 
 

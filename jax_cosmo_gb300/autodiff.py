@@ -32,17 +32,18 @@ PARAM_ORDER = ("Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"
 FISHER_PARAMS = ("Omega_c", "Omega_b", "h", "n_s", "sigma8", "w0", "wa")
 
 
-def jacobian_device(params, ell, probes, n_limber=512, precision="fp64"):
+def jacobian_device(params, ell, probes, n_limber=512, precision="fp64", physics=0):
     """(C_ell [B, n_cls, n_ell], dC/dtheta [B, n_cls, n_ell, 8]) for [B, 8] params on the device.
 
     precision "fp64" (plain) or "fp32c" (float32 lensing kernels and Limber
-    integrand with its reverse sweep, compensated a-sums; float64 tables).
+    integrand with its reverse sweep, compensated a-sums; float64 tables);
+    physics: the code of ``angular_cl.physics_code``.
     """
     from jax_cosmo_gb300.angular_cl import _precision_code
 
     prec = _precision_code(precision)
     device = params.device
-    g, geo, _ = _geometry.get_geometry(probes, ell, n_limber, device)
+    g, geo, _ = _geometry.get_geometry(probes, ell, n_limber, device, physics)
     B = params.shape[0]
     n_cls = _geometry.n_cls_of(g)
     wsz = ctypes.c_size_t()
@@ -59,37 +60,42 @@ def jacobian_device(params, ell, probes, n_limber=512, precision="fp64"):
 
 class _AngularCl(torch.autograd.Function):
     @staticmethod
-    def forward(ctx, params, ell, probes, precision, n_limber):
+    def forward(ctx, params, ell, probes, precision, n_limber, physics):
         from jax_cosmo_gb300.angular_cl import angular_cl_device
 
-        ctx.meta = (ell, probes, n_limber, precision)
+        ctx.meta = (ell, probes, n_limber, precision, physics)
         ctx.save_for_backward(params)
-        return angular_cl_device(params.detach().contiguous(), ell, probes, precision, n_limber)
+        return angular_cl_device(params.detach().contiguous(), ell, probes, precision, n_limber, physics=physics)
 
     @staticmethod
     def backward(ctx, gcl):
         (params,) = ctx.saved_tensors
-        ell, probes, n_limber, precision = ctx.meta
-        _, jac = jacobian_device(params.detach().contiguous(), ell, probes, n_limber, precision)
+        ell, probes, n_limber, precision, physics = ctx.meta
+        _, jac = jacobian_device(params.detach().contiguous(), ell, probes, n_limber, precision, physics)
         gp = torch.einsum("bpl,bpld->bd", gcl.to(torch.float64), jac)
-        return gp, None, None, None, None
+        return gp, None, None, None, None, None
 
 
-def angular_cl_autograd(cosmo, ell, probes, precision="fp64", n_limber=512):
+def angular_cl_autograd(cosmo, ell, probes, precision="fp64", n_limber=512, physics=0):
     device = _lib.require_cuda()
     params = cosmo.param_tensor(device, differentiable=True)
-    return _AngularCl.apply(params, ell, probes, precision, n_limber)
+    return _AngularCl.apply(params, ell, probes, precision, n_limber, physics)
 
 
-def angular_cl_jacobian(cosmo, ell, probes, n_limber=512, precision="fp64"):
+def angular_cl_jacobian(cosmo, ell, probes, n_limber=512, precision="fp64", transfer_fn=None, nonlinear_fn=None):
     """(C_ell, dC_ell/dtheta) with theta = (Omega_c, Omega_b, h, n_s, sigma8, Omega_k, w0, wa).
 
     Shapes [n_cls, n_ell] and [n_cls, n_ell, 8] (a leading batch axis for a
-    batched Cosmology).  precision "fp64" or "fp32c".
+    batched Cosmology).  precision "fp64" or "fp32c"; transfer_fn and
+    nonlinear_fn as in ``angular_cl`` (None: the defaults).
     """
+    from jax_cosmo_gb300 import power, transfer
+    from jax_cosmo_gb300.angular_cl import physics_code
+
+    physics = physics_code(transfer_fn or transfer.Eisenstein_Hu, nonlinear_fn or power.halofit)
     device = _lib.require_cuda()
     params = cosmo.param_tensor(device)
-    cl, jac = jacobian_device(params, _geometry.ell_host(ell), probes, n_limber, precision)
+    cl, jac = jacobian_device(params, _geometry.ell_host(ell), probes, n_limber, precision, physics)
     if cosmo.batch_size is None:
         return cl[0], jac[0]
     return cl, jac

@@ -99,7 +99,10 @@ static int make_header(const jcg_geometry* g, GeoHeader* h) {
     return fail(JCG_ERR_SHAPE, "n_z = %d", n_nodes);
   }
   if (!(g->zmax > 0.0) || !isfinite(g->zmax)) return fail(JCG_ERR_VALUE, "zmax = %g", g->zmax);
+  if ((g->physics & ~(JCG_PK_MASK | JCG_TF_NOWIGGLE)) != 0 || pk_model(g->physics) > JCG_PK_LINEAR)
+    return fail(JCG_ERR_UNSUPPORTED, "physics = 0x%x", g->physics);
   memset(h, 0, sizeof(*h));
+  h->physics = g->physics;
   h->magic = GEO_MAGIC;
   h->n_tr = g->n_tracers;
   h->n_ell = g->n_ell;
@@ -275,6 +278,8 @@ static Batch make_batch(const GeoHeader* h, const void* geo, const double* param
   b.n_wl_groups = h ? h->n_groups : 0;
   b.special_bias = h ? h->special_bias : 0;
   b.has_delta = h ? h->has_delta : 0;
+  b.physics = h ? h->physics : 0;
+  b.physics_or = b.physics;
   return b;
 }
 
@@ -503,13 +508,18 @@ int jcg_eval_points(const double* params, int n_cosmo, const double* a, const do
   int rc = check_common(params, n_cosmo, JCG_FP64, ws, ws_bytes, ws_layout(nullptr, n_cosmo, JCG_FP64).total);
   if (rc) return rc;
   if (n < 1) return fail(JCG_ERR_SHAPE, "n = %d", n);
-  if (what < 0 || what > 13) return fail(JCG_ERR_ARG, "what = %d", what);
-  const bool need_a = (what <= 3) || what >= 5;  // a_of_chi (12) takes chi in a_dev
-  const bool need_k = (what >= 4 && what <= 6);
+  const int phys = what >> 8;
+  if (what < 0 || (what & 0xff) > 13) return fail(JCG_ERR_ARG, "what = %d", what);
+  if ((phys & ~(JCG_PK_MASK | JCG_TF_NOWIGGLE)) != 0 || pk_model(phys) > JCG_PK_LINEAR)
+    return fail(JCG_ERR_UNSUPPORTED, "physics = 0x%x", phys);
+  const int q = what & 0xff;
+  const bool need_a = (q <= 3) || q >= 5;  // a_of_chi (12) takes chi in a_dev
+  const bool need_k = (q >= 4 && q <= 6);
   if ((need_a && !a) || (need_k && !k) || !out) return fail(JCG_ERR_ARG, "NULL input or output");
   ConstTables* c;
   if ((rc = const_tables(&c))) return rc;
-  const Batch b = make_batch(nullptr, nullptr, params, n_cosmo, JCG_FP64, ws, nullptr);
+  Batch b = make_batch(nullptr, nullptr, params, n_cosmo, JCG_FP64, ws, nullptr);
+  b.physics = b.physics_or = phys;
   launch_cosmo_tables(b, c, stream);
   launch_eval_points(params, n_cosmo, b.ctab, c, a, k, n, what, out, stream);
   return cuda_check("eval points");
@@ -830,7 +840,8 @@ extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, int pr
       o += align256(sizeof(double) * (size_t)h.n_tr * h.na);
       it.cl = reqs[i].cl_dev;
       it.precision = precision;
-      it.pad = 0;
+      it.physics = h.physics;
+      b.physics_or |= h.physics;
       b.max_na = max(b.max_na, h.na);
       b.max_ell = max(b.max_ell, h.n_ell);
       b.max_cls = max(b.max_cls, h.n_cls);

@@ -487,7 +487,7 @@ __device__ __forceinline__ void growth_qrT(const BgT<T>& b, double x, T& q, T& r
 
 // transfer.py:47-142, core.py:145-162 (cosmo_scalars of jcg_tables.cu)
 template <class T>
-__device__ void cosmo_scalarsT(const T* p, T* s) {
+__device__ void cosmo_scalarsT(const T* p, T* s, bool nowiggle) {
   for (int i = 0; i < NSCAL; ++i) s[i] = T(p[0] * 0.0);
   const T Oc = p[0], Ob = p[1], h = p[2];
   s[S_OMEGA_C] = Oc;
@@ -547,6 +547,10 @@ __device__ void cosmo_scalarsT(const T* p, T* s) {
   s[S_FC] = fc;
   s[S_LGQ] = xlog(13.41 * k_eq);
   s[S_LGKSILK] = xlog(k_silk);
+  // transfer.py:88-100
+  s[S_AGAM] = 1.0 - 0.328 * xlog(431.0 * w_m) * w_b / w_m + 0.38 * xlog(22.3 * w_m) * ((Ob / Om) * (Ob / Om));
+  s[S_NWQ] = T27 / (Om * h);
+  s[S_TFNW] = T(p[0] * 0.0 + (nowiggle ? 1.0 : 0.0));
 }
 
 // Shuffles of a double or a Dual<1> within a 16-lane half warp (every lane
@@ -567,7 +571,7 @@ __device__ __forceinline__ Dual<1> shfl_t(const Dual<1>& x, int src) {
 // results broadcast by shuffles).  The chain's latency is that of 5 levels
 // instead of about 25 calls.  s is written by every lane.
 template <class T>
-__device__ void cosmo_scalars_warpT(const T* p, T* s, int lane) {
+__device__ void cosmo_scalars_warpT(const T* p, T* s, int lane, bool nowiggle) {
   const T one = T(p[0] * 0.0 + 1.0);
   for (int i = 0; i < NSCAL; ++i) s[i] = T(p[0] * 0.0);
   const T Oc = p[0], Ob = p[1], h = p[2];
@@ -620,13 +624,15 @@ __device__ void cosmo_scalars_warpT(const T* p, T* s, int lane) {
     default: break;
   }
   if (lane == 0) lg = 13.41 * k_eq;
+  if (lane == 1) lg = 431.0 * w_m;
+  if (lane == 2) lg = 22.3 * w_m;
   const T P1 = xpow(pb, pe), S1 = xsqrt(sq), L1 = xlog(lg);
   const T A0 = shfl_t(P1, 0), A1 = shfl_t(P1, 1), A2 = shfl_t(P1, 2), A3 = shfl_t(P1, 3);
   const T A4 = shfl_t(P1, 4), A5 = shfl_t(P1, 5), A6 = shfl_t(P1, 6), A7 = shfl_t(P1, 7);
   const T A8 = shfl_t(P1, 8), A9 = shfl_t(P1, 9), A10 = shfl_t(P1, 10), A11 = shfl_t(P1, 11);
   const T A12 = shfl_t(P1, 12), A13 = shfl_t(P1, 13), A14 = shfl_t(P1, 14), FB3 = shfl_t(P1, 15);
   const T sq6 = shfl_t(S1, 0), sqeq = shfl_t(S1, 1), sqbb = shfl_t(S1, 2);
-  const T lgq = shfl_t(L1, 0);
+  const T lgq = shfl_t(L1, 0), lg431 = shfl_t(L1, 1), lg223 = shfl_t(L1, 2);
   // level 2: pows with parameter-dependent exponents, log(k_silk)
   const T b1 = 0.313 * A0 * (1.0 + 0.607 * A1);
   const T b2 = 0.238 * A2;
@@ -693,12 +699,30 @@ __device__ void cosmo_scalars_warpT(const T* p, T* s, int lane) {
   s[S_QINV] = 1.0 / (13.41 * k_eq);
   s[S_ISH] = 1.0 / sh_d;
   s[S_C142AC] = 14.2 / alpha_c;
+  // transfer.py:88-100
+  s[S_AGAM] = 1.0 - 0.328 * lg431 * w_b / w_m + 0.38 * lg223 * ((Ob / Om) * (Ob / Om));
+  s[S_NWQ] = T27 / (Om * h);
+  s[S_TFNW] = T(p[0] * 0.0 + (nowiggle ? 1.0 : 0.0));
 }
 
-// transfer.py:107-153 at a fixed wavenumber k (lk = log k)
+// transfer.py:88-105, type "eisenhu", at a fixed wavenumber k; not inlined,
+// so that the oscillating fit's callers keep their registers
 template <class T>
+__device__ __noinline__ T eh_nowiggleT(T sh_d, T ag, T nwq, double k) {
+  const T x = 0.43 * k * sh_d, x2 = x * x;
+  const T q = k * nwq / (ag + (1.0 - ag) / (1.0 + x2 * x2));
+  const T L = xlog(2.0 * EULER_E + 1.8 * q);
+  const T C = 14.2 + 731.0 / (1.0 + 62.5 * q);
+  return L / (L + C * q * q);
+}
+
+// transfer.py:107-153 at a fixed wavenumber k (lk = log k); type "eisenhu"
+// (S_TFNW set) by eh_nowiggleT unless NW = false (scalars known to be of type
+// "eisenhu_osc")
+template <bool NW = true, class T>
 __device__ __forceinline__ T eh_transferT(const T* s, double k, double lk) {
   const T k_eq = s[S_K_EQ], sh_d = s[S_SH_D];
+  if (NW && val(s[S_TFNW]) != 0.0) return eh_nowiggleT(sh_d, s[S_AGAM], s[S_NWQ], k);
   const T q = k / (13.41 * k_eq);
   const T q108 = xexp(1.08 * (lk - s[S_LGQ]));
   const T Cb = 386.0 / (1.0 + 69.9 * q108);
@@ -724,11 +748,63 @@ __device__ __forceinline__ T eh_transferT(const T* s, double k, double lk) {
 }
 
 // power.py:42-53 at a fixed wavenumber
-template <class T>
+template <bool NW = true, class T>
 __device__ __forceinline__ T pk_linearT(const T* s, double k, double lk, const T& g) {
-  const T t = eh_transferT(s, k, lk);
+  const T t = eh_transferT<NW>(s, k, lk);
   const T pk = xexp(s[S_NS] * lk) * (t * t) * (g * g);
   return pk * s[S_PKNORM];
+}
+
+// Halofit coefficients at one scale factor from n_eff, C, Omega_m(a),
+// Omega_de(a) and w(a): takahashi2012 (power.py:199-224, 235-238) or smith2003
+// (power.py:182-198, 239-242, with frac = Omega_de / (1 - Omega_m) of
+// power.py:180).  lcf3 = log(c_n f3); mu = 0 for takahashi2012.
+template <class T>
+struct HfCoef {
+  T an, bn, cn, gam, alpha, beta, mu, nu, f1, f2, f3, lcf3;
+};
+template <class T>
+__device__ __forceinline__ HfCoef<T> hf_coefs(int model, const T& n, const T& C, const T& om_m,
+                                              const T& om_de, const T& w) {
+  constexpr double L10 = 2.302585092994046;
+  HfCoef<T> r;
+  const T n2 = n * n, n3 = n2 * n, n4 = n2 * n2;
+  const T lom = xlog(om_m);
+  if (model == JCG_PK_SMITH2003) {
+    const T e_cn = -0.2807 + 0.6669 * n + 0.3214 * n2 - 0.0793 * C;
+    r.an = xexp(L10 * (1.4861 + 1.8369 * n + 1.6762 * n2 + 0.7940 * n3 + 0.1670 * n4 - 0.6206 * C));
+    r.bn = xexp(L10 * (0.9463 + 0.9466 * n + 0.3084 * n2 - 0.9400 * C));
+    r.cn = xexp(L10 * e_cn);
+    r.gam = 0.8649 + 0.2989 * n + 0.1631 * C;
+    r.alpha = 1.3884 + 0.3700 * n - 0.1452 * n2;
+    r.beta = 0.8291 + 0.9854 * n + 0.3401 * n2;
+    r.mu = xexp(L10 * (-3.5442 + 0.1908 * n));
+    r.nu = xexp(L10 * (0.9585 + 1.2857 * n));
+    const T frac = om_de / (1.0 - om_m);
+    const T ofr = 1.0 - frac;
+    r.f1 = frac * xexp(-0.0307 * lom) + ofr * xexp(-0.0732 * lom);
+    r.f2 = frac * xexp(-0.0585 * lom) + ofr * xexp(-0.1423 * lom);
+    r.f3 = frac * xexp(0.0743 * lom) + ofr * xexp(0.0725 * lom);
+    r.lcf3 = L10 * e_cn + xlog(r.f3);
+  } else {
+    const T e_an = 1.5222 + 2.8553 * n + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 - 0.6038 * C +
+                   0.1749 * om_de * (1.0 + w);
+    const T e_bn = -0.5642 + 0.5864 * n + 0.5716 * n2 - 1.5474 * C + 0.2279 * om_de * (1.0 + w);
+    const T e_cn = 0.3698 + 2.0404 * n + 0.8161 * n2 + 0.5869 * C;
+    r.an = xexp(L10 * e_an);
+    r.bn = xexp(L10 * e_bn);
+    r.cn = xexp(L10 * e_cn);
+    r.gam = 0.1971 - 0.0843 * n + 0.8460 * C;
+    r.alpha = xfabs(6.0835 + 1.3373 * n - 0.1959 * n2 - 5.5274 * C);
+    r.beta = 2.0379 - 0.7354 * n + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
+    r.mu = 0.0 * n;
+    r.nu = xexp(L10 * (5.2105 + 3.6902 * n));
+    r.f1 = xexp(-0.0307 * lom);
+    r.f2 = xexp(-0.0585 * lom);
+    r.f3 = xexp(0.0743 * lom);
+    r.lcf3 = L10 * e_cn + 0.0743 * lom;
+  }
+  return r;
 }
 
 }  // namespace jcg

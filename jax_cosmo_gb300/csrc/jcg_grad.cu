@@ -30,7 +30,8 @@ namespace jcg {
 // lane; the sigma^2(R) tangents are FP32 sums; float copies of the chi and
 // P(k) k^3 tangent tables are written for the FP32 stages.  The sequential
 // scans (chi prefix sum, growth RK4, Romberg) stay FP64 Dual<1>.
-template <bool F32T>
+// NW: some item may use the transfer type "eisenhu"
+template <bool F32T, bool NW>
 __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.x;
   if (item >= gb.n_items) return;
@@ -95,7 +96,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       const double k = exp(logk);
       const double x = k * 8.0;
       const double wf = 3.0 * (sin(x) - x * cos(x)) / (x * x * x);
-      const D1 T = eh_transferT(sD, k, logk);
+      const D1 T = eh_transferT<NW>(sD, k, logk);
       const D1 pk = (T * T) * xexp(sD[S_NS] * logk);
       const double kw = k * wf;
       put(fr, NROMB, e, k * (kw * kw) * pk);
@@ -133,7 +134,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     }
     for (int e = t; e < NROMB; e += blockDim.x) {
       const double logk = c->romb_logk[e];
-      const F8 T = eh_transferT(sF, c->romb_k[e], logk);
+      const F8 T = eh_transferT<NW>(sF, c->romb_k[e], logk);
       putf(fr, NROMB, e, c->romb_kw2[e] * ((T * T) * xexp(sF[S_NS] * logk)));
     }
   }
@@ -364,7 +365,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
   if (!F32T) {
     for (int e = it; e < NKH; e += 32) {
       const double k = c->kh[e];
-      const D1 p3 = pk_linearT(sD, k, c->logk[e], g1) * c->kh3[e];
+      const D1 p3 = pk_linearT<NW>(sD, k, c->logk[e], g1) * c->kh3[e];
       if (dir == 0) out->pk3v[e] = p3.v;
       out->pk3d[dir][e] = p3.d[0];
       put(pq, NKH, e, p3 / (2.0 * (PI * PI)));
@@ -382,7 +383,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
         const F8 u = f8_of(gu[e], gu + NKH + e, NKH);
         p3 = ((u * (g1f * g1f)) * sF[S_PKNORM]) * c->kh3[e];
       } else {
-        p3 = pk_linearT(sF, k, c->logk[e], g1f) * c->kh3[e];
+        p3 = pk_linearT<NW>(sF, k, c->logk[e], g1f) * c->kh3[e];
       }
       out->pk3v[e] = p3.v;
 #pragma unroll
@@ -652,25 +653,21 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
   D1 om_m, om_de;
   omT(bg, a, lna, om_m, om_de);
   const D1 w = wT(bg, a);
-  const D1 n2 = neff * neff, n3 = n2 * neff, n4 = n2 * n2;
-  const D1 e_an = 1.5222 + 2.8553 * neff + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 - 0.6038 * C +
-                  0.1749 * om_de * (1.0 + w);
-  const D1 e_bn = -0.5642 + 0.5864 * neff + 0.5716 * n2 - 1.5474 * C + 0.2279 * om_de * (1.0 + w);
-  const D1 e_cn = 0.3698 + 2.0404 * neff + 0.8161 * n2 + 0.5869 * C;
-  const D1 lom = xlog(om_m);
+  const HfCoef<D1> hc = hf_coefs<D1>(pk_model(gi.geo->physics), neff, C, om_m, om_de, w);
   D1 outv[NA_IN];
   outv[A_CHIC] = xfmax(chi, 1.0);
   outv[A_G] = g;
   outv[A_KNL] = knl;
-  outv[A_BETA] = 2.0379 - 0.7354 * neff + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
-  outv[A_ALPHA] = xfabs(6.0835 + 1.3373 * neff - 0.1959 * n2 - 5.5274 * C);
-  outv[A_AN] = xexp(LN10_G * e_an);
-  outv[A_BN] = xexp(LN10_G * e_bn);
-  outv[A_LCF3] = LN10_G * e_cn + 0.0743 * lom;
-  outv[A_F1] = xexp(-0.0307 * lom);
-  outv[A_F2] = xexp(-0.0585 * lom);
-  outv[A_GAM] = 0.1971 - 0.0843 * neff + 0.8460 * C;
-  outv[A_NU] = xexp(LN10_G * (5.2105 + 3.6902 * neff));
+  outv[A_BETA] = hc.beta;
+  outv[A_ALPHA] = hc.alpha;
+  outv[A_AN] = hc.an;
+  outv[A_BN] = hc.bn;
+  outv[A_LCF3] = hc.lcf3;
+  outv[A_F1] = hc.f1;
+  outv[A_F2] = hc.f2;
+  outv[A_GAM] = hc.gam;
+  outv[A_NU] = hc.nu;
+  outv[A_MU] = hc.mu;
   const D1 dchi = dchioverdaT(bg, a, lna);
   outv[A_U] = WS[n] * dchi / xfmax(chi * chi, 1.0) / C2_G;
   if (live) {
@@ -702,9 +699,10 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
         row[F_LG2CF3] = (float)(LOG2E * outv[A_LCF3].v);
         row[F_3MGAMMA] = (float)(3.0 - outv[A_GAM].v);
         row[F_NUN] = (float)outv[A_NU].v;
+        row[F_MUN] = (float)outv[A_MU].v;
         row[F_U] = (float)outv[A_U].v;
       }
-      float* tg = row + NROW32;
+      float* tg = row + NROWV;
       tg[T_CHIC * NDIR + dir] = (float)chic.d[0];
       tg[T_D2FAC * NDIR + dir] = (float)d2fac.d[0];
       tg[T_KNL * NDIR + dir] = (float)kn.d[0];
@@ -717,6 +715,7 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
       tg[T_LG2CF3 * NDIR + dir] = (float)(LOG2E * outv[A_LCF3].d[0]);
       tg[T_3MG * NDIR + dir] = (float)(-outv[A_GAM].d[0]);
       tg[T_NUN * NDIR + dir] = (float)outv[A_NU].d[0];
+      tg[T_MUN * NDIR + dir] = (float)outv[A_MU].d[0];
       tg[T_U * NDIR + dir] = (float)outv[A_U].d[0];
     }
   }
@@ -752,7 +751,7 @@ __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb,
   const int64_t* SG = geo_ptr<int64_t>(geo, geo->off_seg_grow);
   const double a = A[n];
   float* row = gi.rowg + (size_t)n * NROWG;
-  float* tg = row + NROW32;
+  float* tg = row + NROWV;
   auto put_t = [&](int slot, const F8& x, float sc) {
 #pragma unroll
     for (int d = 0; d < NDIR; ++d) tg[slot * NDIR + d] = x.d[d] * sc;
@@ -922,47 +921,97 @@ __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb,
   const double lna = log(a);
   F8 om_m, om_de;
   omT(bg, a, lna, om_m, om_de);
-  const F8 opw = om_de * (1.0 + wT(bg, a));
+  // halofit coefficients (power.py:177-244), each stored as soon as it is
+  // formed (short live ranges of the 8-tangent values)
   const F8 n2 = neff * neff, n3 = n2 * neff, n4 = n2 * n2;
-  {
-    const F8 beta = 2.0379 - 0.7354 * neff + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
-    row[F_BETAN] = (float)beta.v;
-    put_t(T_BETAN, beta, 1.f);
-    const F8 alpha = xfabs(6.0835 + 1.3373 * neff - 0.1959 * n2 - 5.5274 * C);
-    row[F_ALPHAN] = (float)alpha.v;
-    put_t(T_ALPHAN, alpha, 1.f);
-  }
-  {
-    const F8 e_an = 1.5222 + 2.8553 * neff + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 - 0.6038 * C + 0.1749 * opw;
-    const F8 an = xexp(LN10_G * e_an);
-    row[F_AN] = (float)an.v;
-    put_t(T_AN, an, 1.f);
-    const F8 e_bn = -0.5642 + 0.5864 * neff + 0.5716 * n2 - 1.5474 * C + 0.2279 * opw;
-    const F8 bn = xexp(LN10_G * e_bn);
-    row[F_BN] = (float)bn.v;
-    put_t(T_BN, bn, 1.f);
-  }
-  {
-    constexpr double LOG2E = 1.4426950408889634;
-    const F8 lom = xlog(om_m);
-    const F8 e_cn = 0.3698 + 2.0404 * neff + 0.8161 * n2 + 0.5869 * C;
-    const F8 lcf3 = LN10_G * e_cn + 0.0743 * lom;
-    row[F_LG2CF3] = (float)(LOG2E * lcf3.v);
-    put_t(T_LG2CF3, lcf3, (float)LOG2E);
-    const F8 f1 = xexp(-0.0307 * lom);
-    row[F_3F1] = (float)(3.0 * f1.v);
-    put_t(T_3F1, f1, 3.f);
-    const F8 f2 = xexp(-0.0585 * lom);
-    row[F_F2] = (float)f2.v;
-    put_t(T_F2, f2, 1.f);
-  }
-  {
-    const F8 gam = 0.1971 - 0.0843 * neff + 0.8460 * C;
-    row[F_3MGAMMA] = (float)(3.0 - gam.v);
-    put_t(T_3MG, gam, -1.f);
-    const F8 nu = xexp(LN10_G * (5.2105 + 3.6902 * neff));
-    row[F_NUN] = (float)nu.v;
-    put_t(T_NUN, nu, 1.f);
+  constexpr double LOG2E = 1.4426950408889634;
+  if (pk_model(gi.geo->physics) == JCG_PK_SMITH2003) {
+    // power.py:182-198, 239-242
+    {
+      const F8 beta = 0.8291 + 0.9854 * neff + 0.3401 * n2;
+      row[F_BETAN] = (float)beta.v;
+      put_t(T_BETAN, beta, 1.f);
+      const F8 alpha = 1.3884 + 0.3700 * neff - 0.1452 * n2;
+      row[F_ALPHAN] = (float)alpha.v;
+      put_t(T_ALPHAN, alpha, 1.f);
+    }
+    {
+      const F8 an = xexp(LN10_G * (1.4861 + 1.8369 * neff + 1.6762 * n2 + 0.7940 * n3 + 0.1670 * n4 - 0.6206 * C));
+      row[F_AN] = (float)an.v;
+      put_t(T_AN, an, 1.f);
+      const F8 bn = xexp(LN10_G * (0.9463 + 0.9466 * neff + 0.3084 * n2 - 0.9400 * C));
+      row[F_BN] = (float)bn.v;
+      put_t(T_BN, bn, 1.f);
+    }
+    {
+      const F8 lom = xlog(om_m);
+      const F8 frac = om_de / (1.0 - om_m);
+      const F8 ofr = 1.0 - frac;
+      const F8 f1 = frac * xexp(-0.0307 * lom) + ofr * xexp(-0.0732 * lom);
+      row[F_3F1] = (float)(3.0 * f1.v);
+      put_t(T_3F1, f1, 3.f);
+      const F8 f2 = frac * xexp(-0.0585 * lom) + ofr * xexp(-0.1423 * lom);
+      row[F_F2] = (float)f2.v;
+      put_t(T_F2, f2, 1.f);
+      const F8 f3 = frac * xexp(0.0743 * lom) + ofr * xexp(0.0725 * lom);
+      const F8 lcf3 = LN10_G * (-0.2807 + 0.6669 * neff + 0.3214 * n2 - 0.0793 * C) + xlog(f3);
+      row[F_LG2CF3] = (float)(LOG2E * lcf3.v);
+      put_t(T_LG2CF3, lcf3, (float)LOG2E);
+    }
+    {
+      const F8 gam = 0.8649 + 0.2989 * neff + 0.1631 * C;
+      row[F_3MGAMMA] = (float)(3.0 - gam.v);
+      put_t(T_3MG, gam, -1.f);
+      const F8 nu = xexp(LN10_G * (0.9585 + 1.2857 * neff));
+      row[F_NUN] = (float)nu.v;
+      put_t(T_NUN, nu, 1.f);
+      const F8 mu = xexp(LN10_G * (-3.5442 + 0.1908 * neff));
+      row[F_MUN] = (float)mu.v;
+      put_t(T_MUN, mu, 1.f);
+    }
+  } else {
+    const F8 opw = om_de * (1.0 + wT(bg, a));
+    {
+      const F8 beta = 2.0379 - 0.7354 * neff + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
+      row[F_BETAN] = (float)beta.v;
+      put_t(T_BETAN, beta, 1.f);
+      const F8 alpha = xfabs(6.0835 + 1.3373 * neff - 0.1959 * n2 - 5.5274 * C);
+      row[F_ALPHAN] = (float)alpha.v;
+      put_t(T_ALPHAN, alpha, 1.f);
+    }
+    {
+      const F8 e_an = 1.5222 + 2.8553 * neff + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 - 0.6038 * C + 0.1749 * opw;
+      const F8 an = xexp(LN10_G * e_an);
+      row[F_AN] = (float)an.v;
+      put_t(T_AN, an, 1.f);
+      const F8 e_bn = -0.5642 + 0.5864 * neff + 0.5716 * n2 - 1.5474 * C + 0.2279 * opw;
+      const F8 bn = xexp(LN10_G * e_bn);
+      row[F_BN] = (float)bn.v;
+      put_t(T_BN, bn, 1.f);
+    }
+    {
+      const F8 lom = xlog(om_m);
+      const F8 e_cn = 0.3698 + 2.0404 * neff + 0.8161 * n2 + 0.5869 * C;
+      const F8 lcf3 = LN10_G * e_cn + 0.0743 * lom;
+      row[F_LG2CF3] = (float)(LOG2E * lcf3.v);
+      put_t(T_LG2CF3, lcf3, (float)LOG2E);
+      const F8 f1 = xexp(-0.0307 * lom);
+      row[F_3F1] = (float)(3.0 * f1.v);
+      put_t(T_3F1, f1, 3.f);
+      const F8 f2 = xexp(-0.0585 * lom);
+      row[F_F2] = (float)f2.v;
+      put_t(T_F2, f2, 1.f);
+    }
+    {
+      const F8 gam = 0.1971 - 0.0843 * neff + 0.8460 * C;
+      row[F_3MGAMMA] = (float)(3.0 - gam.v);
+      put_t(T_3MG, gam, -1.f);
+      const F8 nu = xexp(LN10_G * (5.2105 + 3.6902 * neff));
+      row[F_NUN] = (float)nu.v;
+      put_t(T_NUN, nu, 1.f);
+      row[F_MUN] = 0.f;
+      put_t(T_MUN, 0.0 * nu, 0.f);
+    }
   }
   {
     const F8 chic = xfmax(chi, 1.0);
@@ -1096,17 +1145,20 @@ __global__ void __launch_bounds__(256) grad_kern_kernel(GradBatch gb, const Cons
 
 // ------------------------------------------------ Limber integrand adjoint --
 struct NodeX {
-  double chic, g, knl, beta, alpha, an, bn, lcf3, f1, f2, gam, nu;
+  double chic, g, knl, beta, alpha, an, bn, lcf3, f1, f2, gam, nu, mu;
 };
 struct NodeK {
   double keq, sh, betac, alphac, alphab, betab, betanode, ksilk, fb, fc, ns, pknorm;
+  double agam, nwq;  // transfer type "eisenhu"
+  bool nw;
 };
 
 // P(k = kh / chic, a) of halofit_node_lk (Eisenstein-Hu x primordial x
 // takahashi2012, transfer.py:107-153, power.py:42-53, 246-260) and its
 // partial derivatives: ga[NodeA] (per-node inputs) and gc[NodeC]
 // (per-cosmology inputs) receive dP/d(input).  Hand-written reverse sweep.
-__device__ double node_fb(double kh, double lkh, const NodeX& x, const NodeK& c, double* ga, double* gc) {
+__device__ double node_fb(double kh, double lkh, const NodeX& x, const NodeK& c, double* ga, double* gc,
+                          bool lin) {
   // forward
   const double k = kh / x.chic;
   const double lk = lkh - log(x.chic);
@@ -1139,7 +1191,18 @@ __device__ double node_fb(double kh, double lkh, const NodeX& x, const NodeK& c,
   const double sinc = sn / arg;
   const double Tbr0 = Tn / E52 + c.alphab / Bb * silk;
   const double Tbar = Tbr0 * sinc;
-  const double T = c.fb * Tbar + c.fc * Tc;
+  // type "eisenhu" (transfer.py:88-105); the oscillating fit above is then
+  // evaluated too but gets a zero adjoint
+  const double xn = 0.43 * k * c.sh, xn2 = xn * xn;
+  const double un = 1.0 / (1.0 + xn2 * xn2);
+  const double gen = c.agam + (1.0 - c.agam) * un;
+  const double qn = k * c.nwq / gen;
+  const double An = 2.0 * EULER_E + 1.8 * qn;
+  const double Ln = log(An);
+  const double rcn = 1.0 / (1.0 + 62.5 * qn);
+  const double Cn = 14.2 + 731.0 * rcn;
+  const double Dtn = Ln + Cn * qn * qn;
+  const double T = c.nw ? Ln / Dtn : c.fb * Tbar + c.fc * Tc;
   const double eP = exp(c.ns * lk);
   const double gg = x.g * x.g;
   const double pklin = eP * (T * T) * gg * c.pknorm;
@@ -1160,19 +1223,20 @@ __device__ double node_fb(double kh, double lkh, const NodeX& x, const NodeK& c,
   const double H3 = exp(E3a * E3b);
   const double D = 1.0 + x.bn * H2 + H3;
   const double d2hp = x.an * H1 / D;
-  const double y2 = y * y, yn = y2 + x.nu;
+  const double y2 = y * y, yn = (y2 + x.mu * y) + x.nu;
   const double Rr = y2 / yn;
   const double d2h = d2hp * Rr;
-  const double S = d2q + d2h;
+  const double S = lin ? d2l : d2q + d2h;  // lin: linear_matter_power
   const double P = TWO_PI2_G / k3 * S;
   // reverse, seed dP/dP = 1
   const double Sb = TWO_PI2_G / k3;
   double k3b = -P / k3;
-  const double d2qb = Sb, d2hb = Sb;
+  const double d2qb = lin ? 0.0 : Sb, d2hb = d2qb;
   const double d2hpb = d2hb * Rr;
   const double Rb = d2hb * d2hp;
   ga[A_NU] += -Rb * y2 / (yn * yn);
-  double yb = 2.0 * y * (Rb * x.nu / (yn * yn));
+  ga[A_MU] += -Rb * y2 * y / (yn * yn);
+  double yb = Rb * y * (x.mu * y + 2.0 * x.nu) / (yn * yn);
   ga[A_AN] += d2hpb * H1 / D;
   const double H1b = d2hpb * x.an / D;
   const double Dbar = -d2hpb * d2hp / D;
@@ -1184,7 +1248,7 @@ __device__ double node_fb(double kh, double lkh, const NodeX& x, const NodeK& c,
   ga[A_F2] += H2b * H2 * ly;
   ga[A_GAM] += -E3 * E3b;
   ga[A_LCF3] += E3 * E3a;
-  double d2lb = d2qb * Q;
+  double d2lb = lin ? Sb : d2qb * Q;
   const double Qb = d2qb * d2l;
   const double pbb = Qb * efy / den_a;
   const double denab = -Qb * Q / den_a;
@@ -1201,7 +1265,21 @@ __device__ double node_fb(double kh, double lkh, const NodeX& x, const NodeK& c,
   const double pklinb = d2lb * k3 / TWO_PI2_G;
   kb += k3b * 3.0 * k * k;
   const double ePb = pklinb * (T * T) * gg * c.pknorm;
-  const double Tbarr = pklinb * eP * 2.0 * T * gg * c.pknorm;
+  const double Tbn = pklinb * eP * 2.0 * T * gg * c.pknorm;  // adjoint of T
+  if (c.nw) {
+    const double Tv = Ln / Dtn;
+    const double Lnb = Tbn * (1.0 - Tv) / Dtn;
+    const double Dtnb = -Tbn * Tv / Dtn;
+    const double qnb = Dtnb * (Cn * 2.0 * qn - qn * qn * 731.0 * 62.5 * rcn * rcn) + Lnb * 1.8 / An;
+    kb += qnb * c.nwq / gen;
+    gc[C_NWQ] += qnb * k / gen;
+    const double genb = -qnb * qn / gen;
+    gc[C_AGAM] += genb * (1.0 - un);
+    const double xnb = -genb * (1.0 - c.agam) * 4.0 * xn2 * xn * un * un;
+    kb += xnb * 0.43 * c.sh;
+    gc[C_SH] += xnb * 0.43 * k;
+  }
+  const double Tbarr = c.nw ? 0.0 : Tbn;
   ga[A_G] += pklinb * eP * (T * T) * 2.0 * x.g * c.pknorm;
   gc[C_PKNORM] += pklinb * eP * (T * T) * gg;
   gc[C_NS] += ePb * eP * lk;
@@ -1266,6 +1344,7 @@ __global__ void __launch_bounds__(GL_THREADS)
   const GradItem gi = grad_item(gb, item);
   const GeoHeader* geo = gi.geo;
   const int n_ell = geo->n_ell, n_cls = geo->n_cls, na = geo->na;
+  const bool lin = pk_model(geo->physics) == JCG_PK_LINEAR;
   const int l0 = blockIdx.x * LT;
   if (l0 >= n_ell) return;
   const int lt = min(LT, n_ell - l0);
@@ -1301,6 +1380,7 @@ __global__ void __launch_bounds__(GL_THREADS)
   ck.alphab = cvs[C_ALPHAB]; ck.betab = cvs[C_BETAB]; ck.betanode = cvs[C_BETANODE];
   ck.ksilk = cvs[C_KSILK]; ck.fb = cvs[C_FB]; ck.fc = cvs[C_FC]; ck.ns = cvs[C_NS];
   ck.pknorm = cvs[C_PKNORM];
+  ck.agam = cvs[C_AGAM]; ck.nwq = cvs[C_NWQ]; ck.nw = tf_nowiggle(geo->physics);
   const double* rowd = gi.rowd;
   const double* kd = gi.kernd;
   const int nout = lt * n_cls * (NDIR + 1);
@@ -1334,11 +1414,11 @@ __global__ void __launch_bounds__(GL_THREADS)
       NodeX nx;
       nx.chic = xv[A_CHIC]; nx.g = xv[A_G]; nx.knl = xv[A_KNL]; nx.beta = xv[A_BETA];
       nx.alpha = xv[A_ALPHA]; nx.an = xv[A_AN]; nx.bn = xv[A_BN]; nx.lcf3 = xv[A_LCF3];
-      nx.f1 = xv[A_F1]; nx.f2 = xv[A_F2]; nx.gam = xv[A_GAM]; nx.nu = xv[A_NU];
+      nx.f1 = xv[A_F1]; nx.f2 = xv[A_F2]; nx.gam = xv[A_GAM]; nx.nu = xv[A_NU]; nx.mu = xv[A_MU];
       double ga[NA_IN], gcv[NC_IN];
       for (int i = 0; i < NA_IN; ++i) ga[i] = 0.0;
       for (int i = 0; i < NC_IN; ++i) gcv[i] = 0.0;
-      const double P = node_fb(khs[l], lkhs[l], nx, ck, ga, gcv);
+      const double P = node_fb(khs[l], lkhs[l], nx, ck, ga, gcv, lin);
       Pv[t * LT + l] = P;
       for (int d = 0; d < NDIR; ++d) {
         double s = 0.0;
@@ -1489,7 +1569,7 @@ __global__ void __launch_bounds__(128) grad_scalars_kernel(GradBatch gb) {
   D1 p[8];
   for (int i = 0; i < 8; ++i) p[i] = mk1(gi.params[i], i == dir ? 1.0 : 0.0);
   D1 s[NSCAL];
-  cosmo_scalarsT(p, s);
+  cosmo_scalarsT(p, s, tf_nowiggle(gi.geo->physics));
   for (int i = 0; i < NSCAL; ++i) {
     if (dir == 0) gi.tab->sv[i] = s[i].v;
     gi.tab->sd[dir][i] = s[i].d[0];
@@ -1505,17 +1585,19 @@ __global__ void __launch_bounds__(128) grad_scalars_warp_kernel(GradBatch gb) {
   D1 p[8];
   for (int i = 0; i < 8; ++i) p[i] = mk1(gi.params[i], i == dir ? 1.0 : 0.0);
   D1 s[NSCAL];
-  cosmo_scalars_warpT<D1>(p, s, lane);
-  D1 v0 = mk1(0.0, 0.0), v1 = v0;
+  cosmo_scalars_warpT<D1>(p, s, lane, tf_nowiggle(gi.geo->physics));
+  D1 v0 = mk1(0.0, 0.0), v1 = v0, v2 = v0;
 #pragma unroll
   for (int k = 0; k < 16; ++k)
-    if (k == lane) v0 = s[k], v1 = s[k + 16];
+    if (k == lane) v0 = s[k], v1 = s[k + 16], v2 = k + 32 < NSCAL ? s[k + 32] : v0;
   if (dir == 0) {
     gi.tab->sv[lane] = v0.v;
     gi.tab->sv[lane + 16] = v1.v;
+    if (lane + 32 < NSCAL) gi.tab->sv[lane + 32] = v2.v;
   }
   gi.tab->sd[dir][lane] = v0.d[0];
   gi.tab->sd[dir][lane + 16] = v1.d[0];
+  if (lane + 32 < NSCAL) gi.tab->sd[dir][lane + 32] = v2.d[0];
 }
 
 void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
@@ -1526,11 +1608,16 @@ void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
     grad_scalars_kernel<<<(gb.n_items * NDIR + 127) / 128, 128, 0, st>>>(gb);
   if (gb.gnode) grad_nodes_kernel<<<dim3(GNODE_CTAS, gb.n_items), 128, 0, st>>>(gb, c);
   if (gb.precision == JCG_FP32C) {
-    cudaFuncSetAttribute(grad_tables_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
-    grad_tables_kernel<true><<<gb.n_items, 128, smt, st>>>(gb, c);
+    if (tf_nowiggle(gb.physics_or)) {
+      cudaFuncSetAttribute(grad_tables_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+      grad_tables_kernel<true, true><<<gb.n_items, 128, smt, st>>>(gb, c);
+    } else {
+      cudaFuncSetAttribute(grad_tables_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+      grad_tables_kernel<true, false><<<gb.n_items, 128, smt, st>>>(gb, c);
+    }
   } else {
-    cudaFuncSetAttribute(grad_tables_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
-    grad_tables_kernel<false><<<gb.n_items, 256, smt, st>>>(gb, c);
+    cudaFuncSetAttribute(grad_tables_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+    grad_tables_kernel<false, true><<<gb.n_items, 256, smt, st>>>(gb, c);
   }
   if (gb.precision == JCG_FP32C) {
     dim3 grw((gb.na + GR32_THREADS - 1) / GR32_THREADS, gb.n_items);
@@ -1653,6 +1740,7 @@ void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, in
   gb.n_cls = h.n_cls;
   gb.n_ell = h.n_ell;
   gb.n_split = grad_n_split(h, n_cosmo, precision);
+  gb.physics_or = h.physics;
   gb.listed = 0;
   gb.items = nullptr;
   launch_grad(gb, c, st);
@@ -1739,6 +1827,7 @@ cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void*
     gb.n_tr = max(gb.n_tr, h.n_tr);
     gb.n_cls = max(gb.n_cls, h.n_cls);
     gb.n_ell = max(gb.n_ell, h.n_ell);
+    gb.physics_or |= h.physics;
   }
   // pageable source: the copy is staged before the call returns, so the
   // host vector can be reused by the next call of this thread

@@ -65,21 +65,24 @@ struct TabD {
 static_assert(sizeof(TabD) % 64 == 0, "TabD alignment");
 
 // per-node inputs of the Limber integrand (node_fb), value + 8 tangents
-enum NodeA { A_CHIC = 0, A_G, A_KNL, A_BETA, A_ALPHA, A_AN, A_BN, A_LCF3, A_F1, A_F2, A_GAM, A_NU, A_U, NA_IN };
+enum NodeA { A_CHIC = 0, A_G, A_KNL, A_BETA, A_ALPHA, A_AN, A_BN, A_LCF3, A_F1, A_F2, A_GAM, A_NU, A_MU, A_U, NA_IN };
 constexpr int NROWD = NA_IN * (NDIR + 1);  // [NA_IN] values then [NDIR][NA_IN] tangents
 // per-cosmology inputs of the integrand
-enum NodeC { C_KEQ = 0, C_SH, C_BETAC, C_ALPHAC, C_ALPHAB, C_BETAB, C_BETANODE, C_KSILK, C_FB, C_FC, C_NS, C_PKNORM, NC_IN };
+enum NodeC { C_KEQ = 0, C_SH, C_BETAC, C_ALPHAC, C_ALPHAB, C_BETAB, C_BETANODE, C_KSILK, C_FB, C_FC, C_NS, C_PKNORM,
+             C_AGAM, C_NWQ, NC_IN };
 __device__ __constant__ const int kNodeCScalar[NC_IN] = {S_K_EQ,  S_SH_D,      S_BETA_C,  S_ALPHA_C,
                                                          S_ALPHA_B, S_BETA_B, S_BETA_NODE, S_K_SILK,
-                                                         S_FB,    S_FC,        S_NS,      S_PKNORM};
+                                                         S_FB,    S_FC,        S_NS,      S_PKNORM,
+                                                         S_AGAM,  S_NWQ};
 
-// FP32 rows of the compensated Limber Jacobian, per node: the 16 values of
-// the forward FP32 row (Row32 order, slot 15 = the Limber weight u), then the
-// tangents [NGT][NDIR] of the independent inputs below (chi_c and k_nl raw,
-// the others in the units of their Row32 slot).
+// FP32 rows of the compensated Limber Jacobian, per node: NROWV values (the
+// 16 of the forward FP32 row in Row32 order, slot 16 = the Limber weight u,
+// padding), then the tangents [NGT][NDIR] of the independent inputs below
+// (chi_c and k_nl raw, the others in the units of their Row32 slot).
 enum GTan { T_CHIC = 0, T_D2FAC, T_KNL, T_BETAN, T_ALPHAN, T_AN, T_3F1, T_F2, T_BN, T_LG2CF3, T_3MG,
-            T_NUN, T_U, NGT };
-constexpr int F_U = 15;
+            T_NUN, T_MUN, T_U, NGT };
+constexpr int F_U = NROW32;
+constexpr int NROWV = NROW32 + 4;
 // Taylor tables of the fp32c moments, per cosmology: values as float pairs
 // [NKH + 1][NTAYLOR] (in the first NPTTV doubles), then tangents float
 // [NKH + 1][NTAYLOR][NDIR]
@@ -89,10 +92,13 @@ __device__ __forceinline__ float* ptt_tangents(double* p) { return reinterpret_c
 __device__ __forceinline__ const float* ptt_tangents(const double* p) {
   return reinterpret_cast<const float*>(p + NPTTV);
 }
-constexpr int NROWG = NROW32 + NGT * NDIR;  // 120 floats
+constexpr int NROWG = NROWV + NGT * NDIR;  // 132 floats
 // per-cosmology Eisenstein-Hu inputs of the FP32 integrand with tangents
 enum ETan { E_KEQ = 0, E_SH, E_C18BC, E_C142AC, E_ALPHAB, E_BETAB, E_BETANODE, E_LG2KSILK, E_FB, E_FC,
             E_NS3, NET };
+// transfer type "eisenhu": alpha_gamma and (T_cmb / 2.7)^2 / (Omega_m h) in
+// the slots of k_eq and 1.8 beta_c (which that fit does not use)
+constexpr int E_AGAM = E_KEQ, E_NWQ = E_C18BC;
 
 // One (cosmology, geometry) pair of a Jacobian batch.  FP64: rowd / kernd;
 // FP32C: rowg / kernf.
@@ -130,6 +136,7 @@ struct GradBatch {
   double* jac;
   double* gnode;  // fp32c, small batches: the table kernel's node values, per item GNODE_STRIDE doubles
   int na, n_tr, n_cls, n_ell, n_split;
+  int physics_or;  // OR of the items' physics switches (selects kernel variants)
 };
 
 // Small fp32c batches spread the table kernel's per-node evaluations over

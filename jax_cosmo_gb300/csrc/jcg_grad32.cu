@@ -237,13 +237,104 @@ void launch_grad_kern32(const GradBatch& gb, const ConstTables* c, cudaStream_t 
 struct EHg {
   float qinv, lg2_qinv, sh, inv_sh, c18bc, c142ac, alpha_b, beta_b, beta_node, lg2_ksilk, fb, fc, ns3,
       inv_keq;
+  float agam, nwq;  // type "eisenhu"
 };
 
-// P of node32 (the forward fp32c integrand) and its reverse sweep.  an[GTan]
-// (T_CHIC..T_NUN) and ae[ETan] receive dP/d(input) in the units of the
-// stored tangents.
+// The power-spectrum part of node32_fb: from the transfer value T at (k, lk),
+// P = k^(ns+3) T^2 D2FAC 2 pi^2 / k^3 (linear) or its halofit form
+// (power.py:246-260), and the reverse sweep: an[] of the row's power inputs
+// (T_D2FAC, T_KNL, T_BETAN..T_MUN), ae[E_NS3], the adjoint Tbv of T, and
+// the adjoints of k, lk and 1/k accumulated into kb, lkb, invkb.  GEN =
+// false: takahashi2012 only (lin and mu_n not read).
+template <bool GEN>
+__device__ __forceinline__ float pk32_fb(const EHg& e, const float* r, float k, float lk, float invk, float T,
+                                         bool lin, float* an, float* ae, float& Tbv, float& kb, float& lkb,
+                                         float& invkb) {
+  const float eP = ex2f(e.ns3 * lk);
+  const float T2 = T * T;
+  const float d2l = eP * T2 * r[F_D2FAC];
+  const float y = k * r[F_INVKNL];
+  const float ly = lk - r[F_LG2KNL];
+  const float efy = ex2f(-LOG2E_F * (y * (0.25f + 0.125f * y)));
+  const float lg1 = lg2f(1.f + d2l);
+  const float pb = ex2f(r[F_BETAN] * lg1);
+  const float rden_a = rcpf(1.f + r[F_ALPHAN] * d2l);
+  const float Q = pb * rden_a * efy;
+  const float d2q = d2l * Q;
+  const float H1 = ex2f(r[F_3F1] * ly);
+  const float H2 = ex2f(r[F_F2] * ly);
+  const float E3b = r[F_LG2CF3] + ly;
+  const float H3 = ex2f(r[F_3MGAMMA] * E3b);
+  const float rD = rcpf(1.f + r[F_BN] * H2 + H3);
+  const float d2hp = r[F_AN] * H1 * rD;
+  const float y2 = y * y;
+  const float ryn = rcpf((GEN ? fmaf(r[F_MUN], y, y2) : y2) + r[F_NUN]);
+  const float Rr = y2 * ryn;
+  const float d2h = d2hp * Rr;
+  const float S = (GEN && lin) ? d2l : d2q + d2h;  // lin: linear_matter_power
+  const float ik3 = invk * invk * invk;
+  const float P = TWO_PI2_F * ik3 * S;
+  // ---- reverse, seed dP/dP = 1
+  const float Sb = TWO_PI2_F * ik3;
+  const float Sh = (GEN && lin) ? 0.f : Sb;  // adjoint of the halofit terms
+  invkb += TWO_PI2_F * S * 3.f * invk * invk;
+  // d2h = d2hp y^2 / (y^2 + mu y + nu)
+  const float d2hpb = Sh * Rr;
+  const float Rrb = Sh * d2hp;
+  const float NUNb = -Rrb * Rr * ryn;
+  const float MUNb = NUNb * y;
+  float yb = GEN ? Rrb * ryn * (2.f * y * (1.f - Rr) - r[F_MUN] * Rr) : 2.f * y * (Rrb * ryn * (1.f - Rr));
+  const float ANb = d2hpb * H1 * rD;
+  const float H1b = d2hpb * r[F_AN] * rD;
+  const float Dbar = -d2hpb * d2hp * rD;
+  const float BNb = Dbar * H2;
+  const float H2b = Dbar * r[F_BN];
+  const float u1 = H1b * H1 * LN2_F, u2 = H2b * H2 * LN2_F, u3 = Dbar * H3 * LN2_F;
+  const float F3F1b = u1 * ly, F2b = u2 * ly, F3MGb = u3 * E3b, LG2CF3b = u3 * r[F_3MGAMMA];
+  const float lyb = u1 * r[F_3F1] + u2 * r[F_F2] + u3 * r[F_3MGAMMA];
+  lkb += lyb;
+  const float LG2KNLb = -lyb;
+  // d2q = d2l Q, Q = (1 + d2l)^beta / (1 + alpha d2l) exp(-f(y))
+  float d2lb = (GEN && lin) ? Sb : Sb * Q;
+  const float Qb = Sh * d2l;
+  const float pbb = Qb * rden_a * efy;
+  const float denab = -Qb * Q * rden_a;
+  const float efyb = Qb * pb * rden_a;
+  const float ALPHANb = denab * d2l;
+  d2lb += denab * r[F_ALPHAN];
+  const float vpb = pbb * pb * LN2_F;
+  const float BETANb = vpb * lg1;
+  d2lb += vpb * r[F_BETAN] * LOG2E_F * rcpf(1.f + d2l);
+  yb -= efyb * efy * (0.25f + 0.25f * y);
+  kb += yb * r[F_INVKNL];
+  const float INVKNLb = yb * k;
+  // d2l = k^(ns+3) T^2 D2FAC
+  const float ePb = d2lb * T2 * r[F_D2FAC];
+  Tbv = d2lb * eP * 2.f * T * r[F_D2FAC];
+  const float vep = ePb * eP * LN2_F;
+  lkb += vep * e.ns3;
+  an[T_D2FAC] = d2lb * eP * T2;
+  an[T_KNL] = -INVKNLb * r[F_INVKNL] * r[F_INVKNL] + LG2KNLb * LOG2E_F * r[F_INVKNL];
+  an[T_BETAN] = BETANb;
+  an[T_ALPHAN] = ALPHANb;
+  an[T_AN] = ANb;
+  an[T_3F1] = F3F1b;
+  an[T_F2] = F2b;
+  an[T_BN] = BNb;
+  an[T_LG2CF3] = LG2CF3b;
+  an[T_3MG] = F3MGb;
+  an[T_NUN] = NUNb;
+  an[T_MUN] = GEN ? MUNb : 0.f;
+  ae[E_NS3] = vep * lk;
+  return P;
+}
+
+// P of node32 (the forward fp32c integrand) and its reverse sweep, transfer
+// type "eisenhu_osc".  an[GTan] (T_CHIC..T_MUN) and ae[ETan] receive
+// dP/d(input) in the units of the stored tangents.
+template <bool GEN>
 __device__ __forceinline__ float node32_fb(const EHg& e, const float* r, float kh, float lg2kh, float invkh,
-                                           float* an, float* ae) {
+                                           float* an, float* ae, bool lin) {
   // ---- forward (same operations as node32)
   const float k = kh * r[F_INVCHI];
   const float lk = lg2kh + r[F_LG2INVCHI];
@@ -285,69 +376,8 @@ __device__ __forceinline__ float node32_fb(const EHg& e, const float* r, float k
   const float Tbr0 = Tn * rE52 + e.alpha_b * rBb * silk;
   const float Tbar = Tbr0 * sinc;
   const float T = e.fb * Tbar + e.fc * Tc;
-  const float eP = ex2f(e.ns3 * lk);
-  const float T2 = T * T;
-  const float d2l = eP * T2 * r[F_D2FAC];
-  const float y = k * r[F_INVKNL];
-  const float ly = lk - r[F_LG2KNL];
-  const float efy = ex2f(-LOG2E_F * (y * (0.25f + 0.125f * y)));
-  const float lg1 = lg2f(1.f + d2l);
-  const float pb = ex2f(r[F_BETAN] * lg1);
-  const float rden_a = rcpf(1.f + r[F_ALPHAN] * d2l);
-  const float Q = pb * rden_a * efy;
-  const float d2q = d2l * Q;
-  const float H1 = ex2f(r[F_3F1] * ly);
-  const float H2 = ex2f(r[F_F2] * ly);
-  const float E3b = r[F_LG2CF3] + ly;
-  const float H3 = ex2f(r[F_3MGAMMA] * E3b);
-  const float rD = rcpf(1.f + r[F_BN] * H2 + H3);
-  const float d2hp = r[F_AN] * H1 * rD;
-  const float y2 = y * y;
-  const float ryn = rcpf(y2 + r[F_NUN]);
-  const float Rr = y2 * ryn;
-  const float d2h = d2hp * Rr;
-  const float S = d2q + d2h;
-  const float ik3 = invk * invk * invk;
-  const float P = TWO_PI2_F * ik3 * S;
-  // ---- reverse, seed dP/dP = 1
-  const float Sb = TWO_PI2_F * ik3;
-  float invkb = TWO_PI2_F * S * 3.f * invk * invk;
-  // d2h = d2hp y^2 / (y^2 + nu)
-  const float d2hpb = Sb * Rr;
-  const float Rrb = Sb * d2hp;
-  const float y2b = Rrb * ryn * (1.f - Rr);
-  const float NUNb = -Rrb * Rr * ryn;
-  float yb = 2.f * y * y2b;
-  const float ANb = d2hpb * H1 * rD;
-  const float H1b = d2hpb * r[F_AN] * rD;
-  const float Dbar = -d2hpb * d2hp * rD;
-  const float BNb = Dbar * H2;
-  const float H2b = Dbar * r[F_BN];
-  const float u1 = H1b * H1 * LN2_F, u2 = H2b * H2 * LN2_F, u3 = Dbar * H3 * LN2_F;
-  const float F3F1b = u1 * ly, F2b = u2 * ly, F3MGb = u3 * E3b, LG2CF3b = u3 * r[F_3MGAMMA];
-  float lkb = u1 * r[F_3F1] + u2 * r[F_F2] + u3 * r[F_3MGAMMA];  // through ly
-  const float LG2KNLb = -lkb;
-  // d2q = d2l Q, Q = (1 + d2l)^beta / (1 + alpha d2l) exp(-f(y))
-  float d2lb = Sb * Q;
-  const float Qb = Sb * d2l;
-  const float pbb = Qb * rden_a * efy;
-  const float denab = -Qb * Q * rden_a;
-  const float efyb = Qb * pb * rden_a;
-  const float ALPHANb = denab * d2l;
-  d2lb += denab * r[F_ALPHAN];
-  const float vpb = pbb * pb * LN2_F;
-  const float BETANb = vpb * lg1;
-  d2lb += vpb * r[F_BETAN] * LOG2E_F * rcpf(1.f + d2l);
-  yb -= efyb * efy * (0.25f + 0.25f * y);
-  float kb = yb * r[F_INVKNL];
-  const float INVKNLb = yb * k;
-  // d2l = k^(ns+3) T^2 D2FAC
-  const float ePb = d2lb * T2 * r[F_D2FAC];
-  const float Tbv = d2lb * eP * 2.f * T * r[F_D2FAC];
-  const float D2FACb = d2lb * eP * T2;
-  const float vep = ePb * eP * LN2_F;
-  const float ns3b = vep * lk;
-  lkb += vep * e.ns3;
+  float Tbv, kb = 0.f, lkb = 0.f, invkb = 0.f;
+  const float P = pk32_fb<GEN>(e, r, k, lk, invk, T, lin, an, ae, Tbv, kb, lkb, invkb);
   // T = fb Tbar + fc Tc
   const float fbb = Tbv * Tbar, fcb = Tbv * Tc;
   const float Tbarb = Tbv * e.fb, Tcb = Tbv * e.fc;
@@ -407,17 +437,6 @@ __device__ __forceinline__ float node32_fb(const EHg& e, const float* r, float k
   // k = kh INVCHI, lk = lg2 kh + LG2INVCHI, 1/k = CHIC / kh
   const float INVCHIb = kb * kh, CHICb = invkb * invkh;
   an[T_CHIC] = -INVCHIb * r[F_INVCHI] * r[F_INVCHI] - lkb * LOG2E_F * r[F_INVCHI] + CHICb;
-  an[T_D2FAC] = D2FACb;
-  an[T_KNL] = -INVKNLb * r[F_INVKNL] * r[F_INVKNL] + LG2KNLb * LOG2E_F * r[F_INVKNL];
-  an[T_BETAN] = BETANb;
-  an[T_ALPHAN] = ALPHANb;
-  an[T_AN] = ANb;
-  an[T_3F1] = F3F1b;
-  an[T_F2] = F2b;
-  an[T_BN] = BNb;
-  an[T_LG2CF3] = LG2CF3b;
-  an[T_3MG] = F3MGb;
-  an[T_NUN] = NUNb;
   ae[E_KEQ] = -(qinvb * e.qinv + lqb * LOG2E_F) * e.inv_keq;
   ae[E_SH] = shb - invshb * e.inv_sh * e.inv_sh;
   ae[E_C18BC] = c18bcb;
@@ -428,7 +447,53 @@ __device__ __forceinline__ float node32_fb(const EHg& e, const float* r, float k
   ae[E_LG2KSILK] = lg2ksilkb;
   ae[E_FB] = fbb;
   ae[E_FC] = fcb;
-  ae[E_NS3] = ns3b;
+  return P;
+}
+
+// node32_fb for transfer type "eisenhu" (transfer.py:88-105).  The no-wiggle
+// inputs use the slots of the oscillating fit: ae[E_AGAM] (= E_KEQ) for
+// alpha_gamma, ae[E_NWQ] (= E_C18BC) for (T_cmb / 2.7)^2 / (Omega_m h),
+// ae[E_SH] for the sound horizon; the other transfer slots are 0.
+__device__ __forceinline__ float node32_fb_nw(const EHg& e, const float* r, float kh, float lg2kh,
+                                              float invkh, float* an, float* ae, bool lin) {
+  const float k = kh * r[F_INVCHI];
+  const float lk = lg2kh + r[F_LG2INVCHI];
+  const float invk = invkh * r[F_CHIC];
+  const float x = 0.43f * k * e.sh, x2 = x * x;
+  const float u = rcpf(1.f + x2 * x2);
+  const float ge = e.agam + (1.f - e.agam) * u;  // gamma_eff / (Omega_m h)
+  const float rge = rcpf(ge);
+  const float q = k * e.nwq * rge;
+  const float A = 2.f * E_F + 1.8f * q;
+  const float L = LN2_F * lg2f(A);
+  const float rc = rcpf(1.f + 62.5f * q);
+  const float C = 14.2f + 731.f * rc;
+  const float qq = q * q;
+  const float rDt = rcpf(L + C * qq);
+  const float T = L * rDt;
+  float Tbv, kb = 0.f, lkb = 0.f, invkb = 0.f;
+  const float P = pk32_fb<true>(e, r, k, lk, invk, T, lin, an, ae, Tbv, kb, lkb, invkb);
+  // T = L / (L + C q^2)
+  const float Lb = Tbv * rDt * (1.f - T);
+  const float Dtb = -Tbv * T * rDt;
+  float qb = Dtb * C * 2.f * q + Lb * 1.8f * rcpf(A);
+  qb -= Dtb * qq * 731.f * 62.5f * rc * rc;
+  // q = k nwq / ge, ge = agam + (1 - agam) / (1 + x^4), x = 0.43 k sh
+  kb += qb * e.nwq * rge;
+  const float nwqb = qb * k * rge;
+  const float geb = -qb * q * rge;
+  const float agamb = geb * (1.f - u);
+  const float xb = -geb * (1.f - e.agam) * 4.f * x2 * x * u * u;
+  kb += xb * 0.43f * e.sh;
+  const float shb = xb * 0.43f * k;
+  const float INVCHIb = kb * kh, CHICb = invkb * invkh;
+  an[T_CHIC] = -INVCHIb * r[F_INVCHI] * r[F_INVCHI] - lkb * LOG2E_F * r[F_INVCHI] + CHICb;
+#pragma unroll
+  for (int j = 0; j < NET; ++j)
+    if (j != E_NS3) ae[j] = 0.f;
+  ae[E_AGAM] = agamb;
+  ae[E_NWQ] = nwqb;
+  ae[E_SH] = shb;
   return P;
 }
 
@@ -457,6 +522,10 @@ static size_t limber32_smem_floats(int n_cls, int n_tr, int LT, int TA) {
 //   phase M: M_p(a) = u K_i K_j and its tangents;
 //   phase A: per (a, ell) P and dP/dtheta (reverse sweep + projection);
 //   phase B: per (ell, pair group) the 9 sums over the chunk, Kahan-added.
+// GEN: some item may use a non-default operator point (transfer type
+// "eisenhu", smith2003, linear_matter_power); a separate instantiation keeps
+// the default one's registers.
+template <bool GEN>
 __global__ void __launch_bounds__(L32_THREADS, 2)
     grad_limber32_kernel(GradBatch gb, const ConstTables* __restrict__ c, int LT, int TA) {
   const int item = blockIdx.z, split = blockIdx.y;
@@ -464,6 +533,8 @@ __global__ void __launch_bounds__(L32_THREADS, 2)
   const GradItem gi = grad_item(gb, item);
   const GeoHeader* geo = gi.geo;
   const int n_ell = geo->n_ell, n_cls = geo->n_cls, na = geo->na, n_tr = geo->n_tr;
+  const bool lin = pk_model(geo->physics) == JCG_PK_LINEAR;
+  const bool nw = GEN && tf_nowiggle(geo->physics);
   const int l0 = blockIdx.x * LT;
   if (l0 >= n_ell) return;
   const int lt = min(LT, n_ell - l0);
@@ -504,6 +575,8 @@ __global__ void __launch_bounds__(L32_THREADS, 2)
       ev[11] = (float)tb->sv[S_FC];
       ev[12] = (float)(tb->sv[S_NS] + 3.0);
       ev[13] = (float)(1.0 / keq);
+      ev[14] = (float)tb->sv[S_AGAM];
+      ev[15] = (float)tb->sv[S_NWQ];
     } else {
       const double* sd = tb->sd[d];
       et[E_KEQ * NDIR + d] = (float)sd[S_K_EQ];
@@ -517,6 +590,10 @@ __global__ void __launch_bounds__(L32_THREADS, 2)
       et[E_FB * NDIR + d] = (float)sd[S_FB];
       et[E_FC * NDIR + d] = (float)sd[S_FC];
       et[E_NS3 * NDIR + d] = (float)sd[S_NS];
+      if (nw) {
+        et[E_AGAM * NDIR + d] = (float)sd[S_AGAM];
+        et[E_NWQ * NDIR + d] = (float)sd[S_NWQ];
+      }
     }
   }
   const double* ELL = geo_ptr<double>(geo, geo->off_ell);
@@ -532,6 +609,7 @@ __global__ void __launch_bounds__(L32_THREADS, 2)
   eh.qinv = ev[0]; eh.lg2_qinv = ev[1]; eh.sh = ev[2]; eh.inv_sh = ev[3]; eh.c18bc = ev[4];
   eh.c142ac = ev[5]; eh.alpha_b = ev[6]; eh.beta_b = ev[7]; eh.beta_node = ev[8]; eh.lg2_ksilk = ev[9];
   eh.fb = ev[10]; eh.fc = ev[11]; eh.ns3 = ev[12]; eh.inv_keq = ev[13];
+  eh.agam = ev[14]; eh.nwq = ev[15];
   // contraction unit of this thread: ell l_u, pairs [p0, p1)
   const int groups = (n_cls + L32_G - 1) / L32_G;
   const int l_u = tid % LT, pg = tid / LT;
@@ -568,7 +646,7 @@ __global__ void __launch_bounds__(L32_THREADS, 2)
       const float u = row[F_U];
       const float kk = Ki[0] * Kj[0];
       Mv[i] = u * kk;
-      const float* du = row + NROW32 + T_U * NDIR;
+      const float* du = row + NROWV + T_U * NDIR;
 #pragma unroll
       for (int d = 0; d < NDIR; ++d) Md[(size_t)i * NDIR + d] = du[d] * kk + u * (Ki[1 + d] * Kj[0] + Ki[0] * Kj[1 + d]);
     }
@@ -577,13 +655,15 @@ __global__ void __launch_bounds__(L32_THREADS, 2)
       const int t = i / lt, l = i % lt;
       const float* row = R + (size_t)t * NROWG;
       float an[NGT], ae[NET];
-      const float P = node32_fb(eh, row, khv[l], lkhv[l], ikhv[l], an, ae);
+      const float P = nw ? node32_fb_nw(eh, row, khv[l], lkhv[l], ikhv[l], an, ae, lin)
+                         : node32_fb<GEN>(eh, row, khv[l], lkhv[l], ikhv[l], an, ae, lin);
       float pd[NDIR];
 #pragma unroll
       for (int d = 0; d < NDIR; ++d) pd[d] = 0.f;
-      const float* tg = row + NROW32;
+      const float* tg = row + NROWV;
 #pragma unroll
       for (int j = 0; j < T_U; ++j) {
+        if (!GEN && j == T_MUN) continue;  // mu_n = 0 for takahashi2012
         const float4 a = *reinterpret_cast<const float4*>(tg + j * NDIR);
         const float4 b = *reinterpret_cast<const float4*>(tg + j * NDIR + 4);
         pd[0] = fmaf(an[j], a.x, pd[0]); pd[1] = fmaf(an[j], a.y, pd[1]);
@@ -663,9 +743,14 @@ void launch_grad_limber32(const GradBatch& gb, const ConstTables* c, cudaStream_
   const int lt = grad_limber32_tile(gb.n_ell, gb.n_cls);
   const int ta = grad_limber32_chunk(gb.n_cls);
   const size_t smem = sizeof(float) * limber32_smem_floats(gb.n_cls, gb.n_tr, lt, ta);
-  cudaFuncSetAttribute(grad_limber32_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   dim3 grid((gb.n_ell + lt - 1) / lt, gb.n_split, gb.n_items);
-  grad_limber32_kernel<<<grid, L32_THREADS, smem, st>>>(gb, c, lt, ta);
+  if (gb.physics_or != 0) {
+    cudaFuncSetAttribute(grad_limber32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    grad_limber32_kernel<true><<<grid, L32_THREADS, smem, st>>>(gb, c, lt, ta);
+  } else {
+    cudaFuncSetAttribute(grad_limber32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    grad_limber32_kernel<false><<<grid, L32_THREADS, smem, st>>>(gb, c, lt, ta);
+  }
 }
 
 }  // namespace jcg

@@ -9,12 +9,12 @@
 // thread-parallel instead.)
 #include "jcg_fp32.cuh"
 #include "jcg_internal.cuh"
+#include "jcg_dual.cuh"
 
 namespace jcg {
 
 constexpr double TWO_PI2 = 2.0 * (PI * PI);  // 2.0 * np.pi**2
 constexpr double C2 = C_KMS * C_KMS;          // const.c**2
-constexpr double LN10 = 2.302585092994046;
 
 struct HfParams {
   double knl, neff, C;
@@ -92,36 +92,34 @@ __device__ HfParams halofit_params_warp(const double* sig, const double* pk3, do
   return hp;
 }
 
-// takahashi2012 coefficients (power.py:177-238) into a FP64 row; one thread.
-__device__ void halofit_coefs(const Bg& bg, double a, double lna, const HfParams& hp, double* row) {
+// halofit coefficients (power.py:177-244; takahashi2012 or smith2003) into a
+// FP64 row; one thread.
+__device__ void halofit_coefs(const Bg& bg, double a, double lna, const HfParams& hp, double* row,
+                              int model) {
   const double n = hp.neff, C = hp.C;
   double om_m, om_de;
   bg_om_l(bg, a, lna, &om_m, &om_de);
   const double w = bg_w(bg, a);
-  const double n2 = n * n, n3 = n2 * n, n4 = n2 * n2;
   row[R_KNL] = hp.knl;
   row[R_NEFF] = n;
   row[R_C] = C;
   row[R_OMM] = om_m;
   row[R_OMDE] = om_de;
   row[R_W] = w;
-  const double e_an = 1.5222 + 2.8553 * n + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 - 0.6038 * C +
-                      0.1749 * om_de * (1 + w);
-  const double e_bn = -0.5642 + 0.5864 * n + 0.5716 * n2 - 1.5474 * C + 0.2279 * om_de * (1 + w);
-  const double e_cn = 0.3698 + 2.0404 * n + 0.8161 * n2 + 0.5869 * C;
-  row[R_AN] = exp(LN10 * e_an);
-  row[R_BN] = exp(LN10 * e_bn);
-  row[R_CN] = exp(LN10 * e_cn);
-  row[R_GAMMAN] = 0.1971 - 0.0843 * n + 0.8460 * C;
-  row[R_ALPHAN] = fabs(6.0835 + 1.3373 * n - 0.1959 * n2 - 5.5274 * C);
-  row[R_BETAN] = 2.0379 - 0.7354 * n + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
-  row[R_NUN] = exp(LN10 * (5.2105 + 3.6902 * n));
-  const double lom = log(om_m);
-  row[R_F1] = exp(-0.0307 * lom);
-  row[R_F2] = exp(-0.0585 * lom);
-  row[R_F3] = exp(0.0743 * lom);
+  const HfCoef<double> h = hf_coefs<double>(model, n, C, om_m, om_de, w);
+  row[R_AN] = h.an;
+  row[R_BN] = h.bn;
+  row[R_CN] = h.cn;
+  row[R_GAMMAN] = h.gam;
+  row[R_ALPHAN] = h.alpha;
+  row[R_BETAN] = h.beta;
+  row[R_NUN] = h.nu;
+  row[R_MUN] = h.mu;
+  row[R_F1] = h.f1;
+  row[R_F2] = h.f2;
+  row[R_F3] = h.f3;
   row[R_LGKNL] = log(hp.knl);
-  row[R_LGCF3] = LN10 * e_cn + 0.0743 * lom;  // log(c_n f3)
+  row[R_LGCF3] = h.lcf3;
 }
 
 __device__ __forceinline__ float ex2a(float x) {
@@ -135,27 +133,52 @@ __device__ __forceinline__ float lg2a(float x) {
   return y;
 }
 
-// fp32c: the takahashi2012 coefficients (power.py:199-238) in float32 from
-// n_eff, C and the float32 background Omega_m(a), Omega_de(a), w(a); the
-// Limber integrand consumes them as float32.  Fills the float row and the
+// fp32c: the halofit coefficients (power.py:177-244) in float32 from n_eff, C
+// and the float32 background Omega_m(a), Omega_de(a), w(a); the Limber
+// integrand consumes them as float32.  Fills the float row and the
 // coefficient fields of the float64 row.
 __device__ void halofit_coefs_fast(const double* s, float om_m, float om_de, float wv,
                                    const HfParams& hp, double chiv, double g, double* row,
-                                   float* f) {
+                                   float* f, int model) {
   const float n = (float)hp.neff, C = (float)hp.C, omde = om_de, w = wv;
   const float n2 = n * n, n3 = n2 * n, n4 = n2 * n2;
   constexpr float LOG2_10 = 3.321928094887362f;
-  const float e_an = 1.5222f + 2.8553f * n + 2.3706f * n2 + 0.9903f * n3 + 0.2250f * n4 -
-                     0.6038f * C + 0.1749f * omde * (1 + w);
-  const float e_bn = -0.5642f + 0.5864f * n + 0.5716f * n2 - 1.5474f * C + 0.2279f * omde * (1 + w);
-  const float e_cn = 0.3698f + 2.0404f * n + 0.8161f * n2 + 0.5869f * C;
-  const float an = ex2a(LOG2_10 * e_an), bn = ex2a(LOG2_10 * e_bn), cn = ex2a(LOG2_10 * e_cn);
-  const float gam = 0.1971f - 0.0843f * n + 0.8460f * C;
-  const float alpha = fabsf(6.0835f + 1.3373f * n - 0.1959f * n2 - 5.5274f * C);
-  const float beta = 2.0379f - 0.7354f * n + 0.3157f * n2 + 1.2490f * n3 + 0.3980f * n4 - 0.1682f * C;
-  const float nun = ex2a(LOG2_10 * (5.2105f + 3.6902f * n));
   const float l2om = lg2a(om_m);
-  const float f1 = ex2a(-0.0307f * l2om), f2 = ex2a(-0.0585f * l2om), f3 = ex2a(0.0743f * l2om);
+  float an, bn, cn, gam, alpha, beta, nun, mun, f1, f2, f3, lg2cf3;
+  if (model == JCG_PK_SMITH2003) {
+    // power.py:182-198, 239-242
+    const float e_cn = -0.2807f + 0.6669f * n + 0.3214f * n2 - 0.0793f * C;
+    an = ex2a(LOG2_10 * (1.4861f + 1.8369f * n + 1.6762f * n2 + 0.7940f * n3 + 0.1670f * n4 - 0.6206f * C));
+    bn = ex2a(LOG2_10 * (0.9463f + 0.9466f * n + 0.3084f * n2 - 0.9400f * C));
+    cn = ex2a(LOG2_10 * e_cn);
+    gam = 0.8649f + 0.2989f * n + 0.1631f * C;
+    alpha = 1.3884f + 0.3700f * n - 0.1452f * n2;
+    beta = 0.8291f + 0.9854f * n + 0.3401f * n2;
+    mun = ex2a(LOG2_10 * (-3.5442f + 0.1908f * n));
+    nun = ex2a(LOG2_10 * (0.9585f + 1.2857f * n));
+    const float frac = omde / (1.f - om_m), ofr = 1.f - frac;
+    f1 = frac * ex2a(-0.0307f * l2om) + ofr * ex2a(-0.0732f * l2om);
+    f2 = frac * ex2a(-0.0585f * l2om) + ofr * ex2a(-0.1423f * l2om);
+    f3 = frac * ex2a(0.0743f * l2om) + ofr * ex2a(0.0725f * l2om);
+    lg2cf3 = LOG2_10 * e_cn + lg2a(f3);
+  } else {
+    const float e_an = 1.5222f + 2.8553f * n + 2.3706f * n2 + 0.9903f * n3 + 0.2250f * n4 -
+                       0.6038f * C + 0.1749f * omde * (1 + w);
+    const float e_bn = -0.5642f + 0.5864f * n + 0.5716f * n2 - 1.5474f * C + 0.2279f * omde * (1 + w);
+    const float e_cn = 0.3698f + 2.0404f * n + 0.8161f * n2 + 0.5869f * C;
+    an = ex2a(LOG2_10 * e_an);
+    bn = ex2a(LOG2_10 * e_bn);
+    cn = ex2a(LOG2_10 * e_cn);
+    gam = 0.1971f - 0.0843f * n + 0.8460f * C;
+    alpha = fabsf(6.0835f + 1.3373f * n - 0.1959f * n2 - 5.5274f * C);
+    beta = 2.0379f - 0.7354f * n + 0.3157f * n2 + 1.2490f * n3 + 0.3980f * n4 - 0.1682f * C;
+    nun = ex2a(LOG2_10 * (5.2105f + 3.6902f * n));
+    mun = 0.f;
+    f1 = ex2a(-0.0307f * l2om);
+    f2 = ex2a(-0.0585f * l2om);
+    f3 = ex2a(0.0743f * l2om);
+    lg2cf3 = LOG2_10 * e_cn + 0.0743f * l2om;
+  }
   const float knl = (float)hp.knl;
   const float chic = fmaxf((float)chiv, 1.f);
   f[F_INVCHI] = 1.f / chic;
@@ -170,9 +193,10 @@ __device__ void halofit_coefs_fast(const double* s, float om_m, float om_de, flo
   f[F_3F1] = 3.f * f1;
   f[F_F2] = f2;
   f[F_BN] = bn;
-  f[F_LG2CF3] = LOG2_10 * e_cn + 0.0743f * l2om;
+  f[F_LG2CF3] = lg2cf3;
   f[F_3MGAMMA] = 3.f - gam;
   f[F_NUN] = nun;
+  f[F_MUN] = mun;
   for (int i = NROW32_USED; i < NROW32; ++i) f[i] = 0.f;
   row[R_KNL] = hp.knl;
   row[R_NEFF] = hp.neff;
@@ -187,6 +211,7 @@ __device__ void halofit_coefs_fast(const double* s, float om_m, float om_de, flo
   row[R_ALPHAN] = alpha;
   row[R_BETAN] = beta;
   row[R_NUN] = nun;
+  row[R_MUN] = mun;
   row[R_F1] = f1;
   row[R_F2] = f2;
   row[R_F3] = f3;
@@ -214,6 +239,7 @@ __device__ void row32_from_row64(const double* s, const double* r, float* f) {
   f[F_LG2CF3] = (float)(LOG2E * r[R_LGCF3]);
   f[F_3MGAMMA] = (float)(3.0 - r[R_GAMMAN]);
   f[F_NUN] = (float)r[R_NUN];
+  f[F_MUN] = (float)r[R_MUN];
   for (int i = NROW32_USED; i < NROW32; ++i) f[i] = 0.f;
 }
 
@@ -278,6 +304,7 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   const Item it = batch_item(bt, item);
   const GeoHeader* geo = it.geo;
   const int na = geo->na;
+  const int model = pk_model(it.physics);
   const int n0 = blockIdx.x * hf_nodes_per_block(FAST);
   if (n0 >= na) return;
   constexpr int NB = hf_nodes_per_block(FAST);
@@ -445,14 +472,14 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
       const float e2 = om3 + (float)s[S_OMEGA_K] * ia2 + ode;
       const float ie2 = rcpf(e2);
       const float omm = om3 * ie2, omde = ode * ie2, wv = w0 + (1.f - af) * wa;
-      halofit_coefs_fast(s, omm, omde, wv, hp, chiv, g_s[t], row, f);
+      halofit_coefs_fast(s, omm, omde, wv, hp, chiv, g_s[t], row, f, model);
       const float dchi = (float)RH * ia2 * rsqrtf(e2);
       const float chic = fmaxf((float)chiv, 1.f);
       row[R_DCHI] = dchi;
       row[R_U] = (double)((float)WS[n] * dchi * rcpf(chic * chic) * (float)(1.0 / C2));
     } else {
       const double lna = log(a);
-      halofit_coefs(bg, a, lna, hp, row);
+      halofit_coefs(bg, a, lna, hp, row, model);
       row[R_LGCHIC] = log(fmax(chiv, 1.0));
       const double dchi = bg_dchioverda_l(bg, a, lna);
       row[R_DCHI] = dchi;
@@ -510,9 +537,10 @@ __device__ double interp_ref_warp(double x, const double* xp, const double* fp, 
 __global__ void eval_points_kernel(const double* __restrict__ params, int n_cosmo,
                                    const CosmoTab* __restrict__ ctab,
                                    const ConstTables* __restrict__ c, const double* __restrict__ av,
-                                   const double* __restrict__ kv, int n, int what,
+                                   const double* __restrict__ kv, int n, int what_phys,
                                    double* __restrict__ out) {
   const int lane = threadIdx.x & 31;
+  const int what = what_phys & 0xff, model = pk_model(what_phys >> 8);
   const long gw = ((long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (gw >= (long)n_cosmo * n) return;
   const int ci = (int)(gw / n), pi = (int)(gw % n);
@@ -564,8 +592,8 @@ __global__ void eval_points_kernel(const double* __restrict__ params, int n_cosm
     if (what == 6) {
       double row[NROW64];
       row[R_G] = g;
-      halofit_coefs(bg, a, log(a), hp, row);
-      v = halofit_node(s, row, k);
+      halofit_coefs(bg, a, log(a), hp, row, model);
+      v = halofit_node(s, row, k, model);
     } else if (what == 7) {
       v = hp.knl;
     } else if (what == 8) {

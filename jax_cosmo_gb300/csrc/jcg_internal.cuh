@@ -99,9 +99,12 @@ enum Scalar {
   S_QINV,       // 1 / (13.41 k_eq)
   S_ISH,        // 1 / sh_d
   S_C142AC,     // 14.2 / alpha_c
+  S_AGAM,       // alpha_gamma of the no-wiggle fit (transfer.py:88-92)
+  S_NWQ,        // (T_cmb / 2.7)^2 / (Omega_m h): q = k S_NWQ / (gamma_eff / (Omega_m h)) (transfer.py:93-100)
+  S_TFNW,       // 1: transfer type "eisenhu" (no wiggles), 0: "eisenhu_osc"
   S_NSCALAR
 };
-constexpr int NSCAL = 32;
+constexpr int NSCAL = 40;
 // ln k grid of the spectral moments: simps over [ln 1e-4, ln 1e4], 256 intervals (power.py:136)
 constexpr double LOG_KMIN = -0x1.26bb1bbb55515p+3;  // np.log(1e-4)
 constexpr double DLOGK = (0x1.26bb1bbb55516p+3 - -0x1.26bb1bbb55515p+3) / 256.0;
@@ -147,6 +150,7 @@ enum Row64 {
   R_LGKNL,     // log(k_nl)
   R_LGCF3,     // log(c_n f3)
   R_LGCHIC,    // log(max(chi, 1))
+  R_MUN,       // mu_n (smith2003, power.py:197; 0 for takahashi2012, power.py:223)
   NROW64_USED
 };
 constexpr int NROW64 = 24;
@@ -161,10 +165,15 @@ enum Row32 {
   F_BETAN, F_ALPHAN, F_AN, F_3F1, F_F2, F_BN, F_LG2CF3, F_3MGAMMA, F_NUN,
   F_INVKNL,      // 1 / k_nl
   F_CHIC,        // max(chi, 1)
+  F_MUN,         // mu_n
   NROW32_USED
 };
 constexpr int NROW32 = 16;
 static_assert(NROW32_USED <= NROW32, "fp32 row too small");
+
+// Physics switches of a request.
+__host__ __device__ __forceinline__ int pk_model(int physics) { return physics & JCG_PK_MASK; }
+__host__ __device__ __forceinline__ bool tf_nowiggle(int physics) { return (physics & JCG_TF_NOWIGGLE) != 0; }
 
 // ------------------------------------------------------ geometry tables ----
 // Cosmology-independent description of one request, stored at the start of the
@@ -185,6 +194,7 @@ struct GeoHeader {
   double bias_eta[MAXTR], bias_z0[MAXTR];
   int special_bias;        // 1: some tracer has IA or a redshift-dependent bias
   int has_delta;           // 1: some WeakLensing tracer has a single-plane n(z)
+  int physics;             // JCG_PK_* | JCG_TF_*
   int nz_kind[MAXTR];      // JCG_NZ_*
   int64_t nzp_off[MAXTR];  // offset of tracer t's points in the n(z) point list
   int64_t nzp_total;       // points over all tracers
@@ -221,7 +231,7 @@ struct Item {
   double* kern;          // [n_tr][na]
   double* cl;            // [n_cls][n_ell] (output)
   int precision;
-  int pad;
+  int physics;           // JCG_PK_* | JCG_TF_*
 };
 
 struct Batch {
@@ -241,6 +251,8 @@ struct Batch {
   int n_wl, n_wl_groups;  // uniform form: WeakLensing tracers and lensing groups
   int special_bias;       // uniform form: IA or a redshift-dependent bias present
   int has_delta;          // uniform form: a single-plane WeakLensing n(z) present
+  int physics;            // uniform form: JCG_PK_* | JCG_TF_*
+  int physics_or;         // OR of the items' switches (selects kernel variants)
 };
 
 __device__ __forceinline__ Item batch_item(const Batch& b, int i) {
@@ -255,7 +267,7 @@ __device__ __forceinline__ Item batch_item(const Batch& b, int i) {
   it.kern = b.kern + (size_t)i * b.max_tr * na;
   it.cl = b.cl + (size_t)i * b.max_cls * b.max_ell;
   it.precision = b.precision;
-  it.pad = 0;
+  it.physics = b.physics;
   return it;
 }
 
@@ -556,7 +568,7 @@ __device__ __forceinline__ double bg_dchioverda(const Bg& c, double a) {
 // rcbrt for tilde_s.  On GB300 a float64 pow costs about two exps and a
 // division about ten float64 operations; the shared forms change results only
 // at the 1e-15 level.
-__device__ __forceinline__ double eh_transfer_lki(const double* s, double k, double lk, double ik) {
+__device__ __forceinline__ double eh_osc_lki(const double* s, double k, double lk, double ik) {
   const double sh_d = s[S_SH_D];
   const double q = k * s[S_QINV];
   const double q108 = exp(1.08 * (lk - s[S_LGQ]));
@@ -588,6 +600,25 @@ __device__ __forceinline__ double eh_transfer_lki(const double* s, double k, dou
   const double sinc = sin(arg) / arg;
   const double Tbar = (Tn * (d1 * d3 * r6) + s[S_ALPHA_B] * (d12 * r6) * silk) * sinc;
   return s[S_FB] * Tbar + s[S_FC] * Tc;
+}
+
+// type "eisenhu" (transfer.py:88-105): gamma_eff = Omega_m h (alpha_g +
+// (1 - alpha_g) / (1 + (0.43 k s)^4)), q = k (T_cmb / 2.7)^2 / gamma_eff
+__device__ __forceinline__ double eh_nowiggle(const double* s, double k) {
+  const double x = 0.43 * k * s[S_SH_D], x2 = x * x;
+  const double ag = s[S_AGAM];
+  const double q = k * s[S_NWQ] / (ag + (1.0 - ag) / (1.0 + x2 * x2));
+  const double L = log(2.0 * EULER_E + 1.8 * q);
+  const double C = 14.2 + 731.0 / (1.0 + 62.5 * q);
+  return L / (L + C * q * q);
+}
+
+// T(k) of the cosmology's transfer type (S_TFNW); NW = false: the scalars
+// are known to hold type "eisenhu_osc"
+template <bool NW = true>
+__device__ __forceinline__ double eh_transfer_lki(const double* s, double k, double lk, double ik) {
+  if (NW && s[S_TFNW] != 0.0) return eh_nowiggle(s, k);
+  return eh_osc_lki(s, k, lk, ik);
 }
 
 __device__ __forceinline__ double eh_transfer_lk(const double* s, double k, double lk) {
@@ -630,11 +661,15 @@ __device__ __forceinline__ double pk_linear(const double* s, double k, double g)
   return pk_linear_lk(s, k, log(k), g);
 }
 
-// halofit takahashi2012 per-node evaluation (power.py:246-260), FP64, with
-// log k given and the row's log k_nl and log(c_n f3).
+// Non-linear power at one node (power.py:246-260), FP64, with log k given and
+// the row's log k_nl and log(c_n f3): halofit (takahashi2012 or smith2003 by
+// the row's coefficients; d2h = d2h' / (1 + mu/y + nu/y^2) evaluated as
+// d2h' y^2 / (y^2 + mu y + nu)), or the linear power for JCG_PK_LINEAR
+// (nonlinear_fn = linear_matter_power).
 __device__ __forceinline__ double halofit_node_lk(const double* s, const double* row, double k,
-                                                  double lk) {
+                                                  double lk, int model) {
   const double pklin = pk_linear_lk(s, k, lk, row[R_G]);
+  if (model == JCG_PK_LINEAR) return pklin;
   const double k3 = k * k * k;
   const double d2l = k3 * pklin / (2.0 * (PI * PI));
   const double y = k / row[R_KNL];
@@ -646,11 +681,11 @@ __device__ __forceinline__ double halofit_node_lk(const double* s, const double*
       row[R_AN] * exp(3 * row[R_F1] * ly) /
       (1.0 + row[R_BN] * exp(row[R_F2] * ly) + exp((3.0 - row[R_GAMMAN]) * (row[R_LGCF3] + ly)));
   const double y2 = y * y;
-  const double d2h = d2hprime * y2 / (y2 + row[R_NUN]);
+  const double d2h = d2hprime * y2 / ((y2 + row[R_MUN] * y) + row[R_NUN]);
   return 2.0 * (PI * PI) / k3 * (d2q + d2h);
 }
-__device__ __forceinline__ double halofit_node(const double* s, const double* row, double k) {
-  return halofit_node_lk(s, row, k, log(k));
+__device__ __forceinline__ double halofit_node(const double* s, const double* row, double k, int model) {
+  return halofit_node_lk(s, row, k, log(k), model);
 }
 
 // ------------------------------------------------------------- launches ----

@@ -28,7 +28,10 @@ constexpr int LB_MAXO = (LB_MAXLT * MAXPAIR + LB_THREADS - 1) / LB_THREADS;  // 
 struct EH32 {
   float qinv, lg2_qinv, sh, inv_sh, c18bc, c142ac, alpha_b, beta_b, beta_node, lg2_ksilk, fb, fc,
       ns3;
+  float agam, nwq;  // type "eisenhu": alpha_gamma, (T_cmb / 2.7)^2 / (Omega_m h)
+  int nw;           // 1: type "eisenhu"
 };
+static_assert(sizeof(EH32) <= 64, "EH32 has 64 bytes of shared memory");
 
 __device__ void make_eh32(const double* s, EH32* e) {
   const double qinv = 1.0 / (13.41 * s[S_K_EQ]);
@@ -45,44 +48,61 @@ __device__ void make_eh32(const double* s, EH32* e) {
   e->fb = (float)s[S_FB];
   e->fc = (float)s[S_FC];
   e->ns3 = (float)(s[S_NS] + 3.0);
+  e->agam = (float)s[S_AGAM];
+  e->nwq = (float)s[S_NWQ];
+  e->nw = s[S_TFNW] != 0.0;
 }
 
-// Eisenstein-Hu (transfer.py:107-153) x primordial x halofit (power.py:246-260)
+// Eisenstein-Hu (transfer.py:88-153, either type) x primordial x halofit (power.py:246-260)
 // at one node in FP32.  kh = l + 1/2, lg2kh = log2(kh), invkh = 1 / kh.
+// lin: the linear power (nonlinear_fn = linear_matter_power).  GEN = false:
+// the default operator points only (eisenhu_osc, takahashi2012; lin, e.nw and
+// mu_n are not read), so that instantiation keeps its registers.
+template <bool GEN>
 __device__ __forceinline__ float node32(const EH32& e, const float* r, float kh, float lg2kh,
-                                        float invkh) {
+                                        float invkh, bool lin) {
   const float k = kh * r[F_INVCHI];
   const float lk = lg2kh + r[F_LG2INVCHI];
   const float invk = invkh * r[F_CHIC];
-  // cold dark matter transfer (EH98 10-12, 17-18)
-  const float q = k * e.qinv;
-  const float lq = lk + e.lg2_qinv;
-  const float q108 = ex2f(1.08f * lq);
-  const float Cb = 386.f * rcpf(1.f + 69.9f * q108);
-  const float L1 = LN2_F * lg2f(E_F + e.c18bc * q);
-  const float L2 = LN2_F * lg2f(E_F + 1.8f * q);
-  const float qq = q * q;
-  const float Ta = L1 * rcpf(L1 + (14.2f + Cb) * qq);
-  const float Tb = L1 * rcpf(L1 + (e.c142ac + Cb) * qq);
-  const float Tn = L2 * rcpf(L2 + (14.2f + Cb) * qq);
-  const float ks = k * e.sh;
-  const float x54 = ks * (1.f / 5.4f);
-  const float x54_2 = x54 * x54;
-  const float f = rcpf(1.f + x54_2 * x54_2);
-  const float Tc = f * Ta + (1.f - f) * Tb;
-  // baryon transfer (EH98 14, 19, 21-24)
-  const float iks = invk * e.inv_sh;
-  const float x52 = ks * (1.f / 5.2f);
-  const float bb = e.beta_b * iks;
-  const float silk = ex2f(-LOG2E_F * ex2f(1.4f * (lk - e.lg2_ksilk)));
-  const float bn = e.beta_node * iks;
-  const float st = e.sh * ex2f((-1.f / 3.f) * lg2f(1.f + bn * bn * bn));
-  const float arg = k * st;
-  const float sinc = sin_reduced(arg) * rcpf(arg);
-  const float Tbar = (Tn * rcpf(1.f + x52 * x52) + e.alpha_b * rcpf(1.f + bb * bb * bb) * silk) * sinc;
-  const float T = e.fb * Tbar + e.fc * Tc;
+  float T;
+  if (GEN && e.nw) {
+    // type "eisenhu" (transfer.py:88-105)
+    const float x = 0.43f * k * e.sh, x2 = x * x;
+    const float q = k * e.nwq * rcpf(e.agam + (1.f - e.agam) * rcpf(1.f + x2 * x2));
+    const float L = LN2_F * lg2f(2.f * E_F + 1.8f * q);
+    T = L * rcpf(L + (14.2f + 731.f * rcpf(1.f + 62.5f * q)) * (q * q));
+  } else {
+    // cold dark matter transfer (EH98 10-12, 17-18)
+    const float q = k * e.qinv;
+    const float lq = lk + e.lg2_qinv;
+    const float q108 = ex2f(1.08f * lq);
+    const float Cb = 386.f * rcpf(1.f + 69.9f * q108);
+    const float L1 = LN2_F * lg2f(E_F + e.c18bc * q);
+    const float L2 = LN2_F * lg2f(E_F + 1.8f * q);
+    const float qq = q * q;
+    const float Ta = L1 * rcpf(L1 + (14.2f + Cb) * qq);
+    const float Tb = L1 * rcpf(L1 + (e.c142ac + Cb) * qq);
+    const float Tn = L2 * rcpf(L2 + (14.2f + Cb) * qq);
+    const float ks = k * e.sh;
+    const float x54 = ks * (1.f / 5.4f);
+    const float x54_2 = x54 * x54;
+    const float f = rcpf(1.f + x54_2 * x54_2);
+    const float Tc = f * Ta + (1.f - f) * Tb;
+    // baryon transfer (EH98 14, 19, 21-24)
+    const float iks = invk * e.inv_sh;
+    const float x52 = ks * (1.f / 5.2f);
+    const float bb = e.beta_b * iks;
+    const float silk = ex2f(-LOG2E_F * ex2f(1.4f * (lk - e.lg2_ksilk)));
+    const float bn = e.beta_node * iks;
+    const float st = e.sh * ex2f((-1.f / 3.f) * lg2f(1.f + bn * bn * bn));
+    const float arg = k * st;
+    const float sinc = sin_reduced(arg) * rcpf(arg);
+    const float Tbar = (Tn * rcpf(1.f + x52 * x52) + e.alpha_b * rcpf(1.f + bb * bb * bb) * silk) * sinc;
+    T = e.fb * Tbar + e.fc * Tc;
+  }
   // linear and halofit power
   const float d2l = ex2f(e.ns3 * lk) * (T * T) * r[F_D2FAC];
+  if (GEN && lin) return TWO_PI2_F * (invk * invk * invk) * d2l;
   const float y = k * r[F_INVKNL];
   const float ly = lk - r[F_LG2KNL];
   const float fy = y * (0.25f + 0.125f * y);
@@ -92,7 +112,9 @@ __device__ __forceinline__ float node32(const EH32& e, const float* r, float kh,
   const float yf2 = ex2f(r[F_F2] * ly);
   const float ycg = ex2f(r[F_3MGAMMA] * (r[F_LG2CF3] + ly));
   const float y2 = y * y;
-  const float d2h = r[F_AN] * yf1 * rcpf(1.f + r[F_BN] * yf2 + ycg) * y2 * rcpf(y2 + r[F_NUN]);
+  // d2h' / (1 + mu / y + nu / y^2) as d2h' y^2 / (y^2 + mu y + nu)
+  const float d2h =
+      r[F_AN] * yf1 * rcpf(1.f + r[F_BN] * yf2 + ycg) * y2 * rcpf((GEN ? fmaf(r[F_MUN], y, y2) : y2) + r[F_NUN]);
   return TWO_PI2_F * (invk * invk * invk) * (d2q + d2h);
 }
 
@@ -108,6 +130,8 @@ __global__ void __launch_bounds__(LB_THREADS)
   const Item it = batch_item(bt, item);
   const GeoHeader* geo = it.geo;
   const int n_ell = geo->n_ell, n_cls = geo->n_cls, na = geo->na;
+  const int model = pk_model(it.physics);
+  const bool lin = model == JCG_PK_LINEAR;
   const int l0 = blockIdx.x * LT;
   if (l0 >= n_ell) return;
   const int lt = min(LT, n_ell - l0);
@@ -173,12 +197,12 @@ __global__ void __launch_bounds__(LB_THREADS)
       const int t = q / lt, l = q - (q / lt) * lt;
       T pv;
       if (FP32) {
-        pv = (T)node32(*e32, reinterpret_cast<const float*>(rowsS) + t * NROW32, kh32[3 * l],
-                       kh32[3 * l + 1], kh32[3 * l + 2]);
+        pv = (T)node32<true>(*e32, reinterpret_cast<const float*>(rowsS) + t * NROW32, kh32[3 * l],
+                       kh32[3 * l + 1], kh32[3 * l + 2], lin);
       } else {
         const double* row = reinterpret_cast<const double*>(rowsS) + t * NROW64;
         const double k = ellv[l] / fmax(row[R_CHI], 1.0);
-        pv = (T)halofit_node_lk(s, row, k, lellv[l] - row[R_LGCHIC]);
+        pv = (T)halofit_node_lk(s, row, k, lellv[l] - row[R_LGCHIC], model);
       }
       Pt[t * LT + l] = pv;
     }
@@ -256,7 +280,10 @@ __host__ __device__ inline L32Layout l32_layout(int n_tr, int n_cls, int LT) {
   return L;
 }
 
-template <int MAXU>
+// GEN: the non-default operator points (transfer type "eisenhu", smith2003,
+// linear_matter_power) are read from each item; only the MAXU = L32_MAXU
+// variant is built with GEN.
+template <int MAXU, bool GEN>
 __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2))
     limber32_kernel(Batch bt, const ConstTables* __restrict__ c, int LT) {
   const int item = blockIdx.y;
@@ -264,6 +291,7 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
   const Item it = batch_item(bt, item);
   const GeoHeader* geo = it.geo;
   const int n_ell = geo->n_ell, n_cls = geo->n_cls, na = geo->na, n_tr = geo->n_tr;
+  const bool lin = pk_model(it.physics) == JCG_PK_LINEAR;
   const int l0 = blockIdx.x * LT;
   if (l0 >= n_ell) return;
   const int lt = min(LT, n_ell - l0);
@@ -325,7 +353,7 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
     for (int q = tid; q < tc * lt; q += LB_THREADS) {
       const int t = __float2int_rz(((float)q + 0.5f) * inv_lt), l = q - t * lt;
       const float4 kk = kh4[l];
-      Pt[t * LT + l] = node32(*e32, rowsS + t * NROW32, kk.x, kk.y, kk.z);
+      Pt[t * LT + l] = node32<GEN>(*e32, rowsS + t * NROW32, kk.x, kk.y, kk.z, lin);
     }
     __syncthreads();
 #pragma unroll
@@ -388,12 +416,12 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
   }
 }
 
-template <int MAXU>
+template <int MAXU, bool GEN = false>
 static void launch_limber32_t(const Batch& b, const ConstTables* c, int lt, cudaStream_t st) {
   const L32Layout L = l32_layout(b.max_tr, b.max_cls, lt);
-  cudaFuncSetAttribute(limber32_kernel<MAXU>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
+  cudaFuncSetAttribute(limber32_kernel<MAXU, GEN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)L.total);
   dim3 grid((b.max_ell + lt - 1) / lt, b.n_items);
-  limber32_kernel<MAXU><<<grid, LB_THREADS, L.total, st>>>(b, c, lt);
+  limber32_kernel<MAXU, GEN><<<grid, LB_THREADS, L.total, st>>>(b, c, lt);
 }
 
 size_t limber_smem_bytes(bool fp32, int n_cls, int LT) {
@@ -427,7 +455,8 @@ void launch_limber(const Batch& b, const ConstTables* c, int lt, cudaStream_t st
     // units per thread: the split path needs one, otherwise lt x ceil(n_cls / 4)
     const int items = lt * ((b.max_cls + 3) / 4);
     const int need = items >= LB_THREADS ? (items + LB_THREADS - 1) / LB_THREADS : 1;
-    if (need <= 1) launch_limber32_t<1>(b, c, lt, st);
+    if (b.physics_or != 0) launch_limber32_t<L32_MAXU, true>(b, c, lt, st);
+    else if (need <= 1) launch_limber32_t<1>(b, c, lt, st);
     else if (need <= 2) launch_limber32_t<2>(b, c, lt, st);
     else if (need <= 3) launch_limber32_t<3>(b, c, lt, st);
     else launch_limber32_t<L32_MAXU>(b, c, lt, st);

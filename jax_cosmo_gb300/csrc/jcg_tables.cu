@@ -314,6 +314,9 @@ void launch_geometry_build(const GeoHeader& h, double* geo, const double* pz, co
 
 // ------------------------------------------------------ cosmology tables ----
 
+// NW: some item may use the transfer type "eisenhu" (a separate
+// instantiation keeps the default one's registers)
+template <bool NW>
 __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const ConstTables* __restrict__ c) {
   const int item = blockIdx.x;
   if (item >= bt.n_items) return;
@@ -350,7 +353,7 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   // factor k (k W(8k))^2 is a constant of the node
   if (t < NROMB) {
     const double logk = c->romb_logk[t];
-    const double T = eh_transfer_lki(s, c->romb_k[t], logk, c->romb_ik[t]);
+    const double T = eh_transfer_lki<NW>(s, c->romb_k[t], logk, c->romb_ik[t]);
     fr[t] = c->romb_kw2[t] * ((T * T) * exp(s[S_NS] * logk));
   }
   __syncthreads();
@@ -407,7 +410,7 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   __syncthreads();
   // linear P(k_i, a = 1) * k_i^3 on the halofit k grid (power.py:102, 124)
   for (int i = t; i < NKH; i += blockDim.x) {
-    const double tk = eh_transfer_lki(s, c->kh[i], c->logk[i], c->ikh[i]);
+    const double tk = eh_transfer_lki<NW>(s, c->kh[i], c->logk[i], c->ikh[i]);
     const double g1 = s[S_G1];
     pk3[i] = exp(s[S_NS] * c->logk[i]) * (tk * tk) * (g1 * g1) * s[S_PKNORM] * c->kh3[i];
   }
@@ -480,20 +483,24 @@ __global__ void __launch_bounds__(128) cosmo_scalars_kernel(Batch bt) {
   const bool valid = g < bt.n_items;
   const Item it = batch_item(bt, valid ? g : bt.n_items - 1);
   double sv[NSCAL];
-  cosmo_scalars_warpT<double>(it.params, sv, lane);
-  double v0 = 0.0, v1 = 0.0;
+  cosmo_scalars_warpT<double>(it.params, sv, lane, tf_nowiggle(it.physics));
+  double v0 = 0.0, v1 = 0.0, v2 = 0.0;
 #pragma unroll
   for (int k = 0; k < 16; ++k)
-    if (k == lane) v0 = sv[k], v1 = sv[k + 16];
+    if (k == lane) v0 = sv[k], v1 = sv[k + 16], v2 = k + 32 < NSCAL ? sv[k + 32] : 0.0;
   if (valid) {
     it.ctab->s[lane] = v0;
     it.ctab->s[lane + 16] = v1;
+    if (lane + 32 < NSCAL) it.ctab->s[lane + 32] = v2;
   }
 }
 
 void launch_cosmo_tables(const Batch& b, const ConstTables* c, cudaStream_t st) {
   cosmo_scalars_kernel<<<(b.n_items + 7) / 8, 128, 0, st>>>(b);
-  cosmo_tables_kernel<<<b.n_items, 256, 0, st>>>(b, c);
+  if (tf_nowiggle(b.physics_or))
+    cosmo_tables_kernel<true><<<b.n_items, 256, 0, st>>>(b, c);
+  else
+    cosmo_tables_kernel<false><<<b.n_items, 256, 0, st>>>(b, c);
 }
 
 }  // namespace jcg

@@ -72,14 +72,18 @@ class ChainModel:
     """
 
     def __init__(self, probes, ell, data, cov=None, *, fiducial=None, f_sky=0.25, n_limber=512,
-                 device=None):
+                 device=None, transfer_fn=None, nonlinear_fn=None):
         from jax_cosmo_gb300 import angular_cl as cl_mod
+        from jax_cosmo_gb300 import power, transfer
         from jax_cosmo_gb300.parameters import Planck15
 
+        tf = transfer_fn or transfer.Eisenstein_Hu
+        nl = nonlinear_fn or power.halofit
+        physics = cl_mod.physics_code(tf, nl)
         self.device = _lib.require_cuda(device)
         self.probes = probes
         self.ell = _geometry.ell_host(ell)
-        self.g, self.geo, _ = _geometry.get_geometry(probes, self.ell, n_limber, self.device)
+        self.g, self.geo, _ = _geometry.get_geometry(probes, self.ell, n_limber, self.device, physics)
         self.n_cls = _geometry.n_cls_of(self.g)
         self.n_ell = int(self.g.n_ell)
         N = self.n_cls * self.n_ell
@@ -89,7 +93,7 @@ class ChainModel:
             raise ValueError(f"data has {self.data.numel()} entries, expected n_cls * n_ell = {N}")
         if cov is None:
             cosmo = fiducial if fiducial is not None else Planck15()
-            _, cov = cl_mod.gaussian_cl_covariance_and_mean(cosmo, self.ell, probes, f_sky=f_sky,
+            _, cov = cl_mod.gaussian_cl_covariance_and_mean(cosmo, self.ell, probes, tf, nl, f_sky=f_sky,
                                                             sparse=True, n_limber=n_limber)
         cov = torch.as_tensor(cov, dtype=torch.float64).to(self.device)
         if cov.shape != (self.n_cls, self.n_cls, self.n_ell):

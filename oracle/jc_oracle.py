@@ -69,6 +69,10 @@ class Cosmo:
     w0: torch.Tensor
     wa: torch.Tensor
     cache: dict = field(default_factory=dict)
+    # the transfer_fn type of every call on this object ("eisenhu_osc" or
+    # "eisenhu", transfer.py:10): the sigma_8 normalisation and the sigma^2(R)
+    # table cached here depend on it
+    transfer: str = "eisenhu_osc"
 
     @classmethod
     def from_vector(cls, v):
@@ -316,7 +320,7 @@ def angular_diameter_distance(c, a):
 
 # ---------------------------------------------------------------- transfer ----
 def eisenstein_hu(c, k):
-    """transfer.py:10-156, type='eisenhu_osc'."""
+    """transfer.py:10-156, type c.transfer ('eisenhu_osc' or 'eisenhu')."""
     T_2_7_sqr = (TCMB / 2.7) ** 2
     h2 = c.h**2
     w_m = c.Omega_m * h2
@@ -348,7 +352,20 @@ def eisenstein_hu(c, k):
         * (1.0 + torch.pow(10.4 * w_m, -0.95))
         / c.h
     )
-    # transfer.py:88-97 (alpha_gamma / gamma_eff only feed the no-wiggle form)
+    if c.transfer == "eisenhu":
+        # transfer.py:88-105: zero-baryon fit with the effective shape gamma_eff(k)
+        alpha_gamma = (
+            1.0
+            - 0.328 * torch.log(431.0 * w_m) * w_b / w_m
+            + 0.38 * torch.log(22.3 * w_m) * (c.Omega_b / c.Omega_m) ** 2
+        )
+        gamma_eff = c.Omega_m * c.h * (alpha_gamma + (1.0 - alpha_gamma) / (1.0 + (0.43 * k * sh_d) ** 4))
+        q = k * (TCMB / 2.7) ** 2 / gamma_eff
+        L = torch.log(2.0 * math.exp(1.0) + 1.8 * q)
+        C = 14.2 + 731.0 / (1.0 + 62.5 * q)
+        return L / (L + C * q * q)
+    if c.transfer != "eisenhu_osc":
+        raise NotImplementedError(c.transfer)
     a1 = torch.pow(46.9 * w_m, 0.670) * (1.0 + torch.pow(32.1 * w_m, -0.532))
     a2 = torch.pow(12.0 * w_m, 0.424) * (1.0 + torch.pow(45.0 * w_m, -0.582))
     alpha_c = torch.pow(a1, -fb) * torch.pow(a2, -(fb**3))
@@ -486,37 +503,65 @@ def halofit_parameters(c, a):
     return out
 
 
-def halofit(c, k, a):
-    """power.py:144-262, prescription='takahashi2012'."""
+def halofit_coefs(n, C, om_m, om_de, ww, prescription="takahashi2012"):
+    """power.py:177-244 -> (a_n, b_n, c_n, gamma_n, alpha_n, beta_n, mu_n, nu_n, f1, f2, f3)."""
+    if prescription == "smith2003":
+        # eq C9 to C18 (power.py:182-198)
+        a_n = 10 ** (1.4861 + 1.8369 * n + 1.6762 * n**2 + 0.7940 * n**3 + 0.1670 * n**4 - 0.6206 * C)
+        b_n = 10 ** (0.9463 + 0.9466 * n + 0.3084 * n**2 - 0.9400 * C)
+        c_n = 10 ** (-0.2807 + 0.6669 * n + 0.3214 * n**2 - 0.0793 * C)
+        gamma_n = 0.8649 + 0.2989 * n + 0.1631 * C
+        alpha_n = 1.3884 + 0.3700 * n - 0.1452 * n**2
+        beta_n = 0.8291 + 0.9854 * n + 0.3401 * n**2
+        mu_n = 10 ** (-3.5442 + 0.1908 * n)
+        nu_n = 10 ** (0.9585 + 1.2857 * n)
+    elif prescription == "takahashi2012":
+        a_n = 10 ** (
+            1.5222 + 2.8553 * n + 2.3706 * n**2 + 0.9903 * n**3 + 0.2250 * n**4
+            - 0.6038 * C + 0.1749 * om_de * (1 + ww)
+        )
+        b_n = 10 ** (-0.5642 + 0.5864 * n + 0.5716 * n**2 - 1.5474 * C + 0.2279 * om_de * (1 + ww))
+        c_n = 10 ** (0.3698 + 2.0404 * n + 0.8161 * n**2 + 0.5869 * C)
+        gamma_n = 0.1971 - 0.0843 * n + 0.8460 * C
+        alpha_n = torch.abs(6.0835 + 1.3373 * n - 0.1959 * n**2 - 5.5274 * C)
+        beta_n = (
+            2.0379 - 0.7354 * n + 0.3157 * n**2 + 1.2490 * n**3 + 0.3980 * n**4 - 0.1682 * C
+        )
+        mu_n = 0.0
+        nu_n = 10 ** (5.2105 + 3.6902 * n)
+    else:
+        raise NotImplementedError(prescription)
+    f1b, f2b, f3b = om_m ** (-0.0307), om_m ** (-0.0585), om_m ** (0.0743)
+    if prescription == "takahashi2012":
+        f1, f2, f3 = f1b, f2b, f3b
+    else:
+        # power.py:180, 227-242
+        frac = om_de / (1.0 - om_m)
+        f1 = frac * f1b + (1 - frac) * om_m ** (-0.0732)
+        f2 = frac * f2b + (1 - frac) * om_m ** (-0.1423)
+        f3 = frac * f3b + (1 - frac) * om_m**0.0725
+    return a_n, b_n, c_n, gamma_n, alpha_n, beta_n, mu_n, nu_n, f1, f2, f3
+
+
+def _halofit_from(k, pklin, k_nl, coefs):
+    """power.py:246-260"""
+    a_n, b_n, c_n, gamma_n, alpha_n, beta_n, mu_n, nu_n, f1, f2, f3 = coefs
+    d2l = k**3 * pklin / (2.0 * math.pi**2)
+    y = k / k_nl
+    fy = y / 4.0 + y**2 / 8.0
+    d2q = d2l * ((1.0 + d2l) ** beta_n / (1 + alpha_n * d2l)) * torch.exp(-fy)
+    d2hprime = a_n * y ** (3 * f1) / (1.0 + b_n * y**f2 + (c_n * f3 * y) ** (3.0 - gamma_n))
+    d2h = d2hprime / (1.0 + mu_n / y + nu_n / y**2)
+    return 2.0 * math.pi**2 / k**3 * (d2q + d2h)
+
+
+def halofit(c, k, a, prescription="takahashi2012"):
+    """power.py:144-262"""
     a = torch.atleast_1d(a)
     pklin = linear_matter_power(c, k, a)
     k_nl, n, C = halofit_parameters(c, a)
-    om_m = Omega_m_a(c, a)
-    om_de = Omega_de_a(c, a)
-    ww = w(c, a)
-    a_n = 10 ** (
-        1.5222 + 2.8553 * n + 2.3706 * n**2 + 0.9903 * n**3 + 0.2250 * n**4
-        - 0.6038 * C + 0.1749 * om_de * (1 + ww)
-    )
-    b_n = 10 ** (-0.5642 + 0.5864 * n + 0.5716 * n**2 - 1.5474 * C + 0.2279 * om_de * (1 + ww))
-    c_n = 10 ** (0.3698 + 2.0404 * n + 0.8161 * n**2 + 0.5869 * C)
-    gamma_n = 0.1971 - 0.0843 * n + 0.8460 * C
-    alpha_n = torch.abs(6.0835 + 1.3373 * n - 0.1959 * n**2 - 5.5274 * C)
-    beta_n = (
-        2.0379 - 0.7354 * n + 0.3157 * n**2 + 1.2490 * n**3 + 0.3980 * n**4 - 0.1682 * C
-    )
-    mu_n = 0.0
-    nu_n = 10 ** (5.2105 + 3.6902 * n)
-    f1 = om_m ** (-0.0307)
-    f2 = om_m ** (-0.0585)
-    f3 = om_m ** (0.0743)
-    fy = lambda x: x / 4.0 + x**2 / 8.0
-    d2l = k**3 * pklin / (2.0 * math.pi**2)
-    y = k / k_nl
-    d2q = d2l * ((1.0 + d2l) ** beta_n / (1 + alpha_n * d2l)) * torch.exp(-fy(y))
-    d2hprime = a_n * y ** (3 * f1) / (1.0 + b_n * y**f2 + (c_n * f3 * y) ** (3.0 - gamma_n))
-    d2h = d2hprime / (1.0 + mu_n / y + nu_n / y**2)
-    return (2.0 * math.pi**2 / k**3 * (d2q + d2h)).squeeze()
+    coefs = halofit_coefs(n, C, Omega_m_a(c, a), Omega_de_a(c, a), w(c, a), prescription)
+    return _halofit_from(k, pklin, k_nl, coefs).squeeze()
 
 
 # ----------------------------------------------------------------- tracers ----
@@ -777,44 +822,26 @@ def limber_nodes(zmax, n_limber=512):
     return np.linspace(a0, 1.0, n_limber + 1), (1.0 - a0) / n_limber
 
 
-def halofit_nodes(c, k, a):
-    """halofit (power.py:144-262) on a [n_ell, n_a] grid of k with a per column."""
+def halofit_nodes(c, k, a, nonlinear="takahashi2012"):
+    """nonlinear_fn (power.py:144-262 halofit with prescription ``nonlinear``, or
+    linear_matter_power for nonlinear="linear") on a [n_ell, n_a] grid of k
+    with a per column."""
     a = torch.atleast_1d(a)
     g = growth_factor(c, a)
     t = eisenstein_hu(c, k)
     pknorm = c.sigma8**2 / sigmasqr(c, 8.0)
     pklin = primordial_matter_power(c, k) * t**2 * g**2
     pklin = pklin * pknorm
+    if nonlinear == "linear":
+        return pklin
     k_nl, n, C = halofit_parameters(c, a)
-    om_m = Omega_m_a(c, a)
-    om_de = Omega_de_a(c, a)
-    ww = w(c, a)
-    a_n = 10 ** (
-        1.5222 + 2.8553 * n + 2.3706 * n**2 + 0.9903 * n**3 + 0.2250 * n**4
-        - 0.6038 * C + 0.1749 * om_de * (1 + ww)
-    )
-    b_n = 10 ** (-0.5642 + 0.5864 * n + 0.5716 * n**2 - 1.5474 * C + 0.2279 * om_de * (1 + ww))
-    c_n = 10 ** (0.3698 + 2.0404 * n + 0.8161 * n**2 + 0.5869 * C)
-    gamma_n = 0.1971 - 0.0843 * n + 0.8460 * C
-    alpha_n = torch.abs(6.0835 + 1.3373 * n - 0.1959 * n**2 - 5.5274 * C)
-    beta_n = (
-        2.0379 - 0.7354 * n + 0.3157 * n**2 + 1.2490 * n**3 + 0.3980 * n**4 - 0.1682 * C
-    )
-    nu_n = 10 ** (5.2105 + 3.6902 * n)
-    f1 = om_m ** (-0.0307)
-    f2 = om_m ** (-0.0585)
-    f3 = om_m ** (0.0743)
-    d2l = k**3 * pklin / (2.0 * math.pi**2)
-    y = k / k_nl
-    fy = y / 4.0 + y**2 / 8.0
-    d2q = d2l * ((1.0 + d2l) ** beta_n / (1 + alpha_n * d2l)) * torch.exp(-fy)
-    d2hprime = a_n * y ** (3 * f1) / (1.0 + b_n * y**f2 + (c_n * f3 * y) ** (3.0 - gamma_n))
-    d2h = d2hprime / (1.0 + 0.0 / y + nu_n / y**2)
-    return 2.0 * math.pi**2 / k**3 * (d2q + d2h)
+    coefs = halofit_coefs(n, C, Omega_m_a(c, a), Omega_de_a(c, a), w(c, a), nonlinear)
+    return _halofit_from(k, pklin, k_nl, coefs)
 
 
-def angular_cl(c, ell, probes, n_limber=512):
-    """angular_cl.py:49-98 -> [n_cls, n_ell].
+def angular_cl(c, ell, probes, n_limber=512, nonlinear="takahashi2012"):
+    """angular_cl.py:49-98 -> [n_cls, n_ell]; nonlinear: the halofit
+    prescription of nonlinear_fn, or "linear" for linear_matter_power.
 
     The reference evaluates the integrand once per ell (vmap); ell-independent
     intermediates (tables, halofit parameters, radial kernels) give identical
@@ -829,7 +856,7 @@ def angular_cl(c, ell, probes, n_limber=512):
     chi = radial_comoving_distance(c, a)
     z = a2z(a)
     k = (ell[:, None] + 0.5) / clip(chi, 1.0)[None, :]
-    pk = halofit_nodes(c, k, a)  # [n_ell, n_a]
+    pk = halofit_nodes(c, k, a, nonlinear)  # [n_ell, n_a]
     kern = torch.cat([probe_kernels_all_ell(c, p, z, ell) for p in probes], dim=1)
     pairs = cl_ordering(kern.shape[1])
     ii = torch.tensor([p[0] for p in pairs])
@@ -870,9 +897,10 @@ def gaussian_cl_covariance(ell, n_tracers, cl_signal, cl_noise, f_sky=0.25, spar
     return to_dense(cov)
 
 
-def gaussian_cl_covariance_and_mean(c, ell, probes, f_sky=0.25, sparse=False, n_limber=512):
+def gaussian_cl_covariance_and_mean(c, ell, probes, f_sky=0.25, sparse=False, n_limber=512,
+                                    nonlinear="takahashi2012"):
     """angular_cl.py:166-196"""
-    cl_signal = angular_cl(c, ell, probes, n_limber=n_limber)
+    cl_signal = angular_cl(c, ell, probes, n_limber=n_limber, nonlinear=nonlinear)
     cl_noise = noise_cl(np.atleast_1d(ell), probes)
     n_tr = sum(p.n_tracers for p in probes)
     cov = gaussian_cl_covariance(ell, n_tr, cl_signal, cl_noise, f_sky, sparse)

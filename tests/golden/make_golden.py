@@ -25,6 +25,13 @@ cl_nz.npz       angular_cl with fu_nz, kde_nz (a seeded 200-galaxy catalog, stor
                 with the fixture) and systematic_shift(smail_nz) bins
 cl_delta.npz    angular_cl with single-plane delta_nz WeakLensing bins beside a
                 smail bin, and a NumberCounts bin
+power2.npz      the non-default operator points: Eisenstein_Hu type "eisenhu"
+                (T, sigma^2(8), linear and halofit P), halofit smith2003 P(k, a),
+                nonlinear_matter_power with linear_matter_power
+                                                          (transfer.py:99-105, power.py:182-244)
+cl_physics.npz  angular_cl, 2 WeakLensing + 1 NumberCounts bins, with
+                nonlinear_fn = halofit(smith2003), linear_matter_power, and
+                transfer_fn = Eisenstein_Hu(type="eisenhu")
 background2.npz transverse / angular diameter distances (Omega_k = 0, > 0, < 0),
                 a_of_chi, growth_rate                     (background.py:245-368, 401-512)
 cov_like.npz    gaussian_cl_covariance_and_mean + gaussian_log_likelihood
@@ -164,6 +171,50 @@ def make_power(jc):
     return out
 
 
+def make_power2(jc):
+    import functools
+
+    k = np.logspace(-4, 4, 97)
+    a_list = np.array([1.0, 0.6, 0.25])
+    rng = np.random.default_rng(9)
+    a_pairs = np.sort(rng.uniform(0.1, 1.0, 48))
+    k_pairs = np.exp(rng.uniform(np.log(1e-3), np.log(50.0), 48))
+    nw = functools.partial(jc.transfer.Eisenstein_Hu, type="eisenhu")
+    smith = functools.partial(jc.power.halofit, prescription="smith2003")
+    out = {"cosmos": COSMOS, "k": k, "a_list": a_list, "a_pairs": a_pairs, "k_pairs": k_pairs}
+    cols = {n: [] for n in ("T_nw", "s8_nw", "plin_nw", "pnl_nw", "pnl_smith", "pnl_smith_pairs", "pnl_lin")}
+    for row in COSMOS:
+        c = _cosmo(jc, row)
+        cols["T_nw"].append(jc.transfer.Eisenstein_Hu(c, k, type="eisenhu"))
+        cols["s8_nw"].append(jc.power.sigmasqr(c, 8.0, nw))
+        c = _cosmo(jc, row)
+        cols["plin_nw"].append([jc.power.linear_matter_power(c, k, a, transfer_fn=nw) for a in a_list])
+        c = _cosmo(jc, row)
+        cols["pnl_nw"].append([jc.power.nonlinear_matter_power(c, k, a, transfer_fn=nw) for a in a_list])
+        c = _cosmo(jc, row)
+        cols["pnl_smith"].append([jc.power.nonlinear_matter_power(c, k, a, nonlinear_fn=smith) for a in a_list])
+        cols["pnl_smith_pairs"].append(jc.power.nonlinear_matter_power(c, k_pairs, a_pairs, nonlinear_fn=smith))
+        cols["pnl_lin"].append(
+            [jc.power.nonlinear_matter_power(c, k, a, nonlinear_fn=jc.power.linear_matter_power) for a in a_list]
+        )
+    out.update({n: np.array(v) for n, v in cols.items()})
+    return out
+
+
+# operator-point variants of the cl_physics fixture: (transfer type, nonlinear_fn)
+PHYSICS_VARIANTS = (("eisenhu_osc", "smith2003"), ("eisenhu_osc", "linear"), ("eisenhu", "takahashi2012"))
+
+
+def _fns(jc, variant):
+    import functools
+
+    tf_type, nl = variant
+    tf = functools.partial(jc.transfer.Eisenstein_Hu, type=tf_type)
+    if nl == "linear":
+        return tf, jc.power.linear_matter_power
+    return tf, functools.partial(jc.power.halofit, prescription=nl)
+
+
 def make_tracers(jc):
     z = np.linspace(0.0, 5.0, 101)
     smail = np.array([[1.0, 2.0, 0.5, 4.0], [1.0, 2.0, 1.0, 4.0], [2.0, 1.5, 0.8, 10.0]])
@@ -241,6 +292,13 @@ def _probes(jc, kind):
             jc.probes.WeakLensing([fu, kde, shift], sigma_e=0.26),
             jc.probes.NumberCounts([kde], jc.bias.constant_linear_bias(1.2)),
         ]
+    if kind == "physics":
+        pa = jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10)
+        pb = jc.redshift.smail_nz(1.0, 2.0, 1.0, gals_per_arcmin2=10)
+        return [
+            jc.probes.WeakLensing([pa, pb], sigma_e=0.26),
+            jc.probes.NumberCounts([pb], jc.bias.constant_linear_bias(1.2)),
+        ]
     if kind == "delta":
         pa = jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10)
         return [
@@ -262,14 +320,17 @@ def nz_catalog():
 
 
 def _cl_worker(args):
-    reference, kind, row, ell = args
+    reference, kind, row, ell, variant = args
     jc = _setup(reference)
     c = _cosmo(jc, row)
-    return jc.angular_cl.angular_cl(c, np.array([ell]), _probes(jc, kind))[:, 0]
+    if variant is None:
+        return jc.angular_cl.angular_cl(c, np.array([ell]), _probes(jc, kind))[:, 0]
+    tf, nl = _fns(jc, variant)
+    return jc.angular_cl.angular_cl(c, np.array([ell]), _probes(jc, kind), tf, nl)[:, 0]
 
 
-def make_cl(reference, pool, kind, cosmo_rows, ell):
-    jobs = [(reference, kind, row, float(l)) for row in cosmo_rows for l in ell]
+def make_cl(reference, pool, kind, cosmo_rows, ell, variant=None):
+    jobs = [(reference, kind, row, float(l), variant) for row in cosmo_rows for l in ell]
     res = pool.map(_cl_worker, jobs)
     n_c, n_l = len(cosmo_rows), len(ell)
     cl = np.array(res).reshape(n_c, n_l, -1).transpose(0, 2, 1)
@@ -364,13 +425,15 @@ def main():
         save("background2", make_background2(jc))
     if want("power"):
         save("power", make_power(jc))
+    if want("power2"):
+        save("power2", make_power2(jc))
     if want("tracers"):
         save("tracers", make_tracers(jc))
     if want("cov_like"):
         save("cov_like", make_cov_like(jc))
     if want("sparse"):
         save("sparse", make_sparse(jc))
-    if want("cl_wl2") or want("cl_mixed") or want("cl_ia") or want("cl_nz") or want("cl_delta"):
+    if any(want(n) for n in ("cl_wl2", "cl_mixed", "cl_ia", "cl_nz", "cl_delta", "cl_physics")):
         import multiprocessing as mp
 
         with mp.get_context("spawn").Pool(args.procs) as pool:
@@ -394,6 +457,14 @@ def main():
             if want("cl_delta"):
                 ell = np.logspace(1, np.log10(5000.0), 10)
                 save("cl_delta", make_cl(args.reference, pool, "delta", COSMOS[[0, 2]], ell))
+            if want("cl_physics"):
+                ell = np.logspace(1, np.log10(5000.0), 10)
+                d = {}
+                for v in PHYSICS_VARIANTS:
+                    r = make_cl(args.reference, pool, "physics", COSMOS[[0, 2]], ell, v)
+                    d["cl_" + "_".join(v)] = r.pop("cl")
+                    d.update(r)
+                save("cl_physics", d)
 
 
 if __name__ == "__main__":

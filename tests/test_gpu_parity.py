@@ -448,3 +448,81 @@ def test_single_plane_nz_vs_golden(golden):
         err = max(float((J[..., d].cpu() - J_o[..., d]).abs().max() / J_o[..., d].abs().max().clamp_min(1e-300))
                   for d in range(8))
         assert err < tol, (prec, err)
+
+
+# ---------------------------------------------- non-default operator points --
+PHYSICS_VARIANTS = (("eisenhu_osc", "smith2003"), ("eisenhu_osc", "linear"), ("eisenhu", "takahashi2012"))
+
+
+def _fns(variant):
+    import functools
+
+    tf_type, nl = variant
+    tf = functools.partial(jc.transfer.Eisenstein_Hu, type=tf_type)
+    if nl == "linear":
+        return tf, jc.power.linear_matter_power
+    return tf, functools.partial(jc.power.halofit, prescription=nl)
+
+
+def _physics_probes():
+    pa = jc.redshift.smail_nz(1.0, 2.0, 0.5, gals_per_arcmin2=10)
+    pb = jc.redshift.smail_nz(1.0, 2.0, 1.0, gals_per_arcmin2=10)
+    return [jc.probes.WeakLensing([pa, pb], sigma_e=0.26),
+            jc.probes.NumberCounts([pb], jc.bias.constant_linear_bias(1.2))]
+
+
+def test_power_operator_points_vs_golden(golden):
+    """Eisenstein_Hu type "eisenhu", halofit smith2003 and linear_matter_power as
+    nonlinear_fn at (k, a) points against the unmodified reference."""
+    import functools
+
+    p = golden("power2")
+    k = p["k"]
+    nw = functools.partial(jc.transfer.Eisenstein_Hu, type="eisenhu")
+    smith = functools.partial(jc.power.halofit, prescription="smith2003")
+    for i, row in enumerate(p["cosmos"]):
+        c = cosmo_of(row)
+        assert rel(jc.transfer.Eisenstein_Hu(c, k, type="eisenhu"), p["T_nw"][i]) < RT64
+        for j, a in enumerate(p["a_list"]):
+            assert rel(jc.power.linear_matter_power(c, k, a, transfer_fn=nw), p["plin_nw"][i][j]) < RT64
+            assert rel(jc.power.nonlinear_matter_power(c, k, a, transfer_fn=nw), p["pnl_nw"][i][j]) < RT64
+            assert rel(jc.power.nonlinear_matter_power(c, k, a, nonlinear_fn=smith), p["pnl_smith"][i][j]) < RT64
+            lin = jc.power.nonlinear_matter_power(c, k, a, nonlinear_fn=jc.power.linear_matter_power)
+            assert rel(lin, p["pnl_lin"][i][j]) < RT64
+        pairs = jc.power.nonlinear_matter_power(c, p["k_pairs"], p["a_pairs"], nonlinear_fn=smith)
+        assert rel(pairs, p["pnl_smith_pairs"][i]) < RT64
+
+
+@pytest.mark.parametrize("variant", PHYSICS_VARIANTS, ids=["smith2003", "linear", "nowiggle"])
+def test_angular_cl_operator_points_vs_golden(golden, variant):
+    """angular_cl with the non-default transfer_fn / nonlinear_fn against the
+    unmodified reference (FP64 and fp32c, batched), and the Jacobian in both
+    precisions against the oracle's autograd."""
+    g = golden("cl_physics")
+    tf, nl = _fns(variant)
+    ref = g["cl_" + "_".join(variant)]
+    cb = cosmo_batch(g["cosmos"])
+    cl = jc.cl.angular_cl(cb, g["ell"], _physics_probes(), tf, nl)
+    cl32 = jc.cl.angular_cl(cb, g["ell"], _physics_probes(), tf, nl, precision="fp32c")
+    for i in range(len(g["cosmos"])):
+        assert rel(cl[i], ref[i]) < RT64
+        assert rel(cl32[i], ref[i]) < RT32
+    # the default operator points give a different answer (the switch is live)
+    assert rel(jc.cl.angular_cl(cb, g["ell"], _physics_probes())[0], ref[0]) > 1e-6
+    ell = g["ell"][::3]
+    pa, pb = O.Smail(1, 2, 0.5, 10.0, 10), O.Smail(1, 2, 1.0, 10.0, 10)
+    oprobes = [O.Probe("wl", [pa, pb], sigma_e=0.26), O.Probe("nc", [pb], bias=1.2)]
+    row = list(g["cosmos"][1])
+
+    def f(v):
+        c = O.Cosmo.from_vector(v)
+        c.transfer = variant[0]
+        return O.angular_cl(c, ell, oprobes, n_limber=128, nonlinear=variant[1])
+
+    J_o = torch.autograd.functional.jacobian(f, torch.tensor(row, dtype=torch.float64), strategy="forward-mode",
+                                             vectorize=True)
+    for prec, tol in (("fp64", 1e-8), ("fp32c", 1e-4)):
+        _, J = jc.autodiff.angular_cl_jacobian(cosmo_of(row), ell, _physics_probes(), 128, prec, tf, nl)
+        err = max(float((J[..., d].cpu() - J_o[..., d]).abs().max() / J_o[..., d].abs().max().clamp_min(1e-300))
+                  for d in range(8))
+        assert err < tol, (prec, err)

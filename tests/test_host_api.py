@@ -1,5 +1,6 @@
 """Host-side logic of the Python API (no GPU): descriptors, orderings, batching."""
 import ctypes
+import functools
 
 import numpy as np
 import pytest
@@ -111,6 +112,21 @@ def test_cosmology_batching():
     assert jc.Cosmology.tree_unflatten(*reversed(c.tree_flatten())).h == 0.6774
 
 
+def test_physics_codes():
+    """The operator points of angular_cl map to the descriptor's physics word
+    (transfer.py:10-156, power.py:144-272)."""
+    tf, hf = jc.transfer.Eisenstein_Hu, jc.power.halofit
+    nw = functools.partial(tf, type="eisenhu")
+    assert jc.cl.physics_code(tf, hf) == 0
+    assert jc.cl.physics_code(functools.partial(tf, type="eisenhu_osc"), functools.partial(hf)) == 0
+    assert jc.cl.physics_code(tf, functools.partial(hf, prescription="smith2003")) == _lib.PK_SMITH2003
+    assert jc.cl.physics_code(tf, jc.power.linear_matter_power) == _lib.PK_LINEAR
+    assert jc.cl.physics_code(nw, hf) == _lib.TF_NOWIGGLE
+    assert jc.cl.physics_code(nw, jc.power.linear_matter_power) == _lib.TF_NOWIGGLE | _lib.PK_LINEAR
+    g = _geometry.describe([jc.probes.WeakLensing([jc.redshift.smail_nz(1.0, 2.0, 0.5)])], 4, physics=0x11)
+    assert g.physics == 0x11
+
+
 def test_smail_nz_host_evaluation_matches_oracle():
     nz = jc.redshift.smail_nz(1.0, 2.0, 0.5, zmax=4.0)
     z = torch.linspace(0, 4, 41, dtype=torch.float64)
@@ -121,9 +137,13 @@ def test_smail_nz_host_evaluation_matches_oracle():
 def test_unsupported_options_raise():
     c = jc.Planck15()
     with pytest.raises(NotImplementedError):
-        jc.cl._check_fns(lambda *a: None, jc.power.halofit)
+        jc.cl.physics_code(lambda *a: None, jc.power.halofit)
     with pytest.raises(NotImplementedError):
-        jc.cl._check_fns(jc.transfer.Eisenstein_Hu, lambda *a: None)
+        jc.cl.physics_code(jc.transfer.Eisenstein_Hu, lambda *a: None)
+    with pytest.raises(NotImplementedError):
+        jc.cl.physics_code(functools.partial(jc.transfer.Eisenstein_Hu, type="bbks"), jc.power.halofit)
+    with pytest.raises(NotImplementedError):
+        jc.cl.physics_code(jc.transfer.Eisenstein_Hu, functools.partial(jc.power.halofit, prescription="x"))
     with pytest.raises(ValueError):
         jc.cl._precision_code("fp16")
     with pytest.raises(NotImplementedError):

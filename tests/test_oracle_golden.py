@@ -191,3 +191,45 @@ def test_interp_quirks():
     xd = torch.tensor([8.0, 4.0, 2.0, 1.0, 0.0], dtype=torch.float64)
     v = float(O.interp(torch.tensor([2.2], dtype=torch.float64), xd, fp))
     assert v == pytest.approx(10.0 + (2.2 - 4.0) * (20.0 - 10.0) / (2.0 - 4.0))
+
+
+PHYSICS_VARIANTS = (("eisenhu_osc", "smith2003"), ("eisenhu_osc", "linear"), ("eisenhu", "takahashi2012"))
+
+
+def physics_probes():
+    pa, pb = O.Smail(1, 2, 0.5, 10.0, 10), O.Smail(1, 2, 1.0, 10.0, 10)
+    return [O.Probe("wl", [pa, pb], sigma_e=0.26), O.Probe("nc", [pb], bias=1.2)]
+
+
+def test_power_operator_points(golden):
+    """Eisenstein_Hu type "eisenhu" (transfer.py:99-105), halofit smith2003
+    (power.py:182-244) and linear_matter_power as nonlinear_fn."""
+    p = golden("power2")
+    k = torch.tensor(p["k"])
+    for i, row in enumerate(p["cosmos"]):
+        cn = O.Cosmo.from_vector(row)
+        cn.transfer = "eisenhu"
+        assert rel(O.eisenstein_hu(cn, k), p["T_nw"][i]) < RTOL
+        assert rel(O.sigmasqr(cn), p["s8_nw"][i]) < RTOL
+        c = O.Cosmo.from_vector(row)
+        for j, a in enumerate(p["a_list"]):
+            at = torch.tensor([a])
+            assert rel(O.linear_matter_power(cn, k, a), p["plin_nw"][i][j]) < RTOL
+            assert rel(O.halofit(cn, k, at), p["pnl_nw"][i][j]) < 1e-11
+            assert rel(O.halofit(c, k, at, "smith2003"), p["pnl_smith"][i][j]) < 1e-11
+            assert rel(O.linear_matter_power(c, k, a), p["pnl_lin"][i][j]) < RTOL
+        pairs = O.halofit(c, torch.tensor(p["k_pairs"]), torch.tensor(p["a_pairs"]), "smith2003")
+        assert rel(pairs, p["pnl_smith_pairs"][i]) < 1e-11
+
+
+@pytest.mark.parametrize("variant", PHYSICS_VARIANTS, ids=["smith2003", "linear", "nowiggle"])
+def test_angular_cl_operator_points(golden, variant):
+    g = golden("cl_physics")
+    tf, nl = variant
+    for i, row in enumerate(g["cosmos"]):
+        c = O.Cosmo.from_vector(row)
+        c.transfer = tf
+        cl = O.angular_cl(c, g["ell"], physics_probes(), nonlinear=nl)
+        ref = g["cl_" + "_".join(variant)][i]
+        assert cl.shape == ref.shape
+        assert rel(cl, ref) < 1e-11
