@@ -85,12 +85,19 @@ extern "C" {
  *   LINEAR         power.linear_matter_power (power.py:21-53), no halofit
  * and the transfer function (transfer_fn):
  *   NOWIGGLE       transfer.Eisenstein_Hu with type "eisenhu" (transfer.py:99-105),
- *                  the zero-baryon fit without oscillations; unset: "eisenhu_osc". */
+ *                  the zero-baryon fit without oscillations; unset: "eisenhu_osc";
+ * and the growth model (GROWTH_GAMMA below). */
 #define JCG_PK_TAKAHASHI2012 0
 #define JCG_PK_SMITH2003 1
 #define JCG_PK_LINEAR 2
 #define JCG_PK_MASK 0x0f
 #define JCG_TF_NOWIGGLE 0x10
+/* Growth from the growth-rate index gamma, f = Omega_m(a)^gamma
+ * (Cosmology(gamma=...), background.py:515-582) instead of the growth ODE.
+ * With this bit the parameter arrays hold 9 values per cosmology, the 9th
+ * gamma; the Jacobians stay with respect to the first 8 (gamma held fixed). */
+#define JCG_GROWTH_GAMMA 0x20
+#define JCG_PHYSICS_ALL (JCG_PK_MASK | JCG_TF_NOWIGGLE | JCG_GROWTH_GAMMA)
 
 /* arithmetic of the Limber stage */
 #define JCG_FP64 0  /* plain: float64 everywhere */
@@ -120,7 +127,7 @@ typedef struct jcg_geometry {
   double bias_eta[JCG_MAX_TRACERS];   /* des_y1_ia_bias eta, z0 (bias.py:55-57) */
   double bias_z0[JCG_MAX_TRACERS];
   int nz_kind[JCG_MAX_TRACERS];       /* JCG_NZ_* */
-  int physics;                        /* JCG_PK_* | JCG_TF_* (0: the reference defaults) */
+  int physics;                        /* JCG_PK_* | JCG_TF_* | JCG_GROWTH_GAMMA (0: the reference defaults) */
 } jcg_geometry;
 
 /* ------------------------------------------------------------- misc ---- */
@@ -288,7 +295,8 @@ int jcg_workspace_read(const jcg_geometry* g, int n_cosmo, int precision, const 
  *  12 a_of_chi(chi), chi in a_dev      background.py:245-267
  *  13 growth_rate(a)                   background.py:401-440 (ODE growth)
  * in the low byte of `what`; bits 8 and up hold the physics switches
- * (JCG_PK_* | JCG_TF_*) << 8 for 4-9.
+ * (JCG_PK_* | JCG_TF_* | JCG_GROWTH_GAMMA) << 8; with JCG_GROWTH_GAMMA params
+ * holds 9 values per cosmology and 1 / 13 are the gamma growth factor / rate.
  * Needs a workspace of jcg_workspace_size(g=NULL -> tables only). */
 int jcg_eval_points(const double* params_dev, int n_cosmo, const double* a_dev,
                     const double* k_dev, int n, int what, double* out_dev, void* workspace,

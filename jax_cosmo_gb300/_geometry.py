@@ -174,7 +174,7 @@ def probe_kernel(probe, cosmo, z, ell):
     z_t = torch.as_tensor(np.atleast_1d(np.asarray(z, dtype=np.float64))).reshape(-1).to(device)
     ell_f = float(np.asarray(ell, dtype=np.float64).reshape(-1)[0])
     ell_t = torch.tensor([ell_f], dtype=torch.float64, device=device)
-    g = describe([probe], 1, 512, n_nodes=z_t.numel())
+    g = describe([probe], 1, 512, n_nodes=z_t.numel(), physics=cosmo.physics_bits())
     size = ctypes.c_size_t()
     _lib.call("jcg_geometry_size", ctypes.byref(g), ctypes.byref(size))
     geo = _lib.workspace(size.value, device)

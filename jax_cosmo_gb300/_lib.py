@@ -45,6 +45,7 @@ FP32C = 1
 # physics switches (jcg_geometry.physics; bits 8+ of jcg_eval_points' what)
 PK_TAKAHASHI2012, PK_SMITH2003, PK_LINEAR = 0, 1, 2
 TF_NOWIGGLE = 0x10
+GROWTH_GAMMA = 0x20
 
 EVAL_CHI, EVAL_GROWTH, EVAL_H, EVAL_DCHI, EVAL_TRANSFER, EVAL_PLIN, EVAL_PNL = range(7)
 EVAL_KNL, EVAL_NEFF, EVAL_C = 7, 8, 9

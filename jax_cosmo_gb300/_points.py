@@ -37,6 +37,7 @@ def evaluate(cosmo, what, a=None, k=None):
     _lib.call("jcg_eval_workspace_size", B, ctypes.byref(wsz))
     ws = _lib.workspace(wsz.value, device)
     out = torch.empty(B, n, dtype=torch.float64, device=device)
+    what = what | (cosmo.physics_bits() << 8)
     _lib.call("jcg_eval_points", _lib.ptr(params), B, _lib.ptr(a_t), _lib.ptr(k_t), n, what,
               _lib.ptr(out), _lib.ptr(ws), ctypes.c_size_t(ws.numel()), _lib.stream_of(device))
     return out if cosmo.batch_size is not None else out[0]

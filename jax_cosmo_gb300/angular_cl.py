@@ -84,7 +84,8 @@ def _precision_code(precision):
 
 
 def angular_cl_device(params, ell, probes, precision="fp64", n_limber=512, out=None, physics=0):
-    """C_ell for a [B, 8] float64 parameter tensor on the device -> [B, n_cls, n_ell].
+    """C_ell for a [B, 8] float64 parameter tensor on the device -> [B, n_cls, n_ell]
+    ([B, 9] with gamma last when ``physics`` has GROWTH_GAMMA).
 
     Lower-level entry used by the public function, the autograd wrapper and the
     serving loop; ``params`` (and ``out``) live on the device, ``ell`` is a host
@@ -122,7 +123,7 @@ def angular_cl(
     A batched cosmology gives [B, n_cls, n_ell].  Differentiable with respect to
     Cosmology parameters that are tensors with ``requires_grad``.
     """
-    physics = physics_code(transfer_fn, nonlinear_fn)
+    physics = physics_code(transfer_fn, nonlinear_fn) | cosmo.physics_bits()
     device = _lib.require_cuda()
     ell_np = _geometry.ell_host(ell)
     if cosmo.requires_grad():

@@ -73,17 +73,23 @@ class _AngularCl(torch.autograd.Function):
         ell, probes, n_limber, precision, physics = ctx.meta
         _, jac = jacobian_device(params.detach().contiguous(), ell, probes, n_limber, precision, physics)
         gp = torch.einsum("bpl,bpld->bd", gcl.to(torch.float64), jac)
+        if params.shape[1] > gp.shape[1]:  # gamma: held fixed (checked in angular_cl_autograd)
+            gp = torch.cat([gp, gp.new_zeros(gp.shape[0], params.shape[1] - gp.shape[1])], dim=1)
         return gp, None, None, None, None, None
 
 
 def angular_cl_autograd(cosmo, ell, probes, precision="fp64", n_limber=512, physics=0):
+    g = getattr(cosmo, "_gamma", None)
+    if isinstance(g, torch.Tensor) and g.requires_grad:
+        raise NotImplementedError("derivatives with respect to gamma are not provided (gamma is held fixed)")
     device = _lib.require_cuda()
     params = cosmo.param_tensor(device, differentiable=True)
     return _AngularCl.apply(params, ell, probes, precision, n_limber, physics)
 
 
 def angular_cl_jacobian(cosmo, ell, probes, n_limber=512, precision="fp64", transfer_fn=None, nonlinear_fn=None):
-    """(C_ell, dC_ell/dtheta) with theta = (Omega_c, Omega_b, h, n_s, sigma8, Omega_k, w0, wa).
+    """(C_ell, dC_ell/dtheta) with theta = (Omega_c, Omega_b, h, n_s, sigma8, Omega_k, w0, wa)
+    (a gamma of the Cosmology is held fixed).
 
     Shapes [n_cls, n_ell] and [n_cls, n_ell, 8] (a leading batch axis for a
     batched Cosmology).  precision "fp64" or "fp32c"; transfer_fn and
@@ -93,6 +99,7 @@ def angular_cl_jacobian(cosmo, ell, probes, n_limber=512, precision="fp64", tran
     from jax_cosmo_gb300.angular_cl import physics_code
 
     physics = physics_code(transfer_fn or transfer.Eisenstein_Hu, nonlinear_fn or power.halofit)
+    physics |= cosmo.physics_bits()
     device = _lib.require_cuda()
     params = cosmo.param_tensor(device)
     cl, jac = jacobian_device(params, _geometry.ell_host(ell), probes, n_limber, precision, physics)

@@ -70,9 +70,9 @@ def radial_comoving_distance(cosmo, a, log10_amin=-3, steps=256):
 
 
 def growth_factor(cosmo, a):
-    """Linear growth factor D(a), D(1) = 1 (background.py:371-398, 443-488)."""
-    if cosmo._flags.get("gamma_growth"):
-        raise NotImplementedError("gamma growth (background.py:515-582) is not accelerated")
+    """Linear growth factor D(a), D(1) = 1: the growth ODE (background.py:371-398,
+    443-488), or with a Cosmology gamma the integral of Omega_m(a)^gamma
+    (background.py:515-552)."""
     return _points.evaluate(cosmo, _lib.EVAL_GROWTH, a=a)
 
 
@@ -94,7 +94,6 @@ def angular_diameter_distance(cosmo, a):
 
 
 def growth_rate(cosmo, a):
-    """Growth rate dlnD/dlna from the growth ODE table (background.py:401-440, 491-512)."""
-    if cosmo._flags.get("gamma_growth"):
-        raise NotImplementedError("gamma growth (background.py:515-582) is not accelerated")
+    """Growth rate dlnD/dlna from the growth ODE table (background.py:401-440, 491-512),
+    or Omega_m(a)^gamma with a Cosmology gamma (background.py:555-582)."""
     return _points.evaluate(cosmo, _lib.EVAL_GROWTH_RATE, a=a)

@@ -13,6 +13,8 @@ import math
 import numpy as np
 import torch
 
+from jax_cosmo_gb300 import _lib
+
 __all__ = ["Cosmology"]
 
 PARAM_NAMES = ("Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa")
@@ -68,7 +70,15 @@ class Cosmology:
 
     # ---------------------------------------------------------------- batch --
     def param_list(self):
-        return [getattr(self, "_" + n) for n in PARAM_NAMES]
+        """The 8 parameters, then gamma when the growth is parametrised by it."""
+        ps = [getattr(self, "_" + n) for n in PARAM_NAMES]
+        if self._flags["gamma_growth"]:
+            ps.append(self._gamma)
+        return ps
+
+    def physics_bits(self):
+        """libjcg physics bits of this cosmology: JCG_GROWTH_GAMMA when gamma is set."""
+        return _lib.GROWTH_GAMMA if self._flags["gamma_growth"] else 0
 
     @property
     def batch_size(self):
@@ -86,11 +96,8 @@ class Cosmology:
         return any(isinstance(v, torch.Tensor) and v.requires_grad for v in self.param_list())
 
     def param_tensor(self, device, differentiable=False):
-        """[B, 8] float64 tensor on ``device`` (B = 1 for a single cosmology)."""
-        if self._flags["gamma_growth"]:
-            raise NotImplementedError(
-                "gamma growth (background.py:515-582) is not on the accelerated path"
-            )
+        """[B, 8] float64 tensor on ``device`` (B = 1 for a single cosmology);
+        [B, 9] with gamma last when the growth is parametrised by gamma."""
         B = self.batch_size or 1
         cols = []
         for v in self.param_list():

@@ -99,7 +99,7 @@ static int make_header(const jcg_geometry* g, GeoHeader* h) {
     return fail(JCG_ERR_SHAPE, "n_z = %d", n_nodes);
   }
   if (!(g->zmax > 0.0) || !isfinite(g->zmax)) return fail(JCG_ERR_VALUE, "zmax = %g", g->zmax);
-  if ((g->physics & ~(JCG_PK_MASK | JCG_TF_NOWIGGLE)) != 0 || pk_model(g->physics) > JCG_PK_LINEAR)
+  if ((g->physics & ~JCG_PHYSICS_ALL) != 0 || pk_model(g->physics) > JCG_PK_LINEAR)
     return fail(JCG_ERR_UNSUPPORTED, "physics = 0x%x", g->physics);
   memset(h, 0, sizeof(*h));
   h->physics = g->physics;
@@ -510,7 +510,7 @@ int jcg_eval_points(const double* params, int n_cosmo, const double* a, const do
   if (n < 1) return fail(JCG_ERR_SHAPE, "n = %d", n);
   const int phys = what >> 8;
   if (what < 0 || (what & 0xff) > 13) return fail(JCG_ERR_ARG, "what = %d", what);
-  if ((phys & ~(JCG_PK_MASK | JCG_TF_NOWIGGLE)) != 0 || pk_model(phys) > JCG_PK_LINEAR)
+  if ((phys & ~JCG_PHYSICS_ALL) != 0 || pk_model(phys) > JCG_PK_LINEAR)
     return fail(JCG_ERR_UNSUPPORTED, "physics = 0x%x", phys);
   const int q = what & 0xff;
   const bool need_a = (q <= 3) || q >= 5;  // a_of_chi (12) takes chi in a_dev

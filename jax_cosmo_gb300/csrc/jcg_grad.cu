@@ -1600,6 +1600,61 @@ __global__ void __launch_bounds__(128) grad_scalars_warp_kernel(GradBatch gb) {
   if (lane + 32 < NSCAL) gi.tab->sd[dir][lane + 32] = v2.d[0];
 }
 
+// Growth for JCG_GROWTH_GAMMA (background.py:515-582) with the tangents of
+// the 8 parameters (gamma held fixed): the forward growth_gamma_kernel's
+// recurrence in Dual<1>, one warp per direction (warp 0 also writes the
+// values).  Replaces the growth-ODE table grad_tables wrote.
+__global__ void __launch_bounds__(32 * NDIR) grad_growth_gamma_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+  const int item = blockIdx.x;
+  if (item >= gb.n_items) return;
+  const GradItem gi = grad_item(gb, item);
+  if (!growth_gamma(gi.geo->physics)) return;
+  __shared__ double fv[NGROW], fmv[NGROW], fd[NDIR][NGROW], fmd[NDIR][NGROW];
+  const int d = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  TabD* tb = gi.tab;
+  const double gam = gi.params[8];
+  D1 sD[NSCAL];
+  for (int i = 0; i < NSCAL; ++i) sD[i] = mk1(tb->sv[i], tb->sd[d][i]);
+  const BgT<D1> bg = make_bgT(sD);
+  auto f_of = [&](double lna) {
+    const double a = exp(lna);
+    D1 om_m, om_de;
+    omT(bg, a, log(a), om_m, om_de);
+    return xexp(gam * xlog(om_m));
+  };
+  for (int i = lane; i < NGROW; i += 32) {
+    const double lna = c->grow_lna[i];
+    const D1 f = f_of(lna);
+    if (d == 0) fv[i] = f.v;
+    fd[d][i] = f.d[0];
+    if (i > 0) {
+      const double lp = c->grow_lna[i - 1];
+      const D1 fm = f_of(lp + (lna - lp) / 2);
+      if (d == 0) fmv[i] = fm.v;
+      fmd[d][i] = fm.d[0];
+    }
+  }
+  __syncthreads();
+  if (lane == 0) {
+    // values: the forward recurrence; tangents: the same sums of tangents
+    D1 y = mk1(c->grow_lna[0], 0.0);
+    D1 ys[NGROW];
+    ys[0] = y;
+    for (int i = 1; i < NGROW; ++i) {
+      const double h = c->grow_lna[i] - c->grow_lna[i - 1];
+      const D1 f0 = mk1(fv[i - 1], fd[d][i - 1]), fm = mk1(fmv[i], fmd[d][i]), f1 = mk1(fv[i], fd[d][i]);
+      y = y + 1.0 / 6.0 * h * (((f0 + 2.0 * fm) + 2.0 * fm) + f1);
+      ys[i] = y;
+    }
+    const D1 el = xexp(ys[NGROW - 1]);
+    for (int i = 0; i < NGROW; ++i) {
+      const D1 g = xexp(ys[i]) / el;
+      if (d == 0) tb->gv[i] = g.v;
+      tb->gd[d][i] = g.d[0];
+    }
+  }
+}
+
 void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
   const size_t smt = grad_tables_smem();
   if (gb.n_items <= GNODE_MAX_ITEMS)
@@ -1619,6 +1674,7 @@ void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
     cudaFuncSetAttribute(grad_tables_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
     grad_tables_kernel<false, true><<<gb.n_items, 256, smt, st>>>(gb, c);
   }
+  if (growth_gamma(gb.physics_or)) grad_growth_gamma_kernel<<<gb.n_items, 32 * NDIR, 0, st>>>(gb, c);
   if (gb.precision == JCG_FP32C) {
     dim3 grw((gb.na + GR32_THREADS - 1) / GR32_THREADS, gb.n_items);
     grad_rows32_kernel<<<grw, GR32_THREADS, 0, st>>>(gb, c);

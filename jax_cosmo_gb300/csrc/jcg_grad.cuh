@@ -158,7 +158,7 @@ __device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
   if (gb.listed) return gb.items[i];
   GradItem r;
   const size_t per = (size_t)gb.n_cls * gb.n_ell;
-  r.params = gb.params + 8 * (size_t)i;
+  r.params = gb.params + (size_t)param_stride(gb.physics_or) * i;
   r.geo = gb.geo;
   r.tab = gb.tab + i;
   r.rowd = gb.rowd ? gb.rowd + (size_t)i * gb.na * NROWD : nullptr;

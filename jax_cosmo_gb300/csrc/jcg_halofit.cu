@@ -572,6 +572,9 @@ __global__ void eval_points_kernel(const double* __restrict__ params, int n_cosm
     // a_of_chi (background.py:245-267): interp(chi, chi table, a table) with the
     // reference's rule on the decreasing chi table
     v = interp_ref_warp(a, ct->chi, c->atab_chi, NCHI, lane);
+  } else if (what == 13 && growth_gamma(what_phys >> 8)) {
+    // growth_rate with gamma: Omega_m(a)^gamma (background.py:555-582)
+    v = pow(bg_omm(bg, a), s[S_GAMMA]);
   } else if (what == 13) {
     // growth_rate (background.py:401-440, 491-512): interp(a, atab, ftab), no clip
     const int2 sg = interp_segment_inc(a, c->atab_grow, NGROW, logspace_guess(a, NGROW));

@@ -102,6 +102,7 @@ enum Scalar {
   S_AGAM,       // alpha_gamma of the no-wiggle fit (transfer.py:88-92)
   S_NWQ,        // (T_cmb / 2.7)^2 / (Omega_m h): q = k S_NWQ / (gamma_eff / (Omega_m h)) (transfer.py:93-100)
   S_TFNW,       // 1: transfer type "eisenhu" (no wiggles), 0: "eisenhu_osc"
+  S_GAMMA,      // growth-rate index gamma (JCG_GROWTH_GAMMA), else 0
   S_NSCALAR
 };
 constexpr int NSCAL = 40;
@@ -174,6 +175,9 @@ static_assert(NROW32_USED <= NROW32, "fp32 row too small");
 // Physics switches of a request.
 __host__ __device__ __forceinline__ int pk_model(int physics) { return physics & JCG_PK_MASK; }
 __host__ __device__ __forceinline__ bool tf_nowiggle(int physics) { return (physics & JCG_TF_NOWIGGLE) != 0; }
+__host__ __device__ __forceinline__ bool growth_gamma(int physics) { return (physics & JCG_GROWTH_GAMMA) != 0; }
+// doubles per cosmology in a parameter array: 8, or 9 with gamma
+__host__ __device__ __forceinline__ int param_stride(int physics) { return growth_gamma(physics) ? 9 : 8; }
 
 // ------------------------------------------------------ geometry tables ----
 // Cosmology-independent description of one request, stored at the start of the
@@ -259,7 +263,7 @@ __device__ __forceinline__ Item batch_item(const Batch& b, int i) {
   if (b.listed) return b.items[i];
   Item it;
   const int na = b.max_na;
-  it.params = b.params + 8 * (size_t)i;
+  it.params = b.params + (size_t)param_stride(b.physics) * i;
   it.geo = b.geo;
   it.ctab = b.ctab + i;
   it.rows64 = b.rows64 ? b.rows64 + (size_t)i * na * NROW64 : nullptr;

@@ -495,12 +495,58 @@ __global__ void __launch_bounds__(128) cosmo_scalars_kernel(Batch bt) {
   }
 }
 
+// Growth for JCG_GROWTH_GAMMA (background.py:515-582): f(a) = Omega_m(a)^gamma
+// at the 128 nodes of the growth table and at the RK4 midpoints in ln a,
+// exp((ln a_{i-1} + ln a_i) / 2).  The reference's odeint with a right-hand
+// side independent of y is y_i = y_{i-1} + h/6 (f_{i-1} + 2 f_m + 2 f_m + f_i),
+// y_0 = ln a_0 (scipy/ode.py:6-22); g_i = exp(y_i) / exp(y_last).  Replaces
+// the growth-ODE tables cosmo_tables wrote (nothing there depends on them
+// but growth(a = 1) = 1, the same for both) and stores the growth rate f at
+// the nodes and gamma in the scalars.  One CTA per cosmology.
+__global__ void __launch_bounds__(128) growth_gamma_kernel(Batch bt, const ConstTables* __restrict__ c) {
+  const int item = blockIdx.x;
+  if (item >= bt.n_items) return;
+  const Item it = batch_item(bt, item);
+  if (!growth_gamma(it.physics)) return;
+  __shared__ double fn[NGROW], fm[NGROW], ys[NGROW];
+  CosmoTab* ct = it.ctab;
+  const double gam = it.params[8];
+  const Bg bg = make_bg(ct->s);
+  const int t = threadIdx.x;
+  for (int i = t; i < NGROW; i += blockDim.x) {
+    const double lna = c->grow_lna[i];
+    fn[i] = pow(bg_omm(bg, exp(lna)), gam);
+    if (i > 0) {
+      const double lp = c->grow_lna[i - 1];
+      fm[i] = pow(bg_omm(bg, exp(lp + (lna - lp) / 2)), gam);
+    }
+  }
+  __syncthreads();
+  if (t == 0) {
+    double y = c->grow_lna[0];
+    ys[0] = y;
+    for (int i = 1; i < NGROW; ++i) {
+      const double h = c->grow_lna[i] - c->grow_lna[i - 1];
+      y = y + 1.0 / 6.0 * h * (((fn[i - 1] + 2.0 * fm[i]) + 2.0 * fm[i]) + fn[i]);
+      ys[i] = y;
+    }
+  }
+  __syncthreads();
+  const double el = exp(ys[NGROW - 1]);
+  for (int i = t; i < NGROW; i += blockDim.x) {
+    ct->g[i] = exp(ys[i]) / el;
+    ct->f[i] = fn[i];
+  }
+  if (t == 0) ct->s[S_GAMMA] = gam;
+}
+
 void launch_cosmo_tables(const Batch& b, const ConstTables* c, cudaStream_t st) {
   cosmo_scalars_kernel<<<(b.n_items + 7) / 8, 128, 0, st>>>(b);
   if (tf_nowiggle(b.physics_or))
     cosmo_tables_kernel<true><<<b.n_items, 256, 0, st>>>(b, c);
   else
     cosmo_tables_kernel<false><<<b.n_items, 256, 0, st>>>(b, c);
+  if (growth_gamma(b.physics_or)) growth_gamma_kernel<<<b.n_items, 128, 0, st>>>(b, c);
 }
 
 }  // namespace jcg

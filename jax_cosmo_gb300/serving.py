@@ -462,6 +462,8 @@ def angular_cl_ragged(items, precision="fp32c", n_limber=512, device=None):
     for i, (cosmo, ell, probes) in enumerate(items):
         if cosmo.batch_size is not None:
             raise ValueError("angular_cl_ragged takes one cosmology per item")
+        if cosmo.physics_bits():
+            raise NotImplementedError("angular_cl_ragged takes cosmologies without gamma growth")
         g, geo, _ = _geometry.get_geometry(probes, _geometry.ell_host(ell), n_limber, device)
         params[i] = cosmo.param_tensor(device)[0]
         out = torch.empty(_geometry.n_cls_of(g), g.n_ell, dtype=torch.float64, device=device)

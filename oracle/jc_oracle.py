@@ -73,6 +73,9 @@ class Cosmo:
     # "eisenhu", transfer.py:10): the sigma_8 normalisation and the sigma^2(R)
     # table cached here depend on it
     transfer: str = "eisenhu_osc"
+    # growth-rate index (core.py:13, 52-54): None -> growth ODE, else
+    # f = Omega_m(a)^gamma (background.py:515-582)
+    gamma: object = None
 
     @classmethod
     def from_vector(cls, v):
@@ -253,8 +256,17 @@ def radial_comoving_distance(c, a):
 
 
 def growth_table(c, log10_amin=-3, steps=128):
-    """background.py:443-487: RK4 of the growth ODE in a on logspace(-3, 0, 128)."""
+    """background.py:443-487: RK4 of the growth ODE in a on logspace(-3, 0, 128);
+    with c.gamma, background.py:515-552: RK4 in ln a of Omega_m(a)^gamma."""
     key = ("growth", log10_amin, steps)
+    if key not in c.cache and c.gamma is not None:
+        atab = _t(np.logspace(log10_amin, 0.0, steps))
+
+        def integrand(y, loga):
+            return Omega_m_a(c, torch.exp(loga)) ** c.gamma
+
+        gtab = torch.exp(odeint_rk4(integrand, torch.log(atab[0]), torch.log(atab)))
+        c.cache[key] = (atab, gtab / gtab[-1])
     if key not in c.cache:
         atab = _t(np.logspace(log10_amin, 0.0, steps))
 
@@ -285,7 +297,10 @@ def growth_factor(c, a):
 
 
 def growth_rate(c, a):
-    """background.py:401-440, 491-512: interp(a, atab, ftab) of the ODE growth, no clip."""
+    """background.py:401-440, 491-512: interp(a, atab, ftab) of the ODE growth, no clip;
+    with c.gamma, Omega_m(a)^gamma (background.py:555-582)."""
+    if c.gamma is not None:
+        return Omega_m_a(c, torch.atleast_1d(_t(a) if not isinstance(a, torch.Tensor) else a)) ** c.gamma
     growth_table(c)
     atab, ftab = c.cache[("growth_rate", -3, 128)]
     a = torch.atleast_1d(_t(a) if not isinstance(a, torch.Tensor) else a)

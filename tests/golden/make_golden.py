@@ -32,6 +32,8 @@ power2.npz      the non-default operator points: Eisenstein_Hu type "eisenhu"
 cl_physics.npz  angular_cl, 2 WeakLensing + 1 NumberCounts bins, with
                 nonlinear_fn = halofit(smith2003), linear_matter_power, and
                 transfer_fn = Eisenstein_Hu(type="eisenhu")
+gamma.npz       growth_factor / growth_rate and angular_cl (the cl_physics probes)
+                of Cosmologies with a growth-rate index gamma (background.py:515-582)
 background2.npz transverse / angular diameter distances (Omega_k = 0, > 0, < 0),
                 a_of_chi, growth_rate                     (background.py:245-368, 401-512)
 cov_like.npz    gaussian_cl_covariance_and_mean + gaussian_log_likelihood
@@ -77,9 +79,24 @@ def _setup(reference):
     return jax_cosmo
 
 
-def _cosmo(jc, row):
+def _cosmo(jc, row, gamma=None):
     names = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
-    return jc.Cosmology(**{n: float(v) for n, v in zip(names, row)})
+    return jc.Cosmology(**{n: float(v) for n, v in zip(names, row)}, gamma=gamma)
+
+
+# gamma values of the gamma-growth fixture, one per cosmology in COSMOS[[0, 2]]
+GAMMAS = (0.55, 0.62)
+
+
+def make_gamma_background(jc):
+    a_q = np.concatenate([np.logspace(-2.5, 0, 41), np.array([0.2, 0.5, 0.999, 1.0])])
+    rows = COSMOS[[0, 2]]
+    D, f = [], []
+    for row, gm in zip(rows, GAMMAS):
+        c = _cosmo(jc, row, gm)
+        D.append(jc.background.growth_factor(c, a_q))
+        f.append(jc.background.growth_rate(c, a_q))
+    return {"cosmos": rows, "gammas": np.array(GAMMAS), "a_q": a_q, "D": np.array(D), "f": np.array(f)}
 
 
 def make_background(jc):
@@ -322,6 +339,8 @@ def nz_catalog():
 def _cl_worker(args):
     reference, kind, row, ell, variant = args
     jc = _setup(reference)
+    if isinstance(variant, float):  # a gamma of the Cosmology, default operator points
+        return jc.angular_cl.angular_cl(_cosmo(jc, row, variant), np.array([ell]), _probes(jc, kind))[:, 0]
     c = _cosmo(jc, row)
     if variant is None:
         return jc.angular_cl.angular_cl(c, np.array([ell]), _probes(jc, kind))[:, 0]
@@ -433,7 +452,7 @@ def main():
         save("cov_like", make_cov_like(jc))
     if want("sparse"):
         save("sparse", make_sparse(jc))
-    if any(want(n) for n in ("cl_wl2", "cl_mixed", "cl_ia", "cl_nz", "cl_delta", "cl_physics")):
+    if any(want(n) for n in ("cl_wl2", "cl_mixed", "cl_ia", "cl_nz", "cl_delta", "cl_physics", "gamma")):
         import multiprocessing as mp
 
         with mp.get_context("spawn").Pool(args.procs) as pool:
@@ -457,6 +476,14 @@ def main():
             if want("cl_delta"):
                 ell = np.logspace(1, np.log10(5000.0), 10)
                 save("cl_delta", make_cl(args.reference, pool, "delta", COSMOS[[0, 2]], ell))
+            if want("gamma"):
+                d = make_gamma_background(jc)
+                ell = np.logspace(1, np.log10(5000.0), 10)
+                cls = []
+                for row, gm in zip(COSMOS[[0, 2]], GAMMAS):
+                    cls.append(make_cl(args.reference, pool, "physics", [row], ell, gm)["cl"][0])
+                d["ell"], d["cl"] = ell, np.array(cls)
+                save("gamma", d)
             if want("cl_physics"):
                 ell = np.logspace(1, np.log10(5000.0), 10)
                 d = {}

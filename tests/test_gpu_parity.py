@@ -526,3 +526,37 @@ def test_angular_cl_operator_points_vs_golden(golden, variant):
         err = max(float((J[..., d].cpu() - J_o[..., d]).abs().max() / J_o[..., d].abs().max().clamp_min(1e-300))
                   for d in range(8))
         assert err < tol, (prec, err)
+
+
+def test_gamma_growth_vs_golden(golden):
+    """Cosmology(gamma=...) (background.py:515-582): growth_factor / growth_rate
+    points and angular_cl (FP64 and fp32c, batched) against the unmodified
+    reference; the Jacobian (gamma held fixed) against the oracle's autograd."""
+    g = golden("gamma")
+    rows, gms = g["cosmos"], g["gammas"]
+    cb = jc.Cosmology(**{n: torch.tensor(rows[:, i]) for i, n in enumerate(NAMES)}, gamma=torch.tensor(gms))
+    assert rel(jc.background.growth_factor(cb, g["a_q"]), g["D"]) < RT64
+    assert rel(jc.background.growth_rate(cb, g["a_q"]), g["f"]) < RT64
+    cl = jc.cl.angular_cl(cb, g["ell"], _physics_probes())
+    cl32 = jc.cl.angular_cl(cb, g["ell"], _physics_probes(), precision="fp32c")
+    for i in range(len(rows)):
+        assert rel(cl[i], g["cl"][i]) < RT64
+        assert rel(cl32[i], g["cl"][i]) < RT32
+    ell = g["ell"][::3]
+    pa, pb = O.Smail(1, 2, 0.5, 10.0, 10), O.Smail(1, 2, 1.0, 10.0, 10)
+    oprobes = [O.Probe("wl", [pa, pb], sigma_e=0.26), O.Probe("nc", [pb], bias=1.2)]
+    row, gm = list(rows[1]), float(gms[1])
+
+    def f(v):
+        c = O.Cosmo.from_vector(v)
+        c.gamma = gm
+        return O.angular_cl(c, ell, oprobes, n_limber=128)
+
+    J_o = torch.autograd.functional.jacobian(f, torch.tensor(row, dtype=torch.float64), strategy="forward-mode",
+                                             vectorize=True)
+    c1 = jc.Cosmology(**{n: float(v) for n, v in zip(NAMES, row)}, gamma=gm)
+    for prec, tol in (("fp64", 1e-8), ("fp32c", 1e-4)):
+        _, J = jc.autodiff.angular_cl_jacobian(c1, ell, _physics_probes(), 128, prec)
+        err = max(float((J[..., d].cpu() - J_o[..., d]).abs().max() / J_o[..., d].abs().max().clamp_min(1e-300))
+                  for d in range(8))
+        assert err < tol, (prec, err)

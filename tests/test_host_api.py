@@ -146,5 +146,9 @@ def test_unsupported_options_raise():
         jc.cl.physics_code(jc.transfer.Eisenstein_Hu, functools.partial(jc.power.halofit, prescription="x"))
     with pytest.raises(ValueError):
         jc.cl._precision_code("fp16")
-    with pytest.raises(NotImplementedError):
-        jc.Cosmology(0.25, 0.05, 0.7, 0.96, 0.8, 0.0, -1.0, 0.0, gamma=0.55).param_tensor("cpu")
+    # gamma growth: the parameter rows carry gamma as a 9th column and the
+    # descriptor's physics word the GROWTH_GAMMA bit
+    cg = jc.Cosmology(0.25, 0.05, 0.7, 0.96, 0.8, 0.0, -1.0, 0.0, gamma=0.55)
+    pg = cg.param_tensor("cpu")
+    assert pg.shape == (1, 9) and float(pg[0, 8]) == 0.55
+    assert cg.physics_bits() == _lib.GROWTH_GAMMA and c.physics_bits() == 0

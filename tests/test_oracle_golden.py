@@ -233,3 +233,17 @@ def test_angular_cl_operator_points(golden, variant):
         ref = g["cl_" + "_".join(variant)][i]
         assert cl.shape == ref.shape
         assert rel(cl, ref) < 1e-11
+
+
+def test_gamma_growth(golden):
+    """Cosmology(gamma=...): growth_factor, growth_rate (background.py:515-582) and
+    angular_cl with that growth."""
+    g = golden("gamma")
+    a = torch.tensor(g["a_q"])
+    for i, (row, gm) in enumerate(zip(g["cosmos"], g["gammas"])):
+        c = O.Cosmo.from_vector(row)
+        c.gamma = float(gm)
+        assert rel(O.growth_factor(c, a), g["D"][i]) < RTOL
+        assert rel(O.growth_rate(c, a), g["f"][i]) < RTOL
+        cl = O.angular_cl(c, g["ell"], physics_probes())
+        assert rel(cl, g["cl"][i]) < 1e-11
