@@ -324,6 +324,23 @@ def gpu_arm(args, rank, world, device):
     res["jacobian"]["fp32c"]["jac_max_err_vs_fp64"] = float(((j32 - j64).abs() / scale).max())
     res["jacobian"]["fp32c"]["jac_err_note"] = "max |J32 - J64| / max |J64| per (cosmology, parameter)"
     del j64, j32
+
+    # the non-default operator points on the same workload (fp32c), each with
+    # its error against the plain fp64 method of the same operator points
+    params_g = torch.cat([params, torch.full((B, 1), 0.55, dtype=torch.float64, device=device)], dim=1)
+    c64v = torch.empty_like(cl)
+    res["operator_points"] = {}
+    for name, phys in (("halofit_smith2003", _lib.PK_SMITH2003), ("linear_matter_power", _lib.PK_LINEAR),
+                       ("eisenhu_nowiggle", _lib.TF_NOWIGGLE), ("gamma_growth_0.55", _lib.GROWTH_GAMMA)):
+        pp = params_g if phys & _lib.GROWTH_GAMMA else params
+        tv, _ = timed(lambda pp=pp, phys=phys: angular_cl_device(pp, ell_np, probes, "fp32c", 512, out=cl,
+                                                                 physics=phys), args.steps, args.warmup)
+        angular_cl_device(pp, ell_np, probes, "fp64", 512, out=c64v, physics=phys)
+        angular_cl_device(pp, ell_np, probes, "fp32c", 512, out=cl, physics=phys)
+        res["operator_points"][name] = {
+            "ms_per_step": tv / args.steps, "cl_per_s": ncl_step / (tv / args.steps * 1e-3),
+            "fp32c_max_rel_err_vs_fp64": float(((cl - c64v).abs() / c64v.abs()).max()),
+        }
     return res
 
 
@@ -590,6 +607,7 @@ def main():
         "plain_fp64_single": res["plain_fp64_single"],
         "batched_over_plain_fp64_single": value / plain,
         "cl_grad": jac,
+        "operator_points": res["operator_points"],
         "loglike_grad_latency_ms": ({"p50": serve["p50_ms"], "p99": serve["p99_ms"]} if serve else None),
         "serving": serve,
         "fp32c_max_rel_err_vs_fp64": res["fp32c_max_rel_err_vs_fp64"],

@@ -348,7 +348,9 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
     chi_s[t] = chi_at(ct, c, a, unpack_seg(SC[n]));
     int ilo = 0, ihi = NKH - 1;
     double t1 = 0.0, t2 = 0.0;
-    if (FAST) {
+    if (model == JCG_PK_LINEAR) {
+      ihi = -1;  // linear_matter_power: the halofit moments are not used
+    } else if (FAST) {
       // exp only for y^2 in [Y2_TAYLOR, Y2_SKIP] (the split point only needs
       // to be consistent, so it is found in FP32); y^2 = kh^2 inv^2 with
       // inv^2 as a float pair for the FP32 terms
@@ -422,7 +424,7 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
       }
     } else {
       const double g2 = g_s[t] * g_s[t];
-      for (int i = lane; i < NKH; i += 32) {
+      for (int i = lane; i <= ihi_s[t]; i += 32) {
         const double y = c->kh[i] * inv;
         const double y2 = y * y;
         const double res = pk3[i] * exp(-y2) * g2 / TWO_PI2;

@@ -281,8 +281,7 @@ __host__ __device__ inline L32Layout l32_layout(int n_tr, int n_cls, int LT) {
 }
 
 // GEN: the non-default operator points (transfer type "eisenhu", smith2003,
-// linear_matter_power) are read from each item; only the MAXU = L32_MAXU
-// variant is built with GEN.
+// linear_matter_power) are read from each item.
 template <int MAXU, bool GEN>
 __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2))
     limber32_kernel(Batch bt, const ConstTables* __restrict__ c, int LT) {
@@ -455,11 +454,20 @@ void launch_limber(const Batch& b, const ConstTables* c, int lt, cudaStream_t st
     // units per thread: the split path needs one, otherwise lt x ceil(n_cls / 4)
     const int items = lt * ((b.max_cls + 3) / 4);
     const int need = items >= LB_THREADS ? (items + LB_THREADS - 1) / LB_THREADS : 1;
-    if (b.physics_or != 0) launch_limber32_t<L32_MAXU, true>(b, c, lt, st);
-    else if (need <= 1) launch_limber32_t<1>(b, c, lt, st);
-    else if (need <= 2) launch_limber32_t<2>(b, c, lt, st);
-    else if (need <= 3) launch_limber32_t<3>(b, c, lt, st);
-    else launch_limber32_t<L32_MAXU>(b, c, lt, st);
+    if (b.physics_or != 0) {
+      if (need <= 1) launch_limber32_t<1, true>(b, c, lt, st);
+      else if (need <= 2) launch_limber32_t<2, true>(b, c, lt, st);
+      else if (need <= 3) launch_limber32_t<3, true>(b, c, lt, st);
+      else launch_limber32_t<L32_MAXU, true>(b, c, lt, st);
+    } else if (need <= 1) {
+      launch_limber32_t<1>(b, c, lt, st);
+    } else if (need <= 2) {
+      launch_limber32_t<2>(b, c, lt, st);
+    } else if (need <= 3) {
+      launch_limber32_t<3>(b, c, lt, st);
+    } else {
+      launch_limber32_t<L32_MAXU>(b, c, lt, st);
+    }
     return;
   }
   const size_t smem = limber_smem_bytes(false, b.max_cls, lt);
