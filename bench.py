@@ -53,22 +53,23 @@ BOX = {
 }
 ORDER = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
 # Per-cosmology figures of the fp32c step's kernels on this workload (na = 513
-# Limber nodes, 5 WL tracers, 100 ell), from one ncu capture at 512
-# cosmologies (profiles/fp32c_step_kernels_b512.md), divided by 512:
+# Limber nodes, 5 WL tracers, 100 ell), from ncu captures at 512 cosmologies
+# (profiles/fp32c_step_kernels_b512.md; the Limber kernel's figures from the
+# capture of its T(k) table form in the same file), divided by 512:
 #   FP64 operations = DFMA x 2 + DADD + DMUL thread instructions (the
 #     cosmo_tables stage is cosmo_scalars_kernel + cosmo_tables_kernel);
 #   traffic = dram__bytes_read.sum + dram__bytes_write.sum;
 #   per Limber node (512 x 100 x 513 nodes): XU (MUFU) thread operations and
 #     warp instructions issued (sm__inst_executed) of limber32_kernel.
 FP64_OPS = {"cosmo_tables": 350_440, "halofit_rows": 83_620}
-TRAFFIC_PER_COSMO = {"cosmo_tables": 1_964, "halofit_rows": 44_141, "tracer_kernels": 9_679, "limber": 123_554}
-MUFU_PER_NODE = 31
-WARP_INSTR_PER_NODE = 9.279
+TRAFFIC_PER_COSMO = {"cosmo_tables": 1_964, "halofit_rows": 44_141, "tracer_kernels": 9_679, "limber": 121_380}
+MUFU_PER_NODE = 17.37
+WARP_INSTR_PER_NODE = 8.196
 # algorithmic bytes per cosmology: what each kernel must read and write once
-#   cosmo_tables: 8 parameters in, the CosmoTab record out (53,952 B)
+#   cosmo_tables: 8 parameters in, the CosmoTab record out (55,040 B)
 #   halofit_rows: the CosmoTab record in, FP64 + FP32 rows out (513 x (24 x 8 + 16 x 4))
 #   limber: FP32 rows (16 x 4) + u (8) + 5 radial kernels (5 x 8) per node in, 15 x 100 C_ell out
-ALG_BYTES = {"cosmo_tables": 64 + 53_952, "halofit_rows": 53_952 + 513 * (24 * 8 + 16 * 4),
+ALG_BYTES = {"cosmo_tables": 64 + 55_040, "halofit_rows": 55_040 + 513 * (24 * 8 + 16 * 4),
              "limber": 513 * (16 * 4 + 8) + 5 * 513 * 8 + 15 * N_ELL * 8}
 KERNEL_NAMES = {"cosmo_tables": "cosmo_scalars_kernel + cosmo_tables_kernel",
                 "halofit_rows": "halofit_rows_kernel<fp32c>",

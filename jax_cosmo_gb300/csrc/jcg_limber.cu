@@ -53,17 +53,10 @@ __device__ void make_eh32(const double* s, EH32* e) {
   e->nw = s[S_TFNW] != 0.0;
 }
 
-// Eisenstein-Hu (transfer.py:88-153, either type) x primordial x halofit (power.py:246-260)
-// at one node in FP32.  kh = l + 1/2, lg2kh = log2(kh), invkh = 1 / kh.
-// lin: the linear power (nonlinear_fn = linear_matter_power).  GEN = false:
-// the default operator points only (eisenhu_osc, takahashi2012; lin, e.nw and
-// mu_n are not read), so that instantiation keeps its registers.
+// Eisenstein-Hu T(k) in FP32 (transfer.py:88-153, either type) at k, lk =
+// log2 k, invk = 1 / k.
 template <bool GEN>
-__device__ __forceinline__ float node32(const EH32& e, const float* r, float kh, float lg2kh,
-                                        float invkh, bool lin) {
-  const float k = kh * r[F_INVCHI];
-  const float lk = lg2kh + r[F_LG2INVCHI];
-  const float invk = invkh * r[F_CHIC];
+__device__ __forceinline__ float eh32_T(const EH32& e, float k, float lk, float invk) {
   float T;
   if (GEN && e.nw) {
     // type "eisenhu" (transfer.py:88-105)
@@ -100,8 +93,20 @@ __device__ __forceinline__ float node32(const EH32& e, const float* r, float kh,
     const float Tbar = (Tn * rcpf(1.f + x52 * x52) + e.alpha_b * rcpf(1.f + bb * bb * bb) * silk) * sinc;
     T = e.fb * Tbar + e.fc * Tc;
   }
+  return T;
+}
+
+// primordial x transfer x halofit (power.py:42-53, 246-260) at one node in
+// FP32 from tk = T(k)^2 k^(n_s + 3): k = kh / max(chi, 1), lk = log2 k,
+// invk = 1 / k.
+// lin: the linear power (nonlinear_fn = linear_matter_power).  GEN = false:
+// the default operator points only (takahashi2012; lin and mu_n are not
+// read), so that instantiation keeps its registers.
+template <bool GEN>
+__device__ __forceinline__ float pk32_T(const EH32& e, const float* r, float k, float lk, float invk, float tk,
+                                        bool lin) {
   // linear and halofit power
-  const float d2l = ex2f(e.ns3 * lk) * (T * T) * r[F_D2FAC];
+  const float d2l = tk * r[F_D2FAC];
   if (GEN && lin) return TWO_PI2_F * (invk * invk * invk) * d2l;
   const float y = k * r[F_INVKNL];
   const float ly = lk - r[F_LG2KNL];
@@ -117,6 +122,34 @@ __device__ __forceinline__ float node32(const EH32& e, const float* r, float kh,
       r[F_AN] * yf1 * rcpf(1.f + r[F_BN] * yf2 + ycg) * y2 * rcpf((GEN ? fmaf(r[F_MUN], y, y2) : y2) + r[F_NUN]);
   return TWO_PI2_F * (invk * invk * invk) * (d2q + d2h);
 }
+
+// Both at one node: kh = l + 1/2, lg2kh = log2(kh), invkh = 1 / kh.
+template <bool GEN>
+__device__ __forceinline__ float node32(const EH32& e, const float* r, float kh, float lg2kh,
+                                        float invkh, bool lin) {
+  const float k = kh * r[F_INVCHI];
+  const float lk = lg2kh + r[F_LG2INVCHI];
+  const float invk = invkh * r[F_CHIC];
+  const float T = eh32_T<GEN>(e, k, lk, invk);
+  return pk32_T<GEN>(e, r, k, lk, invk, ex2f(e.ns3 * lk) * (T * T), lin);
+}
+
+// T(k)^2 k^(n_s + 3) table of the fp32c Limber kernel: NTT nodes uniform in
+// log2 k over the range of one CTA's nodes, values by 4-point Lagrange
+// interpolation (error O(h^4): about 1e-7 relative for the baryon wiggles at
+// this spacing, below the FP32 evaluation's own error)
+constexpr int NTT = 2048;
+__device__ __forceinline__ float tt_interp(const float* tab, float lk, float lk0, float ih) {
+  const float u = (lk - lk0) * ih;
+  int i = __float2int_rd(u);
+  i = max(1, min(i, NTT - 3));
+  const float t = u - (float)i;
+  const float tm1 = t - 1.f, tm2 = t - 2.f, tp1 = t + 1.f;
+  const float a = tm1 * tm2, b = tp1 * t;
+  return (-1.f / 6.f) * (t * a) * tab[i - 1] + 0.5f * (tp1 * a) * tab[i] - 0.5f * (b * tm2) * tab[i + 1] +
+         (1.f / 6.f) * (b * tm1) * tab[i + 2];
+}
+
 
 // ---------------------------------------------------------------- kernel ---
 // MAXO: accumulators per thread, >= ceil(LT * n_cls / LB_THREADS).
@@ -253,7 +286,7 @@ __global__ void __launch_bounds__(LB_THREADS)
 constexpr int L32_MAXU = 5;  // ceil(LB_MAXLT * ceil(MAXPAIR / 4) / LB_THREADS)
 
 struct L32Layout {
-  size_t e32, kh32, rows, ks, us, ms, pt, red, total;
+  size_t e32, kh32, rows, ks, us, ms, pt, red, tab, total;
 };
 __host__ __device__ inline L32Layout l32_layout(int n_tr, int n_cls, int LT) {
   L32Layout L;
@@ -276,6 +309,8 @@ __host__ __device__ inline L32Layout l32_layout(int n_tr, int n_cls, int LT) {
   o = (o + 15) & ~(size_t)15;
   L.red = o;
   o += (size_t)LB_THREADS * 4 * 8;
+  L.tab = o;
+  o += (size_t)(NTT + 16) * 4;
   L.total = o;
   return L;
 }
@@ -321,6 +356,40 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
   }
   __syncthreads();
   if (tid == 0) make_eh32(s, e32);
+  // T^2 k^(n_s+3) table over this CTA's log2 k range: lg2(l + 1/2) of its ell plus the
+  // range of log2(1 / max(chi, 1)) over the item's nodes
+  float* Ttab = reinterpret_cast<float*>(smem_raw + L.tab);
+  float* wmm = Ttab + NTT;  // [8] warp minima, [8] warp maxima
+  {
+    float mn = 3.0e38f, mx = -3.0e38f;
+    for (int n = tid; n < na; n += LB_THREADS) {
+      const float v = it.rows32[(size_t)n * NROW32 + F_LG2INVCHI];
+      mn = fminf(mn, v);
+      mx = fmaxf(mx, v);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      mn = fminf(mn, __shfl_xor_sync(0xffffffffu, mn, o));
+      mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    }
+    if ((tid & 31) == 0) wmm[tid >> 5] = mn, wmm[8 + (tid >> 5)] = mx;
+  }
+  __syncthreads();
+  float tlk0, tih;
+  {
+    float mn = wmm[0], mx = wmm[8];
+#pragma unroll
+    for (int w = 1; w < LB_THREADS / 32; ++w) mn = fminf(mn, wmm[w]), mx = fmaxf(mx, wmm[8 + w]);
+    const float lo = kh4[0].y + mn - 0.01f, hi = kh4[lt - 1].y + mx + 0.01f;
+    const float h = (hi - lo) * (1.f / (float)(NTT - 3));
+    tlk0 = lo - h;  // node 0; nodes 1 .. NTT - 2 span [lo, hi]
+    tih = 1.f / h;
+    for (int j = tid; j < NTT; j += LB_THREADS) {
+      const float lkj = tlk0 + (float)j * h;
+      const float T = eh32_T<GEN>(*e32, ex2f(lkj), lkj, ex2f(-lkj));
+      Ttab[j] = ex2f(e32->ns3 * lkj) * (T * T);
+    }
+  }
   // (t, l) and (t, p) from flat indices without integer division: q < 32 * 136,
   // so (q + 1/2) / n in float is off by far less than 1 / (2 n) of an integer
   const float inv_lt = 1.f / (float)lt, inv_ncp = 1.f / (float)ncp;
@@ -352,7 +421,11 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
     for (int q = tid; q < tc * lt; q += LB_THREADS) {
       const int t = __float2int_rz(((float)q + 0.5f) * inv_lt), l = q - t * lt;
       const float4 kk = kh4[l];
-      Pt[t * LT + l] = node32<GEN>(*e32, rowsS + t * NROW32, kk.x, kk.y, kk.z, lin);
+      const float* r = rowsS + t * NROW32;
+      const float k = kk.x * r[F_INVCHI];
+      const float lk = kk.y + r[F_LG2INVCHI];
+      const float invk = kk.z * r[F_CHIC];
+      Pt[t * LT + l] = pk32_T<GEN>(*e32, r, k, lk, invk, tt_interp(Ttab, lk, tlk0, tih), lin);
     }
     __syncthreads();
 #pragma unroll
