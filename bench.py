@@ -54,15 +54,15 @@ BOX = {
 ORDER = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
 # Per-cosmology figures of the fp32c step's kernels on this workload (na = 513
 # Limber nodes, 5 WL tracers, 100 ell), from ncu captures at 512 cosmologies
-# (profiles/fp32c_step_kernels_b512.md; the Limber kernel's figures from the
-# capture of its T(k) table form in the same file), divided by 512:
+# (profiles/fp32c_step_kernels_b512.md; the Limber kernel's and the table
+# kernels' figures from the later captures in the same file), divided by 512:
 #   FP64 operations = DFMA x 2 + DADD + DMUL thread instructions (the
 #     cosmo_tables stage is cosmo_scalars_kernel + cosmo_tables_kernel);
 #   traffic = dram__bytes_read.sum + dram__bytes_write.sum;
 #   per Limber node (512 x 100 x 513 nodes): XU (MUFU) thread operations and
 #     warp instructions issued (sm__inst_executed) of limber32_kernel.
-FP64_OPS = {"cosmo_tables": 350_440, "halofit_rows": 83_620}
-TRAFFIC_PER_COSMO = {"cosmo_tables": 1_964, "halofit_rows": 44_141, "tracer_kernels": 9_679, "limber": 121_380}
+FP64_OPS = {"cosmo_tables": 234_482, "halofit_rows": 83_620}
+TRAFFIC_PER_COSMO = {"cosmo_tables": 2_108, "halofit_rows": 44_141, "tracer_kernels": 9_679, "limber": 121_380}
 MUFU_PER_NODE = 17.37
 WARP_INSTR_PER_NODE = 8.196
 # algorithmic bytes per cosmology: what each kernel must read and write once

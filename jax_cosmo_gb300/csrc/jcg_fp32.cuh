@@ -114,4 +114,18 @@ __device__ __forceinline__ FF ff_of(double v) {
 }
 __device__ __forceinline__ double ff_to_double(FF x) { return (double)x.hi + (double)x.lo; }
 
+// (ah, al) += a b with a, b float pairs: Dekker's product by FMA and Knuth's
+// two-sum of the high parts; the product's low part and the two-sum's error
+// gather in al (about 2^-46 relative per term; the caller forms ah + al)
+__device__ __forceinline__ void ff_acc_prod(float& ah, float& al, float2 a, float2 b) {
+  const float p = a.x * b.x;
+  float pe = fmaf(a.x, b.x, -p);
+  pe = fmaf(a.x, b.y, pe);
+  pe = fmaf(a.y, b.x, pe);
+  const float s = ah + p;
+  const float bb = s - ah;
+  al += ((ah - (s - bb)) + (p - bb)) + pe;
+  ah = s;
+}
+
 }  // namespace jcg

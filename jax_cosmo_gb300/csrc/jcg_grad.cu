@@ -453,27 +453,30 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
   if (F32T) {
     // value FP64, tangents FP32 (pq tangents rounded once into a float copy)
     float* pqf = reinterpret_cast<float*>(fn);  // fn / fm are free here
-    double* pqs = fm;
+    float2* pqs = reinterpret_cast<float2*>(fm);
     for (int e = t; e < NDIR * NKH; e += blockDim.x) {
       const int d = e / NKH, i = e % NKH;
       pqf[i * NDIR + d] = (float)(c->simpson_kh[i] * pq[(1 + d) * NKH + i]);
     }
-    for (int i = t; i < NKH; i += blockDim.x) pqs[i] = pq[i] * c->simpson_kh[i];
+    for (int i = t; i < NKH; i += blockDim.x) {
+      const FF f = ff_of(pq[i] * c->simpson_kh[i]);
+      pqs[i] = make_float2(f.hi, f.lo);
+    }
     __syncthreads();
     for (int j = t; j < NRT; j += blockDim.x) {
-      double acc = 0.0;
+      // value in float-pair arithmetic (as cosmo_tables' fp32c sums), tangents FP32
+      float ah = 0.f, al = 0.f;
       float ad[NDIR];
 #pragma unroll
       for (int d = 0; d < NDIR; ++d) ad[d] = 0.f;
       for (int i = 0; i < NKH; ++i) {
-        const double e = c->E[i * NRT + j];
-        acc = fma(pqs[i], e, acc);
-        const float f = (float)e;
+        const float2 e = c->Eff[i * NRT + j];
+        ff_acc_prod(ah, al, pqs[i], e);
         const float* q0 = pqf + i * NDIR;
 #pragma unroll
-        for (int d = 0; d < NDIR; ++d) ad[d] = fmaf(q0[d], f, ad[d]);
+        for (int d = 0; d < NDIR; ++d) ad[d] = fmaf(q0[d], e.x, ad[d]);
       }
-      out->sigv[j] = acc;
+      out->sigv[j] = (double)ah + (double)al;
 #pragma unroll
       for (int d = 0; d < NDIR; ++d) out->sigd[d][j] = (double)ad[d];
     }

@@ -56,6 +56,7 @@ struct ConstTables {
   double simpson_kh[NKH];  // Simpson weights (1,4,2,...,4,1) * dx/3 on the ln k grid
   double romb_logk[NROMB]; // romb abscissae in evaluation order (scipy/integrate.py:129-146)
   double E[NKH * NRT];     // exp(-(k_i r_j)^2), i-major: power.py:99-109
+  float2 Eff[NKH * NRT];   // the same as float pairs (hi, lo) (fp32c sigma^2(R) sums)
   double kpw[NTAYLOR][NKH];  // simpson_kh[i] * kh[i]^(2(m+1)): the Taylor prefix sums' weights
   double romb_w[NROMB];      // romb's Richardson combination as weights on romb_logk's values
   // cosmology-independent factors of the table kernel's right-hand sides

@@ -145,7 +145,10 @@ __global__ void const_init_kernel(ConstTables* c) {
     const double lk = np_linspace(kLogKMin, kLogKMax, NKH - 1, i);
     const double lr = np_linspace(kLogKMin, kLogRMax, NRT - 1, j);
     const double y = exp(lk) * exp(lr);
-    c->E[q] = exp(-(y * y));
+    const double e = exp(-(y * y));
+    c->E[q] = e;
+    const float hi = (float)e;
+    c->Eff[q] = make_float2(hi, (float)(e - (double)hi));
   }
 }
 
@@ -421,10 +424,28 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   for (int i = t; i < NKH; i += blockDim.x) pq[i] = c->simpson_kh[i] * (pk3[i] / (2.0 * (PI * PI)));
   __syncthreads();
   CosmoTab* out = it.ctab;
-  for (int j = t; j < NRT; j += blockDim.x) {
-    double acc = 0.0;
-    for (int i = 0; i < NKH; ++i) acc = fma(pq[i], c->E[i * NRT + j], acc);
-    out->sig[j] = acc;
+  if (it.precision == JCG_FP32C) {
+    // fp32c: the same sums in float-pair arithmetic (about 1e-13 relative, all
+    // terms positive): the FP32 pipe instead of the 1/64-rate FP64 one; the
+    // halofit root find on this table then takes the same nodes as with
+    // float64 sums except within ~1e-13 of a decision boundary
+    for (int i = t; i < NKH; i += blockDim.x) {  // wpp is free until the Taylor tables below
+      const FF f = ff_of(pq[i]);
+      wpp[i] = make_float2(f.hi, f.lo);
+    }
+    __syncthreads();
+    for (int j = t; j < NRT; j += blockDim.x) {
+      float ah = 0.f, al = 0.f;
+      for (int i = 0; i < NKH; ++i) ff_acc_prod(ah, al, wpp[i], c->Eff[i * NRT + j]);
+      out->sig[j] = (double)ah + (double)al;
+    }
+    __syncthreads();
+  } else {
+    for (int j = t; j < NRT; j += blockDim.x) {
+      double acc = 0.0;
+      for (int i = 0; i < NKH; ++i) acc = fma(pq[i], c->E[i * NRT + j], acc);
+      out->sig[j] = acc;
+    }
   }
   for (int i = t; i < NSCAL; i += blockDim.x) out->s[i] = s[i];
   for (int i = t; i < NCHI; i += blockDim.x) {
