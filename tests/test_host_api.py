@@ -125,6 +125,15 @@ def test_physics_codes():
     assert jc.cl.physics_code(nw, jc.power.linear_matter_power) == _lib.TF_NOWIGGLE | _lib.PK_LINEAR
     g = _geometry.describe([jc.probes.WeakLensing([jc.redshift.smail_nz(1.0, 2.0, 0.5)])], 4, physics=0x11)
     assert g.physics == 0x11
+    # the library validates the physics word (host-side, no GPU needed)
+    sz = ctypes.c_size_t()
+    lib = _lib.load()
+    for ok in (0, _lib.PK_SMITH2003, _lib.PK_LINEAR | _lib.TF_NOWIGGLE, _lib.GROWTH_GAMMA | _lib.PK_SMITH2003):
+        g.physics = ok
+        assert lib.jcg_geometry_size(ctypes.byref(g), ctypes.byref(sz)) == 0
+    for bad in (3, 0x40, 0x100):
+        g.physics = bad
+        assert lib.jcg_geometry_size(ctypes.byref(g), ctypes.byref(sz)) == _lib.ERR_UNSUPPORTED
 
 
 def test_smail_nz_host_evaluation_matches_oracle():
