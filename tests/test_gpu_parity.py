@@ -189,7 +189,7 @@ C2_SPEC = [("wl", C2_BINS, {"sigma_e": 0.26}), ("nc", C2_BINS, {"bias": 1.2})]
 @pytest.mark.parametrize(
     "spec,ell,n_limber",
     [
-        (C1_SPEC, np.logspace(1, np.log10(3000), 50), 256),  # BASELINE config 1: N = 256, zmax = 4
+        (C1_SPEC, np.logspace(1, np.log10(3000), 50), 256),  # 2 WL bins, N = 256, zmax = 4
         (C2_SPEC, np.logspace(1, np.log10(5000), 24), 512),  # config 2 tracers, 55 spectra
         ([("wl", [(1.0, 2.0, 0.7, 3.0, 5)], {"sigma_e": 0.3, "m": 0.02}),
           ("nc", [(2.0, 1.5, 0.4, 2.5, 3), (1.0, 2.0, 0.9, 5.0, 4)], {"bias": 0.9})],
