@@ -4,7 +4,8 @@ CPU float64 restatement of jax_cosmo's angular-power-spectrum path, written with
 torch on the CPU so that autograd gives the gradient oracle (``jax.grad`` of the
 reference is not available in this environment).  Only ``tests/``,
 ``__graft_entry__.smoke()`` and ``bench.py``'s CPU-baseline / reference legs may
-import this module, and only as the checker or the timed CPU baseline.
+import this module, and only to check results against it or as the timed CPU
+baseline.
 
 Every function follows the reference file and line it names (paths relative to
 the jax_cosmo project root).  It reproduces the reference's numerical quirks:
