@@ -233,6 +233,13 @@ int jcg_jacobian_workspace_size(const jcg_geometry* g, int n_cosmo, int precisio
 int jcg_angular_cl_jacobian(const jcg_geometry* g, const void* geo_dev, const double* params_dev,
                             int n_cosmo, int precision, double* cl_dev, double* jac_dev, void* workspace,
                             size_t workspace_bytes, cudaStream_t stream);
+/* The same with tangent direction gamma_dir (0..7) carrying the derivative
+ * with respect to gamma (JCG_GROWTH_GAMMA, background.py:515-582) instead of
+ * that parameter's: jac_dev[...][gamma_dir] = dC_ij(l)/dgamma, the other 7
+ * columns as above.  gamma_dir = -1 is jcg_angular_cl_jacobian. */
+int jcg_angular_cl_jacobian_dir(const jcg_geometry* g, const void* geo_dev, const double* params_dev,
+                                int n_cosmo, int precision, int gamma_dir, double* cl_dev, double* jac_dev,
+                                void* workspace, size_t workspace_bytes, cudaStream_t stream);
 
 /* ------------------------------------------------ ragged requests ------ */
 /* A list of requests, each with its own geometry (tracers, n(z), ell grid)

@@ -122,6 +122,7 @@ SIGNATURES = {
     "jcg_gaussian_loglike_dense": [_P, _P, _P, _I, _I, _I, _I, _P, _P, _P, _P, _SZ, _P],
     "jcg_jacobian_workspace_size": [_PG, _I, _I, _PSZ],
     "jcg_angular_cl_jacobian": [_PG, _P, _P, _I, _I, _P, _P, _P, _SZ, _P],
+    "jcg_angular_cl_jacobian_dir": [_PG, _P, _P, _I, _I, _I, _P, _P, _P, _SZ, _P],
     "jcg_requests_workspace_size": [_P, _I, _I, _I, _PSZ, _PSZ],
     "jcg_requests_run": [_P, _I, _I, _I, _P, _SZ, _P],
     "jcg_peak_fp64": [_P, _I, _I, _P],

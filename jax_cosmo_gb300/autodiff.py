@@ -32,12 +32,14 @@ PARAM_ORDER = ("Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"
 FISHER_PARAMS = ("Omega_c", "Omega_b", "h", "n_s", "sigma8", "w0", "wa")
 
 
-def jacobian_device(params, ell, probes, n_limber=512, precision="fp64", physics=0):
-    """(C_ell [B, n_cls, n_ell], dC/dtheta [B, n_cls, n_ell, 8]) for [B, 8] params on the device.
+def jacobian_device(params, ell, probes, n_limber=512, precision="fp64", physics=0, gamma_dir=-1):
+    """(C_ell [B, n_cls, n_ell], dC/dtheta [B, n_cls, n_ell, 8]) for [B, 8] params on the device
+    ([B, 9] with gamma last when ``physics`` has GROWTH_GAMMA).
 
     precision "fp64" (plain) or "fp32c" (float32 lensing kernels and Limber
     integrand with its reverse sweep, compensated a-sums; float64 tables);
-    physics: the code of ``angular_cl.physics_code``.
+    physics: the code of ``angular_cl.physics_code``; gamma_dir in 0..7: that
+    column of the Jacobian holds dC/dgamma instead of its parameter's.
     """
     from jax_cosmo_gb300.angular_cl import _precision_code
 
@@ -52,8 +54,9 @@ def jacobian_device(params, ell, probes, n_limber=512, precision="fp64", physics
     cl = torch.empty(B, n_cls, g.n_ell, dtype=torch.float64, device=device)
     jac = torch.empty(B, n_cls, g.n_ell, len(PARAM_ORDER), dtype=torch.float64, device=device)
     _lib.call(
-        "jcg_angular_cl_jacobian", ctypes.byref(g), _lib.ptr(geo), _lib.ptr(params.contiguous()), B, prec,
-        _lib.ptr(cl), _lib.ptr(jac), _lib.ptr(ws), ctypes.c_size_t(ws.numel()), _lib.stream_of(device),
+        "jcg_angular_cl_jacobian_dir", ctypes.byref(g), _lib.ptr(geo), _lib.ptr(params.contiguous()), B, prec,
+        int(gamma_dir), _lib.ptr(cl), _lib.ptr(jac), _lib.ptr(ws), ctypes.c_size_t(ws.numel()),
+        _lib.stream_of(device),
     )
     return cl, jac
 
@@ -71,29 +74,31 @@ class _AngularCl(torch.autograd.Function):
     def backward(ctx, gcl):
         (params,) = ctx.saved_tensors
         ell, probes, n_limber, precision, physics = ctx.meta
-        _, jac = jacobian_device(params.detach().contiguous(), ell, probes, n_limber, precision, physics)
-        gp = torch.einsum("bpl,bpld->bd", gcl.to(torch.float64), jac)
-        if params.shape[1] > gp.shape[1]:  # gamma: held fixed (checked in angular_cl_autograd)
-            gp = torch.cat([gp, gp.new_zeros(gp.shape[0], params.shape[1] - gp.shape[1])], dim=1)
+        p = params.detach().contiguous()
+        g64 = gcl.to(torch.float64)
+        _, jac = jacobian_device(p, ell, probes, n_limber, precision, physics)
+        gp = torch.einsum("bpl,bpld->bd", g64, jac)
+        if params.shape[1] > gp.shape[1]:
+            # gamma (the 9th column): its derivative from a second sweep with
+            # the gamma tangent in direction 0
+            _, jg = jacobian_device(p, ell, probes, n_limber, precision, physics, gamma_dir=0)
+            gp = torch.cat([gp, torch.einsum("bpl,bpl->b", g64, jg[..., 0])[:, None]], dim=1)
         return gp, None, None, None, None, None
 
 
 def angular_cl_autograd(cosmo, ell, probes, precision="fp64", n_limber=512, physics=0):
-    g = getattr(cosmo, "_gamma", None)
-    if isinstance(g, torch.Tensor) and g.requires_grad:
-        raise NotImplementedError("derivatives with respect to gamma are not provided (gamma is held fixed)")
     device = _lib.require_cuda()
     params = cosmo.param_tensor(device, differentiable=True)
     return _AngularCl.apply(params, ell, probes, precision, n_limber, physics)
 
 
 def angular_cl_jacobian(cosmo, ell, probes, n_limber=512, precision="fp64", transfer_fn=None, nonlinear_fn=None):
-    """(C_ell, dC_ell/dtheta) with theta = (Omega_c, Omega_b, h, n_s, sigma8, Omega_k, w0, wa)
-    (a gamma of the Cosmology is held fixed).
+    """(C_ell, dC_ell/dtheta) with theta = (Omega_c, Omega_b, h, n_s, sigma8, Omega_k, w0, wa),
+    and gamma last when the Cosmology has one (the pytree leaves of core.py:52-60).
 
-    Shapes [n_cls, n_ell] and [n_cls, n_ell, 8] (a leading batch axis for a
-    batched Cosmology).  precision "fp64" or "fp32c"; transfer_fn and
-    nonlinear_fn as in ``angular_cl`` (None: the defaults).
+    Shapes [n_cls, n_ell] and [n_cls, n_ell, 8] (9 with gamma; a leading
+    batch axis for a batched Cosmology).  precision "fp64" or "fp32c";
+    transfer_fn and nonlinear_fn as in ``angular_cl`` (None: the defaults).
     """
     from jax_cosmo_gb300 import power, transfer
     from jax_cosmo_gb300.angular_cl import physics_code
@@ -102,7 +107,11 @@ def angular_cl_jacobian(cosmo, ell, probes, n_limber=512, precision="fp64", tran
     physics |= cosmo.physics_bits()
     device = _lib.require_cuda()
     params = cosmo.param_tensor(device)
-    cl, jac = jacobian_device(params, _geometry.ell_host(ell), probes, n_limber, precision, physics)
+    ell_np = _geometry.ell_host(ell)
+    cl, jac = jacobian_device(params, ell_np, probes, n_limber, precision, physics)
+    if params.shape[1] > len(PARAM_ORDER):
+        _, jg = jacobian_device(params, ell_np, probes, n_limber, precision, physics, gamma_dir=0)
+        jac = torch.cat([jac, jg[..., :1]], dim=-1)
     if cosmo.batch_size is None:
         return cl[0], jac[0]
     return cl, jac

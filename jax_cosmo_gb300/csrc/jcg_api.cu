@@ -707,9 +707,18 @@ extern "C" int jcg_jacobian_workspace_size(const jcg_geometry* g, int n_cosmo, i
 extern "C" int jcg_angular_cl_jacobian(const jcg_geometry* g, const void* geo, const double* params,
                                        int n_cosmo, int precision, double* cl, double* jac, void* ws,
                                        size_t ws_bytes, cudaStream_t stream) {
+  return jcg_angular_cl_jacobian_dir(g, geo, params, n_cosmo, precision, -1, cl, jac, ws, ws_bytes, stream);
+}
+
+extern "C" int jcg_angular_cl_jacobian_dir(const jcg_geometry* g, const void* geo, const double* params,
+                                           int n_cosmo, int precision, int gamma_dir, double* cl, double* jac,
+                                           void* ws, size_t ws_bytes, cudaStream_t stream) {
   GeoHeader h;
   int rc = make_header(g, &h);
   if (rc) return rc;
+  if (gamma_dir < -1 || gamma_dir >= 8) return fail(JCG_ERR_ARG, "gamma_dir = %d", gamma_dir);
+  if (gamma_dir >= 0 && !growth_gamma(h.physics))
+    return fail(JCG_ERR_ARG, "gamma_dir = %d without JCG_GROWTH_GAMMA", gamma_dir);
   if (!geo || !params || !jac || !ws) return fail(JCG_ERR_ARG, "NULL pointer");
   if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
   if (precision != JCG_FP64 && precision != JCG_FP32C) return fail(JCG_ERR_ARG, "precision = %d", precision);
@@ -719,7 +728,7 @@ extern "C" int jcg_angular_cl_jacobian(const jcg_geometry* g, const void* geo, c
   if (((uintptr_t)ws) % 256 != 0) return fail(JCG_ERR_ARG, "workspace must be 256-byte aligned");
   ConstTables* c = nullptr;
   if ((rc = const_tables(&c))) return rc;
-  grad_run(static_cast<const GeoHeader*>(geo), h, params, n_cosmo, precision, cl, jac, ws, c, stream);
+  grad_run(static_cast<const GeoHeader*>(geo), h, params, n_cosmo, precision, cl, jac, ws, c, stream, gamma_dir);
   return cuda_check("angular_cl_jacobian");
 }
 

@@ -1570,7 +1570,7 @@ __global__ void __launch_bounds__(128) grad_scalars_kernel(GradBatch gb) {
   if (item >= gb.n_items) return;
   const GradItem gi = grad_item(gb, item);
   D1 p[8];
-  for (int i = 0; i < 8; ++i) p[i] = mk1(gi.params[i], i == dir ? 1.0 : 0.0);
+  for (int i = 0; i < 8; ++i) p[i] = mk1(gi.params[i], (i == dir && dir != gb.gamma_dir) ? 1.0 : 0.0);
   D1 s[NSCAL];
   cosmo_scalarsT(p, s, tf_nowiggle(gi.geo->physics));
   for (int i = 0; i < NSCAL; ++i) {
@@ -1586,7 +1586,7 @@ __global__ void __launch_bounds__(128) grad_scalars_warp_kernel(GradBatch gb) {
   if (item >= gb.n_items) return;
   const GradItem gi = grad_item(gb, item);
   D1 p[8];
-  for (int i = 0; i < 8; ++i) p[i] = mk1(gi.params[i], i == dir ? 1.0 : 0.0);
+  for (int i = 0; i < 8; ++i) p[i] = mk1(gi.params[i], (i == dir && dir != gb.gamma_dir) ? 1.0 : 0.0);
   D1 s[NSCAL];
   cosmo_scalars_warpT<D1>(p, s, lane, tf_nowiggle(gi.geo->physics));
   D1 v0 = mk1(0.0, 0.0), v1 = v0, v2 = v0;
@@ -1615,7 +1615,7 @@ __global__ void __launch_bounds__(32 * NDIR) grad_growth_gamma_kernel(GradBatch 
   __shared__ double fv[NGROW], fmv[NGROW], fd[NDIR][NGROW], fmd[NDIR][NGROW];
   const int d = threadIdx.x >> 5, lane = threadIdx.x & 31;
   TabD* tb = gi.tab;
-  const double gam = gi.params[8];
+  const D1 gam = mk1(gi.params[8], d == gb.gamma_dir ? 1.0 : 0.0);  // d/dgamma in that direction
   D1 sD[NSCAL];
   for (int i = 0; i < NSCAL; ++i) sD[i] = mk1(tb->sv[i], tb->sd[d][i]);
   const BgT<D1> bg = make_bgT(sD);
@@ -1623,7 +1623,7 @@ __global__ void __launch_bounds__(32 * NDIR) grad_growth_gamma_kernel(GradBatch 
     const double a = exp(lna);
     D1 om_m, om_de;
     omT(bg, a, log(a), om_m, om_de);
-    return xexp(gam * xlog(om_m));
+    return xexp(gam * xlog(om_m));  // Omega_m^gamma
   };
   for (int i = lane; i < NGROW; i += 32) {
     const double lna = c->grow_lna[i];
@@ -1768,9 +1768,10 @@ size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
 }
 
 void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, int precision,
-              double* cl, double* jac, void* ws, const ConstTables* c, cudaStream_t st) {
+              double* cl, double* jac, void* ws, const ConstTables* c, cudaStream_t st, int gamma_dir) {
   GradBatch gb;
   memset(&gb, 0, sizeof(gb));
+  gb.gamma_dir = gamma_dir;
   gb.n_items = n_cosmo;
   gb.precision = precision;
   gb.params = params;
@@ -1853,6 +1854,7 @@ cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void*
   size_t o = al256(sizeof(GradItem) * (size_t)n);
   GradBatch gb;
   memset(&gb, 0, sizeof(gb));
+  gb.gamma_dir = -1;
   for (int i = 0; i < n; ++i) {
     const GeoHeader& h = *r[i].h;
     const size_t per = (size_t)h.n_cls * h.n_ell;

@@ -137,6 +137,7 @@ struct GradBatch {
   double* gnode;  // fp32c, small batches: the table kernel's node values, per item GNODE_STRIDE doubles
   int na, n_tr, n_cls, n_ell, n_split;
   int physics_or;  // OR of the items' physics switches (selects kernel variants)
+  int gamma_dir;   // tangent direction carrying d/dgamma instead of its parameter's (-1: none)
 };
 
 // Small fp32c batches spread the table kernel's per-node evaluations over

@@ -110,6 +110,14 @@ def test_jacobian_and_request_validation_on_the_host():
     assert s64.value > 0 and s32.value > 0
     assert lib.jcg_angular_cl_jacobian(ctypes.byref(g), None, None, 1, _lib.FP64, None, None, None, 0,
                                        None) == _lib.ERR_ARG
+    # the gamma direction needs the gamma growth and a direction in 0..7
+    assert lib.jcg_angular_cl_jacobian_dir(ctypes.byref(g), None, None, 1, _lib.FP64, 0, None, None, None, 0,
+                                           None) == _lib.ERR_ARG
+    assert b"GROWTH_GAMMA" in lib.jcg_last_error_string()
+    g.physics = _lib.GROWTH_GAMMA
+    assert lib.jcg_angular_cl_jacobian_dir(ctypes.byref(g), None, None, 1, _lib.FP64, 8, None, None, None, 0,
+                                           None) == _lib.ERR_ARG
+    g.physics = 0
     lo, hi = ctypes.c_size_t(), ctypes.c_size_t()
     table = np.zeros(2, _lib.REQUEST_DTYPE)
     tp = ctypes.c_void_p(table.ctypes.data)

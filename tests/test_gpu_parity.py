@@ -548,15 +548,22 @@ def test_gamma_growth_vs_golden(golden):
     row, gm = list(rows[1]), float(gms[1])
 
     def f(v):
-        c = O.Cosmo.from_vector(v)
-        c.gamma = gm
+        c = O.Cosmo.from_vector(v[:8])
+        c.gamma = v[8]
         return O.angular_cl(c, ell, oprobes, n_limber=128)
 
-    J_o = torch.autograd.functional.jacobian(f, torch.tensor(row, dtype=torch.float64), strategy="forward-mode",
-                                             vectorize=True)
+    J_o = torch.autograd.functional.jacobian(f, torch.tensor(row + [gm], dtype=torch.float64),
+                                             strategy="forward-mode", vectorize=True)
     c1 = jc.Cosmology(**{n: float(v) for n, v in zip(NAMES, row)}, gamma=gm)
     for prec, tol in (("fp64", 1e-8), ("fp32c", 1e-4)):
         _, J = jc.autodiff.angular_cl_jacobian(c1, ell, _physics_probes(), 128, prec)
+        assert J.shape[-1] == 9  # the 8 parameters, then gamma
         err = max(float((J[..., d].cpu() - J_o[..., d]).abs().max() / J_o[..., d].abs().max().clamp_min(1e-300))
-                  for d in range(8))
+                  for d in range(9))
         assert err < tol, (prec, err)
+    # autograd through angular_cl with a gamma tensor that requires grad
+    gt = torch.tensor(gm, dtype=torch.float64, requires_grad=True)
+    c2 = jc.Cosmology(**{n: float(v) for n, v in zip(NAMES, row)}, gamma=gt)
+    jc.cl.angular_cl(c2, ell, _physics_probes(), n_limber=128).sum().backward()
+    ref = float(J_o[..., 8].sum())
+    assert abs(float(gt.grad) - ref) < 1e-8 * abs(ref)
