@@ -461,7 +461,7 @@ def measure_peaks(device):
     out64 = torch.empty(blocks * 256, dtype=torch.float64, device=device)
     out32 = torch.empty(blocks * 256, dtype=torch.float32, device=device)
     res = {}
-    for name, fn, buf, iters in (("fp64", "jcg_peak_fp64", out64, 200), ("mufu", "jcg_peak_mufu", out32, 4000)):
+    for name, fn, buf, iters in (("fp64", "jcg_calib_peak_fp64", out64, 200), ("mufu", "jcg_calib_peak_mufu", out32, 4000)):
         for _ in range(2):
             _lib.call(fn, _lib.ptr(buf), blocks, iters, st)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -95,7 +95,9 @@ extern "C" {
 /* Growth from the growth-rate index gamma, f = Omega_m(a)^gamma
  * (Cosmology(gamma=...), background.py:515-582) instead of the growth ODE.
  * With this bit the parameter arrays hold 9 values per cosmology, the 9th
- * gamma; the Jacobians stay with respect to the first 8 (gamma held fixed). */
+ * gamma.  The Jacobian columns are the first 8 parameters; dC/dgamma comes
+ * from jcg_angular_cl_jacobian_dir with gamma_dir in 0..7.  Ragged requests
+ * (jcg_requests_run, 8 parameters per request) reject this bit. */
 #define JCG_GROWTH_GAMMA 0x20
 #define JCG_PHYSICS_ALL (JCG_PK_MASK | JCG_TF_NOWIGGLE | JCG_GROWTH_GAMMA)
 
@@ -362,14 +364,6 @@ int jcg_sparse_to_dense(const double* sparse_dev, int n, int m, int ndiag, doubl
 /* sparse.dot(A, v) / sparse.dot(v, A) for sparse A (n, m, d) (sparse.py:71-137). */
 int jcg_sparse_dot_vec(const double* sparse_dev, int n, int m, int ndiag, const double* v_dev,
                        int transpose, double* out_dev, cudaStream_t stream);
-
-/* ------------------------------------------------------- calibration ---- */
-/* Not a reference interface: the FP64 FMA and MUFU (ex2) issue peaks of this
- * GPU, the denominators of the FP64-bound and SFU-bound rooflines the
- * benchmark reports.  blocks x 256 threads x iters x 128 operations; out_dev
- * holds blocks * 256 results. */
-int jcg_peak_fp64(double* out_dev, int blocks, int iters, cudaStream_t stream);
-int jcg_peak_mufu(float* out_dev, int blocks, int iters, cudaStream_t stream);
 
 #ifdef __cplusplus
 }

@@ -125,8 +125,8 @@ SIGNATURES = {
     "jcg_angular_cl_jacobian_dir": [_PG, _P, _P, _I, _I, _I, _P, _P, _P, _SZ, _P],
     "jcg_requests_workspace_size": [_P, _I, _I, _I, _PSZ, _PSZ],
     "jcg_requests_run": [_P, _I, _I, _I, _P, _SZ, _P],
-    "jcg_peak_fp64": [_P, _I, _I, _P],
-    "jcg_peak_mufu": [_P, _I, _I, _P],
+    "jcg_calib_peak_fp64": [_P, _I, _I, _P],
+    "jcg_calib_peak_mufu": [_P, _I, _I, _P],
     "jcg_sparse_inv": [_P, _I, _I, _P, _P],
     "jcg_sparse_slogdet": [_P, _I, _I, _P, _P, _P, _P],
     "jcg_sparse_to_dense": [_P, _I, _I, _I, _P, _P],

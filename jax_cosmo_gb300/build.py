@@ -56,7 +56,7 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
     nvcc = nvcc_path()
     os.makedirs(BUILD, exist_ok=True)
     headers = [os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith(".cuh")]
-    headers.append(os.path.join(INCLUDE, "jcg.h"))
+    headers += [os.path.join(INCLUDE, "jcg.h"), os.path.join(INCLUDE, "jcg_calib.h")]
     srcs = sources()
     objs = []
     jobs = []

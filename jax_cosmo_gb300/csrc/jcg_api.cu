@@ -394,9 +394,11 @@ int jcg_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t
 
 static int stage_prepare(const jcg_geometry* g, const void* geo_dev, const double* params,
                          int n_cosmo, int precision, void* ws, size_t ws_bytes, GeoHeader* h,
-                         ConstTables** c, bool need_geo) {
+                         ConstTables** c, bool need_geo, bool need_limber = false) {
   int rc = make_header(g, h);
   if (rc) return rc;
+  if (need_limber && h->custom_nodes)
+    return fail(JCG_ERR_ARG, "a geometry with caller redshift nodes has no Limber grid");
   if (need_geo && !geo_dev) return fail(JCG_ERR_ARG, "geometry buffer is NULL");
   const WsLayout L = ws_layout(h, n_cosmo, precision);
   if ((rc = check_common(params, n_cosmo, precision, ws, ws_bytes, L.total))) return rc;
@@ -441,7 +443,7 @@ int jcg_stage_limber(const jcg_geometry* g, const void* geo, const double* param
                      int precision, double* cl, void* ws, size_t ws_bytes, cudaStream_t stream) {
   GeoHeader h;
   ConstTables* c;
-  int rc = stage_prepare(g, geo, params, n_cosmo, precision, ws, ws_bytes, &h, &c, true);
+  int rc = stage_prepare(g, geo, params, n_cosmo, precision, ws, ws_bytes, &h, &c, true, true);
   if (rc) return rc;
   if (!cl) return fail(JCG_ERR_ARG, "cl output is NULL");
   const Batch b = make_batch(&h, geo, params, n_cosmo, precision, ws, cl);
@@ -453,7 +455,7 @@ int jcg_angular_cl(const jcg_geometry* g, const void* geo, const double* params,
                    int precision, double* cl, void* ws, size_t ws_bytes, cudaStream_t stream) {
   GeoHeader h;
   ConstTables* c;
-  int rc = stage_prepare(g, geo, params, n_cosmo, precision, ws, ws_bytes, &h, &c, true);
+  int rc = stage_prepare(g, geo, params, n_cosmo, precision, ws, ws_bytes, &h, &c, true, true);
   if (rc) return rc;
   if (!cl) return fail(JCG_ERR_ARG, "cl output is NULL");
   const Batch b = make_batch(&h, geo, params, n_cosmo, precision, ws, cl);
@@ -765,6 +767,11 @@ int plan_requests(const jcg_request* reqs, int n, int mode, int precision, ReqPl
       return fail(rc, "request %d: %s", i, why);
     }
     if (plan->hdr[i].custom_nodes) return fail(JCG_ERR_ARG, "request %d: geometry without a Limber grid", i);
+    // a request carries 8 parameters and its outputs 8 derivative columns:
+    // the gamma growth (a 9th parameter) is served by jcg_angular_cl(_jacobian_dir)
+    if (growth_gamma(plan->hdr[i].physics))
+      return fail(JCG_ERR_UNSUPPORTED, "request %d: JCG_GROWTH_GAMMA is not supported by ragged requests "
+                  "(8 parameters per request)", i);
     if (!r.geo_dev || !r.params_dev) return fail(JCG_ERR_ARG, "request %d: NULL geometry or params", i);
     if (mode == JCG_REQ_CL && !r.cl_dev) return fail(JCG_ERR_ARG, "request %d: cl is NULL", i);
     if (mode == JCG_REQ_JACOBIAN && !r.jac_dev) return fail(JCG_ERR_ARG, "request %d: jac is NULL", i);

@@ -4,6 +4,7 @@
 // runs 8 independent dependency chains, enough to fill the pipe; the results
 // are stored so that no chain is dead code.
 #include "jcg_internal.cuh"
+#include "../../include/jcg_calib.h"
 
 namespace jcg {
 
@@ -45,13 +46,13 @@ __global__ void __launch_bounds__(256) peak_mufu_kernel(float* out, int iters) {
 using namespace jcg;
 
 // blocks x 256 threads x iters x 16 x 8 operations (DFMA or MUFU ex2)
-extern "C" int jcg_peak_fp64(double* out_dev, int blocks, int iters, cudaStream_t stream) {
+extern "C" int jcg_calib_peak_fp64(double* out_dev, int blocks, int iters, cudaStream_t stream) {
   if (!out_dev || blocks < 1 || iters < 1) return JCG_ERR_ARG;
   peak_fp64_kernel<<<blocks, 256, 0, stream>>>(out_dev, iters, 0.999999999, 1e-12);
   return cudaGetLastError() == cudaSuccess ? JCG_OK : JCG_ERR_CUDA;
 }
 
-extern "C" int jcg_peak_mufu(float* out_dev, int blocks, int iters, cudaStream_t stream) {
+extern "C" int jcg_calib_peak_mufu(float* out_dev, int blocks, int iters, cudaStream_t stream) {
   if (!out_dev || blocks < 1 || iters < 1) return JCG_ERR_ARG;
   peak_mufu_kernel<<<blocks, 256, 0, stream>>>(out_dev, iters);
   return cudaGetLastError() == cudaSuccess ? JCG_OK : JCG_ERR_CUDA;

@@ -2,7 +2,7 @@
 
 Usage (in a container where the jax_cosmo source tree is present; no GPU needed)::
 
-    python tests/golden/make_golden.py --reference /root/reference [--procs 8]
+    python tests/golden/make_golden.py --reference <path to a jax_cosmo checkout> [--procs 8]
 
 The reference package runs on top of ``jax_standin`` (NumPy, float64).  Every
 fixture is written as a compressed ``.npz``; the committed files are what the

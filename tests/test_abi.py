@@ -12,7 +12,7 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 def _declared():
-    src = open(os.path.join(ROOT, "include", "jcg.h")).read()
+    src = "".join(open(os.path.join(ROOT, "include", h)).read() for h in ("jcg.h", "jcg_calib.h"))
     src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
     return sorted(set(re.findall(r"\b(jcg_[a-z0-9_]+)\s*\(", src)))
 
@@ -159,3 +159,40 @@ def test_jacobian_and_request_validation_on_the_host():
                                          ctypes.byref(hi))
     assert rc == _lib.ERR_ODD_N
     assert b"request 1" in lib.jcg_last_error_string()
+
+
+def test_ragged_requests_refuse_the_gamma_growth_on_the_host():
+    """A request carries 8 parameters and 8 derivative columns, so a geometry
+    with the gamma growth (a 9th parameter) is refused before any launch."""
+    import numpy as np
+
+    lib = _lib.load()
+    g = _geom()
+    g.physics = _lib.GROWTH_GAMMA
+    lo, hi = ctypes.c_size_t(), ctypes.c_size_t()
+    table = np.zeros(1, _lib.REQUEST_DTYPE)
+    fake = 4096  # never dereferenced: the check comes first
+    table[0] = (ctypes.addressof(g), fake, fake, fake, fake, fake, fake, fake)
+    tp = ctypes.c_void_p(table.ctypes.data)
+    for mode in (_lib.REQ_CL, _lib.REQ_JACOBIAN, _lib.REQ_LOGLIKE_GRAD):
+        rc = lib.jcg_requests_workspace_size(tp, 1, mode, _lib.FP32C, ctypes.byref(lo), ctypes.byref(hi))
+        assert rc == _lib.ERR_UNSUPPORTED
+        assert b"GROWTH_GAMMA" in lib.jcg_last_error_string()
+        assert lib.jcg_requests_run(tp, 1, mode, _lib.FP64, None, 0, None) == _lib.ERR_UNSUPPORTED
+
+
+def test_limber_entry_points_refuse_caller_redshift_nodes():
+    """A geometry on caller redshift nodes (jcg_geometry_build_nodes) has no
+    Limber grid: angular_cl and the Limber stage refuse it on the host, as the
+    no-allocation and Jacobian entry points do."""
+    lib = _lib.load()
+    g = _geom()
+    g.n_nodes = 40
+    buf = ctypes.create_string_buffer(1 << 16)
+    addr = ctypes.c_void_p((ctypes.addressof(buf) + 255) // 256 * 256)
+    assert lib.jcg_angular_cl(ctypes.byref(g), addr, addr, 1, _lib.FP64, addr, addr, 1 << 12, None) == _lib.ERR_ARG
+    assert b"Limber grid" in lib.jcg_last_error_string()
+    assert lib.jcg_stage_limber(ctypes.byref(g), addr, addr, 1, _lib.FP32C, addr, addr, 1 << 12,
+                                None) == _lib.ERR_ARG
+    assert b"Limber grid" in lib.jcg_last_error_string()
+    assert lib.jcg_angular_cl_noalloc(ctypes.byref(g), addr, addr, 1, _lib.FP64, addr, None) == _lib.ERR_ARG

@@ -103,9 +103,17 @@ def test_no_alloc_matches_workspace_entry_point_twice(setup, prec, tol):
 
 def test_no_alloc_rejects_requests_above_the_scratch_limit(setup):
     lib, g, geo, ell_t, stream = setup
+    # smallest batch whose scratch (jcg_workspace_size) exceeds the fixed array
     per = ctypes.c_size_t()
     lib.jcg_workspace_size(ctypes.byref(g), 1, _lib.FP64, ctypes.byref(per))
-    n_too_many = _lib.NOALLOC_SCRATCH_BYTES // per.value + 2
+    n_too_many = max(1, _lib.NOALLOC_SCRATCH_BYTES // per.value)
+    need = ctypes.c_size_t()
+    while True:
+        assert lib.jcg_workspace_size(ctypes.byref(g), n_too_many, _lib.FP64, ctypes.byref(need)) == 0
+        if need.value > _lib.NOALLOC_SCRATCH_BYTES:
+            break
+        n_too_many += 1
+    assert need.value > _lib.NOALLOC_SCRATCH_BYTES
     params = _params(3, n_too_many)
     out = torch.empty(n_too_many, _geometry.n_cls_of(g), g.n_ell, dtype=torch.float64, device="cuda")
     rc = lib.jcg_angular_cl_noalloc(ctypes.byref(g), ctypes.c_void_p(geo.data_ptr()),
