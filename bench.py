@@ -346,7 +346,79 @@ def gpu_arm(args, rank, world, device):
     return res
 
 
-def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, seed=SEED):
+def accuracy_arm(device):
+    """Stated errors of the single-cosmology configurations against the float64
+    oracle's stored outputs (tests/golden/c2_oracle.npz, c4_oracle.npz, written
+    by tests/golden/make_oracle_fixtures.py; the tests check the same files and
+    the live oracle):
+
+    * 10 tracers (5 WL + 5 NC, bias 1.2) x 200 ell in [10, 5000], N = 512: the
+      per-spectrum maximum relative error of the FP64 and fp32c C_ell;
+    * 5 WL x 50 ell in [10, 3000], fiducial, stored noisy data: the
+      log-likelihood (mean and covariance at the cosmology) and its gradient
+      over the 8 Cosmology leaves in FP64 and fp32c against the oracle's
+      autograd, and against central differences of the FP64 log-likelihood
+      (step 1e-5 relative, 1e-5 absolute for zero-valued leaves).
+    """
+    import torch
+
+    import jax_cosmo_gb300 as jc
+
+    gold = os.path.join(ROOT, "tests", "golden")
+    out = {}
+    d2 = np.load(os.path.join(gold, "c2_oracle.npz"))
+    fid = [float(v) for v in d2["fid"]]
+    nz = [jc.redshift.smail_nz(1.0, 2.0, float(z0), gals_per_arcmin2=10.0) for z0 in Z0]
+    p2 = [jc.probes.WeakLensing(nz, sigma_e=0.26), jc.probes.NumberCounts(nz, jc.bias.constant_linear_bias(1.2))]
+    ref2 = torch.as_tensor(d2["cl"])
+    c2 = {"workload": "10 tracers (5 WL + 5 NC, bias 1.2), 55 spectra x 200 ell in [10, 5000], N = 512, fiducial"}
+    for prec in ("fp64", "fp32c"):
+        cl = jc.cl.angular_cl(jc.Cosmology(*fid), d2["ell"], p2, precision=prec).cpu()
+        per = ((cl - ref2) / ref2).abs().amax(dim=1)
+        c2[prec] = {"max_rel_err": float(per.max()), "median_rel_err": float(per.median()),
+                    "per_spectrum_max_rel_err": [float("%.3g" % v) for v in per.tolist()]}
+    out["config_10_tracers"] = c2
+    d4 = np.load(os.path.join(gold, "c4_oracle.npz"))
+    ell4 = d4["ell"]
+    p4 = [jc.probes.WeakLensing(nz, sigma_e=0.26)]
+    data = torch.as_tensor(d4["data"], device=device)
+    g_o = d4["grad"]
+    names = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
+
+    def loglike(row, prec="fp64", grad=False):
+        ps = {n: torch.tensor(float(v), dtype=torch.float64, requires_grad=grad) for n, v in zip(names, row)}
+        c = jc.Cosmology(**ps)
+        mu, cov = jc.cl.gaussian_cl_covariance_and_mean(c, ell4, p4, sparse=True, precision=prec)
+        ll = jc.likelihood.gaussian_log_likelihood(data, mu, cov)
+        if grad:
+            ll.backward()
+            return float(ll), np.array([float(ps[n].grad) for n in names])
+        return float(ll)
+
+    c4 = {"workload": "5 WL x 50 ell in [10, 3000], N = 512, fiducial; data = mean + seeded noise from its "
+                      "covariance; loglike of gaussian_cl_covariance_and_mean + gaussian_log_likelihood",
+          "oracle_loglike": float(d4["loglike"])}
+    fd = np.zeros(8)
+    for i in range(8):
+        h = 1e-5 * abs(fid[i]) if fid[i] != 0 else 1e-5
+        up, dn = list(fid), list(fid)
+        up[i] += h
+        dn[i] -= h
+        fd[i] = (loglike(up) - loglike(dn)) / (2 * h)
+    for prec in ("fp64", "fp32c"):
+        ll, g = loglike(fid, prec, True)
+        c4[prec] = {"loglike_rel_err": abs(ll - float(d4["loglike"])) / abs(float(d4["loglike"])),
+                    "grad_max_err_vs_oracle_autograd": float(np.max(np.abs(g - g_o)) / np.max(np.abs(g_o))),
+                    "grad_max_err_vs_fd_fp64": float(np.max(np.abs(g - fd)) / np.max(np.abs(fd))),
+                    "grad": [float(v) for v in g]}
+    c4["oracle_grad"] = [float(v) for v in g_o]
+    c4["err_note"] = ("max |g - g_ref| / max |g_ref| over the 8 leaves; FD: central differences of the FP64 GPU "
+                      "log-likelihood, step 1e-5 relative (1e-5 absolute at zero-valued leaves)")
+    out["config_gradient"] = c4
+    return out
+
+
+def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, seed=SEED, n_check=256):
     """64 synthetic HMC chains against the continuous-batching server.
 
     Each chain (seeded): 1-10 tracers (WeakLensing / NumberCounts mix, smail_nz
@@ -416,7 +488,7 @@ def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, 
         while heap and heap[0][0] <= now:
             _, c = heapq.heappop(heap)
             f = submit(c)
-            if reset and len(sample) < 8 and c % 8 == len(sample):
+            if reset and len(sample) < n_check:
                 sample.append((c, pos[c].copy(), f))
         timeout = max(0.0, heap[0][0] - now) if heap else 0.01
         try:
@@ -429,17 +501,25 @@ def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, 
             pass
     st = srv.stats()
     srv.stop()
-    # served log-likelihoods against the plain float64 method (public API)
-    err = 0.0
+    # served log-likelihoods and gradients against the plain float64 method
+    # (public API: angular_cl_jacobian in FP64, then -J^T P r), every sampled request
+    err_ll, err_g = [], []
     for c, p, f in sample:
         r = f.result()
         m = models[c]
-        mu = jc.cl.angular_cl(jc.Cosmology(*[float(v) for v in p]), m.ell, m.probes).flatten()
-        res = (mu - m.data).reshape(m.n_cls, m.n_ell)
-        ll = -0.5 * float((res * torch.einsum("lpq,ql->pl", m.prec, res)).sum())
-        err = max(err, abs(r.loglike - ll) / abs(ll))
-    st["loglike_max_rel_err_vs_fp64"] = err
-    st["checked_requests"] = len(sample)
+        cl, jac = jc.autodiff.angular_cl_jacobian(jc.Cosmology(*[float(v) for v in p]), m.ell, m.probes)
+        res = (cl.flatten() - m.data).reshape(m.n_cls, m.n_ell)
+        pr = torch.einsum("lpq,ql->pl", m.prec, res)
+        ll = -0.5 * float((res * pr).sum())
+        g = -torch.einsum("pld,pl->d", jac, pr).cpu().numpy()
+        err_ll.append(abs(r.loglike - ll) / abs(ll))
+        err_g.append(float(np.max(np.abs(np.asarray(r.grad) - g)) / np.max(np.abs(g))))
+    st["accuracy_vs_fp64"] = {
+        "checked_requests": len(sample),
+        "loglike_max_rel_err": float(max(err_ll)), "loglike_median_rel_err": float(np.median(err_ll)),
+        "grad_max_err": float(max(err_g)), "grad_median_err": float(np.median(err_g)),
+        "grad_err_note": "max |g - g64| / max |g64| over the 8 Cosmology leaves, per request",
+        "reference": "public API in float64: angular_cl_jacobian, then logL = -r^T P r / 2, grad = -J^T P r"}
     st.update({"chains": n_chains, "think_ms_mean": think_ms, "duration_s": duration_s,
                "tracers_per_chain": [int(m.g.n_tracers) for m in models],
                "n_ell_per_chain": [int(m.n_ell) for m in models], "precision": srv.precision,
@@ -583,6 +663,7 @@ def main():
         if rank == 0:
             print(json.dumps(res["jacobian_only"]))
         return
+    acc = accuracy_arm(device) if rank == 0 else None
     serve = None
     if rank == 0 and not args.no_serving:
         serve = serving_arm(device, duration_s=args.serve_seconds)
@@ -613,6 +694,7 @@ def main():
         "loglike_grad_latency_ms": ({"p50": serve["p50_ms"], "p99": serve["p99_ms"]} if serve else None),
         "serving": serve,
         "fp32c_max_rel_err_vs_fp64": res["fp32c_max_rel_err_vs_fp64"],
+        "accuracy": acc,
         "cosmologies_per_s": value / 1500.0,
         "e2e": {"value": e2e, "unit": "C_ell/s", "h2d_bytes_per_step": res["h2d"],
                 "d2h_bytes_per_step": res["d2h"]},

@@ -243,6 +243,22 @@ int jcg_angular_cl_jacobian_dir(const jcg_geometry* g, const void* geo_dev, cons
                                 int n_cosmo, int precision, int gamma_dir, double* cl_dev, double* jac_dev,
                                 void* workspace, size_t workspace_bytes, cudaStream_t stream);
 
+/* jcg_angular_cl_jacobian in FP64 with the branch of the halofit root find
+ * exposed.  The reference finds the non-linear scale with an interpolation
+ * whose segment is an argmin over the sigma^2(R) table (power.py:112-115,
+ * scipy/interpolate.py:34-59), so C_ell is piecewise smooth in the parameters
+ * and jax.grad / jax.hessian differentiate the piece of the evaluation point
+ * (the argmin is locally constant).  seg_out [n_cosmo][na] (may be NULL)
+ * receives each Limber node's segment (na = n_limber + 1); seg_in (may be
+ * NULL) imposes segments instead of finding them, so that parameter points
+ * near a base point are evaluated on the base point's piece -- the
+ * second-derivative form of jax.hessian (README.md:27) takes central
+ * differences of the exact gradient on that piece.  The gamma growth is not
+ * supported here (JCG_ERR_UNSUPPORTED). */
+int jcg_angular_cl_jacobian_branch(const jcg_geometry* g, const void* geo_dev, const double* params_dev,
+                                   int n_cosmo, const int* seg_in_dev, int* seg_out_dev, double* cl_dev,
+                                   double* jac_dev, void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
 /* ------------------------------------------------ ragged requests ------ */
 /* A list of requests, each with its own geometry (tracers, n(z), ell grid)
  * and cosmology, computed in one launch sequence: the continuous-batching form

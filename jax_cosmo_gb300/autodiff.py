@@ -261,10 +261,100 @@ def fisher_matrix(cosmo, ell, probes, f_sky=0.25, n_limber=512, params=FISHER_PA
     cl, jac = angular_cl_jacobian(cosmo, ell, probes, n_limber, precision)
     if cl.dim() != 2:
         raise ValueError("fisher_matrix takes a single (unbatched) cosmology")
-    sel = [PARAM_ORDER.index(p) for p in params]
+    names = PARAM_ORDER + (("gamma",) if jac.shape[-1] > len(PARAM_ORDER) else ())
+    unknown = [p for p in params if p not in names]
+    if unknown:
+        raise ValueError(f"unknown parameters {unknown}; this cosmology has {names}")
+    sel = [names.index(p) for p in params]
     J = jac[..., sel]  # [n_cls, n_ell, P]
     cov = gaussian_cl_covariance(ell, probes, cl, noise_cl(ell, probes), f_sky, sparse=True)
     Cl = cov.permute(2, 0, 1)  # [n_ell, n_cls, n_cls]
     Jl = J.permute(1, 0, 2)  # [n_ell, n_cls, P]
     X = torch.linalg.solve(Cl, Jl)
     return torch.einsum("lcp,lcq->pq", Jl, X)
+
+
+# ----------------------------------------------------------------- Hessian ---
+def jacobian_branch(params, ell, probes, n_limber=512, seg_in=None, want_seg=False):
+    """FP64 (C_ell, dC/dtheta) of [B, 8] params with the halofit root find's
+    segments exposed (``jcg_angular_cl_jacobian_branch``): ``seg_in`` [B, na]
+    imposes them, ``want_seg`` returns them as a third value."""
+    device = params.device
+    g, geo, _ = _geometry.get_geometry(probes, ell, n_limber, device, 0)
+    B = params.shape[0]
+    n_cls = _geometry.n_cls_of(g)
+    na = int(g.n_limber) + 1
+    wsz = ctypes.c_size_t()
+    _lib.call("jcg_jacobian_workspace_size", ctypes.byref(g), B, _lib.FP64, ctypes.byref(wsz))
+    ws = _lib.workspace(wsz.value, device)
+    cl = torch.empty(B, n_cls, g.n_ell, dtype=torch.float64, device=device)
+    jac = torch.empty(B, n_cls, g.n_ell, len(PARAM_ORDER), dtype=torch.float64, device=device)
+    seg = torch.empty(B, na, dtype=torch.int32, device=device) if want_seg else None
+    if seg_in is not None:
+        seg_in = seg_in.to(device=device, dtype=torch.int32).expand(B, na).contiguous()
+    _lib.call("jcg_angular_cl_jacobian_branch", ctypes.byref(g), _lib.ptr(geo), _lib.ptr(params.contiguous()), B,
+              _lib.ptr(seg_in), _lib.ptr(seg), _lib.ptr(cl), _lib.ptr(jac), _lib.ptr(ws),
+              ctypes.c_size_t(ws.numel()), _lib.stream_of(device))
+    return (cl, jac, seg) if want_seg else (cl, jac)
+
+
+def loglike_hessian(cosmo, ell, probes, data, f_sky=0.25, n_limber=512, include_logdet=True, rel_step=1e-3):
+    """Hessian of the README likelihood over the 8 Cosmology leaves
+    (README.md:14-27: ``F = -jax.hessian(likelihood)(cosmo)``), with
+
+        mu, C = gaussian_cl_covariance_and_mean(cosmo, ell, probes, f_sky)
+        likelihood = gaussian_log_likelihood(data, mu, C, include_logdet)
+
+    mean and covariance both at the cosmology (angular_cl.py:166-196,
+    likelihood.py:9-61).  Returns (H [8, 8], gradient [8], logL).
+
+    The gradient is exact (the hand-written FP64 Jacobian of C_ell, then the
+    covariance and likelihood adjoints).  Each Hessian column is the
+    derivative of that gradient along one leaf, taken by central differences
+    of the exact gradient at steps h and h/2 combined by Richardson
+    extrapolation (error O(h^4)), all 32 parameter points in one batched
+    Jacobian launch.  The points are evaluated on the piece of the base
+    point: the halofit root find's interpolation segments found at the base
+    point are imposed on every perturbed point, which is the derivative
+    jax.hessian takes (the argmin is locally constant).  Steps: rel_step
+    times |theta_b|, or rel_step absolute for a zero-valued leaf.
+    """
+    device = _lib.require_cuda()
+    if cosmo.batch_size is not None:
+        raise ValueError("loglike_hessian takes a single (unbatched) cosmology")
+    if cosmo.physics_bits():
+        raise NotImplementedError("loglike_hessian: the gamma growth is not supported")
+
+    ell_np = _geometry.ell_host(ell)
+    p0 = cosmo.param_tensor(device)[:1]
+    D = len(PARAM_ORDER)
+    _, _, seg = jacobian_branch(p0, ell_np, probes, n_limber, want_seg=True)
+    x0 = p0[0].detach().cpu().numpy()
+    steps = np.where(x0 != 0.0, rel_step * np.abs(x0), rel_step)
+    pts = []
+    for scale in (1.0, 0.5):
+        for b in range(D):
+            for sgn in (1.0, -1.0):
+                x = x0.copy()
+                x[b] += sgn * scale * steps[b]
+                pts.append(x)
+    pts.append(x0)
+    P = torch.as_tensor(np.array(pts), dtype=torch.float64, device=device)
+    cl, jac = jacobian_branch(P, ell_np, probes, n_limber, seg_in=seg)
+    B, n_cls, n_ell = cl.shape
+    _, _, ell_t = _geometry.get_geometry(probes, ell_np, n_limber, device)
+    tracer_noise = torch.cat([p.noise() for p in probes])
+    mu = cl.detach().reshape(B, -1).clone().requires_grad_(True)
+    cov = covariance_autograd(mu.reshape(B, n_cls, n_ell), ell_t, tracer_noise.numel(), None, tracer_noise,
+                              f_sky, True)
+    data_t = torch.as_tensor(data, dtype=torch.float64).to(device).reshape(1, -1).expand(B, -1).contiguous()
+    ll = loglike_autograd(data_t, mu, cov, include_logdet, True, n_cls, n_ell)
+    (dmu,) = torch.autograd.grad(ll.sum(), mu)
+    g = torch.einsum("bn,bnd->bd", dmu, jac.reshape(B, n_cls * n_ell, D))  # exact gradients [B, 8]
+    g = g.cpu().numpy()
+    h = steps
+    d1 = (g[0:2 * D:2] - g[1:2 * D:2]) / (2.0 * h[:, None])               # step h:   rows = leaf b
+    d2 = (g[2 * D:4 * D:2] - g[2 * D + 1:4 * D:2]) / (1.0 * h[:, None])    # step h/2
+    H = (4.0 * d2 - d1) / 3.0
+    H = 0.5 * (H + H.T)
+    return torch.as_tensor(H), torch.as_tensor(g[-1]), float(ll[-1].detach())

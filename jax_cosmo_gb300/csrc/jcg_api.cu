@@ -734,6 +734,28 @@ extern "C" int jcg_angular_cl_jacobian_dir(const jcg_geometry* g, const void* ge
   return cuda_check("angular_cl_jacobian");
 }
 
+extern "C" int jcg_angular_cl_jacobian_branch(const jcg_geometry* g, const void* geo, const double* params,
+                                              int n_cosmo, const int* seg_in, int* seg_out, double* cl,
+                                              double* jac, void* ws, size_t ws_bytes, cudaStream_t stream) {
+  GeoHeader h;
+  int rc = make_header(g, &h);
+  if (rc) return rc;
+  if (growth_gamma(h.physics))
+    return fail(JCG_ERR_UNSUPPORTED, "jcg_angular_cl_jacobian_branch: JCG_GROWTH_GAMMA is not supported");
+  if (!geo || !params || !jac || !ws) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  if (h.custom_nodes) return fail(JCG_ERR_ARG, "a geometry with caller redshift nodes has no Limber grid");
+  if (seg_in && seg_in == seg_out) return fail(JCG_ERR_ARG, "seg_in and seg_out must differ");
+  const size_t need = grad_workspace_bytes(h, n_cosmo, JCG_FP64);
+  if (ws_bytes < need) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need);
+  if (((uintptr_t)ws) % 256 != 0) return fail(JCG_ERR_ARG, "workspace must be 256-byte aligned");
+  ConstTables* c = nullptr;
+  if ((rc = const_tables(&c))) return rc;
+  grad_run(static_cast<const GeoHeader*>(geo), h, params, n_cosmo, JCG_FP64, cl, jac, ws, c, stream, -1, seg_in,
+           seg_out);
+  return cuda_check("angular_cl_jacobian_branch");
+}
+
 // ------------------------------------------------------ ragged requests -----
 namespace {
 

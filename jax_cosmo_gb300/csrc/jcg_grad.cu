@@ -553,8 +553,14 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
   D1 chi = interp_d1(a, c->atab_chi, tb->chiv, tb->chid[dir], unpack_seg(SC[n]));
   chi = xfmax(chi, 0.0);
   const D1 g2 = g * g;
-  int best;
-  {
+  int ind, j2;
+  if (gb.seg_in) {
+    // the segment of another parameter point: differentiate on its branch
+    const int pk = gb.seg_in[(size_t)item * na + n];
+    ind = min(max(pk & 0xffff, 1), NRT - 2);
+    j2 = ind + ((pk >> 16) ? 1 : -1);
+  } else {
+    int best;
     int lo = 0, hi = NRT;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
@@ -572,11 +578,12 @@ __global__ void __launch_bounds__(256) grad_rows_kernel(GradBatch gb, const Cons
         best = cc - 1;
       }
     }
+    ind = best < 1 ? 1 : (best > NRT - 2 ? NRT - 2 : best);
+    const double xpi = tb->sigv[ind] * g2.v;
+    const double xc = fmin(fmax(1.0, tb->sigv[1] * g2.v), tb->sigv[NRT - 2] * g2.v);
+    j2 = ind + ((xc - xpi >= 0.0) ? 1 : -1);
   }
-  const int ind = best < 1 ? 1 : (best > NRT - 2 ? NRT - 2 : best);
-  const double xpi = tb->sigv[ind] * g2.v;
-  const double xc = fmin(fmax(1.0, tb->sigv[1] * g2.v), tb->sigv[NRT - 2] * g2.v);
-  const int j2 = ind + ((xc - xpi >= 0.0) ? 1 : -1);
+  if (gb.seg_out && live && dir == 0) gb.seg_out[(size_t)item * na + n] = ind | ((j2 > ind ? 1 : 0) << 16);
   const D1 xp0 = mk1(tb->sigv[ind], tb->sigd[dir][ind]) * g2;
   const D1 xp1 = mk1(tb->sigv[j2], tb->sigd[dir][j2]) * g2;
   const D1 slope = (c->logr[j2] - c->logr[ind]) / (xp1 - xp0);
@@ -1768,10 +1775,13 @@ size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
 }
 
 void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, int precision,
-              double* cl, double* jac, void* ws, const ConstTables* c, cudaStream_t st, int gamma_dir) {
+              double* cl, double* jac, void* ws, const ConstTables* c, cudaStream_t st, int gamma_dir,
+              const int* seg_in, int* seg_out) {
   GradBatch gb;
   memset(&gb, 0, sizeof(gb));
   gb.gamma_dir = gamma_dir;
+  gb.seg_in = seg_in;
+  gb.seg_out = seg_out;
   gb.n_items = n_cosmo;
   gb.precision = precision;
   gb.params = params;

@@ -138,6 +138,11 @@ struct GradBatch {
   int na, n_tr, n_cls, n_ell, n_split;
   int physics_or;  // OR of the items' physics switches (selects kernel variants)
   int gamma_dir;   // tangent direction carrying d/dgamma instead of its parameter's (-1: none)
+  // FP64 uniform form: the halofit root find's interpolation segment per
+  // (item, Limber node), packed as ind | (side > 0) << 16: recorded into
+  // seg_out, or imposed from seg_in (the branch of another parameter point)
+  const int* seg_in;
+  int* seg_out;
 };
 
 // Small fp32c batches spread the table kernel's per-node evaluations over

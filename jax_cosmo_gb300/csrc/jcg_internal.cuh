@@ -706,7 +706,8 @@ void launch_limber(const Batch& b, const ConstTables* c, int lt, cudaStream_t st
 // derivatives (jcg_grad.cu)
 size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision);
 void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, int precision,
-              double* cl, double* jac, void* ws, const ConstTables* c, cudaStream_t st, int gamma_dir = -1);
+              double* cl, double* jac, void* ws, const ConstTables* c, cudaStream_t st, int gamma_dir = -1,
+              const int* seg_in = nullptr, int* seg_out = nullptr);
 // one request of a ragged Jacobian batch; cl / jac NULL: carved from the workspace
 struct GradReq {
   const GeoHeader* h;      // host copy of the header
