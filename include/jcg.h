@@ -369,14 +369,36 @@ int jcg_gaussian_loglike_dense(const double* data_dev, const double* mu_dev, con
                                size_t workspace_bytes, cudaStream_t stream);
 
 /* sparse.inv / sparse.slogdet of (n, n, ndiag) block-diagonal matrices
- * (sparse.py:295-366), float64, one matrix. */
+ * (sparse.py:295-366), float64, one matrix; n <= JCG_SPARSE_MAX_N.  Each
+ * diagonal's n x n matrix is inverted in place by Gauss-Jordan elimination
+ * with partial pivoting. */
+#define JCG_SPARSE_MAX_N 160
 int jcg_sparse_inv(const double* sparse_dev, int n, int ndiag, double* out_dev, cudaStream_t stream);
+/* sparse.inv of n_batch matrices [n_batch][n][n][ndiag] in one launch (the
+ * batched form the likelihood's derivative and the serving loop use). */
+int jcg_sparse_inv_batched(const double* sparse_dev, int n_batch, int n, int ndiag, double* out_dev,
+                           cudaStream_t stream);
 /* work_dev: 2*ndiag float64 of caller-owned scratch (per-diagonal partials). */
 int jcg_sparse_slogdet(const double* sparse_dev, int n, int ndiag, double* sign_dev,
                        double* logdet_dev, double* work_dev, cudaStream_t stream);
 /* sparse.to_dense (sparse.py:52-68): (n, m, d) -> (n*d, m*d). */
 int jcg_sparse_to_dense(const double* sparse_dev, int n, int m, int ndiag, double* out_dev,
                         cudaStream_t stream);
+/* Products with a block-diagonal operand, float64 (sparse.py:140-292):
+ *   sparse_dot_sparse  A (n, m, d) @ B (m, p, d) -> (n, p, d)          sparse.py:236-260
+ *   sparse_dot_dense   A (n, m, d) @ D (m d, k) -> (n d, k)             sparse.py:164-182
+ *   dense_dot_sparse   D (r, n d) @ A (n, m, d) -> (r, m d)             sparse.py:210-233
+ *   dense_dot_sparse_dot_dense  X (r, n d) @ Y (n, m, d) @ Z (m d, k) -> (r, k)
+ *                      sparse.py:263-292; work_dev holds n d k float64 (Y @ Z). */
+int jcg_sparse_dot_sparse(const double* a_dev, int n, int m, int p, int ndiag, const double* b_dev,
+                          double* out_dev, cudaStream_t stream);
+int jcg_sparse_dot_dense(const double* a_dev, int n, int m, int ndiag, const double* dense_dev, int k,
+                         double* out_dev, cudaStream_t stream);
+int jcg_dense_dot_sparse(const double* dense_dev, int r, const double* a_dev, int n, int m, int ndiag,
+                         double* out_dev, cudaStream_t stream);
+int jcg_dense_dot_sparse_dot_dense(const double* x_dev, int r, const double* y_dev, int n, int m, int ndiag,
+                                   const double* z_dev, int k, double* work_dev, double* out_dev,
+                                   cudaStream_t stream);
 /* sparse.dot(A, v) / sparse.dot(v, A) for sparse A (n, m, d) (sparse.py:71-137). */
 int jcg_sparse_dot_vec(const double* sparse_dev, int n, int m, int ndiag, const double* v_dev,
                        int transpose, double* out_dev, cudaStream_t stream);

@@ -126,6 +126,11 @@ SIGNATURES = {
     "jcg_angular_cl_jacobian_branch": [_PG, _P, _P, _I, _P, _P, _P, _P, _P, _SZ, _P],
     "jcg_requests_workspace_size": [_P, _I, _I, _I, _PSZ, _PSZ],
     "jcg_requests_run": [_P, _I, _I, _I, _P, _SZ, _P],
+    "jcg_sparse_inv_batched": [_P, _I, _I, _I, _P, _P],
+    "jcg_sparse_dot_sparse": [_P, _I, _I, _I, _I, _P, _P, _P],
+    "jcg_sparse_dot_dense": [_P, _I, _I, _I, _P, _I, _P, _P],
+    "jcg_dense_dot_sparse": [_P, _I, _P, _I, _I, _I, _P, _P],
+    "jcg_dense_dot_sparse_dot_dense": [_P, _I, _P, _I, _I, _I, _P, _I, _P, _P, _P],
     "jcg_calib_peak_fp64": [_P, _I, _I, _P],
     "jcg_calib_peak_mufu": [_P, _I, _I, _P],
     "jcg_sparse_inv": [_P, _I, _I, _P, _P],

@@ -221,26 +221,31 @@ def _dense_blocks(C, n_cls, n_ell):
     B = C.shape[0]
     g4 = C.reshape(B, n_cls, n_ell, n_cls, n_ell)
     idx = torch.arange(n_ell, device=C.device)
-    return g4[:, :, idx, :, idx].permute(1, 2, 3, 0).contiguous()
+    return g4[:, :, idx, :, idx].permute(1, 2, 3, 0).contiguous()  # [B, n_cls, n_cls, n_ell]
 
 
 def _sparse_inv_batched(S):
     from jax_cosmo_gb300 import sparse as sp
 
-    return torch.stack([sp.inv(S[i]) for i in range(S.shape[0])])
+    return sp.inv_batched(S)
 
 
 def _dense_inverse(C, status, n_cls, n_ell):
-    """C^-1 per batch entry: per-ell block inverses where C is block diagonal in ell."""
+    """C^-1 of [B, N, N] (cls, ell)-ordered matrices: one batched per-ell block
+    inverse (libjcg) scattered into the dense layout; a matrix flagged as not
+    block diagonal in ell (status 1) is inverted whole (torch Cholesky)."""
     from jax_cosmo_gb300 import sparse as sp
 
-    st = status.tolist()
-    out = torch.empty_like(C)
-    for i, s in enumerate(st):
-        if s == 1:
+    B = C.shape[0]
+    blocks = _dense_blocks(C, n_cls, n_ell)                       # [B, n_cls, n_cls, n_ell]
+    ib = sp.inv_batched(blocks)
+    out = torch.zeros_like(C)
+    idx = torch.arange(n_ell, device=C.device)
+    out.view(B, n_cls, n_ell, n_cls, n_ell)[:, :, idx, :, idx] = ib.permute(3, 0, 1, 2)
+    whole = status == 1
+    if bool(whole.any()):  # a user covariance with ell-ell correlations
+        for i in whole.nonzero().flatten().tolist():
             out[i] = torch.cholesky_inverse(torch.linalg.cholesky(C[i]))
-        else:
-            out[i] = sp.to_dense(sp.inv(_dense_blocks(C[i : i + 1], n_cls, n_ell)[0]))
     return out
 
 

@@ -20,7 +20,14 @@ void launch_covariance(const double* ell, int n_ell, int n_tr, const double* cl,
 void launch_loglike(const double* data, const double* mu, const double* cov, int n_cosmo, int n_cls,
                     int n_ell, int include_logdet, int dense, double* out, int* status,
                     double* partial, int* structure, double* alpha, cudaStream_t st);
-void launch_sparse_inv(const double* sp, int n, int nd, double* out, cudaStream_t st);
+void launch_sparse_inv(const double* sp, int n_batch, int n, int nd, double* out, cudaStream_t st);
+void launch_sparse_dot_sparse(const double* a, const double* b, int n, int m, int p, int nd, double* c,
+                              cudaStream_t st);
+void launch_sparse_dot_dense(const double* a, int n, int m, int nd, const double* d, int K, double* out,
+                             cudaStream_t st);
+void launch_dense_dot_sparse(const double* d, int R, const double* a, int n, int m, int nd, double* out,
+                             cudaStream_t st);
+void launch_gemm_f64(const double* x, const double* t, int M, int Kd, int N, double* c, cudaStream_t st);
 void launch_sparse_slogdet(const double* sp, int n, int nd, double* sign_part, double* ld_part,
                            double* sign_out, double* ld_out, cudaStream_t st);
 void launch_sparse_to_dense(const double* sp, int n, int m, int nd, double* out, cudaStream_t st);
@@ -582,10 +589,15 @@ int jcg_gaussian_loglike_dense(const double* data, const double* mu, const doubl
 }
 
 int jcg_sparse_inv(const double* sp, int n, int nd, double* out, cudaStream_t stream) {
+  return jcg_sparse_inv_batched(sp, 1, n, nd, out, stream);
+}
+
+int jcg_sparse_inv_batched(const double* sp, int n_batch, int n, int nd, double* out, cudaStream_t stream) {
   if (!sp || !out) return fail(JCG_ERR_ARG, "NULL pointer");
-  if (n < 1 || nd < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
-  if (n > 80) return fail(JCG_ERR_SHAPE, "n = %d above the per-diagonal block limit 80", n);
-  launch_sparse_inv(sp, n, nd, out, stream);
+  if (n < 1 || nd < 1 || n_batch < 1 || n_batch > 65535) return fail(JCG_ERR_SHAPE, "bad sizes");
+  if (n > JCG_SPARSE_MAX_N) return fail(JCG_ERR_SHAPE, "n = %d above the block limit %d", n, JCG_SPARSE_MAX_N);
+  if (sp == out) return fail(JCG_ERR_ARG, "sparse inv: input and output must differ");
+  launch_sparse_inv(sp, n_batch, n, nd, out, stream);
   return cuda_check("sparse inv");
 }
 
@@ -593,7 +605,7 @@ int jcg_sparse_slogdet(const double* sp, int n, int nd, double* sign, double* lo
                        cudaStream_t stream) {
   if (!sp || !sign || !logdet || !work) return fail(JCG_ERR_ARG, "NULL pointer");
   if (n < 1 || nd < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
-  if (n > 80) return fail(JCG_ERR_SHAPE, "n = %d above the per-diagonal block limit 80", n);
+  if (n > JCG_SPARSE_MAX_N) return fail(JCG_ERR_SHAPE, "n = %d above the block limit %d", n, JCG_SPARSE_MAX_N);
   launch_sparse_slogdet(sp, n, nd, work, work + nd, sign, logdet, stream);
   return cuda_check("sparse slogdet");
 }
@@ -603,6 +615,40 @@ int jcg_sparse_to_dense(const double* sp, int n, int m, int nd, double* out, cud
   if (n < 1 || m < 1 || nd < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
   launch_sparse_to_dense(sp, n, m, nd, out, stream);
   return cuda_check("sparse to_dense");
+}
+
+int jcg_sparse_dot_sparse(const double* a, int n, int m, int p, int nd, const double* b, double* out,
+                          cudaStream_t stream) {
+  if (!a || !b || !out) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n < 1 || m < 1 || p < 1 || nd < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
+  launch_sparse_dot_sparse(a, b, n, m, p, nd, out, stream);
+  return cuda_check("sparse_dot_sparse");
+}
+
+int jcg_sparse_dot_dense(const double* a, int n, int m, int nd, const double* dense, int k, double* out,
+                         cudaStream_t stream) {
+  if (!a || !dense || !out) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n < 1 || m < 1 || nd < 1 || k < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
+  launch_sparse_dot_dense(a, n, m, nd, dense, k, out, stream);
+  return cuda_check("sparse_dot_dense");
+}
+
+int jcg_dense_dot_sparse(const double* dense, int r, const double* a, int n, int m, int nd, double* out,
+                         cudaStream_t stream) {
+  if (!a || !dense || !out) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n < 1 || m < 1 || nd < 1 || r < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
+  launch_dense_dot_sparse(dense, r, a, n, m, nd, out, stream);
+  return cuda_check("dense_dot_sparse");
+}
+
+int jcg_dense_dot_sparse_dot_dense(const double* x, int r, const double* y, int n, int m, int nd, const double* z,
+                                   int k, double* work, double* out, cudaStream_t stream) {
+  if (!x || !y || !z || !work || !out) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (r < 1 || n < 1 || m < 1 || nd < 1 || k < 1) return fail(JCG_ERR_SHAPE, "bad sizes");
+  if ((long long)n * nd > (1LL << 31) - 1 || (long long)r > 65535LL * 16) return fail(JCG_ERR_SHAPE, "too large");
+  launch_sparse_dot_dense(y, n, m, nd, z, k, work, stream);  // T = Y Z, (n nd, k)
+  launch_gemm_f64(x, work, r, n * nd, k, out, stream);      // X T
+  return cuda_check("dense_dot_sparse_dot_dense");
 }
 
 int jcg_sparse_dot_vec(const double* sp, int n, int m, int nd, const double* v, int transpose,

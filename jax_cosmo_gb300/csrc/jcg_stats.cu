@@ -336,80 +336,110 @@ void launch_loglike(const double* data, const double* mu, const double* cov, int
 }
 
 // -------------------------------------------------- sparse-format algebra ---
-// One CTA per diagonal index l: Gauss-Jordan with partial pivoting of the
-// n x n matrix A_l[i][j] = sparse[i][j][l] (sparse.py:295-315), or its
-// log|det| and sign (sparse.py:322-366 computes the same by Schur complements).
-__global__ void sparse_lu_kernel(const double* __restrict__ sp, int n, int nd, int mode,
-                                 double* __restrict__ out, double* __restrict__ sign_out,
-                                 double* __restrict__ logdet_part) {
+// One CTA per (diagonal index l, matrix b): in-place Gauss-Jordan inversion
+// with partial (row) pivoting of the n x n matrix A_l[i][j] = sparse[b][i][j][l]
+// (sparse.py:295-315), or its log|det| and sign (sparse.py:322-366 computes
+// the same by Schur complements).  In place, so one n x n FP64 block of
+// shared memory: n <= SPARSE_MAX_N.  The row swaps are undone on the columns
+// at the end (the inverse of P A is A^-1 P^T).
+constexpr int SPARSE_MAX_N = 160;
+
+__global__ void __launch_bounds__(256) sparse_gj_kernel(const double* __restrict__ sp, int n, int nd, int mode,
+                                                        double* __restrict__ out, double* __restrict__ sign_part,
+                                                        double* __restrict__ logdet_part) {
   const int l = blockIdx.x;
-  extern __shared__ double sm[];
-  double* A = sm;          // n x n
-  double* X = A + n * n;   // n x n (inverse)
+  const size_t mat = (size_t)blockIdx.y * n * n * nd;
+  extern __shared__ double A[];  // n x n, row-major
+  __shared__ double fcol[SPARSE_MAX_N];
+  __shared__ int perm[SPARSE_MAX_N];
+  __shared__ double wv[8];
+  __shared__ int wi[8];
   __shared__ int piv;
   __shared__ double sgn, ld;
-  const int tid = threadIdx.x, nt = blockDim.x;
-  for (int e = tid; e < n * n; e += nt) {
-    const int i = e / n, j = e % n;
-    A[e] = sp[((size_t)i * n + j) * nd + l];
-    X[e] = (i == j) ? 1.0 : 0.0;
-  }
+  const int tid = threadIdx.x, nt = blockDim.x, lane = tid & 31, warp = tid >> 5;
+  for (int e = tid; e < n * n; e += nt) A[e] = sp[mat + (size_t)e * nd + l];
   if (tid == 0) {
     sgn = 1.0;
     ld = 0.0;
   }
   __syncthreads();
   for (int k = 0; k < n; ++k) {
+    // pivot: the first row i >= k of largest |A[i][k]|
+    double bv = -1.0;
+    int bi = n;
+    for (int i = k + tid; i < n; i += nt) {
+      const double v = fabs(A[i * n + k]);
+      if (v > bv) { bv = v; bi = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const double ov = __shfl_xor_sync(0xffffffffu, bv, o);
+      const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+      if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+    }
+    if (lane == 0) wv[warp] = bv, wi[warp] = bi;
+    __syncthreads();
     if (tid == 0) {
-      int p = k;
-      double best = fabs(A[k * n + k]);
-      for (int i = k + 1; i < n; ++i) {
-        const double v = fabs(A[i * n + k]);
-        if (v > best) { best = v; p = i; }
-      }
+      double v = wv[0];
+      int p = wi[0];
+      for (int w = 1; w < nt / 32; ++w)
+        if (wv[w] > v || (wv[w] == v && wi[w] < p)) v = wv[w], p = wi[w];
+      if (p >= n) p = k;
       piv = p;
-    }
-    __syncthreads();
-    const int p = piv;
-    if (p != k) {
-      for (int j = tid; j < n; j += nt) {
-        double t = A[k * n + j]; A[k * n + j] = A[p * n + j]; A[p * n + j] = t;
-        t = X[k * n + j]; X[k * n + j] = X[p * n + j]; X[p * n + j] = t;
-      }
-    }
-    __syncthreads();
-    const double d = A[k * n + k];
-    if (tid == 0) {
+      perm[k] = p;
+      const double d = A[p * n + k];
       if (p != k) sgn = -sgn;
       sgn *= (d > 0.0) ? 1.0 : ((d < 0.0) ? -1.0 : 0.0);
       ld += log(fabs(d));
     }
-    // normalise row k, eliminate column k from all other rows
-    for (int j = tid; j < n; j += nt) {
-      A[k * n + j] /= d;
-      X[k * n + j] /= d;
-    }
     __syncthreads();
-    for (int e = tid; e < n * n; e += nt) {
-      const int i = e / n, j = e % n;
-      if (i == k) continue;
-      const double f = A[i * n + k];
-      if (j != k) A[i * n + j] -= f * A[k * n + j];
-      X[i * n + j] -= f * X[k * n + j];
-    }
+    const int p = piv;
+    if (p != k)
+      for (int j = tid; j < n; j += nt) {
+        const double t = A[k * n + j];
+        A[k * n + j] = A[p * n + j];
+        A[p * n + j] = t;
+      }
     __syncthreads();
-    for (int i = tid; i < n; i += nt)
-      if (i != k) A[i * n + k] = 0.0;
+    if (mode == 0) {
+      const double pinv = 1.0 / A[k * n + k];
+      for (int i = tid; i < n; i += nt) fcol[i] = A[i * n + k];
+      __syncthreads();
+      for (int j = tid; j < n; j += nt) A[k * n + j] = (j == k) ? pinv : A[k * n + j] * pinv;
+      __syncthreads();
+      for (int e = tid; e < n * n; e += nt) {
+        const int i = e / n, j = e - (e / n) * n;
+        if (i == k) continue;
+        const double f = fcol[i];
+        A[e] = (j == k) ? -f * pinv : A[e] - f * A[k * n + j];
+      }
+    } else {
+      // determinant only: plain elimination below the pivot
+      const double pinv = 1.0 / A[k * n + k];
+      for (int e = tid; e < (n - k - 1) * (n - k); e += nt) {
+        const int i = k + 1 + e / (n - k), j = k + e % (n - k);
+        if (j == k) continue;
+        A[i * n + j] -= A[i * n + k] * pinv * A[k * n + j];
+      }
+    }
     __syncthreads();
   }
   if (mode == 0) {
-    for (int e = tid; e < n * n; e += nt) {
-      const int i = e / n, j = e % n;
-      out[((size_t)i * n + j) * nd + l] = X[e];
+    // undo the row swaps on the columns, last swap first
+    for (int k = n - 1; k >= 0; --k) {
+      const int p = perm[k];
+      if (p != k)
+        for (int i = tid; i < n; i += nt) {
+          const double t = A[i * n + k];
+          A[i * n + k] = A[i * n + p];
+          A[i * n + p] = t;
+        }
+      __syncthreads();
     }
+    for (int e = tid; e < n * n; e += nt) out[mat + (size_t)e * nd + l] = A[e];
   } else if (tid == 0) {
-    sign_out[l] = sgn;
-    logdet_part[l] = ld;
+    sign_part[(size_t)blockIdx.y * nd + l] = sgn;
+    logdet_part[(size_t)blockIdx.y * nd + l] = ld;
   }
 }
 
@@ -426,18 +456,110 @@ __global__ void sparse_slogdet_reduce(const double* sign_part, const double* ld_
   }
 }
 
-void launch_sparse_inv(const double* sp, int n, int nd, double* out, cudaStream_t st) {
-  const size_t smem = 2 * (size_t)n * n * sizeof(double);
-  cudaFuncSetAttribute(sparse_lu_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  sparse_lu_kernel<<<nd, 128, smem, st>>>(sp, n, nd, 0, out, nullptr, nullptr);
+static size_t sparse_gj_smem(int n) { return (size_t)n * n * sizeof(double); }
+
+void launch_sparse_inv(const double* sp, int n_batch, int n, int nd, double* out, cudaStream_t st) {
+  const size_t smem = sparse_gj_smem(n);
+  cudaFuncSetAttribute(sparse_gj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  sparse_gj_kernel<<<dim3(nd, n_batch), 256, smem, st>>>(sp, n, nd, 0, out, nullptr, nullptr);
 }
 
 void launch_sparse_slogdet(const double* sp, int n, int nd, double* sign_part, double* ld_part,
                            double* sign_out, double* ld_out, cudaStream_t st) {
-  const size_t smem = 2 * (size_t)n * n * sizeof(double);
-  cudaFuncSetAttribute(sparse_lu_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  sparse_lu_kernel<<<nd, 128, smem, st>>>(sp, n, nd, 1, nullptr, sign_part, ld_part);
+  const size_t smem = sparse_gj_smem(n);
+  cudaFuncSetAttribute(sparse_gj_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  sparse_gj_kernel<<<dim3(nd, 1), 256, smem, st>>>(sp, n, nd, 1, nullptr, sign_part, ld_part);
   sparse_slogdet_reduce<<<1, 32, 0, st>>>(sign_part, ld_part, nd, sign_out, ld_out);
+}
+
+// Products with at least one block-diagonal operand (sparse.py:140-292), one
+// thread per output element, the fastest index of the output innermost so
+// that loads and stores coalesce.
+// sparse_dot_sparse (sparse.py:236-260): C[i][k][l] = sum_j A[i][j][l] B[j][k][l]
+__global__ void sparse_dot_sparse_kernel(const double* __restrict__ a, const double* __restrict__ b, int n, int m,
+                                         int p, int nd, double* __restrict__ c) {
+  const size_t total = (size_t)n * p * nd;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const int l = (int)(idx % nd);
+    const size_t ik = idx / nd;
+    const int i = (int)(ik / p), k = (int)(ik % p);
+    double acc = 0.0;
+    for (int j = 0; j < m; ++j) acc += a[((size_t)i * m + j) * nd + l] * b[((size_t)j * p + k) * nd + l];
+    c[idx] = acc;
+  }
+}
+
+// sparse_dot_dense (sparse.py:164-182): out[i nd + l][q] = sum_j A[i][j][l] D[j nd + l][q], D (m nd, K)
+__global__ void sparse_dot_dense_kernel(const double* __restrict__ a, int n, int m, int nd,
+                                        const double* __restrict__ d, int K, double* __restrict__ out) {
+  const size_t total = (size_t)n * nd * K;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const int q = (int)(idx % K);
+    const size_t row = idx / K;
+    const int i = (int)(row / nd), l = (int)(row % nd);
+    double acc = 0.0;
+    for (int j = 0; j < m; ++j) acc += a[((size_t)i * m + j) * nd + l] * d[((size_t)j * nd + l) * K + q];
+    out[idx] = acc;
+  }
+}
+
+// dense_dot_sparse (sparse.py:210-233): out[r][j nd + l] = sum_i D[r][i nd + l] A[i][j][l], D (R, n nd)
+__global__ void dense_dot_sparse_kernel(const double* __restrict__ d, int R, const double* __restrict__ a, int n,
+                                        int m, int nd, double* __restrict__ out) {
+  const size_t cols = (size_t)m * nd, total = (size_t)R * cols;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += (size_t)gridDim.x * blockDim.x) {
+    const size_t r = idx / cols, col = idx % cols;
+    const int j = (int)(col / nd), l = (int)(col % nd);
+    const double* dr = d + r * (size_t)n * nd;
+    double acc = 0.0;
+    for (int i = 0; i < n; ++i) acc += dr[(size_t)i * nd + l] * a[((size_t)i * m + j) * nd + l];
+    out[idx] = acc;
+  }
+}
+
+// FP64 C[M][N] = X[M][Kd] T[Kd][N], 16 x 16 tiles through shared memory (the
+// dense step of dense_dot_sparse_dot_dense, sparse.py:263-292)
+__global__ void __launch_bounds__(256) gemm_f64_kernel(const double* __restrict__ x, const double* __restrict__ t,
+                                                       int M, int Kd, int N, double* __restrict__ c) {
+  __shared__ double xs[16][17], ts[16][17];
+  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  const int row = blockIdx.y * 16 + ty, col = blockIdx.x * 16 + tx;
+  double acc = 0.0;
+  for (int k0 = 0; k0 < Kd; k0 += 16) {
+    xs[ty][tx] = (row < M && k0 + tx < Kd) ? x[(size_t)row * Kd + k0 + tx] : 0.0;
+    ts[ty][tx] = (k0 + ty < Kd && col < N) ? t[(size_t)(k0 + ty) * N + col] : 0.0;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < 16; ++k) acc += xs[ty][k] * ts[k][tx];
+    __syncthreads();
+  }
+  if (row < M && col < N) c[(size_t)row * N + col] = acc;
+}
+
+static unsigned grid_for(size_t total) {
+  size_t blocks = (total + 255) / 256;
+  if (blocks > 152 * 32) blocks = 152 * 32;
+  return blocks ? (unsigned)blocks : 1u;
+}
+
+void launch_sparse_dot_sparse(const double* a, const double* b, int n, int m, int p, int nd, double* c,
+                              cudaStream_t st) {
+  sparse_dot_sparse_kernel<<<grid_for((size_t)n * p * nd), 256, 0, st>>>(a, b, n, m, p, nd, c);
+}
+
+void launch_sparse_dot_dense(const double* a, int n, int m, int nd, const double* d, int K, double* out,
+                             cudaStream_t st) {
+  sparse_dot_dense_kernel<<<grid_for((size_t)n * nd * K), 256, 0, st>>>(a, n, m, nd, d, K, out);
+}
+
+void launch_dense_dot_sparse(const double* d, int R, const double* a, int n, int m, int nd, double* out,
+                             cudaStream_t st) {
+  dense_dot_sparse_kernel<<<grid_for((size_t)R * m * nd), 256, 0, st>>>(d, R, a, n, m, nd, out);
+}
+
+void launch_gemm_f64(const double* x, const double* t, int M, int Kd, int N, double* c, cudaStream_t st) {
+  dim3 grid((N + 15) / 16, (M + 15) / 16);
+  gemm_f64_kernel<<<grid, 256, 0, st>>>(x, t, M, Kd, N, c);
 }
 
 // sparse.to_dense (sparse.py:52-68)

@@ -98,12 +98,9 @@ class ChainModel:
         cov = torch.as_tensor(cov, dtype=torch.float64).to(self.device)
         if cov.shape != (self.n_cls, self.n_cls, self.n_ell):
             raise ValueError(f"covariance {tuple(cov.shape)}: expected sparse {(self.n_cls, self.n_cls, self.n_ell)}")
-        # per-ell inverse blocks as [n_ell, n_cls, n_cls]: libjcg's batched
-        # inverse (sparse.inv) up to its 80 x 80 block limit, torch's beyond
-        if self.n_cls <= 80:
-            self.prec = sparse_mod.inv(cov).permute(2, 0, 1).contiguous()
-        else:
-            self.prec = torch.linalg.inv(cov.permute(2, 0, 1)).contiguous()
+        # per-ell inverse blocks as [n_ell, n_cls, n_cls] (libjcg's sparse.inv;
+        # its block limit, 160, is above the 136 spectra of 16 tracers)
+        self.prec = sparse_mod.inv(cov).permute(2, 0, 1).contiguous()
         self.resident_bytes = (self.geo.numel() * self.geo.element_size() + self.data.numel() * 8
                                + self.prec.numel() * 8)
         self._addr = (ctypes.addressof(self.g), self.geo.data_ptr(), self.data.data_ptr(),

@@ -2,8 +2,9 @@
 
 Format (sparse.py:1-11): a 3-D array (ny, nx, ndiag) of ny x nx square blocks,
 each diagonal, the vector at [i, j] being the diagonal of block (i, j).
-``inv``, ``slogdet``, ``to_dense`` and matrix-vector ``dot`` run in libjcg
-(FP64); the other products of ``dot`` are torch einsums on the device.
+``inv``, ``slogdet``, ``to_dense`` and every product of ``dot`` (matrix-vector,
+sparse-dense, dense-sparse, sparse-sparse and the bilinear form) run in
+libjcg (FP64).
 """
 from __future__ import annotations
 
@@ -14,7 +15,8 @@ import torch
 
 from jax_cosmo_gb300 import _lib
 
-__all__ = ["is_sparse", "check_sparse", "to_dense", "dot", "inv", "slogdet", "det"]
+__all__ = ["is_sparse", "check_sparse", "to_dense", "dot", "inv", "inv_batched", "slogdet", "det"]
+MAX_N = 160  # JCG_SPARSE_MAX_N: block size limit of inv / slogdet
 
 
 def _t(x):
@@ -66,23 +68,48 @@ def vec_dot_sparse(vec, sparse):
 
 
 def sparse_dot_dense(sparse, dense):
+    """A @ D, A sparse (n, m, nd), D dense (m nd, k) -> (n nd, k) (sparse.py:164-182)."""
     sp, d = _t(sparse), _t(dense)
     n, m, nd = sp.shape
-    return torch.einsum("ijl,jlk->ilk", sp, d.reshape(m, nd, -1)).reshape(n * nd, -1)
+    d2 = d.reshape(m * nd, -1)
+    out = torch.empty(n * nd, d2.shape[1], dtype=torch.float64, device=sp.device)
+    _lib.call("jcg_sparse_dot_dense", _lib.ptr(sp), n, m, nd, _lib.ptr(d2), d2.shape[1], _lib.ptr(out),
+              _lib.stream_of(sp.device))
+    return out
 
 
 def dense_dot_sparse(dense, sparse):
+    """D @ A, D dense (r, n nd), A sparse (n, m, nd) -> (r, m nd) (sparse.py:210-233)."""
     sp, d = _t(sparse), _t(dense)
     n, m, nd = sp.shape
-    return torch.einsum("kil,ijl->kjl", d.reshape(-1, n, nd), sp).reshape(-1, m * nd)
+    d2 = d.reshape(-1, n * nd)
+    out = torch.empty(d2.shape[0], m * nd, dtype=torch.float64, device=sp.device)
+    _lib.call("jcg_dense_dot_sparse", _lib.ptr(d2), d2.shape[0], _lib.ptr(sp), n, m, nd, _lib.ptr(out),
+              _lib.stream_of(sp.device))
+    return out
 
 
 def sparse_dot_sparse(sparse1, sparse2):
-    return torch.einsum("ijl,jkl->ikl", _t(sparse1), _t(sparse2))
+    """A @ B, both sparse: (n, m, nd) @ (m, p, nd) -> (n, p, nd) (sparse.py:236-260)."""
+    a, b = _t(sparse1), _t(sparse2)
+    n, m, nd = a.shape
+    p = b.shape[1]
+    out = torch.empty(n, p, nd, dtype=torch.float64, device=a.device)
+    _lib.call("jcg_sparse_dot_sparse", _lib.ptr(a), n, m, p, nd, _lib.ptr(b), _lib.ptr(out),
+              _lib.stream_of(a.device))
+    return out
 
 
 def dense_dot_sparse_dot_dense(X, Y, Z):
-    return _t(X) @ sparse_dot_dense(Y, Z)
+    """Bilinear form X @ Y @ Z with Y sparse (sparse.py:263-292)."""
+    x, y, z = _t(X), _t(Y), _t(Z)
+    n, m, nd = y.shape
+    k = z.shape[1]
+    work = torch.empty(n * nd, k, dtype=torch.float64, device=y.device)
+    out = torch.empty(x.shape[0], k, dtype=torch.float64, device=y.device)
+    _lib.call("jcg_dense_dot_sparse_dot_dense", _lib.ptr(x), x.shape[0], _lib.ptr(y), n, m, nd, _lib.ptr(z), k,
+              _lib.ptr(work), _lib.ptr(out), _lib.stream_of(y.device))
+    return out
 
 
 def dot(*args):
@@ -120,6 +147,17 @@ def inv(sparse):
     n, _, nd = sp.shape
     out = torch.empty_like(sp)
     _lib.call("jcg_sparse_inv", _lib.ptr(sp), n, nd, _lib.ptr(out), _lib.stream_of(sp.device))
+    return out
+
+
+def inv_batched(sparse):
+    """``inv`` of a stack [B, n, n, nd] of sparse matrices in one launch."""
+    sp = _t(sparse)
+    if sp.dim() != 4 or sp.shape[1] != sp.shape[2]:
+        raise ValueError(f"expected [B, n, n, ndiag], got {tuple(sp.shape)}")
+    B, n, _, nd = sp.shape
+    out = torch.empty_like(sp)
+    _lib.call("jcg_sparse_inv_batched", _lib.ptr(sp), B, n, nd, _lib.ptr(out), _lib.stream_of(sp.device))
     return out
 
 

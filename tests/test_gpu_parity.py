@@ -330,6 +330,63 @@ def test_sparse_known_answers():
     assert float(jc.sparse.det(Xd)) == pytest.approx(float(np.linalg.det(jc.sparse.to_dense(Xd).cpu().numpy())), rel=1e-6)
 
 
+def test_sparse_products_known_answers():
+    """The product and bilinear-form cases of the reference's
+    tests/test_sparse.py (test_dot, test_bilinear), every product in libjcg,
+    against the dense products of to_dense."""
+    X1 = torch.tensor([[[1.0, 2], [3, 4], [5, 6]], [[4, 5], [6, 7], [8, 9]]], dtype=torch.float64)
+    X2 = torch.tensor([[[1.0, -2], [3, -4]], [[5, 4], [6, -7]], [[5, 6], [9, 8]]], dtype=torch.float64)
+    X1d, X2d = jc.sparse.to_dense(X1).cpu(), jc.sparse.to_dense(X2).cpu()
+    v1, v2 = torch.arange(6, dtype=torch.float64), torch.arange(4, dtype=torch.float64)
+    sp = jc.sparse
+    assert rel(sp.dot(X2, v2), X2d @ v2) < 1e-15
+    assert rel(sp.dot(X1, v1), X1d @ v1) < 1e-15
+    assert rel(sp.dot(v2, X1), v2 @ X1d) < 1e-15
+    assert rel(sp.dot(v1, X2), v1 @ X2d) < 1e-15
+    assert rel(sp.dot(X1, X2d), X1d @ X2d) < 1e-15
+    assert rel(sp.dot(X1d, X2), X1d @ X2d) < 1e-15
+    assert rel(sp.to_dense(sp.dot(X1, X2)), X1d @ X2d) < 1e-15
+    assert rel(sp.to_dense(sp.dot(X2, X1)), X2d @ X1d) < 1e-15
+    X12, X21 = sp.dot(X2, X1), sp.dot(X1, X2)
+    assert rel(sp.dot(X1d, X12, X2d), X1d @ (X2d @ X1d) @ X2d) < 1e-14
+    assert rel(sp.dot(X2d, X21, X1d), X2d @ (X1d @ X2d) @ X1d) < 1e-14
+
+
+def test_sparse_products_random_and_batched_inverse():
+    """Random float64 operands at covariance sizes: every product against the
+    dense product, the batched inverse against per-matrix inverses, and an
+    inverse at the 16-tracer block size (136) against torch.linalg.inv."""
+    def nrel(a, b):  # max error over the largest magnitude: entries cancel to ~0
+        a = a.detach().cpu() if isinstance(a, torch.Tensor) else torch.as_tensor(a)
+        b = b.detach().cpu()
+        return float((a - b).abs().max() / b.abs().max())
+
+    g = torch.Generator().manual_seed(5)
+    A = torch.randn(15, 9, 50, generator=g, dtype=torch.float64)
+    B = torch.randn(9, 7, 50, generator=g, dtype=torch.float64)
+    Ad, Bd = jc.sparse.to_dense(A).cpu(), jc.sparse.to_dense(B).cpu()
+    D = torch.randn(9 * 50, 33, generator=g, dtype=torch.float64)
+    E = torch.randn(21, 15 * 50, generator=g, dtype=torch.float64)
+    assert nrel(jc.sparse.dot(A, D), Ad @ D) < 1e-12
+    assert nrel(jc.sparse.dot(E, A), E @ Ad) < 1e-12
+    assert nrel(jc.sparse.to_dense(jc.sparse.dot(A, B)), Ad @ Bd) < 1e-12
+    Z = torch.randn(7 * 50, 11, generator=g, dtype=torch.float64)
+    assert nrel(jc.sparse.dot(E, jc.sparse.dot(A, B), Z), E @ (Ad @ Bd) @ Z) < 1e-11
+    # SPD blocks: batched inverse == one inverse per matrix; n = 136 vs torch
+    M = torch.randn(3, 20, 20, 8, generator=g, dtype=torch.float64)
+    S = torch.einsum("bikl,bjkl->bijl", M, M) + 20 * torch.eye(20, dtype=torch.float64)[None, :, :, None]
+    inv_b = jc.sparse.inv_batched(S).cpu()
+    for b in range(3):
+        assert torch.equal(inv_b[b], jc.sparse.inv(S[b]).cpu())
+        assert nrel(inv_b[b].permute(2, 0, 1), torch.linalg.inv(S[b].permute(2, 0, 1))) < 1e-12
+    M = torch.randn(136, 136, 4, generator=g, dtype=torch.float64)
+    S = torch.einsum("ikl,jkl->ijl", M, M) + 136 * torch.eye(136, dtype=torch.float64)[:, :, None]
+    assert nrel(jc.sparse.inv(S).cpu().permute(2, 0, 1), torch.linalg.inv(S.permute(2, 0, 1))) < 1e-11
+    sign, ld = jc.sparse.slogdet(S)
+    s_ref, ld_ref = torch.linalg.slogdet(jc.sparse.to_dense(S).cpu())
+    assert float(sign) == float(s_ref) and abs(float(ld) - float(ld_ref)) < 1e-10 * abs(float(ld_ref))
+
+
 def test_fast_moments_match_full_moments():
     """fp32c mode evaluates the halofit moments with exp only where it matters
     (Taylor prefix sums below y^2 = 1, terms under 1e-20 dropped above
