@@ -147,7 +147,7 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -325,6 +325,24 @@ def gpu_arm(args, rank, world, device):
     res["jacobian"]["fp32c"]["cl_max_rel_err_vs_fp64"] = float(((c32 - c64) / c64).abs().max())
     res["jacobian"]["fp32c"]["jac_max_err_vs_fp64"] = float(((j32 - j64).abs() / scale).max())
     res["jacobian"]["fp32c"]["jac_err_note"] = "max |J32 - J64| / max |J64| per (cosmology, parameter)"
+    # C_ell + the gradient of a scalar function of C_ell (a likelihood's
+    # backward pass): the vector-Jacobian product, fp32c, with a seeded cotangent
+    from jax_cosmo_gb300.autodiff import vjp_device
+
+    gen = torch.Generator(device=device).manual_seed(SEED)
+    vb = torch.randn(B, n_cls, n_ell, generator=gen, dtype=torch.float64, device=device)
+    kv = max(1, min(args.steps, 5))
+    tv, _ = timed(lambda: vjp_device(params, ell_np, probes, vb, 512, "fp32c", want_cl=True), kv, 1)
+    g32, c32v = vjp_device(p64, ell_np, probes, vb[:64], 512, "fp32c", want_cl=True)
+    gref = torch.einsum("bpl,bpld->bd", vb[:64], j64)
+    gscale = torch.einsum("bpl,bpld->bd", vb[:64].abs(), j64.abs())
+    res["jacobian"]["fp32c_vjp"] = {
+        "batch": B, "ms_per_step": tv / kv, "steps": kv, "cl_grad_per_s": ncl_step / (tv / kv * 1e-3),
+        "what": "C_ell and the gradient of a scalar of C_ell (vector-Jacobian product with a seeded cotangent; "
+                "the Jacobian is not formed)",
+        "grad_max_err_vs_fp64": float(((g32 - gref).abs() / gscale).max()),
+        "cl_max_rel_err_vs_fp64": float(((c32v - c64) / c64).abs().max()),
+        "err_note": "max |g32 - J64^T v| / (|v|^T |J64|) per (cosmology, parameter)"}
     del j64, j32
 
     # the non-default operator points on the same workload (fp32c), each with
@@ -418,7 +436,8 @@ def accuracy_arm(device):
     return out
 
 
-def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, seed=SEED, n_check=256):
+def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, seed=SEED, n_check=256,
+                sweep=((0.0, 5.0), (0.5, 5.0))):
     """64 synthetic HMC chains against the continuous-batching server.
 
     Each chain (seeded): 1-10 tracers (WeakLensing / NumberCounts mix, smail_nz
@@ -461,8 +480,38 @@ def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, 
         models.append(serving.ChainModel(probes, ell, data, fiducial=start))
         pos.append(p0)
         rngs.append(rng)
+    pos0 = [p.copy() for p in pos]
+    st = run_load(device, models, pos, rngs, lo, hi, width, think_ms, duration_s, warm_s, n_check)
+    st["load_sweep"] = []
+    for tm, dur in sweep:
+        pos = [p.copy() for p in pos0]
+        s2 = run_load(device, models, pos, rngs, lo, hi, width, tm, dur, 2.0, 0)
+        st["load_sweep"].append({"think_ms_mean": tm, "duration_s": dur, "requests_per_s": s2["requests_per_s"],
+                                 "p50_ms": s2["p50_ms"], "p99_ms": s2["p99_ms"], "mean_batch": s2["mean_batch"],
+                                 "max_batch": s2["max_batch"], "completed": s2["completed"]})
+    st.update({"chains": n_chains, "think_ms_mean": think_ms, "duration_s": duration_s,
+               "tracers_per_chain": [int(m.g.n_tracers) for m in models],
+               "n_ell_per_chain": [int(m.n_ell) for m in models], "precision": "fp32c", "dtype": "f32c+f64"})
+    return st
+
+
+def run_load(device, models, pos, rngs, lo, hi, width, think_ms, duration_s, warm_s, n_check):
+    """One load point: each chain submits its next request an exponential
+    think time (mean think_ms; 0 = at once) after its previous result."""
+    import heapq
+    import queue
+
+    import torch
+
+    import jax_cosmo_gb300 as jc
+    from jax_cosmo_gb300 import serving
+
+    n_chains = len(models)
     done_q = queue.Queue()
     srv = serving.Server(device=device, hbm_budget=8 << 30, max_batch=256, n_streams=2).start()
+
+    def think(c):
+        return rngs[c].exponential(think_ms * 1e-3) if think_ms > 0 else 0.0
 
     def submit(c):
         step = rngs[c].normal(0.0, 0.01, 8) * width
@@ -471,7 +520,7 @@ def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, 
         f.add_done_callback(lambda _f, c=c: done_q.put(c))
         return f
 
-    heap = [(time.perf_counter() + rngs[c].exponential(think_ms * 1e-3), c) for c in range(n_chains)]
+    heap = [(time.perf_counter() + think(c), c) for c in range(n_chains)]
     heapq.heapify(heap)
     t_start = time.perf_counter()
     t_measure = t_start + warm_s
@@ -493,17 +542,19 @@ def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, 
         timeout = max(0.0, heap[0][0] - now) if heap else 0.01
         try:
             c = done_q.get(timeout=min(timeout, 0.01))
-            heapq.heappush(heap, (time.perf_counter() + rngs[c].exponential(think_ms * 1e-3), c))
+            heapq.heappush(heap, (time.perf_counter() + think(c), c))
             while True:
                 c = done_q.get_nowait()
-                heapq.heappush(heap, (time.perf_counter() + rngs[c].exponential(think_ms * 1e-3), c))
+                heapq.heappush(heap, (time.perf_counter() + think(c), c))
         except queue.Empty:
             pass
     st = srv.stats()
     srv.stop()
+    if not sample:
+        return st
     # served log-likelihoods and gradients against the plain float64 method
     # (public API: angular_cl_jacobian in FP64, then -J^T P r), every sampled request
-    err_ll, err_g = [], []
+    err_ll, err_g, err_gs = [], [], []
     for c, p, f in sample:
         r = f.result()
         m = models[c]
@@ -514,16 +565,18 @@ def serving_arm(device, duration_s=10.0, warm_s=3.0, n_chains=64, think_ms=2.0, 
         g = -torch.einsum("pld,pl->d", jac, pr).cpu().numpy()
         err_ll.append(abs(r.loglike - ll) / abs(ll))
         err_g.append(float(np.max(np.abs(np.asarray(r.grad) - g)) / np.max(np.abs(g))))
+        gs = torch.einsum("pld,pl->d", jac.abs(), pr.abs()).cpu().numpy()
+        err_gs.append(float(np.max(np.abs(np.asarray(r.grad) - g) / gs)))
     st["accuracy_vs_fp64"] = {
         "checked_requests": len(sample),
         "loglike_max_rel_err": float(max(err_ll)), "loglike_median_rel_err": float(np.median(err_ll)),
         "grad_max_err": float(max(err_g)), "grad_median_err": float(np.median(err_g)),
-        "grad_err_note": "max |g - g64| / max |g64| over the 8 Cosmology leaves, per request",
+        "grad_scaled_max_err": float(max(err_gs)), "grad_scaled_median_err": float(np.median(err_gs)),
+        "grad_err_note": "grad_max_err: max |g - g64| / max |g64| over the 8 Cosmology leaves, per request "
+                         "(large where the gradient cancels near a chain's maximum); grad_scaled: "
+                         "max_d |g_d - g64_d| / sum_{p,l} |J64_pld| |(P r)_pl|, the error against the size of "
+                         "the summed terms",
         "reference": "public API in float64: angular_cl_jacobian, then logL = -r^T P r / 2, grad = -J^T P r"}
-    st.update({"chains": n_chains, "think_ms_mean": think_ms, "duration_s": duration_s,
-               "tracers_per_chain": [int(m.g.n_tracers) for m in models],
-               "n_ell_per_chain": [int(m.n_ell) for m in models], "precision": srv.precision,
-               "dtype": "f32c+f64" if srv.precision == "fp32c" else "f64"})
     return st
 
 

@@ -243,6 +243,21 @@ int jcg_angular_cl_jacobian_dir(const jcg_geometry* g, const void* geo_dev, cons
                                 int n_cosmo, int precision, int gamma_dir, double* cl_dev, double* jac_dev,
                                 void* workspace, size_t workspace_bytes, cudaStream_t stream);
 
+/* Vector-Jacobian product of angular_cl, the form jax.grad takes for a scalar
+ * function of C_ell (README.md:14-27; angular_cl.py:49-98):
+ *   grad_dev [n_cosmo][8] = sum_{p,l} cl_bar_dev[b][p][l] dC_p(l)/dtheta
+ * over the 8 Cosmology leaves (gamma_dir as in jcg_angular_cl_jacobian_dir),
+ * and cl_dev (may be NULL) the C_ell themselves.  The matching adjoint entry
+ * point of angular_cl: a likelihood's backward pass passes d logL / dC_ell
+ * as cl_bar.  JCG_FP32C: tables with tangents, then the Limber integrand's
+ * reverse sweep weighted by sum_p cl_bar_p(l) M_p(a) and summed over ell,
+ * projected on the 8 directions once per Limber node in a; the Jacobian is
+ * never formed.  JCG_FP64: the FP64 Jacobian contracted with cl_bar. */
+int jcg_vjp_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t* bytes);
+int jcg_angular_cl_vjp(const jcg_geometry* g, const void* geo_dev, const double* params_dev, int n_cosmo,
+                       int precision, int gamma_dir, const double* cl_bar_dev, double* cl_dev, double* grad_dev,
+                       void* workspace, size_t workspace_bytes, cudaStream_t stream);
+
 /* jcg_angular_cl_jacobian in FP64 with the branch of the halofit root find
  * exposed.  The reference finds the non-linear scale with an interpolation
  * whose segment is an argmin over the sigma^2(R) table (power.py:112-115,
@@ -273,7 +288,13 @@ int jcg_angular_cl_jacobian_branch(const jcg_geometry* g, const void* geo_dev, c
  *   JCG_REQ_LOGLIKE_GRAD: out -> [9] = logL = -r^T P r / 2 with r = C_ell - data
  *     and its gradient -(dC/dtheta)^T P r over the 8 Cosmology leaves; data
  *     [n_cls*n_ell] in (cls, ell) order, prec [n_ell][n_cls][n_cls] the inverse
- *     covariance blocks; cl / jac optional outputs (NULL: workspace). */
+ *     covariance blocks; cl optional output (NULL: workspace).  FP64: from
+ *     the Jacobian (jac an optional output); JCG_FP32C: C_ell, then the
+ *     product of the cotangent -P r with dC/dtheta (jcg_angular_cl_vjp's
+ *     kernels), jac not written.
+ * The request tables reach the device through a pinned staging ring of the
+ * calling host thread, so the call does not wait for the stream (it waits
+ * only if 16 earlier calls of the thread are still queued). */
 #define JCG_REQ_CL 0
 #define JCG_REQ_JACOBIAN 1
 #define JCG_REQ_LOGLIKE_GRAD 2

@@ -124,6 +124,8 @@ SIGNATURES = {
     "jcg_angular_cl_jacobian": [_PG, _P, _P, _I, _I, _P, _P, _P, _SZ, _P],
     "jcg_angular_cl_jacobian_dir": [_PG, _P, _P, _I, _I, _I, _P, _P, _P, _SZ, _P],
     "jcg_angular_cl_jacobian_branch": [_PG, _P, _P, _I, _P, _P, _P, _P, _P, _SZ, _P],
+    "jcg_vjp_workspace_size": [_PG, _I, _I, _PSZ],
+    "jcg_angular_cl_vjp": [_PG, _P, _P, _I, _I, _I, _P, _P, _P, _P, _SZ, _P],
     "jcg_requests_workspace_size": [_P, _I, _I, _I, _PSZ, _PSZ],
     "jcg_requests_run": [_P, _I, _I, _I, _P, _SZ, _P],
     "jcg_sparse_inv_batched": [_P, _I, _I, _I, _P, _P],

@@ -4,10 +4,10 @@ jax_cosmo differentiates its whole stack with ``jax.grad`` / ``jax.hessian``
 (README.md:14-27).  Here the three functions of the path are
 ``torch.autograd.Function``s whose backward passes run in libjcg:
 
-* ``angular_cl``: backward = v^T J with J = dC_ell/dtheta from
-  ``jcg_angular_cl_jacobian`` (tables differentiated forward, the Limber
-  integrand by a hand-written reverse sweep, FP64; theta = the 8 Cosmology
-  leaves of core.py:98-108);
+* ``angular_cl``: backward = v^T J by ``jcg_angular_cl_vjp`` (tables
+  differentiated forward, the Limber integrand by a hand-written reverse
+  sweep weighted by the cotangent, so that fp32c never forms J; theta = the
+  8 Cosmology leaves of core.py:98-108);
 * ``gaussian_cl_covariance``: the Knox formula (angular_cl.py:144-147) is a
   product of two C_ell, its vector-Jacobian product is applied with index
   additions on the device;
@@ -61,6 +61,31 @@ def jacobian_device(params, ell, probes, n_limber=512, precision="fp64", physics
     return cl, jac
 
 
+def vjp_device(params, ell, probes, cl_bar, n_limber=512, precision="fp64", physics=0, gamma_dir=-1,
+               want_cl=False):
+    """Vector-Jacobian product of angular_cl for [B, 8] params (``jcg_angular_cl_vjp``):
+    grad [B, 8] = sum_{p,l} cl_bar[b, p, l] dC_p(l)/dtheta, and C_ell [B, n_cls, n_ell]
+    when ``want_cl``.  fp32c forms no Jacobian (the Limber integrand's reverse
+    sweep weighted by the cotangent); fp64 contracts the FP64 Jacobian."""
+    from jax_cosmo_gb300.angular_cl import _precision_code
+
+    prec = _precision_code(precision)
+    device = params.device
+    g, geo, _ = _geometry.get_geometry(probes, ell, n_limber, device, physics)
+    B = params.shape[0]
+    n_cls = _geometry.n_cls_of(g)
+    wsz = ctypes.c_size_t()
+    _lib.call("jcg_vjp_workspace_size", ctypes.byref(g), B, prec, ctypes.byref(wsz))
+    ws = _lib.workspace(wsz.value, device)
+    vb = cl_bar.to(device=device, dtype=torch.float64).expand(B, n_cls, g.n_ell).contiguous()
+    grad = torch.empty(B, len(PARAM_ORDER), dtype=torch.float64, device=device)
+    cl = torch.empty(B, n_cls, g.n_ell, dtype=torch.float64, device=device) if want_cl else None
+    _lib.call("jcg_angular_cl_vjp", ctypes.byref(g), _lib.ptr(geo), _lib.ptr(params.contiguous()), B, prec,
+              int(gamma_dir), _lib.ptr(vb), _lib.ptr(cl), _lib.ptr(grad), _lib.ptr(ws), ctypes.c_size_t(ws.numel()),
+              _lib.stream_of(device))
+    return (grad, cl) if want_cl else grad
+
+
 class _AngularCl(torch.autograd.Function):
     @staticmethod
     def forward(ctx, params, ell, probes, precision, n_limber, physics):
@@ -76,13 +101,11 @@ class _AngularCl(torch.autograd.Function):
         ell, probes, n_limber, precision, physics = ctx.meta
         p = params.detach().contiguous()
         g64 = gcl.to(torch.float64)
-        _, jac = jacobian_device(p, ell, probes, n_limber, precision, physics)
-        gp = torch.einsum("bpl,bpld->bd", g64, jac)
+        gp = vjp_device(p, ell, probes, g64, n_limber, precision, physics)
         if params.shape[1] > gp.shape[1]:
-            # gamma (the 9th column): its derivative from a second sweep with
-            # the gamma tangent in direction 0
-            _, jg = jacobian_device(p, ell, probes, n_limber, precision, physics, gamma_dir=0)
-            gp = torch.cat([gp, torch.einsum("bpl,bpl->b", g64, jg[..., 0])[:, None]], dim=1)
+            # gamma (the 9th leaf): a second product with the gamma tangent in direction 0
+            gg = vjp_device(p, ell, probes, g64, n_limber, precision, physics, gamma_dir=0)
+            gp = torch.cat([gp, gg[:, :1]], dim=1)
         return gp, None, None, None, None, None
 
 

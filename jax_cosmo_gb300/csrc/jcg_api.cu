@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "jcg_internal.cuh"
+#include "jcg_grad.cuh"
 
 namespace jcg {
 void launch_covariance(const double* ell, int n_ell, int n_tr, const double* cl,
@@ -84,6 +85,51 @@ static int const_tables(ConstTables** out) {
   *out = g_const_ptr[dev];
   return JCG_OK;
 }
+
+// ------------------------------------------------ pinned staging ring -------
+// Small host tables (the item arrays of ragged requests) reach the device
+// through pinned host memory: a copy from pageable memory may wait for the
+// stream before it returns, a copy from pinned memory does not.  Each host
+// thread owns a ring of slots; a slot is reused once the event recorded after
+// its copy has completed, which only waits when a whole ring of copies is
+// still queued on the GPU.  The buffers are kept until the process exits.
+namespace jcg {
+namespace {
+constexpr int STAGE_SLOTS = 16;
+struct StageSlot {
+  void* buf = nullptr;
+  size_t cap = 0;
+  cudaEvent_t ev = nullptr;
+  bool used = false;
+};
+struct StageRing {
+  StageSlot slot[STAGE_SLOTS];
+  int next = 0;
+};
+}  // namespace
+
+cudaError_t stage_h2d(void* dst_dev, const void* src_host, size_t bytes, cudaStream_t st) {
+  static thread_local StageRing ring;
+  StageSlot& s = ring.slot[ring.next];
+  ring.next = (ring.next + 1) % STAGE_SLOTS;
+  cudaError_t e;
+  if (s.used && (e = cudaEventSynchronize(s.ev)) != cudaSuccess) return e;
+  if (!s.ev && (e = cudaEventCreateWithFlags(&s.ev, cudaEventDisableTiming)) != cudaSuccess) return e;
+  if (s.cap < bytes) {
+    if (s.buf) cudaFreeHost(s.buf);
+    s.buf = nullptr;
+    s.cap = 0;
+    const size_t cap = bytes < 65536 ? 65536 : bytes * 2;
+    if ((e = cudaHostAlloc(&s.buf, cap, cudaHostAllocDefault)) != cudaSuccess) return e;
+    s.cap = cap;
+  }
+  memcpy(s.buf, src_host, bytes);
+  if ((e = cudaMemcpyAsync(dst_dev, s.buf, bytes, cudaMemcpyHostToDevice, st)) != cudaSuccess) return e;
+  if ((e = cudaEventRecord(s.ev, st)) != cudaSuccess) return e;
+  s.used = true;
+  return cudaSuccess;
+}
+}  // namespace jcg
 
 // ----------------------------------------------------------- geometry -------
 static int64_t align8(int64_t v) { return (v + 7) & ~int64_t(7); }  // 64-byte units
@@ -802,6 +848,40 @@ extern "C" int jcg_angular_cl_jacobian_branch(const jcg_geometry* g, const void*
   return cuda_check("angular_cl_jacobian_branch");
 }
 
+extern "C" int jcg_vjp_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t* bytes) {
+  if (!bytes) return fail(JCG_ERR_ARG, "bytes is NULL");
+  if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  if (precision != JCG_FP64 && precision != JCG_FP32C) return fail(JCG_ERR_ARG, "precision = %d", precision);
+  GeoHeader h;
+  const int rc = make_header(g, &h);
+  if (rc) return rc;
+  *bytes = vjp_workspace_bytes(h, n_cosmo, precision);
+  return JCG_OK;
+}
+
+extern "C" int jcg_angular_cl_vjp(const jcg_geometry* g, const void* geo, const double* params, int n_cosmo,
+                                  int precision, int gamma_dir, const double* cl_bar, double* cl, double* grad,
+                                  void* ws, size_t ws_bytes, cudaStream_t stream) {
+  GeoHeader h;
+  int rc = make_header(g, &h);
+  if (rc) return rc;
+  if (gamma_dir < -1 || gamma_dir >= 8) return fail(JCG_ERR_ARG, "gamma_dir = %d", gamma_dir);
+  if (gamma_dir >= 0 && !growth_gamma(h.physics))
+    return fail(JCG_ERR_ARG, "gamma_dir = %d without JCG_GROWTH_GAMMA", gamma_dir);
+  if (!geo || !params || !cl_bar || !grad || !ws) return fail(JCG_ERR_ARG, "NULL pointer");
+  if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  if (precision != JCG_FP64 && precision != JCG_FP32C) return fail(JCG_ERR_ARG, "precision = %d", precision);
+  if (h.custom_nodes) return fail(JCG_ERR_ARG, "a geometry with caller redshift nodes has no Limber grid");
+  const size_t need = vjp_workspace_bytes(h, n_cosmo, precision);
+  if (ws_bytes < need) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need);
+  if (((uintptr_t)ws) % 256 != 0) return fail(JCG_ERR_ARG, "workspace must be 256-byte aligned");
+  ConstTables* c = nullptr;
+  if ((rc = const_tables(&c))) return rc;
+  vjp_run(static_cast<const GeoHeader*>(geo), h, params, n_cosmo, precision, cl_bar, cl, grad, ws, c, stream,
+          gamma_dir);
+  return cuda_check("angular_cl_vjp");
+}
+
 // ------------------------------------------------------ ragged requests -----
 namespace {
 
@@ -850,10 +930,15 @@ int plan_requests(const jcg_request* reqs, int n, int mode, int precision, ReqPl
     q.geo = static_cast<const GeoHeader*>(r.geo_dev);
     q.params = r.params_dev;
     q.cl = r.cl_dev;
-    q.jac = r.jac_dev;
+    q.jac = mode == JCG_REQ_LOGLIKE_GRAD && precision == JCG_FP32C ? nullptr : r.jac_dev;
+    q.out = r.out_dev;
+    q.vbar = nullptr;
   }
   return JCG_OK;
 }
+
+// fp32c log-likelihood requests take the vector-Jacobian form
+bool vjp_mode(int mode, int precision) { return mode == JCG_REQ_LOGLIKE_GRAD && precision == JCG_FP32C; }
 
 size_t cl_listed_bytes(const ReqPlan& p, int precision) {
   size_t o = align256(sizeof(Item) * p.hdr.size());
@@ -881,6 +966,10 @@ extern "C" int jcg_requests_workspace_size(const jcg_request* reqs, int n, int m
     return JCG_OK;
   }
   const size_t extra = mode == JCG_REQ_LOGLIKE_GRAD ? ll_extra_bytes(plan, n) : 0;
+  if (vjp_mode(mode, precision)) {
+    *bytes_min = *bytes_full = extra + grad_listed_bytes(plan.greq.data(), n, 1, precision, true);
+    return JCG_OK;
+  }
   const int ns = grad_listed_auto_split(plan.greq.data(), n, precision);
   *bytes_min = extra + grad_listed_bytes(plan.greq.data(), n, 1, precision);
   *bytes_full = extra + grad_listed_bytes(plan.greq.data(), n, ns, precision);
@@ -931,10 +1020,8 @@ extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, int pr
       b.max_cls = max(b.max_cls, h.n_cls);
       b.max_tr = max(b.max_tr, h.n_tr);
     }
-    // pageable source: staged before the call returns
-    if (cudaMemcpyAsync(dev_items, items.data(), sizeof(Item) * (size_t)n, cudaMemcpyHostToDevice,
-                        stream) != cudaSuccess)
-      return cuda_check("request table copy");
+    if (cudaError_t e = stage_h2d(dev_items, items.data(), sizeof(Item) * (size_t)n, stream))
+      return fail(JCG_ERR_CUDA, "request table copy: %s", cudaGetErrorString(e));
     b.n_items = n;
     b.listed = 1;
     b.items = dev_items;
@@ -946,11 +1033,13 @@ extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, int pr
     return cuda_check("requests angular_cl");
   }
   const size_t extra = mode == JCG_REQ_LOGLIKE_GRAD ? ll_extra_bytes(plan, n) : 0;
-  const size_t need1 = extra + grad_listed_bytes(plan.greq.data(), n, 1, precision);
+  const bool vjp = vjp_mode(mode, precision);
+  const size_t need1 = extra + grad_listed_bytes(plan.greq.data(), n, 1, precision, vjp);
   if (ws_bytes < need1) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, need1);
-  int ns = grad_listed_auto_split(plan.greq.data(), n, precision);
+  int ns = vjp ? 1 : grad_listed_auto_split(plan.greq.data(), n, precision);
   while (ns > 1 && extra + grad_listed_bytes(plan.greq.data(), n, ns, precision) > ws_bytes) --ns;
-  if (cudaError_t e = grad_run_listed(plan.greq.data(), n, ns, precision, base + extra, c, stream))
+  static thread_local GradBatch vgb;
+  if (cudaError_t e = grad_run_listed(plan.greq.data(), n, ns, precision, base + extra, c, stream, vjp, &vgb))
     return fail(JCG_ERR_CUDA, "requests jacobian: %s", cudaGetErrorString(e));
   if (mode == JCG_REQ_LOGLIKE_GRAD) {
     static thread_local std::vector<ReqLL> ll;
@@ -960,6 +1049,7 @@ extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, int pr
     for (int i = 0; i < n; ++i) {
       ll[i].cl = plan.greq[i].cl;
       ll[i].jac = plan.greq[i].jac;
+      ll[i].vbar = plan.greq[i].vbar;
       ll[i].data = reqs[i].data_dev;
       ll[i].prec = reqs[i].prec_dev;
       ll[i].out = reqs[i].out_dev;
@@ -971,10 +1061,11 @@ extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, int pr
       max_cls = max(max_cls, ll[i].n_cls);
     }
     ReqLL* dev_ll = reinterpret_cast<ReqLL*>(base);
-    if (cudaMemcpyAsync(dev_ll, ll.data(), sizeof(ReqLL) * (size_t)n, cudaMemcpyHostToDevice, stream) !=
-        cudaSuccess)
-      return cuda_check("request loglike table copy");
+    if (cudaError_t e = stage_h2d(dev_ll, ll.data(), sizeof(ReqLL) * (size_t)n, stream))
+      return fail(JCG_ERR_CUDA, "request loglike table copy: %s", cudaGetErrorString(e));
     launch_request_loglike(dev_ll, n, max_tiles, max_cls, stream);
+    // fp32c: the gradient as the product of the cotangents -P r with dC/dtheta
+    if (vjp) launch_vjp32_grad(vgb, stream);
   }
   return cuda_check("requests jacobian");
 }

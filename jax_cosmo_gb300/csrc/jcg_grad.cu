@@ -1665,7 +1665,7 @@ __global__ void __launch_bounds__(32 * NDIR) grad_growth_gamma_kernel(GradBatch 
   }
 }
 
-void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
+void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
   const size_t smt = grad_tables_smem();
   if (gb.n_items <= GNODE_MAX_ITEMS)
     grad_scalars_warp_kernel<<<gb.n_items, 16 * NDIR, 0, st>>>(gb);
@@ -1692,12 +1692,19 @@ void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
     dim3 grw((gb.na + 31) / 32, gb.n_items);
     grad_rows_kernel<<<grw, 256, 0, st>>>(gb, c);
   }
-  dim3 gr((gb.na + 7) / 8, gb.n_items);
   if (gb.precision == JCG_FP32C) {
     launch_grad_kern32(gb, c, st);
+  } else {
+    dim3 gr((gb.na + 7) / 8, gb.n_items);
+    grad_kern_kernel<<<gr, 256, 0, st>>>(gb, c);
+  }
+}
+
+void launch_grad(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
+  launch_grad_front(gb, c, st);
+  if (gb.precision == JCG_FP32C) {
     launch_grad_limber32(gb, c, st);
   } else {
-    grad_kern_kernel<<<gr, 256, 0, st>>>(gb, c);
     const int lt = grad_limber_tile(gb.n_ell, gb.n_cls);
     const size_t sml = grad_limber_smem(gb.n_cls, lt);
     cudaFuncSetAttribute(grad_limber_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sml);
@@ -1772,6 +1779,111 @@ size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
   o += al256(sizeof(double) * (size_t)ns * n_cosmo * h.n_cls * h.n_ell * (NDIR + 1));
   o += gnode_bytes(n_cosmo, precision);
   return o;
+}
+
+// ------------------------------------------------- vector-Jacobian product --
+// FP64: the Jacobian, then grad[b][d] = sum_i vbar[b][i] jac[b][i][d] (one CTA
+// per cosmology, fixed-order sums).
+__global__ void vjp_contract_kernel(const double* __restrict__ jac, const double* __restrict__ vbar, int per,
+                                    double* __restrict__ grad) {
+  const int b = blockIdx.x;
+  const double* J = jac + (size_t)b * per * NDIR;
+  const double* v = vbar + (size_t)b * per;
+  double acc[NDIR];
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) acc[d] = 0.0;
+  for (int i = threadIdx.x; i < per; i += blockDim.x) {
+    const double w = v[i];
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) acc[d] += w * J[(size_t)i * NDIR + d];
+  }
+  __shared__ double red[8][NDIR];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) {
+    double x = acc[d];
+    for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+    if (lane == 0) red[warp][d] = x;
+  }
+  __syncthreads();
+  if (threadIdx.x < NDIR) {
+    double x = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) x += red[w][threadIdx.x];
+    grad[(size_t)b * NDIR + threadIdx.x] = x;
+  }
+}
+
+static size_t vjp32_item_bytes(const GeoHeader& h) {
+  const size_t per = (size_t)h.n_cls * h.n_ell;
+  const size_t nch = (size_t)vjp_chunks(h.na);
+  return al256(sizeof(float) * nch * per) + al256(sizeof(double) * nch * NDIR);
+}
+
+size_t vjp_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
+  const size_t per = (size_t)h.n_cls * h.n_ell;
+  if (precision != JCG_FP32C)
+    return grad_workspace_bytes(h, n_cosmo, precision) + al256(sizeof(double) * per * NDIR * (size_t)n_cosmo) +
+           (n_cosmo > 0 ? al256(sizeof(double) * per * (size_t)n_cosmo) : 0);
+  GeoHeader hb = h;
+  hb.na = h.na * n_cosmo;
+  size_t o = al256(sizeof(TabD) * (size_t)n_cosmo);
+  o += ptt_bytes(precision) * n_cosmo;
+  o += rows_bytes(hb, precision);
+  o += kern_bytes(hb, precision);
+  o += al256(sizeof(float) * (size_t)vjp_chunks(h.na) * per * n_cosmo);
+  o += al256(sizeof(double) * (size_t)vjp_chunks(h.na) * NDIR * n_cosmo);
+  o += gnode_bytes(n_cosmo, precision);
+  return o;
+}
+
+void vjp_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, int precision,
+             const double* vbar, double* cl, double* grad, void* ws, const ConstTables* c, cudaStream_t st,
+             int gamma_dir) {
+  char* base = static_cast<char*>(ws);
+  const size_t per = (size_t)h.n_cls * h.n_ell;
+  if (precision != JCG_FP32C) {
+    const size_t gws = grad_workspace_bytes(h, n_cosmo, precision);
+    double* jac = reinterpret_cast<double*>(base + gws);
+    double* cl_ws = reinterpret_cast<double*>(base + gws + al256(sizeof(double) * per * NDIR * (size_t)n_cosmo));
+    grad_run(geo, h, params, n_cosmo, precision, cl ? cl : cl_ws, jac, ws, c, st, gamma_dir);
+    vjp_contract_kernel<<<n_cosmo, 256, 0, st>>>(jac, vbar, (int)per, grad);
+    return;
+  }
+  GradBatch gb;
+  memset(&gb, 0, sizeof(gb));
+  gb.gamma_dir = gamma_dir;
+  gb.n_items = n_cosmo;
+  gb.precision = precision;
+  gb.params = params;
+  gb.geo = geo;
+  GeoHeader hb = h;
+  hb.na = h.na * n_cosmo;
+  size_t o = 0;
+  gb.tab = reinterpret_cast<TabD*>(base + o);
+  o += al256(sizeof(TabD) * (size_t)n_cosmo);
+  gb.ptt = reinterpret_cast<double*>(base + o);
+  o += ptt_bytes(precision) * n_cosmo;
+  gb.rowg = reinterpret_cast<float*>(base + o);
+  o += rows_bytes(hb, precision);
+  gb.kernf = reinterpret_cast<float*>(base + o);
+  o += kern_bytes(hb, precision);
+  gb.cpart = reinterpret_cast<float*>(base + o);
+  o += al256(sizeof(float) * (size_t)vjp_chunks(h.na) * per * n_cosmo);
+  gb.gpart = reinterpret_cast<double*>(base + o);
+  o += al256(sizeof(double) * (size_t)vjp_chunks(h.na) * NDIR * n_cosmo);
+  gb.gnode = gnode_bytes(n_cosmo, precision) ? reinterpret_cast<double*>(base + o) : nullptr;
+  gb.vbar = vbar;
+  gb.grad = grad;
+  gb.cl = cl;
+  gb.na = h.na;
+  gb.n_tr = h.n_tr;
+  gb.n_cls = h.n_cls;
+  gb.n_ell = h.n_ell;
+  gb.n_split = 1;
+  gb.physics_or = h.physics;
+  launch_grad_front(gb, c, st);
+  if (cl) launch_vjp32_cl(gb, st);
+  if (vbar && grad) launch_vjp32_grad(gb, st);
 }
 
 void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, int precision,
@@ -1849,14 +1961,30 @@ int grad_listed_auto_split(const GradReq* r, int n, int precision) {
   return ns < 1 ? 1 : ns;
 }
 
-size_t grad_listed_bytes(const GradReq* r, int n, int n_split, int precision) {
+// per request of the vector-Jacobian form: tables, rows and kernels with
+// tangents, the product kernels' partials, C_ell (when the caller gave none)
+// and the cotangent
+static size_t vjp_item_bytes(const GeoHeader& h, bool own_cl) {
+  const size_t per = (size_t)h.n_cls * h.n_ell;
+  size_t o = al256(sizeof(TabD));
+  o += ptt_bytes(JCG_FP32C);
+  o += rows_bytes(h, JCG_FP32C);
+  o += kern_bytes(h, JCG_FP32C);
+  o += vjp32_item_bytes(h);
+  if (own_cl) o += al256(sizeof(double) * per);
+  o += al256(sizeof(double) * per);
+  return o;
+}
+
+size_t grad_listed_bytes(const GradReq* r, int n, int n_split, int precision, bool vjp) {
   size_t o = al256(sizeof(GradItem) * (size_t)n);
-  for (int i = 0; i < n; ++i) o += grad_item_bytes(*r[i].h, n_split, !r[i].cl, !r[i].jac, precision);
+  for (int i = 0; i < n; ++i)
+    o += vjp ? vjp_item_bytes(*r[i].h, !r[i].cl) : grad_item_bytes(*r[i].h, n_split, !r[i].cl, !r[i].jac, precision);
   return o + gnode_bytes(n, precision);
 }
 
 cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void* ws, const ConstTables* c,
-                            cudaStream_t st) {
+                            cudaStream_t st, bool vjp, GradBatch* gb_out) {
   static thread_local std::vector<GradItem> host;
   host.resize(n);
   char* base = static_cast<char*>(ws);
@@ -1882,36 +2010,57 @@ cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void*
     if (precision == JCG_FP32C) it.kernf = reinterpret_cast<float*>(base + o);
     else it.kernd = reinterpret_cast<double*>(base + o);
     o += kern_bytes(h, precision);
-    it.part = reinterpret_cast<double*>(base + o);
-    o += al256(sizeof(double) * (size_t)n_split * per * (NDIR + 1));
-    if (!r[i].cl) {
-      r[i].cl = reinterpret_cast<double*>(base + o);
+    if (vjp) {
+      const size_t nch = (size_t)vjp_chunks(h.na);
+      it.cpart = reinterpret_cast<float*>(base + o);
+      o += al256(sizeof(float) * nch * per);
+      it.gpart = reinterpret_cast<double*>(base + o);
+      o += al256(sizeof(double) * nch * NDIR);
+      if (!r[i].cl) {
+        r[i].cl = reinterpret_cast<double*>(base + o);
+        o += al256(sizeof(double) * per);
+      }
+      r[i].vbar = reinterpret_cast<double*>(base + o);
       o += al256(sizeof(double) * per);
+      it.vbar = r[i].vbar;
+      it.grad = r[i].out + 1;
+      it.cl = r[i].cl;
+    } else {
+      it.part = reinterpret_cast<double*>(base + o);
+      o += al256(sizeof(double) * (size_t)n_split * per * (NDIR + 1));
+      if (!r[i].cl) {
+        r[i].cl = reinterpret_cast<double*>(base + o);
+        o += al256(sizeof(double) * per);
+      }
+      if (!r[i].jac) {
+        r[i].jac = reinterpret_cast<double*>(base + o);
+        o += al256(sizeof(double) * per * NDIR);
+      }
+      it.cl = r[i].cl;
+      it.jac = r[i].jac;
     }
-    if (!r[i].jac) {
-      r[i].jac = reinterpret_cast<double*>(base + o);
-      o += al256(sizeof(double) * per * NDIR);
-    }
-    it.cl = r[i].cl;
-    it.jac = r[i].jac;
     gb.na = max(gb.na, h.na);
     gb.n_tr = max(gb.n_tr, h.n_tr);
     gb.n_cls = max(gb.n_cls, h.n_cls);
     gb.n_ell = max(gb.n_ell, h.n_ell);
     gb.physics_or |= h.physics;
   }
-  // pageable source: the copy is staged before the call returns, so the
-  // host vector can be reused by the next call of this thread
-  const cudaError_t e = cudaMemcpyAsync(dev_items, host.data(), sizeof(GradItem) * (size_t)n,
-                                        cudaMemcpyHostToDevice, st);
+  // through the calling thread's pinned staging ring: no wait on the stream
+  const cudaError_t e = stage_h2d(dev_items, host.data(), sizeof(GradItem) * (size_t)n, st);
   if (e != cudaSuccess) return e;
   gb.n_items = n;
   gb.listed = 1;
   gb.precision = precision;
   gb.items = dev_items;
-  gb.n_split = n_split;
+  gb.n_split = vjp ? 1 : n_split;
   gb.gnode = gnode_bytes(n, precision) ? reinterpret_cast<double*>(base + o) : nullptr;
-  launch_grad(gb, c, st);
+  if (vjp) {
+    launch_grad_front(gb, c, st);
+    launch_vjp32_cl(gb, st);
+  } else {
+    launch_grad(gb, c, st);
+  }
+  if (gb_out) *gb_out = gb;
   return cudaSuccess;
 }
 

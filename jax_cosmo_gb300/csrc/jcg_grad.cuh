@@ -114,7 +114,23 @@ struct GradItem {
   double* part;    // [n_split][n_cls][n_ell][NDIR + 1] partial sums over a
   double* cl;      // [n_cls][n_ell] (may be NULL)
   double* jac;     // [n_cls][n_ell][NDIR]
+  // vector-Jacobian product (fp32c): the cotangent of C_ell [n_cls][n_ell],
+  // per a-chunk partial C_ell [n_chunk][n_cls][n_ell] and gradients
+  // [n_chunk][NDIR], the gradient out [NDIR]
+  const double* vbar;
+  float* cpart;
+  double* gpart;
+  double* grad;
 };
+
+// a-chunks of the vector-Jacobian product kernels: at most VJ_TA Limber
+// nodes per CTA, the chunks balanced
+constexpr int VJ_TA = 32;
+__host__ __device__ inline int vjp_chunks(int na) { return (na + VJ_TA - 1) / VJ_TA; }
+__host__ __device__ inline int vjp_tav(int na) {
+  const int nc = vjp_chunks(na);
+  return (na + nc - 1) / nc;
+}
 
 // Uniform form: one geometry, per-item pointers from strides.  Listed form:
 // items[] (ragged requests), sizes below are the maxima over the items.
@@ -143,6 +159,11 @@ struct GradBatch {
   // seg_out, or imposed from seg_in (the branch of another parameter point)
   const int* seg_in;
   int* seg_out;
+  // uniform form of the vector-Jacobian product buffers (see GradItem)
+  const double* vbar;
+  float* cpart;
+  double* gpart;
+  double* grad;
 };
 
 // Small fp32c batches spread the table kernel's per-node evaluations over
@@ -172,9 +193,14 @@ __device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
   r.rowg = gb.rowg ? gb.rowg + (size_t)i * gb.na * NROWG : nullptr;
   r.kernf = gb.kernf ? gb.kernf + (size_t)i * gb.n_tr * gb.na * (NDIR + 1) : nullptr;
   r.ptt = gb.ptt ? gb.ptt + (size_t)i * PTT_STRIDE : nullptr;
-  r.part = gb.part + (size_t)i * gb.n_split * per * (NDIR + 1);
   r.cl = gb.cl ? gb.cl + (size_t)i * per : nullptr;
-  r.jac = gb.jac + (size_t)i * per * NDIR;
+  r.jac = gb.jac ? gb.jac + (size_t)i * per * NDIR : nullptr;
+  r.part = gb.part ? gb.part + (size_t)i * gb.n_split * per * (NDIR + 1) : nullptr;
+  const int nch = vjp_chunks(gb.na);
+  r.vbar = gb.vbar ? gb.vbar + (size_t)i * per : nullptr;
+  r.cpart = gb.cpart ? gb.cpart + (size_t)i * nch * per : nullptr;
+  r.gpart = gb.gpart ? gb.gpart + (size_t)i * nch * NDIR : nullptr;
+  r.grad = gb.grad ? gb.grad + (size_t)i * NDIR : nullptr;
   return r;
 }
 
@@ -212,6 +238,12 @@ static __device__ __noinline__ void bias_term_d1(const TabD* tb, const ConstTabl
 // FP32 compensated stages (jcg_grad32.cu)
 void launch_grad_kern32(const GradBatch& gb, const ConstTables* c, cudaStream_t st);
 void launch_grad_limber32(const GradBatch& gb, const ConstTables* c, cudaStream_t st);
+// vector-Jacobian product (jcg_vjp32.cu): C_ell of the items into their cl,
+// and the product with their cotangents vbar into their grad
+void launch_vjp32_cl(const GradBatch& gb, cudaStream_t st);
+void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st);
+// tables, rows and radial kernels with tangents (the stages before Limber)
+void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t st);
 int grad_limber32_tile(int n_ell, int n_cls);
 int grad_limber32_chunk(int n_cls);
 

@@ -715,15 +715,31 @@ struct GradReq {
   const double* params;    // device, 8 parameters
   double* cl;
   double* jac;
+  double* out;             // log-likelihood + gradient [9] (vector-Jacobian form)
+  double* vbar;            // the likelihood's cotangent of C_ell (set by grad_run_listed, vector-Jacobian form)
 };
 int grad_listed_auto_split(const GradReq* r, int n, int precision);
-size_t grad_listed_bytes(const GradReq* r, int n, int n_split, int precision);
+// vjp: the vector-Jacobian form (fp32c log-likelihood requests): no Jacobian,
+// the items' C_ell by the forward form of the product kernel; the caller then
+// forms the cotangents and launches launch_vjp32_grad on *gb_out
+size_t grad_listed_bytes(const GradReq* r, int n, int n_split, int precision, bool vjp = false);
+struct GradBatch;
 cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void* ws, const ConstTables* c,
-                            cudaStream_t st);
+                            cudaStream_t st, bool vjp = false, GradBatch* gb_out = nullptr);
+void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st);
+// vector-Jacobian product of angular_cl, uniform batch (jcg_grad.cu)
+size_t vjp_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision);
+void vjp_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, int precision,
+             const double* vbar, double* cl, double* grad, void* ws, const ConstTables* c, cudaStream_t st,
+             int gamma_dir);
+// host-to-device copy of a small host table through a pinned staging ring of
+// the calling thread (jcg_api.cu): returns without waiting for the stream
+cudaError_t stage_h2d(void* dst_dev, const void* src_host, size_t bytes, cudaStream_t st);
 // log-likelihood and its gradient for a fixed inverse covariance (jcg_stats.cu)
 struct ReqLL {
   const double* cl;     // [n_cls][n_ell]
-  const double* jac;    // [n_cls][n_ell][8]
+  const double* jac;    // [n_cls][n_ell][8], or NULL: the cotangent form below
+  double* vbar;         // [n_cls][n_ell]: receives -P r (d logL / dC_ell) when jac is NULL
   const double* data;   // [n_cls * n_ell]
   const double* prec;   // [n_ell][n_cls][n_cls]
   double* out;          // [9]

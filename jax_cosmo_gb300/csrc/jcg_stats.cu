@@ -272,8 +272,12 @@ __global__ void __launch_bounds__(128) request_loglike_part_kernel(const ReqLL* 
     double alpha = 0.0;
     for (int k = 0; k < n_cls; ++k) alpha += Pl[k] * rs[k * RL_ELL + j];
     acc[0] += rs[p * RL_ELL + j] * alpha;
-    const double* J = q.jac + ((size_t)p * n_ell + l) * 8;
-    for (int d = 0; d < 8; ++d) acc[1 + d] += alpha * J[d];
+    if (q.jac) {
+      const double* J = q.jac + ((size_t)p * n_ell + l) * 8;
+      for (int d = 0; d < 8; ++d) acc[1 + d] += alpha * J[d];
+    } else {
+      q.vbar[(size_t)p * n_ell + l] = -alpha;
+    }
   }
   __shared__ double red[4][9];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -295,6 +299,7 @@ __global__ void request_loglike_sum_kernel(const ReqLL* __restrict__ items, int 
   const int item = idx / 9, s = idx % 9;
   if (item >= n) return;
   const ReqLL q = items[item];
+  if (s > 0 && !q.jac) return;  // the gradient comes from the vector-Jacobian product
   const int tiles = rl_tiles(q.n_ell);
   double v = 0.0;
   for (int t = 0; t < tiles; ++t) v += q.part[(size_t)t * 9 + s];

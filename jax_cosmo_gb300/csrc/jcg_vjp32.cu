@@ -1,0 +1,378 @@
+// Vector-Jacobian product of angular_cl in the fp32c arithmetic: for a
+// cotangent vbar_p(l) of the spectra (the derivative of a likelihood with
+// respect to C_ell), the gradient
+//
+//   g_d = sum_{p,l} vbar_p(l) dC_p(l)/dtheta_d
+//
+// without forming dC/dtheta (angular_cl.py:49-98 differentiated as jax.grad
+// does for a scalar function of it, README.md:14-27).  With
+//   C_p(l) = ef_i(l) ef_j(l) sum_a P(l, a) M_p(a),   M_p(a) = u(a) K_i(a) K_j(a)
+// and v_p(l) = vbar_p(l) ef_i(l) ef_j(l):
+//
+//   g_d = sum_{a,l} W(a, l) dP(l, a)/dtheta_d + sum_{a,p} Q_p(a) dM_p(a)/dtheta_d
+//   W(a, l) = sum_p v_p(l) M_p(a),        Q_p(a) = sum_l v_p(l) P(l, a).
+//
+// dP/dtheta at a node is the reverse sweep of the integrand (jcg_node32.cuh)
+// contracted with the tangents of its inputs; here the adjoints are weighted
+// by W and summed over ell first, so the projection on the 8 tangent
+// directions runs once per a node instead of once per (a, ell) node, and the
+// contraction with the spectra is two small products (W and Q) instead of
+// one per spectrum and direction.
+//
+// One CTA per (chunk of at most VJ_TA a nodes, cosmology); 8 lanes per a
+// node, iterating over ell.  The same kernel in its forward form (FWD) gives
+// the chunk's partial C_ell, from which the serving loop forms the
+// likelihood's cotangent before the product.
+#include "jcg_node32.cuh"
+
+namespace jcg {
+
+constexpr int VJ_THREADS = 256;
+constexpr int VJ_GROUP = 8;      // lanes per a node
+constexpr int VJ_LTMAX = 256;    // ell per tile at most
+constexpr int VJ_VBYTES = 32 * 1024;  // the cotangent tile [n_cls][LT] in shared memory
+
+int vjp_ltile(int n_cls, int n_ell) {
+  int lt = VJ_VBYTES / (4 * (n_cls > 0 ? n_cls : 1));
+  if (lt > VJ_LTMAX) lt = VJ_LTMAX;
+  lt = lt / 8 * 8;
+  if (lt < 8) lt = 8;
+  const int need = (n_ell + 7) / 8 * 8;
+  return lt < need ? lt : need;
+}
+
+struct VjLayout {
+  size_t ev, kh, rows, ks, mv, vs, pt, abar, qd, red, total;
+};
+__host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT) {
+  VjLayout L;
+  size_t o = 0;
+  L.ev = o;                                   // 16 values + [NET][NDIR] tangents (floats)
+  o += 4 * (16 + NET * NDIR);
+  o = (o + 15) & ~(size_t)15;
+  L.kh = o;                                   // [3][LT] l + 1/2, log2(l + 1/2), 1 / (l + 1/2)
+  o += 4 * 3 * (size_t)LT;
+  o = (o + 15) & ~(size_t)15;
+  L.rows = o;                                 // [VJ_TA][NROWG]
+  o += 4 * (size_t)VJ_TA * NROWG;
+  L.ks = o;                                   // [VJ_TA][n_tr][NDIR + 1]
+  o += 4 * (size_t)VJ_TA * n_tr * (NDIR + 1);
+  L.mv = o;                                   // [VJ_TA][n_cls]
+  o += 4 * (size_t)VJ_TA * n_cls;
+  L.vs = o;                                   // [n_cls][LT]
+  o += 4 * (size_t)n_cls * LT;
+  L.pt = o;                                   // [VJ_TA][LT]
+  o += 4 * (size_t)VJ_TA * LT;
+  L.abar = o;                                 // [VJ_TA][NGT]
+  o += 4 * (size_t)VJ_TA * NGT;
+  o = (o + 15) & ~(size_t)15;
+  L.qd = o;                                   // [VJ_TA][n_cls] doubles
+  o += 8 * (size_t)VJ_TA * n_cls;
+  L.red = o;                                  // [VJ_THREADS / 32][NET] floats, then [VJ_TA][NDIR] doubles
+  o += 4 * (size_t)(VJ_THREADS / 32) * NET;
+  o = (o + 15) & ~(size_t)15;
+  o += 8 * (size_t)VJ_TA * NDIR;
+  L.total = o;
+  return L;
+}
+
+// GEN: some item may use a non-default operator point (as grad_limber32).
+// FWD: the forward form (partial C_ell of the chunk, no cotangent).
+template <bool GEN, bool FWD>
+__global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb, int LT) {
+  const int item = blockIdx.y, chunk = blockIdx.x;
+  if (item >= gb.n_items) return;
+  const GradItem gi = grad_item(gb, item);
+  const GeoHeader* geo = gi.geo;
+  const int n_ell = geo->n_ell, n_cls = geo->n_cls, na = geo->na, n_tr = geo->n_tr;
+  const int nch = vjp_chunks(na), tav = vjp_tav(na);
+  if (chunk >= nch) return;
+  const int a0 = chunk * tav, tc = min(tav, na - a0);
+  const bool lin = pk_model(geo->physics) == JCG_PK_LINEAR;
+  const bool nw = GEN && tf_nowiggle(geo->physics);
+  const VjLayout L = vj_layout(n_tr, n_cls, LT);
+  extern __shared__ __align__(16) unsigned char vj_smem[];
+  float* ev = reinterpret_cast<float*>(vj_smem + L.ev);
+  float* et = ev + 16;
+  float* khv = reinterpret_cast<float*>(vj_smem + L.kh);
+  float* lkhv = khv + LT;
+  float* ikhv = lkhv + LT;
+  float* R = reinterpret_cast<float*>(vj_smem + L.rows);
+  float* Ks = reinterpret_cast<float*>(vj_smem + L.ks);
+  float* Mv = reinterpret_cast<float*>(vj_smem + L.mv);
+  float* vS = reinterpret_cast<float*>(vj_smem + L.vs);
+  float* Pt = reinterpret_cast<float*>(vj_smem + L.pt);
+  float* Abar = reinterpret_cast<float*>(vj_smem + L.abar);
+  double* Qd = reinterpret_cast<double*>(vj_smem + L.qd);
+  float* Ered = reinterpret_cast<float*>(vj_smem + L.red);
+  double* gred = reinterpret_cast<double*>(vj_smem + ((L.red + 4 * (VJ_THREADS / 32) * NET + 15) & ~(size_t)15));
+  const int tid = threadIdx.x, grp = tid >> 3, sub = tid & (VJ_GROUP - 1);
+  const TabD* tb = gi.tab;
+  if (tid < NDIR + 1) {
+    // tid 0: the Eisenstein-Hu values; tid 1..8: their tangents in direction tid - 1
+    const int d = tid - 1;
+    const double keq = tb->sv[S_K_EQ], sh = tb->sv[S_SH_D], bc = tb->sv[S_BETA_C], ac = tb->sv[S_ALPHA_C];
+    const double ks = tb->sv[S_K_SILK];
+    if (tid == 0) {
+      const double qinv = 1.0 / (13.41 * keq);
+      ev[0] = (float)qinv;
+      ev[1] = (float)log2(qinv);
+      ev[2] = (float)sh;
+      ev[3] = (float)(1.0 / sh);
+      ev[4] = (float)(1.8 * bc);
+      ev[5] = (float)(14.2 / ac);
+      ev[6] = (float)tb->sv[S_ALPHA_B];
+      ev[7] = (float)tb->sv[S_BETA_B];
+      ev[8] = (float)tb->sv[S_BETA_NODE];
+      ev[9] = (float)log2(ks);
+      ev[10] = (float)tb->sv[S_FB];
+      ev[11] = (float)tb->sv[S_FC];
+      ev[12] = (float)(tb->sv[S_NS] + 3.0);
+      ev[13] = (float)(1.0 / keq);
+      ev[14] = (float)tb->sv[S_AGAM];
+      ev[15] = (float)tb->sv[S_NWQ];
+    } else if (!FWD) {
+      const double* sd = tb->sd[d];
+      for (int j = 0; j < NET; ++j) et[j * NDIR + d] = 0.f;
+      et[E_KEQ * NDIR + d] = (float)sd[S_K_EQ];
+      et[E_SH * NDIR + d] = (float)sd[S_SH_D];
+      et[E_C18BC * NDIR + d] = (float)(1.8 * sd[S_BETA_C]);
+      et[E_C142AC * NDIR + d] = (float)(-14.2 * sd[S_ALPHA_C] / (ac * ac));
+      et[E_ALPHAB * NDIR + d] = (float)sd[S_ALPHA_B];
+      et[E_BETAB * NDIR + d] = (float)sd[S_BETA_B];
+      et[E_BETANODE * NDIR + d] = (float)sd[S_BETA_NODE];
+      et[E_LG2KSILK * NDIR + d] = (float)(sd[S_K_SILK] / (ks * 0.6931471805599453));
+      et[E_FB * NDIR + d] = (float)sd[S_FB];
+      et[E_FC * NDIR + d] = (float)sd[S_FC];
+      et[E_NS3 * NDIR + d] = (float)sd[S_NS];
+      if (nw) {
+        et[E_AGAM * NDIR + d] = (float)sd[S_AGAM];
+        et[E_NWQ * NDIR + d] = (float)sd[S_NWQ];
+      }
+    }
+  }
+  // the chunk's FP32 rows (values and tangents) and radial kernels
+  {
+    const float4* src = reinterpret_cast<const float4*>(gi.rowg + (size_t)a0 * NROWG);
+    float4* dst = reinterpret_cast<float4*>(R);
+    for (int i = tid; i < tc * (NROWG / 4); i += VJ_THREADS) dst[i] = src[i];
+    const int per_t = n_tr * (NDIR + 1);
+    for (int i = tid; i < tc * per_t; i += VJ_THREADS) {
+      const int t = i / per_t, rem = i - t * per_t;
+      const int tr = rem / (NDIR + 1), s = rem - tr * (NDIR + 1);
+      Ks[i] = gi.kernf[((size_t)tr * na + a0 + t) * (NDIR + 1) + s];
+    }
+  }
+  if (!FWD)
+    for (int i = tid; i < tc * n_cls; i += VJ_THREADS) Qd[i] = 0.0;
+  __syncthreads();
+  // M_p(a) = u K_i K_j, the operation order of grad_limber32
+  for (int i = tid; i < tc * n_cls; i += VJ_THREADS) {
+    const int t = i / n_cls, p = i - t * n_cls;
+    const float* Ki = Ks + ((size_t)t * n_tr + geo->pair_i[p]) * (NDIR + 1);
+    const float* Kj = Ks + ((size_t)t * n_tr + geo->pair_j[p]) * (NDIR + 1);
+    Mv[i] = R[(size_t)t * NROWG + F_U] * (Ki[0] * Kj[0]);
+  }
+  EHg eh;
+  eh.qinv = ev[0]; eh.lg2_qinv = ev[1]; eh.sh = ev[2]; eh.inv_sh = ev[3]; eh.c18bc = ev[4];
+  eh.c142ac = ev[5]; eh.alpha_b = ev[6]; eh.beta_b = ev[7]; eh.beta_node = ev[8]; eh.lg2_ksilk = ev[9];
+  eh.fb = ev[10]; eh.fc = ev[11]; eh.ns3 = ev[12]; eh.inv_keq = ev[13];
+  eh.agam = ev[14]; eh.nwq = ev[15];
+  const double* ELL = geo_ptr<double>(geo, geo->off_ell);
+  const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
+  float accA[T_U], accE[NET];
+#pragma unroll
+  for (int j = 0; j < T_U; ++j) accA[j] = 0.f;
+#pragma unroll
+  for (int j = 0; j < NET; ++j) accE[j] = 0.f;
+  for (int l0 = 0; l0 < n_ell; l0 += LT) {
+    const int lt = min(LT, n_ell - l0);
+    __syncthreads();  // the previous tile's Pt / vS are consumed
+    for (int l = tid; l < lt; l += VJ_THREADS) {
+      const double e = ELL[l0 + l] + 0.5;
+      khv[l] = (float)e;
+      lkhv[l] = (float)log2(e);
+      ikhv[l] = (float)(1.0 / e);
+    }
+    if (!FWD)
+      for (int q = tid; q < n_cls * lt; q += VJ_THREADS) {
+        const int p = q / lt, l = q - p * lt;
+        const int ell = l0 + l;
+        const double ef = EF[(size_t)geo->pair_i[p] * n_ell + ell] * EF[(size_t)geo->pair_j[p] * n_ell + ell];
+        vS[p * LT + l] = (float)(gi.vbar[(size_t)p * n_ell + ell] * ef);
+      }
+    __syncthreads();
+    if (grp < tc) {
+      const int t = grp;
+      const float* row = R + (size_t)t * NROWG;
+      const float* mrow = Mv + (size_t)t * n_cls;
+      for (int l = sub; l < lt; l += VJ_GROUP) {
+        float an[NGT], ae[NET];
+        const float P = !GEN ? node32_fb_default(eh, row, khv[l], lkhv[l], ikhv[l], an, ae)
+                        : nw ? node32_fb_nw(eh, row, khv[l], lkhv[l], ikhv[l], an, ae, lin)
+                             : node32_fb<true>(eh, row, khv[l], lkhv[l], ikhv[l], an, ae, lin);
+        Pt[t * LT + l] = P;
+        if (!FWD) {
+          float W = 0.f;
+          for (int p = 0; p < n_cls; ++p) W = fmaf(vS[p * LT + l], mrow[p], W);
+#pragma unroll
+          for (int j = 0; j < T_U; ++j) {
+            if (!GEN && j == T_MUN) continue;  // mu_n = 0 for takahashi2012
+            accA[j] = fmaf(W, an[j], accA[j]);
+          }
+#pragma unroll
+          for (int j = 0; j < NET; ++j) accE[j] = fmaf(W, ae[j], accE[j]);
+        }
+      }
+    }
+    __syncthreads();
+    if (FWD) {
+      // partial C_p(l) of the chunk: sum_t M_p(t) P(t, l)
+      float* cp = gi.cpart + (size_t)chunk * n_cls * n_ell;
+      for (int q = tid; q < n_cls * lt; q += VJ_THREADS) {
+        const int p = q / lt, l = q - p * lt;
+        float s = 0.f;
+        for (int t = 0; t < tc; ++t) s = fmaf(Pt[t * LT + l], Mv[t * n_cls + p], s);
+        cp[(size_t)p * n_ell + l0 + l] = s;
+      }
+    } else {
+      // Q_p(t) += sum_l v_p(l) P(t, l), float sums of at most 32 terms added in double
+      for (int q = tid; q < tc * n_cls; q += VJ_THREADS) {
+        const int t = q / n_cls, p = q - t * n_cls;
+        const float* vp = vS + (size_t)p * LT;
+        const float* pp = Pt + (size_t)t * LT;
+        double s = 0.0;
+        for (int b = 0; b < lt; b += 32) {
+          float f = 0.f;
+          const int e = min(lt, b + 32);
+          for (int l = b; l < e; ++l) f = fmaf(vp[l], pp[l], f);
+          s += (double)f;
+        }
+        Qd[q] += s;
+      }
+    }
+  }
+  if (FWD) return;
+  // adjoints of the node inputs: summed over the a node's 8 lanes; those of
+  // the cosmology's Eisenstein-Hu inputs over the CTA
+#pragma unroll
+  for (int j = 0; j < T_U; ++j) {
+    float v = accA[j];
+    v += __shfl_xor_sync(0xffffffffu, v, 4);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    if (sub == 0 && grp < tc) Abar[grp * NGT + j] = v;
+  }
+  const int warp = tid >> 5, lane = tid & 31;
+#pragma unroll
+  for (int j = 0; j < NET; ++j) {
+    float v = accE[j];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) Ered[warp * NET + j] = v;
+  }
+  __syncthreads();
+  // projection on the tangents: thread (a node t, direction d)
+  {
+    const int t = tid >> 3, d = tid & 7;
+    double gd = 0.0;
+    if (t < tc) {
+      const float* row = R + (size_t)t * NROWG;
+      const float* tg = row + NROWV;
+      float s = 0.f;
+#pragma unroll
+      for (int j = 0; j < T_U; ++j) {
+        if (!GEN && j == T_MUN) continue;
+        s = fmaf(Abar[t * NGT + j], tg[j * NDIR + d], s);
+      }
+      gd = (double)s;
+      // sum_p Q_p (du K_i K_j + u (dK_i K_j + K_i dK_j))
+      const float u = row[F_U], du = tg[T_U * NDIR + d];
+      const double* q = Qd + (size_t)t * n_cls;
+      double sm = 0.0;
+      for (int p = 0; p < n_cls; ++p) {
+        const float* Ki = Ks + ((size_t)t * n_tr + geo->pair_i[p]) * (NDIR + 1);
+        const float* Kj = Ks + ((size_t)t * n_tr + geo->pair_j[p]) * (NDIR + 1);
+        const float dm = fmaf(du, Ki[0] * Kj[0], u * fmaf(Ki[1 + d], Kj[0], Ki[0] * Kj[1 + d]));
+        sm += q[p] * (double)dm;
+      }
+      gd += sm;
+    }
+    if (t == 0) {
+      // the cosmology's Eisenstein-Hu inputs, once per CTA
+      double se = 0.0;
+      for (int j = 0; j < NET; ++j) {
+        double ej = 0.0;
+        for (int w = 0; w < VJ_THREADS / 32; ++w) ej += (double)Ered[w * NET + j];
+        se += ej * (double)et[j * NDIR + d];
+      }
+      gd += se;
+    }
+    gred[t * NDIR + d] = gd;
+  }
+  __syncthreads();
+  if (tid < NDIR) {
+    double g = 0.0;
+    for (int t = 0; t < VJ_TA; ++t) g += gred[t * NDIR + tid];
+    gi.gpart[(size_t)chunk * NDIR + tid] = g;
+  }
+}
+
+// C_ell from the chunks' partials (fixed order), times the ell factors
+__global__ void vjp_cl_reduce_kernel(GradBatch gb) {
+  const int item = blockIdx.y;
+  if (item >= gb.n_items) return;
+  const GradItem gi = grad_item(gb, item);
+  if (!gi.cl) return;
+  const GeoHeader* geo = gi.geo;
+  const int n_ell = geo->n_ell, n_cls = geo->n_cls, nch = vjp_chunks(geo->na);
+  const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
+  const size_t per = (size_t)n_cls * n_ell;
+  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < per; idx += (size_t)gridDim.x * blockDim.x) {
+    const int p = (int)(idx / n_ell), l = (int)(idx % n_ell);
+    double s = 0.0;
+    for (int c = 0; c < nch; ++c) s += (double)gi.cpart[(size_t)c * per + idx];
+    gi.cl[idx] = s * EF[(size_t)geo->pair_i[p] * n_ell + l] * EF[(size_t)geo->pair_j[p] * n_ell + l];
+  }
+}
+
+// the gradient from the chunks' partials (fixed order)
+__global__ void vjp_grad_reduce_kernel(GradBatch gb) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  const int item = idx / NDIR, d = idx % NDIR;
+  if (item >= gb.n_items) return;
+  const GradItem gi = grad_item(gb, item);
+  const int nch = vjp_chunks(gi.geo->na);
+  double g = 0.0;
+  for (int c = 0; c < nch; ++c) g += gi.gpart[(size_t)c * NDIR + d];
+  gi.grad[d] = g;
+}
+
+template <bool GEN, bool FWD>
+static void launch_vjp_t(const GradBatch& gb, cudaStream_t st) {
+  const int LT = vjp_ltile(gb.n_cls, gb.n_ell);
+  const size_t smem = vj_layout(gb.n_tr, gb.n_cls, LT).total;
+  cudaFuncSetAttribute(grad_vjp32_kernel<GEN, FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  dim3 grid(vjp_chunks(gb.na), gb.n_items);
+  grad_vjp32_kernel<GEN, FWD><<<grid, VJ_THREADS, smem, st>>>(gb, LT);
+}
+
+// forward: C_ell into the items' cl (uniform batch: gb.cl)
+void launch_vjp32_cl(const GradBatch& gb, cudaStream_t st) {
+  if (gb.physics_or != 0) launch_vjp_t<true, true>(gb, st);
+  else launch_vjp_t<false, true>(gb, st);
+  const size_t per = (size_t)gb.n_cls * gb.n_ell;
+  size_t bx = (per + 255) / 256;
+  const size_t cap = (152 * 16 + gb.n_items - 1) / gb.n_items;
+  if (bx > cap) bx = cap;
+  vjp_cl_reduce_kernel<<<dim3((unsigned)(bx ? bx : 1), gb.n_items), 256, 0, st>>>(gb);
+}
+
+// the product with the items' cotangents vbar into their grad
+void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st) {
+  if (gb.physics_or != 0) launch_vjp_t<true, false>(gb, st);
+  else launch_vjp_t<false, false>(gb, st);
+  vjp_grad_reduce_kernel<<<(gb.n_items * NDIR + 127) / 128, 128, 0, st>>>(gb);
+}
+
+}  // namespace jcg

@@ -163,8 +163,10 @@ class _Arena:
 class _CudaBackend:
     """One CUDA stream, pinned staging and device slots per batch slot."""
 
-    def __init__(self, device, arena_bytes, n_streams, max_batch, precision):
+    def __init__(self, device, arena_bytes, n_streams, max_batch, precision, trace=False):
         self.device = _lib.require_cuda(device)
+        self.trace = trace
+        self.trace_log = []  # (slot, start event, end event) of every launch when tracing
         self.precision = precision
         self.arena = torch.empty(max(int(arena_bytes), _ALIGN), dtype=torch.uint8, device=self.device)
         self.streams = [torch.cuda.Stream(self.device) for _ in range(n_streams)]
@@ -198,13 +200,18 @@ class _CudaBackend:
         for i, r in enumerate(reqs):
             r.model._fill(table, i, p0 + 64 * i, o0 + 72 * i)
         with torch.cuda.stream(s):
+            if self.trace:
+                e0 = torch.cuda.Event(enable_timing=True)
+                e0.record(s)
             pd[:n].copy_(ph[:n], non_blocking=True)
             _lib.call("jcg_requests_run", ctypes.c_void_p(table.ctypes.data), n, _lib.REQ_LOGLIKE_GRAD,
                       self.precision, ctypes.c_void_p(self.arena.data_ptr() + off), ctypes.c_size_t(nbytes),
                       ctypes.c_void_p(s.cuda_stream))
             self.out_host[slot][:n].copy_(self.out_dev[slot][:n], non_blocking=True)
-            ev = torch.cuda.Event()
+            ev = torch.cuda.Event(enable_timing=self.trace)
             ev.record(s)
+            if self.trace:
+                self.trace_log.append((slot, e0, ev))
         self.events[slot] = ev
         self.launches += 1
 
@@ -245,7 +252,7 @@ class Server:
     """
 
     def __init__(self, device=None, hbm_budget=1 << 30, max_batch=512, n_streams=2, timeout_s=60.0,
-                 poll_s=50e-6, precision="fp32c", backend=None):
+                 poll_s=50e-6, precision="fp32c", backend=None, trace=False):
         from jax_cosmo_gb300.angular_cl import _precision_code
 
         if n_streams < 1 or max_batch < 1:
@@ -257,7 +264,7 @@ class Server:
         self.poll_s = float(poll_s)
         self._arena = _Arena(hbm_budget)
         self._backend = backend if backend is not None else _CudaBackend(device, self._arena.size, n_streams,
-                                                                          self.max_batch, prec)
+                                                                          self.max_batch, prec, trace)
         self._slots = [None] * n_streams
         self._dead = [False] * n_streams
         self._pending = collections.deque()
@@ -307,6 +314,19 @@ class Server:
 
     def __exit__(self, *exc):
         self.stop()
+
+    def device_intervals(self):
+        """With ``trace=True``: (stream slot, start ms, end ms) of every launched
+        batch on the GPU's clock (CUDA events around the batch's copies and
+        kernels on its stream), relative to the first batch's start.  Call
+        after ``stop``."""
+        log = getattr(self._backend, "trace_log", [])
+        if not log:
+            return []
+        for _, _, e1 in log:
+            e1.synchronize()
+        ref = log[0][1]
+        return [(slot, ref.elapsed_time(e0), ref.elapsed_time(e1)) for slot, e0, e1 in log]
 
     def reset_stats(self):
         """Forget latencies and counts so far (e.g. after a warm-up period)."""

@@ -256,3 +256,67 @@ def test_fisher_matrix_vs_oracle():
     assert F.shape == (7, 7)
     err = float((F.cpu() - F_o).abs().max() / F_o.abs().max())
     assert err < TOL_G, err
+
+
+def _vjp_case(spec, ell, physics=0, gamma=None, B=5, seed=3):
+    """A batch around the fiducial, a seeded cotangent and the FP64 Jacobian."""
+    from jax_cosmo_gb300 import _geometry
+    from jax_cosmo_gb300.autodiff import jacobian_device
+
+    rng = np.random.default_rng(seed)
+    rows = np.array([FID] * B) * (1.0 + 0.04 * rng.uniform(-1, 1, (B, 8)))
+    rows[:, 5] = 0.0
+    rows[:, 7] = 0.02 * rng.uniform(-1, 1, B)
+    if gamma is not None:
+        rows = np.concatenate([rows, np.full((B, 1), gamma)], axis=1)
+    params = torch.as_tensor(rows, device="cuda").contiguous()
+    probes = jc_probes(spec)
+    ell = _geometry.ell_host(ell)
+    n_cls = sum(len(b) for _, b, _ in spec)
+    n_cls = n_cls * (n_cls + 1) // 2
+    vbar = torch.as_tensor(rng.standard_normal((B, n_cls, len(ell))), device="cuda")
+    cl64, J64 = jacobian_device(params, ell, probes, 512, "fp64", physics)
+    return params, probes, ell, vbar, cl64, J64
+
+
+@pytest.mark.parametrize("physics", [0, "smith2003", "linear", "nowiggle"])
+def test_vjp_matches_jacobian_contraction(physics):
+    """jcg_angular_cl_vjp against the FP64 Jacobian contracted with the same
+    cotangent: FP64 to 1e-12 and fp32c to 1e-4 of the scale sum |v| |J| per
+    (cosmology, direction) (a cotangent of random signs cancels, so the scale
+    is that of the summed terms); the forward form's C_ell (fp32c) against
+    the FP64 C_ell at 1e-5."""
+    from jax_cosmo_gb300 import _lib
+    from jax_cosmo_gb300.autodiff import vjp_device
+
+    code = {0: 0, "smith2003": _lib.PK_SMITH2003, "linear": _lib.PK_LINEAR, "nowiggle": _lib.TF_NOWIGGLE}[physics]
+    params, probes, ell, vbar, cl64, J64 = _vjp_case(MIXED, np.logspace(1, np.log10(3000), 37), code)
+    ref = torch.einsum("bpl,bpld->bd", vbar, J64)
+    scale = torch.einsum("bpl,bpld->bd", vbar.abs(), J64.abs())
+    for prec, tol in (("fp64", 1e-12), ("fp32c", 1e-4)):
+        g, cl = vjp_device(params, ell, probes, vbar, 512, prec, code, want_cl=True)
+        err = float(((g - ref).abs() / scale).max())
+        print(physics, prec, "vjp err / sum|v||J|: %.2e" % err)
+        assert err < tol, (prec, err)
+        assert float(((cl - cl64).abs() / cl64.abs()).max()) < (1e-12 if prec == "fp64" else 1e-5)
+
+
+def test_vjp_gamma_direction_and_many_ell():
+    """The gamma growth's derivative through gamma_dir, and an ell grid longer
+    than one cotangent tile of the product kernel (16 tracers, 300 ell)."""
+    from jax_cosmo_gb300 import _lib
+    from jax_cosmo_gb300.autodiff import jacobian_device, vjp_device
+
+    params, probes, ell, vbar, _, _ = _vjp_case(WL5, np.logspace(1, np.log10(3000), 29), _lib.GROWTH_GAMMA, 0.55, B=3)
+    _, Jg = jacobian_device(params, ell, probes, 512, "fp64", _lib.GROWTH_GAMMA, gamma_dir=2)
+    ref = torch.einsum("bpl,bpld->bd", vbar, Jg)
+    scale = torch.einsum("bpl,bpld->bd", vbar.abs(), Jg.abs())
+    g = vjp_device(params, ell, probes, vbar, 512, "fp32c", _lib.GROWTH_GAMMA, gamma_dir=2)
+    assert float(((g - ref).abs() / scale).max()) < 1e-4
+    spec16 = [("wl", [(1.0, 2.0, z0, 6.0, 10) for z0 in np.linspace(0.3, 1.6, 10)], {"sigma_e": 0.26}),
+              ("nc", [(1.0, 2.0, z0, 6.0, 5) for z0 in np.linspace(0.4, 1.2, 6)], {"bias": 1.3})]
+    params, probes, ell, vbar, _, J64 = _vjp_case(spec16, np.logspace(1, np.log10(5000), 300), B=2)
+    ref = torch.einsum("bpl,bpld->bd", vbar, J64)
+    scale = torch.einsum("bpl,bpld->bd", vbar.abs(), J64.abs())
+    g = vjp_device(params, ell, probes, vbar, 512, "fp32c")
+    assert float(((g - ref).abs() / scale).max()) < 1e-4

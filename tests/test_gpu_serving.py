@@ -154,3 +154,67 @@ def test_small_hbm_budget_admission():
     assert st["completed"] == 12 and st["failed"] == 0
     assert st["arena_peak_bytes"] <= budget
     assert all(np.isfinite(r.loglike) and np.all(np.isfinite(r.grad)) for r in res)
+
+
+def test_batches_overlap_on_two_streams():
+    """Continuous batching: requests that arrive while a batch runs launch on
+    the second stream at once, and the two batches' device intervals (CUDA
+    events around each batch on its stream) intersect."""
+    models = [make_model(s, max_ell=500)[0] for s in (51, 52, 53, 54)]
+    rng = np.random.default_rng(4)
+    with serving.Server(hbm_budget=4 << 30, n_streams=2, max_batch=24, trace=True) as srv:
+        futs = [srv.submit(models[k % 4], box_point(rng)) for k in range(96)]
+        res = [f.result(timeout=300) for f in futs]
+    iv = srv.device_intervals()
+    assert len(res) == 96 and all(np.isfinite(r.loglike) for r in res)
+    assert {s for s, _, _ in iv} == {0, 1}
+    overlaps = [(a, b) for a in iv for b in iv
+                if a[0] == 0 and b[0] == 1 and b[1] < a[2] and a[1] < b[2]]
+    print("batches", len(iv), "overlapping pairs", len(overlaps), "first intervals", iv[:4])
+    assert overlaps, iv
+
+
+def test_requests_run_does_not_wait_for_the_stream():
+    """jcg_requests_run returns while earlier work still runs on its stream:
+    the request tables go through the pinned staging ring, not a pageable
+    copy.  A 50 ms spin kernel (torch.cuda._sleep, a bounded wait) is queued
+    first; the call returns in a small fraction of it, and the results equal
+    those of an unobstructed call."""
+    import ctypes
+    import time
+
+    from jax_cosmo_gb300 import _lib
+
+    model = make_model(61, max_ell=80)[0]
+    n = 8
+    rng = np.random.default_rng(6)
+    params = torch.as_tensor(np.array([box_point(rng) for _ in range(n)]), device="cuda").contiguous()
+    out = torch.zeros(n, 9, dtype=torch.float64, device="cuda")
+    table = np.zeros(n, _lib.REQUEST_DTYPE)
+    for i in range(n):
+        model._fill(table, i, params.data_ptr() + 64 * i, out.data_ptr() + 72 * i)
+    tp = ctypes.c_void_p(table.ctypes.data)
+    lo, hi = ctypes.c_size_t(), ctypes.c_size_t()
+    _lib.call("jcg_requests_workspace_size", tp, n, _lib.REQ_LOGLIKE_GRAD, _lib.FP32C, ctypes.byref(lo),
+              ctypes.byref(hi))
+    ws = _lib.workspace(hi.value, params.device)
+    stream = torch.cuda.current_stream()
+    st = ctypes.c_void_p(stream.cuda_stream)
+
+    def run():
+        _lib.call("jcg_requests_run", tp, n, _lib.REQ_LOGLIKE_GRAD, _lib.FP32C, _lib.ptr(ws),
+                  ctypes.c_size_t(ws.numel()), st)
+
+    run()  # first call: constant tables and the staging ring are set up
+    torch.cuda.synchronize()
+    ref = out.clone()
+    out.zero_()
+    torch.cuda.synchronize()
+    torch.cuda._sleep(100_000_000)  # about 50 ms at the 2.07 GHz SM clock
+    t0 = time.perf_counter()
+    run()
+    dt = time.perf_counter() - t0
+    torch.cuda.synchronize()
+    print("jcg_requests_run host time %.3f ms behind a 50 ms kernel" % (dt * 1e3))
+    assert dt < 0.01, dt
+    assert torch.equal(out, ref)
