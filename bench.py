@@ -223,6 +223,16 @@ def gpu_arm(args, rank, world, device):
         torch.cuda.synchronize(device)
         return float(np.sum(times)), times
 
+    if args.vjp_only:
+        # the fp32c C_ell + vector-Jacobian product alone (a profiling entry)
+        from jax_cosmo_gb300.autodiff import vjp_device
+
+        gen = torch.Generator(device=device).manual_seed(SEED)
+        vb = torch.randn(B, 15, N_ELL, generator=gen, dtype=torch.float64, device=device)
+        tv, _ = timed(lambda: vjp_device(params, ell_np, probes, vb, 512, "fp32c", want_cl=True), args.steps,
+                      args.warmup)
+        return {"jacobian_only": {"batch": B, "ms_per_step": tv / args.steps, "what": "C_ell + VJP",
+                                  "cl_grad_per_s": B * 15 * N_ELL / (tv / args.steps * 1e-3)}}
     if args.jacobian_only:
         # the fp32c Jacobian alone (a profiling entry: one kernel family per launch list)
         from jax_cosmo_gb300.autodiff import jacobian_device
@@ -664,6 +674,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--jacobian-only", action="store_true",
                     help="time only the fp32c C_ell + Jacobian of the batch (profiling)")
+    ap.add_argument("--vjp-only", action="store_true",
+                    help="time only the fp32c C_ell + vector-Jacobian product of the batch (profiling)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     world = int(os.environ.get("WORLD_SIZE", "1"))
