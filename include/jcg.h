@@ -321,7 +321,9 @@ int jcg_requests_run(const jcg_request* reqs, int n, int mode, int precision, vo
 
 /* Copy stage outputs for cosmology `index` out of a workspace (device to device).
  * what: 0 chi table [256], 1 growth table [128], 2 scalars [32],
- *       3 halofit rows [na][24] (FP64), 4 radial kernels [n_tracers][na]. */
+ *       3 halofit rows [na][24] (FP64), 4 radial kernels [n_tracers][na],
+ *       5 P(k, a = 1) k^3 on the halofit k grid [257], 6 sigma^2(R) without
+ *       the growth factor [256] (power.py:93-111). */
 int jcg_workspace_read(const jcg_geometry* g, int n_cosmo, int precision, const void* workspace,
                        int index, int what, double* out_dev, size_t out_count,
                        cudaStream_t stream);

@@ -543,6 +543,8 @@ int jcg_workspace_read(const jcg_geometry* g, int n_cosmo, int precision, const 
       src = reinterpret_cast<const double*>(base + L.kern) + (size_t)index * h.n_tr * h.na;
       count = (size_t)h.n_tr * h.na;
       break;
+    case 5: src = ct->pk3; count = NKH; break;
+    case 6: src = ct->sig; count = NRT; break;
     default: return fail(JCG_ERR_ARG, "what = %d", what);
   }
   if (out_count < count) return fail(JCG_ERR_SHAPE, "output holds %zu values, need %zu", out_count, count);

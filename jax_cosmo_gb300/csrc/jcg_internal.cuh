@@ -82,6 +82,16 @@ struct ConstTables {
   float kh2_lo[NKH + 1];
   float tay_rho[NTAYLOR][2];
   float tay_c[NTAYLOR][2];
+  // fp32c table stages in float pairs (hi, lo): the tables of the pair exp
+  // and sin, and pair copies of the abscissae and factors above
+  float2 exp2_ff[64];          // 2^(j/64)
+  float2 sincos_ff[256];       // sin, cos of j pi/64, j < 128 (interleaved)
+  float2 romb_k_ff[NROMB], romb_logk_ff[NROMB], romb_ik_ff[NROMB], romb_kw2_ff[NROMB];
+  float2 kh_ff[NKH], logk_ff[NKH], ikh_ff[NKH], kh3_ff[NKH], simpson_ff[NKH];
+  float2 chi_a_ff[NCHI], lna_chi_ff[NCHI], chi_ia_ff[NCHI], chi_am_ff[NCHI], chi_lnam_ff[NCHI], chi_iam_ff[NCHI];
+  float2 grow_a_ff[NGROW], grow_lna_ff[NGROW], grow_ia_ff[NGROW], grow_am_ff[NGROW], grow_lnam_ff[NGROW],
+      grow_iam_ff[NGROW];
+  double chi_ida[NCHI];        // 1 / (atab_chi[i + 1] - atab_chi[i]) (i < NCHI - 1)
 };
 
 // ------------------------------------------------- per-cosmology tables -----

@@ -8,6 +8,7 @@
 #include "jcg_fp32.cuh"
 #include "jcg_internal.cuh"
 #include "jcg_dual.cuh"
+#include "jcg_ff.cuh"
 
 namespace jcg {
 
@@ -152,8 +153,57 @@ __global__ void const_init_kernel(ConstTables* c) {
   }
 }
 
+// float-pair copies of the grids (after const_init_kernel), and the tables
+// of the pair exp (2^(j/64)) and sin (sin, cos of j pi/64)
+__device__ __forceinline__ float2 f2_of(double v) {
+  const float hi = (float)v;
+  return make_float2(hi, (float)(v - (double)hi));
+}
+
+__global__ void const_ff_kernel(ConstTables* c) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nth = gridDim.x * blockDim.x;
+  for (int j = tid; j < 64; j += nth) c->exp2_ff[j] = f2_of(kExp2Tab64[j]);
+  for (int j = tid; j < 128; j += nth) {
+    const double a = (double)j * (PI / 64.0);
+    c->sincos_ff[2 * j] = f2_of(sin(a));
+    c->sincos_ff[2 * j + 1] = f2_of(cos(a));
+  }
+  for (int e = tid; e < NROMB; e += nth) {
+    c->romb_k_ff[e] = f2_of(c->romb_k[e]);
+    c->romb_logk_ff[e] = f2_of(c->romb_logk[e]);
+    c->romb_ik_ff[e] = f2_of(c->romb_ik[e]);
+    c->romb_kw2_ff[e] = f2_of(c->romb_kw2[e]);
+  }
+  for (int i = tid; i < NKH; i += nth) {
+    c->kh_ff[i] = f2_of(c->kh[i]);
+    c->logk_ff[i] = f2_of(c->logk[i]);
+    c->ikh_ff[i] = f2_of(c->ikh[i]);
+    c->kh3_ff[i] = f2_of(c->kh3[i]);
+    c->simpson_ff[i] = f2_of(c->simpson_kh[i]);
+  }
+  for (int i = tid; i < NCHI; i += nth) {
+    c->chi_a_ff[i] = f2_of(c->chi_a[i]);
+    c->lna_chi_ff[i] = f2_of(c->lna_chi[i]);
+    c->chi_ia_ff[i] = f2_of(c->chi_ia[i]);
+    c->chi_am_ff[i] = f2_of(c->chi_am[i]);
+    c->chi_lnam_ff[i] = f2_of(c->chi_lnam[i]);
+    c->chi_iam_ff[i] = f2_of(c->chi_iam[i]);
+    c->chi_ida[i] = i < NCHI - 1 ? 1.0 / (c->atab_chi[i + 1] - c->atab_chi[i]) : 0.0;
+  }
+  for (int i = tid; i < NGROW; i += nth) {
+    c->grow_a_ff[i] = f2_of(c->atab_grow[i]);
+    c->grow_lna_ff[i] = f2_of(c->grow_lna[i]);
+    c->grow_ia_ff[i] = f2_of(c->grow_ia[i]);
+    c->grow_am_ff[i] = f2_of(c->grow_am[i]);
+    c->grow_lnam_ff[i] = f2_of(c->grow_lnam[i]);
+    c->grow_iam_ff[i] = f2_of(c->grow_iam[i]);
+  }
+}
+
 void launch_const_init(ConstTables* c, cudaStream_t st) {
   const_init_kernel<<<128, 256, 0, st>>>(c);
+  const_ff_kernel<<<4, 256, 0, st>>>(c);
 }
 
 // ------------------------------------------------------------- geometry -----
@@ -318,8 +368,11 @@ void launch_geometry_build(const GeoHeader& h, double* geo, const double* pz, co
 // ------------------------------------------------------ cosmology tables ----
 
 // NW: some item may use the transfer type "eisenhu" (a separate
-// instantiation keeps the default one's registers)
-template <bool NW>
+// instantiation keeps the default one's registers).  FAST (fp32c): the
+// per-node evaluations (chi and growth right-hand sides, the Romberg
+// integrand, P(k) k^3) in float-pair arithmetic on the FP32 pipe; the scans,
+// sigma8's weighted sum and the tables' values stay float64.
+template <bool NW, bool FAST>
 __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const ConstTables* __restrict__ c) {
   const int item = blockIdx.x;
   if (item >= bt.n_items) return;
@@ -336,28 +389,62 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   __shared__ double mv[4 * NGROW];  // per-step growth matrices
   __shared__ double yv[2 * NGROW];  // growth ODE solution (D, dD/da) unnormalised
   __shared__ float2 wpp[NKH];       // fp32c: w pk3 as float pairs
+  __shared__ FF sff[FAST ? NSCAL : 1];                  // fp32c: the scalars as pairs
+  __shared__ float2 e2s[FAST ? 64 : 1], scs[FAST ? 256 : 1];  // tables of the pair exp and sin
+  FF* pk3ff = reinterpret_cast<FF*>(pq);                // fp32c: P(k) k^3 as pairs (pq is free until then)
   const int t = threadIdx.x;
-  for (int i = t; i < NSCAL; i += blockDim.x) s[i] = it.ctab->s[i];  // from cosmo_scalars_kernel
+  for (int i = t; i < NSCAL; i += blockDim.x) {
+    s[i] = it.ctab->s[i];  // from cosmo_scalars_kernel
+    if (FAST) sff[i] = ff_of(s[i]);
+  }
+  if (FAST) {
+    for (int i = t; i < 64; i += blockDim.x) e2s[i] = c->exp2_ff[i];
+    for (int i = t; i < 256; i += blockDim.x) scs[i] = c->sincos_ff[i];
+  }
   __syncthreads();
   const Bg bg = make_bg(s);
+  const auto F2 = [](float2 v) { return FF{v.x, v.y}; };
+  BgF bgf;
+  if (FAST) bgf = BgF{sff[S_OMEGA_M], sff[S_OMEGA_K], sff[S_OMEGA_DE], sff[S_W0], sff[S_WA]};
   // chi RK4 in ln a (background.py:227-231, scipy/ode.py:11-19): the
   // right-hand side does not depend on chi, so each step needs f at its two
   // ends (shared with the neighbouring steps) and at its midpoint.
-  if (t < NCHI) {
-    fnode[t] = dchi_dlna_c(bg, c->chi_a[t], c->lna_chi[t], c->chi_ia[t]);
-    if (t > 0) inc[t] = dchi_dlna_c(bg, c->chi_am[t], c->chi_lnam[t], c->chi_iam[t]);
-  }
-  // growth ODE coefficients at nodes and midpoints
-  if (t < NGROW) {
-    growth_qr_c(bg, c->atab_grow[t], c->grow_lna[t], c->grow_ia[t], qa[t], ra[t]);
-    if (t > 0) growth_qr_c(bg, c->grow_am[t], c->grow_lnam[t], c->grow_iam[t], qm[t], rm[t]);
-  }
-  // sigmasqr(8) integrand at the romb nodes (power.py:70-75): the window
-  // factor k (k W(8k))^2 is a constant of the node
-  if (t < NROMB) {
-    const double logk = c->romb_logk[t];
-    const double T = eh_transfer_lki<NW>(s, c->romb_k[t], logk, c->romb_ik[t]);
-    fr[t] = c->romb_kw2[t] * ((T * T) * exp(s[S_NS] * logk));
+  if (FAST) {
+    if (t < NCHI) {
+      fnode[t] = ffd(ff_dchi_dlna(bgf, F2(c->chi_a_ff[t]), F2(c->lna_chi_ff[t]), F2(c->chi_ia_ff[t]), e2s));
+      if (t > 0) inc[t] = ffd(ff_dchi_dlna(bgf, F2(c->chi_am_ff[t]), F2(c->chi_lnam_ff[t]), F2(c->chi_iam_ff[t]), e2s));
+    }
+    if (t < NGROW) {
+      FF q, r;
+      ff_growth_qr(bgf, F2(c->grow_a_ff[t]), F2(c->grow_lna_ff[t]), F2(c->grow_ia_ff[t]), e2s, q, r);
+      qa[t] = ffd(q), ra[t] = ffd(r);
+      if (t > 0) {
+        ff_growth_qr(bgf, F2(c->grow_am_ff[t]), F2(c->grow_lnam_ff[t]), F2(c->grow_iam_ff[t]), e2s, q, r);
+        qm[t] = ffd(q), rm[t] = ffd(r);
+      }
+    }
+    if (t < NROMB) {
+      const FF logk = F2(c->romb_logk_ff[t]);
+      const FF T = ff_eh_transfer<NW>(sff, F2(c->romb_k_ff[t]), logk, F2(c->romb_ik_ff[t]), s[S_TFNW] != 0.0, e2s, scs);
+      fr[t] = ffd(F2(c->romb_kw2_ff[t]) * (ff_sqr(T) * ff_exp(sff[S_NS] * logk, e2s)));
+    }
+  } else {
+    if (t < NCHI) {
+      fnode[t] = dchi_dlna_c(bg, c->chi_a[t], c->lna_chi[t], c->chi_ia[t]);
+      if (t > 0) inc[t] = dchi_dlna_c(bg, c->chi_am[t], c->chi_lnam[t], c->chi_iam[t]);
+    }
+    // growth ODE coefficients at nodes and midpoints
+    if (t < NGROW) {
+      growth_qr_c(bg, c->atab_grow[t], c->grow_lna[t], c->grow_ia[t], qa[t], ra[t]);
+      if (t > 0) growth_qr_c(bg, c->grow_am[t], c->grow_lnam[t], c->grow_iam[t], qm[t], rm[t]);
+    }
+    // sigmasqr(8) integrand at the romb nodes (power.py:70-75): the window
+    // factor k (k W(8k))^2 is a constant of the node
+    if (t < NROMB) {
+      const double logk = c->romb_logk[t];
+      const double T = eh_transfer_lki<NW>(s, c->romb_k[t], logk, c->romb_ik[t]);
+      fr[t] = c->romb_kw2[t] * ((T * T) * exp(s[S_NS] * logk));
+    }
   }
   __syncthreads();
   // growth: one RK4 step is linear in y = (D, dD/da), y_i = M_i y_{i-1};
@@ -412,28 +499,40 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   }
   __syncthreads();
   // linear P(k_i, a = 1) * k_i^3 on the halofit k grid (power.py:102, 124)
-  for (int i = t; i < NKH; i += blockDim.x) {
-    const double tk = eh_transfer_lki<NW>(s, c->kh[i], c->logk[i], c->ikh[i]);
-    const double g1 = s[S_G1];
-    pk3[i] = exp(s[S_NS] * c->logk[i]) * (tk * tk) * (g1 * g1) * s[S_PKNORM] * c->kh3[i];
+  if (FAST) {
+    const FF g1 = ff_of(s[S_G1]);
+    const FF fac = ff_sqr(g1) * ff_of(s[S_PKNORM]);  // sigma8^2 / sigmasqr(8), set above
+    for (int i = t; i < NKH; i += blockDim.x) {
+      const FF lk = F2(c->logk_ff[i]);
+      const FF tk = ff_eh_transfer<NW>(sff, F2(c->kh_ff[i]), lk, F2(c->ikh_ff[i]), s[S_TFNW] != 0.0, e2s, scs);
+      const FF p = ff_exp(sff[S_NS] * lk, e2s) * ff_sqr(tk) * fac * F2(c->kh3_ff[i]);
+      pk3[i] = ffd(p);
+      // sigma^2(R) sums' k-node factor w pk k^3 / (2 pi^2) as a pair
+      const FF w = F2(c->simpson_ff[i]) * p * ffc(1.0 / (2.0 * (PI * PI)));
+      wpp[i] = make_float2(w.hi, w.lo);
+      pk3ff[i] = p;
+    }
+  } else {
+    for (int i = t; i < NKH; i += blockDim.x) {
+      const double tk = eh_transfer_lki<NW>(s, c->kh[i], c->logk[i], c->ikh[i]);
+      const double g1 = s[S_G1];
+      pk3[i] = exp(s[S_NS] * c->logk[i]) * (tk * tk) * (g1 * g1) * s[S_PKNORM] * c->kh3[i];
+    }
   }
   __syncthreads();
   // sigma^2(R_j) without g^2: simps over ln k of pk k^3 exp(-(k R)^2) / (2 pi^2),
   // with the Simpson weights and 1 / (2 pi^2) folded into the k-node factor:
   // one FMA per (k, R) term
-  for (int i = t; i < NKH; i += blockDim.x) pq[i] = c->simpson_kh[i] * (pk3[i] / (2.0 * (PI * PI)));
-  __syncthreads();
+  if (!FAST) {
+    for (int i = t; i < NKH; i += blockDim.x) pq[i] = c->simpson_kh[i] * (pk3[i] / (2.0 * (PI * PI)));
+    __syncthreads();
+  }
   CosmoTab* out = it.ctab;
-  if (it.precision == JCG_FP32C) {
+  if (FAST) {
     // fp32c: the same sums in float-pair arithmetic (about 1e-13 relative, all
     // terms positive): the FP32 pipe instead of the 1/64-rate FP64 one; the
     // halofit root find on this table then takes the same nodes as with
     // float64 sums except within ~1e-13 of a decision boundary
-    for (int i = t; i < NKH; i += blockDim.x) {  // wpp is free until the Taylor tables below
-      const FF f = ff_of(pq[i]);
-      wpp[i] = make_float2(f.hi, f.lo);
-    }
-    __syncthreads();
     for (int j = t; j < NRT; j += blockDim.x) {
       float ah = 0.f, al = 0.f;
       for (int i = 0; i < NKH; ++i) ff_acc_prod(ah, al, wpp[i], c->Eff[i * NRT + j]);
@@ -450,21 +549,23 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   for (int i = t; i < NSCAL; i += blockDim.x) out->s[i] = s[i];
   for (int i = t; i < NCHI; i += blockDim.x) {
     // segment [i, i+1] slope of the chi table: the `a` of scipy/interpolate.py:55
+    // (fp32c: times the reciprocal of the node spacing)
     const double sl = (i < NCHI - 1)
-                          ? (chis[i + 1] - chis[i]) / (c->atab_chi[i + 1] - c->atab_chi[i])
+                          ? (FAST ? (chis[i + 1] - chis[i]) * c->chi_ida[i]
+                                  : (chis[i + 1] - chis[i]) / (c->atab_chi[i + 1] - c->atab_chi[i]))
                           : 0.0;
     out->chi_slope[i] = sl;
     out->chi32[i] = (float)chis[i];
     out->slope32[i] = (float)sl;
   }
-  if (it.precision == JCG_FP32C) {
+  if (FAST) {
     // fp32c halofit moments: w pk3 as float pairs (float copy for the exp
     // terms), then the Taylor tables by the contracting recurrence
     // Q_m[i + 1] = (Q_m[i] + w_i pk3_i) rho_m in float pairs, one lane per m
     for (int i = t; i < NKH + 15; i += blockDim.x) {
       float hi = 0.f;
       if (i < NKH) {
-        const FF w = ff_of(c->simpson_kh[i] * pk3[i]);
+        const FF w = F2(c->simpson_ff[i]) * pk3ff[i];
         hi = w.hi;
         wpp[i] = make_float2(w.hi, w.lo);
       }
@@ -564,9 +665,11 @@ __global__ void __launch_bounds__(128) growth_gamma_kernel(Batch bt, const Const
 void launch_cosmo_tables(const Batch& b, const ConstTables* c, cudaStream_t st) {
   cosmo_scalars_kernel<<<(b.n_items + 7) / 8, 128, 0, st>>>(b);
   if (tf_nowiggle(b.physics_or))
-    cosmo_tables_kernel<true><<<b.n_items, 256, 0, st>>>(b, c);
+    b.precision == JCG_FP32C ? cosmo_tables_kernel<true, true><<<b.n_items, 256, 0, st>>>(b, c)
+                             : cosmo_tables_kernel<true, false><<<b.n_items, 256, 0, st>>>(b, c);
   else
-    cosmo_tables_kernel<false><<<b.n_items, 256, 0, st>>>(b, c);
+    b.precision == JCG_FP32C ? cosmo_tables_kernel<false, true><<<b.n_items, 256, 0, st>>>(b, c)
+                             : cosmo_tables_kernel<false, false><<<b.n_items, 256, 0, st>>>(b, c);
   if (growth_gamma(b.physics_or)) growth_gamma_kernel<<<b.n_items, 128, 0, st>>>(b, c);
 }
 
