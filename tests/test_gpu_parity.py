@@ -664,7 +664,9 @@ def test_fp32c_float_pair_tables_match_fp64():
         out[prec] = tabs
     for what, name in ((0, "chi"), (1, "growth"), (5, "P(k) k^3"), (6, "sigma^2(R)")):
         a, b = out[_lib.FP32C][what], out[_lib.FP64][what]
-        mask = b.abs() > 0
+        # relative per entry, except where the table is rounding noise around
+        # zero (chi at a = 1 is a difference of two equal prefix sums)
+        mask = b.abs() > 1e-9 * b.abs().amax(dim=1, keepdim=True)
         err = float(((a - b).abs()[mask] / b.abs()[mask]).max())
         print(name, "fp32c float-pair vs fp64: max rel err %.2e" % err)
         assert err < 1e-12, (name, err)
