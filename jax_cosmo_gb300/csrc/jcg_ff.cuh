@@ -130,9 +130,10 @@ __device__ __forceinline__ FF ff_log(FF x, const float2* __restrict__ tab) {
   return (ff(y0) + t) - 0.5f * t.hi * t.hi;
 }
 
-// sin(x), 0 <= x < 2^18 pi (see above).  `sc`: sin and cos of j pi/64, j =
-// 0..127, as float pairs (sin in .x/.y of sc[2j], cos in sc[2j + 1]).
-__device__ __forceinline__ FF ff_sin(FF x, const float2* __restrict__ sc) {
+// sin(x), |x| < 2^18 pi (see above), and cos(x) into *cos_out if given.
+// `sc`: sin and cos of j pi/64, j = 0..127, as float pairs (sin in .x/.y of
+// sc[2j], cos in sc[2j + 1]).
+__device__ __forceinline__ FF ff_sin(FF x, const float2* __restrict__ sc, FF* cos_out = nullptr) {
   // by 2 pi: 2 pi = 6.25 + P2 + P3 + P4 (m 6.25 exact for m < 2^18; m P2
   // and m P3 by two-products, so that the reduced argument keeps ~1e-16
   // absolute accuracy up to the largest m)
@@ -159,9 +160,187 @@ __device__ __forceinline__ FF ff_sin(FF x, const float2* __restrict__ sc) {
   const FF sr = (r - r3 * ffc(1.0 / 6.0)) + r3.hi * r2f * 0.008333334f;
   const FF cr = (1.f - ff_scale2(r2, 0.5f)) + r2f * r2f * (0.041666668f - r2f * 0.0013888889f);
   const float2 s = sc[2 * j], c = sc[2 * j + 1];
+  if (cos_out) *cos_out = FF{c.x, c.y} * cr - FF{s.x, s.y} * sr;
   return FF{s.x, s.y} * cr + FF{c.x, c.y} * sr;
 }
 
+}  // namespace jcg
+
+// ------------------------------------------- tables as literal constants ---
+// The same tables in global memory (read through L1), for code without a
+// staged copy: the forward-mode tangent types below.
+namespace jcg {
+// 2^(j/64), j = 0..63, as float pairs (hi, lo)
+__device__ const float2 kExp2FF[64] = {
+    {0x1.0000000000000p+0f, 0.0f}, {0x1.02c9a40000000p+0f, -0x1.887fa00000000p-28f},
+    {0x1.059b0e0000000p+0f, -0x1.9d4f520000000p-25f}, {0x1.0874520000000p+0f, -0x1.e2990e0000000p-26f},
+    {0x1.0b55860000000p+0f, 0x1.9f31220000000p-25f}, {0x1.0e3ec40000000p+0f, -0x1.a585cc0000000p-25f},
+    {0x1.11301e0000000p+0f, -0x1.fdb4960000000p-25f}, {0x1.1429aa0000000p+0f, 0x1.d525bc0000000p-25f},
+    {0x1.172b840000000p+0f, -0x1.c157420000000p-27f}, {0x1.1a35be0000000p+0f, 0x1.6df96e0000000p-25f},
+    {0x1.1d48740000000p+0f, -0x1.d2e8ca0000000p-25f}, {0x1.2063b80000000p+0f, 0x1.0c519a0000000p-25f},
+    {0x1.2387a60000000p+0f, 0x1.ceac480000000p-25f}, {0x1.26b4560000000p+0f, 0x1.789f380000000p-26f},
+    {0x1.29e9e00000000p+0f, -0x1.5c04240000000p-25f}, {0x1.2d285a0000000p+0f, 0x1.b900c20000000p-26f},
+    {0x1.306fe00000000p+0f, 0x1.4636e20000000p-25f}, {0x1.33c08c0000000p+0f, -0x1.b37d200000000p-25f},
+    {0x1.371a740000000p+0f, -0x1.18aac60000000p-25f}, {0x1.3a7db40000000p+0f, -0x1.634c020000000p-25f},
+    {0x1.3dea640000000p+0f, 0x1.8246840000000p-25f}, {0x1.4160a20000000p+0f, 0x1.f72e2a0000000p-28f},
+    {0x1.44e0860000000p+0f, 0x1.8624b40000000p-30f}, {0x1.486a2c0000000p+0f, -0x1.47d8660000000p-25f},
+    {0x1.4bfdae0000000p+0f, -0x1.593abc0000000p-25f}, {0x1.4f9b280000000p+0f, -0x1.2c5a6c0000000p-25f},
+    {0x1.5342b60000000p+0f, -0x1.2c56100000000p-25f}, {0x1.56f4740000000p+0f, -0x1.295b040000000p-25f},
+    {0x1.5ab07e0000000p+0f, -0x1.5bd5ec0000000p-27f}, {0x1.5e76f20000000p+0f, -0x1.4a5bd60000000p-25f},
+    {0x1.6247ec0000000p+0f, -0x1.f8b5500000000p-25f}, {0x1.6623880000000p+0f, 0x1.2a91120000000p-27f},
+    {0x1.6a09e60000000p+0f, 0x1.9fcef40000000p-26f}, {0x1.6dfb240000000p+0f, -0x1.cd72e80000000p-27f},
+    {0x1.71f75e0000000p+0f, 0x1.1d8bee0000000p-25f}, {0x1.75feb60000000p+0f, -0x1.37b3060000000p-25f},
+    {0x1.7a11480000000p+0f, -0x1.829fd00000000p-25f}, {0x1.7e2f340000000p+0f, -0x1.2616340000000p-25f},
+    {0x1.82589a0000000p+0f, -0x1.accc7c0000000p-26f}, {0x1.868d9a0000000p+0f, -0x1.2edb440000000p-26f},
+    {0x1.8ace540000000p+0f, 0x1.15506e0000000p-27f}, {0x1.8f1aea0000000p+0f, -0x1.baa2320000000p-26f},
+    {0x1.93737c0000000p+0f, -0x1.e647440000000p-25f}, {0x1.97d82a0000000p+0f, -0x1.0d8d840000000p-31f},
+    {0x1.9c49180000000p+0f, 0x1.51f8480000000p-27f}, {0x1.a0c6680000000p+0f, -0x1.2886a60000000p-26f},
+    {0x1.a5503c0000000p+0f, -0x1.b83b540000000p-25f}, {0x1.a9e6b60000000p+0f, -0x1.50c0480000000p-25f},
+    {0x1.ae89fa0000000p+0f, -0x1.a94b140000000p-26f}, {0x1.b33a2c0000000p+0f, -0x1.ec3a820000000p-26f},
+    {0x1.b7f7700000000p+0f, -0x1.a094380000000p-25f}, {0x1.bcc1ea0000000p+0f, -0x1.f687c60000000p-25f},
+    {0x1.c199be0000000p+0f, -0x1.3d56b20000000p-27f}, {0x1.c67f120000000p+0f, 0x1.cafa2a0000000p-25f},
+    {0x1.cb720e0000000p+0f, -0x1.8837cc0000000p-27f}, {0x1.d072d40000000p+0f, 0x1.40f1300000000p-25f},
+    {0x1.d5818e0000000p+0f, -0x1.822dbc0000000p-27f}, {0x1.da9e600000000p+0f, 0x1.ed99420000000p-27f},
+    {0x1.dfc9740000000p+0f, -0x1.908c940000000p-25f}, {0x1.e502ee0000000p+0f, 0x1.e2cffe0000000p-26f},
+    {0x1.ea4afa0000000p+0f, 0x1.52486c0000000p-27f}, {0x1.efa1be0000000p+0f, 0x1.cc2b440000000p-25f},
+    {0x1.f507660000000p+0f, -0x1.246eb00000000p-26f}, {0x1.fa7c180000000p+0f, 0x1.9e90d80000000p-28f},
+};
+// sin and cos of j pi/64, j = 0..127, interleaved, as float pairs (hi, lo)
+__device__ const float2 kSinCosFF[256] = {
+    {0.0f, 0.0f}, {0x1.0000000000000p+0f, 0.0f},
+    {0x1.91f6600000000p-5f, -0x1.de44fe0000000p-30f}, {0x1.ff621e0000000p-1f, 0x1.bcb6be0000000p-28f},
+    {0x1.917a6c0000000p-4f, -0x1.eb25ea0000000p-31f}, {0x1.fd88da0000000p-1f, 0x1.e892920000000p-28f},
+    {0x1.2c81060000000p-3f, 0x1.d1cc280000000p-28f}, {0x1.fa75580000000p-1f, -0x1.eeb5d20000000p-30f},
+    {0x1.8f8b840000000p-3f, -0x1.cb2cfa0000000p-30f}, {0x1.f6297c0000000p-1f, 0x1.feeb960000000p-26f},
+    {0x1.f19f980000000p-3f, -0x1.37a83a0000000p-29f}, {0x1.f0a7f00000000p-1f, -0x1.1b73ca0000000p-27f},
+    {0x1.2940620000000p-2f, 0x1.dab3e00000000p-27f}, {0x1.e9f4160000000p-1f, -0x1.273a440000000p-26f},
+    {0x1.58f9a80000000p-2f, -0x1.4a9c040000000p-27f}, {0x1.e212100000000p-1f, 0x1.3da1ba0000000p-27f},
+    {0x1.87de2a0000000p-2f, 0x1.abaa580000000p-28f}, {0x1.d906bc0000000p-1f, 0x1.e651a80000000p-26f},
+    {0x1.b5d1000000000p-2f, 0x1.3c2b980000000p-27f}, {0x1.ced7b00000000p-1f, -0x1.7867120000000p-26f},
+    {0x1.e2b5d40000000p-2f, -0x1.fe42720000000p-28f}, {0x1.c38b300000000p-1f, -0x1.cfe84a0000000p-26f},
+    {0x1.07387a0000000p-1f, -0x1.b740040000000p-27f}, {0x1.b728340000000p-1f, 0x1.465b900000000p-27f},
+    {0x1.1c73b40000000p-1f, -0x1.9465ce0000000p-27f}, {0x1.a9b6620000000p-1f, 0x1.21d4340000000p-26f},
+    {0x1.30ff800000000p-1f, -0x1.8f47e60000000p-28f}, {0x1.9b3e040000000p-1f, 0x1.fce1d00000000p-27f},
+    {0x1.44cf320000000p-1f, 0x1.4247760000000p-27f}, {0x1.8bc8060000000p-1f, 0x1.62a2e80000000p-26f},
+    {0x1.57d6940000000p-1f, -0x1.6e626c0000000p-26f}, {0x1.7b5df20000000p-1f, 0x1.3557d80000000p-28f},
+    {0x1.6a09e60000000p-1f, 0x1.9fcef40000000p-27f}, {0x1.6a09e60000000p-1f, 0x1.9fcef40000000p-27f},
+    {0x1.7b5df20000000p-1f, 0x1.3557d80000000p-28f}, {0x1.57d6940000000p-1f, -0x1.6e626c0000000p-26f},
+    {0x1.8bc8060000000p-1f, 0x1.62a2e80000000p-26f}, {0x1.44cf320000000p-1f, 0x1.4247760000000p-27f},
+    {0x1.9b3e040000000p-1f, 0x1.fce1d00000000p-27f}, {0x1.30ff800000000p-1f, -0x1.8f47e60000000p-28f},
+    {0x1.a9b6620000000p-1f, 0x1.21d4340000000p-26f}, {0x1.1c73b40000000p-1f, -0x1.9465ce0000000p-27f},
+    {0x1.b728340000000p-1f, 0x1.465b900000000p-27f}, {0x1.07387a0000000p-1f, -0x1.b740040000000p-27f},
+    {0x1.c38b300000000p-1f, -0x1.cfe84a0000000p-26f}, {0x1.e2b5d40000000p-2f, -0x1.fe42720000000p-28f},
+    {0x1.ced7b00000000p-1f, -0x1.7867120000000p-26f}, {0x1.b5d1000000000p-2f, 0x1.3c2b980000000p-27f},
+    {0x1.d906bc0000000p-1f, 0x1.e651a80000000p-26f}, {0x1.87de2a0000000p-2f, 0x1.abaa580000000p-28f},
+    {0x1.e212100000000p-1f, 0x1.3da1ba0000000p-27f}, {0x1.58f9a80000000p-2f, -0x1.4a9c040000000p-27f},
+    {0x1.e9f4160000000p-1f, -0x1.273a440000000p-26f}, {0x1.2940620000000p-2f, 0x1.dab3e00000000p-27f},
+    {0x1.f0a7f00000000p-1f, -0x1.1b73ca0000000p-27f}, {0x1.f19f980000000p-3f, -0x1.37a83a0000000p-29f},
+    {0x1.f6297c0000000p-1f, 0x1.feeb960000000p-26f}, {0x1.8f8b840000000p-3f, -0x1.cb2cfa0000000p-30f},
+    {0x1.fa75580000000p-1f, -0x1.eeb5d20000000p-30f}, {0x1.2c81060000000p-3f, 0x1.d1cc280000000p-28f},
+    {0x1.fd88da0000000p-1f, 0x1.e892920000000p-28f}, {0x1.917a6c0000000p-4f, -0x1.eb25ea0000000p-31f},
+    {0x1.ff621e0000000p-1f, 0x1.bcb6be0000000p-28f}, {0x1.91f6600000000p-5f, -0x1.de44fe0000000p-30f},
+    {0x1.0000000000000p+0f, 0.0f}, {0.0f, 0.0f},
+    {0x1.ff621e0000000p-1f, 0x1.bcb6be0000000p-28f}, {-0x1.91f6600000000p-5f, 0x1.de44fe0000000p-30f},
+    {0x1.fd88da0000000p-1f, 0x1.e892920000000p-28f}, {-0x1.917a6c0000000p-4f, 0x1.eb25ea0000000p-31f},
+    {0x1.fa75580000000p-1f, -0x1.eeb5d20000000p-30f}, {-0x1.2c81060000000p-3f, -0x1.d1cc280000000p-28f},
+    {0x1.f6297c0000000p-1f, 0x1.feeb960000000p-26f}, {-0x1.8f8b840000000p-3f, 0x1.cb2cfa0000000p-30f},
+    {0x1.f0a7f00000000p-1f, -0x1.1b73ca0000000p-27f}, {-0x1.f19f980000000p-3f, 0x1.37a83a0000000p-29f},
+    {0x1.e9f4160000000p-1f, -0x1.273a440000000p-26f}, {-0x1.2940620000000p-2f, -0x1.dab3e00000000p-27f},
+    {0x1.e212100000000p-1f, 0x1.3da1ba0000000p-27f}, {-0x1.58f9a80000000p-2f, 0x1.4a9c040000000p-27f},
+    {0x1.d906bc0000000p-1f, 0x1.e651a80000000p-26f}, {-0x1.87de2a0000000p-2f, -0x1.abaa580000000p-28f},
+    {0x1.ced7b00000000p-1f, -0x1.7867120000000p-26f}, {-0x1.b5d1000000000p-2f, -0x1.3c2b980000000p-27f},
+    {0x1.c38b300000000p-1f, -0x1.cfe84a0000000p-26f}, {-0x1.e2b5d40000000p-2f, 0x1.fe42720000000p-28f},
+    {0x1.b728340000000p-1f, 0x1.465b900000000p-27f}, {-0x1.07387a0000000p-1f, 0x1.b740040000000p-27f},
+    {0x1.a9b6620000000p-1f, 0x1.21d4340000000p-26f}, {-0x1.1c73b40000000p-1f, 0x1.9465ce0000000p-27f},
+    {0x1.9b3e040000000p-1f, 0x1.fce1d00000000p-27f}, {-0x1.30ff800000000p-1f, 0x1.8f47e60000000p-28f},
+    {0x1.8bc8060000000p-1f, 0x1.62a2e80000000p-26f}, {-0x1.44cf320000000p-1f, -0x1.4247760000000p-27f},
+    {0x1.7b5df20000000p-1f, 0x1.3557d80000000p-28f}, {-0x1.57d6940000000p-1f, 0x1.6e626c0000000p-26f},
+    {0x1.6a09e60000000p-1f, 0x1.9fcef40000000p-27f}, {-0x1.6a09e60000000p-1f, -0x1.9fcef40000000p-27f},
+    {0x1.57d6940000000p-1f, -0x1.6e626c0000000p-26f}, {-0x1.7b5df20000000p-1f, -0x1.3557d80000000p-28f},
+    {0x1.44cf320000000p-1f, 0x1.4247760000000p-27f}, {-0x1.8bc8060000000p-1f, -0x1.62a2e80000000p-26f},
+    {0x1.30ff800000000p-1f, -0x1.8f47e60000000p-28f}, {-0x1.9b3e040000000p-1f, -0x1.fce1d00000000p-27f},
+    {0x1.1c73b40000000p-1f, -0x1.9465ce0000000p-27f}, {-0x1.a9b6620000000p-1f, -0x1.21d4340000000p-26f},
+    {0x1.07387a0000000p-1f, -0x1.b740040000000p-27f}, {-0x1.b728340000000p-1f, -0x1.465b900000000p-27f},
+    {0x1.e2b5d40000000p-2f, -0x1.fe42720000000p-28f}, {-0x1.c38b300000000p-1f, 0x1.cfe84a0000000p-26f},
+    {0x1.b5d1000000000p-2f, 0x1.3c2b980000000p-27f}, {-0x1.ced7b00000000p-1f, 0x1.7867120000000p-26f},
+    {0x1.87de2a0000000p-2f, 0x1.abaa580000000p-28f}, {-0x1.d906bc0000000p-1f, -0x1.e651a80000000p-26f},
+    {0x1.58f9a80000000p-2f, -0x1.4a9c040000000p-27f}, {-0x1.e212100000000p-1f, -0x1.3da1ba0000000p-27f},
+    {0x1.2940620000000p-2f, 0x1.dab3e00000000p-27f}, {-0x1.e9f4160000000p-1f, 0x1.273a440000000p-26f},
+    {0x1.f19f980000000p-3f, -0x1.37a83a0000000p-29f}, {-0x1.f0a7f00000000p-1f, 0x1.1b73ca0000000p-27f},
+    {0x1.8f8b840000000p-3f, -0x1.cb2cfa0000000p-30f}, {-0x1.f6297c0000000p-1f, -0x1.feeb960000000p-26f},
+    {0x1.2c81060000000p-3f, 0x1.d1cc280000000p-28f}, {-0x1.fa75580000000p-1f, 0x1.eeb5d20000000p-30f},
+    {0x1.917a6c0000000p-4f, -0x1.eb25ea0000000p-31f}, {-0x1.fd88da0000000p-1f, -0x1.e892920000000p-28f},
+    {0x1.91f6600000000p-5f, -0x1.de44fe0000000p-30f}, {-0x1.ff621e0000000p-1f, -0x1.bcb6be0000000p-28f},
+    {0.0f, 0.0f}, {-0x1.0000000000000p+0f, 0.0f},
+    {-0x1.91f6600000000p-5f, 0x1.de44fe0000000p-30f}, {-0x1.ff621e0000000p-1f, -0x1.bcb6be0000000p-28f},
+    {-0x1.917a6c0000000p-4f, 0x1.eb25ea0000000p-31f}, {-0x1.fd88da0000000p-1f, -0x1.e892920000000p-28f},
+    {-0x1.2c81060000000p-3f, -0x1.d1cc280000000p-28f}, {-0x1.fa75580000000p-1f, 0x1.eeb5d20000000p-30f},
+    {-0x1.8f8b840000000p-3f, 0x1.cb2cfa0000000p-30f}, {-0x1.f6297c0000000p-1f, -0x1.feeb960000000p-26f},
+    {-0x1.f19f980000000p-3f, 0x1.37a83a0000000p-29f}, {-0x1.f0a7f00000000p-1f, 0x1.1b73ca0000000p-27f},
+    {-0x1.2940620000000p-2f, -0x1.dab3e00000000p-27f}, {-0x1.e9f4160000000p-1f, 0x1.273a440000000p-26f},
+    {-0x1.58f9a80000000p-2f, 0x1.4a9c040000000p-27f}, {-0x1.e212100000000p-1f, -0x1.3da1ba0000000p-27f},
+    {-0x1.87de2a0000000p-2f, -0x1.abaa580000000p-28f}, {-0x1.d906bc0000000p-1f, -0x1.e651a80000000p-26f},
+    {-0x1.b5d1000000000p-2f, -0x1.3c2b980000000p-27f}, {-0x1.ced7b00000000p-1f, 0x1.7867120000000p-26f},
+    {-0x1.e2b5d40000000p-2f, 0x1.fe42720000000p-28f}, {-0x1.c38b300000000p-1f, 0x1.cfe84a0000000p-26f},
+    {-0x1.07387a0000000p-1f, 0x1.b740040000000p-27f}, {-0x1.b728340000000p-1f, -0x1.465b900000000p-27f},
+    {-0x1.1c73b40000000p-1f, 0x1.9465ce0000000p-27f}, {-0x1.a9b6620000000p-1f, -0x1.21d4340000000p-26f},
+    {-0x1.30ff800000000p-1f, 0x1.8f47e60000000p-28f}, {-0x1.9b3e040000000p-1f, -0x1.fce1d00000000p-27f},
+    {-0x1.44cf320000000p-1f, -0x1.4247760000000p-27f}, {-0x1.8bc8060000000p-1f, -0x1.62a2e80000000p-26f},
+    {-0x1.57d6940000000p-1f, 0x1.6e626c0000000p-26f}, {-0x1.7b5df20000000p-1f, -0x1.3557d80000000p-28f},
+    {-0x1.6a09e60000000p-1f, -0x1.9fcef40000000p-27f}, {-0x1.6a09e60000000p-1f, -0x1.9fcef40000000p-27f},
+    {-0x1.7b5df20000000p-1f, -0x1.3557d80000000p-28f}, {-0x1.57d6940000000p-1f, 0x1.6e626c0000000p-26f},
+    {-0x1.8bc8060000000p-1f, -0x1.62a2e80000000p-26f}, {-0x1.44cf320000000p-1f, -0x1.4247760000000p-27f},
+    {-0x1.9b3e040000000p-1f, -0x1.fce1d00000000p-27f}, {-0x1.30ff800000000p-1f, 0x1.8f47e60000000p-28f},
+    {-0x1.a9b6620000000p-1f, -0x1.21d4340000000p-26f}, {-0x1.1c73b40000000p-1f, 0x1.9465ce0000000p-27f},
+    {-0x1.b728340000000p-1f, -0x1.465b900000000p-27f}, {-0x1.07387a0000000p-1f, 0x1.b740040000000p-27f},
+    {-0x1.c38b300000000p-1f, 0x1.cfe84a0000000p-26f}, {-0x1.e2b5d40000000p-2f, 0x1.fe42720000000p-28f},
+    {-0x1.ced7b00000000p-1f, 0x1.7867120000000p-26f}, {-0x1.b5d1000000000p-2f, -0x1.3c2b980000000p-27f},
+    {-0x1.d906bc0000000p-1f, -0x1.e651a80000000p-26f}, {-0x1.87de2a0000000p-2f, -0x1.abaa580000000p-28f},
+    {-0x1.e212100000000p-1f, -0x1.3da1ba0000000p-27f}, {-0x1.58f9a80000000p-2f, 0x1.4a9c040000000p-27f},
+    {-0x1.e9f4160000000p-1f, 0x1.273a440000000p-26f}, {-0x1.2940620000000p-2f, -0x1.dab3e00000000p-27f},
+    {-0x1.f0a7f00000000p-1f, 0x1.1b73ca0000000p-27f}, {-0x1.f19f980000000p-3f, 0x1.37a83a0000000p-29f},
+    {-0x1.f6297c0000000p-1f, -0x1.feeb960000000p-26f}, {-0x1.8f8b840000000p-3f, 0x1.cb2cfa0000000p-30f},
+    {-0x1.fa75580000000p-1f, 0x1.eeb5d20000000p-30f}, {-0x1.2c81060000000p-3f, -0x1.d1cc280000000p-28f},
+    {-0x1.fd88da0000000p-1f, -0x1.e892920000000p-28f}, {-0x1.917a6c0000000p-4f, 0x1.eb25ea0000000p-31f},
+    {-0x1.ff621e0000000p-1f, -0x1.bcb6be0000000p-28f}, {-0x1.91f6600000000p-5f, 0x1.de44fe0000000p-30f},
+    {-0x1.0000000000000p+0f, 0.0f}, {0.0f, 0.0f},
+    {-0x1.ff621e0000000p-1f, -0x1.bcb6be0000000p-28f}, {0x1.91f6600000000p-5f, -0x1.de44fe0000000p-30f},
+    {-0x1.fd88da0000000p-1f, -0x1.e892920000000p-28f}, {0x1.917a6c0000000p-4f, -0x1.eb25ea0000000p-31f},
+    {-0x1.fa75580000000p-1f, 0x1.eeb5d20000000p-30f}, {0x1.2c81060000000p-3f, 0x1.d1cc280000000p-28f},
+    {-0x1.f6297c0000000p-1f, -0x1.feeb960000000p-26f}, {0x1.8f8b840000000p-3f, -0x1.cb2cfa0000000p-30f},
+    {-0x1.f0a7f00000000p-1f, 0x1.1b73ca0000000p-27f}, {0x1.f19f980000000p-3f, -0x1.37a83a0000000p-29f},
+    {-0x1.e9f4160000000p-1f, 0x1.273a440000000p-26f}, {0x1.2940620000000p-2f, 0x1.dab3e00000000p-27f},
+    {-0x1.e212100000000p-1f, -0x1.3da1ba0000000p-27f}, {0x1.58f9a80000000p-2f, -0x1.4a9c040000000p-27f},
+    {-0x1.d906bc0000000p-1f, -0x1.e651a80000000p-26f}, {0x1.87de2a0000000p-2f, 0x1.abaa580000000p-28f},
+    {-0x1.ced7b00000000p-1f, 0x1.7867120000000p-26f}, {0x1.b5d1000000000p-2f, 0x1.3c2b980000000p-27f},
+    {-0x1.c38b300000000p-1f, 0x1.cfe84a0000000p-26f}, {0x1.e2b5d40000000p-2f, -0x1.fe42720000000p-28f},
+    {-0x1.b728340000000p-1f, -0x1.465b900000000p-27f}, {0x1.07387a0000000p-1f, -0x1.b740040000000p-27f},
+    {-0x1.a9b6620000000p-1f, -0x1.21d4340000000p-26f}, {0x1.1c73b40000000p-1f, -0x1.9465ce0000000p-27f},
+    {-0x1.9b3e040000000p-1f, -0x1.fce1d00000000p-27f}, {0x1.30ff800000000p-1f, -0x1.8f47e60000000p-28f},
+    {-0x1.8bc8060000000p-1f, -0x1.62a2e80000000p-26f}, {0x1.44cf320000000p-1f, 0x1.4247760000000p-27f},
+    {-0x1.7b5df20000000p-1f, -0x1.3557d80000000p-28f}, {0x1.57d6940000000p-1f, -0x1.6e626c0000000p-26f},
+    {-0x1.6a09e60000000p-1f, -0x1.9fcef40000000p-27f}, {0x1.6a09e60000000p-1f, 0x1.9fcef40000000p-27f},
+    {-0x1.57d6940000000p-1f, 0x1.6e626c0000000p-26f}, {0x1.7b5df20000000p-1f, 0x1.3557d80000000p-28f},
+    {-0x1.44cf320000000p-1f, -0x1.4247760000000p-27f}, {0x1.8bc8060000000p-1f, 0x1.62a2e80000000p-26f},
+    {-0x1.30ff800000000p-1f, 0x1.8f47e60000000p-28f}, {0x1.9b3e040000000p-1f, 0x1.fce1d00000000p-27f},
+    {-0x1.1c73b40000000p-1f, 0x1.9465ce0000000p-27f}, {0x1.a9b6620000000p-1f, 0x1.21d4340000000p-26f},
+    {-0x1.07387a0000000p-1f, 0x1.b740040000000p-27f}, {0x1.b728340000000p-1f, 0x1.465b900000000p-27f},
+    {-0x1.e2b5d40000000p-2f, 0x1.fe42720000000p-28f}, {0x1.c38b300000000p-1f, -0x1.cfe84a0000000p-26f},
+    {-0x1.b5d1000000000p-2f, -0x1.3c2b980000000p-27f}, {0x1.ced7b00000000p-1f, -0x1.7867120000000p-26f},
+    {-0x1.87de2a0000000p-2f, -0x1.abaa580000000p-28f}, {0x1.d906bc0000000p-1f, 0x1.e651a80000000p-26f},
+    {-0x1.58f9a80000000p-2f, 0x1.4a9c040000000p-27f}, {0x1.e212100000000p-1f, 0x1.3da1ba0000000p-27f},
+    {-0x1.2940620000000p-2f, -0x1.dab3e00000000p-27f}, {0x1.e9f4160000000p-1f, -0x1.273a440000000p-26f},
+    {-0x1.f19f980000000p-3f, 0x1.37a83a0000000p-29f}, {0x1.f0a7f00000000p-1f, -0x1.1b73ca0000000p-27f},
+    {-0x1.8f8b840000000p-3f, 0x1.cb2cfa0000000p-30f}, {0x1.f6297c0000000p-1f, 0x1.feeb960000000p-26f},
+    {-0x1.2c81060000000p-3f, -0x1.d1cc280000000p-28f}, {0x1.fa75580000000p-1f, -0x1.eeb5d20000000p-30f},
+    {-0x1.917a6c0000000p-4f, 0x1.eb25ea0000000p-31f}, {0x1.fd88da0000000p-1f, 0x1.e892920000000p-28f},
+    {-0x1.91f6600000000p-5f, 0x1.de44fe0000000p-30f}, {0x1.ff621e0000000p-1f, 0x1.bcb6be0000000p-28f},
+};
+
+__device__ __forceinline__ FF ff_exp(FF x) { return ff_exp(x, kExp2FF); }
+__device__ __forceinline__ FF ff_log(FF x) { return ff_log(x, kExp2FF); }
+__device__ __forceinline__ FF ff_sin(FF x) { return ff_sin(x, kSinCosFF); }
+__device__ __forceinline__ FF ff_sincos(FF x, FF* c) { return ff_sin(x, kSinCosFF, c); }
 }  // namespace jcg
 
 // ------------------------------------------------ physics in float pairs ---

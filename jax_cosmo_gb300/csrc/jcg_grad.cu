@@ -19,9 +19,12 @@
 
 #include "jcg_fp32.cuh"
 #include "jcg_grad.cuh"
+#include "jcg_dualff.cuh"
 
 namespace jcg {
 
+// value as a float pair, 8 FP32 tangents: the fp32c table stages (jcg_dualff.cuh)
+typedef DualFF<NDIR> FF8;
 
 // Tables of one cosmology with tangents.  Lanes: dir = tid & 7, item = tid >> 3.
 // F32T (fp32c Jacobian): the per-node evaluations (ODE right-hand sides,
@@ -59,8 +62,8 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     if (dir == 0) arr[e] = x.v;
     arr[(1 + dir) * stride + e] = x.d[0];
   };
-  auto putf = [&](double* arr, int stride, int e, const F8& x) {
-    arr[e] = x.v;
+  auto putf = [&](double* arr, int stride, int e, const auto& x) {
+    arr[e] = val(x);
 #pragma unroll
     for (int d = 0; d < NDIR; ++d) arr[(1 + d) * stride + e] = x.d[d];
   };
@@ -106,9 +109,9 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     const double* src = gb.gnode + (size_t)item * GNODE_STRIDE;
     for (int i = t; i < GNODE_U; i += blockDim.x) fn[i] = src[i];
   } else {
-    F8 sF[NSCAL];
-    for (int i = 0; i < NSCAL; ++i) sF[i] = f8_of(sv[i], sd + i, NSCAL);
-    const BgT<F8> bgf = make_bgT(sF);
+    FF8 sF[NSCAL];
+    for (int i = 0; i < NSCAL; ++i) sF[i] = ff8_of(sv[i], sd + i, NSCAL);
+    const BgT<FF8> bgf = make_bgT(sF);
     // cosmology-independent abscissae, logs, reciprocals and window factors
     // from the constant grids
     for (int e = t; e < 2 * NCHI; e += blockDim.x) {
@@ -120,7 +123,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       }
     }
     for (int e = t; e < 2 * NGROW; e += blockDim.x) {
-      F8 q, r;
+      FF8 q, r;
       if (e < NGROW) {
         growth_qr_cT(bgf, c->atab_grow[e], c->grow_lna[e], c->grow_ia[e], q, r);
         putf(qr + 0 * (NDIR + 1) * NGROW, NGROW, e, q);
@@ -134,7 +137,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     }
     for (int e = t; e < NROMB; e += blockDim.x) {
       const double logk = c->romb_logk[e];
-      const F8 T = eh_transferT<NW>(sF, c->romb_k[e], logk);
+      const FF8 T = eh_transferT<NW>(sF, c->romb_k[e], logk);
       putf(fr, NROMB, e, c->romb_kw2[e] * ((T * T) * xexp(sF[S_NS] * logk)));
     }
   }
@@ -156,18 +159,18 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       const double* RA = qr + (NDIR + 1) * NGROW;
       const double* QM = qr + 2 * (NDIR + 1) * NGROW;
       const double* RM = qr + 3 * (NDIR + 1) * NGROW;
-      auto g8 = [&](const double* arr, int e) { return f8_of(arr[e], arr + NGROW + e, NGROW); };
-      const F8 qa0 = g8(QA, t - 1), ra0 = g8(RA, t - 1), qm = g8(QM, t), rm = g8(RM, t);
-      const F8 qa1 = g8(QA, t), ra1 = g8(RA, t);
+      auto g8 = [&](const double* arr, int e) { return ff8_of(arr[e], arr + NGROW + e, NGROW); };
+      const FF8 qa0 = g8(QA, t - 1), ra0 = g8(RA, t - 1), qm = g8(QM, t), rm = g8(RM, t);
+      const FF8 qa1 = g8(QA, t), ra1 = g8(RA, t);
       const double hh = c->atab_grow[t] - c->atab_grow[t - 1];
-      const F8 one = fconst<NDIR>(1.0), zero = fconst<NDIR>(0.0);
-      F8 o0, o1;
+      const FF8 one = ffd_const<NDIR>(1.0), zero = ffd_const<NDIR>(0.0);
+      FF8 o0, o1;
       growth_rk4_step(one, zero, qa0, ra0, qm, rm, qa1, ra1, hh, o0, o1);  // column 0
-      m4[0] = o0.v, m4[2] = o1.v;
+      m4[0] = val(o0), m4[2] = val(o1);
 #pragma unroll
       for (int d = 0; d < NDIR; ++d) dm4[0][d] = o0.d[d], dm4[2][d] = o1.d[d];
       growth_rk4_step(zero, one, qa0, ra0, qm, rm, qa1, ra1, hh, o0, o1);  // column 1
-      m4[1] = o0.v, m4[3] = o1.v;
+      m4[1] = val(o0), m4[3] = val(o1);
 #pragma unroll
       for (int d = 0; d < NDIR; ++d) dm4[1][d] = o0.d[d], dm4[3][d] = o1.d[d];
     }
@@ -371,21 +374,21 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       put(pq, NKH, e, p3 / (2.0 * (PI * PI)));
     }
   } else {
-    F8 sF[NSCAL];
-    for (int i = 0; i < NSCAL; ++i) sF[i] = f8_of(sv[i], sd + i, NSCAL);
-    const F8 g1f = f8_of(g1s[0], g1s + 1, 1);
+    FF8 sF[NSCAL];
+    for (int i = 0; i < NSCAL; ++i) sF[i] = ff8_of(sv[i], sd + i, NSCAL);
+    const FF8 g1f = ff8_of(g1s[0], g1s + 1, 1);
     const double* gu = gb.gnode ? gb.gnode + (size_t)item * GNODE_STRIDE + GNODE_U : nullptr;
     for (int e = t; e < NKH; e += blockDim.x) {
       const double k = c->kh[e];
-      F8 p3;
+      FF8 p3;
       if (gu) {
         // pk_linearT's order: ((exp(n_s ln k) T^2) g^2) pknorm, then k^3
-        const F8 u = f8_of(gu[e], gu + NKH + e, NKH);
+        const FF8 u = ff8_of(gu[e], gu + NKH + e, NKH);
         p3 = ((u * (g1f * g1f)) * sF[S_PKNORM]) * c->kh3[e];
       } else {
         p3 = pk_linearT<NW>(sF, k, c->logk[e], g1f) * c->kh3[e];
       }
-      out->pk3v[e] = p3.v;
+      out->pk3v[e] = val(p3);
 #pragma unroll
       for (int d = 0; d < NDIR; ++d) {
         out->pk3d[d][e] = p3.d[d];
@@ -1518,12 +1521,12 @@ __global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const Con
   if (e >= GNODE_WORK) return;
   const GradItem gi = grad_item(gb, item);
   const TabD* tb = gi.tab;
-  F8 sF[NSCAL];
-  for (int i = 0; i < NSCAL; ++i) sF[i] = f8_of(tb->sv[i], &tb->sd[0][i], NSCAL);
-  const BgT<F8> bgf = make_bgT(sF);
+  FF8 sF[NSCAL];
+  for (int i = 0; i < NSCAL; ++i) sF[i] = ff8_of(tb->sv[i], &tb->sd[0][i], NSCAL);
+  const BgT<FF8> bgf = make_bgT(sF);
   double* dst = gb.gnode + (size_t)item * GNODE_STRIDE;
-  auto putf = [&](int off, int stride, int i, const F8& x) {
-    dst[off + i] = x.v;
+  auto putf = [&](int off, int stride, int i, const FF8& x) {
+    dst[off + i] = val(x);
 #pragma unroll
     for (int d = 0; d < NDIR; ++d) dst[off + (1 + d) * stride + i] = x.d[d];
   };
@@ -1540,7 +1543,7 @@ __global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const Con
   }
   w -= NCHI - 1;
   if (w < NGROW) {
-    F8 q, r;
+    FF8 q, r;
     growth_qr_cT(bgf, c->atab_grow[w], c->grow_lna[w], c->grow_ia[w], q, r);
     putf(GNODE_QR, NGROW, w, q);
     putf(GNODE_QR + (NDIR + 1) * NGROW, NGROW, w, r);
@@ -1549,7 +1552,7 @@ __global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const Con
   w -= NGROW;
   if (w < NGROW - 1) {
     const int i = w + 1;
-    F8 q, r;
+    FF8 q, r;
     growth_qr_cT(bgf, c->grow_am[i], c->grow_lnam[i], c->grow_iam[i], q, r);
     putf(GNODE_QR + 2 * (NDIR + 1) * NGROW, NGROW, i, q);
     putf(GNODE_QR + 3 * (NDIR + 1) * NGROW, NGROW, i, r);
@@ -1558,13 +1561,13 @@ __global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const Con
   w -= NGROW - 1;
   if (w < NROMB) {
     const double logk = c->romb_logk[w];
-    const F8 T = eh_transferT(sF, c->romb_k[w], logk);
+    const FF8 T = eh_transferT(sF, c->romb_k[w], logk);
     putf(GNODE_FR, NROMB, w, c->romb_kw2[w] * ((T * T) * xexp(sF[S_NS] * logk)));
     return;
   }
   w -= NROMB;
   {
-    const F8 T = eh_transferT(sF, c->kh[w], c->logk[w]);
+    const FF8 T = eh_transferT(sF, c->kh[w], c->logk[w]);
     putf(GNODE_U, NKH, w, xexp(sF[S_NS] * c->logk[w]) * (T * T));
   }
 }
