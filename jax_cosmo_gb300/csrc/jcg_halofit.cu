@@ -8,6 +8,7 @@
 // rate is ~1/70 of its FP32 rate, so the per-node scalar work runs
 // thread-parallel instead.)
 #include "jcg_fp32.cuh"
+#include "jcg_ff.cuh"
 #include "jcg_internal.cuh"
 #include "jcg_dual.cuh"
 
@@ -291,6 +292,40 @@ __device__ __forceinline__ double root_knl_thread(const double* sig, double g2,
   return 1.0 / R;                          // power.py:118
 }
 
+// fp32c: the same root find with the interpolation (power.py:112-115) in
+// float pairs: the segment is chosen in float64 exactly as above (the
+// decision), then R = exp(root) with root = logr[ind] + slope (1 - xp_ind) by
+// the pair quotient and exp.  Returns R = 1 / k_nl.
+__device__ __forceinline__ FF root_R_ff(const double* sig, double g2, const ConstTables* __restrict__ c,
+                                        const float2* e2) {
+  int lo = 0, hi = NRT;
+  while (lo < hi) {
+    const int mid = (lo + hi) >> 1;
+    if (sig[mid] * g2 > 1.0) lo = mid + 1;
+    else hi = mid;
+  }
+  const int cc = lo;
+  int best = cc < NRT ? cc : NRT - 1;
+  if (cc >= 1) {
+    const double dlo = 1.0 - sig[cc - 1] * g2;
+    if (cc < NRT) {
+      const double dhi = 1.0 - sig[cc] * g2;
+      best = (dlo * dlo <= dhi * dhi) ? cc - 1 : cc;
+    } else {
+      best = cc - 1;
+    }
+  }
+  const int ind = best < 1 ? 1 : (best > NRT - 2 ? NRT - 2 : best);
+  const double xp_ind = sig[ind] * g2;
+  const double lo_v = sig[1] * g2, hi_v = sig[NRT - 2] * g2;
+  const double xc = fmin(fmax(1.0, lo_v), hi_v);
+  const int j2 = ind + ((xc - xp_ind >= 0.0) ? 1 : -1);
+  const FF slope = ff_of(c->logr[j2] - c->logr[ind]) / ff_of(sig[j2] * g2 - xp_ind);
+  const FF root = ff_of(c->logr[ind]) + slope * ff_of(1.0 - xp_ind);
+  const FF R = ff_exp(root, e2);
+  return R.hi < 1e-6f ? ff_of(1e-6) : R;  // power.py:115
+}
+
 // Three phases per block of 64 Limber nodes of one cosmology:
 //  1a thread per node: growth, chi, root find, k_nl; FAST: the exp index
 //     range and the Taylor part of the moments;
@@ -315,7 +350,10 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   __shared__ int ilo_s[NB], ihi_s[NB];
   __shared__ float iv2h_s[NB], iv2l_s[NB], f1_s[NB], f2_s[NB];
   __shared__ float wpf[FAST ? NKH : 1], k2h[FAST ? NKH + 1 : 1], k2l[FAST ? NKH + 1 : 1];
+  __shared__ float2 e2s[FAST ? 64 : 1];
   const CosmoTab* ct = it.ctab;
+  if (FAST)
+    for (int i = threadIdx.x; i < 64; i += blockDim.x) e2s[i] = c->exp2_ff[i];
   for (int i = threadIdx.x; i < NRT; i += blockDim.x) sig[i] = ct->sig[i];
   if (FAST) {
     for (int i = threadIdx.x; i < NKH + 1; i += blockDim.x) {
@@ -338,10 +376,22 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
     const int n = n0 + t;
     const double a = A[n];
-    const double g = clip_lohi(interp_eval(a, c->atab_grow, ct->g, unpack_seg(SG[n])), 0.0, 1.0);
-    const double g2 = g * g;
-    const double knl = root_knl_thread(sig, g2, c);
-    const double inv = 1.0 / knl;  // y = k * (1 / k_nl)
+    double g, knl, inv;
+    FF iv2;
+    if (FAST) {
+      // growth by the segment's node spacing reciprocal (no float64 division)
+      const int2 sg = unpack_seg(SG[n]);
+      const double sl = (ct->g[sg.y] - ct->g[sg.x]) * c->grow_ida[min(sg.x, sg.y)] * (sg.y > sg.x ? 1.0 : -1.0);
+      g = clip_lohi(ct->g[sg.x] + sl * (a - c->atab_grow[sg.x]), 0.0, 1.0);
+      const FF R = root_R_ff(sig, g * g, c, e2s);
+      inv = ffd(R);
+      knl = ffd(ff_rcp(R));
+      iv2 = ff_sqr(R);
+    } else {
+      g = clip_lohi(interp_eval(a, c->atab_grow, ct->g, unpack_seg(SG[n])), 0.0, 1.0);
+      knl = root_knl_thread(sig, g * g, c);
+      inv = 1.0 / knl;  // y = k * (1 / k_nl)
+    }
     g_s[t] = g;
     knl_s[t] = knl;
     inv_s[t] = inv;
@@ -360,7 +410,6 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
       ihi = (int)ceilf((HLY2S - linv - (float)LOG_KMIN) * (float)(1.0 / DLOGK));
       ilo = max(0, min(ilo, NKH));
       ihi = max(ilo - 1, min(ihi, NKH - 1));
-      const FF iv2 = ff_of(inv * inv);
       iv2h_s[t] = iv2.hi;
       iv2l_s[t] = iv2.lo;
       // sum_{i < ilo} w pk3 y^2 e^{-y^2} = sum_m (-1)^m / m! x^(m+1) Q_m[ilo]
@@ -449,9 +498,9 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
     const double a = A[n];
     double s1 = FAST ? (double)f1_s[t] : s1_s[t], s2 = FAST ? (double)f2_s[t] : s2_s[t];
     if (FAST) {
-      const double g2 = g_s[t] * g_s[t];
-      s1 = (s1 + 2.0 * t1_s[t]) * g2 / TWO_PI2;
-      s2 = (s2 + 4.0 * t2_s[t]) * g2 / TWO_PI2;
+      const double g2 = g_s[t] * g_s[t] * (1.0 / TWO_PI2);
+      s1 = (s1 + 2.0 * t1_s[t]) * g2;
+      s2 = (s2 + 4.0 * t2_s[t]) * g2;
     }
     HfParams hp;
     hp.knl = knl_s[t];
@@ -489,7 +538,15 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
     }
     if (it.rows64) {
       double* dst = it.rows64 + (size_t)n * NROW64;
-      for (int i = 0; i < NROW64; ++i) dst[i] = row[i];
+      if (FAST) {
+        // fp32c: the Limber weight and the halofit parameters (the rest of
+        // the integrand's inputs are in the FP32 row)
+        constexpr int keep[] = {R_CHI, R_G, R_KNL, R_NEFF, R_C, R_DCHI, R_U};
+#pragma unroll
+        for (int q = 0; q < 7; ++q) dst[keep[q]] = row[keep[q]];
+      } else {
+        for (int i = 0; i < NROW64; ++i) dst[i] = row[i];
+      }
     }
     if (it.rows32) {
       if (!FAST) row32_from_row64(s, row, f);

@@ -92,6 +92,7 @@ struct ConstTables {
   float2 grow_a_ff[NGROW], grow_lna_ff[NGROW], grow_ia_ff[NGROW], grow_am_ff[NGROW], grow_lnam_ff[NGROW],
       grow_iam_ff[NGROW];
   double chi_ida[NCHI];        // 1 / (atab_chi[i + 1] - atab_chi[i]) (i < NCHI - 1)
+  double grow_ida[NGROW];      // 1 / (atab_grow[i + 1] - atab_grow[i]) (i < NGROW - 1)
 };
 
 // ------------------------------------------------- per-cosmology tables -----

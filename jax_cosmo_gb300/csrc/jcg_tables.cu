@@ -198,6 +198,7 @@ __global__ void const_ff_kernel(ConstTables* c) {
     c->grow_am_ff[i] = f2_of(c->grow_am[i]);
     c->grow_lnam_ff[i] = f2_of(c->grow_lnam[i]);
     c->grow_iam_ff[i] = f2_of(c->grow_iam[i]);
+    c->grow_ida[i] = i < NGROW - 1 ? 1.0 / (c->atab_grow[i + 1] - c->atab_grow[i]) : 0.0;
   }
 }
 
