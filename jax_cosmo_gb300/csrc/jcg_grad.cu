@@ -747,6 +747,15 @@ __device__ __forceinline__ F8 interp_f8(double x, const double* xp, const double
 // tangents FP32), the same operations as grad_rows_kernel's FP32C path: root
 // find, moments (exp terms for y^2 in [1, 60], Taylor prefix tables below),
 // takahashi2012 coefficients, Limber weight; the row is written as computed.
+// interpolation on the segment sg of a table with tangents, by the segment's
+// node-spacing reciprocal ida (no float64 division)
+__device__ __forceinline__ FF8 interp_ff8(double x, const double* xp, const double* ida, const double* fv,
+                                         const double* fd, int stride, int2 sg) {
+  const FF8 f0 = ff8_of(fv[sg.x], fd + sg.x, stride), f1 = ff8_of(fv[sg.y], fd + sg.y, stride);
+  const double inv = ida[min(sg.x, sg.y)] * (sg.y > sg.x ? 1.0 : -1.0);
+  return f0 + (f1 - f0) * (inv * (x - xp[sg.x]));
+}
+
 constexpr int GR32_THREADS = 64;
 
 __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
@@ -765,29 +774,30 @@ __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb,
   const double a = A[n];
   float* row = gi.rowg + (size_t)n * NROWG;
   float* tg = row + NROWV;
-  auto put_t = [&](int slot, const F8& x, float sc) {
+  auto put_t = [&](int slot, const FF8& x, float sc) {
 #pragma unroll
     for (int d = 0; d < NDIR; ++d) tg[slot * NDIR + d] = x.d[d] * sc;
   };
-  F8 g = interp_f8(a, c->atab_grow, tb->gv, &tb->gd[0][0], NGROW, unpack_seg(SG[n]));
+  FF8 g = interp_ff8(a, c->atab_grow, c->grow_ida, tb->gv, &tb->gd[0][0], NGROW, unpack_seg(SG[n]));
   g = xfmin(xfmax(g, 0.0), 1.0);
-  F8 chi = interp_f8(a, c->atab_chi, tb->chiv, &tb->chid[0][0], NCHI, unpack_seg(SC[n]));
+  FF8 chi = interp_ff8(a, c->atab_chi, c->chi_ida, tb->chiv, &tb->chid[0][0], NCHI, unpack_seg(SC[n]));
   chi = xfmax(chi, 0.0);
-  const F8 g2 = g * g;
+  const FF8 g2 = g * g;
+  const double g2v = val(g2);
   int best;
   {
     int lo = 0, hi = NRT;
     while (lo < hi) {
       const int mid = (lo + hi) >> 1;
-      if (tb->sigv[mid] * g2.v > 1.0) lo = mid + 1;
+      if (tb->sigv[mid] * g2v > 1.0) lo = mid + 1;
       else hi = mid;
     }
     const int cc = lo;
     best = cc < NRT ? cc : NRT - 1;
     if (cc >= 1) {
-      const double dlo = 1.0 - tb->sigv[cc - 1] * g2.v;
+      const double dlo = 1.0 - tb->sigv[cc - 1] * g2v;
       if (cc < NRT) {
-        const double dhi = 1.0 - tb->sigv[cc] * g2.v;
+        const double dhi = 1.0 - tb->sigv[cc] * g2v;
         best = (dlo * dlo <= dhi * dhi) ? cc - 1 : cc;
       } else {
         best = cc - 1;
@@ -795,33 +805,32 @@ __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb,
     }
   }
   const int ind = best < 1 ? 1 : (best > NRT - 2 ? NRT - 2 : best);
-  const double xpi = tb->sigv[ind] * g2.v;
-  const double xc = fmin(fmax(1.0, tb->sigv[1] * g2.v), tb->sigv[NRT - 2] * g2.v);
+  const double xpi = tb->sigv[ind] * g2v;
+  const double xc = fmin(fmax(1.0, tb->sigv[1] * g2v), tb->sigv[NRT - 2] * g2v);
   const int j2 = ind + ((xc - xpi >= 0.0) ? 1 : -1);
-  const F8 xp0 = f8_of(tb->sigv[ind], &tb->sigd[0][ind], NRT) * g2;
-  const F8 xp1 = f8_of(tb->sigv[j2], &tb->sigd[0][j2], NRT) * g2;
-  const F8 slope = (c->logr[j2] - c->logr[ind]) / (xp1 - xp0);
-  const F8 bb = c->logr[ind] - slope * xp0;
-  const F8 root = slope * 1.0 + bb;
-  const F8 R = xfmax(xexp(root), 1e-6);
-  const F8 knl = 1.0 / R;
-  const F8 inv = 1.0 / knl;
-  row[F_LG2KNL] = (float)log2(knl.v);
-  row[F_INVKNL] = (float)(1.0 / knl.v);
+  const FF8 xp0 = ff8_of(tb->sigv[ind], &tb->sigd[0][ind], NRT) * g2;
+  const FF8 xp1 = ff8_of(tb->sigv[j2], &tb->sigd[0][j2], NRT) * g2;
+  const FF8 slope = (c->logr[j2] - c->logr[ind]) / (xp1 - xp0);
+  const FF8 bb = c->logr[ind] - slope * xp0;
+  const FF8 root = slope * 1.0 + bb;
+  const FF8 R = xfmax(xexp(root), 1e-6);
+  const FF8 knl = 1.0 / R;
+  const FF8 inv = 1.0 / knl;
+  row[F_LG2KNL] = (ff_log(knl.v) * ffc(1.4426950408889634)).hi;
+  row[F_INVKNL] = inv.v.hi;
   put_t(T_KNL, knl, 1.f);
   // moments: the exp terms for y^2 in [Y2_TAYLOR, Y2_SKIP] in FP32 from a
   // float-pair y^2 (values summed in float pairs), below Y2_TAYLOR the Taylor
   // series from the float-pair tables (Horner with derivatives); the
   // derivatives with respect to R and the tangents in FP32
-  const double Rv = inv.v;
-  const float iR = (float)(1.0 / Rv);
-  const float linv = LN2_F * lg2f((float)Rv);
+  const float iR = knl.v.hi;
+  const float linv = LN2_F * lg2f(inv.v.hi);
   constexpr float HLY2T = 0.0f, HLY2S = 2.0471425f;  // 0.5 log(Y2_TAYLOR), 0.5 log(Y2_SKIP)
   int ilo = (int)floorf((HLY2T - linv - (float)LOG_KMIN) * (float)(1.0 / DLOGK));
   int ihi = (int)ceilf((HLY2S - linv - (float)LOG_KMIN) * (float)(1.0 / DLOGK));
   ilo = max(0, min(ilo, NKH));
   ihi = max(ilo - 1, min(ihi, NKH - 1));
-  const FF R2 = ff_of(Rv * Rv);
+  const FF R2 = ff_sqr(inv.v);
   constexpr float Q3S = (float)(1.0 / TWO_PI2_G);
   FF s1p, s2p;
   s1p.hi = s1p.lo = s2p.hi = s2p.lo = 0.f;
@@ -912,133 +921,133 @@ __global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb,
     s1r += 2.f * t1r;
     s2r += 4.f * t2r;
   }
-  F8 S1, S2;
-  S1.v = s1;
-  S2.v = s2;
+  FF8 S1, S2;
+  S1.v = ff_of(s1);
+  S2.v = ff_of(s2);
   const float f1r = s1r, f2r = s2r;
 #pragma unroll
   for (int d = 0; d < NDIR; ++d) {
     S1.d[d] = s1d[d] + 2.f * t1d[d] + f1r * inv.d[d];
     S2.d[d] = s2d[d] + 4.f * t2d[d] + f2r * inv.d[d];
   }
-  const F8 I1 = S1 * g2, I2 = S2 * g2;
-  const F8 neff = I1 - 3.0;
-  const F8 C = I1 * I1 + I2;
+  const FF8 I1 = S1 * g2, I2 = S2 * g2;
+  const FF8 neff = I1 - 3.0;
+  const FF8 C = I1 * I1 + I2;
   // coefficients (power.py:177-238)
-  BgT<F8> bg;
-  bg.Om = f8_of(tb->sv[S_OMEGA_M], &tb->sd[0][S_OMEGA_M], NSCAL);
-  bg.Ok = f8_of(tb->sv[S_OMEGA_K], &tb->sd[0][S_OMEGA_K], NSCAL);
-  bg.Ode = f8_of(tb->sv[S_OMEGA_DE], &tb->sd[0][S_OMEGA_DE], NSCAL);
-  bg.w0 = f8_of(tb->sv[S_W0], &tb->sd[0][S_W0], NSCAL);
-  bg.wa = f8_of(tb->sv[S_WA], &tb->sd[0][S_WA], NSCAL);
+  BgT<FF8> bg;
+  bg.Om = ff8_of(tb->sv[S_OMEGA_M], &tb->sd[0][S_OMEGA_M], NSCAL);
+  bg.Ok = ff8_of(tb->sv[S_OMEGA_K], &tb->sd[0][S_OMEGA_K], NSCAL);
+  bg.Ode = ff8_of(tb->sv[S_OMEGA_DE], &tb->sd[0][S_OMEGA_DE], NSCAL);
+  bg.w0 = ff8_of(tb->sv[S_W0], &tb->sd[0][S_W0], NSCAL);
+  bg.wa = ff8_of(tb->sv[S_WA], &tb->sd[0][S_WA], NSCAL);
   const double lna = log(a);
-  F8 om_m, om_de;
+  FF8 om_m, om_de;
   omT(bg, a, lna, om_m, om_de);
   // halofit coefficients (power.py:177-244), each stored as soon as it is
   // formed (short live ranges of the 8-tangent values)
-  const F8 n2 = neff * neff, n3 = n2 * neff, n4 = n2 * n2;
+  const FF8 n2 = neff * neff, n3 = n2 * neff, n4 = n2 * n2;
   constexpr double LOG2E = 1.4426950408889634;
   if (pk_model(gi.geo->physics) == JCG_PK_SMITH2003) {
     // power.py:182-198, 239-242
     {
-      const F8 beta = 0.8291 + 0.9854 * neff + 0.3401 * n2;
-      row[F_BETAN] = (float)beta.v;
+      const FF8 beta = 0.8291 + 0.9854 * neff + 0.3401 * n2;
+      row[F_BETAN] = beta.v.hi;
       put_t(T_BETAN, beta, 1.f);
-      const F8 alpha = 1.3884 + 0.3700 * neff - 0.1452 * n2;
-      row[F_ALPHAN] = (float)alpha.v;
+      const FF8 alpha = 1.3884 + 0.3700 * neff - 0.1452 * n2;
+      row[F_ALPHAN] = alpha.v.hi;
       put_t(T_ALPHAN, alpha, 1.f);
     }
     {
-      const F8 an = xexp(LN10_G * (1.4861 + 1.8369 * neff + 1.6762 * n2 + 0.7940 * n3 + 0.1670 * n4 - 0.6206 * C));
-      row[F_AN] = (float)an.v;
+      const FF8 an = xexp(LN10_G * (1.4861 + 1.8369 * neff + 1.6762 * n2 + 0.7940 * n3 + 0.1670 * n4 - 0.6206 * C));
+      row[F_AN] = an.v.hi;
       put_t(T_AN, an, 1.f);
-      const F8 bn = xexp(LN10_G * (0.9463 + 0.9466 * neff + 0.3084 * n2 - 0.9400 * C));
-      row[F_BN] = (float)bn.v;
+      const FF8 bn = xexp(LN10_G * (0.9463 + 0.9466 * neff + 0.3084 * n2 - 0.9400 * C));
+      row[F_BN] = bn.v.hi;
       put_t(T_BN, bn, 1.f);
     }
     {
-      const F8 lom = xlog(om_m);
-      const F8 frac = om_de / (1.0 - om_m);
-      const F8 ofr = 1.0 - frac;
-      const F8 f1 = frac * xexp(-0.0307 * lom) + ofr * xexp(-0.0732 * lom);
-      row[F_3F1] = (float)(3.0 * f1.v);
+      const FF8 lom = xlog(om_m);
+      const FF8 frac = om_de / (1.0 - om_m);
+      const FF8 ofr = 1.0 - frac;
+      const FF8 f1 = frac * xexp(-0.0307 * lom) + ofr * xexp(-0.0732 * lom);
+      row[F_3F1] = 3.f * f1.v.hi;
       put_t(T_3F1, f1, 3.f);
-      const F8 f2 = frac * xexp(-0.0585 * lom) + ofr * xexp(-0.1423 * lom);
-      row[F_F2] = (float)f2.v;
+      const FF8 f2 = frac * xexp(-0.0585 * lom) + ofr * xexp(-0.1423 * lom);
+      row[F_F2] = f2.v.hi;
       put_t(T_F2, f2, 1.f);
-      const F8 f3 = frac * xexp(0.0743 * lom) + ofr * xexp(0.0725 * lom);
-      const F8 lcf3 = LN10_G * (-0.2807 + 0.6669 * neff + 0.3214 * n2 - 0.0793 * C) + xlog(f3);
-      row[F_LG2CF3] = (float)(LOG2E * lcf3.v);
+      const FF8 f3 = frac * xexp(0.0743 * lom) + ofr * xexp(0.0725 * lom);
+      const FF8 lcf3 = LN10_G * (-0.2807 + 0.6669 * neff + 0.3214 * n2 - 0.0793 * C) + xlog(f3);
+      row[F_LG2CF3] = (lcf3.v * ffc(LOG2E)).hi;
       put_t(T_LG2CF3, lcf3, (float)LOG2E);
     }
     {
-      const F8 gam = 0.8649 + 0.2989 * neff + 0.1631 * C;
-      row[F_3MGAMMA] = (float)(3.0 - gam.v);
+      const FF8 gam = 0.8649 + 0.2989 * neff + 0.1631 * C;
+      row[F_3MGAMMA] = (3.f - gam.v).hi;
       put_t(T_3MG, gam, -1.f);
-      const F8 nu = xexp(LN10_G * (0.9585 + 1.2857 * neff));
-      row[F_NUN] = (float)nu.v;
+      const FF8 nu = xexp(LN10_G * (0.9585 + 1.2857 * neff));
+      row[F_NUN] = nu.v.hi;
       put_t(T_NUN, nu, 1.f);
-      const F8 mu = xexp(LN10_G * (-3.5442 + 0.1908 * neff));
-      row[F_MUN] = (float)mu.v;
+      const FF8 mu = xexp(LN10_G * (-3.5442 + 0.1908 * neff));
+      row[F_MUN] = mu.v.hi;
       put_t(T_MUN, mu, 1.f);
     }
   } else {
-    const F8 opw = om_de * (1.0 + wT(bg, a));
+    const FF8 opw = om_de * (1.0 + wT(bg, a));
     {
-      const F8 beta = 2.0379 - 0.7354 * neff + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
-      row[F_BETAN] = (float)beta.v;
+      const FF8 beta = 2.0379 - 0.7354 * neff + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
+      row[F_BETAN] = beta.v.hi;
       put_t(T_BETAN, beta, 1.f);
-      const F8 alpha = xfabs(6.0835 + 1.3373 * neff - 0.1959 * n2 - 5.5274 * C);
-      row[F_ALPHAN] = (float)alpha.v;
+      const FF8 alpha = xfabs(6.0835 + 1.3373 * neff - 0.1959 * n2 - 5.5274 * C);
+      row[F_ALPHAN] = alpha.v.hi;
       put_t(T_ALPHAN, alpha, 1.f);
     }
     {
-      const F8 e_an = 1.5222 + 2.8553 * neff + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 - 0.6038 * C + 0.1749 * opw;
-      const F8 an = xexp(LN10_G * e_an);
-      row[F_AN] = (float)an.v;
+      const FF8 e_an = 1.5222 + 2.8553 * neff + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 - 0.6038 * C + 0.1749 * opw;
+      const FF8 an = xexp(LN10_G * e_an);
+      row[F_AN] = an.v.hi;
       put_t(T_AN, an, 1.f);
-      const F8 e_bn = -0.5642 + 0.5864 * neff + 0.5716 * n2 - 1.5474 * C + 0.2279 * opw;
-      const F8 bn = xexp(LN10_G * e_bn);
-      row[F_BN] = (float)bn.v;
+      const FF8 e_bn = -0.5642 + 0.5864 * neff + 0.5716 * n2 - 1.5474 * C + 0.2279 * opw;
+      const FF8 bn = xexp(LN10_G * e_bn);
+      row[F_BN] = bn.v.hi;
       put_t(T_BN, bn, 1.f);
     }
     {
-      const F8 lom = xlog(om_m);
-      const F8 e_cn = 0.3698 + 2.0404 * neff + 0.8161 * n2 + 0.5869 * C;
-      const F8 lcf3 = LN10_G * e_cn + 0.0743 * lom;
-      row[F_LG2CF3] = (float)(LOG2E * lcf3.v);
+      const FF8 lom = xlog(om_m);
+      const FF8 e_cn = 0.3698 + 2.0404 * neff + 0.8161 * n2 + 0.5869 * C;
+      const FF8 lcf3 = LN10_G * e_cn + 0.0743 * lom;
+      row[F_LG2CF3] = (lcf3.v * ffc(LOG2E)).hi;
       put_t(T_LG2CF3, lcf3, (float)LOG2E);
-      const F8 f1 = xexp(-0.0307 * lom);
-      row[F_3F1] = (float)(3.0 * f1.v);
+      const FF8 f1 = xexp(-0.0307 * lom);
+      row[F_3F1] = 3.f * f1.v.hi;
       put_t(T_3F1, f1, 3.f);
-      const F8 f2 = xexp(-0.0585 * lom);
-      row[F_F2] = (float)f2.v;
+      const FF8 f2 = xexp(-0.0585 * lom);
+      row[F_F2] = f2.v.hi;
       put_t(T_F2, f2, 1.f);
     }
     {
-      const F8 gam = 0.1971 - 0.0843 * neff + 0.8460 * C;
-      row[F_3MGAMMA] = (float)(3.0 - gam.v);
+      const FF8 gam = 0.1971 - 0.0843 * neff + 0.8460 * C;
+      row[F_3MGAMMA] = (3.f - gam.v).hi;
       put_t(T_3MG, gam, -1.f);
-      const F8 nu = xexp(LN10_G * (5.2105 + 3.6902 * neff));
-      row[F_NUN] = (float)nu.v;
+      const FF8 nu = xexp(LN10_G * (5.2105 + 3.6902 * neff));
+      row[F_NUN] = nu.v.hi;
       put_t(T_NUN, nu, 1.f);
       row[F_MUN] = 0.f;
       put_t(T_MUN, 0.0 * nu, 0.f);
     }
   }
   {
-    const F8 chic = xfmax(chi, 1.0);
-    row[F_INVCHI] = (float)(1.0 / chic.v);
-    row[F_LG2INVCHI] = (float)(-log2(chic.v));
-    row[F_CHIC] = (float)chic.v;
+    const FF8 chic = xfmax(chi, 1.0);
+    row[F_INVCHI] = ff_rcp(chic.v).hi;
+    row[F_LG2INVCHI] = -(ff_log(chic.v) * ffc(LOG2E)).hi;
+    row[F_CHIC] = chic.v.hi;
     put_t(T_CHIC, chic, 1.f);
-    const F8 pkn = f8_of(tb->sv[S_PKNORM], &tb->sd[0][S_PKNORM], NSCAL);
-    const F8 d2fac = g * g * pkn / TWO_PI2_G;
-    row[F_D2FAC] = (float)d2fac.v;
+    const FF8 pkn = ff8_of(tb->sv[S_PKNORM], &tb->sd[0][S_PKNORM], NSCAL);
+    const FF8 d2fac = g * g * pkn / TWO_PI2_G;
+    row[F_D2FAC] = d2fac.v.hi;
     put_t(T_D2FAC, d2fac, 1.f);
-    const F8 dchi = dchioverdaT(bg, a, lna);
-    const F8 u = WS[n] * dchi / xfmax(chi * chi, 1.0) / C2_G;
-    row[F_U] = (float)u.v;
+    const FF8 dchi = dchioverdaT(bg, a, lna);
+    const FF8 u = WS[n] * dchi / xfmax(chi * chi, 1.0) / C2_G;
+    row[F_U] = u.v.hi;
     put_t(T_U, u, 1.f);
   }
 }
