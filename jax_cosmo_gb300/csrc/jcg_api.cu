@@ -245,6 +245,8 @@ static int make_header(const jcg_geometry* g, GeoHeader* h) {
   h->off_ell = take(h->n_ell);
   h->off_ellfac = take((int64_t)h->n_tr * h->n_ell);
   h->off_lg2ellh = take(h->n_ell);
+  h->off_kh4 = take(2 * (int64_t)h->n_ell);
+  h->off_ef32 = take(((int64_t)h->n_tr * h->n_ell + 1) / 2);
   const int64_t half = ((int64_t)na * NZP + 1) / 2;  // 4-byte arrays in 8-byte units
   for (int q = 0; q < h->n_groups; ++q) {
     h->off_ap[q] = take((int64_t)na * NZP);

@@ -397,6 +397,52 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       putf(pq, NKH, e, p3 / (2.0 * (PI * PI)));
     }
   }
+  if (F32T && t < NDIR + 1) {
+    // the Limber kernels' FP32 Eisenstein-Hu inputs and their tangents,
+    // once per cosmology: t 0 the values, t 1..8 direction t - 1
+    const int d = t - 1;
+    const double keq = sv[S_K_EQ], sh = sv[S_SH_D], bc = sv[S_BETA_C], ac = sv[S_ALPHA_C];
+    const double ks = sv[S_K_SILK];
+    if (t == 0) {
+      const double qinv = 1.0 / (13.41 * keq);
+      float* ev = out->ehv;
+      ev[0] = (float)qinv;
+      ev[1] = (float)log2(qinv);
+      ev[2] = (float)sh;
+      ev[3] = (float)(1.0 / sh);
+      ev[4] = (float)(1.8 * bc);
+      ev[5] = (float)(14.2 / ac);
+      ev[6] = (float)sv[S_ALPHA_B];
+      ev[7] = (float)sv[S_BETA_B];
+      ev[8] = (float)sv[S_BETA_NODE];
+      ev[9] = (float)log2(ks);
+      ev[10] = (float)sv[S_FB];
+      ev[11] = (float)sv[S_FC];
+      ev[12] = (float)(sv[S_NS] + 3.0);
+      ev[13] = (float)(1.0 / keq);
+      ev[14] = (float)sv[S_AGAM];
+      ev[15] = (float)sv[S_NWQ];
+    } else {
+      const double* sdd = sd + d * NSCAL;
+      float* et = out->eht;
+      for (int j = 0; j < NET; ++j) et[j * NDIR + d] = 0.f;
+      et[E_KEQ * NDIR + d] = (float)sdd[S_K_EQ];
+      et[E_SH * NDIR + d] = (float)sdd[S_SH_D];
+      et[E_C18BC * NDIR + d] = (float)(1.8 * sdd[S_BETA_C]);
+      et[E_C142AC * NDIR + d] = (float)(-14.2 * sdd[S_ALPHA_C] / (ac * ac));
+      et[E_ALPHAB * NDIR + d] = (float)sdd[S_ALPHA_B];
+      et[E_BETAB * NDIR + d] = (float)sdd[S_BETA_B];
+      et[E_BETANODE * NDIR + d] = (float)sdd[S_BETA_NODE];
+      et[E_LG2KSILK * NDIR + d] = (float)(sdd[S_K_SILK] / (ks * 0.6931471805599453));
+      et[E_FB * NDIR + d] = (float)sdd[S_FB];
+      et[E_FC * NDIR + d] = (float)sdd[S_FC];
+      et[E_NS3 * NDIR + d] = (float)sdd[S_NS];
+      if (sv[S_TFNW] != 0.0) {  // type "eisenhu": its two inputs in the slots of k_eq and 1.8 beta_c
+        et[E_AGAM * NDIR + d] = (float)sdd[S_AGAM];
+        et[E_NWQ * NDIR + d] = (float)sdd[S_NWQ];
+      }
+    }
+  }
   __syncthreads();
   if (F32T && gi.ptt) {
     // Taylor tables of the fp32c moments, scaled to the table row so that no

@@ -60,6 +60,11 @@ struct TabD {
   float s32[NDIR + 1][NCHI];   // segment slopes (chi[i+1] - chi[i]) / (a[i+1] - a[i]) and tangents
   float pk3df[NKH][NDIR];      // P(k) k^3 tangents, node-major
   float padf[8];
+  // the Eisenstein-Hu inputs of the FP32 integrand (EHg order) and their
+  // tangents [NET][NDIR], formed once per cosmology for the Limber kernels
+  float ehv[16];
+  float eht[88];   // NET x NDIR
+  float padg[8];
   float wq3f[NKH + 15];        // simpson_kh[i] * P(k_i) k_i^3 / (2 pi^2), float; padded to 64 bytes
 };
 static_assert(sizeof(TabD) % 64 == 0, "TabD alignment");
@@ -96,6 +101,7 @@ constexpr int NROWG = NROWV + NGT * NDIR;  // 132 floats
 // per-cosmology Eisenstein-Hu inputs of the FP32 integrand with tangents
 enum ETan { E_KEQ = 0, E_SH, E_C18BC, E_C142AC, E_ALPHAB, E_BETAB, E_BETANODE, E_LG2KSILK, E_FB, E_FC,
             E_NS3, NET };
+static_assert(NET * NDIR <= 88, "TabD::eht holds the Eisenstein-Hu tangents");
 // transfer type "eisenhu": alpha_gamma and (T_cmb / 2.7)^2 / (Omega_m h) in
 // the slots of k_eq and 1.8 beta_c (which that fit does not use)
 constexpr int E_AGAM = E_KEQ, E_NWQ = E_C18BC;

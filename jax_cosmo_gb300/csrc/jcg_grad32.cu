@@ -290,48 +290,10 @@ __global__ void __launch_bounds__(L32_THREADS, 2)
   float* Pd = Pv + (size_t)TA * LT;                   // [TA][NDIR][LT]
   const int tid = threadIdx.x;
   const TabD* tb = gi.tab;
-  if (tid < NDIR + 1) {
-    // tid 0: values; tid 1..8: tangents of direction tid - 1
-    const int d = tid - 1;
-    const double keq = tb->sv[S_K_EQ], sh = tb->sv[S_SH_D], bc = tb->sv[S_BETA_C], ac = tb->sv[S_ALPHA_C];
-    const double ks = tb->sv[S_K_SILK];
-    if (tid == 0) {
-      const double qinv = 1.0 / (13.41 * keq);
-      ev[0] = (float)qinv;
-      ev[1] = (float)log2(qinv);
-      ev[2] = (float)sh;
-      ev[3] = (float)(1.0 / sh);
-      ev[4] = (float)(1.8 * bc);
-      ev[5] = (float)(14.2 / ac);
-      ev[6] = (float)tb->sv[S_ALPHA_B];
-      ev[7] = (float)tb->sv[S_BETA_B];
-      ev[8] = (float)tb->sv[S_BETA_NODE];
-      ev[9] = (float)log2(ks);
-      ev[10] = (float)tb->sv[S_FB];
-      ev[11] = (float)tb->sv[S_FC];
-      ev[12] = (float)(tb->sv[S_NS] + 3.0);
-      ev[13] = (float)(1.0 / keq);
-      ev[14] = (float)tb->sv[S_AGAM];
-      ev[15] = (float)tb->sv[S_NWQ];
-    } else {
-      const double* sd = tb->sd[d];
-      et[E_KEQ * NDIR + d] = (float)sd[S_K_EQ];
-      et[E_SH * NDIR + d] = (float)sd[S_SH_D];
-      et[E_C18BC * NDIR + d] = (float)(1.8 * sd[S_BETA_C]);
-      et[E_C142AC * NDIR + d] = (float)(-14.2 * sd[S_ALPHA_C] / (ac * ac));
-      et[E_ALPHAB * NDIR + d] = (float)sd[S_ALPHA_B];
-      et[E_BETAB * NDIR + d] = (float)sd[S_BETA_B];
-      et[E_BETANODE * NDIR + d] = (float)sd[S_BETA_NODE];
-      et[E_LG2KSILK * NDIR + d] = (float)(sd[S_K_SILK] / (ks * 0.6931471805599453));
-      et[E_FB * NDIR + d] = (float)sd[S_FB];
-      et[E_FC * NDIR + d] = (float)sd[S_FC];
-      et[E_NS3 * NDIR + d] = (float)sd[S_NS];
-      if (nw) {
-        et[E_AGAM * NDIR + d] = (float)sd[S_AGAM];
-        et[E_NWQ * NDIR + d] = (float)sd[S_NWQ];
-      }
-    }
-  }
+  // the Eisenstein-Hu inputs and their tangents (formed once per cosmology
+  // by the table stage)
+  for (int i = tid; i < 16; i += L32_THREADS) ev[i] = tb->ehv[i];
+  for (int i = tid; i < NET * NDIR; i += L32_THREADS) et[i] = tb->eht[i];
   const double* ELL = geo_ptr<double>(geo, geo->off_ell);
   const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
   for (int l = tid; l < lt; l += L32_THREADS) {

@@ -222,6 +222,8 @@ struct GeoHeader {
   int64_t off_nzl;                                   // [n_tr][na] n_t(z_n)
   int64_t off_ell, off_ellfac;                       // [n_ell], [n_tr][n_ell]
   int64_t off_lg2ellh;                               // [n_ell] log2(ell + 1/2) (fp32 path)
+  int64_t off_kh4;                                   // [n_ell] float4 (l + 1/2, log2(l + 1/2), 1 / (l + 1/2), 0)
+  int64_t off_ef32;                                  // [n_tr][n_ell] float ell factors
   int64_t off_ap[MAXTR];                             // per group [na][NZP] a' nodes
   int64_t off_segp[MAXTR];                           // per group [na][NZP] packed segments
   int64_t off_q32[MAXTR];      // per group [na][NZP] int32: nearest node | segment << 16

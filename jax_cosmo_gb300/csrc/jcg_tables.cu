@@ -326,7 +326,12 @@ __global__ void geo_tables_kernel(const GeoHeader* __restrict__ hp, double* geo,
       f = sqrt((e - 1) * (e) * (e + 1) * (e + 2)) / ((e + 0.5) * (e + 0.5));
     }
     EF[q] = f;
-    if (t == 0) LG[l] = log2(e + 0.5);
+    reinterpret_cast<float*>(geo + h.off_ef32)[q] = (float)f;
+    if (t == 0) {
+      LG[l] = log2(e + 0.5);
+      reinterpret_cast<float4*>(geo + h.off_kh4)[l] =
+          make_float4((float)(e + 0.5), (float)log2(e + 0.5), (float)(1.0 / (e + 0.5)), 0.f);
+    }
   }
   // lensing grids: z' = linspace(z, zmax_probe, 257) per Limber node (probes.py:51)
   for (int g = 0; g < h.n_groups; ++g) {

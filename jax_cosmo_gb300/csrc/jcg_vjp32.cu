@@ -24,6 +24,7 @@
 // the chunk's partial C_ell, from which the serving loop forms the
 // likelihood's cotangent before the product.
 #include "jcg_node32.cuh"
+#include "jcg_ff.cuh"
 
 namespace jcg {
 
@@ -66,7 +67,7 @@ __host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT) {
   L.abar = o;                                 // [VJ_TA][NGT]
   o += 4 * (size_t)VJ_TA * NGT;
   o = (o + 15) & ~(size_t)15;
-  L.qd = o;                                   // [VJ_TA][n_cls] doubles
+  L.qd = o;                                   // [VJ_TA][n_cls] float pairs
   o += 8 * (size_t)VJ_TA * n_cls;
   L.red = o;                                  // [VJ_THREADS / 32][NET] floats, then [VJ_TA][NDIR] doubles
   o += 4 * (size_t)(VJ_THREADS / 32) * NET;
@@ -103,54 +104,16 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   float* vS = reinterpret_cast<float*>(vj_smem + L.vs);
   float* Pt = reinterpret_cast<float*>(vj_smem + L.pt);
   float* Abar = reinterpret_cast<float*>(vj_smem + L.abar);
-  double* Qd = reinterpret_cast<double*>(vj_smem + L.qd);
+  float2* Qd = reinterpret_cast<float2*>(vj_smem + L.qd);  // Q_p(t) as (hi, lo)
   float* Ered = reinterpret_cast<float*>(vj_smem + L.red);
   double* gred = reinterpret_cast<double*>(vj_smem + ((L.red + 4 * (VJ_THREADS / 32) * NET + 15) & ~(size_t)15));
   const int tid = threadIdx.x, grp = tid >> 3, sub = tid & (VJ_GROUP - 1);
   const TabD* tb = gi.tab;
-  if (tid < NDIR + 1) {
-    // tid 0: the Eisenstein-Hu values; tid 1..8: their tangents in direction tid - 1
-    const int d = tid - 1;
-    const double keq = tb->sv[S_K_EQ], sh = tb->sv[S_SH_D], bc = tb->sv[S_BETA_C], ac = tb->sv[S_ALPHA_C];
-    const double ks = tb->sv[S_K_SILK];
-    if (tid == 0) {
-      const double qinv = 1.0 / (13.41 * keq);
-      ev[0] = (float)qinv;
-      ev[1] = (float)log2(qinv);
-      ev[2] = (float)sh;
-      ev[3] = (float)(1.0 / sh);
-      ev[4] = (float)(1.8 * bc);
-      ev[5] = (float)(14.2 / ac);
-      ev[6] = (float)tb->sv[S_ALPHA_B];
-      ev[7] = (float)tb->sv[S_BETA_B];
-      ev[8] = (float)tb->sv[S_BETA_NODE];
-      ev[9] = (float)log2(ks);
-      ev[10] = (float)tb->sv[S_FB];
-      ev[11] = (float)tb->sv[S_FC];
-      ev[12] = (float)(tb->sv[S_NS] + 3.0);
-      ev[13] = (float)(1.0 / keq);
-      ev[14] = (float)tb->sv[S_AGAM];
-      ev[15] = (float)tb->sv[S_NWQ];
-    } else if (!FWD) {
-      const double* sd = tb->sd[d];
-      for (int j = 0; j < NET; ++j) et[j * NDIR + d] = 0.f;
-      et[E_KEQ * NDIR + d] = (float)sd[S_K_EQ];
-      et[E_SH * NDIR + d] = (float)sd[S_SH_D];
-      et[E_C18BC * NDIR + d] = (float)(1.8 * sd[S_BETA_C]);
-      et[E_C142AC * NDIR + d] = (float)(-14.2 * sd[S_ALPHA_C] / (ac * ac));
-      et[E_ALPHAB * NDIR + d] = (float)sd[S_ALPHA_B];
-      et[E_BETAB * NDIR + d] = (float)sd[S_BETA_B];
-      et[E_BETANODE * NDIR + d] = (float)sd[S_BETA_NODE];
-      et[E_LG2KSILK * NDIR + d] = (float)(sd[S_K_SILK] / (ks * 0.6931471805599453));
-      et[E_FB * NDIR + d] = (float)sd[S_FB];
-      et[E_FC * NDIR + d] = (float)sd[S_FC];
-      et[E_NS3 * NDIR + d] = (float)sd[S_NS];
-      if (nw) {
-        et[E_AGAM * NDIR + d] = (float)sd[S_AGAM];
-        et[E_NWQ * NDIR + d] = (float)sd[S_NWQ];
-      }
-    }
-  }
+  // the Eisenstein-Hu inputs and their tangents (formed once per cosmology
+  // by the table stage)
+  for (int i = tid; i < 16; i += VJ_THREADS) ev[i] = tb->ehv[i];
+  if (!FWD)
+    for (int i = tid; i < NET * NDIR; i += VJ_THREADS) et[i] = tb->eht[i];
   // the chunk's FP32 rows (values and tangents) and radial kernels
   {
     const float4* src = reinterpret_cast<const float4*>(gi.rowg + (size_t)a0 * NROWG);
@@ -164,7 +127,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
     }
   }
   if (!FWD)
-    for (int i = tid; i < tc * n_cls; i += VJ_THREADS) Qd[i] = 0.0;
+    for (int i = tid; i < tc * n_cls; i += VJ_THREADS) Qd[i] = make_float2(0.f, 0.f);
   __syncthreads();
   // M_p(a) = u K_i K_j, the operation order of grad_limber32
   for (int i = tid; i < tc * n_cls; i += VJ_THREADS) {
@@ -178,8 +141,8 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   eh.c142ac = ev[5]; eh.alpha_b = ev[6]; eh.beta_b = ev[7]; eh.beta_node = ev[8]; eh.lg2_ksilk = ev[9];
   eh.fb = ev[10]; eh.fc = ev[11]; eh.ns3 = ev[12]; eh.inv_keq = ev[13];
   eh.agam = ev[14]; eh.nwq = ev[15];
-  const double* ELL = geo_ptr<double>(geo, geo->off_ell);
-  const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
+  const float4* KH4 = geo_ptr<float4>(geo, geo->off_kh4);
+  const float* EF32 = geo_ptr<float>(geo, geo->off_ef32);
   float accA[T_U], accE[NET];
 #pragma unroll
   for (int j = 0; j < T_U; ++j) accA[j] = 0.f;
@@ -189,17 +152,17 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
     const int lt = min(LT, n_ell - l0);
     __syncthreads();  // the previous tile's Pt / vS are consumed
     for (int l = tid; l < lt; l += VJ_THREADS) {
-      const double e = ELL[l0 + l] + 0.5;
-      khv[l] = (float)e;
-      lkhv[l] = (float)log2(e);
-      ikhv[l] = (float)(1.0 / e);
+      const float4 k4 = KH4[l0 + l];
+      khv[l] = k4.x;
+      lkhv[l] = k4.y;
+      ikhv[l] = k4.z;
     }
     if (!FWD)
       for (int q = tid; q < n_cls * lt; q += VJ_THREADS) {
         const int p = q / lt, l = q - p * lt;
         const int ell = l0 + l;
-        const double ef = EF[(size_t)geo->pair_i[p] * n_ell + ell] * EF[(size_t)geo->pair_j[p] * n_ell + ell];
-        vS[p * LT + l] = (float)(gi.vbar[(size_t)p * n_ell + ell] * ef);
+        const float ef = EF32[(size_t)geo->pair_i[p] * n_ell + ell] * EF32[(size_t)geo->pair_j[p] * n_ell + ell];
+        vS[p * LT + l] = (float)gi.vbar[(size_t)p * n_ell + ell] * ef;
       }
     __syncthreads();
     if (grp < tc) {
@@ -236,19 +199,20 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
         cp[(size_t)p * n_ell + l0 + l] = s;
       }
     } else {
-      // Q_p(t) += sum_l v_p(l) P(t, l), float sums of at most 32 terms added in double
+      // Q_p(t) += sum_l v_p(l) P(t, l): float sums of at most 32 terms,
+      // added in float-pair arithmetic
       for (int q = tid; q < tc * n_cls; q += VJ_THREADS) {
         const int t = q / n_cls, p = q - t * n_cls;
         const float* vp = vS + (size_t)p * LT;
         const float* pp = Pt + (size_t)t * LT;
-        double s = 0.0;
+        FF s{Qd[q].x, Qd[q].y};
         for (int b = 0; b < lt; b += 32) {
           float f = 0.f;
           const int e = min(lt, b + 32);
           for (int l = b; l < e; ++l) f = fmaf(vp[l], pp[l], f);
-          s += (double)f;
+          s = s + f;
         }
-        Qd[q] += s;
+        Qd[q] = make_float2(s.hi, s.lo);
       }
     }
   }
@@ -286,27 +250,27 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
         s = fmaf(Abar[t * NGT + j], tg[j * NDIR + d], s);
       }
       gd = (double)s;
-      // sum_p Q_p (du K_i K_j + u (dK_i K_j + K_i dK_j))
+      // sum_p Q_p (du K_i K_j + u (dK_i K_j + K_i dK_j)), in float pairs
       const float u = row[F_U], du = tg[T_U * NDIR + d];
-      const double* q = Qd + (size_t)t * n_cls;
-      double sm = 0.0;
+      const float2* q = Qd + (size_t)t * n_cls;
+      FF sm{0.f, 0.f};
       for (int p = 0; p < n_cls; ++p) {
         const float* Ki = Ks + ((size_t)t * n_tr + geo->pair_i[p]) * (NDIR + 1);
         const float* Kj = Ks + ((size_t)t * n_tr + geo->pair_j[p]) * (NDIR + 1);
         const float dm = fmaf(du, Ki[0] * Kj[0], u * fmaf(Ki[1 + d], Kj[0], Ki[0] * Kj[1 + d]));
-        sm += q[p] * (double)dm;
+        sm = sm + FF{q[p].x, q[p].y} * dm;
       }
-      gd += sm;
+      gd += ffd(sm);
     }
     if (t == 0) {
       // the cosmology's Eisenstein-Hu inputs, once per CTA
-      double se = 0.0;
+      FF se{0.f, 0.f};
       for (int j = 0; j < NET; ++j) {
-        double ej = 0.0;
-        for (int w = 0; w < VJ_THREADS / 32; ++w) ej += (double)Ered[w * NET + j];
-        se += ej * (double)et[j * NDIR + d];
+        FF ej{0.f, 0.f};
+        for (int w = 0; w < VJ_THREADS / 32; ++w) ej = ej + Ered[w * NET + j];
+        se = se + ej * et[j * NDIR + d];
       }
-      gd += se;
+      gd += ffd(se);
     }
     gred[t * NDIR + d] = gd;
   }
