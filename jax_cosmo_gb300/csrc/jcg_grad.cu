@@ -1874,7 +1874,8 @@ __global__ void vjp_contract_kernel(const double* __restrict__ jac, const double
 static size_t vjp32_item_bytes(const GeoHeader& h) {
   const size_t per = (size_t)h.n_cls * h.n_ell;
   const size_t nch = (size_t)vjp_chunks(h.na);
-  return al256(sizeof(float) * nch * per) + al256(sizeof(double) * nch * NDIR);
+  return al256(sizeof(float) * nch * per) + al256(sizeof(double) * nch * NDIR) +
+         al256(sizeof(float) * (size_t)h.n_tr * h.na) + al256(sizeof(double) * (size_t)kv_chunks(h.na) * NDIR);
 }
 
 size_t vjp_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
@@ -1890,6 +1891,8 @@ size_t vjp_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
   o += kern_bytes(hb, precision);
   o += al256(sizeof(float) * (size_t)vjp_chunks(h.na) * per * n_cosmo);
   o += al256(sizeof(double) * (size_t)vjp_chunks(h.na) * NDIR * n_cosmo);
+  o += al256(sizeof(float) * (size_t)h.n_tr * h.na * n_cosmo);
+  o += al256(sizeof(double) * (size_t)kv_chunks(h.na) * NDIR * n_cosmo);
   o += gnode_bytes(n_cosmo, precision);
   return o;
 }
@@ -1929,7 +1932,12 @@ void vjp_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int
   o += al256(sizeof(float) * (size_t)vjp_chunks(h.na) * per * n_cosmo);
   gb.gpart = reinterpret_cast<double*>(base + o);
   o += al256(sizeof(double) * (size_t)vjp_chunks(h.na) * NDIR * n_cosmo);
+  gb.kbar = reinterpret_cast<float*>(base + o);
+  o += al256(sizeof(float) * (size_t)h.n_tr * h.na * n_cosmo);
+  gb.kpart = reinterpret_cast<double*>(base + o);
+  o += al256(sizeof(double) * (size_t)kv_chunks(h.na) * NDIR * n_cosmo);
   gb.gnode = gnode_bytes(n_cosmo, precision) ? reinterpret_cast<double*>(base + o) : nullptr;
+  gb.vjp_rev = (vbar && grad) ? 1 : 0;
   gb.vbar = vbar;
   gb.grad = grad;
   gb.cl = cl;
@@ -2074,6 +2082,10 @@ cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void*
       o += al256(sizeof(float) * nch * per);
       it.gpart = reinterpret_cast<double*>(base + o);
       o += al256(sizeof(double) * nch * NDIR);
+      it.kbar = reinterpret_cast<float*>(base + o);
+      o += al256(sizeof(float) * (size_t)h.n_tr * h.na);
+      it.kpart = reinterpret_cast<double*>(base + o);
+      o += al256(sizeof(double) * (size_t)kv_chunks(h.na) * NDIR);
       if (!r[i].cl) {
         r[i].cl = reinterpret_cast<double*>(base + o);
         o += al256(sizeof(double) * per);
@@ -2111,6 +2123,7 @@ cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void*
   gb.precision = precision;
   gb.items = dev_items;
   gb.n_split = vjp ? 1 : n_split;
+  gb.vjp_rev = vjp ? 1 : 0;
   gb.gnode = gnode_bytes(n, precision) ? reinterpret_cast<double*>(base + o) : nullptr;
   if (vjp) {
     launch_grad_front(gb, c, st);

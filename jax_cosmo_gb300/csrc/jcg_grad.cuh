@@ -127,7 +127,16 @@ struct GradItem {
   float* cpart;
   double* gpart;
   double* grad;
+  // reverse form of the lensing integral (vector-Jacobian product): the
+  // cotangents of the WeakLensing kernels [n_tr][na] and per node-chunk
+  // gradient partials [n_kchunk][NDIR]
+  float* kbar;
+  double* kpart;
 };
+
+// node chunks of the reverse lensing kernel
+constexpr int KV_NODES = 32;
+__host__ __device__ inline int kv_chunks(int na) { return (na + KV_NODES - 1) / KV_NODES; }
 
 // a-chunks of the vector-Jacobian product kernels: at most VJ_TA Limber
 // nodes per CTA, the chunks balanced
@@ -170,6 +179,12 @@ struct GradBatch {
   float* cpart;
   double* gpart;
   double* grad;
+  float* kbar;
+  double* kpart;
+  // 1: vector-Jacobian form with the lensing integral in reverse: the kernel
+  // stage writes no tangents of the WeakLensing shear integral, the product
+  // kernel writes their cotangents, the reverse lensing kernel adds theirs
+  int vjp_rev;
 };
 
 // Small fp32c batches spread the table kernel's per-node evaluations over
@@ -207,6 +222,8 @@ __device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
   r.cpart = gb.cpart ? gb.cpart + (size_t)i * nch * per : nullptr;
   r.gpart = gb.gpart ? gb.gpart + (size_t)i * nch * NDIR : nullptr;
   r.grad = gb.grad ? gb.grad + (size_t)i * NDIR : nullptr;
+  r.kbar = gb.kbar ? gb.kbar + (size_t)i * gb.n_tr * gb.na : nullptr;
+  r.kpart = gb.kpart ? gb.kpart + (size_t)i * kv_chunks(gb.na) * NDIR : nullptr;
   return r;
 }
 

@@ -27,7 +27,10 @@ namespace jcg {
 // accumulated as sum W r, sum W ic, sum W ic (1 - r) dchi'.
 constexpr int GK_NODES = 128;  // nodes per CTA at most (8 warps x 16)
 
-template <int TP>
+// REV (vector-Jacobian form): the shear integral's tangents are not formed
+// (written as 0; grad_kernrev32_kernel applies their cotangents in reverse),
+// the NumberCounts, NLA and single-plane terms keep theirs.
+template <int TP, bool REV>
 __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const ConstTables* __restrict__ c, int npc) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
@@ -95,6 +98,7 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
     float dchi_wl[NDIR];
 #pragma unroll
     for (int d = 0; d < NDIR; ++d) dchi_wl[d] = craw_w > 0.f ? dchi[d][xw] + dslope[d][mw] * DXWL[n] : 0.f;
+    (void)dchi_wl;
     const float zp1 = (float)(1.0 + Z[n]);
     const size_t row = (size_t)n * NZP;
     // WeakLensing tracers: passes of up to TP tracers of one lensing group
@@ -127,6 +131,12 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
         if (!(diff > 0.f)) continue;  // then craw > 0 too
         const float ic = rcpf(fmaxf(chip, 1.f));
         const float r = diff * ic;
+        if (REV) {
+#pragma unroll
+          for (int u = 0; u < TP; ++u)
+            if (tl[u] >= 0) av[u] = fmaf(W[u][j], r, av[u]);
+          continue;
+        }
         const float h = chip > 1.f ? ic * (1.f - r) : ic;
         float dcp[NDIR];
 #pragma unroll
@@ -147,9 +157,11 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) {
           av[u] += __shfl_xor_sync(0xffffffffu, av[u], o);
-          at[u] += __shfl_xor_sync(0xffffffffu, at[u], o);
+          if (!REV) {
+            at[u] += __shfl_xor_sync(0xffffffffu, at[u], o);
 #pragma unroll
-          for (int d = 0; d < NDIR; ++d) ad[u][d] += __shfl_xor_sync(0xffffffffu, ad[u][d], o);
+            for (int d = 0; d < NDIR; ++d) ad[u][d] += __shfl_xor_sync(0xffffffffu, ad[u][d], o);
+          }
         }
       }
       if (lane < NDIR) {
@@ -170,7 +182,7 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
           const float fac = cff * zp1;
           const float acc = av[u];
           const float kv = fac * chi_wl * acc;
-          const float kd = fac * (dlcf * chi_wl * acc + dcw * acc + chi_wl * (adir - dcw * at[u]));
+          const float kd = REV ? 0.f : fac * (dlcf * chi_wl * acc + dcw * acc + chi_wl * (adir - dcw * at[u]));
           float* dst = gi.kernf + ((size_t)t * na + n) * (NDIR + 1);
           if (dir == 0) dst[0] = kv * m1;
           dst[1 + dir] = kd * m1;
@@ -228,9 +240,17 @@ void launch_grad_kern32(const GradBatch& gb, const ConstTables* c, cudaStream_t 
   int npc = GK_NODES;
   while (npc > 8 && (long)((gb.na + npc - 1) / npc) * gb.n_items < target) npc /= 2;
   dim3 grid((gb.na + npc - 1) / npc, gb.n_items);
-  if (gb.n_tr <= 3) grad_kern32_kernel<3><<<grid, 256, 0, st>>>(gb, c, npc);
-  else if (gb.n_tr <= 5) grad_kern32_kernel<5><<<grid, 256, 0, st>>>(gb, c, npc);
-  else grad_kern32_kernel<8><<<grid, 256, 0, st>>>(gb, c, npc);
+  if (gb.vjp_rev) {
+    if (gb.n_tr <= 3) grad_kern32_kernel<3, true><<<grid, 256, 0, st>>>(gb, c, npc);
+    else if (gb.n_tr <= 5) grad_kern32_kernel<5, true><<<grid, 256, 0, st>>>(gb, c, npc);
+    else grad_kern32_kernel<8, true><<<grid, 256, 0, st>>>(gb, c, npc);
+  } else if (gb.n_tr <= 3) {
+    grad_kern32_kernel<3, false><<<grid, 256, 0, st>>>(gb, c, npc);
+  } else if (gb.n_tr <= 5) {
+    grad_kern32_kernel<5, false><<<grid, 256, 0, st>>>(gb, c, npc);
+  } else {
+    grad_kern32_kernel<8, false><<<grid, 256, 0, st>>>(gb, c, npc);
+  }
 }
 
 constexpr int L32_THREADS = 256;

@@ -236,6 +236,22 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
     if (lane == 0) Ered[warp * NET + j] = v;
   }
   __syncthreads();
+  // reverse lensing: the cotangents of the WeakLensing shear kernels,
+  // Kbar_i(t) = u(t) sum_p Q_p(t) dK_i K_j / dK_i (both factors of an auto pair)
+  if (gb.vjp_rev)
+    for (int q = tid; q < tc * n_tr; q += VJ_THREADS) {
+      const int t = q / n_tr, i = q - t * n_tr;
+      if (geo->kind[i] != JCG_TRACER_WL || geo->nz_kind[i] == JCG_NZ_DELTA) continue;
+      const float2* qv = Qd + (size_t)t * n_cls;
+      const float* K = Ks + (size_t)t * n_tr * (NDIR + 1);
+      FF kb{0.f, 0.f};
+      for (int p = 0; p < n_cls; ++p) {
+        const int pi = geo->pair_i[p], pj = geo->pair_j[p];
+        if (pi == i) kb = kb + FF{qv[p].x, qv[p].y} * K[pj * (NDIR + 1)];
+        if (pj == i) kb = kb + FF{qv[p].x, qv[p].y} * K[pi * (NDIR + 1)];
+      }
+      gi.kbar[(size_t)i * na + a0 + t] = R[(size_t)t * NROWG + F_U] * kb.hi;
+    }
   // projection on the tangents: thread (a node t, direction d)
   {
     const int t = tid >> 3, d = tid & 7;
@@ -300,6 +316,178 @@ __global__ void vjp_cl_reduce_kernel(GradBatch gb) {
   }
 }
 
+// Reverse form of the WeakLensing shear kernel (probes.py:44-51, 71-73)
+//   K_i(a) = (1 + m_i) cf (1 + z) chi_w acc_i,  acc_i = sum_j W_ij r_j,
+//   r_j = max(chi'_j - chi_w, 0) / max(chi'_j, 1),  cf = 3 H0^2 Omega_m / 2c
+// given the cotangents Kbar_i(a) of the product kernel: the gradient
+//   sum_{a,i} Kbar_i(a) dK_i(a)/dtheta
+//   = dlncf L + sum_a cw(a) dchi_w(a) + sum_{a,j} c_j(a) dchi'_j(a)
+// with L = sum Kbar_i K_i, cw = fac sum_i Kbar_i (1 + m_i) (acc_i - chi_w at_i)
+// (at_i = sum_j W_ij / max(chi'_j, 1) over chi'_j > chi_w) and c_j = fac chi_w
+// h_j sum_i Kbar_i (1 + m_i) W_ij, h_j = (1 - r_j [chi'_j > 1]) / max(chi'_j, 1).
+// chi' and chi_w are interpolations chi[x] + slope[m] dx of the chi table, so
+// their cotangents gather on the table's nodes and segment slopes
+// (shared-memory adds) and meet the table's 8 tangents once per CTA, instead
+// of the 8 tangents meeting every lensing point.  One CTA per KV_NODES
+// Limber nodes of one cosmology, one warp per node, lanes over the 257 z'
+// points, the WeakLensing tracers of one lensing group per pass.
+template <int TP>
+__global__ void __launch_bounds__(256) grad_kernrev32_kernel(GradBatch gb) {
+  const int item = blockIdx.y, chunk = blockIdx.x;
+  if (item >= gb.n_items) return;
+  const GradItem gi = grad_item(gb, item);
+  const GeoHeader* geo = gi.geo;
+  const int na = geo->na, n_tr = geo->n_tr;
+  const int n0 = chunk * KV_NODES;
+  if (n0 >= na) return;
+  __shared__ int ptr_t[JCG_MAX_TRACERS * TP];
+  __shared__ int pgroup[JCG_MAX_TRACERS];
+  __shared__ int npass_s;
+  __shared__ float chi[NCHI], slope[NCHI];
+  __shared__ float cbar[NCHI], sbar[NCHI];
+  __shared__ float lsum[8];
+  __shared__ double red[8][NDIR];
+  const TabD* tb = gi.tab;
+  if (threadIdx.x == 0) {
+    int np = 0;
+    for (int g = 0; g < geo->n_groups; ++g) {
+      int u = TP;
+      for (int t = 0; t < n_tr; ++t) {
+        if (geo->kind[t] != JCG_TRACER_WL || geo->group[t] != g || geo->nz_kind[t] == JCG_NZ_DELTA) continue;
+        if (u == TP) {
+          pgroup[np] = g;
+          for (int v = 0; v < TP; ++v) ptr_t[np * TP + v] = -1;
+          ++np;
+          u = 0;
+        }
+        ptr_t[(np - 1) * TP + u++] = t;
+      }
+    }
+    npass_s = np;
+  }
+  for (int i = threadIdx.x; i < NCHI; i += blockDim.x) {
+    chi[i] = tb->c32[0][i];
+    slope[i] = tb->s32[0][i];
+    cbar[i] = 0.f;
+    sbar[i] = 0.f;
+  }
+  __syncthreads();
+  const int npass = npass_s;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const double* Z = geo_ptr<double>(geo, geo->off_z);
+  const int32_t* QWL = geo_ptr<int32_t>(geo, geo->off_qwl32);
+  const float* DXWL = geo_ptr<float>(geo, geo->off_dxwl32);
+  const float cff = (float)(3.0 * (H0 * H0) * tb->sv[S_OMEGA_M] / 2.0 / C_KMS);  // probes.py:71
+  float lacc = 0.f;  // sum Kbar K over this lane's nodes (lane 0)
+  const int n_end = min(na, n0 + KV_NODES);
+  for (int n = n0 + warp; n < n_end; n += 8) {
+    const int qw = QWL[n];
+    const int xw = qw & 0xffff, mw = qw >> 16;
+    const float dxw = DXWL[n];
+    const float craw_w = chi[xw] + slope[mw] * dxw;
+    const float chi_wl = fmaxf(craw_w, 0.f);
+    const float fac = cff * (float)(1.0 + Z[n]);
+    const size_t row = (size_t)n * NZP;
+    for (int pass = 0; pass < npass; ++pass) {
+      const int g = pgroup[pass];
+      float kb[TP], av[TP], at[TP];
+      const float* W[TP];
+      bool any = false;
+#pragma unroll
+      for (int u = 0; u < TP; ++u) {
+        const int t = ptr_t[pass * TP + u];
+        kb[u] = t >= 0 ? gi.kbar[(size_t)t * na + n] * (1.f + (float)geo->mult[t]) : 0.f;
+        W[u] = t >= 0 ? geo_ptr<float>(geo, geo->off_W32[t]) + row : nullptr;
+        any |= kb[u] != 0.f;
+        av[u] = 0.f;
+        at[u] = 0.f;
+      }
+      if (!any) continue;  // the same on every lane of the warp
+      const int32_t* Q32 = geo_ptr<int32_t>(geo, geo->off_q32[g]) + row;
+      const float* DX32 = geo_ptr<float>(geo, geo->off_dx32[g]) + row;
+      const float cj_fac = fac * chi_wl;
+      for (int j = lane; j < NZP; j += 32) {
+        const int q = Q32[j];
+        const int x = q & 0xffff, m = q >> 16;
+        const float dx = DX32[j];
+        const float craw = chi[x] + slope[m] * dx;
+        const float chip = fmaxf(craw, 0.f);
+        const float diff = chip - chi_wl;
+        if (!(diff > 0.f)) continue;  // then craw > 0 too
+        const float ic = rcpf(fmaxf(chip, 1.f));
+        const float r = diff * ic;
+        const float h = chip > 1.f ? ic * (1.f - r) : ic;
+        float sw = 0.f;
+#pragma unroll
+        for (int u = 0; u < TP; ++u) {
+          if (W[u]) {
+            const float w = W[u][j];
+            av[u] = fmaf(w, r, av[u]);
+            at[u] = fmaf(w, ic, at[u]);
+            sw = fmaf(kb[u], w, sw);
+          }
+        }
+        const float cj = cj_fac * h * sw;
+        atomicAdd(&cbar[x], cj);
+        atomicAdd(&sbar[m], cj * dx);
+      }
+      float cw = 0.f, lk = 0.f;
+#pragma unroll
+      for (int u = 0; u < TP; ++u) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          av[u] += __shfl_xor_sync(0xffffffffu, av[u], o);
+          at[u] += __shfl_xor_sync(0xffffffffu, at[u], o);
+        }
+        cw = fmaf(kb[u], av[u] - chi_wl * at[u], cw);
+        lk = fmaf(kb[u], av[u], lk);
+      }
+      if (lane == 0) {
+        lacc = fmaf(fac * chi_wl, lk, lacc);
+        if (craw_w > 0.f) {
+          atomicAdd(&cbar[xw], fac * cw);
+          atomicAdd(&sbar[mw], fac * cw * dxw);
+        }
+      }
+    }
+  }
+  if (lane == 0) lsum[warp] = lacc;
+  __syncthreads();
+  // meet the chi table's tangents: sum_x cbar dchi_d[x] + sbar dslope_d[x]
+  double acc[NDIR];
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) acc[d] = 0.0;
+  {
+    float s[NDIR];
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) s[d] = 0.f;
+    for (int x = threadIdx.x; x < NCHI; x += blockDim.x) {
+      const float cb = cbar[x], sb = sbar[x];
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) s[d] = fmaf(cb, tb->c32[1 + d][x], fmaf(sb, tb->s32[1 + d][x], s[d]));
+    }
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) {
+      float v = s[d];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp][d] = (double)v;
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < NDIR) {
+    const int d = threadIdx.x;
+    double g = 0.0, L = 0.0;
+    for (int w = 0; w < 8; ++w) {
+      g += red[w][d];
+      L += (double)lsum[w];
+    }
+    // d ln cf / dtheta = d Omega_m / Omega_m
+    g += L * (tb->sd[d][S_OMEGA_M] / tb->sv[S_OMEGA_M]);
+    gi.kpart[(size_t)chunk * NDIR + d] = g;
+  }
+}
+
 // the gradient from the chunks' partials (fixed order)
 __global__ void vjp_grad_reduce_kernel(GradBatch gb) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -309,6 +497,10 @@ __global__ void vjp_grad_reduce_kernel(GradBatch gb) {
   const int nch = vjp_chunks(gi.geo->na);
   double g = 0.0;
   for (int c = 0; c < nch; ++c) g += gi.gpart[(size_t)c * NDIR + d];
+  if (gb.vjp_rev) {
+    const int nk = kv_chunks(gi.geo->na);
+    for (int c = 0; c < nk; ++c) g += gi.kpart[(size_t)c * NDIR + d];
+  }
   gi.grad[d] = g;
 }
 
@@ -336,6 +528,12 @@ void launch_vjp32_cl(const GradBatch& gb, cudaStream_t st) {
 void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st) {
   if (gb.physics_or != 0) launch_vjp_t<true, false>(gb, st);
   else launch_vjp_t<false, false>(gb, st);
+  if (gb.vjp_rev) {
+    dim3 grid(kv_chunks(gb.na), gb.n_items);
+    if (gb.n_tr <= 3) grad_kernrev32_kernel<3><<<grid, 256, 0, st>>>(gb);
+    else if (gb.n_tr <= 5) grad_kernrev32_kernel<5><<<grid, 256, 0, st>>>(gb);
+    else grad_kernrev32_kernel<8><<<grid, 256, 0, st>>>(gb);
+  }
   vjp_grad_reduce_kernel<<<(gb.n_items * NDIR + 127) / 128, 128, 0, st>>>(gb);
 }
 
