@@ -1823,7 +1823,10 @@ static size_t ptt_bytes(int precision) {
 
 // node scratch of the small-batch fp32c table path
 static size_t gnode_bytes(int n, int precision) {
-  return (precision == JCG_FP32C && n <= GNODE_MAX_ITEMS) ? al256(sizeof(double) * GNODE_STRIDE * (size_t)n) : 0;
+  // fp32c: the table stage's node evaluations always run in their own kernel
+  // (one node per thread at full occupancy; the table kernel's 255-register
+  // threads keep the scans)
+  return precision == JCG_FP32C ? al256(sizeof(double) * GNODE_STRIDE * (size_t)n) : 0;
 }
 
 size_t grad_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {

@@ -187,13 +187,13 @@ struct GradBatch {
   int vjp_rev;
 };
 
-// Small fp32c batches spread the table kernel's per-node evaluations over
+// fp32c batches spread the table kernel's per-node evaluations over
 // GNODE_CTAS CTAs per cosmology (grad_nodes_kernel) and hand them over in
 // the table kernel's shared-memory layout: chi right-hand sides at nodes and
 // midpoints [2][NDIR + 1][NCHI], growth coefficients [4][NDIR + 1][NGROW],
 // the Romberg integrand [NDIR + 1][NROMB], then exp(n_s ln k) T(k)^2 on the
 // P(k) grid [NDIR + 1][NKH] (value, then 8 tangents).
-constexpr int GNODE_MAX_ITEMS = 128;
+constexpr int GNODE_MAX_ITEMS = 128;  // up to this many cosmologies the scalars run on half warps
 constexpr int GNODE_FM = (NDIR + 1) * NCHI;
 constexpr int GNODE_QR = 2 * (NDIR + 1) * NCHI;
 constexpr int GNODE_FR = GNODE_QR + 4 * (NDIR + 1) * NGROW;

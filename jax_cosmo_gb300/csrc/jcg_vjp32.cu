@@ -326,11 +326,15 @@ __global__ void vjp_cl_reduce_kernel(GradBatch gb) {
 // (at_i = sum_j W_ij / max(chi'_j, 1) over chi'_j > chi_w) and c_j = fac chi_w
 // h_j sum_i Kbar_i (1 + m_i) W_ij, h_j = (1 - r_j [chi'_j > 1]) / max(chi'_j, 1).
 // chi' and chi_w are interpolations chi[x] + slope[m] dx of the chi table, so
-// their cotangents gather on the table's nodes and segment slopes
-// (shared-memory adds) and meet the table's 8 tangents once per CTA, instead
-// of the 8 tangents meeting every lensing point.  One CTA per KV_NODES
-// Limber nodes of one cosmology, one warp per node, lanes over the 257 z'
-// points, the WeakLensing tracers of one lensing group per pass.
+// their cotangents gather on the table's nodes and segment slopes and meet
+// the table's 8 tangents once per CTA, instead of the 8 tangents meeting
+// every lensing point.  One CTA per KV_NODES Limber nodes of one cosmology,
+// one warp per node, lanes over the 257 z' points, the WeakLensing tracers
+// of one lensing group per pass.  The gather is deterministic: the table
+// index of consecutive z' points is monotone, so a segmented warp scan sums
+// each index's run and the run's last lane adds it to the warp's own copy
+// of the table cotangents; the 8 copies are added in a fixed order (the
+// same result alone and in any batch, bit for bit).
 template <int TP>
 __global__ void __launch_bounds__(256) grad_kernrev32_kernel(GradBatch gb) {
   const int item = blockIdx.y, chunk = blockIdx.x;
@@ -344,7 +348,7 @@ __global__ void __launch_bounds__(256) grad_kernrev32_kernel(GradBatch gb) {
   __shared__ int pgroup[JCG_MAX_TRACERS];
   __shared__ int npass_s;
   __shared__ float chi[NCHI], slope[NCHI];
-  __shared__ float cbar[NCHI], sbar[NCHI];
+  __shared__ float cbw[8][NCHI], sbw[8][NCHI];  // per-warp table cotangents
   __shared__ float lsum[8];
   __shared__ double red[8][NDIR];
   const TabD* tb = gi.tab;
@@ -368,8 +372,10 @@ __global__ void __launch_bounds__(256) grad_kernrev32_kernel(GradBatch gb) {
   for (int i = threadIdx.x; i < NCHI; i += blockDim.x) {
     chi[i] = tb->c32[0][i];
     slope[i] = tb->s32[0][i];
-    cbar[i] = 0.f;
-    sbar[i] = 0.f;
+  }
+  for (int i = threadIdx.x; i < 8 * NCHI; i += blockDim.x) {
+    (&cbw[0][0])[i] = 0.f;
+    (&sbw[0][0])[i] = 0.f;
   }
   __syncthreads();
   const int npass = npass_s;
@@ -406,30 +412,50 @@ __global__ void __launch_bounds__(256) grad_kernrev32_kernel(GradBatch gb) {
       const int32_t* Q32 = geo_ptr<int32_t>(geo, geo->off_q32[g]) + row;
       const float* DX32 = geo_ptr<float>(geo, geo->off_dx32[g]) + row;
       const float cj_fac = fac * chi_wl;
-      for (int j = lane; j < NZP; j += 32) {
-        const int q = Q32[j];
-        const int x = q & 0xffff, m = q >> 16;
-        const float dx = DX32[j];
-        const float craw = chi[x] + slope[m] * dx;
-        const float chip = fmaxf(craw, 0.f);
-        const float diff = chip - chi_wl;
-        if (!(diff > 0.f)) continue;  // then craw > 0 too
-        const float ic = rcpf(fmaxf(chip, 1.f));
-        const float r = diff * ic;
-        const float h = chip > 1.f ? ic * (1.f - r) : ic;
-        float sw = 0.f;
+      float* cb = cbw[warp];
+      float* sb = sbw[warp];
+      for (int jb = 0; jb < NZP; jb += 32) {
+        const int j = jb + lane;
+        int x = -1, m = -1;
+        float cj = 0.f, cjdx = 0.f;
+        if (j < NZP) {
+          const int q = Q32[j];
+          x = q & 0xffff, m = q >> 16;
+          const float dx = DX32[j];
+          const float craw = chi[x] + slope[m] * dx;
+          const float chip = fmaxf(craw, 0.f);
+          const float diff = chip - chi_wl;
+          if (diff > 0.f) {  // then craw > 0 too
+            const float ic = rcpf(fmaxf(chip, 1.f));
+            const float r = diff * ic;
+            const float h = chip > 1.f ? ic * (1.f - r) : ic;
+            float sw = 0.f;
 #pragma unroll
-        for (int u = 0; u < TP; ++u) {
-          if (W[u]) {
-            const float w = W[u][j];
-            av[u] = fmaf(w, r, av[u]);
-            at[u] = fmaf(w, ic, at[u]);
-            sw = fmaf(kb[u], w, sw);
+            for (int u = 0; u < TP; ++u) {
+              if (W[u]) {
+                const float w = W[u][j];
+                av[u] = fmaf(w, r, av[u]);
+                at[u] = fmaf(w, ic, at[u]);
+                sw = fmaf(kb[u], w, sw);
+              }
+            }
+            cj = cj_fac * h * sw;
+            cjdx = cj * dx;
           }
         }
-        const float cj = cj_fac * h * sw;
-        atomicAdd(&cbar[x], cj);
-        atomicAdd(&sbar[m], cj * dx);
+        // segmented inclusive scans over runs of equal x and of equal m
+        // (both monotone in j), then the run's last lane adds the run
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const float vc = __shfl_up_sync(0xffffffffu, cj, o), vs = __shfl_up_sync(0xffffffffu, cjdx, o);
+          const int kx = __shfl_up_sync(0xffffffffu, x, o), km = __shfl_up_sync(0xffffffffu, m, o);
+          if (lane >= o && kx == x) cj += vc;
+          if (lane >= o && km == m) cjdx += vs;
+        }
+        const int nx = __shfl_down_sync(0xffffffffu, x, 1), nm = __shfl_down_sync(0xffffffffu, m, 1);
+        if (x >= 0 && (lane == 31 || nx != x)) cb[x] += cj;
+        if (m >= 0 && (lane == 31 || nm != m)) sb[m] += cjdx;
+        __syncwarp();
       }
       float cw = 0.f, lk = 0.f;
 #pragma unroll
@@ -445,10 +471,11 @@ __global__ void __launch_bounds__(256) grad_kernrev32_kernel(GradBatch gb) {
       if (lane == 0) {
         lacc = fmaf(fac * chi_wl, lk, lacc);
         if (craw_w > 0.f) {
-          atomicAdd(&cbar[xw], fac * cw);
-          atomicAdd(&sbar[mw], fac * cw * dxw);
+          cb[xw] += fac * cw;
+          sb[mw] += fac * cw * dxw;
         }
       }
+      __syncwarp();
     }
   }
   if (lane == 0) lsum[warp] = lacc;
@@ -462,7 +489,8 @@ __global__ void __launch_bounds__(256) grad_kernrev32_kernel(GradBatch gb) {
 #pragma unroll
     for (int d = 0; d < NDIR; ++d) s[d] = 0.f;
     for (int x = threadIdx.x; x < NCHI; x += blockDim.x) {
-      const float cb = cbar[x], sb = sbar[x];
+      float cb = 0.f, sb = 0.f;
+      for (int w = 0; w < 8; ++w) cb += cbw[w][x], sb += sbw[w][x];
 #pragma unroll
       for (int d = 0; d < NDIR; ++d) s[d] = fmaf(cb, tb->c32[1 + d][x], fmaf(sb, tb->s32[1 + d][x], s[d]));
     }
