@@ -223,6 +223,11 @@ def gpu_arm(args, rank, world, device):
         torch.cuda.synchronize(device)
         return float(np.sum(times)), times
 
+    if args.fwd_only:
+        # the fp32c angular_cl step alone (a profiling entry)
+        tf, _ = timed(lambda: step("fp32c"), args.steps, args.warmup)
+        return {"jacobian_only": {"batch": B, "ms_per_step": tf / args.steps, "what": "C_ell fp32c",
+                                  "cl_per_s": B * 15 * N_ELL / (tf / args.steps * 1e-3)}}
     if args.vjp_only:
         # the fp32c C_ell + vector-Jacobian product alone (a profiling entry)
         from jax_cosmo_gb300.autodiff import vjp_device
@@ -674,6 +679,8 @@ def main():
     ap.add_argument("--serve-seconds", type=float, default=10.0)
     ap.add_argument("--jacobian-only", action="store_true",
                     help="time only the fp32c C_ell + Jacobian of the batch (profiling)")
+    ap.add_argument("--fwd-only", action="store_true",
+                    help="time only the fp32c C_ell step of the batch (profiling)")
     ap.add_argument("--vjp-only", action="store_true",
                     help="time only the fp32c C_ell + vector-Jacobian product of the batch (profiling)")
     args = ap.parse_args()

@@ -1572,12 +1572,15 @@ int grad_limber_tile(int n_ell, int n_cls) {
 __global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= GNODE_WORK) return;
   const GradItem gi = grad_item(gb, item);
   const TabD* tb = gi.tab;
-  FF8 sF[NSCAL];
-  for (int i = 0; i < NSCAL; ++i) sF[i] = ff8_of(tb->sv[i], &tb->sd[0][i], NSCAL);
+  // the cosmology's scalars with tangents, shared by the CTA (a per-thread
+  // copy would sit in local memory)
+  __shared__ FF8 sF[NSCAL];
+  for (int i = threadIdx.x; i < NSCAL; i += blockDim.x) sF[i] = ff8_of(tb->sv[i], &tb->sd[0][i], NSCAL);
+  __syncthreads();
+  const int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= GNODE_WORK) return;
   const BgT<FF8> bgf = make_bgT(sF);
   double* dst = gb.gnode + (size_t)item * GNODE_STRIDE;
   auto putf = [&](int off, int stride, int i, const FF8& x) {
@@ -1896,6 +1899,7 @@ size_t vjp_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
   o += al256(sizeof(double) * (size_t)vjp_chunks(h.na) * NDIR * n_cosmo);
   o += al256(sizeof(float) * (size_t)h.n_tr * h.na * n_cosmo);
   o += al256(sizeof(double) * (size_t)kv_chunks(h.na) * NDIR * n_cosmo);
+  o += al256(sizeof(int) * 9 * (size_t)kv_chunks(h.na));
   o += gnode_bytes(n_cosmo, precision);
   return o;
 }
@@ -1939,8 +1943,14 @@ void vjp_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int
   o += al256(sizeof(float) * (size_t)h.n_tr * h.na * n_cosmo);
   gb.kpart = reinterpret_cast<double*>(base + o);
   o += al256(sizeof(double) * (size_t)kv_chunks(h.na) * NDIR * n_cosmo);
+  gb.krev_owner = reinterpret_cast<int*>(base + o);
+  o += al256(sizeof(int) * 9 * (size_t)kv_chunks(h.na));
   gb.gnode = gnode_bytes(n_cosmo, precision) ? reinterpret_cast<double*>(base + o) : nullptr;
   gb.vjp_rev = (vbar && grad) ? 1 : 0;
+  gb.krev_u = gb.vjp_rev && krev_uniform_ok(h);
+  gb.krev_wbase = krev_wbase(h);
+  gb.n_wl = h.n_wl;
+  gb.kern_rest = h.n_nc > 0 || h.special_bias;
   gb.vbar = vbar;
   gb.grad = grad;
   gb.cl = cl;
@@ -1951,6 +1961,13 @@ void vjp_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int
   gb.n_split = 1;
   gb.physics_or = h.physics;
   launch_grad_front(gb, c, st);
+  if (cl && vbar && grad) {
+    // the caller's cotangent: one pass gives the partial C_ell and the product
+    gb.vjp_cl = 1;
+    launch_vjp32_grad(gb, st);
+    launch_vjp32_cl_reduce(gb, st);
+    return;
+  }
   if (cl) launch_vjp32_cl(gb, st);
   if (vbar && grad) launch_vjp32_grad(gb, st);
 }

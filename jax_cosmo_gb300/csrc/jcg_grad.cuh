@@ -134,8 +134,8 @@ struct GradItem {
   double* kpart;
 };
 
-// node chunks of the reverse lensing kernel
-constexpr int KV_NODES = 32;
+// node chunks of the reverse lensing kernels
+constexpr int KV_NODES = 16;
 __host__ __device__ inline int kv_chunks(int na) { return (na + KV_NODES - 1) / KV_NODES; }
 
 // a-chunks of the vector-Jacobian product kernels: at most VJ_TA Limber
@@ -185,6 +185,17 @@ struct GradBatch {
   // stage writes no tangents of the WeakLensing shear integral, the product
   // kernel writes their cotangents, the reverse lensing kernel adds theirs
   int vjp_rev;
+  // uniform form of the reverse lensing integral (one geometry, one lensing
+  // group, no single-plane n(z), 1..8 WeakLensing tracers): lanes over
+  // cosmologies.  krev_wbase: the first chi table segment a Limber node or
+  // lensing point can fall in; krev_owner: [kv_chunks][9] the segment ranges
+  // of the 8 warps per node chunk; kern_rest: NumberCounts or NLA terms (the
+  // per-cosmology kernel stage still runs for them)
+  int krev_u, krev_wbase, n_wl, kern_rest;
+  int* krev_owner;
+  // 1: the cotangent does not depend on C_ell (given by the caller), so the
+  // product kernel also writes the chunks' partial C_ell (no forward pass)
+  int vjp_cl;
 };
 
 // fp32c batches spread the table kernel's per-node evaluations over
@@ -264,7 +275,12 @@ void launch_grad_limber32(const GradBatch& gb, const ConstTables* c, cudaStream_
 // vector-Jacobian product (jcg_vjp32.cu): C_ell of the items into their cl,
 // and the product with their cotangents vbar into their grad
 void launch_vjp32_cl(const GradBatch& gb, cudaStream_t st);
+void launch_vjp32_cl_reduce(const GradBatch& gb, cudaStream_t st);
 void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st);
+// uniform reverse lensing: the shear kernels' values (lanes over cosmologies)
+void launch_kernval32u(const GradBatch& gb, cudaStream_t st);
+int krev_wbase(const GeoHeader& h);
+bool krev_uniform_ok(const GeoHeader& h);
 // tables, rows and radial kernels with tangents (the stages before Limber)
 void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t st);
 int grad_limber32_tile(int n_ell, int n_cls);

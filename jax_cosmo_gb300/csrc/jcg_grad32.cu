@@ -29,8 +29,10 @@ constexpr int GK_NODES = 128;  // nodes per CTA at most (8 warps x 16)
 
 // REV (vector-Jacobian form): the shear integral's tangents are not formed
 // (written as 0; grad_kernrev32_kernel applies their cotangents in reverse),
-// the NumberCounts, NLA and single-plane terms keep theirs.
-template <int TP, bool REV>
+// the NumberCounts, NLA and single-plane terms keep theirs.  UW: the shear
+// values come from grad_kernval32u_kernel (uniform batch), this kernel adds
+// the other terms only.
+template <int TP, bool REV, bool UW = false>
 __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const ConstTables* __restrict__ c, int npc) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
@@ -74,7 +76,7 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
     }
   }
   __syncthreads();
-  const int npass = npass_s;
+  const int npass = UW ? 0 : npass_s;
   const float* chi = ctab[0];
   const float* slope = stab[0];
   const float(*dchi)[NCHI] = ctab + 1;
@@ -240,7 +242,15 @@ void launch_grad_kern32(const GradBatch& gb, const ConstTables* c, cudaStream_t 
   int npc = GK_NODES;
   while (npc > 8 && (long)((gb.na + npc - 1) / npc) * gb.n_items < target) npc /= 2;
   dim3 grid((gb.na + npc - 1) / npc, gb.n_items);
-  if (gb.vjp_rev) {
+  if (gb.krev_u) {
+    // uniform batch: the shear values in the lanes-over-cosmologies layout,
+    // then the NumberCounts / NLA terms (if any) per cosmology
+    launch_kernval32u(gb, st);
+    if (!gb.kern_rest) return;
+    if (gb.n_tr <= 3) grad_kern32_kernel<3, true, true><<<grid, 256, 0, st>>>(gb, c, npc);
+    else if (gb.n_tr <= 5) grad_kern32_kernel<5, true, true><<<grid, 256, 0, st>>>(gb, c, npc);
+    else grad_kern32_kernel<8, true, true><<<grid, 256, 0, st>>>(gb, c, npc);
+  } else if (gb.vjp_rev) {
     if (gb.n_tr <= 3) grad_kern32_kernel<3, true><<<grid, 256, 0, st>>>(gb, c, npc);
     else if (gb.n_tr <= 5) grad_kern32_kernel<5, true><<<grid, 256, 0, st>>>(gb, c, npc);
     else grad_kern32_kernel<8, true><<<grid, 256, 0, st>>>(gb, c, npc);

@@ -189,7 +189,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
       }
     }
     __syncthreads();
-    if (FWD) {
+    if (FWD || gb.vjp_cl) {
       // partial C_p(l) of the chunk: sum_t M_p(t) P(t, l)
       float* cp = gi.cpart + (size_t)chunk * n_cls * n_ell;
       for (int q = tid; q < n_cls * lt; q += VJ_THREADS) {
@@ -198,7 +198,8 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
         for (int t = 0; t < tc; ++t) s = fmaf(Pt[t * LT + l], Mv[t * n_cls + p], s);
         cp[(size_t)p * n_ell + l0 + l] = s;
       }
-    } else {
+    }
+    if (!FWD) {
       // Q_p(t) += sum_l v_p(l) P(t, l): float sums of at most 32 terms,
       // added in float-pair arithmetic
       for (int q = tid; q < tc * n_cls; q += VJ_THREADS) {
@@ -516,6 +517,347 @@ __global__ void __launch_bounds__(256) grad_kernrev32_kernel(GradBatch gb) {
   }
 }
 
+// ------------------------------------------------ uniform reverse lensing --
+// A batch sharing one geometry (one lensing group, no single-plane n(z)):
+// lanes are 32 cosmologies, as in the forward tracer32_uniform_kernel, so the
+// lensing grid of a node (segments, offsets, n(z') weights) is read once per
+// 32 cosmologies, every branch on it is warp-uniform, and each lane reads its
+// cosmology's chi table from shared memory ([segment][cosmology]).  Only the
+// table segments from krev_wbase up can hold a Limber node or lensing point
+// (a >= z2a(max(zmax, probe zmax))), so the shared tables start there.
+constexpr int KU_PAD = 33;
+constexpr int KU_NODES = 32;  // nodes per CTA of the value kernel
+
+__host__ __device__ inline size_t ku_val_smem(int wn) { return sizeof(float) * 2 * (size_t)wn * KU_PAD; }
+__host__ __device__ inline size_t ku_rev_smem(int wn) {
+  return sizeof(float) * ((size_t)5 * wn * KU_PAD + (size_t)8 * KV_NODES * KU_PAD + 8 * KU_PAD);
+}
+
+bool krev_uniform_ok(const GeoHeader& h) {
+  return !h.custom_nodes && h.n_wl >= 1 && h.n_wl <= 8 && h.n_groups == 1 && !h.has_delta;
+}
+
+// first chi table segment (atab_chi = logspace(-3, 0, NCHI)) that a Limber
+// node or a lensing point can fall in, two segments of margin
+int krev_wbase(const GeoHeader& h) {
+  const double zm = fmax(h.zmax, h.group_zmax[0]);
+  const double t = (log10(1.0 / (1.0 + zm)) + 3.0) * (NCHI - 1) / 3.0;
+  int w = (int)floor(t) - 2;
+  if (!(t > 2.0)) w = 0;
+  return w > NCHI - 2 ? NCHI - 2 : w;
+}
+
+// K_t(a) of the WeakLensing tracers (probes.py:44-51, 71-73) with no shear
+// tangents (the reverse kernel below takes the integral's cotangents):
+//   K = cf (1 + z) chi_w sum_j W_tj r_j (1 + m_t),
+// the per-cosmology grad_kern32_kernel's values in the lanes-over-cosmologies
+// layout.  Writes the value and 8 zero tangents of each (tracer, node); the
+// kernel stage adds NLA terms to them afterwards.
+template <int NW>
+__global__ void __launch_bounds__(256) grad_kernval32u_kernel(GradBatch gb) {
+  const GeoHeader* geo = gb.geo;
+  const int na = geo->na, n_tr = geo->n_tr;
+  const int n0 = blockIdx.x * KU_NODES, c0 = blockIdx.y * 32;
+  if (n0 >= na || c0 >= gb.n_items) return;
+  const int wbase = gb.krev_wbase, wn = NCHI - wbase;
+  extern __shared__ float kv_smem[];
+  float* chiT = kv_smem;             // [wn][KU_PAD]
+  float* slT = kv_smem + wn * KU_PAD;  // [wn][KU_PAD]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int idx = tid; idx < 32 * wn; idx += blockDim.x) {
+    const int cc = idx / wn, i = idx % wn;
+    const int ci = c0 + cc;
+    float cv = 0.f, sv = 0.f;
+    if (ci < gb.n_items) {
+      cv = gb.tab[ci].c32[0][wbase + i];
+      sv = gb.tab[ci].s32[0][wbase + i];
+    }
+    chiT[i * KU_PAD + cc] = cv;
+    slT[i * KU_PAD + cc] = sv;
+  }
+  __syncthreads();
+  const int ci = c0 + lane;
+  const bool live = ci < gb.n_items;
+  const TabD* tb = gb.tab + (live ? ci : c0);
+  const float cff = (float)(3.0 * (H0 * H0) * tb->sv[S_OMEGA_M] / 2.0 / C_KMS);  // probes.py:71
+  int wl_t[NW];
+  float m1[NW];
+  {
+    int u = 0;
+    for (int t = 0; t < n_tr && u < NW; ++t)
+      if (geo->kind[t] == JCG_TRACER_WL) wl_t[u++] = t;
+#pragma unroll
+    for (int v = 0; v < NW; ++v) m1[v] = 1.f + (float)geo->mult[wl_t[v]];
+  }
+  const double* Z = geo_ptr<double>(geo, geo->off_z);
+  const int32_t* QWL = geo_ptr<int32_t>(geo, geo->off_qwl32);
+  const float* DXWL = geo_ptr<float>(geo, geo->off_dxwl32);
+  const int32_t* Q32b = geo_ptr<int32_t>(geo, geo->off_q32[0]);
+  const float* DX32b = geo_ptr<float>(geo, geo->off_dx32[0]);
+  const float* Wb[NW];
+#pragma unroll
+  for (int u = 0; u < NW; ++u) Wb[u] = geo_ptr<float>(geo, geo->off_W32[wl_t[u]]);
+  float* kf = gb.kernf + (size_t)(live ? ci : c0) * n_tr * na * (NDIR + 1);
+  const int n_end = min(na, n0 + KU_NODES);
+  for (int n = n0 + warp; n < n_end; n += 8) {
+    const int qw = QWL[n];
+    const float craw_w = chiT[((qw & 0xffff) - wbase) * KU_PAD + lane] + slT[((qw >> 16) - wbase) * KU_PAD + lane] * DXWL[n];
+    const float chi_wl = fmaxf(craw_w, 0.f);
+    float acc[NW];
+#pragma unroll
+    for (int u = 0; u < NW; ++u) acc[u] = 0.f;
+    const size_t row = (size_t)n * NZP;
+    for (int j0 = 0; j0 < NZP; j0 += 32) {
+      const int jl = j0 + lane;
+      const bool in = jl < NZP;
+      const int qv = in ? Q32b[row + jl] : 0;
+      const float dxv = in ? DX32b[row + jl] : 0.f;
+      float wv[NW];
+#pragma unroll
+      for (int u = 0; u < NW; ++u) wv[u] = in ? Wb[u][row + jl] : 0.f;
+      const int cnt = min(32, NZP - j0);
+      for (int jj = 0; jj < cnt; ++jj) {
+        const int q = __shfl_sync(0xffffffffu, qv, jj);
+        const float dx = __shfl_sync(0xffffffffu, dxv, jj);
+        const float chip =
+            fmaxf(chiT[((q & 0xffff) - wbase) * KU_PAD + lane] + slT[((q >> 16) - wbase) * KU_PAD + lane] * dx, 0.f);
+        const float diff = chip - chi_wl;
+        const float r = diff > 0.f ? diff * rcpf(fmaxf(chip, 1.f)) : 0.f;
+#pragma unroll
+        for (int u = 0; u < NW; ++u) acc[u] = fmaf(__shfl_sync(0xffffffffu, wv[u], jj), r, acc[u]);
+      }
+    }
+    if (live) {
+      const float fac = cff * (float)(1.0 + Z[n]);
+#pragma unroll
+      for (int u = 0; u < NW; ++u) {
+        float* dst = kf + ((size_t)wl_t[u] * na + n) * (NDIR + 1);
+        dst[0] = fac * chi_wl * acc[u] * m1[u];
+#pragma unroll
+        for (int d = 0; d < NDIR; ++d) dst[1 + d] = 0.f;
+      }
+    }
+  }
+}
+
+// Segment ownership of the 8 warps of grad_kernrev32u_kernel per chunk of
+// KV_NODES nodes: warp w takes the chunk's lensing points whose chi table
+// segment m lies in [b_w, b_{w+1}); the boundaries split the chunk's points
+// into near-equal eighths.  (Integer histogram: the same bounds every run.)
+__global__ void __launch_bounds__(256) kernrev_owner_kernel(const GeoHeader* geo, int* bounds) {
+  const int chunk = blockIdx.x, na = geo->na;
+  const int n0 = chunk * KV_NODES, n_end = min(na, n0 + KV_NODES);
+  __shared__ int hist[NCHI];
+  for (int i = threadIdx.x; i < NCHI; i += blockDim.x) hist[i] = 0;
+  __syncthreads();
+  const int32_t* Q32 = geo_ptr<int32_t>(geo, geo->off_q32[0]) + (size_t)n0 * NZP;
+  const int cnt = (n_end - n0) * NZP;
+  for (int i = threadIdx.x; i < cnt; i += blockDim.x) atomicAdd(&hist[Q32[i] >> 16], 1);
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int* b = bounds + (size_t)chunk * 9;
+    b[0] = 0;
+    int below = 0, w = 1;  // below: points with a segment < m
+    for (int m = 0; m < NCHI; ++m) {
+      while (w < 8 && (long long)below * 8 >= (long long)w * cnt) b[w++] = m;
+      below += hist[m];
+    }
+    while (w < 8) b[w++] = NCHI;
+    b[8] = NCHI;
+  }
+}
+
+// Reverse form of the shear integral (the same sums as grad_kernrev32_kernel,
+// whose header derives them), lanes over 32 cosmologies.  The warps share a
+// chunk of KV_NODES nodes and split its lensing points by segment
+// (kernrev_owner_kernel), so the segment-indexed cotangents
+//   cL[m] (chi at node m), cR[m] (chi at node m + 1), sB[m] (slope of m)
+// of a lane are written by one warp only, in a fixed order.  The segment of
+// consecutive points changes every few points: the current run's sums stay
+// in registers and go to shared memory when it changes.  The chi_w
+// cotangents (one per node and warp) and the sums for d ln cf wait in shared
+// memory; at the end warp d meets them all with tangent d of each lane's
+// chi table.  One partial gradient per (cosmology, node chunk) in kpart.
+template <int NW>
+__global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
+  const GeoHeader* geo = gb.geo;
+  const int na = geo->na, n_tr = geo->n_tr;
+  const int chunk = blockIdx.x, c0 = blockIdx.y * 32;
+  const int n0 = chunk * KV_NODES;
+  if (n0 >= na || c0 >= gb.n_items) return;
+  const int n_end = min(na, n0 + KV_NODES);
+  const int wbase = gb.krev_wbase, wn = NCHI - wbase;
+  extern __shared__ float kr_smem[];
+  float* chiT = kr_smem;                        // [wn][KU_PAD]
+  float* slT = chiT + wn * KU_PAD;              // [wn][KU_PAD]
+  float* cL = slT + wn * KU_PAD;                // [wn][KU_PAD]
+  float* cR = cL + wn * KU_PAD;                 // [wn][KU_PAD]
+  float* sB = cR + wn * KU_PAD;                 // [wn][KU_PAD]
+  float* cwS = sB + wn * KU_PAD;                // [8][KV_NODES][KU_PAD]
+  float* lS = cwS + 8 * KV_NODES * KU_PAD;      // [8][KU_PAD]
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  for (int idx = tid; idx < 32 * wn; idx += blockDim.x) {
+    const int cc = idx / wn, i = idx % wn;
+    const int ci = c0 + cc;
+    float cv = 0.f, sv = 0.f;
+    if (ci < gb.n_items) {
+      cv = gb.tab[ci].c32[0][wbase + i];
+      sv = gb.tab[ci].s32[0][wbase + i];
+    }
+    chiT[i * KU_PAD + cc] = cv;
+    slT[i * KU_PAD + cc] = sv;
+    cL[i * KU_PAD + cc] = 0.f;
+    cR[i * KU_PAD + cc] = 0.f;
+    sB[i * KU_PAD + cc] = 0.f;
+  }
+  for (int idx = tid; idx < 8 * KV_NODES * KU_PAD; idx += blockDim.x) cwS[idx] = 0.f;
+  __syncthreads();
+  const int ci = c0 + lane;
+  const bool live = ci < gb.n_items;
+  const TabD* tb = gb.tab + (live ? ci : c0);
+  const float cff = (float)(3.0 * (H0 * H0) * tb->sv[S_OMEGA_M] / 2.0 / C_KMS);  // probes.py:71
+  const float* kbar = gb.kbar + (size_t)(live ? ci : c0) * n_tr * na;
+  int wl_t[NW];
+  float m1[NW];
+  {
+    int u = 0;
+    for (int t = 0; t < n_tr && u < NW; ++t)
+      if (geo->kind[t] == JCG_TRACER_WL) wl_t[u++] = t;
+#pragma unroll
+    for (int v = 0; v < NW; ++v) m1[v] = 1.f + (float)geo->mult[wl_t[v]];
+  }
+  const double* Z = geo_ptr<double>(geo, geo->off_z);
+  const int32_t* QWL = geo_ptr<int32_t>(geo, geo->off_qwl32);
+  const float* DXWL = geo_ptr<float>(geo, geo->off_dxwl32);
+  const int32_t* Q32b = geo_ptr<int32_t>(geo, geo->off_q32[0]);
+  const float* DX32b = geo_ptr<float>(geo, geo->off_dx32[0]);
+  const float* Wb[NW];
+#pragma unroll
+  for (int u = 0; u < NW; ++u) Wb[u] = geo_ptr<float>(geo, geo->off_W32[wl_t[u]]);
+  const int blo = gb.krev_owner[chunk * 9 + warp], bhi = gb.krev_owner[chunk * 9 + warp + 1];
+  int key = -1;           // the current run's segment query (nearest | segment << 16)
+  float rc = 0.f, rcd = 0.f;  // the run's chi' cotangent, and times dx
+  float lacc = 0.f;       // sum_n fac chi_w sum_j sw r  (the d ln cf sum)
+  auto flush = [&]() {
+    const int m = key >> 16, i = (m - wbase) * KU_PAD + lane;
+    if ((key & 0xffff) == m) cL[i] += rc;
+    else cR[i] += rc;
+    sB[i] += rcd;
+  };
+  for (int n = n0; n < n_end; ++n) {
+    const int qw = QWL[n];
+    const float craw_w =
+        chiT[((qw & 0xffff) - wbase) * KU_PAD + lane] + slT[((qw >> 16) - wbase) * KU_PAD + lane] * DXWL[n];
+    const float chi_wl = fmaxf(craw_w, 0.f);
+    const float fac = cff * (float)(1.0 + Z[n]);
+    const float cjf = fac * chi_wl;
+    float kb[NW];
+#pragma unroll
+    for (int u = 0; u < NW; ++u) kb[u] = kbar[(size_t)wl_t[u] * na + n] * m1[u];
+    const size_t row = (size_t)n * NZP;
+    float lk = 0.f, cwa = 0.f;
+    for (int j0 = 0; j0 < NZP; j0 += 32) {
+      const int jl = j0 + lane;
+      const int qv = jl < NZP ? Q32b[row + jl] : -1;
+      const int mv = qv >> 16;  // -1 past the row's end
+      unsigned mask = __ballot_sync(0xffffffffu, mv >= blo && mv < bhi);
+      if (!mask) continue;
+      const bool own = (mask >> lane) & 1u;
+      const float dxv = own ? DX32b[row + jl] : 0.f;
+      float wv[NW];
+#pragma unroll
+      for (int u = 0; u < NW; ++u) wv[u] = own ? Wb[u][row + jl] : 0.f;
+      while (mask) {
+        const int jj = __ffs(mask) - 1;
+        mask &= mask - 1;
+        const int q = __shfl_sync(0xffffffffu, qv, jj);
+        const float dx = __shfl_sync(0xffffffffu, dxv, jj);
+        float sw = 0.f;  // sum_t Kbar_t (1 + m_t) W_tj
+#pragma unroll
+        for (int u = 0; u < NW; ++u) sw = fmaf(kb[u], __shfl_sync(0xffffffffu, wv[u], jj), sw);
+        if (q != key) {  // warp-uniform
+          if (key >= 0) flush();
+          key = q;
+          rc = 0.f;
+          rcd = 0.f;
+        }
+        const float chip =
+            fmaxf(chiT[((q & 0xffff) - wbase) * KU_PAD + lane] + slT[((q >> 16) - wbase) * KU_PAD + lane] * dx, 0.f);
+        const float diff = chip - chi_wl;
+        if (diff > 0.f) {  // then the chi' clip is inactive too
+          const float ic = rcpf(fmaxf(chip, 1.f));
+          const float r = diff * ic;
+          const float h = chip > 1.f ? ic * (1.f - r) : ic;  // dr / dchi'
+          lk = fmaf(sw, r, lk);
+          cwa = fmaf(sw, fmaf(-chi_wl, ic, r), cwa);  // dr / dchi_w = -ic
+          const float ch = cjf * h * sw;
+          rc += ch;
+          rcd = fmaf(ch, dx, rcd);
+        }
+      }
+    }
+    lacc = fmaf(cjf, lk, lacc);
+    cwS[(warp * KV_NODES + (n - n0)) * KU_PAD + lane] = craw_w > 0.f ? fac * cwa : 0.f;
+  }
+  if (key >= 0) flush();
+  lS[warp * KU_PAD + lane] = lacc;
+  __syncthreads();
+  if (!live) return;
+  // warp d: the table cotangents against tangent d of the lane's chi table
+  const int d = warp;
+  const float* dc = tb->c32[1 + d];
+  const float* ds = tb->s32[1 + d];
+  float g = 0.f;
+  for (int i = 0; i < wn; ++i) {
+    const float cn = cL[i * KU_PAD + lane] + (i > 0 ? cR[(i - 1) * KU_PAD + lane] : 0.f);
+    g = fmaf(cn, dc[wbase + i], fmaf(sB[i * KU_PAD + lane], ds[wbase + i], g));
+  }
+  for (int n = n0; n < n_end; ++n) {
+    float cw = 0.f;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) cw += cwS[(w * KV_NODES + (n - n0)) * KU_PAD + lane];
+    const int qw = QWL[n];
+    g = fmaf(cw, fmaf(ds[qw >> 16], DXWL[n], dc[qw & 0xffff]), g);
+  }
+  float L = 0.f;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) L += lS[w * KU_PAD + lane];
+  // d ln cf / dtheta = d Omega_m / Omega_m
+  gb.kpart[((size_t)ci * kv_chunks(na) + chunk) * NDIR + d] =
+      (double)g + (double)L * (tb->sd[d][S_OMEGA_M] / tb->sv[S_OMEGA_M]);
+}
+
+template <int NW>
+static void launch_ku(const GradBatch& gb, cudaStream_t st, bool rev) {
+  const int wn = NCHI - gb.krev_wbase;
+  if (rev) {
+    const size_t smem = ku_rev_smem(wn);
+    cudaFuncSetAttribute(grad_kernrev32u_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid(kv_chunks(gb.na), (gb.n_items + 31) / 32);
+    grad_kernrev32u_kernel<NW><<<grid, 256, smem, st>>>(gb);
+  } else {
+    const size_t smem = ku_val_smem(wn);
+    cudaFuncSetAttribute(grad_kernval32u_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    dim3 grid((gb.na + KU_NODES - 1) / KU_NODES, (gb.n_items + 31) / 32);
+    grad_kernval32u_kernel<NW><<<grid, 256, smem, st>>>(gb);
+  }
+}
+
+static void launch_ku_nw(const GradBatch& gb, cudaStream_t st, bool rev) {
+  switch (gb.n_wl) {
+    case 1: launch_ku<1>(gb, st, rev); return;
+    case 2: launch_ku<2>(gb, st, rev); return;
+    case 3: launch_ku<3>(gb, st, rev); return;
+    case 4: launch_ku<4>(gb, st, rev); return;
+    case 5: launch_ku<5>(gb, st, rev); return;
+    case 6: launch_ku<6>(gb, st, rev); return;
+    case 7: launch_ku<7>(gb, st, rev); return;
+    default: launch_ku<8>(gb, st, rev); return;
+  }
+}
+
+void launch_kernval32u(const GradBatch& gb, cudaStream_t st) { launch_ku_nw(gb, st, false); }
+
 // the gradient from the chunks' partials (fixed order)
 __global__ void vjp_grad_reduce_kernel(GradBatch gb) {
   const int idx = blockIdx.x * blockDim.x + threadIdx.x;
@@ -545,6 +887,12 @@ static void launch_vjp_t(const GradBatch& gb, cudaStream_t st) {
 void launch_vjp32_cl(const GradBatch& gb, cudaStream_t st) {
   if (gb.physics_or != 0) launch_vjp_t<true, true>(gb, st);
   else launch_vjp_t<false, true>(gb, st);
+  launch_vjp32_cl_reduce(gb, st);
+}
+
+// C_ell from the chunks' partials (written by the forward kernel, or by the
+// product kernel when vjp_cl is set)
+void launch_vjp32_cl_reduce(const GradBatch& gb, cudaStream_t st) {
   const size_t per = (size_t)gb.n_cls * gb.n_ell;
   size_t bx = (per + 255) / 256;
   const size_t cap = (152 * 16 + gb.n_items - 1) / gb.n_items;
@@ -556,7 +904,10 @@ void launch_vjp32_cl(const GradBatch& gb, cudaStream_t st) {
 void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st) {
   if (gb.physics_or != 0) launch_vjp_t<true, false>(gb, st);
   else launch_vjp_t<false, false>(gb, st);
-  if (gb.vjp_rev) {
+  if (gb.vjp_rev && gb.krev_u) {
+    kernrev_owner_kernel<<<kv_chunks(gb.na), 256, 0, st>>>(gb.geo, gb.krev_owner);
+    launch_ku_nw(gb, st, true);
+  } else if (gb.vjp_rev) {
     dim3 grid(kv_chunks(gb.na), gb.n_items);
     if (gb.n_tr <= 3) grad_kernrev32_kernel<3><<<grid, 256, 0, st>>>(gb);
     else if (gb.n_tr <= 5) grad_kernrev32_kernel<5><<<grid, 256, 0, st>>>(gb);

@@ -355,3 +355,41 @@ def test_vjp_reverse_lensing_with_ia_groups_and_single_plane():
     err = float(((g - ref).abs() / scale).max())
     print("reverse lensing vjp err / sum|v||J|: %.2e" % err)
     assert err < 1e-4, err
+
+
+def test_vjp_uniform_reverse_lensing_lanes_over_cosmologies():
+    """A uniform fp32c batch with one lensing group and no single-plane bin
+    takes the shear integral's values and cotangents with lanes over
+    cosmologies (the chi table's segments split among the warps).  37
+    cosmologies (a partial group of 32 lanes), 3 WeakLensing bins with NLA
+    and multiplicative bias next to an inverse-growth NumberCounts bin:
+    against the FP64 Jacobian contracted with the cotangent at 1e-4 of the
+    summed terms, and one cosmology alone equal bit for bit to its row of the
+    batch."""
+    from jax_cosmo_gb300 import _geometry
+    from jax_cosmo_gb300.autodiff import jacobian_device, vjp_device
+
+    ell = _geometry.ell_host(np.geomspace(10, 3000, 19))
+    nzs = [jc.redshift.smail_nz(1.0, 2.0, z0, gals_per_arcmin2=8, zmax=5.0) for z0 in (0.4, 0.8, 1.2)]
+    probes = [jc.probes.WeakLensing(nzs, ia_bias=jc.bias.des_y1_ia_bias(1.1, 0.5, 0.62),
+                                    multiplicative_bias=[0.01, -0.01, 0.02]),
+              jc.probes.NumberCounts([nzs[1]], jc.bias.inverse_growth_linear_bias(1.4))]
+    rng = np.random.default_rng(29)
+    B = 37
+    rows = np.array([FID] * B) * (1.0 + 0.05 * rng.uniform(-1, 1, (B, 8)))
+    rows[:, 5] = 0.0
+    rows[:, 7] = 0.03 * rng.uniform(-1, 1, B)
+    params = torch.as_tensor(rows, device="cuda").contiguous()
+    _, J64 = jacobian_device(params, ell, probes, 256, "fp64")
+    vbar = torch.as_tensor(rng.standard_normal((B,) + tuple(J64.shape[1:3])), device="cuda")
+    ref = torch.einsum("bpl,bpld->bd", vbar, J64)
+    scale = torch.einsum("bpl,bpld->bd", vbar.abs(), J64.abs())
+    g, cl = vjp_device(params, ell, probes, vbar, 256, "fp32c", want_cl=True)
+    err = float(((g - ref).abs() / scale).max())
+    print("uniform reverse lensing vjp err / sum|v||J|: %.2e" % err)
+    assert err < 1e-4, err
+    k = 33
+    g1, cl1 = vjp_device(params[k:k + 1].contiguous(), ell, probes, vbar[k:k + 1].contiguous(), 256, "fp32c",
+                         want_cl=True)
+    assert torch.equal(g1[0], g[k])
+    assert torch.equal(cl1[0], cl[k])
