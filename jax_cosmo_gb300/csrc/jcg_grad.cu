@@ -33,12 +33,42 @@ typedef DualFF<NDIR> FF8;
 // lane; the sigma^2(R) tangents are FP32 sums; float copies of the chi and
 // P(k) k^3 tangent tables are written for the FP32 stages.  The sequential
 // scans (chi prefix sum, growth RK4, Romberg) stay FP64 Dual<1>.
+// chi_scan_warp (jcg_internal.cuh) for a tangent component: the RK4
+// increments in FP32 (their inputs are FP32 tangents), the prefix sums in
+// float pairs, chi_i = Y[-1] - Y_i rounded to float64 at the end.
+__device__ __forceinline__ void chi_scan_warp_ff(const double* fnode, const double* fmid, const double* lna,
+                                                 int lane, double* out) {
+  FF loc[8];
+  FF s{0.f, 0.f};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int i = lane * 8 + k;
+    if (i > 0) {
+      const float h6 = (float)((lna[i] - lna[i - 1]) * (1.0 / 6.0));
+      const float fmv = (float)fmid[i];
+      s = s + h6 * ((((float)fnode[i - 1] + 2.f * fmv) + 2.f * fmv) + (float)fnode[i]);
+    }
+    loc[k] = s;
+  }
+  FF x = s;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const FF u{__shfl_up_sync(0xffffffffu, x.hi, o), __shfl_up_sync(0xffffffffu, x.lo, o)};
+    if (lane >= o) x = u + x;
+  }
+  FF off{__shfl_up_sync(0xffffffffu, x.hi, 1), __shfl_up_sync(0xffffffffu, x.lo, 1)};
+  if (lane == 0) off = FF{0.f, 0.f};
+  const FF tot{__shfl_sync(0xffffffffu, x.hi, 31), __shfl_sync(0xffffffffu, x.lo, 31)};
+#pragma unroll
+  for (int k = 0; k < 8; ++k) out[lane * 8 + k] = ffd(tot - (off + loc[k]));
+}
+
 // NW: some item may use the transfer type "eisenhu"
 template <bool F32T, bool NW>
 __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.x;
   if (item >= gb.n_items) return;
-  extern __shared__ double sm[];
+  extern __shared__ __align__(16) double sm[];
   double* sv = sm;                      // NSCAL
   double* sd = sv + NSCAL;              // [NDIR][NSCAL]
   double* fn = sd + NDIR * NSCAL;       // [NDIR+1][NCHI] f at nodes
@@ -105,9 +135,25 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       put(fr, NROMB, e, k * (kw * kw) * pk);
     }
   } else if (gb.gnode) {
-    // node values from grad_nodes_kernel: the same layout as fn .. fr here
-    const double* src = gb.gnode + (size_t)item * GNODE_STRIDE;
-    for (int i = t; i < GNODE_U; i += blockDim.x) fn[i] = src[i];
+    // node values from grad_nodes_kernel: the same layout as fn .. fr here;
+    // 16-byte copies, eight in flight per thread
+    static_assert((9 * NSCAL) % 2 == 0 && GNODE_STRIDE % 2 == 0, "16-byte aligned node copy");
+    const double2* src = reinterpret_cast<const double2*>(gb.gnode + (size_t)item * GNODE_STRIDE);
+    double2* dst = reinterpret_cast<double2*>(fn);
+    constexpr int NV = (GNODE_U + 1) / 2;
+    for (int i0 = t; i0 < NV; i0 += 8 * blockDim.x) {
+      double2 v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = i0 + u * blockDim.x;
+        if (i < NV) v[u] = src[i];
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int i = i0 + u * blockDim.x;
+        if (i < NV) dst[i] = v[u];
+      }
+    }
   } else {
     FF8 sF[NSCAL];
     for (int i = 0; i < NSCAL; ++i) sF[i] = ff8_of(sv[i], sd + i, NSCAL);
@@ -193,9 +239,10 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       for (int k = 0; k < 4; ++k) out->gv[lane * 4 + k] = ys[k] / yf;
     } else {
       // chi for the value and the 8 tangents
-      for (int comp = warp - 1; comp < NDIR + 1; comp += 3)
-        chi_scan_warp(fn + comp * NCHI, fm + comp * NCHI, c->lna_chi, lane,
-                      comp == 0 ? out->chiv : out->chid[comp - 1]);
+      for (int comp = warp - 1; comp < NDIR + 1; comp += 3) {
+        if (comp == 0) chi_scan_warp(fn, fm, c->lna_chi, lane, out->chiv);
+        else chi_scan_warp_ff(fn + comp * NCHI, fm + comp * NCHI, c->lna_chi, lane, out->chid[comp - 1]);
+      }
       // sigmasqr(8) (power.py:70-78): romb is linear in the integrand values,
       // sum_e w_e f_e with the weights of the Richardson combination
       for (int comp = warp - 1; comp < NDIR + 1; comp += 3) {
@@ -213,6 +260,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     __syncthreads();
     // growth tangents: dy_i = M_i dy_{i-1} + dM_i y_{i-1}, dy_0 = 0, as an
     // FP32 scan of affine maps (A, b), one direction per warp and pass
+    const double iyf = 1.0 / Yv[(NGROW - 1) * 2];
     for (int d = warp; d < NDIR; d += 4) {
       float A[4] = {1.f, 0.f, 0.f, 1.f}, b[2] = {0.f, 0.f};
       float Mf[4][4], bf[4][2];
@@ -254,11 +302,10 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
         dy[k] = x0;
       }
       const float dyf = __shfl_sync(0xffffffffu, x0, 31);
-      const double yf = Yv[(NGROW - 1) * 2];
       for (int k = 0; k < 4; ++k) {
         const int i = lane * 4 + k;
-        const double D = Yv[i * 2] / yf;
-        out->gd[d][i] = ((double)dy[k] - D * (double)dyf) / yf;
+        const double D = Yv[i * 2] * iyf;
+        out->gd[d][i] = ((double)dy[k] - D * (double)dyf) * iyf;
       }
     }
   } else if (lane < NDIR) {
@@ -374,27 +421,19 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       put(pq, NKH, e, p3 / (2.0 * (PI * PI)));
     }
   } else {
-    FF8 sF[NSCAL];
-    for (int i = 0; i < NSCAL; ++i) sF[i] = ff8_of(sv[i], sd + i, NSCAL);
+    // the node values exp(n_s ln k) T(k)^2 from grad_nodes_kernel, in
+    // pk_linearT's order: ((u g^2) pknorm), then k^3
     const FF8 g1f = ff8_of(g1s[0], g1s + 1, 1);
-    const double* gu = gb.gnode ? gb.gnode + (size_t)item * GNODE_STRIDE + GNODE_U : nullptr;
+    const FF8 g1sq = g1f * g1f;
+    const FF8 pkn = ff8_of(sv[S_PKNORM], sd + S_PKNORM, NSCAL);
+    const double* gu = gb.gnode + (size_t)item * GNODE_STRIDE + GNODE_U;
     for (int e = t; e < NKH; e += blockDim.x) {
-      const double k = c->kh[e];
-      FF8 p3;
-      if (gu) {
-        // pk_linearT's order: ((exp(n_s ln k) T^2) g^2) pknorm, then k^3
-        const FF8 u = ff8_of(gu[e], gu + NKH + e, NKH);
-        p3 = ((u * (g1f * g1f)) * sF[S_PKNORM]) * c->kh3[e];
-      } else {
-        p3 = pk_linearT<NW>(sF, k, c->logk[e], g1f) * c->kh3[e];
-      }
+      const FF8 u = ff8_of(gu[e], gu + NKH + e, NKH);
+      const FF8 p3 = ((u * g1sq) * pkn) * c->kh3[e];
       out->pk3v[e] = val(p3);
-#pragma unroll
-      for (int d = 0; d < NDIR; ++d) {
-        out->pk3d[d][e] = p3.d[d];
-        out->pk3df[e][d] = p3.d[d];
-      }
-      putf(pq, NKH, e, p3 / (2.0 * (PI * PI)));
+      float4* pd = reinterpret_cast<float4*>(&out->pk3df[e][0]);
+      pd[0] = make_float4(p3.d[0], p3.d[1], p3.d[2], p3.d[3]);
+      pd[1] = make_float4(p3.d[4], p3.d[5], p3.d[6], p3.d[7]);
     }
   }
   if (F32T && t < NDIR + 1) {
@@ -444,92 +483,8 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     }
   }
   __syncthreads();
-  if (F32T && gi.ptt) {
-    // Taylor tables of the fp32c moments, scaled to the table row so that no
-    // power of k overflows.  Values: float pairs R_m[i] = c_m Q_m[i],
-    // c_m = (-1)^m / m!, Q_m[i] = sum_{k < i} w_k q3_k (kh_k / kh_i)^(2(m+1))
-    // (one lane per m); tangents (FP32, one thread per (m, d)):
-    // sum_{k < i} w_k dq3_k (kh_k / kh_i)^(2(m+1)).  Both by the contracting
-    // recurrence Q_m[i+1] = (Q_m[i] + w_i q3_i) (kh_i / kh_{i+1})^(2(m+1)),
-    // kh_i = exp(ln 1e-4 + i dlnk).
-    float2* pv = reinterpret_cast<float2*>(gi.ptt);  // [NKH + 1][NTAYLOR]
-    float* pdv = ptt_tangents(gi.ptt);
-    float* pqw = reinterpret_cast<float*>(fn);  // [NKH][NDIR] w dq3, fn is free here
-    float2* wpp = reinterpret_cast<float2*>(fm);  // [NKH] w q3 as float pairs, fm is free here
-    for (int e = t; e < NDIR * NKH; e += blockDim.x) {
-      const int d = e / NKH, i = e % NKH;
-      pqw[i * NDIR + d] = (float)(c->simpson_kh[i] * pq[(1 + d) * NKH + i]);
-    }
-    for (int i = t; i < NKH + 15; i += blockDim.x) {
-      float hi = 0.f;
-      if (i < NKH) {
-        const FF w = ff_of(c->simpson_kh[i] * pq[i]);
-        wpp[i] = make_float2(w.hi, w.lo);
-        hi = w.hi;
-      }
-      out->wq3f[i] = hi;
-    }
-    __syncthreads();
-    if (t < NTAYLOR) {
-      const int m = t;
-      FF rho, cm, q;
-      rho.hi = c->tay_rho[m][0], rho.lo = c->tay_rho[m][1];
-      cm.hi = c->tay_c[m][0], cm.lo = c->tay_c[m][1];
-      q.hi = 0.f, q.lo = 0.f;
-      pv[m] = make_float2(0.f, 0.f);
-      for (int i = 0; i < NKH; ++i) {
-        FF w;
-        w.hi = wpp[i].x, w.lo = wpp[i].y;
-        q = ff_mul(ff_add(q, w), rho);
-        const FF r = ff_mul(cm, q);
-        pv[(size_t)(i + 1) * NTAYLOR + m] = make_float2(r.hi, r.lo);
-      }
-    }
-    for (int job = t; job < NTAYLOR * NDIR; job += blockDim.x) {
-      const int m = job / NDIR, d = job % NDIR;
-      const float rho = (float)exp(-2.0 * DLOGK * (m + 1));
-      float acc = 0.f;
-      pdv[(size_t)m * NDIR + d] = 0.f;
-      for (int i = 0; i < NKH; ++i) {
-        acc = (acc + pqw[i * NDIR + d]) * rho;
-        pdv[((size_t)(i + 1) * NTAYLOR + m) * NDIR + d] = acc;
-      }
-    }
-    __syncthreads();
-  }
-  // sigma^2(R_j) without g^2 (power.py:98-111), value and tangents
+  // fp32c: the Taylor tables and sigma^2(R) follow in grad_moments32_kernel
   const double dx = (c->logk[NKH - 1] - c->logk[0]) / 256;
-  if (F32T) {
-    // value FP64, tangents FP32 (pq tangents rounded once into a float copy)
-    float* pqf = reinterpret_cast<float*>(fn);  // fn / fm are free here
-    float2* pqs = reinterpret_cast<float2*>(fm);
-    for (int e = t; e < NDIR * NKH; e += blockDim.x) {
-      const int d = e / NKH, i = e % NKH;
-      pqf[i * NDIR + d] = (float)(c->simpson_kh[i] * pq[(1 + d) * NKH + i]);
-    }
-    for (int i = t; i < NKH; i += blockDim.x) {
-      const FF f = ff_of(pq[i] * c->simpson_kh[i]);
-      pqs[i] = make_float2(f.hi, f.lo);
-    }
-    __syncthreads();
-    for (int j = t; j < NRT; j += blockDim.x) {
-      // value in float-pair arithmetic (as cosmo_tables' fp32c sums), tangents FP32
-      float ah = 0.f, al = 0.f;
-      float ad[NDIR];
-#pragma unroll
-      for (int d = 0; d < NDIR; ++d) ad[d] = 0.f;
-      for (int i = 0; i < NKH; ++i) {
-        const float2 e = c->Eff[i * NRT + j];
-        ff_acc_prod(ah, al, pqs[i], e);
-        const float* q0 = pqf + i * NDIR;
-#pragma unroll
-        for (int d = 0; d < NDIR; ++d) ad[d] = fmaf(q0[d], e.x, ad[d]);
-      }
-      out->sigv[j] = (double)ah + (double)al;
-#pragma unroll
-      for (int d = 0; d < NDIR; ++d) out->sigd[d][j] = (double)ad[d];
-    }
-  }
   for (int e = F32T ? (NDIR + 1) * NRT : t; e < (NDIR + 1) * NRT; e += blockDim.x) {
     const int comp = e / NRT, j = e % NRT;
     const double* w = pq + comp * NKH;
@@ -552,11 +507,103 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     for (int e = t; e < (NDIR + 1) * NCHI; e += blockDim.x) {
       const int comp = e / NCHI, i = e % NCHI;
       const double* ch = comp == 0 ? out->chiv : out->chid[comp - 1];
-      double sl = 0.0;
-      if (i + 1 < NCHI) sl = (ch[i + 1] - ch[i]) / (c->atab_chi[i + 1] - c->atab_chi[i]);
+      const double sl = i + 1 < NCHI ? (ch[i + 1] - ch[i]) * c->chi_ida[i] : 0.0;
       out->c32[comp][i] = (float)ch[i];
       out->s32[comp][i] = (float)sl;
     }
+  }
+}
+
+// fp32c: the tables of the moments that grad_rows32_kernel reads, from the
+// P(k) k^3 table grad_tables_kernel wrote (pk3v, pk3df), one CTA of NRT
+// threads per cosmology, at full occupancy (the serial recurrences of one
+// cosmology overlap with other cosmologies' work):
+//   Taylor tables, scaled to the table row so that no power of k overflows.
+//   Values: float pairs R_m[i] = c_m Q_m[i], c_m = (-1)^m / m!,
+//   Q_m[i] = sum_{k < i} w_k q3_k (kh_k / kh_i)^(2(m+1)) (one lane per m);
+//   tangents (FP32, one thread per (m, d)): sum_{k < i} w_k dq3_k
+//   (kh_k / kh_i)^(2(m+1)).  Both by the contracting recurrence
+//   Q_m[i+1] = (Q_m[i] + w_i q3_i) (kh_i / kh_{i+1})^(2(m+1)),
+//   kh_i = exp(ln 1e-4 + i dlnk);
+//   sigma^2(R_j) without g^2 (power.py:98-111): value in float-pair
+//   arithmetic (as cosmo_tables' fp32c sums), tangents FP32, one thread per j.
+// q3 = P(k) k^3 / (2 pi^2), w the Simpson weights.
+static_assert(NRT == 256, "one thread per sigma^2(R) node");
+__global__ void __launch_bounds__(NRT) grad_moments32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+  const int item = blockIdx.x;
+  if (item >= gb.n_items) return;
+  const GradItem gi = grad_item(gb, item);
+  TabD* out = gi.tab;
+  __shared__ __align__(16) float2 wq[NKH];          // w q3 as float pairs
+  __shared__ __align__(16) float wqd[NKH][NDIR];    // w dq3 (rows read as float4)
+  const int t = threadIdx.x;
+  constexpr double INV2PI2 = 1.0 / (2.0 * (PI * PI));
+  for (int i = t; i < NKH + 15; i += blockDim.x) {
+    float hi = 0.f;
+    if (i < NKH) {
+      const double sw = c->simpson_kh[i] * INV2PI2;
+      const FF w = ff_of(sw * out->pk3v[i]);
+      wq[i] = make_float2(w.hi, w.lo);
+      hi = w.hi;
+      const float swf = (float)sw;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) wqd[i][d] = swf * out->pk3df[i][d];
+    }
+    out->wq3f[i] = hi;
+  }
+  __syncthreads();
+  if (gi.ptt) {
+    float2* pv = reinterpret_cast<float2*>(gi.ptt);  // [NKH + 1][NTAYLOR]
+    float* pdv = ptt_tangents(gi.ptt);
+    if (t < NTAYLOR) {
+      const int m = t;
+      FF rho, cm, q;
+      rho.hi = c->tay_rho[m][0], rho.lo = c->tay_rho[m][1];
+      cm.hi = c->tay_c[m][0], cm.lo = c->tay_c[m][1];
+      q.hi = 0.f, q.lo = 0.f;
+      pv[m] = make_float2(0.f, 0.f);
+      for (int i = 0; i < NKH; ++i) {
+        FF w;
+        w.hi = wq[i].x, w.lo = wq[i].y;
+        q = ff_mul(ff_add(q, w), rho);
+        const FF r = ff_mul(cm, q);
+        pv[(size_t)(i + 1) * NTAYLOR + m] = make_float2(r.hi, r.lo);
+      }
+    } else if (t >= 32 && t < 32 + NTAYLOR * NDIR) {
+      const int job = t - 32, m = job / NDIR, d = job % NDIR;
+      const float rho = c->tay_rho[m][0];
+      float acc = 0.f;
+      pdv[(size_t)m * NDIR + d] = 0.f;
+      for (int i = 0; i < NKH; ++i) {
+        acc = (acc + wqd[i][d]) * rho;
+        pdv[((size_t)(i + 1) * NTAYLOR + m) * NDIR + d] = acc;
+      }
+    }
+  }
+  {
+    const int j = t;
+    float ah = 0.f, al = 0.f;
+    float ad[NDIR];
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) ad[d] = 0.f;
+#pragma unroll 4
+    for (int i = 0; i < NKH; ++i) {
+      const float2 e = c->Eff[i * NRT + j];
+      ff_acc_prod(ah, al, wq[i], e);
+      const float4 q0 = *reinterpret_cast<const float4*>(&wqd[i][0]);
+      const float4 q1 = *reinterpret_cast<const float4*>(&wqd[i][4]);
+      ad[0] = fmaf(q0.x, e.x, ad[0]);
+      ad[1] = fmaf(q0.y, e.x, ad[1]);
+      ad[2] = fmaf(q0.z, e.x, ad[2]);
+      ad[3] = fmaf(q0.w, e.x, ad[3]);
+      ad[4] = fmaf(q1.x, e.x, ad[4]);
+      ad[5] = fmaf(q1.y, e.x, ad[5]);
+      ad[6] = fmaf(q1.z, e.x, ad[6]);
+      ad[7] = fmaf(q1.w, e.x, ad[7]);
+    }
+    out->sigv[j] = (double)ah + (double)al;
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) out->sigd[d][j] = (double)ad[d];
   }
 }
 
@@ -804,7 +851,7 @@ __device__ __forceinline__ FF8 interp_ff8(double x, const double* xp, const doub
 
 constexpr int GR32_THREADS = 64;
 
-__global__ void __launch_bounds__(GR32_THREADS) grad_rows32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+__global__ void __launch_bounds__(GR32_THREADS, 8) grad_rows32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
   const GradItem gi = grad_item(gb, item);
@@ -1745,6 +1792,7 @@ void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t s
     cudaFuncSetAttribute(grad_tables_kernel<false, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
     grad_tables_kernel<false, true><<<gb.n_items, 256, smt, st>>>(gb, c);
   }
+  if (gb.precision == JCG_FP32C) grad_moments32_kernel<<<gb.n_items, NRT, 0, st>>>(gb, c);
   if (growth_gamma(gb.physics_or)) grad_growth_gamma_kernel<<<gb.n_items, 32 * NDIR, 0, st>>>(gb, c);
   if (gb.precision == JCG_FP32C) {
     dim3 grw((gb.na + GR32_THREADS - 1) / GR32_THREADS, gb.n_items);

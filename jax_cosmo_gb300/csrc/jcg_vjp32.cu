@@ -60,8 +60,8 @@ __host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT) {
   o += 4 * (size_t)VJ_TA * n_tr * (NDIR + 1);
   L.mv = o;                                   // [VJ_TA][n_cls]
   o += 4 * (size_t)VJ_TA * n_cls;
-  L.vs = o;                                   // [n_cls][LT]
-  o += 4 * (size_t)n_cls * LT;
+  L.vs = o;                                   // [n_cls][LT + 1] (odd stride: no bank conflicts across p)
+  o += 4 * (size_t)n_cls * (LT + 1);
   L.pt = o;                                   // [VJ_TA][LT]
   o += 4 * (size_t)VJ_TA * LT;
   L.abar = o;                                 // [VJ_TA][NGT]
@@ -162,7 +162,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
         const int p = q / lt, l = q - p * lt;
         const int ell = l0 + l;
         const float ef = EF32[(size_t)geo->pair_i[p] * n_ell + ell] * EF32[(size_t)geo->pair_j[p] * n_ell + ell];
-        vS[p * LT + l] = (float)gi.vbar[(size_t)p * n_ell + ell] * ef;
+        vS[p * (LT + 1) + l] = (float)gi.vbar[(size_t)p * n_ell + ell] * ef;
       }
     __syncthreads();
     if (grp < tc) {
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
         Pt[t * LT + l] = P;
         if (!FWD) {
           float W = 0.f;
-          for (int p = 0; p < n_cls; ++p) W = fmaf(vS[p * LT + l], mrow[p], W);
+          for (int p = 0; p < n_cls; ++p) W = fmaf(vS[p * (LT + 1) + l], mrow[p], W);
 #pragma unroll
           for (int j = 0; j < T_U; ++j) {
             if (!GEN && j == T_MUN) continue;  // mu_n = 0 for takahashi2012
@@ -204,7 +204,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
       // added in float-pair arithmetic
       for (int q = tid; q < tc * n_cls; q += VJ_THREADS) {
         const int t = q / n_cls, p = q - t * n_cls;
-        const float* vp = vS + (size_t)p * LT;
+        const float* vp = vS + (size_t)p * (LT + 1);
         const float* pp = Pt + (size_t)t * LT;
         FF s{Qd[q].x, Qd[q].y};
         for (int b = 0; b < lt; b += 32) {
@@ -311,8 +311,17 @@ __global__ void vjp_cl_reduce_kernel(GradBatch gb) {
   const size_t per = (size_t)n_cls * n_ell;
   for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < per; idx += (size_t)gridDim.x * blockDim.x) {
     const int p = (int)(idx / n_ell), l = (int)(idx % n_ell);
+    // chunks added in order; loads issued eight at a time
     double s = 0.0;
-    for (int c = 0; c < nch; ++c) s += (double)gi.cpart[(size_t)c * per + idx];
+    int c = 0;
+    for (; c + 8 <= nch; c += 8) {
+      float v[8];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = gi.cpart[(size_t)(c + k) * per + idx];
+#pragma unroll
+      for (int k = 0; k < 8; ++k) s += (double)v[k];
+    }
+    for (; c < nch; ++c) s += (double)gi.cpart[(size_t)c * per + idx];
     gi.cl[idx] = s * EF[(size_t)geo->pair_i[p] * n_ell + l] * EF[(size_t)geo->pair_j[p] * n_ell + l];
   }
 }
@@ -530,7 +539,7 @@ constexpr int KU_NODES = 32;  // nodes per CTA of the value kernel
 
 __host__ __device__ inline size_t ku_val_smem(int wn) { return sizeof(float) * 2 * (size_t)wn * KU_PAD; }
 __host__ __device__ inline size_t ku_rev_smem(int wn) {
-  return sizeof(float) * ((size_t)5 * wn * KU_PAD + (size_t)8 * KV_NODES * KU_PAD + 8 * KU_PAD);
+  return sizeof(float) * ((size_t)4 * wn * KU_PAD + (size_t)8 * KV_NODES * KU_PAD + 16 * KU_PAD);
 }
 
 bool krev_uniform_ok(const GeoHeader& h) {
@@ -670,9 +679,11 @@ __global__ void __launch_bounds__(256) kernrev_owner_kernel(const GeoHeader* geo
 // Reverse form of the shear integral (the same sums as grad_kernrev32_kernel,
 // whose header derives them), lanes over 32 cosmologies.  The warps share a
 // chunk of KV_NODES nodes and split its lensing points by segment
-// (kernrev_owner_kernel), so the segment-indexed cotangents
-//   cL[m] (chi at node m), cR[m] (chi at node m + 1), sB[m] (slope of m)
-// of a lane are written by one warp only, in a fixed order.  The segment of
+// (kernrev_owner_kernel), so the cotangents of a lane's chi table nodes
+// cN[x] and segment slopes sB[m] are written by one warp only, in a fixed
+// order: warp w owns the slopes of [b_w, b_{w+1}) and the nodes
+// [b_w, b_{w+1} - 1]; what its top segment gives node b_{w+1} it keeps in a
+// register (bS in shared memory at the end).    The segment of
 // consecutive points changes every few points: the current run's sums stay
 // in registers and go to shared memory when it changes.  The chi_w
 // cotangents (one per node and warp) and the sums for d ln cf wait in shared
@@ -690,11 +701,11 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
   extern __shared__ float kr_smem[];
   float* chiT = kr_smem;                        // [wn][KU_PAD]
   float* slT = chiT + wn * KU_PAD;              // [wn][KU_PAD]
-  float* cL = slT + wn * KU_PAD;                // [wn][KU_PAD]
-  float* cR = cL + wn * KU_PAD;                 // [wn][KU_PAD]
-  float* sB = cR + wn * KU_PAD;                 // [wn][KU_PAD]
+  float* cN = slT + wn * KU_PAD;                // [wn][KU_PAD]
+  float* sB = cN + wn * KU_PAD;                 // [wn][KU_PAD]
   float* cwS = sB + wn * KU_PAD;                // [8][KV_NODES][KU_PAD]
   float* lS = cwS + 8 * KV_NODES * KU_PAD;      // [8][KU_PAD]
+  float* bS = lS + 8 * KU_PAD;                  // [8][KU_PAD]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int idx = tid; idx < 32 * wn; idx += blockDim.x) {
     const int cc = idx / wn, i = idx % wn;
@@ -706,8 +717,7 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
     }
     chiT[i * KU_PAD + cc] = cv;
     slT[i * KU_PAD + cc] = sv;
-    cL[i * KU_PAD + cc] = 0.f;
-    cR[i * KU_PAD + cc] = 0.f;
+    cN[i * KU_PAD + cc] = 0.f;
     sB[i * KU_PAD + cc] = 0.f;
   }
   for (int idx = tid; idx < 8 * KV_NODES * KU_PAD; idx += blockDim.x) cwS[idx] = 0.f;
@@ -738,10 +748,12 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
   int key = -1;           // the current run's segment query (nearest | segment << 16)
   float rc = 0.f, rcd = 0.f;  // the run's chi' cotangent, and times dx
   float lacc = 0.f;       // sum_n fac chi_w sum_j sw r  (the d ln cf sum)
+  float bacc = 0.f;       // node bhi's cotangent from segment bhi - 1
   auto flush = [&]() {
     const int m = key >> 16, i = (m - wbase) * KU_PAD + lane;
-    if ((key & 0xffff) == m) cL[i] += rc;
-    else cR[i] += rc;
+    if ((key & 0xffff) == m) cN[i] += rc;
+    else if (m + 1 < bhi) cN[i + KU_PAD] += rc;
+    else bacc += rc;
     sB[i] += rcd;
   };
   for (int n = n0; n < n_end; ++n) {
@@ -801,6 +813,7 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
   }
   if (key >= 0) flush();
   lS[warp * KU_PAD + lane] = lacc;
+  bS[warp * KU_PAD + lane] = bacc;
   __syncthreads();
   if (!live) return;
   // warp d: the table cotangents against tangent d of the lane's chi table
@@ -808,9 +821,11 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
   const float* dc = tb->c32[1 + d];
   const float* ds = tb->s32[1 + d];
   float g = 0.f;
-  for (int i = 0; i < wn; ++i) {
-    const float cn = cL[i * KU_PAD + lane] + (i > 0 ? cR[(i - 1) * KU_PAD + lane] : 0.f);
-    g = fmaf(cn, dc[wbase + i], fmaf(sB[i * KU_PAD + lane], ds[wbase + i], g));
+  for (int i = 0; i < wn; ++i) g = fmaf(cN[i * KU_PAD + lane], dc[wbase + i], fmaf(sB[i * KU_PAD + lane], ds[wbase + i], g));
+#pragma unroll
+  for (int w = 0; w < 7; ++w) {
+    const int x = gb.krev_owner[chunk * 9 + w + 1];
+    if (x < NCHI) g = fmaf(bS[w * KU_PAD + lane], dc[x], g);
   }
   for (int n = n0; n < n_end; ++n) {
     float cw = 0.f;
