@@ -1948,6 +1948,7 @@ size_t vjp_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
   o += al256(sizeof(float) * (size_t)h.n_tr * h.na * n_cosmo);
   o += al256(sizeof(double) * (size_t)kv_chunks(h.na) * NDIR * n_cosmo);
   o += al256(sizeof(int) * 9 * (size_t)kv_chunks(h.na));
+  o += al256(sizeof(unsigned) * (size_t)n_cosmo);
   o += gnode_bytes(n_cosmo, precision);
   return o;
 }
@@ -1993,6 +1994,8 @@ void vjp_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int
   o += al256(sizeof(double) * (size_t)kv_chunks(h.na) * NDIR * n_cosmo);
   gb.krev_owner = reinterpret_cast<int*>(base + o);
   o += al256(sizeof(int) * 9 * (size_t)kv_chunks(h.na));
+  gb.cl_count = reinterpret_cast<unsigned*>(base + o);
+  o += al256(sizeof(unsigned) * (size_t)n_cosmo);
   gb.gnode = gnode_bytes(n_cosmo, precision) ? reinterpret_cast<double*>(base + o) : nullptr;
   gb.vjp_rev = (vbar && grad) ? 1 : 0;
   gb.krev_u = gb.vjp_rev && krev_uniform_ok(h);
@@ -2013,7 +2016,6 @@ void vjp_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int
     // the caller's cotangent: one pass gives the partial C_ell and the product
     gb.vjp_cl = 1;
     launch_vjp32_grad(gb, st);
-    launch_vjp32_cl_reduce(gb, st);
     return;
   }
   if (cl) launch_vjp32_cl(gb, st);
@@ -2114,7 +2116,7 @@ size_t grad_listed_bytes(const GradReq* r, int n, int n_split, int precision, bo
   size_t o = al256(sizeof(GradItem) * (size_t)n);
   for (int i = 0; i < n; ++i)
     o += vjp ? vjp_item_bytes(*r[i].h, !r[i].cl) : grad_item_bytes(*r[i].h, n_split, !r[i].cl, !r[i].jac, precision);
-  return o + gnode_bytes(n, precision);
+  return o + gnode_bytes(n, precision) + (vjp ? al256(sizeof(unsigned) * (size_t)n) : 0);
 }
 
 cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void* ws, const ConstTables* c,
@@ -2193,6 +2195,8 @@ cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void*
   gb.n_split = vjp ? 1 : n_split;
   gb.vjp_rev = vjp ? 1 : 0;
   gb.gnode = gnode_bytes(n, precision) ? reinterpret_cast<double*>(base + o) : nullptr;
+  o += gnode_bytes(n, precision);
+  if (vjp) gb.cl_count = reinterpret_cast<unsigned*>(base + o);
   if (vjp) {
     launch_grad_front(gb, c, st);
     launch_vjp32_cl(gb, st);

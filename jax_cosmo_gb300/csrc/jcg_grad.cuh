@@ -196,6 +196,9 @@ struct GradBatch {
   // 1: the cotangent does not depend on C_ell (given by the caller), so the
   // product kernel also writes the chunks' partial C_ell (no forward pass)
   int vjp_cl;
+  // per item: chunk CTAs done with their partial C_ell (the last one adds
+  // them up and resets the count)
+  unsigned* cl_count;
 };
 
 // fp32c batches spread the table kernel's per-node evaluations over
@@ -275,7 +278,6 @@ void launch_grad_limber32(const GradBatch& gb, const ConstTables* c, cudaStream_
 // vector-Jacobian product (jcg_vjp32.cu): C_ell of the items into their cl,
 // and the product with their cotangents vbar into their grad
 void launch_vjp32_cl(const GradBatch& gb, cudaStream_t st);
-void launch_vjp32_cl_reduce(const GradBatch& gb, cudaStream_t st);
 void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st);
 // uniform reverse lensing: the shear kernels' values (lanes over cosmologies)
 void launch_kernval32u(const GradBatch& gb, cudaStream_t st);

@@ -42,8 +42,13 @@ int vjp_ltile(int n_cls, int n_ell) {
   return lt < need ? lt : need;
 }
 
+// row stride of the [.][LT] tiles: >= LT, a multiple of 4 (float4 rows) and
+// 8 mod 32, so that 8 consecutive columns of 4 consecutive rows fall in 32
+// distinct banks
+__host__ __device__ inline int vj_stride(int LT) { return LT + (40 - LT % 32) % 32; }
+
 struct VjLayout {
-  size_t ev, kh, rows, ks, mv, vs, pt, abar, qd, red, total;
+  size_t ev, kh, rows, ks, mv, mt, vs, pt, ws, abar, qd, red, total;
 };
 __host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT) {
   VjLayout L;
@@ -60,10 +65,15 @@ __host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT) {
   o += 4 * (size_t)VJ_TA * n_tr * (NDIR + 1);
   L.mv = o;                                   // [VJ_TA][n_cls]
   o += 4 * (size_t)VJ_TA * n_cls;
-  L.vs = o;                                   // [n_cls][LT + 1] (odd stride: no bank conflicts across p)
-  o += 4 * (size_t)n_cls * (LT + 1);
-  L.pt = o;                                   // [VJ_TA][LT]
-  o += 4 * (size_t)VJ_TA * LT;
+  o = (o + 15) & ~(size_t)15;
+  L.mt = o;                                   // [n_cls][VJ_TA] (M transposed)
+  o += 4 * (size_t)VJ_TA * n_cls;
+  L.vs = o;                                   // [n_cls][vj_stride(LT)]
+  o += 4 * (size_t)n_cls * vj_stride(LT);
+  L.pt = o;                                   // [VJ_TA][vj_stride(LT)] P(t, l)
+  o += 4 * (size_t)VJ_TA * vj_stride(LT);
+  L.ws = o;                                   // [VJ_TA][vj_stride(LT)] W(t, l)
+  o += 4 * (size_t)VJ_TA * vj_stride(LT);
   L.abar = o;                                 // [VJ_TA][NGT]
   o += 4 * (size_t)VJ_TA * NGT;
   o = (o + 15) & ~(size_t)15;
@@ -101,8 +111,11 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   float* R = reinterpret_cast<float*>(vj_smem + L.rows);
   float* Ks = reinterpret_cast<float*>(vj_smem + L.ks);
   float* Mv = reinterpret_cast<float*>(vj_smem + L.mv);
+  float* MT = reinterpret_cast<float*>(vj_smem + L.mt);
   float* vS = reinterpret_cast<float*>(vj_smem + L.vs);
   float* Pt = reinterpret_cast<float*>(vj_smem + L.pt);
+  float* Ws = reinterpret_cast<float*>(vj_smem + L.ws);
+  const int TS = vj_stride(LT);
   float* Abar = reinterpret_cast<float*>(vj_smem + L.abar);
   float2* Qd = reinterpret_cast<float2*>(vj_smem + L.qd);  // Q_p(t) as (hi, lo)
   float* Ered = reinterpret_cast<float*>(vj_smem + L.red);
@@ -134,7 +147,9 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
     const int t = i / n_cls, p = i - t * n_cls;
     const float* Ki = Ks + ((size_t)t * n_tr + geo->pair_i[p]) * (NDIR + 1);
     const float* Kj = Ks + ((size_t)t * n_tr + geo->pair_j[p]) * (NDIR + 1);
-    Mv[i] = R[(size_t)t * NROWG + F_U] * (Ki[0] * Kj[0]);
+    const float m = R[(size_t)t * NROWG + F_U] * (Ki[0] * Kj[0]);
+    Mv[i] = m;
+    MT[p * VJ_TA + t] = m;
   }
   EHg eh;
   eh.qinv = ev[0]; eh.lg2_qinv = ev[1]; eh.sh = ev[2]; eh.inv_sh = ev[3]; eh.c18bc = ev[4];
@@ -162,22 +177,46 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
         const int p = q / lt, l = q - p * lt;
         const int ell = l0 + l;
         const float ef = EF32[(size_t)geo->pair_i[p] * n_ell + ell] * EF32[(size_t)geo->pair_j[p] * n_ell + ell];
-        vS[p * (LT + 1) + l] = (float)gi.vbar[(size_t)p * n_ell + ell] * ef;
+        vS[p * TS + l] = (float)gi.vbar[(size_t)p * n_ell + ell] * ef;
       }
     __syncthreads();
+    const int L4 = (lt + 3) >> 2;
+    if (!FWD) {
+      // W(t, l) = sum_p M_p(t) v_p(l) in 4 x 4 blocks (rows past tc and
+      // columns past lt are not read)
+      for (int w = tid; w < (VJ_TA / 4) * L4; w += VJ_THREADS) {
+        const int tb = w / L4, lq = (w - tb * L4) * 4, t0 = tb * 4;
+        float4 a[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) a[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        for (int p = 0; p < n_cls; ++p) {
+          const float4 m = *reinterpret_cast<const float4*>(MT + p * VJ_TA + t0);
+          const float4 v = *reinterpret_cast<const float4*>(vS + p * TS + lq);
+          const float mm[4] = {m.x, m.y, m.z, m.w};
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            a[i].x = fmaf(mm[i], v.x, a[i].x);
+            a[i].y = fmaf(mm[i], v.y, a[i].y);
+            a[i].z = fmaf(mm[i], v.z, a[i].z);
+            a[i].w = fmaf(mm[i], v.w, a[i].w);
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i) *reinterpret_cast<float4*>(Ws + (t0 + i) * TS + lq) = a[i];
+      }
+      __syncthreads();
+    }
     if (grp < tc) {
       const int t = grp;
       const float* row = R + (size_t)t * NROWG;
-      const float* mrow = Mv + (size_t)t * n_cls;
       for (int l = sub; l < lt; l += VJ_GROUP) {
         float an[NGT], ae[NET];
         const float P = !GEN ? node32_fb_default(eh, row, khv[l], lkhv[l], ikhv[l], an, ae)
                         : nw ? node32_fb_nw(eh, row, khv[l], lkhv[l], ikhv[l], an, ae, lin)
                              : node32_fb<true>(eh, row, khv[l], lkhv[l], ikhv[l], an, ae, lin);
-        Pt[t * LT + l] = P;
+        Pt[t * TS + l] = P;
         if (!FWD) {
-          float W = 0.f;
-          for (int p = 0; p < n_cls; ++p) W = fmaf(vS[p * (LT + 1) + l], mrow[p], W);
+          const float W = Ws[t * TS + l];
 #pragma unroll
           for (int j = 0; j < T_U; ++j) {
             if (!GEN && j == T_MUN) continue;  // mu_n = 0 for takahashi2012
@@ -190,32 +229,103 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
     }
     __syncthreads();
     if (FWD || gb.vjp_cl) {
-      // partial C_p(l) of the chunk: sum_t M_p(t) P(t, l)
+      // partial C_p(l) of the chunk: sum_t M_p(t) P(t, l), t in order, in
+      // blocks of 2 spectra x 4 ell
       float* cp = gi.cpart + (size_t)chunk * n_cls * n_ell;
-      for (int q = tid; q < n_cls * lt; q += VJ_THREADS) {
-        const int p = q / lt, l = q - p * lt;
-        float s = 0.f;
-        for (int t = 0; t < tc; ++t) s = fmaf(Pt[t * LT + l], Mv[t * n_cls + p], s);
-        cp[(size_t)p * n_ell + l0 + l] = s;
+      const int P2 = (n_cls + 1) >> 1;
+      for (int w = tid; w < P2 * L4; w += VJ_THREADS) {
+        const int pb = w / L4, lq = (w - pb * L4) * 4, p0 = pb * 2;
+        const bool two = p0 + 1 < n_cls;
+        float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = c0;
+        for (int t = 0; t < tc; ++t) {
+          const float4 pt = *reinterpret_cast<const float4*>(Pt + t * TS + lq);
+          const float m0 = Mv[t * n_cls + p0], m1 = two ? Mv[t * n_cls + p0 + 1] : 0.f;
+          c0.x = fmaf(pt.x, m0, c0.x), c0.y = fmaf(pt.y, m0, c0.y), c0.z = fmaf(pt.z, m0, c0.z), c0.w = fmaf(pt.w, m0, c0.w);
+          c1.x = fmaf(pt.x, m1, c1.x), c1.y = fmaf(pt.y, m1, c1.y), c1.z = fmaf(pt.z, m1, c1.z), c1.w = fmaf(pt.w, m1, c1.w);
+        }
+        const float r0[4] = {c0.x, c0.y, c0.z, c0.w}, r1[4] = {c1.x, c1.y, c1.z, c1.w};
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          if (lq + k >= lt) break;
+          cp[(size_t)p0 * n_ell + l0 + lq + k] = r0[k];
+          if (two) cp[(size_t)(p0 + 1) * n_ell + l0 + lq + k] = r1[k];
+        }
       }
     }
     if (!FWD) {
-      // Q_p(t) += sum_l v_p(l) P(t, l): float sums of at most 32 terms,
-      // added in float-pair arithmetic
-      for (int q = tid; q < tc * n_cls; q += VJ_THREADS) {
-        const int t = q / n_cls, p = q - t * n_cls;
-        const float* vp = vS + (size_t)p * (LT + 1);
-        const float* pp = Pt + (size_t)t * LT;
-        FF s{Qd[q].x, Qd[q].y};
-        for (int b = 0; b < lt; b += 32) {
-          float f = 0.f;
-          const int e = min(lt, b + 32);
-          for (int l = b; l < e; ++l) f = fmaf(vp[l], pp[l], f);
-          s = s + f;
+      // Q_p(t) += sum_l v_p(l) P(t, l): blocks of 4 a nodes x 4 spectra
+      // (p = 16 g + b + 4 k), each summed over 8 ell slices in FP32 and the
+      // slices added by shuffles, then added to Q in float-pair arithmetic
+      const int NPG = (n_cls + 15) >> 4;
+      for (int w = tid; w < (VJ_THREADS) * NPG; w += VJ_THREADS) {
+        const int pg = w / VJ_THREADS, r = w - pg * VJ_THREADS;
+        const int slice = r & 7, blk = r >> 3, t0 = (blk >> 2) * 4, pb = blk & 3;
+        int pk[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k) pk[k] = pg * 16 + pb + 4 * k;
+        float acc[4][4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int k = 0; k < 4; ++k) acc[i][k] = 0.f;
+        for (int l = slice; l < lt; l += 8) {
+          float pt[4], v[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) pt[i] = Pt[(t0 + i) * TS + l];
+#pragma unroll
+          for (int k = 0; k < 4; ++k) v[k] = pk[k] < n_cls ? vS[pk[k] * TS + l] : 0.f;
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) acc[i][k] = fmaf(pt[i], v[k], acc[i][k]);
         }
-        Qd[q] = make_float2(s.hi, s.lo);
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            float x = acc[i][k];
+            x += __shfl_xor_sync(0xffffffffu, x, 4);
+            x += __shfl_xor_sync(0xffffffffu, x, 2);
+            x += __shfl_xor_sync(0xffffffffu, x, 1);
+            acc[i][k] = x;
+          }
+        if (slice == 0) {
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const int t = t0 + i, p = pk[k];
+              if (t < tc && p < n_cls) {
+                const int q = t * n_cls + p;
+                const FF sq = FF{Qd[q].x, Qd[q].y} + acc[i][k];
+                Qd[q] = make_float2(sq.hi, sq.lo);
+              }
+            }
+        }
       }
     }
+  }
+  if (FWD || gb.vjp_cl) {
+    // C_ell of the item once all its chunks are in: the last chunk CTA to
+    // finish adds the partials in chunk order (the same sum whichever CTA
+    // it is), times the ell factors, and resets the count
+    __shared__ int s_last;
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) s_last = atomicAdd(&gb.cl_count[item], 1u) == (unsigned)(nch - 1);
+    __syncthreads();
+    if (s_last && gi.cl) {
+      __threadfence();
+      const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
+      const size_t per = (size_t)n_cls * n_ell;
+      for (int idx = tid; idx < (int)per; idx += VJ_THREADS) {
+        const int p = idx / n_ell, l = idx - p * n_ell;
+        double s = 0.0;
+        for (int c = 0; c < nch; ++c) s += (double)__ldcg(gi.cpart + (size_t)c * per + idx);
+        gi.cl[idx] = s * EF[(size_t)geo->pair_i[p] * n_ell + l] * EF[(size_t)geo->pair_j[p] * n_ell + l];
+      }
+    }
+    if (s_last && tid == 0) gb.cl_count[item] = 0;
   }
   if (FWD) return;
   // adjoints of the node inputs: summed over the a node's 8 lanes; those of
@@ -296,33 +406,6 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
     double g = 0.0;
     for (int t = 0; t < VJ_TA; ++t) g += gred[t * NDIR + tid];
     gi.gpart[(size_t)chunk * NDIR + tid] = g;
-  }
-}
-
-// C_ell from the chunks' partials (fixed order), times the ell factors
-__global__ void vjp_cl_reduce_kernel(GradBatch gb) {
-  const int item = blockIdx.y;
-  if (item >= gb.n_items) return;
-  const GradItem gi = grad_item(gb, item);
-  if (!gi.cl) return;
-  const GeoHeader* geo = gi.geo;
-  const int n_ell = geo->n_ell, n_cls = geo->n_cls, nch = vjp_chunks(geo->na);
-  const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
-  const size_t per = (size_t)n_cls * n_ell;
-  for (size_t idx = (size_t)blockIdx.x * blockDim.x + threadIdx.x; idx < per; idx += (size_t)gridDim.x * blockDim.x) {
-    const int p = (int)(idx / n_ell), l = (int)(idx % n_ell);
-    // chunks added in order; loads issued eight at a time
-    double s = 0.0;
-    int c = 0;
-    for (; c + 8 <= nch; c += 8) {
-      float v[8];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) v[k] = gi.cpart[(size_t)(c + k) * per + idx];
-#pragma unroll
-      for (int k = 0; k < 8; ++k) s += (double)v[k];
-    }
-    for (; c < nch; ++c) s += (double)gi.cpart[(size_t)c * per + idx];
-    gi.cl[idx] = s * EF[(size_t)geo->pair_i[p] * n_ell + l] * EF[(size_t)geo->pair_j[p] * n_ell + l];
   }
 }
 
@@ -745,16 +828,19 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
 #pragma unroll
   for (int u = 0; u < NW; ++u) Wb[u] = geo_ptr<float>(geo, geo->off_W32[wl_t[u]]);
   const int blo = gb.krev_owner[chunk * 9 + warp], bhi = gb.krev_owner[chunk * 9 + warp + 1];
-  int key = -1;           // the current run's segment query (nearest | segment << 16)
-  float rc = 0.f, rcd = 0.f;  // the run's chi' cotangent, and times dx
+  float rc = 0.f, rcd = 0.f;  // the current run's chi' cotangent, and times dx
   float lacc = 0.f;       // sum_n fac chi_w sum_j sw r  (the d ln cf sum)
   float bacc = 0.f;       // node bhi's cotangent from segment bhi - 1
-  auto flush = [&]() {
-    const int m = key >> 16, i = (m - wbase) * KU_PAD + lane;
-    if ((key & 0xffff) == m) cN[i] += rc;
+  // a run (consecutive points of one segment query, nearest | segment << 16)
+  // ends: its sums go to the table cotangents
+  auto flush = [&](int q) {
+    const int m = q >> 16, i = (m - wbase) * KU_PAD + lane;
+    if ((q & 0xffff) == m) cN[i] += rc;
     else if (m + 1 < bhi) cN[i + KU_PAD] += rc;
     else bacc += rc;
     sB[i] += rcd;
+    rc = 0.f;
+    rcd = 0.f;
   };
   for (int n = n0; n < n_end; ++n) {
     const int qw = QWL[n];
@@ -772,27 +858,24 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
       const int jl = j0 + lane;
       const int qv = jl < NZP ? Q32b[row + jl] : -1;
       const int mv = qv >> 16;  // -1 past the row's end
-      unsigned mask = __ballot_sync(0xffffffffu, mv >= blo && mv < bhi);
+      const unsigned mask = __ballot_sync(0xffffffffu, mv >= blo && mv < bhi);
       if (!mask) continue;
+      // the segment falls along the row: a warp's points of a chunk are consecutive
+      const int jf = __ffs(mask) - 1, cnt = __popc(mask);
       const bool own = (mask >> lane) & 1u;
       const float dxv = own ? DX32b[row + jl] : 0.f;
       float wv[NW];
 #pragma unroll
       for (int u = 0; u < NW; ++u) wv[u] = own ? Wb[u][row + jl] : 0.f;
-      while (mask) {
-        const int jj = __ffs(mask) - 1;
-        mask &= mask - 1;
+      const int qn = __shfl_down_sync(0xffffffffu, qv, 1);
+      const unsigned ends = __ballot_sync(0xffffffffu, own && (lane == jf + cnt - 1 || qn != qv));
+      for (int k = 0; k < cnt; ++k) {
+        const int jj = jf + k;
         const int q = __shfl_sync(0xffffffffu, qv, jj);
         const float dx = __shfl_sync(0xffffffffu, dxv, jj);
         float sw = 0.f;  // sum_t Kbar_t (1 + m_t) W_tj
 #pragma unroll
         for (int u = 0; u < NW; ++u) sw = fmaf(kb[u], __shfl_sync(0xffffffffu, wv[u], jj), sw);
-        if (q != key) {  // warp-uniform
-          if (key >= 0) flush();
-          key = q;
-          rc = 0.f;
-          rcd = 0.f;
-        }
         const float chip =
             fmaxf(chiT[((q & 0xffff) - wbase) * KU_PAD + lane] + slT[((q >> 16) - wbase) * KU_PAD + lane] * dx, 0.f);
         const float diff = chip - chi_wl;
@@ -806,12 +889,12 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
           rc += ch;
           rcd = fmaf(ch, dx, rcd);
         }
+        if ((ends >> jj) & 1u) flush(q);  // warp-uniform
       }
     }
     lacc = fmaf(cjf, lk, lacc);
     cwS[(warp * KV_NODES + (n - n0)) * KU_PAD + lane] = craw_w > 0.f ? fac * cwa : 0.f;
   }
-  if (key >= 0) flush();
   lS[warp * KU_PAD + lane] = lacc;
   bS[warp * KU_PAD + lane] = bacc;
   __syncthreads();
@@ -894,6 +977,7 @@ static void launch_vjp_t(const GradBatch& gb, cudaStream_t st) {
   const int LT = vjp_ltile(gb.n_cls, gb.n_ell);
   const size_t smem = vj_layout(gb.n_tr, gb.n_cls, LT).total;
   cudaFuncSetAttribute(grad_vjp32_kernel<GEN, FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (FWD || gb.vjp_cl) cudaMemsetAsync(gb.cl_count, 0, sizeof(unsigned) * (size_t)gb.n_items, st);
   dim3 grid(vjp_chunks(gb.na), gb.n_items);
   grad_vjp32_kernel<GEN, FWD><<<grid, VJ_THREADS, smem, st>>>(gb, LT);
 }
@@ -902,17 +986,6 @@ static void launch_vjp_t(const GradBatch& gb, cudaStream_t st) {
 void launch_vjp32_cl(const GradBatch& gb, cudaStream_t st) {
   if (gb.physics_or != 0) launch_vjp_t<true, true>(gb, st);
   else launch_vjp_t<false, true>(gb, st);
-  launch_vjp32_cl_reduce(gb, st);
-}
-
-// C_ell from the chunks' partials (written by the forward kernel, or by the
-// product kernel when vjp_cl is set)
-void launch_vjp32_cl_reduce(const GradBatch& gb, cudaStream_t st) {
-  const size_t per = (size_t)gb.n_cls * gb.n_ell;
-  size_t bx = (per + 255) / 256;
-  const size_t cap = (152 * 16 + gb.n_items - 1) / gb.n_items;
-  if (bx > cap) bx = cap;
-  vjp_cl_reduce_kernel<<<dim3((unsigned)(bx ? bx : 1), gb.n_items), 256, 0, st>>>(gb);
 }
 
 // the product with the items' cotangents vbar into their grad
