@@ -87,6 +87,18 @@ __host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT) {
   return L;
 }
 
+// asynchronous global -> shared copies (no register staging; all of a
+// thread's copies in flight at once), completed by cp_async_wait_all
+__device__ __forceinline__ void cp_async16(void* s, const void* g) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(s)), "l"(g)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* s, const void* g) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(s)), "l"(g)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+
 // GEN: some item may use a non-default operator point (as grad_limber32).
 // FWD: the forward form (partial C_ell of the chunk, no cotangent).
 template <bool GEN, bool FWD>
@@ -123,24 +135,48 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   const int tid = threadIdx.x, grp = tid >> 3, sub = tid & (VJ_GROUP - 1);
   const TabD* tb = gi.tab;
   // the Eisenstein-Hu inputs and their tangents (formed once per cosmology
-  // by the table stage)
-  for (int i = tid; i < 16; i += VJ_THREADS) ev[i] = tb->ehv[i];
+  // by the table stage), the chunk's FP32 rows (values and tangents) and
+  // radial kernels: asynchronous copies
+  for (int i = tid; i < 16; i += VJ_THREADS) cp_async4(ev + i, tb->ehv + i);
   if (!FWD)
-    for (int i = tid; i < NET * NDIR; i += VJ_THREADS) et[i] = tb->eht[i];
-  // the chunk's FP32 rows (values and tangents) and radial kernels
+    for (int i = tid; i < NET * NDIR; i += VJ_THREADS) cp_async4(et + i, tb->eht + i);
   {
-    const float4* src = reinterpret_cast<const float4*>(gi.rowg + (size_t)a0 * NROWG);
-    float4* dst = reinterpret_cast<float4*>(R);
-    for (int i = tid; i < tc * (NROWG / 4); i += VJ_THREADS) dst[i] = src[i];
-    const int per_t = n_tr * (NDIR + 1);
-    for (int i = tid; i < tc * per_t; i += VJ_THREADS) {
-      const int t = i / per_t, rem = i - t * per_t;
-      const int tr = rem / (NDIR + 1), s = rem - tr * (NDIR + 1);
-      Ks[i] = gi.kernf[((size_t)tr * na + a0 + t) * (NDIR + 1) + s];
+    const float* src = gi.rowg + (size_t)a0 * NROWG;
+    for (int i = tid; i < tc * (NROWG / 4); i += VJ_THREADS) cp_async16(R + 4 * i, src + 4 * i);
+    // K rows [t][tracer][NDIR + 1]: consecutive threads on consecutive nodes
+    for (int i = tid; i < tc * n_tr; i += VJ_THREADS) {
+      const int tr = i / tc, t = i - tr * tc;
+      const float* ks = gi.kernf + ((size_t)tr * na + a0 + t) * (NDIR + 1);
+      float* kd = Ks + ((size_t)t * n_tr + tr) * (NDIR + 1);
+#pragma unroll
+      for (int k = 0; k < NDIR + 1; ++k) cp_async4(kd + k, ks + k);
     }
   }
   if (!FWD)
     for (int i = tid; i < tc * n_cls; i += VJ_THREADS) Qd[i] = make_float2(0.f, 0.f);
+  const float4* KH4 = geo_ptr<float4>(geo, geo->off_kh4);
+  const float* EF32 = geo_ptr<float>(geo, geo->off_ef32);
+  // an ell tile's (l + 1/2) factors and, for the product, its cotangents
+  // v_p(l) = vbar_p(l) ef_i(l) ef_j(l); the first tile while the copies fly
+  auto fill_tile = [&](int l0, int lt) {
+    for (int l = tid; l < lt; l += VJ_THREADS) {
+      const float4 k4 = KH4[l0 + l];
+      khv[l] = k4.x;
+      lkhv[l] = k4.y;
+      ikhv[l] = k4.z;
+    }
+    if (!FWD)
+      for (int l = tid; l < lt; l += VJ_THREADS) {
+        const int ell = l0 + l;
+#pragma unroll 4
+        for (int p = 0; p < n_cls; ++p) {
+          const float ef = EF32[(size_t)geo->pair_i[p] * n_ell + ell] * EF32[(size_t)geo->pair_j[p] * n_ell + ell];
+          vS[p * TS + l] = (float)gi.vbar[(size_t)p * n_ell + ell] * ef;
+        }
+      }
+  };
+  fill_tile(0, min(LT, n_ell));
+  cp_async_wait_all();
   __syncthreads();
   // M_p(a) = u K_i K_j, the operation order of grad_limber32
   for (int i = tid; i < tc * n_cls; i += VJ_THREADS) {
@@ -156,8 +192,6 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   eh.c142ac = ev[5]; eh.alpha_b = ev[6]; eh.beta_b = ev[7]; eh.beta_node = ev[8]; eh.lg2_ksilk = ev[9];
   eh.fb = ev[10]; eh.fc = ev[11]; eh.ns3 = ev[12]; eh.inv_keq = ev[13];
   eh.agam = ev[14]; eh.nwq = ev[15];
-  const float4* KH4 = geo_ptr<float4>(geo, geo->off_kh4);
-  const float* EF32 = geo_ptr<float>(geo, geo->off_ef32);
   float accA[T_U], accE[NET];
 #pragma unroll
   for (int j = 0; j < T_U; ++j) accA[j] = 0.f;
@@ -165,21 +199,11 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   for (int j = 0; j < NET; ++j) accE[j] = 0.f;
   for (int l0 = 0; l0 < n_ell; l0 += LT) {
     const int lt = min(LT, n_ell - l0);
-    __syncthreads();  // the previous tile's Pt / vS are consumed
-    for (int l = tid; l < lt; l += VJ_THREADS) {
-      const float4 k4 = KH4[l0 + l];
-      khv[l] = k4.x;
-      lkhv[l] = k4.y;
-      ikhv[l] = k4.z;
+    if (l0 > 0) {
+      __syncthreads();  // the previous tile's Pt / vS are consumed
+      fill_tile(l0, lt);
     }
-    if (!FWD)
-      for (int q = tid; q < n_cls * lt; q += VJ_THREADS) {
-        const int p = q / lt, l = q - p * lt;
-        const int ell = l0 + l;
-        const float ef = EF32[(size_t)geo->pair_i[p] * n_ell + ell] * EF32[(size_t)geo->pair_j[p] * n_ell + ell];
-        vS[p * TS + l] = (float)gi.vbar[(size_t)p * n_ell + ell] * ef;
-      }
-    __syncthreads();
+    __syncthreads();  // the tile's factors and cotangents (first tile: and M)
     const int L4 = (lt + 3) >> 2;
     if (!FWD) {
       // W(t, l) = sum_p M_p(t) v_p(l) in 4 x 4 blocks (rows past tc and
@@ -347,6 +371,11 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
     if (lane == 0) Ered[warp * NET + j] = v;
   }
   __syncthreads();
+  // the Eisenstein-Hu adjoints over the warps, one thread per input (float
+  // pairs), into the first row of Ered
+  FF ej{0.f, 0.f};
+  if (tid < NET)
+    for (int w = 0; w < VJ_THREADS / 32; ++w) ej = ej + Ered[w * NET + tid];
   // reverse lensing: the cotangents of the WeakLensing shear kernels,
   // Kbar_i(t) = u(t) sum_p Q_p(t) dK_i K_j / dK_i (both factors of an auto pair)
   if (gb.vjp_rev)
@@ -363,6 +392,12 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
       }
       gi.kbar[(size_t)i * na + a0 + t] = R[(size_t)t * NROWG + F_U] * kb.hi;
     }
+  __syncthreads();  // every read of Ered is done
+  if (tid < NET) {
+    Ered[2 * tid] = ej.hi;
+    Ered[2 * tid + 1] = ej.lo;
+  }
+  __syncthreads();
   // projection on the tangents: thread (a node t, direction d)
   {
     const int t = tid >> 3, d = tid & 7;
@@ -392,11 +427,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
     if (t == 0) {
       // the cosmology's Eisenstein-Hu inputs, once per CTA
       FF se{0.f, 0.f};
-      for (int j = 0; j < NET; ++j) {
-        FF ej{0.f, 0.f};
-        for (int w = 0; w < VJ_THREADS / 32; ++w) ej = ej + Ered[w * NET + j];
-        se = se + ej * et[j * NDIR + d];
-      }
+      for (int j = 0; j < NET; ++j) se = se + FF{Ered[2 * j], Ered[2 * j + 1]} * et[j * NDIR + d];
       gd += ffd(se);
     }
     gred[t * NDIR + d] = gd;
