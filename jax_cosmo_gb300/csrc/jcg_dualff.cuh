@@ -201,6 +201,64 @@ __device__ __forceinline__ DualFF<N> xfmin(const DualFF<N>& a, double c) {
   return (d.hi > 0.f || (d.hi == 0.f && d.lo >= 0.f)) ? a : ffd_const<N>(c);
 }
 
+// a float pair stored as float2 (hi, lo)
+__device__ __forceinline__ FF f2ff(float2 v) { return FF{v.x, v.y}; }
+
+// float-pair scalars (grid abscissae held as pairs: no FP64 conversions)
+template <int N>
+__device__ __forceinline__ DualFF<N> operator+(const DualFF<N>& a, FF b) {
+  DualFF<N> r = a;
+  r.v = a.v + b;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualFF<N> operator+(FF a, const DualFF<N>& b) {
+  return b + a;
+}
+template <int N>
+__device__ __forceinline__ DualFF<N> operator-(const DualFF<N>& a, FF b) {
+  DualFF<N> r = a;
+  r.v = a.v - b;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualFF<N> operator-(FF a, const DualFF<N>& b) {
+  DualFF<N> r;
+  r.v = a - b.v;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = -b.d[i];
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualFF<N> operator*(const DualFF<N>& a, FF b) {
+  DualFF<N> r;
+  r.v = a.v * b;
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = a.d[i] * b.hi;
+  return r;
+}
+template <int N>
+__device__ __forceinline__ DualFF<N> operator*(FF a, const DualFF<N>& b) {
+  return b * a;
+}
+template <int N>
+__device__ __forceinline__ DualFF<N> operator/(FF a, const DualFF<N>& b) {
+  DualFF<N> r;
+  r.v = a / b.v;
+  const float s = -r.v.hi * rcpf(b.v.hi);
+#pragma unroll
+  for (int i = 0; i < N; ++i) r.d[i] = s * b.d[i];
+  return r;
+}
+// DualFF<8> from a float-pair value (float2 hi, lo) and 8 float tangents
+__device__ __forceinline__ DualFF<NDIR> ff8_of(float2 v, const float* d) {
+  DualFF<NDIR> r;
+  r.v = FF{v.x, v.y};
+#pragma unroll
+  for (int i = 0; i < NDIR; ++i) r.d[i] = d[i];
+  return r;
+}
+
 // DualFF<8> from a value and 8 double tangents at stride `stride`
 __device__ __forceinline__ DualFF<NDIR> ff8_of(double v, const double* d, int stride) {
   DualFF<NDIR> r;

@@ -503,6 +503,22 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     for (int d = 0; d < NDIR; ++d) out->sd[d][i] = sd[d * NSCAL + i];
   }
   if (F32T) {
+    // float-pair copies for the row stage
+    for (int i = t; i < NSCAL; i += blockDim.x) {
+      const FF v = ff_of(sv[i]);
+      out->svF[i] = make_float2(v.hi, v.lo);
+      for (int d = 0; d < NDIR; ++d) out->sdF[i][d] = (float)sd[d * NSCAL + i];
+    }
+    for (int i = t; i < NCHI; i += blockDim.x) {
+      const FF v = ff_of(out->chiv[i]);
+      out->chiF[i] = make_float2(v.hi, v.lo);
+      for (int d = 0; d < NDIR; ++d) out->chidF[i][d] = (float)out->chid[d][i];
+    }
+    for (int i = t; i < NGROW; i += blockDim.x) {
+      const FF v = ff_of(out->gv[i]);
+      out->gF[i] = make_float2(v.hi, v.lo);
+      for (int d = 0; d < NDIR; ++d) out->gdF[i][d] = (float)out->gd[d][i];
+    }
     // float chi tables and segment slopes with tangents (the FP32 lensing stage)
     for (int e = t; e < (NDIR + 1) * NCHI; e += blockDim.x) {
       const int comp = e / NCHI, i = e % NCHI;
@@ -602,8 +618,13 @@ __global__ void __launch_bounds__(NRT) grad_moments32_kernel(GradBatch gb, const
       ad[7] = fmaf(q1.w, e.x, ad[7]);
     }
     out->sigv[j] = (double)ah + (double)al;
+    const FF sv = ff_two_sum(ah, al);
+    out->sigF[j] = make_float2(sv.hi, sv.lo);
 #pragma unroll
-    for (int d = 0; d < NDIR; ++d) out->sigd[d][j] = (double)ad[d];
+    for (int d = 0; d < NDIR; ++d) {
+      out->sigd[d][j] = (double)ad[d];
+      out->sigdF[j][d] = ad[d];
+    }
   }
 }
 
@@ -842,11 +863,12 @@ __device__ __forceinline__ F8 interp_f8(double x, const double* xp, const double
 // takahashi2012 coefficients, Limber weight; the row is written as computed.
 // interpolation on the segment sg of a table with tangents, by the segment's
 // node-spacing reciprocal ida (no float64 division)
-__device__ __forceinline__ FF8 interp_ff8(double x, const double* xp, const double* ida, const double* fv,
-                                         const double* fd, int stride, int2 sg) {
-  const FF8 f0 = ff8_of(fv[sg.x], fd + sg.x, stride), f1 = ff8_of(fv[sg.y], fd + sg.y, stride);
-  const double inv = ida[min(sg.x, sg.y)] * (sg.y > sg.x ? 1.0 : -1.0);
-  return f0 + (f1 - f0) * (inv * (x - xp[sg.x]));
+__device__ __forceinline__ FF8 interp_ff8(FF x, const float2* xp, const float2* ida, const float2* fv,
+                                         const float (*fd)[NDIR], int2 sg) {
+  const FF8 f0 = ff8_of(fv[sg.x], fd[sg.x]), f1 = ff8_of(fv[sg.y], fd[sg.y]);
+  const FF iv = f2ff(ida[min(sg.x, sg.y)]);
+  const FF inv = sg.y > sg.x ? iv : -iv;
+  return f0 + (f1 - f0) * (inv * (x - f2ff(xp[sg.x])));
 }
 
 constexpr int GR32_THREADS = 64;
@@ -865,15 +887,16 @@ __global__ void __launch_bounds__(GR32_THREADS, 8) grad_rows32_kernel(GradBatch 
   const int64_t* SC = geo_ptr<int64_t>(geo, geo->off_seg_chi);
   const int64_t* SG = geo_ptr<int64_t>(geo, geo->off_seg_grow);
   const double a = A[n];
+  const FF aF = ff_of(a);
   float* row = gi.rowg + (size_t)n * NROWG;
   float* tg = row + NROWV;
   auto put_t = [&](int slot, const FF8& x, float sc) {
 #pragma unroll
     for (int d = 0; d < NDIR; ++d) tg[slot * NDIR + d] = x.d[d] * sc;
   };
-  FF8 g = interp_ff8(a, c->atab_grow, c->grow_ida, tb->gv, &tb->gd[0][0], NGROW, unpack_seg(SG[n]));
+  FF8 g = interp_ff8(aF, c->grow_a_ff, c->grow_ida_ff, tb->gF, tb->gdF, unpack_seg(SG[n]));
   g = xfmin(xfmax(g, 0.0), 1.0);
-  FF8 chi = interp_ff8(a, c->atab_chi, c->chi_ida, tb->chiv, &tb->chid[0][0], NCHI, unpack_seg(SC[n]));
+  FF8 chi = interp_ff8(aF, c->atab_chi_ff, c->chi_ida_ff, tb->chiF, tb->chidF, unpack_seg(SC[n]));
   chi = xfmax(chi, 0.0);
   const FF8 g2 = g * g;
   const double g2v = val(g2);
@@ -901,10 +924,10 @@ __global__ void __launch_bounds__(GR32_THREADS, 8) grad_rows32_kernel(GradBatch 
   const double xpi = tb->sigv[ind] * g2v;
   const double xc = fmin(fmax(1.0, tb->sigv[1] * g2v), tb->sigv[NRT - 2] * g2v);
   const int j2 = ind + ((xc - xpi >= 0.0) ? 1 : -1);
-  const FF8 xp0 = ff8_of(tb->sigv[ind], &tb->sigd[0][ind], NRT) * g2;
-  const FF8 xp1 = ff8_of(tb->sigv[j2], &tb->sigd[0][j2], NRT) * g2;
-  const FF8 slope = (c->logr[j2] - c->logr[ind]) / (xp1 - xp0);
-  const FF8 bb = c->logr[ind] - slope * xp0;
+  const FF8 xp0 = ff8_of(tb->sigF[ind], tb->sigdF[ind]) * g2;
+  const FF8 xp1 = ff8_of(tb->sigF[j2], tb->sigdF[j2]) * g2;
+  const FF8 slope = (f2ff(c->logr_ff[j2]) - f2ff(c->logr_ff[ind])) / (xp1 - xp0);
+  const FF8 bb = f2ff(c->logr_ff[ind]) - slope * xp0;
   const FF8 root = slope * 1.0 + bb;
   const FF8 R = xfmax(xexp(root), 1e-6);
   const FF8 knl = 1.0 / R;
@@ -959,7 +982,7 @@ __global__ void __launch_bounds__(GR32_THREADS, 8) grad_rows32_kernel(GradBatch 
       s2d[d] = fmaf(w2, p[d], s2d[d]);
     }
   }
-  double s1 = ff_to_double(s1p), s2 = ff_to_double(s2p);
+  FF s1 = s1p, s2 = s2p;
   float t1d[NDIR], t2d[NDIR];
 #pragma unroll
   for (int d = 0; d < NDIR; ++d) t1d[d] = t2d[d] = 0.f;
@@ -984,9 +1007,8 @@ __global__ void __launch_bounds__(GR32_THREADS, 8) grad_rows32_kernel(GradBatch 
       df = fmaf(df, x.hi, pf);
       pf = fmaf(pf, x.hi, r.hi);
     }
-    const FF f1 = ff_mul(x, P);
-    const double t1 = ff_to_double(f1);
-    const double t2 = t1 + ff_to_double(ff_mul(ff_mul(x, x), D));
+    const FF t1 = ff_mul(x, P);
+    const FF t2 = t1 + ff_mul(ff_mul(x, x), D);
     const float xs = x.hi, dxr = 2.f * xs * iR;
     const float t1r = (pf + xs * df) * dxr;
     const float t2r = (pf + 3.f * xs * df + xs * xs * (2.f * ddf)) * dxr;
@@ -1009,14 +1031,14 @@ __global__ void __launch_bounds__(GR32_THREADS, 8) grad_rows32_kernel(GradBatch 
         t2d[d] = fmaf(a1, dm[d], fmaf(-a2, dm1[d], t2d[d]));
       }
     }
-    s1 += 2.0 * t1;
-    s2 += 4.0 * t2;
+    s1 = s1 + ff_scale2(t1, 2.f);
+    s2 = s2 + ff_scale2(t2, 4.f);
     s1r += 2.f * t1r;
     s2r += 4.f * t2r;
   }
   FF8 S1, S2;
-  S1.v = ff_of(s1);
-  S2.v = ff_of(s2);
+  S1.v = s1;
+  S2.v = s2;
   const float f1r = s1r, f2r = s2r;
 #pragma unroll
   for (int d = 0; d < NDIR; ++d) {
@@ -1028,14 +1050,20 @@ __global__ void __launch_bounds__(GR32_THREADS, 8) grad_rows32_kernel(GradBatch 
   const FF8 C = I1 * I1 + I2;
   // coefficients (power.py:177-238)
   BgT<FF8> bg;
-  bg.Om = ff8_of(tb->sv[S_OMEGA_M], &tb->sd[0][S_OMEGA_M], NSCAL);
-  bg.Ok = ff8_of(tb->sv[S_OMEGA_K], &tb->sd[0][S_OMEGA_K], NSCAL);
-  bg.Ode = ff8_of(tb->sv[S_OMEGA_DE], &tb->sd[0][S_OMEGA_DE], NSCAL);
-  bg.w0 = ff8_of(tb->sv[S_W0], &tb->sd[0][S_W0], NSCAL);
-  bg.wa = ff8_of(tb->sv[S_WA], &tb->sd[0][S_WA], NSCAL);
-  const double lna = log(a);
-  FF8 om_m, om_de;
-  omT(bg, a, lna, om_m, om_de);
+  bg.Om = ff8_of(tb->svF[S_OMEGA_M], tb->sdF[S_OMEGA_M]);
+  bg.Ok = ff8_of(tb->svF[S_OMEGA_K], tb->sdF[S_OMEGA_K]);
+  bg.Ode = ff8_of(tb->svF[S_OMEGA_DE], tb->sdF[S_OMEGA_DE]);
+  bg.w0 = ff8_of(tb->svF[S_W0], tb->sdF[S_W0]);
+  bg.wa = ff8_of(tb->svF[S_WA], tb->sdF[S_WA]);
+  // E^2(a) and its dark-energy factor once (esqrT, background.py:47-66), in
+  // float pairs from ln a and 1 / a; Omega_m(a), Omega_de(a) (omT) and
+  // dchi/da (dchioverdaT) from them
+  const FF lna = ff_log(aF), ia = ff_rcp(aF), ia2 = ia * ia;
+  const FF8 fde = -3.0 * (1.0 + bg.w0 + bg.wa) * lna + 3.0 * bg.wa * (aF - ffc(1.0));
+  const FF8 efde = xexp(fde);
+  const FF8 esq = bg.Om * (ia2 * ia) + bg.Ok * ia2 + bg.Ode * efde;
+  const FF8 om_m = bg.Om * (ia2 * ia) / esq;
+  const FF8 om_de = bg.Ode * efde / esq;
   // halofit coefficients (power.py:177-244), each stored as soon as it is
   // formed (short live ranges of the 8-tangent values)
   const FF8 n2 = neff * neff, n3 = n2 * neff, n4 = n2 * n2;
@@ -1085,7 +1113,7 @@ __global__ void __launch_bounds__(GR32_THREADS, 8) grad_rows32_kernel(GradBatch 
       put_t(T_MUN, mu, 1.f);
     }
   } else {
-    const FF8 opw = om_de * (1.0 + wT(bg, a));
+    const FF8 opw = om_de * (1.0 + (bg.w0 + (ffc(1.0) - aF) * bg.wa));  // wT (background.py:53)
     {
       const FF8 beta = 2.0379 - 0.7354 * neff + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
       row[F_BETAN] = beta.v.hi;
@@ -1134,11 +1162,11 @@ __global__ void __launch_bounds__(GR32_THREADS, 8) grad_rows32_kernel(GradBatch 
     row[F_LG2INVCHI] = -(ff_log(chic.v) * ffc(LOG2E)).hi;
     row[F_CHIC] = chic.v.hi;
     put_t(T_CHIC, chic, 1.f);
-    const FF8 pkn = ff8_of(tb->sv[S_PKNORM], &tb->sd[0][S_PKNORM], NSCAL);
+    const FF8 pkn = ff8_of(tb->svF[S_PKNORM], tb->sdF[S_PKNORM]);
     const FF8 d2fac = g * g * pkn / TWO_PI2_G;
     row[F_D2FAC] = d2fac.v.hi;
     put_t(T_D2FAC, d2fac, 1.f);
-    const FF8 dchi = dchioverdaT(bg, a, lna);
+    const FF8 dchi = (ffc(RH) * ia2) / xsqrt(esq);
     const FF8 u = WS[n] * dchi / xfmax(chi * chi, 1.0) / C2_G;
     row[F_U] = u.v.hi;
     put_t(T_U, u, 1.f);
@@ -1612,10 +1640,70 @@ int grad_limber_tile(int n_ell, int n_cls) {
   return (n_ell + tiles - 1) / tiles;
 }
 
-// Small fp32c batches: the table kernel's per-node evaluations (chi
-// right-hand sides, growth coefficients, Romberg integrand, exp(n_s ln k) T^2
-// on the P(k) grid), one per thread over GNODE_CTAS CTAs per cosmology, in
-// DualF<8> as in the table kernel.
+// The per-node physics of the fp32c table stage with the abscissae as float
+// pairs (ConstTables' *_ff grids): dchi_dlna_cT, growth_qr_cT and
+// eh_transferT / eh_nowiggleT of jcg_dual.cuh with FF in place of their
+// double arguments, the same operations in the same order, so that no
+// operand is converted from float64 at run time.
+__device__ __forceinline__ FF8 dchi_dlna_f8(const BgT<FF8>& c, FF a, FF lna, FF ia) {
+  const FF8 f = -3.0 * (1.0 + c.w0 + c.wa) * lna + 3.0 * c.wa * (a - ffc(1.0));
+  const FF8 ef = xexp(f);
+  const FF ia2 = ia * ia;
+  const FF8 e2 = c.Om * (ia2 * ia) + c.Ok * ia2 + c.Ode * ef;
+  return (ffc(RH) * ia) / xsqrt(e2);
+}
+__device__ __forceinline__ void growth_qr_f8(const BgT<FF8>& b, FF x, FF lnx, FF ix, FF8& q, FF8& r) {
+  const FF8 f = -3.0 * (1.0 + b.w0 + b.wa) * lnx + 3.0 * b.wa * (x - ffc(1.0));
+  const FF8 ef = xexp(f);
+  const FF ix2 = ix * ix, ix3 = ix2 * ix;
+  const FF8 ie2 = 1.0 / (b.Om * ix3 + b.Ok * ix2 + b.Ode * ef);
+  const FF8 omm = b.Om * ix3 * ie2, omde = b.Ode * ef * ie2;
+  const FF8 w = b.w0 + (ffc(1.0) - x) * b.wa;  // wT (background.py:53)
+  q = (2.0 - 0.5 * (omm + (1.0 + 3.0 * w) * omde)) * ix;
+  r = 1.5 * omm * ix2;
+}
+__device__ __noinline__ FF8 eh_nowiggle_f8(FF8 sh_d, FF8 ag, FF8 nwq, FF k) {
+  const FF8 x = (ffc(0.43) * k) * sh_d, x2 = x * x;
+  const FF8 q = k * nwq / (ag + (1.0 - ag) / (1.0 + x2 * x2));
+  const FF8 L = xlog(2.0 * EULER_E + 1.8 * q);
+  const FF8 C = 14.2 + 731.0 / (1.0 + 62.5 * q);
+  return L / (L + C * q * q);
+}
+__device__ __forceinline__ FF8 eh_transfer_f8(const FF8* s, FF k, FF lk) {
+  const FF8 k_eq = s[S_K_EQ], sh_d = s[S_SH_D];
+  if (s[S_TFNW].v.hi != 0.f) return eh_nowiggle_f8(sh_d, s[S_AGAM], s[S_NWQ], k);
+  const FF8 q = k / (13.41 * k_eq);
+  const FF8 q108 = xexp(1.08 * (lk - s[S_LGQ]));
+  const FF8 Cb = 386.0 / (1.0 + 69.9 * q108);
+  const FF8 qq = q * q;
+  const FF8 L1 = xlog(EULER_E + 1.8 * s[S_BETA_C] * q);
+  const FF8 L2 = xlog(EULER_E + 1.8 * q);
+  const FF8 Ta = L1 / (L1 + (14.2 + Cb) * qq);
+  const FF8 Tb = L1 / (L1 + (14.2 / s[S_ALPHA_C] + Cb) * qq);
+  const FF8 Tn = L2 / (L2 + (14.2 + Cb) * qq);
+  const FF8 ksh = k * sh_d;
+  const FF8 x54 = ksh / 5.4, x54s = x54 * x54;
+  const FF8 f = 1.0 / (1.0 + x54s * x54s);
+  const FF8 Tc = f * Ta + (1.0 - f) * Tb;
+  const FF8 bn = s[S_BETA_NODE] / ksh;
+  const FF8 tilde_s = sh_d / xcbrt(1.0 + bn * bn * bn);
+  const FF8 x52 = ksh / 5.2;
+  const FF8 bb = s[S_BETA_B] / ksh;
+  const FF8 silk = xexp(-xexp(1.4 * (lk - s[S_LGKSILK])));
+  const FF8 arg = k * tilde_s;
+  const FF8 sinc = xsin(arg) / arg;
+  const FF8 Tbar = (Tn / (1.0 + x52 * x52) + s[S_ALPHA_B] / (1.0 + bb * bb * bb) * silk) * sinc;
+  return s[S_FB] * Tbar + s[S_FC] * Tc;
+}
+
+// fp32c: the table kernel's per-node evaluations (chi right-hand sides,
+// growth coefficients, Romberg integrand, exp(n_s ln k) T^2 on the P(k)
+// grid), one per thread, in DualFF<8> with float-pair abscissae.
+// KIND 0: chi right-hand sides (nodes, midpoints); 1: growth coefficients
+// (nodes, midpoints); 2: Eisenstein-Hu at the Romberg and P(k) nodes.  One
+// launch per kind keeps each kernel's code small (the three inlined bodies in
+// one kernel thrashed the instruction cache).
+template <int KIND>
 __global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.y;
   if (item >= gb.n_items) return;
@@ -1626,8 +1714,7 @@ __global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const Con
   __shared__ FF8 sF[NSCAL];
   for (int i = threadIdx.x; i < NSCAL; i += blockDim.x) sF[i] = ff8_of(tb->sv[i], &tb->sd[0][i], NSCAL);
   __syncthreads();
-  const int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= GNODE_WORK) return;
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const BgT<FF8> bgf = make_bgT(sF);
   double* dst = gb.gnode + (size_t)item * GNODE_STRIDE;
   auto putf = [&](int off, int stride, int i, const FF8& x) {
@@ -1635,45 +1722,33 @@ __global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const Con
 #pragma unroll
     for (int d = 0; d < NDIR; ++d) dst[off + (1 + d) * stride + i] = x.d[d];
   };
-  int w = e;
-  if (w < NCHI) {
-    putf(0, NCHI, w, dchi_dlna_cT(bgf, c->chi_a[w], c->lna_chi[w], c->chi_ia[w]));
-    return;
-  }
-  w -= NCHI;
-  if (w < NCHI - 1) {
-    const int i = w + 1;
-    putf(GNODE_FM, NCHI, i, dchi_dlna_cT(bgf, c->chi_am[i], c->chi_lnam[i], c->chi_iam[i]));
-    return;
-  }
-  w -= NCHI - 1;
-  if (w < NGROW) {
+  if (KIND == 0) {
+    if (w < NCHI) {
+      putf(0, NCHI, w, dchi_dlna_f8(bgf, f2ff(c->chi_a_ff[w]), f2ff(c->lna_chi_ff[w]), f2ff(c->chi_ia_ff[w])));
+    } else if (w < 2 * NCHI - 1) {
+      const int i = w - NCHI + 1;
+      putf(GNODE_FM, NCHI, i, dchi_dlna_f8(bgf, f2ff(c->chi_am_ff[i]), f2ff(c->chi_lnam_ff[i]), f2ff(c->chi_iam_ff[i])));
+    }
+  } else if (KIND == 1) {
     FF8 q, r;
-    growth_qr_cT(bgf, c->atab_grow[w], c->grow_lna[w], c->grow_ia[w], q, r);
-    putf(GNODE_QR, NGROW, w, q);
-    putf(GNODE_QR + (NDIR + 1) * NGROW, NGROW, w, r);
-    return;
-  }
-  w -= NGROW;
-  if (w < NGROW - 1) {
-    const int i = w + 1;
-    FF8 q, r;
-    growth_qr_cT(bgf, c->grow_am[i], c->grow_lnam[i], c->grow_iam[i], q, r);
-    putf(GNODE_QR + 2 * (NDIR + 1) * NGROW, NGROW, i, q);
-    putf(GNODE_QR + 3 * (NDIR + 1) * NGROW, NGROW, i, r);
-    return;
-  }
-  w -= NGROW - 1;
-  if (w < NROMB) {
-    const double logk = c->romb_logk[w];
-    const FF8 T = eh_transferT(sF, c->romb_k[w], logk);
-    putf(GNODE_FR, NROMB, w, c->romb_kw2[w] * ((T * T) * xexp(sF[S_NS] * logk)));
-    return;
-  }
-  w -= NROMB;
-  {
-    const FF8 T = eh_transferT(sF, c->kh[w], c->logk[w]);
-    putf(GNODE_U, NKH, w, xexp(sF[S_NS] * c->logk[w]) * (T * T));
+    if (w < NGROW) {
+      growth_qr_f8(bgf, f2ff(c->grow_a_ff[w]), f2ff(c->grow_lna_ff[w]), f2ff(c->grow_ia_ff[w]), q, r);
+      putf(GNODE_QR, NGROW, w, q);
+      putf(GNODE_QR + (NDIR + 1) * NGROW, NGROW, w, r);
+    } else if (w < 2 * NGROW - 1) {
+      const int i = w - NGROW + 1;
+      growth_qr_f8(bgf, f2ff(c->grow_am_ff[i]), f2ff(c->grow_lnam_ff[i]), f2ff(c->grow_iam_ff[i]), q, r);
+      putf(GNODE_QR + 2 * (NDIR + 1) * NGROW, NGROW, i, q);
+      putf(GNODE_QR + 3 * (NDIR + 1) * NGROW, NGROW, i, r);
+    }
+  } else if (w < NROMB + NKH) {
+    const bool romb = w < NROMB;
+    const int i = romb ? w : w - NROMB;
+    const FF logk = f2ff(romb ? c->romb_logk_ff[i] : c->logk_ff[i]);
+    const FF8 T = eh_transfer_f8(sF, f2ff(romb ? c->romb_k_ff[i] : c->kh_ff[i]), logk);
+    const FF8 TT = T * T, ex = xexp(sF[S_NS] * logk);
+    if (romb) putf(GNODE_FR, NROMB, i, f2ff(c->romb_kw2_ff[i]) * (TT * ex));
+    else putf(GNODE_U, NKH, i, ex * TT);
   }
 }
 
@@ -1767,8 +1842,13 @@ __global__ void __launch_bounds__(32 * NDIR) grad_growth_gamma_kernel(GradBatch 
     const D1 el = xexp(ys[NGROW - 1]);
     for (int i = 0; i < NGROW; ++i) {
       const D1 g = xexp(ys[i]) / el;
-      if (d == 0) tb->gv[i] = g.v;
+      if (d == 0) {
+        tb->gv[i] = g.v;
+        const FF gf = ff_of(g.v);
+        tb->gF[i] = make_float2(gf.hi, gf.lo);  // the row stage's copy
+      }
       tb->gd[d][i] = g.d[0];
+      tb->gdF[i][d] = (float)g.d[0];
     }
   }
 }
@@ -1779,7 +1859,11 @@ void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t s
     grad_scalars_warp_kernel<<<gb.n_items, 16 * NDIR, 0, st>>>(gb);
   else
     grad_scalars_kernel<<<(gb.n_items * NDIR + 127) / 128, 128, 0, st>>>(gb);
-  if (gb.gnode) grad_nodes_kernel<<<dim3(GNODE_CTAS, gb.n_items), 128, 0, st>>>(gb, c);
+  if (gb.gnode) {
+    grad_nodes_kernel<0><<<dim3((2 * NCHI - 1 + 127) / 128, gb.n_items), 128, 0, st>>>(gb, c);
+    grad_nodes_kernel<1><<<dim3((2 * NGROW - 1 + 127) / 128, gb.n_items), 128, 0, st>>>(gb, c);
+    grad_nodes_kernel<2><<<dim3((NROMB + NKH + 127) / 128, gb.n_items), 128, 0, st>>>(gb, c);
+  }
   if (gb.precision == JCG_FP32C) {
     if (tf_nowiggle(gb.physics_or)) {
       cudaFuncSetAttribute(grad_tables_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);

@@ -66,6 +66,16 @@ struct TabD {
   float eht[88];   // NET x NDIR
   float padg[8];
   float wq3f[NKH + 15];        // simpson_kh[i] * P(k_i) k_i^3 / (2 pi^2), float; padded to 64 bytes
+  // fp32c row stage: the scalars, chi, growth and sigma^2(R) tables above as
+  // float-pair values and float tangents (node-major, rows of 8)
+  float2 svF[NSCAL];
+  float sdF[NSCAL][NDIR];
+  float2 chiF[NCHI];
+  float chidF[NCHI][NDIR];
+  float2 gF[NGROW];
+  float gdF[NGROW][NDIR];
+  float2 sigF[NRT];
+  float sigdF[NRT][NDIR];
 };
 static_assert(sizeof(TabD) % 64 == 0, "TabD alignment");
 
@@ -201,8 +211,8 @@ struct GradBatch {
   unsigned* cl_count;
 };
 
-// fp32c batches spread the table kernel's per-node evaluations over
-// GNODE_CTAS CTAs per cosmology (grad_nodes_kernel) and hand them over in
+// fp32c batches run the table kernel's per-node evaluations in
+// grad_nodes_kernel (one node per thread) and hand them over in
 // the table kernel's shared-memory layout: chi right-hand sides at nodes and
 // midpoints [2][NDIR + 1][NCHI], growth coefficients [4][NDIR + 1][NGROW],
 // the Romberg integrand [NDIR + 1][NROMB], then exp(n_s ln k) T(k)^2 on the
@@ -213,8 +223,6 @@ constexpr int GNODE_QR = 2 * (NDIR + 1) * NCHI;
 constexpr int GNODE_FR = GNODE_QR + 4 * (NDIR + 1) * NGROW;
 constexpr int GNODE_U = GNODE_FR + (NDIR + 1) * NROMB;
 constexpr size_t GNODE_STRIDE = (size_t)(GNODE_U + (NDIR + 1) * NKH + 31) / 32 * 32;
-constexpr int GNODE_WORK = NCHI + (NCHI - 1) + NGROW + (NGROW - 1) + NROMB + NKH;  // 1152
-constexpr int GNODE_CTAS = (GNODE_WORK + 127) / 128;
 
 __device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
   if (gb.listed) return gb.items[i];

@@ -93,6 +93,8 @@ struct ConstTables {
       grow_iam_ff[NGROW];
   double chi_ida[NCHI];        // 1 / (atab_chi[i + 1] - atab_chi[i]) (i < NCHI - 1)
   double grow_ida[NGROW];      // 1 / (atab_grow[i + 1] - atab_grow[i]) (i < NGROW - 1)
+  float2 chi_ida_ff[NCHI], grow_ida_ff[NGROW], logr_ff[NRT];  // pair copies of the three above
+  float2 atab_chi_ff[NCHI];    // pair copy of atab_chi
 };
 
 // ------------------------------------------------- per-cosmology tables -----

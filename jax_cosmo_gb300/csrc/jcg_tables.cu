@@ -190,7 +190,10 @@ __global__ void const_ff_kernel(ConstTables* c) {
     c->chi_lnam_ff[i] = f2_of(c->chi_lnam[i]);
     c->chi_iam_ff[i] = f2_of(c->chi_iam[i]);
     c->chi_ida[i] = i < NCHI - 1 ? 1.0 / (c->atab_chi[i + 1] - c->atab_chi[i]) : 0.0;
+    c->chi_ida_ff[i] = f2_of(c->chi_ida[i]);
+    c->atab_chi_ff[i] = f2_of(c->atab_chi[i]);
   }
+  for (int j = tid; j < NRT; j += nth) c->logr_ff[j] = f2_of(c->logr[j]);
   for (int i = tid; i < NGROW; i += nth) {
     c->grow_a_ff[i] = f2_of(c->atab_grow[i]);
     c->grow_lna_ff[i] = f2_of(c->grow_lna[i]);
@@ -199,6 +202,7 @@ __global__ void const_ff_kernel(ConstTables* c) {
     c->grow_lnam_ff[i] = f2_of(c->grow_lnam[i]);
     c->grow_iam_ff[i] = f2_of(c->grow_iam[i]);
     c->grow_ida[i] = i < NGROW - 1 ? 1.0 / (c->atab_grow[i + 1] - c->atab_grow[i]) : 0.0;
+    c->grow_ida_ff[i] = f2_of(c->grow_ida[i]);
   }
 }
 

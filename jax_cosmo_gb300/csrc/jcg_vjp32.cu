@@ -168,10 +168,12 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
     if (!FWD)
       for (int l = tid; l < lt; l += VJ_THREADS) {
         const int ell = l0 + l;
-#pragma unroll 4
-        for (int p = 0; p < n_cls; ++p) {
-          const float ef = EF32[(size_t)geo->pair_i[p] * n_ell + ell] * EF32[(size_t)geo->pair_j[p] * n_ell + ell];
-          vS[p * TS + l] = (float)gi.vbar[(size_t)p * n_ell + ell] * ef;
+        // the pairs in the geometry's order: (i, j >= i) row by row
+        int p = 0;
+        for (int i = 0; i < n_tr; ++i) {
+          const float efi = EF32[(size_t)i * n_ell + ell];
+          for (int j = i; j < n_tr; ++j, ++p)
+            vS[p * TS + l] = (float)gi.vbar[(size_t)p * n_ell + ell] * (efi * EF32[(size_t)j * n_ell + ell]);
         }
       }
   };
@@ -179,13 +181,17 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   cp_async_wait_all();
   __syncthreads();
   // M_p(a) = u K_i K_j, the operation order of grad_limber32
-  for (int i = tid; i < tc * n_cls; i += VJ_THREADS) {
-    const int t = i / n_cls, p = i - t * n_cls;
-    const float* Ki = Ks + ((size_t)t * n_tr + geo->pair_i[p]) * (NDIR + 1);
-    const float* Kj = Ks + ((size_t)t * n_tr + geo->pair_j[p]) * (NDIR + 1);
-    const float m = R[(size_t)t * NROWG + F_U] * (Ki[0] * Kj[0]);
-    Mv[i] = m;
-    MT[p * VJ_TA + t] = m;
+  // (one thread per (a node, first tracer i); pair p = (i, j >= i))
+  for (int q = tid; q < tc * n_tr; q += VJ_THREADS) {
+    const int t = q / n_tr, i = q - t * n_tr;
+    const float* Kt = Ks + (size_t)t * n_tr * (NDIR + 1);
+    const float u = R[(size_t)t * NROWG + F_U], ki = Kt[i * (NDIR + 1)];
+    int p = i * n_tr - (i * (i - 1)) / 2;
+    for (int j = i; j < n_tr; ++j, ++p) {
+      const float m = u * (ki * Kt[j * (NDIR + 1)]);
+      Mv[t * n_cls + p] = m;
+      MT[p * VJ_TA + t] = m;
+    }
   }
   EHg eh;
   eh.qinv = ev[0]; eh.lg2_qinv = ev[1]; eh.sh = ev[2]; eh.inv_sh = ev[3]; eh.c18bc = ev[4];
@@ -385,10 +391,13 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
       const float2* qv = Qd + (size_t)t * n_cls;
       const float* K = Ks + (size_t)t * n_tr * (NDIR + 1);
       FF kb{0.f, 0.f};
-      for (int p = 0; p < n_cls; ++p) {
-        const int pi = geo->pair_i[p], pj = geo->pair_j[p];
-        if (pi == i) kb = kb + FF{qv[p].x, qv[p].y} * K[pj * (NDIR + 1)];
-        if (pj == i) kb = kb + FF{qv[p].x, qv[p].y} * K[pi * (NDIR + 1)];
+      for (int j = 0; j < n_tr; ++j) {
+        const int lo = min(i, j), hi = max(i, j);
+        const int p = lo * n_tr - (lo * (lo - 1)) / 2 + (hi - lo);
+        const FF qp{qv[p].x, qv[p].y};
+        const float kj = K[j * (NDIR + 1)];
+        kb = kb + qp * kj;
+        if (j == i) kb = kb + qp * kj;  // both factors of the auto pair
       }
       gi.kbar[(size_t)i * na + a0 + t] = R[(size_t)t * NROWG + F_U] * kb.hi;
     }
@@ -416,11 +425,15 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
       const float u = row[F_U], du = tg[T_U * NDIR + d];
       const float2* q = Qd + (size_t)t * n_cls;
       FF sm{0.f, 0.f};
-      for (int p = 0; p < n_cls; ++p) {
-        const float* Ki = Ks + ((size_t)t * n_tr + geo->pair_i[p]) * (NDIR + 1);
-        const float* Kj = Ks + ((size_t)t * n_tr + geo->pair_j[p]) * (NDIR + 1);
-        const float dm = fmaf(du, Ki[0] * Kj[0], u * fmaf(Ki[1 + d], Kj[0], Ki[0] * Kj[1 + d]));
-        sm = sm + FF{q[p].x, q[p].y} * dm;
+      int p = 0;
+      for (int i = 0; i < n_tr; ++i) {
+        const float* Ki = Ks + ((size_t)t * n_tr + i) * (NDIR + 1);
+        const float ki0 = Ki[0], kid = Ki[1 + d];
+        for (int j = i; j < n_tr; ++j, ++p) {
+          const float* Kj = Ks + ((size_t)t * n_tr + j) * (NDIR + 1);
+          const float dm = fmaf(du, ki0 * Kj[0], u * fmaf(kid, Kj[0], ki0 * Kj[1 + d]));
+          sm = sm + FF{q[p].x, q[p].y} * dm;
+        }
       }
       gd += ffd(sm);
     }
@@ -651,9 +664,44 @@ __global__ void __launch_bounds__(256) grad_kernrev32_kernel(GradBatch gb) {
 constexpr int KU_PAD = 33;
 constexpr int KU_NODES = 32;  // nodes per CTA of the value kernel
 
-__host__ __device__ inline size_t ku_val_smem(int wn) { return sizeof(float) * 2 * (size_t)wn * KU_PAD; }
-__host__ __device__ inline size_t ku_rev_smem(int wn) {
-  return sizeof(float) * ((size_t)4 * wn * KU_PAD + (size_t)8 * KV_NODES * KU_PAD + 16 * KU_PAD);
+// a lensing point's record (segment query, offset, the NW weights) as float4s,
+// staged per warp in shared memory and read back by broadcast (fewer
+// shared-memory/shuffle operations per point than one shuffle per value)
+template <int NW>
+struct KuRec {
+  static constexpr int N4 = (NW + 2 + 3) / 4;
+};
+__host__ __device__ inline size_t ku_rec_bytes(int nw) { return sizeof(float4) * 8 * 32 * (size_t)((nw + 2 + 3) / 4); }
+__host__ __device__ inline size_t ku_val_smem(int wn, int nw) {
+  return ku_rec_bytes(nw) + sizeof(float) * 2 * (size_t)wn * KU_PAD;
+}
+__host__ __device__ inline size_t ku_rev_smem(int wn, int nw) {
+  return ku_rec_bytes(nw) + sizeof(float) * ((size_t)4 * wn * KU_PAD + (size_t)8 * KV_NODES * KU_PAD + 16 * KU_PAD);
+}
+template <int NW>
+__device__ __forceinline__ void ku_put_rec(float4* rec, int q, float dx, const float* w) {
+  float v[4 * KuRec<NW>::N4];
+  v[0] = __int_as_float(q);
+  v[1] = dx;
+#pragma unroll
+  for (int u = 0; u < NW; ++u) v[2 + u] = w[u];
+#pragma unroll
+  for (int u = NW + 2; u < 4 * KuRec<NW>::N4; ++u) v[u] = 0.f;
+#pragma unroll
+  for (int i = 0; i < KuRec<NW>::N4; ++i) rec[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+template <int NW>
+__device__ __forceinline__ void ku_get_rec(const float4* rec, int& q, float& dx, float* w) {
+  float v[4 * KuRec<NW>::N4];
+#pragma unroll
+  for (int i = 0; i < KuRec<NW>::N4; ++i) {
+    const float4 r = rec[i];
+    v[4 * i] = r.x, v[4 * i + 1] = r.y, v[4 * i + 2] = r.z, v[4 * i + 3] = r.w;
+  }
+  q = __float_as_int(v[0]);
+  dx = v[1];
+#pragma unroll
+  for (int u = 0; u < NW; ++u) w[u] = v[2 + u];
 }
 
 bool krev_uniform_ok(const GeoHeader& h) {
@@ -683,9 +731,10 @@ __global__ void __launch_bounds__(256) grad_kernval32u_kernel(GradBatch gb) {
   const int n0 = blockIdx.x * KU_NODES, c0 = blockIdx.y * 32;
   if (n0 >= na || c0 >= gb.n_items) return;
   const int wbase = gb.krev_wbase, wn = NCHI - wbase;
-  extern __shared__ float kv_smem[];
-  float* chiT = kv_smem;             // [wn][KU_PAD]
-  float* slT = kv_smem + wn * KU_PAD;  // [wn][KU_PAD]
+  extern __shared__ __align__(16) float kv_smem[];
+  float4* recs = reinterpret_cast<float4*>(kv_smem);  // [8][32][N4] point records
+  float* chiT = kv_smem + 4 * 8 * 32 * KuRec<NW>::N4;  // [wn][KU_PAD]
+  float* slT = chiT + wn * KU_PAD;   // [wn][KU_PAD]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   for (int idx = tid; idx < 32 * wn; idx += blockDim.x) {
     const int cc = idx / wn, i = idx % wn;
@@ -739,16 +788,21 @@ __global__ void __launch_bounds__(256) grad_kernval32u_kernel(GradBatch gb) {
 #pragma unroll
       for (int u = 0; u < NW; ++u) wv[u] = in ? Wb[u][row + jl] : 0.f;
       const int cnt = min(32, NZP - j0);
+      float4* recw = recs + warp * 32 * KuRec<NW>::N4;
+      ku_put_rec<NW>(recw + lane * KuRec<NW>::N4, qv, dxv, wv);
+      __syncwarp();
       for (int jj = 0; jj < cnt; ++jj) {
-        const int q = __shfl_sync(0xffffffffu, qv, jj);
-        const float dx = __shfl_sync(0xffffffffu, dxv, jj);
+        int q;
+        float dx, w[NW];
+        ku_get_rec<NW>(recw + jj * KuRec<NW>::N4, q, dx, w);
         const float chip =
             fmaxf(chiT[((q & 0xffff) - wbase) * KU_PAD + lane] + slT[((q >> 16) - wbase) * KU_PAD + lane] * dx, 0.f);
         const float diff = chip - chi_wl;
         const float r = diff > 0.f ? diff * rcpf(fmaxf(chip, 1.f)) : 0.f;
 #pragma unroll
-        for (int u = 0; u < NW; ++u) acc[u] = fmaf(__shfl_sync(0xffffffffu, wv[u], jj), r, acc[u]);
+        for (int u = 0; u < NW; ++u) acc[u] = fmaf(w[u], r, acc[u]);
       }
+      __syncwarp();
     }
     if (live) {
       const float fac = cff * (float)(1.0 + Z[n]);
@@ -812,8 +866,9 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
   if (n0 >= na || c0 >= gb.n_items) return;
   const int n_end = min(na, n0 + KV_NODES);
   const int wbase = gb.krev_wbase, wn = NCHI - wbase;
-  extern __shared__ float kr_smem[];
-  float* chiT = kr_smem;                        // [wn][KU_PAD]
+  extern __shared__ __align__(16) float kr_smem[];
+  float4* recs = reinterpret_cast<float4*>(kr_smem);  // [8][32][N4] point records
+  float* chiT = kr_smem + 4 * 8 * 32 * KuRec<NW>::N4;  // [wn][KU_PAD]
   float* slT = chiT + wn * KU_PAD;              // [wn][KU_PAD]
   float* cN = slT + wn * KU_PAD;                // [wn][KU_PAD]
   float* sB = cN + wn * KU_PAD;                 // [wn][KU_PAD]
@@ -900,13 +955,17 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
       for (int u = 0; u < NW; ++u) wv[u] = own ? Wb[u][row + jl] : 0.f;
       const int qn = __shfl_down_sync(0xffffffffu, qv, 1);
       const unsigned ends = __ballot_sync(0xffffffffu, own && (lane == jf + cnt - 1 || qn != qv));
+      float4* recw = recs + warp * 32 * KuRec<NW>::N4;
+      if (own) ku_put_rec<NW>(recw + lane * KuRec<NW>::N4, qv, dxv, wv);
+      __syncwarp();
       for (int k = 0; k < cnt; ++k) {
         const int jj = jf + k;
-        const int q = __shfl_sync(0xffffffffu, qv, jj);
-        const float dx = __shfl_sync(0xffffffffu, dxv, jj);
+        int q;
+        float dx, w[NW];
+        ku_get_rec<NW>(recw + jj * KuRec<NW>::N4, q, dx, w);
         float sw = 0.f;  // sum_t Kbar_t (1 + m_t) W_tj
 #pragma unroll
-        for (int u = 0; u < NW; ++u) sw = fmaf(kb[u], __shfl_sync(0xffffffffu, wv[u], jj), sw);
+        for (int u = 0; u < NW; ++u) sw = fmaf(kb[u], w[u], sw);
         const float chip =
             fmaxf(chiT[((q & 0xffff) - wbase) * KU_PAD + lane] + slT[((q >> 16) - wbase) * KU_PAD + lane] * dx, 0.f);
         const float diff = chip - chi_wl;
@@ -922,6 +981,7 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
         }
         if ((ends >> jj) & 1u) flush(q);  // warp-uniform
       }
+      __syncwarp();
     }
     lacc = fmaf(cjf, lk, lacc);
     cwS[(warp * KV_NODES + (n - n0)) * KU_PAD + lane] = craw_w > 0.f ? fac * cwa : 0.f;
@@ -960,12 +1020,12 @@ template <int NW>
 static void launch_ku(const GradBatch& gb, cudaStream_t st, bool rev) {
   const int wn = NCHI - gb.krev_wbase;
   if (rev) {
-    const size_t smem = ku_rev_smem(wn);
+    const size_t smem = ku_rev_smem(wn, NW);
     cudaFuncSetAttribute(grad_kernrev32u_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid(kv_chunks(gb.na), (gb.n_items + 31) / 32);
     grad_kernrev32u_kernel<NW><<<grid, 256, smem, st>>>(gb);
   } else {
-    const size_t smem = ku_val_smem(wn);
+    const size_t smem = ku_val_smem(wn, NW);
     cudaFuncSetAttribute(grad_kernval32u_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     dim3 grid((gb.na + KU_NODES - 1) / KU_NODES, (gb.n_items + 31) / 32);
     grad_kernval32u_kernel<NW><<<grid, 256, smem, st>>>(gb);
