@@ -54,24 +54,57 @@ BOX = {
 }
 ORDER = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
 # Per-cosmology figures of the fp32c step's kernels on this workload (na = 513
-# Limber nodes, 5 WL tracers, 100 ell), from ncu captures at 512 cosmologies
-# (profiles/fp32c_step_kernels_b512.md; the Limber kernel's and the table
-# kernels' figures from the later captures in the same file), divided by 512:
-#   FP64 operations = DFMA x 2 + DADD + DMUL thread instructions (the
-#     cosmo_tables stage is cosmo_scalars_kernel + cosmo_tables_kernel);
+# Limber nodes, 5 WL tracers, 100 ell), from ncu captures at 2048 cosmologies
+# (working sets above L2), one kernel per capture
+# (profiles/fp32c_kernels_b2048_per_kernel.md), divided by 2048:
+#   warp instructions issued (sm__inst_executed); the table stage is
+#     cosmo_scalars_kernel + cosmo_tables_kernel;
+#   FP64 operations = DFMA x 2 + DADD + DMUL thread instructions;
 #   traffic = dram__bytes_read.sum + dram__bytes_write.sum;
-#   per Limber node (512 x 100 x 513 nodes): XU (MUFU) thread operations and
-#     warp instructions issued (sm__inst_executed) of limber32_kernel.
-FP64_OPS = {"cosmo_tables": 234_482, "halofit_rows": 83_620}
-TRAFFIC_PER_COSMO = {"cosmo_tables": 2_108, "halofit_rows": 44_141, "tracer_kernels": 9_679, "limber": 121_380}
+#   per Limber node (100 x 513 per cosmology): XU (MUFU) thread operations
+#     and warp instructions of limber32_kernel.
+WARP_INSTR_PER_COSMO = {"cosmo_tables": 1_983 + 78_961, "halofit_rows": 89_616, "tracer_kernels": 134_702}
+FP64_OPS = {"cosmo_tables": 14_262 + 26_177, "halofit_rows": 28_215}
+TRAFFIC_PER_COSMO = {"cosmo_tables": 94 + 28_018, "halofit_rows": 157_294, "tracer_kernels": 5_940, "limber": 129_634}
 MUFU_PER_NODE = 17.37
 WARP_INSTR_PER_NODE = 8.196
 # algorithmic bytes per cosmology: what each kernel must read and write once
 #   cosmo_tables: 8 parameters in, the CosmoTab record out (55,040 B)
-#   halofit_rows: the CosmoTab record in, FP64 + FP32 rows out (513 x (24 x 8 + 16 x 4))
+#   halofit_rows: the CosmoTab record in, FP64 + FP32 rows out (513 x (7 x 8 + 16 x 4))
+#   tracer_kernels: the FP32 chi table and slopes in (2 x 256 x 4), 5 kernels out (5 x 513 x 8)
 #   limber: FP32 rows (16 x 4) + u (8) + 5 radial kernels (5 x 8) per node in, 15 x 100 C_ell out
-ALG_BYTES = {"cosmo_tables": 64 + 55_040, "halofit_rows": 55_040 + 513 * (24 * 8 + 16 * 4),
+ALG_BYTES = {"cosmo_tables": 64 + 55_040, "halofit_rows": 55_040 + 513 * (7 * 8 + 16 * 4),
+             "tracer_kernels": 2 * 256 * 4 + 5 * 513 * 8,
              "limber": 513 * (16 * 4 + 8) + 5 * 513 * 8 + 15 * N_ELL * 8}
+# the fp32c vector-Jacobian product's stages (jcg_calib_vjp_stages masks) and
+# their per-cosmology figures from the same captures: warp instructions,
+# traffic, and algorithmic bytes (inputs read once, outputs written once,
+# scratch excluded):
+#   tables: parameters in; the TabD record (122,944 B) and the Taylor tables
+#     (206,592 B) out.  Kernels: grad_scalars, grad_nodes<0..2>, grad_tables,
+#     grad_moments32;
+#   rows: TabD's float copies, P(k) and Taylor tables in (245,152 B), rows
+#     out (513 x 132 x 4);
+#   kernels: the chi table in (2 x 256 x 4), 5 radial kernels with 8 zero
+#     tangents out (5 x 513 x 9 x 4).  grad_kernval32u;
+#   product: rows, radial kernels, cotangent and Eisenstein-Hu inputs in;
+#     C_ell, the shear kernels' cotangents and the chunk gradients out.
+#     grad_vjp32 (the dominant kernel: 23.66 warp instructions and 44.4 MUFU
+#     operations per Limber node);
+#   reverse: the shear cotangents and the chi table's tangents in, the chunk
+#     gradients out.  kernrev_owner, grad_kernrev32u, vjp_grad_reduce.
+VJP_STAGES = (("tables", 1), ("rows", 2), ("kernels", 4), ("product", 8), ("reverse", 16))
+VJP_WARP_INSTR_PER_COSMO = {"tables": 3_788 + 10_076 + 6_714 + 40_181 + 30_021 + 69_596, "rows": 155_894,
+                            "kernels": 122_648, "product": 1_213_587, "reverse": 94 + 300_726 + 112}
+VJP_TRAFFIC_PER_COSMO = {"tables": 240 + 10_609 + 10_022 + 5_777 + 161_077 + 218_388, "rows": 492_652,
+                         "kernels": 98_331, "product": 490_850, "reverse": 260 + 21_395 + 3_206}
+VJP_ALG_BYTES = {"tables": 64 + 122_944 + 206_592, "rows": 245_152 + 513 * 132 * 4,
+                 "kernels": 2 * 256 * 4 + 5 * 513 * 9 * 4,
+                 "product": 513 * 132 * 4 + 5 * 513 * 9 * 4 + 15 * N_ELL * 8 + 416 + 15 * N_ELL * 8 + 5 * 513 * 4
+                 + 17 * 8 * 8,
+                 "reverse": 5 * 513 * 4 + 2 * 8 * 256 * 4 + 33 * 8 * 8}
+VJP_PRODUCT_WARP_INSTR_PER_NODE = 23.66
+VJP_PRODUCT_MUFU_PER_NODE = 44.4
 KERNEL_NAMES = {"cosmo_tables": "cosmo_scalars_kernel + cosmo_tables_kernel",
                 "halofit_rows": "halofit_rows_kernel<fp32c>",
                 "tracer_kernels": "tracer32_uniform_kernel<5>", "limber": "limber32_kernel<1>"}
@@ -351,8 +384,32 @@ def gpu_arm(args, rank, world, device):
     g32, c32v = vjp_device(p64, ell_np, probes, vb[:64], 512, "fp32c", want_cl=True)
     gref = torch.einsum("bpl,bpld->bd", vb[:64], j64)
     gscale = torch.einsum("bpl,bpld->bd", vb[:64].abs(), j64.abs())
+    # each stage of the fp32c product alone (jcg_calib_vjp_stages on a workspace
+    # a full call filled), for the per-kernel rooflines
+    import ctypes
+
+    gv_, geov_, _ = _geometry.get_geometry(probes, ell_np, 512, device, 0)
+    wszv = ctypes.c_size_t()
+    _lib.call("jcg_vjp_workspace_size", ctypes.byref(gv_), B, _lib.FP32C, ctypes.byref(wszv))
+    wsv = _lib.workspace(wszv.value, device)
+    grad_v = torch.empty(B, 8, dtype=torch.float64, device=device)
+    cl_v = torch.empty(B, n_cls, n_ell, dtype=torch.float64, device=device)
+    stv = _lib.stream_of(device)
+
+    def vstage(mask):
+        _lib.call("jcg_calib_vjp_stages", ctypes.byref(gv_), _lib.ptr(geov_), _lib.ptr(params), B, _lib.ptr(vb),
+                  _lib.ptr(cl_v), _lib.ptr(grad_v), _lib.ptr(wsv), ctypes.c_size_t(wsv.numel()), ctypes.c_uint(mask),
+                  stv)
+
+    vstage(31)
+    vjp_stages = {}
+    for name, mask in VJP_STAGES:
+        t, _ = timed(lambda m=mask: vstage(m), kv, 1)
+        vjp_stages[name] = t / kv
+    del wsv
     res["jacobian"]["fp32c_vjp"] = {
         "batch": B, "ms_per_step": tv / kv, "steps": kv, "cl_grad_per_s": ncl_step / (tv / kv * 1e-3),
+        "stages_ms": vjp_stages, "rooflines": vjp_rooflines(vjp_stages, B, {"sm_count": torch.cuda.get_device_properties(device).multi_processor_count, "clocks": clk}),
         "what": "C_ell and the gradient of a scalar of C_ell (vector-Jacobian product with a seeded cotangent; "
                 "the Jacobian is not formed)",
         "grad_max_err_vs_fp64": float(((g32 - gref).abs() / gscale).max()),
@@ -624,6 +681,11 @@ def measure_peaks(device):
                                    "iteration, SMs x 8 blocks x 256 threads, CUDA events"}
 
 
+def _issue_peak(res):
+    mhz = (res.get("clocks") or {}).get("sm_mhz") or 2070.0
+    return 4 * res.get("sm_count", 152) * mhz * 1e6
+
+
 def rooflines(res, B, live):
     """Per-kernel rooflines of the fp32c step; the dominant kernel first."""
     peaks = {}
@@ -633,6 +695,7 @@ def rooflines(res, B, live):
         pass
     hbm = peaks.get("hbm_gbs", 6800.0)
     stages = res["stages_ms"]
+    peak_issue = _issue_peak(res)
     out = {}
     for k, ms in stages.items():
         t = ms * 1e-3
@@ -644,13 +707,11 @@ def rooflines(res, B, live):
             e["traffic"] = TRAFFIC_PER_COSMO[k] * B
         if k in FP64_OPS:
             ach = FP64_OPS[k] * B / t / 1e12
-            e.update({"bound": "fp64", "achieved": ach, "peak": live["fp64_tflops"], "unit": "TFLOP/s",
-                      "frac": ach / live["fp64_tflops"], "peak_source": "measured live (calibration kernel)"})
-        elif k == "limber":
-            # issue-bound: every pipe below half busy, 66% of cycles issue
+            e["fp64"] = {"achieved": ach, "peak": live["fp64_tflops"], "unit": "TFLOP/s",
+                         "frac": ach / live["fp64_tflops"], "peak_source": "measured live (calibration kernel)"}
+        if k == "limber":
+            # issue-bound: every pipe below half busy
             nodes = B * N_ELL * 513
-            mhz = (res.get("clocks") or {}).get("sm_mhz") or 2070.0
-            peak_issue = 4 * res.get("sm_count", 152) * mhz * 1e6
             ach = nodes * WARP_INSTR_PER_NODE / t
             mufu = nodes * MUFU_PER_NODE / t
             e.update({"bound": "issue", "achieved": ach / 1e9, "peak": peak_issue / 1e9, "unit": "Gwarp-instr/s",
@@ -659,12 +720,42 @@ def rooflines(res, B, live):
                       "sfu": {"achieved_gmufu_s": mufu / 1e9, "peak_gmufu_s": live["mufu_per_s"] / 1e9,
                               "frac": mufu / live["mufu_per_s"], "mufu_per_node": MUFU_PER_NODE,
                               "peak_source": "measured live (calibration kernel)"}})
-        else:
-            e.update({"bound": "lsu", "note": "FP32 lensing integral, lanes over cosmologies; z' grid broadcast "
-                                              "by shuffles (LSU pipe 54% busy at 512 cosmologies)"})
+        elif k in WARP_INSTR_PER_COSMO:
+            ach = WARP_INSTR_PER_COSMO[k] * B / t
+            e.update({"bound": "issue", "achieved": ach / 1e9, "peak": peak_issue / 1e9, "unit": "Gwarp-instr/s",
+                      "frac": ach / peak_issue, "warp_instr_per_cosmology": WARP_INSTR_PER_COSMO[k],
+                      "peak_source": "4 warp instructions per SM per clock x SMs x sampled SM clock"})
         out[k] = e
     dom = max(stages, key=lambda k: stages[k])
     return dom, out
+
+
+def vjp_rooflines(stages_ms, B, res):
+    """Per-stage rooflines of the fp32c vector-Jacobian product (all bound by
+    instruction issue and latency; HBM fractions beside)."""
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    hbm = peaks.get("hbm_gbs", 6800.0)
+    peak_issue = _issue_peak(res)
+    out = {}
+    for k, ms in stages_ms.items():
+        t = ms * 1e-3
+        ach = VJP_WARP_INSTR_PER_COSMO[k] * B / t
+        e = {"ms": ms, "bound": "issue", "achieved": ach / 1e9, "peak": peak_issue / 1e9, "unit": "Gwarp-instr/s",
+             "frac": ach / peak_issue, "warp_instr_per_cosmology": VJP_WARP_INSTR_PER_COSMO[k],
+             "algorithmic_bytes_per_launch": VJP_ALG_BYTES[k] * B,
+             "hbm_frac": VJP_ALG_BYTES[k] * B / t / 1e9 / hbm, "traffic": VJP_TRAFFIC_PER_COSMO[k] * B}
+        if k == "product":
+            nodes = B * N_ELL * 513
+            e["warp_instr_per_node"] = VJP_PRODUCT_WARP_INSTR_PER_NODE
+            e["mufu_per_node"] = VJP_PRODUCT_MUFU_PER_NODE
+            e["kernel"] = "grad_vjp32_kernel<0, 0>"
+            e["gnodes_per_s"] = nodes / t / 1e9
+        out[k] = e
+    return out
 
 
 def main():

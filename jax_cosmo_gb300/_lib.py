@@ -135,6 +135,7 @@ SIGNATURES = {
     "jcg_dense_dot_sparse_dot_dense": [_P, _I, _P, _I, _I, _I, _P, _I, _P, _P, _P],
     "jcg_calib_peak_fp64": [_P, _I, _I, _P],
     "jcg_calib_peak_mufu": [_P, _I, _I, _P],
+    "jcg_calib_vjp_stages": [_PG, _P, _P, _I, _P, _P, _P, _P, _SZ, ctypes.c_uint, _P],
     "jcg_sparse_inv": [_P, _I, _I, _P, _P],
     "jcg_sparse_slogdet": [_P, _I, _I, _P, _P, _P, _P],
     "jcg_sparse_to_dense": [_P, _I, _I, _I, _P, _P],

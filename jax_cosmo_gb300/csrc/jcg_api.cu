@@ -863,9 +863,28 @@ extern "C" int jcg_vjp_workspace_size(const jcg_geometry* g, int n_cosmo, int pr
   return JCG_OK;
 }
 
+static int vjp_checked(const jcg_geometry* g, const void* geo, const double* params, int n_cosmo, int precision,
+                       int gamma_dir, const double* cl_bar, double* cl, double* grad, void* ws, size_t ws_bytes,
+                       cudaStream_t stream, unsigned stages);
+
 extern "C" int jcg_angular_cl_vjp(const jcg_geometry* g, const void* geo, const double* params, int n_cosmo,
                                   int precision, int gamma_dir, const double* cl_bar, double* cl, double* grad,
                                   void* ws, size_t ws_bytes, cudaStream_t stream) {
+  return vjp_checked(g, geo, params, n_cosmo, precision, gamma_dir, cl_bar, cl, grad, ws, ws_bytes, stream, GS_ALL);
+}
+
+// measurement tooling (jcg_calib.h): the fp32c pipeline's stages selected by
+// a mask, on a workspace that a full call filled
+extern "C" int jcg_calib_vjp_stages(const jcg_geometry* g, const void* geo, const double* params, int n_cosmo,
+                                    const double* cl_bar, double* cl, double* grad, void* ws, size_t ws_bytes,
+                                    unsigned stage_mask, cudaStream_t stream) {
+  if ((stage_mask & ~(unsigned)GS_ALL) != 0 || stage_mask == 0) return fail(JCG_ERR_ARG, "stage_mask = 0x%x", stage_mask);
+  return vjp_checked(g, geo, params, n_cosmo, JCG_FP32C, -1, cl_bar, cl, grad, ws, ws_bytes, stream, stage_mask);
+}
+
+static int vjp_checked(const jcg_geometry* g, const void* geo, const double* params, int n_cosmo, int precision,
+                       int gamma_dir, const double* cl_bar, double* cl, double* grad, void* ws, size_t ws_bytes,
+                       cudaStream_t stream, unsigned stages) {
   GeoHeader h;
   int rc = make_header(g, &h);
   if (rc) return rc;
@@ -882,7 +901,7 @@ extern "C" int jcg_angular_cl_vjp(const jcg_geometry* g, const void* geo, const 
   ConstTables* c = nullptr;
   if ((rc = const_tables(&c))) return rc;
   vjp_run(static_cast<const GeoHeader*>(geo), h, params, n_cosmo, precision, cl_bar, cl, grad, ws, c, stream,
-          gamma_dir);
+          gamma_dir, stages);
   return cuda_check("angular_cl_vjp");
 }
 

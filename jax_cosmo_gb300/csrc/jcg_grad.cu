@@ -1853,8 +1853,9 @@ __global__ void __launch_bounds__(32 * NDIR) grad_growth_gamma_kernel(GradBatch 
   }
 }
 
-void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t st) {
+void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t st, unsigned stages) {
   const size_t smt = grad_tables_smem();
+  if (stages & GS_TABLES) {
   if (gb.n_items <= GNODE_MAX_ITEMS)
     grad_scalars_warp_kernel<<<gb.n_items, 16 * NDIR, 0, st>>>(gb);
   else
@@ -1878,18 +1879,23 @@ void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t s
   }
   if (gb.precision == JCG_FP32C) grad_moments32_kernel<<<gb.n_items, NRT, 0, st>>>(gb, c);
   if (growth_gamma(gb.physics_or)) grad_growth_gamma_kernel<<<gb.n_items, 32 * NDIR, 0, st>>>(gb, c);
-  if (gb.precision == JCG_FP32C) {
-    dim3 grw((gb.na + GR32_THREADS - 1) / GR32_THREADS, gb.n_items);
-    grad_rows32_kernel<<<grw, GR32_THREADS, 0, st>>>(gb, c);
-  } else {
-    dim3 grw((gb.na + 31) / 32, gb.n_items);
-    grad_rows_kernel<<<grw, 256, 0, st>>>(gb, c);
   }
-  if (gb.precision == JCG_FP32C) {
-    launch_grad_kern32(gb, c, st);
-  } else {
-    dim3 gr((gb.na + 7) / 8, gb.n_items);
-    grad_kern_kernel<<<gr, 256, 0, st>>>(gb, c);
+  if (stages & GS_ROWS) {
+    if (gb.precision == JCG_FP32C) {
+      dim3 grw((gb.na + GR32_THREADS - 1) / GR32_THREADS, gb.n_items);
+      grad_rows32_kernel<<<grw, GR32_THREADS, 0, st>>>(gb, c);
+    } else {
+      dim3 grw((gb.na + 31) / 32, gb.n_items);
+      grad_rows_kernel<<<grw, 256, 0, st>>>(gb, c);
+    }
+  }
+  if (stages & GS_KERNELS) {
+    if (gb.precision == JCG_FP32C) {
+      launch_grad_kern32(gb, c, st);
+    } else {
+      dim3 gr((gb.na + 7) / 8, gb.n_items);
+      grad_kern_kernel<<<gr, 256, 0, st>>>(gb, c);
+    }
   }
 }
 
@@ -2032,6 +2038,7 @@ size_t vjp_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
   o += al256(sizeof(float) * (size_t)h.n_tr * h.na * n_cosmo);
   o += al256(sizeof(double) * (size_t)kv_chunks(h.na) * NDIR * n_cosmo);
   o += al256(sizeof(int) * 9 * (size_t)kv_chunks(h.na));
+  o += al256(sizeof(int) * 8 * (size_t)h.na);
   o += al256(sizeof(unsigned) * (size_t)n_cosmo);
   o += gnode_bytes(n_cosmo, precision);
   return o;
@@ -2039,7 +2046,7 @@ size_t vjp_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision) {
 
 void vjp_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, int precision,
              const double* vbar, double* cl, double* grad, void* ws, const ConstTables* c, cudaStream_t st,
-             int gamma_dir) {
+             int gamma_dir, unsigned stages) {
   char* base = static_cast<char*>(ws);
   const size_t per = (size_t)h.n_cls * h.n_ell;
   if (precision != JCG_FP32C) {
@@ -2078,6 +2085,8 @@ void vjp_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int
   o += al256(sizeof(double) * (size_t)kv_chunks(h.na) * NDIR * n_cosmo);
   gb.krev_owner = reinterpret_cast<int*>(base + o);
   o += al256(sizeof(int) * 9 * (size_t)kv_chunks(h.na));
+  gb.krev_ranges = reinterpret_cast<int*>(base + o);
+  o += al256(sizeof(int) * 8 * (size_t)h.na);
   gb.cl_count = reinterpret_cast<unsigned*>(base + o);
   o += al256(sizeof(unsigned) * (size_t)n_cosmo);
   gb.gnode = gnode_bytes(n_cosmo, precision) ? reinterpret_cast<double*>(base + o) : nullptr;
@@ -2095,15 +2104,15 @@ void vjp_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int
   gb.n_ell = h.n_ell;
   gb.n_split = 1;
   gb.physics_or = h.physics;
-  launch_grad_front(gb, c, st);
+  launch_grad_front(gb, c, st, stages);
   if (cl && vbar && grad) {
     // the caller's cotangent: one pass gives the partial C_ell and the product
     gb.vjp_cl = 1;
-    launch_vjp32_grad(gb, st);
+    launch_vjp32_grad(gb, st, stages);
     return;
   }
-  if (cl) launch_vjp32_cl(gb, st);
-  if (vbar && grad) launch_vjp32_grad(gb, st);
+  if (cl && (stages & GS_PRODUCT)) launch_vjp32_cl(gb, st);
+  if (vbar && grad) launch_vjp32_grad(gb, st, stages);
 }
 
 void grad_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, int precision,

@@ -203,6 +203,7 @@ struct GradBatch {
   // per-cosmology kernel stage still runs for them)
   int krev_u, krev_wbase, n_wl, kern_rest;
   int* krev_owner;
+  int* krev_ranges;  // [na][8] each warp's points of a node, jlo | jhi << 16
   // 1: the cotangent does not depend on C_ell (given by the caller), so the
   // product kernel also writes the chunks' partial C_ell (no forward pass)
   int vjp_cl;
@@ -280,19 +281,24 @@ static __device__ __noinline__ void bias_term_d1(const TabD* tb, const ConstTabl
   *kd = k.d[0];
 }
 
+// stages of the fp32c gradient pipeline (a mask selects some, for timing):
+// tables (scalars, node evaluations, tables, moments), rows, radial kernels,
+// the product kernel, the reverse lensing kernel with the gradient sum
+enum GradStage : unsigned { GS_TABLES = 1, GS_ROWS = 2, GS_KERNELS = 4, GS_PRODUCT = 8, GS_REVERSE = 16, GS_ALL = 31 };
+
 // FP32 compensated stages (jcg_grad32.cu)
 void launch_grad_kern32(const GradBatch& gb, const ConstTables* c, cudaStream_t st);
 void launch_grad_limber32(const GradBatch& gb, const ConstTables* c, cudaStream_t st);
 // vector-Jacobian product (jcg_vjp32.cu): C_ell of the items into their cl,
 // and the product with their cotangents vbar into their grad
 void launch_vjp32_cl(const GradBatch& gb, cudaStream_t st);
-void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st);
+void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st, unsigned stages = GS_ALL);
 // uniform reverse lensing: the shear kernels' values (lanes over cosmologies)
 void launch_kernval32u(const GradBatch& gb, cudaStream_t st);
 int krev_wbase(const GeoHeader& h);
 bool krev_uniform_ok(const GeoHeader& h);
 // tables, rows and radial kernels with tangents (the stages before Limber)
-void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t st);
+void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t st, unsigned stages = GS_ALL);
 int grad_limber32_tile(int n_ell, int n_cls);
 int grad_limber32_chunk(int n_cls);
 

@@ -741,12 +741,12 @@ size_t grad_listed_bytes(const GradReq* r, int n, int n_split, int precision, bo
 struct GradBatch;
 cudaError_t grad_run_listed(GradReq* r, int n, int n_split, int precision, void* ws, const ConstTables* c,
                             cudaStream_t st, bool vjp = false, GradBatch* gb_out = nullptr);
-void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st);
+void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st, unsigned stages);
 // vector-Jacobian product of angular_cl, uniform batch (jcg_grad.cu)
 size_t vjp_workspace_bytes(const GeoHeader& h, int n_cosmo, int precision);
 void vjp_run(const GeoHeader* geo, const GeoHeader& h, const double* params, int n_cosmo, int precision,
              const double* vbar, double* cl, double* grad, void* ws, const ConstTables* c, cudaStream_t st,
-             int gamma_dir);
+             int gamma_dir, unsigned stages = 31u);
 // host-to-device copy of a small host table through a pinned staging ring of
 // the calling thread (jcg_api.cu): returns without waiting for the stream
 cudaError_t stage_h2d(void* dst_dev, const void* src_host, size_t bytes, cudaStream_t st);

@@ -158,23 +158,25 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   const float* EF32 = geo_ptr<float>(geo, geo->off_ef32);
   // an ell tile's (l + 1/2) factors and, for the product, its cotangents
   // v_p(l) = vbar_p(l) ef_i(l) ef_j(l); the first tile while the copies fly
+  // (read-only loads, free to move past the shared-memory stores)
   auto fill_tile = [&](int l0, int lt) {
     for (int l = tid; l < lt; l += VJ_THREADS) {
-      const float4 k4 = KH4[l0 + l];
+      const float4 k4 = __ldg(KH4 + l0 + l);
       khv[l] = k4.x;
       lkhv[l] = k4.y;
       ikhv[l] = k4.z;
     }
     if (!FWD)
-      for (int l = tid; l < lt; l += VJ_THREADS) {
+      for (int w = tid; w < lt * n_tr; w += VJ_THREADS) {
+        // one thread per (ell, first tracer i); the pairs in the geometry's
+        // order: (i, j >= i) row by row
+        const int i = w / lt, l = w - i * lt;
         const int ell = l0 + l;
-        // the pairs in the geometry's order: (i, j >= i) row by row
-        int p = 0;
-        for (int i = 0; i < n_tr; ++i) {
-          const float efi = EF32[(size_t)i * n_ell + ell];
-          for (int j = i; j < n_tr; ++j, ++p)
-            vS[p * TS + l] = (float)gi.vbar[(size_t)p * n_ell + ell] * (efi * EF32[(size_t)j * n_ell + ell]);
-        }
+        const float efi = __ldg(EF32 + (size_t)i * n_ell + ell);
+        int p = i * n_tr - (i * (i - 1)) / 2;
+        for (int j = i; j < n_tr; ++j, ++p)
+          vS[p * TS + l] =
+              (float)__ldg(gi.vbar + (size_t)p * n_ell + ell) * (efi * __ldg(EF32 + (size_t)j * n_ell + ell));
       }
   };
   fill_tile(0, min(LT, n_ell));
@@ -821,7 +823,10 @@ __global__ void __launch_bounds__(256) grad_kernval32u_kernel(GradBatch gb) {
 // KV_NODES nodes: warp w takes the chunk's lensing points whose chi table
 // segment m lies in [b_w, b_{w+1}); the boundaries split the chunk's points
 // into near-equal eighths.  (Integer histogram: the same bounds every run.)
-__global__ void __launch_bounds__(256) kernrev_owner_kernel(const GeoHeader* geo, int* bounds) {
+// Also each warp's range of points [jlo, jhi) on every node of the chunk
+// (contiguous: the segment is monotone along a node's z' grid), packed
+// jlo | jhi << 16 into ranges[node][warp].
+__global__ void __launch_bounds__(256) kernrev_owner_kernel(const GeoHeader* geo, int* bounds, int* ranges) {
   const int chunk = blockIdx.x, na = geo->na;
   const int n0 = chunk * KV_NODES, n_end = min(na, n0 + KV_NODES);
   __shared__ int hist[NCHI];
@@ -841,6 +846,24 @@ __global__ void __launch_bounds__(256) kernrev_owner_kernel(const GeoHeader* geo
     }
     while (w < 8) b[w++] = NCHI;
     b[8] = NCHI;
+  }
+  __syncthreads();
+  // thread (node, warp): the warp's points on the node
+  const int* b = bounds + (size_t)chunk * 9;
+  for (int q = threadIdx.x; q < (n_end - n0) * 8; q += blockDim.x) {
+    const int nl = q >> 3, w = q & 7;
+    const int blo = b[w], bhi = b[w + 1];
+    const int32_t* row = Q32 + (size_t)nl * NZP;
+    int jlo = NZP, jhi = 0;
+    for (int j = 0; j < NZP; ++j) {
+      const int m = row[j] >> 16;
+      if (m >= blo && m < bhi) {
+        jlo = min(jlo, j);
+        jhi = j + 1;
+      }
+    }
+    if (jhi <= jlo) jlo = jhi = 0;
+    ranges[(size_t)(n0 + nl) * 8 + w] = jlo | (jhi << 16);
   }
 }
 
@@ -913,7 +936,7 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
   const float* Wb[NW];
 #pragma unroll
   for (int u = 0; u < NW; ++u) Wb[u] = geo_ptr<float>(geo, geo->off_W32[wl_t[u]]);
-  const int blo = gb.krev_owner[chunk * 9 + warp], bhi = gb.krev_owner[chunk * 9 + warp + 1];
+  const int bhi = gb.krev_owner[chunk * 9 + warp + 1];
   float rc = 0.f, rcd = 0.f;  // the current run's chi' cotangent, and times dx
   float lacc = 0.f;       // sum_n fac chi_w sum_j sw r  (the d ln cf sum)
   float bacc = 0.f;       // node bhi's cotangent from segment bhi - 1
@@ -940,15 +963,13 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
     for (int u = 0; u < NW; ++u) kb[u] = kbar[(size_t)wl_t[u] * na + n] * m1[u];
     const size_t row = (size_t)n * NZP;
     float lk = 0.f, cwa = 0.f;
-    for (int j0 = 0; j0 < NZP; j0 += 32) {
+    const int jr = gb.krev_ranges[(size_t)n * 8 + warp];
+    const int jlo = jr & 0xffff, jhi = jr >> 16;
+    for (int j0 = jlo; j0 < jhi; j0 += 32) {
       const int jl = j0 + lane;
-      const int qv = jl < NZP ? Q32b[row + jl] : -1;
-      const int mv = qv >> 16;  // -1 past the row's end
-      const unsigned mask = __ballot_sync(0xffffffffu, mv >= blo && mv < bhi);
-      if (!mask) continue;
-      // the segment falls along the row: a warp's points of a chunk are consecutive
-      const int jf = __ffs(mask) - 1, cnt = __popc(mask);
-      const bool own = (mask >> lane) & 1u;
+      const bool own = jl < jhi;
+      const int cnt = min(32, jhi - j0), jf = 0;
+      const int qv = own ? Q32b[row + jl] : -1;
       const float dxv = own ? DX32b[row + jl] : 0.f;
       float wv[NW];
 #pragma unroll
@@ -1080,11 +1101,14 @@ void launch_vjp32_cl(const GradBatch& gb, cudaStream_t st) {
 }
 
 // the product with the items' cotangents vbar into their grad
-void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st) {
-  if (gb.physics_or != 0) launch_vjp_t<true, false>(gb, st);
-  else launch_vjp_t<false, false>(gb, st);
+void launch_vjp32_grad(const GradBatch& gb, cudaStream_t st, unsigned stages) {
+  if (stages & GS_PRODUCT) {
+    if (gb.physics_or != 0) launch_vjp_t<true, false>(gb, st);
+    else launch_vjp_t<false, false>(gb, st);
+  }
+  if (!(stages & GS_REVERSE)) return;
   if (gb.vjp_rev && gb.krev_u) {
-    kernrev_owner_kernel<<<kv_chunks(gb.na), 256, 0, st>>>(gb.geo, gb.krev_owner);
+    kernrev_owner_kernel<<<kv_chunks(gb.na), 256, 0, st>>>(gb.geo, gb.krev_owner, gb.krev_ranges);
     launch_ku_nw(gb, st, true);
   } else if (gb.vjp_rev) {
     dim3 grid(kv_chunks(gb.na), gb.n_items);
