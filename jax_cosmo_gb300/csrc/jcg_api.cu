@@ -331,6 +331,7 @@ static Batch make_batch(const GeoHeader* h, const void* geo, const double* param
   b.max_tr = h ? h->n_tr : 0;
   b.n_wl = h ? h->n_wl : 0;
   b.n_wl_groups = h ? h->n_groups : 0;
+  b.chi_wbase = h ? krev_wbase(*h) : 0;
   b.special_bias = h ? h->special_bias : 0;
   b.has_delta = h ? h->has_delta : 0;
   b.physics = h ? h->physics : 0;

@@ -269,6 +269,7 @@ struct Batch {
   int precision;
   int max_na, max_ell, max_cls, max_tr;
   int n_wl, n_wl_groups;  // uniform form: WeakLensing tracers and lensing groups
+  int chi_wbase;          // uniform form: first chi table segment a Limber node or lensing point can fall in
   int special_bias;       // uniform form: IA or a redshift-dependent bias present
   int has_delta;          // uniform form: a single-plane WeakLensing n(z) present
   int physics;            // uniform form: JCG_PK_* | JCG_TF_*
@@ -716,6 +717,40 @@ void launch_geometry_build(const GeoHeader& h, double* geo, const double* pz, co
 void launch_nz_points(const GeoHeader& h, const double* z_nodes, double* out, cudaStream_t st);
 void launch_cosmo_tables(const Batch& b, const ConstTables* c, cudaStream_t st);
 void launch_halofit_rows(const Batch& b, const ConstTables* c, cudaStream_t st);
+// a lensing point's record (segment query, offset, the NW weights) as float4s,
+// staged per warp in shared memory and read back by broadcast (fewer
+// shared-memory/shuffle operations per point than one shuffle per value)
+template <int NW>
+struct KuRec {
+  static constexpr int N4 = (NW + 2 + 3) / 4;
+};
+__host__ __device__ inline size_t ku_rec_bytes(int nw) { return sizeof(float4) * 8 * 32 * (size_t)((nw + 2 + 3) / 4); }
+template <int NW>
+__device__ __forceinline__ void ku_put_rec(float4* rec, int q, float dx, const float* w) {
+  float v[4 * KuRec<NW>::N4];
+  v[0] = __int_as_float(q);
+  v[1] = dx;
+#pragma unroll
+  for (int u = 0; u < NW; ++u) v[2 + u] = w[u];
+#pragma unroll
+  for (int u = NW + 2; u < 4 * KuRec<NW>::N4; ++u) v[u] = 0.f;
+#pragma unroll
+  for (int i = 0; i < KuRec<NW>::N4; ++i) rec[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
+}
+template <int NW>
+__device__ __forceinline__ void ku_get_rec(const float4* rec, int& q, float& dx, float* w) {
+  float v[4 * KuRec<NW>::N4];
+#pragma unroll
+  for (int i = 0; i < KuRec<NW>::N4; ++i) {
+    const float4 r = rec[i];
+    v[4 * i] = r.x, v[4 * i + 1] = r.y, v[4 * i + 2] = r.z, v[4 * i + 3] = r.w;
+  }
+  q = __float_as_int(v[0]);
+  dx = v[1];
+#pragma unroll
+  for (int u = 0; u < NW; ++u) w[u] = v[2 + u];
+}
+
 void launch_tracer_kernels(const Batch& b, const ConstTables* c, cudaStream_t st);
 void launch_limber(const Batch& b, const ConstTables* c, int lt, cudaStream_t st);
 // derivatives (jcg_grad.cu)

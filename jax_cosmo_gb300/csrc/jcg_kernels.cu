@@ -158,10 +158,16 @@ __global__ void __launch_bounds__(TK_WARPS * 32)
 // FP32 lensing kernel for a batch sharing one geometry: lanes are 32
 // cosmologies, warps walk the nodes.  The cosmology-independent lensing grid of
 // a node (segments, offsets, n(z') weights) is the same for every lane, so it
-// is read once per 32 cosmologies; each lane reads its cosmology's chi table
-// from shared memory ([segment][cosmology], conflict-free).
+// is read once per 32 cosmologies, in coalesced chunks of 32 points staged as
+// point records in the warp's shared memory and read back by broadcast; each
+// lane reads its cosmology's chi table from shared memory ([segment][cosmology],
+// conflict-free), from the first segment a point can fall in (chi_wbase) on,
+// once per run of points with the same segment query.
 constexpr int TU_NODES = 32;
 constexpr int TU_PAD = 33;
+__host__ __device__ inline size_t tu_smem(int wn, int nw) {
+  return ku_rec_bytes(nw) + sizeof(float) * 2 * (size_t)wn * TU_PAD;
+}
 
 template <int NW>  // WeakLensing tracers (one lensing group)
 __global__ void __launch_bounds__(256)
@@ -171,18 +177,20 @@ __global__ void __launch_bounds__(256)
   const int n0 = blockIdx.x * TU_NODES;
   const int c0 = blockIdx.y * 32;
   if (n0 >= na || c0 >= bt.n_items) return;
-  extern __shared__ float tu_smem[];
-  float* chiT = tu_smem;               // [NCHI][TU_PAD]
-  float* slT = tu_smem + NCHI * TU_PAD;  // [NCHI][TU_PAD]
+  extern __shared__ __align__(16) float tu_sm[];
+  const int wbase = bt.chi_wbase, wn = NCHI - wbase;
+  float4* recs = reinterpret_cast<float4*>(tu_sm);    // [8][32][N4] point records
+  float* chiT = tu_sm + 4 * 8 * 32 * KuRec<NW>::N4;  // [wn][TU_PAD]
+  float* slT = chiT + wn * TU_PAD;                    // [wn][TU_PAD]
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  for (int idx = tid; idx < 32 * NCHI; idx += blockDim.x) {
-    const int cc = idx / NCHI, sidx = idx % NCHI;
+  for (int idx = tid; idx < 32 * wn; idx += blockDim.x) {
+    const int cc = idx / wn, sidx = idx % wn;
     const int ci = c0 + cc;
     float cv = 0.f, sv = 0.f;
     if (ci < bt.n_items) {
       const CosmoTab* ct = bt.ctab + ci;
-      cv = ct->chi32[sidx];
-      sv = ct->slope32[sidx];
+      cv = ct->chi32[wbase + sidx];
+      sv = ct->slope32[wbase + sidx];
     }
     chiT[sidx * TU_PAD + cc] = cv;
     slT[sidx * TU_PAD + cc] = sv;
@@ -211,10 +219,11 @@ __global__ void __launch_bounds__(256)
   }
   const int32_t* Q32b = geo_ptr<int32_t>(geo, geo->off_q32[0]);
   const float* DX32b = geo_ptr<float>(geo, geo->off_dx32[0]);
+  float4* recw = recs + warp * 32 * KuRec<NW>::N4;
   for (int n = n0 + warp; n < n_end; n += 8) {
     const int qw = QWL[n];
-    const float chi_wl =
-        fmaxf(chiT[(qw & 0xffff) * TU_PAD + lane] + slT[(qw >> 16) * TU_PAD + lane] * DXWL[n], 0.f);
+    const float chi_wl = fmaxf(
+        chiT[((qw & 0xffff) - wbase) * TU_PAD + lane] + slT[((qw >> 16) - wbase) * TU_PAD + lane] * DXWL[n], 0.f);
     float acc[NW];
 #pragma unroll
     for (int u = 0; u < NW; ++u) acc[u] = 0.f;
@@ -223,8 +232,8 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
     for (int u = 0; u < NW; ++u) Wr[u] = geo_ptr<float>(geo, geo->off_W32[wl_t[u]]) + row;
     // the node's lensing grid in chunks of 32 z' points: one coalesced load
-    // per lane, then broadcast point by point with shuffles (same order of
-    // accumulation as a plain loop over j)
+    // per lane, staged as records and read back point by point (same order
+    // of accumulation as a plain loop over j)
     for (int j0 = 0; j0 < NZP; j0 += 32) {
       const int jl = j0 + lane;
       const bool in = jl < NZP;
@@ -234,14 +243,25 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
       for (int u = 0; u < NW; ++u) wv[u] = in ? Wr[u][jl] : 0.f;
       const int cnt = min(32, NZP - j0);
+      ku_put_rec<NW>(recw + lane * KuRec<NW>::N4, qv, dxv, wv);
+      const int qp = __shfl_up_sync(0xffffffffu, qv, 1);
+      const unsigned starts = __ballot_sync(0xffffffffu, lane == 0 || qp != qv);
+      __syncwarp();
+      float cx = 0.f, sx = 0.f;  // chi[x], slope[m] of the current run
       for (int jj = 0; jj < cnt; ++jj) {
-        const int q = __shfl_sync(0xffffffffu, qv, jj);
-        const float dx = __shfl_sync(0xffffffffu, dxv, jj);
-        const float chip = fmaxf(chiT[(q & 0xffff) * TU_PAD + lane] + slT[(q >> 16) * TU_PAD + lane] * dx, 0.f);
+        int q;
+        float dx, w[NW];
+        ku_get_rec<NW>(recw + jj * KuRec<NW>::N4, q, dx, w);
+        if ((starts >> jj) & 1u) {  // warp-uniform
+          cx = chiT[((q & 0xffff) - wbase) * TU_PAD + lane];
+          sx = slT[((q >> 16) - wbase) * TU_PAD + lane];
+        }
+        const float chip = fmaxf(cx + sx * dx, 0.f);
         const float ratio = fmaxf(chip - chi_wl, 0.f) * rcp_approx(fmaxf(chip, 1.f));
 #pragma unroll
-        for (int u = 0; u < NW; ++u) acc[u] += __shfl_sync(0xffffffffu, wv[u], jj) * ratio;
+        for (int u = 0; u < NW; ++u) acc[u] += w[u] * ratio;
       }
+      __syncwarp();
     }
     if (live) {
       const double z = Z[n];
@@ -263,7 +283,7 @@ __global__ void __launch_bounds__(256)
 
 template <int NW>
 static void launch_tu(const Batch& b, const ConstTables* c, cudaStream_t st) {
-  const size_t smem = 2 * NCHI * TU_PAD * sizeof(float);
+  const size_t smem = tu_smem(NCHI - b.chi_wbase, NW);
   cudaFuncSetAttribute(tracer32_uniform_kernel<NW>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)smem);
   dim3 grid((b.max_na + TU_NODES - 1) / TU_NODES, (b.n_items + 31) / 32);

@@ -666,46 +666,12 @@ __global__ void __launch_bounds__(256) grad_kernrev32_kernel(GradBatch gb) {
 constexpr int KU_PAD = 33;
 constexpr int KU_NODES = 32;  // nodes per CTA of the value kernel
 
-// a lensing point's record (segment query, offset, the NW weights) as float4s,
-// staged per warp in shared memory and read back by broadcast (fewer
-// shared-memory/shuffle operations per point than one shuffle per value)
-template <int NW>
-struct KuRec {
-  static constexpr int N4 = (NW + 2 + 3) / 4;
-};
-__host__ __device__ inline size_t ku_rec_bytes(int nw) { return sizeof(float4) * 8 * 32 * (size_t)((nw + 2 + 3) / 4); }
 __host__ __device__ inline size_t ku_val_smem(int wn, int nw) {
   return ku_rec_bytes(nw) + sizeof(float) * 2 * (size_t)wn * KU_PAD;
 }
 __host__ __device__ inline size_t ku_rev_smem(int wn, int nw) {
   return ku_rec_bytes(nw) + sizeof(float) * ((size_t)4 * wn * KU_PAD + (size_t)8 * KV_NODES * KU_PAD + 16 * KU_PAD);
 }
-template <int NW>
-__device__ __forceinline__ void ku_put_rec(float4* rec, int q, float dx, const float* w) {
-  float v[4 * KuRec<NW>::N4];
-  v[0] = __int_as_float(q);
-  v[1] = dx;
-#pragma unroll
-  for (int u = 0; u < NW; ++u) v[2 + u] = w[u];
-#pragma unroll
-  for (int u = NW + 2; u < 4 * KuRec<NW>::N4; ++u) v[u] = 0.f;
-#pragma unroll
-  for (int i = 0; i < KuRec<NW>::N4; ++i) rec[i] = make_float4(v[4 * i], v[4 * i + 1], v[4 * i + 2], v[4 * i + 3]);
-}
-template <int NW>
-__device__ __forceinline__ void ku_get_rec(const float4* rec, int& q, float& dx, float* w) {
-  float v[4 * KuRec<NW>::N4];
-#pragma unroll
-  for (int i = 0; i < KuRec<NW>::N4; ++i) {
-    const float4 r = rec[i];
-    v[4 * i] = r.x, v[4 * i + 1] = r.y, v[4 * i + 2] = r.z, v[4 * i + 3] = r.w;
-  }
-  q = __float_as_int(v[0]);
-  dx = v[1];
-#pragma unroll
-  for (int u = 0; u < NW; ++u) w[u] = v[2 + u];
-}
-
 bool krev_uniform_ok(const GeoHeader& h) {
   return !h.custom_nodes && h.n_wl >= 1 && h.n_wl <= 8 && h.n_groups == 1 && !h.has_delta;
 }
@@ -713,7 +679,9 @@ bool krev_uniform_ok(const GeoHeader& h) {
 // first chi table segment (atab_chi = logspace(-3, 0, NCHI)) that a Limber
 // node or a lensing point can fall in, two segments of margin
 int krev_wbase(const GeoHeader& h) {
-  const double zm = fmax(h.zmax, h.group_zmax[0]);
+  if (h.custom_nodes) return 0;  // nodes at the caller's redshifts: the whole table
+  double zm = h.zmax;
+  for (int g = 0; g < h.n_groups; ++g) zm = fmax(zm, h.group_zmax[g]);
   const double t = (log10(1.0 / (1.0 + zm)) + 3.0) * (NCHI - 1) / 3.0;
   int w = (int)floor(t) - 2;
   if (!(t > 2.0)) w = 0;
@@ -792,13 +760,20 @@ __global__ void __launch_bounds__(256) grad_kernval32u_kernel(GradBatch gb) {
       const int cnt = min(32, NZP - j0);
       float4* recw = recs + warp * 32 * KuRec<NW>::N4;
       ku_put_rec<NW>(recw + lane * KuRec<NW>::N4, qv, dxv, wv);
+      // runs of equal segment query share chi[x] and slope[m]: read at a run's start
+      const int qp = __shfl_up_sync(0xffffffffu, qv, 1);
+      const unsigned starts = __ballot_sync(0xffffffffu, lane == 0 || qp != qv);
       __syncwarp();
+      float cx = 0.f, sx = 0.f;
       for (int jj = 0; jj < cnt; ++jj) {
         int q;
         float dx, w[NW];
         ku_get_rec<NW>(recw + jj * KuRec<NW>::N4, q, dx, w);
-        const float chip =
-            fmaxf(chiT[((q & 0xffff) - wbase) * KU_PAD + lane] + slT[((q >> 16) - wbase) * KU_PAD + lane] * dx, 0.f);
+        if ((starts >> jj) & 1u) {  // warp-uniform
+          cx = chiT[((q & 0xffff) - wbase) * KU_PAD + lane];
+          sx = slT[((q >> 16) - wbase) * KU_PAD + lane];
+        }
+        const float chip = fmaxf(cx + sx * dx, 0.f);
         const float diff = chip - chi_wl;
         const float r = diff > 0.f ? diff * rcpf(fmaxf(chip, 1.f)) : 0.f;
 #pragma unroll
@@ -976,9 +951,12 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
       for (int u = 0; u < NW; ++u) wv[u] = own ? Wb[u][row + jl] : 0.f;
       const int qn = __shfl_down_sync(0xffffffffu, qv, 1);
       const unsigned ends = __ballot_sync(0xffffffffu, own && (lane == jf + cnt - 1 || qn != qv));
+      const int qp = __shfl_up_sync(0xffffffffu, qv, 1);
+      const unsigned starts = __ballot_sync(0xffffffffu, own && (lane == jf || qp != qv));
       float4* recw = recs + warp * 32 * KuRec<NW>::N4;
       if (own) ku_put_rec<NW>(recw + lane * KuRec<NW>::N4, qv, dxv, wv);
       __syncwarp();
+      float cx = 0.f, sx = 0.f;  // chi[x], slope[m] of the current run
       for (int k = 0; k < cnt; ++k) {
         const int jj = jf + k;
         int q;
@@ -987,8 +965,11 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
         float sw = 0.f;  // sum_t Kbar_t (1 + m_t) W_tj
 #pragma unroll
         for (int u = 0; u < NW; ++u) sw = fmaf(kb[u], w[u], sw);
-        const float chip =
-            fmaxf(chiT[((q & 0xffff) - wbase) * KU_PAD + lane] + slT[((q >> 16) - wbase) * KU_PAD + lane] * dx, 0.f);
+        if ((starts >> jj) & 1u) {  // warp-uniform
+          cx = chiT[((q & 0xffff) - wbase) * KU_PAD + lane];
+          sx = slT[((q >> 16) - wbase) * KU_PAD + lane];
+        }
+        const float chip = fmaxf(cx + sx * dx, 0.f);
         const float diff = chip - chi_wl;
         if (diff > 0.f) {  // then the chi' clip is inactive too
           const float ic = rcpf(fmaxf(chip, 1.f));
