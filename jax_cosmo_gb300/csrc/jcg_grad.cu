@@ -871,15 +871,24 @@ __device__ __forceinline__ FF8 interp_ff8(FF x, const float2* xp, const float2* 
   return f0 + (f1 - f0) * (inv * (x - f2ff(xp[sg.x])));
 }
 
-constexpr int GR32_THREADS = 64;
+constexpr int GR32_THREADS = 256;  // nodes of one cosmology per CTA (its tables shared in L1)
 
-__global__ void __launch_bounds__(GR32_THREADS, 8) grad_rows32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
-  const int item = blockIdx.y;
+// Uniform batches: one flat index over (cosmology, node), so that no CTA is
+// left with a node or two of a cosmology (na = 2^k + 1); listed: a 2-D grid.
+__global__ void __launch_bounds__(GR32_THREADS, 2) grad_rows32_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+  int item, n;
+  if (!gb.listed) {
+    const long long idx = (long long)blockIdx.x * GR32_THREADS + threadIdx.x;
+    item = (int)(idx / gb.na);
+    n = (int)(idx - (long long)item * gb.na);
+  } else {
+    item = blockIdx.y;
+    n = blockIdx.x * GR32_THREADS + threadIdx.x;
+  }
   if (item >= gb.n_items) return;
   const GradItem gi = grad_item(gb, item);
   const GeoHeader* geo = gi.geo;
   const int na = geo->na;
-  const int n = blockIdx.x * GR32_THREADS + threadIdx.x;
   if (n >= na) return;
   const TabD* tb = gi.tab;
   const double* A = geo_ptr<double>(geo, geo->off_a);
@@ -1882,7 +1891,8 @@ void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t s
   }
   if (stages & GS_ROWS) {
     if (gb.precision == JCG_FP32C) {
-      dim3 grw((gb.na + GR32_THREADS - 1) / GR32_THREADS, gb.n_items);
+      const dim3 grw = gb.listed ? dim3((gb.na + GR32_THREADS - 1) / GR32_THREADS, gb.n_items)
+                                 : dim3((unsigned)(((long long)gb.na * gb.n_items + GR32_THREADS - 1) / GR32_THREADS));
       grad_rows32_kernel<<<grw, GR32_THREADS, 0, st>>>(gb, c);
     } else {
       dim3 grw((gb.na + 31) / 32, gb.n_items);

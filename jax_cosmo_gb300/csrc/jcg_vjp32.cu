@@ -49,6 +49,7 @@ __host__ __device__ inline int vj_stride(int LT) { return LT + (40 - LT % 32) % 
 
 struct VjLayout {
   size_t ev, kh, rows, ks, mv, mt, vs, pt, ws, abar, qd, red, total;
+  size_t rows_b, ks_b;  // the second buffer of each (the next chunk's copies)
 };
 __host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT) {
   VjLayout L;
@@ -61,8 +62,14 @@ __host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT) {
   o = (o + 15) & ~(size_t)15;
   L.rows = o;                                 // [VJ_TA][NROWG]
   o += 4 * (size_t)VJ_TA * NROWG;
+  L.rows_b = o;
+  o += 4 * (size_t)VJ_TA * NROWG;
   L.ks = o;                                   // [VJ_TA][n_tr][NDIR + 1]
   o += 4 * (size_t)VJ_TA * n_tr * (NDIR + 1);
+  o = (o + 15) & ~(size_t)15;
+  L.ks_b = o;
+  o += 4 * (size_t)VJ_TA * n_tr * (NDIR + 1);
+  o = (o + 15) & ~(size_t)15;
   L.mv = o;                                   // [VJ_TA][n_cls]
   o += 4 * (size_t)VJ_TA * n_cls;
   o = (o + 15) & ~(size_t)15;
@@ -98,19 +105,21 @@ __device__ __forceinline__ void cp_async4(void* s, const void* g) {
                : "memory");
 }
 __device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;\n" ::: "memory"); }
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+// wait for all committed groups but the most recent one
+__device__ __forceinline__ void cp_async_wait_prior() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
 
 // GEN: some item may use a non-default operator point (as grad_limber32).
 // FWD: the forward form (partial C_ell of the chunk, no cotangent).
 template <bool GEN, bool FWD>
-__global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb, int LT) {
-  const int item = blockIdx.y, chunk = blockIdx.x;
+__global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb, int LT, int G) {
+  const int item = blockIdx.y;
   if (item >= gb.n_items) return;
   const GradItem gi = grad_item(gb, item);
   const GeoHeader* geo = gi.geo;
   const int n_ell = geo->n_ell, n_cls = geo->n_cls, na = geo->na, n_tr = geo->n_tr;
   const int nch = vjp_chunks(na), tav = vjp_tav(na);
-  if (chunk >= nch) return;
-  const int a0 = chunk * tav, tc = min(tav, na - a0);
+  if ((int)blockIdx.x >= nch) return;
   const bool lin = pk_model(geo->physics) == JCG_PK_LINEAR;
   const bool nw = GEN && tf_nowiggle(geo->physics);
   const VjLayout L = vj_layout(n_tr, n_cls, LT);
@@ -120,8 +129,10 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   float* khv = reinterpret_cast<float*>(vj_smem + L.kh);
   float* lkhv = khv + LT;
   float* ikhv = lkhv + LT;
-  float* R = reinterpret_cast<float*>(vj_smem + L.rows);
-  float* Ks = reinterpret_cast<float*>(vj_smem + L.ks);
+  float* const R0 = reinterpret_cast<float*>(vj_smem + L.rows);
+  float* const R1 = reinterpret_cast<float*>(vj_smem + L.rows_b);
+  float* const K0 = reinterpret_cast<float*>(vj_smem + L.ks);
+  float* const K1 = reinterpret_cast<float*>(vj_smem + L.ks_b);
   float* Mv = reinterpret_cast<float*>(vj_smem + L.mv);
   float* MT = reinterpret_cast<float*>(vj_smem + L.mt);
   float* vS = reinterpret_cast<float*>(vj_smem + L.vs);
@@ -134,31 +145,36 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   double* gred = reinterpret_cast<double*>(vj_smem + ((L.red + 4 * (VJ_THREADS / 32) * NET + 15) & ~(size_t)15));
   const int tid = threadIdx.x, grp = tid >> 3, sub = tid & (VJ_GROUP - 1);
   const TabD* tb = gi.tab;
-  // the Eisenstein-Hu inputs and their tangents (formed once per cosmology
-  // by the table stage), the chunk's FP32 rows (values and tangents) and
-  // radial kernels: asynchronous copies
-  for (int i = tid; i < 16; i += VJ_THREADS) cp_async4(ev + i, tb->ehv + i);
-  if (!FWD)
-    for (int i = tid; i < NET * NDIR; i += VJ_THREADS) cp_async4(et + i, tb->eht + i);
-  {
-    const float* src = gi.rowg + (size_t)a0 * NROWG;
-    for (int i = tid; i < tc * (NROWG / 4); i += VJ_THREADS) cp_async16(R + 4 * i, src + 4 * i);
+  // a chunk's FP32 rows (values and tangents) and radial kernels into buffer
+  // b: asynchronous copies (one commit group per chunk)
+  auto copy_chunk = [&](int ch, int b) {
+    const int c0 = ch * tav, cc = min(tav, na - c0);
+    const float* src = gi.rowg + (size_t)c0 * NROWG;
+    float* R = b ? R1 : R0;
+    for (int i = tid; i < cc * (NROWG / 4); i += VJ_THREADS) cp_async16(R + 4 * i, src + 4 * i);
     // K rows [t][tracer][NDIR + 1]: consecutive threads on consecutive nodes
-    for (int i = tid; i < tc * n_tr; i += VJ_THREADS) {
-      const int tr = i / tc, t = i - tr * tc;
-      const float* ks = gi.kernf + ((size_t)tr * na + a0 + t) * (NDIR + 1);
-      float* kd = Ks + ((size_t)t * n_tr + tr) * (NDIR + 1);
+    float* K = b ? K1 : K0;
+    for (int i = tid; i < cc * n_tr; i += VJ_THREADS) {
+      const int tr = i / cc, t = i - tr * cc;
+      const float* ks = gi.kernf + ((size_t)tr * na + c0 + t) * (NDIR + 1);
+      float* kd = K + ((size_t)t * n_tr + tr) * (NDIR + 1);
 #pragma unroll
       for (int k = 0; k < NDIR + 1; ++k) cp_async4(kd + k, ks + k);
     }
-  }
+  };
+  // the Eisenstein-Hu inputs and their tangents (formed once per cosmology
+  // by the table stage) and the first chunk's rows
+  for (int i = tid; i < 16; i += VJ_THREADS) cp_async4(ev + i, tb->ehv + i);
   if (!FWD)
-    for (int i = tid; i < tc * n_cls; i += VJ_THREADS) Qd[i] = make_float2(0.f, 0.f);
+    for (int i = tid; i < NET * NDIR; i += VJ_THREADS) cp_async4(et + i, tb->eht + i);
+  copy_chunk(blockIdx.x, 0);
+  cp_async_commit();
   const float4* KH4 = geo_ptr<float4>(geo, geo->off_kh4);
   const float* EF32 = geo_ptr<float>(geo, geo->off_ef32);
   // an ell tile's (l + 1/2) factors and, for the product, its cotangents
-  // v_p(l) = vbar_p(l) ef_i(l) ef_j(l); the first tile while the copies fly
-  // (read-only loads, free to move past the shared-memory stores)
+  // v_p(l) = vbar_p(l) ef_i(l) ef_j(l); with one tile, once per CTA while the
+  // first copies fly (read-only loads, free to move past the shared-memory
+  // stores)
   auto fill_tile = [&](int l0, int lt) {
     for (int l = tid; l < lt; l += VJ_THREADS) {
       const float4 k4 = __ldg(KH4 + l0 + l);
@@ -179,279 +195,297 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
               (float)__ldg(gi.vbar + (size_t)p * n_ell + ell) * (efi * __ldg(EF32 + (size_t)j * n_ell + ell));
       }
   };
-  fill_tile(0, min(LT, n_ell));
-  cp_async_wait_all();
-  __syncthreads();
-  // M_p(a) = u K_i K_j, the operation order of grad_limber32
-  // (one thread per (a node, first tracer i); pair p = (i, j >= i))
-  for (int q = tid; q < tc * n_tr; q += VJ_THREADS) {
-    const int t = q / n_tr, i = q - t * n_tr;
-    const float* Kt = Ks + (size_t)t * n_tr * (NDIR + 1);
-    const float u = R[(size_t)t * NROWG + F_U], ki = Kt[i * (NDIR + 1)];
-    int p = i * n_tr - (i * (i - 1)) / 2;
-    for (int j = i; j < n_tr; ++j, ++p) {
-      const float m = u * (ki * Kt[j * (NDIR + 1)]);
-      Mv[t * n_cls + p] = m;
-      MT[p * VJ_TA + t] = m;
+  const bool one_tile = n_ell <= LT;
+  if (one_tile) fill_tile(0, n_ell);
+  // the CTA's chunks blockIdx.x, blockIdx.x + G, ...: the next chunk's rows
+  // are copied while this one runs
+  for (int chunk = blockIdx.x, it = 0; chunk < nch; chunk += G, ++it) {
+    const int buf = it & 1;
+    float* R = buf ? R1 : R0;
+    float* Ks = buf ? K1 : K0;
+    if (chunk + G < nch) copy_chunk(chunk + G, buf ^ 1);
+    cp_async_commit();
+    cp_async_wait_prior();  // every group but the one just committed
+    if (!one_tile) fill_tile(0, min(LT, n_ell));
+    const int a0 = chunk * tav, tc = min(tav, na - a0);
+    if (!FWD)
+      for (int i = tid; i < tc * n_cls; i += VJ_THREADS) Qd[i] = make_float2(0.f, 0.f);
+    __syncthreads();
+    // M_p(a) = u K_i K_j, the operation order of grad_limber32
+    // (one thread per (a node, first tracer i); pair p = (i, j >= i))
+    for (int q = tid; q < tc * n_tr; q += VJ_THREADS) {
+      const int t = q / n_tr, i = q - t * n_tr;
+      const float* Kt = Ks + (size_t)t * n_tr * (NDIR + 1);
+      const float u = R[(size_t)t * NROWG + F_U], ki = Kt[i * (NDIR + 1)];
+      int p = i * n_tr - (i * (i - 1)) / 2;
+      for (int j = i; j < n_tr; ++j, ++p) {
+        const float m = u * (ki * Kt[j * (NDIR + 1)]);
+        Mv[t * n_cls + p] = m;
+        MT[p * VJ_TA + t] = m;
+      }
     }
-  }
-  EHg eh;
-  eh.qinv = ev[0]; eh.lg2_qinv = ev[1]; eh.sh = ev[2]; eh.inv_sh = ev[3]; eh.c18bc = ev[4];
-  eh.c142ac = ev[5]; eh.alpha_b = ev[6]; eh.beta_b = ev[7]; eh.beta_node = ev[8]; eh.lg2_ksilk = ev[9];
-  eh.fb = ev[10]; eh.fc = ev[11]; eh.ns3 = ev[12]; eh.inv_keq = ev[13];
-  eh.agam = ev[14]; eh.nwq = ev[15];
-  float accA[T_U], accE[NET];
+    EHg eh;
+    eh.qinv = ev[0]; eh.lg2_qinv = ev[1]; eh.sh = ev[2]; eh.inv_sh = ev[3]; eh.c18bc = ev[4];
+    eh.c142ac = ev[5]; eh.alpha_b = ev[6]; eh.beta_b = ev[7]; eh.beta_node = ev[8]; eh.lg2_ksilk = ev[9];
+    eh.fb = ev[10]; eh.fc = ev[11]; eh.ns3 = ev[12]; eh.inv_keq = ev[13];
+    eh.agam = ev[14]; eh.nwq = ev[15];
+    float accA[T_U], accE[NET];
 #pragma unroll
-  for (int j = 0; j < T_U; ++j) accA[j] = 0.f;
+    for (int j = 0; j < T_U; ++j) accA[j] = 0.f;
 #pragma unroll
-  for (int j = 0; j < NET; ++j) accE[j] = 0.f;
-  for (int l0 = 0; l0 < n_ell; l0 += LT) {
-    const int lt = min(LT, n_ell - l0);
-    if (l0 > 0) {
-      __syncthreads();  // the previous tile's Pt / vS are consumed
-      fill_tile(l0, lt);
-    }
-    __syncthreads();  // the tile's factors and cotangents (first tile: and M)
-    const int L4 = (lt + 3) >> 2;
-    if (!FWD) {
-      // W(t, l) = sum_p M_p(t) v_p(l) in 4 x 4 blocks (rows past tc and
-      // columns past lt are not read)
-      for (int w = tid; w < (VJ_TA / 4) * L4; w += VJ_THREADS) {
-        const int tb = w / L4, lq = (w - tb * L4) * 4, t0 = tb * 4;
-        float4 a[4];
+    for (int j = 0; j < NET; ++j) accE[j] = 0.f;
+    for (int l0 = 0; l0 < n_ell; l0 += LT) {
+      const int lt = min(LT, n_ell - l0);
+      if (l0 > 0) {
+        __syncthreads();  // the previous tile's Pt / vS are consumed
+        fill_tile(l0, lt);
+      }
+      __syncthreads();  // the tile's factors and cotangents (first tile: and M)
+      const int L4 = (lt + 3) >> 2;
+      if (!FWD) {
+        // W(t, l) = sum_p M_p(t) v_p(l) in 4 x 4 blocks (rows past tc and
+        // columns past lt are not read)
+        for (int w = tid; w < (VJ_TA / 4) * L4; w += VJ_THREADS) {
+          const int tb = w / L4, lq = (w - tb * L4) * 4, t0 = tb * 4;
+          float4 a[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) a[i] = make_float4(0.f, 0.f, 0.f, 0.f);
-        for (int p = 0; p < n_cls; ++p) {
-          const float4 m = *reinterpret_cast<const float4*>(MT + p * VJ_TA + t0);
-          const float4 v = *reinterpret_cast<const float4*>(vS + p * TS + lq);
-          const float mm[4] = {m.x, m.y, m.z, m.w};
+          for (int i = 0; i < 4; ++i) a[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+          for (int p = 0; p < n_cls; ++p) {
+            const float4 m = *reinterpret_cast<const float4*>(MT + p * VJ_TA + t0);
+            const float4 v = *reinterpret_cast<const float4*>(vS + p * TS + lq);
+            const float mm[4] = {m.x, m.y, m.z, m.w};
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            a[i].x = fmaf(mm[i], v.x, a[i].x);
-            a[i].y = fmaf(mm[i], v.y, a[i].y);
-            a[i].z = fmaf(mm[i], v.z, a[i].z);
-            a[i].w = fmaf(mm[i], v.w, a[i].w);
+            for (int i = 0; i < 4; ++i) {
+              a[i].x = fmaf(mm[i], v.x, a[i].x);
+              a[i].y = fmaf(mm[i], v.y, a[i].y);
+              a[i].z = fmaf(mm[i], v.z, a[i].z);
+              a[i].w = fmaf(mm[i], v.w, a[i].w);
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i) *reinterpret_cast<float4*>(Ws + (t0 + i) * TS + lq) = a[i];
+        }
+        __syncthreads();
+      }
+      if (grp < tc) {
+        const int t = grp;
+        const float* row = R + (size_t)t * NROWG;
+        for (int l = sub; l < lt; l += VJ_GROUP) {
+          float an[NGT], ae[NET];
+          const float P = !GEN ? node32_fb_default(eh, row, khv[l], lkhv[l], ikhv[l], an, ae)
+                          : nw ? node32_fb_nw(eh, row, khv[l], lkhv[l], ikhv[l], an, ae, lin)
+                               : node32_fb<true>(eh, row, khv[l], lkhv[l], ikhv[l], an, ae, lin);
+          Pt[t * TS + l] = P;
+          if (!FWD) {
+            const float W = Ws[t * TS + l];
+#pragma unroll
+            for (int j = 0; j < T_U; ++j) {
+              if (!GEN && j == T_MUN) continue;  // mu_n = 0 for takahashi2012
+              accA[j] = fmaf(W, an[j], accA[j]);
+            }
+#pragma unroll
+            for (int j = 0; j < NET; ++j) accE[j] = fmaf(W, ae[j], accE[j]);
           }
         }
-#pragma unroll
-        for (int i = 0; i < 4; ++i) *reinterpret_cast<float4*>(Ws + (t0 + i) * TS + lq) = a[i];
       }
       __syncthreads();
-    }
-    if (grp < tc) {
-      const int t = grp;
-      const float* row = R + (size_t)t * NROWG;
-      for (int l = sub; l < lt; l += VJ_GROUP) {
-        float an[NGT], ae[NET];
-        const float P = !GEN ? node32_fb_default(eh, row, khv[l], lkhv[l], ikhv[l], an, ae)
-                        : nw ? node32_fb_nw(eh, row, khv[l], lkhv[l], ikhv[l], an, ae, lin)
-                             : node32_fb<true>(eh, row, khv[l], lkhv[l], ikhv[l], an, ae, lin);
-        Pt[t * TS + l] = P;
-        if (!FWD) {
-          const float W = Ws[t * TS + l];
-#pragma unroll
-          for (int j = 0; j < T_U; ++j) {
-            if (!GEN && j == T_MUN) continue;  // mu_n = 0 for takahashi2012
-            accA[j] = fmaf(W, an[j], accA[j]);
+      if (FWD || gb.vjp_cl) {
+        // partial C_p(l) of the chunk: sum_t M_p(t) P(t, l), t in order, in
+        // blocks of 2 spectra x 4 ell
+        float* cp = gi.cpart + (size_t)chunk * n_cls * n_ell;
+        const int P2 = (n_cls + 1) >> 1;
+        for (int w = tid; w < P2 * L4; w += VJ_THREADS) {
+          const int pb = w / L4, lq = (w - pb * L4) * 4, p0 = pb * 2;
+          const bool two = p0 + 1 < n_cls;
+          float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = c0;
+          for (int t = 0; t < tc; ++t) {
+            const float4 pt = *reinterpret_cast<const float4*>(Pt + t * TS + lq);
+            const float m0 = Mv[t * n_cls + p0], m1 = two ? Mv[t * n_cls + p0 + 1] : 0.f;
+            c0.x = fmaf(pt.x, m0, c0.x), c0.y = fmaf(pt.y, m0, c0.y), c0.z = fmaf(pt.z, m0, c0.z), c0.w = fmaf(pt.w, m0, c0.w);
+            c1.x = fmaf(pt.x, m1, c1.x), c1.y = fmaf(pt.y, m1, c1.y), c1.z = fmaf(pt.z, m1, c1.z), c1.w = fmaf(pt.w, m1, c1.w);
           }
+          const float r0[4] = {c0.x, c0.y, c0.z, c0.w}, r1[4] = {c1.x, c1.y, c1.z, c1.w};
 #pragma unroll
-          for (int j = 0; j < NET; ++j) accE[j] = fmaf(W, ae[j], accE[j]);
+          for (int k = 0; k < 4; ++k) {
+            if (lq + k >= lt) break;
+            cp[(size_t)p0 * n_ell + l0 + lq + k] = r0[k];
+            if (two) cp[(size_t)(p0 + 1) * n_ell + l0 + lq + k] = r1[k];
+          }
         }
       }
-    }
-    __syncthreads();
-    if (FWD || gb.vjp_cl) {
-      // partial C_p(l) of the chunk: sum_t M_p(t) P(t, l), t in order, in
-      // blocks of 2 spectra x 4 ell
-      float* cp = gi.cpart + (size_t)chunk * n_cls * n_ell;
-      const int P2 = (n_cls + 1) >> 1;
-      for (int w = tid; w < P2 * L4; w += VJ_THREADS) {
-        const int pb = w / L4, lq = (w - pb * L4) * 4, p0 = pb * 2;
-        const bool two = p0 + 1 < n_cls;
-        float4 c0 = make_float4(0.f, 0.f, 0.f, 0.f), c1 = c0;
-        for (int t = 0; t < tc; ++t) {
-          const float4 pt = *reinterpret_cast<const float4*>(Pt + t * TS + lq);
-          const float m0 = Mv[t * n_cls + p0], m1 = two ? Mv[t * n_cls + p0 + 1] : 0.f;
-          c0.x = fmaf(pt.x, m0, c0.x), c0.y = fmaf(pt.y, m0, c0.y), c0.z = fmaf(pt.z, m0, c0.z), c0.w = fmaf(pt.w, m0, c0.w);
-          c1.x = fmaf(pt.x, m1, c1.x), c1.y = fmaf(pt.y, m1, c1.y), c1.z = fmaf(pt.z, m1, c1.z), c1.w = fmaf(pt.w, m1, c1.w);
-        }
-        const float r0[4] = {c0.x, c0.y, c0.z, c0.w}, r1[4] = {c1.x, c1.y, c1.z, c1.w};
+      if (!FWD) {
+        // Q_p(t) += sum_l v_p(l) P(t, l): blocks of 4 a nodes x 4 spectra
+        // (p = 16 g + b + 4 k), each summed over 8 ell slices in FP32 and the
+        // slices added by shuffles, then added to Q in float-pair arithmetic
+        const int NPG = (n_cls + 15) >> 4;
+        for (int w = tid; w < (VJ_THREADS) * NPG; w += VJ_THREADS) {
+          const int pg = w / VJ_THREADS, r = w - pg * VJ_THREADS;
+          const int slice = r & 7, blk = r >> 3, t0 = (blk >> 2) * 4, pb = blk & 3;
+          int pk[4];
 #pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          if (lq + k >= lt) break;
-          cp[(size_t)p0 * n_ell + l0 + lq + k] = r0[k];
-          if (two) cp[(size_t)(p0 + 1) * n_ell + l0 + lq + k] = r1[k];
-        }
-      }
-    }
-    if (!FWD) {
-      // Q_p(t) += sum_l v_p(l) P(t, l): blocks of 4 a nodes x 4 spectra
-      // (p = 16 g + b + 4 k), each summed over 8 ell slices in FP32 and the
-      // slices added by shuffles, then added to Q in float-pair arithmetic
-      const int NPG = (n_cls + 15) >> 4;
-      for (int w = tid; w < (VJ_THREADS) * NPG; w += VJ_THREADS) {
-        const int pg = w / VJ_THREADS, r = w - pg * VJ_THREADS;
-        const int slice = r & 7, blk = r >> 3, t0 = (blk >> 2) * 4, pb = blk & 3;
-        int pk[4];
-#pragma unroll
-        for (int k = 0; k < 4; ++k) pk[k] = pg * 16 + pb + 4 * k;
-        float acc[4][4];
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int k = 0; k < 4; ++k) acc[i][k] = 0.f;
-        for (int l = slice; l < lt; l += 8) {
-          float pt[4], v[4];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) pt[i] = Pt[(t0 + i) * TS + l];
-#pragma unroll
-          for (int k = 0; k < 4; ++k) v[k] = pk[k] < n_cls ? vS[pk[k] * TS + l] : 0.f;
+          for (int k = 0; k < 4; ++k) pk[k] = pg * 16 + pb + 4 * k;
+          float acc[4][4];
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int k = 0; k < 4; ++k) acc[i][k] = fmaf(pt[i], v[k], acc[i][k]);
-        }
+            for (int k = 0; k < 4; ++k) acc[i][k] = 0.f;
+          for (int l = slice; l < lt; l += 8) {
+            float pt[4], v[4];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+            for (int i = 0; i < 4; ++i) pt[i] = Pt[(t0 + i) * TS + l];
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            float x = acc[i][k];
-            x += __shfl_xor_sync(0xffffffffu, x, 4);
-            x += __shfl_xor_sync(0xffffffffu, x, 2);
-            x += __shfl_xor_sync(0xffffffffu, x, 1);
-            acc[i][k] = x;
+            for (int k = 0; k < 4; ++k) v[k] = pk[k] < n_cls ? vS[pk[k] * TS + l] : 0.f;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+              for (int k = 0; k < 4; ++k) acc[i][k] = fmaf(pt[i], v[k], acc[i][k]);
           }
-        if (slice == 0) {
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
             for (int k = 0; k < 4; ++k) {
-              const int t = t0 + i, p = pk[k];
-              if (t < tc && p < n_cls) {
-                const int q = t * n_cls + p;
-                const FF sq = FF{Qd[q].x, Qd[q].y} + acc[i][k];
-                Qd[q] = make_float2(sq.hi, sq.lo);
-              }
+              float x = acc[i][k];
+              x += __shfl_xor_sync(0xffffffffu, x, 4);
+              x += __shfl_xor_sync(0xffffffffu, x, 2);
+              x += __shfl_xor_sync(0xffffffffu, x, 1);
+              acc[i][k] = x;
             }
+          if (slice == 0) {
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+              for (int k = 0; k < 4; ++k) {
+                const int t = t0 + i, p = pk[k];
+                if (t < tc && p < n_cls) {
+                  const int q = t * n_cls + p;
+                  const FF sq = FF{Qd[q].x, Qd[q].y} + acc[i][k];
+                  Qd[q] = make_float2(sq.hi, sq.lo);
+                }
+              }
+          }
         }
       }
     }
-  }
-  if (FWD || gb.vjp_cl) {
-    // C_ell of the item once all its chunks are in: the last chunk CTA to
-    // finish adds the partials in chunk order (the same sum whichever CTA
-    // it is), times the ell factors, and resets the count
-    __shared__ int s_last;
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) s_last = atomicAdd(&gb.cl_count[item], 1u) == (unsigned)(nch - 1);
-    __syncthreads();
-    if (s_last && gi.cl) {
+    if (FWD || gb.vjp_cl) {
+      // C_ell of the item once all its chunks are in: the last chunk CTA to
+      // finish adds the partials in chunk order (the same sum whichever CTA
+      // it is), times the ell factors, and resets the count
+      __shared__ int s_last;
       __threadfence();
-      const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
-      const size_t per = (size_t)n_cls * n_ell;
-      for (int idx = tid; idx < (int)per; idx += VJ_THREADS) {
-        const int p = idx / n_ell, l = idx - p * n_ell;
-        double s = 0.0;
-        for (int c = 0; c < nch; ++c) s += (double)__ldcg(gi.cpart + (size_t)c * per + idx);
-        gi.cl[idx] = s * EF[(size_t)geo->pair_i[p] * n_ell + l] * EF[(size_t)geo->pair_j[p] * n_ell + l];
-      }
-    }
-    if (s_last && tid == 0) gb.cl_count[item] = 0;
-  }
-  if (FWD) return;
-  // adjoints of the node inputs: summed over the a node's 8 lanes; those of
-  // the cosmology's Eisenstein-Hu inputs over the CTA
-#pragma unroll
-  for (int j = 0; j < T_U; ++j) {
-    float v = accA[j];
-    v += __shfl_xor_sync(0xffffffffu, v, 4);
-    v += __shfl_xor_sync(0xffffffffu, v, 2);
-    v += __shfl_xor_sync(0xffffffffu, v, 1);
-    if (sub == 0 && grp < tc) Abar[grp * NGT + j] = v;
-  }
-  const int warp = tid >> 5, lane = tid & 31;
-#pragma unroll
-  for (int j = 0; j < NET; ++j) {
-    float v = accE[j];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) Ered[warp * NET + j] = v;
-  }
-  __syncthreads();
-  // the Eisenstein-Hu adjoints over the warps, one thread per input (float
-  // pairs), into the first row of Ered
-  FF ej{0.f, 0.f};
-  if (tid < NET)
-    for (int w = 0; w < VJ_THREADS / 32; ++w) ej = ej + Ered[w * NET + tid];
-  // reverse lensing: the cotangents of the WeakLensing shear kernels,
-  // Kbar_i(t) = u(t) sum_p Q_p(t) dK_i K_j / dK_i (both factors of an auto pair)
-  if (gb.vjp_rev)
-    for (int q = tid; q < tc * n_tr; q += VJ_THREADS) {
-      const int t = q / n_tr, i = q - t * n_tr;
-      if (geo->kind[i] != JCG_TRACER_WL || geo->nz_kind[i] == JCG_NZ_DELTA) continue;
-      const float2* qv = Qd + (size_t)t * n_cls;
-      const float* K = Ks + (size_t)t * n_tr * (NDIR + 1);
-      FF kb{0.f, 0.f};
-      for (int j = 0; j < n_tr; ++j) {
-        const int lo = min(i, j), hi = max(i, j);
-        const int p = lo * n_tr - (lo * (lo - 1)) / 2 + (hi - lo);
-        const FF qp{qv[p].x, qv[p].y};
-        const float kj = K[j * (NDIR + 1)];
-        kb = kb + qp * kj;
-        if (j == i) kb = kb + qp * kj;  // both factors of the auto pair
-      }
-      gi.kbar[(size_t)i * na + a0 + t] = R[(size_t)t * NROWG + F_U] * kb.hi;
-    }
-  __syncthreads();  // every read of Ered is done
-  if (tid < NET) {
-    Ered[2 * tid] = ej.hi;
-    Ered[2 * tid + 1] = ej.lo;
-  }
-  __syncthreads();
-  // projection on the tangents: thread (a node t, direction d)
-  {
-    const int t = tid >> 3, d = tid & 7;
-    double gd = 0.0;
-    if (t < tc) {
-      const float* row = R + (size_t)t * NROWG;
-      const float* tg = row + NROWV;
-      float s = 0.f;
-#pragma unroll
-      for (int j = 0; j < T_U; ++j) {
-        if (!GEN && j == T_MUN) continue;
-        s = fmaf(Abar[t * NGT + j], tg[j * NDIR + d], s);
-      }
-      gd = (double)s;
-      // sum_p Q_p (du K_i K_j + u (dK_i K_j + K_i dK_j)), in float pairs
-      const float u = row[F_U], du = tg[T_U * NDIR + d];
-      const float2* q = Qd + (size_t)t * n_cls;
-      FF sm{0.f, 0.f};
-      int p = 0;
-      for (int i = 0; i < n_tr; ++i) {
-        const float* Ki = Ks + ((size_t)t * n_tr + i) * (NDIR + 1);
-        const float ki0 = Ki[0], kid = Ki[1 + d];
-        for (int j = i; j < n_tr; ++j, ++p) {
-          const float* Kj = Ks + ((size_t)t * n_tr + j) * (NDIR + 1);
-          const float dm = fmaf(du, ki0 * Kj[0], u * fmaf(kid, Kj[0], ki0 * Kj[1 + d]));
-          sm = sm + FF{q[p].x, q[p].y} * dm;
+      __syncthreads();
+      if (tid == 0) s_last = atomicAdd(&gb.cl_count[item], 1u) == (unsigned)(nch - 1);
+      __syncthreads();
+      if (s_last && gi.cl) {
+        __threadfence();
+        const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
+        const size_t per = (size_t)n_cls * n_ell;
+        for (int idx = tid; idx < (int)per; idx += VJ_THREADS) {
+          const int p = idx / n_ell, l = idx - p * n_ell;
+          double s = 0.0;
+          for (int c = 0; c < nch; ++c) s += (double)__ldcg(gi.cpart + (size_t)c * per + idx);
+          gi.cl[idx] = s * EF[(size_t)geo->pair_i[p] * n_ell + l] * EF[(size_t)geo->pair_j[p] * n_ell + l];
         }
       }
-      gd += ffd(sm);
+      if (s_last && tid == 0) gb.cl_count[item] = 0;
     }
-    if (t == 0) {
-      // the cosmology's Eisenstein-Hu inputs, once per CTA
-      FF se{0.f, 0.f};
-      for (int j = 0; j < NET; ++j) se = se + FF{Ered[2 * j], Ered[2 * j + 1]} * et[j * NDIR + d];
-      gd += ffd(se);
+    if (FWD) {
+      __syncthreads();  // this chunk's buffers and scratch are free
+      continue;
     }
-    gred[t * NDIR + d] = gd;
-  }
-  __syncthreads();
-  if (tid < NDIR) {
-    double g = 0.0;
-    for (int t = 0; t < VJ_TA; ++t) g += gred[t * NDIR + tid];
-    gi.gpart[(size_t)chunk * NDIR + tid] = g;
+    // adjoints of the node inputs: summed over the a node's 8 lanes; those of
+    // the cosmology's Eisenstein-Hu inputs over the CTA
+#pragma unroll
+    for (int j = 0; j < T_U; ++j) {
+      float v = accA[j];
+      v += __shfl_xor_sync(0xffffffffu, v, 4);
+      v += __shfl_xor_sync(0xffffffffu, v, 2);
+      v += __shfl_xor_sync(0xffffffffu, v, 1);
+      if (sub == 0 && grp < tc) Abar[grp * NGT + j] = v;
+    }
+    const int warp = tid >> 5, lane = tid & 31;
+#pragma unroll
+    for (int j = 0; j < NET; ++j) {
+      float v = accE[j];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) Ered[warp * NET + j] = v;
+    }
+    __syncthreads();
+    // the Eisenstein-Hu adjoints over the warps, one thread per input (float
+    // pairs), into the first row of Ered
+    FF ej{0.f, 0.f};
+    if (tid < NET)
+      for (int w = 0; w < VJ_THREADS / 32; ++w) ej = ej + Ered[w * NET + tid];
+    // reverse lensing: the cotangents of the WeakLensing shear kernels,
+    // Kbar_i(t) = u(t) sum_p Q_p(t) dK_i K_j / dK_i (both factors of an auto pair)
+    if (gb.vjp_rev)
+      for (int q = tid; q < tc * n_tr; q += VJ_THREADS) {
+        const int t = q / n_tr, i = q - t * n_tr;
+        if (geo->kind[i] != JCG_TRACER_WL || geo->nz_kind[i] == JCG_NZ_DELTA) continue;
+        const float2* qv = Qd + (size_t)t * n_cls;
+        const float* K = Ks + (size_t)t * n_tr * (NDIR + 1);
+        FF kb{0.f, 0.f};
+        for (int j = 0; j < n_tr; ++j) {
+          const int lo = min(i, j), hi = max(i, j);
+          const int p = lo * n_tr - (lo * (lo - 1)) / 2 + (hi - lo);
+          const FF qp{qv[p].x, qv[p].y};
+          const float kj = K[j * (NDIR + 1)];
+          kb = kb + qp * kj;
+          if (j == i) kb = kb + qp * kj;  // both factors of the auto pair
+        }
+        gi.kbar[(size_t)i * na + a0 + t] = R[(size_t)t * NROWG + F_U] * kb.hi;
+      }
+    __syncthreads();  // every read of Ered is done
+    if (tid < NET) {
+      Ered[2 * tid] = ej.hi;
+      Ered[2 * tid + 1] = ej.lo;
+    }
+    __syncthreads();
+    // projection on the tangents: thread (a node t, direction d)
+    {
+      const int t = tid >> 3, d = tid & 7;
+      double gd = 0.0;
+      if (t < tc) {
+        const float* row = R + (size_t)t * NROWG;
+        const float* tg = row + NROWV;
+        float s = 0.f;
+#pragma unroll
+        for (int j = 0; j < T_U; ++j) {
+          if (!GEN && j == T_MUN) continue;
+          s = fmaf(Abar[t * NGT + j], tg[j * NDIR + d], s);
+        }
+        gd = (double)s;
+        // sum_p Q_p (du K_i K_j + u (dK_i K_j + K_i dK_j)), in float pairs
+        const float u = row[F_U], du = tg[T_U * NDIR + d];
+        const float2* q = Qd + (size_t)t * n_cls;
+        FF sm{0.f, 0.f};
+        int p = 0;
+        for (int i = 0; i < n_tr; ++i) {
+          const float* Ki = Ks + ((size_t)t * n_tr + i) * (NDIR + 1);
+          const float ki0 = Ki[0], kid = Ki[1 + d];
+          for (int j = i; j < n_tr; ++j, ++p) {
+            const float* Kj = Ks + ((size_t)t * n_tr + j) * (NDIR + 1);
+            const float dm = fmaf(du, ki0 * Kj[0], u * fmaf(kid, Kj[0], ki0 * Kj[1 + d]));
+            sm = sm + FF{q[p].x, q[p].y} * dm;
+          }
+        }
+        gd += ffd(sm);
+      }
+      if (t == 0) {
+        // the cosmology's Eisenstein-Hu inputs, once per CTA
+        FF se{0.f, 0.f};
+        for (int j = 0; j < NET; ++j) se = se + FF{Ered[2 * j], Ered[2 * j + 1]} * et[j * NDIR + d];
+        gd += ffd(se);
+      }
+      gred[t * NDIR + d] = gd;
+    }
+    __syncthreads();
+    if (tid < NDIR) {
+      double g = 0.0;
+      for (int t = 0; t < VJ_TA; ++t) g += gred[t * NDIR + tid];
+      gi.gpart[(size_t)chunk * NDIR + tid] = g;
+    }
+    __syncthreads();  // this chunk's buffers and scratch are free
   }
 }
 
@@ -760,20 +794,13 @@ __global__ void __launch_bounds__(256) grad_kernval32u_kernel(GradBatch gb) {
       const int cnt = min(32, NZP - j0);
       float4* recw = recs + warp * 32 * KuRec<NW>::N4;
       ku_put_rec<NW>(recw + lane * KuRec<NW>::N4, qv, dxv, wv);
-      // runs of equal segment query share chi[x] and slope[m]: read at a run's start
-      const int qp = __shfl_up_sync(0xffffffffu, qv, 1);
-      const unsigned starts = __ballot_sync(0xffffffffu, lane == 0 || qp != qv);
       __syncwarp();
-      float cx = 0.f, sx = 0.f;
       for (int jj = 0; jj < cnt; ++jj) {
         int q;
         float dx, w[NW];
         ku_get_rec<NW>(recw + jj * KuRec<NW>::N4, q, dx, w);
-        if ((starts >> jj) & 1u) {  // warp-uniform
-          cx = chiT[((q & 0xffff) - wbase) * KU_PAD + lane];
-          sx = slT[((q >> 16) - wbase) * KU_PAD + lane];
-        }
-        const float chip = fmaxf(cx + sx * dx, 0.f);
+        const float chip =
+            fmaxf(chiT[((q & 0xffff) - wbase) * KU_PAD + lane] + slT[((q >> 16) - wbase) * KU_PAD + lane] * dx, 0.f);
         const float diff = chip - chi_wl;
         const float r = diff > 0.f ? diff * rcpf(fmaxf(chip, 1.f)) : 0.f;
 #pragma unroll
@@ -951,12 +978,9 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
       for (int u = 0; u < NW; ++u) wv[u] = own ? Wb[u][row + jl] : 0.f;
       const int qn = __shfl_down_sync(0xffffffffu, qv, 1);
       const unsigned ends = __ballot_sync(0xffffffffu, own && (lane == jf + cnt - 1 || qn != qv));
-      const int qp = __shfl_up_sync(0xffffffffu, qv, 1);
-      const unsigned starts = __ballot_sync(0xffffffffu, own && (lane == jf || qp != qv));
       float4* recw = recs + warp * 32 * KuRec<NW>::N4;
       if (own) ku_put_rec<NW>(recw + lane * KuRec<NW>::N4, qv, dxv, wv);
       __syncwarp();
-      float cx = 0.f, sx = 0.f;  // chi[x], slope[m] of the current run
       for (int k = 0; k < cnt; ++k) {
         const int jj = jf + k;
         int q;
@@ -965,11 +989,8 @@ __global__ void __launch_bounds__(256) grad_kernrev32u_kernel(GradBatch gb) {
         float sw = 0.f;  // sum_t Kbar_t (1 + m_t) W_tj
 #pragma unroll
         for (int u = 0; u < NW; ++u) sw = fmaf(kb[u], w[u], sw);
-        if ((starts >> jj) & 1u) {  // warp-uniform
-          cx = chiT[((q & 0xffff) - wbase) * KU_PAD + lane];
-          sx = slT[((q >> 16) - wbase) * KU_PAD + lane];
-        }
-        const float chip = fmaxf(cx + sx * dx, 0.f);
+        const float chip =
+            fmaxf(chiT[((q & 0xffff) - wbase) * KU_PAD + lane] + slT[((q >> 16) - wbase) * KU_PAD + lane] * dx, 0.f);
         const float diff = chip - chi_wl;
         if (diff > 0.f) {  // then the chi' clip is inactive too
           const float ic = rcpf(fmaxf(chip, 1.f));
@@ -1071,8 +1092,13 @@ static void launch_vjp_t(const GradBatch& gb, cudaStream_t st) {
   const size_t smem = vj_layout(gb.n_tr, gb.n_cls, LT).total;
   cudaFuncSetAttribute(grad_vjp32_kernel<GEN, FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   if (FWD || gb.vjp_cl) cudaMemsetAsync(gb.cl_count, 0, sizeof(unsigned) * (size_t)gb.n_items, st);
-  dim3 grid(vjp_chunks(gb.na), gb.n_items);
-  grad_vjp32_kernel<GEN, FWD><<<grid, VJ_THREADS, smem, st>>>(gb, LT);
+  // chunks per cosmology spread over G CTAs (each loops over its chunks),
+  // G as small as keeps about 4 CTAs per SM in the grid
+  const int nch = vjp_chunks(gb.na);
+  int G = (4 * device_sm_count() + gb.n_items - 1) / gb.n_items;
+  G = G < 1 ? 1 : (G > nch ? nch : G);
+  dim3 grid(G, gb.n_items);
+  grad_vjp32_kernel<GEN, FWD><<<grid, VJ_THREADS, smem, st>>>(gb, LT, G);
 }
 
 // forward: C_ell into the items' cl (uniform batch: gb.cl)
