@@ -1778,6 +1778,30 @@ __global__ void __launch_bounds__(128) grad_scalars_kernel(GradBatch gb) {
   }
 }
 
+// fp32c: the scalars with all 8 tangents in DualFF<8> (value as a float
+// pair, no float64), one thread per cosmology: the same chain as
+// grad_scalars_kernel without the FP64 pipe (the float64 Dual<1> chain per
+// (cosmology, direction) is bound by it).
+__global__ void __launch_bounds__(64) grad_scalars32_kernel(GradBatch gb) {
+  const int item = blockIdx.x * blockDim.x + threadIdx.x;
+  if (item >= gb.n_items) return;
+  const GradItem gi = grad_item(gb, item);
+  FF8 p[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    p[i].v = ff_of(gi.params[i]);
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) p[i].d[d] = (i == d && d != gb.gamma_dir) ? 1.f : 0.f;
+  }
+  FF8 s[NSCAL];
+  cosmo_scalarsT(p, s, tf_nowiggle(gi.geo->physics));
+  for (int i = 0; i < NSCAL; ++i) {
+    gi.tab->sv[i] = ffd(s[i].v);
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) gi.tab->sd[d][i] = s[i].d[d];
+  }
+}
+
 // Small batches: one half warp per (cosmology, direction), the chain's
 // independent calls on different lanes (cosmo_scalars_warpT).
 __global__ void __launch_bounds__(128) grad_scalars_warp_kernel(GradBatch gb) {
@@ -1867,6 +1891,8 @@ void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t s
   if (stages & GS_TABLES) {
   if (gb.n_items <= GNODE_MAX_ITEMS)
     grad_scalars_warp_kernel<<<gb.n_items, 16 * NDIR, 0, st>>>(gb);
+  else if (gb.precision == JCG_FP32C)
+    grad_scalars32_kernel<<<(gb.n_items + 63) / 64, 64, 0, st>>>(gb);
   else
     grad_scalars_kernel<<<(gb.n_items * NDIR + 127) / 128, 128, 0, st>>>(gb);
   if (gb.gnode) {

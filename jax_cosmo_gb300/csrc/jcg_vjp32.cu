@@ -50,8 +50,15 @@ __host__ __device__ inline int vj_stride(int LT) { return LT + (40 - LT % 32) % 
 struct VjLayout {
   size_t ev, kh, rows, ks, mv, mt, vs, pt, ws, abar, qd, red, total;
   size_t rows_b, ks_b;  // the second buffer of each (the next chunk's copies)
+  size_t cacc;
 };
-__host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT) {
+// C_ell summed in shared memory (float64, chunk order) when one CTA runs all
+// of a cosmology's chunks in one ell tile and the sums fit
+constexpr int VJ_CACC_MAX = 3072;  // n_cls x n_ell doubles (24 kB)
+__host__ __device__ inline int vj_cacc(int n_cls, int n_ell, int LT, int G) {
+  return G == 1 && n_ell <= LT && n_cls * n_ell <= VJ_CACC_MAX ? n_cls * n_ell : 0;
+}
+__host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT, int ncacc = 0) {
   VjLayout L;
   size_t o = 0;
   L.ev = o;                                   // 16 values + [NET][NDIR] tangents (floats)
@@ -90,6 +97,9 @@ __host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT) {
   o += 4 * (size_t)(VJ_THREADS / 32) * NET;
   o = (o + 15) & ~(size_t)15;
   o += 8 * (size_t)VJ_TA * NDIR;
+  o = (o + 15) & ~(size_t)15;
+  L.cacc = o;                                 // [n_cls][n_ell] doubles (or none)
+  o += 8 * (size_t)ncacc;
   L.total = o;
   return L;
 }
@@ -122,8 +132,10 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   if ((int)blockIdx.x >= nch) return;
   const bool lin = pk_model(geo->physics) == JCG_PK_LINEAR;
   const bool nw = GEN && tf_nowiggle(geo->physics);
-  const VjLayout L = vj_layout(n_tr, n_cls, LT);
+  const int ncacc = (FWD || gb.vjp_cl) && !gb.listed ? vj_cacc(n_cls, n_ell, LT, G) : 0;  // as the launch
+  const VjLayout L = vj_layout(n_tr, n_cls, LT, ncacc);
   extern __shared__ __align__(16) unsigned char vj_smem[];
+  double* Cacc = reinterpret_cast<double*>(vj_smem + L.cacc);
   float* ev = reinterpret_cast<float*>(vj_smem + L.ev);
   float* et = ev + 16;
   float* khv = reinterpret_cast<float*>(vj_smem + L.kh);
@@ -197,6 +209,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   };
   const bool one_tile = n_ell <= LT;
   if (one_tile) fill_tile(0, n_ell);
+  for (int i = tid; i < ncacc; i += VJ_THREADS) Cacc[i] = 0.0;
   // the CTA's chunks blockIdx.x, blockIdx.x + G, ...: the next chunk's rows
   // are copied while this one runs
   for (int chunk = blockIdx.x, it = 0; chunk < nch; chunk += G, ++it) {
@@ -308,8 +321,13 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
             if (lq + k >= lt) break;
-            cp[(size_t)p0 * n_ell + l0 + lq + k] = r0[k];
-            if (two) cp[(size_t)(p0 + 1) * n_ell + l0 + lq + k] = r1[k];
+            if (ncacc) {  // the chunks in order, as the global sum below
+              Cacc[p0 * n_ell + lq + k] += (double)r0[k];
+              if (two) Cacc[(p0 + 1) * n_ell + lq + k] += (double)r1[k];
+            } else {
+              cp[(size_t)p0 * n_ell + l0 + lq + k] = r0[k];
+              if (two) cp[(size_t)(p0 + 1) * n_ell + l0 + lq + k] = r1[k];
+            }
           }
         }
       }
@@ -366,7 +384,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
         }
       }
     }
-    if (FWD || gb.vjp_cl) {
+    if ((FWD || gb.vjp_cl) && !ncacc) {
       // C_ell of the item once all its chunks are in: the last chunk CTA to
       // finish adds the partials in chunk order (the same sum whichever CTA
       // it is), times the ell factors, and resets the count
@@ -381,8 +399,17 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
         const size_t per = (size_t)n_cls * n_ell;
         for (int idx = tid; idx < (int)per; idx += VJ_THREADS) {
           const int p = idx / n_ell, l = idx - p * n_ell;
+          // chunks added in order; loads issued eight at a time
           double s = 0.0;
-          for (int c = 0; c < nch; ++c) s += (double)__ldcg(gi.cpart + (size_t)c * per + idx);
+          int c = 0;
+          for (; c + 8 <= nch; c += 8) {
+            float v[8];
+#pragma unroll
+            for (int k = 0; k < 8; ++k) v[k] = __ldcg(gi.cpart + (size_t)(c + k) * per + idx);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) s += (double)v[k];
+          }
+          for (; c < nch; ++c) s += (double)__ldcg(gi.cpart + (size_t)c * per + idx);
           gi.cl[idx] = s * EF[(size_t)geo->pair_i[p] * n_ell + l] * EF[(size_t)geo->pair_j[p] * n_ell + l];
         }
       }
@@ -486,6 +513,14 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
       gi.gpart[(size_t)chunk * NDIR + tid] = g;
     }
     __syncthreads();  // this chunk's buffers and scratch are free
+  }
+  if (ncacc && gi.cl) {
+    // every chunk of the cosmology ran here: C_ell from the sums
+    const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
+    for (int idx = tid; idx < ncacc; idx += VJ_THREADS) {
+      const int p = idx / n_ell, l = idx - p * n_ell;
+      gi.cl[idx] = Cacc[idx] * EF[(size_t)geo->pair_i[p] * n_ell + l] * EF[(size_t)geo->pair_j[p] * n_ell + l];
+    }
   }
 }
 
@@ -1089,14 +1124,16 @@ __global__ void vjp_grad_reduce_kernel(GradBatch gb) {
 template <bool GEN, bool FWD>
 static void launch_vjp_t(const GradBatch& gb, cudaStream_t st) {
   const int LT = vjp_ltile(gb.n_cls, gb.n_ell);
-  const size_t smem = vj_layout(gb.n_tr, gb.n_cls, LT).total;
-  cudaFuncSetAttribute(grad_vjp32_kernel<GEN, FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  if (FWD || gb.vjp_cl) cudaMemsetAsync(gb.cl_count, 0, sizeof(unsigned) * (size_t)gb.n_items, st);
   // chunks per cosmology spread over G CTAs (each loops over its chunks),
   // G as small as keeps about 4 CTAs per SM in the grid
   const int nch = vjp_chunks(gb.na);
   int G = (4 * device_sm_count() + gb.n_items - 1) / gb.n_items;
   G = G < 1 ? 1 : (G > nch ? nch : G);
+  // (a listed batch's sizes are maxima: its items take the global sums)
+  const int ncacc = (FWD || gb.vjp_cl) && !gb.listed ? vj_cacc(gb.n_cls, gb.n_ell, LT, G) : 0;
+  const size_t smem = vj_layout(gb.n_tr, gb.n_cls, LT, ncacc).total;
+  cudaFuncSetAttribute(grad_vjp32_kernel<GEN, FWD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if ((FWD || gb.vjp_cl) && !ncacc) cudaMemsetAsync(gb.cl_count, 0, sizeof(unsigned) * (size_t)gb.n_items, st);
   dim3 grid(G, gb.n_items);
   grad_vjp32_kernel<GEN, FWD><<<grid, VJ_THREADS, smem, st>>>(gb, LT, G);
 }

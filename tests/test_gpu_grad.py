@@ -393,3 +393,29 @@ def test_vjp_uniform_reverse_lensing_lanes_over_cosmologies():
                          want_cl=True)
     assert torch.equal(g1[0], g[k])
     assert torch.equal(cl1[0], cl[k])
+
+
+def test_vjp_large_batch_matches_small_batches_bit_for_bit():
+    """At 640 cosmologies the product kernel runs all chunks of a cosmology
+    in one CTA (C_ell summed in shared memory, chunk order); at 160 per call
+    the chunks spread over CTAs (C_ell summed by the last chunk's CTA).  The
+    same sums in the same order: C_ell and the gradient equal bit for bit
+    (both sizes above the small-batch scalar kernel's 128)."""
+    from jax_cosmo_gb300.autodiff import vjp_device
+
+    rng = np.random.default_rng(41)
+    B = 640
+    rows = np.array([FID] * B) * (1.0 + 0.05 * rng.uniform(-1, 1, (B, 8)))
+    rows[:, 5] = 0.0
+    rows[:, 7] = 0.03 * rng.uniform(-1, 1, B)
+    params = torch.as_tensor(rows, device="cuda").contiguous()
+    probes = jc_probes(WL5)
+    ell = np.geomspace(20, 3000, 40)
+    n_cls = 15
+    vbar = torch.as_tensor(rng.standard_normal((B, n_cls, len(ell))), device="cuda")
+    g, cl = vjp_device(params, ell, probes, vbar, 256, "fp32c", want_cl=True)
+    for i in range(0, B, 160):
+        gi, cli = vjp_device(params[i:i + 160].contiguous(), ell, probes, vbar[i:i + 160].contiguous(), 256,
+                             "fp32c", want_cl=True)
+        assert torch.equal(gi, g[i:i + 160])
+        assert torch.equal(cli, cl[i:i + 160])
