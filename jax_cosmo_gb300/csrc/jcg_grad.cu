@@ -863,6 +863,47 @@ __device__ __forceinline__ F8 interp_f8(double x, const double* xp, const double
 // takahashi2012 coefficients, Limber weight; the row is written as computed.
 // interpolation on the segment sg of a table with tangents, by the segment's
 // node-spacing reciprocal ida (no float64 division)
+// float value with 8 float tangents (the row stage's halofit coefficients,
+// which the Limber integrand consumes as float)
+struct S8 {
+  float v;
+  float d[NDIR];
+};
+__device__ __forceinline__ S8 s8_of(const FF8& x) {
+  S8 r;
+  r.v = x.v.hi;
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) r.d[d] = x.d[d];
+  return r;
+}
+__device__ __forceinline__ S8 s8_scale(const S8& x, float c) {
+  S8 r;
+  r.v = c * x.v;
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) r.d[d] = c * x.d[d];
+  return r;
+}
+__device__ __forceinline__ S8 s8_ex2(const S8& x) {  // 2^x
+  S8 r;
+  r.v = ex2f(x.v);
+  const float s = r.v * LN2_F;
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) r.d[d] = s * x.d[d];
+  return r;
+}
+__device__ __forceinline__ S8 s8_lg2(const S8& x) {  // log2 x
+  S8 r;
+  r.v = lg2f(x.v);
+  const float s = LOG2E_F * rcpf(x.v);
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) r.d[d] = s * x.d[d];
+  return r;
+}
+__device__ __forceinline__ void put_s8(float* tg, int slot, const S8& x, float sc) {
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) tg[slot * NDIR + d] = x.d[d] * sc;
+}
+
 __device__ __forceinline__ FF8 interp_ff8(FF x, const float2* xp, const float2* ida, const float2* fv,
                                          const float (*fd)[NDIR], int2 sg) {
   const FF8 f0 = ff8_of(fv[sg.x], fd[sg.x]), f1 = ff8_of(fv[sg.y], fd[sg.y]);
@@ -1073,98 +1114,151 @@ __global__ void __launch_bounds__(GR32_THREADS, 2) grad_rows32_kernel(GradBatch 
   const FF8 esq = bg.Om * (ia2 * ia) + bg.Ok * ia2 + bg.Ode * efde;
   const FF8 om_m = bg.Om * (ia2 * ia) / esq;
   const FF8 om_de = bg.Ode * efde / esq;
-  // halofit coefficients (power.py:177-244), each stored as soon as it is
-  // formed (short live ranges of the 8-tangent values)
-  const FF8 n2 = neff * neff, n3 = n2 * neff, n4 = n2 * n2;
-  constexpr double LOG2E = 1.4426950408889634;
+  // halofit coefficients (power.py:177-244) in float values with float
+  // tangents (S8), the forward fp32c rows' arithmetic (halofit_coefs_fast:
+  // the same float expressions, MUFU ex2 / lg2), each stored as soon as it is
+  // formed
+  const S8 nS = s8_of(neff), Cs = s8_of(C), omm = s8_of(om_m), omde = s8_of(om_de);
+  const float nv = nS.v, n2 = nv * nv, n3 = n2 * nv, n4 = n2 * n2, Cv = Cs.v;
+  // d/dn of c1 n + c2 n^2 + c3 n^3 + c4 n^4
+  auto dpoly = [&](float c1, float c2, float c3, float c4) { return c1 + nv * (2.f * c2 + nv * (3.f * c3 + nv * 4.f * c4)); };
+  auto lin = [&](float v, float dn, float dC) {  // value v, tangent dn dneff + dC dC
+    S8 r;
+    r.v = v;
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) r.d[d] = fmaf(dn, nS.d[d], dC * Cs.d[d]);
+    return r;
+  };
+  constexpr float LOG2_10 = 3.321928094887362f, LN10_F = 2.302585092994046f;
+  const S8 l2om = s8_lg2(omm);
   if (pk_model(gi.geo->physics) == JCG_PK_SMITH2003) {
     // power.py:182-198, 239-242
     {
-      const FF8 beta = 0.8291 + 0.9854 * neff + 0.3401 * n2;
-      row[F_BETAN] = beta.v.hi;
-      put_t(T_BETAN, beta, 1.f);
-      const FF8 alpha = 1.3884 + 0.3700 * neff - 0.1452 * n2;
-      row[F_ALPHAN] = alpha.v.hi;
-      put_t(T_ALPHAN, alpha, 1.f);
+      const S8 beta = lin(0.8291f + 0.9854f * nv + 0.3401f * n2, dpoly(0.9854f, 0.3401f, 0.f, 0.f), 0.f);
+      row[F_BETAN] = beta.v;
+      put_s8(tg, T_BETAN, beta, 1.f);
+      const S8 alpha = lin(1.3884f + 0.3700f * nv - 0.1452f * n2, dpoly(0.3700f, -0.1452f, 0.f, 0.f), 0.f);
+      row[F_ALPHAN] = alpha.v;
+      put_s8(tg, T_ALPHAN, alpha, 1.f);
     }
     {
-      const FF8 an = xexp(LN10_G * (1.4861 + 1.8369 * neff + 1.6762 * n2 + 0.7940 * n3 + 0.1670 * n4 - 0.6206 * C));
-      row[F_AN] = an.v.hi;
-      put_t(T_AN, an, 1.f);
-      const FF8 bn = xexp(LN10_G * (0.9463 + 0.9466 * neff + 0.3084 * n2 - 0.9400 * C));
-      row[F_BN] = bn.v.hi;
-      put_t(T_BN, bn, 1.f);
+      const S8 e_an = lin(1.4861f + 1.8369f * nv + 1.6762f * n2 + 0.7940f * n3 + 0.1670f * n4 - 0.6206f * Cv,
+                          dpoly(1.8369f, 1.6762f, 0.7940f, 0.1670f), -0.6206f);
+      const S8 an = s8_ex2(s8_scale(e_an, LOG2_10));
+      row[F_AN] = an.v;
+      put_s8(tg, T_AN, an, 1.f);
+      const S8 e_bn = lin(0.9463f + 0.9466f * nv + 0.3084f * n2 - 0.9400f * Cv, dpoly(0.9466f, 0.3084f, 0.f, 0.f), -0.9400f);
+      const S8 bn = s8_ex2(s8_scale(e_bn, LOG2_10));
+      row[F_BN] = bn.v;
+      put_s8(tg, T_BN, bn, 1.f);
     }
     {
-      const FF8 lom = xlog(om_m);
-      const FF8 frac = om_de / (1.0 - om_m);
-      const FF8 ofr = 1.0 - frac;
-      const FF8 f1 = frac * xexp(-0.0307 * lom) + ofr * xexp(-0.0732 * lom);
-      row[F_3F1] = 3.f * f1.v.hi;
-      put_t(T_3F1, f1, 3.f);
-      const FF8 f2 = frac * xexp(-0.0585 * lom) + ofr * xexp(-0.1423 * lom);
-      row[F_F2] = f2.v.hi;
-      put_t(T_F2, f2, 1.f);
-      const FF8 f3 = frac * xexp(0.0743 * lom) + ofr * xexp(0.0725 * lom);
-      const FF8 lcf3 = LN10_G * (-0.2807 + 0.6669 * neff + 0.3214 * n2 - 0.0793 * C) + xlog(f3);
-      row[F_LG2CF3] = (lcf3.v * ffc(LOG2E)).hi;
-      put_t(T_LG2CF3, lcf3, (float)LOG2E);
+      // frac = Omega_de / (1 - Omega_m) (power.py:180)
+      const float ir = rcpf(1.f - omm.v);
+      S8 frac;
+      frac.v = omde.v * ir;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) frac.d[d] = (omde.d[d] + frac.v * omm.d[d]) * ir;
+      auto mix = [&](float p1, float p2) {  // frac om^p1 + (1 - frac) om^p2
+        const S8 x1 = s8_ex2(s8_scale(l2om, p1)), x2 = s8_ex2(s8_scale(l2om, p2));
+        S8 r;
+        r.v = frac.v * x1.v + (1.f - frac.v) * x2.v;
+#pragma unroll
+        for (int d = 0; d < NDIR; ++d)
+          r.d[d] = fmaf(frac.d[d], x1.v - x2.v, fmaf(frac.v, x1.d[d], (1.f - frac.v) * x2.d[d]));
+        return r;
+      };
+      const S8 f1 = mix(-0.0307f, -0.0732f);
+      row[F_3F1] = 3.f * f1.v;
+      put_s8(tg, T_3F1, f1, 3.f);
+      const S8 f2 = mix(-0.0585f, -0.1423f);
+      row[F_F2] = f2.v;
+      put_s8(tg, T_F2, f2, 1.f);
+      const S8 f3 = mix(0.0743f, 0.0725f);
+      const S8 e_cn = lin(-0.2807f + 0.6669f * nv + 0.3214f * n2 - 0.0793f * Cv, dpoly(0.6669f, 0.3214f, 0.f, 0.f),
+                          -0.0793f);
+      const S8 lg2f3 = s8_lg2(f3);
+      S8 lg2cf3;
+      lg2cf3.v = LOG2_10 * e_cn.v + lg2f3.v;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) lg2cf3.d[d] = fmaf(LOG2_10, e_cn.d[d], lg2f3.d[d]);
+      row[F_LG2CF3] = lg2cf3.v;
+      put_s8(tg, T_LG2CF3, lg2cf3, 1.f);
     }
     {
-      const FF8 gam = 0.8649 + 0.2989 * neff + 0.1631 * C;
-      row[F_3MGAMMA] = (3.f - gam.v).hi;
-      put_t(T_3MG, gam, -1.f);
-      const FF8 nu = xexp(LN10_G * (0.9585 + 1.2857 * neff));
-      row[F_NUN] = nu.v.hi;
-      put_t(T_NUN, nu, 1.f);
-      const FF8 mu = xexp(LN10_G * (-3.5442 + 0.1908 * neff));
-      row[F_MUN] = mu.v.hi;
-      put_t(T_MUN, mu, 1.f);
+      const S8 gam = lin(0.8649f + 0.2989f * nv + 0.1631f * Cv, 0.2989f, 0.1631f);
+      row[F_3MGAMMA] = 3.f - gam.v;
+      put_s8(tg, T_3MG, gam, -1.f);
+      const S8 nu = s8_ex2(s8_scale(lin(0.9585f + 1.2857f * nv, 1.2857f, 0.f), LOG2_10));
+      row[F_NUN] = nu.v;
+      put_s8(tg, T_NUN, nu, 1.f);
+      const S8 mu = s8_ex2(s8_scale(lin(-3.5442f + 0.1908f * nv, 0.1908f, 0.f), LOG2_10));
+      row[F_MUN] = mu.v;
+      put_s8(tg, T_MUN, mu, 1.f);
     }
   } else {
-    const FF8 opw = om_de * (1.0 + (bg.w0 + (ffc(1.0) - aF) * bg.wa));  // wT (background.py:53)
+    // opw = Omega_de(a) (1 + w(a)), w = w0 + (1 - a) wa (background.py:53)
+    const S8 w = s8_of(bg.w0 + (ffc(1.0) - aF) * bg.wa);
+    S8 opw;
+    opw.v = omde.v * (1.f + w.v);
+#pragma unroll
+    for (int d = 0; d < NDIR; ++d) opw.d[d] = fmaf(omde.d[d], 1.f + w.v, omde.v * w.d[d]);
+    auto with_opw = [&](S8 x, float c) {
+      x.v = x.v + c * opw.v;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) x.d[d] = fmaf(c, opw.d[d], x.d[d]);
+      return x;
+    };
     {
-      const FF8 beta = 2.0379 - 0.7354 * neff + 0.3157 * n2 + 1.2490 * n3 + 0.3980 * n4 - 0.1682 * C;
-      row[F_BETAN] = beta.v.hi;
-      put_t(T_BETAN, beta, 1.f);
-      const FF8 alpha = xfabs(6.0835 + 1.3373 * neff - 0.1959 * n2 - 5.5274 * C);
-      row[F_ALPHAN] = alpha.v.hi;
-      put_t(T_ALPHAN, alpha, 1.f);
+      const S8 beta = lin(2.0379f - 0.7354f * nv + 0.3157f * n2 + 1.2490f * n3 + 0.3980f * n4 - 0.1682f * Cv,
+                          dpoly(-0.7354f, 0.3157f, 1.2490f, 0.3980f), -0.1682f);
+      row[F_BETAN] = beta.v;
+      put_s8(tg, T_BETAN, beta, 1.f);
+      S8 alpha = lin(6.0835f + 1.3373f * nv - 0.1959f * n2 - 5.5274f * Cv, dpoly(1.3373f, -0.1959f, 0.f, 0.f), -5.5274f);
+      if (alpha.v < 0.f) alpha = s8_scale(alpha, -1.f);  // fabs, the selected branch's tangent
+      row[F_ALPHAN] = alpha.v;
+      put_s8(tg, T_ALPHAN, alpha, 1.f);
     }
     {
-      const FF8 e_an = 1.5222 + 2.8553 * neff + 2.3706 * n2 + 0.9903 * n3 + 0.2250 * n4 - 0.6038 * C + 0.1749 * opw;
-      const FF8 an = xexp(LN10_G * e_an);
-      row[F_AN] = an.v.hi;
-      put_t(T_AN, an, 1.f);
-      const FF8 e_bn = -0.5642 + 0.5864 * neff + 0.5716 * n2 - 1.5474 * C + 0.2279 * opw;
-      const FF8 bn = xexp(LN10_G * e_bn);
-      row[F_BN] = bn.v.hi;
-      put_t(T_BN, bn, 1.f);
+      const S8 e_an = with_opw(lin(1.5222f + 2.8553f * nv + 2.3706f * n2 + 0.9903f * n3 + 0.2250f * n4 - 0.6038f * Cv,
+                                   dpoly(2.8553f, 2.3706f, 0.9903f, 0.2250f), -0.6038f), 0.1749f);
+      const S8 an = s8_ex2(s8_scale(e_an, LOG2_10));
+      row[F_AN] = an.v;
+      put_s8(tg, T_AN, an, 1.f);
+      const S8 e_bn = with_opw(lin(-0.5642f + 0.5864f * nv + 0.5716f * n2 - 1.5474f * Cv,
+                                   dpoly(0.5864f, 0.5716f, 0.f, 0.f), -1.5474f), 0.2279f);
+      const S8 bn = s8_ex2(s8_scale(e_bn, LOG2_10));
+      row[F_BN] = bn.v;
+      put_s8(tg, T_BN, bn, 1.f);
     }
     {
-      const FF8 lom = xlog(om_m);
-      const FF8 e_cn = 0.3698 + 2.0404 * neff + 0.8161 * n2 + 0.5869 * C;
-      const FF8 lcf3 = LN10_G * e_cn + 0.0743 * lom;
-      row[F_LG2CF3] = (lcf3.v * ffc(LOG2E)).hi;
-      put_t(T_LG2CF3, lcf3, (float)LOG2E);
-      const FF8 f1 = xexp(-0.0307 * lom);
-      row[F_3F1] = 3.f * f1.v.hi;
-      put_t(T_3F1, f1, 3.f);
-      const FF8 f2 = xexp(-0.0585 * lom);
-      row[F_F2] = f2.v.hi;
-      put_t(T_F2, f2, 1.f);
+      const S8 e_cn = lin(0.3698f + 2.0404f * nv + 0.8161f * n2 + 0.5869f * Cv, dpoly(2.0404f, 0.8161f, 0.f, 0.f), 0.5869f);
+      S8 lg2cf3;
+      lg2cf3.v = LOG2_10 * e_cn.v + 0.0743f * l2om.v;
+#pragma unroll
+      for (int d = 0; d < NDIR; ++d) lg2cf3.d[d] = fmaf(LOG2_10, e_cn.d[d], 0.0743f * l2om.d[d]);
+      row[F_LG2CF3] = lg2cf3.v;
+      put_s8(tg, T_LG2CF3, lg2cf3, 1.f);
+      const S8 f1 = s8_ex2(s8_scale(l2om, -0.0307f));
+      row[F_3F1] = 3.f * f1.v;
+      put_s8(tg, T_3F1, f1, 3.f);
+      const S8 f2 = s8_ex2(s8_scale(l2om, -0.0585f));
+      row[F_F2] = f2.v;
+      put_s8(tg, T_F2, f2, 1.f);
     }
     {
-      const FF8 gam = 0.1971 - 0.0843 * neff + 0.8460 * C;
-      row[F_3MGAMMA] = (3.f - gam.v).hi;
-      put_t(T_3MG, gam, -1.f);
-      const FF8 nu = xexp(LN10_G * (5.2105 + 3.6902 * neff));
-      row[F_NUN] = nu.v.hi;
-      put_t(T_NUN, nu, 1.f);
+      const S8 gam = lin(0.1971f - 0.0843f * nv + 0.8460f * Cv, -0.0843f, 0.8460f);
+      row[F_3MGAMMA] = 3.f - gam.v;
+      put_s8(tg, T_3MG, gam, -1.f);
+      const S8 nu = s8_ex2(s8_scale(lin(5.2105f + 3.6902f * nv, 3.6902f, 0.f), LOG2_10));
+      row[F_NUN] = nu.v;
+      put_s8(tg, T_NUN, nu, 1.f);
       row[F_MUN] = 0.f;
-      put_t(T_MUN, 0.0 * nu, 0.f);
+      put_s8(tg, T_MUN, s8_scale(nu, 0.f), 0.f);
     }
   }
+  (void)LN10_F;
+  constexpr double LOG2E = 1.4426950408889634;
   {
     const FF8 chic = xfmax(chi, 1.0);
     row[F_INVCHI] = ff_rcp(chic.v).hi;
