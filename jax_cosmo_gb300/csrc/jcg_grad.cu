@@ -33,20 +33,49 @@ typedef DualFF<NDIR> FF8;
 // lane; the sigma^2(R) tangents are FP32 sums; float copies of the chi and
 // P(k) k^3 tangent tables are written for the FP32 stages.  The sequential
 // scans (chi prefix sum, growth RK4, Romberg) stay FP64 Dual<1>.
-// chi_scan_warp (jcg_internal.cuh) for a tangent component: the RK4
-// increments in FP32 (their inputs are FP32 tangents), the prefix sums in
-// float pairs, chi_i = Y[-1] - Y_i rounded to float64 at the end.
-__device__ __forceinline__ void chi_scan_warp_ff(const double* fnode, const double* fmid, const double* lna,
-                                                 int lane, double* out) {
+// fp32c node values in 8-byte slots of the [component][node] arrays: the
+// value as a float pair (hi, lo), a tangent as a float in the slot's low
+// half; written by grad_nodes_kernel, read by grad_tables_kernel with no
+// float64 conversion on either side.
+__device__ __forceinline__ void put_slots(double* arr, int stride, int e, const FF8& x) {
+  *reinterpret_cast<float2*>(arr + e) = make_float2(x.v.hi, x.v.lo);
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) *reinterpret_cast<float*>(arr + (1 + d) * stride + e) = x.d[d];
+}
+__device__ __forceinline__ FF slot_v(const double* arr, int e) {
+  const float2 v = *reinterpret_cast<const float2*>(arr + e);
+  return FF{v.x, v.y};
+}
+__device__ __forceinline__ float slot_t(const double* arr, int e) { return *reinterpret_cast<const float*>(arr + e); }
+__device__ __forceinline__ FF8 ff8_slots(const double* arr, int stride, int e) {
+  FF8 r;
+  r.v = slot_v(arr, e);
+#pragma unroll
+  for (int d = 0; d < NDIR; ++d) r.d[d] = slot_t(arr + (1 + d) * stride, e);
+  return r;
+}
+
+// The chi table (background.py:227-233) of one component for one warp, in
+// float pairs from the slot arrays: prefix sums of the RK4 increments
+// h/6 (f_{i-1} + 2 fm_i + 2 fm_i + f_i) in ln a (scipy/ode.py:21, the first
+// step has h = 0), then chi_i = Y[-1] - Y_i.  Lane l holds nodes
+// 8l .. 8l + 7 (returned in v).  The value (comp 0) forms its increments in
+// float pairs; a tangent in FP32 (its inputs are FP32).
+__device__ __forceinline__ void chi_scan_ff(const double* fnode, const double* fmid, const float2* h6, bool value,
+                                            int lane, FF* v) {
   FF loc[8];
   FF s{0.f, 0.f};
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
     const int i = lane * 8 + k;
     if (i > 0) {
-      const float h6 = (float)((lna[i] - lna[i - 1]) * (1.0 / 6.0));
-      const float fmv = (float)fmid[i];
-      s = s + h6 * ((((float)fnode[i - 1] + 2.f * fmv) + 2.f * fmv) + (float)fnode[i]);
+      if (value) {
+        const FF fmv = slot_v(fmid, i);
+        s = s + (((slot_v(fnode, i - 1) + ff_scale2(fmv, 2.f)) + ff_scale2(fmv, 2.f)) + slot_v(fnode, i)) * f2ff(h6[i]);
+      } else {
+        const float fmv = slot_t(fmid, i);
+        s = s + h6[i].x * (((slot_t(fnode, i - 1) + 2.f * fmv) + 2.f * fmv) + slot_t(fnode, i));
+      }
     }
     loc[k] = s;
   }
@@ -60,7 +89,7 @@ __device__ __forceinline__ void chi_scan_warp_ff(const double* fnode, const doub
   if (lane == 0) off = FF{0.f, 0.f};
   const FF tot{__shfl_sync(0xffffffffu, x.hi, 31), __shfl_sync(0xffffffffu, x.lo, 31)};
 #pragma unroll
-  for (int k = 0; k < 8; ++k) out[lane * 8 + k] = ffd(tot - (off + loc[k]));
+  for (int k = 0; k < 8; ++k) v[k] = tot - (off + loc[k]);
 }
 
 // NW: some item may use the transfer type "eisenhu"
@@ -134,8 +163,8 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       const double kw = k * wf;
       put(fr, NROMB, e, k * (kw * kw) * pk);
     }
-  } else if (gb.gnode) {
-    // node values from grad_nodes_kernel: the same layout as fn .. fr here;
+  } else {
+    // node values from grad_nodes_kernel (slots): the same layout as fn .. fr here;
     // 16-byte copies, eight in flight per thread
     static_assert((9 * NSCAL) % 2 == 0 && GNODE_STRIDE % 2 == 0, "16-byte aligned node copy");
     const double2* src = reinterpret_cast<const double2*>(gb.gnode + (size_t)item * GNODE_STRIDE);
@@ -153,38 +182,6 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
         const int i = i0 + u * blockDim.x;
         if (i < NV) dst[i] = v[u];
       }
-    }
-  } else {
-    FF8 sF[NSCAL];
-    for (int i = 0; i < NSCAL; ++i) sF[i] = ff8_of(sv[i], sd + i, NSCAL);
-    const BgT<FF8> bgf = make_bgT(sF);
-    // cosmology-independent abscissae, logs, reciprocals and window factors
-    // from the constant grids
-    for (int e = t; e < 2 * NCHI; e += blockDim.x) {
-      if (e < NCHI) {
-        putf(fn, NCHI, e, dchi_dlna_cT(bgf, c->chi_a[e], c->lna_chi[e], c->chi_ia[e]));
-      } else if (e > NCHI) {
-        const int i = e - NCHI;
-        putf(fm, NCHI, i, dchi_dlna_cT(bgf, c->chi_am[i], c->chi_lnam[i], c->chi_iam[i]));
-      }
-    }
-    for (int e = t; e < 2 * NGROW; e += blockDim.x) {
-      FF8 q, r;
-      if (e < NGROW) {
-        growth_qr_cT(bgf, c->atab_grow[e], c->grow_lna[e], c->grow_ia[e], q, r);
-        putf(qr + 0 * (NDIR + 1) * NGROW, NGROW, e, q);
-        putf(qr + 1 * (NDIR + 1) * NGROW, NGROW, e, r);
-      } else if (e > NGROW) {
-        const int i = e - NGROW;
-        growth_qr_cT(bgf, c->grow_am[i], c->grow_lnam[i], c->grow_iam[i], q, r);
-        putf(qr + 2 * (NDIR + 1) * NGROW, NGROW, i, q);
-        putf(qr + 3 * (NDIR + 1) * NGROW, NGROW, i, r);
-      }
-    }
-    for (int e = t; e < NROMB; e += blockDim.x) {
-      const double logk = c->romb_logk[e];
-      const FF8 T = eh_transferT<NW>(sF, c->romb_k[e], logk);
-      putf(fr, NROMB, e, c->romb_kw2[e] * ((T * T) * xexp(sF[S_NS] * logk)));
     }
   }
   __syncthreads();
@@ -205,7 +202,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       const double* RA = qr + (NDIR + 1) * NGROW;
       const double* QM = qr + 2 * (NDIR + 1) * NGROW;
       const double* RM = qr + 3 * (NDIR + 1) * NGROW;
-      auto g8 = [&](const double* arr, int e) { return ff8_of(arr[e], arr + NGROW + e, NGROW); };
+      auto g8 = [&](const double* arr, int e) { return ff8_slots(arr, NGROW, e); };
       const FF8 qa0 = g8(QA, t - 1), ra0 = g8(RA, t - 1), qm = g8(QM, t), rm = g8(RM, t);
       const FF8 qa1 = g8(QA, t), ra1 = g8(RA, t);
       const double hh = c->atab_grow[t] - c->atab_grow[t - 1];
@@ -224,10 +221,13 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     double* Mv = qr;                                          // [NGROW][4]
     float* dMv = reinterpret_cast<float*>(qr + 4 * NGROW);    // [NGROW][4][NDIR]
     double* Yv = qr + 4 * NGROW + 2 * NDIR * NGROW;           // [NGROW][2] y_i
+    float* Mvf = reinterpret_cast<float*>(Yv + 2 * NGROW);   // [NGROW][4] float copies
+    float* Yvf = Mvf + 4 * NGROW;                             // [NGROW][2] float copies
     if (t < NGROW) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         Mv[t * 4 + q] = m4[q];
+        Mvf[t * 4 + q] = (float)m4[q];
 #pragma unroll
         for (int d = 0; d < NDIR; ++d) dMv[(t * 4 + q) * NDIR + d] = dm4[q][d];
       }
@@ -236,39 +236,67 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     if (warp == 0) {
       double ys[4];
       const double yf = growth_scan_warp(Mv, c->atab_grow[0], 1.0, lane, ys, Yv);
-      for (int k = 0; k < 4; ++k) out->gv[lane * 4 + k] = ys[k] / yf;
+      const double iyf = 1.0 / yf;
+      for (int k = 0; k < 4; ++k) {
+        const int i = lane * 4 + k;
+        const double gvv = ys[k] * iyf;
+        out->gv[i] = gvv;
+        const FF gf = ff_of(gvv);
+        out->gF[i] = make_float2(gf.hi, gf.lo);  // the row stage's copy
+        Yvf[i * 2] = (float)Yv[i * 2];
+        Yvf[i * 2 + 1] = (float)Yv[i * 2 + 1];
+      }
     } else {
-      // chi for the value and the 8 tangents
+      // chi for the value and the 8 tangents, in float pairs; the FP32 tables
+      // (values, segment slopes) and the row stage's copies straight from
+      // the sums
       for (int comp = warp - 1; comp < NDIR + 1; comp += 3) {
-        if (comp == 0) chi_scan_warp(fn, fm, c->lna_chi, lane, out->chiv);
-        else chi_scan_warp_ff(fn + comp * NCHI, fm + comp * NCHI, c->lna_chi, lane, out->chid[comp - 1]);
+        FF v[8];
+        chi_scan_ff(fn + comp * NCHI, fm + comp * NCHI, c->chi_h6_ff, comp == 0, lane, v);
+        const FF vn{__shfl_down_sync(0xffffffffu, v[0].hi, 1), __shfl_down_sync(0xffffffffu, v[0].lo, 1)};
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          const int i = lane * 8 + k;
+          const FF nxt = k < 7 ? v[k + 1] : vn;
+          out->c32[comp][i] = v[k].hi;
+          out->s32[comp][i] = i + 1 < NCHI ? ((nxt - v[k]) * f2ff(c->chi_ida_ff[i])).hi : 0.f;
+          if (comp == 0) out->chiF[i] = make_float2(v[k].hi, v[k].lo);
+          else out->chidF[i][comp - 1] = v[k].hi;
+        }
       }
       // sigmasqr(8) (power.py:70-78): romb is linear in the integrand values,
-      // sum_e w_e f_e with the weights of the Richardson combination
+      // sum_e w_e f_e with the weights of the Richardson combination (the
+      // value in float pairs, a tangent in FP32)
       for (int comp = warp - 1; comp < NDIR + 1; comp += 3) {
-        double s = 0.0;
-        for (int e = lane; e < NROMB; e += 32) s = fma(c->romb_w[e], fr[comp * NROMB + e], s);
+        const double* fc = fr + comp * NROMB;
+        if (comp == 0) {
+          FF sf{0.f, 0.f};
+          for (int e = lane; e < NROMB; e += 32) sf = sf + f2ff(c->romb_w_ff[e]) * slot_v(fc, e);
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) {
-          const double sig8 = 1.0 / (2.0 * (PI * PI)) * s;
-          if (comp == 0) sv[S_SIGMASQR8] = sig8;
-          else sd[(comp - 1) * NSCAL + S_SIGMASQR8] = sig8;
+          for (int o = 16; o > 0; o >>= 1)
+            sf = sf + FF{__shfl_xor_sync(0xffffffffu, sf.hi, o), __shfl_xor_sync(0xffffffffu, sf.lo, o)};
+          if (lane == 0) sv[S_SIGMASQR8] = ffd(sf * ffc(1.0 / (2.0 * (PI * PI))));
+        } else {
+          float sf = 0.f;
+          for (int e = lane; e < NROMB; e += 32) sf = fmaf(c->romb_w_ff[e].x, slot_t(fc, e), sf);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) sf += __shfl_xor_sync(0xffffffffu, sf, o);
+          if (lane == 0) sd[(comp - 1) * NSCAL + S_SIGMASQR8] = (double)(sf * (float)(1.0 / (2.0 * (PI * PI))));
         }
       }
     }
     __syncthreads();
     // growth tangents: dy_i = M_i dy_{i-1} + dM_i y_{i-1}, dy_0 = 0, as an
     // FP32 scan of affine maps (A, b), one direction per warp and pass
-    const double iyf = 1.0 / Yv[(NGROW - 1) * 2];
+    const float iyf = 1.f / Yvf[(NGROW - 1) * 2];
     for (int d = warp; d < NDIR; d += 4) {
       float A[4] = {1.f, 0.f, 0.f, 1.f}, b[2] = {0.f, 0.f};
       float Mf[4][4], bf[4][2];
       for (int k = 0; k < 4; ++k) {
         const int i = lane * 4 + k;
 #pragma unroll
-        for (int q = 0; q < 4; ++q) Mf[k][q] = (float)Mv[i * 4 + q];
-        const float yp0 = i > 0 ? (float)Yv[(i - 1) * 2] : 0.f, yp1 = i > 0 ? (float)Yv[(i - 1) * 2 + 1] : 0.f;
+        for (int q = 0; q < 4; ++q) Mf[k][q] = Mvf[i * 4 + q];
+        const float yp0 = i > 0 ? Yvf[(i - 1) * 2] : 0.f, yp1 = i > 0 ? Yvf[(i - 1) * 2 + 1] : 0.f;
         const float* dM = dMv + i * 4 * NDIR + d;
         bf[k][0] = dM[0] * yp0 + dM[NDIR] * yp1;
         bf[k][1] = dM[2 * NDIR] * yp0 + dM[3 * NDIR] * yp1;
@@ -304,8 +332,10 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       const float dyf = __shfl_sync(0xffffffffu, x0, 31);
       for (int k = 0; k < 4; ++k) {
         const int i = lane * 4 + k;
-        const double D = Yv[i * 2] * iyf;
-        out->gd[d][i] = ((double)dy[k] - D * (double)dyf) * iyf;
+        const float D = Yvf[i * 2] * iyf;
+        const float gdv = (dy[k] - D * dyf) * iyf;
+        out->gd[d][i] = (double)gdv;
+        out->gdF[i][d] = gdv;  // the row stage's copy
       }
     }
   } else if (lane < NDIR) {
@@ -428,7 +458,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     const FF8 pkn = ff8_of(sv[S_PKNORM], sd + S_PKNORM, NSCAL);
     const double* gu = gb.gnode + (size_t)item * GNODE_STRIDE + GNODE_U;
     for (int e = t; e < NKH; e += blockDim.x) {
-      const FF8 u = ff8_of(gu[e], gu + NKH + e, NKH);
+      const FF8 u = ff8_slots(gu, NKH, e);
       const FF8 p3 = ((u * g1sq) * pkn) * c->kh3[e];
       out->pk3v[e] = val(p3);
       float4* pd = reinterpret_cast<float4*>(&out->pk3df[e][0]);
@@ -509,24 +539,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       out->svF[i] = make_float2(v.hi, v.lo);
       for (int d = 0; d < NDIR; ++d) out->sdF[i][d] = (float)sd[d * NSCAL + i];
     }
-    for (int i = t; i < NCHI; i += blockDim.x) {
-      const FF v = ff_of(out->chiv[i]);
-      out->chiF[i] = make_float2(v.hi, v.lo);
-      for (int d = 0; d < NDIR; ++d) out->chidF[i][d] = (float)out->chid[d][i];
-    }
-    for (int i = t; i < NGROW; i += blockDim.x) {
-      const FF v = ff_of(out->gv[i]);
-      out->gF[i] = make_float2(v.hi, v.lo);
-      for (int d = 0; d < NDIR; ++d) out->gdF[i][d] = (float)out->gd[d][i];
-    }
-    // float chi tables and segment slopes with tangents (the FP32 lensing stage)
-    for (int e = t; e < (NDIR + 1) * NCHI; e += blockDim.x) {
-      const int comp = e / NCHI, i = e % NCHI;
-      const double* ch = comp == 0 ? out->chiv : out->chid[comp - 1];
-      const double sl = i + 1 < NCHI ? (ch[i + 1] - ch[i]) * c->chi_ida[i] : 0.0;
-      out->c32[comp][i] = (float)ch[i];
-      out->s32[comp][i] = (float)sl;
-    }
+    // (the FP32 chi tables, slopes and the row stage's copies come from the scans)
   }
 }
 
@@ -1820,11 +1833,7 @@ __global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const Con
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const BgT<FF8> bgf = make_bgT(sF);
   double* dst = gb.gnode + (size_t)item * GNODE_STRIDE;
-  auto putf = [&](int off, int stride, int i, const FF8& x) {
-    dst[off + i] = val(x);
-#pragma unroll
-    for (int d = 0; d < NDIR; ++d) dst[off + (1 + d) * stride + i] = x.d[d];
-  };
+  auto putf = [&](int off, int stride, int i, const FF8& x) { put_slots(dst + off, stride, i, x); };
   if (KIND == 0) {
     if (w < NCHI) {
       putf(0, NCHI, w, dchi_dlna_f8(bgf, f2ff(c->chi_a_ff[w]), f2ff(c->lna_chi_ff[w]), f2ff(c->chi_ia_ff[w])));

@@ -210,7 +210,11 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
             if (d == dir) dcw = dchi_wl[d];
           const double a0 = 1.0 / (1.0 + geo->nz_z0[t]);
           const int2 sg0 = interp_segment_inc(a0, c->atab_chi, NCHI, logspace_guess(a0, NCHI));
-          const D1 chi0 = xfmax(interp_d1(a0, c->atab_chi, tb->chiv, tb->chid[dir], sg0), 0.0);
+          // chi(z0) from the float-pair chi table and its float tangents
+          const double ida = 1.0 / (c->atab_chi[sg0.y] - c->atab_chi[sg0.x]);
+          const D1 f0 = mk1((double)tb->chiF[sg0.x].x + (double)tb->chiF[sg0.x].y, (double)tb->chidF[sg0.x][dir]);
+          const D1 f1 = mk1((double)tb->chiF[sg0.y].x + (double)tb->chiF[sg0.y].y, (double)tb->chidF[sg0.y][dir]);
+          const D1 chi0 = xfmax(f0 + (f1 - f0) * (ida * (a0 - c->atab_chi[sg0.x])), 0.0);
           const D1 r = xfmax(chi0 - mk1((double)chi_wl, (double)dcw), 0.0) / xfmax(chi0, 1.0);
           const float rv = (float)r.v, rd = (float)r.d[0];
           const float fac = cff * zp1, m1 = 1.f + (float)geo->mult[t];

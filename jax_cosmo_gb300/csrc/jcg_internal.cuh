@@ -95,6 +95,8 @@ struct ConstTables {
   double grow_ida[NGROW];      // 1 / (atab_grow[i + 1] - atab_grow[i]) (i < NGROW - 1)
   float2 chi_ida_ff[NCHI], grow_ida_ff[NGROW], logr_ff[NRT];  // pair copies of the three above
   float2 atab_chi_ff[NCHI];    // pair copy of atab_chi
+  float2 chi_h6_ff[NCHI];      // (lna_chi[i] - lna_chi[i - 1]) / 6 as pairs (i >= 1; 0 at i = 0)
+  float2 romb_w_ff[NROMB];     // pair copy of romb_w
 };
 
 // ------------------------------------------------- per-cosmology tables -----

@@ -170,6 +170,7 @@ __global__ void const_ff_kernel(ConstTables* c) {
     c->sincos_ff[2 * j + 1] = f2_of(cos(a));
   }
   for (int e = tid; e < NROMB; e += nth) {
+    c->romb_w_ff[e] = f2_of(c->romb_w[e]);
     c->romb_k_ff[e] = f2_of(c->romb_k[e]);
     c->romb_logk_ff[e] = f2_of(c->romb_logk[e]);
     c->romb_ik_ff[e] = f2_of(c->romb_ik[e]);
@@ -192,6 +193,7 @@ __global__ void const_ff_kernel(ConstTables* c) {
     c->chi_ida[i] = i < NCHI - 1 ? 1.0 / (c->atab_chi[i + 1] - c->atab_chi[i]) : 0.0;
     c->chi_ida_ff[i] = f2_of(c->chi_ida[i]);
     c->atab_chi_ff[i] = f2_of(c->atab_chi[i]);
+    c->chi_h6_ff[i] = f2_of(i > 0 ? (c->lna_chi[i] - c->lna_chi[i - 1]) * (1.0 / 6.0) : 0.0);
   }
   for (int j = tid; j < NRT; j += nth) c->logr_ff[j] = f2_of(c->logr[j]);
   for (int i = tid; i < NGROW; i += nth) {
