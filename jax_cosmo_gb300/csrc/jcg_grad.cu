@@ -33,36 +33,41 @@ typedef DualFF<NDIR> FF8;
 // lane; the sigma^2(R) tangents are FP32 sums; float copies of the chi and
 // P(k) k^3 tangent tables are written for the FP32 stages.  The sequential
 // scans (chi prefix sum, growth RK4, Romberg) stay FP64 Dual<1>.
-// fp32c node values in 8-byte slots of the [component][node] arrays: the
-// value as a float pair (hi, lo), a tangent as a float in the slot's low
-// half; written by grad_nodes_kernel, read by grad_tables_kernel with no
-// float64 conversion on either side.
-__device__ __forceinline__ void put_slots(double* arr, int stride, int e, const FF8& x) {
-  *reinterpret_cast<float2*>(arr + e) = make_float2(x.v.hi, x.v.lo);
+// fp32c node arrays, packed: [n] float-pair values (float2), then
+// [NDIR][n] float tangents (5 n doubles of storage); written by
+// grad_nodes_kernel, read by grad_tables_kernel, no float64 conversion on
+// either side.
+__device__ __forceinline__ void put_packed(double* arr, int n, int e, const FF8& x) {
+  reinterpret_cast<float2*>(arr)[e] = make_float2(x.v.hi, x.v.lo);
+  float* tg = reinterpret_cast<float*>(arr + n);
 #pragma unroll
-  for (int d = 0; d < NDIR; ++d) *reinterpret_cast<float*>(arr + (1 + d) * stride + e) = x.d[d];
+  for (int d = 0; d < NDIR; ++d) tg[d * n + e] = x.d[d];
 }
-__device__ __forceinline__ FF slot_v(const double* arr, int e) {
-  const float2 v = *reinterpret_cast<const float2*>(arr + e);
+__device__ __forceinline__ FF packed_v(const double* arr, int e) {
+  const float2 v = reinterpret_cast<const float2*>(arr)[e];
   return FF{v.x, v.y};
 }
-__device__ __forceinline__ float slot_t(const double* arr, int e) { return *reinterpret_cast<const float*>(arr + e); }
-__device__ __forceinline__ FF8 ff8_slots(const double* arr, int stride, int e) {
+__device__ __forceinline__ float packed_t(const double* arr, int n, int d, int e) {
+  return reinterpret_cast<const float*>(arr + n)[d * n + e];
+}
+__device__ __forceinline__ FF8 ff8_packed(const double* arr, int n, int e) {
   FF8 r;
-  r.v = slot_v(arr, e);
+  r.v = packed_v(arr, e);
 #pragma unroll
-  for (int d = 0; d < NDIR; ++d) r.d[d] = slot_t(arr + (1 + d) * stride, e);
+  for (int d = 0; d < NDIR; ++d) r.d[d] = packed_t(arr, n, d, e);
   return r;
 }
 
 // The chi table (background.py:227-233) of one component for one warp, in
-// float pairs from the slot arrays: prefix sums of the RK4 increments
+// float pairs from the packed arrays: prefix sums of the RK4 increments
 // h/6 (f_{i-1} + 2 fm_i + 2 fm_i + f_i) in ln a (scipy/ode.py:21, the first
 // step has h = 0), then chi_i = Y[-1] - Y_i.  Lane l holds nodes
 // 8l .. 8l + 7 (returned in v).  The value (comp 0) forms its increments in
 // float pairs; a tangent in FP32 (its inputs are FP32).
-__device__ __forceinline__ void chi_scan_ff(const double* fnode, const double* fmid, const float2* h6, bool value,
+__device__ __forceinline__ void chi_scan_ff(const double* fnode, const double* fmid, const float2* h6, int comp,
                                             int lane, FF* v) {
+  const bool value = comp == 0;
+  const int d = comp - 1;
   FF loc[8];
   FF s{0.f, 0.f};
 #pragma unroll
@@ -70,11 +75,12 @@ __device__ __forceinline__ void chi_scan_ff(const double* fnode, const double* f
     const int i = lane * 8 + k;
     if (i > 0) {
       if (value) {
-        const FF fmv = slot_v(fmid, i);
-        s = s + (((slot_v(fnode, i - 1) + ff_scale2(fmv, 2.f)) + ff_scale2(fmv, 2.f)) + slot_v(fnode, i)) * f2ff(h6[i]);
+        const FF fmv = packed_v(fmid, i);
+        s = s + (((packed_v(fnode, i - 1) + ff_scale2(fmv, 2.f)) + ff_scale2(fmv, 2.f)) + packed_v(fnode, i)) *
+                    f2ff(h6[i]);
       } else {
-        const float fmv = slot_t(fmid, i);
-        s = s + h6[i].x * (((slot_t(fnode, i - 1) + 2.f * fmv) + 2.f * fmv) + slot_t(fnode, i));
+        const float fmv = packed_t(fmid, NCHI, d, i);
+        s = s + h6[i].x * (((packed_t(fnode, NCHI, d, i - 1) + 2.f * fmv) + 2.f * fmv) + packed_t(fnode, NCHI, d, i));
       }
     }
     loc[k] = s;
@@ -94,18 +100,20 @@ __device__ __forceinline__ void chi_scan_ff(const double* fnode, const double* f
 
 // NW: some item may use the transfer type "eisenhu"
 template <bool F32T, bool NW>
-__global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
+__global__ void __launch_bounds__(F32T ? 128 : 256, F32T ? 4 : 1) grad_tables_kernel(GradBatch gb, const ConstTables* __restrict__ c) {
   const int item = blockIdx.x;
   if (item >= gb.n_items) return;
   extern __shared__ __align__(16) double sm[];
   double* sv = sm;                      // NSCAL
   double* sd = sv + NSCAL;              // [NDIR][NSCAL]
-  double* fn = sd + NDIR * NSCAL;       // [NDIR+1][NCHI] f at nodes
-  double* fm = fn + (NDIR + 1) * NCHI;  // [NDIR+1][NCHI] f at midpoints
-  double* qr = fm + (NDIR + 1) * NCHI;  // [4][NDIR+1][NGROW] qa, ra, qm, rm
-  double* fr = qr + 4 * (NDIR + 1) * NGROW;   // [NDIR+1][NROMB]
-  double* g1s = fr + (NDIR + 1) * NROMB;      // [NDIR+1]
-  double* pq = qr;                            // [NDIR+1][NKH], after the growth RK4
+  // FP64: [NDIR+1][n] doubles per array; fp32c: the packed layout of
+  // grad_nodes_kernel (GNODE_* offsets)
+  double* fn = sd + NDIR * NSCAL;       // f at the chi nodes
+  double* fm = fn + (F32T ? GNODE_FM : (NDIR + 1) * NCHI);  // f at the chi midpoints
+  double* qr = fn + (F32T ? GNODE_QR : 2 * (NDIR + 1) * NCHI);  // qa, ra, qm, rm
+  double* fr = fn + (F32T ? GNODE_FR : 2 * (NDIR + 1) * NCHI + 4 * (NDIR + 1) * NGROW);  // Romberg integrand
+  double* g1s = F32T ? fn + GNODE_U : fr + (NDIR + 1) * NROMB;  // [NDIR+1]
+  double* pq = qr;                            // FP64: [NDIR+1][NKH], after the growth RK4
   const int t = threadIdx.x, dir = t & 7, it = t >> 3;
   const GradItem gi = grad_item(gb, item);
   TabD* out = gi.tab;
@@ -164,12 +172,13 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       put(fr, NROMB, e, k * (kw * kw) * pk);
     }
   } else {
-    // node values from grad_nodes_kernel (slots): the same layout as fn .. fr here;
+    // node values from grad_nodes_kernel: the same packed layout as fn .. fr here;
     // 16-byte copies, eight in flight per thread
     static_assert((9 * NSCAL) % 2 == 0 && GNODE_STRIDE % 2 == 0, "16-byte aligned node copy");
+    static_assert(GNODE_U % 2 == 0, "whole 16-byte node copies");
     const double2* src = reinterpret_cast<const double2*>(gb.gnode + (size_t)item * GNODE_STRIDE);
     double2* dst = reinterpret_cast<double2*>(fn);
-    constexpr int NV = (GNODE_U + 1) / 2;
+    constexpr int NV = GNODE_U / 2;
     for (int i0 = t; i0 < NV; i0 += 8 * blockDim.x) {
       double2 v[8];
 #pragma unroll
@@ -199,10 +208,10 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       for (int d = 0; d < NDIR; ++d) dm4[q][d] = 0.f;
     if (t >= 1 && t < NGROW) {
       const double* QA = qr;
-      const double* RA = qr + (NDIR + 1) * NGROW;
-      const double* QM = qr + 2 * (NDIR + 1) * NGROW;
-      const double* RM = qr + 3 * (NDIR + 1) * NGROW;
-      auto g8 = [&](const double* arr, int e) { return ff8_slots(arr, NGROW, e); };
+      const double* RA = qr + 5 * NGROW;
+      const double* QM = qr + 10 * NGROW;
+      const double* RM = qr + 15 * NGROW;
+      auto g8 = [&](const double* arr, int e) { return ff8_packed(arr, NGROW, e); };
       const FF8 qa0 = g8(QA, t - 1), ra0 = g8(RA, t - 1), qm = g8(QM, t), rm = g8(RM, t);
       const FF8 qa1 = g8(QA, t), ra1 = g8(RA, t);
       const double hh = c->atab_grow[t] - c->atab_grow[t - 1];
@@ -223,6 +232,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     double* Yv = qr + 4 * NGROW + 2 * NDIR * NGROW;           // [NGROW][2] y_i
     float* Mvf = reinterpret_cast<float*>(Yv + 2 * NGROW);   // [NGROW][4] float copies
     float* Yvf = Mvf + 4 * NGROW;                             // [NGROW][2] float copies
+    static_assert(4 * NGROW + 2 * NDIR * NGROW + 2 * NGROW + 3 * NGROW <= GNODE_QR_SPAN, "growth scratch span");
     if (t < NGROW) {
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
@@ -252,7 +262,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       // the sums
       for (int comp = warp - 1; comp < NDIR + 1; comp += 3) {
         FF v[8];
-        chi_scan_ff(fn + comp * NCHI, fm + comp * NCHI, c->chi_h6_ff, comp == 0, lane, v);
+        chi_scan_ff(fn, fm, c->chi_h6_ff, comp, lane, v);
         const FF vn{__shfl_down_sync(0xffffffffu, v[0].hi, 1), __shfl_down_sync(0xffffffffu, v[0].lo, 1)};
 #pragma unroll
         for (int k = 0; k < 8; ++k) {
@@ -268,17 +278,16 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
       // sum_e w_e f_e with the weights of the Richardson combination (the
       // value in float pairs, a tangent in FP32)
       for (int comp = warp - 1; comp < NDIR + 1; comp += 3) {
-        const double* fc = fr + comp * NROMB;
         if (comp == 0) {
           FF sf{0.f, 0.f};
-          for (int e = lane; e < NROMB; e += 32) sf = sf + f2ff(c->romb_w_ff[e]) * slot_v(fc, e);
+          for (int e = lane; e < NROMB; e += 32) sf = sf + f2ff(c->romb_w_ff[e]) * packed_v(fr, e);
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1)
             sf = sf + FF{__shfl_xor_sync(0xffffffffu, sf.hi, o), __shfl_xor_sync(0xffffffffu, sf.lo, o)};
           if (lane == 0) sv[S_SIGMASQR8] = ffd(sf * ffc(1.0 / (2.0 * (PI * PI))));
         } else {
           float sf = 0.f;
-          for (int e = lane; e < NROMB; e += 32) sf = fmaf(c->romb_w_ff[e].x, slot_t(fc, e), sf);
+          for (int e = lane; e < NROMB; e += 32) sf = fmaf(c->romb_w_ff[e].x, packed_t(fr, NROMB, comp - 1, e), sf);
 #pragma unroll
           for (int o = 16; o > 0; o >>= 1) sf += __shfl_xor_sync(0xffffffffu, sf, o);
           if (lane == 0) sd[(comp - 1) * NSCAL + S_SIGMASQR8] = (double)(sf * (float)(1.0 / (2.0 * (PI * PI))));
@@ -458,7 +467,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256) grad_tables_kernel(GradBatch
     const FF8 pkn = ff8_of(sv[S_PKNORM], sd + S_PKNORM, NSCAL);
     const double* gu = gb.gnode + (size_t)item * GNODE_STRIDE + GNODE_U;
     for (int e = t; e < NKH; e += blockDim.x) {
-      const FF8 u = ff8_slots(gu, NKH, e);
+      const FF8 u = ff8_packed(gu, NKH, e);
       const FF8 p3 = ((u * g1sq) * pkn) * c->kh3[e];
       out->pk3v[e] = val(p3);
       float4* pd = reinterpret_cast<float4*>(&out->pk3df[e][0]);
@@ -641,8 +650,9 @@ __global__ void __launch_bounds__(NRT) grad_moments32_kernel(GradBatch gb, const
   }
 }
 
-size_t grad_tables_smem() {
+size_t grad_tables_smem(bool f32t) {
   static_assert(4 * NGROW >= NKH, "P(k) k^3 staging aliases the growth coefficients");
+  if (f32t) return sizeof(double) * (NSCAL * (1 + NDIR) + GNODE_U + NDIR + 1);
   return sizeof(double) * (NSCAL * (1 + NDIR) + (NDIR + 1) * (2 * NCHI + 4 * NGROW + NROMB + 1));
 }
 
@@ -1833,10 +1843,10 @@ __global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const Con
   const int w = blockIdx.x * blockDim.x + threadIdx.x;
   const BgT<FF8> bgf = make_bgT(sF);
   double* dst = gb.gnode + (size_t)item * GNODE_STRIDE;
-  auto putf = [&](int off, int stride, int i, const FF8& x) { put_slots(dst + off, stride, i, x); };
+  auto putf = [&](int off, int n, int i, const FF8& x) { put_packed(dst + off, n, i, x); };
   if (KIND == 0) {
     if (w < NCHI) {
-      putf(0, NCHI, w, dchi_dlna_f8(bgf, f2ff(c->chi_a_ff[w]), f2ff(c->lna_chi_ff[w]), f2ff(c->chi_ia_ff[w])));
+      putf(GNODE_FN, NCHI, w, dchi_dlna_f8(bgf, f2ff(c->chi_a_ff[w]), f2ff(c->lna_chi_ff[w]), f2ff(c->chi_ia_ff[w])));
     } else if (w < 2 * NCHI - 1) {
       const int i = w - NCHI + 1;
       putf(GNODE_FM, NCHI, i, dchi_dlna_f8(bgf, f2ff(c->chi_am_ff[i]), f2ff(c->chi_lnam_ff[i]), f2ff(c->chi_iam_ff[i])));
@@ -1846,12 +1856,12 @@ __global__ void __launch_bounds__(128) grad_nodes_kernel(GradBatch gb, const Con
     if (w < NGROW) {
       growth_qr_f8(bgf, f2ff(c->grow_a_ff[w]), f2ff(c->grow_lna_ff[w]), f2ff(c->grow_ia_ff[w]), q, r);
       putf(GNODE_QR, NGROW, w, q);
-      putf(GNODE_QR + (NDIR + 1) * NGROW, NGROW, w, r);
+      putf(GNODE_QR + 5 * NGROW, NGROW, w, r);
     } else if (w < 2 * NGROW - 1) {
       const int i = w - NGROW + 1;
       growth_qr_f8(bgf, f2ff(c->grow_am_ff[i]), f2ff(c->grow_lnam_ff[i]), f2ff(c->grow_iam_ff[i]), q, r);
-      putf(GNODE_QR + 2 * (NDIR + 1) * NGROW, NGROW, i, q);
-      putf(GNODE_QR + 3 * (NDIR + 1) * NGROW, NGROW, i, r);
+      putf(GNODE_QR + 10 * NGROW, NGROW, i, q);
+      putf(GNODE_QR + 15 * NGROW, NGROW, i, r);
     }
   } else if (w < NROMB + NKH) {
     const bool romb = w < NROMB;
@@ -1990,7 +2000,7 @@ __global__ void __launch_bounds__(32 * NDIR) grad_growth_gamma_kernel(GradBatch 
 }
 
 void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t st, unsigned stages) {
-  const size_t smt = grad_tables_smem();
+  const size_t smt = grad_tables_smem(gb.precision == JCG_FP32C);
   if (stages & GS_TABLES) {
   if (gb.n_items <= GNODE_MAX_ITEMS)
     grad_scalars_warp_kernel<<<gb.n_items, 16 * NDIR, 0, st>>>(gb);
@@ -2006,9 +2016,13 @@ void launch_grad_front(const GradBatch& gb, const ConstTables* c, cudaStream_t s
   if (gb.precision == JCG_FP32C) {
     if (tf_nowiggle(gb.physics_or)) {
       cudaFuncSetAttribute(grad_tables_kernel<true, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+      cudaFuncSetAttribute(grad_tables_kernel<true, true>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);  // four CTAs per SM
       grad_tables_kernel<true, true><<<gb.n_items, 128, smt, st>>>(gb, c);
     } else {
       cudaFuncSetAttribute(grad_tables_kernel<true, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smt);
+      cudaFuncSetAttribute(grad_tables_kernel<true, false>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                           (int)cudaSharedmemCarveoutMaxShared);  // four CTAs per SM
       grad_tables_kernel<true, false><<<gb.n_items, 128, smt, st>>>(gb, c);
     }
   } else {

@@ -213,17 +213,21 @@ struct GradBatch {
 };
 
 // fp32c batches run the table kernel's per-node evaluations in
-// grad_nodes_kernel (one node per thread) and hand them over in
-// the table kernel's shared-memory layout: chi right-hand sides at nodes and
-// midpoints [2][NDIR + 1][NCHI], growth coefficients [4][NDIR + 1][NGROW],
-// the Romberg integrand [NDIR + 1][NROMB], then exp(n_s ln k) T(k)^2 on the
-// P(k) grid [NDIR + 1][NKH] (value, then 8 tangents).
+// grad_nodes_kernel (one node per thread) and hand them over in the table
+// kernel's shared-memory layout, each node array packed as [n] float-pair
+// values then [NDIR][n] float tangents (5 n doubles): chi right-hand sides at
+// nodes and midpoints, growth coefficients qa, ra, qm, rm (in a span that the
+// table kernel reuses for the growth scan's scratch), the Romberg integrand,
+// then exp(n_s ln k) T(k)^2 on the P(k) grid (read from global memory).
 constexpr int GNODE_MAX_ITEMS = 128;  // up to this many cosmologies the scalars run on half warps
-constexpr int GNODE_FM = (NDIR + 1) * NCHI;
-constexpr int GNODE_QR = 2 * (NDIR + 1) * NCHI;
-constexpr int GNODE_FR = GNODE_QR + 4 * (NDIR + 1) * NGROW;
-constexpr int GNODE_U = GNODE_FR + (NDIR + 1) * NROMB;
-constexpr size_t GNODE_STRIDE = (size_t)(GNODE_U + (NDIR + 1) * NKH + 31) / 32 * 32;
+constexpr int GNODE_FN = 0;
+constexpr int GNODE_FM = 5 * NCHI;
+constexpr int GNODE_QR = 10 * NCHI;
+constexpr int GNODE_QR_SPAN = 3200;  // >= 4 x 5 x NGROW and the growth scan's scratch
+constexpr int GNODE_FR = GNODE_QR + GNODE_QR_SPAN;
+constexpr int GNODE_U = (GNODE_FR + 5 * NROMB + 1) / 2 * 2;  // 16-byte aligned
+constexpr size_t GNODE_STRIDE = (size_t)(GNODE_U + 5 * NKH + 31) / 32 * 32;
+static_assert(GNODE_QR_SPAN >= 20 * NGROW, "growth coefficients fit their span");
 
 __device__ __forceinline__ GradItem grad_item(const GradBatch& gb, int i) {
   if (gb.listed) return gb.items[i];
