@@ -52,9 +52,9 @@ struct VjLayout {
   size_t rows_b, ks_b;  // the second buffer of each (the next chunk's copies)
   size_t cacc;
 };
-// C_ell summed in shared memory (float64, chunk order) when one CTA runs all
-// of a cosmology's chunks in one ell tile and the sums fit
-constexpr int VJ_CACC_MAX = 3072;  // n_cls x n_ell doubles (24 kB)
+// C_ell summed in shared memory (float pairs, chunk order) when one CTA runs
+// all of a cosmology's chunks in one ell tile and the sums fit
+constexpr int VJ_CACC_MAX = 3072;  // n_cls x n_ell float pairs (24 kB)
 __host__ __device__ inline int vj_cacc(int n_cls, int n_ell, int LT, int G) {
   return G == 1 && n_ell <= LT && n_cls * n_ell <= VJ_CACC_MAX ? n_cls * n_ell : 0;
 }
@@ -93,12 +93,12 @@ __host__ __device__ inline VjLayout vj_layout(int n_tr, int n_cls, int LT, int n
   o = (o + 15) & ~(size_t)15;
   L.qd = o;                                   // [VJ_TA][n_cls] float pairs
   o += 8 * (size_t)VJ_TA * n_cls;
-  L.red = o;                                  // [VJ_THREADS / 32][NET] floats, then [VJ_TA][NDIR] doubles
+  L.red = o;                                  // [VJ_THREADS / 32][NET] floats, then [VJ_TA][NDIR] doubles of room
   o += 4 * (size_t)(VJ_THREADS / 32) * NET;
   o = (o + 15) & ~(size_t)15;
   o += 8 * (size_t)VJ_TA * NDIR;
   o = (o + 15) & ~(size_t)15;
-  L.cacc = o;                                 // [n_cls][n_ell] doubles (or none)
+  L.cacc = o;                                 // [n_cls][n_ell] float pairs (or none)
   o += 8 * (size_t)ncacc;
   L.total = o;
   return L;
@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   const int ncacc = (FWD || gb.vjp_cl) && !gb.listed ? vj_cacc(n_cls, n_ell, LT, G) : 0;  // as the launch
   const VjLayout L = vj_layout(n_tr, n_cls, LT, ncacc);
   extern __shared__ __align__(16) unsigned char vj_smem[];
-  double* Cacc = reinterpret_cast<double*>(vj_smem + L.cacc);
+  float2* Cacc = reinterpret_cast<float2*>(vj_smem + L.cacc);
   float* ev = reinterpret_cast<float*>(vj_smem + L.ev);
   float* et = ev + 16;
   float* khv = reinterpret_cast<float*>(vj_smem + L.kh);
@@ -154,7 +154,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   float* Abar = reinterpret_cast<float*>(vj_smem + L.abar);
   float2* Qd = reinterpret_cast<float2*>(vj_smem + L.qd);  // Q_p(t) as (hi, lo)
   float* Ered = reinterpret_cast<float*>(vj_smem + L.red);
-  double* gred = reinterpret_cast<double*>(vj_smem + ((L.red + 4 * (VJ_THREADS / 32) * NET + 15) & ~(size_t)15));
+  float2* gred = reinterpret_cast<float2*>(vj_smem + ((L.red + 4 * (VJ_THREADS / 32) * NET + 15) & ~(size_t)15));
   const int tid = threadIdx.x, grp = tid >> 3, sub = tid & (VJ_GROUP - 1);
   const TabD* tb = gi.tab;
   // a chunk's FP32 rows (values and tangents) and radial kernels into buffer
@@ -209,7 +209,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
   };
   const bool one_tile = n_ell <= LT;
   if (one_tile) fill_tile(0, n_ell);
-  for (int i = tid; i < ncacc; i += VJ_THREADS) Cacc[i] = 0.0;
+  for (int i = tid; i < ncacc; i += VJ_THREADS) Cacc[i] = make_float2(0.f, 0.f);
   // the CTA's chunks blockIdx.x, blockIdx.x + G, ...: the next chunk's rows
   // are copied while this one runs
   for (int chunk = blockIdx.x, it = 0; chunk < nch; chunk += G, ++it) {
@@ -322,8 +322,14 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
           for (int k = 0; k < 4; ++k) {
             if (lq + k >= lt) break;
             if (ncacc) {  // the chunks in order, as the global sum below
-              Cacc[p0 * n_ell + lq + k] += (double)r0[k];
-              if (two) Cacc[(p0 + 1) * n_ell + lq + k] += (double)r1[k];
+              float2* c0p = Cacc + p0 * n_ell + lq + k;
+              const FF s0 = FF{c0p->x, c0p->y} + r0[k];
+              *c0p = make_float2(s0.hi, s0.lo);
+              if (two) {
+                float2* c1p = c0p + n_ell;
+                const FF s1 = FF{c1p->x, c1p->y} + r1[k];
+                *c1p = make_float2(s1.hi, s1.lo);
+              }
             } else {
               cp[(size_t)p0 * n_ell + l0 + lq + k] = r0[k];
               if (two) cp[(size_t)(p0 + 1) * n_ell + l0 + lq + k] = r1[k];
@@ -399,18 +405,18 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
         const size_t per = (size_t)n_cls * n_ell;
         for (int idx = tid; idx < (int)per; idx += VJ_THREADS) {
           const int p = idx / n_ell, l = idx - p * n_ell;
-          // chunks added in order; loads issued eight at a time
-          double s = 0.0;
+          // chunks added in order, in float pairs; loads issued eight at a time
+          FF s{0.f, 0.f};
           int c = 0;
           for (; c + 8 <= nch; c += 8) {
             float v[8];
 #pragma unroll
             for (int k = 0; k < 8; ++k) v[k] = __ldcg(gi.cpart + (size_t)(c + k) * per + idx);
 #pragma unroll
-            for (int k = 0; k < 8; ++k) s += (double)v[k];
+            for (int k = 0; k < 8; ++k) s = s + v[k];
           }
-          for (; c < nch; ++c) s += (double)__ldcg(gi.cpart + (size_t)c * per + idx);
-          gi.cl[idx] = s * EF[(size_t)geo->pair_i[p] * n_ell + l] * EF[(size_t)geo->pair_j[p] * n_ell + l];
+          for (; c < nch; ++c) s = s + __ldcg(gi.cpart + (size_t)c * per + idx);
+          gi.cl[idx] = ffd(s) * EF[(size_t)geo->pair_i[p] * n_ell + l] * EF[(size_t)geo->pair_j[p] * n_ell + l];
         }
       }
       if (s_last && tid == 0) gb.cl_count[item] = 0;
@@ -468,10 +474,12 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
       Ered[2 * tid + 1] = ej.lo;
     }
     __syncthreads();
-    // projection on the tangents: thread (a node t, direction d)
+    // projection on the tangents: thread (a node t, direction d), in float
+    // pairs; the sum over t by shuffles within the warp (4 nodes), then over
+    // the 8 warps in order
     {
       const int t = tid >> 3, d = tid & 7;
-      double gd = 0.0;
+      FF gd{0.f, 0.f};
       if (t < tc) {
         const float* row = R + (size_t)t * NROWG;
         const float* tg = row + NROWV;
@@ -481,7 +489,6 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
           if (!GEN && j == T_MUN) continue;
           s = fmaf(Abar[t * NGT + j], tg[j * NDIR + d], s);
         }
-        gd = (double)s;
         // sum_p Q_p (du K_i K_j + u (dK_i K_j + K_i dK_j)), in float pairs
         const float u = row[F_U], du = tg[T_U * NDIR + d];
         const float2* q = Qd + (size_t)t * n_cls;
@@ -496,21 +503,24 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
             sm = sm + FF{q[p].x, q[p].y} * dm;
           }
         }
-        gd += ffd(sm);
+        gd = sm + s;
       }
       if (t == 0) {
         // the cosmology's Eisenstein-Hu inputs, once per CTA
         FF se{0.f, 0.f};
         for (int j = 0; j < NET; ++j) se = se + FF{Ered[2 * j], Ered[2 * j + 1]} * et[j * NDIR + d];
-        gd += ffd(se);
+        gd = gd + se;
       }
-      gred[t * NDIR + d] = gd;
+#pragma unroll
+      for (int o = 8; o < 32; o <<= 1)
+        gd = gd + FF{__shfl_xor_sync(0xffffffffu, gd.hi, o), __shfl_xor_sync(0xffffffffu, gd.lo, o)};
+      if (lane < NDIR) gred[warp * NDIR + lane] = make_float2(gd.hi, gd.lo);
     }
     __syncthreads();
     if (tid < NDIR) {
-      double g = 0.0;
-      for (int t = 0; t < VJ_TA; ++t) g += gred[t * NDIR + tid];
-      gi.gpart[(size_t)chunk * NDIR + tid] = g;
+      FF g{0.f, 0.f};
+      for (int w = 0; w < VJ_THREADS / 32; ++w) g = g + FF{gred[w * NDIR + tid].x, gred[w * NDIR + tid].y};
+      gi.gpart[(size_t)chunk * NDIR + tid] = ffd(g);
     }
     __syncthreads();  // this chunk's buffers and scratch are free
   }
@@ -519,7 +529,8 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
     const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
     for (int idx = tid; idx < ncacc; idx += VJ_THREADS) {
       const int p = idx / n_ell, l = idx - p * n_ell;
-      gi.cl[idx] = Cacc[idx] * EF[(size_t)geo->pair_i[p] * n_ell + l] * EF[(size_t)geo->pair_j[p] * n_ell + l];
+      gi.cl[idx] = ffd(FF{Cacc[idx].x, Cacc[idx].y}) * EF[(size_t)geo->pair_i[p] * n_ell + l] *
+                   EF[(size_t)geo->pair_j[p] * n_ell + l];
     }
   }
 }
