@@ -286,16 +286,13 @@ def gpu_arm(args, rank, world, device):
     clk = clocks.stop()
     # plain float64 method on the same workload (fewer steps: it is ~100x slower)
     t64, per64 = timed(lambda: step("fp64"), max(1, min(args.steps, 2)), 1)
-    # e2e through the public API: pinned host params in, C_ell out
+    # e2e through the public host-buffer entry (jcg_angular_cl_host): pinned
+    # host params in, C_ell out to pinned host memory, both inside each step
     host_p = torch.as_tensor(P).pin_memory()
     host_cl = torch.empty(B, n_cls, n_ell, dtype=torch.float64).pin_memory()
-    cosmo_cols = None
 
     def e2e_step():
-        dev_p = host_p.to(device, non_blocking=True)
-        cosmo = jc.Cosmology(*[dev_p[:, i] for i in range(8)])
-        out = jc.cl.angular_cl(cosmo, ell_np, probes, precision="fp32c")
-        host_cl.copy_(out, non_blocking=True)
+        jc.cl.angular_cl_host(host_p, ell_np, probes, precision="fp32c", out=host_cl)
 
     t_e2e, _ = timed(e2e_step, args.steps, args.warmup)
     # Limber kernel alone (the dominant kernel) for the roofline, same stream

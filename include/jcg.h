@@ -206,6 +206,24 @@ int jcg_angular_cl(const jcg_geometry* g, const void* geo_dev, const double* par
 int jcg_angular_cl_noalloc(const jcg_geometry* g, const void* geo_dev, const double* params_dev,
                            int n_cosmo, int precision, double* cl_dev, cudaStream_t stream);
 
+/* jcg_angular_cl with host buffers: params_host [n_cosmo][8] (9 with the
+ * gamma growth) and cl_host [n_cosmo][n_cls][n_ell] in host memory, the
+ * boundary of a caller that holds no device arrays (a JAX host callback
+ * binding angular_cl.py:49-98, a CPU sampler).  The parameters are copied in
+ * on `stream`; the Limber stage runs over up to JCG_HOST_SLICES ranges of
+ * cosmologies and each range's C_ell are copied out on a copy stream of the
+ * calling thread while the next range computes; `stream` then waits for the
+ * last copy, so cl_host is complete once `stream` is synchronised.  With
+ * pinned host memory (cudaHostAlloc / cudaHostRegister) the call returns
+ * without waiting; with pageable memory the copies wait for the GPU.  The
+ * workspace (jcg_host_workspace_size) is jcg_angular_cl's plus device copies
+ * of the parameters and the C_ell. */
+#define JCG_HOST_SLICES 4
+int jcg_host_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t* bytes);
+int jcg_angular_cl_host(const jcg_geometry* g, const void* geo_dev, const double* params_host, int n_cosmo,
+                        int precision, double* cl_host, void* workspace, size_t workspace_bytes,
+                        cudaStream_t stream);
+
 /* Stage entry points of the same pipeline (for tests and for callers that keep
  * tables resident).  The workspace is the one of jcg_angular_cl. */
 int jcg_stage_cosmo_tables(const jcg_geometry* g, const double* params_dev, int n_cosmo,

@@ -109,6 +109,8 @@ SIGNATURES = {
     "jcg_workspace_size": [_PG, _I, _I, _PSZ],
     "jcg_angular_cl": [_PG, _P, _P, _I, _I, _P, _P, _SZ, _P],
     "jcg_angular_cl_noalloc": [_PG, _P, _P, _I, _I, _P, _P],
+    "jcg_host_workspace_size": [_PG, _I, _I, _PSZ],
+    "jcg_angular_cl_host": [_PG, _P, _P, _I, _I, _P, _P, _SZ, _P],
     "jcg_stage_cosmo_tables": [_PG, _P, _I, _I, _P, _SZ, _P],
     "jcg_stage_halofit_rows": [_PG, _P, _P, _I, _I, _P, _SZ, _P],
     "jcg_stage_tracer_kernels": [_PG, _P, _P, _I, _I, _P, _SZ, _P],

@@ -109,6 +109,43 @@ def angular_cl_device(params, ell, probes, precision="fp64", n_limber=512, out=N
     return out
 
 
+def angular_cl_host(params, ell, probes, precision="fp64", n_limber=512, out=None, physics=0, device=None):
+    """C_ell for a [B, 8] float64 parameter tensor in HOST memory -> a host
+    [B, n_cls, n_ell] tensor (``jcg_angular_cl_host``).
+
+    The caller without device arrays (a JAX host callback, a CPU sampler):
+    the parameters go to the GPU and the C_ell come back inside the call, the
+    copies out overlapping the Limber integral of the next range of
+    cosmologies.  Pinned tensors (``pin_memory()``) keep the call
+    asynchronous: ``out`` is complete after ``torch.cuda.synchronize()`` (or
+    the current stream's synchronisation); with pageable tensors the call
+    returns after the copies.  ``[B, 9]`` with gamma last when ``physics``
+    has GROWTH_GAMMA.
+    """
+    device = _lib.require_cuda(device)
+    if params.device.type != "cpu" or params.dtype != torch.float64 or params.dim() != 2:
+        raise ValueError("params must be a [B, 8] float64 host tensor")
+    params = params.contiguous()
+    g, geo, _ = _geometry.get_geometry(probes, ell, n_limber, device, physics)
+    B = params.shape[0]
+    prec = _precision_code(precision)
+    n_cls = _geometry.n_cls_of(g)
+    if out is None:
+        out = torch.empty(B, n_cls, g.n_ell, dtype=torch.float64, pin_memory=params.is_pinned())
+    elif out.device.type != "cpu" or out.shape != (B, n_cls, g.n_ell) or not out.is_contiguous():
+        raise ValueError("out must be a contiguous [B, n_cls, n_ell] float64 host tensor")
+    wsz = ctypes.c_size_t()
+    _lib.call("jcg_host_workspace_size", ctypes.byref(g), B, prec, ctypes.byref(wsz))
+    ws = _lib.workspace(wsz.value, device)
+    _lib.call(
+        "jcg_angular_cl_host", ctypes.byref(g), _lib.ptr(geo), _lib.ptr(params), B, prec,
+        _lib.ptr(out), _lib.ptr(ws), ctypes.c_size_t(ws.numel()), _lib.stream_of(device),
+    )
+    # ws returns to the allocator of the current stream, which has waited for
+    # the copies: later work that reuses it runs after them
+    return out
+
+
 def angular_cl(
     cosmo,
     ell,

@@ -791,6 +791,124 @@ extern "C" int jcg_angular_cl_noalloc(const jcg_geometry* g, const void* geo, co
   return cuda_check("angular_cl_noalloc");
 }
 
+// ------------------------------------------------------- host buffers -----
+// jcg_angular_cl with the parameters and the C_ell in host memory.  The
+// workspace is jcg_angular_cl's followed by device copies of the parameters
+// and of the C_ell.  The Limber stage runs as up to JCG_HOST_SLICES launches
+// over ranges of cosmologies; each range's C_ell leave on a copy stream of
+// the calling thread as soon as its launch ends, so the copies run under the
+// remaining launches; the stream then waits for the last copy.
+namespace {
+struct HostLayout {
+  size_t params, cl, total;
+};
+struct HostCopy {
+  cudaStream_t copy = nullptr;
+  cudaEvent_t ev[JCG_HOST_SLICES + 1] = {};
+};
+}  // namespace
+
+static HostLayout host_layout(const GeoHeader& h, int n_cosmo, int precision) {
+  HostLayout L;
+  const size_t a = 256;
+  size_t o = (ws_layout(&h, n_cosmo, precision).total + a - 1) / a * a;
+  L.params = o;
+  o += ((size_t)n_cosmo * param_stride(h.physics) * sizeof(double) + a - 1) / a * a;
+  L.cl = o;
+  o += ((size_t)n_cosmo * h.n_cls * h.n_ell * sizeof(double) + a - 1) / a * a;
+  L.total = o;
+  return L;
+}
+
+// cosmologies [i0, i0 + n) of a uniform batch (the indexing of batch_item)
+static Batch batch_slice(const Batch& b, int i0, int n) {
+  Batch s = b;
+  const size_t na = (size_t)b.max_na;
+  s.n_items = n;
+  s.params = b.params + (size_t)param_stride(b.physics) * i0;
+  s.ctab = b.ctab + i0;
+  if (b.rows64) s.rows64 = b.rows64 + (size_t)i0 * na * NROW64;
+  if (b.rows32) s.rows32 = b.rows32 + (size_t)i0 * na * NROW32;
+  s.kern = b.kern + (size_t)i0 * b.max_tr * na;
+  s.cl = b.cl + (size_t)i0 * b.max_cls * b.max_ell;
+  return s;
+}
+
+// the copy stream and events of the calling host thread on device dev
+static int host_copy(int dev, HostCopy** out) {
+  static thread_local HostCopy hc[64];
+  HostCopy& r = hc[dev];
+  if (!r.copy) {
+    if (cudaStreamCreateWithFlags(&r.copy, cudaStreamNonBlocking) != cudaSuccess) {
+      r.copy = nullptr;
+      return cuda_check("copy stream");
+    }
+    for (int i = 0; i <= JCG_HOST_SLICES; ++i)
+      if (cudaEventCreateWithFlags(&r.ev[i], cudaEventDisableTiming) != cudaSuccess) return cuda_check("copy events");
+  }
+  *out = &r;
+  return JCG_OK;
+}
+
+// ranges of at least 1024 cosmologies, at most JCG_HOST_SLICES of them
+static int host_slices(int n_cosmo) {
+  const int ns = n_cosmo / 1024;
+  return ns < 1 ? 1 : (ns > JCG_HOST_SLICES ? JCG_HOST_SLICES : ns);
+}
+
+extern "C" int jcg_host_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t* bytes) {
+  if (!bytes) return fail(JCG_ERR_ARG, "bytes is NULL");
+  if (n_cosmo < 1) return fail(JCG_ERR_SHAPE, "n_cosmo = %d", n_cosmo);
+  if (precision != JCG_FP64 && precision != JCG_FP32C) return fail(JCG_ERR_ARG, "precision = %d", precision);
+  GeoHeader h;
+  const int rc = make_header(g, &h);
+  if (rc) return rc;
+  *bytes = host_layout(h, n_cosmo, precision).total;
+  return JCG_OK;
+}
+
+extern "C" int jcg_angular_cl_host(const jcg_geometry* g, const void* geo, const double* params_host,
+                                   int n_cosmo, int precision, double* cl_host, void* ws, size_t ws_bytes,
+                                   cudaStream_t stream) {
+  GeoHeader h;
+  int rc = make_header(g, &h);
+  if (rc) return rc;
+  if (!geo || !cl_host) return fail(JCG_ERR_ARG, "geometry or cl is NULL");
+  if (h.custom_nodes) return fail(JCG_ERR_ARG, "a geometry with caller redshift nodes has no Limber grid");
+  if ((rc = check_common(params_host, n_cosmo, precision, ws, ws_bytes, 0))) return rc;
+  const HostLayout HL = host_layout(h, n_cosmo, precision);
+  if (ws_bytes < HL.total) return fail(JCG_ERR_WORKSPACE, "workspace %zu bytes, need %zu", ws_bytes, HL.total);
+  ConstTables* c = nullptr;
+  if ((rc = const_tables(&c))) return rc;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return fail(JCG_ERR_CUDA, "cudaGetDevice failed");
+  HostCopy* hc = nullptr;
+  if ((rc = host_copy(dev, &hc))) return rc;
+  char* base = static_cast<char*>(ws);
+  double* dparams = reinterpret_cast<double*>(base + HL.params);
+  double* dcl = reinterpret_cast<double*>(base + HL.cl);
+  const size_t pbytes = (size_t)n_cosmo * param_stride(h.physics) * sizeof(double);
+  if (cudaMemcpyAsync(dparams, params_host, pbytes, cudaMemcpyHostToDevice, stream) != cudaSuccess)
+    return cuda_check("angular_cl_host parameters");
+  const Batch b = make_batch(&h, geo, dparams, n_cosmo, precision, ws, dcl);
+  launch_cosmo_tables(b, c, stream);
+  launch_halofit_rows(b, c, stream);
+  launch_tracer_kernels(b, c, stream);
+  const int ns = host_slices(n_cosmo), lt = limber_tile(h.n_ell);
+  const size_t per = (size_t)h.n_cls * h.n_ell;
+  for (int k = 0; k < ns; ++k) {
+    const int i0 = (int)((long long)n_cosmo * k / ns), i1 = (int)((long long)n_cosmo * (k + 1) / ns);
+    launch_limber(batch_slice(b, i0, i1 - i0), c, lt, stream);
+    if (cudaEventRecord(hc->ev[k], stream) != cudaSuccess || cudaStreamWaitEvent(hc->copy, hc->ev[k], 0) != cudaSuccess ||
+        cudaMemcpyAsync(cl_host + (size_t)i0 * per, dcl + (size_t)i0 * per, (size_t)(i1 - i0) * per * sizeof(double),
+                        cudaMemcpyDeviceToHost, hc->copy) != cudaSuccess)
+      return cuda_check("angular_cl_host copies");
+  }
+  if (cudaEventRecord(hc->ev[ns], hc->copy) != cudaSuccess || cudaStreamWaitEvent(stream, hc->ev[ns], 0) != cudaSuccess)
+    return cuda_check("angular_cl_host join");
+  return cuda_check("angular_cl_host");
+}
+
 // --------------------------------------------------------- derivatives -----
 extern "C" int jcg_jacobian_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t* bytes) {
   if (!bytes) return fail(JCG_ERR_ARG, "bytes is NULL");

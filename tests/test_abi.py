@@ -82,6 +82,16 @@ def test_null_pointer_and_workspace_checks_do_not_touch_the_device():
                             ctypes.c_void_p(addr), ctypes.c_void_p(addr), 16, None)
     assert rc == _lib.ERR_WORKSPACE
     assert lib.jcg_gaussian_covariance(None, 3, 2, None, None, None, 1, 0.25, 1, None, None) == _lib.ERR_ARG
+    # host-buffer entry: NULL geometry, then a workspace below jcg_host_workspace_size
+    assert lib.jcg_angular_cl_host(ctypes.byref(g), None, ctypes.c_void_p(addr), 1, 0, ctypes.c_void_p(addr),
+                                   ctypes.c_void_p(addr), 16, None) == _lib.ERR_ARG
+    rc = lib.jcg_angular_cl_host(ctypes.byref(g), ctypes.c_void_p(addr), ctypes.c_void_p(addr), 1, 0,
+                                 ctypes.c_void_p(addr), ctypes.c_void_p(addr), 16, None)
+    assert rc == _lib.ERR_WORKSPACE
+    s1, s2 = ctypes.c_size_t(), ctypes.c_size_t()
+    assert lib.jcg_workspace_size(ctypes.byref(g), 7, 1, ctypes.byref(s1)) == 0
+    assert lib.jcg_host_workspace_size(ctypes.byref(g), 7, 1, ctypes.byref(s2)) == 0
+    assert s2.value >= s1.value + 7 * 8 * 8
 
 
 def test_error_mapping():
@@ -196,3 +206,5 @@ def test_limber_entry_points_refuse_caller_redshift_nodes():
                                 None) == _lib.ERR_ARG
     assert b"Limber grid" in lib.jcg_last_error_string()
     assert lib.jcg_angular_cl_noalloc(ctypes.byref(g), addr, addr, 1, _lib.FP64, addr, None) == _lib.ERR_ARG
+    assert lib.jcg_angular_cl_host(ctypes.byref(g), addr, addr, 1, _lib.FP64, addr, addr, 1 << 12,
+                                   None) == _lib.ERR_ARG
