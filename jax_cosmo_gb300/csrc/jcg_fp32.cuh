@@ -128,41 +128,4 @@ __device__ __forceinline__ void ff_acc_prod(float& ah, float& al, float2 a, floa
   ah = s;
 }
 
-// The contracting recurrence of the halofit moments' Taylor tables,
-// q[0] = 0, q[i + 1] = (q[i] + w[i]) rho (i < n), written as c q[i] at
-// dst[i * stride] for i = 0 .. n, by one warp in float pairs.  Lane l runs
-// its block of B = n / 32 steps (the last lane also the n - 32 B left), the
-// blocks' sums b_l (run from 0) are combined by an inclusive Kogge-Stone
-// scan, v_l = sum_{l' <= l} rho^(B (l - l')) b_l', and each lane runs its
-// block again from the carry v_{l-1}: 2 B + 5 dependent steps instead of n.
-// All terms are positive (w >= 0, rho > 0), so the order of the sums moves
-// the result by float-pair rounding only.
-__device__ __forceinline__ void ff_taylor_scan_warp(const float2* __restrict__ w, int n, FF rho, FF c, int lane,
-                                                    float2* __restrict__ dst, int stride) {
-  const int B = n >> 5;
-  const int i0 = lane * B, i1 = lane == 31 ? n : i0 + B;
-  FF b{0.f, 0.f};
-  for (int i = i0; i < i1; ++i) b = ff_mul(ff_add(b, FF{w[i].x, w[i].y}), rho);
-  // rho^B by squaring and multiplying
-  FF pw{1.f, 0.f}, base = rho;
-  for (int e = B; e > 0; e >>= 1) {
-    if (e & 1) pw = ff_mul(pw, base);
-    base = ff_mul(base, base);
-  }
-#pragma unroll
-  for (int s = 1; s < 32; s <<= 1) {
-    const float uh = __shfl_up_sync(0xffffffffu, b.hi, s), ul = __shfl_up_sync(0xffffffffu, b.lo, s);
-    if (lane >= s) b = ff_add(b, ff_mul(pw, FF{uh, ul}));
-    pw = ff_mul(pw, pw);
-  }
-  const float ch = __shfl_up_sync(0xffffffffu, b.hi, 1), cl = __shfl_up_sync(0xffffffffu, b.lo, 1);
-  FF q = lane == 0 ? FF{0.f, 0.f} : FF{ch, cl};
-  if (lane == 0) dst[0] = make_float2(0.f, 0.f);
-  for (int i = i0; i < i1; ++i) {
-    q = ff_mul(ff_add(q, FF{w[i].x, w[i].y}), rho);
-    const FF r = ff_mul(c, q);
-    dst[(size_t)(i + 1) * stride] = make_float2(r.hi, r.lo);
-  }
-}
-
 }  // namespace jcg

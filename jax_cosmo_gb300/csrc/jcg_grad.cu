@@ -558,7 +558,7 @@ __global__ void __launch_bounds__(F32T ? 128 : 256, F32T ? 4 : 1) grad_tables_ke
 // cosmology overlap with other cosmologies' work):
 //   Taylor tables, scaled to the table row so that no power of k overflows.
 //   Values: float pairs R_m[i] = c_m Q_m[i], c_m = (-1)^m / m!,
-//   Q_m[i] = sum_{k < i} w_k q3_k (kh_k / kh_i)^(2(m+1)) (one warp per m);
+//   Q_m[i] = sum_{k < i} w_k q3_k (kh_k / kh_i)^(2(m+1)) (one lane per m);
 //   tangents (FP32, one thread per (m, d)): sum_{k < i} w_k dq3_k
 //   (kh_k / kh_i)^(2(m+1)).  Both by the contracting recurrence
 //   Q_m[i+1] = (Q_m[i] + w_i q3_i) (kh_i / kh_{i+1})^(2(m+1)),
@@ -593,12 +593,22 @@ __global__ void __launch_bounds__(NRT) grad_moments32_kernel(GradBatch gb, const
   if (gi.ptt) {
     float2* pv = reinterpret_cast<float2*>(gi.ptt);  // [NKH + 1][NTAYLOR]
     float* pdv = ptt_tangents(gi.ptt);
-    // values: one warp per m (a block scan over the lanes)
-    for (int m = t >> 5; m < NTAYLOR; m += NRT >> 5)
-      ff_taylor_scan_warp(wq, NKH, FF{c->tay_rho[m][0], c->tay_rho[m][1]}, FF{c->tay_c[m][0], c->tay_c[m][1]},
-                          t & 31, pv + m, NTAYLOR);
-    if (t < NTAYLOR * NDIR) {
-      const int job = t, m = job / NDIR, d = job % NDIR;
+    if (t < NTAYLOR) {
+      const int m = t;
+      FF rho, cm, q;
+      rho.hi = c->tay_rho[m][0], rho.lo = c->tay_rho[m][1];
+      cm.hi = c->tay_c[m][0], cm.lo = c->tay_c[m][1];
+      q.hi = 0.f, q.lo = 0.f;
+      pv[m] = make_float2(0.f, 0.f);
+      for (int i = 0; i < NKH; ++i) {
+        FF w;
+        w.hi = wq[i].x, w.lo = wq[i].y;
+        q = ff_mul(ff_add(q, w), rho);
+        const FF r = ff_mul(cm, q);
+        pv[(size_t)(i + 1) * NTAYLOR + m] = make_float2(r.hi, r.lo);
+      }
+    } else if (t >= 32 && t < 32 + NTAYLOR * NDIR) {
+      const int job = t - 32, m = job / NDIR, d = job % NDIR;
       const float rho = c->tay_rho[m][0];
       float acc = 0.f;
       pdv[(size_t)m * NDIR + d] = 0.f;

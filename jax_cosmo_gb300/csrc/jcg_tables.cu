@@ -573,8 +573,7 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
   if (FAST) {
     // fp32c halofit moments: w pk3 as float pairs (float copy for the exp
     // terms), then the Taylor tables by the contracting recurrence
-    // Q_m[i + 1] = (Q_m[i] + w_i pk3_i) rho_m in float pairs, one warp per m
-    // (a block scan over the lanes)
+    // Q_m[i + 1] = (Q_m[i] + w_i pk3_i) rho_m in float pairs, one lane per m
     for (int i = t; i < NKH + 15; i += blockDim.x) {
       float hi = 0.f;
       if (i < NKH) {
@@ -585,9 +584,22 @@ __global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const Const
       out->wpk3f[i] = hi;
     }
     __syncthreads();
-    for (int m = warp; m < NTAYLOR; m += blockDim.x >> 5)
-      ff_taylor_scan_warp(wpp, NKH, FF{c->tay_rho[m][0], c->tay_rho[m][1]}, FF{c->tay_c[m][0], c->tay_c[m][1]}, lane,
-                          out->rtay[m], 1);
+    if (t < NTAYLOR) {
+      const int m = t;
+      FF rho, cm, q;
+      rho.hi = c->tay_rho[m][0], rho.lo = c->tay_rho[m][1];
+      cm.hi = c->tay_c[m][0], cm.lo = c->tay_c[m][1];
+      q.hi = 0.f, q.lo = 0.f;
+      float2* dst = out->rtay[m];
+      dst[0] = make_float2(0.f, 0.f);
+      for (int i = 0; i < NKH; ++i) {
+        FF w;
+        w.hi = wpp[i].x, w.lo = wpp[i].y;
+        q = ff_mul(ff_add(q, w), rho);
+        const FF r = ff_mul(cm, q);
+        dst[i + 1] = make_float2(r.hi, r.lo);
+      }
+    }
   }
   for (int i = t; i < NCHI; i += blockDim.x) out->chi[i] = chis[i];
   for (int i = t; i < NGROW; i += blockDim.x) out->g[i] = gs[i];
