@@ -326,55 +326,86 @@ __device__ __forceinline__ FF root_R_ff(const double* sig, double g2, const Cons
   return R.hi < 1e-6f ? ff_of(1e-6) : R;  // power.py:115
 }
 
-// Three phases per block of 64 Limber nodes of one cosmology:
+// Three phases per block of Limber nodes:
 //  1a thread per node: growth, chi, root find, k_nl; FAST: the exp index
 //     range and the Taylor part of the moments;
 //  1b warp per node: the exp part of the moments (power.py:121-136);
 //  2  thread per node: n_eff, C and the takahashi2012 coefficients.
+// A block takes 64 nodes of one cosmology (float64), or 256 consecutive
+// nodes of the batch's flat (cosmology, node) index (fp32c, one geometry,
+// at least 256 nodes per cosmology: each block spans at most two
+// cosmologies, whose tables it holds side by side, and no block runs short),
+// or 256 nodes of one cosmology (fp32c otherwise).
+__host__ __device__ inline bool hf_flat(const Batch& b) {
+  return b.precision == JCG_FP32C && !b.listed && b.max_na >= hf_nodes_per_block(true);
+}
 template <bool FAST>
 __global__ void __launch_bounds__(HF_WARPS * 32)
     halofit_rows_kernel(Batch bt, const ConstTables* __restrict__ c) {
-  const int item = blockIdx.y;
-  if (item >= bt.n_items) return;
-  const Item it = batch_item(bt, item);
-  const GeoHeader* geo = it.geo;
-  const int na = geo->na;
-  const int model = pk_model(it.physics);
-  const int n0 = blockIdx.x * hf_nodes_per_block(FAST);
-  if (n0 >= na) return;
   constexpr int NB = hf_nodes_per_block(FAST);
-  __shared__ double sig[NRT];
+  constexpr int NSL = FAST ? 2 : 1;  // cosmologies per block at most
+  const bool flat = FAST && hf_flat(bt);
+  int item0, n0, cnt, nsl;
+  if (flat) {
+    const long long f0 = (long long)blockIdx.x * NB, nf = (long long)bt.n_items * bt.max_na;
+    if (f0 >= nf) return;
+    item0 = (int)(f0 / bt.max_na);
+    n0 = (int)(f0 - (long long)item0 * bt.max_na);
+    cnt = (int)min((long long)NB, nf - f0);
+    nsl = n0 + cnt > bt.max_na ? 2 : 1;
+  } else {
+    item0 = blockIdx.y;
+    if (item0 >= bt.n_items) return;
+    n0 = blockIdx.x * NB;
+    const int na_i = batch_item(bt, item0).geo->na;
+    if (n0 >= na_i) return;
+    cnt = min(na_i - n0, NB);
+    nsl = 1;
+  }
+  const Item itA = batch_item(bt, item0);
+  const Item itB = nsl > 1 ? batch_item(bt, item0 + 1) : itA;
+  const GeoHeader* geo = itA.geo;
+  const int na = geo->na;
+  const int model = pk_model(itA.physics);
+  __shared__ double sigS[NSL][NRT];
   __shared__ double pk3[FAST ? 1 : NKH];
-  __shared__ double s[NSCAL];
+  __shared__ double sS[NSL][NSCAL];
   __shared__ double knl_s[NB], inv_s[NB], g_s[NB], chi_s[NB], t1_s[NB], t2_s[NB], s1_s[NB], s2_s[NB];
   __shared__ int ilo_s[NB], ihi_s[NB];
   __shared__ float iv2h_s[NB], iv2l_s[NB], f1_s[NB], f2_s[NB];
-  __shared__ float wpf[FAST ? NKH : 1], k2h[FAST ? NKH + 1 : 1], k2l[FAST ? NKH + 1 : 1];
+  __shared__ float wpfS[NSL][FAST ? NKH : 1], k2h[FAST ? NKH + 1 : 1], k2l[FAST ? NKH + 1 : 1];
   __shared__ float2 e2s[FAST ? 64 : 1];
-  const CosmoTab* ct = it.ctab;
   if (FAST)
     for (int i = threadIdx.x; i < 64; i += blockDim.x) e2s[i] = c->exp2_ff[i];
-  for (int i = threadIdx.x; i < NRT; i += blockDim.x) sig[i] = ct->sig[i];
+  for (int k = 0; k < nsl; ++k) {
+    const CosmoTab* ctk = k ? itB.ctab : itA.ctab;
+    for (int i = threadIdx.x; i < NRT; i += blockDim.x) sigS[k][i] = ctk->sig[i];
+    for (int i = threadIdx.x; i < NSCAL; i += blockDim.x) sS[k][i] = ctk->s[i];
+    if (FAST)
+      for (int i = threadIdx.x; i < NKH; i += blockDim.x) wpfS[k][i] = ctk->wpk3f[i];
+  }
   if (FAST) {
     for (int i = threadIdx.x; i < NKH + 1; i += blockDim.x) {
-      if (i < NKH) wpf[i] = ct->wpk3f[i];
       k2h[i] = c->kh2_hi[i];
       k2l[i] = c->kh2_lo[i];
     }
   } else {
-    for (int i = threadIdx.x; i < NKH; i += blockDim.x) pk3[i] = ct->pk3[i];
+    for (int i = threadIdx.x; i < NKH; i += blockDim.x) pk3[i] = itA.ctab->pk3[i];
   }
-  for (int i = threadIdx.x; i < NSCAL; i += blockDim.x) s[i] = ct->s[i];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const double* A = geo_ptr<double>(geo, geo->off_a);
   const double* WS = geo_ptr<double>(geo, geo->off_wsimp);
   const int64_t* SC = geo_ptr<int64_t>(geo, geo->off_seg_chi);
   const int64_t* SG = geo_ptr<int64_t>(geo, geo->off_seg_grow);
-  const int cnt = min(na - n0, NB);
+  // node t of the block: its cosmology's slot and its index on the Limber grid
+  auto slot_of = [&](int t) { return n0 + t >= na ? 1 : 0; };
+  auto node_of = [&](int t) { return n0 + t >= na ? n0 + t - na : n0 + t; };
   // phase 1a
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-    const int n = n0 + t;
+    const int n = node_of(t), slt = slot_of(t);
+    const double* sig = sigS[slt];
+    const CosmoTab* ct = slt ? itB.ctab : itA.ctab;
     const double a = A[n];
     double g, knl, inv;
     FF iv2;
@@ -445,6 +476,7 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   // phase 1b
   for (int t = warp; t < cnt; t += HF_WARPS) {
     const double inv = inv_s[t];
+    const float* wpf = wpfS[slot_of(t)];
     double s1 = 0.0, s2 = 0.0;
     if (FAST) {
       // FP32 terms: y^2 = kh^2 inv^2 as a float pair (hi p, lo e), exp(-y^2)
@@ -492,9 +524,11 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
   }
   __syncthreads();
   // phase 2
-  const Bg bg = make_bg(s);
   for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
-    const int n = n0 + t;
+    const int n = node_of(t), slt = slot_of(t);
+    const double* s = sS[slt];
+    double* const rows64 = slt ? itB.rows64 : itA.rows64;
+    float* const rows32 = slt ? itB.rows32 : itA.rows32;
     const double a = A[n];
     double s1 = FAST ? (double)f1_s[t] : s1_s[t], s2 = FAST ? (double)f2_s[t] : s2_s[t];
     if (FAST) {
@@ -530,14 +564,15 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
       row[R_U] = (double)((float)WS[n] * dchi * rcpf(chic * chic) * (float)(1.0 / C2));
     } else {
       const double lna = log(a);
+      const Bg bg = make_bg(s);
       halofit_coefs(bg, a, lna, hp, row, model);
       row[R_LGCHIC] = log(fmax(chiv, 1.0));
       const double dchi = bg_dchioverda_l(bg, a, lna);
       row[R_DCHI] = dchi;
       row[R_U] = WS[n] * dchi / fmax(chiv * chiv, 1.0) / C2;
     }
-    if (it.rows64) {
-      double* dst = it.rows64 + (size_t)n * NROW64;
+    if (rows64) {
+      double* dst = rows64 + (size_t)n * NROW64;
       if (FAST) {
         // fp32c: the Limber weight and the halofit parameters (the rest of
         // the integrand's inputs are in the FP32 row)
@@ -548,9 +583,9 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
         for (int i = 0; i < NROW64; ++i) dst[i] = row[i];
       }
     }
-    if (it.rows32) {
+    if (rows32) {
       if (!FAST) row32_from_row64(s, row, f);
-      float* dst = it.rows32 + (size_t)n * NROW32;
+      float* dst = rows32 + (size_t)n * NROW32;
       for (int i = 0; i < NROW32; ++i) dst[i] = f[i];
     }
   }
@@ -559,6 +594,7 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
 void launch_halofit_rows(const Batch& b, const ConstTables* c, cudaStream_t st) {
   const int nb = hf_nodes_per_block(b.precision == JCG_FP32C);
   dim3 grid((b.max_na + nb - 1) / nb, b.n_items);
+  if (hf_flat(b)) grid = dim3((unsigned)(((long long)b.n_items * b.max_na + nb - 1) / nb), 1);
   if (b.precision == JCG_FP32C)
     halofit_rows_kernel<true><<<grid, HF_WARPS * 32, 0, st>>>(b, c);
   else

@@ -383,9 +383,11 @@ void launch_geometry_build(const GeoHeader& h, double* geo, const double* pz, co
 // instantiation keeps the default one's registers).  FAST (fp32c): the
 // per-node evaluations (chi and growth right-hand sides, the Romberg
 // integrand, P(k) k^3) in float-pair arithmetic on the FP32 pipe; the scans,
-// sigma8's weighted sum and the tables' values stay float64.
+// sigma8's weighted sum and the tables' values stay float64.  Most phases
+// keep one or two warps of a block busy, so the fp32c form is held to 64
+// registers: four blocks per SM overlap their phases.
 template <bool NW, bool FAST>
-__global__ void __launch_bounds__(256) cosmo_tables_kernel(Batch bt, const ConstTables* __restrict__ c) {
+__global__ void __launch_bounds__(256, FAST ? 4 : 3) cosmo_tables_kernel(Batch bt, const ConstTables* __restrict__ c) {
   const int item = blockIdx.x;
   if (item >= bt.n_items) return;
   const Item it = batch_item(bt, item);
