@@ -479,7 +479,7 @@ def accuracy_arm(device):
         ll = jc.likelihood.gaussian_log_likelihood(data, mu, cov)
         if grad:
             ll.backward()
-            return float(ll), np.array([float(ps[n].grad) for n in names])
+            return float(ll.detach()), np.array([float(ps[n].grad) for n in names])
         return float(ll)
 
     c4 = {"workload": "5 WL x 50 ell in [10, 3000], N = 512, fiducial; data = mean + seeded noise from its "
