@@ -55,17 +55,22 @@ BOX = {
 ORDER = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
 # Per-cosmology figures of the fp32c step's kernels on this workload (na = 513
 # Limber nodes, 5 WL tracers, 100 ell), from ncu captures at 2048 cosmologies
-# (working sets above L2), one kernel per capture
-# (profiles/fp32c_kernels_b2048_per_kernel.md), divided by 2048:
+# (working sets above L2; the table stage's traffic at 4096), one kernel per
+# capture (profiles/fp32c_kernels_b2048_per_kernel.md), per cosmology:
 #   warp instructions issued (sm__inst_executed); the table stage is
 #     cosmo_scalars_kernel + cosmo_tables_kernel;
 #   FP64 operations = DFMA x 2 + DADD + DMUL thread instructions;
 #   traffic = dram__bytes_read.sum + dram__bytes_write.sum;
 #   per Limber node (100 x 513 per cosmology): XU (MUFU) thread operations
 #     and warp instructions of limber32_kernel.
-WARP_INSTR_PER_COSMO = {"cosmo_tables": 1_983 + 78_961, "halofit_rows": 89_616, "tracer_kernels": 134_702}
+WARP_INSTR_PER_COSMO = {"cosmo_tables": 1_983 + 79_204, "halofit_rows": 94_952, "tracer_kernels": 121_650}
 FP64_OPS = {"cosmo_tables": 14_262 + 26_177, "halofit_rows": 28_215}
-TRAFFIC_PER_COSMO = {"cosmo_tables": 94 + 28_018, "halofit_rows": 157_294, "tracer_kernels": 5_940, "limber": 129_634}
+TRAFFIC_PER_COSMO = {"cosmo_tables": 79 + 42_722, "halofit_rows": 157_904, "tracer_kernels": 6_550, "limber": 129_632}
+# the table stage writes its 55,040-byte record and reads little: its traffic
+# is taken at the benched batch (4096), and what the L2 still holds of its
+# writes when the kernel ends reaches DRAM after it
+TRAFFIC_NOTE = {"cosmo_tables": "DRAM bytes of the kernels at 4096 cosmologies; up to one L2 (126 MB) of the "
+                                "225 MB of records they write is written back after the kernel ends"}
 MUFU_PER_NODE = 17.37
 WARP_INSTR_PER_NODE = 8.196
 # algorithmic bytes per cosmology: what each kernel must read and write once
@@ -81,7 +86,7 @@ ALG_BYTES = {"cosmo_tables": 64 + 55_040, "halofit_rows": 55_040 + 513 * (7 * 8 
 # traffic, and algorithmic bytes (inputs read once, outputs written once,
 # scratch excluded):
 #   tables: parameters in; the TabD record (122,944 B) and the Taylor tables
-#     (206,592 B) out.  Kernels: grad_scalars, grad_nodes<0..2>, grad_tables,
+#     (206,592 B) out.  Kernels: grad_scalars32, grad_nodes<0..2>, grad_tables,
 #     grad_moments32;
 #   rows: TabD's float copies, P(k) and Taylor tables in (245,152 B), rows
 #     out (513 x 132 x 4);
@@ -89,22 +94,22 @@ ALG_BYTES = {"cosmo_tables": 64 + 55_040, "halofit_rows": 55_040 + 513 * (7 * 8 
 #     tangents out (5 x 513 x 9 x 4).  grad_kernval32u;
 #   product: rows, radial kernels, cotangent and Eisenstein-Hu inputs in;
 #     C_ell, the shear kernels' cotangents and the chunk gradients out.
-#     grad_vjp32 (the dominant kernel: 23.66 warp instructions and 44.4 MUFU
+#     grad_vjp32 (the dominant kernel: 22.23 warp instructions and 35.5 MUFU
 #     operations per Limber node);
 #   reverse: the shear cotangents and the chi table's tangents in, the chunk
 #     gradients out.  kernrev_owner, grad_kernrev32u, vjp_grad_reduce.
 VJP_STAGES = (("tables", 1), ("rows", 2), ("kernels", 4), ("product", 8), ("reverse", 16))
-VJP_WARP_INSTR_PER_COSMO = {"tables": 3_788 + 10_076 + 6_714 + 40_181 + 30_021 + 69_596, "rows": 155_894,
-                            "kernels": 122_648, "product": 1_213_587, "reverse": 94 + 300_726 + 112}
-VJP_TRAFFIC_PER_COSMO = {"tables": 240 + 10_609 + 10_022 + 5_777 + 161_077 + 218_388, "rows": 492_652,
-                         "kernels": 98_331, "product": 490_850, "reverse": 260 + 21_395 + 3_206}
+VJP_WARP_INSTR_PER_COSMO = {"tables": 338 + 9_420 + 5_970 + 39_574 + 22_665 + 69_596, "rows": 126_589,
+                            "kernels": 122_648, "product": 1_140_434, "reverse": 211 + 280_478 + 112}
+VJP_TRAFFIC_PER_COSMO = {"tables": 346 + 3_339 + 3_320 + 3_077 + 104_278 + 218_538, "rows": 485_339,
+                         "kernels": 98_580, "product": 397_755, "reverse": 261 + 21_404 + 3_206}
 VJP_ALG_BYTES = {"tables": 64 + 122_944 + 206_592, "rows": 245_152 + 513 * 132 * 4,
                  "kernels": 2 * 256 * 4 + 5 * 513 * 9 * 4,
                  "product": 513 * 132 * 4 + 5 * 513 * 9 * 4 + 15 * N_ELL * 8 + 416 + 15 * N_ELL * 8 + 5 * 513 * 4
                  + 17 * 8 * 8,
                  "reverse": 5 * 513 * 4 + 2 * 8 * 256 * 4 + 33 * 8 * 8}
-VJP_PRODUCT_WARP_INSTR_PER_NODE = 23.66
-VJP_PRODUCT_MUFU_PER_NODE = 44.4
+VJP_PRODUCT_WARP_INSTR_PER_NODE = 22.23
+VJP_PRODUCT_MUFU_PER_NODE = 35.5
 KERNEL_NAMES = {"cosmo_tables": "cosmo_scalars_kernel + cosmo_tables_kernel",
                 "halofit_rows": "halofit_rows_kernel<fp32c>",
                 "tracer_kernels": "tracer32_uniform_kernel<5>", "limber": "limber32_kernel<1>"}
@@ -172,7 +177,15 @@ class ClockSampler:
     def __init__(self, device_index):
         self.dev = device_index
         self.proc = None
+        self.skip = 0
         self.path = os.path.join(tempfile.gettempdir(), f"jcg_clocks_{os.getpid()}.csv")
+
+    def _lines(self):
+        try:
+            with open(self.path) as f:
+                return [ln for ln in f.read().split("\n") if ln.count(",") >= 8]
+        except OSError:
+            return []
 
     def start(self):
         try:
@@ -180,10 +193,19 @@ class ClockSampler:
             self.fh = open(self.path, "w")
             self.proc = subprocess.Popen(
                 ["nvidia-smi", f"--id={self.dev}", f"--query-gpu={self.QUERY}",
-                 "--format=csv,noheader,nounits", "-lms", "50"],
+                 "--format=csv,noheader,nounits", "-lms", "10"],
                 stdout=self.fh, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
+            return
+        # the sampler is running once its first line is out; samples before
+        # mark() (idle) are not counted
+        t0 = time.time()
+        while not self._lines() and time.time() - t0 < 5.0 and self.proc.poll() is None:
+            time.sleep(0.01)
+
+    def mark(self):
+        self.skip = len(self._lines())
 
     def stop(self):
         if self.proc is None:
@@ -195,7 +217,8 @@ class ClockSampler:
             self.proc.kill()
         self.fh.close()
         sm, smax, reasons = [], [], set()
-        for line in open(self.path):
+        lines = self._lines()
+        for line in (lines[self.skip:] or lines[-1:]):
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -282,6 +305,7 @@ def gpu_arm(args, rank, world, device):
     # headline: fp32c, inputs resident
     clocks = ClockSampler(device.index)
     clocks.start()
+    clocks.mark()
     t_fast, per = timed(lambda: step("fp32c"), args.steps, args.warmup)
     clk = clocks.stop()
     # plain float64 method on the same workload (fewer steps: it is ~100x slower)
@@ -702,6 +726,8 @@ def rooflines(res, B, live):
             e["hbm_frac"] = ALG_BYTES[k] * B / t / 1e9 / hbm
         if k in TRAFFIC_PER_COSMO:
             e["traffic"] = TRAFFIC_PER_COSMO[k] * B
+            if k in TRAFFIC_NOTE:
+                e["traffic_note"] = TRAFFIC_NOTE[k]
         if k in FP64_OPS:
             ach = FP64_OPS[k] * B / t / 1e12
             e["fp64"] = {"achieved": ach, "peak": live["fp64_tflops"], "unit": "TFLOP/s",
