@@ -210,8 +210,9 @@ int jcg_angular_cl_noalloc(const jcg_geometry* g, const void* geo_dev, const dou
  * gamma growth) and cl_host [n_cosmo][n_cls][n_ell] in host memory, the
  * boundary of a caller that holds no device arrays (a JAX host callback
  * binding angular_cl.py:49-98, a CPU sampler).  The parameters are copied in
- * on `stream`; the Limber stage runs over up to JCG_HOST_SLICES ranges of
- * cosmologies and each range's C_ell are copied out on a copy stream of the
+ * on `stream`; the Limber stage runs over at most JCG_HOST_SLICES ranges of
+ * cosmologies (from 2048 cosmologies on: the first three quarters, then the
+ * last quarter) and each range's C_ell are copied out on a copy stream of the
  * calling thread while the next range computes; `stream` then waits for the
  * last copy, so cl_host is complete once `stream` is synchronised.  With
  * pinned host memory (cudaHostAlloc / cudaHostRegister) the call returns

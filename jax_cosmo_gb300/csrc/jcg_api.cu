@@ -794,10 +794,10 @@ extern "C" int jcg_angular_cl_noalloc(const jcg_geometry* g, const void* geo, co
 // ------------------------------------------------------- host buffers -----
 // jcg_angular_cl with the parameters and the C_ell in host memory.  The
 // workspace is jcg_angular_cl's followed by device copies of the parameters
-// and of the C_ell.  The Limber stage runs as up to JCG_HOST_SLICES launches
-// over ranges of cosmologies; each range's C_ell leave on a copy stream of
-// the calling thread as soon as its launch ends, so the copies run under the
-// remaining launches; the stream then waits for the last copy.
+// and of the C_ell.  The Limber stage runs as one or two launches over ranges
+// of cosmologies; each range's C_ell leave on a copy stream of the calling
+// thread as soon as its launch ends, so the first copy runs under the second
+// launch; the stream then waits for the last copy.
 namespace {
 struct HostLayout {
   size_t params, cl, total;
@@ -850,10 +850,20 @@ static int host_copy(int dev, HostCopy** out) {
   return JCG_OK;
 }
 
-// ranges of at least 1024 cosmologies, at most JCG_HOST_SLICES of them
-static int host_slices(int n_cosmo) {
-  const int ns = n_cosmo / 1024;
-  return ns < 1 ? 1 : (ns > JCG_HOST_SLICES ? JCG_HOST_SLICES : ns);
+// The Limber launches' ranges [b[k], b[k + 1]): one below 2048 cosmologies,
+// else the first three quarters and the last quarter.  Only the last range's
+// copy is not under a Limber launch, so it is the short one; the first
+// range's copy (three times longer) runs under the last launch, and each
+// extra launch costs a partly idle last wave of CTAs.
+static int host_ranges(int n_cosmo, int* b) {
+  b[0] = 0;
+  if (n_cosmo < 2048) {
+    b[1] = n_cosmo;
+    return 1;
+  }
+  b[1] = n_cosmo - n_cosmo / 4;
+  b[2] = n_cosmo;
+  return 2;
 }
 
 extern "C" int jcg_host_workspace_size(const jcg_geometry* g, int n_cosmo, int precision, size_t* bytes) {
@@ -894,10 +904,11 @@ extern "C" int jcg_angular_cl_host(const jcg_geometry* g, const void* geo, const
   launch_cosmo_tables(b, c, stream);
   launch_halofit_rows(b, c, stream);
   launch_tracer_kernels(b, c, stream);
-  const int ns = host_slices(n_cosmo), lt = limber_tile(h.n_ell);
+  int rb[JCG_HOST_SLICES + 1];
+  const int ns = host_ranges(n_cosmo, rb), lt = limber_tile(h.n_ell);
   const size_t per = (size_t)h.n_cls * h.n_ell;
   for (int k = 0; k < ns; ++k) {
-    const int i0 = (int)((long long)n_cosmo * k / ns), i1 = (int)((long long)n_cosmo * (k + 1) / ns);
+    const int i0 = rb[k], i1 = rb[k + 1];
     launch_limber(batch_slice(b, i0, i1 - i0), c, lt, stream);
     if (cudaEventRecord(hc->ev[k], stream) != cudaSuccess || cudaStreamWaitEvent(hc->copy, hc->ev[k], 0) != cudaSuccess ||
         cudaMemcpyAsync(cl_host + (size_t)i0 * per, dcl + (size_t)i0 * per, (size_t)(i1 - i0) * per * sizeof(double),

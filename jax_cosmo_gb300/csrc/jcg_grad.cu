@@ -1027,6 +1027,7 @@ __global__ void __launch_bounds__(GR32_THREADS, 2) grad_rows32_kernel(GradBatch 
   float s1d[NDIR], s2d[NDIR];
 #pragma unroll
   for (int d = 0; d < NDIR; ++d) s1d[d] = s2d[d] = 0.f;
+#pragma unroll 2
   for (int i = ilo; i <= ihi; ++i) {
     const float kh = c->kh2_hi[i];
     const float pp = kh * R2.hi;
