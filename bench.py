@@ -63,24 +63,25 @@ ORDER = ["Omega_c", "Omega_b", "h", "n_s", "sigma8", "Omega_k", "w0", "wa"]
 #   traffic = dram__bytes_read.sum + dram__bytes_write.sum;
 #   per Limber node (100 x 513 per cosmology): XU (MUFU) thread operations
 #     and warp instructions of limber32_kernel.
-WARP_INSTR_PER_COSMO = {"cosmo_tables": 1_983 + 79_204, "halofit_rows": 94_952, "tracer_kernels": 121_650}
-FP64_OPS = {"cosmo_tables": 14_262 + 26_177, "halofit_rows": 28_215}
-TRAFFIC_PER_COSMO = {"cosmo_tables": 79 + 42_722, "halofit_rows": 157_904, "tracer_kernels": 6_550, "limber": 129_632}
-# the table stage writes its 55,040-byte record and reads little: its traffic
+WARP_INSTR_PER_COSMO = {"cosmo_tables": 1_984 + 79_846, "halofit_rows": 95_982, "tracer_kernels": 123_066}
+FP64_OPS = {"cosmo_tables": 14_262 + 26_309, "halofit_rows": 28_728}
+TRAFFIC_PER_COSMO = {"cosmo_tables": 79 + 42_725, "halofit_rows": 160_853, "tracer_kernels": 4_150, "limber": 51_366}
+# the table stage writes its 55,104-byte record and reads little: its traffic
 # is taken at the benched batch (4096), and what the L2 still holds of its
 # writes when the kernel ends reaches DRAM after it
 TRAFFIC_NOTE = {"cosmo_tables": "DRAM bytes of the kernels at 4096 cosmologies; up to one L2 (126 MB) of the "
-                                "225 MB of records they write is written back after the kernel ends"}
-MUFU_PER_NODE = 17.37
-WARP_INSTR_PER_NODE = 8.196
+                                "226 MB of records they write is written back after the kernel ends"}
+MUFU_PER_NODE = 17.36
+WARP_INSTR_PER_NODE = 8.109
 # algorithmic bytes per cosmology: what each kernel must read and write once
-#   cosmo_tables: 8 parameters in, the CosmoTab record out (55,040 B)
-#   halofit_rows: the CosmoTab record in, FP64 + FP32 rows out (513 x (7 x 8 + 16 x 4))
-#   tracer_kernels: the FP32 chi table and slopes in (2 x 256 x 4), 5 kernels out (5 x 513 x 8)
-#   limber: FP32 rows (16 x 4) + u (8) + 5 radial kernels (5 x 8) per node in, 15 x 100 C_ell out
-ALG_BYTES = {"cosmo_tables": 64 + 55_040, "halofit_rows": 55_040 + 513 * (7 * 8 + 16 * 4),
-             "tracer_kernels": 2 * 256 * 4 + 5 * 513 * 8,
-             "limber": 513 * (16 * 4 + 8) + 5 * 513 * 8 + 15 * N_ELL * 8}
+#   cosmo_tables: 8 parameters in, the CosmoTab record out (55,104 B)
+#   halofit_rows: the CosmoTab record in, FP64 + FP32 rows and the float
+#     Limber weight out (513 x (7 x 8 + 16 x 4 + 4))
+#   tracer_kernels: the FP32 chi table and slopes in (2 x 256 x 4), 5 float kernels out (5 x 513 x 4)
+#   limber: FP32 rows (16 x 4) + u (4) + 5 float radial kernels (5 x 4) per node in, 15 x 100 C_ell out
+ALG_BYTES = {"cosmo_tables": 64 + 55_104, "halofit_rows": 55_104 + 513 * (7 * 8 + 16 * 4 + 4),
+             "tracer_kernels": 2 * 256 * 4 + 5 * 513 * 4,
+             "limber": 513 * (16 * 4 + 4) + 5 * 513 * 4 + 15 * N_ELL * 8}
 # the fp32c vector-Jacobian product's stages (jcg_calib_vjp_stages masks) and
 # their per-cosmology figures from the same captures: warp instructions,
 # traffic, and algorithmic bytes (inputs read once, outputs written once,

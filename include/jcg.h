@@ -342,7 +342,8 @@ int jcg_requests_run(const jcg_request* reqs, int n, int mode, int precision, vo
  * what: 0 chi table [256], 1 growth table [128], 2 scalars [32],
  *       3 halofit rows [na][24] (FP64; with JCG_FP32C only chi, growth, k_nl,
  *       n_eff, C, dchi/da and the Limber weight are written), 4 radial
- *       kernels [n_tracers][na],
+ *       kernels [n_tracers][na] (FP64 workspaces; with JCG_FP32C the kernels
+ *       are kept as float and this copy is refused),
  *       5 P(k, a = 1) k^3 on the halofit k grid [257], 6 sigma^2(R) without
  *       the growth factor [256] (power.py:93-111). */
 int jcg_workspace_read(const jcg_geometry* g, int n_cosmo, int precision, const void* workspace,

@@ -275,7 +275,7 @@ static int make_header(const jcg_geometry* g, GeoHeader* h) {
 
 // ---------------------------------------------------------- workspace -------
 struct WsLayout {
-  size_t ctab, rows64, rows32, kern, total;
+  size_t ctab, rows64, rows32, kern, u32, kern32, total;
 };
 
 static size_t align256(size_t v) { return (v + 255) & ~size_t(255); }
@@ -293,6 +293,12 @@ static WsLayout ws_layout(const GeoHeader* h, int n_cosmo, int precision) {
   if (precision == JCG_FP32C) o = align256(o + sizeof(float) * NROW32 * na * n_cosmo);
   L.kern = o;
   o = align256(o + sizeof(double) * ntr * na * n_cosmo);
+  // fp32c: float copies of the Limber weight and the radial kernels (what
+  // the Limber kernel reads, contiguous)
+  L.u32 = o;
+  if (precision == JCG_FP32C) o = align256(o + sizeof(float) * na * n_cosmo);
+  L.kern32 = o;
+  if (precision == JCG_FP32C) o = align256(o + sizeof(float) * ntr * na * n_cosmo);
   L.total = o;
   return L;
 }
@@ -323,6 +329,8 @@ static Batch make_batch(const GeoHeader* h, const void* geo, const double* param
   b.rows64 = reinterpret_cast<double*>(base + L.rows64);
   b.rows32 = precision == JCG_FP32C ? reinterpret_cast<float*>(base + L.rows32) : nullptr;
   b.kern = reinterpret_cast<double*>(base + L.kern);
+  b.u32 = precision == JCG_FP32C && h ? reinterpret_cast<float*>(base + L.u32) : nullptr;
+  b.kern32 = precision == JCG_FP32C && h ? reinterpret_cast<float*>(base + L.kern32) : nullptr;
   b.cl = cl;
   b.precision = precision;
   b.max_na = h ? h->na : 0;
@@ -543,6 +551,7 @@ int jcg_workspace_read(const jcg_geometry* g, int n_cosmo, int precision, const 
       count = (size_t)h.na * NROW64;
       break;
     case 4:
+      if (precision == JCG_FP32C) return fail(JCG_ERR_UNSUPPORTED, "fp32c workspaces keep the radial kernels as float");
       src = reinterpret_cast<const double*>(base + L.kern) + (size_t)index * h.n_tr * h.na;
       count = (size_t)h.n_tr * h.na;
       break;
@@ -830,6 +839,8 @@ static Batch batch_slice(const Batch& b, int i0, int n) {
   if (b.rows64) s.rows64 = b.rows64 + (size_t)i0 * na * NROW64;
   if (b.rows32) s.rows32 = b.rows32 + (size_t)i0 * na * NROW32;
   s.kern = b.kern + (size_t)i0 * b.max_tr * na;
+  if (b.u32) s.u32 = b.u32 + (size_t)i0 * na;
+  if (b.kern32) s.kern32 = b.kern32 + (size_t)i0 * b.max_tr * na;
   s.cl = b.cl + (size_t)i0 * b.max_cls * b.max_ell;
   return s;
 }
@@ -1164,6 +1175,8 @@ extern "C" int jcg_requests_run(const jcg_request* reqs, int n, int mode, int pr
       }
       it.kern = reinterpret_cast<double*>(base + o);
       o += align256(sizeof(double) * (size_t)h.n_tr * h.na);
+      it.u32 = nullptr;  // ragged requests: the Limber kernel converts the FP64 columns
+      it.kern32 = nullptr;
       it.cl = reqs[i].cl_dev;
       it.precision = precision;
       it.physics = h.physics;

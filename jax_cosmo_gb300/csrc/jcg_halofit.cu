@@ -340,7 +340,7 @@ __host__ __device__ inline bool hf_flat(const Batch& b) {
   return b.precision == JCG_FP32C && !b.listed && b.max_na >= hf_nodes_per_block(true);
 }
 template <bool FAST>
-__global__ void __launch_bounds__(HF_WARPS * 32)
+__global__ void __launch_bounds__(HF_WARPS * 32, FAST ? 6 : 1)
     halofit_rows_kernel(Batch bt, const ConstTables* __restrict__ c) {
   constexpr int NB = hf_nodes_per_block(FAST);
   constexpr int NSL = FAST ? 2 : 1;  // cosmologies per block at most
@@ -529,6 +529,7 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
     const double* s = sS[slt];
     double* const rows64 = slt ? itB.rows64 : itA.rows64;
     float* const rows32 = slt ? itB.rows32 : itA.rows32;
+    float* const u32 = slt ? itB.u32 : itA.u32;
     const double a = A[n];
     double s1 = FAST ? (double)f1_s[t] : s1_s[t], s2 = FAST ? (double)f2_s[t] : s2_s[t];
     if (FAST) {
@@ -561,7 +562,9 @@ __global__ void __launch_bounds__(HF_WARPS * 32)
       const float dchi = (float)RH * ia2 * rsqrtf(e2);
       const float chic = fmaxf((float)chiv, 1.f);
       row[R_DCHI] = dchi;
-      row[R_U] = (double)((float)WS[n] * dchi * rcpf(chic * chic) * (float)(1.0 / C2));
+      const float uf = (float)WS[n] * dchi * rcpf(chic * chic) * (float)(1.0 / C2);
+      row[R_U] = (double)uf;
+      if (u32) u32[n] = uf;  // the Limber kernel's float copy
     } else {
       const double lna = log(a);
       const Bg bg = make_bg(s);

@@ -130,6 +130,16 @@ constexpr double Y2_SKIP = 60.0;    // above: exp(-y^2) y^4 P k^3 < 1e-20 of the
 constexpr int PAD_CT = 7;        // keeps sizeof(CosmoTab) a multiple of 64
 static_assert(S_NSCALAR <= NSCAL, "scalar block too small");
 
+// Per-cosmology Eisenstein-Hu inputs of the FP32 transfer function
+// (transfer.py:47-97 reduced to the factors eh32_T multiplies by).
+struct EH32 {
+  float qinv, lg2_qinv, sh, inv_sh, c18bc, c142ac, alpha_b, beta_b, beta_node, lg2_ksilk, fb, fc,
+      ns3;
+  float agam, nwq;  // type "eisenhu": alpha_gamma, (T_cmb / 2.7)^2 / (Omega_m h)
+  int nw;           // 1: type "eisenhu"
+};
+static_assert(sizeof(EH32) == 64, "EH32 is 64 bytes");
+
 struct CosmoTab {
   double s[NSCAL];
   double chi[NCHI];    // background.py:231-233  chi table on atab_chi
@@ -145,9 +155,32 @@ struct CosmoTab {
   // Float pairs R_m[i] = c_m Q_m[i], c_m = (-1)^m / m!,
   // Q_m[i] = sum_{k < i} w_k P(k_k) k_k^3 (k_k / k_i)^(2(m+1)), m < NTAYLOR
   float2 rtay[NTAYLOR][NKH + 1];
+  EH32 eh32;               // fp32c Limber integrand's transfer inputs (from s)
   double pad[PAD_CT];
 };
 static_assert(sizeof(CosmoTab) % 64 == 0, "CosmoTab must keep 64-byte alignment");
+
+// the EH32 of a cosmology from its scalars, once per cosmology (table stage)
+__device__ inline void make_eh32(const double* s, EH32* e) {
+  const double qinv = 1.0 / (13.41 * s[S_K_EQ]);
+  e->qinv = (float)qinv;
+  e->lg2_qinv = (float)log2(qinv);
+  e->sh = (float)s[S_SH_D];
+  e->inv_sh = (float)(1.0 / s[S_SH_D]);
+  e->c18bc = (float)(1.8 * s[S_BETA_C]);
+  e->c142ac = (float)(14.2 / s[S_ALPHA_C]);
+  e->alpha_b = (float)s[S_ALPHA_B];
+  e->beta_b = (float)s[S_BETA_B];
+  e->beta_node = (float)s[S_BETA_NODE];
+  e->lg2_ksilk = (float)log2(s[S_K_SILK]);
+  e->fb = (float)s[S_FB];
+  e->fc = (float)s[S_FC];
+  e->ns3 = (float)(s[S_NS] + 3.0);
+  e->agam = (float)s[S_AGAM];
+  e->nwq = (float)s[S_NWQ];
+  e->nw = s[S_TFNW] != 0.0;
+}
+
 
 // ------------------------------------------------- per-(cosmology, a) rows --
 // FP64 row written by the halofit-row kernel for every Limber node.
@@ -254,6 +287,8 @@ struct Item {
   double* cl;            // [n_cls][n_ell] (output)
   int precision;
   int physics;           // JCG_PK_* | JCG_TF_*
+  float* u32;            // fp32c, may be NULL: [na] the Limber weight u of the FP64 row, as float
+  float* kern32;         // fp32c, may be NULL: [n_tr][na] the radial kernels, as float
 };
 
 struct Batch {
@@ -268,6 +303,8 @@ struct Batch {
   float* rows32;
   double* kern;
   double* cl;
+  float* u32;            // uniform fp32c form (else NULL): [n_items][max_na]
+  float* kern32;         // uniform fp32c form (else NULL): [n_items][max_tr][max_na]
   int precision;
   int max_na, max_ell, max_cls, max_tr;
   int n_wl, n_wl_groups;  // uniform form: WeakLensing tracers and lensing groups
@@ -291,6 +328,8 @@ __device__ __forceinline__ Item batch_item(const Batch& b, int i) {
   it.cl = b.cl + (size_t)i * b.max_cls * b.max_ell;
   it.precision = b.precision;
   it.physics = b.physics;
+  it.u32 = b.u32 ? b.u32 + (size_t)i * na : nullptr;
+  it.kern32 = b.kern32 ? b.kern32 + (size_t)i * b.max_tr * na : nullptr;
   return it;
 }
 

@@ -149,7 +149,8 @@ __global__ void __launch_bounds__(TK_WARPS * 32)
         } else {
           kv = NZL[(size_t)t * na + n] * bias_at(geo, t, z, dz) * hz;
         }
-        it.kern[(size_t)t * na + n] = kv;
+        if (it.kern32) it.kern32[(size_t)t * na + n] = (float)kv;  // fp32c: what the Limber kernel reads
+        else it.kern[(size_t)t * na + n] = kv;
       }
     }
   }
@@ -202,6 +203,7 @@ __global__ void __launch_bounds__(256)
   const double om = ct->s[S_OMEGA_M];
   const Bg bg = make_bg(ct->s);
   const double cf = 3.0 * (H0 * H0) * om / 2.0 / C_KMS;  // probes.py:71
+  const float cff = (float)cf;
   const int n_tr = geo->n_tr;
   const double* Z = geo_ptr<double>(geo, geo->off_z);
   const double* AWL = geo_ptr<double>(geo, geo->off_awl);
@@ -209,6 +211,7 @@ __global__ void __launch_bounds__(256)
   const float* DXWL = geo_ptr<float>(geo, geo->off_dxwl32);
   const double* NZL = geo_ptr<double>(geo, geo->off_nzl);
   double* kern = bt.kern + (size_t)(live ? ci : 0) * bt.max_tr * na;
+  float* kern32 = bt.kern32 ? bt.kern32 + (size_t)(live ? ci : 0) * bt.max_tr * na : nullptr;
   const int n_end = min(na, n0 + TU_NODES);
   // the WeakLensing tracers in order, and their float weights
   int wl_t[NW];
@@ -265,17 +268,24 @@ __global__ void __launch_bounds__(256)
     }
     if (live) {
       const double z = Z[n];
+      const float zf1 = (float)(1.0 + z);
 #pragma unroll
       for (int u = 0; u < NW; ++u) {
         const int t = wl_t[u];
-        kern[(size_t)t * na + n] =
-            cf * ((double)acc[u] * (1.0 + z) * (double)chi_wl) * (1.0 + geo->mult[t]);
+        if (kern32) {  // what the Limber kernel reads: the same product in FP32
+          kern32[(size_t)t * na + n] = cff * (acc[u] * zf1 * chi_wl) * (float)(1.0 + geo->mult[t]);
+        } else {
+          kern[(size_t)t * na + n] = cf * ((double)acc[u] * (1.0 + z) * (double)chi_wl) * (1.0 + geo->mult[t]);
+        }
       }
       if (geo->n_nc > 0) {
         const double hz = bg_H(bg, AWL[n]);
         for (int t = 0; t < n_tr; ++t)
-          if (geo->kind[t] != JCG_TRACER_WL)
-            kern[(size_t)t * na + n] = NZL[(size_t)t * na + n] * geo->bias[t] * hz;
+          if (geo->kind[t] != JCG_TRACER_WL) {
+            const double kv = NZL[(size_t)t * na + n] * geo->bias[t] * hz;
+            if (kern32) kern32[(size_t)t * na + n] = (float)kv;
+            else kern[(size_t)t * na + n] = kv;
+          }
       }
     }
   }

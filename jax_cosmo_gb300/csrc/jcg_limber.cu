@@ -25,34 +25,6 @@ constexpr int LB_MAXLT = 32;
 constexpr int LB_MAXO = (LB_MAXLT * MAXPAIR + LB_THREADS - 1) / LB_THREADS;  // 17
 
 // Per-cosmology Eisenstein & Hu constants of the FP32 node.
-struct EH32 {
-  float qinv, lg2_qinv, sh, inv_sh, c18bc, c142ac, alpha_b, beta_b, beta_node, lg2_ksilk, fb, fc,
-      ns3;
-  float agam, nwq;  // type "eisenhu": alpha_gamma, (T_cmb / 2.7)^2 / (Omega_m h)
-  int nw;           // 1: type "eisenhu"
-};
-static_assert(sizeof(EH32) <= 64, "EH32 has 64 bytes of shared memory");
-
-__device__ void make_eh32(const double* s, EH32* e) {
-  const double qinv = 1.0 / (13.41 * s[S_K_EQ]);
-  e->qinv = (float)qinv;
-  e->lg2_qinv = (float)log2(qinv);
-  e->sh = (float)s[S_SH_D];
-  e->inv_sh = (float)(1.0 / s[S_SH_D]);
-  e->c18bc = (float)(1.8 * s[S_BETA_C]);
-  e->c142ac = (float)(14.2 / s[S_ALPHA_C]);
-  e->alpha_b = (float)s[S_ALPHA_B];
-  e->beta_b = (float)s[S_BETA_B];
-  e->beta_node = (float)s[S_BETA_NODE];
-  e->lg2_ksilk = (float)log2(s[S_K_SILK]);
-  e->fb = (float)s[S_FB];
-  e->fc = (float)s[S_FC];
-  e->ns3 = (float)(s[S_NS] + 3.0);
-  e->agam = (float)s[S_AGAM];
-  e->nwq = (float)s[S_NWQ];
-  e->nw = s[S_TFNW] != 0.0;
-}
-
 // Eisenstein-Hu T(k) in FP32 (transfer.py:88-153, either type) at k, lk =
 // log2 k, invk = 1 / k.
 template <bool GEN>
@@ -335,7 +307,6 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
   const int units = items * nsplit;
   const L32Layout L = l32_layout(n_tr, n_cls, LT);
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* s = reinterpret_cast<double*>(smem_raw);
   EH32* e32 = reinterpret_cast<EH32*>(smem_raw + L.e32);
   float4* kh4 = reinterpret_cast<float4*>(smem_raw + L.kh32);
   float* rowsS = reinterpret_cast<float*>(smem_raw + L.rows);
@@ -346,16 +317,14 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
   float* Pt = reinterpret_cast<float*>(smem_raw + L.pt);
   double* red = reinterpret_cast<double*>(smem_raw + L.red);
   const int tid = threadIdx.x;
-  const double* ELL = geo_ptr<double>(geo, geo->off_ell);
   const double* EF = geo_ptr<double>(geo, geo->off_ellfac);
-  for (int i = tid; i < NSCAL; i += LB_THREADS) s[i] = it.ctab->s[i];
-  for (int l = tid; l < lt; l += LB_THREADS) {
-    const double e = ELL[l0 + l] + 0.5;
-    // k = kh / max(chi, 1): kh, log2(kh), 1 / kh
-    kh4[l] = make_float4((float)e, (float)(1.4426950408889634 * log(e)), (float)(1.0 / e), 0.f);
-  }
+  // k = kh / max(chi, 1): kh = l + 1/2, log2(kh), 1 / kh from the geometry;
+  // the transfer inputs from the table stage
+  const float4* KH4 = geo_ptr<float4>(geo, geo->off_kh4);
+  for (int l = tid; l < lt; l += LB_THREADS) kh4[l] = KH4[l0 + l];
+  for (int i = tid; i < (int)(sizeof(EH32) / 4); i += LB_THREADS)
+    reinterpret_cast<int*>(e32)[i] = reinterpret_cast<const int*>(&it.ctab->eh32)[i];
   __syncthreads();
-  if (tid == 0) make_eh32(s, e32);
   // T^2 k^(n_s+3) table over this CTA's log2 k range: lg2(l + 1/2) of its ell plus the
   // range of log2(1 / max(chi, 1)) over the item's nodes
   float* Ttab = reinterpret_cast<float*>(smem_raw + L.tab);
@@ -396,6 +365,8 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
   const float* rows32 = it.rows32;
   const double* rows64 = it.rows64;
   const double* kern = it.kern;
+  const float* kern32 = it.kern32;
+  const float* u32 = it.u32;
   float acc[MAXU][4], comp[MAXU][4];
 #pragma unroll
   for (int r = 0; r < MAXU; ++r)
@@ -406,9 +377,10 @@ __global__ void __launch_bounds__(LB_THREADS, MAXU <= 1 ? 5 : (MAXU <= 3 ? 3 : 2
     for (int i = tid; i < tc * NROW32; i += LB_THREADS) rowsS[i] = rows32[(size_t)base * NROW32 + i];
     for (int q = tid; q < n_tr * tc; q += LB_THREADS) {
       const int tr = q / tc, t = q - tr * tc;
-      Ks[tr * LB_TA + t] = (float)kern[(size_t)tr * na + base + t];
+      Ks[tr * LB_TA + t] = kern32 ? kern32[(size_t)tr * na + base + t] : (float)kern[(size_t)tr * na + base + t];
     }
-    for (int t = tid; t < tc; t += LB_THREADS) us[t] = (float)rows64[(size_t)(base + t) * NROW64 + R_U];
+    for (int t = tid; t < tc; t += LB_THREADS)
+      us[t] = u32 ? u32[base + t] : (float)rows64[(size_t)(base + t) * NROW64 + R_U];
     __syncthreads();
     // M_ij(a) = (K_i K_j) u_a, zero-padded to ncp spectra
     for (int q = tid; q < tc * ncp; q += LB_THREADS) {

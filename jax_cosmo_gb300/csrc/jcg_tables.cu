@@ -606,6 +606,9 @@ __global__ void __launch_bounds__(256, FAST ? 4 : 3) cosmo_tables_kernel(Batch b
   for (int i = t; i < NCHI; i += blockDim.x) out->chi[i] = chis[i];
   for (int i = t; i < NGROW; i += blockDim.x) out->g[i] = gs[i];
   for (int i = t; i < NKH; i += blockDim.x) out->pk3[i] = pk3[i];
+  // the fp32c Limber kernel's transfer inputs, by a warp that the Taylor
+  // recurrences (warp 0) leave idle
+  if (t == 32) make_eh32(s, &out->eh32);
 }
 
 // The scalars, one half warp per cosmology: the independent pow / sqrt /
