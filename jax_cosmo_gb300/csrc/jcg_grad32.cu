@@ -229,7 +229,9 @@ __global__ void __launch_bounds__(256, 2) grad_kern32_kernel(GradBatch gb, const
         if (wl) {
           const float m1 = 1.f + (float)geo->mult[t];
           if (dir == 0) dst[0] += (float)kv * m1;
-          dst[1 + dir] += (float)kd * m1;
+          // UW: the shear tangents are zero and not stored by the value kernel
+          if (UW) dst[1 + dir] = (float)kd * m1;
+          else dst[1 + dir] += (float)kd * m1;
         } else {
           if (dir == 0) dst[0] = (float)kv;
           dst[1 + dir] = (float)kd;

@@ -164,14 +164,23 @@ __global__ void __launch_bounds__(VJ_THREADS, 2) grad_vjp32_kernel(GradBatch gb,
     const float* src = gi.rowg + (size_t)c0 * NROWG;
     float* R = b ? R1 : R0;
     for (int i = tid; i < cc * (NROWG / 4); i += VJ_THREADS) cp_async16(R + 4 * i, src + 4 * i);
-    // K rows [t][tracer][NDIR + 1]: consecutive threads on consecutive nodes
+    // K rows [t][tracer][NDIR + 1]: consecutive threads on consecutive nodes.
+    // With the shear integral in reverse over a uniform batch, a WeakLensing
+    // kernel without NLA term has zero tangents, which the value kernel does
+    // not store: they are set here.
     float* K = b ? K1 : K0;
     for (int i = tid; i < cc * n_tr; i += VJ_THREADS) {
       const int tr = i / cc, t = i - tr * cc;
       const float* ks = gi.kernf + ((size_t)tr * na + c0 + t) * (NDIR + 1);
       float* kd = K + ((size_t)t * n_tr + tr) * (NDIR + 1);
+      if (gb.krev_u && geo->kind[tr] == JCG_TRACER_WL && geo->bias_kind[tr] == JCG_BIAS_NONE) {
+        cp_async4(kd, ks);
 #pragma unroll
-      for (int k = 0; k < NDIR + 1; ++k) cp_async4(kd + k, ks + k);
+        for (int k = 1; k < NDIR + 1; ++k) kd[k] = 0.f;
+      } else {
+#pragma unroll
+        for (int k = 0; k < NDIR + 1; ++k) cp_async4(kd + k, ks + k);
+      }
     }
   };
   // the Eisenstein-Hu inputs and their tangents (formed once per cosmology
@@ -858,10 +867,9 @@ __global__ void __launch_bounds__(256) grad_kernval32u_kernel(GradBatch gb) {
       const float fac = cff * (float)(1.0 + Z[n]);
 #pragma unroll
       for (int u = 0; u < NW; ++u) {
-        float* dst = kf + ((size_t)wl_t[u] * na + n) * (NDIR + 1);
-        dst[0] = fac * chi_wl * acc[u] * m1[u];
-#pragma unroll
-        for (int d = 0; d < NDIR; ++d) dst[1 + d] = 0.f;
+        // the value only: the shear integral's tangents are zero (taken in
+        // reverse), and the product kernel fills them in shared memory
+        kf[((size_t)wl_t[u] * na + n) * (NDIR + 1)] = fac * chi_wl * acc[u] * m1[u];
       }
     }
   }
