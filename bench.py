@@ -91,25 +91,27 @@ ALG_BYTES = {"cosmo_tables": 64 + 55_104, "halofit_rows": 55_104 + 513 * (7 * 8 
 #     grad_moments32;
 #   rows: TabD's float copies, P(k) and Taylor tables in (245,152 B), rows
 #     out (513 x 132 x 4);
-#   kernels: the chi table in (2 x 256 x 4), 5 radial kernels with 8 zero
-#     tangents out (5 x 513 x 9 x 4).  grad_kernval32u;
+#   kernels: the chi table in (2 x 256 x 4), the values of 5 radial kernels
+#     out (5 x 513 x 4; their zero tangents are not stored).  grad_kernval32u
+#     (its traffic is above these bytes: each 4-byte value lands in a 36-byte
+#     record, so the L2 reads the sector before merging it);
 #   product: rows, radial kernels, cotangent and Eisenstein-Hu inputs in;
 #     C_ell, the shear kernels' cotangents and the chunk gradients out.
-#     grad_vjp32 (the dominant kernel: 22.23 warp instructions and 35.5 MUFU
+#     grad_vjp32 (the dominant kernel: 22.25 warp instructions and 35.5 MUFU
 #     operations per Limber node);
 #   reverse: the shear cotangents and the chi table's tangents in, the chunk
 #     gradients out.  kernrev_owner, grad_kernrev32u, vjp_grad_reduce.
 VJP_STAGES = (("tables", 1), ("rows", 2), ("kernels", 4), ("product", 8), ("reverse", 16))
 VJP_WARP_INSTR_PER_COSMO = {"tables": 338 + 9_420 + 5_970 + 39_574 + 22_665 + 69_596, "rows": 126_589,
-                            "kernels": 122_648, "product": 1_140_434, "reverse": 211 + 280_478 + 112}
+                            "kernels": 122_006, "product": 1_141_466, "reverse": 211 + 280_478 + 112}
 VJP_TRAFFIC_PER_COSMO = {"tables": 346 + 3_339 + 3_320 + 3_077 + 104_278 + 218_538, "rows": 485_339,
-                         "kernels": 98_580, "product": 397_755, "reverse": 261 + 21_404 + 3_206}
+                         "kernels": 157_559, "product": 397_623, "reverse": 261 + 21_404 + 3_206}
 VJP_ALG_BYTES = {"tables": 64 + 122_944 + 206_592, "rows": 245_152 + 513 * 132 * 4,
-                 "kernels": 2 * 256 * 4 + 5 * 513 * 9 * 4,
+                 "kernels": 2 * 256 * 4 + 5 * 513 * 4,
                  "product": 513 * 132 * 4 + 5 * 513 * 9 * 4 + 15 * N_ELL * 8 + 416 + 15 * N_ELL * 8 + 5 * 513 * 4
                  + 17 * 8 * 8,
                  "reverse": 5 * 513 * 4 + 2 * 8 * 256 * 4 + 33 * 8 * 8}
-VJP_PRODUCT_WARP_INSTR_PER_NODE = 22.23
+VJP_PRODUCT_WARP_INSTR_PER_NODE = 22.25
 VJP_PRODUCT_MUFU_PER_NODE = 35.5
 KERNEL_NAMES = {"cosmo_tables": "cosmo_scalars_kernel + cosmo_tables_kernel",
                 "halofit_rows": "halofit_rows_kernel<fp32c>",
