@@ -210,8 +210,8 @@ __global__ void __launch_bounds__(256)
   const int32_t* QWL = geo_ptr<int32_t>(geo, geo->off_qwl32);
   const float* DXWL = geo_ptr<float>(geo, geo->off_dxwl32);
   const double* NZL = geo_ptr<double>(geo, geo->off_nzl);
-  // the kernels as float (what the fp32c Limber kernel reads)
-  float* kern32 = bt.kern32 + (size_t)(live ? ci : 0) * bt.max_tr * na;
+  double* kern = bt.kern + (size_t)(live ? ci : 0) * bt.max_tr * na;
+  float* kern32 = bt.kern32 ? bt.kern32 + (size_t)(live ? ci : 0) * bt.max_tr * na : nullptr;
   const int n_end = min(na, n0 + TU_NODES);
   // the WeakLensing tracers in order, and their float weights
   int wl_t[NW];
@@ -220,9 +220,6 @@ __global__ void __launch_bounds__(256)
     for (int t = 0; t < n_tr && u < NW; ++t)
       if (geo->kind[t] == JCG_TRACER_WL) wl_t[u++] = t;
   }
-  float m1f[NW];  // 1 + m of each WeakLensing tracer
-#pragma unroll
-  for (int u = 0; u < NW; ++u) m1f[u] = (float)(1.0 + geo->mult[wl_t[u]]);
   const int32_t* Q32b = geo_ptr<int32_t>(geo, geo->off_q32[0]);
   const float* DX32b = geo_ptr<float>(geo, geo->off_dx32[0]);
   float4* recw = recs + warp * 32 * KuRec<NW>::N4;
@@ -273,11 +270,22 @@ __global__ void __launch_bounds__(256)
       const double z = Z[n];
       const float zf1 = (float)(1.0 + z);
 #pragma unroll
-      for (int u = 0; u < NW; ++u) kern32[(size_t)wl_t[u] * na + n] = cff * (acc[u] * zf1 * chi_wl) * m1f[u];
+      for (int u = 0; u < NW; ++u) {
+        const int t = wl_t[u];
+        if (kern32) {  // what the Limber kernel reads: the same product in FP32
+          kern32[(size_t)t * na + n] = cff * (acc[u] * zf1 * chi_wl) * (float)(1.0 + geo->mult[t]);
+        } else {
+          kern[(size_t)t * na + n] = cf * ((double)acc[u] * (1.0 + z) * (double)chi_wl) * (1.0 + geo->mult[t]);
+        }
+      }
       if (geo->n_nc > 0) {
         const double hz = bg_H(bg, AWL[n]);
         for (int t = 0; t < n_tr; ++t)
-          if (geo->kind[t] != JCG_TRACER_WL) kern32[(size_t)t * na + n] = (float)(NZL[(size_t)t * na + n] * geo->bias[t] * hz);
+          if (geo->kind[t] != JCG_TRACER_WL) {
+            const double kv = NZL[(size_t)t * na + n] * geo->bias[t] * hz;
+            if (kern32) kern32[(size_t)t * na + n] = (float)kv;
+            else kern[(size_t)t * na + n] = kv;
+          }
       }
     }
   }
@@ -293,8 +301,8 @@ static void launch_tu(const Batch& b, const ConstTables* c, cudaStream_t st) {
 }
 
 void launch_tracer_kernels(const Batch& b, const ConstTables* c, cudaStream_t st) {
-  if (b.precision == JCG_FP32C && !b.listed && b.kern32 && !b.special_bias && !b.has_delta && b.n_wl_groups == 1 &&
-      b.n_wl >= 1 && b.n_wl <= 8) {
+  if (b.precision == JCG_FP32C && !b.listed && !b.special_bias && !b.has_delta && b.n_wl_groups == 1 && b.n_wl >= 1 &&
+      b.n_wl <= 8) {
     switch (b.n_wl) {
       case 1: launch_tu<1>(b, c, st); return;
       case 2: launch_tu<2>(b, c, st); return;
